@@ -1,0 +1,210 @@
+/*
+ * pyfrb200 -- C ABI of the GB300-native flux-reconstruction right-hand
+ * side and Runge-Kutta stage update (the `b200` backend).
+ *
+ * Every entry point returns an int status: 0 on success, nonzero on error,
+ * with a message available from b200_get_last_error().  Pointers are raw
+ * device pointers unless stated otherwise; `stream` is a cudaStream_t
+ * passed as void*.  Fields use the reference CUDA backend's AoSoA layout
+ * with a SoA block of 32: a field of io-shape (nrow, nvars, neles) with
+ * leading dimension `ld` stores variable v of element e on row r at
+ *     r*ld + (e/32)*32*nvars + v*32 + e%32.
+ * Interface views are (base pointer, gather map) pairs: the map holds
+ * element offsets from the base (int32 or int64, selected by `ix64`), the
+ * variables of a point are 32 elements apart, and vector views add a
+ * per-point row stride for the spatial index.
+ *
+ * Each declaration cites the reference interface it replaces (paths within
+ * the PyFR source tree).
+ */
+#ifndef PYFRB200_H
+#define PYFRB200_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Gas and viscosity constants of the flux kernels ([constants] gamma, mu,
+ * Pr, cpTref, cpTs; viscosity-correction = sutherland when sutherland != 0);
+ * pyfr/solvers/navstokes/kernels/flux.mako:48-105. */
+typedef struct {
+    double gamma, mu, pr, cpTref, cpTs;
+    int sutherland;
+} b200_gas_t;
+
+/* Riemann solver ids: [solver-interfaces] riemann-solver */
+#define B200_RSOLVER_RUSANOV 0
+#define B200_RSOLVER_HLLC 1
+
+/* ---- context, memory, streams, events, graphs ------------------------ */
+/* Replace the driver wrappers of pyfr/backends/cuda/driver.py (context,
+ * mem_alloc/memset/memcpy, streams, events, graphs) used by
+ * pyfr/backends/cuda/base.py:9-144 and pyfr/backends/cuda/types.py. */
+const char *b200_version(void);
+int b200_get_last_error(char *buf, size_t len);
+int b200_init(int device);
+int b200_device_info(int *sm_count, int *cc_major, int *cc_minor, size_t *free_bytes,
+                     size_t *total_bytes, char *name, size_t namelen);
+int b200_malloc(void **ptr, size_t nbytes);          /* zero-filled, as base.py:137-144 */
+int b200_free(void *ptr);
+int b200_host_alloc(void **ptr, size_t nbytes);      /* page-locked host memory */
+int b200_host_free(void *ptr);
+int b200_memset(void *ptr, int value, size_t nbytes, void *stream);
+int b200_memcpy_htod(void *dst, const void *src, size_t nbytes, void *stream);
+int b200_memcpy_dtoh(void *dst, const void *src, size_t nbytes, void *stream);
+int b200_memcpy_dtod(void *dst, const void *src, size_t nbytes, void *stream);
+int b200_stream_create(void **stream);
+int b200_stream_destroy(void *stream);
+int b200_stream_sync(void *stream);
+int b200_device_sync(void);
+int b200_event_create(void **evt);
+int b200_event_destroy(void *evt);
+int b200_event_record(void *evt, void *stream);
+int b200_event_sync(void *evt);
+int b200_event_elapsed(float *ms, void *start, void *stop);
+/* Graph capture of a kernel sequence; replaces CUDAGraph
+ * (pyfr/backends/cuda/types.py:79-116). */
+int b200_graph_begin_capture(void *stream);
+int b200_graph_end_capture(void *stream, void **gexec);
+int b200_graph_launch(void *gexec, void *stream);
+int b200_graph_destroy(void *gexec);
+
+/* ---- operator apply: out = alpha*A@B + beta*out ----------------------- */
+/* Replaces the `mul` providers CUDAGiMMiKKernels.mul
+ * (pyfr/backends/cuda/gimmik.py:23-121) and CUDACUBLASLtKernels.mul
+ * (pyfr/backends/cuda/cublaslt.py:169-280).  `a` is the dense m x k
+ * operator on the host (row-major); the handle keeps its nonzeros on the
+ * device.  B and out are row-major with leading dimensions ldb/ldc. */
+int b200_mul_create(const double *a, int m, int k, void **handle);
+int b200_mul_nnz(void *handle, int *nnz);
+int b200_mul_destroy(void *handle);
+int b200_mul_f64(void *handle, const double *b, int64_t ldb, double *c, int64_t ldc,
+                 int64_t ncol, double alpha, double beta, void *stream);
+int b200_mul_f32(void *handle, const float *b, int64_t ldb, float *c, int64_t ldc,
+                 int64_t ncol, float alpha, float beta, void *stream);
+
+/* ---- element pointwise kernels over [nupts, neles] ------------------- */
+/* Geometry: linear != 0 computes the metric terms from the element
+ * vertices `verts` (nverts, ndims, neles) at the reference solution points
+ * `upts` (nupts x ndims, row-major with leading dimension ldup); linear == 0
+ * reads stored metric terms `smats` (ndims, nupts, ndims, neles) and
+ * `rcpdjac` (nupts x neles, leading dimension ldr). */
+
+/* Euler transformed flux; pyfr/solvers/euler/kernels/tflux.mako:8-30,
+ * provider call pyfr/solvers/euler/elements.py:149-206. */
+int b200_tflux_euler_f64(int ndims, int nupts, int64_t neles, int linear, double gamma,
+                         const double *u, int64_t ldu, double *f, int64_t ldf,
+                         const double *smats, int64_t lds, const double *verts, int64_t ldv,
+                         const double *upts, int64_t ldup, void *stream);
+int b200_tflux_euler_f32(int ndims, int nupts, int64_t neles, int linear, double gamma,
+                         const float *u, int64_t ldu, float *f, int64_t ldf,
+                         const float *smats, int64_t lds, const float *verts, int64_t ldv,
+                         const float *upts, int64_t ldup, void *stream);
+
+/* Navier-Stokes fused gradient transform + transformed flux;
+ * pyfr/solvers/navstokes/kernels/tflux.mako:13-50, provider call
+ * pyfr/solvers/navstokes/elements.py:64-128.  gradu is updated in place. */
+int b200_tflux_ns_f64(int ndims, int nupts, int64_t neles, int linear, const b200_gas_t *gas,
+                      const double *u, int64_t ldu, double *f, int64_t ldf, double *gradu,
+                      int64_t ldg, const double *smats, int64_t lds, const double *rcpdjac,
+                      int64_t ldr, const double *verts, int64_t ldv, const double *upts,
+                      int64_t ldup, void *stream);
+int b200_tflux_ns_f32(int ndims, int nupts, int64_t neles, int linear, const b200_gas_t *gas,
+                      const float *u, int64_t ldu, float *f, int64_t ldf, float *gradu,
+                      int64_t ldg, const float *smats, int64_t lds, const float *rcpdjac,
+                      int64_t ldr, const float *verts, int64_t ldv, const float *upts,
+                      int64_t ldup, void *stream);
+
+/* Physical gradient; pyfr/solvers/baseadvecdiff/kernels/gradcoru.mako:10-24. */
+int b200_gradcoru_f64(int ndims, int nupts, int64_t neles, int linear, double *gradu,
+                      int64_t ldg, const double *smats, int64_t lds, const double *rcpdjac,
+                      int64_t ldr, const double *verts, int64_t ldv, const double *upts,
+                      int64_t ldup, void *stream);
+int b200_gradcoru_f32(int ndims, int nupts, int64_t neles, int linear, float *gradu,
+                      int64_t ldg, const float *smats, int64_t lds, const float *rcpdjac,
+                      int64_t ldr, const float *verts, int64_t ldv, const float *upts,
+                      int64_t ldup, void *stream);
+
+/* R <- -R/|J|; pyfr/solvers/baseadvec/kernels/negdivconf.mako:7-22 (no
+ * source terms). */
+int b200_negdivconf_f64(int nvars, int nupts, int64_t neles, double *r, int64_t ldr,
+                        const double *rcpdjac, int64_t ldj, void *stream);
+int b200_negdivconf_f32(int nvars, int nupts, int64_t neles, float *r, int64_t ldr,
+                        const float *rcpdjac, int64_t ldj, void *stream);
+
+/* ---- interface kernels over the interior flux-point pairs ------------ */
+/* Euler common normal flux, written +/- to both sides;
+ * pyfr/solvers/euler/kernels/intcflux.mako:6-22 with
+ * rsolvers/rusanov.mako:4-26 or rsolvers/hllc.mako:4-77.  nl is the
+ * (ndims x n) matrix of scaled left normals, leading dimension ldn. */
+int b200_intcflux_euler_f64(int ndims, int64_t n, int rsolver, double gamma, double *ul_base,
+                            const void *ul_map, double *ur_base, const void *ur_map, int ix64,
+                            const double *nl, int64_t ldn, void *stream);
+int b200_intcflux_euler_f32(int ndims, int64_t n, int rsolver, double gamma, float *ul_base,
+                            const void *ul_map, float *ur_base, const void *ur_map, int ix64,
+                            const float *nl, int64_t ldn, void *stream);
+
+/* Navier-Stokes common flux (Riemann + LDG viscous with beta, tau);
+ * pyfr/solvers/navstokes/kernels/intcflux.mako:10-54. */
+int b200_intcflux_ns_f64(int ndims, int64_t n, int rsolver, const b200_gas_t *gas, double beta,
+                         double tau, double *ul_base, const void *ul_map, double *ur_base,
+                         const void *ur_map, const double *gl_base, const void *gl_map,
+                         const void *gl_rstr, const double *gr_base, const void *gr_map,
+                         const void *gr_rstr, int ix64, const double *nl, int64_t ldn,
+                         void *stream);
+int b200_intcflux_ns_f32(int ndims, int64_t n, int rsolver, const b200_gas_t *gas, double beta,
+                         double tau, float *ul_base, const void *ul_map, float *ur_base,
+                         const void *ur_map, const float *gl_base, const void *gl_map,
+                         const void *gl_rstr, const float *gr_base, const void *gr_map,
+                         const void *gr_rstr, int ix64, const float *nl, int64_t ldn,
+                         void *stream);
+
+/* LDG common solution; pyfr/solvers/navstokes/kernels/intconu.mako:4-19. */
+int b200_intconu_f64(int nvars, int64_t n, double beta, const double *lin_base,
+                     const void *lin_map, const double *rin_base, const void *rin_map,
+                     double *lout_base, const void *lout_map, double *rout_base,
+                     const void *rout_map, int ix64, void *stream);
+int b200_intconu_f32(int nvars, int64_t n, double beta, const float *lin_base,
+                     const void *lin_map, const float *rin_base, const void *rin_map,
+                     float *lout_base, const void *lout_map, float *rout_base,
+                     const void *rout_map, int ix64, void *stream);
+
+/* ---- integrator register kernels (flat over n scalars) --------------- */
+/* RK stage of the two-register low-storage schemes;
+ * pyfr/integrators/explicit/kernels/rkvdh2.mako:4-31 and
+ * pyfr/integrators/explicit/steppers.py:165-190. */
+int b200_rkvdh2_f64(int64_t n, int stage, int nstages, int errest, double dt, double a,
+                    double b, double e, double *r1, double *r2, double *rold, double *rerr,
+                    void *stream);
+int b200_rkvdh2_f32(int64_t n, int stage, int nstages, int errest, double dt, double a,
+                    double b, double e, float *r1, float *r2, float *rold, float *rerr,
+                    void *stream);
+
+/* x0 <- a[0]*x0 + sum_{k>=1} a[k]*xs[k]; xs is a host array of nv device
+ * pointers (xs[0] ignored), nv <= 8; pyfr/backends/cuda/kernels/axnpby.mako. */
+int b200_axnpby_f64(int64_t n, int nv, double *x0, const double *const *xs, const double *a,
+                    void *stream);
+int b200_axnpby_f32(int64_t n, int nv, float *x0, const float *const *xs, const double *a,
+                    void *stream);
+
+/* PI-controller error norm: out[0] = sum (or max when uniform != 0) over
+ * the valid points of (err/(atol[v] + rtol*|curr|))^2 (|.| when uniform);
+ * atol_dev holds nvars device doubles, scratch at least one double per
+ * block (nscratch).  Replaces the reduction kernel of
+ * pyfr/backends/cuda/kernels/reduction.mako:4-95 as called from
+ * pyfr/integrators/controllers.py:105-117. */
+int b200_errest_f64(int nupts, int nvars, int64_t neles, int64_t ld, const double *curr,
+                    const double *err, const double *atol_dev, double rtol, int uniform,
+                    double *scratch, int nscratch, double *out, void *stream);
+int b200_errest_f32(int nupts, int nvars, int64_t neles, int64_t ld, const float *curr,
+                    const float *err, const double *atol_dev, double rtol, int uniform,
+                    double *scratch, int nscratch, double *out, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PYFRB200_H */

@@ -1,0 +1,367 @@
+"""CPU oracle for the flux-reconstruction right-hand side and RK45 stages.
+
+TEST INFRASTRUCTURE ONLY: this module is the checker that the CUDA path
+is compared against.  It is imported by ``tests/``, by
+``__graft_entry__.smoke()`` and by ``bench.py``'s CPU baseline leg, never by
+the product package.
+
+It restates, in plain numpy on a simple (npts, nvars, neles) layout, the
+arithmetic of the reference's OpenMP/CUDA kernels on this path:
+
+  operator applies (mul)     pyfr/solvers/baseadvec/elements.py:73-100,
+                             pyfr/solvers/baseadvecdiff/elements.py:48-101
+  Euler flux / tflux         pyfr/solvers/euler/kernels/flux.mako:3-26,
+                             pyfr/solvers/euler/kernels/tflux.mako:8-30
+  Rusanov / HLLC             pyfr/solvers/euler/kernels/rsolvers/rusanov.mako:4-26,
+                             pyfr/solvers/euler/kernels/rsolvers/hllc.mako:4-77
+  intcflux (Euler, NS)       pyfr/solvers/euler/kernels/intcflux.mako:6-22,
+                             pyfr/solvers/navstokes/kernels/intcflux.mako:10-54
+  intconu                    pyfr/solvers/navstokes/kernels/intconu.mako:4-19
+  viscous flux               pyfr/solvers/navstokes/kernels/flux.mako:48-105
+  gradient transform         pyfr/solvers/baseadvecdiff/kernels/transform_grad.mako:3-10
+  negdivconf                 pyfr/solvers/baseadvec/kernels/negdivconf.mako:7-22
+  rkvdh2 / RK45              pyfr/integrators/explicit/kernels/rkvdh2.mako:4-31,
+                             pyfr/integrators/explicit/steppers.py:165-243
+  graph order (Euler, NS)    pyfr/solvers/baseadvec/system.py:58-136,
+                             pyfr/solvers/baseadvecdiff/system.py:54-231
+
+Everything the oracle needs about the discretisation is passed in: the
+operator matrices (tests feed the ones generated by the reference's own
+``pyfr/shapes.py``, see tests/golden/make_golden.py), the element
+vertices, the interface connectivity and the reference element's points.
+Flux points of the two sides of an interface are paired here by matching
+physical coordinates (modulo the mesh periods), an algorithm independent
+of the sort-based pairing the product uses.
+
+Pinning: the operator matrices are checked against the reference's
+golden file ``pyfr/tests/hex-gleg-ord3.npz`` and against matrices generated
+by the reference itself; the pointwise kernel arithmetic has no golden
+vectors in the reference (parity of that part rests on this restatement
+plus invariants: free-stream preservation, conservation, Riemann
+consistency and the exact advected vortex).
+"""
+
+import numpy as np
+
+
+# ---------------------------------------------------------------------------
+# Physics
+# ---------------------------------------------------------------------------
+
+def inviscid_flux(u, gamma):
+    """u: (nvars, ...) -> F: (ndims, nvars, ...), p, v (ndims, ...)."""
+    nv = u.shape[0]
+    nd = nv - 2
+    rho, E = u[0], u[-1]
+    invrho = 1.0/rho
+    rhov = u[1:nd + 1]
+    v = invrho*rhov
+    p = (gamma - 1)*(E - 0.5*invrho*np.sum(rhov*rhov, axis=0))
+    f = np.empty((nd,) + u.shape)
+    for i in range(nd):
+        f[i, 0] = rhov[i]
+        f[i, -1] = (E + p)*v[i]
+        for j in range(nd):
+            f[i, j + 1] = rhov[i]*v[j] + (p if i == j else 0)
+    return f, p, v
+
+
+def viscous_flux(u, grad, c):
+    """Negated-stress viscous flux; grad: (ndims, nvars, ...)."""
+    nv = u.shape[0]
+    nd = nv - 2
+    rho, E = u[0], u[-1]
+    rcprho = 1.0/rho
+    vel = rcprho*u[1:nd + 1]
+    dv = np.array([[grad[d, i + 1] - vel[i]*grad[d, 0] for d in range(nd)]
+                   for i in range(nd)])
+
+    if c.get('sutherland', False):
+        cpT = c['gamma']*(rcprho*E - 0.5*np.sum(vel*vel, axis=0))
+        Trat = cpT/c['cpTref']
+        mu = c['mu']*(c['cpTref'] + c['cpTs'])*Trat*np.sqrt(Trat)/(cpT + c['cpTs'])
+    else:
+        mu = c['mu']
+
+    dT = np.array([rcprho*(grad[d, -1] - (rcprho*grad[d, 0]*E +
+                                          sum(vel[i]*dv[i, d] for i in range(nd))))
+                   for d in range(nd)])
+    div = sum(dv[i, i] for i in range(nd))
+    tau = np.empty((nd, nd) + rho.shape)
+    for i in range(nd):
+        tau[i, i] = -2*mu*rcprho*(dv[i, i] - div/3.0)
+        for j in range(i + 1, nd):
+            tau[i, j] = tau[j, i] = -mu*rcprho*(dv[j, i] + dv[i, j])
+
+    f = np.zeros((nd, nv) + rho.shape)
+    for d in range(nd):
+        for i in range(nd):
+            f[d, i + 1] = tau[i, d]
+        f[d, -1] = sum(vel[i]*tau[i, d] for i in range(nd)) \
+            - mu*c['gamma']/c['Pr']*dT[d]
+    return f
+
+
+def rusanov(ul, ur, n, gamma):
+    fl, pl, vl = inviscid_flux(ul, gamma)
+    fr, pr, vr = inviscid_flux(ur, gamma)
+    nv = np.sum(n*(vl + vr), axis=0)
+    a = np.sqrt(0.25*gamma*(pl + pr)/(ul[0] + ur[0])) + 0.25*np.abs(nv)
+    return 0.5*np.einsum('d...,dv...->v...', n, fl + fr) + a*(ul - ur)
+
+
+def hllc(ul, ur, n, gamma):
+    nvars = ul.shape[0]
+    fl, pl, vl = inviscid_flux(ul, gamma)
+    fr, pr, vr = inviscid_flux(ur, gamma)
+    nvl, nvr = np.sum(n*vl, axis=0), np.sum(n*vr, axis=0)
+    al, ar = np.sqrt(gamma*pl/ul[0]), np.sqrt(gamma*pr/ur[0])
+    sql, sqr = np.sqrt(ul[0]), np.sqrt(ur[0])
+    nvroe = (sql*nvl + sqr*nvr)/(sql + sqr)
+    H = (sql*(pr + ur[-1]) + sqr*(pl + ul[-1]))/(sql*ur[0] + sqr*ul[0])
+    va = (vl*sql + vr*sqr)/(sql + sqr)
+    a = np.sqrt((gamma - 1)*(H - 0.5*np.sum(va*va, axis=0)))
+    sl = np.minimum(nvroe - a, nvl - al)
+    sr = np.maximum(nvroe + a, nvr + ar)
+    ss = (pr - pl + ul[0]*nvl*(sl - nvl) - ur[0]*nvr*(sr - nvr)) / \
+         (ul[0]*(sl - nvl) - ur[0]*(sr - nvr))
+    lc, rc = (sl - nvl)/(sl - ss), (sr - nvr)/(sr - ss)
+
+    usl, usr = np.empty_like(ul), np.empty_like(ur)
+    usl[0], usr[0] = lc*ul[0], rc*ur[0]
+    for i in range(nvars - 2):
+        usl[i + 1] = usl[0]*(vl[i] + (ss - nvl)*n[i])
+        usr[i + 1] = usr[0]*(vr[i] + (ss - nvr)*n[i])
+    usl[-1] = lc*(ul[-1] + (ss - nvl)*(ul[0]*ss + pl/(sl - nvl)))
+    usr[-1] = rc*(ur[-1] + (ss - nvr)*(ur[0]*ss + pr/(sr - nvr)))
+
+    nfl = np.einsum('d...,dv...->v...', n, fl)
+    nfr = np.einsum('d...,dv...->v...', n, fr)
+    nfsl = nfl + sl*(usl - ul)
+    nfsr = nfr + sr*(usr - ur)
+    return np.where(0 <= sl, nfl,
+                    np.where((sl <= 0) & (0 <= ss), nfsl,
+                             np.where((ss <= 0) & (0 <= sr), nfsr, nfr)))
+
+
+RSOLVERS = {'rusanov': rusanov, 'hllc': hllc}
+
+
+# ---------------------------------------------------------------------------
+# Geometry of linear elements
+# ---------------------------------------------------------------------------
+
+def vertex_signs(ndims):
+    return np.array([[1.0 if (v >> d) & 1 else -1.0 for d in range(ndims)]
+                     for v in range(2**ndims)])
+
+
+def shape_values(pts, ndims):
+    s = vertex_signs(ndims)
+    return np.prod(1 + pts[:, None, :]*s[None], axis=2)/2**ndims
+
+
+def jacobian(verts, pts):
+    """J[p, i, j, e] = dX_j/dxi_i for linear elements; verts (nv, ne, nd)."""
+    nd = verts.shape[2]
+    s = vertex_signs(nd)
+    dN = np.empty((len(pts), nd, len(s)))
+    for i in range(nd):
+        t = np.ones((len(pts), len(s)))
+        for d in range(nd):
+            t = t*(s[None, :, d] if d == i else 1 + pts[:, None, d]*s[None, :, d])
+        dN[:, i] = t/2**nd
+    return np.einsum('piv,vej->pije', dN, verts)
+
+
+def smats_djac(verts, pts):
+    J = jacobian(verts, pts)
+    nd = J.shape[1]
+    s = np.empty_like(J)
+    if nd == 2:
+        s[:, 0, 0], s[:, 0, 1] = J[:, 1, 1], -J[:, 1, 0]
+        s[:, 1, 0], s[:, 1, 1] = -J[:, 0, 1], J[:, 0, 0]
+        d = s[:, 0, 0]*s[:, 1, 1] - s[:, 0, 1]*s[:, 1, 0]
+    else:
+        for i in range(3):
+            a, b = (i + 1) % 3, (i + 2) % 3
+            s[:, i] = np.cross(J[:, a], J[:, b], axisa=1, axisb=1, axisc=1)
+        d = np.einsum('pje,pje->pe', J[:, 0], s[:, 0])
+    return s, d
+
+
+# ---------------------------------------------------------------------------
+# The discretisation
+# ---------------------------------------------------------------------------
+
+class Discretisation:
+    """Everything the oracle RHS needs for one element type.
+
+    ops: dict with 'M0', 'M132' (= M1 - M3*M2), 'M3', and for NS 'M460'
+    (= M4 - M6*M0), 'M6'; basis: dict with 'upts', 'fpts', 'norm_fpts',
+    'facefpts' (list of index lists); verts: (nverts, neles, ndims);
+    lhs/rhs: arrays (ninters, 2) of (element, face); periods: per-dim
+    period of the mesh (or None).
+    """
+
+    def __init__(self, ops, basis, verts, lhs, rhs, periods=None):
+        self.ops = {k: np.asarray(v, dtype=float) for k, v in ops.items()}
+        self.upts = np.asarray(basis['upts'], dtype=float)
+        self.fpts = np.asarray(basis['fpts'], dtype=float)
+        self.norm_fpts = np.asarray(basis['norm_fpts'], dtype=float)
+        self.facefpts = [np.asarray(f) for f in basis['facefpts']]
+        self.verts = np.asarray(verts, dtype=float)
+        self.nverts, self.neles, self.ndims = self.verts.shape
+        self.nupts, self.nfpts = len(self.upts), len(self.fpts)
+
+        # Metric terms at the solution and flux points
+        self.smats_u, self.djac_u = smats_djac(self.verts, self.upts)
+        s_f, _ = smats_djac(self.verts, self.fpts)
+        # Scaled normals S^T n at the flux points: (nfpts, ndims, neles)
+        self.pnorm = np.einsum('plke,pl->pke', s_f, self.norm_fpts)
+        self.ploc_f = np.einsum('pv,ved->pde',
+                                shape_values(self.fpts, self.ndims), self.verts)
+
+        self._pair(np.asarray(lhs), np.asarray(rhs), periods)
+
+    def _pair(self, lhs, rhs, periods):
+        """Pair the flux points of the two sides of every interface by
+        matching physical coordinates (modulo periods)."""
+        li, ri = [], []
+        for (el, fl), (er, fr) in zip(lhs, rhs):
+            pl = self.facefpts[fl]
+            pr = self.facefpts[fr]
+            xl = self.ploc_f[pl, :, el]
+            xr = self.ploc_f[pr, :, er]
+            d = xl[:, None, :] - xr[None, :, :]
+            if periods is not None:
+                P = np.asarray(periods)
+                d = d - P*np.rint(d/P)
+            match = np.argmin(np.sum(d*d, axis=2), axis=1)
+            if len(set(match.tolist())) != len(pl):
+                raise RuntimeError('Flux points of an interface do not pair')
+            li.extend((p, el) for p in pl)
+            ri.extend((pr[m], er) for m in match)
+
+        self.pl = np.array(li)
+        self.pr = np.array(ri)
+        self.nl = self.pnorm[self.pl[:, 0], :, self.pl[:, 1]].T   # (nd, n)
+
+    # ---- operator applies ---------------------------------------------------
+
+    @staticmethod
+    def apply(op, x):
+        """op (m, k) @ x (k, nvars, neles) -> (m, nvars, neles)."""
+        return np.einsum('mk,kve->mve', op, x)
+
+    def _gather(self, fld, side):
+        p = self.pl if side == 'l' else self.pr
+        return fld[p[:, 0], :, p[:, 1]].T                        # (nvars, n)
+
+    def _scatter(self, fld, side, vals):
+        p = self.pl if side == 'l' else self.pr
+        fld[p[:, 0], :, p[:, 1]] = vals.T
+
+    # ---- right-hand sides ----------------------------------------------------
+
+    def _transform_flux(self, f):
+        # f: (ndims, nupts, nvars, neles) physical -> reference (smats)
+        return np.einsum('pike,kpve->ipve', self.smats_u, f)
+
+    def rhs_euler(self, u, c, rsolver='rusanov'):
+        gamma = c['gamma']
+        nd = self.ndims
+        uf = self.apply(self.ops['M0'], u)
+
+        # Common interface flux (intcflux)
+        ul, ur = self._gather(uf, 'l'), self._gather(uf, 'r')
+        mag = np.sqrt(np.sum(self.nl**2, axis=0))
+        fn = RSOLVERS[rsolver](ul, ur, self.nl/mag, gamma)
+        self._scatter(uf, 'l', mag*fn)
+        self._scatter(uf, 'r', -mag*fn)
+
+        # Transformed flux at the solution points (tflux)
+        fp, _, _ = inviscid_flux(u.transpose(1, 0, 2), gamma)   # (nd, nv, p, e)
+        ft = self._transform_flux(fp.transpose(0, 2, 1, 3))
+
+        r = self.apply(self.ops['M132'], ft.reshape(nd*self.nupts, -1, self.neles))
+        r += self.apply(self.ops['M3'], uf)
+        return -r/self.djac_u[:, None, :]
+
+    def rhs_ns(self, u, c, rsolver='rusanov', grads_out=None):
+        gamma, beta, tau = c['gamma'], c['ldg-beta'], c['ldg-tau']
+        nd, nupts, nfpts, ne = self.ndims, self.nupts, self.nfpts, self.neles
+        uf = self.apply(self.ops['M0'], u)
+
+        # Common solution (intconu) on the flux points
+        ul, ur = self._gather(uf, 'l'), self._gather(uf, 'r')
+        if beta == -0.5:
+            cl, cr = ul, ul
+        elif beta == 0.5:
+            cl, cr = ur, ur
+        else:
+            cl = cr = ur*(0.5 + beta) + ul*(0.5 - beta)
+        comm = uf.copy()
+        self._scatter(comm, 'l', cl)
+        self._scatter(comm, 'r', cr)
+
+        # Corrected reference gradient, transformed to physical space
+        g = self.apply(self.ops['M460'], u) + self.apply(self.ops['M6'], comm)
+        g = g.reshape(nd, nupts, -1, ne)
+        g = np.einsum('pkie,kpve->ipve', self.smats_u, g)/self.djac_u[None, :, None, :]
+        if grads_out is not None:
+            grads_out.append(g)
+
+        # Flux at the solution points
+        ut = u.transpose(1, 0, 2)
+        fi, _, _ = inviscid_flux(ut, gamma)
+        fv = viscous_flux(ut, g.transpose(0, 2, 1, 3), c)
+        ft = self._transform_flux((fi + fv).transpose(0, 2, 1, 3))
+
+        # Physical gradient at the flux points and the common flux
+        gf = np.stack([self.apply(self.ops['M0'], g[d]) for d in range(nd)])
+        # Advanced indices split by a slice put the point axis first
+        gl = gf[:, self.pl[:, 0], :, self.pl[:, 1]].transpose(1, 2, 0)
+        gr = gf[:, self.pr[:, 0], :, self.pr[:, 1]].transpose(1, 2, 0)
+        mag = np.sqrt(np.sum(self.nl**2, axis=0))
+        n = self.nl/mag
+        fic = RSOLVERS[rsolver](ul, ur, n, gamma)
+        fvl = np.einsum('dn,dvn->vn', n, viscous_flux(ul, gl, c))
+        fvr = np.einsum('dn,dvn->vn', n, viscous_flux(ur, gr, c))
+        if beta == -0.5:
+            fvc = fvr
+        elif beta == 0.5:
+            fvc = fvl
+        else:
+            fvc = (0.5 + beta)*fvl + (0.5 - beta)*fvr
+        fvc = fvc + tau*(ul - ur)
+        self._scatter(uf, 'l', mag*(fic + fvc))
+        self._scatter(uf, 'r', -mag*(fic + fvc))
+
+        r = self.apply(self.ops['M132'], ft.reshape(nd*nupts, -1, ne))
+        r += self.apply(self.ops['M3'], uf)
+        return -r/self.djac_u[:, None, :]
+
+
+# ---------------------------------------------------------------------------
+# Time integration
+# ---------------------------------------------------------------------------
+
+RK45_A = [970286171893 / 4311952581923, 6584761158862 / 12103376702013,
+          2251764453980 / 15575788980749, 26877169314380 / 34165994151039]
+RK45_B = [1153189308089 / 22510343858157, 1772645290293 / 4653164025191,
+          -1672844663538 / 4480602732383, 2114624349019 / 3568978502595,
+          5198255086312 / 14908931495163]
+
+
+def rk45_step(rhs, u, dt):
+    """One step of the two-register RK45 scheme (rkvdh2 semantics)."""
+    r1, r2 = u.copy(), u
+    ns = len(RK45_B)
+    for i in range(ns):
+        r2 = rhs(r2 if i else r1)
+        if i < ns - 1:
+            r1, r2 = r1 + dt*RK45_B[i]*r2, r1 + dt*RK45_A[i]*r2
+        else:
+            r1 = r1 + dt*RK45_B[i]*r2
+    return r1

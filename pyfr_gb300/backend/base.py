@@ -1,0 +1,285 @@
+"""The ``b200`` backend: a GB300-native implementation of the reference's
+backend interface (``pyfr/backends/base/backend.py:32-226`` with the
+concrete attributes of ``pyfr/backends/cuda/base.py:9-144``).
+
+One process drives one GPU through the pyfrb200 C ABI.  Matrices are
+allocated in named extents, kernels are obtained from the providers by
+name (``backend.kernel('mul', ...)``, ``backend.kernel('tflux', ...)``),
+and graphs are captured as CUDA graphs.  There is no CPU fallback: if the
+library or the GPU is missing, construction raises.
+"""
+
+from collections import namedtuple
+from contextlib import contextmanager
+import ctypes as C
+import itertools as it
+from weakref import WeakValueDictionary
+
+import numpy as np
+
+from pyfr_gb300.backend import types
+from pyfr_gb300.backend.lib import get_lib, B200Error
+
+
+MemoryInfo = namedtuple('MemoryInfo', ['current', 'peak', 'free', 'total'])
+
+
+class NotSuitableError(Exception):
+    pass
+
+
+def _recordmat(fn):
+    def newfn(self, *args, **kwargs):
+        m = fn(self, *args, **kwargs)
+        if not hasattr(m, 'mid'):
+            m.mid = next(self._mat_counter)
+            self.mats[m.mid] = m
+        return m
+    newfn.__name__ = fn.__name__
+    return newfn
+
+
+class B200Backend:
+    name = 'b200'
+    blocks = False
+    has_double = True
+
+    def __init__(self, cfg):
+        self.cfg = cfg
+
+        prec = cfg.get('backend', 'precision', 'double')
+        if prec not in {'single', 'double'}:
+            raise ValueError('Backend precision must be either single or '
+                             'double')
+        self.fpdtype = np.dtype(prec).type
+        self.fpdtype_eps = float(np.finfo(self.fpdtype).eps)
+        self.fpdtype_max = float(np.finfo(self.fpdtype).max)
+
+        match cfg.get('backend', 'memory-model', 'normal'):
+            case 'normal':
+                self.ixdtype = np.int32
+            case 'large':
+                self.ixdtype = np.int64
+            case _:
+                raise ValueError('Backend memory model must be either normal '
+                                 'or large')
+
+        self.autotune_ifac = cfg.getfloat('backend', 'autotune-ifac', 0.95)
+
+        # Layout constants (as the reference CUDA backend)
+        self.alignb = 128
+        self.soasz = 32
+        self.csubsz = self.soasz
+
+        # Execution options of this backend
+        self.use_cuda_graphs = cfg.getbool('backend-b200', 'cuda-graphs', True)
+        self.fusion = cfg.getbool('backend-b200', 'fusion', True)
+
+        self.mats = WeakValueDictionary()
+        self._mat_counter = it.count()
+        self._extents = {}
+        self._allocs = []
+        self._mem_cur = self._mem_peak = 0
+
+        # Bring up the device
+        self.lib = lib = get_lib()
+        devid = cfg.get('backend-b200', 'device-id', '0')
+        lib.init(int(devid))
+
+        s = C.c_void_p()
+        lib.stream_create(C.byref(s))
+        self._stream = s.value
+
+        self.const_matrix_cls = types.ConstMatrix
+        self.matrix_cls = types.Matrix
+        self.matrix_slice_cls = types.MatrixSlice
+        self.xchg_matrix_cls = types.XchgMatrix
+        self.view_cls = types.View
+        self.xchg_view_cls = types.XchgView
+        self.graph_cls = types.Graph
+        self.ordered_meta_kernel_cls = types.OrderedMetaKernel
+        self.unordered_meta_kernel_cls = types.UnorderedMetaKernel
+
+        from pyfr_gb300.backend import blasext, fused, mul, pointwise
+        self._providers = [pointwise.PointwiseKernelProvider(self),
+                           blasext.BlasExtKernels(self),
+                           mul.MulKernels(self)]
+        self.pointwise = self._providers[0]
+        self._fuser = fused.Fuser(self)
+
+    # ---- device plumbing --------------------------------------------------
+
+    @property
+    def stream(self):
+        return self._stream
+
+    @property
+    def platform_id(self):
+        name = C.create_string_buffer(256)
+        self.lib.device_info(None, None, None, None, None, name, 256)
+        return name.value.decode()
+
+    def _malloc_impl(self, nbytes):
+        p = C.c_void_p()
+        self.lib.malloc(C.byref(p), nbytes)
+        self._allocs.append((p.value, nbytes))
+        self._mem_cur += nbytes
+        self._mem_peak = max(self._mem_peak, self._mem_cur)
+        return p.value
+
+    def memcpy_htod(self, dst, src, nbytes):
+        src = np.ascontiguousarray(src)
+        self.lib.memcpy_htod(dst, src.ctypes.data, nbytes, self._stream)
+        self.lib.stream_sync(self._stream)
+
+    def memcpy_dtoh(self, dst, src, nbytes):
+        self.lib.memcpy_dtoh(dst.ctypes.data, src, nbytes, self._stream)
+        self.lib.stream_sync(self._stream)
+
+    def wait(self):
+        self.lib.stream_sync(self._stream)
+
+    def memory_info(self):
+        f, t = C.c_size_t(), C.c_size_t()
+        self.lib.device_info(None, None, None, C.byref(f), C.byref(t), None, 0)
+        return MemoryInfo(self._mem_cur, self._mem_peak, f.value, t.value)
+
+    def capture(self, launch, stream):
+        self.lib.graph_begin_capture(stream)
+        try:
+            launch(stream)
+        except BaseException:
+            g = C.c_void_p()
+            try:
+                self.lib.graph_end_capture(stream, C.byref(g))
+            except B200Error:
+                pass
+            else:
+                self.lib.graph_destroy(g.value)
+            raise
+        g = C.c_void_p()
+        self.lib.graph_end_capture(stream, C.byref(g))
+        return g.value
+
+    def release_gexec(self, gexec):
+        if gexec:
+            self.lib.graph_destroy(gexec)
+
+    # ---- allocation (pyfr/backends/base/backend.py:94-165) ----------------
+
+    def _extent_alloc_bytes(self, nbytes):
+        return nbytes - (nbytes % -self.alignb)
+
+    def malloc(self, obj, extent):
+        if extent is None:
+            ext = types.Extent()
+            ext.reserve(obj, self._extent_alloc_bytes(obj.nbytes))
+            ext.commit(self._malloc_checked)
+        else:
+            ext = self._extents.setdefault(extent, types.Extent(extent))
+            ext.reserve(obj, self._extent_alloc_bytes(obj.nbytes))
+
+    def commit(self):
+        for ext in self._extents.values():
+            ext.commit(self._malloc_checked)
+        self._extents.clear()
+
+    def _malloc_checked(self, nbytes):
+        if self.ixdtype == np.int32 and nbytes > 4*2**31 - 1:
+            raise RuntimeError('Allocation too large for normal backend '
+                               'memory-model')
+        return self._malloc_impl(nbytes)
+
+    @_recordmat
+    def const_matrix(self, initval, dtype=None, tags=set()):
+        dtype = dtype or self.fpdtype
+        initval = np.asarray(initval)
+
+        # Reuse an identical constant (pyfr/backends/base/backend.py:134-145)
+        for m in list(self.mats.values()):
+            if (isinstance(m, self.const_matrix_cls) and
+                m.dtype == np.dtype(dtype) and m.ioshape == initval.shape and
+                set(tags).issubset(m.tags) and
+                getattr(m, '_host', None) is not None and
+                np.array_equal(m._host, initval)):
+                return m
+
+        m = self.const_matrix_cls(self, dtype, initval, tags)
+        m._host = np.array(initval, dtype=dtype)
+        return m
+
+    @_recordmat
+    def matrix(self, ioshape, initval=None, extent=None, tags=set(),
+               dtype=None):
+        dtype = dtype or self.fpdtype
+        return self.matrix_cls(self, dtype, ioshape, initval, extent, tags)
+
+    @_recordmat
+    def matrix_slice(self, mat, ra, rb, ca, cb):
+        return self.matrix_slice_cls(self, mat, ra, rb, ca, cb)
+
+    @_recordmat
+    def xchg_matrix(self, ioshape, initval=None, extent=None, tags=set()):
+        return self.xchg_matrix_cls(self, self.fpdtype, ioshape, initval,
+                                    extent, tags)
+
+    def xchg_matrix_for_view(self, view, tags=set()):
+        return self.xchg_matrix((view.nvrow, view.nvcol*view.n), tags=tags)
+
+    def view(self, matmap, rmap, cmap, rstridemap=1, vshape=(), tags=set()):
+        return self.view_cls(self, matmap, rmap, cmap, rstridemap, vshape,
+                             tags)
+
+    def xchg_view(self, matmap, rmap, cmap, rstridemap=1, vshape=(),
+                  tags=set()):
+        return self.xchg_view_cls(self, matmap, rmap, cmap, rstridemap,
+                                  vshape, tags)
+
+    # ---- kernels (pyfr/backends/base/backend.py:177-226) ------------------
+
+    @contextmanager
+    def region(self, name):
+        yield
+
+    def kernel(self, name, *args, **kwargs):
+        best = None
+        for prov in self._providers:
+            meth = getattr(prov, name, None)
+            if meth is None:
+                continue
+            try:
+                kern = meth(*args, **kwargs)
+            except NotSuitableError:
+                continue
+
+            if best is None or kern.dt < self.autotune_ifac*best.dt:
+                best = kern
+                if np.isnan(best.dt):
+                    return best
+
+        if best is None:
+            raise KeyError(f'Kernel {name!r} has no providers')
+        return best
+
+    def ordered_meta_kernel(self, kerns):
+        return self.ordered_meta_kernel_cls(kerns)
+
+    def unordered_meta_kernel(self, kerns, splits=None):
+        return self.unordered_meta_kernel_cls(kerns, splits)
+
+    def graph(self):
+        return self.graph_cls(self)
+
+    def fuse(self, klist, groups):
+        return self._fuser.fuse(klist, groups) if self.fusion else klist
+
+    def run_kernels(self, kernels, wait=False):
+        for k in kernels:
+            k.run(self._stream)
+        if wait:
+            self.wait()
+
+    def run_graph(self, graph, wait=False):
+        graph.run(self._stream)
+        if wait:
+            self.wait()

@@ -1,0 +1,133 @@
+"""ctypes binding of the pyfrb200 C ABI (``include/pyfrb200.h``).
+
+Follows the pattern of ``pyfr/ctypesutil.py:8-40`` (LibWrapper): every
+function is declared once with its argument types, and a nonzero status is
+raised as a Python exception carrying the library's last error message.
+There is no fallback: if the shared library is missing or cannot be
+loaded, construction fails.
+"""
+
+import ctypes as C
+from pathlib import Path
+
+LIBPATH = Path(__file__).resolve().parent.parent / '_lib' / 'libpyfrb200.so'
+
+vp, i32, i64, f64, f32, sz = (C.c_void_p, C.c_int, C.c_int64, C.c_double,
+                              C.c_float, C.c_size_t)
+pd, pf = C.POINTER(C.c_double), C.POINTER(C.c_float)
+
+
+class B200Error(RuntimeError):
+    pass
+
+
+class Gas(C.Structure):
+    _fields_ = [('gamma', f64), ('mu', f64), ('pr', f64), ('cpTref', f64),
+                ('cpTs', f64), ('sutherland', i32)]
+
+
+def _sig_pointwise(fp):
+    return {
+        'tflux_euler': [i32, i32, i64, i32, f64, vp, i64, vp, i64, vp, i64, vp,
+                        i64, vp, i64, vp],
+        'tflux_ns': [i32, i32, i64, i32, C.POINTER(Gas), vp, i64, vp, i64, vp,
+                     i64, vp, i64, vp, i64, vp, i64, vp, i64, vp],
+        'gradcoru': [i32, i32, i64, i32, vp, i64, vp, i64, vp, i64, vp, i64,
+                     vp, i64, vp],
+        'negdivconf': [i32, i32, i64, vp, i64, vp, i64, vp],
+        'intcflux_euler': [i32, i64, i32, f64, vp, vp, vp, vp, i32, vp, i64,
+                           vp],
+        'intcflux_ns': [i32, i64, i32, C.POINTER(Gas), f64, f64, vp, vp, vp,
+                        vp, vp, vp, vp, vp, vp, vp, i32, vp, i64, vp],
+        'intconu': [i32, i64, f64, vp, vp, vp, vp, vp, vp, vp, vp, i32, vp],
+        'rkvdh2': [i64, i32, i32, i32, f64, f64, f64, f64, vp, vp, vp, vp, vp],
+        'axnpby': [i64, i32, vp, C.POINTER(vp), C.POINTER(f64), vp],
+        'errest': [i32, i32, i64, i64, vp, vp, vp, f64, i32, vp, i32, vp, vp],
+        'mul': [vp, vp, i64, vp, i64, i64, fp, fp, vp],
+    }
+
+
+_SIGS = {
+    'b200_init': [i32],
+    'b200_get_last_error': [C.c_char_p, sz],
+    'b200_device_info': [C.POINTER(i32), C.POINTER(i32), C.POINTER(i32),
+                         C.POINTER(sz), C.POINTER(sz), C.c_char_p, sz],
+    'b200_malloc': [C.POINTER(vp), sz],
+    'b200_free': [vp],
+    'b200_host_alloc': [C.POINTER(vp), sz],
+    'b200_host_free': [vp],
+    'b200_memset': [vp, i32, sz, vp],
+    'b200_memcpy_htod': [vp, vp, sz, vp],
+    'b200_memcpy_dtoh': [vp, vp, sz, vp],
+    'b200_memcpy_dtod': [vp, vp, sz, vp],
+    'b200_stream_create': [C.POINTER(vp)],
+    'b200_stream_destroy': [vp],
+    'b200_stream_sync': [vp],
+    'b200_device_sync': [],
+    'b200_event_create': [C.POINTER(vp)],
+    'b200_event_destroy': [vp],
+    'b200_event_record': [vp, vp],
+    'b200_event_sync': [vp],
+    'b200_event_elapsed': [C.POINTER(f32), vp, vp],
+    'b200_graph_begin_capture': [vp],
+    'b200_graph_end_capture': [vp, C.POINTER(vp)],
+    'b200_graph_launch': [vp, vp],
+    'b200_graph_destroy': [vp],
+    'b200_mul_create': [pd, i32, i32, C.POINTER(vp)],
+    'b200_mul_nnz': [vp, C.POINTER(i32)],
+    'b200_mul_destroy': [vp],
+}
+
+for _fp, _suf in ((f64, 'f64'), (f32, 'f32')):
+    for _name, _args in _sig_pointwise(_fp).items():
+        _SIGS[f'b200_{_name}_{_suf}'] = _args
+
+
+def exported_symbols():
+    """Names of every entry point the Python side binds."""
+    return sorted(_SIGS) + ['b200_version']
+
+
+class Lib:
+    """Loaded library with status-checked entry points as attributes
+    (``lib.mul_f64(...)`` calls ``b200_mul_f64``)."""
+
+    def __init__(self, path=LIBPATH):
+        if not Path(path).exists():
+            raise B200Error(f'pyfrb200 library not built: {path} is missing '
+                            '(run __graft_entry__.build())')
+
+        self._lib = lib = C.CDLL(str(path))
+        lib.b200_version.restype = C.c_char_p
+        lib.b200_version.argtypes = []
+        self.version = lib.b200_version().decode()
+
+        for name, args in _SIGS.items():
+            fn = getattr(lib, name)
+            fn.argtypes = args
+            fn.restype = C.c_int
+            setattr(self, name.removeprefix('b200_'), self._wrap(name, fn))
+
+    def _wrap(self, name, fn):
+        def call(*args):
+            rc = fn(*args)
+            if rc:
+                raise B200Error(f'{name} failed (status {rc}): '
+                                f'{self.last_error()}')
+        call.__name__ = name
+        return call
+
+    def last_error(self):
+        buf = C.create_string_buffer(512)
+        self._lib.b200_get_last_error(buf, 512)
+        return buf.value.decode(errors='replace')
+
+
+_LIB = None
+
+
+def get_lib():
+    global _LIB
+    if _LIB is None:
+        _LIB = Lib()
+    return _LIB

@@ -1,0 +1,270 @@
+"""Pointwise kernel provider of the ``b200`` backend.
+
+The reference renders a Mako template per kernel module and compiles it at
+run time (``pyfr/backends/base/provider.py:173-206``).  Here every module
+on the right-hand-side path maps to a hand-written CUDA kernel of the
+pyfrb200 library; ``register(modpath)`` exposes the kernel that module
+defines under its name, and calling it takes the same arguments as the
+reference's generated kernel: ``name(tplargs, dims, extrns={}, **args)``.
+Scalar arguments that are not supplied become runtime-bindable
+(``rtnames``), as with ``pyfr/backends/base/provider.py:134-141``.
+"""
+
+import ctypes as C
+
+import numpy as np
+
+from pyfr_gb300.backend.lib import Gas
+from pyfr_gb300.backend.types import BindableKernel, Kernel, NullKernel
+
+RSOLVERS = {'rusanov': 0, 'hllc': 1}
+
+
+def _gas(c, visc_corr='none'):
+    return Gas(gamma=c['gamma'], mu=c.get('mu', 0.0), pr=c.get('Pr', 1.0),
+               cpTref=c.get('cpTref', 1.0), cpTs=c.get('cpTs', 1.0),
+               sutherland=int(visc_corr == 'sutherland'))
+
+
+def _mat(m):
+    """(device pointer, leading dimension) of a matrix argument."""
+    if m is None:
+        return None, 0
+    return m.data, m.leaddim
+
+
+def _view(v):
+    """(base pointer, map pointer, row-stride pointer) of a view."""
+    return (v.basedata, v.mapping.data,
+            v.rstrides.data if v.rstrides is not None else None)
+
+
+class PointwiseKernelProvider:
+    def __init__(self, backend):
+        self.backend = backend
+        self._registered = {}
+
+    @property
+    def _sfx(self):
+        return 'f64' if self.backend.fpdtype == np.float64 else 'f32'
+
+    def _fn(self, name):
+        return getattr(self.backend.lib, f'{name}_{self._sfx}')
+
+    @property
+    def _ix64(self):
+        return int(self.backend.ixdtype == np.int64)
+
+    def register(self, mod):
+        """Expose the kernel defined by reference module ``mod``."""
+        name = mod.rsplit('.', 1)[-1]
+        builder = _BUILDERS.get(mod)
+
+        def kernel_meth(tplargs, dims, extrns={}, **kwargs):
+            if builder is None:
+                raise NotImplementedError(
+                    f'Kernel {name!r} of {mod} is not provided by the b200 '
+                    'backend')
+            return builder(self, tplargs, dims, extrns, **kwargs)
+
+        self._registered[name] = mod
+        setattr(self, name, kernel_meth)
+
+    # ---- element kernels ---------------------------------------------------
+
+    def _geom(self, tplargs, smats=None, rcpdjac=None, verts=None, upts=None):
+        linear = 'linear' in tplargs.get('ktype', 'curved')
+        if linear:
+            return 1, (None, 0), (None, 0), _mat(verts), _mat(upts)
+        return 0, _mat(smats), _mat(rcpdjac), (None, 0), (None, 0)
+
+    def _tflux_euler(self, tplargs, dims, extrns, u, f, smats=None,
+                     verts=None, upts=None):
+        nupts, neles = dims
+        lin, (sp, sl), _, (vp, vl), (upp, upl) = self._geom(
+            tplargs, smats=smats, verts=verts, upts=upts)
+        fn, gamma = self._fn('tflux_euler'), tplargs['c']['gamma']
+        up, ul = _mat(u)
+        fp, fl = _mat(f)
+        nd = tplargs['ndims']
+
+        def run(stream):
+            fn(nd, nupts, neles, lin, gamma, up, ul, fp, fl, sp, sl, vp, vl,
+               upp, upl, stream)
+
+        return Kernel(run, mats=[u, f, smats, verts, upts], name='tflux',
+                      meta=dict(kind='tflux_euler', tplargs=tplargs,
+                                dims=dims, u=u, f=f, smats=smats,
+                                verts=verts, upts=upts))
+
+    def _tflux_ns(self, tplargs, dims, extrns, u, f, gradu=None, smats=None,
+                  rcpdjac=None, verts=None, upts=None, artvisc_vtx=None):
+        if tplargs.get('shock_capturing', 'none') not in (None, 'none'):
+            raise NotImplementedError('Artificial viscosity is not supported')
+        if 'fused' not in tplargs.get('ktype', ''):
+            raise NotImplementedError('Only the fused gradient/flux form of '
+                                      'the Navier-Stokes flux is provided')
+
+        nupts, neles = dims
+        lin, (sp, sl), (rp, rl), (vp, vl), (upp, upl) = self._geom(
+            tplargs, smats, rcpdjac, verts, upts)
+        gas = _gas(tplargs['c'], tplargs.get('visc_corr', 'none'))
+        fn, nd = self._fn('tflux_ns'), tplargs['ndims']
+        up, ul = _mat(u)
+        fp, fl = _mat(f)
+        gp, gl = _mat(gradu)
+
+        def run(stream):
+            fn(nd, nupts, neles, lin, C.byref(gas), up, ul, fp, fl, gp, gl,
+               sp, sl, rp, rl, vp, vl, upp, upl, stream)
+
+        return Kernel(run, mats=[u, f, gradu, smats, rcpdjac, verts, upts],
+                      misc=[gas], name='tflux',
+                      meta=dict(kind='tflux_ns', tplargs=tplargs, dims=dims,
+                                u=u, f=f, gradu=gradu, smats=smats,
+                                rcpdjac=rcpdjac, verts=verts, upts=upts))
+
+    def _gradcoru(self, tplargs, dims, extrns, gradu, smats=None,
+                  rcpdjac=None, verts=None, upts=None):
+        nupts, neles = dims
+        lin, (sp, sl), (rp, rl), (vp, vl), (upp, upl) = self._geom(
+            tplargs, smats, rcpdjac, verts, upts)
+        fn, nd = self._fn('gradcoru'), tplargs['ndims']
+        gp, gl = _mat(gradu)
+
+        def run(stream):
+            fn(nd, nupts, neles, lin, gp, gl, sp, sl, rp, rl, vp, vl, upp,
+               upl, stream)
+
+        return Kernel(run, mats=[gradu, smats, rcpdjac, verts, upts],
+                      name='gradcoru',
+                      meta=dict(kind='gradcoru', tplargs=tplargs, dims=dims,
+                                gradu=gradu))
+
+    def _negdivconf(self, tplargs, dims, extrns, tdivtconf, rcpdjac,
+                    ploc=None, u=None, **kw):
+        if tplargs.get('src_macros'):
+            raise NotImplementedError('Source terms are not supported')
+
+        nupts, neles = dims
+        fn, nv = self._fn('negdivconf'), tplargs['nvars']
+        tp, tl = _mat(tdivtconf)
+        rp, rl = _mat(rcpdjac)
+
+        # `t` is accepted (and ignored) as the reference binds it at run time
+        def run(stream, t=None):
+            fn(nv, nupts, neles, tp, tl, rp, rl, stream)
+
+        return BindableKernel(run, ['t'], {'t': kw.get('t', 0.0)},
+                              mats=[tdivtconf, rcpdjac], name='negdivconf',
+                              meta=dict(kind='negdivconf', tplargs=tplargs,
+                                        dims=dims, tdivtconf=tdivtconf,
+                                        rcpdjac=rcpdjac))
+
+    def _evalsrcmacros(self, tplargs, dims, extrns, **kw):
+        if tplargs.get('src_macros'):
+            raise NotImplementedError('Source terms are not supported')
+        return NullKernel()
+
+    # ---- interface kernels ---------------------------------------------------
+
+    def _intcflux_euler(self, tplargs, dims, extrns, ul, ur, nl):
+        (n,) = dims
+        rs = RSOLVERS[tplargs['rsolver']]
+        fn, nd, gamma = (self._fn('intcflux_euler'), tplargs['ndims'],
+                         tplargs['c']['gamma'])
+        lb, lm, _ = _view(ul)
+        rb, rm, _ = _view(ur)
+        np_, nlp = _mat(nl)
+        ix64 = self._ix64
+
+        def run(stream):
+            fn(nd, n, rs, gamma, lb, lm, rb, rm, ix64, np_, nlp, stream)
+
+        return Kernel(run, mats=[nl], views=[ul, ur], name='intcflux',
+                      meta=dict(kind='intcflux_euler', tplargs=tplargs,
+                                dims=dims, ul=ul, ur=ur, nl=nl))
+
+    def _intcflux_ns(self, tplargs, dims, extrns, ul, ur, gradul, gradur, nl,
+                     artvisc=None):
+        if artvisc is not None:
+            raise NotImplementedError('Artificial viscosity is not supported')
+
+        (n,) = dims
+        c = tplargs['c']
+        rs = RSOLVERS[tplargs['rsolver']]
+        gas = _gas(c, tplargs.get('visc_corr', 'none'))
+        beta, tau = c['ldg-beta'], c['ldg-tau']
+        fn, nd = self._fn('intcflux_ns'), tplargs['ndims']
+        lb, lm, _ = _view(ul)
+        rb, rm, _ = _view(ur)
+        glb, glm, glr = _view(gradul)
+        grb, grm, grr = _view(gradur)
+        np_, nlp = _mat(nl)
+        ix64 = self._ix64
+
+        def run(stream):
+            fn(nd, n, rs, C.byref(gas), beta, tau, lb, lm, rb, rm, glb, glm,
+               glr, grb, grm, grr, ix64, np_, nlp, stream)
+
+        return Kernel(run, mats=[nl], views=[ul, ur, gradul, gradur],
+                      misc=[gas], name='intcflux',
+                      meta=dict(kind='intcflux_ns', tplargs=tplargs,
+                                dims=dims))
+
+    def _intconu(self, tplargs, dims, extrns, ulin, urin, ulout, urout):
+        (n,) = dims
+        beta = tplargs['c']['ldg-beta']
+        fn, nv = self._fn('intconu'), tplargs['nvars']
+        a = [_view(v)[:2] for v in (ulin, urin, ulout, urout)]
+        ix64 = self._ix64
+
+        def run(stream):
+            fn(nv, n, beta, *a[0], *a[1], *a[2], *a[3], ix64, stream)
+
+        return Kernel(run, views=[ulin, urin, ulout, urout], name='intconu',
+                      meta=dict(kind='intconu', tplargs=tplargs, dims=dims))
+
+    # ---- integrator kernels ----------------------------------------------------
+
+    def _rkvdh2(self, tplargs, dims, extrns, r1, r2, rold=None, rerr=None,
+                dt=None):
+        stage, nstages = tplargs['stage'], tplargs['nstages']
+        errest = bool(tplargs['errest'])
+        a = tplargs['a'][stage] if stage < nstages - 1 else 0.0
+        b = tplargs['b'][stage]
+        e = tplargs['e'][stage] if errest else 0.0
+        n = r1.nrow*r1.leaddim
+        fn = self._fn('rkvdh2')
+        p1, p2 = r1.data, r2.data
+        po = rold.data if rold is not None else None
+        pe = rerr.data if rerr is not None else None
+
+        def run(stream, dt):
+            fn(n, stage, nstages, int(errest), dt, a, b, e, p1, p2, po, pe,
+               stream)
+
+        return BindableKernel(run, ['dt'], {'dt': dt if dt is not None
+                                            else 0.0},
+                              mats=[r1, r2, rold, rerr], name='rkvdh2',
+                              meta=dict(kind='rkvdh2', tplargs=tplargs,
+                                        dims=dims, r1=r1, r2=r2))
+
+
+_BUILDERS = {
+    'pyfr.solvers.euler.kernels.tflux': PointwiseKernelProvider._tflux_euler,
+    'pyfr.solvers.navstokes.kernels.tflux': PointwiseKernelProvider._tflux_ns,
+    'pyfr.solvers.baseadvecdiff.kernels.gradcoru':
+        PointwiseKernelProvider._gradcoru,
+    'pyfr.solvers.baseadvec.kernels.negdivconf':
+        PointwiseKernelProvider._negdivconf,
+    'pyfr.solvers.baseadvec.kernels.evalsrcmacros':
+        PointwiseKernelProvider._evalsrcmacros,
+    'pyfr.solvers.euler.kernels.intcflux':
+        PointwiseKernelProvider._intcflux_euler,
+    'pyfr.solvers.navstokes.kernels.intcflux':
+        PointwiseKernelProvider._intcflux_ns,
+    'pyfr.solvers.navstokes.kernels.intconu': PointwiseKernelProvider._intconu,
+    'pyfr.integrators.explicit.kernels.rkvdh2':
+        PointwiseKernelProvider._rkvdh2,
+}

@@ -1,0 +1,206 @@
+// Register-level kernels of the time integrator:
+//   rkvdh2    two-register low-storage RK stage update with optional
+//             embedded error accumulation
+//             (pyfr/integrators/explicit/kernels/rkvdh2.mako:4-31)
+//   axnpby    x0 <- a0*x0 + sum_i a_i*x_i
+//             (pyfr/backends/cuda/kernels/axnpby.mako:4-44)
+//   errest    sum (or max) over all solution points of
+//             (err / (atol_v + rtol*|curr|))^2, the error norm of the PI
+//             controller (pyfr/integrators/controllers.py:105-117), reduced
+//             deterministically in FP64 (fixed block partials, then one
+//             ordered final pass).
+// The register kernels treat the whole allocation (rows x leading
+// dimension, padding included) as a flat array: the padding columns of
+// every register stay exactly zero, so updating them is harmless.
+#include "common.cuh"
+#include "../../include/pyfrb200.h"
+
+namespace {
+
+constexpr int BX_BLOCK = 256;
+constexpr int MAX_AXNPBY = 8;
+
+template <typename T>
+__global__ void __launch_bounds__(BX_BLOCK)
+rkvdh2_kernel(int64_t n, int last, int errest, int first, T dta, T dtb, T dte,
+              T *__restrict__ r1, T *__restrict__ r2, T *__restrict__ rold,
+              T *__restrict__ rerr) {
+    for (int64_t i = (int64_t)blockIdx.x * BX_BLOCK + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * BX_BLOCK) {
+        const T t1 = r1[i], t2 = r2[i];
+        if (errest) {
+            if (first) {
+                rerr[i] = dte * t2;
+                rold[i] = t1;
+            } else {
+                rerr[i] = rerr[i] + dte * t2;
+            }
+        }
+        if (!last) {
+            r1[i] = t1 + dta * t2;
+            r2[i] = t1 + dtb * t2;
+        } else {
+            r1[i] = t1 + dtb * t2;
+        }
+    }
+}
+
+template <typename T>
+struct AxnpbyArgs {
+    const T *x[MAX_AXNPBY];
+    T a[MAX_AXNPBY];
+};
+
+template <typename T>
+__global__ void __launch_bounds__(BX_BLOCK)
+axnpby_kernel(int64_t n, int nv, T *__restrict__ x0, AxnpbyArgs<T> args) {
+    const T a0 = args.a[0];
+    for (int64_t i = (int64_t)blockIdx.x * BX_BLOCK + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * BX_BLOCK) {
+        T acc = 0;
+        for (int k = 1; k < nv; k++) acc += args.a[k] * args.x[k][i];
+        if (a0 == T(0))
+            x0[i] = acc;
+        else if (a0 == T(1))
+            x0[i] += acc;
+        else
+            x0[i] = a0 * x0[i] + acc;
+    }
+}
+
+// Block partials of the error norm over the valid points of one element
+// type; layout (nupts, nvars, neles) AoSoA with leading dimension ld.
+template <typename T>
+__global__ void __launch_bounds__(BX_BLOCK)
+errest_partial_kernel(int nupts, int nvars, int64_t neles, int64_t ld, const T *__restrict__ curr,
+                      const T *__restrict__ err, const double *__restrict__ atol, double rtol,
+                      int uniform, double *__restrict__ partial) {
+    __shared__ double red[BX_BLOCK / 32];
+    const int64_t npts = (int64_t)nupts * neles;
+    double acc = 0;
+    for (int64_t p = (int64_t)blockIdx.x * BX_BLOCK + threadIdx.x; p < npts;
+         p += (int64_t)gridDim.x * BX_BLOCK) {
+        const int upt = (int)(p / neles);
+        const int64_t e = p % neles;
+        for (int v = 0; v < nvars; v++) {
+            const int64_t ix = upt * ld + b200::soa_off(e, v, nvars);
+            const double q = (double)err[ix] / (atol[v] + rtol * fabs((double)curr[ix]));
+            acc = uniform ? fmax(acc, fabs(q)) : acc + q * q;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const double y = __shfl_xor_sync(0xffffffffu, acc, o);
+        acc = uniform ? fmax(acc, y) : acc + y;
+    }
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = red[0];
+        for (int w = 1; w < BX_BLOCK / 32; w++) s = uniform ? fmax(s, red[w]) : s + red[w];
+        partial[blockIdx.x] = s;
+    }
+}
+
+__global__ void errest_final_kernel(int nblk, int uniform, const double *__restrict__ partial,
+                                    double *__restrict__ out) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double s = 0;
+        for (int i = 0; i < nblk; i++) s = uniform ? fmax(s, partial[i]) : s + partial[i];
+        out[0] = s;
+    }
+}
+
+unsigned grid_for(int64_t n) {
+    int64_t g = (n + BX_BLOCK - 1) / BX_BLOCK;
+    const int64_t cap = 152 * 16;
+    return (unsigned)(g < 1 ? 1 : (g > cap ? cap : g));
+}
+
+template <typename T>
+int rkvdh2(int64_t n, int stage, int nstages, int errest, double dt, double a, double b,
+           double e, T *r1, T *r2, T *rold, T *rerr, cudaStream_t s) {
+    if (n <= 0) return B200_OK;
+    if (stage < 0 || stage >= nstages)
+        return b200::set_error(B200_ERR_ARG, "rkvdh2: stage %d out of range", stage);
+    if (errest && (!rold || !rerr))
+        return b200::set_error(B200_ERR_ARG, "rkvdh2: error estimate needs rold and rerr");
+    rkvdh2_kernel<T><<<grid_for(n), BX_BLOCK, 0, s>>>(
+        n, stage == nstages - 1, errest, stage == 0, (T)(dt * a), (T)(dt * b), (T)(dt * e), r1,
+        r2, rold, rerr);
+    B200_CHECK_LAUNCH("rkvdh2");
+    return B200_OK;
+}
+
+template <typename T>
+int axnpby(int64_t n, int nv, T *x0, const T *const *xs, const double *a, cudaStream_t s) {
+    if (n <= 0) return B200_OK;
+    if (nv < 1 || nv > MAX_AXNPBY)
+        return b200::set_error(B200_ERR_ARG, "axnpby: nv=%d out of range", nv);
+    AxnpbyArgs<T> args = {};
+    for (int k = 0; k < nv; k++) {
+        args.x[k] = k ? xs[k] : x0;
+        args.a[k] = (T)a[k];
+    }
+    axnpby_kernel<T><<<grid_for(n), BX_BLOCK, 0, s>>>(n, nv, x0, args);
+    B200_CHECK_LAUNCH("axnpby");
+    return B200_OK;
+}
+
+template <typename T>
+int errest(int nupts, int nvars, int64_t neles, int64_t ld, const T *curr, const T *err,
+           const double *atol_dev, double rtol, int uniform, double *scratch, int nscratch,
+           double *out, cudaStream_t s) {
+    if (nscratch < 1) return b200::set_error(B200_ERR_ARG, "errest: no scratch");
+    int64_t g = ((int64_t)nupts * neles + BX_BLOCK - 1) / BX_BLOCK;
+    int nblk = (int)(g < 1 ? 1 : (g > nscratch ? nscratch : g));
+    errest_partial_kernel<T><<<nblk, BX_BLOCK, 0, s>>>(nupts, nvars, neles, ld, curr, err,
+                                                       atol_dev, rtol, uniform, scratch);
+    B200_CHECK_LAUNCH("errest_partial");
+    errest_final_kernel<<<1, 32, 0, s>>>(nblk, uniform, scratch, out);
+    B200_CHECK_LAUNCH("errest_final");
+    return B200_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int b200_rkvdh2_f64(int64_t n, int stage, int nstages, int errest, double dt, double a,
+                    double b, double e, double *r1, double *r2, double *rold, double *rerr,
+                    void *stream) {
+    return rkvdh2<double>(n, stage, nstages, errest, dt, a, b, e, r1, r2, rold, rerr,
+                          (cudaStream_t)stream);
+}
+
+int b200_rkvdh2_f32(int64_t n, int stage, int nstages, int errest, double dt, double a,
+                    double b, double e, float *r1, float *r2, float *rold, float *rerr,
+                    void *stream) {
+    return rkvdh2<float>(n, stage, nstages, errest, dt, a, b, e, r1, r2, rold, rerr,
+                         (cudaStream_t)stream);
+}
+
+int b200_axnpby_f64(int64_t n, int nv, double *x0, const double *const *xs, const double *a,
+                    void *stream) {
+    return axnpby<double>(n, nv, x0, xs, a, (cudaStream_t)stream);
+}
+
+int b200_axnpby_f32(int64_t n, int nv, float *x0, const float *const *xs, const double *a,
+                    void *stream) {
+    return axnpby<float>(n, nv, x0, xs, a, (cudaStream_t)stream);
+}
+
+int b200_errest_f64(int nupts, int nvars, int64_t neles, int64_t ld, const double *curr,
+                    const double *err, const double *atol_dev, double rtol, int uniform,
+                    double *scratch, int nscratch, double *out, void *stream) {
+    return errest<double>(nupts, nvars, neles, ld, curr, err, atol_dev, rtol, uniform, scratch,
+                          nscratch, out, (cudaStream_t)stream);
+}
+
+int b200_errest_f32(int nupts, int nvars, int64_t neles, int64_t ld, const float *curr,
+                    const float *err, const double *atol_dev, double rtol, int uniform,
+                    double *scratch, int nscratch, double *out, void *stream) {
+    return errest<float>(nupts, nvars, neles, ld, curr, err, atol_dev, rtol, uniform, scratch,
+                         nscratch, out, (cudaStream_t)stream);
+}
+
+}  // extern "C"

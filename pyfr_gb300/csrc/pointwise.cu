@@ -1,0 +1,600 @@
+// Pointwise and interface kernels of the right-hand side.
+//
+// Element kernels run over [nupts, neles] (one thread per solution point,
+// consecutive threads on consecutive elements, so every access to an AoSoA
+// field is a coalesced 32-element segment).  Interface kernels run over the
+// interior flux-point pairs and reach both sides through the view gather
+// maps (element offsets into the flux-point buffer, variable stride 32),
+// the addressing of pyfr/backends/base/types.py:260-320.
+//
+//   tflux (Euler)      pyfr/solvers/euler/kernels/tflux.mako:8-30
+//   tflux (NS, fused)  pyfr/solvers/navstokes/kernels/tflux.mako:13-50
+//   gradcoru           pyfr/solvers/baseadvecdiff/kernels/gradcoru.mako:10-24
+//   negdivconf         pyfr/solvers/baseadvec/kernels/negdivconf.mako:7-22
+//   intcflux (Euler)   pyfr/solvers/euler/kernels/intcflux.mako:6-22
+//   intcflux (NS)      pyfr/solvers/navstokes/kernels/intcflux.mako:10-54
+//   intconu            pyfr/solvers/navstokes/kernels/intconu.mako:4-19
+#include "common.cuh"
+#include "physics.cuh"
+#include "../../include/pyfrb200.h"
+
+using b200::Gas;
+using b200::soa_off;
+
+namespace {
+
+constexpr int PW_BLOCK = 128;
+
+template <typename T>
+struct ElemGeom {
+    const T *smats;  int64_t lds;
+    const T *rcpdjac; int64_t ldr;
+    const T *verts;  int64_t ldv;
+    const T *upts;   int64_t ldup;
+    int linear;
+};
+
+// Metric terms at solution point `upt` of element `e`: from the vertices
+// (linear elements) or from the stored per-point smats and 1/|J|.
+template <int ND, typename T>
+__device__ __forceinline__ void elem_metrics(const ElemGeom<T> &g, int nupts, int upt,
+                                             int64_t e, T s[ND][ND], T &rcpdjac,
+                                             bool need_rcp) {
+    if (g.linear) {
+        T V[1 << ND][ND], x[ND], d;
+#pragma unroll
+        for (int v = 0; v < (1 << ND); v++)
+#pragma unroll
+            for (int k = 0; k < ND; k++) V[v][k] = g.verts[v * g.ldv + soa_off(e, k, ND)];
+#pragma unroll
+        for (int k = 0; k < ND; k++) x[k] = g.upts[upt * g.ldup + k];
+        b200::linear_smats<ND, T>(V, x, s, d);
+        rcpdjac = need_rcp ? T(1) / d : T(0);
+    } else {
+#pragma unroll
+        for (int i = 0; i < ND; i++)
+#pragma unroll
+            for (int j = 0; j < ND; j++)
+                s[i][j] = g.smats[(int64_t)(i * nupts + upt) * g.lds + soa_off(e, j, ND)];
+        rcpdjac = need_rcp ? g.rcpdjac[(int64_t)upt * g.ldr + e] : T(0);
+    }
+}
+
+template <int ND, typename T>
+__global__ void __launch_bounds__(PW_BLOCK)
+tflux_euler_kernel(int nupts, int64_t neles, T gamma, const T *__restrict__ u, int64_t ldu,
+                   T *__restrict__ f, int64_t ldf, ElemGeom<T> geo) {
+    constexpr int NV = ND + 2;
+    const int64_t e = (int64_t)blockIdx.x * PW_BLOCK + threadIdx.x;
+    const int upt = blockIdx.y;
+    if (e >= neles) return;
+
+    T s[ND][ND], rcp;
+    elem_metrics<ND, T>(geo, nupts, upt, e, s, rcp, false);
+
+    T uu[NV];
+#pragma unroll
+    for (int v = 0; v < NV; v++) uu[v] = u[upt * ldu + soa_off(e, v, NV)];
+
+    T ft[ND][NV], p, vel[ND];
+    b200::inviscid_flux<ND, T>(uu, ft, p, vel, gamma);
+
+#pragma unroll
+    for (int i = 0; i < ND; i++)
+#pragma unroll
+        for (int j = 0; j < NV; j++) {
+            T acc = 0;
+#pragma unroll
+            for (int k = 0; k < ND; k++) acc += s[i][k] * ft[k][j];
+            f[(int64_t)(i * nupts + upt) * ldf + soa_off(e, j, NV)] = acc;
+        }
+}
+
+template <int ND, typename T>
+__global__ void __launch_bounds__(PW_BLOCK)
+tflux_ns_kernel(int nupts, int64_t neles, Gas gas, const T *__restrict__ u, int64_t ldu,
+                T *__restrict__ f, int64_t ldf, T *__restrict__ gradu, int64_t ldg,
+                ElemGeom<T> geo) {
+    constexpr int NV = ND + 2;
+    const int64_t e = (int64_t)blockIdx.x * PW_BLOCK + threadIdx.x;
+    const int upt = blockIdx.y;
+    if (e >= neles) return;
+
+    T s[ND][ND], rcp;
+    elem_metrics<ND, T>(geo, nupts, upt, e, s, rcp, true);
+
+    // Transform the corrected reference gradient to physical space, in place
+    T tg[ND][NV], gr[ND][NV];
+#pragma unroll
+    for (int d = 0; d < ND; d++)
+#pragma unroll
+        for (int v = 0; v < NV; v++) tg[d][v] = gradu[(int64_t)(d * nupts + upt) * ldg + soa_off(e, v, NV)];
+#pragma unroll
+    for (int i = 0; i < ND; i++)
+#pragma unroll
+        for (int j = 0; j < NV; j++) {
+            T acc = 0;
+#pragma unroll
+            for (int k = 0; k < ND; k++) acc += s[k][i] * tg[k][j];
+            gr[i][j] = rcp * acc;
+            gradu[(int64_t)(i * nupts + upt) * ldg + soa_off(e, j, NV)] = gr[i][j];
+        }
+
+    T uu[NV];
+#pragma unroll
+    for (int v = 0; v < NV; v++) uu[v] = u[upt * ldu + soa_off(e, v, NV)];
+
+    T ft[ND][NV], p, vel[ND];
+    b200::inviscid_flux<ND, T>(uu, ft, p, vel, T(gas.gamma));
+    b200::viscous_flux_add<ND, T>(uu, gr, ft, gas);
+
+#pragma unroll
+    for (int i = 0; i < ND; i++)
+#pragma unroll
+        for (int j = 0; j < NV; j++) {
+            T acc = 0;
+#pragma unroll
+            for (int k = 0; k < ND; k++) acc += s[i][k] * ft[k][j];
+            f[(int64_t)(i * nupts + upt) * ldf + soa_off(e, j, NV)] = acc;
+        }
+}
+
+template <int ND, typename T>
+__global__ void __launch_bounds__(PW_BLOCK)
+gradcoru_kernel(int nupts, int64_t neles, T *__restrict__ gradu, int64_t ldg, ElemGeom<T> geo) {
+    constexpr int NV = ND + 2;
+    const int64_t e = (int64_t)blockIdx.x * PW_BLOCK + threadIdx.x;
+    const int upt = blockIdx.y;
+    if (e >= neles) return;
+
+    T s[ND][ND], rcp;
+    elem_metrics<ND, T>(geo, nupts, upt, e, s, rcp, true);
+
+    T tg[ND][NV];
+#pragma unroll
+    for (int d = 0; d < ND; d++)
+#pragma unroll
+        for (int v = 0; v < NV; v++) tg[d][v] = gradu[(int64_t)(d * nupts + upt) * ldg + soa_off(e, v, NV)];
+#pragma unroll
+    for (int i = 0; i < ND; i++)
+#pragma unroll
+        for (int j = 0; j < NV; j++) {
+            T acc = 0;
+#pragma unroll
+            for (int k = 0; k < ND; k++) acc += s[k][i] * tg[k][j];
+            gradu[(int64_t)(i * nupts + upt) * ldg + soa_off(e, j, NV)] = rcp * acc;
+        }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(PW_BLOCK)
+negdivconf_kernel(int nvars, int64_t neles, T *__restrict__ r, int64_t ldr,
+                  const T *__restrict__ rcpdjac, int64_t ldj) {
+    const int64_t e = (int64_t)blockIdx.x * PW_BLOCK + threadIdx.x;
+    const int upt = blockIdx.y;
+    if (e >= neles) return;
+    const T rj = rcpdjac[(int64_t)upt * ldj + e];
+    for (int v = 0; v < nvars; v++) {
+        T *p = r + upt * ldr + soa_off(e, v, nvars);
+        *p = -rj * *p;
+    }
+}
+
+template <typename T>
+struct ScalView {
+    T *base;
+    const void *map;
+};
+
+template <typename T>
+struct VectView {
+    const T *base;
+    const void *map;
+    const void *rstr;
+};
+
+template <int ND, typename T>
+__global__ void __launch_bounds__(PW_BLOCK)
+intcflux_euler_kernel(int64_t n, int rs, T gamma, ScalView<T> vl, ScalView<T> vr, int ix64,
+                      const T *__restrict__ nl, int64_t ldn) {
+    constexpr int NV = ND + 2;
+    const int64_t i = (int64_t)blockIdx.x * PW_BLOCK + threadIdx.x;
+    if (i >= n) return;
+
+    T *pl = vl.base + b200::load_ix(vl.map, ix64, i);
+    T *pr = vr.base + b200::load_ix(vr.map, ix64, i);
+
+    T ul[NV], ur[NV], nn[ND], mag = 0;
+#pragma unroll
+    for (int v = 0; v < NV; v++) {
+        ul[v] = pl[v * B200_SOASZ];
+        ur[v] = pr[v * B200_SOASZ];
+    }
+#pragma unroll
+    for (int d = 0; d < ND; d++) {
+        nn[d] = nl[d * ldn + i];
+        mag += nn[d] * nn[d];
+    }
+    mag = sqrt(mag);
+    const T inv = T(1) / mag;
+#pragma unroll
+    for (int d = 0; d < ND; d++) nn[d] = inv * nn[d];
+
+    T fn[NV];
+    b200::rsolve<ND, T>(rs, ul, ur, nn, fn, gamma);
+
+#pragma unroll
+    for (int v = 0; v < NV; v++) {
+        pl[v * B200_SOASZ] = mag * fn[v];
+        pr[v * B200_SOASZ] = -mag * fn[v];
+    }
+}
+
+template <int ND, typename T>
+__global__ void __launch_bounds__(PW_BLOCK)
+intcflux_ns_kernel(int64_t n, int rs, Gas gas, T beta, T tau, ScalView<T> vl, ScalView<T> vr,
+                   VectView<T> gl, VectView<T> gr, int ix64, const T *__restrict__ nl,
+                   int64_t ldn) {
+    constexpr int NV = ND + 2;
+    const int64_t i = (int64_t)blockIdx.x * PW_BLOCK + threadIdx.x;
+    if (i >= n) return;
+
+    T *pl = vl.base + b200::load_ix(vl.map, ix64, i);
+    T *pr = vr.base + b200::load_ix(vr.map, ix64, i);
+
+    T ul[NV], ur[NV], nn[ND], mag = 0;
+#pragma unroll
+    for (int v = 0; v < NV; v++) {
+        ul[v] = pl[v * B200_SOASZ];
+        ur[v] = pr[v * B200_SOASZ];
+    }
+#pragma unroll
+    for (int d = 0; d < ND; d++) {
+        nn[d] = nl[d * ldn + i];
+        mag += nn[d] * nn[d];
+    }
+    mag = sqrt(mag);
+    const T inv = T(1) / mag;
+#pragma unroll
+    for (int d = 0; d < ND; d++) nn[d] = inv * nn[d];
+
+    T fi[NV];
+    b200::rsolve<ND, T>(rs, ul, ur, nn, fi, T(gas.gamma));
+
+    // LDG viscous common flux from the left and/or right states
+    T fvl[ND][NV], fvr[ND][NV];
+#pragma unroll
+    for (int d = 0; d < ND; d++)
+#pragma unroll
+        for (int v = 0; v < NV; v++) fvl[d][v] = fvr[d][v] = 0;
+
+    if (beta != T(-0.5)) {
+        const T *g = gl.base + b200::load_ix(gl.map, ix64, i);
+        const int64_t rstr = b200::load_ix(gl.rstr, ix64, i);
+        T gg[ND][NV];
+#pragma unroll
+        for (int d = 0; d < ND; d++)
+#pragma unroll
+            for (int v = 0; v < NV; v++) gg[d][v] = g[d * rstr + v * B200_SOASZ];
+        b200::viscous_flux_add<ND, T>(ul, gg, fvl, gas);
+    }
+    if (beta != T(0.5)) {
+        const T *g = gr.base + b200::load_ix(gr.map, ix64, i);
+        const int64_t rstr = b200::load_ix(gr.rstr, ix64, i);
+        T gg[ND][NV];
+#pragma unroll
+        for (int d = 0; d < ND; d++)
+#pragma unroll
+            for (int v = 0; v < NV; v++) gg[d][v] = g[d * rstr + v * B200_SOASZ];
+        b200::viscous_flux_add<ND, T>(ur, gg, fvr, gas);
+    }
+
+#pragma unroll
+    for (int v = 0; v < NV; v++) {
+        T nfl = 0, nfr = 0;
+#pragma unroll
+        for (int d = 0; d < ND; d++) {
+            nfl += nn[d] * fvl[d][v];
+            nfr += nn[d] * fvr[d][v];
+        }
+        T fvc;
+        if (beta == T(-0.5))
+            fvc = nfr;
+        else if (beta == T(0.5))
+            fvc = nfl;
+        else
+            fvc = (T(0.5) + beta) * nfl + (T(0.5) - beta) * nfr;
+        if (tau != T(0)) fvc += tau * (ul[v] - ur[v]);
+
+        pl[v * B200_SOASZ] = mag * (fi[v] + fvc);
+        pr[v * B200_SOASZ] = -mag * (fi[v] + fvc);
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(PW_BLOCK)
+intconu_kernel(int64_t n, int nvars, T beta, ScalView<T> lin, ScalView<T> rin,
+               ScalView<T> lout, ScalView<T> rout, int ix64) {
+    const int64_t i = (int64_t)blockIdx.x * PW_BLOCK + threadIdx.x;
+    if (i >= n) return;
+
+    const T *pli = lin.base + b200::load_ix(lin.map, ix64, i);
+    const T *pri = rin.base + b200::load_ix(rin.map, ix64, i);
+    T *plo = lout.base + b200::load_ix(lout.map, ix64, i);
+    T *pro = rout.base + b200::load_ix(rout.map, ix64, i);
+
+    for (int v = 0; v < nvars; v++) {
+        const int o = v * B200_SOASZ;
+        if (beta == T(-0.5)) {
+            pro[o] = pli[o];
+        } else if (beta == T(0.5)) {
+            plo[o] = pri[o];
+        } else {
+            const T c = pri[o] * (T(0.5) + beta) + pli[o] * (T(0.5) - beta);
+            plo[o] = c;
+            pro[o] = c;
+        }
+    }
+}
+
+template <typename T>
+ElemGeom<T> make_geom(int linear, const T *smats, int64_t lds, const T *rcpdjac, int64_t ldr,
+                      const T *verts, int64_t ldv, const T *upts, int64_t ldup) {
+    ElemGeom<T> g;
+    g.smats = smats; g.lds = lds;
+    g.rcpdjac = rcpdjac; g.ldr = ldr;
+    g.verts = verts; g.ldv = ldv;
+    g.upts = upts; g.ldup = ldup;
+    g.linear = linear;
+    return g;
+}
+
+int check_geom(int linear, const void *smats, const void *rcpdjac, const void *verts,
+               const void *upts, bool need_rcp) {
+    if (linear && (!verts || !upts))
+        return b200::set_error(B200_ERR_ARG, "linear elements need verts and upts");
+    if (!linear && (!smats || (need_rcp && !rcpdjac)))
+        return b200::set_error(B200_ERR_ARG, "curved elements need smats (and rcpdjac)");
+    return B200_OK;
+}
+
+template <typename T>
+int tflux_euler(int ndims, int nupts, int64_t neles, int linear, double gamma, const T *u,
+                int64_t ldu, T *f, int64_t ldf, const T *smats, int64_t lds, const T *verts,
+                int64_t ldv, const T *upts, int64_t ldup, cudaStream_t st) {
+    if (neles <= 0 || nupts <= 0) return B200_OK;
+    int rc = check_geom(linear, smats, nullptr, verts, upts, false);
+    if (rc) return rc;
+    auto geo = make_geom<T>(linear, smats, lds, nullptr, 0, verts, ldv, upts, ldup);
+    dim3 grid(b200::ceil_div(neles, PW_BLOCK), nupts);
+    if (ndims == 2)
+        tflux_euler_kernel<2, T><<<grid, PW_BLOCK, 0, st>>>(nupts, neles, (T)gamma, u, ldu, f, ldf, geo);
+    else if (ndims == 3)
+        tflux_euler_kernel<3, T><<<grid, PW_BLOCK, 0, st>>>(nupts, neles, (T)gamma, u, ldu, f, ldf, geo);
+    else
+        return b200::set_error(B200_ERR_ARG, "tflux: ndims must be 2 or 3");
+    B200_CHECK_LAUNCH("tflux_euler");
+    return B200_OK;
+}
+
+template <typename T>
+int tflux_ns(int ndims, int nupts, int64_t neles, int linear, const b200_gas_t *gas,
+             const T *u, int64_t ldu, T *f, int64_t ldf, T *gradu, int64_t ldg, const T *smats,
+             int64_t lds, const T *rcpdjac, int64_t ldr, const T *verts, int64_t ldv,
+             const T *upts, int64_t ldup, cudaStream_t st) {
+    if (neles <= 0 || nupts <= 0) return B200_OK;
+    if (!gas) return b200::set_error(B200_ERR_ARG, "tflux_ns: null gas constants");
+    int rc = check_geom(linear, smats, rcpdjac, verts, upts, true);
+    if (rc) return rc;
+    auto geo = make_geom<T>(linear, smats, lds, rcpdjac, ldr, verts, ldv, upts, ldup);
+    Gas g = *reinterpret_cast<const Gas *>(gas);
+    dim3 grid(b200::ceil_div(neles, PW_BLOCK), nupts);
+    if (ndims == 2)
+        tflux_ns_kernel<2, T><<<grid, PW_BLOCK, 0, st>>>(nupts, neles, g, u, ldu, f, ldf, gradu, ldg, geo);
+    else if (ndims == 3)
+        tflux_ns_kernel<3, T><<<grid, PW_BLOCK, 0, st>>>(nupts, neles, g, u, ldu, f, ldf, gradu, ldg, geo);
+    else
+        return b200::set_error(B200_ERR_ARG, "tflux_ns: ndims must be 2 or 3");
+    B200_CHECK_LAUNCH("tflux_ns");
+    return B200_OK;
+}
+
+template <typename T>
+int gradcoru(int ndims, int nupts, int64_t neles, int linear, T *gradu, int64_t ldg,
+             const T *smats, int64_t lds, const T *rcpdjac, int64_t ldr, const T *verts,
+             int64_t ldv, const T *upts, int64_t ldup, cudaStream_t st) {
+    if (neles <= 0 || nupts <= 0) return B200_OK;
+    int rc = check_geom(linear, smats, rcpdjac, verts, upts, true);
+    if (rc) return rc;
+    auto geo = make_geom<T>(linear, smats, lds, rcpdjac, ldr, verts, ldv, upts, ldup);
+    dim3 grid(b200::ceil_div(neles, PW_BLOCK), nupts);
+    if (ndims == 2)
+        gradcoru_kernel<2, T><<<grid, PW_BLOCK, 0, st>>>(nupts, neles, gradu, ldg, geo);
+    else if (ndims == 3)
+        gradcoru_kernel<3, T><<<grid, PW_BLOCK, 0, st>>>(nupts, neles, gradu, ldg, geo);
+    else
+        return b200::set_error(B200_ERR_ARG, "gradcoru: ndims must be 2 or 3");
+    B200_CHECK_LAUNCH("gradcoru");
+    return B200_OK;
+}
+
+template <typename T>
+int intcflux_euler(int ndims, int64_t n, int rsolver, double gamma, T *ul_base,
+                   const void *ul_map, T *ur_base, const void *ur_map, int ix64, const T *nl,
+                   int64_t ldn, cudaStream_t st) {
+    if (n <= 0) return B200_OK;
+    if (rsolver != b200::RS_RUSANOV && rsolver != b200::RS_HLLC)
+        return b200::set_error(B200_ERR_ARG, "intcflux: unknown Riemann solver %d", rsolver);
+    ScalView<T> l{ul_base, ul_map}, r{ur_base, ur_map};
+    unsigned grid = b200::ceil_div(n, PW_BLOCK);
+    if (ndims == 2)
+        intcflux_euler_kernel<2, T><<<grid, PW_BLOCK, 0, st>>>(n, rsolver, (T)gamma, l, r, ix64, nl, ldn);
+    else if (ndims == 3)
+        intcflux_euler_kernel<3, T><<<grid, PW_BLOCK, 0, st>>>(n, rsolver, (T)gamma, l, r, ix64, nl, ldn);
+    else
+        return b200::set_error(B200_ERR_ARG, "intcflux: ndims must be 2 or 3");
+    B200_CHECK_LAUNCH("intcflux_euler");
+    return B200_OK;
+}
+
+template <typename T>
+int intcflux_ns(int ndims, int64_t n, int rsolver, const b200_gas_t *gas, double beta,
+                double tau, T *ul_base, const void *ul_map, T *ur_base, const void *ur_map,
+                const T *gl_base, const void *gl_map, const void *gl_rstr, const T *gr_base,
+                const void *gr_map, const void *gr_rstr, int ix64, const T *nl, int64_t ldn,
+                cudaStream_t st) {
+    if (n <= 0) return B200_OK;
+    if (!gas) return b200::set_error(B200_ERR_ARG, "intcflux_ns: null gas constants");
+    if (rsolver != b200::RS_RUSANOV && rsolver != b200::RS_HLLC)
+        return b200::set_error(B200_ERR_ARG, "intcflux: unknown Riemann solver %d", rsolver);
+    ScalView<T> l{ul_base, ul_map}, r{ur_base, ur_map};
+    VectView<T> gl{gl_base, gl_map, gl_rstr}, gr{gr_base, gr_map, gr_rstr};
+    Gas g = *reinterpret_cast<const Gas *>(gas);
+    unsigned grid = b200::ceil_div(n, PW_BLOCK);
+    if (ndims == 2)
+        intcflux_ns_kernel<2, T><<<grid, PW_BLOCK, 0, st>>>(n, rsolver, g, (T)beta, (T)tau, l, r, gl, gr, ix64, nl, ldn);
+    else if (ndims == 3)
+        intcflux_ns_kernel<3, T><<<grid, PW_BLOCK, 0, st>>>(n, rsolver, g, (T)beta, (T)tau, l, r, gl, gr, ix64, nl, ldn);
+    else
+        return b200::set_error(B200_ERR_ARG, "intcflux_ns: ndims must be 2 or 3");
+    B200_CHECK_LAUNCH("intcflux_ns");
+    return B200_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int b200_tflux_euler_f64(int ndims, int nupts, int64_t neles, int linear, double gamma,
+                         const double *u, int64_t ldu, double *f, int64_t ldf,
+                         const double *smats, int64_t lds, const double *verts, int64_t ldv,
+                         const double *upts, int64_t ldup, void *stream) {
+    return tflux_euler<double>(ndims, nupts, neles, linear, gamma, u, ldu, f, ldf, smats, lds,
+                               verts, ldv, upts, ldup, (cudaStream_t)stream);
+}
+
+int b200_tflux_euler_f32(int ndims, int nupts, int64_t neles, int linear, double gamma,
+                         const float *u, int64_t ldu, float *f, int64_t ldf,
+                         const float *smats, int64_t lds, const float *verts, int64_t ldv,
+                         const float *upts, int64_t ldup, void *stream) {
+    return tflux_euler<float>(ndims, nupts, neles, linear, gamma, u, ldu, f, ldf, smats, lds,
+                              verts, ldv, upts, ldup, (cudaStream_t)stream);
+}
+
+int b200_tflux_ns_f64(int ndims, int nupts, int64_t neles, int linear, const b200_gas_t *gas,
+                      const double *u, int64_t ldu, double *f, int64_t ldf, double *gradu,
+                      int64_t ldg, const double *smats, int64_t lds, const double *rcpdjac,
+                      int64_t ldr, const double *verts, int64_t ldv, const double *upts,
+                      int64_t ldup, void *stream) {
+    return tflux_ns<double>(ndims, nupts, neles, linear, gas, u, ldu, f, ldf, gradu, ldg, smats,
+                            lds, rcpdjac, ldr, verts, ldv, upts, ldup, (cudaStream_t)stream);
+}
+
+int b200_tflux_ns_f32(int ndims, int nupts, int64_t neles, int linear, const b200_gas_t *gas,
+                      const float *u, int64_t ldu, float *f, int64_t ldf, float *gradu,
+                      int64_t ldg, const float *smats, int64_t lds, const float *rcpdjac,
+                      int64_t ldr, const float *verts, int64_t ldv, const float *upts,
+                      int64_t ldup, void *stream) {
+    return tflux_ns<float>(ndims, nupts, neles, linear, gas, u, ldu, f, ldf, gradu, ldg, smats,
+                           lds, rcpdjac, ldr, verts, ldv, upts, ldup, (cudaStream_t)stream);
+}
+
+int b200_gradcoru_f64(int ndims, int nupts, int64_t neles, int linear, double *gradu,
+                      int64_t ldg, const double *smats, int64_t lds, const double *rcpdjac,
+                      int64_t ldr, const double *verts, int64_t ldv, const double *upts,
+                      int64_t ldup, void *stream) {
+    return gradcoru<double>(ndims, nupts, neles, linear, gradu, ldg, smats, lds, rcpdjac, ldr,
+                            verts, ldv, upts, ldup, (cudaStream_t)stream);
+}
+
+int b200_gradcoru_f32(int ndims, int nupts, int64_t neles, int linear, float *gradu,
+                      int64_t ldg, const float *smats, int64_t lds, const float *rcpdjac,
+                      int64_t ldr, const float *verts, int64_t ldv, const float *upts,
+                      int64_t ldup, void *stream) {
+    return gradcoru<float>(ndims, nupts, neles, linear, gradu, ldg, smats, lds, rcpdjac, ldr,
+                           verts, ldv, upts, ldup, (cudaStream_t)stream);
+}
+
+int b200_negdivconf_f64(int nvars, int nupts, int64_t neles, double *r, int64_t ldr,
+                        const double *rcpdjac, int64_t ldj, void *stream) {
+    if (neles <= 0 || nupts <= 0) return B200_OK;
+    dim3 grid(b200::ceil_div(neles, PW_BLOCK), nupts);
+    negdivconf_kernel<double><<<grid, PW_BLOCK, 0, (cudaStream_t)stream>>>(nvars, neles, r, ldr, rcpdjac, ldj);
+    B200_CHECK_LAUNCH("negdivconf");
+    return B200_OK;
+}
+
+int b200_negdivconf_f32(int nvars, int nupts, int64_t neles, float *r, int64_t ldr,
+                        const float *rcpdjac, int64_t ldj, void *stream) {
+    if (neles <= 0 || nupts <= 0) return B200_OK;
+    dim3 grid(b200::ceil_div(neles, PW_BLOCK), nupts);
+    negdivconf_kernel<float><<<grid, PW_BLOCK, 0, (cudaStream_t)stream>>>(nvars, neles, r, ldr, rcpdjac, ldj);
+    B200_CHECK_LAUNCH("negdivconf");
+    return B200_OK;
+}
+
+int b200_intcflux_euler_f64(int ndims, int64_t n, int rsolver, double gamma, double *ul_base,
+                            const void *ul_map, double *ur_base, const void *ur_map, int ix64,
+                            const double *nl, int64_t ldn, void *stream) {
+    return intcflux_euler<double>(ndims, n, rsolver, gamma, ul_base, ul_map, ur_base, ur_map,
+                                  ix64, nl, ldn, (cudaStream_t)stream);
+}
+
+int b200_intcflux_euler_f32(int ndims, int64_t n, int rsolver, double gamma, float *ul_base,
+                            const void *ul_map, float *ur_base, const void *ur_map, int ix64,
+                            const float *nl, int64_t ldn, void *stream) {
+    return intcflux_euler<float>(ndims, n, rsolver, gamma, ul_base, ul_map, ur_base, ur_map,
+                                 ix64, nl, ldn, (cudaStream_t)stream);
+}
+
+int b200_intcflux_ns_f64(int ndims, int64_t n, int rsolver, const b200_gas_t *gas, double beta,
+                         double tau, double *ul_base, const void *ul_map, double *ur_base,
+                         const void *ur_map, const double *gl_base, const void *gl_map,
+                         const void *gl_rstr, const double *gr_base, const void *gr_map,
+                         const void *gr_rstr, int ix64, const double *nl, int64_t ldn,
+                         void *stream) {
+    return intcflux_ns<double>(ndims, n, rsolver, gas, beta, tau, ul_base, ul_map, ur_base,
+                               ur_map, gl_base, gl_map, gl_rstr, gr_base, gr_map, gr_rstr, ix64,
+                               nl, ldn, (cudaStream_t)stream);
+}
+
+int b200_intcflux_ns_f32(int ndims, int64_t n, int rsolver, const b200_gas_t *gas, double beta,
+                         double tau, float *ul_base, const void *ul_map, float *ur_base,
+                         const void *ur_map, const float *gl_base, const void *gl_map,
+                         const void *gl_rstr, const float *gr_base, const void *gr_map,
+                         const void *gr_rstr, int ix64, const float *nl, int64_t ldn,
+                         void *stream) {
+    return intcflux_ns<float>(ndims, n, rsolver, gas, beta, tau, ul_base, ul_map, ur_base,
+                              ur_map, gl_base, gl_map, gl_rstr, gr_base, gr_map, gr_rstr, ix64,
+                              nl, ldn, (cudaStream_t)stream);
+}
+
+int b200_intconu_f64(int nvars, int64_t n, double beta, const double *lin_base,
+                     const void *lin_map, const double *rin_base, const void *rin_map,
+                     double *lout_base, const void *lout_map, double *rout_base,
+                     const void *rout_map, int ix64, void *stream) {
+    if (n <= 0) return B200_OK;
+    ScalView<double> li{const_cast<double *>(lin_base), lin_map};
+    ScalView<double> ri{const_cast<double *>(rin_base), rin_map};
+    ScalView<double> lo{lout_base, lout_map}, ro{rout_base, rout_map};
+    intconu_kernel<double><<<b200::ceil_div(n, PW_BLOCK), PW_BLOCK, 0, (cudaStream_t)stream>>>(
+        n, nvars, beta, li, ri, lo, ro, ix64);
+    B200_CHECK_LAUNCH("intconu");
+    return B200_OK;
+}
+
+int b200_intconu_f32(int nvars, int64_t n, double beta, const float *lin_base,
+                     const void *lin_map, const float *rin_base, const void *rin_map,
+                     float *lout_base, const void *lout_map, float *rout_base,
+                     const void *rout_map, int ix64, void *stream) {
+    if (n <= 0) return B200_OK;
+    ScalView<float> li{const_cast<float *>(lin_base), lin_map};
+    ScalView<float> ri{const_cast<float *>(rin_base), rin_map};
+    ScalView<float> lo{lout_base, lout_map}, ro{rout_base, rout_map};
+    intconu_kernel<float><<<b200::ceil_div(n, PW_BLOCK), PW_BLOCK, 0, (cudaStream_t)stream>>>(
+        n, nvars, (float)beta, li, ri, lo, ro, ix64);
+    B200_CHECK_LAUNCH("intconu");
+    return B200_OK;
+}
+
+}  // extern "C"

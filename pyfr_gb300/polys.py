@@ -1,0 +1,136 @@
+"""Orthonormal and nodal polynomial bases on the reference line, quad and hex.
+
+The flux-reconstruction operators are built from the same mathematical
+objects as ``pyfr/polys.py`` (orthonormal Legendre products, Vandermonde
+inversion to a nodal basis at the solution points,
+``pyfr/polys.py:46-88`` and ``pyfr/polys.py:126-150,402-433``).  This
+module is a fresh, vectorised statement of that mathematics: the nodal
+basis that results is independent of how the orthonormal modes are
+enumerated, so only the ordering of the nodal points has to agree with the
+reference (x fastest, then y, then z).
+"""
+
+import itertools as it
+
+import numpy as np
+
+
+def legendre_orthonormal(order, x):
+    """Values and first derivatives of the L2-orthonormal Legendre
+    polynomials sqrt(k + 1/2) P_k(x) for k = 0..order.
+
+    Returns two arrays of shape (order + 1, len(x)).
+    """
+    x = np.asarray(x, dtype=float)
+    p = np.zeros((order + 1,) + x.shape)
+    dp = np.zeros_like(p)
+
+    p[0] = 1.0
+    if order >= 1:
+        p[1] = x
+        dp[1] = 1.0
+
+    # Bonnet recursion for P_k and the derivative identity
+    # P'_k = k P_{k-1} + x P'_{k-1}
+    for k in range(2, order + 1):
+        p[k] = ((2*k - 1)*x*p[k - 1] - (k - 1)*p[k - 2]) / k
+        dp[k] = k*p[k - 1] + x*dp[k - 1]
+
+    scale = np.sqrt(np.arange(order + 1) + 0.5)
+    shp = (-1,) + (1,)*x.ndim
+    return scale.reshape(shp)*p, scale.reshape(shp)*dp
+
+
+class TensorProdBasis:
+    """Tensor-product orthonormal basis of degree ``order`` in each of
+    ``ndims`` reference coordinates, with a nodal basis at ``pts``."""
+
+    def __init__(self, ndims, order, pts=None):
+        self.ndims = ndims
+        self.order = order
+        self.pts = None if pts is None else np.atleast_2d(pts)
+
+        # Multi-indices of the modes
+        self.modes = list(it.product(range(order + 1), repeat=ndims))
+
+    def _factors(self, pts):
+        pts = np.atleast_2d(np.asarray(pts, dtype=float))
+        if pts.shape[-1] != self.ndims:
+            pts = pts.reshape(-1, self.ndims)
+
+        return [legendre_orthonormal(self.order, pts[:, d])
+                for d in range(self.ndims)]
+
+    def ortho_basis_at(self, pts):
+        """Orthonormal modes at ``pts``; shape (nmodes, npts)."""
+        f = self._factors(pts)
+        out = []
+        for m in self.modes:
+            v = f[0][0][m[0]].copy()
+            for d in range(1, self.ndims):
+                v *= f[d][0][m[d]]
+            out.append(v)
+
+        return np.array(out)
+
+    def jac_ortho_basis_at(self, pts):
+        """Reference-space gradients of the modes; shape
+        (ndims, nmodes, npts)."""
+        f = self._factors(pts)
+        out = np.empty((self.ndims, len(self.modes), len(f[0][0][0])))
+        for i, m in enumerate(self.modes):
+            for g in range(self.ndims):
+                v = np.ones_like(f[0][0][0])
+                for d in range(self.ndims):
+                    v = v*(f[d][1][m[d]] if d == g else f[d][0][m[d]])
+                out[g, i] = v
+
+        return out
+
+    @property
+    def vdm(self):
+        return self.ortho_basis_at(self.pts)
+
+    @property
+    def invvdm(self):
+        return np.linalg.inv(self.vdm)
+
+    def nodal_basis_at(self, epts):
+        """Lagrange basis of the nodal points evaluated at ``epts``;
+        shape (nepts, nnodes)."""
+        return (self.invvdm @ self.ortho_basis_at(epts)).T
+
+    def jac_nodal_basis_at(self, epts):
+        """Gradient of the Lagrange basis at ``epts``; shape
+        (ndims, nnodes, nepts)."""
+        return self.invvdm @ self.jac_ortho_basis_at(epts)
+
+
+def tidy(arr, tol=1e-10):
+    """Flush entries below ``tol`` to exact zero and give entries whose
+    magnitudes agree to a relative ``tol`` one common magnitude.
+
+    Operator matrices in the reference go through the same kind of clean-up
+    (``pyfr/nputil.py:23-60``), so that analytically-zero entries are exact
+    zeros (the sparsity pattern the operator kernels exploit) and entries
+    equal by symmetry are bit-identical.
+    """
+    a = np.array(arr, dtype=float, copy=True)
+    a[np.abs(a) < tol] = 0.0
+
+    flat = a.reshape(-1)
+    mag = np.abs(flat)
+    order = np.argsort(mag, kind='stable')
+    smag = mag[order]
+
+    # Split the sorted magnitudes into runs of near-equal values
+    brk = ~np.isclose(smag[1:], smag[:-1], rtol=tol, atol=0.1*tol)
+    starts = np.concatenate([[0], np.flatnonzero(brk) + 1])
+    ends = np.concatenate([starts[1:], [len(smag)]])
+    for s, e in zip(starts, ends):
+        if e - s > 1:
+            rep = np.median(smag[s:e])
+            idx = order[s:e]
+            flat[idx] = np.copysign(rep, flat[idx])
+
+    return a

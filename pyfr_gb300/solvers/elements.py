@@ -1,0 +1,438 @@
+"""Element types of the Euler and Navier-Stokes systems.
+
+Each class allocates its scratch fields on the backend and declares its
+kernels exactly as the reference elements do: same kernel names, same
+operator expressions, same arguments
+(``pyfr/solvers/base/elements.py:218-266``,
+``pyfr/solvers/baseadvec/elements.py:61-128``,
+``pyfr/solvers/baseadvecdiff/elements.py:26-120``,
+``pyfr/solvers/euler/elements.py:149-206``,
+``pyfr/solvers/navstokes/elements.py:30-128``).
+
+Geometry is that of linear (multilinear) elements: the metric terms are
+computed from the vertices; the kernels either recompute them at each
+solution point from the vertices ('linear' kernel type, as the reference
+does for uncurved elements) or read them from stored per-point arrays
+('curved' kernel type).
+"""
+
+from functools import cached_property
+
+import numpy as np
+
+from pyfr_gb300.mesh import fuzzy_face_order
+from pyfr_gb300.shapes import get_shape
+
+
+_NPEVAL_SYMS = {k: getattr(np, k) for k in
+                ('sin', 'cos', 'tan', 'exp', 'log', 'sqrt', 'tanh', 'sinh',
+                 'cosh', 'arctan2', 'abs', 'pi')}
+_NPEVAL_SYMS |= {'pow': np.power, 'min': np.minimum, 'max': np.maximum,
+                 'atan2': np.arctan2, 'fabs': np.abs}
+
+
+def npeval(expr, env):
+    """Evaluate an initial-condition expression over numpy arrays."""
+    if '**' in expr or '^' in expr:
+        raise ValueError('Direct exponentiation is not supported; use pow')
+    return eval(expr, {'__builtins__': {}}, _NPEVAL_SYMS | env)
+
+
+class BaseElements:
+    def __init__(self, etype, eles, cfg):
+        self.cfg = cfg
+        self.eles = eles
+        self.nspts, self.neles, self.ndims = eles.shape
+
+        order = cfg.getint('solver', 'order')
+        upts = cfg.get(f'solver-elements-{etype}', 'soln-pts',
+                       'gauss-legendre')
+        kind = 'line' if self.ndims == 2 else 'quad'
+        fpts = cfg.get(f'solver-interfaces-{kind}', 'flux-pts',
+                       'gauss-legendre')
+        self.basis = get_shape(etype, order, upts, fpts)
+        self.name = etype
+
+        if cfg.get('solver', 'anti-alias', 'none') != 'none':
+            raise NotImplementedError('Anti-aliasing is not supported')
+
+        self.convars = self.convarnames(self.ndims)
+        self.nvars = len(self.convars)
+        self.nupts = self.basis.nupts
+        self.nfpts = self.basis.nfpts
+        self.nfacefpts = self.basis.nfacefpts
+        self.kernels = {}
+        self._be = None
+
+    # ---- geometry (linear elements) -----------------------------------------
+
+    def ploc_at_np(self, pts):
+        pts = getattr(self.basis, pts) if isinstance(pts, str) else pts
+        sf = self.basis.shape_fn(pts)                    # (npts, nverts)
+        ploc = np.einsum('pv,ved->pde', sf, self.eles)
+        return ploc
+
+    def _jac_at(self, pts):
+        pts = getattr(self.basis, pts) if isinstance(pts, str) else pts
+        dsf = self.basis.shape_jac(pts)                  # (npts, i, nverts)
+        return np.einsum('piv,vej->pije', dsf, self.eles)
+
+    def smats_djac_at_np(self, pts):
+        """Adjugate metric S[i][j] (npts, ndims, ndims, neles) and |J|."""
+        J = self._jac_at(pts)
+        if self.ndims == 2:
+            s = np.empty_like(J)
+            s[:, 0, 0], s[:, 0, 1] = J[:, 1, 1], -J[:, 1, 0]
+            s[:, 1, 0], s[:, 1, 1] = -J[:, 0, 1], J[:, 0, 0]
+            d = s[:, 0, 0]*s[:, 1, 1] - s[:, 0, 1]*s[:, 1, 0]
+        else:
+            s = np.empty_like(J)
+            for i in range(3):
+                a, b = (i + 1) % 3, (i + 2) % 3
+                s[:, i] = np.cross(J[:, a], J[:, b], axisa=1, axisb=1,
+                                   axisc=1)
+            d = np.einsum('pje,pje->pe', J[:, 0], s[:, 0])
+        return s, d
+
+    def smat_at_np(self, pts):
+        s, _ = self.smats_djac_at_np(pts)
+        return s.transpose(1, 0, 2, 3)      # (ndims_i, npts, ndims_j, neles)
+
+    def rcpdjac_at_np(self, pts):
+        _, d = self.smats_djac_at_np(pts)
+        if np.any(d < -1e-5):
+            raise RuntimeError('Negative mesh Jacobians detected')
+        return 1.0 / d
+
+    @cached_property
+    def _pnorm_fpts(self):
+        s, _ = self.smats_djac_at_np('fpts')             # (p, l, k, e)
+        pn = np.einsum('plke,pl->pek', s, self.basis.norm_fpts)
+        if np.any(np.sqrt(np.einsum('...i,...i', pn, pn)) < 1e-10):
+            raise RuntimeError('Zero face normals detected')
+        return pn                                        # (nfpts, neles, ndims)
+
+    @cached_property
+    def plocfpts(self):
+        return self.ploc_at_np('fpts').transpose(0, 2, 1)   # (nfpts, neles, d)
+
+    @cached_property
+    def srtd_face_fpts(self):
+        """Flux-point indices of each face, in physical-coordinate order,
+        per element: list over faces of (neles, nfacefpts) arrays."""
+        out = []
+        for ffpts in self.basis.facefpts:
+            ffpts = np.asarray(ffpts)
+            coords = self.plocfpts[ffpts].transpose(1, 2, 0)
+            out.append(ffpts[fuzzy_face_order(coords)])
+        return out
+
+    # ---- initial conditions ------------------------------------------------
+
+    def set_ics_from_cfg(self):
+        consts = self.cfg.items_as('constants', float)
+        coords = self.ploc_at_np('upts')                 # (nupts, ndims, neles)
+        env = consts | dict(zip('xyz', coords.swapaxes(0, 1)))
+        pris = [np.broadcast_to(npeval(self.cfg.getexpr('soln-ics', v), env),
+                                (self.nupts, self.neles))
+                for v in self.privarnames(self.ndims)]
+
+        ics = np.empty((self.nupts, self.nvars, self.neles))
+        for i, v in enumerate(self.pri_to_con(pris, self.cfg)):
+            ics[:, i] = v
+        return ics
+
+    # ---- backend set-up -------------------------------------------------------
+
+    @property
+    def mesh_regions(self):
+        off = self.linoff
+        if off == 0:
+            return {'linear': self.neles}
+        elif off >= self.neles:
+            return {'curved': self.neles}
+        return {'curved': off, 'linear': self.neles - off}
+
+    def _slice_mat(self, mat, region):
+        if mat is None:
+            return None
+        off = self.linoff
+        if len(mat.ioshape) >= 3:
+            off *= mat.ioshape[-2]
+        else:
+            off = min(off, mat.ncol)
+        if region == 'curved':
+            return mat.slice(None, None, 0, off)
+        return mat.slice(None, None, off, mat.ncol)
+
+    def _make_sliced_kernel(self, kseq):
+        kl = list(kseq)
+        if len(kl) > 1:
+            return self._be.unordered_meta_kernel(kl, [self.linoff])
+        return kl[0]
+
+    def set_backend(self, backend, nonce, linoff):
+        self._be = be = backend
+        self.grad_fusion = not be.blocks
+
+        csub = backend.csubsz
+        self.linoff = linoff - linoff % -csub if self.basis.order >= 2 else self.neles
+
+        ndims, nvars, neles = self.ndims, self.nvars, self.neles
+        abufs = []
+
+        def alloc(ex, shape):
+            m = be.matrix(shape, extent=nonce + ex, tags={'align'})
+            abufs.append(m)
+            return m
+
+        sbufs = self._scratch_bufs
+        if 'scal_fpts' in sbufs:
+            self._scal_fpts = alloc('scal_fpts', (self.nfpts, nvars, neles))
+        if 'vect_upts' in sbufs:
+            self._vect_upts = alloc('vect_upts', (ndims, self.nupts, nvars, neles))
+        if 'vect_fpts' in sbufs:
+            self._vect_fpts = alloc('vect_fpts', (ndims, self.nfpts, nvars, neles))
+        if 'grad_upts' in sbufs:
+            self._grad_upts = alloc('grad_upts', (ndims, self.nupts, nvars, neles))
+        elif hasattr(self, '_vect_upts'):
+            self._grad_upts = self._vect_upts
+        if 'vect_fpts' in sbufs:
+            self._comm_fpts = self._vect_fpts.slice(0, self.nfpts)
+
+        self.scal_upts = []
+
+    def alloc_bank(self, extent, ic=None):
+        m = self._be.matrix((self.nupts, self.nvars, self.neles), ic,
+                            extent=extent, tags={'align'})
+        self.scal_upts.append(m)
+        return m
+
+    def opmat(self, expr):
+        key = ('opmat', expr)
+        if key not in self.__dict__:
+            self.__dict__[key] = self._be.const_matrix(
+                self.basis.opmat(expr), tags={expr, 'align'})
+        return self.__dict__[key]
+
+    def _cached(self, key, fn):
+        if key not in self.__dict__:
+            self.__dict__[key] = fn()
+        return self.__dict__[key]
+
+    def rcpdjac_at(self, name, side=None):
+        m = self._cached(('rcpdjac', name), lambda: self._be.const_matrix(
+            self.rcpdjac_at_np(name), tags={'align'}))
+        return self._slice_mat(m, side) if side else m
+
+    def curved_smat_at(self, name):
+        return self._cached(('csmat', name), lambda: self._be.const_matrix(
+            self.smat_at_np(name)[..., :self.linoff], tags={'align'}))
+
+    def ploc_at(self, name, side=None):
+        m = self._cached(('ploc', name), lambda: self._be.const_matrix(
+            self.ploc_at_np(name), tags={'align'}))
+        return self._slice_mat(m, side) if side else m
+
+    @cached_property
+    def upts(self):
+        return self._be.const_matrix(self.basis.upts)
+
+    # ---- interface helpers (pyfr/solvers/base/elements.py:446-469) --------
+
+    def get_pnorms_for_inters(self, eidxs, fidx):
+        fpts_idx = self.srtd_face_fpts[fidx][eidxs]
+        pn = self._pnorm_fpts[fpts_idx, eidxs[:, None]]
+        return pn.reshape(-1, self.ndims),
+
+    def _inters_map(self, eidxs, fidx, mid, rmap, lda=None):
+        nfp = self.nfacefpts[fidx]
+        n = len(eidxs)
+        cmap = np.repeat(eidxs, nfp)
+        if lda is None:
+            return np.full(n*nfp, mid), rmap.ravel(), cmap
+        return np.full(n*nfp, mid), rmap.ravel(), cmap, np.full(n*nfp, lda)
+
+    def get_vect_fpts_for_inters(self, eidxs, fidx):
+        rmap = self.srtd_face_fpts[fidx][eidxs]
+        return self._inters_map(eidxs, fidx, self._vect_fpts.mid, rmap,
+                                self.nfpts)
+
+    def get_comm_fpts_for_inters(self, eidxs, fidx):
+        rmap = self.srtd_face_fpts[fidx][eidxs]
+        return self._inters_map(eidxs, fidx, self._comm_fpts.mid, rmap)
+
+
+class FluidElements:
+    """Variables and conversions of the compressible equations
+    (``pyfr/solvers/euler/elements.py:71-136``)."""
+
+    @staticmethod
+    def privarnames(ndims):
+        return ['rho', 'u', 'v', 'p'] if ndims == 2 else \
+               ['rho', 'u', 'v', 'w', 'p']
+
+    @staticmethod
+    def convarnames(ndims):
+        return ['rho', 'rhou', 'rhov', 'E'] if ndims == 2 else \
+               ['rho', 'rhou', 'rhov', 'rhow', 'E']
+
+    @staticmethod
+    def pri_to_con(pris, cfg):
+        rho, p = pris[0], pris[-1]
+        rhovs = [rho*c for c in pris[1:-1]]
+        gamma = cfg.getfloat('constants', 'gamma')
+        E = p/(gamma - 1) + 0.5*rho*sum(c*c for c in pris[1:-1])
+        return [rho, *rhovs, E]
+
+    @staticmethod
+    def con_to_pri(cons, cfg):
+        rho, E = cons[0], cons[-1]
+        vs = [rhov/rho for rhov in cons[1:-1]]
+        gamma = cfg.getfloat('constants', 'gamma')
+        p = (gamma - 1)*(E - 0.5*rho*sum(v*v for v in vs))
+        return [rho, *vs, p]
+
+
+class EulerElements(FluidElements, BaseElements):
+    _scratch_bufs = {'scal_fpts', 'vect_upts'}
+
+    def set_backend(self, backend, nonce, linoff):
+        super().set_backend(backend, nonce, linoff)
+        be, kernels = self._be, self.kernels
+
+        be.pointwise.register('pyfr.solvers.baseadvec.kernels.negdivconf')
+        be.pointwise.register('pyfr.solvers.euler.kernels.tflux')
+
+        # Interpolate the solution to the flux points
+        kernels['disu'] = lambda uin: be.kernel(
+            'mul', self.opmat('M0'), self.scal_upts[uin], out=self._scal_fpts)
+
+        # Transformed flux
+        tplargs = dict(ndims=self.ndims, nvars=self.nvars,
+                       nverts=len(self.basis.linspts),
+                       c=self.cfg.items_as('constants', float))
+        r, s = self.mesh_regions, self._slice_mat
+        tdisf = []
+        if 'curved' in r:
+            tdisf.append(lambda uin: be.kernel(
+                'tflux', tplargs=tplargs | {'ktype': 'curved'},
+                dims=[self.nupts, r['curved']],
+                u=s(self.scal_upts[uin], 'curved'),
+                f=s(self._vect_upts, 'curved'),
+                smats=self.curved_smat_at('upts')))
+        if 'linear' in r:
+            tdisf.append(lambda uin: be.kernel(
+                'tflux', tplargs=tplargs | {'ktype': 'linear'},
+                dims=[self.nupts, r['linear']],
+                u=s(self.scal_upts[uin], 'linear'),
+                f=s(self._vect_upts, 'linear'),
+                verts=self.ploc_at('linspts', 'linear'), upts=self.upts))
+        kernels['tdisf'] = lambda uin: self._make_sliced_kernel(
+            k(uin) for k in tdisf)
+
+        # Divergence of the partially corrected flux and the correction
+        kernels['tdivtpcorf'] = lambda fout: be.kernel(
+            'mul', self.opmat('M1 - M3*M2'), self._vect_upts,
+            out=self.scal_upts[fout])
+        kernels['tdivtconf'] = lambda fout: be.kernel(
+            'mul', self.opmat('M3'), self._scal_fpts,
+            out=self.scal_upts[fout], beta=1.0)
+
+        kernels['negdivconf'] = lambda fout: be.kernel(
+            'negdivconf', tplargs=dict(ndims=self.ndims, nvars=self.nvars,
+                                       src_macros=[]),
+            dims=[self.nupts, self.neles], tdivtconf=self.scal_upts[fout],
+            rcpdjac=self.rcpdjac_at('upts'))
+
+
+class NavierStokesElements(FluidElements, BaseElements):
+    _scratch_bufs = {'scal_fpts', 'vect_fpts', 'vect_upts', 'grad_upts'}
+
+    def set_backend(self, backend, nonce, linoff):
+        super().set_backend(backend, nonce, linoff)
+        be, kernels = self._be, self.kernels
+
+        be.pointwise.register('pyfr.solvers.baseadvec.kernels.negdivconf')
+        be.pointwise.register('pyfr.solvers.baseadvecdiff.kernels.gradcoru')
+        be.pointwise.register('pyfr.solvers.navstokes.kernels.tflux')
+
+        kernels['disu'] = lambda uin: be.kernel(
+            'mul', self.opmat('M0'), self.scal_upts[uin], out=self._scal_fpts)
+
+        if abs(self.cfg.getfloat('solver-interfaces', 'ldg-beta')) == 0.5:
+            kernels['copy_fpts'] = lambda: be.kernel(
+                'copy', self._comm_fpts, self._scal_fpts)
+
+        kernels['tgradpcoru_upts'] = lambda uin: be.kernel(
+            'mul', self.opmat('M4 - M6*M0'), self.scal_upts[uin],
+            out=self._grad_upts)
+        kernels['tgradcoru_upts'] = lambda: be.kernel(
+            'mul', self.opmat('M6'), self._comm_fpts, out=self._grad_upts,
+            beta=1.0)
+
+        r, s = self.mesh_regions, self._slice_mat
+        gtpl = dict(ndims=self.ndims, nvars=self.nvars,
+                    nverts=len(self.basis.linspts))
+        gradcoru_u = []
+        if 'curved' in r:
+            gradcoru_u.append(lambda: be.kernel(
+                'gradcoru', tplargs=gtpl | {'ktype': 'curved'},
+                dims=[self.nupts, r['curved']],
+                gradu=s(self._grad_upts, 'curved'),
+                smats=self.curved_smat_at('upts'),
+                rcpdjac=self.rcpdjac_at('upts', 'curved')))
+        if 'linear' in r:
+            gradcoru_u.append(lambda: be.kernel(
+                'gradcoru', tplargs=gtpl | {'ktype': 'linear'},
+                dims=[self.nupts, r['linear']],
+                gradu=s(self._grad_upts, 'linear'), upts=self.upts,
+                verts=self.ploc_at('linspts', 'linear')))
+        kernels['gradcoru_u'] = lambda: self._make_sliced_kernel(
+            k() for k in gradcoru_u)
+
+        def gradcoru_fpts():
+            nupts, nfpts = self.nupts, self.nfpts
+            vupts, vfpts = self._grad_upts, self._vect_fpts
+            muls = [be.kernel('mul', self.opmat('M0'),
+                              vupts.slice(i*nupts, (i + 1)*nupts),
+                              vfpts.slice(i*nfpts, (i + 1)*nfpts))
+                    for i in range(self.ndims)]
+            return be.unordered_meta_kernel(muls)
+        kernels['gradcoru_fpts'] = gradcoru_fpts
+
+        visc_corr = self.cfg.get('solver', 'viscosity-correction', 'none')
+        tplargs = dict(ndims=self.ndims, nvars=self.nvars,
+                       nverts=len(self.basis.linspts),
+                       c=self.cfg.items_as('constants', float),
+                       shock_capturing='none', visc_corr=visc_corr)
+        tdisf = []
+        for rgn in ('curved', 'linear'):
+            if rgn not in r:
+                continue
+            kw = dict(upts=self.upts)
+            if rgn == 'curved':
+                kw |= dict(smats=self.curved_smat_at('upts'),
+                           rcpdjac=self.rcpdjac_at('upts', 'curved'))
+            else:
+                kw |= dict(verts=self.ploc_at('linspts', 'linear'))
+            kw |= dict(f=s(self._vect_upts, rgn), gradu=s(self._grad_upts, rgn))
+            tdisf.append((f'{rgn}-fused', r[rgn], rgn, kw))
+
+        kernels['tdisf_fused'] = lambda uin: self._make_sliced_kernel(
+            be.kernel('tflux', tplargs=tplargs | {'ktype': kt},
+                      dims=[self.nupts, n], u=s(self.scal_upts[uin], rgn),
+                      **kw)
+            for kt, n, rgn, kw in tdisf)
+
+        kernels['tdivtpcorf'] = lambda fout: be.kernel(
+            'mul', self.opmat('M1 - M3*M2'), self._vect_upts,
+            out=self.scal_upts[fout])
+        kernels['tdivtconf'] = lambda fout: be.kernel(
+            'mul', self.opmat('M3'), self._scal_fpts,
+            out=self.scal_upts[fout], beta=1.0)
+        kernels['negdivconf'] = lambda fout: be.kernel(
+            'negdivconf', tplargs=dict(ndims=self.ndims, nvars=self.nvars,
+                                       src_macros=[]),
+            dims=[self.nupts, self.neles], tdivtconf=self.scal_upts[fout],
+            rcpdjac=self.rcpdjac_at('upts'))

@@ -1,0 +1,145 @@
+"""Interior interfaces of the Euler and Navier-Stokes systems.
+
+Builds the left/right gather views over the flux-point fields and the
+scaled left normals, with the reference's memory-access permutation (all
+interface arrays ordered by the left side's flux-point address,
+``pyfr/solvers/base/inters.py:70-90``,
+``pyfr/solvers/baseadvec/inters.py:8-28``), and declares the interface
+kernels (``pyfr/solvers/euler/inters.py:28-38``,
+``pyfr/solvers/navstokes/inters.py:29-48``).
+"""
+
+import numpy as np
+
+
+def inter_arrays(side, meth, elemap, perm=Ellipsis):
+    """Concatenate the per-(etype, face) arrays of ``meth`` in interface
+    order, then apply ``perm``."""
+    parts, reorder = [], []
+    for etype, fidx, eidxs, idx in side.foreach():
+        parts.append(getattr(elemap[etype], meth)(eidxs, fidx))
+        reorder.append(np.repeat(idx, elemap[etype].nfacefpts[fidx]))
+
+    if not parts:
+        return []
+
+    ro = np.argsort(np.concatenate(reorder), kind='stable')[perm]
+    return [np.concatenate(a)[ro] for a in zip(*parts)]
+
+
+def field_view_arrays(side, field, elemap):
+    """(matmap, rowmap, colmap) of a flux-point field over one side."""
+    matmap, rowmap, colmap, reorder = [], [], [], []
+    for etype, fidx, eidxs, idx in side.foreach():
+        mat, eles = field[etype], elemap[etype]
+        fpts = eles.srtd_face_fpts[fidx][eidxs]
+        nfp = fpts.shape[1]
+        matmap.append(np.full(len(eidxs)*nfp, mat.mid))
+        rowmap.append(fpts.ravel())
+        colmap.append(np.repeat(eidxs, nfp))
+        reorder.append(np.repeat(idx, nfp))
+
+    ro = np.argsort(np.concatenate(reorder), kind='stable')
+    return (np.concatenate(matmap)[ro], np.concatenate(rowmap)[ro],
+            np.concatenate(colmap)[ro])
+
+
+class BaseIntInters:
+    def __init__(self, be, lhs, rhs, elemap, cfg):
+        self._be = be
+        self.elemap = elemap
+        self.cfg = cfg
+        self.lhs, self.rhs = lhs, rhs
+
+        first = next(iter(elemap.values()))
+        self.ndims, self.nvars = first.ndims, first.nvars
+        self.ninters = len(lhs)
+        self.ninterfpts = sum(elemap[et].nfacefpts[fi]*len(ei)
+                              for et, fi, ei in lhs.items())
+
+        self.c = cfg.items_as('constants', float)
+        self.kernels = {}
+
+        # Order all interface arrays by the left side's flux-point address
+        scal = {t: e._scal_fpts for t, e in elemap.items()}
+        self._perm = self._perm_for_field(self._perm_side(), scal)
+        self._pnorm_lhs = self._const_mat(lhs, 'get_pnorms_for_inters')
+
+    def _perm_side(self):
+        return self.lhs
+
+    def _perm_for_field(self, side, field):
+        m, r, c = field_view_arrays(side, field, self.elemap)
+        v = self._be.view(m, r, c, vshape=())
+        return np.argsort(v.mapping._host[0], kind='stable')
+
+    def _const_mat(self, side, meth):
+        m = inter_arrays(side, meth, self.elemap, self._perm)
+        m = m[0] if m else np.empty((0, self.ndims))
+        return self._be.const_matrix(np.atleast_2d(m.T))
+
+    def _view(self, side, meth, vshape=()):
+        vm = inter_arrays(side, meth, self.elemap, self._perm)
+        return self._be.view(*vm, vshape=vshape)
+
+    def _scal_view(self, side, meth):
+        return self._view(side, meth, (self.nvars,))
+
+    def _vect_view(self, side, meth):
+        return self._view(side, meth, (self.ndims, self.nvars))
+
+
+class EulerIntInters(BaseIntInters):
+    def __init__(self, *args, **kwargs):
+        super().__init__(*args, **kwargs)
+
+        rsolver = self.cfg.get('solver-interfaces', 'riemann-solver')
+        p_min = self.cfg.getfloat('solver-interfaces', 'p-min',
+                                  5*self._be.fpdtype_eps)
+        self._tplargs = dict(ndims=self.ndims, nvars=self.nvars,
+                             rsolver=rsolver, c=self.c, p_min=p_min)
+
+        self._be.pointwise.register('pyfr.solvers.euler.kernels.intcflux')
+        self.kernels['comm_flux'] = lambda: self._be.kernel(
+            'intcflux', tplargs=self._tplargs, dims=[self.ninterfpts],
+            ul=self.scal_lhs, ur=self.scal_rhs, nl=self._pnorm_lhs)
+
+
+class NavierStokesIntInters(BaseIntInters):
+    def __init__(self, be, lhs, rhs, elemap, cfg):
+        self.cfg = cfg
+        super().__init__(be, lhs, rhs, elemap, cfg)
+
+        self._vect_lhs = self._vect_view(lhs, 'get_vect_fpts_for_inters')
+        self._vect_rhs = self._vect_view(rhs, 'get_vect_fpts_for_inters')
+        self._comm_lhs = self._scal_view(lhs, 'get_comm_fpts_for_inters')
+        self._comm_rhs = self._scal_view(rhs, 'get_comm_fpts_for_inters')
+
+        self.c |= cfg.items_as('solver-interfaces', float)
+
+        rsolver = cfg.get('solver-interfaces', 'riemann-solver')
+        visc_corr = cfg.get('solver', 'viscosity-correction', 'none')
+        p_min = cfg.getfloat('solver-interfaces', 'p-min',
+                             5*self._be.fpdtype_eps)
+        self._tplargs = dict(ndims=self.ndims, nvars=self.nvars,
+                             rsolver=rsolver, visc_corr=visc_corr,
+                             shock_capturing='none', c=self.c, p_min=p_min)
+
+        be = self._be
+        be.pointwise.register('pyfr.solvers.navstokes.kernels.intconu')
+        be.pointwise.register('pyfr.solvers.navstokes.kernels.intcflux')
+
+        self.kernels['con_u'] = lambda: be.kernel(
+            'intconu', tplargs=self._tplargs, dims=[self.ninterfpts],
+            ulin=self.scal_lhs, urin=self.scal_rhs,
+            ulout=self._comm_lhs, urout=self._comm_rhs)
+        self.kernels['comm_flux'] = lambda: be.kernel(
+            'intcflux', tplargs=self._tplargs, dims=[self.ninterfpts],
+            ul=self.scal_lhs, ur=self.scal_rhs,
+            gradul=self._vect_lhs, gradur=self._vect_rhs, nl=self._pnorm_lhs)
+
+    def _perm_side(self):
+        # For beta = -1/2 order by the right side instead
+        # (pyfr/solvers/baseadvecdiff/inters.py:21-28)
+        beta = self.cfg.getfloat('solver-interfaces', 'ldg-beta')
+        return self.lhs if beta != -0.5 else self.rhs

@@ -1,0 +1,290 @@
+"""Systems: element loading, register banks, interface views, kernel
+generation and the per-RHS dependency graphs.
+
+``EulerSystem.rhs`` runs two graphs and ``NavierStokesSystem.rhs`` three,
+with the kernel order, dependencies and fusion groups of
+``pyfr/solvers/baseadvec/system.py:57-136`` and
+``pyfr/solvers/baseadvecdiff/system.py:53-231``; the gradient-only pass
+for diagnostics follows ``pyfr/solvers/baseadvecdiff/system.py:233-286``.
+"""
+
+from collections import defaultdict
+from itertools import count, zip_longest
+import inspect
+
+import numpy as np
+
+from pyfr_gb300.backend.types import NullKernel
+from pyfr_gb300.solvers.elements import EulerElements, NavierStokesElements
+from pyfr_gb300.solvers.inters import (EulerIntInters, NavierStokesIntInters,
+                                       field_view_arrays)
+
+
+class BaseSystem:
+    elementscls = None
+    intinterscls = None
+    _nonce_seq = count()
+
+    def __init__(self, backend, mesh, initsoln, nregs, cfg):
+        self.backend = backend
+        self.mesh = mesh
+        self.cfg = cfg
+        self.ndims = mesh.ndims
+        self.nonce = nonce = str(next(self._nonce_seq))
+
+        # Elements and initial conditions
+        elemap = {et: self.elementscls(et, spts, cfg)
+                  for et, spts in mesh.spts.items()}
+        eles = list(elemap.values())
+        self.nvars = eles[0].nvars
+
+        if initsoln is not None:
+            ics = [np.asarray(initsoln[et]) for et in elemap]
+        else:
+            ics = [e.set_ics_from_cfg() for e in eles]
+
+        for et, e in elemap.items():
+            curved = mesh.spts_curved.get(et, np.zeros(e.neles, dtype=bool))
+            linoff = np.max(*np.nonzero(curved), initial=-1) + 1
+            e.set_backend(backend, nonce, linoff)
+        backend.commit()
+
+        self.ele_map = elemap
+        self.ele_types = list(elemap)
+        self.ele_ndofs = [e.neles*e.nupts*e.nvars for e in eles]
+        self.ele_shapes = {et: (e.nupts, e.nvars, e.neles)
+                           for et, e in elemap.items()}
+        self.ele_ploc_upts = [e.ploc_at_np('upts') for e in eles]
+
+        # Register banks (all of them hold right-hand-side data)
+        self.nrhs = nregs
+        self.ele_banks = [[e.alloc_bank(f'bank_{id(e)}_{i}',
+                                        ic if i == 0 else None)
+                           for i in range(nregs)] for e, ic in zip(eles, ics)]
+        backend.commit()
+
+        lhs, rhs = mesh.con
+        self._int_inters = [self.intinterscls(backend, lhs, rhs, elemap, cfg)]
+
+    @property
+    def gndofs(self):
+        return sum(self.ele_ndofs)
+
+    def make_field_views(self, field, vshape=()):
+        out = []
+        for i in self._int_inters:
+            views = []
+            for side in (i.lhs, i.rhs):
+                m, r, c = field_view_arrays(side, field, self.ele_map)
+                p = i._perm
+                views.append(self.backend.view(m[p], r[p], c[p],
+                                               vshape=vshape))
+            out.append(tuple(views))
+        return out
+
+    def commit(self):
+        scal = {et: e._scal_fpts for et, e in self.ele_map.items()}
+        for i, (l, r) in zip(self._int_inters, self.make_field_views(
+                scal, vshape=(self.nvars,))):
+            i.scal_lhs, i.scal_rhs = l, r
+
+        self.backend.commit()
+        self._gen_kernels()
+        self.backend.commit()
+        self._graph_cache = {}
+
+    def _gen_kernels(self):
+        self._kernels = kernels = defaultdict(list)
+        self._ktags = {}
+
+        provs = [('eles', list(self.ele_map.values())),
+                 ('iint', self._int_inters)]
+        for pn, plist in provs:
+            for p in plist:
+                for kn, kget in p.kernels.items():
+                    params = inspect.signature(kget).parameters
+                    if 'uin' in params or 'fout' in params:
+                        for i in range(self.nrhs):
+                            k = kget(i)
+                            if isinstance(k, NullKernel):
+                                continue
+                            key = (f'{pn}/{kn}', i, None) if 'uin' in params \
+                                else (f'{pn}/{kn}', None, i)
+                            kernels[key].append(k)
+                            self._ktags[k] = f'{pn}/{id(p)}'
+                    else:
+                        k = kget()
+                        if isinstance(k, NullKernel):
+                            continue
+                        kernels[f'{pn}/{kn}', None, None].append(k)
+                        self._ktags[k] = f'{pn}/{id(p)}'
+
+    def _get_kernels(self, uinbank, foutbank):
+        kernels = defaultdict(list)
+        for (kn, ui, fo), k in self._kernels.items():
+            if ((ui is None and fo is None) or
+                    (ui is not None and ui == uinbank) or
+                    (fo is not None and fo == foutbank)):
+                kernels[kn].extend(k)
+        return kernels
+
+    def _kdeps(self, kdict, kern, *dnames):
+        return [k for n in dnames for k in kdict[n]
+                if self._ktags[kern] == self._ktags[k]]
+
+    def _group(self, g, kerns, subs=[]):
+        kerns = [k for k in kerns if k is not None]
+        subs = [[(k, n) for k, n in s if k] for s in subs]
+        g.group(kerns, [s for s in subs if len(s) > 1])
+
+    def _rhs_graphs_cached(self, uin, fout):
+        key = ('rhs', uin, fout)
+        if key not in self._graph_cache:
+            self._graph_cache[key] = self._rhs_graphs(uin, fout)
+        return self._graph_cache[key]
+
+    def rhs_graphs(self, uinbank, foutbank):
+        return self._rhs_graphs_cached(uinbank, foutbank)
+
+    def rhs(self, t, uinbank, foutbank):
+        if uinbank >= self.nrhs or foutbank >= self.nrhs:
+            raise ValueError('Invalid register numbers')
+        for g in self._rhs_graphs_cached(uinbank, foutbank):
+            self.backend.run_graph(g)
+
+    def ele_scal_upts(self, idx):
+        return [eb[idx].get() for eb in self.ele_banks]
+
+    def set_ele_scal_upts(self, idx, arrs):
+        for eb, a in zip(self.ele_banks, arrs):
+            eb[idx].set(a)
+
+
+class EulerSystem(BaseSystem):
+    name = 'euler'
+    elementscls = EulerElements
+    intinterscls = EulerIntInters
+
+    def _rhs_graphs(self, uinbank, foutbank):
+        k = self._get_kernels(uinbank, foutbank)
+
+        def deps(dk, *names):
+            return self._kdeps(k, dk, *names)
+
+        g_intf = self.backend.graph()
+        g_intf.add_all(k['eles/disu'])
+        g_intf.add_all(k['iint/comm_flux'], deps=k['eles/disu'])
+        g_intf.commit()
+
+        g_flux_div = self.backend.graph()
+        for l in k['eles/tdisf']:
+            g_flux_div.add(l)
+        for l in k['eles/tdivtpcorf']:
+            g_flux_div.add(l, deps=deps(l, 'eles/tdisf'))
+        for l in k['eles/tdivtconf']:
+            g_flux_div.add(l, deps=deps(l, 'eles/tdivtpcorf'))
+        for l in k['eles/negdivconf']:
+            g_flux_div.add(l, deps=deps(l, 'eles/tdivtconf'))
+
+        kgroup = [k['eles/tdisf'], k['eles/tdivtpcorf'], k['eles/tdivtconf'],
+                  k['eles/negdivconf']]
+        for ks in zip_longest(*kgroup):
+            self._group(g_flux_div, ks, subs=[[(ks[0], 'f'), (ks[1], 'b')]])
+        g_flux_div.commit()
+
+        return g_intf, g_flux_div
+
+
+class NavierStokesSystem(BaseSystem):
+    name = 'navier-stokes'
+    elementscls = NavierStokesElements
+    intinterscls = NavierStokesIntInters
+
+    def _rhs_graphs(self, uinbank, foutbank):
+        k = self._get_kernels(uinbank, foutbank)
+
+        def deps(dk, *names):
+            return self._kdeps(k, dk, *names)
+
+        # Graph 1: solution at the flux points and the common solution
+        g_soln = self.backend.graph()
+        g_soln.add_all(k['eles/disu'])
+        for l in k['eles/copy_fpts']:
+            g_soln.add(l, deps=deps(l, 'eles/disu'))
+        kdeps = k['eles/copy_fpts'] or k['eles/disu']
+        g_soln.add_all(k['iint/con_u'], deps=kdeps)
+        g_soln.commit()
+
+        # Graph 2: corrected gradient, fused flux, face gradients, common
+        # flux and the divergence of the partially corrected flux
+        g_grad_flux = self.backend.graph()
+        g_grad_flux.add_all(k['eles/tgradpcoru_upts'])
+        for l in k['eles/tgradcoru_upts']:
+            g_grad_flux.add(l, deps=deps(l, 'eles/tgradpcoru_upts'))
+        for l in k['eles/tdisf_fused']:
+            g_grad_flux.add(l, deps=deps(l, 'eles/tgradcoru_upts'))
+        for l in k['eles/gradcoru_fpts']:
+            g_grad_flux.add(l, deps=deps(l, 'eles/tdisf_fused'))
+        g_grad_flux.add_all(k['iint/comm_flux'], deps=k['eles/gradcoru_fpts'])
+        for l in k['eles/tdivtpcorf']:
+            g_grad_flux.add(l, deps=deps(l, 'eles/tdisf_fused'))
+
+        kgroup = [k['eles/tgradpcoru_upts'], k['eles/tgradcoru_upts'],
+                  k['eles/tdisf_fused'], k['eles/gradcoru_fpts'],
+                  k['eles/tdivtpcorf']]
+        for ks in zip_longest(*kgroup):
+            self._group(g_grad_flux, ks, subs=[
+                [(ks[0], 'out'), (ks[1], 'out'), (ks[2], 'gradu'),
+                 (ks[3], 'b')],
+                [(ks[2], 'f'), (ks[4], 'b')],
+            ])
+        g_grad_flux.commit()
+
+        # Graph 3: correction and physical divergence
+        g_div = self.backend.graph()
+        g_div.add_all(k['eles/tdivtconf'])
+        for l in k['eles/negdivconf']:
+            g_div.add(l, deps=deps(l, 'eles/tdivtconf'))
+        for k1, k2 in zip_longest(k['eles/tdivtconf'], k['eles/negdivconf']):
+            self._group(g_div, [k1, k2])
+        g_div.commit()
+
+        return g_soln, g_grad_flux, g_div
+
+    def _compute_grads_graph(self, uinbank):
+        key = ('grads', uinbank)
+        if key in self._graph_cache:
+            return self._graph_cache[key]
+
+        k = self._get_kernels(uinbank, None)
+
+        def deps(dk, *names):
+            return self._kdeps(k, dk, *names)
+
+        g = self.backend.graph()
+        g.add_all(k['eles/disu'])
+        for l in k['eles/copy_fpts']:
+            g.add(l, deps=deps(l, 'eles/disu'))
+        kdeps = k['eles/copy_fpts'] or k['eles/disu']
+        g.add_all(k['iint/con_u'], deps=kdeps)
+        g.add_all(k['eles/tgradpcoru_upts'], deps=k['iint/con_u'])
+        for l in k['eles/tgradcoru_upts']:
+            g.add(l, deps=deps(l, 'eles/tgradpcoru_upts') + k['iint/con_u'])
+        for l in k['eles/gradcoru_u']:
+            g.add(l, deps=deps(l, 'eles/tgradcoru_upts'))
+        g.commit()
+
+        self._graph_cache[key] = (g,)
+        return (g,)
+
+    def compute_grads(self, t, uinbank):
+        for g in self._compute_grads_graph(uinbank):
+            self.backend.run_graph(g)
+
+    def grad_upts(self):
+        """Physical gradients (ndims, nupts, nvars, neles) per element type
+        after ``compute_grads``."""
+        return [e._grad_upts.get() for e in self.ele_map.values()]
+
+
+SYSTEMS = {'euler': EulerSystem, 'navier-stokes': NavierStokesSystem}

@@ -1,0 +1,197 @@
+"""Generate golden fixtures from the reference implementation itself.
+
+Run in a container that has the PyFR source tree (read-only) at
+/root/reference; the GPU hosts do not need it, they use the committed
+``.npz`` files this script writes next to itself:
+
+  python tests/golden/make_golden.py
+
+What is generated (all with the reference's own code):
+
+* ``operators.npz``: for each (shape, order, point set) the operator
+  matrices m0, m1, m2, m3, m4, m6 and the combined expressions
+  'M1 - M3*M2', 'M4 - M6*M0' from ``pyfr.shapes`` (``opmat``), plus the
+  solution/flux points, face normals and face point lists.  Before writing,
+  the hex p=3 Gauss-Legendre matrices are checked against the reference's
+  own golden file ``pyfr/tests/hex-gleg-ord3.npz`` (its unit test
+  ``pyfr/tests/test_ele_mats.py``).
+* ``geometry_<case>.npz``: element geometry computed by the reference's
+  ``EulerElements``/``NavierStokesElements`` (``pyfr/solvers/base/elements.py``)
+  on small periodic meshes whose interior vertices are randomly perturbed
+  (valid multilinear elements): sorted face flux points, scaled normals,
+  1/|J| at the solution points, metric terms and physical point locations,
+  and the initial conditions evaluated by ``set_ics_from_cfg``.
+
+The reference needs third-party packages that are not installed here
+(platformdirs, mako, h5py, mpi4py, gimmik, pytools, rtree); none of them is
+used by the code paths above, so empty stand-in modules are registered
+before importing it.
+"""
+
+from io import BytesIO
+from pathlib import Path
+import sys
+import types
+
+import numpy as np
+
+REF = Path('/root/reference')
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parent.parent
+
+
+def _install_standins():
+    class _Any:
+        def __init__(self, *a, **k):
+            pass
+
+        def __call__(self, *a, **k):
+            return _Any()
+
+        def __getattr__(self, n):
+            return _Any()
+
+        def __mro_entries__(self, bases):
+            return (object,)
+
+    for name in ['platformdirs', 'mako', 'mako.lookup', 'mako.template',
+                 'mako.runtime', 'mako.exceptions', 'h5py', 'mpi4py',
+                 'mpi4py.MPI', 'gimmik', 'pytools', 'pytools.prefork',
+                 'rtree', 'rtree.index']:
+        m = types.ModuleType(name)
+        m.__getattr__ = lambda n: _Any()
+        m.__path__ = []
+        sys.modules[name] = m
+
+    sys.modules['platformdirs'].user_cache_dir = lambda *a, **k: '/tmp/pyfrc'
+    sys.modules['mpi4py.MPI'].__file__ = 'libc.so.6'
+    sys.modules['mpi4py'].MPI = sys.modules['mpi4py.MPI']
+
+
+def _cfg(etype, order, upts, fpts, consts=None, ics=None, extra=()):
+    from pyfr.inifile import Inifile
+
+    cfg = Inifile()
+    cfg.set('solver', 'order', str(order))
+    fkind = {'quad': 'line', 'hex': 'quad'}[etype]
+    cfg.set(f'solver-interfaces-{fkind}', 'flux-pts', fpts)
+    cfg.set(f'solver-elements-{etype}', 'soln-pts', upts)
+    for k, v in (consts or {}).items():
+        cfg.set('constants', k, repr(v))
+    for k, v in (ics or {}).items():
+        cfg.set('soln-ics', k, v)
+    for s, k, v in extra:
+        cfg.set(s, k, v)
+    return cfg
+
+
+OPERATOR_CASES = [
+    ('quad', 2, 'gauss-legendre'), ('quad', 3, 'gauss-legendre'),
+    ('quad', 4, 'gauss-legendre'), ('quad', 3, 'gauss-legendre-lobatto'),
+    ('hex', 2, 'gauss-legendre'), ('hex', 3, 'gauss-legendre'),
+    ('hex', 4, 'gauss-legendre'),
+]
+
+
+def make_operators():
+    from pyfr.shapes import HexShape, QuadShape
+
+    shapes = {'quad': QuadShape, 'hex': HexShape}
+    out = {}
+    for etype, order, pts in OPERATOR_CASES:
+        cfg = _cfg(etype, order, pts, pts)
+        s = shapes[etype](None, cfg)
+        key = f'{etype}_p{order}_{pts}'
+        for m in ('m0', 'm1', 'm2', 'm3', 'm4', 'm6'):
+            out[f'{key}/{m}'] = getattr(s, m)
+        out[f'{key}/M132'] = s.opmat('M1 - M3*M2')
+        out[f'{key}/M460'] = s.opmat('M4 - M6*M0')
+        out[f'{key}/upts'] = s.upts
+        out[f'{key}/fpts'] = s.fpts
+        out[f'{key}/norm_fpts'] = s.norm_fpts
+        out[f'{key}/nfacefpts'] = np.array(s.nfacefpts)
+
+    # The reference's own golden values for hex p=3 (test_ele_mats.py)
+    ref = np.load(BytesIO((REF / 'pyfr/tests/hex-gleg-ord3.npz').read_bytes()))
+    for m in ('m0', 'm1', 'm2', 'm3'):
+        if not np.allclose(ref[m], out[f'hex_p3_gauss-legendre/{m}']):
+            raise RuntimeError(f'reference {m} does not match its golden file')
+        out[f'refgolden/hex_p3/{m}'] = ref[m]
+
+    np.savez_compressed(HERE / 'operators.npz', **out)
+    print('operators.npz:', len(out), 'arrays')
+
+
+def perturbed_box(etype, n, lo, hi, amp, seed):
+    """Periodic box with interior vertices jittered (same jitter on
+    periodic images so the mesh stays periodic)."""
+    sys.path.insert(0, str(REPO))
+    from pyfr_gb300.mesh import periodic_box
+
+    mesh = periodic_box(etype, n, lo, hi)
+    ndims = mesh.ndims
+    h = (hi - lo)/n
+    rng = np.random.default_rng(seed)
+    jit = rng.uniform(-amp*h, amp*h, size=(n,)*ndims + (ndims,))
+
+    spts = mesh.spts[etype]
+    for v in range(spts.shape[0]):
+        idx = np.rint((spts[v] - lo)/h).astype(int) % n      # (neles, ndims)
+        spts[v] += jit[tuple(idx[:, d] for d in range(ndims))]
+    return mesh
+
+
+GEOM_CASES = {
+    'quad_p3': dict(etype='quad', order=3, n=4, system='euler'),
+    'hex_p3': dict(etype='hex', order=3, n=3, system='navier-stokes'),
+}
+
+
+def make_geometry():
+    from pyfr.shapes import HexShape, QuadShape
+    from pyfr.solvers.euler.elements import EulerElements
+    from pyfr.solvers.navstokes.elements import NavierStokesElements
+
+    shapes = {'quad': QuadShape, 'hex': HexShape}
+    for name, c in GEOM_CASES.items():
+        etype, order, n = c['etype'], c['order'], c['n']
+        mesh = perturbed_box(etype, n, -1.0, 1.0, 0.12, seed=7)
+        spts = mesh.spts[etype]
+
+        if etype == 'quad':
+            ics = dict(rho='1 + 0.2*sin(pi*x)*cos(pi*y)', u='0.5 + 0.1*y',
+                       v='-0.3 + 0.1*x', p='1 + 0.1*cos(pi*x)')
+            elescls = EulerElements
+        else:
+            ics = dict(rho='1 + 0.2*sin(pi*x)*cos(pi*y)*cos(pi*z)',
+                       u='0.5 + 0.1*y', v='-0.3 + 0.1*z', w='0.2*x',
+                       p='1 + 0.1*cos(pi*x)')
+            elescls = NavierStokesElements
+
+        cfg = _cfg(etype, order, 'gauss-legendre', 'gauss-legendre',
+                   consts=dict(gamma=1.4), ics=ics)
+        e = elescls(shapes[etype], spts, cfg)
+
+        out = dict(spts=spts, upts=e.basis.upts, fpts=e.basis.fpts)
+        for fi, sf in enumerate(e.srtd_face_fpts):
+            out[f'srtd_face_fpts/{fi}'] = sf
+        out['pnorm_fpts'] = e._pnorm_fpts
+        out['rcpdjac_upts'] = e.rcpdjac_at_np('upts')
+        out['smat_upts'] = e.smat_at_np('upts')
+        out['ploc_upts'] = e.ploc_at_np('upts')
+        out['ics'] = e.set_ics_from_cfg()
+        lhs, rhs = mesh.con
+        out['lhs'] = np.stack([lhs.eidxs, lhs.fidxs], axis=1)
+        out['rhs'] = np.stack([rhs.eidxs, rhs.fidxs], axis=1)
+        for k, v in ics.items():
+            out[f'icexpr/{k}'] = np.array(v)
+
+        np.savez_compressed(HERE / f'geometry_{name}.npz', **out)
+        print(f'geometry_{name}.npz')
+
+
+if __name__ == '__main__':
+    sys.path.insert(0, str(REF))
+    _install_standins()
+    make_operators()
+    make_geometry()

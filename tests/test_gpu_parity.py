@@ -1,0 +1,232 @@
+"""Parity of the CUDA path (through the b200 backend and the C ABI) with the
+CPU oracle.  Plain FP64: relative max-norm tolerance 1e-10 on every
+conserved variable, as required of the plain form."""
+import numpy as np
+import pytest
+
+from oracle.fr_oracle import rk45_step
+from tests.oracle_util import basis_of, disc_for_mesh, ops_from_golden
+from oracle.fr_oracle import Discretisation
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+
+
+def _relerr(a, b):
+    return np.abs(a - b).max()/max(np.abs(b).max(), 1e-300)
+
+
+@pytest.fixture(scope='module')
+def built():
+    import __graft_entry__ as ge
+    ge.build_library()
+
+
+def _backend(cfg, graphs=True):
+    from pyfr_gb300.backend import B200Backend
+    cfg.set('backend-b200', 'cuda-graphs', str(graphs).lower())
+    return B200Backend(cfg)
+
+
+def _golden_mesh(g, etype):
+    from pyfr_gb300.mesh import Mesh, Side
+    n = len(g['lhs'])
+    lhs = Side([etype]*n, g['lhs'][:, 0], g['lhs'][:, 1])
+    rhs = Side([etype]*n, g['rhs'][:, 0], g['rhs'][:, 1])
+    nd = g['spts'].shape[2]
+    return Mesh(ndims=nd, spts={etype: g['spts']}, con=(lhs, rhs),
+                spts_curved={etype: np.zeros(g['spts'].shape[1], bool)},
+                periods=(2.0,)*nd)
+
+
+# ---------------------------------------------------------------------------
+
+@pytest.mark.parametrize('key', ['quad_p3_gauss-legendre', 'hex_p3_gauss-legendre',
+                                 'hex_p4_gauss-legendre', 'quad_p2_gauss-legendre'])
+@pytest.mark.parametrize('opname', ['m0', 'M132', 'm3', 'M460', 'm6'])
+def test_mul_matches_numpy(built, golden, key, opname):
+    from pyfr_gb300.inifile import Inifile
+    a = golden['operators'][f'{key}/{opname}']
+    cfg = Inifile()
+    be = _backend(cfg)
+    rng = np.random.default_rng(3)
+    nvars, neles = 5, 77
+    b = rng.normal(size=(a.shape[1], nvars, neles))
+    c0 = rng.normal(size=(a.shape[0], nvars, neles))
+
+    A = be.const_matrix(a)
+    B = be.matrix(b.shape, b, tags={'align'})
+    C = be.matrix(c0.shape, c0, tags={'align'})
+    be.commit()
+
+    for alpha, beta in [(1.0, 0.0), (2.0, 1.0), (-0.5, 0.25)]:
+        C.set(c0)
+        be.run_kernels([be.kernel('mul', A, B, out=C, alpha=alpha, beta=beta)],
+                       wait=True)
+        ref = alpha*np.einsum('mk,kve->mve', a, b) + beta*c0
+        np.testing.assert_allclose(C.get(), ref, rtol=1e-13, atol=1e-13)
+
+
+@pytest.mark.parametrize('rsolver', ['rusanov', 'hllc'])
+def test_euler_rhs_vortex(built, rsolver):
+    from pyfr_gb300.cases import euler_vortex
+    from pyfr_gb300.solvers.system import EulerSystem
+    cfg, mesh = euler_vortex(n=12, order=3, rsolver=rsolver)
+    be = _backend(cfg)
+    s = EulerSystem(be, mesh, None, 2, cfg)
+    s.commit()
+    s.rhs(0.0, 0, 1)
+    (u,), (r,) = s.ele_scal_upts(0), s.ele_scal_upts(1)
+
+    d = disc_for_mesh(mesh, 3)
+    ref = d.rhs_euler(u, cfg.items_as('constants', float), rsolver)
+    assert _relerr(r, ref) < TOL
+
+
+def test_euler_rhs_distorted_mesh_reference_geometry(built, golden):
+    """Distorted periodic quads; the oracle uses the reference's operator
+    matrices and the reference's initial condition."""
+    from pyfr_gb300.inifile import Inifile
+    from pyfr_gb300.solvers.system import EulerSystem
+    from pyfr_gb300.shapes import get_shape
+    g = golden['geometry_quad_p3']
+    mesh = _golden_mesh(g, 'quad')
+    cfg = Inifile()
+    cfg.set('constants', 'gamma', 1.4)
+    cfg.set('solver', 'order', 3)
+    cfg.set('solver-interfaces', 'riemann-solver', 'rusanov')
+    be = _backend(cfg)
+    s = EulerSystem(be, mesh, {'quad': g['ics']}, 2, cfg)
+    s.commit()
+    s.rhs(0.0, 0, 1)
+    (r,) = s.ele_scal_upts(1)
+
+    ops = ops_from_golden(golden['operators'], 'quad_p3_gauss-legendre')
+    d = Discretisation(ops, basis_of(get_shape('quad', 3)), g['spts'],
+                       g['lhs'], g['rhs'], periods=(2.0, 2.0))
+    ref = d.rhs_euler(g['ics'], dict(gamma=1.4))
+    assert _relerr(r, ref) < TOL
+
+
+def test_ns_rhs_distorted_hex_reference_geometry(built, golden):
+    from pyfr_gb300.inifile import Inifile
+    from pyfr_gb300.solvers.system import NavierStokesSystem
+    from pyfr_gb300.shapes import get_shape
+    g = golden['geometry_hex_p3']
+    mesh = _golden_mesh(g, 'hex')
+    cfg = Inifile()
+    for k, v in dict(gamma=1.4, mu=0.05, Pr=0.72).items():
+        cfg.set('constants', k, v)
+    cfg.set('solver', 'order', 3)
+    cfg.set('solver-interfaces', 'riemann-solver', 'rusanov')
+    cfg.set('solver-interfaces', 'ldg-beta', 0.5)
+    cfg.set('solver-interfaces', 'ldg-tau', 0.1)
+    be = _backend(cfg)
+    s = NavierStokesSystem(be, mesh, {'hex': g['ics']}, 2, cfg)
+    s.commit()
+    s.rhs(0.0, 0, 1)
+    (r,) = s.ele_scal_upts(1)
+
+    ops = ops_from_golden(golden['operators'], 'hex_p3_gauss-legendre', True)
+    d = Discretisation(ops, basis_of(get_shape('hex', 3)), g['spts'],
+                       g['lhs'], g['rhs'], periods=(2.0,)*3)
+    c = dict(gamma=1.4, mu=0.05, Pr=0.72, **{'ldg-beta': 0.5, 'ldg-tau': 0.1})
+    ref = d.rhs_ns(g['ics'], c)
+    assert _relerr(r, ref) < TOL
+
+
+@pytest.mark.parametrize('beta,tau,rsolver', [(0.5, 0.1, 'rusanov'),
+                                              (0.0, 0.2, 'hllc'),
+                                              (-0.5, 0.0, 'rusanov')])
+def test_ns_rhs_tgv(built, beta, tau, rsolver):
+    from pyfr_gb300.cases import ns_tgv
+    from pyfr_gb300.solvers.system import NavierStokesSystem
+    cfg, mesh = ns_tgv(n=5, order=3, beta=beta, tau=tau, rsolver=rsolver)
+    be = _backend(cfg)
+    s = NavierStokesSystem(be, mesh, None, 2, cfg)
+    s.commit()
+    s.rhs(0.0, 0, 1)
+    (u,), (r,) = s.ele_scal_upts(0), s.ele_scal_upts(1)
+
+    d = disc_for_mesh(mesh, 3, ns=True)
+    c = cfg.items_as('constants', float) | cfg.items_as('solver-interfaces',
+                                                       float)
+    ref = d.rhs_ns(u, c, rsolver)
+    assert _relerr(r, ref) < TOL
+
+
+@pytest.mark.parametrize('graphs', [True, False])
+def test_rk45_vortex_steps(built, graphs):
+    from pyfr_gb300.cases import euler_vortex
+    from pyfr_gb300.integrators import RKVdH2Integrator
+    from pyfr_gb300.solvers.system import EulerSystem
+    cfg, mesh = euler_vortex(n=10, order=3, dt=2e-3)
+    be = _backend(cfg, graphs)
+    intg = RKVdH2Integrator(be, EulerSystem, mesh, cfg)
+    (u,) = intg.soln
+    intg.run_steps(10)
+    (ug,) = intg.soln
+
+    d = disc_for_mesh(mesh, 3)
+    c = cfg.items_as('constants', float)
+    for _ in range(10):
+        u = rk45_step(lambda x: d.rhs_euler(x, c), u, intg.dt)
+    assert _relerr(ug, u) < TOL
+
+
+def test_rk45_tgv_steps(built):
+    from pyfr_gb300.cases import ns_tgv
+    from pyfr_gb300.integrators import RKVdH2Integrator
+    from pyfr_gb300.solvers.system import NavierStokesSystem
+    cfg, mesh = ns_tgv(n=4, order=3, dt=1e-3)
+    be = _backend(cfg)
+    intg = RKVdH2Integrator(be, NavierStokesSystem, mesh, cfg)
+    (u,) = intg.soln
+    intg.run_steps(3)
+    (ug,) = intg.soln
+
+    d = disc_for_mesh(mesh, 3, ns=True)
+    c = cfg.items_as('constants', float) | cfg.items_as('solver-interfaces',
+                                                       float)
+    for _ in range(3):
+        u = rk45_step(lambda x: d.rhs_ns(x, c), u, intg.dt)
+    assert _relerr(ug, u) < TOL
+
+
+def test_gradients_for_diagnostics(built):
+    from pyfr_gb300.cases import ns_tgv
+    from pyfr_gb300.solvers.system import NavierStokesSystem
+    cfg, mesh = ns_tgv(n=4, order=3)
+    be = _backend(cfg)
+    s = NavierStokesSystem(be, mesh, None, 2, cfg)
+    s.commit()
+    s.compute_grads(0.0, 0)
+    (g,) = s.grad_upts()
+    (u,) = s.ele_scal_upts(0)
+
+    d = disc_for_mesh(mesh, 3, ns=True)
+    c = cfg.items_as('constants', float) | cfg.items_as('solver-interfaces',
+                                                       float)
+    gl = []
+    d.rhs_ns(u, c, grads_out=gl)
+    assert _relerr(g, gl[0]) < TOL
+
+
+def test_pi_controller_error_norm(built):
+    from pyfr_gb300.inifile import Inifile
+    cfg = Inifile()
+    be = _backend(cfg)
+    rng = np.random.default_rng(5)
+    shape = (16, 4, 45)
+    cur, err = rng.normal(size=shape), 1e-6*rng.normal(size=shape)
+    C = be.matrix(shape, cur, tags={'align'})
+    E = be.matrix(shape, err, tags={'align'})
+    be.commit()
+    atols = [1e-6, 2e-6, 3e-6, 4e-6]
+    k = be.kernel('errest', C, E, atols)
+    k.bind(rtol=1e-5)
+    k.run(be.stream)
+    be.wait()
+    ref = np.sum((err/(np.array(atols)[None, :, None] + 1e-5*np.abs(cur)))**2)
+    assert abs(k.retval[0] - ref) <= 1e-12*ref

@@ -1,0 +1,55 @@
+"""Operator matrices against the reference's own values."""
+import numpy as np
+import pytest
+
+from pyfr_gb300.shapes import get_shape
+
+CASES = [('quad', 2, 'gauss-legendre'), ('quad', 3, 'gauss-legendre'),
+         ('quad', 4, 'gauss-legendre'), ('quad', 3, 'gauss-legendre-lobatto'),
+         ('hex', 2, 'gauss-legendre'), ('hex', 3, 'gauss-legendre'),
+         ('hex', 4, 'gauss-legendre')]
+
+
+@pytest.mark.parametrize('etype,order,pts', CASES)
+def test_operators_match_reference(golden, etype, order, pts):
+    ref = golden['operators']
+    key = f'{etype}_p{order}_{pts}'
+    s = get_shape(etype, order, pts, pts)
+
+    np.testing.assert_allclose(s.upts, ref[f'{key}/upts'], atol=1e-14)
+    np.testing.assert_allclose(s.fpts, ref[f'{key}/fpts'], atol=1e-14)
+    np.testing.assert_array_equal(s.norm_fpts, ref[f'{key}/norm_fpts'])
+    np.testing.assert_array_equal(s.nfacefpts, ref[f'{key}/nfacefpts'])
+
+    for m in ('m0', 'm1', 'm2', 'm3', 'm4', 'm6'):
+        np.testing.assert_allclose(getattr(s, m), ref[f'{key}/{m}'],
+                                   rtol=0, atol=1e-11, err_msg=m)
+    np.testing.assert_allclose(s.opmat('M1 - M3*M2'), ref[f'{key}/M132'],
+                               rtol=0, atol=1e-11)
+    np.testing.assert_allclose(s.opmat('M4 - M6*M0'), ref[f'{key}/M460'],
+                               rtol=0, atol=1e-11)
+
+
+@pytest.mark.parametrize('etype,order,pts', CASES)
+def test_sparsity_pattern_matches_reference(golden, etype, order, pts):
+    # Exact zeros drive the sparse operator kernels: patterns must agree
+    ref = golden['operators']
+    key = f'{etype}_p{order}_{pts}'
+    s = get_shape(etype, order, pts, pts)
+    for m, e in (('m0', 'M0'), ('m3', 'M3'), ('M132', 'M1 - M3*M2'),
+                 ('M460', 'M4 - M6*M0'), ('m6', 'M6')):
+        np.testing.assert_array_equal(s.opmat(e) != 0, ref[f'{key}/{m}'] != 0)
+
+
+def test_reference_golden_file(golden):
+    # pyfr/tests/test_ele_mats.py: hex p=3 Gauss-Legendre m0..m3
+    ref = golden['operators']
+    s = get_shape('hex', 3)
+    for m in ('m0', 'm1', 'm2', 'm3'):
+        assert np.allclose(getattr(s, m), ref[f'refgolden/hex_p3/{m}'])
+
+
+def test_opmat_rejects_bad_expression():
+    s = get_shape('quad', 2)
+    with pytest.raises(ValueError):
+        s.opmat('M0.__class__')

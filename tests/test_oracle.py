@@ -1,0 +1,78 @@
+"""The oracle against the reference's fixtures and physical invariants."""
+import numpy as np
+import pytest
+
+from oracle.fr_oracle import Discretisation, hllc, inviscid_flux, rusanov
+from tests.oracle_util import basis_of, ops_from_golden
+from pyfr_gb300.shapes import get_shape
+
+GAS = dict(gamma=1.4, mu=0.01, Pr=0.72, **{'ldg-beta': 0.5, 'ldg-tau': 0.1})
+
+
+def _disc(golden, case, etype, ns):
+    g = golden[f'geometry_{case}']
+    ops = ops_from_golden(golden['operators'], f'{etype}_p3_gauss-legendre',
+                          ns)
+    s = get_shape(etype, 3)
+    return Discretisation(ops, basis_of(s), g['spts'], g['lhs'], g['rhs'],
+                          periods=(2.0,)*s.ndims), g
+
+
+@pytest.mark.parametrize('case,etype', [('quad_p3', 'quad'), ('hex_p3', 'hex')])
+def test_oracle_geometry_is_the_references(golden, case, etype):
+    d, g = _disc(golden, case, etype, etype == 'hex')
+    np.testing.assert_allclose(1/d.djac_u, g['rcpdjac_upts'], rtol=1e-11)
+    np.testing.assert_allclose(d.pnorm.transpose(0, 2, 1), g['pnorm_fpts'],
+                               rtol=1e-11, atol=1e-13)
+
+
+@pytest.mark.parametrize('case,etype', [('quad_p3', 'quad'), ('hex_p3', 'hex')])
+def test_oracle_pairing_is_the_references(golden, case, etype):
+    # The reference pairs the k-th sorted flux point of each side
+    d, g = _disc(golden, case, etype, False)
+    srt = [g[f'srtd_face_fpts/{f}'] for f in range(len(d.facefpts))]
+    ref = set()
+    for (el, fl), (er, fr) in zip(g['lhs'], g['rhs']):
+        for a, b in zip(srt[fl][el], srt[fr][er]):
+            ref.add((a, el, b, er))
+    mine = {(a, el, b, er) for (a, el), (b, er) in zip(d.pl, d.pr)}
+    assert mine == ref
+
+
+@pytest.mark.parametrize('rs', [rusanov, hllc])
+def test_riemann_consistency_and_symmetry(rs):
+    rng = np.random.default_rng(1)
+    n = rng.normal(size=(3, 50))
+    n /= np.linalg.norm(n, axis=0)
+    u = np.stack([1 + 0.1*rng.random(50), *(0.3*rng.normal(size=(3, 50))),
+                  2.5 + 0.1*rng.random(50)])
+    u2 = u*(1 + 0.05*rng.normal(size=u.shape))
+    f, _, _ = inviscid_flux(u, 1.4)
+    np.testing.assert_allclose(rs(u, u, n, 1.4),
+                               np.einsum('dn,dvn->vn', n, f), atol=1e-13)
+    np.testing.assert_allclose(rs(u, u2, n, 1.4), -rs(u2, u, -n, 1.4),
+                               atol=1e-12)
+
+
+@pytest.mark.parametrize('case,etype', [('quad_p3', 'quad'), ('hex_p3', 'hex')])
+def test_free_stream_preserved_on_distorted_mesh(golden, case, etype):
+    d, g = _disc(golden, case, etype, etype == 'hex')
+    nd = d.ndims
+    cons = np.array([1.2, *[0.3*(i + 1) for i in range(nd)], 3.0])
+    u = np.broadcast_to(cons[None, :, None], (d.nupts, nd + 2, d.neles)).copy()
+    r = d.rhs_ns(u, GAS) if etype == 'hex' else d.rhs_euler(u, GAS)
+    assert np.abs(r).max() < 1e-11
+
+
+@pytest.mark.parametrize('case,etype', [('quad_p3', 'quad'), ('hex_p3', 'hex')])
+def test_discrete_conservation(golden, case, etype):
+    d, g = _disc(golden, case, etype, etype == 'hex')
+    u = g['ics']
+    r = d.rhs_ns(u, GAS) if etype == 'hex' else d.rhs_euler(u, GAS)
+    s = get_shape(etype, 3)
+    x, w = np.polynomial.legendre.leggauss(4)
+    wts = np.prod(np.array(np.meshgrid(*[w]*s.ndims, indexing='ij')), axis=0)
+    wts = wts.T.reshape(-1) if s.ndims == 2 else wts.transpose(2, 1, 0).reshape(-1)
+    tot = np.einsum('p,pve,pe->v', wts, r, d.djac_u)
+    scale = np.einsum('p,pve,pe->v', wts, np.abs(r), d.djac_u)
+    assert np.all(np.abs(tot) <= 1e-12*scale)
