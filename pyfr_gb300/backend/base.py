@@ -74,6 +74,8 @@ class B200Backend:
         # Execution options of this backend
         self.use_cuda_graphs = cfg.getbool('backend-b200', 'cuda-graphs', True)
         self.fusion = cfg.getbool('backend-b200', 'fusion', True)
+        self.precompute_metrics = cfg.getbool('backend-b200',
+                                              'precompute-metrics', True)
 
         self.mats = WeakValueDictionary()
         self._mat_counter = it.count()

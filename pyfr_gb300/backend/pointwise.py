@@ -33,6 +33,47 @@ def _mat(m):
     return m.data, m.leaddim
 
 
+def linear_metrics(verts, upts):
+    """Adjugate metric terms S[i][j] (ndims, nupts, ndims, neles) and 1/|J|
+    (nupts, neles) of multilinear elements at reference points ``upts``;
+    verts has io-shape (nverts, ndims, neles), vertex order
+    first-coordinate-fastest.  Same arithmetic as the kernels' in-place
+    computation (pyfr/solvers/baseadvec/kernels/smats.mako:3-25)."""
+    nverts, nd, ne = verts.shape
+    sg = np.array([[1.0 if (v >> d) & 1 else -1.0 for d in range(nd)]
+                   for v in range(nverts)])
+    x = np.asarray(upts, dtype=float)
+    dN = np.empty((len(x), nd, nverts))
+    for i in range(nd):
+        t = np.ones((len(x), nverts))
+        for k in range(nd):
+            t = t*(sg[None, :, k] if k == i else 1 + x[:, None, k]*sg[None, :, k])
+        dN[:, i] = t/nverts
+    J = np.einsum('piv,vje->pije', dN, verts)          # (p, i, j, e)
+    S = np.empty_like(J)
+    if nd == 2:
+        S[:, 0, 0], S[:, 0, 1] = J[:, 1, 1], -J[:, 1, 0]
+        S[:, 1, 0], S[:, 1, 1] = -J[:, 0, 1], J[:, 0, 0]
+        d = S[:, 0, 0]*S[:, 1, 1] - S[:, 0, 1]*S[:, 1, 0]
+    else:
+        for i in range(3):
+            a, b = (i + 1) % 3, (i + 2) % 3
+            S[:, i] = np.cross(J[:, a], J[:, b], axisa=1, axisb=1, axisc=1)
+        d = np.einsum('pje,pje->pe', J[:, 0], S[:, 0])
+    return S.transpose(1, 0, 2, 3), 1.0/d
+
+
+def _host_of(m):
+    """Host copy of a constant matrix or of a whole-width slice of one."""
+    if hasattr(m, '_host'):
+        return m._host
+    p = getattr(m, 'parent', None)
+    if p is not None and hasattr(p, '_host') and m.ca == 0 and \
+            m.cb == p.ncol and m.ra == 0 and m.rb == p.nrow:
+        return p._host
+    return None
+
+
 def _view(v):
     """(base pointer, map pointer, row-stride pointer) of a view."""
     return (v.basedata, v.mapping.data,
@@ -43,6 +84,7 @@ class PointwiseKernelProvider:
     def __init__(self, backend):
         self.backend = backend
         self._registered = {}
+        self._metrics = {}
 
     @property
     def _sfx(self):
@@ -74,9 +116,30 @@ class PointwiseKernelProvider:
 
     def _geom(self, tplargs, smats=None, rcpdjac=None, verts=None, upts=None):
         linear = 'linear' in tplargs.get('ktype', 'curved')
+        if linear and self.backend.precompute_metrics:
+            # FP64 arithmetic is scarce on this GPU while bandwidth is not:
+            # read stored per-point metric terms (10 values) instead of
+            # rebuilding the Jacobian from the vertices (~200 flops)
+            m = self._stored_metrics(verts, upts)
+            if m is not None:
+                smats, rcpdjac = m
+                linear = False
         if linear:
             return 1, (None, 0), (None, 0), _mat(verts), _mat(upts)
         return 0, _mat(smats), _mat(rcpdjac), (None, 0), (None, 0)
+
+    def _stored_metrics(self, verts, upts):
+        vh, uh = _host_of(verts), _host_of(upts)
+        if vh is None or uh is None:
+            return None
+        key = (id(vh), id(uh))
+        if key not in self._metrics:
+            be = self.backend
+            sm, rj = linear_metrics(vh, uh)
+            self._metrics[key] = (be.const_matrix(sm, tags={'align'}),
+                                  be.const_matrix(rj, tags={'align'}),
+                                  vh, uh)
+        return self._metrics[key][:2]
 
     def _tflux_euler(self, tplargs, dims, extrns, u, f, smats=None,
                      verts=None, upts=None):

@@ -38,7 +38,12 @@ __device__ __forceinline__ const double *vals<double>(const MulHandle &h) { retu
 template <>
 __device__ __forceinline__ const float *vals<float>(const MulHandle &h) { return h.val32; }
 
-template <typename T>
+// Epilogue modes: FP64 arithmetic is the scarce resource on this GPU, so
+// the common cases alpha = 1 with beta = 0 or beta = 1 issue no FP64 work
+// beyond the FMAs of the product (beta = 1 accumulates onto the loaded C).
+enum { EPI_SET = 0, EPI_ADD = 1, EPI_GENERAL = 2, EPI_SCALE = 3 };
+
+template <typename T, int EPI>
 __global__ void __launch_bounds__(MUL_WARPS * 32)
 mul_csr_kernel(MulHandle h, const T *__restrict__ b, int64_t ldb, T *__restrict__ c,
                int64_t ldc, int64_t ncol, T alpha, T beta) {
@@ -58,9 +63,15 @@ mul_csr_kernel(MulHandle h, const T *__restrict__ b, int64_t ldb, T *__restrict_
 
     const T *__restrict__ av = vals<T>(h);
     const int64_t ca = col0 + lane, cb = col0 + lane + 32;
+    const bool oka = ca < ncol, okb = cb < ncol;
 
     for (int row = warp; row < h.m; row += MUL_WARPS) {
-        T acc0 = 0, acc1 = 0;
+        T *crow = c + row * ldc;
+        T acc0 = T(0), acc1 = T(0);
+        if (EPI == EPI_ADD) {
+            if (oka) acc0 = crow[ca];
+            if (okb) acc1 = crow[cb];
+        }
         const int p0 = __ldg(h.rowptr + row), p1 = __ldg(h.rowptr + row + 1);
         for (int p = p0; p < p1; p++) {
             const T a = __ldg(av + p);
@@ -69,9 +80,15 @@ mul_csr_kernel(MulHandle h, const T *__restrict__ b, int64_t ldb, T *__restrict_
             acc1 = fma(a, bs[kk * MUL_NCOL + lane + 32], acc1);
         }
 
-        T *crow = c + row * ldc;
-        if (ca < ncol) crow[ca] = (beta != T(0)) ? alpha * acc0 + beta * crow[ca] : alpha * acc0;
-        if (cb < ncol) crow[cb] = (beta != T(0)) ? alpha * acc1 + beta * crow[cb] : alpha * acc1;
+        if (EPI == EPI_GENERAL) {
+            if (oka) acc0 = alpha * acc0 + beta * crow[ca];
+            if (okb) acc1 = alpha * acc1 + beta * crow[cb];
+        } else if (EPI == EPI_SCALE) {
+            acc0 *= alpha;
+            acc1 *= alpha;
+        }
+        if (oka) crow[ca] = acc0;
+        if (okb) crow[cb] = acc1;
     }
 }
 
@@ -85,18 +102,29 @@ int launch_mul(const MulHandle *h, const T *b, int64_t ldb, T *c, int64_t ldc, i
     size_t smem = (size_t)h->k * MUL_NCOL * sizeof(T);
     if (smem > 227 * 1024)
         return b200::set_error(B200_ERR_UNSUPPORTED, "mul: k=%d too large for the tile", h->k);
-    // Opt in to the largest tile once, outside any stream capture that
-    // a later call may be part of
+    // Opt in to the largest tile once per instantiation, outside any
+    // stream capture that a later call may be part of
     static bool opted_in = false;
     if (!opted_in) {
-        cudaError_t e = cudaFuncSetAttribute(mul_csr_kernel<T>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             227 * 1024);
-        if (e != cudaSuccess) return b200::check_cuda(e, "mul: smem attribute");
+        void (*fns[4])(MulHandle, const T *, int64_t, T *, int64_t, int64_t, T, T) = {
+            mul_csr_kernel<T, EPI_SET>, mul_csr_kernel<T, EPI_ADD>,
+            mul_csr_kernel<T, EPI_GENERAL>, mul_csr_kernel<T, EPI_SCALE>};
+        for (auto fn : fns) {
+            cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 227 * 1024);
+            if (e != cudaSuccess) return b200::check_cuda(e, "mul: smem attribute");
+        }
         opted_in = true;
     }
     unsigned grid = b200::ceil_div(ncol, MUL_NCOL);
-    mul_csr_kernel<T><<<grid, MUL_WARPS * 32, smem, s>>>(*h, b, ldb, c, ldc, ncol, alpha, beta);
+    if (alpha == T(1) && beta == T(0))
+        mul_csr_kernel<T, EPI_SET><<<grid, MUL_WARPS * 32, smem, s>>>(*h, b, ldb, c, ldc, ncol, alpha, beta);
+    else if (alpha == T(1) && beta == T(1))
+        mul_csr_kernel<T, EPI_ADD><<<grid, MUL_WARPS * 32, smem, s>>>(*h, b, ldb, c, ldc, ncol, alpha, beta);
+    else if (beta == T(0))
+        mul_csr_kernel<T, EPI_SCALE><<<grid, MUL_WARPS * 32, smem, s>>>(*h, b, ldb, c, ldc, ncol, alpha, beta);
+    else
+        mul_csr_kernel<T, EPI_GENERAL><<<grid, MUL_WARPS * 32, smem, s>>>(*h, b, ldb, c, ldc, ncol, alpha, beta);
     B200_CHECK_LAUNCH("mul_csr_kernel");
     return B200_OK;
 }
