@@ -203,6 +203,20 @@ int b200_errest_f32(int nupts, int nvars, int64_t neles, int64_t ld, const float
                     const float *err, const double *atol_dev, double rtol, int uniform,
                     double *scratch, int nscratch, double *out, void *stream);
 
+/* Allocation-free variant of b200_errest_f64; it has no counterpart in the
+ * reference.  It is for callers that cannot give the library scratch memory:
+ * an asynchronous step loop cannot pay the device synchronisation of
+ * cudaFree, and an application whose own pool allocator owns all device
+ * memory cannot make a raw allocation.  The partial sums live in a static
+ * device array of 4096 doubles that the library holds on every GPU it is
+ * loaded on; nblocks (the number of partial sums, as nscratch above) must
+ * be in [1, 4096] or the call fails with B200_ERR_ARG.  The first call on
+ * a device looks up the array's device address (make it before any stream
+ * capture); calls that overlap on the GPU race on the shared array. */
+int b200_errest_static_f64(int nupts, int nvars, int64_t neles, int64_t ld, const double *curr,
+                           const double *err, const double *atol_dev, double rtol, int uniform,
+                           int nblocks, double *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

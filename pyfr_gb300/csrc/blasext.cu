@@ -12,6 +12,8 @@
 // The register kernels treat the whole allocation (rows x leading
 // dimension, padding included) as a flat array: the padding columns of
 // every register stay exactly zero, so updating them is harmless.
+#include <mutex>
+
 #include "common.cuh"
 #include "../../include/pyfrb200.h"
 
@@ -161,9 +163,75 @@ int errest(int nupts, int nvars, int64_t neles, int64_t ld, const T *curr, const
     return B200_OK;
 }
 
+// ---- Allocation-free error norm ---------------------------------------
+// Some callers cannot hand this library a scratch buffer.  An integrator
+// that keeps its whole step loop asynchronous cannot call cudaMalloc or
+// cudaFree on the way (cudaFree synchronises the device and stalls the
+// queued stages).  A host application that owns every byte of device
+// memory through its own pool allocator cannot make a raw allocation at
+// all.  For them the error norm keeps its block partials in this
+// fixed-size file-scope array instead.  Every GPU that loads the library
+// holds it (B200_ERREST_STATIC_MAX_BLOCKS doubles, 32 KiB) until the
+// process exits.
+#define B200_ERREST_STATIC_MAX_BLOCKS 4096
+#define B200_ERREST_STATIC_MAX_DEVICES 64
+
+static __device__ __align__(256) double g_errest_scratch[B200_ERREST_STATIC_MAX_BLOCKS];
+
+// Device address of g_errest_scratch on the current device.  In host code
+// the array's name is only a host-side stand-in, so the address is looked
+// up with cudaGetSymbolAddress once per device, with that device current,
+// and cached.
+static double *g_errest_scratch_dev[B200_ERREST_STATIC_MAX_DEVICES];
+static std::mutex g_errest_scratch_mtx;
+
+static int errest_static_scratch(double **ptr) {
+    int dev = -1;
+    int rc = b200::check_cuda(cudaGetDevice(&dev), "errest_static: cudaGetDevice");
+    if (rc) return rc;
+    if (dev < 0 || dev >= B200_ERREST_STATIC_MAX_DEVICES)
+        return b200::set_error(B200_ERR_UNSUPPORTED, "errest_static: device %d out of range", dev);
+
+    std::lock_guard<std::mutex> lock(g_errest_scratch_mtx);
+    if (!g_errest_scratch_dev[dev]) {
+        void *p = nullptr;
+        rc = b200::check_cuda(cudaGetSymbolAddress(&p, g_errest_scratch),
+                              "errest_static: cudaGetSymbolAddress");
+        if (rc) return rc;
+        g_errest_scratch_dev[dev] = static_cast<double *>(p);
+    }
+    *ptr = g_errest_scratch_dev[dev];
+    return B200_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+// Same result as b200_errest_f64 with `nblocks` partial sums, but the
+// partials live in the library's own static device array, so the call
+// allocates nothing.  nblocks must lie in [1, 4096].  The first call on
+// a device looks up the array's device address; make that first call
+// before any stream capture.  All calls share the array and it keeps the
+// last call's partials; each call overwrites every slot it reads, so
+// nothing has to be cleared between calls.  Calls whose kernels overlap on
+// the GPU (different streams, or different host threads) race on the
+// shared array and give wrong results.
+int b200_errest_static_f64(int nupts, int nvars, int64_t neles, int64_t ld, const double *curr,
+                           const double *err, const double *atol_dev, double rtol, int uniform,
+                           int nblocks, double *out, void *stream) {
+    if (nblocks < 1 || nblocks > B200_ERREST_STATIC_MAX_BLOCKS)
+        return b200::set_error(B200_ERR_ARG,
+                               "errest_static: nblocks=%d outside [1, %d] (the static scratch "
+                               "holds %d partial sums)",
+                               nblocks, B200_ERREST_STATIC_MAX_BLOCKS,
+                               B200_ERREST_STATIC_MAX_BLOCKS);
+    double *scratch = nullptr;
+    int rc = errest_static_scratch(&scratch);
+    if (rc) return rc;
+    return errest<double>(nupts, nvars, neles, ld, curr, err, atol_dev, rtol, uniform, scratch,
+                          nblocks, out, (cudaStream_t)stream);
+}
 
 int b200_rkvdh2_f64(int64_t n, int stage, int nstages, int errest, double dt, double a,
                     double b, double e, double *r1, double *r2, double *rold, double *rerr,
