@@ -25,6 +25,8 @@ import threading
 import time
 from pathlib import Path
 
+import numpy as np
+
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
@@ -108,9 +110,10 @@ class ClockSampler:
 # Algorithmic bytes of each kernel launch (FP64 unless noted)
 # ---------------------------------------------------------------------------
 
-def kernel_bytes(k, itemsize):
+def kernel_bytes(k, be):
     m = k.meta
     kind = m.get('kind', k.name)
+    itemsize = 8 if be.fpdtype == np.float64 else 4
     if k.name == 'mul':
         a, b, out = m['a'], m['b'], m['out']
         ncol = b.ncol
@@ -140,6 +143,9 @@ def kernel_bytes(k, itemsize):
     if kind == 'rkvdh2':
         r1 = m['r1']
         return 4*r1.nrow*r1.leaddim*itemsize
+    if kind == 'rkmixed':
+        # FP64 accumulator read + write, FP32 RHS read, FP32 input write
+        return m['n']*(8 + 8 + 4 + 4)
     return 0
 
 
@@ -155,27 +161,44 @@ def flat_kernels(klist):
 # GPU arm
 # ---------------------------------------------------------------------------
 
-def run_gpu(args, rank, world):
-    import ctypes as C
+class Dist:
+    def __init__(self, world):
+        self.world = world
 
-    import numpy as np
+    def barrier(self):
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.barrier()
 
-    import __graft_entry__ as ge
-    ge.build_library()
+    def allmax(self, x):
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+            t = torch.tensor([x], dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            return float(t.item())
+        return x
 
+
+def make_form(form, args):
     from pyfr_gb300.backend import B200Backend
     from pyfr_gb300.cases import ns_tgv
-    from pyfr_gb300.integrators import RKVdH2Integrator
+    from pyfr_gb300.integrators import MixedRKIntegrator, RKVdH2Integrator
     from pyfr_gb300.solvers.system import NavierStokesSystem
 
-    cfg, mesh = ns_tgv(n=args.n, order=3, dt=args.dt)
+    prec = 'double' if form == 'plain' else 'single'
+    cfg, mesh = ns_tgv(n=args.n, order=3, dt=args.dt, precision=prec)
     cfg.set('backend-b200', 'device-id', str(args.local_rank))
     be = B200Backend(cfg)
+    icls = RKVdH2Integrator if form == 'plain' else MixedRKIntegrator
+    return icls(be, NavierStokesSystem, mesh, cfg)
+
+
+def measure(intg, args, dist, e2e=True, profile=True):
+    import ctypes as C
+
+    be = intg.backend
     lib, stream = be.lib, be.stream
-    intg = RKVdH2Integrator(be, NavierStokesSystem, mesh, cfg)
-    gndofs = intg.gndofs
-    nstages = intg.nstages
-    itemsize = 8
 
     def ev():
         e = C.c_void_p()
@@ -187,122 +210,127 @@ def run_gpu(args, rank, world):
         lib.event_elapsed(C.byref(ms), a, b)
         return ms.value
 
-    def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
-
-    def allmax(x):
-        if world > 1:
-            import torch
-            import torch.distributed as dist
-            t = torch.tensor([x], dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            return float(t.item())
-        return x
+    def one_step():
+        (idx,) = intg.step(intg.tcurr, intg.dt)[:1]
+        intg.idxcurr = idx
+        intg.tcurr += intg.dt
 
     # Warm-up (also captures the step graphs)
     for _ in range(args.warmup):
-        intg.run_steps(1)
+        one_step()
     be.wait()
 
     # Device-resident timed region
     e0, e1 = ev(), ev()
-    barrier()
+    dist.barrier()
     be.wait()
     with ClockSampler(args.local_rank) as clk:
         lib.event_record(e0, stream)
         for _ in range(args.steps):
-            (idx,) = intg.step(intg.tcurr, intg.dt)[:1]
-            intg.idxcurr = idx
-            intg.tcurr += intg.dt
+            one_step()
         lib.event_record(e1, stream)
         lib.event_sync(e1)
     be.wait()
-    barrier()
-    t_ms = allmax(elapsed(e0, e1))
+    dist.barrier()
+    res = dict(t_ms=dist.allmax(elapsed(e0, e1)), clocks=clk.summary(),
+               gndofs=intg.gndofs, nstages=intg.nstages,
+               soln=intg.soln, nsteps=args.warmup + args.steps)
 
-    (u,) = intg.soln
-    finite = bool(np.isfinite(u).all())
+    klist, _ = intg.step_kernels(intg.idxcurr, intg.dt)
+    klist = list(flat_kernels(klist))
+    res['launches'] = len(klist)*args.steps
 
-    # Kernel launches per step
-    klist = []
-    r1, r2, rs = intg._regs(intg.idxcurr)
-    for i in range(nstages):
-        for g in intg.system.rhs_graphs(r2 if i else r1, r2):
-            klist.extend(flat_kernels(g.klist))
-        klist.extend(intg._rk_kerns(i, r1, r2, *rs))
-        r1, r2 = r2, r1
-    launches_per_step = len(klist)
+    if profile:
+        # Per-kernel durations with events on the launching stream
+        per = {}
+        evs = [ev() for _ in range(len(klist) + 1)]
+        for _ in range(3):
+            lib.event_record(evs[0], stream)
+            for i, k in enumerate(klist):
+                k.run(stream)
+                lib.event_record(evs[i + 1], stream)
+            lib.event_sync(evs[-1])
+            for i, k in enumerate(klist):
+                name = k.meta.get('kind', k.name)
+                d = per.setdefault(name, {'ms': 0.0, 'n': 0, 'bytes': 0})
+                d['ms'] += elapsed(evs[i], evs[i + 1])
+                d['n'] += 1
+                d['bytes'] += kernel_bytes(k, be)
+        be.wait()
+        tot = sum(d['ms'] for d in per.values())
+        dom = max(per, key=lambda n: per[n]['ms'])
+        d = per[dom]
+        peak, peak_kind = _peaks()
+        achieved = d['bytes']/(d['ms']*1e-3)/1e9
+        res['kernels'] = {
+            n: {'share': round(v['ms']/tot, 4),
+                'avg_us': round(1e3*v['ms']/v['n'], 2),
+                'gbs': round(v['bytes']/(v['ms']*1e-3)/1e9, 1)}
+            for n, v in sorted(per.items(), key=lambda x: -x[1]['ms'])}
+        res['roofline'] = {
+            'bound': 'hbm', 'kernel': dom, 'achieved': round(achieved, 1),
+            'peak': peak, 'unit': 'GB/s', 'frac': round(achieved/peak, 4),
+            'traffic': None, 'peak_source': peak_kind,
+            'alg_bytes_per_launch': int(d['bytes']/d['n']),
+            'avg_launch_us': round(1e3*d['ms']/d['n'], 2)}
 
-    # Per-kernel durations with events on the launching stream
-    per = {}
-    nrep = 3
-    evs = [ev() for _ in range(len(klist) + 1)]
-    for _ in range(nrep):
-        lib.event_record(evs[0], stream)
-        for i, k in enumerate(klist):
-            if hasattr(k, 'rtargs'):
-                k.bind(dt=intg.dt)
-            k.run(stream)
-            lib.event_record(evs[i + 1], stream)
-        lib.event_sync(evs[-1])
-        for i, k in enumerate(klist):
-            name = k.meta.get('kind', k.name)
-            d = per.setdefault(name, {'ms': 0.0, 'n': 0, 'bytes': 0})
-            d['ms'] += elapsed(evs[i], evs[i + 1])
-            d['n'] += 1
-            d['bytes'] += kernel_bytes(k, itemsize)
-    be.wait()
-    tot = sum(d['ms'] for d in per.values())
-    dom = max(per, key=lambda n: per[n]['ms'])
-    d = per[dom]
-    peak, peak_kind = _peaks()
-    achieved = d['bytes']/(d['ms']*1e-3)/1e9
-    kernels = {n: {'share': round(v['ms']/tot, 4),
-                   'avg_us': round(1e3*v['ms']/v['n'], 2),
-                   'gbs': round(v['bytes']/(v['ms']*1e-3)/1e9, 1)}
-               for n, v in sorted(per.items(), key=lambda x: -x[1]['ms'])}
+    if e2e:
+        # End to end through the public API: the solution goes in from
+        # pinned host memory and comes back every step
+        mats = intg.acc if hasattr(intg, 'acc') else \
+            [b[intg.idxcurr] for b in intg.system.ele_banks]
+        m = mats[0]
+        nbytes = m.nbytes
+        hbuf = C.c_void_p()
+        lib.host_alloc(C.byref(hbuf), nbytes)
+        lib.memcpy_dtoh(hbuf.value, m.data, nbytes, stream)
+        be.wait()
+        dist.barrier()
+        lib.event_record(e0, stream)
+        for _ in range(args.steps):
+            if hasattr(intg, 'acc'):
+                lib.memcpy_htod(m.data, hbuf.value, nbytes, stream)
+                bank = intg.system.ele_banks[0][0]
+                lib.cast_f64_f32(m.nrow*m.leaddim, m.data, bank.data, stream)
+                one_step()
+            else:
+                dst = intg.system.ele_banks[0][intg.idxcurr]
+                lib.memcpy_htod(dst.data, hbuf.value, nbytes, stream)
+                one_step()
+                m = intg.system.ele_banks[0][intg.idxcurr]
+            lib.memcpy_dtoh(hbuf.value, m.data, nbytes, stream)
+        lib.event_record(e1, stream)
+        lib.event_sync(e1)
+        dist.barrier()
+        res['te2e_ms'] = dist.allmax(elapsed(e0, e1))
+        res['e2e_bytes'] = nbytes
+        lib.host_free(hbuf.value)
 
-    # End-to-end through the public API: pinned host solution in, one step,
-    # solution out, every step
-    bank = intg.system.ele_banks[0]
-    nbytes = bank[0].nbytes
-    hbuf = C.c_void_p()
-    lib.host_alloc(C.byref(hbuf), nbytes)
-    lib.memcpy_dtoh(hbuf.value, bank[intg.idxcurr].data, nbytes, stream)
-    be.wait()
-    for _ in range(2):
-        intg.run_steps(1)
-    be.wait()
-    barrier()
-    t0 = time.perf_counter()
-    lib.event_record(e0, stream)
-    for _ in range(args.steps):
-        lib.memcpy_htod(bank[intg.idxcurr].data, hbuf.value, nbytes, stream)
-        (idx,) = intg.step(intg.tcurr, intg.dt)[:1]
-        intg.idxcurr = idx
-        intg.tcurr += intg.dt
-        lib.memcpy_dtoh(hbuf.value, bank[idx].data, nbytes, stream)
-    lib.event_record(e1, stream)
-    lib.event_sync(e1)
-    wall_e2e = time.perf_counter() - t0
-    barrier()
-    te2e_ms = allmax(elapsed(e0, e1))
-    lib.host_free(hbuf.value)
-
-    res = dict(
-        t_ms=t_ms, te2e_ms=te2e_ms, wall_e2e=wall_e2e, gndofs=gndofs,
-        nstages=nstages, finite=finite, clocks=clk.summary(),
-        launches=launches_per_step*args.steps, kernels=kernels,
-        roofline={'bound': 'hbm', 'kernel': dom,
-                  'achieved': round(achieved, 1), 'peak': peak,
-                  'unit': 'GB/s', 'frac': round(achieved/peak, 4),
-                  'traffic': None, 'peak_source': peak_kind,
-                  'alg_bytes_per_launch': int(d['bytes']/d['n']),
-                  'avg_launch_us': round(1e3*d['ms']/d['n'], 2)},
-        e2e_bytes=nbytes, neles=mesh.spts['hex'].shape[1])
     return res
+
+
+def run_gpu(args, dist):
+    import __graft_entry__ as ge
+    ge.build_library()
+
+    import numpy as np
+
+    plain = make_form('plain', args)
+    rp = measure(plain, args, dist)
+    rp['neles'] = args.n**3
+    del plain
+
+    out = {'plain': rp}
+    if args.chosen:
+        chosen = make_form('chosen', args)
+        rc = measure(chosen, args, dist, e2e=True, profile=True)
+        # Same initial condition, same number of steps of the same dt:
+        # relative L2 error of the chosen form against the FP64 run
+        (up,), (uc,) = rp['soln'], rc['soln']
+        rc['l2_err'] = float(np.linalg.norm((uc - up).ravel()) /
+                             np.linalg.norm(up.ravel()))
+        out['chosen'] = rc
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -341,6 +369,8 @@ def main():
     ap.add_argument('--n', type=int, default=48)
     ap.add_argument('--dt', type=float, default=5e-4)
     ap.add_argument('--cpu-sample', type=int, default=12)
+    ap.add_argument('--no-chosen', dest='chosen', action='store_false',
+                    help='skip the chosen precision form')
     args = ap.parse_args()
 
     world = int(os.environ.get('WORLD_SIZE', '1'))
@@ -381,15 +411,35 @@ def main():
                     'd2h_bytes_per_step': 0}}))
         return
 
-    res = run_gpu(args, rank, world)
+    allres = run_gpu(args, Dist(world))
     if rank != 0:
         return
 
-    nrhs = res['nstages']*args.steps
-    value = world*res['gndofs']*nrhs/(res['t_ms']*1e-3)/1e9
-    e2e = world*res['gndofs']*nrhs/(res['te2e_ms']*1e-3)/1e9
+    def gdofs(r, key='t_ms'):
+        return world*r['gndofs']*r['nstages']*args.steps/(r[key]*1e-3)/1e9
+
+    res = allres['plain']
+    value, e2e = gdofs(res), gdofs(res, 'te2e_ms')
+    finite = bool(all(np.isfinite(u).all() for u in res['soln']))
 
     cpu_v, cpu_dt, cpu_ndofs = run_cpu_sample(args.cpu_sample, 1)
+
+    chosen = None
+    if 'chosen' in allres:
+        rc = allres['chosen']
+        chosen = {
+            'form': 'FP32 operators (sparse SIMT) and fluxes, FP64 RK '
+                    'accumulation',
+            'value': gdofs(rc), 'unit': 'GDoF/s',
+            'ms_per_step': rc['t_ms']/args.steps,
+            'e2e': {'value': gdofs(rc, 'te2e_ms'), 'unit': 'GDoF/s',
+                    'h2d_bytes_per_step': rc['e2e_bytes'],
+                    'd2h_bytes_per_step': rc['e2e_bytes']},
+            'l2_err_vs_fp64': rc['l2_err'],
+            'l2_err_after_steps': rc['nsteps'],
+            'speedup_vs_plain': gdofs(rc)/value,
+            'roofline': rc.get('roofline'), 'kernels': rc.get('kernels'),
+            'clocks': rc['clocks'], 'gpu_launches': rc['launches']}
 
     out = {
         'metric': METRIC, 'value': value, 'unit': 'GDoF/s',
@@ -399,7 +449,7 @@ def main():
         'data': 'synthetic', 'config': workload | {
             'ndofs': res['gndofs'], 'dt': args.dt,
             'parallelism': 'replicas' if world > 1 else 'single-gpu'},
-        'finite': res['finite'],
+        'finite': finite,
         'clocks': res['clocks'],
         'e2e': {'value': e2e, 'unit': 'GDoF/s',
                 'h2d_bytes_per_step': res['e2e_bytes'],
@@ -407,6 +457,7 @@ def main():
         'gpu_launches': res['launches'],
         'roofline': res['roofline'],
         'kernels': res['kernels'],
+        'chosen': chosen,
         'cpu_baseline': {'value': cpu_v, 'unit': 'GDoF/s', 'cores': 1,
                          'kind': 'port',
                          'sample': f'one RHS of the numpy oracle on a '

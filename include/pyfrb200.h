@@ -183,6 +183,18 @@ int b200_rkvdh2_f32(int64_t n, int stage, int nstages, int errest, double dt, do
                     double b, double e, float *r1, float *r2, float *rold, float *rerr,
                     void *stream);
 
+/* Mixed-precision form of the rkvdh2 stage (FP32 right-hand side, FP64
+ * solution accumulator): acc <- acc + dt*b*rhs and u32 <- next stage's
+ * FP32 input (acc + dt*a*rhs, or the new acc at the last stage); the
+ * embedded error registers as in rkvdh2.  Replaces the rkvdh2 kernel
+ * (pyfr/integrators/explicit/kernels/rkvdh2.mako:4-31) for the chosen
+ * precision form, whose second register is only ever an RHS input. */
+int b200_rkmixed_f64f32(int64_t n, int stage, int nstages, int errest, double dt, double a,
+                        double b, double e, double *acc, const float *rhs, float *u32,
+                        double *rold, double *rerr, void *stream);
+/* dst <- (float) src over n scalars. */
+int b200_cast_f64_f32(int64_t n, const double *src, float *dst, void *stream);
+
 /* x0 <- a[0]*x0 + sum_{k>=1} a[k]*xs[k]; xs is a host array of nv device
  * pointers (xs[0] ignored), nv <= 8; pyfr/backends/cuda/kernels/axnpby.mako. */
 int b200_axnpby_f64(int64_t n, int nv, double *x0, const double *const *xs, const double *a,

@@ -94,7 +94,8 @@ class BlasExtKernels:
         be.commit()
 
         host = np.zeros(1)
-        fn = getattr(be.lib, f'errest_{self._sfx}')
+        fn = be.lib.errest_f64 if curr.dtype == np.float64 else \
+            be.lib.errest_f32
         uniform = int(norm == 'uniform')
         ld, sp, nsc = curr.leaddim, self._scratch.data, self.MAX_ERREST_BLOCKS
         cp, ep, ap, op = curr.data, err.data, atol.data, out.data

@@ -76,6 +76,9 @@ _SIGS = {
     'b200_mul_create': [pd, i32, i32, C.POINTER(vp)],
     'b200_mul_nnz': [vp, C.POINTER(i32)],
     'b200_mul_destroy': [vp],
+    'b200_rkmixed_f64f32': [i64, i32, i32, i32, f64, f64, f64, f64, vp, vp,
+                            vp, vp, vp, vp],
+    'b200_cast_f64_f32': [i64, vp, vp, vp],
 }
 
 for _fp, _suf in ((f64, 'f64'), (f32, 'f32')):

@@ -47,6 +47,40 @@ rkvdh2_kernel(int64_t n, int last, int errest, int first, T dta, T dtb, T dte,
     }
 }
 
+// Mixed-precision low-storage stage: the RHS is evaluated in FP32, the
+// solution is accumulated in FP64.  In the two-register scheme the
+// second register only carries the next stage's RHS input, so here it is
+// written directly as the FP32 input of the next RHS evaluation:
+//   next input = acc + dt*a*R   (FP32),   acc <- acc + dt*b*R   (FP64)
+// and at the last stage the input of the next step is the new acc.
+__global__ void __launch_bounds__(BX_BLOCK)
+rkmixed_kernel(int64_t n, int last, int errest, int first, double dta, double dtb, double dte,
+               double *__restrict__ acc, const float *__restrict__ rhs, float *__restrict__ u32,
+               double *__restrict__ rold, double *__restrict__ rerr) {
+    for (int64_t i = (int64_t)blockIdx.x * BX_BLOCK + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * BX_BLOCK) {
+        const double t = acc[i], r = (double)rhs[i];
+        if (errest) {
+            if (first) {
+                rerr[i] = dte * r;
+                rold[i] = t;
+            } else {
+                rerr[i] = rerr[i] + dte * r;
+            }
+        }
+        const double nacc = t + dtb * r;
+        acc[i] = nacc;
+        u32[i] = last ? (float)nacc : (float)(t + dta * r);
+    }
+}
+
+__global__ void __launch_bounds__(BX_BLOCK)
+cast_f64_f32_kernel(int64_t n, const double *__restrict__ src, float *__restrict__ dst) {
+    for (int64_t i = (int64_t)blockIdx.x * BX_BLOCK + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * BX_BLOCK)
+        dst[i] = (float)src[i];
+}
+
 template <typename T>
 struct AxnpbyArgs {
     const T *x[MAX_AXNPBY];
@@ -245,6 +279,29 @@ int b200_rkvdh2_f32(int64_t n, int stage, int nstages, int errest, double dt, do
                     void *stream) {
     return rkvdh2<float>(n, stage, nstages, errest, dt, a, b, e, r1, r2, rold, rerr,
                          (cudaStream_t)stream);
+}
+
+int b200_rkmixed_f64f32(int64_t n, int stage, int nstages, int errest, double dt, double a,
+                        double b, double e, double *acc, const float *rhs, float *u32,
+                        double *rold, double *rerr, void *stream) {
+    if (n <= 0) return B200_OK;
+    if (stage < 0 || stage >= nstages)
+        return b200::set_error(B200_ERR_ARG, "rkmixed: stage %d out of range", stage);
+    if (errest && (!rold || !rerr))
+        return b200::set_error(B200_ERR_ARG, "rkmixed: error estimate needs rold and rerr");
+    const int last = stage == nstages - 1;
+    rkmixed_kernel<<<grid_for(n), BX_BLOCK, 0, (cudaStream_t)stream>>>(
+        n, last, errest, stage == 0, dt * (last ? 0.0 : a), dt * b, dt * e, acc, rhs, u32, rold,
+        rerr);
+    B200_CHECK_LAUNCH("rkmixed");
+    return B200_OK;
+}
+
+int b200_cast_f64_f32(int64_t n, const double *src, float *dst, void *stream) {
+    if (n <= 0) return B200_OK;
+    cast_f64_f32_kernel<<<grid_for(n), BX_BLOCK, 0, (cudaStream_t)stream>>>(n, src, dst);
+    B200_CHECK_LAUNCH("cast_f64_f32");
+    return B200_OK;
 }
 
 int b200_axnpby_f64(int64_t n, int nv, double *x0, const double *const *xs, const double *a,

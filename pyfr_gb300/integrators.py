@@ -14,9 +14,10 @@ single launch.
 """
 
 import math
-import time
 
 import numpy as np
+
+from pyfr_gb300.backend.types import Kernel
 
 RK_COEFFS = {
     'rk45': dict(
@@ -62,8 +63,11 @@ class RKVdH2Integrator:
         self.errest = self.controller == 'pi'
         nregs = 4 if self.errest else 2
 
-        self.system = systemcls(backend, mesh, initsoln, nregs, cfg)
+        self._nregs = nregs
+        self.system = self._make_system(backend, systemcls, mesh, initsoln,
+                                        cfg)
         self.system.commit()
+        self._setup_registers(initsoln)
         backend.commit()
 
         self.tcurr = cfg.getfloat(sect, 'tstart', 0.0)
@@ -97,6 +101,15 @@ class RKVdH2Integrator:
     def gndofs(self):
         return self.system.gndofs
 
+    def _make_system(self, backend, systemcls, mesh, initsoln, cfg):
+        return systemcls(backend, mesh, initsoln, self._nregs, cfg)
+
+    def _setup_registers(self, initsoln):
+        pass
+
+    def _reject(self, iprev):
+        self.idxcurr = iprev
+
     # ---- one step ----------------------------------------------------------
 
     def _rk_kerns(self, stage, r1, r2, rold=None, rerr=None):
@@ -124,18 +137,26 @@ class RKVdH2Integrator:
         r2, *rs = [r for r in regs if r != r1]
         return r1, r2, rs
 
-    def _enqueue_step(self, t, dt, idx, stream):
-        """Enqueue every stage of one step; returns the register indices."""
+    def step_kernels(self, idx, dt):
+        """The kernels of one step starting from register ``idx``, in launch
+        order, and the resulting register indices."""
         r1, r2, rs = self._regs(idx)
-        for i, ci in enumerate(self.c):
+        kl = []
+        for i in range(self.nstages):
             for g in self.system.rhs_graphs(r2 if i else r1, r2):
-                for k in g.klist:
-                    k.run(stream)
+                kl.extend(g.klist)
             for k in self._rk_kerns(i, r1, r2, *rs):
                 k.bind(dt=dt)
-                k.run(stream)
+                kl.append(k)
             r1, r2 = r2, r1
-        return (r2, *rs) if rs else (r2,)
+        return kl, ((r2, *rs) if rs else (r2,))
+
+    def _enqueue_step(self, t, dt, idx, stream):
+        """Enqueue every stage of one step; returns the register indices."""
+        kl, regs = self.step_kernels(idx, dt)
+        for k in kl:
+            k.run(stream)
+        return regs
 
     def step(self, t, dt):
         be, stream = self.backend, self.backend.stream
@@ -206,7 +227,7 @@ class RKVdH2Integrator:
             else:
                 if dt <= self.dtmin:
                     raise RuntimeError('Minimum sized time step rejected')
-                self.idxcurr = iprev
+                self._reject(iprev)
                 self.nrjctsteps += 1
 
         self.backend.wait()
@@ -224,3 +245,96 @@ class RKVdH2Integrator:
     @property
     def soln(self):
         return self.system.ele_scal_upts(self.idxcurr)
+
+
+class MixedRKIntegrator(RKVdH2Integrator):
+    """The chosen precision form: right-hand sides in FP32 (the system is
+    built on a single-precision backend), the solution accumulated in FP64.
+
+    The low-storage scheme's second register only ever carries the input
+    of the next RHS evaluation, so it is kept in FP32 (system bank 0) and
+    written by the stage kernel; system bank 1 receives the FP32 RHS; the
+    solution itself (and the PI controller's error registers) are FP64.
+    """
+
+    def __init__(self, backend, systemcls, mesh, cfg, initsoln=None):
+        if backend.fpdtype != np.float32:
+            raise ValueError('The mixed-precision integrator needs a '
+                             'single-precision backend')
+        super().__init__(backend, systemcls, mesh, cfg, initsoln)
+
+    def _make_system(self, backend, systemcls, mesh, initsoln, cfg):
+        return systemcls(backend, mesh, initsoln, 2, cfg)
+
+    def _setup_registers(self, initsoln):
+        be, sysm = self.backend, self.system
+        if initsoln is not None:
+            ics = [np.asarray(initsoln[et], dtype=np.float64)
+                   for et in sysm.ele_types]
+        else:
+            ics = [e.set_ics_from_cfg() for e in sysm.ele_map.values()]
+
+        def reg(ic=None):
+            return [be.matrix(ic_.shape, ic_ if ic is not None else None,
+                              tags={'align'}, dtype=np.float64)
+                    for ic_ in (ic if ic is not None else ics)]
+
+        self.acc = reg(ics)
+        self.rold = reg() if self.errest else None
+        self.rerr = reg() if self.errest else None
+        be.commit()
+
+    def _stage_kernel(self, i, j, dt):
+        lib, nst, errest = self.backend.lib, self.nstages, int(self.errest)
+        bank, acc = self.system.ele_banks[j], self.acc[j]
+        n = acc.nrow*acc.leaddim
+        a = self.a[i] if i < nst - 1 else 0.0
+        b = self.b[i]
+        e = self.e[i] if self.errest else 0.0
+        ro = self.rold[j].data if self.errest else None
+        re = self.rerr[j].data if self.errest else None
+        pa, pr, pu = acc.data, bank[1].data, bank[0].data
+
+        def run(stream):
+            lib.rkmixed_f64f32(n, i, nst, errest, dt, a, b, e, pa, pr, pu, ro,
+                               re, stream)
+
+        return Kernel(run, mats=[acc, bank[0], bank[1]], name='rkmixed',
+                      meta=dict(kind='rkmixed', n=n))
+
+    def step_kernels(self, idx, dt):
+        kl = []
+        for i in range(self.nstages):
+            for g in self.system.rhs_graphs(0, 1):
+                kl.extend(g.klist)
+            kl.extend(self._stage_kernel(i, j, dt)
+                      for j in range(len(self.acc)))
+        return kl, ((0, 1, 2) if self.errest else (0,))
+
+    def _reject(self, iprev):
+        self._restore_previous()
+
+    def _restore_previous(self):
+        lib, stream = self.backend.lib, self.backend.stream
+        for j, bank in enumerate(self.system.ele_banks):
+            acc = self.acc[j]
+            lib.memcpy_dtod(acc.data, self.rold[j].data, acc.nbytes, stream)
+            lib.cast_f64_f32(acc.nrow*acc.leaddim, acc.data, bank[0].data,
+                             stream)
+
+    def _errest(self, icurr, ierr):
+        if 'mixed' not in self._ekerns:
+            self._ekerns['mixed'] = [
+                self.backend.kernel('errest', a, r, self._atols)
+                for a, r in zip(self.acc, self.rerr)]
+        ks = self._ekerns['mixed']
+        for k in ks:
+            k.bind(rtol=self._rtol)
+            k.run(self.backend.stream)
+        self.backend.wait()
+        err = math.sqrt(sum(k.retval[0] for k in ks) / self.gndofs)
+        return err if not math.isnan(err) else 100
+
+    @property
+    def soln(self):
+        return [a.get() for a in self.acc]

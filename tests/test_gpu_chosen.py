@@ -1,0 +1,73 @@
+"""The chosen precision form: FP32 right-hand side (operators and fluxes),
+FP64 solution accumulation.  Its solution must stay within a relative L2
+error of 1e-6 of the FP64 oracle; single RHS evaluations are checked at
+FP32 accuracy (relative max-norm 1e-4 of the RHS scale)."""
+import numpy as np
+import pytest
+
+from oracle.fr_oracle import rk45_step
+from tests.oracle_util import disc_for_mesh
+
+pytestmark = pytest.mark.gpu
+
+L2_TOL = 1e-6
+
+
+def _l2rel(a, b):
+    return np.linalg.norm((a - b).ravel())/np.linalg.norm(b.ravel())
+
+
+@pytest.fixture(scope='module')
+def built():
+    import __graft_entry__ as ge
+    ge.build_library()
+
+
+def test_fp32_ns_rhs(built):
+    from pyfr_gb300.backend import B200Backend
+    from pyfr_gb300.cases import ns_tgv
+    from pyfr_gb300.solvers.system import NavierStokesSystem
+    cfg, mesh = ns_tgv(n=5, order=3, precision='single')
+    be = B200Backend(cfg)
+    s = NavierStokesSystem(be, mesh, None, 2, cfg)
+    s.commit()
+    s.rhs(0.0, 0, 1)
+    (u,), (r,) = s.ele_scal_upts(0), s.ele_scal_upts(1)
+    assert r.dtype == np.float32
+
+    d = disc_for_mesh(mesh, 3, ns=True)
+    c = cfg.items_as('constants', float) | cfg.items_as('solver-interfaces',
+                                                       float)
+    ref = d.rhs_ns(u.astype(np.float64), c)
+    assert np.abs(r - ref).max() <= 1e-4*np.abs(ref).max()
+
+
+@pytest.mark.parametrize('case', ['vortex', 'tgv'])
+def test_mixed_rk45_l2_error(built, case):
+    from pyfr_gb300.backend import B200Backend
+    from pyfr_gb300.cases import euler_vortex, ns_tgv
+    from pyfr_gb300.integrators import MixedRKIntegrator
+    from pyfr_gb300.solvers.system import EulerSystem, NavierStokesSystem
+
+    if case == 'vortex':
+        cfg, mesh = euler_vortex(n=10, order=3, dt=2e-3, precision='single')
+        scls, nsteps, ns = EulerSystem, 20, False
+    else:
+        cfg, mesh = ns_tgv(n=5, order=3, dt=5e-4, precision='single')
+        scls, nsteps, ns = NavierStokesSystem, 10, True
+
+    be = B200Backend(cfg)
+    intg = MixedRKIntegrator(be, scls, mesh, cfg)
+    (u,) = intg.soln
+    assert u.dtype == np.float64
+    intg.run_steps(nsteps)
+    (ug,) = intg.soln
+
+    d = disc_for_mesh(mesh, 3, ns=ns)
+    c = cfg.items_as('constants', float) | cfg.items_as('solver-interfaces',
+                                                       float)
+    rhs = (lambda x: d.rhs_ns(x, c)) if ns else (lambda x: d.rhs_euler(x, c))
+    for _ in range(nsteps):
+        u = rk45_step(rhs, u, intg.dt)
+
+    assert _l2rel(ug, u) <= L2_TOL
