@@ -229,6 +229,23 @@ int b200_errest_static_f64(int nupts, int nvars, int64_t neles, int64_t ld, cons
                            const double *err, const double *atol_dev, double rtol, int uniform,
                            int nblocks, double *out, void *stream);
 
+/* ---- field integrals (kinetic energy, enstrophy, volume) ------------- */
+/* out[0] = sum w*rho*|u|^2, out[1] = sum w*rho*|curl u|^2, out[2] = sum w
+ * over all solution points, w = quadrature weight * |J| held in `wts`
+ * (nupts x neles, leading dimension ldw, FP64); u is the conserved
+ * solution, gradu its physical gradient (ndims, nupts, nvars, neles).
+ * Accumulated in FP64; scratch holds 3 doubles per block (nscratch
+ * blocks).  Replaces the fieldeval reduction of the integrate plugin
+ * (pyfr/plugins/fieldeval.py:25-248, pyfr/plugins/kernels/fieldeval.mako)
+ * for its documented Taylor-Green integrands. */
+int b200_integrals_f64(int ndims, int nupts, int64_t neles, const double *u, int64_t ldu,
+                       const double *gradu, int64_t ldg, const double *wts, int64_t ldw,
+                       double *scratch, int nscratch, double *out, void *stream);
+/* Same with FP32 gradients (the chosen precision form). */
+int b200_integrals_f64f32(int ndims, int nupts, int64_t neles, const double *u, int64_t ldu,
+                          const float *gradu, int64_t ldg, const double *wts, int64_t ldw,
+                          double *scratch, int nscratch, double *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -227,24 +227,34 @@ class Discretisation:
     def _pair(self, lhs, rhs, periods):
         """Pair the flux points of the two sides of every interface by
         matching physical coordinates (modulo periods)."""
-        li, ri = [], []
-        for (el, fl), (er, fr) in zip(lhs, rhs):
-            pl = self.facefpts[fl]
-            pr = self.facefpts[fr]
-            xl = self.ploc_f[pl, :, el]
-            xr = self.ploc_f[pr, :, er]
-            d = xl[:, None, :] - xr[None, :, :]
+        # Interfaces are processed in batches sharing (left face, right face)
+        nint = len(lhs)
+        nfp = len(self.facefpts[0])
+        li = np.empty((nint, nfp, 2), dtype=np.int64)
+        ri = np.empty((nint, nfp, 2), dtype=np.int64)
+        keys = lhs[:, 1]*64 + rhs[:, 1]
+        for key in np.unique(keys):
+            idx = np.flatnonzero(keys == key)
+            fl, fr = lhs[idx[0], 1], rhs[idx[0], 1]
+            el, er = lhs[idx, 0], rhs[idx, 0]
+            pl = np.asarray(self.facefpts[fl])
+            pr = np.asarray(self.facefpts[fr])
+            xl = self.ploc_f[pl][:, :, el]                    # (nfp, nd, n)
+            xr = self.ploc_f[pr][:, :, er]
+            d = xl[:, None] - xr[None, :]                     # (nfp, nfp, nd, n)
             if periods is not None:
-                P = np.asarray(periods)
+                P = np.asarray(periods)[:, None]
                 d = d - P*np.rint(d/P)
-            match = np.argmin(np.sum(d*d, axis=2), axis=1)
-            if len(set(match.tolist())) != len(pl):
+            match = np.argmin(np.sum(d*d, axis=2), axis=1)    # (nfp, n)
+            if np.any(np.sort(match, axis=0) != np.arange(nfp)[:, None]):
                 raise RuntimeError('Flux points of an interface do not pair')
-            li.extend((p, el) for p in pl)
-            ri.extend((pr[m], er) for m in match)
+            li[idx, :, 0] = pl[None, :]
+            li[idx, :, 1] = el[:, None]
+            ri[idx, :, 0] = pr[match.T]
+            ri[idx, :, 1] = er[:, None]
 
-        self.pl = np.array(li)
-        self.pr = np.array(ri)
+        self.pl = li.reshape(-1, 2)
+        self.pr = ri.reshape(-1, 2)
         self.nl = self.pnorm[self.pl[:, 0], :, self.pl[:, 1]].T   # (nd, n)
 
     # ---- operator applies ---------------------------------------------------

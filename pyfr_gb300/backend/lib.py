@@ -79,6 +79,12 @@ _SIGS = {
     'b200_rkmixed_f64f32': [i64, i32, i32, i32, f64, f64, f64, f64, vp, vp,
                             vp, vp, vp, vp],
     'b200_cast_f64_f32': [i64, vp, vp, vp],
+    'b200_integrals_f64': [i32, i32, i64, vp, i64, vp, i64, vp, i64, vp, i32,
+                           vp, vp],
+    'b200_integrals_f64f32': [i32, i32, i64, vp, i64, vp, i64, vp, i64, vp,
+                              i32, vp, vp],
+    'b200_errest_static_f64': [i32, i32, i64, i64, vp, vp, vp, f64, i32, i32,
+                               vp, vp],
 }
 
 for _fp, _suf in ((f64, 'f64'), (f32, 'f32')):

@@ -92,3 +92,28 @@ def test_mixed_rk45_l2_error(built, case):
         u = rk45_step(rhs, u, intg.dt)
 
     assert _l2rel(ug, u) <= L2_TOL
+
+
+def test_kinetic_energy_history(built):
+    """Kinetic-energy history of the chosen form against the FP64 plain
+    form: relative difference at most 1e-8 at every logged step."""
+    from pyfr_gb300.backend import B200Backend
+    from pyfr_gb300.cases import ns_tgv
+    from pyfr_gb300.integrators import MixedRKIntegrator, RKVdH2Integrator
+    from pyfr_gb300.plugins import FieldIntegrals
+    from pyfr_gb300.solvers.system import NavierStokesSystem
+
+    hist = {}
+    for form, prec, icls in [('plain', 'double', RKVdH2Integrator),
+                             ('chosen', 'single', MixedRKIntegrator)]:
+        cfg, mesh = ns_tgv(n=6, order=3, dt=5e-4, precision=prec)
+        intg = icls(B200Backend(cfg), NavierStokesSystem, mesh, cfg)
+        fi = FieldIntegrals(intg)
+        h = []
+        for _ in range(10):
+            intg.run_steps(2)
+            h.append(fi()['E'])
+        hist[form] = np.array(h)
+
+    rel = np.abs(hist['chosen'] - hist['plain'])/np.abs(hist['plain'])
+    assert rel.max() <= 1e-8

@@ -230,3 +230,39 @@ def test_pi_controller_error_norm(built):
     be.wait()
     ref = np.sum((err/(np.array(atols)[None, :, None] + 1e-5*np.abs(cur)))**2)
     assert abs(k.retval[0] - ref) <= 1e-12*ref
+
+
+def test_field_integrals_plain(built):
+    """Kinetic energy and enstrophy integrals against the oracle's
+    gradients and the solution-point quadrature."""
+    from pyfr_gb300.cases import ns_tgv
+    from pyfr_gb300.integrators import RKVdH2Integrator
+    from pyfr_gb300.plugins import FieldIntegrals
+    from pyfr_gb300.shapes import tensor_rule
+    from pyfr_gb300.solvers.system import NavierStokesSystem
+    cfg, mesh = ns_tgv(n=4, order=3)
+    be = _backend(cfg)
+    intg = RKVdH2Integrator(be, NavierStokesSystem, mesh, cfg)
+    intg.run_steps(2)
+    got = FieldIntegrals(intg)()
+
+    (u,) = intg.soln
+    d = disc_for_mesh(mesh, 3, ns=True)
+    c = cfg.items_as('constants', float) | cfg.items_as('solver-interfaces',
+                                                       float)
+    gl = []
+    d.rhs_ns(u, c, grads_out=gl)
+    g = gl[0]                                   # (nd, nupts, nvars, neles)
+    _, qw = tensor_rule('gauss-legendre', 4, 3)
+    w = qw[:, None]*d.djac_u
+    rho = u[:, 0]
+    vel = u[:, 1:4]/rho[:, None]
+    du = (g[:, :, 1:4] - vel[None]*g[:, :, :1])/rho[None, :, None]  # (d,p,i,e)
+    w1 = du[1, :, 2] - du[2, :, 1]
+    w2 = du[2, :, 0] - du[0, :, 2]
+    w3 = du[0, :, 1] - du[1, :, 0]
+    E = np.sum(w*rho*np.sum(vel**2, axis=1))
+    enst = np.sum(w*rho*(w1**2 + w2**2 + w3**2))
+    assert abs(got['E'] - E) <= 1e-12*E
+    assert abs(got['enst'] - enst) <= 1e-10*enst
+    assert abs(got['vol'] - (2*np.pi)**3) <= 1e-12*(2*np.pi)**3
