@@ -86,6 +86,19 @@ int b200_mul_f64(void *handle, const double *b, int64_t ldb, double *c, int64_t 
 int b200_mul_f32(void *handle, const float *b, int64_t ldb, float *c, int64_t ldc,
                  int64_t ncol, float alpha, float beta, void *stream);
 
+/* Tensor-core operator apply for FP32 data (the chosen precision form):
+ * A and B are split into BF16 hi/lo halves and out = alpha*(Ahi*Bhi +
+ * Ahi*Blo + Alo*Bhi) + beta*out is formed with tcgen05.mma (FP32
+ * accumulation in tensor memory).  Same contract as b200_mul_f32 plus:
+ * operands 16-byte aligned, ldb/ldc/ncol multiples of 4.  _create fails
+ * with B200_ERR_UNSUPPORTED (and reports the shared memory it would need)
+ * when the operator does not fit the kernel's shared-memory budget.
+ * `err` is a device int that records a pipeline timeout (0 = none). */
+int b200_mul_bf16x3_create(const double *a, int m, int k, void **handle, size_t *smem_bytes);
+int b200_mul_bf16x3_destroy(void *handle);
+int b200_mul_bf16x3(void *handle, const float *b, int64_t ldb, float *c, int64_t ldc,
+                    int64_t ncol, float alpha, float beta, int *err, void *stream);
+
 /* ---- element pointwise kernels over [nupts, neles] ------------------- */
 /* Geometry: linear != 0 computes the metric terms from the element
  * vertices `verts` (nverts, ndims, neles) at the reference solution points

@@ -76,6 +76,9 @@ class B200Backend:
         self.fusion = cfg.getbool('backend-b200', 'fusion', True)
         self.precompute_metrics = cfg.getbool('backend-b200',
                                               'precompute-metrics', True)
+        self.mul_precision = cfg.get('backend-b200', 'mul-precision', 'native')
+        if self.mul_precision not in {'native', 'bf16x3'}:
+            raise ValueError('mul-precision must be native or bf16x3')
 
         self.mats = WeakValueDictionary()
         self._mat_counter = it.count()
@@ -105,9 +108,34 @@ class B200Backend:
         from pyfr_gb300.backend import blasext, fused, mul, pointwise
         self._providers = [pointwise.PointwiseKernelProvider(self),
                            blasext.BlasExtKernels(self),
+                           mul.TensorMulKernels(self),
                            mul.MulKernels(self)]
         self.pointwise = self._providers[0]
         self._fuser = fused.Fuser(self)
+        self._status = None
+
+    # ---- device status word (pipeline timeouts inside kernels) -------------
+
+    @property
+    def status_word(self):
+        """Device address of an int that kernels set on a bounded-wait
+        timeout; 0 means no error."""
+        if self._status is None:
+            p = C.c_void_p()
+            self.lib.malloc(C.byref(p), 16)
+            self._status = p.value
+        return self._status
+
+    def check_status(self):
+        """Raise if any kernel recorded a timeout since the last check."""
+        if self._status is None:
+            return
+        v = np.zeros(1, dtype=np.int32)
+        self.lib.memcpy_dtoh(v.ctypes.data, self._status, 4, self._stream)
+        self.lib.stream_sync(self._stream)
+        if v[0]:
+            self.lib.memset(self._status, 0, 4, self._stream)
+            raise B200Error(f'kernel pipeline timeout (code {int(v[0])})')
 
     # ---- device plumbing --------------------------------------------------
 
@@ -140,6 +168,7 @@ class B200Backend:
 
     def wait(self):
         self.lib.stream_sync(self._stream)
+        self.check_status()
 
     def memory_info(self):
         f, t = C.c_size_t(), C.c_size_t()

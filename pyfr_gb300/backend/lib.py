@@ -85,6 +85,9 @@ _SIGS = {
                               i32, vp, vp],
     'b200_errest_static_f64': [i32, i32, i64, i64, vp, vp, vp, f64, i32, i32,
                                vp, vp],
+    'b200_mul_bf16x3_create': [pd, i32, i32, C.POINTER(vp), C.POINTER(sz)],
+    'b200_mul_bf16x3_destroy': [vp],
+    'b200_mul_bf16x3': [vp, vp, i64, vp, i64, i64, f32, f32, vp, vp],
 }
 
 for _fp, _suf in ((f64, 'f64'), (f32, 'f32')):

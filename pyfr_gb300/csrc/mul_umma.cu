@@ -1,0 +1,444 @@
+// Operator apply on the 5th-generation tensor cores, split-BF16 form:
+//     out = alpha * A @ B + beta * out        (FP32 in, FP32 out)
+// with A = Ahi + Alo and B = Bhi + Blo split into BF16 halves and the
+// product formed as Ahi*Bhi + Ahi*Blo + Alo*Bhi (three tcgen05.mma per K
+// step, FP32 accumulation in tensor memory).  This is the chosen-precision
+// replacement of the reference's `mul` providers
+// (pyfr/backends/cuda/gimmik.py:23-121, pyfr/backends/cuda/cublaslt.py:169-280).
+//
+// One persistent CTA per SM walks 64-column tiles of B/out:
+//   warp 4 lane 0   bulk-copies (TMA engine, cp.async.bulk) each FP32 B
+//                   tile row by row into one of two staging buffers;
+//   warps 5-8       split the staged tile into BF16 hi/lo in the
+//                   canonical K-major no-swizzle UMMA layout (two stages);
+//   warp 9 lane 0   issues the MMAs into one of two TMEM accumulators;
+//   warps 0-3       read the accumulator (tcgen05.ld, one row per thread)
+//                   and write alpha*D + beta*out.
+// The operator halves are laid out on the host in the same canonical
+// layout and bulk-copied into shared memory once per CTA.  All hand-offs
+// are mbarriers; every wait is bounded and records an error code instead
+// of hanging.
+#include <cuda_bf16.h>
+#include <stdlib.h>
+#include <string.h>
+#include <vector>
+
+#include "common.cuh"
+#include "../../include/pyfrb200.h"
+
+namespace {
+
+constexpr int NT = 64;            // columns per tile (UMMA N)
+constexpr int MTILE = 128;        // UMMA M
+constexpr int NTHREADS = 320;     // 10 warps
+constexpr int NCONV = 128;        // converter threads (warps 5-8)
+constexpr int NEPI = 128;         // epilogue threads (warps 0-3)
+constexpr int MAX_MT = 4;         // up to 512 operator rows (TMEM: 2*4*64 cols)
+constexpr long long WAIT_LIMIT = 1LL << 22;
+
+struct UmmaHandle {
+    int m, k, mpad, kpad, mt;
+    unsigned char *aimg;   // device: [hi | lo], each mpad x kpad bf16 canonical
+    size_t aimg_bytes;
+    size_t smem_bytes;
+};
+
+struct Layout {
+    uint32_t a_hi, a_lo, b32[2], bhi[2], blo[2], bar, tslot, abort_flag;
+    uint32_t total;
+};
+
+__host__ __device__ inline Layout make_layout(int mpad, int kpad, int k) {
+    Layout L;
+    uint32_t off = 0;
+    const uint32_t abytes = (uint32_t)mpad * kpad * 2;
+    const uint32_t b32bytes = (uint32_t)k * NT * 4;
+    const uint32_t b16bytes = (uint32_t)NT * kpad * 2;
+    L.a_hi = off; off += abytes;
+    L.a_lo = off; off += abytes;
+    for (int s = 0; s < 2; s++) { L.b32[s] = off; off += (b32bytes + 127) & ~127u; }
+    for (int s = 0; s < 2; s++) { L.bhi[s] = off; off += b16bytes; L.blo[s] = off; off += b16bytes; }
+    L.bar = off; off += 16 * 8;
+    L.tslot = off; off += 8;
+    L.abort_flag = off; off += 8;
+    L.total = off;
+    return L;
+}
+
+// Barrier indices within the barrier block
+enum { BAR_A = 0, BAR_FULL32 = 1, BAR_EMPTY32 = 3, BAR_FULL16 = 5, BAR_EMPTY16 = 7,
+       BAR_ACCFULL = 9, BAR_ACCEMPTY = 11, BAR_DRAIN = 13 };
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void bar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(bar), "r"(count));
+}
+
+__device__ __forceinline__ void bar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" :: "r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void bar_arrive_tx(uint32_t bar, uint32_t tx) {
+    asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;"
+                 :: "r"(bar), "r"(tx) : "memory");
+}
+
+__device__ __forceinline__ bool bar_try(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile("{\n.reg .pred P1;\nmbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\n"
+                 "selp.b32 %0, 1, 0, P1;\n}\n"
+                 : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+    return ok != 0;
+}
+
+// Bounded wait: false (and the CTA's abort flag set, error recorded) if the
+// phase does not complete within the limit or another role aborted.
+__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity, volatile int *abort_flag,
+                                         int *err, int code) {
+    for (long long it = 0; it < WAIT_LIMIT; it++) {
+        if (bar_try(bar, parity)) return true;
+        if (*abort_flag) return false;
+        if (it > 32) __nanosleep(64);
+    }
+    *abort_flag = 1;
+    atomicCAS(err, 0, code);
+    return false;
+}
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes,
+                                         uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(dst), "l"(src), "r"(bytes), "r"(bar) : "memory");
+}
+
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+    d |= (uint64_t)1 << 46;                 // descriptor version for tcgen05
+    return d;                               // no swizzle, base offset 0
+}
+
+// kind::f16 instruction descriptor: BF16 A/B, FP32 D, both K-major
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+           ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma(uint32_t dtmem, uint64_t ad, uint64_t bd, uint32_t idesc,
+                                     uint32_t acc) {
+    asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                 :: "r"(dtmem), "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                 :: "r"(bar) : "memory");
+}
+
+struct UmmaArgs {
+    const unsigned char *aimg;
+    const float *b;
+    float *c;
+    int64_t ldb, ldc, ncol;
+    int m, k, kpad, mt;
+    float alpha, beta;
+    int epi;            // 0: alpha*D, 1: alpha*D + beta*C
+    int *err;
+};
+
+__global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(UmmaArgs p) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    const Layout L = make_layout(p.mt * MTILE, p.kpad, p.k);
+    const uint32_t sbase = smem_addr(smem);
+    const uint32_t bar0 = sbase + L.bar;
+    auto bar = [&](int i) { return bar0 + 8u * i; };
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + L.abort_flag);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + L.tslot);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int64_t ntiles = (p.ncol + NT - 1) / NT;
+    const int mt = p.mt;
+    const uint32_t tcols = 2 * mt * NT <= 32 ? 32 : (2 * mt * NT <= 64 ? 64 :
+                          (2 * mt * NT <= 128 ? 128 : (2 * mt * NT <= 256 ? 256 : 512)));
+
+    if (tid == 0) {
+        *abort_flag = 0;
+        bar_init(bar(BAR_A), 1);
+        for (int s = 0; s < 2; s++) {
+            bar_init(bar(BAR_FULL32 + s), 1);
+            bar_init(bar(BAR_EMPTY32 + s), NCONV);
+            bar_init(bar(BAR_FULL16 + s), NCONV);
+            bar_init(bar(BAR_EMPTY16 + s), 1);
+            bar_init(bar(BAR_ACCFULL + s), 1);
+            bar_init(bar(BAR_ACCEMPTY + s), NEPI);
+        }
+        bar_init(bar(BAR_DRAIN), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     :: "r"(smem_addr(tslot)), "r"(tcols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = *tslot;
+
+    const uint32_t abytes = (uint32_t)(mt * MTILE) * p.kpad * 2;
+    const uint32_t SBO = (uint32_t)p.kpad * 16, LBO = 128;
+
+    if (warp == 4) {
+        // ---- producer: operator image once, then the FP32 B tiles ----
+        if (lane == 0) {
+            bar_arrive_tx(bar(BAR_A), 2 * abytes);
+            bulk_g2s(sbase + L.a_hi, p.aimg, 2 * abytes, bar(BAR_A));
+        }
+        int i = 0;
+        for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
+            const int s = i & 1;
+            if (i >= 2 && !bar_wait(bar(BAR_EMPTY32 + s), ((i >> 1) + 1) & 1, abort_flag, p.err, 1))
+                break;
+            if (lane == 0) {
+                const int64_t col0 = t * NT;
+                const int64_t nc = p.ncol - col0 < NT ? p.ncol - col0 : NT;
+                const uint32_t rowb = (uint32_t)nc * 4;
+                bar_arrive_tx(bar(BAR_FULL32 + s), rowb * p.k);
+                for (int r = 0; r < p.k; r++)
+                    bulk_g2s(sbase + L.b32[s] + (uint32_t)r * NT * 4, p.b + r * p.ldb + col0, rowb,
+                             bar(BAR_FULL32 + s));
+            }
+            __syncwarp();
+        }
+    } else if (warp >= 5 && warp <= 8) {
+        // ---- converters: FP32 stage -> BF16 hi/lo canonical K-major ----
+        const int ct = tid - 5 * 32;
+        const int n = ct % NT;
+        int i = 0;
+        for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
+            const int s = i & 1;
+            if (!bar_wait(bar(BAR_FULL32 + s), (i >> 1) & 1, abort_flag, p.err, 2)) break;
+            if (i >= 2 && !bar_wait(bar(BAR_EMPTY16 + s), ((i >> 1) + 1) & 1, abort_flag, p.err, 3))
+                break;
+            const float *b32 = reinterpret_cast<const float *>(smem + L.b32[s]);
+            unsigned char *bhi = smem + L.bhi[s], *blo = smem + L.blo[s];
+            for (int k8 = ct / NT; k8 < p.kpad / 8; k8 += NCONV / NT) {
+                uint32_t hw[4], lw[4];
+#pragma unroll
+                for (int j = 0; j < 8; j += 2) {
+                    const int r0 = k8 * 8 + j;
+                    const float x0 = r0 < p.k ? b32[r0 * NT + n] : 0.f;
+                    const float x1 = r0 + 1 < p.k ? b32[(r0 + 1) * NT + n] : 0.f;
+                    const __nv_bfloat16 h0 = __float2bfloat16_rn(x0);
+                    const __nv_bfloat16 h1 = __float2bfloat16_rn(x1);
+                    const __nv_bfloat16 l0 = __float2bfloat16_rn(x0 - __bfloat162float(h0));
+                    const __nv_bfloat16 l1 = __float2bfloat16_rn(x1 - __bfloat162float(h1));
+                    hw[j / 2] = (uint32_t)__bfloat16_as_ushort(h0) |
+                                ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+                    lw[j / 2] = (uint32_t)__bfloat16_as_ushort(l0) |
+                                ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+                }
+                const uint32_t off = (uint32_t)(n / 8) * SBO + (uint32_t)k8 * LBO + (n % 8) * 16;
+                *reinterpret_cast<uint4 *>(bhi + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+                *reinterpret_cast<uint4 *>(blo + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            bar_arrive(bar(BAR_EMPTY32 + s));
+            bar_arrive(bar(BAR_FULL16 + s));
+        }
+    } else if (warp == 9) {
+        // ---- MMA issuer ----
+        if (lane == 0) {
+            const uint32_t idesc = idesc_bf16(MTILE, NT);
+            bool ok = bar_wait(bar(BAR_A), 0, abort_flag, p.err, 4);
+            int i = 0;
+            for (int64_t t = blockIdx.x; ok && t < ntiles; t += gridDim.x, i++) {
+                const int s = i & 1, bsel = i & 1;
+                if (!bar_wait(bar(BAR_FULL16 + s), (i >> 1) & 1, abort_flag, p.err, 5)) break;
+                if (i >= 2 &&
+                    !bar_wait(bar(BAR_ACCEMPTY + bsel), ((i >> 1) + 1) & 1, abort_flag, p.err, 6))
+                    break;
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                for (int q = 0; q < mt; q++) {
+                    const uint32_t d = tmem + (uint32_t)(bsel * mt + q) * NT;
+                    const uint32_t ahi = sbase + L.a_hi + (uint32_t)q * MTILE * p.kpad * 2;
+                    const uint32_t alo = sbase + L.a_lo + (uint32_t)q * MTILE * p.kpad * 2;
+                    for (int ks = 0; ks < p.kpad / 16; ks++) {
+                        const uint32_t ko = (uint32_t)ks * 2 * LBO;
+                        const uint64_t dah = sdesc(ahi + ko, LBO, SBO);
+                        const uint64_t dal = sdesc(alo + ko, LBO, SBO);
+                        const uint64_t dbh = sdesc(sbase + L.bhi[s] + ko, LBO, SBO);
+                        const uint64_t dbl = sdesc(sbase + L.blo[s] + ko, LBO, SBO);
+                        umma(d, dah, dbh, idesc, ks > 0);
+                        umma(d, dah, dbl, idesc, 1);
+                        umma(d, dal, dbh, idesc, 1);
+                    }
+                }
+                umma_commit(bar(BAR_EMPTY16 + s));
+                umma_commit(bar(BAR_ACCFULL + bsel));
+            }
+            // Drain: every MMA issued so far has completed once this arrives
+            umma_commit(bar(BAR_DRAIN));
+            bar_wait(bar(BAR_DRAIN), 0, abort_flag, p.err, 7);
+        }
+        __syncwarp();
+    } else {
+        // ---- epilogue: TMEM -> registers -> out ----
+        const int row_in_tile = warp * 32 + lane;
+        int i = 0;
+        for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
+            const int bsel = i & 1;
+            if (!bar_wait(bar(BAR_ACCFULL + bsel), (i >> 1) & 1, abort_flag, p.err, 8)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const int64_t col0 = t * NT;
+            for (int q = 0; q < mt; q++) {
+                const int row = q * MTILE + row_in_tile;
+                float *crow = p.c + (int64_t)row * p.ldc + col0;
+                for (int cc = 0; cc < NT; cc += 8) {
+                    uint32_t v[8];
+                    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) +
+                                           (uint32_t)(bsel * mt + q) * NT + cc;
+                    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                                 : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]),
+                                   "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+                                 : "r"(taddr));
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                    // ncol is a multiple of 4: store whole float4 halves only
+                    const int64_t left = p.ncol - (col0 + cc);
+                    if (row < p.m && left > 0) {
+                        float o[8];
+#pragma unroll
+                        for (int j = 0; j < 8; j++) o[j] = p.alpha * __uint_as_float(v[j]);
+                        float4 *dst = reinterpret_cast<float4 *>(crow + cc);
+                        if (p.epi) {
+                            const float4 c0 = dst[0];
+                            o[0] += p.beta * c0.x; o[1] += p.beta * c0.y;
+                            o[2] += p.beta * c0.z; o[3] += p.beta * c0.w;
+                            if (left >= 8) {
+                                const float4 c1 = dst[1];
+                                o[4] += p.beta * c1.x; o[5] += p.beta * c1.y;
+                                o[6] += p.beta * c1.z; o[7] += p.beta * c1.w;
+                            }
+                        }
+                        dst[0] = make_float4(o[0], o[1], o[2], o[3]);
+                        if (left >= 8) dst[1] = make_float4(o[4], o[5], o[6], o[7]);
+                    }
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            bar_arrive(bar(BAR_ACCEMPTY + bsel));
+        }
+    }
+
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
+                     :: "r"(tmem), "r"(tcols));
+}
+
+// Host: split A into BF16 hi/lo and lay both out in the canonical K-major
+// no-swizzle layout ((r/8)*SBO + (k/8)*128 + (r%8)*16 + (k%8)*2 bytes).
+void build_image(const double *a, int m, int k, int mpad, int kpad, std::vector<uint16_t> &img) {
+    const size_t n = (size_t)mpad * kpad;
+    img.assign(2 * n, 0);
+    const size_t SBO = (size_t)kpad * 16;
+    for (int r = 0; r < m; r++)
+        for (int c = 0; c < k; c++) {
+            const float x = (float)a[(size_t)r * k + c];
+            const __nv_bfloat16 h = __float2bfloat16_rn(x);
+            const __nv_bfloat16 l = __float2bfloat16_rn(x - __bfloat162float(h));
+            const size_t off = (r / 8) * SBO + (c / 8) * 128 + (r % 8) * 16 + (c % 8) * 2;
+            img[off / 2] = __bfloat16_as_ushort(h);
+            img[n + off / 2] = __bfloat16_as_ushort(l);
+        }
+}
+
+int g_sm_count = 0;
+
+}  // namespace
+
+extern "C" {
+
+int b200_mul_bf16x3_create(const double *a, int m, int k, void **handle, size_t *smem_bytes) {
+    if (!a || !handle || m <= 0 || k <= 0)
+        return b200::set_error(B200_ERR_ARG, "mul_bf16x3_create: bad arguments");
+    const int mpad = (m + MTILE - 1) / MTILE * MTILE, kpad = (k + 15) / 16 * 16;
+    const int mt = mpad / MTILE;
+    const Layout L = make_layout(mpad, kpad, k);
+    if (smem_bytes) *smem_bytes = L.total;
+    if (mt > MAX_MT || L.total > 227 * 1024 || kpad / 16 * 3 * mt > 1024)
+        return b200::set_error(B200_ERR_UNSUPPORTED,
+                               "mul_bf16x3: operator %dx%d needs %u bytes of shared memory", m,
+                               k, L.total);
+
+    std::vector<uint16_t> img;
+    build_image(a, m, k, mpad, kpad, img);
+
+    UmmaHandle *h = (UmmaHandle *)calloc(1, sizeof(UmmaHandle));
+    if (!h) return b200::set_error(B200_ERR_STATE, "mul_bf16x3_create: out of host memory");
+    h->m = m; h->k = k; h->mpad = mpad; h->kpad = kpad; h->mt = mt;
+    h->aimg_bytes = img.size() * 2;
+    h->smem_bytes = L.total;
+    int rc = b200::check_cuda(cudaMalloc(&h->aimg, h->aimg_bytes), "mul_bf16x3_create");
+    if (!rc)
+        rc = b200::check_cuda(cudaMemcpy(h->aimg, img.data(), h->aimg_bytes,
+                                         cudaMemcpyHostToDevice), "mul_bf16x3_create");
+    if (rc) {
+        cudaFree(h->aimg);
+        free(h);
+        return rc;
+    }
+    *handle = h;
+    return B200_OK;
+}
+
+int b200_mul_bf16x3_destroy(void *handle) {
+    if (!handle) return B200_OK;
+    UmmaHandle *h = (UmmaHandle *)handle;
+    cudaFree(h->aimg);
+    free(h);
+    return B200_OK;
+}
+
+int b200_mul_bf16x3(void *handle, const float *b, int64_t ldb, float *c, int64_t ldc,
+                    int64_t ncol, float alpha, float beta, int *err, void *stream) {
+    UmmaHandle *h = (UmmaHandle *)handle;
+    if (!h || !err) return b200::set_error(B200_ERR_ARG, "mul_bf16x3: null handle/status");
+    if (ncol <= 0) return B200_OK;
+    if (ldb < ncol || ldc < ncol)
+        return b200::set_error(B200_ERR_ARG, "mul_bf16x3: leading dimension smaller than ncol");
+    // Bulk copies need 16-byte aligned rows and 16-byte multiples
+    if ((((uintptr_t)b) & 15) || (((uintptr_t)c) & 15) || (ldb % 4) || (ldc % 4) || (ncol % 4))
+        return b200::set_error(B200_ERR_ARG, "mul_bf16x3: operands must be 16-byte aligned");
+
+    if (!g_sm_count) {
+        int dev;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev);
+        cudaError_t e = cudaFuncSetAttribute(mul_umma_kernel,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             227 * 1024);
+        if (e != cudaSuccess) return b200::check_cuda(e, "mul_bf16x3: smem attribute");
+    }
+
+    UmmaArgs p;
+    p.aimg = h->aimg; p.b = b; p.c = c; p.ldb = ldb; p.ldc = ldc; p.ncol = ncol;
+    p.m = h->m; p.k = h->k; p.kpad = h->kpad; p.mt = h->mt;
+    p.alpha = alpha; p.beta = beta; p.epi = beta != 0.0f; p.err = err;
+
+    const int64_t ntiles = (ncol + NT - 1) / NT;
+    const unsigned grid = (unsigned)(ntiles < g_sm_count ? ntiles : g_sm_count);
+    mul_umma_kernel<<<grid, NTHREADS, h->smem_bytes, (cudaStream_t)stream>>>(p);
+    B200_CHECK_LAUNCH("mul_umma_kernel");
+    return B200_OK;
+}
+
+}  // extern "C"

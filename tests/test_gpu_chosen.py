@@ -23,6 +23,39 @@ def built():
     ge.build_library()
 
 
+@pytest.mark.parametrize('key', ['hex_p3_gauss-legendre', 'quad_p3_gauss-legendre',
+                                 'hex_p2_gauss-legendre'])
+@pytest.mark.parametrize('opname', ['m0', 'M132', 'm3', 'M460', 'm6'])
+def test_mul_bf16x3_tensor_cores(built, golden, key, opname):
+    """Split-BF16 tcgen05 operator apply against an FP64 product: the
+    error of the three-product split is bounded by ~2^-16 |A||B|."""
+    from pyfr_gb300.backend import B200Backend
+    from pyfr_gb300.inifile import Inifile
+    a = golden['operators'][f'{key}/{opname}']
+    cfg = Inifile()
+    cfg.set('backend', 'precision', 'single')
+    cfg.set('backend-b200', 'mul-precision', 'bf16x3')
+    be = B200Backend(cfg)
+    rng = np.random.default_rng(7)
+    for nvars, neles in [(5, 77), (4, 1000)]:
+        b = rng.normal(size=(a.shape[1], nvars, neles))
+        c0 = rng.normal(size=(a.shape[0], nvars, neles))
+        A = be.const_matrix(a)
+        B = be.matrix(b.shape, b, tags={'align'})
+        C = be.matrix(c0.shape, c0, tags={'align'})
+        be.commit()
+        bound = 1e-4*np.einsum('mk,kve->mve', np.abs(a), np.abs(b)) + 1e-6
+        for alpha, beta in [(1.0, 0.0), (1.0, 1.0), (-0.5, 0.25)]:
+            C.set(c0)
+            k = be.kernel('mul', A, B, out=C, alpha=alpha, beta=beta)
+            assert k.meta['impl'] == 'bf16x3'
+            be.run_kernels([k], wait=True)
+            ref = alpha*np.einsum('mk,kve->mve', a, b.astype(np.float32)) + \
+                beta*c0.astype(np.float32)
+            assert np.all(np.abs(C.get() - ref) <= abs(alpha)*bound +
+                          1e-6*np.abs(ref))
+
+
 def test_fp32_ns_rhs(built):
     """The TGV fluxes carry the mean pressure p0 = 1/(gamma Ma^2) ~ 71
     while the RHS is O(1): FP32 rounding of the fluxes (relative 6e-8 of
@@ -65,8 +98,9 @@ def test_fp32_euler_rhs(built):
     assert np.abs(r - ref).max() <= 1e-4*np.abs(ref).max()
 
 
+@pytest.mark.parametrize('mulprec', ['native', 'bf16x3'])
 @pytest.mark.parametrize('case', ['vortex', 'tgv'])
-def test_mixed_rk45_l2_error(built, case):
+def test_mixed_rk45_l2_error(built, case, mulprec):
     from pyfr_gb300.backend import B200Backend
     from pyfr_gb300.cases import euler_vortex, ns_tgv
     from pyfr_gb300.integrators import MixedRKIntegrator
@@ -78,6 +112,7 @@ def test_mixed_rk45_l2_error(built, case):
     else:
         cfg, mesh = ns_tgv(n=5, order=3, dt=5e-4, precision='single')
         scls, nsteps, ns = NavierStokesSystem, 10, True
+    cfg.set('backend-b200', 'mul-precision', mulprec)
 
     be = B200Backend(cfg)
     intg = MixedRKIntegrator(be, scls, mesh, cfg)
