@@ -6,7 +6,8 @@
 // replacement of the reference's `mul` providers
 // (pyfr/backends/cuda/gimmik.py:23-121, pyfr/backends/cuda/cublaslt.py:169-280).
 //
-// One persistent CTA per SM walks 64-column tiles of B/out:
+// One persistent CTA per SM walks 64- (or, for long operators, 32-)
+// column tiles of B/out:
 //   warp 4 lane 0   bulk-copies (TMA engine, cp.async.bulk) each FP32 B
 //                   tile row by row into one of two staging buffers;
 //   warps 5-8       split the staged tile into BF16 hi/lo in the
@@ -28,7 +29,6 @@
 
 namespace {
 
-constexpr int NT = 64;            // columns per tile (UMMA N)
 constexpr int MTILE = 128;        // UMMA M
 constexpr int NTHREADS = 320;     // 10 warps
 constexpr int NCONV = 128;        // converter threads (warps 5-8)
@@ -37,7 +37,7 @@ constexpr int MAX_MT = 4;         // up to 512 operator rows (TMEM: 2*4*64 cols)
 constexpr long long WAIT_LIMIT = 1LL << 22;
 
 struct UmmaHandle {
-    int m, k, mpad, kpad, mt;
+    int m, k, mpad, kpad, mt, nt;
     unsigned char *aimg;   // device: [hi | lo], each mpad x kpad bf16 canonical
     size_t aimg_bytes;
     size_t smem_bytes;
@@ -48,6 +48,7 @@ struct Layout {
     uint32_t total;
 };
 
+template <int NT>
 __host__ __device__ inline Layout make_layout(int mpad, int kpad, int k) {
     Layout L;
     uint32_t off = 0;
@@ -152,9 +153,10 @@ struct UmmaArgs {
     int *err;
 };
 
+template <int NT>
 __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(UmmaArgs p) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    const Layout L = make_layout(p.mt * MTILE, p.kpad, p.k);
+    const Layout L = make_layout<NT>(p.mt * MTILE, p.kpad, p.k);
     const uint32_t sbase = smem_addr(smem);
     const uint32_t bar0 = sbase + L.bar;
     auto bar = [&](int i) { return bar0 + 8u * i; };
@@ -372,7 +374,13 @@ int b200_mul_bf16x3_create(const double *a, int m, int k, void **handle, size_t 
         return b200::set_error(B200_ERR_ARG, "mul_bf16x3_create: bad arguments");
     const int mpad = (m + MTILE - 1) / MTILE * MTILE, kpad = (k + 15) / 16 * 16;
     const int mt = mpad / MTILE;
-    const Layout L = make_layout(mpad, kpad, k);
+    // Widest column tile whose pipeline fits in shared memory
+    int nt = 64;
+    Layout L = make_layout<64>(mpad, kpad, k);
+    if (L.total > 227 * 1024) {
+        nt = 32;
+        L = make_layout<32>(mpad, kpad, k);
+    }
     if (smem_bytes) *smem_bytes = L.total;
     if (mt > MAX_MT || L.total > 227 * 1024 || kpad / 16 * 3 * mt > 1024)
         return b200::set_error(B200_ERR_UNSUPPORTED,
@@ -384,7 +392,7 @@ int b200_mul_bf16x3_create(const double *a, int m, int k, void **handle, size_t 
 
     UmmaHandle *h = (UmmaHandle *)calloc(1, sizeof(UmmaHandle));
     if (!h) return b200::set_error(B200_ERR_STATE, "mul_bf16x3_create: out of host memory");
-    h->m = m; h->k = k; h->mpad = mpad; h->kpad = kpad; h->mt = mt;
+    h->m = m; h->k = k; h->mpad = mpad; h->kpad = kpad; h->mt = mt; h->nt = nt;
     h->aimg_bytes = img.size() * 2;
     h->smem_bytes = L.total;
     int rc = b200::check_cuda(cudaMalloc(&h->aimg, h->aimg_bytes), "mul_bf16x3_create");
@@ -423,9 +431,12 @@ int b200_mul_bf16x3(void *handle, const float *b, int64_t ldb, float *c, int64_t
         int dev;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev);
-        cudaError_t e = cudaFuncSetAttribute(mul_umma_kernel,
+        cudaError_t e = cudaFuncSetAttribute(mul_umma_kernel<64>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              227 * 1024);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(mul_umma_kernel<32>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
         if (e != cudaSuccess) return b200::check_cuda(e, "mul_bf16x3: smem attribute");
     }
 
@@ -434,9 +445,12 @@ int b200_mul_bf16x3(void *handle, const float *b, int64_t ldb, float *c, int64_t
     p.m = h->m; p.k = h->k; p.kpad = h->kpad; p.mt = h->mt;
     p.alpha = alpha; p.beta = beta; p.epi = beta != 0.0f; p.err = err;
 
-    const int64_t ntiles = (ncol + NT - 1) / NT;
+    const int64_t ntiles = (ncol + h->nt - 1) / h->nt;
     const unsigned grid = (unsigned)(ntiles < g_sm_count ? ntiles : g_sm_count);
-    mul_umma_kernel<<<grid, NTHREADS, h->smem_bytes, (cudaStream_t)stream>>>(p);
+    if (h->nt == 64)
+        mul_umma_kernel<64><<<grid, NTHREADS, h->smem_bytes, (cudaStream_t)stream>>>(p);
+    else
+        mul_umma_kernel<32><<<grid, NTHREADS, h->smem_bytes, (cudaStream_t)stream>>>(p);
     B200_CHECK_LAUNCH("mul_umma_kernel");
     return B200_OK;
 }
