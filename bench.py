@@ -190,7 +190,7 @@ def make_form(form, args):
     cfg, mesh = ns_tgv(n=args.n, order=3, dt=args.dt, precision=prec)
     cfg.set('backend-b200', 'device-id', str(args.local_rank))
     if form == 'chosen':
-        cfg.set('backend-b200', 'mul-precision', 'bf16x3')
+        cfg.set('backend-b200', 'mul-precision', args.chosen_mul)
     be = B200Backend(cfg)
     icls = RKVdH2Integrator if form == 'plain' else MixedRKIntegrator
     return icls(be, NavierStokesSystem, mesh, cfg)
@@ -311,6 +311,23 @@ def measure(intg, args, dist, e2e=True, profile=True):
     return res
 
 
+def history(intg, nsteps, every):
+    """Advance to step ``nsteps`` (counted from the initial condition),
+    logging the normalised kinetic energy E_k = int rho|u|^2/(2 V) every
+    ``every`` steps; returns the final solution and the E_k history."""
+    from pyfr_gb300.plugins import FieldIntegrals
+
+    fi = FieldIntegrals(intg)
+    hist = {}
+    while intg.nsteps < nsteps:
+        k = min(every - intg.nsteps % every, nsteps - intg.nsteps)
+        intg.run_steps(k)
+        if intg.nsteps % every == 0:
+            r = fi()
+            hist[intg.nsteps] = 0.5*r['E']/r['vol']
+    return intg.soln, hist
+
+
 def run_gpu(args, dist):
     import __graft_entry__ as ge
     ge.build_library()
@@ -320,18 +337,25 @@ def run_gpu(args, dist):
     plain = make_form('plain', args)
     rp = measure(plain, args, dist)
     rp['neles'] = args.n**3
+    (up,), hp = history(plain, args.accuracy_steps, args.ke_every)
     del plain
 
     out = {'plain': rp}
-    if args.chosen:
-        chosen = make_form('chosen', args)
-        rc = measure(chosen, args, dist, e2e=True, profile=True)
-        # Same initial condition, same number of steps of the same dt:
-        # relative L2 error of the chosen form against the FP64 run
-        (up,), (uc,) = rp['soln'], rc['soln']
+    forms = ['chosen', 'fp32'] if args.chosen else []
+    for form in forms:
+        intg = make_form(form, args)
+        rc = measure(intg, args, dist, e2e=form == 'chosen',
+                     profile=form == 'chosen')
+        # Same initial condition and dt, advanced to the same step:
+        # relative L2 error and kinetic-energy history error vs FP64
+        (uc,), hc = history(intg, args.accuracy_steps, args.ke_every)
         rc['l2_err'] = float(np.linalg.norm((uc - up).ravel()) /
                              np.linalg.norm(up.ravel()))
-        out['chosen'] = rc
+        rc['ke_err'] = float(max(abs(hc[s] - hp[s]) for s in hp))
+        rc['ke_final'] = hc[max(hc)]
+        out[form] = rc
+        del intg
+    out['plain']['ke_final'] = hp[max(hp)]
     return out
 
 
@@ -382,6 +406,12 @@ def main():
     ap.add_argument('--cpu-seconds', type=float, default=10.0)
     ap.add_argument('--no-chosen', dest='chosen', action='store_false',
                     help='skip the chosen precision form')
+    ap.add_argument('--chosen-mul', default='bf16x3',
+                    help='operator precision of the chosen form')
+    ap.add_argument('--accuracy-steps', type=int, default=200,
+                    help='steps after which the chosen form is compared '
+                         'with FP64')
+    ap.add_argument('--ke-every', type=int, default=10)
     args = ap.parse_args()
 
     world = int(os.environ.get('WORLD_SIZE', '1'))
@@ -434,22 +464,37 @@ def main():
                                                         args.cpu_seconds)
 
     chosen = None
-    if 'chosen' in allres:
-        rc = allres['chosen']
-        chosen = {
-            'form': 'operator contractions split-BF16 x3 on tcgen05 tensor '
-                    'cores (FP32 accumulate), FP32 fluxes, FP64 RK '
-                    'accumulation',
+    labels = {
+        'chosen': f'operator contractions {args.chosen_mul} (split-BF16 x3 '
+                  'on tcgen05 tensor cores, FP32 accumulate), FP32 fluxes, '
+                  'FP64 RK accumulation',
+        'fp32': 'operator contractions FP32 (sparse, CUDA cores), FP32 '
+                'fluxes, FP64 RK accumulation'}
+    variants = {}
+    for form in ('chosen', 'fp32'):
+        if form not in allres:
+            continue
+        rc = allres[form]
+        variants[form] = {
+            'form': labels[form],
             'value': gdofs(rc), 'unit': 'GDoF/s',
             'ms_per_step': rc['t_ms']/args.steps,
-            'e2e': {'value': gdofs(rc, 'te2e_ms'), 'unit': 'GDoF/s',
-                    'h2d_bytes_per_step': rc['e2e_bytes'],
-                    'd2h_bytes_per_step': rc['e2e_bytes']},
             'l2_err_vs_fp64': rc['l2_err'],
-            'l2_err_after_steps': rc['nsteps'],
+            'ke_hist_max_abs_err_vs_fp64': rc['ke_err'],
+            'accuracy_after_steps': args.accuracy_steps,
             'speedup_vs_plain': gdofs(rc)/value,
-            'roofline': rc.get('roofline'), 'kernels': rc.get('kernels'),
             'clocks': rc['clocks'], 'gpu_launches': rc['launches']}
+        if 'te2e_ms' in rc:
+            variants[form]['e2e'] = {
+                'value': gdofs(rc, 'te2e_ms'), 'unit': 'GDoF/s',
+                'h2d_bytes_per_step': rc['e2e_bytes'],
+                'd2h_bytes_per_step': rc['e2e_bytes']}
+        if 'roofline' in rc:
+            variants[form] |= {'roofline': rc['roofline'],
+                               'kernels': rc['kernels']}
+    chosen = variants.pop('chosen', None)
+    if chosen is not None:
+        chosen['other_variants'] = variants
 
     out = {
         'metric': METRIC, 'value': value, 'unit': 'GDoF/s',

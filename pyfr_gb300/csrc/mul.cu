@@ -102,20 +102,6 @@ int launch_mul(const MulHandle *h, const T *b, int64_t ldb, T *c, int64_t ldc, i
     size_t smem = (size_t)h->k * MUL_NCOL * sizeof(T);
     if (smem > 227 * 1024)
         return b200::set_error(B200_ERR_UNSUPPORTED, "mul: k=%d too large for the tile", h->k);
-    // Opt in to the largest tile once per instantiation, outside any
-    // stream capture that a later call may be part of
-    static bool opted_in = false;
-    if (!opted_in) {
-        void (*fns[4])(MulHandle, const T *, int64_t, T *, int64_t, int64_t, T, T) = {
-            mul_csr_kernel<T, EPI_SET>, mul_csr_kernel<T, EPI_ADD>,
-            mul_csr_kernel<T, EPI_GENERAL>, mul_csr_kernel<T, EPI_SCALE>};
-        for (auto fn : fns) {
-            cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 227 * 1024);
-            if (e != cudaSuccess) return b200::check_cuda(e, "mul: smem attribute");
-        }
-        opted_in = true;
-    }
     unsigned grid = b200::ceil_div(ncol, MUL_NCOL);
     if (alpha == T(1) && beta == T(0))
         mul_csr_kernel<T, EPI_SET><<<grid, MUL_WARPS * 32, smem, s>>>(*h, b, ldb, c, ldc, ncol, alpha, beta);
@@ -129,6 +115,22 @@ int launch_mul(const MulHandle *h, const T *b, int64_t ldb, T *c, int64_t ldc, i
     return B200_OK;
 }
 
+// Opt every instantiation in to the largest tile.  Called from
+// b200_mul_create, which never runs inside a stream capture: changing a
+// function attribute while a capture is open invalidates the capture.
+template <typename T>
+int opt_in_smem() {
+    void (*fns[4])(MulHandle, const T *, int64_t, T *, int64_t, int64_t, T, T) = {
+        mul_csr_kernel<T, EPI_SET>, mul_csr_kernel<T, EPI_ADD>,
+        mul_csr_kernel<T, EPI_GENERAL>, mul_csr_kernel<T, EPI_SCALE>};
+    for (auto fn : fns) {
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             227 * 1024);
+        if (e != cudaSuccess) return b200::check_cuda(e, "mul: smem attribute");
+    }
+    return B200_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -136,6 +138,9 @@ extern "C" {
 int b200_mul_create(const double *a, int m, int k, void **handle) {
     if (!a || !handle || m <= 0 || k <= 0)
         return b200::set_error(B200_ERR_ARG, "mul_create: bad arguments");
+    int orc = opt_in_smem<double>();
+    if (!orc) orc = opt_in_smem<float>();
+    if (orc) return orc;
 
     std::vector<int> rowptr(m + 1, 0), colidx;
     std::vector<double> v64;

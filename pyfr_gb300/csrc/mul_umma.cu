@@ -387,6 +387,29 @@ int b200_mul_bf16x3_create(const double *a, int m, int k, void **handle, size_t 
                                "mul_bf16x3: operator %dx%d needs %u bytes of shared memory", m,
                                k, L.total);
 
+    // One-time device set-up here rather than at launch: changing a
+    // function attribute while a stream capture is open invalidates it
+    if (!g_sm_count) {
+        int dev, sms = 0;
+        int rc0 = b200::check_cuda(cudaGetDevice(&dev), "mul_bf16x3_create");
+        if (!rc0)
+            rc0 = b200::check_cuda(
+                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev),
+                "mul_bf16x3_create");
+        if (!rc0)
+            rc0 = b200::check_cuda(cudaFuncSetAttribute(mul_umma_kernel<64>,
+                                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                        227 * 1024),
+                                   "mul_bf16x3: smem attribute");
+        if (!rc0)
+            rc0 = b200::check_cuda(cudaFuncSetAttribute(mul_umma_kernel<32>,
+                                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                        227 * 1024),
+                                   "mul_bf16x3: smem attribute");
+        if (rc0) return rc0;
+        g_sm_count = sms;
+    }
+
     std::vector<uint16_t> img;
     build_image(a, m, k, mpad, kpad, img);
 
@@ -427,18 +450,8 @@ int b200_mul_bf16x3(void *handle, const float *b, int64_t ldb, float *c, int64_t
     if ((((uintptr_t)b) & 15) || (((uintptr_t)c) & 15) || (ldb % 4) || (ldc % 4) || (ncol % 4))
         return b200::set_error(B200_ERR_ARG, "mul_bf16x3: operands must be 16-byte aligned");
 
-    if (!g_sm_count) {
-        int dev;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev);
-        cudaError_t e = cudaFuncSetAttribute(mul_umma_kernel<64>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             227 * 1024);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(mul_umma_kernel<32>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        if (e != cudaSuccess) return b200::check_cuda(e, "mul_bf16x3: smem attribute");
-    }
+    if (!g_sm_count)
+        return b200::set_error(B200_ERR_STATE, "mul_bf16x3: no handle created on this device");
 
     UmmaArgs p;
     p.aimg = h->aimg; p.b = b; p.c = c; p.ldb = ldb; p.ldc = ldc; p.ncol = ncol;
