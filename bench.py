@@ -292,8 +292,7 @@ def measure(intg, args, dist, e2e=True, profile=True):
         for _ in range(args.steps):
             if hasattr(intg, 'acc'):
                 lib.memcpy_htod(m.data, hbuf.value, nbytes, stream)
-                bank = intg.system.ele_banks[0][0]
-                lib.cast_f64_f32(m.nrow*m.leaddim, m.data, bank.data, stream)
+                intg.refresh_input(stream)
                 one_step()
             else:
                 dst = intg.system.ele_banks[0][intg.idxcurr]

@@ -29,10 +29,17 @@ extern "C" {
 
 /* Gas and viscosity constants of the flux kernels ([constants] gamma, mu,
  * Pr, cpTref, cpTs; viscosity-correction = sutherland when sutherland != 0);
- * pyfr/solvers/navstokes/kernels/flux.mako:48-105. */
+ * pyfr/solvers/navstokes/kernels/flux.mako:48-105.
+ * shifted != 0 (Navier-Stokes kernels, Rusanov only): the solution inputs
+ * are perturbations du = u - u_ref from the constant state
+ * (rho_ref, 0, p_ref/(gamma - 1)) and the constant momentum flux p_ref*I is
+ * left out; the right-hand side is the same in exact arithmetic but its
+ * low-precision rounding no longer scales with the mean pressure. */
 typedef struct {
     double gamma, mu, pr, cpTref, cpTs;
     int sutherland;
+    int shifted;
+    double rho_ref, p_ref;
 } b200_gas_t;
 
 /* Riemann solver ids: [solver-interfaces] riemann-solver */
@@ -198,15 +205,20 @@ int b200_rkvdh2_f32(int64_t n, int stage, int nstages, int errest, double dt, do
 
 /* Mixed-precision form of the rkvdh2 stage (FP32 right-hand side, FP64
  * solution accumulator): acc <- acc + dt*b*rhs and u32 <- next stage's
- * FP32 input (acc + dt*a*rhs, or the new acc at the last stage); the
- * embedded error registers as in rkvdh2.  Replaces the rkvdh2 kernel
+ * FP32 input (acc + dt*a*rhs, or the new acc at the last stage), minus the
+ * per-variable reference state uref[nvars] (a host array; null or nvars = 0
+ * for none) subtracted in FP64 before rounding; the embedded error
+ * registers as in rkvdh2.  Replaces the rkvdh2 kernel
  * (pyfr/integrators/explicit/kernels/rkvdh2.mako:4-31) for the chosen
  * precision form, whose second register is only ever an RHS input. */
 int b200_rkmixed_f64f32(int64_t n, int stage, int nstages, int errest, double dt, double a,
                         double b, double e, double *acc, const float *rhs, float *u32,
-                        double *rold, double *rerr, void *stream);
-/* dst <- (float) src over n scalars. */
-int b200_cast_f64_f32(int64_t n, const double *src, float *dst, void *stream);
+                        double *rold, double *rerr, int nvars, const double *uref,
+                        void *stream);
+/* dst <- (float)(src - uref[v]) over n scalars of an AoSoA field with
+ * nvars variables (uref null: no shift). */
+int b200_cast_f64_f32(int64_t n, const double *src, float *dst, int nvars, const double *uref,
+                      void *stream);
 
 /* x0 <- a[0]*x0 + sum_{k>=1} a[k]*xs[k]; xs is a host array of nv device
  * pointers (xs[0] ignored), nv <= 8; pyfr/backends/cuda/kernels/axnpby.mako. */

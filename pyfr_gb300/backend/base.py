@@ -76,6 +76,10 @@ class B200Backend:
         self.fusion = cfg.getbool('backend-b200', 'fusion', True)
         self.precompute_metrics = cfg.getbool('backend-b200',
                                               'precompute-metrics', True)
+        # Constant (rho_ref, p_ref) that Navier-Stokes kernels subtract from
+        # their inputs; set by the mixed-precision integrator before the
+        # kernels are built (None: inputs are the conserved variables)
+        self.ref_state = None
         self.mul_precision = cfg.get('backend-b200', 'mul-precision', 'native')
         if self.mul_precision not in {'native', 'bf16x3'}:
             raise ValueError('mul-precision must be native or bf16x3')

@@ -23,7 +23,8 @@ class B200Error(RuntimeError):
 
 class Gas(C.Structure):
     _fields_ = [('gamma', f64), ('mu', f64), ('pr', f64), ('cpTref', f64),
-                ('cpTs', f64), ('sutherland', i32)]
+                ('cpTs', f64), ('sutherland', i32), ('shifted', i32),
+                ('rho_ref', f64), ('p_ref', f64)]
 
 
 def _sig_pointwise(fp):
@@ -77,8 +78,8 @@ _SIGS = {
     'b200_mul_nnz': [vp, C.POINTER(i32)],
     'b200_mul_destroy': [vp],
     'b200_rkmixed_f64f32': [i64, i32, i32, i32, f64, f64, f64, f64, vp, vp,
-                            vp, vp, vp, vp],
-    'b200_cast_f64_f32': [i64, vp, vp, vp],
+                            vp, vp, vp, i32, vp, vp],
+    'b200_cast_f64_f32': [i64, vp, vp, i32, vp, vp],
     'b200_integrals_f64': [i32, i32, i64, vp, i64, vp, i64, vp, i64, vp, i32,
                            vp, vp],
     'b200_integrals_f64f32': [i32, i32, i64, vp, i64, vp, i64, vp, i64, vp,

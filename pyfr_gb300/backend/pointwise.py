@@ -20,10 +20,14 @@ from pyfr_gb300.backend.types import BindableKernel, Kernel, NullKernel
 RSOLVERS = {'rusanov': 0, 'hllc': 1}
 
 
-def _gas(c, visc_corr='none'):
-    return Gas(gamma=c['gamma'], mu=c.get('mu', 0.0), pr=c.get('Pr', 1.0),
-               cpTref=c.get('cpTref', 1.0), cpTs=c.get('cpTs', 1.0),
-               sutherland=int(visc_corr == 'sutherland'))
+def _gas(c, visc_corr='none', ref_state=None):
+    g = Gas(gamma=c['gamma'], mu=c.get('mu', 0.0), pr=c.get('Pr', 1.0),
+            cpTref=c.get('cpTref', 1.0), cpTs=c.get('cpTs', 1.0),
+            sutherland=int(visc_corr == 'sutherland'))
+    if ref_state is not None:
+        g.shifted = 1
+        g.rho_ref, g.p_ref = ref_state
+    return g
 
 
 def _mat(m):
@@ -171,7 +175,8 @@ class PointwiseKernelProvider:
         nupts, neles = dims
         lin, (sp, sl), (rp, rl), (vp, vl), (upp, upl) = self._geom(
             tplargs, smats, rcpdjac, verts, upts)
-        gas = _gas(tplargs['c'], tplargs.get('visc_corr', 'none'))
+        gas = _gas(tplargs['c'], tplargs.get('visc_corr', 'none'),
+                   self.backend.ref_state)
         fn, nd = self._fn('tflux_ns'), tplargs['ndims']
         up, ul = _mat(u)
         fp, fl = _mat(f)
@@ -256,7 +261,10 @@ class PointwiseKernelProvider:
         (n,) = dims
         c = tplargs['c']
         rs = RSOLVERS[tplargs['rsolver']]
-        gas = _gas(c, tplargs.get('visc_corr', 'none'))
+        if self.backend.ref_state is not None and tplargs['rsolver'] != 'rusanov':
+            raise NotImplementedError('The reference-state shift needs the '
+                                      'Rusanov Riemann solver')
+        gas = _gas(c, tplargs.get('visc_corr', 'none'), self.backend.ref_state)
         beta, tau = c['ldg-beta'], c['ldg-tau']
         fn, nd = self._fn('intcflux_ns'), tplargs['ndims']
         lb, lm, _ = _view(ul)

@@ -53,10 +53,23 @@ rkvdh2_kernel(int64_t n, int last, int errest, int first, T dta, T dtb, T dte,
 // written directly as the FP32 input of the next RHS evaluation:
 //   next input = acc + dt*a*R   (FP32),   acc <- acc + dt*b*R   (FP64)
 // and at the last stage the input of the next step is the new acc.
+// Constant per-variable offset subtracted (in FP64) before the FP32
+// rounding of the RHS input: the input of the next RHS is u - u_ref.
+// Variable v of an AoSoA field sits at flat index i with
+// v = (i mod (32*nvars)) / 32.
+struct RefState {
+    double v[8];
+    int nvars;
+};
+
+__device__ __forceinline__ double ref_of(const RefState &r, int64_t i) {
+    return r.nvars ? r.v[(int)((i % (32 * r.nvars)) / 32)] : 0.0;
+}
+
 __global__ void __launch_bounds__(BX_BLOCK)
 rkmixed_kernel(int64_t n, int last, int errest, int first, double dta, double dtb, double dte,
                double *__restrict__ acc, const float *__restrict__ rhs, float *__restrict__ u32,
-               double *__restrict__ rold, double *__restrict__ rerr) {
+               double *__restrict__ rold, double *__restrict__ rerr, RefState ref) {
     for (int64_t i = (int64_t)blockIdx.x * BX_BLOCK + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * BX_BLOCK) {
         const double t = acc[i], r = (double)rhs[i];
@@ -70,15 +83,25 @@ rkmixed_kernel(int64_t n, int last, int errest, int first, double dta, double dt
         }
         const double nacc = t + dtb * r;
         acc[i] = nacc;
-        u32[i] = last ? (float)nacc : (float)(t + dta * r);
+        u32[i] = (float)((last ? nacc : t + dta * r) - ref_of(ref, i));
     }
 }
 
 __global__ void __launch_bounds__(BX_BLOCK)
-cast_f64_f32_kernel(int64_t n, const double *__restrict__ src, float *__restrict__ dst) {
+cast_f64_f32_kernel(int64_t n, const double *__restrict__ src, float *__restrict__ dst,
+                    RefState ref) {
     for (int64_t i = (int64_t)blockIdx.x * BX_BLOCK + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * BX_BLOCK)
-        dst[i] = (float)src[i];
+        dst[i] = (float)(src[i] - ref_of(ref, i));
+}
+
+int make_ref(int nvars, const double *uref, RefState &r) {
+    r = RefState{};
+    if (!uref || nvars <= 0) return B200_OK;
+    if (nvars > 8) return b200::set_error(B200_ERR_ARG, "reference state: nvars > 8");
+    for (int v = 0; v < nvars; v++) r.v[v] = uref[v];
+    r.nvars = nvars;
+    return B200_OK;
 }
 
 template <typename T>
@@ -283,23 +306,31 @@ int b200_rkvdh2_f32(int64_t n, int stage, int nstages, int errest, double dt, do
 
 int b200_rkmixed_f64f32(int64_t n, int stage, int nstages, int errest, double dt, double a,
                         double b, double e, double *acc, const float *rhs, float *u32,
-                        double *rold, double *rerr, void *stream) {
+                        double *rold, double *rerr, int nvars, const double *uref,
+                        void *stream) {
     if (n <= 0) return B200_OK;
     if (stage < 0 || stage >= nstages)
         return b200::set_error(B200_ERR_ARG, "rkmixed: stage %d out of range", stage);
     if (errest && (!rold || !rerr))
         return b200::set_error(B200_ERR_ARG, "rkmixed: error estimate needs rold and rerr");
+    RefState ref;
+    int rc = make_ref(nvars, uref, ref);
+    if (rc) return rc;
     const int last = stage == nstages - 1;
     rkmixed_kernel<<<grid_for(n), BX_BLOCK, 0, (cudaStream_t)stream>>>(
         n, last, errest, stage == 0, dt * (last ? 0.0 : a), dt * b, dt * e, acc, rhs, u32, rold,
-        rerr);
+        rerr, ref);
     B200_CHECK_LAUNCH("rkmixed");
     return B200_OK;
 }
 
-int b200_cast_f64_f32(int64_t n, const double *src, float *dst, void *stream) {
+int b200_cast_f64_f32(int64_t n, const double *src, float *dst, int nvars, const double *uref,
+                      void *stream) {
     if (n <= 0) return B200_OK;
-    cast_f64_f32_kernel<<<grid_for(n), BX_BLOCK, 0, (cudaStream_t)stream>>>(n, src, dst);
+    RefState ref;
+    int rc = make_ref(nvars, uref, ref);
+    if (rc) return rc;
+    cast_f64_f32_kernel<<<grid_for(n), BX_BLOCK, 0, (cudaStream_t)stream>>>(n, src, dst, ref);
     B200_CHECK_LAUNCH("cast_f64_f32");
     return B200_OK;
 }

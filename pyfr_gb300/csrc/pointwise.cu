@@ -125,8 +125,14 @@ tflux_ns_kernel(int nupts, int64_t neles, Gas gas, const T *__restrict__ u, int6
     for (int v = 0; v < NV; v++) uu[v] = u[upt * ldu + soa_off(e, v, NV)];
 
     T ft[ND][NV], p, vel[ND];
-    b200::inviscid_flux<ND, T>(uu, ft, p, vel, T(gas.gamma));
-    b200::viscous_flux_add<ND, T>(uu, gr, ft, gas);
+    if (gas.shifted) {
+        T uf[NV];
+        b200::inviscid_flux_shift<ND, T>(uu, ft, p, vel, uf, gas);
+        b200::viscous_flux_add<ND, T>(uf, gr, ft, gas);
+    } else {
+        b200::inviscid_flux<ND, T>(uu, ft, p, vel, T(gas.gamma));
+        b200::viscous_flux_add<ND, T>(uu, gr, ft, gas);
+    }
 
 #pragma unroll
     for (int i = 0; i < ND; i++)
@@ -258,8 +264,19 @@ intcflux_ns_kernel(int64_t n, int rs, Gas gas, T beta, T tau, ScalView<T> vl, Sc
 #pragma unroll
     for (int d = 0; d < ND; d++) nn[d] = inv * nn[d];
 
-    T fi[NV];
-    b200::rsolve<ND, T>(rs, ul, ur, nn, fi, T(gas.gamma));
+    // Riemann flux; with a shifted input the viscous terms need the full
+    // states, which the shifted flux reconstructs
+    T fi[NV], ufl[NV], ufr[NV];
+    if (gas.shifted) {
+        b200::rsolve_rusanov_shift<ND, T>(ul, ur, nn, fi, ufl, ufr, gas);
+    } else {
+        b200::rsolve<ND, T>(rs, ul, ur, nn, fi, T(gas.gamma));
+#pragma unroll
+        for (int v = 0; v < NV; v++) {
+            ufl[v] = ul[v];
+            ufr[v] = ur[v];
+        }
+    }
 
     // LDG viscous common flux from the left and/or right states
     T fvl[ND][NV], fvr[ND][NV];
@@ -276,7 +293,7 @@ intcflux_ns_kernel(int64_t n, int rs, Gas gas, T beta, T tau, ScalView<T> vl, Sc
         for (int d = 0; d < ND; d++)
 #pragma unroll
             for (int v = 0; v < NV; v++) gg[d][v] = g[d * rstr + v * B200_SOASZ];
-        b200::viscous_flux_add<ND, T>(ul, gg, fvl, gas);
+        b200::viscous_flux_add<ND, T>(ufl, gg, fvl, gas);
     }
     if (beta != T(0.5)) {
         const T *g = gr.base + b200::load_ix(gr.map, ix64, i);
@@ -286,7 +303,7 @@ intcflux_ns_kernel(int64_t n, int rs, Gas gas, T beta, T tau, ScalView<T> vl, Sc
         for (int d = 0; d < ND; d++)
 #pragma unroll
             for (int v = 0; v < NV; v++) gg[d][v] = g[d * rstr + v * B200_SOASZ];
-        b200::viscous_flux_add<ND, T>(ur, gg, fvr, gas);
+        b200::viscous_flux_add<ND, T>(ufr, gg, fvr, gas);
     }
 
 #pragma unroll
@@ -450,6 +467,9 @@ int intcflux_ns(int ndims, int64_t n, int rsolver, const b200_gas_t *gas, double
     ScalView<T> l{ul_base, ul_map}, r{ur_base, ur_map};
     VectView<T> gl{gl_base, gl_map, gl_rstr}, gr{gr_base, gr_map, gr_rstr};
     Gas g = *reinterpret_cast<const Gas *>(gas);
+    if (g.shifted && rsolver != b200::RS_RUSANOV)
+        return b200::set_error(B200_ERR_UNSUPPORTED,
+                               "intcflux_ns: shifted inputs need the Rusanov solver");
     unsigned grid = b200::ceil_div(n, PW_BLOCK);
     if (ndims == 2)
         intcflux_ns_kernel<2, T><<<grid, PW_BLOCK, 0, st>>>(n, rsolver, g, (T)beta, (T)tau, l, r, gl, gr, ix64, nl, ldn);

@@ -264,15 +264,42 @@ class MixedRKIntegrator(RKVdH2Integrator):
         super().__init__(backend, systemcls, mesh, cfg, initsoln)
 
     def _make_system(self, backend, systemcls, mesh, initsoln, cfg):
-        return systemcls(backend, mesh, initsoln, 2, cfg)
+        sysm = systemcls(backend, mesh, initsoln, 2, cfg)
+
+        if initsoln is not None:
+            self._ics = [np.asarray(initsoln[et], dtype=np.float64)
+                         for et in sysm.ele_types]
+        else:
+            self._ics = [e.set_ics_from_cfg() for e in sysm.ele_map.values()]
+
+        # Reference-state shift of the FP32 right-hand side (Navier-Stokes
+        # with the Rusanov solver): the volume means of rho and p of the
+        # initial condition.  Must be set before the kernels are built.
+        self.uref = None
+        shift = cfg.get('backend-b200', 'reference-shift', 'auto')
+        rs = cfg.get('solver-interfaces', 'riemann-solver')
+        if shift == 'auto' and sysm.name == 'navier-stokes' and rs == 'rusanov':
+            gamma = cfg.getfloat('constants', 'gamma')
+            rho = np.concatenate([u[:, 0].ravel() for u in self._ics])
+            pri = [e.con_to_pri(list(u.swapaxes(0, 1)), cfg)[-1]
+                   for e, u in zip(sysm.ele_map.values(), self._ics)]
+            p = np.concatenate([x.ravel() for x in pri])
+            rho_ref, p_ref = float(rho.mean()), float(p.mean())
+            backend.ref_state = (rho_ref, p_ref)
+            nv = sysm.nvars
+            self.uref = np.zeros(nv)
+            self.uref[0], self.uref[-1] = rho_ref, p_ref/(gamma - 1)
+
+        return sysm
+
+    def _uref_args(self):
+        if self.uref is None:
+            return 0, None
+        return len(self.uref), self.uref.ctypes.data
 
     def _setup_registers(self, initsoln):
         be, sysm = self.backend, self.system
-        if initsoln is not None:
-            ics = [np.asarray(initsoln[et], dtype=np.float64)
-                   for et in sysm.ele_types]
-        else:
-            ics = [e.set_ics_from_cfg() for e in sysm.ele_map.values()]
+        ics = self._ics
 
         def reg(ic=None):
             return [be.matrix(ic_.shape, ic_ if ic is not None else None,
@@ -283,6 +310,16 @@ class MixedRKIntegrator(RKVdH2Integrator):
         self.rold = reg() if self.errest else None
         self.rerr = reg() if self.errest else None
         be.commit()
+        self.refresh_input(be.stream)
+        be.wait()
+
+    def refresh_input(self, stream):
+        """Enqueue the FP32 RHS input (u - u_ref) from the FP64 solution."""
+        lib, nv_uref = self.backend.lib, self._uref_args()
+        for j, bank in enumerate(self.system.ele_banks):
+            acc = self.acc[j]
+            lib.cast_f64_f32(acc.nrow*acc.leaddim, acc.data, bank[0].data,
+                             *nv_uref, stream)
 
     def _stage_kernel(self, i, j, dt):
         lib, nst, errest = self.backend.lib, self.nstages, int(self.errest)
@@ -294,10 +331,11 @@ class MixedRKIntegrator(RKVdH2Integrator):
         ro = self.rold[j].data if self.errest else None
         re = self.rerr[j].data if self.errest else None
         pa, pr, pu = acc.data, bank[1].data, bank[0].data
+        nvu, pref = self._uref_args()
 
         def run(stream):
             lib.rkmixed_f64f32(n, i, nst, errest, dt, a, b, e, pa, pr, pu, ro,
-                               re, stream)
+                               re, nvu, pref, stream)
 
         return Kernel(run, mats=[acc, bank[0], bank[1]], name='rkmixed',
                       meta=dict(kind='rkmixed', n=n))
@@ -316,11 +354,10 @@ class MixedRKIntegrator(RKVdH2Integrator):
 
     def _restore_previous(self):
         lib, stream = self.backend.lib, self.backend.stream
-        for j, bank in enumerate(self.system.ele_banks):
+        for j in range(len(self.acc)):
             acc = self.acc[j]
             lib.memcpy_dtod(acc.data, self.rold[j].data, acc.nbytes, stream)
-            lib.cast_f64_f32(acc.nrow*acc.leaddim, acc.data, bank[0].data,
-                             stream)
+        self.refresh_input(stream)
 
     def _errest(self, icurr, ierr):
         if 'mixed' not in self._ekerns:
