@@ -324,6 +324,9 @@ def history(intg, nsteps, every):
         if intg.nsteps % every == 0:
             r = fi()
             hist[intg.nsteps] = 0.5*r['E']/r['vol']
+    if intg.nsteps not in hist:
+        r = fi()
+        hist[intg.nsteps] = 0.5*r['E']/r['vol']
     return intg.soln, hist
 
 
@@ -350,7 +353,8 @@ def run_gpu(args, dist):
         (uc,), hc = history(intg, args.accuracy_steps, args.ke_every)
         rc['l2_err'] = float(np.linalg.norm((uc - up).ravel()) /
                              np.linalg.norm(up.ravel()))
-        rc['ke_err'] = float(max(abs(hc[s] - hp[s]) for s in hp))
+        common = [s for s in hp if s in hc]
+        rc['ke_err'] = float(max(abs(hc[s] - hp[s]) for s in common))
         rc['ke_final'] = hc[max(hc)]
         out[form] = rc
         del intg
