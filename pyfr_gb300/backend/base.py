@@ -161,6 +161,18 @@ class B200Backend:
         self._mem_peak = max(self._mem_peak, self._mem_cur)
         return p.value
 
+    def free_matrix(self, m):
+        """Release a matrix that owns its allocation (one made without a
+        named extent); using it afterwards is an error."""
+        for i, (p, n) in enumerate(self._allocs):
+            if p == m.basedata and m.offset == 0:
+                self.lib.free(p)
+                self._mem_cur -= n
+                del self._allocs[i]
+                m.basedata = None
+                return
+        raise ValueError('Matrix does not own an allocation')
+
     def memcpy_htod(self, dst, src, nbytes):
         src = np.ascontiguousarray(src)
         self.lib.memcpy_htod(dst, src.ctypes.data, nbytes, self._stream)

@@ -246,6 +246,30 @@ class RKVdH2Integrator:
     def soln(self):
         return self.system.ele_scal_upts(self.idxcurr)
 
+    def _state_mats(self):
+        return [m for bank in self.system.ele_banks for m in bank]
+
+    def snapshot(self):
+        """Device copies of every register, restored by ``restore``."""
+        be, lib = self.backend, self.backend.lib
+        snap = []
+        for m in self._state_mats():
+            c = be.matrix(m.ioshape, tags={'align'}, dtype=m.dtype)
+            be.commit()
+            lib.memcpy_dtod(c.data, m.data, m.nbytes, be.stream)
+            snap.append(c)
+        be.wait()
+        return snap
+
+    def restore(self, snap, release=True):
+        be, lib = self.backend, self.backend.lib
+        for m, c in zip(self._state_mats(), snap):
+            lib.memcpy_dtod(m.data, c.data, m.nbytes, be.stream)
+        be.wait()
+        if release:
+            for c in snap:
+                be.free_matrix(c)
+
 
 class MixedRKIntegrator(RKVdH2Integrator):
     """The chosen precision form: right-hand sides in FP32 (the system is
@@ -291,6 +315,12 @@ class MixedRKIntegrator(RKVdH2Integrator):
             self.uref[0], self.uref[-1] = rho_ref, p_ref/(gamma - 1)
 
         return sysm
+
+    def _state_mats(self):
+        mats = [m for bank in self.system.ele_banks for m in bank] + self.acc
+        if self.errest:
+            mats += self.rold + self.rerr
+        return mats
 
     def _uref_args(self):
         if self.uref is None:
