@@ -36,30 +36,36 @@ constexpr int NEPI = 128;         // epilogue threads (warps 0-3)
 constexpr int MAX_MT = 4;         // up to 512 operator rows (TMEM: 2*4*64 cols)
 constexpr long long WAIT_LIMIT = 1LL << 22;
 
+constexpr int MAX_S32 = 4;        // FP32 staging stages (bytes in flight)
+
 struct UmmaHandle {
-    int m, k, mpad, kpad, mt, nt;
+    int m, k, mpad, kpad, mt, nt, s32;
     unsigned char *aimg;   // device: [hi | lo], each mpad x kpad bf16 canonical
     size_t aimg_bytes;
     size_t smem_bytes;
 };
 
+// Shared-memory plan; stage buffers are addressed arithmetically (a
+// runtime-indexed array here would live in local memory)
 struct Layout {
-    uint32_t a_hi, a_lo, b32[2], bhi[2], blo[2], bar, tslot, abort_flag;
-    uint32_t total;
+    uint32_t a_hi, a_lo;
+    uint32_t b32, b32_stride;     // FP32 staging stage s at b32 + s*b32_stride
+    uint32_t b16, b16_stride;     // BF16 stage s: hi at b16 + s*b16_stride, lo after hi
+    uint32_t b16_half;            // bytes of one (hi or lo) BF16 tile
+    uint32_t bar, tslot, abort_flag, total;
 };
 
-template <int NT>
-__host__ __device__ inline Layout make_layout(int mpad, int kpad, int k) {
+__host__ __device__ inline Layout make_layout(int mpad, int kpad, int k, int nt, int s32) {
     Layout L;
     uint32_t off = 0;
     const uint32_t abytes = (uint32_t)mpad * kpad * 2;
-    const uint32_t b32bytes = (uint32_t)k * NT * 4;
-    const uint32_t b16bytes = (uint32_t)NT * kpad * 2;
+    const uint32_t b32bytes = ((uint32_t)k * nt * 4 + 127) & ~127u;
+    const uint32_t b16bytes = (uint32_t)nt * kpad * 2;
     L.a_hi = off; off += abytes;
     L.a_lo = off; off += abytes;
-    for (int s = 0; s < 2; s++) { L.b32[s] = off; off += (b32bytes + 127) & ~127u; }
-    for (int s = 0; s < 2; s++) { L.bhi[s] = off; off += b16bytes; L.blo[s] = off; off += b16bytes; }
-    L.bar = off; off += 16 * 8;
+    L.b32 = off; L.b32_stride = b32bytes; off += s32 * b32bytes;
+    L.b16 = off; L.b16_stride = 2 * b16bytes; L.b16_half = b16bytes; off += 2 * 2 * b16bytes;
+    L.bar = off; off += 24 * 8;
     L.tslot = off; off += 8;
     L.abort_flag = off; off += 8;
     L.total = off;
@@ -67,8 +73,9 @@ __host__ __device__ inline Layout make_layout(int mpad, int kpad, int k) {
 }
 
 // Barrier indices within the barrier block
-enum { BAR_A = 0, BAR_FULL32 = 1, BAR_EMPTY32 = 3, BAR_FULL16 = 5, BAR_EMPTY16 = 7,
-       BAR_ACCFULL = 9, BAR_ACCEMPTY = 11, BAR_DRAIN = 13 };
+enum { BAR_A = 0, BAR_FULL32 = 1, BAR_EMPTY32 = 1 + MAX_S32, BAR_FULL16 = 1 + 2 * MAX_S32,
+       BAR_EMPTY16 = 3 + 2 * MAX_S32, BAR_ACCFULL = 5 + 2 * MAX_S32,
+       BAR_ACCEMPTY = 7 + 2 * MAX_S32, BAR_DRAIN = 9 + 2 * MAX_S32 };
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -147,7 +154,7 @@ struct UmmaArgs {
     const float *b;
     float *c;
     int64_t ldb, ldc, ncol;
-    int m, k, kpad, mt;
+    int m, k, kpad, mt, s32;
     float alpha, beta;
     int epi;            // 0: alpha*D, 1: alpha*D + beta*C
     int *err;
@@ -156,7 +163,8 @@ struct UmmaArgs {
 template <int NT>
 __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(UmmaArgs p) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    const Layout L = make_layout<NT>(p.mt * MTILE, p.kpad, p.k);
+    const Layout L = make_layout(p.mt * MTILE, p.kpad, p.k, NT, p.s32);
+    const int S32 = p.s32;
     const uint32_t sbase = smem_addr(smem);
     const uint32_t bar0 = sbase + L.bar;
     auto bar = [&](int i) { return bar0 + 8u * i; };
@@ -172,9 +180,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(UmmaArgs p) {
     if (tid == 0) {
         *abort_flag = 0;
         bar_init(bar(BAR_A), 1);
-        for (int s = 0; s < 2; s++) {
+        for (int s = 0; s < S32; s++) {
             bar_init(bar(BAR_FULL32 + s), 1);
             bar_init(bar(BAR_EMPTY32 + s), NCONV);
+        }
+        for (int s = 0; s < 2; s++) {
             bar_init(bar(BAR_FULL16 + s), NCONV);
             bar_init(bar(BAR_EMPTY16 + s), 1);
             bar_init(bar(BAR_ACCFULL + s), 1);
@@ -198,24 +208,31 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(UmmaArgs p) {
 
     if (warp == 4) {
         // ---- producer: operator image once, then the FP32 B tiles ----
-        if (lane == 0) {
-            bar_arrive_tx(bar(BAR_A), 2 * abytes);
-            bulk_g2s(sbase + L.a_hi, p.aimg, 2 * abytes, bar(BAR_A));
+        // (every lane issues a share of the row copies of a tile)
+        if (lane == 0) bar_arrive_tx(bar(BAR_A), 2 * abytes);
+        __syncwarp();
+        {
+            const uint32_t chunk = ((2 * abytes / 32) + 15) & ~15u;
+            const uint32_t a0 = lane * chunk;
+            if (a0 < 2 * abytes) {
+                const uint32_t nb = 2 * abytes - a0 < chunk ? 2 * abytes - a0 : chunk;
+                bulk_g2s(sbase + L.a_hi + a0, p.aimg + a0, nb, bar(BAR_A));
+            }
         }
         int i = 0;
         for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
-            const int s = i & 1;
-            if (i >= 2 && !bar_wait(bar(BAR_EMPTY32 + s), ((i >> 1) + 1) & 1, abort_flag, p.err, 1))
+            const int s = i % S32, ph = (i / S32) & 1;
+            if (i >= S32 && !bar_wait(bar(BAR_EMPTY32 + s), ph ^ 1, abort_flag, p.err, 1))
                 break;
-            if (lane == 0) {
-                const int64_t col0 = t * NT;
-                const int64_t nc = p.ncol - col0 < NT ? p.ncol - col0 : NT;
-                const uint32_t rowb = (uint32_t)nc * 4;
-                bar_arrive_tx(bar(BAR_FULL32 + s), rowb * p.k);
-                for (int r = 0; r < p.k; r++)
-                    bulk_g2s(sbase + L.b32[s] + (uint32_t)r * NT * 4, p.b + r * p.ldb + col0, rowb,
-                             bar(BAR_FULL32 + s));
-            }
+            const int64_t col0 = t * NT;
+            const int64_t nc = p.ncol - col0 < NT ? p.ncol - col0 : NT;
+            const uint32_t rowb = (uint32_t)nc * 4;
+            const uint32_t dst = sbase + L.b32 + (uint32_t)s * L.b32_stride;
+            if (lane == 0) bar_arrive_tx(bar(BAR_FULL32 + s), rowb * p.k);
+            __syncwarp();
+            for (int r = lane; r < p.k; r += 32)
+                bulk_g2s(dst + (uint32_t)r * NT * 4, p.b + r * p.ldb + col0, rowb,
+                         bar(BAR_FULL32 + s));
             __syncwarp();
         }
     } else if (warp >= 5 && warp <= 8) {
@@ -224,12 +241,13 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(UmmaArgs p) {
         const int n = ct % NT;
         int i = 0;
         for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
-            const int s = i & 1;
-            if (!bar_wait(bar(BAR_FULL32 + s), (i >> 1) & 1, abort_flag, p.err, 2)) break;
-            if (i >= 2 && !bar_wait(bar(BAR_EMPTY16 + s), ((i >> 1) + 1) & 1, abort_flag, p.err, 3))
+            const int s = i % S32, s2 = i & 1;
+            if (!bar_wait(bar(BAR_FULL32 + s), (i / S32) & 1, abort_flag, p.err, 2)) break;
+            if (i >= 2 && !bar_wait(bar(BAR_EMPTY16 + s2), ((i >> 1) + 1) & 1, abort_flag, p.err, 3))
                 break;
-            const float *b32 = reinterpret_cast<const float *>(smem + L.b32[s]);
-            unsigned char *bhi = smem + L.bhi[s], *blo = smem + L.blo[s];
+            const float *b32 = reinterpret_cast<const float *>(smem + L.b32 + s * L.b32_stride);
+            unsigned char *bhi = smem + L.b16 + s2 * L.b16_stride;
+            unsigned char *blo = bhi + L.b16_half;
             for (int k8 = ct / NT; k8 < p.kpad / 8; k8 += NCONV / NT) {
                 uint32_t hw[4], lw[4];
 #pragma unroll
@@ -252,7 +270,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(UmmaArgs p) {
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             bar_arrive(bar(BAR_EMPTY32 + s));
-            bar_arrive(bar(BAR_FULL16 + s));
+            bar_arrive(bar(BAR_FULL16 + s2));
         }
     } else if (warp == 9) {
         // ---- MMA issuer ----
@@ -275,8 +293,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(UmmaArgs p) {
                         const uint32_t ko = (uint32_t)ks * 2 * LBO;
                         const uint64_t dah = sdesc(ahi + ko, LBO, SBO);
                         const uint64_t dal = sdesc(alo + ko, LBO, SBO);
-                        const uint64_t dbh = sdesc(sbase + L.bhi[s] + ko, LBO, SBO);
-                        const uint64_t dbl = sdesc(sbase + L.blo[s] + ko, LBO, SBO);
+                        const uint32_t bst = sbase + L.b16 + s * L.b16_stride;
+                        const uint64_t dbh = sdesc(bst + ko, LBO, SBO);
+                        const uint64_t dbl = sdesc(bst + L.b16_half + ko, LBO, SBO);
                         umma(d, dah, dbh, idesc, ks > 0);
                         umma(d, dah, dbl, idesc, 1);
                         umma(d, dal, dbh, idesc, 1);
@@ -374,12 +393,20 @@ int b200_mul_bf16x3_create(const double *a, int m, int k, void **handle, size_t 
         return b200::set_error(B200_ERR_ARG, "mul_bf16x3_create: bad arguments");
     const int mpad = (m + MTILE - 1) / MTILE * MTILE, kpad = (k + 15) / 16 * 16;
     const int mt = mpad / MTILE;
-    // Widest column tile whose pipeline fits in shared memory
-    int nt = 64;
-    Layout L = make_layout<64>(mpad, kpad, k);
-    if (L.total > 227 * 1024) {
-        nt = 32;
-        L = make_layout<32>(mpad, kpad, k);
+    // Widest column tile, then the deepest FP32 staging (bytes in flight
+    // per SM), whose pipeline fits in shared memory
+    int nt = 0, s32 = 0;
+    Layout L = make_layout(mpad, kpad, k, 32, 2);
+    for (int cand_nt : {64, 32}) {
+        for (int cand_s = MAX_S32; cand_s >= 2 && !nt; cand_s--) {
+            Layout c = make_layout(mpad, kpad, k, cand_nt, cand_s);
+            if (c.total <= 227 * 1024) {
+                nt = cand_nt;
+                s32 = cand_s;
+                L = c;
+            }
+        }
+        if (nt) break;
     }
     if (smem_bytes) *smem_bytes = L.total;
     if (mt > MAX_MT || L.total > 227 * 1024 || kpad / 16 * 3 * mt > 1024)
@@ -415,7 +442,7 @@ int b200_mul_bf16x3_create(const double *a, int m, int k, void **handle, size_t 
 
     UmmaHandle *h = (UmmaHandle *)calloc(1, sizeof(UmmaHandle));
     if (!h) return b200::set_error(B200_ERR_STATE, "mul_bf16x3_create: out of host memory");
-    h->m = m; h->k = k; h->mpad = mpad; h->kpad = kpad; h->mt = mt; h->nt = nt;
+    h->m = m; h->k = k; h->mpad = mpad; h->kpad = kpad; h->mt = mt; h->nt = nt; h->s32 = s32;
     h->aimg_bytes = img.size() * 2;
     h->smem_bytes = L.total;
     int rc = b200::check_cuda(cudaMalloc(&h->aimg, h->aimg_bytes), "mul_bf16x3_create");
@@ -455,7 +482,7 @@ int b200_mul_bf16x3(void *handle, const float *b, int64_t ldb, float *c, int64_t
 
     UmmaArgs p;
     p.aimg = h->aimg; p.b = b; p.c = c; p.ldb = ldb; p.ldc = ldc; p.ncol = ncol;
-    p.m = h->m; p.k = h->k; p.kpad = h->kpad; p.mt = h->mt;
+    p.m = h->m; p.k = h->k; p.kpad = h->kpad; p.mt = h->mt; p.s32 = h->s32;
     p.alpha = alpha; p.beta = beta; p.epi = beta != 0.0f; p.err = err;
 
     const int64_t ntiles = (ncol + h->nt - 1) / h->nt;

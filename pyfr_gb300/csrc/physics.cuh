@@ -28,6 +28,36 @@ struct Gas {
     double rho_ref, p_ref;
 };
 
+// The same constants in the kernel's arithmetic type, with every derived
+// quantity formed once on the host: on this GPU a per-thread FP64
+// division costs more than the whole FP32 flux evaluation.
+template <typename T>
+struct GasK {
+    T gamma, gm1, mu, gamma_pr, rcp_cpTref, mu_ctt, cpTs, quarter_gamma;
+    T rho_ref, p_ref, e_ref, h_ref;
+    int sutherland, shifted;
+};
+
+template <typename T>
+inline GasK<T> gas_consts(const Gas &g) {
+    GasK<T> k;
+    k.gamma = (T)g.gamma;
+    k.gm1 = (T)(g.gamma - 1.0);
+    k.mu = (T)g.mu;
+    k.gamma_pr = (T)(g.gamma / g.pr);
+    k.rcp_cpTref = (T)(1.0 / g.cpTref);
+    k.mu_ctt = (T)(g.mu * (g.cpTref + g.cpTs));
+    k.cpTs = (T)g.cpTs;
+    k.quarter_gamma = (T)(0.25 * g.gamma);
+    k.rho_ref = (T)g.rho_ref;
+    k.p_ref = (T)g.p_ref;
+    k.e_ref = (T)(g.p_ref / (g.gamma - 1.0));
+    k.h_ref = (T)(g.gamma / (g.gamma - 1.0) * g.p_ref);
+    k.sutherland = g.sutherland;
+    k.shifted = g.shifted;
+    return k;
+}
+
 enum RSolver { RS_RUSANOV = 0, RS_HLLC = 1 };
 
 template <int ND, typename T>
@@ -57,7 +87,7 @@ __device__ __forceinline__ void inviscid_flux(const T *s, T f[ND][ND + 2], T &p,
 // physical gradient of the conserved variables.
 template <int ND, typename T>
 __device__ __forceinline__ void viscous_flux_add(const T *uin, const T grad[ND][ND + 2],
-                                                 T fout[ND][ND + 2], const Gas &g) {
+                                                 T fout[ND][ND + 2], const GasK<T> &g) {
     constexpr int NV = ND + 2;
     const T rho = uin[0], E = uin[NV - 1];
     const T rcprho = T(1) / rho;
@@ -77,11 +107,11 @@ __device__ __forceinline__ void viscous_flux_add(const T *uin, const T grad[ND][
         T ke = 0;
 #pragma unroll
         for (int i = 0; i < ND; i++) ke += vel[i] * vel[i];
-        const T cpT = T(g.gamma) * (rcprho * E - T(0.5) * ke);
-        const T Trat = T(1.0 / g.cpTref) * cpT;
-        mu_c = T(g.mu * (g.cpTref + g.cpTs)) * Trat * sqrt(Trat) / (cpT + T(g.cpTs));
+        const T cpT = g.gamma * (rcprho * E - T(0.5) * ke);
+        const T Trat = g.rcp_cpTref * cpT;
+        mu_c = g.mu_ctt * Trat * sqrt(Trat) / (cpT + g.cpTs);
     } else {
-        mu_c = T(g.mu);
+        mu_c = g.mu;
     }
 
     // Temperature derivatives (c_v dT/dx_d)
@@ -108,7 +138,7 @@ __device__ __forceinline__ void viscous_flux_add(const T *uin, const T grad[ND][
         }
     }
 
-    const T kcoef = -mu_c * T(g.gamma / g.pr);
+    const T kcoef = -mu_c * g.gamma_pr;
 #pragma unroll
     for (int d = 0; d < ND; d++) {
         T e = kcoef * dT[d];
@@ -152,10 +182,10 @@ __device__ __forceinline__ void rsolve_rusanov(const T *ul, const T *ur, const T
 // pressure in p and the full state in ufull (for the viscous terms).
 template <int ND, typename T>
 __device__ __forceinline__ void inviscid_flux_shift(const T *s, T f[ND][ND + 2], T &p, T v[ND],
-                                                    T ufull[ND + 2], const Gas &g) {
+                                                    T ufull[ND + 2], const GasK<T> &g) {
     constexpr int NV = ND + 2;
-    const T gm1 = T(g.gamma - 1.0);
-    const T rho = T(g.rho_ref) + s[0], invrho = T(1) / rho, dE = s[NV - 1];
+    const T gm1 = g.gm1;
+    const T rho = g.rho_ref + s[0], invrho = T(1) / rho, dE = s[NV - 1];
     T dot = 0;
 #pragma unroll
     for (int i = 0; i < ND; i++) {
@@ -163,8 +193,8 @@ __device__ __forceinline__ void inviscid_flux_shift(const T *s, T f[ND][ND + 2],
         dot += s[i + 1] * v[i];
     }
     const T dp = gm1 * (dE - T(0.5) * dot);
-    p = T(g.p_ref) + dp;
-    const T hv = T(g.gamma / (g.gamma - 1.0) * g.p_ref) + dE + dp;
+    p = g.p_ref + dp;
+    const T hv = g.h_ref + dE + dp;
 #pragma unroll
     for (int i = 0; i < ND; i++) {
         f[i][0] = s[i + 1];
@@ -175,14 +205,15 @@ __device__ __forceinline__ void inviscid_flux_shift(const T *s, T f[ND][ND + 2],
     ufull[0] = rho;
 #pragma unroll
     for (int i = 0; i < ND; i++) ufull[i + 1] = s[i + 1];
-    ufull[NV - 1] = T(g.p_ref / (g.gamma - 1.0)) + dE;
+    ufull[NV - 1] = g.e_ref + dE;
 }
 
 // Rusanov flux on perturbation inputs (dissipation acts on differences, so
 // the shift cancels there)
 template <int ND, typename T>
 __device__ __forceinline__ void rsolve_rusanov_shift(const T *ul, const T *ur, const T *n, T *nf,
-                                                     T ufl[ND + 2], T ufr[ND + 2], const Gas &g) {
+                                                     T ufl[ND + 2], T ufr[ND + 2],
+                                                     const GasK<T> &g) {
     constexpr int NV = ND + 2;
     T fl[ND][NV], fr[ND][NV], vl[ND], vr[ND], pl, pr;
     inviscid_flux_shift<ND, T>(ul, fl, pl, vl, ufl, g);
@@ -191,7 +222,7 @@ __device__ __forceinline__ void rsolve_rusanov_shift(const T *ul, const T *ur, c
     T nv = 0;
 #pragma unroll
     for (int i = 0; i < ND; i++) nv += n[i] * (vl[i] + vr[i]);
-    const T a = sqrt(T(0.25 * g.gamma) * (pl + pr) / (ufl[0] + ufr[0])) + T(0.25) * fabs(nv);
+    const T a = sqrt(g.quarter_gamma * (pl + pr) / (ufl[0] + ufr[0])) + T(0.25) * fabs(nv);
 
 #pragma unroll
     for (int i = 0; i < NV; i++) {

@@ -92,7 +92,7 @@ tflux_euler_kernel(int nupts, int64_t neles, T gamma, const T *__restrict__ u, i
 
 template <int ND, typename T>
 __global__ void __launch_bounds__(PW_BLOCK)
-tflux_ns_kernel(int nupts, int64_t neles, Gas gas, const T *__restrict__ u, int64_t ldu,
+tflux_ns_kernel(int nupts, int64_t neles, b200::GasK<T> gas, const T *__restrict__ u, int64_t ldu,
                 T *__restrict__ f, int64_t ldf, T *__restrict__ gradu, int64_t ldg,
                 ElemGeom<T> geo) {
     constexpr int NV = ND + 2;
@@ -130,7 +130,7 @@ tflux_ns_kernel(int nupts, int64_t neles, Gas gas, const T *__restrict__ u, int6
         b200::inviscid_flux_shift<ND, T>(uu, ft, p, vel, uf, gas);
         b200::viscous_flux_add<ND, T>(uf, gr, ft, gas);
     } else {
-        b200::inviscid_flux<ND, T>(uu, ft, p, vel, T(gas.gamma));
+        b200::inviscid_flux<ND, T>(uu, ft, p, vel, gas.gamma);
         b200::viscous_flux_add<ND, T>(uu, gr, ft, gas);
     }
 
@@ -238,7 +238,7 @@ intcflux_euler_kernel(int64_t n, int rs, T gamma, ScalView<T> vl, ScalView<T> vr
 
 template <int ND, typename T>
 __global__ void __launch_bounds__(PW_BLOCK)
-intcflux_ns_kernel(int64_t n, int rs, Gas gas, T beta, T tau, ScalView<T> vl, ScalView<T> vr,
+intcflux_ns_kernel(int64_t n, int rs, b200::GasK<T> gas, T beta, T tau, ScalView<T> vl, ScalView<T> vr,
                    VectView<T> gl, VectView<T> gr, int ix64, const T *__restrict__ nl,
                    int64_t ldn) {
     constexpr int NV = ND + 2;
@@ -270,7 +270,7 @@ intcflux_ns_kernel(int64_t n, int rs, Gas gas, T beta, T tau, ScalView<T> vl, Sc
     if (gas.shifted) {
         b200::rsolve_rusanov_shift<ND, T>(ul, ur, nn, fi, ufl, ufr, gas);
     } else {
-        b200::rsolve<ND, T>(rs, ul, ur, nn, fi, T(gas.gamma));
+        b200::rsolve<ND, T>(rs, ul, ur, nn, fi, gas.gamma);
 #pragma unroll
         for (int v = 0; v < NV; v++) {
             ufl[v] = ul[v];
@@ -404,7 +404,7 @@ int tflux_ns(int ndims, int nupts, int64_t neles, int linear, const b200_gas_t *
     int rc = check_geom(linear, smats, rcpdjac, verts, upts, true);
     if (rc) return rc;
     auto geo = make_geom<T>(linear, smats, lds, rcpdjac, ldr, verts, ldv, upts, ldup);
-    Gas g = *reinterpret_cast<const Gas *>(gas);
+    const auto g = b200::gas_consts<T>(*reinterpret_cast<const Gas *>(gas));
     dim3 grid(b200::ceil_div(neles, PW_BLOCK), nupts);
     if (ndims == 2)
         tflux_ns_kernel<2, T><<<grid, PW_BLOCK, 0, st>>>(nupts, neles, g, u, ldu, f, ldf, gradu, ldg, geo);
@@ -466,7 +466,7 @@ int intcflux_ns(int ndims, int64_t n, int rsolver, const b200_gas_t *gas, double
         return b200::set_error(B200_ERR_ARG, "intcflux: unknown Riemann solver %d", rsolver);
     ScalView<T> l{ul_base, ul_map}, r{ur_base, ur_map};
     VectView<T> gl{gl_base, gl_map, gl_rstr}, gr{gr_base, gr_map, gr_rstr};
-    Gas g = *reinterpret_cast<const Gas *>(gas);
+    const auto g = b200::gas_consts<T>(*reinterpret_cast<const Gas *>(gas));
     if (g.shifted && rsolver != b200::RS_RUSANOV)
         return b200::set_error(B200_ERR_UNSUPPORTED,
                                "intcflux_ns: shifted inputs need the Rusanov solver");
