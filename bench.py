@@ -129,8 +129,12 @@ def kernel_bytes(k, be):
     if kind in ('intcflux_ns', 'intcflux_euler'):
         (n,) = m['dims']
         nd, nv = m['tplargs']['ndims'], m['tplargs']['nvars']
-        vals = 4*nv + nd + (2*nd*nv if kind == 'intcflux_ns' else 0)
-        maps = 2 + (4 if kind == 'intcflux_ns' else 0)
+        # Gradients are read from one side when ldg-beta = +-1/2
+        nsides = 0
+        if kind == 'intcflux_ns':
+            nsides = 1 if abs(m['tplargs']['c']['ldg-beta']) == 0.5 else 2
+        vals = 4*nv + nd + nsides*nd*nv
+        maps = 2 + 2*nsides
         return n*(vals*itemsize + maps*4)
     if kind == 'intconu':
         (n,) = m['dims']

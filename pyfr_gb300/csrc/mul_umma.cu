@@ -320,35 +320,48 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(UmmaArgs p) {
             const int64_t col0 = t * NT;
             for (int q = 0; q < mt; q++) {
                 const int row = q * MTILE + row_in_tile;
+                const bool rowok = row < p.m;
                 float *crow = p.c + (int64_t)row * p.ldc + col0;
-                for (int cc = 0; cc < NT; cc += 8) {
-                    uint32_t v[8];
+                // 32 columns per round: the C reads (beta != 0) and the TMEM
+                // read are all in flight before the single wait
+                for (int cc = 0; cc < NT; cc += 32) {
+                    const int64_t left = p.ncol - (col0 + cc);     // multiple of 4
+                    const int nq = !rowok || left <= 0 ? 0 : (left >= 32 ? 8 : (int)(left / 4));
+                    float4 cv[8];
+                    if (p.epi) {
+#pragma unroll
+                        for (int j = 0; j < 8; j++)
+                            if (j < nq) cv[j] = reinterpret_cast<const float4 *>(crow + cc)[j];
+                    }
+                    uint32_t v[32];
                     const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) +
                                            (uint32_t)(bsel * mt + q) * NT + cc;
-                    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                                 : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]),
-                                   "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
-                                 : "r"(taddr));
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+                        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
+                          "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]),
+                          "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]),
+                          "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+                          "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]),
+                          "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                        : "r"(taddr));
                     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                    // ncol is a multiple of 4: store whole float4 halves only
-                    const int64_t left = p.ncol - (col0 + cc);
-                    if (row < p.m && left > 0) {
-                        float o[8];
+                    float4 *dst = reinterpret_cast<float4 *>(crow + cc);
 #pragma unroll
-                        for (int j = 0; j < 8; j++) o[j] = p.alpha * __uint_as_float(v[j]);
-                        float4 *dst = reinterpret_cast<float4 *>(crow + cc);
-                        if (p.epi) {
-                            const float4 c0 = dst[0];
-                            o[0] += p.beta * c0.x; o[1] += p.beta * c0.y;
-                            o[2] += p.beta * c0.z; o[3] += p.beta * c0.w;
-                            if (left >= 8) {
-                                const float4 c1 = dst[1];
-                                o[4] += p.beta * c1.x; o[5] += p.beta * c1.y;
-                                o[6] += p.beta * c1.z; o[7] += p.beta * c1.w;
+                    for (int j = 0; j < 8; j++) {
+                        if (j < nq) {
+                            float4 o = make_float4(p.alpha * __uint_as_float(v[4 * j]),
+                                                   p.alpha * __uint_as_float(v[4 * j + 1]),
+                                                   p.alpha * __uint_as_float(v[4 * j + 2]),
+                                                   p.alpha * __uint_as_float(v[4 * j + 3]));
+                            if (p.epi) {
+                                o.x += p.beta * cv[j].x; o.y += p.beta * cv[j].y;
+                                o.z += p.beta * cv[j].z; o.w += p.beta * cv[j].w;
                             }
+                            dst[j] = o;
                         }
-                        dst[0] = make_float4(o[0], o[1], o[2], o[3]);
-                        if (left >= 8) dst[1] = make_float4(o[4], o[5], o[6], o[7]);
                     }
                 }
             }
