@@ -19,6 +19,8 @@
 // layout and bulk-copied into shared memory once per CTA.  All hand-offs
 // are mbarriers; every wait is bounded and records an error code instead
 // of hanging.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <stdlib.h>
 #include <string.h>
@@ -149,7 +151,17 @@ __device__ __forceinline__ void umma_commit(uint32_t bar) {
                  :: "r"(bar) : "memory");
 }
 
+// One 2-D TMA load of a k-row x NT-column box of B into the dense FP32
+// staging buffer (columns past ncol are zero-filled by the hardware)
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y,
+                                            uint32_t bar) {
+    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                 " [%0], [%1, {%2, %3}], [%4];"
+                 :: "r"(dst), "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar) : "memory");
+}
+
 struct UmmaArgs {
+    CUtensorMap tmap;           // B as a (k x ncol) FP32 tensor, box NT x k
     const unsigned char *aimg;
     const float *b;
     float *c;
@@ -161,7 +173,7 @@ struct UmmaArgs {
 };
 
 template <int NT>
-__global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(UmmaArgs p) {
+__global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_constant__ UmmaArgs p) {
     extern __shared__ __align__(1024) unsigned char smem[];
     const Layout L = make_layout(p.mt * MTILE, p.kpad, p.k, NT, p.s32);
     const int S32 = p.s32;
@@ -224,15 +236,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(UmmaArgs p) {
             const int s = i % S32, ph = (i / S32) & 1;
             if (i >= S32 && !bar_wait(bar(BAR_EMPTY32 + s), ph ^ 1, abort_flag, p.err, 1))
                 break;
-            const int64_t col0 = t * NT;
-            const int64_t nc = p.ncol - col0 < NT ? p.ncol - col0 : NT;
-            const uint32_t rowb = (uint32_t)nc * 4;
             const uint32_t dst = sbase + L.b32 + (uint32_t)s * L.b32_stride;
-            if (lane == 0) bar_arrive_tx(bar(BAR_FULL32 + s), rowb * p.k);
-            __syncwarp();
-            for (int r = lane; r < p.k; r += 32)
-                bulk_g2s(dst + (uint32_t)r * NT * 4, p.b + r * p.ldb + col0, rowb,
-                         bar(BAR_FULL32 + s));
+            if (lane == 0) {
+                bar_arrive_tx(bar(BAR_FULL32 + s), (uint32_t)p.k * NT * 4);
+                tma_load_2d(dst, &p.tmap, (int)(t * NT), 0, bar(BAR_FULL32 + s));
+            }
             __syncwarp();
         }
     } else if (warp >= 5 && warp <= 8) {
@@ -396,6 +404,24 @@ void build_image(const double *a, int m, int k, int mpad, int kpad, std::vector<
 }
 
 int g_sm_count = 0;
+PFN_cuTensorMapEncodeTiled_v12000 g_encode_tiled = nullptr;
+
+// Tensor map of B: rank 2, dims (ncol, k) innermost first, row stride
+// ldb*4 bytes, box (nt, k), no swizzle, out-of-range elements read as 0
+int encode_b_map(CUtensorMap *map, const float *b, int64_t ldb, int64_t ncol, int k, int nt) {
+    cuuint64_t gdim[2] = {(cuuint64_t)ncol, (cuuint64_t)k};
+    cuuint64_t gstride[1] = {(cuuint64_t)ldb * 4};
+    cuuint32_t box[2] = {(cuuint32_t)nt, (cuuint32_t)k};
+    cuuint32_t estride[2] = {1, 1};
+    CUresult r = g_encode_tiled(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)b, gdim, gstride,
+                                box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS)
+        return b200::set_error(B200_ERR_CUDA, "mul_bf16x3: cuTensorMapEncodeTiled failed (%d)",
+                               (int)r);
+    return B200_OK;
+}
 
 }  // namespace
 
@@ -422,7 +448,8 @@ int b200_mul_bf16x3_create(const double *a, int m, int k, void **handle, size_t 
         if (nt) break;
     }
     if (smem_bytes) *smem_bytes = L.total;
-    if (mt > MAX_MT || L.total > 227 * 1024 || kpad / 16 * 3 * mt > 1024)
+    // (a TMA box spans at most 256 rows of B)
+    if (mt > MAX_MT || !nt || L.total > 227 * 1024 || k > 256 || kpad / 16 * 3 * mt > 1024)
         return b200::set_error(B200_ERR_UNSUPPORTED,
                                "mul_bf16x3: operator %dx%d needs %u bytes of shared memory", m,
                                k, L.total);
@@ -446,6 +473,16 @@ int b200_mul_bf16x3_create(const double *a, int m, int k, void **handle, size_t 
                                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                         227 * 1024),
                                    "mul_bf16x3: smem attribute");
+        if (!rc0) {
+            void *fn = nullptr;
+            cudaDriverEntryPointQueryResult q;
+            rc0 = b200::check_cuda(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn,
+                                                                    12000, cudaEnableDefault, &q),
+                                   "mul_bf16x3: driver entry point");
+            if (!rc0 && (q != cudaDriverEntryPointSuccess || !fn))
+                rc0 = b200::set_error(B200_ERR_CUDA, "mul_bf16x3: cuTensorMapEncodeTiled missing");
+            g_encode_tiled = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+        }
         if (rc0) return rc0;
         g_sm_count = sms;
     }
@@ -494,6 +531,8 @@ int b200_mul_bf16x3(void *handle, const float *b, int64_t ldb, float *c, int64_t
         return b200::set_error(B200_ERR_STATE, "mul_bf16x3: no handle created on this device");
 
     UmmaArgs p;
+    int rc = encode_b_map(&p.tmap, b, ldb, ncol, h->k, h->nt);
+    if (rc) return rc;
     p.aimg = h->aimg; p.b = b; p.c = c; p.ldb = ldb; p.ldc = ldc; p.ncol = ncol;
     p.m = h->m; p.k = h->k; p.kpad = h->kpad; p.mt = h->mt; p.s32 = h->s32;
     p.alpha = alpha; p.beta = beta; p.epi = beta != 0.0f; p.err = err;
