@@ -107,6 +107,8 @@ class TensorMulKernels:
         _check_shapes(a, b, out)
         if b.leaddim % 4 or out.leaddim % 4 or b.ncol % 4:
             raise NotSuitableError('unaligned operands')
+        if beta not in (0.0, 1.0):
+            raise NotSuitableError('the tensor-core epilogue stores or adds')
 
         h, smem, host = self._handle(a)
         ncol, ldb, ldc = b.ncol, b.leaddim, out.leaddim

@@ -54,8 +54,11 @@ struct Layout {
     uint32_t b32, b32_stride;     // FP32 staging stage s at b32 + s*b32_stride
     uint32_t b16, b16_stride;     // BF16 stage s: hi at b16 + s*b16_stride, lo after hi
     uint32_t b16_half;            // bytes of one (hi or lo) BF16 tile
+    uint32_t epi;                 // 4 warps x (32 rows x 128 B), 1024-aligned, swizzled
     uint32_t bar, tslot, abort_flag, total;
 };
+
+constexpr uint32_t EPI_WARP_BYTES = 32 * 128;
 
 __host__ __device__ inline Layout make_layout(int mpad, int kpad, int k, int nt, int s32) {
     Layout L;
@@ -67,6 +70,8 @@ __host__ __device__ inline Layout make_layout(int mpad, int kpad, int k, int nt,
     L.a_lo = off; off += abytes;
     L.b32 = off; L.b32_stride = b32bytes; off += s32 * b32bytes;
     L.b16 = off; L.b16_stride = 2 * b16bytes; L.b16_half = b16bytes; off += 2 * 2 * b16bytes;
+    off = (off + 1023) & ~1023u;
+    L.epi = off; off += 4 * EPI_WARP_BYTES;
     L.bar = off; off += 24 * 8;
     L.tslot = off; off += 8;
     L.abort_flag = off; off += 8;
@@ -160,8 +165,24 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map
                  :: "r"(dst), "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar) : "memory");
 }
 
+// Store (or add, for beta = 1) a 32x32 FP32 tile from 128-byte-swizzled
+// shared memory into out through the tensor map of out
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, uint32_t src, int x, int y,
+                                             int add) {
+    if (add)
+        asm volatile("cp.reduce.async.bulk.tensor.2d.global.shared::cta.add.tile.bulk_group"
+                     " [%0, {%1, %2}], [%3];"
+                     :: "l"((uint64_t)map), "r"(x), "r"(y), "r"(src) : "memory");
+    else
+        asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.tile.bulk_group"
+                     " [%0, {%1, %2}], [%3];"
+                     :: "l"((uint64_t)map), "r"(x), "r"(y), "r"(src) : "memory");
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+
 struct UmmaArgs {
     CUtensorMap tmap;           // B as a (k x ncol) FP32 tensor, box NT x k
+    CUtensorMap cmap;           // out as a (m x ncol) FP32 tensor, box 32 x 32, 128B swizzle
     const unsigned char *aimg;
     const float *b;
     float *c;
@@ -318,8 +339,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
         }
         __syncwarp();
     } else {
-        // ---- epilogue: TMEM -> registers -> out ----
-        const int row_in_tile = warp * 32 + lane;
+        // ---- epilogue: TMEM -> registers -> shared memory -> TMA store ----
         int i = 0;
         for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
             const int bsel = i & 1;
@@ -327,20 +347,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
             asm volatile("tcgen05.fence::after_thread_sync;");
             const int64_t col0 = t * NT;
             for (int q = 0; q < mt; q++) {
-                const int row = q * MTILE + row_in_tile;
-                const bool rowok = row < p.m;
-                float *crow = p.c + (int64_t)row * p.ldc + col0;
-                // 32 columns per round: the C reads (beta != 0) and the TMEM
-                // read are all in flight before the single wait
+                // 32x32 sub-tiles: TMEM -> registers -> swizzled shared
+                // memory -> one TMA store (or reduce-add) per warp; rows
+                // beyond m and columns beyond ncol are clipped by the TMA
                 for (int cc = 0; cc < NT; cc += 32) {
-                    const int64_t left = p.ncol - (col0 + cc);     // multiple of 4
-                    const int nq = !rowok || left <= 0 ? 0 : (left >= 32 ? 8 : (int)(left / 4));
-                    float4 cv[8];
-                    if (p.epi) {
-#pragma unroll
-                        for (int j = 0; j < 8; j++)
-                            if (j < nq) cv[j] = reinterpret_cast<const float4 *>(crow + cc)[j];
-                    }
+                    if (col0 + cc >= p.ncol) break;
                     uint32_t v[32];
                     const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) +
                                            (uint32_t)(bsel * mt + q) * NT + cc;
@@ -356,26 +367,33 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
                           "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
                         : "r"(taddr));
                     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                    float4 *dst = reinterpret_cast<float4 *>(crow + cc);
+
+                    // The previous store from this warp's buffer must have
+                    // finished reading it
+                    if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+                    __syncwarp();
+                    unsigned char *buf = smem + L.epi + warp * EPI_WARP_BYTES;
 #pragma unroll
                     for (int j = 0; j < 8; j++) {
-                        if (j < nq) {
-                            float4 o = make_float4(p.alpha * __uint_as_float(v[4 * j]),
-                                                   p.alpha * __uint_as_float(v[4 * j + 1]),
-                                                   p.alpha * __uint_as_float(v[4 * j + 2]),
-                                                   p.alpha * __uint_as_float(v[4 * j + 3]));
-                            if (p.epi) {
-                                o.x += p.beta * cv[j].x; o.y += p.beta * cv[j].y;
-                                o.z += p.beta * cv[j].z; o.w += p.beta * cv[j].w;
-                            }
-                            dst[j] = o;
-                        }
+                        const float4 o = make_float4(p.alpha * __uint_as_float(v[4 * j]),
+                                                     p.alpha * __uint_as_float(v[4 * j + 1]),
+                                                     p.alpha * __uint_as_float(v[4 * j + 2]),
+                                                     p.alpha * __uint_as_float(v[4 * j + 3]));
+                        *reinterpret_cast<float4 *>(buf + lane * 128 + ((j ^ (lane & 7)) * 16)) = o;
                     }
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    __syncwarp();
+                    if (lane == 0 && q * MTILE + warp * 32 < p.m)
+                        tma_store_2d(&p.cmap, sbase + L.epi + warp * EPI_WARP_BYTES,
+                                     (int)(col0 + cc), q * MTILE + warp * 32, p.epi);
                 }
             }
             asm volatile("tcgen05.fence::before_thread_sync;");
             bar_arrive(bar(BAR_ACCEMPTY + bsel));
         }
+        // Every store issued by this warp has completed before exit
+        if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+        __syncwarp();
     }
 
     asm volatile("tcgen05.fence::before_thread_sync;");
@@ -419,6 +437,23 @@ int encode_b_map(CUtensorMap *map, const float *b, int64_t ldb, int64_t ncol, in
                                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS)
         return b200::set_error(B200_ERR_CUDA, "mul_bf16x3: cuTensorMapEncodeTiled failed (%d)",
+                               (int)r);
+    return B200_OK;
+}
+
+// Tensor map of out: dims (ncol, m), row stride ldc*4 bytes, box 32 x 32
+// with the 128-byte swizzle the epilogue writes its staging tiles in
+int encode_c_map(CUtensorMap *map, float *c, int64_t ldc, int64_t ncol, int m) {
+    cuuint64_t gdim[2] = {(cuuint64_t)ncol, (cuuint64_t)m};
+    cuuint64_t gstride[1] = {(cuuint64_t)ldc * 4};
+    cuuint32_t box[2] = {32, 32};
+    cuuint32_t estride[2] = {1, 1};
+    CUresult r = g_encode_tiled(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)c, gdim, gstride,
+                                box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS)
+        return b200::set_error(B200_ERR_CUDA, "mul_bf16x3: cuTensorMapEncodeTiled (out) failed (%d)",
                                (int)r);
     return B200_OK;
 }
@@ -530,8 +565,12 @@ int b200_mul_bf16x3(void *handle, const float *b, int64_t ldb, float *c, int64_t
     if (!g_sm_count)
         return b200::set_error(B200_ERR_STATE, "mul_bf16x3: no handle created on this device");
 
+    // The epilogue stores (beta = 0) or adds (beta = 1) through the TMA
+    if (beta != 0.0f && beta != 1.0f)
+        return b200::set_error(B200_ERR_UNSUPPORTED, "mul_bf16x3: beta must be 0 or 1");
     UmmaArgs p;
     int rc = encode_b_map(&p.tmap, b, ldb, ncol, h->k, h->nt);
+    if (!rc) rc = encode_c_map(&p.cmap, c, ldc, ncol, h->m);
     if (rc) return rc;
     p.aimg = h->aimg; p.b = b; p.c = c; p.ldb = ldb; p.ldc = ldc; p.ncol = ncol;
     p.m = h->m; p.k = h->k; p.kpad = h->kpad; p.mt = h->mt; p.s32 = h->s32;

@@ -45,10 +45,11 @@ def test_mul_bf16x3_tensor_cores(built, golden, key, opname):
         C = be.matrix(c0.shape, c0, tags={'align'})
         be.commit()
         bound = 1e-4*np.einsum('mk,kve->mve', np.abs(a), np.abs(b)) + 1e-6
-        for alpha, beta in [(1.0, 0.0), (1.0, 1.0), (-0.5, 0.25)]:
+        for alpha, beta in [(1.0, 0.0), (1.0, 1.0), (-0.5, 1.0), (2.0, 0.25)]:
             C.set(c0)
             k = be.kernel('mul', A, B, out=C, alpha=alpha, beta=beta)
-            assert k.meta['impl'] == 'bf16x3'
+            # The tensor-core epilogue stores or adds; other beta fall back
+            assert k.meta['impl'] == ('bf16x3' if beta in (0.0, 1.0) else 'csr')
             be.run_kernels([k], wait=True)
             ref = alpha*np.einsum('mk,kve->mve', a, b.astype(np.float32)) + \
                 beta*c0.astype(np.float32)
