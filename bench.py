@@ -423,6 +423,10 @@ def main():
                     help='steps after which the chosen form is compared '
                          'with FP64')
     ap.add_argument('--ke-every', type=int, default=10)
+    ap.add_argument('--only', choices=['plain', 'chosen', 'fp32'],
+                    help='time one precision form alone (no accuracy '
+                         'history, end-to-end loop or CPU sample): the '
+                         'command to run under a profiler')
     args = ap.parse_args()
 
     world = int(os.environ.get('WORLD_SIZE', '1'))
@@ -457,6 +461,19 @@ def main():
                              'sample': sample},
             'e2e': {'value': v, 'unit': 'GDoF/s', 'h2d_bytes_per_step': 0,
                     'd2h_bytes_per_step': 0}}))
+        return
+
+    if args.only:
+        import __graft_entry__ as ge
+        ge.build_library()
+        intg = make_form(args.only, args)
+        r = measure(intg, args, Dist(world), e2e=False, profile=False)
+        if rank == 0:
+            print(json.dumps({
+                'form': args.only, 'n': args.n, 'steps': args.steps,
+                'ms_per_step': r['t_ms']/args.steps,
+                'gdofs': world*r['gndofs']*r['nstages']*args.steps /
+                (r['t_ms']*1e-3)/1e9}))
         return
 
     allres = run_gpu(args, Dist(world))

@@ -31,10 +31,14 @@ extern "C" {
  * Pr, cpTref, cpTs; viscosity-correction = sutherland when sutherland != 0);
  * pyfr/solvers/navstokes/kernels/flux.mako:48-105.
  * shifted != 0 (Navier-Stokes kernels, Rusanov only): the solution inputs
- * are perturbations du = u - u_ref from the constant state
- * (rho_ref, 0, p_ref/(gamma - 1)) and the constant momentum flux p_ref*I is
- * left out; the right-hand side is the same in exact arithmetic but its
- * low-precision rounding no longer scales with the mean pressure. */
+ * are q = T(u - u_ref), the perturbation from the constant state
+ * (rho_ref, 0, E_ref = p_ref/(gamma - 1)) with its energy component
+ * replaced by dE - h_ref*drho (h_ref = gamma/(gamma - 1) p_ref/rho_ref);
+ * the kernels compute the right-hand side of q, i.e. T times that of u
+ * (energy row minus h_ref times the mass row), with the constant fluxes
+ * p_ref*I and H_ref*v left out.  Exact in exact arithmetic; the
+ * low-precision rounding no longer scales with the mean pressure and
+ * enthalpy. */
 typedef struct {
     double gamma, mu, pr, cpTref, cpTs;
     int sutherland;
@@ -204,17 +208,16 @@ int b200_rkvdh2_f32(int64_t n, int stage, int nstages, int errest, double dt, do
                     void *stream);
 
 /* Mixed-precision form of the rkvdh2 stage (FP32 right-hand side, FP64
- * solution accumulator): acc <- acc + dt*b*rhs and u32 <- next stage's
- * FP32 input (acc + dt*a*rhs, or the new acc at the last stage), minus the
- * per-variable reference state uref[nvars] (a host array; null or nvars = 0
- * for none) subtracted in FP64 before rounding; the embedded error
- * registers as in rkvdh2.  Replaces the rkvdh2 kernel
+ * solution accumulator): acc <- acc + dt*b*rhs in FP64 and u32 <- the next
+ * stage's FP32 input, fl32(acc) + fl32(dt*a)*rhs formed in FP32 (the new
+ * fl32(acc) at the last stage); the embedded error registers as in rkvdh2.
+ * A solution kept relative to a constant reference state (u - u_ref) is
+ * stored as that difference in acc.  Replaces the rkvdh2 kernel
  * (pyfr/integrators/explicit/kernels/rkvdh2.mako:4-31) for the chosen
  * precision form, whose second register is only ever an RHS input. */
 int b200_rkmixed_f64f32(int64_t n, int stage, int nstages, int errest, double dt, double a,
                         double b, double e, double *acc, const float *rhs, float *u32,
-                        double *rold, double *rerr, int nvars, const double *uref,
-                        void *stream);
+                        double *rold, double *rerr, void *stream);
 /* dst <- (float)(src - uref[v]) over n scalars of an AoSoA field with
  * nvars variables (uref null: no shift). */
 int b200_cast_f64_f32(int64_t n, const double *src, float *dst, int nvars, const double *uref,
@@ -236,6 +239,13 @@ int b200_axnpby_f32(int64_t n, int nv, float *x0, const float *const *xs, const 
 int b200_errest_f64(int nupts, int nvars, int64_t neles, int64_t ld, const double *curr,
                     const double *err, const double *atol_dev, double rtol, int uniform,
                     double *scratch, int nscratch, double *out, void *stream);
+/* Same for a solution stored relative to a reference state: curr holds q
+ * with u_v = uref[v] + q_v, plus hcoef*q_0 for the last variable (uref:
+ * nvars host doubles), and the norm uses |u|. */
+int b200_errest_shifted_f64(int nupts, int nvars, int64_t neles, int64_t ld, const double *curr,
+                            const double *err, const double *atol_dev, double rtol, int uniform,
+                            const double *uref, double hcoef, double *scratch, int nscratch,
+                            double *out, void *stream);
 int b200_errest_f32(int nupts, int nvars, int64_t neles, int64_t ld, const float *curr,
                     const float *err, const double *atol_dev, double rtol, int uniform,
                     double *scratch, int nscratch, double *out, void *stream);
@@ -266,10 +276,13 @@ int b200_errest_static_f64(int nupts, int nvars, int64_t neles, int64_t ld, cons
 int b200_integrals_f64(int ndims, int nupts, int64_t neles, const double *u, int64_t ldu,
                        const double *gradu, int64_t ldg, const double *wts, int64_t ldw,
                        double *scratch, int nscratch, double *out, void *stream);
-/* Same with FP32 gradients (the chosen precision form). */
+/* Same with FP32 gradients (the chosen precision form); density and
+ * momentum are u_v + uref[v] (uref: ndims + 2 host doubles, or null) for a
+ * solution kept relative to a reference state (the energy is not used). */
 int b200_integrals_f64f32(int ndims, int nupts, int64_t neles, const double *u, int64_t ldu,
                           const float *gradu, int64_t ldg, const double *wts, int64_t ldw,
-                          double *scratch, int nscratch, double *out, void *stream);
+                          const double *uref, double *scratch, int nscratch, double *out,
+                          void *stream);
 
 #ifdef __cplusplus
 }

@@ -12,7 +12,9 @@ library or the GPU is missing, construction raises.
 from collections import namedtuple
 from contextlib import contextmanager
 import ctypes as C
+import gc
 import itertools as it
+import weakref
 from weakref import WeakValueDictionary
 
 import numpy as np
@@ -20,6 +22,30 @@ import numpy as np
 from pyfr_gb300.backend import types
 from pyfr_gb300.backend.lib import get_lib, B200Error
 
+
+# Releases of device resources (graph executables, allocations, operator
+# handles) requested while a stream capture was open: the runtime would
+# invalidate the capture, and the finaliser of any backend's objects may
+# run then.  Process-wide, run when the outermost capture ends.
+_CAPTURE_DEPTH = 0
+_DEFERRED = []
+
+
+def release(fn, *args):
+    """Call ``fn(*args)`` now, or once no stream capture is open."""
+    if _CAPTURE_DEPTH:
+        _DEFERRED.append((fn, args))
+    else:
+        fn(*args)
+
+
+def _free_allocs(lib, allocs):
+    for p, _ in allocs:
+        try:
+            lib.free(p)
+        except B200Error:
+            pass
+    allocs.clear()
 
 MemoryInfo = namedtuple('MemoryInfo', ['current', 'peak', 'free', 'total'])
 
@@ -98,6 +124,9 @@ class B200Backend:
         s = C.c_void_p()
         lib.stream_create(C.byref(s))
         self._stream = s.value
+
+        # Device memory goes back when the backend is collected
+        weakref.finalize(self, release, _free_allocs, lib, self._allocs)
 
         self.const_matrix_cls = types.ConstMatrix
         self.matrix_cls = types.Matrix
@@ -192,25 +221,43 @@ class B200Backend:
         return MemoryInfo(self._mem_cur, self._mem_peak, f.value, t.value)
 
     def capture(self, launch, stream):
-        self.lib.graph_begin_capture(stream)
+        """Record ``launch(stream)`` into a CUDA graph and return its
+        executable.  While a capture is open no graph or memory may be
+        released (the runtime invalidates the capture), so the cyclic
+        garbage collector, whose finalisers release graphs, is paused and
+        releases requested meanwhile are deferred until the capture ends."""
+        global _CAPTURE_DEPTH
+        gc_was_enabled = gc.isenabled()
+        gc.disable()
+        _CAPTURE_DEPTH += 1
         try:
-            launch(stream)
-        except BaseException:
-            g = C.c_void_p()
+            self.lib.graph_begin_capture(stream)
             try:
-                self.lib.graph_end_capture(stream, C.byref(g))
-            except B200Error:
-                pass
-            else:
-                self.lib.graph_destroy(g.value)
-            raise
-        g = C.c_void_p()
-        self.lib.graph_end_capture(stream, C.byref(g))
-        return g.value
+                launch(stream)
+            except BaseException:
+                g = C.c_void_p()
+                try:
+                    self.lib.graph_end_capture(stream, C.byref(g))
+                except B200Error:
+                    pass
+                else:
+                    _DEFERRED.append((self.lib.graph_destroy, (g.value,)))
+                raise
+            g = C.c_void_p()
+            self.lib.graph_end_capture(stream, C.byref(g))
+            return g.value
+        finally:
+            _CAPTURE_DEPTH -= 1
+            if not _CAPTURE_DEPTH:
+                while _DEFERRED:
+                    fn, args = _DEFERRED.pop()
+                    fn(*args)
+            if gc_was_enabled:
+                gc.enable()
 
     def release_gexec(self, gexec):
         if gexec:
-            self.lib.graph_destroy(gexec)
+            release(self.lib.graph_destroy, gexec)
 
     # ---- allocation (pyfr/backends/base/backend.py:94-165) ----------------
 

@@ -76,9 +76,12 @@ class BlasExtKernels:
 
         return Kernel(run, mats=[m], name='zero')
 
-    def errest(self, curr, err, atols, norm='l2'):
+    def errest(self, curr, err, atols, norm='l2', uref=None, hcoef=0.0):
         """Error norm of the PI controller over one element type's
-        registers of io-shape (nupts, nvars, neles)."""
+        registers of io-shape (nupts, nvars, neles).  With ``uref`` (one
+        FP64 value per variable) the current solution is stored as q with
+        u_v = uref_v + q_v (plus hcoef*q_0 for the last variable), and the
+        norm scales with |u|."""
         be = self.backend
         nupts, nvars, neles = curr.ioshape
         if curr.traits != err.traits:
@@ -94,16 +97,31 @@ class BlasExtKernels:
         be.commit()
 
         host = np.zeros(1)
-        fn = be.lib.errest_f64 if curr.dtype == np.float64 else \
-            be.lib.errest_f32
         uniform = int(norm == 'uniform')
         ld, sp, nsc = curr.leaddim, self._scratch.data, self.MAX_ERREST_BLOCKS
         cp, ep, ap, op = curr.data, err.data, atol.data, out.data
+
+        if uref is not None:
+            if curr.dtype != np.float64:
+                raise ValueError('A shifted error norm needs FP64 registers')
+            uref = np.ascontiguousarray(uref, dtype=np.float64)
+            if uref.shape != (nvars,):
+                raise ValueError('uref needs one value per variable')
+            shifted, pu = be.lib.errest_shifted_f64, uref.ctypes.data
+
+            def fn(*a):
+                shifted(*a[:9], pu, hcoef, *a[9:])
+        elif curr.dtype == np.float64:
+            fn = be.lib.errest_f64
+        else:
+            fn = be.lib.errest_f32
 
         def run(stream, rtol):
             fn(nupts, nvars, neles, ld, cp, ep, ap, rtol, uniform, sp, nsc, op,
                stream)
             be.lib.memcpy_dtoh(host.ctypes.data, op, 8, stream)
 
-        return ErrestKernel(run, out, host, mats=[curr, err, atol, out],
-                            name='errest')
+        k = ErrestKernel(run, out, host, mats=[curr, err, atol, out],
+                         name='errest')
+        k._uref = uref
+        return k

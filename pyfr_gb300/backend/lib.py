@@ -78,12 +78,14 @@ _SIGS = {
     'b200_mul_nnz': [vp, C.POINTER(i32)],
     'b200_mul_destroy': [vp],
     'b200_rkmixed_f64f32': [i64, i32, i32, i32, f64, f64, f64, f64, vp, vp,
-                            vp, vp, vp, i32, vp, vp],
+                            vp, vp, vp, vp],
     'b200_cast_f64_f32': [i64, vp, vp, i32, vp, vp],
     'b200_integrals_f64': [i32, i32, i64, vp, i64, vp, i64, vp, i64, vp, i32,
                            vp, vp],
     'b200_integrals_f64f32': [i32, i32, i64, vp, i64, vp, i64, vp, i64, vp,
-                              i32, vp, vp],
+                              vp, i32, vp, vp],
+    'b200_errest_shifted_f64': [i32, i32, i64, i64, vp, vp, vp, f64, i32, vp,
+                                f64, vp, i32, vp, vp],
     'b200_errest_static_f64': [i32, i32, i64, i64, vp, vp, vp, f64, i32, i32,
                                vp, vp],
     'b200_mul_bf16x3_create': [pd, i32, i32, C.POINTER(vp), C.POINTER(sz)],

@@ -17,6 +17,7 @@ kernel that applies it.
 """
 
 import ctypes as C
+import weakref
 
 import numpy as np
 
@@ -31,10 +32,20 @@ def _check_shapes(a, b, out):
         raise ValueError('The operator of mul must be a constant matrix')
 
 
+def _destroy_handles(destroy, handles):
+    for h in handles.values():
+        if h is not None:
+            destroy(h[0])
+    handles.clear()
+
+
 class MulKernels:
     def __init__(self, backend):
+        from pyfr_gb300.backend.base import release
         self.backend = backend
         self._handles = {}
+        weakref.finalize(self, release, _destroy_handles,
+                         backend.lib.mul_destroy, self._handles)
 
     def _handle(self, a):
         key = a.mid
@@ -75,8 +86,11 @@ class MulKernels:
 
 class TensorMulKernels:
     def __init__(self, backend):
+        from pyfr_gb300.backend.base import release
         self.backend = backend
         self._handles = {}
+        weakref.finalize(self, release, _destroy_handles,
+                         backend.lib.mul_bf16x3_destroy, self._handles)
 
     def _handle(self, a):
         from pyfr_gb300.backend.base import NotSuitableError

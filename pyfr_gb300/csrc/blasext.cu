@@ -51,14 +51,69 @@ rkvdh2_kernel(int64_t n, int last, int errest, int first, T dta, T dtb, T dte,
 // solution is accumulated in FP64.  In the two-register scheme the
 // second register only carries the next stage's RHS input, so here it is
 // written directly as the FP32 input of the next RHS evaluation:
-//   next input = acc + dt*a*R   (FP32),   acc <- acc + dt*b*R   (FP64)
-// and at the last stage the input of the next step is the new acc.
+//   acc <- acc + dt*b*R                      (FP64, one FMA per value)
+//   u32 <- fl32(acc) + fl32(dt*a)*R          (FP32)
+// and at the last stage u32 <- fl32(new acc), the input of the next step.
+// The RHS input only needs FP32 accuracy: forming it in FP32 from the
+// rounded accumulator costs at most 1.5 ulp where rounding the FP64 sum
+// would cost 0.5, and leaves the narrow FP64 unit one FMA per value (the
+// conversions run on the integer pipes).  A caller that keeps the solution
+// relative to a constant reference state stores u - u_ref in acc; the
+// stage is the same.
+template <bool ERR>
+__device__ __forceinline__ float rkmixed_value(int64_t i, double &t, float rf, int last,
+                                               int first, float dta, double dtb, double dte,
+                                               double *__restrict__ rold,
+                                               double *__restrict__ rerr) {
+    const double r = b200::widen_f32(rf);
+    if (ERR) {
+        if (first) {
+            rerr[i] = dte * r;
+            rold[i] = t;
+        } else {
+            rerr[i] = rerr[i] + dte * r;
+        }
+    }
+    const float t32 = b200::narrow_f64(t);
+    t = fma(dtb, r, t);
+    return last ? b200::narrow_f64(t) : fmaf(dta, rf, t32);
+}
+
+// Four values per thread and iteration (two 16-byte FP64 loads and one
+// 16-byte FP32 load in flight) over the first n4 quads, scalar after.
+template <bool ERR>
+__global__ void __launch_bounds__(BX_BLOCK)
+rkmixed_kernel(int64_t n, int64_t n4, int last, int first, float dta, double dtb, double dte,
+               double *__restrict__ acc, const float *__restrict__ rhs, float *__restrict__ u32,
+               double *__restrict__ rold, double *__restrict__ rerr) {
+    const int64_t stride = (int64_t)gridDim.x * BX_BLOCK;
+    const int64_t tid = (int64_t)blockIdx.x * BX_BLOCK + threadIdx.x;
+    double2 *acc2 = reinterpret_cast<double2 *>(acc);
+    for (int64_t q = tid; q < n4; q += stride) {
+        double2 a01 = acc2[2 * q], a23 = acc2[2 * q + 1];
+        const float4 r = reinterpret_cast<const float4 *>(rhs)[q];
+        float4 o;
+        o.x = rkmixed_value<ERR>(4 * q + 0, a01.x, r.x, last, first, dta, dtb, dte, rold, rerr);
+        o.y = rkmixed_value<ERR>(4 * q + 1, a01.y, r.y, last, first, dta, dtb, dte, rold, rerr);
+        o.z = rkmixed_value<ERR>(4 * q + 2, a23.x, r.z, last, first, dta, dtb, dte, rold, rerr);
+        o.w = rkmixed_value<ERR>(4 * q + 3, a23.y, r.w, last, first, dta, dtb, dte, rold, rerr);
+        acc2[2 * q] = a01;
+        acc2[2 * q + 1] = a23;
+        reinterpret_cast<float4 *>(u32)[q] = o;
+    }
+    for (int64_t i = 4 * n4 + tid; i < n; i += stride) {
+        double t = acc[i];
+        u32[i] = rkmixed_value<ERR>(i, t, rhs[i], last, first, dta, dtb, dte, rold, rerr);
+        acc[i] = t;
+    }
+}
+
 // Constant per-variable offset subtracted (in FP64) before the FP32
-// rounding of the RHS input: the input of the next RHS is u - u_ref.
-// Variable v of an AoSoA field sits at flat index i with
-// v = (i mod (32*nvars)) / 32.
+// rounding: dst = fl32(src - u_ref).  Variable v of an AoSoA field sits
+// at flat index i with v = (i mod (32*nvars)) / 32.
 struct RefState {
     double v[8];
+    double hcoef;       // u_last = v[last] + q_last + hcoef*q_0 (errest)
     int nvars;
 };
 
@@ -67,32 +122,11 @@ __device__ __forceinline__ double ref_of(const RefState &r, int64_t i) {
 }
 
 __global__ void __launch_bounds__(BX_BLOCK)
-rkmixed_kernel(int64_t n, int last, int errest, int first, double dta, double dtb, double dte,
-               double *__restrict__ acc, const float *__restrict__ rhs, float *__restrict__ u32,
-               double *__restrict__ rold, double *__restrict__ rerr, RefState ref) {
-    for (int64_t i = (int64_t)blockIdx.x * BX_BLOCK + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * BX_BLOCK) {
-        const double t = acc[i], r = (double)rhs[i];
-        if (errest) {
-            if (first) {
-                rerr[i] = dte * r;
-                rold[i] = t;
-            } else {
-                rerr[i] = rerr[i] + dte * r;
-            }
-        }
-        const double nacc = t + dtb * r;
-        acc[i] = nacc;
-        u32[i] = (float)((last ? nacc : t + dta * r) - ref_of(ref, i));
-    }
-}
-
-__global__ void __launch_bounds__(BX_BLOCK)
 cast_f64_f32_kernel(int64_t n, const double *__restrict__ src, float *__restrict__ dst,
                     RefState ref) {
     for (int64_t i = (int64_t)blockIdx.x * BX_BLOCK + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * BX_BLOCK)
-        dst[i] = (float)(src[i] - ref_of(ref, i));
+        dst[i] = b200::narrow_f64(src[i] - ref_of(ref, i));
 }
 
 int make_ref(int nvars, const double *uref, RefState &r) {
@@ -133,7 +167,7 @@ template <typename T>
 __global__ void __launch_bounds__(BX_BLOCK)
 errest_partial_kernel(int nupts, int nvars, int64_t neles, int64_t ld, const T *__restrict__ curr,
                       const T *__restrict__ err, const double *__restrict__ atol, double rtol,
-                      int uniform, double *__restrict__ partial) {
+                      int uniform, RefState ref, double *__restrict__ partial) {
     __shared__ double red[BX_BLOCK / 32];
     const int64_t npts = (int64_t)nupts * neles;
     double acc = 0;
@@ -143,7 +177,13 @@ errest_partial_kernel(int nupts, int nvars, int64_t neles, int64_t ld, const T *
         const int64_t e = p % neles;
         for (int v = 0; v < nvars; v++) {
             const int64_t ix = upt * ld + b200::soa_off(e, v, nvars);
-            const double q = (double)err[ix] / (atol[v] + rtol * fabs((double)curr[ix]));
+            double c = (double)curr[ix];
+            if (ref.nvars) {
+                c += ref.v[v];
+                if (v == nvars - 1)
+                    c += ref.hcoef * (double)curr[upt * ld + b200::soa_off(e, 0, nvars)];
+            }
+            const double q = (double)err[ix] / (atol[v] + rtol * fabs(c));
             acc = uniform ? fmax(acc, fabs(q)) : acc + q * q;
         }
     }
@@ -208,12 +248,12 @@ int axnpby(int64_t n, int nv, T *x0, const T *const *xs, const double *a, cudaSt
 template <typename T>
 int errest(int nupts, int nvars, int64_t neles, int64_t ld, const T *curr, const T *err,
            const double *atol_dev, double rtol, int uniform, double *scratch, int nscratch,
-           double *out, cudaStream_t s) {
+           double *out, cudaStream_t s, const RefState &ref = RefState{}) {
     if (nscratch < 1) return b200::set_error(B200_ERR_ARG, "errest: no scratch");
     int64_t g = ((int64_t)nupts * neles + BX_BLOCK - 1) / BX_BLOCK;
     int nblk = (int)(g < 1 ? 1 : (g > nscratch ? nscratch : g));
     errest_partial_kernel<T><<<nblk, BX_BLOCK, 0, s>>>(nupts, nvars, neles, ld, curr, err,
-                                                       atol_dev, rtol, uniform, scratch);
+                                                       atol_dev, rtol, uniform, ref, scratch);
     B200_CHECK_LAUNCH("errest_partial");
     errest_final_kernel<<<1, 32, 0, s>>>(nblk, uniform, scratch, out);
     B200_CHECK_LAUNCH("errest_final");
@@ -306,20 +346,23 @@ int b200_rkvdh2_f32(int64_t n, int stage, int nstages, int errest, double dt, do
 
 int b200_rkmixed_f64f32(int64_t n, int stage, int nstages, int errest, double dt, double a,
                         double b, double e, double *acc, const float *rhs, float *u32,
-                        double *rold, double *rerr, int nvars, const double *uref,
-                        void *stream) {
+                        double *rold, double *rerr, void *stream) {
     if (n <= 0) return B200_OK;
     if (stage < 0 || stage >= nstages)
         return b200::set_error(B200_ERR_ARG, "rkmixed: stage %d out of range", stage);
     if (errest && (!rold || !rerr))
         return b200::set_error(B200_ERR_ARG, "rkmixed: error estimate needs rold and rerr");
-    RefState ref;
-    int rc = make_ref(nvars, uref, ref);
-    if (rc) return rc;
     const int last = stage == nstages - 1;
-    rkmixed_kernel<<<grid_for(n), BX_BLOCK, 0, (cudaStream_t)stream>>>(
-        n, last, errest, stage == 0, dt * (last ? 0.0 : a), dt * b, dt * e, acc, rhs, u32, rold,
-        rerr, ref);
+    const bool aligned = !(((uintptr_t)acc | (uintptr_t)rhs | (uintptr_t)u32) & 15);
+    const int64_t n4 = aligned ? n / 4 : 0;
+    const float dta = (float)(dt * (last ? 0.0 : a));
+    auto s = (cudaStream_t)stream;
+    if (errest)
+        rkmixed_kernel<true><<<grid_for(n / 4 + 1), BX_BLOCK, 0, s>>>(
+            n, n4, last, stage == 0, dta, dt * b, dt * e, acc, rhs, u32, rold, rerr);
+    else
+        rkmixed_kernel<false><<<grid_for(n / 4 + 1), BX_BLOCK, 0, s>>>(
+            n, n4, last, stage == 0, dta, dt * b, dt * e, acc, rhs, u32, rold, rerr);
     B200_CHECK_LAUNCH("rkmixed");
     return B200_OK;
 }
@@ -350,6 +393,18 @@ int b200_errest_f64(int nupts, int nvars, int64_t neles, int64_t ld, const doubl
                     double *scratch, int nscratch, double *out, void *stream) {
     return errest<double>(nupts, nvars, neles, ld, curr, err, atol_dev, rtol, uniform, scratch,
                           nscratch, out, (cudaStream_t)stream);
+}
+
+int b200_errest_shifted_f64(int nupts, int nvars, int64_t neles, int64_t ld, const double *curr,
+                            const double *err, const double *atol_dev, double rtol, int uniform,
+                            const double *uref, double hcoef, double *scratch, int nscratch,
+                            double *out, void *stream) {
+    RefState ref;
+    int rc = make_ref(nvars, uref, ref);
+    if (rc) return rc;
+    ref.hcoef = hcoef;
+    return errest<double>(nupts, nvars, neles, ld, curr, err, atol_dev, rtol, uniform, scratch,
+                          nscratch, out, (cudaStream_t)stream, ref);
 }
 
 int b200_errest_f32(int nupts, int nvars, int64_t neles, int64_t ld, const float *curr,

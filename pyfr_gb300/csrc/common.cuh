@@ -34,6 +34,41 @@ __device__ __forceinline__ int64_t load_ix(const void *map, int ix64, int64_t i)
 
 inline unsigned ceil_div(int64_t a, int64_t b) { return (unsigned)((a + b - 1) / b); }
 
+// FP32 <-> FP64 conversions on the integer pipes.  GB300's FP64 unit is
+// narrow (about 2 operations per clock per SM) and executes the hardware
+// conversions too, so a bandwidth-bound kernel that widens and narrows
+// every element is FP64-bound.  These build the result from the IEEE 754
+// binary32/binary64 encodings (1/8/23 and 1/11/52 bits, exponent biases 127
+// and 1023) for the normal range and for signed zeros, which is where
+// solution and RHS values live; subnormal, infinite and NaN operands take
+// the hardware conversion.  Both are exact in the sense of IEEE 754: the
+// widening is exact and the narrowing rounds to nearest, ties to even.
+__device__ __forceinline__ double widen_f32(float f) {
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t a = u & 0x7fffffffu;
+    const uint64_t s = (uint64_t)(u & 0x80000000u) << 32;
+    if (a - 0x00800000u < 0x7f000000u)  // biased exponent in [1, 254]
+        return __longlong_as_double((long long)(s | ((uint64_t)a << 29) +
+                                                         ((uint64_t)(1023 - 127) << 52)));
+    if (a == 0) return __longlong_as_double((long long)s);
+    return (double)f;
+}
+
+__device__ __forceinline__ float narrow_f64(double d) {
+    const uint64_t u = (uint64_t)__double_as_longlong(d);
+    const uint64_t a = u & 0x7fffffffffffffffull;
+    const uint32_t s = (uint32_t)(u >> 32) & 0x80000000u;
+    // Binary64 exponents 897..1150 are the binary32 normals 1..254
+    if (a - (897ull << 52) < (254ull << 52)) {
+        uint32_t r = (uint32_t)((a >> 29) - (896ull << 23));
+        const uint32_t rem = (uint32_t)a & 0x1fffffffu;
+        r += (uint32_t)(rem > 0x10000000u) | ((uint32_t)(rem == 0x10000000u) & r);
+        return __uint_as_float(s | r);
+    }
+    if (a == 0) return __uint_as_float(s);
+    return (float)d;
+}
+
 }  // namespace b200
 
 // Status codes of the C ABI

@@ -18,11 +18,17 @@ namespace {
 constexpr int IG_BLOCK = 256;
 constexpr int IG_NOUT = 3;
 
+// Constant per-variable offset added to the stored solution (a solution
+// kept relative to a reference state); zero when there is none.
+struct URef {
+    double v[5];
+};
+
 template <int ND, typename TU, typename TG>
 __global__ void __launch_bounds__(IG_BLOCK)
 integrals_partial_kernel(int nupts, int64_t neles, const TU *__restrict__ u, int64_t ldu,
                          const TG *__restrict__ g, int64_t ldg, const double *__restrict__ wts,
-                         int64_t ldw, double *__restrict__ partial) {
+                         int64_t ldw, URef uref, double *__restrict__ partial) {
     constexpr int NV = ND + 2;
     __shared__ double red[IG_NOUT][IG_BLOCK / 32];
     double acc[IG_NOUT] = {0, 0, 0};
@@ -36,7 +42,8 @@ integrals_partial_kernel(int nupts, int64_t neles, const TU *__restrict__ u, int
 
         double s[NV];
 #pragma unroll
-        for (int v = 0; v < NV; v++) s[v] = (double)u[upt * ldu + b200::soa_off(e, v, NV)];
+        for (int v = 0; v < NV; v++)
+            s[v] = (double)u[upt * ldu + b200::soa_off(e, v, NV)] + uref.v[v];
         const double rho = s[0], invrho = 1.0 / rho;
         double vel[ND], ke = 0;
 #pragma unroll
@@ -99,20 +106,23 @@ __global__ void integrals_final_kernel(int nblk, const double *__restrict__ part
 
 template <typename TU, typename TG>
 int integrals(int ndims, int nupts, int64_t neles, const TU *u, int64_t ldu, const TG *g,
-              int64_t ldg, const double *wts, int64_t ldw, double *scratch, int nscratch,
-              double *out, cudaStream_t s) {
+              int64_t ldg, const double *wts, int64_t ldw, const double *uref, double *scratch,
+              int nscratch, double *out, cudaStream_t s) {
     if (nscratch < 1) return b200::set_error(B200_ERR_ARG, "integrals: no scratch");
     if (!u || !g || !wts || !out)
         return b200::set_error(B200_ERR_ARG, "integrals: null argument");
     const int64_t npts = (int64_t)nupts * neles;
     int64_t want = (npts + IG_BLOCK - 1) / IG_BLOCK;
     int nblk = (int)(want < 1 ? 1 : (want > nscratch ? nscratch : want));
+    URef ur = {};
+    if (uref)
+        for (int v = 0; v < ndims + 2 && v < 5; v++) ur.v[v] = uref[v];
     if (ndims == 3)
         integrals_partial_kernel<3, TU, TG><<<nblk, IG_BLOCK, 0, s>>>(nupts, neles, u, ldu, g, ldg,
-                                                                      wts, ldw, scratch);
+                                                                      wts, ldw, ur, scratch);
     else if (ndims == 2)
         integrals_partial_kernel<2, TU, TG><<<nblk, IG_BLOCK, 0, s>>>(nupts, neles, u, ldu, g, ldg,
-                                                                      wts, ldw, scratch);
+                                                                      wts, ldw, ur, scratch);
     else
         return b200::set_error(B200_ERR_ARG, "integrals: ndims must be 2 or 3");
     B200_CHECK_LAUNCH("integrals_partial");
@@ -128,15 +138,16 @@ extern "C" {
 int b200_integrals_f64(int ndims, int nupts, int64_t neles, const double *u, int64_t ldu,
                        const double *gradu, int64_t ldg, const double *wts, int64_t ldw,
                        double *scratch, int nscratch, double *out, void *stream) {
-    return integrals<double, double>(ndims, nupts, neles, u, ldu, gradu, ldg, wts, ldw, scratch,
-                                     nscratch, out, (cudaStream_t)stream);
+    return integrals<double, double>(ndims, nupts, neles, u, ldu, gradu, ldg, wts, ldw, nullptr,
+                                     scratch, nscratch, out, (cudaStream_t)stream);
 }
 
 int b200_integrals_f64f32(int ndims, int nupts, int64_t neles, const double *u, int64_t ldu,
                           const float *gradu, int64_t ldg, const double *wts, int64_t ldw,
-                          double *scratch, int nscratch, double *out, void *stream) {
-    return integrals<double, float>(ndims, nupts, neles, u, ldu, gradu, ldg, wts, ldw, scratch,
-                                    nscratch, out, (cudaStream_t)stream);
+                          const double *uref, double *scratch, int nscratch, double *out,
+                          void *stream) {
+    return integrals<double, float>(ndims, nupts, neles, u, ldu, gradu, ldg, wts, ldw, uref,
+                                    scratch, nscratch, out, (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -1,24 +1,33 @@
 // Operator apply on the 5th-generation tensor cores, split-BF16 form:
-//     out = alpha * A @ B + beta * out        (FP32 in, FP32 out)
+//     out = alpha * A @ B + beta * out        (FP32 in, FP32 out, beta 0 or 1)
 // with A = Ahi + Alo and B = Bhi + Blo split into BF16 halves and the
 // product formed as Ahi*Bhi + Ahi*Blo + Alo*Bhi (three tcgen05.mma per K
 // step, FP32 accumulation in tensor memory).  This is the chosen-precision
 // replacement of the reference's `mul` providers
 // (pyfr/backends/cuda/gimmik.py:23-121, pyfr/backends/cuda/cublaslt.py:169-280).
 //
-// One persistent CTA per SM walks 64- (or, for long operators, 32-)
-// column tiles of B/out:
-//   warp 4 lane 0   bulk-copies (TMA engine, cp.async.bulk) each FP32 B
-//                   tile row by row into one of two staging buffers;
-//   warps 5-8       split the staged tile into BF16 hi/lo in the
-//                   canonical K-major no-swizzle UMMA layout (two stages);
+// Orientation: the streamed data is the M side of the MMA.  One
+// tcgen05.mma forms D[128 x N] += B^T[128 x 16] A^T[16 x N] for 128 columns
+// of B/out at once, N being the operator's rows rounded up to 32 (at most
+// 256).  Every operator row is then applied to a data tile with one read
+// of that tile from shared memory, and the accumulator holds one column of
+// out per TMEM lane with the operator rows along its columns.
+//
+// One persistent CTA per SM walks 128-column tiles of B/out, each in
+// chunks of 32 rows of B (K):
+//   warp 4 lane 0   loads each 32 x 128 FP32 chunk with one 2-D tensor TMA
+//                   into a ring of staging buffers;
+//   warps 5-8       split a staged chunk into BF16 hi/lo in the canonical
+//                   K-major no-swizzle UMMA layout (one column per thread);
 //   warp 9 lane 0   issues the MMAs into one of two TMEM accumulators;
-//   warps 0-3       read the accumulator (tcgen05.ld, one row per thread)
-//                   and write alpha*D + beta*out.
-// The operator halves are laid out on the host in the same canonical
-// layout and bulk-copied into shared memory once per CTA.  All hand-offs
-// are mbarriers; every wait is bounded and records an error code instead
-// of hanging.
+//   warps 0-3       read the accumulator (tcgen05.ld, one column of out per
+//                   thread, 32 operator rows per load), scale by alpha into
+//                   a 32 x 32 staging tile and write it with a TMA tensor
+//                   store (beta = 0) or reduce-add (beta = 1).
+// The operator halves are laid out on the host in the canonical layout
+// and bulk-copied into shared memory once per CTA.  All hand-offs are
+// mbarriers; every wait is bounded and records an error code instead of
+// hanging.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -31,18 +40,24 @@
 
 namespace {
 
-constexpr int MTILE = 128;        // UMMA M
+constexpr int TCOLS = 128;        // columns of B/out per tile (UMMA M)
+constexpr int KC = 32;            // rows of B per pipeline chunk
 constexpr int NTHREADS = 320;     // 10 warps
 constexpr int NCONV = 128;        // converter threads (warps 5-8)
 constexpr int NEPI = 128;         // epilogue threads (warps 0-3)
-constexpr int MAX_MT = 4;         // up to 512 operator rows (TMEM: 2*4*64 cols)
+constexpr int MAX_N = 256;        // UMMA N limit (operator rows, padded)
+constexpr int MAX_S32 = 8;        // FP32 chunk stages (bytes in flight)
+constexpr int MAX_S16 = 4;        // BF16 chunk stages
 constexpr long long WAIT_LIMIT = 1LL << 22;
 
-constexpr int MAX_S32 = 4;        // FP32 staging stages (bytes in flight)
+constexpr uint32_t CHUNK32 = KC * TCOLS * 4;       // 16 KB FP32 chunk
+constexpr uint32_t CHUNK16 = KC * TCOLS * 2;       // 8 KB per BF16 half
+constexpr uint32_t SBO_CHUNK = KC * 16;            // 8-row group stride of a chunk
+constexpr uint32_t EPI_BUF = 32 * 32 * 4;          // one 32 x 32 FP32 staging tile
 
 struct UmmaHandle {
-    int m, k, mpad, kpad, mt, nt, s32;
-    unsigned char *aimg;   // device: [hi | lo], each mpad x kpad bf16 canonical
+    int m, k, npad, kfull, s32, s16;
+    unsigned char *aimg;   // device: [hi | lo], each npad x kfull bf16 canonical
     size_t aimg_bytes;
     size_t smem_bytes;
 };
@@ -51,28 +66,23 @@ struct UmmaHandle {
 // runtime-indexed array here would live in local memory)
 struct Layout {
     uint32_t a_hi, a_lo;
-    uint32_t b32, b32_stride;     // FP32 staging stage s at b32 + s*b32_stride
-    uint32_t b16, b16_stride;     // BF16 stage s: hi at b16 + s*b16_stride, lo after hi
-    uint32_t b16_half;            // bytes of one (hi or lo) BF16 tile
-    uint32_t epi;                 // 4 warps x (32 rows x 128 B), 1024-aligned, swizzled
+    uint32_t b32;                 // FP32 stage s at b32 + s*CHUNK32
+    uint32_t b16;                 // BF16 stage s: hi at b16 + s*2*CHUNK16, lo after
+    uint32_t epi;                 // 4 warps x 2 staging tiles, 1024-aligned
     uint32_t bar, tslot, abort_flag, total;
 };
 
-constexpr uint32_t EPI_WARP_BYTES = 32 * 128;
-
-__host__ __device__ inline Layout make_layout(int mpad, int kpad, int k, int nt, int s32) {
+__host__ __device__ inline Layout make_layout(int npad, int kfull, int s32, int s16) {
     Layout L;
     uint32_t off = 0;
-    const uint32_t abytes = (uint32_t)mpad * kpad * 2;
-    const uint32_t b32bytes = ((uint32_t)k * nt * 4 + 127) & ~127u;
-    const uint32_t b16bytes = (uint32_t)nt * kpad * 2;
+    const uint32_t abytes = (uint32_t)npad * kfull * 2;
     L.a_hi = off; off += abytes;
     L.a_lo = off; off += abytes;
-    L.b32 = off; L.b32_stride = b32bytes; off += s32 * b32bytes;
-    L.b16 = off; L.b16_stride = 2 * b16bytes; L.b16_half = b16bytes; off += 2 * 2 * b16bytes;
     off = (off + 1023) & ~1023u;
-    L.epi = off; off += 4 * EPI_WARP_BYTES;
-    L.bar = off; off += 24 * 8;
+    L.b32 = off; off += s32 * CHUNK32;
+    L.b16 = off; off += s16 * 2 * CHUNK16;
+    L.epi = off; off += 8 * EPI_BUF;
+    L.bar = off; off += 32 * 8;
     L.tslot = off; off += 8;
     L.abort_flag = off; off += 8;
     L.total = off;
@@ -81,8 +91,9 @@ __host__ __device__ inline Layout make_layout(int mpad, int kpad, int k, int nt,
 
 // Barrier indices within the barrier block
 enum { BAR_A = 0, BAR_FULL32 = 1, BAR_EMPTY32 = 1 + MAX_S32, BAR_FULL16 = 1 + 2 * MAX_S32,
-       BAR_EMPTY16 = 3 + 2 * MAX_S32, BAR_ACCFULL = 5 + 2 * MAX_S32,
-       BAR_ACCEMPTY = 7 + 2 * MAX_S32, BAR_DRAIN = 9 + 2 * MAX_S32 };
+       BAR_EMPTY16 = 1 + 2 * MAX_S32 + MAX_S16, BAR_ACCFULL = 1 + 2 * MAX_S32 + 2 * MAX_S16,
+       BAR_ACCEMPTY = 3 + 2 * MAX_S32 + 2 * MAX_S16, BAR_DRAIN = 5 + 2 * MAX_S32 + 2 * MAX_S16 };
+static_assert(BAR_DRAIN < 32, "barrier block holds 32 slots");
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -156,8 +167,8 @@ __device__ __forceinline__ void umma_commit(uint32_t bar) {
                  :: "r"(bar) : "memory");
 }
 
-// One 2-D TMA load of a k-row x NT-column box of B into the dense FP32
-// staging buffer (columns past ncol are zero-filled by the hardware)
+// One 2-D TMA load of a KC-row x TCOLS-column box of B into a dense FP32
+// staging buffer (rows past k and columns past ncol are zero-filled)
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y,
                                             uint32_t bar) {
     asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
@@ -165,7 +176,7 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map
                  :: "r"(dst), "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar) : "memory");
 }
 
-// Store (or add, for beta = 1) a 32x32 FP32 tile from 128-byte-swizzled
+// Store (or add, for beta = 1) a 32 x 32 FP32 tile from dense row-major
 // shared memory into out through the tensor map of out
 __device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, uint32_t src, int x, int y,
                                              int add) {
@@ -181,23 +192,20 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, uint32_t sr
 }
 
 struct UmmaArgs {
-    CUtensorMap tmap;           // B as a (k x ncol) FP32 tensor, box NT x k
-    CUtensorMap cmap;           // out as a (m x ncol) FP32 tensor, box 32 x 32, 128B swizzle
+    CUtensorMap tmap;           // B as a (k x ncol) FP32 tensor, box TCOLS x KC
+    CUtensorMap cmap;           // out as a (m x ncol) FP32 tensor, box 32 x 32
     const unsigned char *aimg;
-    const float *b;
-    float *c;
-    int64_t ldb, ldc, ncol;
-    int m, k, kpad, mt, s32;
-    float alpha, beta;
-    int epi;            // 0: alpha*D, 1: alpha*D + beta*C
+    int64_t ncol;
+    int m, npad, kfull, s32, s16;
+    float alpha;
+    int epi;            // 0: store alpha*D, 1: add alpha*D to out
     int *err;
 };
 
-template <int NT>
 __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_constant__ UmmaArgs p) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    const Layout L = make_layout(p.mt * MTILE, p.kpad, p.k, NT, p.s32);
-    const int S32 = p.s32;
+    const Layout L = make_layout(p.npad, p.kfull, p.s32, p.s16);
+    const int S32 = p.s32, S16 = p.s16;
     const uint32_t sbase = smem_addr(smem);
     const uint32_t bar0 = sbase + L.bar;
     auto bar = [&](int i) { return bar0 + 8u * i; };
@@ -205,10 +213,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
     uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + L.tslot);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int64_t ntiles = (p.ncol + NT - 1) / NT;
-    const int mt = p.mt;
-    const uint32_t tcols = 2 * mt * NT <= 32 ? 32 : (2 * mt * NT <= 64 ? 64 :
-                          (2 * mt * NT <= 128 ? 128 : (2 * mt * NT <= 256 ? 256 : 512)));
+    const int64_t ntiles = (p.ncol + TCOLS - 1) / TCOLS;
+    const int npad = p.npad, nch = p.kfull / KC;
+    const uint32_t tcols = 2 * npad <= 32 ? 32 : (2 * npad <= 64 ? 64 :
+                          (2 * npad <= 128 ? 128 : (2 * npad <= 256 ? 256 : 512)));
 
     if (tid == 0) {
         *abort_flag = 0;
@@ -217,9 +225,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
             bar_init(bar(BAR_FULL32 + s), 1);
             bar_init(bar(BAR_EMPTY32 + s), NCONV);
         }
-        for (int s = 0; s < 2; s++) {
+        for (int s = 0; s < S16; s++) {
             bar_init(bar(BAR_FULL16 + s), NCONV);
             bar_init(bar(BAR_EMPTY16 + s), 1);
+        }
+        for (int s = 0; s < 2; s++) {
             bar_init(bar(BAR_ACCFULL + s), 1);
             bar_init(bar(BAR_ACCEMPTY + s), NEPI);
         }
@@ -236,12 +246,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = *tslot;
 
-    const uint32_t abytes = (uint32_t)(mt * MTILE) * p.kpad * 2;
-    const uint32_t SBO = (uint32_t)p.kpad * 16, LBO = 128;
+    const uint32_t abytes = (uint32_t)npad * p.kfull * 2;
+    const uint32_t SBO_OP = (uint32_t)p.kfull * 16, LBO = 128;
 
     if (warp == 4) {
-        // ---- producer: operator image once, then the FP32 B tiles ----
-        // (every lane issues a share of the row copies of a tile)
+        // ---- producer: operator image once, then the FP32 chunks of B ----
         if (lane == 0) bar_arrive_tx(bar(BAR_A), 2 * abytes);
         __syncwarp();
         {
@@ -252,85 +261,108 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
                 bulk_g2s(sbase + L.a_hi + a0, p.aimg + a0, nb, bar(BAR_A));
             }
         }
-        int i = 0;
-        for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
-            const int s = i % S32, ph = (i / S32) & 1;
-            if (i >= S32 && !bar_wait(bar(BAR_EMPTY32 + s), ph ^ 1, abort_flag, p.err, 1))
-                break;
-            const uint32_t dst = sbase + L.b32 + (uint32_t)s * L.b32_stride;
-            if (lane == 0) {
-                bar_arrive_tx(bar(BAR_FULL32 + s), (uint32_t)p.k * NT * 4);
-                tma_load_2d(dst, &p.tmap, (int)(t * NT), 0, bar(BAR_FULL32 + s));
-            }
-            __syncwarp();
-        }
-    } else if (warp >= 5 && warp <= 8) {
-        // ---- converters: FP32 stage -> BF16 hi/lo canonical K-major ----
-        const int ct = tid - 5 * 32;
-        const int n = ct % NT;
-        int i = 0;
-        for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
-            const int s = i % S32, s2 = i & 1;
-            if (!bar_wait(bar(BAR_FULL32 + s), (i / S32) & 1, abort_flag, p.err, 2)) break;
-            if (i >= 2 && !bar_wait(bar(BAR_EMPTY16 + s2), ((i >> 1) + 1) & 1, abort_flag, p.err, 3))
-                break;
-            const float *b32 = reinterpret_cast<const float *>(smem + L.b32 + s * L.b32_stride);
-            unsigned char *bhi = smem + L.b16 + s2 * L.b16_stride;
-            unsigned char *blo = bhi + L.b16_half;
-            for (int k8 = ct / NT; k8 < p.kpad / 8; k8 += NCONV / NT) {
-                uint32_t hw[4], lw[4];
-#pragma unroll
-                for (int j = 0; j < 8; j += 2) {
-                    const int r0 = k8 * 8 + j;
-                    const float x0 = r0 < p.k ? b32[r0 * NT + n] : 0.f;
-                    const float x1 = r0 + 1 < p.k ? b32[(r0 + 1) * NT + n] : 0.f;
-                    const __nv_bfloat16 h0 = __float2bfloat16_rn(x0);
-                    const __nv_bfloat16 h1 = __float2bfloat16_rn(x1);
-                    const __nv_bfloat16 l0 = __float2bfloat16_rn(x0 - __bfloat162float(h0));
-                    const __nv_bfloat16 l1 = __float2bfloat16_rn(x1 - __bfloat162float(h1));
-                    hw[j / 2] = (uint32_t)__bfloat16_as_ushort(h0) |
-                                ((uint32_t)__bfloat16_as_ushort(h1) << 16);
-                    lw[j / 2] = (uint32_t)__bfloat16_as_ushort(l0) |
-                                ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+        if (lane == 0) {
+            int64_t j = 0;
+            for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+                bool ok = true;
+                for (int c = 0; c < nch; c++, j++) {
+                    const int s = (int)(j % S32);
+                    if (j >= S32 &&
+                        !bar_wait(bar(BAR_EMPTY32 + s), (uint32_t)((j / S32) & 1) ^ 1, abort_flag,
+                                  p.err, 1)) {
+                        ok = false;
+                        break;
+                    }
+                    bar_arrive_tx(bar(BAR_FULL32 + s), CHUNK32);
+                    tma_load_2d(sbase + L.b32 + (uint32_t)s * CHUNK32, &p.tmap, (int)(t * TCOLS),
+                                c * KC, bar(BAR_FULL32 + s));
                 }
-                const uint32_t off = (uint32_t)(n / 8) * SBO + (uint32_t)k8 * LBO + (n % 8) * 16;
-                *reinterpret_cast<uint4 *>(bhi + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-                *reinterpret_cast<uint4 *>(blo + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+                if (!ok) break;
             }
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            bar_arrive(bar(BAR_EMPTY32 + s));
-            bar_arrive(bar(BAR_FULL16 + s2));
+        }
+        __syncwarp();
+    } else if (warp >= 5 && warp <= 8) {
+        // ---- converters: FP32 chunk -> BF16 hi/lo canonical K-major ----
+        // thread ct owns column ct of the tile
+        const int ct = tid - 5 * 32;
+        const uint32_t coff = (uint32_t)(ct / 8) * SBO_CHUNK + (uint32_t)(ct % 8) * 16;
+        int64_t j = 0;
+        bool ok = true;
+        for (int64_t t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
+            for (int c = 0; c < nch; c++, j++) {
+                const int s = (int)(j % S32), s2 = (int)(j % S16);
+                if (!bar_wait(bar(BAR_FULL32 + s), (uint32_t)((j / S32) & 1), abort_flag, p.err, 2) ||
+                    (j >= S16 && !bar_wait(bar(BAR_EMPTY16 + s2), (uint32_t)((j / S16) & 1) ^ 1,
+                                           abort_flag, p.err, 3))) {
+                    ok = false;
+                    break;
+                }
+                const float *b32 = reinterpret_cast<const float *>(smem + L.b32 + s * CHUNK32);
+                unsigned char *bhi = smem + L.b16 + s2 * 2 * CHUNK16;
+                unsigned char *blo = bhi + CHUNK16;
+#pragma unroll
+                for (int k8 = 0; k8 < KC / 8; k8++) {
+                    uint32_t hw[4], lw[4];
+#pragma unroll
+                    for (int jj = 0; jj < 8; jj += 2) {
+                        const float x0 = b32[(k8 * 8 + jj) * TCOLS + ct];
+                        const float x1 = b32[(k8 * 8 + jj + 1) * TCOLS + ct];
+                        const __nv_bfloat16 h0 = __float2bfloat16_rn(x0);
+                        const __nv_bfloat16 h1 = __float2bfloat16_rn(x1);
+                        const __nv_bfloat16 l0 = __float2bfloat16_rn(x0 - __bfloat162float(h0));
+                        const __nv_bfloat16 l1 = __float2bfloat16_rn(x1 - __bfloat162float(h1));
+                        hw[jj / 2] = (uint32_t)__bfloat16_as_ushort(h0) |
+                                     ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+                        lw[jj / 2] = (uint32_t)__bfloat16_as_ushort(l0) |
+                                     ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+                    }
+                    const uint32_t off = coff + (uint32_t)k8 * LBO;
+                    *reinterpret_cast<uint4 *>(bhi + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+                    *reinterpret_cast<uint4 *>(blo + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+                }
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                bar_arrive(bar(BAR_EMPTY32 + s));
+                bar_arrive(bar(BAR_FULL16 + s2));
+            }
         }
     } else if (warp == 9) {
         // ---- MMA issuer ----
         if (lane == 0) {
-            const uint32_t idesc = idesc_bf16(MTILE, NT);
+            const uint32_t idesc = idesc_bf16(TCOLS, npad);
             bool ok = bar_wait(bar(BAR_A), 0, abort_flag, p.err, 4);
+            int64_t j = 0;
             int i = 0;
             for (int64_t t = blockIdx.x; ok && t < ntiles; t += gridDim.x, i++) {
-                const int s = i & 1, bsel = i & 1;
-                if (!bar_wait(bar(BAR_FULL16 + s), (i >> 1) & 1, abort_flag, p.err, 5)) break;
+                const int bsel = i & 1;
                 if (i >= 2 &&
-                    !bar_wait(bar(BAR_ACCEMPTY + bsel), ((i >> 1) + 1) & 1, abort_flag, p.err, 6))
+                    !bar_wait(bar(BAR_ACCEMPTY + bsel), ((i >> 1) & 1) ^ 1, abort_flag, p.err, 6))
                     break;
                 asm volatile("tcgen05.fence::after_thread_sync;");
-                for (int q = 0; q < mt; q++) {
-                    const uint32_t d = tmem + (uint32_t)(bsel * mt + q) * NT;
-                    const uint32_t ahi = sbase + L.a_hi + (uint32_t)q * MTILE * p.kpad * 2;
-                    const uint32_t alo = sbase + L.a_lo + (uint32_t)q * MTILE * p.kpad * 2;
-                    for (int ks = 0; ks < p.kpad / 16; ks++) {
-                        const uint32_t ko = (uint32_t)ks * 2 * LBO;
-                        const uint64_t dah = sdesc(ahi + ko, LBO, SBO);
-                        const uint64_t dal = sdesc(alo + ko, LBO, SBO);
-                        const uint32_t bst = sbase + L.b16 + s * L.b16_stride;
-                        const uint64_t dbh = sdesc(bst + ko, LBO, SBO);
-                        const uint64_t dbl = sdesc(bst + L.b16_half + ko, LBO, SBO);
-                        umma(d, dah, dbh, idesc, ks > 0);
-                        umma(d, dah, dbl, idesc, 1);
-                        umma(d, dal, dbh, idesc, 1);
+                const uint32_t d = tmem + (uint32_t)(bsel * npad);
+                for (int c = 0; c < nch; c++, j++) {
+                    const int s2 = (int)(j % S16);
+                    if (!bar_wait(bar(BAR_FULL16 + s2), (uint32_t)((j / S16) & 1), abort_flag,
+                                  p.err, 5)) {
+                        ok = false;
+                        break;
                     }
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    const uint32_t bhi = sbase + L.b16 + (uint32_t)s2 * 2 * CHUNK16;
+#pragma unroll
+                    for (int ks = 0; ks < KC / 16; ks++) {
+                        const uint32_t ko = (uint32_t)ks * 2 * LBO;
+                        const uint32_t kg = (uint32_t)(c * (KC / 16) + ks) * 2 * LBO;
+                        const uint64_t dh = sdesc(bhi + ko, LBO, SBO_CHUNK);
+                        const uint64_t dl = sdesc(bhi + CHUNK16 + ko, LBO, SBO_CHUNK);
+                        const uint64_t oh = sdesc(sbase + L.a_hi + kg, LBO, SBO_OP);
+                        const uint64_t ol = sdesc(sbase + L.a_lo + kg, LBO, SBO_OP);
+                        umma(d, dh, oh, idesc, (c | ks) != 0);
+                        umma(d, dl, oh, idesc, 1);
+                        umma(d, dh, ol, idesc, 1);
+                    }
+                    umma_commit(bar(BAR_EMPTY16 + s2));
                 }
-                umma_commit(bar(BAR_EMPTY16 + s));
+                if (!ok) break;
                 umma_commit(bar(BAR_ACCFULL + bsel));
             }
             // Drain: every MMA issued so far has completed once this arrives
@@ -340,53 +372,46 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
         __syncwarp();
     } else {
         // ---- epilogue: TMEM -> registers -> shared memory -> TMA store ----
-        int i = 0;
+        // warp w holds columns 32w..32w+31 of the tile (its TMEM lanes)
+        int i = 0, sb = 0;
         for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
             const int bsel = i & 1;
             if (!bar_wait(bar(BAR_ACCFULL + bsel), (i >> 1) & 1, abort_flag, p.err, 8)) break;
             asm volatile("tcgen05.fence::after_thread_sync;");
-            const int64_t col0 = t * NT;
-            for (int q = 0; q < mt; q++) {
-                // 32x32 sub-tiles: TMEM -> registers -> swizzled shared
-                // memory -> one TMA store (or reduce-add) per warp; rows
-                // beyond m and columns beyond ncol are clipped by the TMA
-                for (int cc = 0; cc < NT; cc += 32) {
-                    if (col0 + cc >= p.ncol) break;
-                    uint32_t v[32];
-                    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) +
-                                           (uint32_t)(bsel * mt + q) * NT + cc;
-                    asm volatile(
-                        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-                        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-                        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-                        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
-                          "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]),
-                          "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]),
-                          "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
-                          "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]),
-                          "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-                        : "r"(taddr));
-                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            const int64_t x0 = t * TCOLS + warp * 32;
+            // (a warp whose columns all lie past ncol has nothing to store,
+            // and must not touch its staging tiles: a store may still be
+            // reading them)
+            for (int g = 0; x0 < p.ncol && g < npad / 32; g++) {
+                uint32_t v[32];
+                const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) +
+                                       (uint32_t)(bsel * npad + g * 32);
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+                    "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                    "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
+                      "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]),
+                      "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]),
+                      "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+                      "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]),
+                      "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                    : "r"(taddr));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 
-                    // The previous store from this warp's buffer must have
-                    // finished reading it
-                    if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
-                    __syncwarp();
-                    unsigned char *buf = smem + L.epi + warp * EPI_WARP_BYTES;
+                // The store issued two stores ago from this buffer must
+                // have finished reading it
+                if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+                __syncwarp();
+                float *buf = reinterpret_cast<float *>(smem + L.epi + (warp * 2 + sb) * EPI_BUF);
 #pragma unroll
-                    for (int j = 0; j < 8; j++) {
-                        const float4 o = make_float4(p.alpha * __uint_as_float(v[4 * j]),
-                                                     p.alpha * __uint_as_float(v[4 * j + 1]),
-                                                     p.alpha * __uint_as_float(v[4 * j + 2]),
-                                                     p.alpha * __uint_as_float(v[4 * j + 3]));
-                        *reinterpret_cast<float4 *>(buf + lane * 128 + ((j ^ (lane & 7)) * 16)) = o;
-                    }
-                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    __syncwarp();
-                    if (lane == 0 && q * MTILE + warp * 32 < p.m)
-                        tma_store_2d(&p.cmap, sbase + L.epi + warp * EPI_WARP_BYTES,
-                                     (int)(col0 + cc), q * MTILE + warp * 32, p.epi);
-                }
+                for (int r = 0; r < 32; r++) buf[r * 32 + lane] = p.alpha * __uint_as_float(v[r]);
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                __syncwarp();
+                if (lane == 0)
+                    tma_store_2d(&p.cmap, sbase + L.epi + (warp * 2 + sb) * EPI_BUF, (int)x0,
+                                 g * 32, p.epi);
+                sb ^= 1;
             }
             asm volatile("tcgen05.fence::before_thread_sync;");
             bar_arrive(bar(BAR_ACCEMPTY + bsel));
@@ -405,11 +430,12 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
 }
 
 // Host: split A into BF16 hi/lo and lay both out in the canonical K-major
-// no-swizzle layout ((r/8)*SBO + (k/8)*128 + (r%8)*16 + (k%8)*2 bytes).
-void build_image(const double *a, int m, int k, int mpad, int kpad, std::vector<uint16_t> &img) {
-    const size_t n = (size_t)mpad * kpad;
+// no-swizzle layout ((r/8)*SBO + (k/8)*128 + (r%8)*16 + (k%8)*2 bytes,
+// SBO = kfull*16); rows past m and columns past k are zero.
+void build_image(const double *a, int m, int k, int npad, int kfull, std::vector<uint16_t> &img) {
+    const size_t n = (size_t)npad * kfull;
     img.assign(2 * n, 0);
-    const size_t SBO = (size_t)kpad * 16;
+    const size_t SBO = (size_t)kfull * 16;
     for (int r = 0; r < m; r++)
         for (int c = 0; c < k; c++) {
             const float x = (float)a[(size_t)r * k + c];
@@ -425,11 +451,11 @@ int g_sm_count = 0;
 PFN_cuTensorMapEncodeTiled_v12000 g_encode_tiled = nullptr;
 
 // Tensor map of B: rank 2, dims (ncol, k) innermost first, row stride
-// ldb*4 bytes, box (nt, k), no swizzle, out-of-range elements read as 0
-int encode_b_map(CUtensorMap *map, const float *b, int64_t ldb, int64_t ncol, int k, int nt) {
+// ldb*4 bytes, box (TCOLS, KC), no swizzle, out-of-range elements read as 0
+int encode_b_map(CUtensorMap *map, const float *b, int64_t ldb, int64_t ncol, int k) {
     cuuint64_t gdim[2] = {(cuuint64_t)ncol, (cuuint64_t)k};
     cuuint64_t gstride[1] = {(cuuint64_t)ldb * 4};
-    cuuint32_t box[2] = {(cuuint32_t)nt, (cuuint32_t)k};
+    cuuint32_t box[2] = {(cuuint32_t)TCOLS, (cuuint32_t)KC};
     cuuint32_t estride[2] = {1, 1};
     CUresult r = g_encode_tiled(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)b, gdim, gstride,
                                 box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -441,8 +467,8 @@ int encode_b_map(CUtensorMap *map, const float *b, int64_t ldb, int64_t ncol, in
     return B200_OK;
 }
 
-// Tensor map of out: dims (ncol, m), row stride ldc*4 bytes, box 32 x 32
-// with the 128-byte swizzle the epilogue writes its staging tiles in
+// Tensor map of out: dims (ncol, m), row stride ldc*4 bytes, box 32 x 32,
+// dense row-major staging tiles
 int encode_c_map(CUtensorMap *map, float *c, int64_t ldc, int64_t ncol, int m) {
     cuuint64_t gdim[2] = {(cuuint64_t)ncol, (cuuint64_t)m};
     cuuint64_t gstride[1] = {(cuuint64_t)ldc * 4};
@@ -450,7 +476,7 @@ int encode_c_map(CUtensorMap *map, float *c, int64_t ldc, int64_t ncol, int m) {
     cuuint32_t estride[2] = {1, 1};
     CUresult r = g_encode_tiled(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)c, gdim, gstride,
                                 box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                                CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS)
         return b200::set_error(B200_ERR_CUDA, "mul_bf16x3: cuTensorMapEncodeTiled (out) failed (%d)",
@@ -465,29 +491,27 @@ extern "C" {
 int b200_mul_bf16x3_create(const double *a, int m, int k, void **handle, size_t *smem_bytes) {
     if (!a || !handle || m <= 0 || k <= 0)
         return b200::set_error(B200_ERR_ARG, "mul_bf16x3_create: bad arguments");
-    const int mpad = (m + MTILE - 1) / MTILE * MTILE, kpad = (k + 15) / 16 * 16;
-    const int mt = mpad / MTILE;
-    // Widest column tile, then the deepest FP32 staging (bytes in flight
-    // per SM), whose pipeline fits in shared memory
-    int nt = 0, s32 = 0;
-    Layout L = make_layout(mpad, kpad, k, 32, 2);
-    for (int cand_nt : {64, 32}) {
-        for (int cand_s = MAX_S32; cand_s >= 2 && !nt; cand_s--) {
-            Layout c = make_layout(mpad, kpad, k, cand_nt, cand_s);
-            if (c.total <= 227 * 1024) {
-                nt = cand_nt;
-                s32 = cand_s;
-                L = c;
-            }
+    const int npad = (m + 31) / 32 * 32, kfull = (k + KC - 1) / KC * KC;
+    // Two BF16 stages, then the deepest FP32 staging (bytes in flight per
+    // SM) that fits in shared memory; a third BF16 stage if room is left
+    int s32 = 0, s16 = 2;
+    Layout L = make_layout(npad, kfull, 2, 2);
+    for (int cand = MAX_S32; cand >= 2 && !s32; cand--) {
+        Layout c = make_layout(npad, kfull, cand, 2);
+        if (c.total <= 227 * 1024) {
+            s32 = cand;
+            L = c;
         }
-        if (nt) break;
+    }
+    if (s32 == MAX_S32 && make_layout(npad, kfull, s32, 3).total <= 227 * 1024) {
+        s16 = 3;
+        L = make_layout(npad, kfull, s32, s16);
     }
     if (smem_bytes) *smem_bytes = L.total;
-    // (a TMA box spans at most 256 rows of B)
-    if (mt > MAX_MT || !nt || L.total > 227 * 1024 || k > 256 || kpad / 16 * 3 * mt > 1024)
+    if (npad > MAX_N || !s32 || L.total > 227 * 1024)
         return b200::set_error(B200_ERR_UNSUPPORTED,
-                               "mul_bf16x3: operator %dx%d needs %u bytes of shared memory", m,
-                               k, L.total);
+                               "mul_bf16x3: operator %dx%d needs %u bytes of shared memory "
+                               "(or more than %d rows)", m, k, L.total, MAX_N);
 
     // One-time device set-up here rather than at launch: changing a
     // function attribute while a stream capture is open invalidates it
@@ -499,12 +523,7 @@ int b200_mul_bf16x3_create(const double *a, int m, int k, void **handle, size_t 
                 cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev),
                 "mul_bf16x3_create");
         if (!rc0)
-            rc0 = b200::check_cuda(cudaFuncSetAttribute(mul_umma_kernel<64>,
-                                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                        227 * 1024),
-                                   "mul_bf16x3: smem attribute");
-        if (!rc0)
-            rc0 = b200::check_cuda(cudaFuncSetAttribute(mul_umma_kernel<32>,
+            rc0 = b200::check_cuda(cudaFuncSetAttribute(mul_umma_kernel,
                                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                         227 * 1024),
                                    "mul_bf16x3: smem attribute");
@@ -523,11 +542,11 @@ int b200_mul_bf16x3_create(const double *a, int m, int k, void **handle, size_t 
     }
 
     std::vector<uint16_t> img;
-    build_image(a, m, k, mpad, kpad, img);
+    build_image(a, m, k, npad, kfull, img);
 
     UmmaHandle *h = (UmmaHandle *)calloc(1, sizeof(UmmaHandle));
     if (!h) return b200::set_error(B200_ERR_STATE, "mul_bf16x3_create: out of host memory");
-    h->m = m; h->k = k; h->mpad = mpad; h->kpad = kpad; h->mt = mt; h->nt = nt; h->s32 = s32;
+    h->m = m; h->k = k; h->npad = npad; h->kfull = kfull; h->s32 = s32; h->s16 = s16;
     h->aimg_bytes = img.size() * 2;
     h->smem_bytes = L.total;
     int rc = b200::check_cuda(cudaMalloc(&h->aimg, h->aimg_bytes), "mul_bf16x3_create");
@@ -558,7 +577,8 @@ int b200_mul_bf16x3(void *handle, const float *b, int64_t ldb, float *c, int64_t
     if (ncol <= 0) return B200_OK;
     if (ldb < ncol || ldc < ncol)
         return b200::set_error(B200_ERR_ARG, "mul_bf16x3: leading dimension smaller than ncol");
-    // Bulk copies need 16-byte aligned rows and 16-byte multiples
+    // Tensor maps need 16-byte aligned bases and row strides; tiles start
+    // at multiples of 32 columns (128 bytes)
     if ((((uintptr_t)b) & 15) || (((uintptr_t)c) & 15) || (ldb % 4) || (ldc % 4) || (ncol % 4))
         return b200::set_error(B200_ERR_ARG, "mul_bf16x3: operands must be 16-byte aligned");
 
@@ -569,19 +589,16 @@ int b200_mul_bf16x3(void *handle, const float *b, int64_t ldb, float *c, int64_t
     if (beta != 0.0f && beta != 1.0f)
         return b200::set_error(B200_ERR_UNSUPPORTED, "mul_bf16x3: beta must be 0 or 1");
     UmmaArgs p;
-    int rc = encode_b_map(&p.tmap, b, ldb, ncol, h->k, h->nt);
+    int rc = encode_b_map(&p.tmap, b, ldb, ncol, h->k);
     if (!rc) rc = encode_c_map(&p.cmap, c, ldc, ncol, h->m);
     if (rc) return rc;
-    p.aimg = h->aimg; p.b = b; p.c = c; p.ldb = ldb; p.ldc = ldc; p.ncol = ncol;
-    p.m = h->m; p.k = h->k; p.kpad = h->kpad; p.mt = h->mt; p.s32 = h->s32;
-    p.alpha = alpha; p.beta = beta; p.epi = beta != 0.0f; p.err = err;
+    p.aimg = h->aimg; p.ncol = ncol;
+    p.m = h->m; p.npad = h->npad; p.kfull = h->kfull; p.s32 = h->s32; p.s16 = h->s16;
+    p.alpha = alpha; p.epi = beta != 0.0f; p.err = err;
 
-    const int64_t ntiles = (ncol + h->nt - 1) / h->nt;
+    const int64_t ntiles = (ncol + TCOLS - 1) / TCOLS;
     const unsigned grid = (unsigned)(ntiles < g_sm_count ? ntiles : g_sm_count);
-    if (h->nt == 64)
-        mul_umma_kernel<64><<<grid, NTHREADS, h->smem_bytes, (cudaStream_t)stream>>>(p);
-    else
-        mul_umma_kernel<32><<<grid, NTHREADS, h->smem_bytes, (cudaStream_t)stream>>>(p);
+    mul_umma_kernel<<<grid, NTHREADS, h->smem_bytes, (cudaStream_t)stream>>>(p);
     B200_CHECK_LAUNCH("mul_umma_kernel");
     return B200_OK;
 }

@@ -16,11 +16,17 @@ namespace b200 {
 
 // Gas / viscosity constants shared by all flux kernels (POD, matches the
 // b200_gas_t struct of the C ABI).  When `shifted` is set the kernels'
-// input is the perturbation du = u - u_ref from a constant reference state
-// (rho_ref, 0, E_ref = p_ref/(gamma - 1)), and the constant part p_ref*I
-// of the momentum flux is dropped: the flux-reconstruction divergence of a
-// constant flux field is exactly zero, so the right-hand side is unchanged
-// in exact arithmetic while FP32 rounding no longer scales with p_ref.
+// input is q = T(u - u_ref): the perturbation from a constant reference
+// state (rho_ref, 0, E_ref = p_ref/(gamma - 1)) with the energy component
+// replaced by dE - h_ref*drho, h_ref = gamma/(gamma - 1) p_ref/rho_ref the
+// reference specific enthalpy.  T is linear and constant, so the system in
+// q is the system in u multiplied by T: the mass and momentum equations are
+// unchanged and the energy equation is the energy equation minus h_ref
+// times the mass equation.  Its inviscid flux is (dE - h_ref*drho + dp) v
+// instead of (H_ref + dE + dp) v, and the constant part p_ref*I of the
+// momentum flux is dropped (the flux-reconstruction divergence of a
+// constant flux field is exactly zero).  Every flux is then of the size of
+// the perturbation, so FP32 rounding no longer scales with p_ref or H_ref.
 struct Gas {
     double gamma, mu, pr, cpTref, cpTs;
     int sutherland;
@@ -34,7 +40,7 @@ struct Gas {
 template <typename T>
 struct GasK {
     T gamma, gm1, mu, gamma_pr, rcp_cpTref, mu_ctt, cpTs, quarter_gamma;
-    T rho_ref, p_ref, e_ref, h_ref;
+    T rho_ref, p_ref, e_ref, h_ref, hs_ref;
     int sutherland, shifted;
 };
 
@@ -53,6 +59,7 @@ inline GasK<T> gas_consts(const Gas &g) {
     k.p_ref = (T)g.p_ref;
     k.e_ref = (T)(g.p_ref / (g.gamma - 1.0));
     k.h_ref = (T)(g.gamma / (g.gamma - 1.0) * g.p_ref);
+    k.hs_ref = (T)(g.rho_ref != 0.0 ? g.gamma / (g.gamma - 1.0) * g.p_ref / g.rho_ref : 0.0);
     k.sutherland = g.sutherland;
     k.shifted = g.shifted;
     return k;
@@ -175,17 +182,18 @@ __device__ __forceinline__ void rsolve_rusanov(const T *ul, const T *ur, const T
     }
 }
 
-// Inviscid flux from the perturbation input s = u - u_ref (see Gas):
-// rho = rho_ref + s[0], m = s[1..ND], dp = p - p_ref from
-// (gamma - 1)(dE - |m|^2/(2 rho)); momentum flux m v + dp I; energy flux
-// (H_ref + dE + dp) v with H_ref = gamma/(gamma - 1) p_ref.  Returns the full
-// pressure in p and the full state in ufull (for the viscous terms).
+// Inviscid flux from the transformed input s = q = T(u - u_ref) (see Gas):
+// rho = rho_ref + s[0], m = s[1..ND], dE = s[E] + hs_ref*s[0], dp = p - p_ref
+// from (gamma - 1)(dE - |m|^2/(2 rho)); mass flux m, momentum flux
+// m v + dp I, energy flux (s[E] + dp) v.  Returns the full pressure in p and
+// the full state in ufull (for the viscous terms).
 template <int ND, typename T>
 __device__ __forceinline__ void inviscid_flux_shift(const T *s, T f[ND][ND + 2], T &p, T v[ND],
                                                     T ufull[ND + 2], const GasK<T> &g) {
     constexpr int NV = ND + 2;
     const T gm1 = g.gm1;
-    const T rho = g.rho_ref + s[0], invrho = T(1) / rho, dE = s[NV - 1];
+    const T rho = g.rho_ref + s[0], invrho = T(1) / rho;
+    const T dE = s[NV - 1] + g.hs_ref * s[0];
     T dot = 0;
 #pragma unroll
     for (int i = 0; i < ND; i++) {
@@ -194,7 +202,7 @@ __device__ __forceinline__ void inviscid_flux_shift(const T *s, T f[ND][ND + 2],
     }
     const T dp = gm1 * (dE - T(0.5) * dot);
     p = g.p_ref + dp;
-    const T hv = g.h_ref + dE + dp;
+    const T hv = s[NV - 1] + dp;
 #pragma unroll
     for (int i = 0; i < ND; i++) {
         f[i][0] = s[i + 1];
@@ -208,8 +216,23 @@ __device__ __forceinline__ void inviscid_flux_shift(const T *s, T f[ND][ND + 2],
     ufull[NV - 1] = g.e_ref + dE;
 }
 
-// Rusanov flux on perturbation inputs (dissipation acts on differences, so
-// the shift cancels there)
+// Gradient of the full state from the gradient of q (the energy row of
+// T^-1; the reference state itself is constant)
+template <int ND, typename T>
+__device__ __forceinline__ void unshift_grad(const T gq[ND][ND + 2], T gu[ND][ND + 2],
+                                             const GasK<T> &g) {
+    constexpr int NV = ND + 2;
+#pragma unroll
+    for (int d = 0; d < ND; d++) {
+#pragma unroll
+        for (int v = 0; v < NV - 1; v++) gu[d][v] = gq[d][v];
+        gu[d][NV - 1] = gq[d][NV - 1] + g.hs_ref * gq[d][0];
+    }
+}
+
+// Rusanov flux on transformed inputs: the dissipation acts on differences
+// of q, which are T times the differences of u, so the flux is T times the
+// Rusanov flux of the full states
 template <int ND, typename T>
 __device__ __forceinline__ void rsolve_rusanov_shift(const T *ul, const T *ur, const T *n, T *nf,
                                                      T ufl[ND + 2], T ufr[ND + 2],

@@ -126,9 +126,10 @@ tflux_ns_kernel(int nupts, int64_t neles, b200::GasK<T> gas, const T *__restrict
 
     T ft[ND][NV], p, vel[ND];
     if (gas.shifted) {
-        T uf[NV];
+        T uf[NV], gu[ND][NV];
         b200::inviscid_flux_shift<ND, T>(uu, ft, p, vel, uf, gas);
-        b200::viscous_flux_add<ND, T>(uf, gr, ft, gas);
+        b200::unshift_grad<ND, T>(gr, gu, gas);
+        b200::viscous_flux_add<ND, T>(uf, gu, ft, gas);
     } else {
         b200::inviscid_flux<ND, T>(uu, ft, p, vel, gas.gamma);
         b200::viscous_flux_add<ND, T>(uu, gr, ft, gas);
@@ -293,7 +294,13 @@ intcflux_ns_kernel(int64_t n, int rs, b200::GasK<T> gas, T beta, T tau, ScalView
         for (int d = 0; d < ND; d++)
 #pragma unroll
             for (int v = 0; v < NV; v++) gg[d][v] = g[d * rstr + v * B200_SOASZ];
-        b200::viscous_flux_add<ND, T>(ufl, gg, fvl, gas);
+        if (gas.shifted) {
+            T gu[ND][NV];
+            b200::unshift_grad<ND, T>(gg, gu, gas);
+            b200::viscous_flux_add<ND, T>(ufl, gu, fvl, gas);
+        } else {
+            b200::viscous_flux_add<ND, T>(ufl, gg, fvl, gas);
+        }
     }
     if (beta != T(0.5)) {
         const T *g = gr.base + b200::load_ix(gr.map, ix64, i);
@@ -303,7 +310,13 @@ intcflux_ns_kernel(int64_t n, int rs, b200::GasK<T> gas, T beta, T tau, ScalView
         for (int d = 0; d < ND; d++)
 #pragma unroll
             for (int v = 0; v < NV; v++) gg[d][v] = g[d * rstr + v * B200_SOASZ];
-        b200::viscous_flux_add<ND, T>(ufr, gg, fvr, gas);
+        if (gas.shifted) {
+            T gu[ND][NV];
+            b200::unshift_grad<ND, T>(gg, gu, gas);
+            b200::viscous_flux_add<ND, T>(ufr, gu, fvr, gas);
+        } else {
+            b200::viscous_flux_add<ND, T>(ufr, gg, fvr, gas);
+        }
     }
 
 #pragma unroll

@@ -279,6 +279,12 @@ class MixedRKIntegrator(RKVdH2Integrator):
     of the next RHS evaluation, so it is kept in FP32 (system bank 0) and
     written by the stage kernel; system bank 1 receives the FP32 RHS; the
     solution itself (and the PI controller's error registers) are FP64.
+
+    With a reference state the system works in q = T(u - u_ref) (the
+    perturbation from u_ref with the energy replaced by dE - h_ref*drho,
+    see ``b200_gas_t``), and the FP64 accumulator holds q: the stage kernel
+    then forms the FP32 input with no FP64 arithmetic beyond its one FMA.
+    ``soln`` maps q back to u.
     """
 
     def __init__(self, backend, systemcls, mesh, cfg, initsoln=None):
@@ -299,7 +305,7 @@ class MixedRKIntegrator(RKVdH2Integrator):
         # Reference-state shift of the FP32 right-hand side (Navier-Stokes
         # with the Rusanov solver): the volume means of rho and p of the
         # initial condition.  Must be set before the kernels are built.
-        self.uref = None
+        self.uref, self.hs_ref = None, 0.0
         shift = cfg.get('backend-b200', 'reference-shift', 'auto')
         rs = cfg.get('solver-interfaces', 'riemann-solver')
         if shift == 'auto' and sysm.name == 'navier-stokes' and rs == 'rusanov':
@@ -313,6 +319,7 @@ class MixedRKIntegrator(RKVdH2Integrator):
             nv = sysm.nvars
             self.uref = np.zeros(nv)
             self.uref[0], self.uref[-1] = rho_ref, p_ref/(gamma - 1)
+            self.hs_ref = gamma/(gamma - 1)*p_ref/rho_ref
 
         return sysm
 
@@ -321,11 +328,6 @@ class MixedRKIntegrator(RKVdH2Integrator):
         if self.errest:
             mats += self.rold + self.rerr
         return mats
-
-    def _uref_args(self):
-        if self.uref is None:
-            return 0, None
-        return len(self.uref), self.uref.ctypes.data
 
     def _setup_registers(self, initsoln):
         be, sysm = self.backend, self.system
@@ -336,20 +338,36 @@ class MixedRKIntegrator(RKVdH2Integrator):
                               tags={'align'}, dtype=np.float64)
                     for ic_ in (ic if ic is not None else ics)]
 
-        self.acc = reg(ics)
+        self.acc = reg([self.to_q(ic) for ic in ics])
         self.rold = reg() if self.errest else None
         self.rerr = reg() if self.errest else None
         be.commit()
         self.refresh_input(be.stream)
         be.wait()
 
+    def to_q(self, u):
+        """Solution (nupts, nvars, neles) -> the integrated variables."""
+        if self.uref is None:
+            return np.asarray(u, dtype=np.float64)
+        q = u - self.uref[None, :, None]
+        q[:, -1] -= self.hs_ref*q[:, 0]
+        return q
+
+    def from_q(self, q):
+        if self.uref is None:
+            return q
+        u = q + self.uref[None, :, None]
+        u[:, -1] += self.hs_ref*q[:, 0]
+        return u
+
     def refresh_input(self, stream):
-        """Enqueue the FP32 RHS input (u - u_ref) from the FP64 solution."""
-        lib, nv_uref = self.backend.lib, self._uref_args()
+        """Enqueue the FP32 RHS input from the FP64 accumulator (which
+        holds q when there is a reference state)."""
+        lib = self.backend.lib
         for j, bank in enumerate(self.system.ele_banks):
             acc = self.acc[j]
             lib.cast_f64_f32(acc.nrow*acc.leaddim, acc.data, bank[0].data,
-                             *nv_uref, stream)
+                             0, None, stream)
 
     def _stage_kernel(self, i, j, dt):
         lib, nst, errest = self.backend.lib, self.nstages, int(self.errest)
@@ -361,11 +379,10 @@ class MixedRKIntegrator(RKVdH2Integrator):
         ro = self.rold[j].data if self.errest else None
         re = self.rerr[j].data if self.errest else None
         pa, pr, pu = acc.data, bank[1].data, bank[0].data
-        nvu, pref = self._uref_args()
 
         def run(stream):
             lib.rkmixed_f64f32(n, i, nst, errest, dt, a, b, e, pa, pr, pu, ro,
-                               re, nvu, pref, stream)
+                               re, stream)
 
         return Kernel(run, mats=[acc, bank[0], bank[1]], name='rkmixed',
                       meta=dict(kind='rkmixed', n=n))
@@ -392,7 +409,8 @@ class MixedRKIntegrator(RKVdH2Integrator):
     def _errest(self, icurr, ierr):
         if 'mixed' not in self._ekerns:
             self._ekerns['mixed'] = [
-                self.backend.kernel('errest', a, r, self._atols)
+                self.backend.kernel('errest', a, r, self._atols,
+                                    uref=self.uref, hcoef=self.hs_ref)
                 for a, r in zip(self.acc, self.rerr)]
         ks = self._ekerns['mixed']
         for k in ks:
@@ -404,4 +422,4 @@ class MixedRKIntegrator(RKVdH2Integrator):
 
     @property
     def soln(self):
-        return [a.get() for a in self.acc]
+        return [self.from_q(a.get()) for a in self.acc]

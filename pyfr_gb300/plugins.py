@@ -54,11 +54,17 @@ class FieldIntegrals:
         for j, (eles, wmat) in enumerate(self._edata):
             u = intg.acc[j] if mixed else sysm.ele_banks[j][uidx]
             g = eles._grad_upts
-            fn = lib.integrals_f64f32 if g.dtype == np.float32 else \
-                lib.integrals_f64
-            fn(eles.ndims, eles.nupts, eles.neles, u.data, u.leaddim, g.data,
-               g.leaddim, wmat.data, wmat.leaddim, self._scratch.data,
-               self.NBLK, self._out.data, stream)
+            args = (eles.ndims, eles.nupts, eles.neles, u.data, u.leaddim,
+                    g.data, g.leaddim, wmat.data, wmat.leaddim)
+            if g.dtype == np.float32:
+                # The mixed integrator may store u - u_ref
+                uref = getattr(intg, 'uref', None) if mixed else None
+                pu = None if uref is None else uref.ctypes.data
+                lib.integrals_f64f32(*args, pu, self._scratch.data, self.NBLK,
+                                     self._out.data, stream)
+            else:
+                lib.integrals_f64(*args, self._scratch.data, self.NBLK,
+                                  self._out.data, stream)
             lib.memcpy_dtoh(self._host.ctypes.data, self._out.data, 24, stream)
             be.wait()
             total += self._host
