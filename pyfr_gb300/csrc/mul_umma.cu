@@ -14,16 +14,23 @@
 // out per TMEM lane with the operator rows along its columns.
 //
 // One persistent CTA per SM walks 128-column tiles of B/out, each in
-// chunks of 32 rows of B (K):
-//   warp 4 lane 0   loads each 32 x 128 FP32 chunk with one 2-D tensor TMA
-//                   into a ring of staging buffers;
-//   warps 5-8       split a staged chunk into BF16 hi/lo in the canonical
-//                   K-major no-swizzle UMMA layout (one column per thread);
-//   warp 9 lane 0   issues the MMAs into one of two TMEM accumulators;
-//   warps 0-3       read the accumulator (tcgen05.ld, one column of out per
-//                   thread, 32 operator rows per load), scale by alpha into
-//                   a 32 x 32 staging tile and write it with a TMA tensor
-//                   store (beta = 0) or reduce-add (beta = 1).
+// chunks of 32 rows of B (K), through one ring of 16 KB stages:
+//   warp 16 lane 0  loads each 32 x 128 FP32 chunk with one 2-D tensor TMA
+//                   into a free stage;
+//   warps 8-15      split the staged chunk into BF16 hi/lo in place: every
+//                   thread reads its half column (16 values), the converter
+//                   warps meet at a named barrier, then write the halves in
+//                   the canonical K-major no-swizzle UMMA layout over the
+//                   same 16 KB;
+//   warp 17 lane 0  issues the MMAs into one of two TMEM accumulators; the
+//                   completion of a chunk's MMAs frees its stage;
+//   warps 0-7       read the accumulator (tcgen05.ld, one column of out per
+//                   thread, 32 operator rows per load) in two sets of four,
+//                   one warp per TMEM lane quadrant, the sets taking
+//                   alternate 32-row groups; a set scales its group by
+//                   alpha into one 128 x 32 staging tile (two per set) and
+//                   writes it with a TMA tensor store (beta = 0) or
+//                   reduce-add (beta = 1) of 512-byte rows.
 // The operator halves are laid out on the host in the canonical layout
 // and bulk-copied into shared memory once per CTA.  All hand-offs are
 // mbarriers; every wait is bounded and records an error code instead of
@@ -42,21 +49,24 @@ namespace {
 
 constexpr int TCOLS = 128;        // columns of B/out per tile (UMMA M)
 constexpr int KC = 32;            // rows of B per pipeline chunk
-constexpr int NTHREADS = 320;     // 10 warps
-constexpr int NCONV = 128;        // converter threads (warps 5-8)
-constexpr int NEPI = 128;         // epilogue threads (warps 0-3)
+constexpr int NTHREADS = 576;     // 18 warps
+constexpr int NEPI = 256;         // epilogue threads (warps 0-7)
+constexpr int NCONV = 256;        // converter threads (warps 8-15)
+constexpr int WARP_CONV = 8, WARP_PROD = 16, WARP_MMA = 17;
+constexpr int CONV_BARRIER = 1;   // named barrier of the converter warps
+constexpr int EPI_BARRIER = 2;    // named barriers 2, 3: the epilogue sets
 constexpr int MAX_N = 256;        // UMMA N limit (operator rows, padded)
-constexpr int MAX_S32 = 8;        // FP32 chunk stages (bytes in flight)
-constexpr int MAX_S16 = 4;        // BF16 chunk stages
+constexpr int MAX_S = 10;         // ring stages (bytes in flight)
+constexpr int EB = 2;             // staging tiles per epilogue set
 constexpr long long WAIT_LIMIT = 1LL << 22;
 
-constexpr uint32_t CHUNK32 = KC * TCOLS * 4;       // 16 KB FP32 chunk
-constexpr uint32_t CHUNK16 = KC * TCOLS * 2;       // 8 KB per BF16 half
+constexpr uint32_t CHUNK32 = KC * TCOLS * 4;       // 16 KB FP32 chunk (one stage)
+constexpr uint32_t CHUNK16 = KC * TCOLS * 2;       // 8 KB per BF16 half of a stage
 constexpr uint32_t SBO_CHUNK = KC * 16;            // 8-row group stride of a chunk
-constexpr uint32_t EPI_BUF = 32 * 32 * 4;          // one 32 x 32 FP32 staging tile
+constexpr uint32_t EPI_BUF = 32 * TCOLS * 4;       // one 32-row x 128-column staging tile
 
 struct UmmaHandle {
-    int m, k, npad, kfull, s32, s16;
+    int m, k, npad, kfull, ns;
     unsigned char *aimg;   // device: [hi | lo], each npad x kfull bf16 canonical
     size_t aimg_bytes;
     size_t smem_bytes;
@@ -66,34 +76,33 @@ struct UmmaHandle {
 // runtime-indexed array here would live in local memory)
 struct Layout {
     uint32_t a_hi, a_lo;
-    uint32_t b32;                 // FP32 stage s at b32 + s*CHUNK32
-    uint32_t b16;                 // BF16 stage s: hi at b16 + s*2*CHUNK16, lo after
-    uint32_t epi;                 // 4 warps x 2 staging tiles, 1024-aligned
+    uint32_t ring;                // stage s at ring + s*CHUNK32: FP32 chunk, then
+                                  // BF16 hi (first 8 KB) and lo (second 8 KB)
+    uint32_t epi;                 // staging tile b of set h at epi + (h*EB + b)*EPI_BUF
     uint32_t bar, tslot, abort_flag, total;
 };
 
-__host__ __device__ inline Layout make_layout(int npad, int kfull, int s32, int s16) {
+__host__ __device__ inline Layout make_layout(int npad, int kfull, int ns) {
     Layout L;
     uint32_t off = 0;
     const uint32_t abytes = (uint32_t)npad * kfull * 2;
     L.a_hi = off; off += abytes;
     L.a_lo = off; off += abytes;
     off = (off + 1023) & ~1023u;
-    L.b32 = off; off += s32 * CHUNK32;
-    L.b16 = off; off += s16 * 2 * CHUNK16;
-    L.epi = off; off += 8 * EPI_BUF;
-    L.bar = off; off += 32 * 8;
+    L.ring = off; off += ns * CHUNK32;
+    L.epi = off; off += 2 * EB * EPI_BUF;
+    L.bar = off; off += 40 * 8;
     L.tslot = off; off += 8;
     L.abort_flag = off; off += 8;
     L.total = off;
     return L;
 }
 
-// Barrier indices within the barrier block
-enum { BAR_A = 0, BAR_FULL32 = 1, BAR_EMPTY32 = 1 + MAX_S32, BAR_FULL16 = 1 + 2 * MAX_S32,
-       BAR_EMPTY16 = 1 + 2 * MAX_S32 + MAX_S16, BAR_ACCFULL = 1 + 2 * MAX_S32 + 2 * MAX_S16,
-       BAR_ACCEMPTY = 3 + 2 * MAX_S32 + 2 * MAX_S16, BAR_DRAIN = 5 + 2 * MAX_S32 + 2 * MAX_S16 };
-static_assert(BAR_DRAIN < 32, "barrier block holds 32 slots");
+// Barrier indices within the barrier block: per stage, loaded (TMA),
+// converted (converter warps) and free (MMA completion)
+enum { BAR_A = 0, BAR_LOADED = 1, BAR_CONVERTED = 1 + MAX_S, BAR_FREE = 1 + 2 * MAX_S,
+       BAR_ACCFULL = 1 + 3 * MAX_S, BAR_ACCEMPTY = 3 + 3 * MAX_S, BAR_DRAIN = 5 + 3 * MAX_S };
+static_assert(BAR_DRAIN < 40, "barrier block holds 40 slots");
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -132,6 +141,13 @@ __device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity, volatile
     *abort_flag = 1;
     atomicCAS(err, 0, code);
     return false;
+}
+
+// Bounded wait that ignores the abort flag: for copies in flight that must
+// land before the CTA exits
+__device__ __forceinline__ void bar_drain(uint32_t bar, uint32_t parity) {
+    for (long long it = 0; it < WAIT_LIMIT && !bar_try(bar, parity); it++)
+        if (it > 32) __nanosleep(64);
 }
 
 __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes,
@@ -176,8 +192,8 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map
                  :: "r"(dst), "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar) : "memory");
 }
 
-// Store (or add, for beta = 1) a 32 x 32 FP32 tile from dense row-major
-// shared memory into out through the tensor map of out
+// Store (or add, for beta = 1) a 32-row x 128-column FP32 tile from dense
+// row-major shared memory into out through the tensor map of out
 __device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, uint32_t src, int x, int y,
                                              int add) {
     if (add)
@@ -193,10 +209,10 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, uint32_t sr
 
 struct UmmaArgs {
     CUtensorMap tmap;           // B as a (k x ncol) FP32 tensor, box TCOLS x KC
-    CUtensorMap cmap;           // out as a (m x ncol) FP32 tensor, box 32 x 32
+    CUtensorMap cmap;           // out as a (m x ncol) FP32 tensor, box TCOLS x 32
     const unsigned char *aimg;
     int64_t ncol;
-    int m, npad, kfull, s32, s16;
+    int m, npad, kfull, ns;
     float alpha;
     int epi;            // 0: store alpha*D, 1: add alpha*D to out
     int *err;
@@ -204,8 +220,8 @@ struct UmmaArgs {
 
 __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_constant__ UmmaArgs p) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    const Layout L = make_layout(p.npad, p.kfull, p.s32, p.s16);
-    const int S32 = p.s32, S16 = p.s16;
+    const Layout L = make_layout(p.npad, p.kfull, p.ns);
+    const int NS = p.ns;
     const uint32_t sbase = smem_addr(smem);
     const uint32_t bar0 = sbase + L.bar;
     auto bar = [&](int i) { return bar0 + 8u * i; };
@@ -221,13 +237,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
     if (tid == 0) {
         *abort_flag = 0;
         bar_init(bar(BAR_A), 1);
-        for (int s = 0; s < S32; s++) {
-            bar_init(bar(BAR_FULL32 + s), 1);
-            bar_init(bar(BAR_EMPTY32 + s), NCONV);
-        }
-        for (int s = 0; s < S16; s++) {
-            bar_init(bar(BAR_FULL16 + s), NCONV);
-            bar_init(bar(BAR_EMPTY16 + s), 1);
+        for (int s = 0; s < NS; s++) {
+            bar_init(bar(BAR_LOADED + s), 1);
+            bar_init(bar(BAR_CONVERTED + s), NCONV);
+            bar_init(bar(BAR_FREE + s), 1);
         }
         for (int s = 0; s < 2; s++) {
             bar_init(bar(BAR_ACCFULL + s), 1);
@@ -249,7 +262,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
     const uint32_t abytes = (uint32_t)npad * p.kfull * 2;
     const uint32_t SBO_OP = (uint32_t)p.kfull * 16, LBO = 128;
 
-    if (warp == 4) {
+    if (warp == WARP_PROD) {
         // ---- producer: operator image once, then the FP32 chunks of B ----
         if (lane == 0) bar_arrive_tx(bar(BAR_A), 2 * abytes);
         __syncwarp();
@@ -266,66 +279,74 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
             for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
                 bool ok = true;
                 for (int c = 0; c < nch; c++, j++) {
-                    const int s = (int)(j % S32);
-                    if (j >= S32 &&
-                        !bar_wait(bar(BAR_EMPTY32 + s), (uint32_t)((j / S32) & 1) ^ 1, abort_flag,
+                    const int s = (int)(j % NS);
+                    if (j >= NS &&
+                        !bar_wait(bar(BAR_FREE + s), (uint32_t)((j / NS) & 1) ^ 1, abort_flag,
                                   p.err, 1)) {
                         ok = false;
                         break;
                     }
-                    bar_arrive_tx(bar(BAR_FULL32 + s), CHUNK32);
-                    tma_load_2d(sbase + L.b32 + (uint32_t)s * CHUNK32, &p.tmap, (int)(t * TCOLS),
-                                c * KC, bar(BAR_FULL32 + s));
+                    bar_arrive_tx(bar(BAR_LOADED + s), CHUNK32);
+                    tma_load_2d(sbase + L.ring + (uint32_t)s * CHUNK32, &p.tmap, (int)(t * TCOLS),
+                                c * KC, bar(BAR_LOADED + s));
                 }
                 if (!ok) break;
             }
+            // Every copy into shared memory has landed before the CTA may
+            // exit (after an abort nobody else waits for them)
+            bar_drain(bar(BAR_A), 0);
+            for (int64_t q = j > NS ? j - NS : 0; q < j; q++)
+                bar_drain(bar(BAR_LOADED + (int)(q % NS)), (uint32_t)((q / NS) & 1));
         }
         __syncwarp();
-    } else if (warp >= 5 && warp <= 8) {
-        // ---- converters: FP32 chunk -> BF16 hi/lo canonical K-major ----
-        // thread ct owns column ct of the tile
-        const int ct = tid - 5 * 32;
-        const uint32_t coff = (uint32_t)(ct / 8) * SBO_CHUNK + (uint32_t)(ct % 8) * 16;
+    } else if (warp >= WARP_CONV && warp < WARP_CONV + NCONV / 32) {
+        // ---- converters: FP32 chunk -> BF16 hi/lo canonical K-major, in place ----
+        // thread ct owns rows 16h..16h+15 of column cc of the chunk
+        const int ct = tid - WARP_CONV * 32, cc = ct % TCOLS, h = ct / TCOLS;
+        const uint32_t coff = (uint32_t)(cc / 8) * SBO_CHUNK + (uint32_t)(cc % 8) * 16;
         int64_t j = 0;
         bool ok = true;
         for (int64_t t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
             for (int c = 0; c < nch; c++, j++) {
-                const int s = (int)(j % S32), s2 = (int)(j % S16);
-                if (!bar_wait(bar(BAR_FULL32 + s), (uint32_t)((j / S32) & 1), abort_flag, p.err, 2) ||
-                    (j >= S16 && !bar_wait(bar(BAR_EMPTY16 + s2), (uint32_t)((j / S16) & 1) ^ 1,
-                                           abort_flag, p.err, 3))) {
+                const int s = (int)(j % NS);
+                // (a converter that gives up still meets the others at the
+                // named barrier below, so none of them waits there forever)
+                ok = bar_wait(bar(BAR_LOADED + s), (uint32_t)((j / NS) & 1), abort_flag, p.err, 2);
+                unsigned char *stage = smem + L.ring + s * CHUNK32;
+                const float *b32 = reinterpret_cast<const float *>(stage);
+                float x[16];
+                if (ok) {
+#pragma unroll
+                    for (int r = 0; r < 16; r++) x[r] = b32[(16 * h + r) * TCOLS + cc];
+                }
+                asm volatile("bar.sync %0, %1;" :: "n"(CONV_BARRIER), "n"(NCONV) : "memory");
+                if (!ok || *abort_flag) {
                     ok = false;
                     break;
                 }
-                const float *b32 = reinterpret_cast<const float *>(smem + L.b32 + s * CHUNK32);
-                unsigned char *bhi = smem + L.b16 + s2 * 2 * CHUNK16;
-                unsigned char *blo = bhi + CHUNK16;
 #pragma unroll
-                for (int k8 = 0; k8 < KC / 8; k8++) {
+                for (int q = 0; q < 2; q++) {
                     uint32_t hw[4], lw[4];
 #pragma unroll
                     for (int jj = 0; jj < 8; jj += 2) {
-                        const float x0 = b32[(k8 * 8 + jj) * TCOLS + ct];
-                        const float x1 = b32[(k8 * 8 + jj + 1) * TCOLS + ct];
-                        const __nv_bfloat16 h0 = __float2bfloat16_rn(x0);
-                        const __nv_bfloat16 h1 = __float2bfloat16_rn(x1);
-                        const __nv_bfloat16 l0 = __float2bfloat16_rn(x0 - __bfloat162float(h0));
-                        const __nv_bfloat16 l1 = __float2bfloat16_rn(x1 - __bfloat162float(h1));
-                        hw[jj / 2] = (uint32_t)__bfloat16_as_ushort(h0) |
-                                     ((uint32_t)__bfloat16_as_ushort(h1) << 16);
-                        lw[jj / 2] = (uint32_t)__bfloat16_as_ushort(l0) |
-                                     ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+                        const float x0 = x[8 * q + jj], x1 = x[8 * q + jj + 1];
+                        // (the low half of a bfloat162 is its first value)
+                        const __nv_bfloat162 h2 = __floats2bfloat162_rn(x0, x1);
+                        const float2 hf = __bfloat1622float2(h2);
+                        const __nv_bfloat162 l2 = __floats2bfloat162_rn(x0 - hf.x, x1 - hf.y);
+                        hw[jj / 2] = *reinterpret_cast<const uint32_t *>(&h2);
+                        lw[jj / 2] = *reinterpret_cast<const uint32_t *>(&l2);
                     }
-                    const uint32_t off = coff + (uint32_t)k8 * LBO;
-                    *reinterpret_cast<uint4 *>(bhi + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-                    *reinterpret_cast<uint4 *>(blo + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+                    const uint32_t off = coff + (uint32_t)(2 * h + q) * LBO;
+                    *reinterpret_cast<uint4 *>(stage + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+                    *reinterpret_cast<uint4 *>(stage + CHUNK16 + off) =
+                        make_uint4(lw[0], lw[1], lw[2], lw[3]);
                 }
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                bar_arrive(bar(BAR_EMPTY32 + s));
-                bar_arrive(bar(BAR_FULL16 + s2));
+                bar_arrive(bar(BAR_CONVERTED + s));
             }
         }
-    } else if (warp == 9) {
+    } else if (warp == WARP_MMA) {
         // ---- MMA issuer ----
         if (lane == 0) {
             const uint32_t idesc = idesc_bf16(TCOLS, npad);
@@ -340,14 +361,14 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
                 asm volatile("tcgen05.fence::after_thread_sync;");
                 const uint32_t d = tmem + (uint32_t)(bsel * npad);
                 for (int c = 0; c < nch; c++, j++) {
-                    const int s2 = (int)(j % S16);
-                    if (!bar_wait(bar(BAR_FULL16 + s2), (uint32_t)((j / S16) & 1), abort_flag,
+                    const int s2 = (int)(j % NS);
+                    if (!bar_wait(bar(BAR_CONVERTED + s2), (uint32_t)((j / NS) & 1), abort_flag,
                                   p.err, 5)) {
                         ok = false;
                         break;
                     }
                     asm volatile("tcgen05.fence::after_thread_sync;");
-                    const uint32_t bhi = sbase + L.b16 + (uint32_t)s2 * 2 * CHUNK16;
+                    const uint32_t bhi = sbase + L.ring + (uint32_t)s2 * CHUNK32;
 #pragma unroll
                     for (int ks = 0; ks < KC / 16; ks++) {
                         const uint32_t ko = (uint32_t)ks * 2 * LBO;
@@ -360,7 +381,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
                         umma(d, dl, oh, idesc, 1);
                         umma(d, dh, ol, idesc, 1);
                     }
-                    umma_commit(bar(BAR_EMPTY16 + s2));
+                    umma_commit(bar(BAR_FREE + s2));
                 }
                 if (!ok) break;
                 umma_commit(bar(BAR_ACCFULL + bsel));
@@ -372,19 +393,22 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
         __syncwarp();
     } else {
         // ---- epilogue: TMEM -> registers -> shared memory -> TMA store ----
-        // warp w holds columns 32w..32w+31 of the tile (its TMEM lanes)
+        // warp w reads TMEM lane quadrant w%4 (columns 32(w%4)..+31 of the
+        // tile); set h = w/4 takes the row groups g with g%2 == h.  The
+        // set's waits are collective (named barrier, then the abort flag)
+        // so that no warp of a set is left at a barrier the others skip.
+        const int quad = warp % 4, half = warp / 4;
+        const bool issuer = quad == 0 && lane == 0;
         int i = 0, sb = 0;
         for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
             const int bsel = i & 1;
-            if (!bar_wait(bar(BAR_ACCFULL + bsel), (i >> 1) & 1, abort_flag, p.err, 8)) break;
+            const bool ok = bar_wait(bar(BAR_ACCFULL + bsel), (i >> 1) & 1, abort_flag, p.err, 8);
+            asm volatile("bar.sync %0, %1;" :: "r"(EPI_BARRIER + half), "n"(128) : "memory");
+            if (!ok || *abort_flag) break;
             asm volatile("tcgen05.fence::after_thread_sync;");
-            const int64_t x0 = t * TCOLS + warp * 32;
-            // (a warp whose columns all lie past ncol has nothing to store,
-            // and must not touch its staging tiles: a store may still be
-            // reading them)
-            for (int g = 0; x0 < p.ncol && g < npad / 32; g++) {
+            for (int g = half; g < npad / 32; g += 2) {
                 uint32_t v[32];
-                const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) +
+                const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) +
                                        (uint32_t)(bsel * npad + g * 32);
                 asm volatile(
                     "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
@@ -399,25 +423,25 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
                     : "r"(taddr));
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 
-                // The store issued two stores ago from this buffer must
-                // have finished reading it
-                if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
-                __syncwarp();
-                float *buf = reinterpret_cast<float *>(smem + L.epi + (warp * 2 + sb) * EPI_BUF);
+                // The store issued EB stores ago from this staging tile
+                // must have finished reading it
+                if (issuer) asm volatile("cp.async.bulk.wait_group.read %0;" :: "n"(EB - 1) : "memory");
+                asm volatile("bar.sync %0, %1;" :: "r"(EPI_BARRIER + half), "n"(128) : "memory");
+                const uint32_t boff = L.epi + (uint32_t)(half * EB + sb) * EPI_BUF;
+                float *buf = reinterpret_cast<float *>(smem + boff) + quad * 32 + lane;
 #pragma unroll
-                for (int r = 0; r < 32; r++) buf[r * 32 + lane] = p.alpha * __uint_as_float(v[r]);
+                for (int r = 0; r < 32; r++) buf[r * TCOLS] = p.alpha * __uint_as_float(v[r]);
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                __syncwarp();
-                if (lane == 0)
-                    tma_store_2d(&p.cmap, sbase + L.epi + (warp * 2 + sb) * EPI_BUF, (int)x0,
-                                 g * 32, p.epi);
-                sb ^= 1;
+                asm volatile("bar.sync %0, %1;" :: "r"(EPI_BARRIER + half), "n"(128) : "memory");
+                // (columns past ncol are clipped by the TMA)
+                if (issuer) tma_store_2d(&p.cmap, sbase + boff, (int)(t * TCOLS), g * 32, p.epi);
+                sb = sb + 1 == EB ? 0 : sb + 1;
             }
             asm volatile("tcgen05.fence::before_thread_sync;");
             bar_arrive(bar(BAR_ACCEMPTY + bsel));
         }
-        // Every store issued by this warp has completed before exit
-        if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+        // Every store issued by this set has completed before exit
+        if (issuer) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
         __syncwarp();
     }
 
@@ -467,12 +491,12 @@ int encode_b_map(CUtensorMap *map, const float *b, int64_t ldb, int64_t ncol, in
     return B200_OK;
 }
 
-// Tensor map of out: dims (ncol, m), row stride ldc*4 bytes, box 32 x 32,
+// Tensor map of out: dims (ncol, m), row stride ldc*4 bytes, box TCOLS x 32,
 // dense row-major staging tiles
 int encode_c_map(CUtensorMap *map, float *c, int64_t ldc, int64_t ncol, int m) {
     cuuint64_t gdim[2] = {(cuuint64_t)ncol, (cuuint64_t)m};
     cuuint64_t gstride[1] = {(cuuint64_t)ldc * 4};
-    cuuint32_t box[2] = {32, 32};
+    cuuint32_t box[2] = {(cuuint32_t)TCOLS, 32};
     cuuint32_t estride[2] = {1, 1};
     CUresult r = g_encode_tiled(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)c, gdim, gstride,
                                 box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -492,23 +516,18 @@ int b200_mul_bf16x3_create(const double *a, int m, int k, void **handle, size_t 
     if (!a || !handle || m <= 0 || k <= 0)
         return b200::set_error(B200_ERR_ARG, "mul_bf16x3_create: bad arguments");
     const int npad = (m + 31) / 32 * 32, kfull = (k + KC - 1) / KC * KC;
-    // Two BF16 stages, then the deepest FP32 staging (bytes in flight per
-    // SM) that fits in shared memory; a third BF16 stage if room is left
-    int s32 = 0, s16 = 2;
-    Layout L = make_layout(npad, kfull, 2, 2);
-    for (int cand = MAX_S32; cand >= 2 && !s32; cand--) {
-        Layout c = make_layout(npad, kfull, cand, 2);
+    // The deepest ring (bytes in flight per SM) that fits in shared memory
+    int ns = 0;
+    Layout L = make_layout(npad, kfull, 2);
+    for (int cand = MAX_S; cand >= 3 && !ns; cand--) {
+        Layout c = make_layout(npad, kfull, cand);
         if (c.total <= 227 * 1024) {
-            s32 = cand;
+            ns = cand;
             L = c;
         }
     }
-    if (s32 == MAX_S32 && make_layout(npad, kfull, s32, 3).total <= 227 * 1024) {
-        s16 = 3;
-        L = make_layout(npad, kfull, s32, s16);
-    }
     if (smem_bytes) *smem_bytes = L.total;
-    if (npad > MAX_N || !s32 || L.total > 227 * 1024)
+    if (npad > MAX_N || !ns || L.total > 227 * 1024)
         return b200::set_error(B200_ERR_UNSUPPORTED,
                                "mul_bf16x3: operator %dx%d needs %u bytes of shared memory "
                                "(or more than %d rows)", m, k, L.total, MAX_N);
@@ -546,7 +565,7 @@ int b200_mul_bf16x3_create(const double *a, int m, int k, void **handle, size_t 
 
     UmmaHandle *h = (UmmaHandle *)calloc(1, sizeof(UmmaHandle));
     if (!h) return b200::set_error(B200_ERR_STATE, "mul_bf16x3_create: out of host memory");
-    h->m = m; h->k = k; h->npad = npad; h->kfull = kfull; h->s32 = s32; h->s16 = s16;
+    h->m = m; h->k = k; h->npad = npad; h->kfull = kfull; h->ns = ns;
     h->aimg_bytes = img.size() * 2;
     h->smem_bytes = L.total;
     int rc = b200::check_cuda(cudaMalloc(&h->aimg, h->aimg_bytes), "mul_bf16x3_create");
@@ -593,7 +612,7 @@ int b200_mul_bf16x3(void *handle, const float *b, int64_t ldb, float *c, int64_t
     if (!rc) rc = encode_c_map(&p.cmap, c, ldc, ncol, h->m);
     if (rc) return rc;
     p.aimg = h->aimg; p.ncol = ncol;
-    p.m = h->m; p.npad = h->npad; p.kfull = h->kfull; p.s32 = h->s32; p.s16 = h->s16;
+    p.m = h->m; p.npad = h->npad; p.kfull = h->kfull; p.ns = h->ns;
     p.alpha = alpha; p.epi = beta != 0.0f; p.err = err;
 
     const int64_t ntiles = (ncol + TCOLS - 1) / TCOLS;
