@@ -115,10 +115,15 @@ def kernel_bytes(k, be):
     kind = m.get('kind', k.name)
     itemsize = 8 if be.fpdtype == np.float64 else 4
     if k.name == 'mul':
+        # out = alpha*S*(A@B [+ A2@B2]) + beta*out over nbatch slices:
+        # read B (and B2), write out (and read it when beta = 1), read S
         a, b, out = m['a'], m['b'], m['out']
-        ncol = b.ncol
+        ncol, nb = b.ncol, m.get('nbatch', 1)
+        kin = a.ncol + (m['a2'].ncol if m.get('a2') is not None else 0)
         nout = a.nrow*ncol*(2 if m['beta'] else 1)
-        return (a.ncol*ncol + nout)*itemsize
+        rs = m.get('rowscale')
+        srows = rs.nrow*rs.ncol if rs is not None else 0
+        return (nb*(kin*ncol + nout) + srows)*itemsize
     if kind in ('tflux_ns', 'tflux_euler'):
         nupts, neles = m['dims']
         nd, nv = m['tplargs']['ndims'], m['tplargs']['nvars']
@@ -193,8 +198,12 @@ def make_form(form, args):
     prec = 'double' if form == 'plain' else 'single'
     cfg, mesh = ns_tgv(n=args.n, order=3, dt=args.dt, precision=prec)
     cfg.set('backend-b200', 'device-id', str(args.local_rank))
-    if form == 'chosen':
-        cfg.set('backend-b200', 'mul-precision', args.chosen_mul)
+    # The chosen form: split-BF16 operands with all four products; the
+    # three-product split is reported beside it
+    if form in ('chosen', 'bf16x3'):
+        cfg.set('backend-b200', 'mul-precision', 'bf16x3')
+        cfg.set('backend-b200', 'split-products',
+                str(args.chosen_products) if form == 'chosen' else '3')
     be = B200Backend(cfg)
     icls = RKVdH2Integrator if form == 'plain' else MixedRKIntegrator
     return icls(be, NavierStokesSystem, mesh, cfg)
@@ -352,7 +361,7 @@ def run_gpu(args, dist):
     del plain
 
     out = {'plain': rp}
-    forms = ['chosen', 'fp32'] if args.chosen else []
+    forms = ['chosen', 'bf16x3', 'fp32'] if args.chosen else []
     for form in forms:
         intg = make_form(form, args)
         rc = measure(intg, args, dist)
@@ -417,13 +426,13 @@ def main():
     ap.add_argument('--cpu-seconds', type=float, default=10.0)
     ap.add_argument('--no-chosen', dest='chosen', action='store_false',
                     help='skip the chosen precision form')
-    ap.add_argument('--chosen-mul', default='bf16x3',
-                    help='operator precision of the chosen form')
+    ap.add_argument('--chosen-products', type=int, default=4, choices=[3, 4],
+                    help='split-BF16 products of the chosen form')
     ap.add_argument('--accuracy-steps', type=int, default=200,
                     help='steps after which the chosen form is compared '
                          'with FP64')
     ap.add_argument('--ke-every', type=int, default=10)
-    ap.add_argument('--only', choices=['plain', 'chosen', 'fp32'],
+    ap.add_argument('--only', choices=['plain', 'chosen', 'bf16x3', 'fp32'],
                     help='time one precision form alone (no accuracy '
                          'history, end-to-end loop or CPU sample): the '
                          'command to run under a profiler')
@@ -493,13 +502,17 @@ def main():
 
     chosen = None
     labels = {
-        'chosen': f'operator contractions {args.chosen_mul} (split-BF16 x3 '
-                  'on tcgen05 tensor cores, FP32 accumulate), FP32 fluxes, '
-                  'FP64 RK accumulation',
+        'chosen': f'operator contractions split-BF16 hi/lo, '
+                  f'{args.chosen_products} products, on tcgen05 tensor cores '
+                  '(FP32 accumulate, fused applies), FP32 fluxes on the '
+                  'reference-state transform, FP64 RK accumulation',
+        'bf16x3': 'operator contractions split-BF16 hi/lo, 3 products '
+                  '(Ahi*Bhi + Ahi*Blo + Alo*Bhi) on tcgen05 tensor cores, '
+                  'otherwise as chosen',
         'fp32': 'operator contractions FP32 (sparse, CUDA cores), FP32 '
                 'fluxes, FP64 RK accumulation'}
     variants = {}
-    for form in ('chosen', 'fp32'):
+    for form in ('chosen', 'bf16x3', 'fp32'):
         if form not in allres:
             continue
         rc = allres[form]

@@ -110,6 +110,39 @@ int b200_mul_bf16x3_destroy(void *handle);
 int b200_mul_bf16x3(void *handle, const float *b, int64_t ldb, float *c, int64_t ldc,
                     int64_t ncol, float alpha, float beta, int *err, void *stream);
 
+/* Fused operator applies of the chosen form.  A handle made by _create_cat
+ * holds two operator blocks, m x k1 and m x k2 (both host, row-major), that
+ * act on two inputs, as one operator [A1 | A2] on B1 stacked over B2:
+ *     out_z = alpha * S (.) (A1 @ B1_z + A2 @ B2_z) + beta * out_z
+ * for the nbatch slices z (slice z of B1 starts bstride1 elements after
+ * slice z-1, likewise B2 and out).  S is an optional row scale read in the
+ * epilogue: S[r*ldr + e] for row r and element e of the column, the
+ * columns being an AoSoA field with nvars variables (slices: one).  This
+ * fuses, on the reference's NS graph: tgradpcoru_upts + tgradcoru_upts
+ * (pyfr/solvers/baseadvecdiff/elements.py:48-55, blocks M4-M6*M0 and M6),
+ * tdivtpcorf + tdivtconf + negdivconf (pyfr/solvers/baseadvec/elements.py:
+ * 91-120: blocks M1-M3*M2 and M3, alpha = -1, S = 1/|J|), and the ndims
+ * gradcoru_fpts products (pyfr/solvers/baseadvecdiff/elements.py:87-101,
+ * one handle, nbatch = ndims).  k2 = 0 makes a one-block handle. */
+typedef struct {
+    const float *b1, *b2;       /* b2 null for a one-block handle */
+    int64_t ldb1, ldb2;
+    float *c;
+    int64_t ldc, ncol;
+    int nbatch;                 /* >= 1 */
+    int64_t bstride1, bstride2, cstride;
+    float alpha, beta;          /* beta 0 or 1 */
+    const float *rowscale;      /* null: none */
+    int64_t ldr;
+    int nvars;
+    int products;               /* 3 (or 0): Ahi*Bhi + Ahi*Blo + Alo*Bhi;
+                                   4: plus Alo*Blo */
+    int *err;                   /* device int: pipeline timeout code */
+} b200_mul_bf16x3_args_t;
+int b200_mul_bf16x3_create_cat(const double *a1, int k1, const double *a2, int k2, int m,
+                                void **handle, size_t *smem_bytes);
+int b200_mul_bf16x3_apply(void *handle, const b200_mul_bf16x3_args_t *args, void *stream);
+
 /* ---- element pointwise kernels over [nupts, neles] ------------------- */
 /* Geometry: linear != 0 computes the metric terms from the element
  * vertices `verts` (nverts, ndims, neles) at the reference solution points

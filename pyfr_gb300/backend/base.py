@@ -110,6 +110,23 @@ class B200Backend:
         if self.mul_precision not in {'native', 'bf16x3'}:
             raise ValueError('mul-precision must be native or bf16x3')
 
+        # Split-BF16 products: 3 (Ahi Bhi + Ahi Blo + Alo Bhi) or 4 (plus
+        # Alo Blo)
+        self.split_products = cfg.getint('backend-b200', 'split-products', 3)
+        if self.split_products not in {3, 4}:
+            raise ValueError('split-products must be 3 or 4')
+
+        # Fused operator applies (mul_cat, mul_batched): the tensor-core
+        # provider serves them, so by default they follow mul-precision
+        fuse = cfg.get('backend-b200', 'fuse-operators', 'auto')
+        if fuse not in {'auto', 'true', 'false'}:
+            raise ValueError('fuse-operators must be auto, true or false')
+        tensor = self.mul_precision == 'bf16x3' and self.fpdtype == np.float32
+        if fuse == 'true' and not tensor:
+            raise ValueError('fuse-operators needs single precision with '
+                             'mul-precision = bf16x3')
+        self.fuse_operators = tensor and fuse != 'false'
+
         self.mats = WeakValueDictionary()
         self._mat_counter = it.count()
         self._extents = {}

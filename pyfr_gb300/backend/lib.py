@@ -21,6 +21,19 @@ class B200Error(RuntimeError):
     pass
 
 
+class MulArgs(C.Structure):
+    """``b200_mul_bf16x3_args_t``"""
+    _fields_ = [('b1', C.c_void_p), ('b2', C.c_void_p),
+                ('ldb1', C.c_int64), ('ldb2', C.c_int64),
+                ('c', C.c_void_p), ('ldc', C.c_int64), ('ncol', C.c_int64),
+                ('nbatch', C.c_int), ('bstride1', C.c_int64),
+                ('bstride2', C.c_int64), ('cstride', C.c_int64),
+                ('alpha', C.c_float), ('beta', C.c_float),
+                ('rowscale', C.c_void_p), ('ldr', C.c_int64),
+                ('nvars', C.c_int), ('products', C.c_int),
+                ('err', C.c_void_p)]
+
+
 class Gas(C.Structure):
     _fields_ = [('gamma', f64), ('mu', f64), ('pr', f64), ('cpTref', f64),
                 ('cpTs', f64), ('sutherland', i32), ('shifted', i32),
@@ -91,6 +104,9 @@ _SIGS = {
     'b200_mul_bf16x3_create': [pd, i32, i32, C.POINTER(vp), C.POINTER(sz)],
     'b200_mul_bf16x3_destroy': [vp],
     'b200_mul_bf16x3': [vp, vp, i64, vp, i64, i64, f32, f32, vp, vp],
+    'b200_mul_bf16x3_create_cat': [pd, i32, pd, i32, i32, C.POINTER(vp),
+                                   C.POINTER(sz)],
+    'b200_mul_bf16x3_apply': [vp, C.c_void_p, vp],
 }
 
 for _fp, _suf in ((f64, 'f64'), (f32, 'f32')):

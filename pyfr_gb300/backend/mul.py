@@ -9,6 +9,7 @@ raises NotSuitableError so that the backend tries the next one
 * ``TensorMulKernels``: split-BF16 (three products) tcgen05 kernel for
   single-precision data, selected by ``[backend-b200] mul-precision =
   bf16x3``; declines operators whose tiles do not fit in shared memory.
+  It also provides the fused ``mul_cat`` and ``mul_batched`` forms.
 * ``MulKernels``: sparse (CSR) kernel in the backend's precision, FP64 or
   FP32; always suitable.
 
@@ -21,7 +22,7 @@ import weakref
 
 import numpy as np
 
-from pyfr_gb300.backend.lib import B200Error
+from pyfr_gb300.backend.lib import B200Error, MulArgs
 from pyfr_gb300.backend.types import Kernel
 
 
@@ -85,6 +86,17 @@ class MulKernels:
 
 
 class TensorMulKernels:
+    """Split-BF16 tcgen05 operator applies (``mul``) plus the fused forms
+    the Navier-Stokes graph uses in the chosen precision form:
+
+    * ``mul_cat(a1, b1, a2, b2, out, alpha, beta, rowscale)``:
+      out = alpha*S*(a1@b1 + a2@b2) + beta*out with S the optional
+      per-(row, element) scale ``rowscale`` (an (m, neles) matrix);
+    * ``mul_batched(a, b, out, nbatch)``: out_z = a@b_z over nbatch equal
+      row slices of b and out.
+
+    Operator data is uploaded once per operator (or operator pair)."""
+
     def __init__(self, backend):
         from pyfr_gb300.backend.base import release
         self.backend = backend
@@ -92,48 +104,129 @@ class TensorMulKernels:
         weakref.finalize(self, release, _destroy_handles,
                          backend.lib.mul_bf16x3_destroy, self._handles)
 
-    def _handle(self, a):
-        from pyfr_gb300.backend.base import NotSuitableError
-
-        key = a.mid
-        if key not in self._handles:
-            host = np.ascontiguousarray(a._host, dtype=np.float64)
-            h, smem = C.c_void_p(), C.c_size_t()
-            try:
-                self.backend.lib.mul_bf16x3_create(
-                    host.ctypes.data_as(C.POINTER(C.c_double)), host.shape[0],
-                    host.shape[1], C.byref(h), C.byref(smem))
-            except B200Error:
-                self._handles[key] = None
-            else:
-                self._handles[key] = (h.value, smem.value, host)
-
-        if self._handles[key] is None:
-            raise NotSuitableError('operator too large for the tensor tiles')
-        return self._handles[key]
-
-    def mul(self, a, b, out, alpha=1.0, beta=0.0):
+    def _suitable(self):
         from pyfr_gb300.backend.base import NotSuitableError
 
         be = self.backend
         if be.fpdtype != np.float32 or be.mul_precision != 'bf16x3':
             raise NotSuitableError('tensor-core mul serves bf16x3 FP32 data')
+
+    def _handle(self, *ops):
+        from pyfr_gb300.backend.base import NotSuitableError
+
+        key = tuple(a.mid for a in ops)
+        if key not in self._handles:
+            hosts = [np.ascontiguousarray(a._host, dtype=np.float64)
+                     for a in ops]
+            a1 = hosts[0]
+            a2 = hosts[1] if len(hosts) > 1 else None
+            h, smem = C.c_void_p(), C.c_size_t()
+            pd = C.POINTER(C.c_double)
+            try:
+                self.backend.lib.mul_bf16x3_create_cat(
+                    a1.ctypes.data_as(pd), a1.shape[1],
+                    a2.ctypes.data_as(pd) if a2 is not None else None,
+                    a2.shape[1] if a2 is not None else 0, a1.shape[0],
+                    C.byref(h), C.byref(smem))
+            except B200Error:
+                self._handles[key] = None
+            else:
+                self._handles[key] = (h.value, smem.value, hosts)
+
+        if self._handles[key] is None:
+            raise NotSuitableError('operator too large for the tensor tiles')
+        return self._handles[key]
+
+    @staticmethod
+    def _aligned(*mats):
+        return all(m.leaddim % 4 == 0 for m in mats)
+
+    def _kernel(self, handle, args, mats, meta):
+        be = self.backend
+        args.err = be.status_word
+        args.products = be.split_products
+        meta['products'] = be.split_products
+        fn = be.lib.mul_bf16x3_apply
+        pa = C.addressof(args)
+
+        def run(stream):
+            fn(handle, pa, stream)
+
+        k = Kernel(run, mats=mats, name='mul', meta=meta)
+        k._args = args
+        return k
+
+    def mul(self, a, b, out, alpha=1.0, beta=0.0):
+        from pyfr_gb300.backend.base import NotSuitableError
+
+        self._suitable()
         _check_shapes(a, b, out)
-        if b.leaddim % 4 or out.leaddim % 4 or b.ncol % 4:
+        if not self._aligned(b, out) or b.ncol % 4:
             raise NotSuitableError('unaligned operands')
         if beta not in (0.0, 1.0):
             raise NotSuitableError('the tensor-core epilogue stores or adds')
 
-        h, smem, host = self._handle(a)
-        ncol, ldb, ldc = b.ncol, b.leaddim, out.leaddim
-        al, bt = C.c_float(alpha), C.c_float(beta)
-        bp, cp = b.data, out.data
-        err = be.status_word
-        fn = be.lib.mul_bf16x3
+        h, smem, (host,) = self._handle(a)
+        args = MulArgs(b1=b.data, ldb1=b.leaddim, c=out.data, ldc=out.leaddim,
+                       ncol=b.ncol, nbatch=1, alpha=alpha, beta=beta)
+        return self._kernel(h, args, [a, b, out],
+                            dict(a=a, b=b, out=out, alpha=alpha, beta=beta,
+                                 op=host, impl='bf16x3', smem=smem))
 
-        def run(stream):
-            fn(h, bp, ldb, cp, ldc, ncol, al, bt, err, stream)
+    def mul_cat(self, a1, b1, a2, b2, out, alpha=1.0, beta=0.0,
+                rowscale=None):
+        from pyfr_gb300.backend.base import NotSuitableError
 
-        return Kernel(run, mats=[a, b, out], name='mul',
-                      meta=dict(a=a, b=b, out=out, alpha=alpha, beta=beta,
-                                op=host, impl='bf16x3', smem=smem))
+        self._suitable()
+        _check_shapes(a1, b1, out)
+        _check_shapes(a2, b2, out)
+        if b1.ncol != b2.ncol:
+            raise ValueError('Incompatible matrices for out = a1*b1 + a2*b2')
+        if not self._aligned(b1, b2, out) or b1.ncol % 4:
+            raise NotSuitableError('unaligned operands')
+        if beta not in (0.0, 1.0):
+            raise NotSuitableError('the tensor-core epilogue stores or adds')
+        nvars = ldr = 0
+        if rowscale is not None:
+            if len(out.ioshape) != 3 or rowscale.nrow != out.nrow:
+                raise ValueError('A row scale needs an (nrow, nvars, neles) '
+                                 'output and one row per output row')
+            nvars, ldr = out.ioshape[1], rowscale.leaddim
+            if rowscale.dtype != np.float32:
+                raise ValueError('The row scale must be FP32')
+
+        h, smem, (h1, h2) = self._handle(a1, a2)
+        args = MulArgs(b1=b1.data, ldb1=b1.leaddim, b2=b2.data,
+                       ldb2=b2.leaddim, c=out.data, ldc=out.leaddim,
+                       ncol=b1.ncol, nbatch=1, alpha=alpha, beta=beta,
+                       rowscale=rowscale.data if rowscale is not None else None,
+                       ldr=ldr, nvars=nvars)
+        mats = [a1, b1, a2, b2, out] + ([rowscale] if rowscale is not None else [])
+        return self._kernel(h, args, mats,
+                            dict(a=a1, b=b1, a2=a2, b2=b2, out=out,
+                                 alpha=alpha, beta=beta, op=h1, op2=h2,
+                                 rowscale=rowscale, impl='bf16x3-cat',
+                                 smem=smem))
+
+    def mul_batched(self, a, b, out, nbatch, alpha=1.0, beta=0.0):
+        from pyfr_gb300.backend.base import NotSuitableError
+
+        self._suitable()
+        m, k = a.nrow, a.ncol
+        if b.nrow != nbatch*k or out.nrow != nbatch*m or b.ncol != out.ncol:
+            raise ValueError('Incompatible matrices for batched out = a*b')
+        if 'const' not in a.tags:
+            raise ValueError('The operator of mul must be a constant matrix')
+        if not self._aligned(b, out) or b.ncol % 4:
+            raise NotSuitableError('unaligned operands')
+        if beta not in (0.0, 1.0):
+            raise NotSuitableError('the tensor-core epilogue stores or adds')
+
+        h, smem, (host,) = self._handle(a)
+        args = MulArgs(b1=b.data, ldb1=b.leaddim, c=out.data, ldc=out.leaddim,
+                       ncol=b.ncol, nbatch=nbatch, bstride1=k*b.leaddim,
+                       cstride=m*out.leaddim, alpha=alpha, beta=beta)
+        return self._kernel(h, args, [a, b, out],
+                            dict(a=a, b=b, out=out, alpha=alpha, beta=beta,
+                                 op=host, nbatch=nbatch,
+                                 impl='bf16x3-batched', smem=smem))

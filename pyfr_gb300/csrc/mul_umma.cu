@@ -2,9 +2,17 @@
 //     out = alpha * A @ B + beta * out        (FP32 in, FP32 out, beta 0 or 1)
 // with A = Ahi + Alo and B = Bhi + Blo split into BF16 halves and the
 // product formed as Ahi*Bhi + Ahi*Blo + Alo*Bhi (three tcgen05.mma per K
-// step, FP32 accumulation in tensor memory).  This is the chosen-precision
+// step, FP32 accumulation in tensor memory), or with Alo*Blo as a fourth
+// product (the exact product of the split operands).  This is the chosen-precision
 // replacement of the reference's `mul` providers
 // (pyfr/backends/cuda/gimmik.py:23-121, pyfr/backends/cuda/cublaslt.py:169-280).
+//
+// The general form (b200_mul_bf16x3_apply) fuses what the reference runs
+// as separate kernels:
+//     out_z = alpha * S (.) (A1 @ B1_z + A2 @ B2_z) + beta * out_z
+// with a second operator block A2 on a second input B2 (concatenated along
+// K), z over nbatch equally strided slices of B and out, and S an optional
+// per-(row, element) scale read in the epilogue.
 //
 // Orientation: the streamed data is the M side of the MMA.  One
 // tcgen05.mma forms D[128 x N] += B^T[128 x 16] A^T[16 x N] for 128 columns
@@ -57,7 +65,7 @@ constexpr int CONV_BARRIER = 1;   // named barrier of the converter warps
 constexpr int EPI_BARRIER = 2;    // named barriers 2, 3: the epilogue sets
 constexpr int MAX_N = 256;        // UMMA N limit (operator rows, padded)
 constexpr int MAX_S = 10;         // ring stages (bytes in flight)
-constexpr int EB = 2;             // staging tiles per epilogue set
+constexpr int MAX_EB = 2;         // staging tiles per epilogue set (1 when short of room)
 constexpr long long WAIT_LIMIT = 1LL << 22;
 
 constexpr uint32_t CHUNK32 = KC * TCOLS * 4;       // 16 KB FP32 chunk (one stage)
@@ -66,7 +74,7 @@ constexpr uint32_t SBO_CHUNK = KC * 16;            // 8-row group stride of a ch
 constexpr uint32_t EPI_BUF = 32 * TCOLS * 4;       // one 32-row x 128-column staging tile
 
 struct UmmaHandle {
-    int m, k, npad, kfull, ns;
+    int m, k1, k2, nch1, npad, kfull, ns, eb;
     unsigned char *aimg;   // device: [hi | lo], each npad x kfull bf16 canonical
     size_t aimg_bytes;
     size_t smem_bytes;
@@ -78,11 +86,11 @@ struct Layout {
     uint32_t a_hi, a_lo;
     uint32_t ring;                // stage s at ring + s*CHUNK32: FP32 chunk, then
                                   // BF16 hi (first 8 KB) and lo (second 8 KB)
-    uint32_t epi;                 // staging tile b of set h at epi + (h*EB + b)*EPI_BUF
+    uint32_t epi;                 // staging tile b of set h at epi + (h*eb + b)*EPI_BUF
     uint32_t bar, tslot, abort_flag, total;
 };
 
-__host__ __device__ inline Layout make_layout(int npad, int kfull, int ns) {
+__host__ __device__ inline Layout make_layout(int npad, int kfull, int ns, int eb) {
     Layout L;
     uint32_t off = 0;
     const uint32_t abytes = (uint32_t)npad * kfull * 2;
@@ -90,7 +98,7 @@ __host__ __device__ inline Layout make_layout(int npad, int kfull, int ns) {
     L.a_lo = off; off += abytes;
     off = (off + 1023) & ~1023u;
     L.ring = off; off += ns * CHUNK32;
-    L.epi = off; off += 2 * EB * EPI_BUF;
+    L.epi = off; off += 2 * eb * EPI_BUF;
     L.bar = off; off += 40 * 8;
     L.tslot = off; off += 8;
     L.abort_flag = off; off += 8;
@@ -183,44 +191,47 @@ __device__ __forceinline__ void umma_commit(uint32_t bar) {
                  :: "r"(bar) : "memory");
 }
 
-// One 2-D TMA load of a KC-row x TCOLS-column box of B into a dense FP32
-// staging buffer (rows past k and columns past ncol are zero-filled)
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y,
-                                            uint32_t bar) {
-    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-                 " [%0], [%1, {%2, %3}], [%4];"
-                 :: "r"(dst), "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar) : "memory");
+// One 3-D TMA load of a KC-row x TCOLS-column box of slice z of B into a
+// dense FP32 staging buffer (rows past k and columns past ncol are
+// zero-filled)
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, int x, int y,
+                                            int z, uint32_t bar) {
+    asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                 " [%0], [%1, {%2, %3, %4}], [%5];"
+                 :: "r"(dst), "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(bar) : "memory");
 }
 
 // Store (or add, for beta = 1) a 32-row x 128-column FP32 tile from dense
-// row-major shared memory into out through the tensor map of out
-__device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, uint32_t src, int x, int y,
-                                             int add) {
+// row-major shared memory into slice z of out through the tensor map of out
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap *map, uint32_t src, int x, int y,
+                                             int z, int add) {
     if (add)
-        asm volatile("cp.reduce.async.bulk.tensor.2d.global.shared::cta.add.tile.bulk_group"
-                     " [%0, {%1, %2}], [%3];"
-                     :: "l"((uint64_t)map), "r"(x), "r"(y), "r"(src) : "memory");
+        asm volatile("cp.reduce.async.bulk.tensor.3d.global.shared::cta.add.tile.bulk_group"
+                     " [%0, {%1, %2, %3}], [%4];"
+                     :: "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(src) : "memory");
     else
-        asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.tile.bulk_group"
-                     " [%0, {%1, %2}], [%3];"
-                     :: "l"((uint64_t)map), "r"(x), "r"(y), "r"(src) : "memory");
+        asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group"
+                     " [%0, {%1, %2, %3}], [%4];"
+                     :: "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(src) : "memory");
     asm volatile("cp.async.bulk.commit_group;" ::: "memory");
 }
 
 struct UmmaArgs {
-    CUtensorMap tmap;           // B as a (k x ncol) FP32 tensor, box TCOLS x KC
-    CUtensorMap cmap;           // out as a (m x ncol) FP32 tensor, box TCOLS x 32
+    CUtensorMap tmap[2];        // B1, B2 as (nbatch x k_i x ncol) FP32 tensors, box TCOLS x KC x 1
+    CUtensorMap cmap;           // out as a (nbatch x m x ncol) FP32 tensor, box TCOLS x 32 x 1
     const unsigned char *aimg;
-    int64_t ncol;
-    int m, npad, kfull, ns;
+    const float *rs;            // row scale S (null: none), S[row*ldr + element]
+    int64_t ncol, ntc, ldr;     // ntc: column tiles per slice
+    int m, npad, kfull, nch1, ns, eb, nbatch, nvars, products;
     float alpha;
-    int epi;            // 0: store alpha*D, 1: add alpha*D to out
+    int epi;            // 0: store, 1: add to out
     int *err;
 };
 
 __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_constant__ UmmaArgs p) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    const Layout L = make_layout(p.npad, p.kfull, p.ns);
+    const Layout L = make_layout(p.npad, p.kfull, p.ns, p.eb);
+    const int eb = p.eb;
     const int NS = p.ns;
     const uint32_t sbase = smem_addr(smem);
     const uint32_t bar0 = sbase + L.bar;
@@ -229,7 +240,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
     uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + L.tslot);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int64_t ntiles = (p.ncol + TCOLS - 1) / TCOLS;
+    // tile T covers columns (T % ntc)*TCOLS.. of slice T / ntc
+    const int64_t ntiles = p.ntc * p.nbatch;
     const int npad = p.npad, nch = p.kfull / KC;
     const uint32_t tcols = 2 * npad <= 32 ? 32 : (2 * npad <= 64 ? 64 :
                           (2 * npad <= 128 ? 128 : (2 * npad <= 256 ? 256 : 512)));
@@ -286,9 +298,12 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
                         ok = false;
                         break;
                     }
+                    // chunks of the first block, then of the second
+                    const int src = c < p.nch1 ? 0 : 1;
                     bar_arrive_tx(bar(BAR_LOADED + s), CHUNK32);
-                    tma_load_2d(sbase + L.ring + (uint32_t)s * CHUNK32, &p.tmap, (int)(t * TCOLS),
-                                c * KC, bar(BAR_LOADED + s));
+                    tma_load_3d(sbase + L.ring + (uint32_t)s * CHUNK32, &p.tmap[src],
+                                (int)((t % p.ntc) * TCOLS), (src ? c - p.nch1 : c) * KC,
+                                (int)(t / p.ntc), bar(BAR_LOADED + s));
                 }
                 if (!ok) break;
             }
@@ -380,6 +395,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
                         umma(d, dh, oh, idesc, (c | ks) != 0);
                         umma(d, dl, oh, idesc, 1);
                         umma(d, dh, ol, idesc, 1);
+                        if (p.products == 4) umma(d, dl, ol, idesc, 1);
                     }
                     umma_commit(bar(BAR_FREE + s2));
                 }
@@ -406,7 +422,24 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
             asm volatile("bar.sync %0, %1;" :: "r"(EPI_BARRIER + half), "n"(128) : "memory");
             if (!ok || *abort_flag) break;
             asm volatile("tcgen05.fence::after_thread_sync;");
+            const int64_t x0 = (t % p.ntc) * TCOLS;
+            const int z = (int)(t / p.ntc);
+            // Element of this thread's column (AoSoA: blocks of 32 elements
+            // with the variables of a block contiguous), for the row scale
+            const int64_t col = x0 + quad * 32 + lane;
+            const int64_t ele = (col / (32 * p.nvars)) * 32 + col % 32;
             for (int g = half; g < npad / 32; g += 2) {
+                float f[32];
+                if (p.rs) {
+#pragma unroll
+                    for (int r = 0; r < 32; r++)
+                        f[r] = col < p.ncol && g * 32 + r < p.m
+                                   ? p.alpha * __ldg(p.rs + (int64_t)(g * 32 + r) * p.ldr + ele)
+                                   : 0.f;
+                } else {
+#pragma unroll
+                    for (int r = 0; r < 32; r++) f[r] = p.alpha;
+                }
                 uint32_t v[32];
                 const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) +
                                        (uint32_t)(bsel * npad + g * 32);
@@ -423,19 +456,24 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
                     : "r"(taddr));
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 
-                // The store issued EB stores ago from this staging tile
+                // The store issued eb stores ago from this staging tile
                 // must have finished reading it
-                if (issuer) asm volatile("cp.async.bulk.wait_group.read %0;" :: "n"(EB - 1) : "memory");
+                if (issuer) {
+                    if (eb == 2)
+                        asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+                    else
+                        asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+                }
                 asm volatile("bar.sync %0, %1;" :: "r"(EPI_BARRIER + half), "n"(128) : "memory");
-                const uint32_t boff = L.epi + (uint32_t)(half * EB + sb) * EPI_BUF;
+                const uint32_t boff = L.epi + (uint32_t)(half * eb + sb) * EPI_BUF;
                 float *buf = reinterpret_cast<float *>(smem + boff) + quad * 32 + lane;
 #pragma unroll
-                for (int r = 0; r < 32; r++) buf[r * TCOLS] = p.alpha * __uint_as_float(v[r]);
+                for (int r = 0; r < 32; r++) buf[r * TCOLS] = f[r] * __uint_as_float(v[r]);
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 asm volatile("bar.sync %0, %1;" :: "r"(EPI_BARRIER + half), "n"(128) : "memory");
                 // (columns past ncol are clipped by the TMA)
-                if (issuer) tma_store_2d(&p.cmap, sbase + boff, (int)(t * TCOLS), g * 32, p.epi);
-                sb = sb + 1 == EB ? 0 : sb + 1;
+                if (issuer) tma_store_3d(&p.cmap, sbase + boff, (int)x0, g * 32, z, p.epi);
+                sb = sb + 1 == eb ? 0 : sb + 1;
             }
             asm volatile("tcgen05.fence::before_thread_sync;");
             bar_arrive(bar(BAR_ACCEMPTY + bsel));
@@ -453,16 +491,17 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
                      :: "r"(tmem), "r"(tcols));
 }
 
-// Host: split A into BF16 hi/lo and lay both out in the canonical K-major
-// no-swizzle layout ((r/8)*SBO + (k/8)*128 + (r%8)*16 + (k%8)*2 bytes,
-// SBO = kfull*16); rows past m and columns past k are zero.
-void build_image(const double *a, int m, int k, int npad, int kfull, std::vector<uint16_t> &img) {
-    const size_t n = (size_t)npad * kfull;
-    img.assign(2 * n, 0);
+// Host: split [A1 | A2] into BF16 hi/lo and lay both out in the canonical
+// K-major no-swizzle layout ((r/8)*SBO + (k/8)*128 + (r%8)*16 + (k%8)*2
+// bytes, SBO = kfull*16), A2's columns starting at column k2off (a chunk
+// boundary); rows past m and the padding columns are zero.
+void build_block(const double *a, int m, int k, int koff, int kfull, size_t n,
+                 std::vector<uint16_t> &img) {
     const size_t SBO = (size_t)kfull * 16;
     for (int r = 0; r < m; r++)
-        for (int c = 0; c < k; c++) {
-            const float x = (float)a[(size_t)r * k + c];
+        for (int c0 = 0; c0 < k; c0++) {
+            const int c = koff + c0;
+            const float x = (float)a[(size_t)r * k + c0];
             const __nv_bfloat16 h = __float2bfloat16_rn(x);
             const __nv_bfloat16 l = __float2bfloat16_rn(x - __bfloat162float(h));
             const size_t off = (r / 8) * SBO + (c / 8) * 128 + (r % 8) * 16 + (c % 8) * 2;
@@ -474,14 +513,16 @@ void build_image(const double *a, int m, int k, int npad, int kfull, std::vector
 int g_sm_count = 0;
 PFN_cuTensorMapEncodeTiled_v12000 g_encode_tiled = nullptr;
 
-// Tensor map of B: rank 2, dims (ncol, k) innermost first, row stride
-// ldb*4 bytes, box (TCOLS, KC), no swizzle, out-of-range elements read as 0
-int encode_b_map(CUtensorMap *map, const float *b, int64_t ldb, int64_t ncol, int k) {
-    cuuint64_t gdim[2] = {(cuuint64_t)ncol, (cuuint64_t)k};
-    cuuint64_t gstride[1] = {(cuuint64_t)ldb * 4};
-    cuuint32_t box[2] = {(cuuint32_t)TCOLS, (cuuint32_t)KC};
-    cuuint32_t estride[2] = {1, 1};
-    CUresult r = g_encode_tiled(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)b, gdim, gstride,
+// Tensor map of B: rank 3, dims (ncol, k, nbatch) innermost first, row
+// stride ldb*4 bytes, slice stride bs*4 bytes, box (TCOLS, KC, 1), no
+// swizzle, out-of-range elements read as 0
+int encode_b_map(CUtensorMap *map, const float *b, int64_t ldb, int64_t ncol, int k, int nbatch,
+                 int64_t bs) {
+    cuuint64_t gdim[3] = {(cuuint64_t)ncol, (cuuint64_t)k, (cuuint64_t)nbatch};
+    cuuint64_t gstride[2] = {(cuuint64_t)ldb * 4, (cuuint64_t)bs * 4};
+    cuuint32_t box[3] = {(cuuint32_t)TCOLS, (cuuint32_t)KC, 1};
+    cuuint32_t estride[3] = {1, 1, 1};
+    CUresult r = g_encode_tiled(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void *)b, gdim, gstride,
                                 box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
                                 CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -491,14 +532,15 @@ int encode_b_map(CUtensorMap *map, const float *b, int64_t ldb, int64_t ncol, in
     return B200_OK;
 }
 
-// Tensor map of out: dims (ncol, m), row stride ldc*4 bytes, box TCOLS x 32,
-// dense row-major staging tiles
-int encode_c_map(CUtensorMap *map, float *c, int64_t ldc, int64_t ncol, int m) {
-    cuuint64_t gdim[2] = {(cuuint64_t)ncol, (cuuint64_t)m};
-    cuuint64_t gstride[1] = {(cuuint64_t)ldc * 4};
-    cuuint32_t box[2] = {(cuuint32_t)TCOLS, 32};
-    cuuint32_t estride[2] = {1, 1};
-    CUresult r = g_encode_tiled(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)c, gdim, gstride,
+// Tensor map of out: dims (ncol, m, nbatch), row stride ldc*4 bytes, slice
+// stride cs*4 bytes, box (TCOLS, 32, 1), dense row-major staging tiles
+int encode_c_map(CUtensorMap *map, float *c, int64_t ldc, int64_t ncol, int m, int nbatch,
+                 int64_t cs) {
+    cuuint64_t gdim[3] = {(cuuint64_t)ncol, (cuuint64_t)m, (cuuint64_t)nbatch};
+    cuuint64_t gstride[2] = {(cuuint64_t)ldc * 4, (cuuint64_t)cs * 4};
+    cuuint32_t box[3] = {(cuuint32_t)TCOLS, 32, 1};
+    cuuint32_t estride[3] = {1, 1, 1};
+    CUresult r = g_encode_tiled(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void *)c, gdim, gstride,
                                 box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
                                 CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -512,25 +554,34 @@ int encode_c_map(CUtensorMap *map, float *c, int64_t ldc, int64_t ncol, int m) {
 
 extern "C" {
 
-int b200_mul_bf16x3_create(const double *a, int m, int k, void **handle, size_t *smem_bytes) {
-    if (!a || !handle || m <= 0 || k <= 0)
+int b200_mul_bf16x3_create_cat(const double *a1, int k1, const double *a2, int k2, int m,
+                                void **handle, size_t *smem_bytes) {
+    if (!a1 || !handle || m <= 0 || k1 <= 0 || k2 < 0 || (k2 > 0 && !a2))
         return b200::set_error(B200_ERR_ARG, "mul_bf16x3_create: bad arguments");
-    const int npad = (m + 31) / 32 * 32, kfull = (k + KC - 1) / KC * KC;
+    const int nch1 = (k1 + KC - 1) / KC, nch2 = (k2 + KC - 1) / KC;
+    const int npad = (m + 31) / 32 * 32, kfull = (nch1 + nch2) * KC;
     // The deepest ring (bytes in flight per SM) that fits in shared memory
-    int ns = 0;
-    Layout L = make_layout(npad, kfull, 2);
-    for (int cand = MAX_S; cand >= 3 && !ns; cand--) {
-        Layout c = make_layout(npad, kfull, cand);
-        if (c.total <= 227 * 1024) {
-            ns = cand;
-            L = c;
+    // with two staging tiles per epilogue set, or failing four stages that
+    // way, with one
+    int ns = 0, eb = MAX_EB;
+    Layout L = make_layout(npad, kfull, 2, eb);
+    for (; eb >= 1 && ns < 4; eb--) {
+        ns = 0;
+        for (int cand = MAX_S; cand >= 3 && !ns; cand--) {
+            Layout c = make_layout(npad, kfull, cand, eb);
+            if (c.total <= 227 * 1024) {
+                ns = cand;
+                L = c;
+            }
         }
+        if (ns >= 4) break;
     }
+    if (eb < 1) eb = 1;
     if (smem_bytes) *smem_bytes = L.total;
     if (npad > MAX_N || !ns || L.total > 227 * 1024)
         return b200::set_error(B200_ERR_UNSUPPORTED,
-                               "mul_bf16x3: operator %dx%d needs %u bytes of shared memory "
-                               "(or more than %d rows)", m, k, L.total, MAX_N);
+                               "mul_bf16x3: operator %dx(%d+%d) needs %u bytes of shared memory "
+                               "(or more than %d rows)", m, k1, k2, L.total, MAX_N);
 
     // One-time device set-up here rather than at launch: changing a
     // function attribute while a stream capture is open invalidates it
@@ -560,12 +611,15 @@ int b200_mul_bf16x3_create(const double *a, int m, int k, void **handle, size_t 
         g_sm_count = sms;
     }
 
-    std::vector<uint16_t> img;
-    build_image(a, m, k, npad, kfull, img);
+    const size_t n = (size_t)npad * kfull;
+    std::vector<uint16_t> img(2 * n, 0);
+    build_block(a1, m, k1, 0, kfull, n, img);
+    if (k2) build_block(a2, m, k2, nch1 * KC, kfull, n, img);
 
     UmmaHandle *h = (UmmaHandle *)calloc(1, sizeof(UmmaHandle));
     if (!h) return b200::set_error(B200_ERR_STATE, "mul_bf16x3_create: out of host memory");
-    h->m = m; h->k = k; h->npad = npad; h->kfull = kfull; h->ns = ns;
+    h->m = m; h->k1 = k1; h->k2 = k2; h->nch1 = nch1; h->npad = npad; h->kfull = kfull;
+    h->ns = ns; h->eb = eb;
     h->aimg_bytes = img.size() * 2;
     h->smem_bytes = L.total;
     int rc = b200::check_cuda(cudaMalloc(&h->aimg, h->aimg_bytes), "mul_bf16x3_create");
@@ -581,6 +635,10 @@ int b200_mul_bf16x3_create(const double *a, int m, int k, void **handle, size_t 
     return B200_OK;
 }
 
+int b200_mul_bf16x3_create(const double *a, int m, int k, void **handle, size_t *smem_bytes) {
+    return b200_mul_bf16x3_create_cat(a, k, nullptr, 0, m, handle, smem_bytes);
+}
+
 int b200_mul_bf16x3_destroy(void *handle) {
     if (!handle) return B200_OK;
     UmmaHandle *h = (UmmaHandle *)handle;
@@ -589,37 +647,69 @@ int b200_mul_bf16x3_destroy(void *handle) {
     return B200_OK;
 }
 
-int b200_mul_bf16x3(void *handle, const float *b, int64_t ldb, float *c, int64_t ldc,
-                    int64_t ncol, float alpha, float beta, int *err, void *stream) {
+int b200_mul_bf16x3_apply(void *handle, const b200_mul_bf16x3_args_t *a, void *stream) {
     UmmaHandle *h = (UmmaHandle *)handle;
-    if (!h || !err) return b200::set_error(B200_ERR_ARG, "mul_bf16x3: null handle/status");
-    if (ncol <= 0) return B200_OK;
-    if (ldb < ncol || ldc < ncol)
+    if (!h || !a || !a->err) return b200::set_error(B200_ERR_ARG, "mul_bf16x3: null handle/args");
+    if (a->ncol <= 0 || a->nbatch == 0) return B200_OK;
+    if (a->nbatch < 0 || !a->b1 || !a->c || (h->k2 && !a->b2))
+        return b200::set_error(B200_ERR_ARG, "mul_bf16x3: bad arguments");
+    if (a->ldb1 < a->ncol || a->ldc < a->ncol || (h->k2 && a->ldb2 < a->ncol))
         return b200::set_error(B200_ERR_ARG, "mul_bf16x3: leading dimension smaller than ncol");
-    // Tensor maps need 16-byte aligned bases and row strides; tiles start
-    // at multiples of 32 columns (128 bytes)
-    if ((((uintptr_t)b) & 15) || (((uintptr_t)c) & 15) || (ldb % 4) || (ldc % 4) || (ncol % 4))
+    // Tensor maps need 16-byte aligned bases and strides; tiles start at
+    // multiples of 32 columns (128 bytes)
+    const uintptr_t ptrs = (uintptr_t)a->b1 | (uintptr_t)a->b2 | (uintptr_t)a->c;
+    if ((ptrs & 15) || (a->ldb1 % 4) || (a->ldc % 4) || (a->ncol % 4) ||
+        (h->k2 && a->ldb2 % 4) ||
+        (a->nbatch > 1 && ((a->bstride1 % 4) || (a->cstride % 4) || (h->k2 && a->bstride2 % 4))))
         return b200::set_error(B200_ERR_ARG, "mul_bf16x3: operands must be 16-byte aligned");
+    if (a->products != 0 && a->products != 3 && a->products != 4)
+        return b200::set_error(B200_ERR_ARG, "mul_bf16x3: products must be 3 or 4");
+    if (a->rowscale && (a->nvars <= 0 || a->ldr <= 0 || a->nbatch != 1))
+        return b200::set_error(B200_ERR_ARG, "mul_bf16x3: row scale needs nvars, ldr, one slice");
 
     if (!g_sm_count)
         return b200::set_error(B200_ERR_STATE, "mul_bf16x3: no handle created on this device");
 
     // The epilogue stores (beta = 0) or adds (beta = 1) through the TMA
-    if (beta != 0.0f && beta != 1.0f)
+    if (a->beta != 0.0f && a->beta != 1.0f)
         return b200::set_error(B200_ERR_UNSUPPORTED, "mul_bf16x3: beta must be 0 or 1");
     UmmaArgs p;
-    int rc = encode_b_map(&p.tmap, b, ldb, ncol, h->k);
-    if (!rc) rc = encode_c_map(&p.cmap, c, ldc, ncol, h->m);
+    const int one = a->nbatch == 1;
+    int rc = encode_b_map(&p.tmap[0], a->b1, a->ldb1, a->ncol, h->k1, a->nbatch,
+                          one ? a->ldb1 * h->k1 : a->bstride1);
+    if (!rc && h->k2)
+        rc = encode_b_map(&p.tmap[1], a->b2, a->ldb2, a->ncol, h->k2, a->nbatch,
+                          one ? a->ldb2 * h->k2 : a->bstride2);
+    else
+        p.tmap[1] = p.tmap[0];
+    if (!rc)
+        rc = encode_c_map(&p.cmap, a->c, a->ldc, a->ncol, h->m, a->nbatch,
+                          one ? a->ldc * h->m : a->cstride);
     if (rc) return rc;
-    p.aimg = h->aimg; p.ncol = ncol;
-    p.m = h->m; p.npad = h->npad; p.kfull = h->kfull; p.ns = h->ns;
-    p.alpha = alpha; p.epi = beta != 0.0f; p.err = err;
+    p.aimg = h->aimg; p.rs = a->rowscale; p.ldr = a->ldr; p.nvars = a->nvars;
+    p.ncol = a->ncol; p.ntc = (a->ncol + TCOLS - 1) / TCOLS;
+    p.m = h->m; p.npad = h->npad; p.kfull = h->kfull; p.nch1 = h->nch1; p.ns = h->ns;
+    p.eb = h->eb;
+    p.nbatch = a->nbatch;
+    p.alpha = a->alpha; p.epi = a->beta != 0.0f; p.err = a->err;
+    p.products = a->products == 4 ? 4 : 3;
 
-    const int64_t ntiles = (ncol + TCOLS - 1) / TCOLS;
+    const int64_t ntiles = p.ntc * p.nbatch;
     const unsigned grid = (unsigned)(ntiles < g_sm_count ? ntiles : g_sm_count);
     mul_umma_kernel<<<grid, NTHREADS, h->smem_bytes, (cudaStream_t)stream>>>(p);
     B200_CHECK_LAUNCH("mul_umma_kernel");
     return B200_OK;
+}
+
+int b200_mul_bf16x3(void *handle, const float *b, int64_t ldb, float *c, int64_t ldc,
+                    int64_t ncol, float alpha, float beta, int *err, void *stream) {
+    b200_mul_bf16x3_args_t a = {};
+    a.b1 = b; a.ldb1 = ldb; a.c = c; a.ldc = ldc; a.ncol = ncol; a.nbatch = 1;
+    a.alpha = alpha; a.beta = beta; a.err = err;
+    if (!handle || !err) return b200::set_error(B200_ERR_ARG, "mul_bf16x3: null handle/status");
+    if (((UmmaHandle *)handle)->k2)
+        return b200::set_error(B200_ERR_ARG, "mul_bf16x3: two-block operator needs _apply");
+    return b200_mul_bf16x3_apply(handle, &a, stream);
 }
 
 }  // extern "C"

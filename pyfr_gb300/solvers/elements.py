@@ -294,7 +294,34 @@ class FluidElements:
         return [rho, *vs, p]
 
 
-class EulerElements(FluidElements, BaseElements):
+class _DivergenceMixin:
+    def _divergence_kernels(self):
+        """tdivtpcorf, tdivtconf and negdivconf
+        (pyfr/solvers/baseadvec/elements.py:91-120), or, with fused
+        operators, all three as one kernel:
+        R = -(1/|J|)((M1 - M3.M2) F + M3 Fc)."""
+        be, kernels = self._be, self.kernels
+        if be.fuse_operators:
+            kernels['tdivtconf_cat'] = lambda fout: be.kernel(
+                'mul_cat', self.opmat('M1 - M3*M2'), self._vect_upts,
+                self.opmat('M3'), self._scal_fpts, out=self.scal_upts[fout],
+                alpha=-1.0, rowscale=self.rcpdjac_at('upts'))
+            return
+
+        kernels['tdivtpcorf'] = lambda fout: be.kernel(
+            'mul', self.opmat('M1 - M3*M2'), self._vect_upts,
+            out=self.scal_upts[fout])
+        kernels['tdivtconf'] = lambda fout: be.kernel(
+            'mul', self.opmat('M3'), self._scal_fpts,
+            out=self.scal_upts[fout], beta=1.0)
+        kernels['negdivconf'] = lambda fout: be.kernel(
+            'negdivconf', tplargs=dict(ndims=self.ndims, nvars=self.nvars,
+                                       src_macros=[]),
+            dims=[self.nupts, self.neles], tdivtconf=self.scal_upts[fout],
+            rcpdjac=self.rcpdjac_at('upts'))
+
+
+class EulerElements(_DivergenceMixin, FluidElements, BaseElements):
     _scratch_bufs = {'scal_fpts', 'vect_upts'}
 
     def set_backend(self, backend, nonce, linoff):
@@ -332,21 +359,10 @@ class EulerElements(FluidElements, BaseElements):
             k(uin) for k in tdisf)
 
         # Divergence of the partially corrected flux and the correction
-        kernels['tdivtpcorf'] = lambda fout: be.kernel(
-            'mul', self.opmat('M1 - M3*M2'), self._vect_upts,
-            out=self.scal_upts[fout])
-        kernels['tdivtconf'] = lambda fout: be.kernel(
-            'mul', self.opmat('M3'), self._scal_fpts,
-            out=self.scal_upts[fout], beta=1.0)
-
-        kernels['negdivconf'] = lambda fout: be.kernel(
-            'negdivconf', tplargs=dict(ndims=self.ndims, nvars=self.nvars,
-                                       src_macros=[]),
-            dims=[self.nupts, self.neles], tdivtconf=self.scal_upts[fout],
-            rcpdjac=self.rcpdjac_at('upts'))
+        self._divergence_kernels()
 
 
-class NavierStokesElements(FluidElements, BaseElements):
+class NavierStokesElements(_DivergenceMixin, FluidElements, BaseElements):
     _scratch_bufs = {'scal_fpts', 'vect_fpts', 'vect_upts', 'grad_upts'}
 
     def set_backend(self, backend, nonce, linoff):
@@ -364,12 +380,19 @@ class NavierStokesElements(FluidElements, BaseElements):
             kernels['copy_fpts'] = lambda: be.kernel(
                 'copy', self._comm_fpts, self._scal_fpts)
 
-        kernels['tgradpcoru_upts'] = lambda uin: be.kernel(
-            'mul', self.opmat('M4 - M6*M0'), self.scal_upts[uin],
-            out=self._grad_upts)
-        kernels['tgradcoru_upts'] = lambda: be.kernel(
-            'mul', self.opmat('M6'), self._comm_fpts, out=self._grad_upts,
-            beta=1.0)
+        if be.fuse_operators:
+            # Corrected gradient in one operator apply: [M4-M6.M0 | M6]
+            # on the solution stacked over the common solution
+            kernels['tgradcoru_upts_cat'] = lambda uin: be.kernel(
+                'mul_cat', self.opmat('M4 - M6*M0'), self.scal_upts[uin],
+                self.opmat('M6'), self._comm_fpts, out=self._grad_upts)
+        else:
+            kernels['tgradpcoru_upts'] = lambda uin: be.kernel(
+                'mul', self.opmat('M4 - M6*M0'), self.scal_upts[uin],
+                out=self._grad_upts)
+            kernels['tgradcoru_upts'] = lambda: be.kernel(
+                'mul', self.opmat('M6'), self._comm_fpts,
+                out=self._grad_upts, beta=1.0)
 
         r, s = self.mesh_regions, self._slice_mat
         gtpl = dict(ndims=self.ndims, nvars=self.nvars,
@@ -394,6 +417,10 @@ class NavierStokesElements(FluidElements, BaseElements):
         def gradcoru_fpts():
             nupts, nfpts = self.nupts, self.nfpts
             vupts, vfpts = self._grad_upts, self._vect_fpts
+            if be.fuse_operators:
+                # The ndims products as one launch over ndims slices
+                return be.kernel('mul_batched', self.opmat('M0'), vupts,
+                                 vfpts, nbatch=self.ndims)
             muls = [be.kernel('mul', self.opmat('M0'),
                               vupts.slice(i*nupts, (i + 1)*nupts),
                               vfpts.slice(i*nfpts, (i + 1)*nfpts))
@@ -425,14 +452,4 @@ class NavierStokesElements(FluidElements, BaseElements):
                       **kw)
             for kt, n, rgn, kw in tdisf)
 
-        kernels['tdivtpcorf'] = lambda fout: be.kernel(
-            'mul', self.opmat('M1 - M3*M2'), self._vect_upts,
-            out=self.scal_upts[fout])
-        kernels['tdivtconf'] = lambda fout: be.kernel(
-            'mul', self.opmat('M3'), self._scal_fpts,
-            out=self.scal_upts[fout], beta=1.0)
-        kernels['negdivconf'] = lambda fout: be.kernel(
-            'negdivconf', tplargs=dict(ndims=self.ndims, nvars=self.nvars,
-                                       src_macros=[]),
-            dims=[self.nupts, self.neles], tdivtconf=self.scal_upts[fout],
-            rcpdjac=self.rcpdjac_at('upts'))
+        self._divergence_kernels()

@@ -179,6 +179,13 @@ class EulerSystem(BaseSystem):
         g_flux_div = self.backend.graph()
         for l in k['eles/tdisf']:
             g_flux_div.add(l)
+        if k['eles/tdivtconf_cat']:
+            # Fused divergence, correction and negdivconf
+            for l in k['eles/tdivtconf_cat']:
+                g_flux_div.add(l, deps=deps(l, 'eles/tdisf'))
+            g_flux_div.commit()
+            return g_intf, g_flux_div
+
         for l in k['eles/tdivtpcorf']:
             g_flux_div.add(l, deps=deps(l, 'eles/tdisf'))
         for l in k['eles/tdivtconf']:
@@ -214,6 +221,9 @@ class NavierStokesSystem(BaseSystem):
         kdeps = k['eles/copy_fpts'] or k['eles/disu']
         g_soln.add_all(k['iint/con_u'], deps=kdeps)
         g_soln.commit()
+
+        if k['eles/tgradcoru_upts_cat']:
+            return (g_soln,) + self._rhs_graphs_fused(k, deps)
 
         # Graph 2: corrected gradient, fused flux, face gradients, common
         # flux and the divergence of the partially corrected flux
@@ -251,6 +261,25 @@ class NavierStokesSystem(BaseSystem):
 
         return g_soln, g_grad_flux, g_div
 
+    def _rhs_graphs_fused(self, k, deps):
+        """Graphs 2 and 3 with fused operator applies: the corrected
+        gradient in one apply, the face gradients in one launch, and the
+        divergence, correction and negdivconf in one apply (which then
+        waits for the common flux)."""
+        g_grad_flux = self.backend.graph()
+        g_grad_flux.add_all(k['eles/tgradcoru_upts_cat'])
+        for l in k['eles/tdisf_fused']:
+            g_grad_flux.add(l, deps=deps(l, 'eles/tgradcoru_upts_cat'))
+        for l in k['eles/gradcoru_fpts']:
+            g_grad_flux.add(l, deps=deps(l, 'eles/tdisf_fused'))
+        g_grad_flux.add_all(k['iint/comm_flux'], deps=k['eles/gradcoru_fpts'])
+        g_grad_flux.commit()
+
+        g_div = self.backend.graph()
+        g_div.add_all(k['eles/tdivtconf_cat'])
+        g_div.commit()
+        return g_grad_flux, g_div
+
     def _compute_grads_graph(self, uinbank):
         key = ('grads', uinbank)
         if key in self._graph_cache:
@@ -267,11 +296,16 @@ class NavierStokesSystem(BaseSystem):
             g.add(l, deps=deps(l, 'eles/disu'))
         kdeps = k['eles/copy_fpts'] or k['eles/disu']
         g.add_all(k['iint/con_u'], deps=kdeps)
-        g.add_all(k['eles/tgradpcoru_upts'], deps=k['iint/con_u'])
-        for l in k['eles/tgradcoru_upts']:
-            g.add(l, deps=deps(l, 'eles/tgradpcoru_upts') + k['iint/con_u'])
-        for l in k['eles/gradcoru_u']:
-            g.add(l, deps=deps(l, 'eles/tgradcoru_upts'))
+        if k['eles/tgradcoru_upts_cat']:
+            g.add_all(k['eles/tgradcoru_upts_cat'], deps=k['iint/con_u'])
+            for l in k['eles/gradcoru_u']:
+                g.add(l, deps=deps(l, 'eles/tgradcoru_upts_cat'))
+        else:
+            g.add_all(k['eles/tgradpcoru_upts'], deps=k['iint/con_u'])
+            for l in k['eles/tgradcoru_upts']:
+                g.add(l, deps=deps(l, 'eles/tgradpcoru_upts') + k['iint/con_u'])
+            for l in k['eles/gradcoru_u']:
+                g.add(l, deps=deps(l, 'eles/tgradcoru_upts'))
         g.commit()
 
         self._graph_cache[key] = (g,)

@@ -57,6 +57,113 @@ def test_mul_bf16x3_tensor_cores(built, golden, key, opname):
                           1e-6*np.abs(ref))
 
 
+@pytest.mark.parametrize('neles', [77, 1000])
+def test_mul_bf16x3_cat_rowscale(built, golden, neles):
+    """Fused apply out = alpha*S*(A1@B1 + A2@B2) (+ out): the divergence,
+    correction and negdivconf of the reference in one kernel."""
+    from pyfr_gb300.backend import B200Backend
+    from pyfr_gb300.inifile import Inifile
+    ops = golden['operators']
+    a1 = ops['hex_p3_gauss-legendre/M132']
+    a2 = ops['hex_p3_gauss-legendre/m3']
+    cfg = Inifile()
+    cfg.set('backend', 'precision', 'single')
+    cfg.set('backend-b200', 'mul-precision', 'bf16x3')
+    be = B200Backend(cfg)
+    rng = np.random.default_rng(11)
+    nv = 5
+    b1 = rng.normal(size=(a1.shape[1], nv, neles))
+    b2 = rng.normal(size=(a2.shape[1], nv, neles))
+    c0 = rng.normal(size=(a1.shape[0], nv, neles))
+    sc = rng.uniform(0.5, 2.0, size=(a1.shape[0], neles))
+    A1, A2 = be.const_matrix(a1), be.const_matrix(a2)
+    B1 = be.matrix(b1.shape, b1, tags={'align'})
+    B2 = be.matrix(b2.shape, b2, tags={'align'})
+    C_ = be.matrix(c0.shape, c0, tags={'align'})
+    S = be.matrix(sc.shape, sc, tags={'align'})
+    be.commit()
+    b1f, b2f = b1.astype(np.float32), b2.astype(np.float32)
+    prod = np.einsum('mk,kve->mve', a1, b1f) + np.einsum('mk,kve->mve', a2, b2f)
+    bound = 1e-4*(np.einsum('mk,kve->mve', np.abs(a1), np.abs(b1f)) +
+                  np.einsum('mk,kve->mve', np.abs(a2), np.abs(b2f))) + 1e-6
+    for alpha, beta, rs in [(1.0, 0.0, None), (-1.0, 0.0, S), (0.5, 1.0, S)]:
+        C_.set(c0)
+        k = be.kernel('mul_cat', A1, B1, A2, B2, out=C_, alpha=alpha,
+                      beta=beta, rowscale=rs)
+        assert k.meta['impl'] == 'bf16x3-cat'
+        be.run_kernels([k], wait=True)
+        f = alpha*(sc[:, None, :] if rs is not None else 1.0)
+        ref = f*prod + beta*c0.astype(np.float32)
+        assert np.all(np.abs(C_.get() - ref) <= np.abs(f)*bound +
+                      1e-6*np.abs(ref))
+
+
+def test_mul_bf16x3_batched(built, golden):
+    """ndims products of one operator as one launch over row slices."""
+    from pyfr_gb300.backend import B200Backend
+    from pyfr_gb300.inifile import Inifile
+    a = golden['operators']['hex_p3_gauss-legendre/m0']
+    cfg = Inifile()
+    cfg.set('backend', 'precision', 'single')
+    cfg.set('backend-b200', 'mul-precision', 'bf16x3')
+    be = B200Backend(cfg)
+    rng = np.random.default_rng(12)
+    nb, nv, neles = 3, 5, 333
+    b = rng.normal(size=(nb, a.shape[1], nv, neles))
+    B = be.matrix(b.shape, b, tags={'align'})
+    C_ = be.matrix((nb, a.shape[0], nv, neles), tags={'align'})
+    A = be.const_matrix(a)
+    be.commit()
+    k = be.kernel('mul_batched', A, B, C_, nbatch=nb)
+    be.run_kernels([k], wait=True)
+    bf = b.astype(np.float32)
+    ref = np.einsum('mk,zkve->zmve', a, bf)
+    bound = 1e-4*np.einsum('mk,zkve->zmve', np.abs(a), np.abs(bf)) + 1e-6
+    assert np.all(np.abs(C_.get() - ref) <= bound)
+
+
+def test_fused_ns_rhs_matches_oracle(built):
+    """The fused graph (corrected gradient, face gradients, and divergence
+    with negdivconf as three fused applies) against the unfused graph, both
+    split-BF16 on the reference-state transform of the TGV.  Split-BF16
+    products carry about 2^-16 sum|a||b| of error, and the divergence
+    operator's rows sum to tens, so the RHS error is about 1e-3 of its
+    size (bound 3e-3); fusing must not make it worse (it skips two FP32
+    roundings of partial results)."""
+    from pyfr_gb300.backend import B200Backend
+    from pyfr_gb300.cases import ns_tgv
+    from pyfr_gb300.solvers.system import NavierStokesSystem
+    out = {}
+    for fuse in ('true', 'false'):
+        cfg, mesh = ns_tgv(n=5, order=3, precision='single')
+        cfg.set('backend-b200', 'mul-precision', 'bf16x3')
+        cfg.set('backend-b200', 'fuse-operators', fuse)
+        gamma = cfg.getfloat('constants', 'gamma')
+        be = B200Backend(cfg)
+        assert be.fuse_operators == (fuse == 'true')
+        s = NavierStokesSystem(be, mesh, None, 2, cfg)
+        (eles,) = s.ele_map.values()
+        u = eles.set_ics_from_cfg()
+        rho_ref, p_ref = 1.0, cfg.getfloat('constants', 'p0')
+        hs = gamma/(gamma - 1)*p_ref/rho_ref
+        be.ref_state = (rho_ref, p_ref)
+        s.commit()
+        q = u - np.array([rho_ref, 0, 0, 0, p_ref/(gamma - 1)])[None, :, None]
+        q[:, -1] -= hs*q[:, 0]
+        s.ele_banks[0][0].set(q.astype(np.float32))
+        s.rhs(0.0, 0, 1)
+        (out[fuse],) = s.ele_scal_upts(1)
+
+    d = disc_for_mesh(mesh, 3, ns=True)
+    c = cfg.items_as('constants', float) | cfg.items_as('solver-interfaces',
+                                                       float)
+    ref = d.rhs_ns(u, c)
+    ref[:, -1] -= hs*ref[:, 0]
+    err = {f: np.abs(out[f] - ref).max()/np.abs(ref).max() for f in out}
+    assert err['false'] <= 3e-3
+    assert err['true'] <= 1.5*err['false']
+
+
 def test_fp32_ns_rhs(built):
     """The TGV fluxes carry the mean pressure p0 = 1/(gamma Ma^2) ~ 71
     while the RHS is O(1): FP32 rounding of the fluxes (relative 6e-8 of
@@ -134,7 +241,7 @@ def test_fp32_euler_rhs(built):
     assert np.abs(r - ref).max() <= 1e-4*np.abs(ref).max()
 
 
-@pytest.mark.parametrize('mulprec', ['native', 'bf16x3'])
+@pytest.mark.parametrize('mulprec', ['native', 'bf16x3', 'bf16x3-unfused'])
 @pytest.mark.parametrize('case', ['vortex', 'tgv'])
 def test_mixed_rk45_l2_error(built, case, mulprec):
     from pyfr_gb300.backend import B200Backend
@@ -148,7 +255,9 @@ def test_mixed_rk45_l2_error(built, case, mulprec):
     else:
         cfg, mesh = ns_tgv(n=5, order=3, dt=5e-4, precision='single')
         scls, nsteps, ns = NavierStokesSystem, 10, True
-    cfg.set('backend-b200', 'mul-precision', mulprec)
+    cfg.set('backend-b200', 'mul-precision', mulprec.split('-')[0])
+    if mulprec.endswith('unfused'):
+        cfg.set('backend-b200', 'fuse-operators', 'false')
 
     be = B200Backend(cfg)
     intg = MixedRKIntegrator(be, scls, mesh, cfg)
@@ -167,11 +276,13 @@ def test_mixed_rk45_l2_error(built, case, mulprec):
     assert _l2rel(ug, u) <= L2_TOL
 
 
-def test_kinetic_energy_history(built):
+@pytest.mark.parametrize('mul', ['native', 'bf16x3-4'])
+def test_kinetic_energy_history(built, mul):
     """Kinetic-energy history of the chosen form against the FP64 plain
     form.  The history is the normalised Taylor-Green kinetic energy
     E_k = int rho |u|^2 / (2 rho0 V) (about 0.125 here); the chosen form
-    must stay within 1e-8 of the FP64 value at every logged step."""
+    must stay within 1e-8 of the FP64 value at every logged step.  Operator
+    contractions in FP32 (native) or split-BF16 with four products."""
     from pyfr_gb300.backend import B200Backend
     from pyfr_gb300.cases import ns_tgv
     from pyfr_gb300.integrators import MixedRKIntegrator, RKVdH2Integrator
@@ -182,6 +293,9 @@ def test_kinetic_energy_history(built):
     for form, prec, icls in [('plain', 'double', RKVdH2Integrator),
                              ('chosen', 'single', MixedRKIntegrator)]:
         cfg, mesh = ns_tgv(n=6, order=3, dt=5e-4, precision=prec)
+        if form == 'chosen' and mul != 'native':
+            cfg.set('backend-b200', 'mul-precision', 'bf16x3')
+            cfg.set('backend-b200', 'split-products', '4')
         intg = icls(B200Backend(cfg), NavierStokesSystem, mesh, cfg)
         fi = FieldIntegrals(intg)
         h = []
