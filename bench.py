@@ -260,7 +260,7 @@ def measure(intg, args, dist, e2e=True, profile=True):
         # replayed steps are undone afterwards so the solution history
         # stays in step with the other forms
         snap = intg.snapshot()
-        per = {}
+        per, ops = {}, {}
         evs = [ev() for _ in range(len(klist) + 1)]
         for _ in range(3):
             lib.event_record(evs[0], stream)
@@ -271,9 +271,21 @@ def measure(intg, args, dist, e2e=True, profile=True):
             for i, k in enumerate(klist):
                 name = k.meta.get('kind', k.name)
                 d = per.setdefault(name, {'ms': 0.0, 'n': 0, 'bytes': 0})
-                d['ms'] += elapsed(evs[i], evs[i + 1])
+                t_ms, nb = elapsed(evs[i], evs[i + 1]), kernel_bytes(k, be)
+                d['ms'] += t_ms
                 d['n'] += 1
-                d['bytes'] += kernel_bytes(k, be)
+                d['bytes'] += nb
+                if k.name == 'mul':
+                    # Per operator apply: impl, shape(s), slices, beta
+                    m = k.meta
+                    key = f"{m.get('impl')} {m['a'].nrow}x{m['a'].ncol}"
+                    if m.get('a2') is not None:
+                        key += f"+{m['a2'].ncol}"
+                    key += f" x{m.get('nbatch', 1)} beta={m['beta']:g}"
+                    o = ops.setdefault(key, {'ms': 0.0, 'n': 0, 'bytes': 0})
+                    o['ms'] += t_ms
+                    o['n'] += 1
+                    o['bytes'] += nb
         be.wait()
         intg.restore(snap)
         del snap
@@ -287,6 +299,10 @@ def measure(intg, args, dist, e2e=True, profile=True):
                 'avg_us': round(1e3*v['ms']/v['n'], 2),
                 'gbs': round(v['bytes']/(v['ms']*1e-3)/1e9, 1)}
             for n, v in sorted(per.items(), key=lambda x: -x[1]['ms'])}
+        res['mul_ops'] = {
+            n: {'avg_us': round(1e3*v['ms']/v['n'], 2),
+                'gbs': round(v['bytes']/(v['ms']*1e-3)/1e9, 1)}
+            for n, v in sorted(ops.items(), key=lambda x: -x[1]['ms'])}
         res['roofline'] = {
             'bound': 'hbm', 'kernel': dom, 'achieved': round(achieved, 1),
             'peak': peak, 'unit': 'GB/s', 'frac': round(achieved/peak, 4),
@@ -532,7 +548,8 @@ def main():
                 'd2h_bytes_per_step': rc['e2e_bytes']}
         if 'roofline' in rc:
             variants[form] |= {'roofline': rc['roofline'],
-                               'kernels': rc['kernels']}
+                               'kernels': rc['kernels'],
+                               'mul_ops': rc['mul_ops']}
     chosen = variants.pop('chosen', None)
     if chosen is not None:
         chosen['other_variants'] = variants
@@ -553,6 +570,7 @@ def main():
         'gpu_launches': res['launches'],
         'roofline': res['roofline'],
         'kernels': res['kernels'],
+        'mul_ops': res['mul_ops'],
         'chosen': chosen,
         'cpu_baseline': {'value': cpu_v, 'unit': 'GDoF/s',
                          'cores': cpu_cores(), 'kind': 'port',

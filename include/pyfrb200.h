@@ -228,6 +228,18 @@ int b200_intconu_f32(int nvars, int64_t n, double beta, const float *lin_base,
                      const void *lin_map, const float *rin_base, const void *rin_map,
                      float *lout_base, const void *lout_map, float *rout_base,
                      const void *rout_map, int ix64, void *stream);
+/* Same, writing the common solution to both sides for every beta (for
+ * beta = +-1/2 the reference writes one side and relies on a prior copy of
+ * the solution into the output for the other; when every flux point lies
+ * on an interior interface this writes both and the copy is not needed). */
+int b200_intconu_both_f64(int nvars, int64_t n, double beta, const double *lin_base,
+                          const void *lin_map, const double *rin_base, const void *rin_map,
+                          double *lout_base, const void *lout_map, double *rout_base,
+                          const void *rout_map, int ix64, void *stream);
+int b200_intconu_both_f32(int nvars, int64_t n, double beta, const float *lin_base,
+                          const void *lin_map, const float *rin_base, const void *rin_map,
+                          float *lout_base, const void *lout_map, float *rout_base,
+                          const void *rout_map, int ix64, void *stream);
 
 /* ---- integrator register kernels (flat over n scalars) --------------- */
 /* RK stage of the two-register low-storage schemes;

@@ -54,6 +54,8 @@ def _sig_pointwise(fp):
         'intcflux_ns': [i32, i64, i32, C.POINTER(Gas), f64, f64, vp, vp, vp,
                         vp, vp, vp, vp, vp, vp, vp, i32, vp, i64, vp],
         'intconu': [i32, i64, f64, vp, vp, vp, vp, vp, vp, vp, vp, i32, vp],
+        'intconu_both': [i32, i64, f64, vp, vp, vp, vp, vp, vp, vp, vp, i32,
+                         vp],
         'rkvdh2': [i64, i32, i32, i32, f64, f64, f64, f64, vp, vp, vp, vp, vp],
         'axnpby': [i64, i32, vp, C.POINTER(vp), C.POINTER(f64), vp],
         'errest': [i32, i32, i64, i64, vp, vp, vp, f64, i32, vp, i32, vp, vp],

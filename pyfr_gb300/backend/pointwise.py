@@ -286,7 +286,10 @@ class PointwiseKernelProvider:
     def _intconu(self, tplargs, dims, extrns, ulin, urin, ulout, urout):
         (n,) = dims
         beta = tplargs['c']['ldg-beta']
-        fn, nv = self._fn('intconu'), tplargs['nvars']
+        # both_sides: write the common solution to both sides (no prior
+        # copy of the solution into the outputs is needed)
+        name = 'intconu_both' if tplargs.get('both_sides') else 'intconu'
+        fn, nv = self._fn(name), tplargs['nvars']
         a = [_view(v)[:2] for v in (ulin, urin, ulout, urout)]
         ix64 = self._ix64
 

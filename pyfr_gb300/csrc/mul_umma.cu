@@ -562,8 +562,10 @@ int b200_mul_bf16x3_create_cat(const double *a1, int k1, const double *a2, int k
     const int npad = (m + 31) / 32 * 32, kfull = (nch1 + nch2) * KC;
     // The deepest ring (bytes in flight per SM) that fits in shared memory
     // with two staging tiles per epilogue set, or failing four stages that
-    // way, with one
-    int ns = 0, eb = MAX_EB;
+    // way, with one.  An operator of at most 64 rows gives each set one
+    // store per tile, which a second staging tile would not overlap with
+    // anything: it takes one and the ring the room.
+    int ns = 0, eb = npad <= 64 ? 1 : MAX_EB;
     Layout L = make_layout(npad, kfull, 2, eb);
     for (; eb >= 1 && ns < 4; eb--) {
         ns = 0;

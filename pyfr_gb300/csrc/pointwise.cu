@@ -344,7 +344,7 @@ intcflux_ns_kernel(int64_t n, int rs, b200::GasK<T> gas, T beta, T tau, ScalView
 template <typename T>
 __global__ void __launch_bounds__(PW_BLOCK)
 intconu_kernel(int64_t n, int nvars, T beta, ScalView<T> lin, ScalView<T> rin,
-               ScalView<T> lout, ScalView<T> rout, int ix64) {
+               ScalView<T> lout, ScalView<T> rout, int ix64, int both) {
     const int64_t i = (int64_t)blockIdx.x * PW_BLOCK + threadIdx.x;
     if (i >= n) return;
 
@@ -356,9 +356,13 @@ intconu_kernel(int64_t n, int nvars, T beta, ScalView<T> lin, ScalView<T> rin,
     for (int v = 0; v < nvars; v++) {
         const int o = v * B200_SOASZ;
         if (beta == T(-0.5)) {
-            pro[o] = pli[o];
+            const T c = pli[o];
+            pro[o] = c;
+            if (both) plo[o] = c;
         } else if (beta == T(0.5)) {
-            plo[o] = pri[o];
+            const T c = pri[o];
+            plo[o] = c;
+            if (both) pro[o] = c;
         } else {
             const T c = pri[o] * (T(0.5) + beta) + pli[o] * (T(0.5) - beta);
             plo[o] = c;
@@ -494,6 +498,20 @@ int intcflux_ns(int ndims, int64_t n, int rsolver, const b200_gas_t *gas, double
     return B200_OK;
 }
 
+template <typename T>
+int intconu(int nvars, int64_t n, double beta, const T *lin_base, const void *lin_map,
+            const T *rin_base, const void *rin_map, T *lout_base, const void *lout_map,
+            T *rout_base, const void *rout_map, int ix64, int both, cudaStream_t st) {
+    if (n <= 0) return B200_OK;
+    ScalView<T> li{const_cast<T *>(lin_base), lin_map};
+    ScalView<T> ri{const_cast<T *>(rin_base), rin_map};
+    ScalView<T> lo{lout_base, lout_map}, ro{rout_base, rout_map};
+    intconu_kernel<T><<<b200::ceil_div(n, PW_BLOCK), PW_BLOCK, 0, st>>>(
+        n, nvars, (T)beta, li, ri, lo, ro, ix64, both);
+    B200_CHECK_LAUNCH("intconu");
+    return B200_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -606,28 +624,32 @@ int b200_intconu_f64(int nvars, int64_t n, double beta, const double *lin_base,
                      const void *lin_map, const double *rin_base, const void *rin_map,
                      double *lout_base, const void *lout_map, double *rout_base,
                      const void *rout_map, int ix64, void *stream) {
-    if (n <= 0) return B200_OK;
-    ScalView<double> li{const_cast<double *>(lin_base), lin_map};
-    ScalView<double> ri{const_cast<double *>(rin_base), rin_map};
-    ScalView<double> lo{lout_base, lout_map}, ro{rout_base, rout_map};
-    intconu_kernel<double><<<b200::ceil_div(n, PW_BLOCK), PW_BLOCK, 0, (cudaStream_t)stream>>>(
-        n, nvars, beta, li, ri, lo, ro, ix64);
-    B200_CHECK_LAUNCH("intconu");
-    return B200_OK;
+    return intconu<double>(nvars, n, beta, lin_base, lin_map, rin_base, rin_map, lout_base,
+                           lout_map, rout_base, rout_map, ix64, 0, (cudaStream_t)stream);
 }
 
 int b200_intconu_f32(int nvars, int64_t n, double beta, const float *lin_base,
                      const void *lin_map, const float *rin_base, const void *rin_map,
                      float *lout_base, const void *lout_map, float *rout_base,
                      const void *rout_map, int ix64, void *stream) {
-    if (n <= 0) return B200_OK;
-    ScalView<float> li{const_cast<float *>(lin_base), lin_map};
-    ScalView<float> ri{const_cast<float *>(rin_base), rin_map};
-    ScalView<float> lo{lout_base, lout_map}, ro{rout_base, rout_map};
-    intconu_kernel<float><<<b200::ceil_div(n, PW_BLOCK), PW_BLOCK, 0, (cudaStream_t)stream>>>(
-        n, nvars, (float)beta, li, ri, lo, ro, ix64);
-    B200_CHECK_LAUNCH("intconu");
-    return B200_OK;
+    return intconu<float>(nvars, n, beta, lin_base, lin_map, rin_base, rin_map, lout_base,
+                          lout_map, rout_base, rout_map, ix64, 0, (cudaStream_t)stream);
+}
+
+int b200_intconu_both_f64(int nvars, int64_t n, double beta, const double *lin_base,
+                          const void *lin_map, const double *rin_base, const void *rin_map,
+                          double *lout_base, const void *lout_map, double *rout_base,
+                          const void *rout_map, int ix64, void *stream) {
+    return intconu<double>(nvars, n, beta, lin_base, lin_map, rin_base, rin_map, lout_base,
+                           lout_map, rout_base, rout_map, ix64, 1, (cudaStream_t)stream);
+}
+
+int b200_intconu_both_f32(int nvars, int64_t n, double beta, const float *lin_base,
+                          const void *lin_map, const float *rin_base, const void *rin_map,
+                          float *lout_base, const void *lout_map, float *rout_base,
+                          const void *rout_map, int ix64, void *stream) {
+    return intconu<float>(nvars, n, beta, lin_base, lin_map, rin_base, rin_map, lout_base,
+                          lout_map, rout_base, rout_map, ix64, 1, (cudaStream_t)stream);
 }
 
 }  // extern "C"

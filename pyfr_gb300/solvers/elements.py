@@ -20,6 +20,7 @@ from functools import cached_property
 
 import numpy as np
 
+from pyfr_gb300.backend.types import NullKernel
 from pyfr_gb300.mesh import fuzzy_face_order
 from pyfr_gb300.shapes import get_shape
 
@@ -39,6 +40,8 @@ def npeval(expr, env):
 
 
 class BaseElements:
+    # Set by the system: every flux point lies on an interior interface
+    comm_covered = False
     def __init__(self, etype, eles, cfg):
         self.cfg = cfg
         self.eles = eles
@@ -376,9 +379,12 @@ class NavierStokesElements(_DivergenceMixin, FluidElements, BaseElements):
         kernels['disu'] = lambda uin: be.kernel(
             'mul', self.opmat('M0'), self.scal_upts[uin], out=self._scal_fpts)
 
+        # (not needed when the interfaces write the common solution to
+        # both sides of every flux point: comm_covered, set by the system)
         if abs(self.cfg.getfloat('solver-interfaces', 'ldg-beta')) == 0.5:
-            kernels['copy_fpts'] = lambda: be.kernel(
-                'copy', self._comm_fpts, self._scal_fpts)
+            kernels['copy_fpts'] = lambda: NullKernel() \
+                if self.comm_covered else be.kernel(
+                    'copy', self._comm_fpts, self._scal_fpts)
 
         if be.fuse_operators:
             # Corrected gradient in one operator apply: [M4-M6.M0 | M6]

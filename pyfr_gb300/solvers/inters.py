@@ -45,6 +45,9 @@ def field_view_arrays(side, field, elemap):
 
 
 class BaseIntInters:
+    # Set by the system: every flux point lies on an interior interface
+    covers = False
+
     def __init__(self, be, lhs, rhs, elemap, cfg):
         self._be = be
         self.elemap = elemap
@@ -130,7 +133,8 @@ class NavierStokesIntInters(BaseIntInters):
         be.pointwise.register('pyfr.solvers.navstokes.kernels.intcflux')
 
         self.kernels['con_u'] = lambda: be.kernel(
-            'intconu', tplargs=self._tplargs, dims=[self.ninterfpts],
+            'intconu', tplargs=self._tplargs | {'both_sides': self.covers},
+            dims=[self.ninterfpts],
             ulin=self.scal_lhs, urin=self.scal_rhs,
             ulout=self._comm_lhs, urout=self._comm_rhs)
         self.kernels['comm_flux'] = lambda: be.kernel(

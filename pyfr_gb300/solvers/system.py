@@ -82,7 +82,24 @@ class BaseSystem:
             out.append(tuple(views))
         return out
 
+    def _interfaces_cover_fpts(self):
+        """True when every face of every element is one side of an interior
+        interface (a fully periodic mesh): the common solution can then be
+        written to both sides of each interface point with no copy."""
+        nside = defaultdict(int)
+        for i in self._int_inters:
+            for side in (i.lhs, i.rhs):
+                for et in side.etypes.tolist():
+                    nside[et] += 1
+        return all(nside[et] == e.neles*len(e.basis.faces)
+                   for et, e in self.ele_map.items())
+
     def commit(self):
+        covered = self._interfaces_cover_fpts()
+        for e in self.ele_map.values():
+            e.comm_covered = covered
+        for i in self._int_inters:
+            i.covers = covered
         scal = {et: e._scal_fpts for et, e in self.ele_map.items()}
         for i, (l, r) in zip(self._int_inters, self.make_field_views(
                 scal, vshape=(self.nvars,))):
