@@ -204,6 +204,8 @@ def make_form(form, args):
         cfg.set('backend-b200', 'mul-precision', 'bf16x3')
         cfg.set('backend-b200', 'split-products',
                 str(args.chosen_products) if form == 'chosen' else '3')
+    elif form == 'tf32':
+        cfg.set('backend-b200', 'mul-precision', 'tf32')
     be = B200Backend(cfg)
     icls = RKVdH2Integrator if form == 'plain' else MixedRKIntegrator
     return icls(be, NavierStokesSystem, mesh, cfg)
@@ -377,7 +379,7 @@ def run_gpu(args, dist):
     del plain
 
     out = {'plain': rp}
-    forms = ['chosen', 'bf16x3', 'fp32'] if args.chosen else []
+    forms = ['chosen', 'bf16x3', 'tf32', 'fp32'] if args.chosen else []
     for form in forms:
         intg = make_form(form, args)
         rc = measure(intg, args, dist)
@@ -448,7 +450,8 @@ def main():
                     help='steps after which the chosen form is compared '
                          'with FP64')
     ap.add_argument('--ke-every', type=int, default=10)
-    ap.add_argument('--only', choices=['plain', 'chosen', 'bf16x3', 'fp32'],
+    ap.add_argument('--only', choices=['plain', 'chosen', 'bf16x3', 'tf32',
+                                       'fp32'],
                     help='time one precision form alone (no accuracy '
                          'history, end-to-end loop or CPU sample): the '
                          'command to run under a profiler')
@@ -525,10 +528,12 @@ def main():
         'bf16x3': 'operator contractions split-BF16 hi/lo, 3 products '
                   '(Ahi*Bhi + Ahi*Blo + Alo*Bhi) on tcgen05 tensor cores, '
                   'otherwise as chosen',
+        'tf32': 'operator contractions TF32 (one product) on tcgen05 '
+                'tensor cores, otherwise as chosen',
         'fp32': 'operator contractions FP32 (sparse, CUDA cores), FP32 '
                 'fluxes, FP64 RK accumulation'}
     variants = {}
-    for form in ('chosen', 'bf16x3', 'fp32'):
+    for form in ('chosen', 'bf16x3', 'tf32', 'fp32'):
         if form not in allres:
             continue
         rc = allres[form]

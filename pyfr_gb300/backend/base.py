@@ -107,8 +107,8 @@ class B200Backend:
         # kernels are built (None: inputs are the conserved variables)
         self.ref_state = None
         self.mul_precision = cfg.get('backend-b200', 'mul-precision', 'native')
-        if self.mul_precision not in {'native', 'bf16x3'}:
-            raise ValueError('mul-precision must be native or bf16x3')
+        if self.mul_precision not in {'native', 'bf16x3', 'tf32'}:
+            raise ValueError('mul-precision must be native, bf16x3 or tf32')
 
         # Split-BF16 products: 3 (Ahi Bhi + Ahi Blo + Alo Bhi) or 4 (plus
         # Alo Blo)
@@ -121,10 +121,11 @@ class B200Backend:
         fuse = cfg.get('backend-b200', 'fuse-operators', 'auto')
         if fuse not in {'auto', 'true', 'false'}:
             raise ValueError('fuse-operators must be auto, true or false')
-        tensor = self.mul_precision == 'bf16x3' and self.fpdtype == np.float32
+        tensor = (self.mul_precision in {'bf16x3', 'tf32'} and
+                  self.fpdtype == np.float32)
         if fuse == 'true' and not tensor:
             raise ValueError('fuse-operators needs single precision with '
-                             'mul-precision = bf16x3')
+                             'mul-precision = bf16x3 or tf32')
         self.fuse_operators = tensor and fuse != 'false'
 
         self.mats = WeakValueDictionary()

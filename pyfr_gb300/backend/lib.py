@@ -109,6 +109,9 @@ _SIGS = {
     'b200_mul_bf16x3_create_cat': [pd, i32, pd, i32, i32, C.POINTER(vp),
                                    C.POINTER(sz)],
     'b200_mul_bf16x3_apply': [vp, C.c_void_p, vp],
+    'b200_mul_tf32_create': [pd, i32, i32, C.POINTER(vp), C.POINTER(sz)],
+    'b200_mul_tf32_create_cat': [pd, i32, pd, i32, i32, C.POINTER(vp),
+                                 C.POINTER(sz)],
 }
 
 for _fp, _suf in ((f64, 'f64'), (f32, 'f32')):

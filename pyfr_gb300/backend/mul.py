@@ -108,8 +108,10 @@ class TensorMulKernels:
         from pyfr_gb300.backend.base import NotSuitableError
 
         be = self.backend
-        if be.fpdtype != np.float32 or be.mul_precision != 'bf16x3':
-            raise NotSuitableError('tensor-core mul serves bf16x3 FP32 data')
+        if be.fpdtype != np.float32 or be.mul_precision not in ('bf16x3',
+                                                                'tf32'):
+            raise NotSuitableError('tensor-core mul serves bf16x3 or tf32 '
+                                   'FP32 data')
 
     def _handle(self, *ops):
         from pyfr_gb300.backend.base import NotSuitableError
@@ -122,8 +124,12 @@ class TensorMulKernels:
             a2 = hosts[1] if len(hosts) > 1 else None
             h, smem = C.c_void_p(), C.c_size_t()
             pd = C.POINTER(C.c_double)
+            lib = self.backend.lib
+            create = lib.mul_tf32_create_cat \
+                if self.backend.mul_precision == 'tf32' else \
+                lib.mul_bf16x3_create_cat
             try:
-                self.backend.lib.mul_bf16x3_create_cat(
+                create(
                     a1.ctypes.data_as(pd), a1.shape[1],
                     a2.ctypes.data_as(pd) if a2 is not None else None,
                     a2.shape[1] if a2 is not None else 0, a1.shape[0],
@@ -146,6 +152,8 @@ class TensorMulKernels:
         args.err = be.status_word
         args.products = be.split_products
         meta['products'] = be.split_products
+        if be.mul_precision == 'tf32':
+            meta['impl'] = meta['impl'].replace('bf16x3', 'tf32')
         fn = be.lib.mul_bf16x3_apply
         pa = C.addressof(args)
 

@@ -7,6 +7,10 @@
 // replacement of the reference's `mul` providers
 // (pyfr/backends/cuda/gimmik.py:23-121, pyfr/backends/cuda/cublaslt.py:169-280).
 //
+// A TF32 variant (b200_mul_tf32_create*) runs the same pipeline with one
+// tcgen05.mma.kind::tf32 product per K step: the converters round the
+// staged FP32 chunk to TF32 in place and the operator image is TF32.
+//
 // The general form (b200_mul_bf16x3_apply) fuses what the reference runs
 // as separate kernels:
 //     out_z = alpha * S (.) (A1 @ B1_z + A2 @ B2_z) + beta * out_z
@@ -25,10 +29,11 @@
 // chunks of 32 rows of B (K), through one ring of 16 KB stages:
 //   warp 16 lane 0  loads each 32 x 128 FP32 chunk with one 2-D tensor TMA
 //                   into a free stage;
-//   warps 8-15      split the staged chunk into BF16 hi/lo in place: every
-//                   thread reads its half column (16 values), the converter
-//                   warps meet at a named barrier, then write the halves in
-//                   the canonical K-major no-swizzle UMMA layout over the
+//   warps 8-15      split a staged chunk into BF16 hi/lo in place, in two
+//                   groups of four warps that take alternate chunks: every
+//                   thread reads its column of the chunk (32 values), the
+//                   group meets at a named barrier, then writes the halves
+//                   in the canonical K-major no-swizzle UMMA layout over the
 //                   same 16 KB;
 //   warp 17 lane 0  issues the MMAs into one of two TMEM accumulators; the
 //                   completion of a chunk's MMAs frees its stage;
@@ -61,7 +66,8 @@ constexpr int NTHREADS = 576;     // 18 warps
 constexpr int NEPI = 256;         // epilogue threads (warps 0-7)
 constexpr int NCONV = 256;        // converter threads (warps 8-15)
 constexpr int WARP_CONV = 8, WARP_PROD = 16, WARP_MMA = 17;
-constexpr int CONV_BARRIER = 1;   // named barrier of the converter warps
+constexpr int CONV_BARRIER = 1;   // named barriers 1, 4: the two converter groups
+constexpr int CONV_BARRIER2 = 4;
 constexpr int EPI_BARRIER = 2;    // named barriers 2, 3: the epilogue sets
 constexpr int MAX_N = 256;        // UMMA N limit (operator rows, padded)
 constexpr int MAX_S = 10;         // ring stages (bytes in flight)
@@ -75,6 +81,7 @@ constexpr uint32_t EPI_BUF = 32 * TCOLS * 4;       // one 32-row x 128-column st
 
 struct UmmaHandle {
     int m, k1, k2, nch1, npad, kfull, ns, eb;
+    int tf32;              // operator image and MMAs in TF32 (one product)
     unsigned char *aimg;   // device: [hi | lo], each npad x kfull bf16 canonical
     size_t aimg_bytes;
     size_t smem_bytes;
@@ -179,6 +186,26 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
            ((uint32_t)(M >> 4) << 24);
 }
 
+// kind::tf32 instruction descriptor: TF32 A/B (format 2), FP32 D, K-major
+__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) |
+           ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_tf32(uint32_t dtmem, uint64_t ad, uint64_t bd,
+                                          uint32_t idesc, uint32_t acc) {
+    asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                 "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n"
+                 :: "r"(dtmem), "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+}
+
+// FP32 -> TF32 (round to nearest, ties away from zero), as FP32 bits
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+
 __device__ __forceinline__ void umma(uint32_t dtmem, uint64_t ad, uint64_t bd, uint32_t idesc,
                                      uint32_t acc) {
     asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
@@ -228,6 +255,7 @@ struct UmmaArgs {
     int *err;
 };
 
+template <bool TF32>
 __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_constant__ UmmaArgs p) {
     extern __shared__ __align__(1024) unsigned char smem[];
     const Layout L = make_layout(p.npad, p.kfull, p.ns, p.eb);
@@ -251,7 +279,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
         bar_init(bar(BAR_A), 1);
         for (int s = 0; s < NS; s++) {
             bar_init(bar(BAR_LOADED + s), 1);
-            bar_init(bar(BAR_CONVERTED + s), NCONV);
+            bar_init(bar(BAR_CONVERTED + s), NCONV / 2);
             bar_init(bar(BAR_FREE + s), 1);
         }
         for (int s = 0; s < 2; s++) {
@@ -272,7 +300,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
     const uint32_t tmem = *tslot;
 
     const uint32_t abytes = (uint32_t)npad * p.kfull * 2;
-    const uint32_t SBO_OP = (uint32_t)p.kfull * 16, LBO = 128;
+    // 8-row group strides of the operator image and of a converted chunk:
+    // (K extent / elements per 16-byte core-matrix row) x 128 bytes
+    const uint32_t SBO_OP = (uint32_t)p.kfull * (TF32 ? 32 : 16), LBO = 128;
+    const uint32_t SBO_D = TF32 ? KC * 32 : SBO_CHUNK;
 
     if (warp == WARP_PROD) {
         // ---- producer: operator image once, then the FP32 chunks of B ----
@@ -315,32 +346,47 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
         }
         __syncwarp();
     } else if (warp >= WARP_CONV && warp < WARP_CONV + NCONV / 32) {
-        // ---- converters: FP32 chunk -> BF16 hi/lo canonical K-major, in place ----
-        // thread ct owns rows 16h..16h+15 of column cc of the chunk
-        const int ct = tid - WARP_CONV * 32, cc = ct % TCOLS, h = ct / TCOLS;
-        const uint32_t coff = (uint32_t)(cc / 8) * SBO_CHUNK + (uint32_t)(cc % 8) * 16;
+        // ---- converters: FP32 chunk -> BF16 hi/lo (or TF32) canonical
+        // K-major, in place.  Two groups of four warps take alternate
+        // chunks, so that two chunks are converted at once; thread ct of a
+        // group owns column cc of its chunks.
+        const int ct = tid - WARP_CONV * 32, cc = ct % TCOLS, grp = ct / TCOLS;
+        const uint32_t gbar = grp ? CONV_BARRIER2 : CONV_BARRIER;
+        const uint32_t coff = (uint32_t)(cc / 8) * SBO_D + (uint32_t)(cc % 8) * 16;
         int64_t j = 0;
         bool ok = true;
         for (int64_t t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
             for (int c = 0; c < nch; c++, j++) {
+                if ((int)(j & 1) != grp) continue;
                 const int s = (int)(j % NS);
-                // (a converter that gives up still meets the others at the
-                // named barrier below, so none of them waits there forever)
+                // (a converter that gives up still meets the others of its
+                // group at the named barrier below, so none of them waits
+                // there forever)
                 ok = bar_wait(bar(BAR_LOADED + s), (uint32_t)((j / NS) & 1), abort_flag, p.err, 2);
                 unsigned char *stage = smem + L.ring + s * CHUNK32;
                 const float *b32 = reinterpret_cast<const float *>(stage);
-                float x[16];
+                float x[KC];
                 if (ok) {
 #pragma unroll
-                    for (int r = 0; r < 16; r++) x[r] = b32[(16 * h + r) * TCOLS + cc];
+                    for (int r = 0; r < KC; r++) x[r] = b32[r * TCOLS + cc];
                 }
-                asm volatile("bar.sync %0, %1;" :: "n"(CONV_BARRIER), "n"(NCONV) : "memory");
+                asm volatile("bar.sync %0, %1;" :: "r"(gbar), "n"(NCONV / 2) : "memory");
                 if (!ok || *abort_flag) {
                     ok = false;
                     break;
                 }
+                if (TF32) {
+                    // eight 16-byte core-matrix rows of 4 TF32 values each
 #pragma unroll
-                for (int q = 0; q < 2; q++) {
+                    for (int q = 0; q < KC / 4; q++) {
+                        const uint32_t off = coff + (uint32_t)q * LBO;
+                        *reinterpret_cast<uint4 *>(stage + off) =
+                            make_uint4(to_tf32(x[4 * q]), to_tf32(x[4 * q + 1]),
+                                       to_tf32(x[4 * q + 2]), to_tf32(x[4 * q + 3]));
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < KC / 8 && !TF32; q++) {
                     uint32_t hw[4], lw[4];
 #pragma unroll
                     for (int jj = 0; jj < 8; jj += 2) {
@@ -352,7 +398,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
                         hw[jj / 2] = *reinterpret_cast<const uint32_t *>(&h2);
                         lw[jj / 2] = *reinterpret_cast<const uint32_t *>(&l2);
                     }
-                    const uint32_t off = coff + (uint32_t)(2 * h + q) * LBO;
+                    const uint32_t off = coff + (uint32_t)q * LBO;
                     *reinterpret_cast<uint4 *>(stage + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
                     *reinterpret_cast<uint4 *>(stage + CHUNK16 + off) =
                         make_uint4(lw[0], lw[1], lw[2], lw[3]);
@@ -364,7 +410,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
     } else if (warp == WARP_MMA) {
         // ---- MMA issuer ----
         if (lane == 0) {
-            const uint32_t idesc = idesc_bf16(TCOLS, npad);
+            const uint32_t idesc = TF32 ? idesc_tf32(TCOLS, npad) : idesc_bf16(TCOLS, npad);
             bool ok = bar_wait(bar(BAR_A), 0, abort_flag, p.err, 4);
             int64_t j = 0;
             int i = 0;
@@ -384,8 +430,18 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
                     }
                     asm volatile("tcgen05.fence::after_thread_sync;");
                     const uint32_t bhi = sbase + L.ring + (uint32_t)s2 * CHUNK32;
+                    if (TF32) {
+                        // K steps of 8 (32 bytes: two core matrices)
 #pragma unroll
-                    for (int ks = 0; ks < KC / 16; ks++) {
+                        for (int ks = 0; ks < KC / 8; ks++) {
+                            const uint32_t ko = (uint32_t)ks * 2 * LBO;
+                            const uint32_t kg = (uint32_t)(c * (KC / 8) + ks) * 2 * LBO;
+                            umma_tf32(d, sdesc(bhi + ko, LBO, SBO_D),
+                                      sdesc(sbase + L.a_hi + kg, LBO, SBO_OP), idesc, (c | ks) != 0);
+                        }
+                    }
+#pragma unroll
+                    for (int ks = 0; ks < KC / 16 && !TF32; ks++) {
                         const uint32_t ko = (uint32_t)ks * 2 * LBO;
                         const uint32_t kg = (uint32_t)(c * (KC / 16) + ks) * 2 * LBO;
                         const uint64_t dh = sdesc(bhi + ko, LBO, SBO_CHUNK);
@@ -510,6 +566,25 @@ void build_block(const double *a, int m, int k, int koff, int kfull, size_t n,
         }
 }
 
+// Host: round [A1 | A2] to TF32 (nearest, ties to even, on the binary32
+// encoding: 10 stored mantissa bits) and lay it out in the canonical K-major
+// no-swizzle layout for 4-byte elements ((r/8)*SBO + (k/4)*128 + (r%8)*16 +
+// (k%4)*4 bytes, SBO = kfull*32).
+void build_block_tf32(const double *a, int m, int k, int koff, int kfull,
+                      std::vector<uint16_t> &img) {
+    const size_t SBO = (size_t)kfull * 32;
+    uint32_t *w = reinterpret_cast<uint32_t *>(img.data());
+    for (int r = 0; r < m; r++)
+        for (int c0 = 0; c0 < k; c0++) {
+            const int c = koff + c0;
+            const float x = (float)a[(size_t)r * k + c0];
+            uint32_t u;
+            memcpy(&u, &x, 4);
+            if ((u & 0x7f800000u) != 0x7f800000u) u = (u + 0xfffu + ((u >> 13) & 1u)) & ~0x1fffu;
+            w[((r / 8) * SBO + (c / 4) * 128 + (r % 8) * 16 + (c % 4) * 4) / 4] = u;
+        }
+}
+
 int g_sm_count = 0;
 PFN_cuTensorMapEncodeTiled_v12000 g_encode_tiled = nullptr;
 
@@ -554,8 +629,12 @@ int encode_c_map(CUtensorMap *map, float *c, int64_t ldc, int64_t ncol, int m, i
 
 extern "C" {
 
-int b200_mul_bf16x3_create_cat(const double *a1, int k1, const double *a2, int k2, int m,
-                                void **handle, size_t *smem_bytes) {
+}  // extern "C"
+
+namespace {
+
+int create_impl(const double *a1, int k1, const double *a2, int k2, int m, int tf32,
+                void **handle, size_t *smem_bytes) {
     if (!a1 || !handle || m <= 0 || k1 <= 0 || k2 < 0 || (k2 > 0 && !a2))
         return b200::set_error(B200_ERR_ARG, "mul_bf16x3_create: bad arguments");
     const int nch1 = (k1 + KC - 1) / KC, nch2 = (k2 + KC - 1) / KC;
@@ -595,10 +674,15 @@ int b200_mul_bf16x3_create_cat(const double *a1, int k1, const double *a2, int k
                 cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev),
                 "mul_bf16x3_create");
         if (!rc0)
-            rc0 = b200::check_cuda(cudaFuncSetAttribute(mul_umma_kernel,
+            rc0 = b200::check_cuda(cudaFuncSetAttribute(mul_umma_kernel<false>,
                                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                         227 * 1024),
                                    "mul_bf16x3: smem attribute");
+        if (!rc0)
+            rc0 = b200::check_cuda(cudaFuncSetAttribute(mul_umma_kernel<true>,
+                                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                        227 * 1024),
+                                   "mul_tf32: smem attribute");
         if (!rc0) {
             void *fn = nullptr;
             cudaDriverEntryPointQueryResult q;
@@ -615,13 +699,18 @@ int b200_mul_bf16x3_create_cat(const double *a1, int k1, const double *a2, int k
 
     const size_t n = (size_t)npad * kfull;
     std::vector<uint16_t> img(2 * n, 0);
-    build_block(a1, m, k1, 0, kfull, n, img);
-    if (k2) build_block(a2, m, k2, nch1 * KC, kfull, n, img);
+    if (tf32) {
+        build_block_tf32(a1, m, k1, 0, kfull, img);
+        if (k2) build_block_tf32(a2, m, k2, nch1 * KC, kfull, img);
+    } else {
+        build_block(a1, m, k1, 0, kfull, n, img);
+        if (k2) build_block(a2, m, k2, nch1 * KC, kfull, n, img);
+    }
 
     UmmaHandle *h = (UmmaHandle *)calloc(1, sizeof(UmmaHandle));
     if (!h) return b200::set_error(B200_ERR_STATE, "mul_bf16x3_create: out of host memory");
     h->m = m; h->k1 = k1; h->k2 = k2; h->nch1 = nch1; h->npad = npad; h->kfull = kfull;
-    h->ns = ns; h->eb = eb;
+    h->ns = ns; h->eb = eb; h->tf32 = tf32;
     h->aimg_bytes = img.size() * 2;
     h->smem_bytes = L.total;
     int rc = b200::check_cuda(cudaMalloc(&h->aimg, h->aimg_bytes), "mul_bf16x3_create");
@@ -637,8 +726,26 @@ int b200_mul_bf16x3_create_cat(const double *a1, int k1, const double *a2, int k
     return B200_OK;
 }
 
+}  // namespace
+
+extern "C" {
+
+int b200_mul_bf16x3_create_cat(const double *a1, int k1, const double *a2, int k2, int m,
+                                void **handle, size_t *smem_bytes) {
+    return create_impl(a1, k1, a2, k2, m, 0, handle, smem_bytes);
+}
+
 int b200_mul_bf16x3_create(const double *a, int m, int k, void **handle, size_t *smem_bytes) {
-    return b200_mul_bf16x3_create_cat(a, k, nullptr, 0, m, handle, smem_bytes);
+    return create_impl(a, k, nullptr, 0, m, 0, handle, smem_bytes);
+}
+
+int b200_mul_tf32_create_cat(const double *a1, int k1, const double *a2, int k2, int m,
+                             void **handle, size_t *smem_bytes) {
+    return create_impl(a1, k1, a2, k2, m, 1, handle, smem_bytes);
+}
+
+int b200_mul_tf32_create(const double *a, int m, int k, void **handle, size_t *smem_bytes) {
+    return create_impl(a, k, nullptr, 0, m, 1, handle, smem_bytes);
 }
 
 int b200_mul_bf16x3_destroy(void *handle) {
@@ -698,7 +805,10 @@ int b200_mul_bf16x3_apply(void *handle, const b200_mul_bf16x3_args_t *a, void *s
 
     const int64_t ntiles = p.ntc * p.nbatch;
     const unsigned grid = (unsigned)(ntiles < g_sm_count ? ntiles : g_sm_count);
-    mul_umma_kernel<<<grid, NTHREADS, h->smem_bytes, (cudaStream_t)stream>>>(p);
+    if (h->tf32)
+        mul_umma_kernel<true><<<grid, NTHREADS, h->smem_bytes, (cudaStream_t)stream>>>(p);
+    else
+        mul_umma_kernel<false><<<grid, NTHREADS, h->smem_bytes, (cudaStream_t)stream>>>(p);
     B200_CHECK_LAUNCH("mul_umma_kernel");
     return B200_OK;
 }

@@ -26,15 +26,22 @@ def built():
 @pytest.mark.parametrize('key', ['hex_p3_gauss-legendre', 'quad_p3_gauss-legendre',
                                  'hex_p2_gauss-legendre'])
 @pytest.mark.parametrize('opname', ['m0', 'M132', 'm3', 'M460', 'm6'])
-def test_mul_bf16x3_tensor_cores(built, golden, key, opname):
-    """Split-BF16 tcgen05 operator apply against an FP64 product: the
-    error of the three-product split is bounded by ~2^-16 |A||B|."""
+@pytest.mark.parametrize('prec', ['bf16x3-3', 'bf16x3-4', 'tf32'])
+def test_mul_tensor_cores(built, golden, key, opname, prec):
+    """tcgen05 operator apply against an FP64 product.  Split BF16 with
+    three products is bounded by ~2^-16 sum|a||b| (bound 1e-4), with four
+    by ~2^-17 (bound 5e-5); TF32 rounds both operands to 11 significant
+    bits, ~2^-10 sum|a||b| (bound 2e-3)."""
     from pyfr_gb300.backend import B200Backend
     from pyfr_gb300.inifile import Inifile
     a = golden['operators'][f'{key}/{opname}']
     cfg = Inifile()
     cfg.set('backend', 'precision', 'single')
-    cfg.set('backend-b200', 'mul-precision', 'bf16x3')
+    mp, _, nprod = prec.partition('-')
+    cfg.set('backend-b200', 'mul-precision', mp)
+    if nprod:
+        cfg.set('backend-b200', 'split-products', nprod)
+    rel = {'bf16x3-3': 1e-4, 'bf16x3-4': 5e-5, 'tf32': 2e-3}[prec]
     be = B200Backend(cfg)
     rng = np.random.default_rng(7)
     for nvars, neles in [(5, 77), (4, 1000)]:
@@ -44,12 +51,12 @@ def test_mul_bf16x3_tensor_cores(built, golden, key, opname):
         B = be.matrix(b.shape, b, tags={'align'})
         C = be.matrix(c0.shape, c0, tags={'align'})
         be.commit()
-        bound = 1e-4*np.einsum('mk,kve->mve', np.abs(a), np.abs(b)) + 1e-6
+        bound = rel*np.einsum('mk,kve->mve', np.abs(a), np.abs(b)) + 1e-6
         for alpha, beta in [(1.0, 0.0), (1.0, 1.0), (-0.5, 1.0), (2.0, 0.25)]:
             C.set(c0)
             k = be.kernel('mul', A, B, out=C, alpha=alpha, beta=beta)
             # The tensor-core epilogue stores or adds; other beta fall back
-            assert k.meta['impl'] == ('bf16x3' if beta in (0.0, 1.0) else 'csr')
+            assert k.meta['impl'] == (mp if beta in (0.0, 1.0) else 'csr')
             be.run_kernels([k], wait=True)
             ref = alpha*np.einsum('mk,kve->mve', a, b.astype(np.float32)) + \
                 beta*c0.astype(np.float32)
