@@ -151,7 +151,7 @@ __device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity, volatile
     for (long long it = 0; it < WAIT_LIMIT; it++) {
         if (bar_try(bar, parity)) return true;
         if (*abort_flag) return false;
-        if (it > 32) __nanosleep(64);
+        if (it > 4096) __nanosleep(64);
     }
     *abort_flag = 1;
     atomicCAS(err, 0, code);
@@ -162,7 +162,7 @@ __device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity, volatile
 // land before the CTA exits
 __device__ __forceinline__ void bar_drain(uint32_t bar, uint32_t parity) {
     for (long long it = 0; it < WAIT_LIMIT && !bar_try(bar, parity); it++)
-        if (it > 32) __nanosleep(64);
+        if (it > 4096) __nanosleep(64);
 }
 
 __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes,
@@ -261,6 +261,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
     const Layout L = make_layout(p.npad, p.kfull, p.ns, p.eb);
     const int eb = p.eb;
     const int NS = p.ns;
+    // (the host plans an even ring of at least four stages; see create)
+    if ((NS & 1) || NS < 4 || NS > MAX_S) {
+        if (threadIdx.x == 0) atomicCAS(p.err, 0, 9);
+        return;
+    }
     const uint32_t sbase = smem_addr(smem);
     const uint32_t bar0 = sbase + L.bar;
     auto bar = [&](int i) { return bar0 + 8u * i; };
@@ -459,8 +464,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
                 umma_commit(bar(BAR_ACCFULL + bsel));
             }
             // Drain: every MMA issued so far has completed once this arrives
+            // (waited for even after an abort: tensor memory is released
+            // when the CTA ends)
             umma_commit(bar(BAR_DRAIN));
-            bar_wait(bar(BAR_DRAIN), 0, abort_flag, p.err, 7);
+            bar_drain(bar(BAR_DRAIN), 0);
         }
         __syncwarp();
     } else {
@@ -472,30 +479,37 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
         const int quad = warp % 4, half = warp / 4;
         const bool issuer = quad == 0 && lane == 0;
         int i = 0, sb = 0;
+        // Row-scale factors alpha*S[row, element] of row group g for this
+        // thread's column (alpha alone without a scale)
+        auto load_scale = [&](float *f, int g, int64_t col, int64_t ele) {
+            if (p.rs) {
+#pragma unroll
+                for (int r = 0; r < 32; r++)
+                    f[r] = col < p.ncol && g * 32 + r < p.m
+                               ? p.alpha * __ldg(p.rs + (int64_t)(g * 32 + r) * p.ldr + ele)
+                               : 0.f;
+            } else {
+#pragma unroll
+                for (int r = 0; r < 32; r++) f[r] = p.alpha;
+            }
+        };
         for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
             const int bsel = i & 1;
-            const bool ok = bar_wait(bar(BAR_ACCFULL + bsel), (i >> 1) & 1, abort_flag, p.err, 8);
-            asm volatile("bar.sync %0, %1;" :: "r"(EPI_BARRIER + half), "n"(128) : "memory");
-            if (!ok || *abort_flag) break;
-            asm volatile("tcgen05.fence::after_thread_sync;");
             const int64_t x0 = (t % p.ntc) * TCOLS;
             const int z = (int)(t / p.ntc);
             // Element of this thread's column (AoSoA: blocks of 32 elements
             // with the variables of a block contiguous), for the row scale
             const int64_t col = x0 + quad * 32 + lane;
             const int64_t ele = (col / (32 * p.nvars)) * 32 + col % 32;
+            // The first group's scale loads are in flight during the wait
+            float f[32];
+            load_scale(f, half, col, ele);
+            const bool ok = bar_wait(bar(BAR_ACCFULL + bsel), (i >> 1) & 1, abort_flag, p.err, 8);
+            asm volatile("bar.sync %0, %1;" :: "r"(EPI_BARRIER + half), "n"(128) : "memory");
+            if (!ok || *abort_flag) break;
+            asm volatile("tcgen05.fence::after_thread_sync;");
             for (int g = half; g < npad / 32; g += 2) {
-                float f[32];
-                if (p.rs) {
-#pragma unroll
-                    for (int r = 0; r < 32; r++)
-                        f[r] = col < p.ncol && g * 32 + r < p.m
-                                   ? p.alpha * __ldg(p.rs + (int64_t)(g * 32 + r) * p.ldr + ele)
-                                   : 0.f;
-                } else {
-#pragma unroll
-                    for (int r = 0; r < 32; r++) f[r] = p.alpha;
-                }
+                if (g != half) load_scale(f, g, col, ele);
                 uint32_t v[32];
                 const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) +
                                        (uint32_t)(bsel * npad + g * 32);
@@ -641,14 +655,18 @@ int create_impl(const double *a1, int k1, const double *a2, int k2, int m, int t
     const int npad = (m + 31) / 32 * 32, kfull = (nch1 + nch2) * KC;
     // The deepest ring (bytes in flight per SM) that fits in shared memory
     // with two staging tiles per epilogue set, or failing four stages that
-    // way, with one.  An operator of at most 64 rows gives each set one
+    // way, with one.  The ring has an even number of stages: each converter
+    // group takes every other chunk, so with an even ring a stage's previous
+    // chunk belongs to the same group, which has consumed it before it waits
+    // for the stage again (with an odd ring the group could take the phase
+    // of the other group's pending chunk, one phase back, for its own).  An operator of at most 64 rows gives each set one
     // store per tile, which a second staging tile would not overlap with
     // anything: it takes one and the ring the room.
     int ns = 0, eb = npad <= 64 ? 1 : MAX_EB;
     Layout L = make_layout(npad, kfull, 2, eb);
     for (; eb >= 1 && ns < 4; eb--) {
         ns = 0;
-        for (int cand = MAX_S; cand >= 3 && !ns; cand--) {
+        for (int cand = MAX_S; cand >= 4 && !ns; cand -= 2) {
             Layout c = make_layout(npad, kfull, cand, eb);
             if (c.total <= 227 * 1024) {
                 ns = cand;
@@ -659,7 +677,7 @@ int create_impl(const double *a1, int k1, const double *a2, int k2, int m, int t
     }
     if (eb < 1) eb = 1;
     if (smem_bytes) *smem_bytes = L.total;
-    if (npad > MAX_N || !ns || L.total > 227 * 1024)
+    if (npad > MAX_N || !ns || (ns & 1) || L.total > 227 * 1024)
         return b200::set_error(B200_ERR_UNSUPPORTED,
                                "mul_bf16x3: operator %dx(%d+%d) needs %u bytes of shared memory "
                                "(or more than %d rows)", m, k1, k2, L.total, MAX_N);
