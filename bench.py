@@ -397,6 +397,83 @@ def run_gpu(args, dist):
     return out
 
 
+def run_large(args, dist):
+    """The large configuration: the chosen form on an n^3 TGV (memory model
+    large, 64-bit gather maps) under the PI controller (rtol = atol =
+    1e-6, error norm reduced in FP64) for a number of accepted steps, and
+    the plain FP64 form on a smaller mesh with fixed steps for comparison.
+    GDoF/s counts every RHS evaluation, rejected attempts included."""
+    import ctypes as C
+
+    import __graft_entry__ as ge
+    from pyfr_gb300.backend import B200Backend
+    from pyfr_gb300.cases import ns_tgv
+    from pyfr_gb300.integrators import MixedRKIntegrator, RKVdH2Integrator
+    from pyfr_gb300.solvers.system import NavierStokesSystem
+    ge.build_library()
+
+    def timed(intg, fn):
+        lib, stream = intg.backend.lib, intg.backend.stream
+        ev = [C.c_void_p(), C.c_void_p()]
+        for e in ev:
+            lib.event_create(C.byref(e))
+        intg.backend.wait()
+        dist.barrier()
+        with ClockSampler(args.local_rank) as clk:
+            lib.event_record(ev[0].value, stream)
+            out = fn()
+            lib.event_record(ev[1].value, stream)
+            lib.event_sync(ev[1].value)
+        ms = C.c_float()
+        lib.event_elapsed(C.byref(ms), ev[0].value, ev[1].value)
+        return out, dist.allmax(ms.value), clk.summary()
+
+    res = {}
+    t0 = time.perf_counter()
+    cfg, mesh = ns_tgv(n=args.large_n, order=3, dt=args.dt, precision='single',
+                       memory_model='large')
+    cfg.set('backend-b200', 'device-id', str(args.local_rank))
+    cfg.set('backend-b200', 'mul-precision', 'bf16x3')
+    cfg.set('backend-b200', 'split-products', str(args.chosen_products))
+    sect = 'solver-time-integrator'
+    cfg.set(sect, 'controller', 'pi')
+    cfg.set(sect, 'rtol', '1e-6')
+    cfg.set(sect, 'atol', '1e-6')
+    intg = MixedRKIntegrator(B200Backend(cfg), NavierStokesSystem, mesh, cfg)
+    setup_s = time.perf_counter() - t0
+    intg.run_pi_steps(2)                  # warm-up (graph captures)
+    n0, r0 = intg.nacptsteps, intg.nrjctsteps
+    attempts, ms, clk = timed(intg, lambda: intg.run_pi_steps(args.large_steps))
+    nrhs = attempts*intg.nstages
+    be = intg.backend
+    res['chosen'] = {
+        'neles': args.large_n**3, 'ndofs': intg.gndofs,
+        'accepted_steps': intg.nacptsteps - n0,
+        'rejected_steps': intg.nrjctsteps - r0,
+        'dt_final': intg.dt, 't_final': intg.tcurr,
+        'ms': ms, 'gdofs': dist.world*intg.gndofs*nrhs/(ms*1e-3)/1e9,
+        'device_gb': be.memory_info().peak/1e9, 'setup_s': setup_s,
+        'clocks': clk}
+    del intg, be
+
+    t0 = time.perf_counter()
+    cfg, mesh = ns_tgv(n=args.large_plain_n, order=3, dt=args.dt,
+                       precision='double', memory_model='large')
+    cfg.set('backend-b200', 'device-id', str(args.local_rank))
+    intg = RKVdH2Integrator(B200Backend(cfg), NavierStokesSystem, mesh, cfg)
+    setup_s = time.perf_counter() - t0
+    intg.run_steps(1)
+    _, ms, clk = timed(intg, lambda: intg.run_steps(args.large_plain_steps))
+    nrhs = args.large_plain_steps*intg.nstages
+    res['plain'] = {
+        'neles': args.large_plain_n**3, 'ndofs': intg.gndofs,
+        'steps': args.large_plain_steps, 'ms': ms,
+        'gdofs': dist.world*intg.gndofs*nrhs/(ms*1e-3)/1e9,
+        'device_gb': intg.backend.memory_info().peak/1e9, 'setup_s': setup_s,
+        'clocks': clk}
+    return res
+
+
 # ---------------------------------------------------------------------------
 # CPU arm (the oracle restatement, bounded sample)
 # ---------------------------------------------------------------------------
@@ -450,6 +527,14 @@ def main():
                     help='steps after which the chosen form is compared '
                          'with FP64')
     ap.add_argument('--ke-every', type=int, default=10)
+    ap.add_argument('--large', action='store_true',
+                    help='the large configuration (chosen form at '
+                         '--large-n^3 under the PI controller, plain FP64 at '
+                         '--large-plain-n^3) instead of the headline run')
+    ap.add_argument('--large-n', type=int, default=128)
+    ap.add_argument('--large-steps', type=int, default=100)
+    ap.add_argument('--large-plain-n', type=int, default=96)
+    ap.add_argument('--large-plain-steps', type=int, default=5)
     ap.add_argument('--only', choices=['plain', 'chosen', 'bf16x3', 'tf32',
                                        'fp32'],
                     help='time one precision form alone (no accuracy '
@@ -489,6 +574,23 @@ def main():
                              'sample': sample},
             'e2e': {'value': v, 'unit': 'GDoF/s', 'h2d_bytes_per_step': 0,
                     'd2h_bytes_per_step': 0}}))
+        return
+
+    if args.large:
+        r = run_large(args, Dist(world))
+        if rank == 0:
+            print(json.dumps({
+                'metric': METRIC, 'unit': 'GDoF/s', 'n_gpus': world,
+                'config': {
+                    'workload': f'3-D Navier-Stokes Taylor-Green vortex, '
+                                f'{args.large_n}^3 hex, p=3, chosen form, '
+                                'RK45 with the PI controller (rtol = atol = '
+                                '1e-6, FP64 error norm), memory-model large; '
+                                f'plain FP64 at {args.large_plain_n}^3',
+                    'accepted_steps': args.large_steps},
+                'data': 'synthetic', 'chosen': r['chosen'],
+                'plain': r['plain'],
+                'speedup_vs_plain': r['chosen']['gdofs']/r['plain']['gdofs']}))
         return
 
     if args.only:

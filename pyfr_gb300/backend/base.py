@@ -47,6 +47,10 @@ def _free_allocs(lib, allocs):
             pass
     allocs.clear()
 
+# Constants up to this many elements keep a host copy after set-up (for
+# reuse of identical constants and for the operator handles)
+HOST_KEEP = 1 << 20
+
 MemoryInfo = namedtuple('MemoryInfo', ['current', 'peak', 'free', 'total'])
 
 
@@ -307,8 +311,9 @@ class B200Backend:
         dtype = dtype or self.fpdtype
         initval = np.asarray(initval)
 
-        # Reuse an identical constant (pyfr/backends/base/backend.py:134-145)
-        for m in list(self.mats.values()):
+        # Reuse an identical constant (pyfr/backends/base/backend.py:134-145);
+        # only small constants (operators) are compared
+        for m in list(self.mats.values()) if initval.size <= HOST_KEEP else []:
             if (isinstance(m, self.const_matrix_cls) and
                 m.dtype == np.dtype(dtype) and m.ioshape == initval.shape and
                 set(tags).issubset(m.tags) and
@@ -319,6 +324,15 @@ class B200Backend:
         m = self.const_matrix_cls(self, dtype, initval, tags)
         m._host = np.array(initval, dtype=dtype)
         return m
+
+    def release_host_copies(self):
+        """Drop the host copies of large constants (geometry, gather maps):
+        they serve the set-up only; operators keep theirs."""
+        for m in list(self.mats.values()):
+            h = getattr(m, '_host', None)
+            if isinstance(m, self.const_matrix_cls) and h is not None and \
+                    h.size > HOST_KEEP:
+                del m._host
 
     @_recordmat
     def matrix(self, ioshape, initval=None, extent=None, tags=set(),

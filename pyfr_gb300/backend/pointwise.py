@@ -14,6 +14,8 @@ import ctypes as C
 
 import numpy as np
 
+from pyfr_gb300.shapes import adjugate_det
+
 from pyfr_gb300.backend.lib import Gas
 from pyfr_gb300.backend.types import BindableKernel, Kernel, NullKernel
 
@@ -53,17 +55,10 @@ def linear_metrics(verts, upts):
         for k in range(nd):
             t = t*(sg[None, :, k] if k == i else 1 + x[:, None, k]*sg[None, :, k])
         dN[:, i] = t/nverts
-    J = np.einsum('piv,vje->pije', dN, verts)          # (p, i, j, e)
-    S = np.empty_like(J)
-    if nd == 2:
-        S[:, 0, 0], S[:, 0, 1] = J[:, 1, 1], -J[:, 1, 0]
-        S[:, 1, 0], S[:, 1, 1] = -J[:, 0, 1], J[:, 0, 0]
-        d = S[:, 0, 0]*S[:, 1, 1] - S[:, 0, 1]*S[:, 1, 0]
-    else:
-        for i in range(3):
-            a, b = (i + 1) % 3, (i + 2) % 3
-            S[:, i] = np.cross(J[:, a], J[:, b], axisa=1, axisb=1, axisc=1)
-        d = np.einsum('pje,pje->pe', J[:, 0], S[:, 0])
+    # J[p, i, j, e] as one matrix product over the vertex index
+    npt = len(x)
+    J = (dN.reshape(npt*nd, nverts) @ verts.reshape(nverts, nd*ne))
+    S, d = adjugate_det(J.reshape(npt, nd, nd, ne))
     return S.transpose(1, 0, 2, 3), 1.0/d
 
 

@@ -86,7 +86,11 @@ class RKVdH2Integrator:
             convars = self.system.ele_map[self.system.ele_types[0]].convars
             atols = [cfg.getfloat(sect, f'atol-{v}', cfg.getfloat(sect, 'atol'))
                      for v in convars]
-            if any(a < 10*backend.fpdtype_eps for a in atols):
+            # (tolerances are checked against the precision of the stored
+            # solution, as pyfr/integrators/controllers.py:57-72 does)
+            if self._rtol < 10*self.state_eps:
+                raise ValueError('Relative tolerance too small')
+            if any(a < 10*self.state_eps for a in atols):
                 raise ValueError('Absolute tolerance too small')
             self._atols = atols
             self._saffac = cfg.getfloat(sect, 'safety-fact', 0.8)
@@ -211,26 +215,50 @@ class RKVdH2Integrator:
                 self.nacptsteps += 1
                 continue
 
-            icurr, iprev, ierr = self.step(self.tcurr, dt)
-            err = self._errest(icurr, ierr)
-            expa = self._pi_alpha / self.stepper_order
-            expb = self._pi_beta / self.stepper_order
-            fac = err**-expa * self._errprev**expb
-            fac = min(self._maxfac, max(self._minfac, self._saffac*fac))
-            self.dt = max(fac*dt, self.dtmin)
-
-            if err < 1.0:
-                self._errprev = err
-                self.idxcurr = icurr
-                self.tcurr += dt
-                self.nacptsteps += 1
-            else:
-                if dt <= self.dtmin:
-                    raise RuntimeError('Minimum sized time step rejected')
-                self._reject(iprev)
-                self.nrjctsteps += 1
+            self._pi_step(dt)
 
         self.backend.wait()
+
+    def _pi_step(self, dt):
+        """One attempted step of size dt under the PI controller
+        (pyfr/integrators/explicit/controllers.py:87-125); returns whether
+        it was accepted."""
+        icurr, iprev, ierr = self.step(self.tcurr, dt)
+        err = self._errest(icurr, ierr)
+        expa = self._pi_alpha / self.stepper_order
+        expb = self._pi_beta / self.stepper_order
+        # (an exactly zero error, a steady solution, takes the largest
+        # growth factor instead of dividing by zero)
+        fac = max(err, 1e-300)**-expa * self._errprev**expb
+        fac = min(self._maxfac, max(self._minfac, self._saffac*fac))
+        self.dt = max(fac*dt, self.dtmin)
+
+        if err < 1.0:
+            self._errprev = err
+            self.idxcurr = icurr
+            self.tcurr += dt
+            self.nacptsteps += 1
+            return True
+
+        if dt <= self.dtmin:
+            raise RuntimeError('Minimum sized time step rejected')
+        self._reject(iprev)
+        self.nrjctsteps += 1
+        return False
+
+    def run_pi_steps(self, nsteps):
+        """Take nsteps accepted steps under the PI controller (rejected
+        attempts are retried with the reduced dt); returns the number of
+        attempts."""
+        if self.controller != 'pi':
+            raise ValueError('run_pi_steps needs controller = pi')
+        attempts = 0
+        target = self.nacptsteps + nsteps
+        while self.nacptsteps < target:
+            self._pi_step(min(self.dt, self.dtmax))
+            attempts += 1
+        self.backend.wait()
+        return attempts
 
     def run_steps(self, nsteps, dt=None):
         """Advance a fixed number of steps of size dt (default the
@@ -241,6 +269,11 @@ class RKVdH2Integrator:
             self.idxcurr = idx
             self.tcurr += dt
         self.backend.wait()
+
+    @property
+    def state_eps(self):
+        """Machine epsilon of the stored solution."""
+        return self.backend.fpdtype_eps
 
     @property
     def soln(self):
@@ -344,6 +377,11 @@ class MixedRKIntegrator(RKVdH2Integrator):
         be.commit()
         self.refresh_input(be.stream)
         be.wait()
+
+    @property
+    def state_eps(self):
+        # The solution and the error registers are FP64
+        return float(np.finfo(np.float64).eps)
 
     def to_q(self, u):
         """Solution (nupts, nvars, neles) -> the integrated variables."""

@@ -249,3 +249,25 @@ def get_shape(name, order, upts_rule='gauss-legendre',
         return SHAPES[name](order, upts_rule, fpts_rule)
     except KeyError:
         raise ValueError(f'Unsupported element type {name!r}') from None
+
+
+def adjugate_det(J):
+    """Adjugate (transposed cofactor) metric S and determinant of Jacobians
+    J[p, i, j, e] = dx_j/dxi_i: S[p, i, k] is the cross product of rows
+    i+1 and i+2 (3-D) so that S^T J = |J| I, the metric terms of
+    pyfr/solvers/baseadvec/kernels/smats.mako:3-25."""
+    S = np.empty_like(J)
+    if J.shape[1] == 2:
+        S[:, 0, 0], S[:, 0, 1] = J[:, 1, 1], -J[:, 1, 0]
+        S[:, 1, 0], S[:, 1, 1] = -J[:, 0, 1], J[:, 0, 0]
+        d = S[:, 0, 0]*S[:, 1, 1] - S[:, 0, 1]*S[:, 1, 0]
+    else:
+        Jc = [[np.ascontiguousarray(J[:, i, j]) for j in range(3)]
+              for i in range(3)]
+        for i in range(3):
+            a, b = Jc[(i + 1) % 3], Jc[(i + 2) % 3]
+            for k in range(3):
+                k1, k2 = (k + 1) % 3, (k + 2) % 3
+                S[:, i, k] = a[k1]*b[k2] - a[k2]*b[k1]
+        d = Jc[0][0]*S[:, 0, 0] + Jc[0][1]*S[:, 0, 1] + Jc[0][2]*S[:, 0, 2]
+    return S, d

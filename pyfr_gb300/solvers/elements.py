@@ -22,7 +22,7 @@ import numpy as np
 
 from pyfr_gb300.backend.types import NullKernel
 from pyfr_gb300.mesh import fuzzy_face_order
-from pyfr_gb300.shapes import get_shape
+from pyfr_gb300.shapes import adjugate_det, get_shape
 
 
 _NPEVAL_SYMS = {k: getattr(np, k) for k in
@@ -72,29 +72,28 @@ class BaseElements:
     def ploc_at_np(self, pts):
         pts = getattr(self.basis, pts) if isinstance(pts, str) else pts
         sf = self.basis.shape_fn(pts)                    # (npts, nverts)
-        ploc = np.einsum('pv,ved->pde', sf, self.eles)
-        return ploc
+        # (as one matrix product: sf @ eles over the vertex index)
+        nv, ne, nd = self.eles.shape
+        ploc = (sf @ self.eles.reshape(nv, ne*nd)).reshape(-1, ne, nd)
+        return ploc.transpose(0, 2, 1)                   # (npts, ndims, neles)
 
     def _jac_at(self, pts):
         pts = getattr(self.basis, pts) if isinstance(pts, str) else pts
         dsf = self.basis.shape_jac(pts)                  # (npts, i, nverts)
-        return np.einsum('piv,vej->pije', dsf, self.eles)
+        npt, ni, nv = dsf.shape
+        _, ne, nd = self.eles.shape
+        J = dsf.reshape(npt*ni, nv) @ self.eles.reshape(nv, ne*nd)
+        return J.reshape(npt, ni, ne, nd).transpose(0, 1, 3, 2)  # (p, i, j, e)
 
     def smats_djac_at_np(self, pts):
         """Adjugate metric S[i][j] (npts, ndims, ndims, neles) and |J|."""
-        J = self._jac_at(pts)
-        if self.ndims == 2:
-            s = np.empty_like(J)
-            s[:, 0, 0], s[:, 0, 1] = J[:, 1, 1], -J[:, 1, 0]
-            s[:, 1, 0], s[:, 1, 1] = -J[:, 0, 1], J[:, 0, 0]
-            d = s[:, 0, 0]*s[:, 1, 1] - s[:, 0, 1]*s[:, 1, 0]
-        else:
-            s = np.empty_like(J)
-            for i in range(3):
-                a, b = (i + 1) % 3, (i + 2) % 3
-                s[:, i] = np.cross(J[:, a], J[:, b], axisa=1, axisb=1,
-                                   axisc=1)
-            d = np.einsum('pje,pje->pe', J[:, 0], s[:, 0])
+        key = pts if isinstance(pts, str) else None
+        cache = self.__dict__.setdefault('_smats_cache', {})
+        if key in cache:
+            return cache[key]
+        s, d = adjugate_det(self._jac_at(pts))
+        if key is not None:
+            cache[key] = (s, d)
         return s, d
 
     def smat_at_np(self, pts):
@@ -217,6 +216,11 @@ class BaseElements:
             self.__dict__[key] = self._be.const_matrix(
                 self.basis.opmat(expr), tags={expr, 'align'})
         return self.__dict__[key]
+
+    def release_host_geometry(self):
+        """Drop cached host-side metric arrays (recomputed if needed)."""
+        for k in ('_smats_cache', '_pnorm_fpts', 'plocfpts'):
+            self.__dict__.pop(k, None)
 
     def _cached(self, key, fn):
         if key not in self.__dict__:

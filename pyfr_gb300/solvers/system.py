@@ -110,6 +110,12 @@ class BaseSystem:
         self.backend.commit()
         self._graph_cache = {}
 
+        # Host-side geometry and gather maps were only needed to build the
+        # kernels
+        for e in self.ele_map.values():
+            e.release_host_geometry()
+        self.backend.release_host_copies()
+
     def _gen_kernels(self):
         self._kernels = kernels = defaultdict(list)
         self._ktags = {}

@@ -156,6 +156,32 @@ def test_ns_rhs_tgv(built, beta, tau, rsolver):
     assert _relerr(r, ref) < TOL
 
 
+@pytest.mark.parametrize('prec', ['double', 'single'])
+def test_ns_rhs_large_memory_model(built, prec):
+    """memory-model = large: 64-bit interface gather maps (the reference's
+    ixdtype int64), as the 128^3 configuration needs; same RHS as the
+    oracle (FP64: 1e-10; FP32: 1e-4 of p0/h)."""
+    from pyfr_gb300.cases import ns_tgv
+    from pyfr_gb300.solvers.system import NavierStokesSystem
+    cfg, mesh = ns_tgv(n=4, order=3, precision=prec)
+    cfg.set('backend', 'memory-model', 'large')
+    be = _backend(cfg)
+    assert be.ixdtype == np.int64
+    s = NavierStokesSystem(be, mesh, None, 2, cfg)
+    s.commit()
+    s.rhs(0.0, 0, 1)
+    (u,), (r,) = s.ele_scal_upts(0), s.ele_scal_upts(1)
+
+    d = disc_for_mesh(mesh, 3, ns=True)
+    c = cfg.items_as('constants', float) | cfg.items_as('solver-interfaces',
+                                                       float)
+    ref = d.rhs_ns(u.astype(np.float64), c)
+    if prec == 'double':
+        assert _relerr(r, ref) < TOL
+    else:
+        assert np.abs(r - ref).max() <= 1e-4*c['p0']/(2*np.pi/4)
+
+
 @pytest.mark.parametrize('graphs', [True, False])
 def test_rk45_vortex_steps(built, graphs):
     from pyfr_gb300.cases import euler_vortex
