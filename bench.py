@@ -18,6 +18,7 @@ import argparse
 import json
 import math
 import os
+import resource
 import statistics
 import subprocess
 import sys
@@ -590,7 +591,9 @@ def main():
                     'accepted_steps': args.large_steps},
                 'data': 'synthetic', 'chosen': r['chosen'],
                 'plain': r['plain'],
-                'speedup_vs_plain': r['chosen']['gdofs']/r['plain']['gdofs']}))
+                'speedup_vs_plain': r['chosen']['gdofs']/r['plain']['gdofs'],
+                'host_maxrss_gb': resource.getrusage(
+                    resource.RUSAGE_SELF).ru_maxrss/2**20}))
         return
 
     if args.only:

@@ -260,6 +260,17 @@ int b200_rkvdh2_f32(int64_t n, int stage, int nstages, int errest, double dt, do
                     double b, double e, float *r1, float *r2, float *rold, float *rerr,
                     void *stream);
 
+/* Same with the step size read from device memory at run time (dt_dev: one
+ * double), so that one captured step graph serves every dt an adaptive
+ * controller picks (the reference rebinds the kernel argument instead,
+ * pyfr/backends/cuda/provider.py:15-125). */
+int b200_rkvdh2_dt_f64(int64_t n, int stage, int nstages, int errest, const double *dt_dev,
+                       double a, double b, double e, double *r1, double *r2, double *rold,
+                       double *rerr, void *stream);
+int b200_rkvdh2_dt_f32(int64_t n, int stage, int nstages, int errest, const double *dt_dev,
+                       double a, double b, double e, float *r1, float *r2, float *rold,
+                       float *rerr, void *stream);
+
 /* Mixed-precision form of the rkvdh2 stage (FP32 right-hand side, FP64
  * solution accumulator): acc <- acc + dt*b*rhs in FP64 and u32 <- the next
  * stage's FP32 input, fl32(acc) + fl32(dt*a)*rhs formed in FP32 (the new
@@ -271,6 +282,10 @@ int b200_rkvdh2_f32(int64_t n, int stage, int nstages, int errest, double dt, do
 int b200_rkmixed_f64f32(int64_t n, int stage, int nstages, int errest, double dt, double a,
                         double b, double e, double *acc, const float *rhs, float *u32,
                         double *rold, double *rerr, void *stream);
+/* Same with the step size read from device memory (dt_dev: one double). */
+int b200_rkmixed_dt_f64f32(int64_t n, int stage, int nstages, int errest, const double *dt_dev,
+                           double a, double b, double e, double *acc, const float *rhs,
+                           float *u32, double *rold, double *rerr, void *stream);
 /* dst <- (float)(src - uref[v]) over n scalars of an AoSoA field with
  * nvars variables (uref null: no shift). */
 int b200_cast_f64_f32(int64_t n, const double *src, float *dst, int nvars, const double *uref,

@@ -57,6 +57,8 @@ def _sig_pointwise(fp):
         'intconu_both': [i32, i64, f64, vp, vp, vp, vp, vp, vp, vp, vp, i32,
                          vp],
         'rkvdh2': [i64, i32, i32, i32, f64, f64, f64, f64, vp, vp, vp, vp, vp],
+        'rkvdh2_dt': [i64, i32, i32, i32, vp, f64, f64, f64, vp, vp, vp, vp,
+                      vp],
         'axnpby': [i64, i32, vp, C.POINTER(vp), C.POINTER(f64), vp],
         'errest': [i32, i32, i64, i64, vp, vp, vp, f64, i32, vp, i32, vp, vp],
         'mul': [vp, vp, i64, vp, i64, i64, fp, fp, vp],
@@ -94,6 +96,8 @@ _SIGS = {
     'b200_mul_destroy': [vp],
     'b200_rkmixed_f64f32': [i64, i32, i32, i32, f64, f64, f64, f64, vp, vp,
                             vp, vp, vp, vp],
+    'b200_rkmixed_dt_f64f32': [i64, i32, i32, i32, vp, f64, f64, f64, vp, vp,
+                               vp, vp, vp, vp],
     'b200_cast_f64_f32': [i64, vp, vp, i32, vp, vp],
     'b200_integrals_f64': [i32, i32, i64, vp, i64, vp, i64, vp, i64, vp, i32,
                            vp, vp],

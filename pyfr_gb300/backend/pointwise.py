@@ -297,21 +297,32 @@ class PointwiseKernelProvider:
     # ---- integrator kernels ----------------------------------------------------
 
     def _rkvdh2(self, tplargs, dims, extrns, r1, r2, rold=None, rerr=None,
-                dt=None):
+                dt=None, dtdev=None):
+        """The rkvdh2 stage; with ``dtdev`` (a 1x1 FP64 matrix) the step
+        size is read from device memory at run time, so that a captured
+        step serves every dt and the bound dt is not used."""
         stage, nstages = tplargs['stage'], tplargs['nstages']
         errest = bool(tplargs['errest'])
         a = tplargs['a'][stage] if stage < nstages - 1 else 0.0
         b = tplargs['b'][stage]
         e = tplargs['e'][stage] if errest else 0.0
         n = r1.nrow*r1.leaddim
-        fn = self._fn('rkvdh2')
         p1, p2 = r1.data, r2.data
         po = rold.data if rold is not None else None
         pe = rerr.data if rerr is not None else None
 
-        def run(stream, dt):
-            fn(n, stage, nstages, int(errest), dt, a, b, e, p1, p2, po, pe,
-               stream)
+        if dtdev is not None:
+            fnd, pdt = self._fn('rkvdh2_dt'), dtdev.data
+
+            def run(stream, dt):
+                fnd(n, stage, nstages, int(errest), pdt, a, b, e, p1, p2, po,
+                    pe, stream)
+        else:
+            fn = self._fn('rkvdh2')
+
+            def run(stream, dt):
+                fn(n, stage, nstages, int(errest), dt, a, b, e, p1, p2, po,
+                   pe, stream)
 
         return BindableKernel(run, ['dt'], {'dt': dt if dt is not None
                                             else 0.0},

@@ -22,11 +22,37 @@ namespace {
 constexpr int BX_BLOCK = 256;
 constexpr int MAX_AXNPBY = 8;
 
+// Stage coefficients a, b, e and the step size: dt itself, or read from
+// device memory (dtp) so that a captured step graph serves every dt.  The
+// products dt*a, dt*b, dt*e are formed once per block.
+struct StageCoef {
+    const double *dtp;
+    double dt, a, b, e;
+};
+
+__device__ __forceinline__ void stage_products(const StageCoef &c, double &da, double &db,
+                                               double &de) {
+    __shared__ double sh[3];
+    if (threadIdx.x == 0) {
+        const double h = c.dtp ? *c.dtp : c.dt;
+        sh[0] = h * c.a;
+        sh[1] = h * c.b;
+        sh[2] = h * c.e;
+    }
+    __syncthreads();
+    da = sh[0];
+    db = sh[1];
+    de = sh[2];
+}
+
 template <typename T>
 __global__ void __launch_bounds__(BX_BLOCK)
-rkvdh2_kernel(int64_t n, int last, int errest, int first, T dta, T dtb, T dte,
+rkvdh2_kernel(int64_t n, int last, int errest, int first, StageCoef co,
               T *__restrict__ r1, T *__restrict__ r2, T *__restrict__ rold,
               T *__restrict__ rerr) {
+    double da, db, de;
+    stage_products(co, da, db, de);
+    const T dta = (T)da, dtb = (T)db, dte = (T)de;
     for (int64_t i = (int64_t)blockIdx.x * BX_BLOCK + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * BX_BLOCK) {
         const T t1 = r1[i], t2 = r2[i];
@@ -83,9 +109,12 @@ __device__ __forceinline__ float rkmixed_value(int64_t i, double &t, float rf, i
 // 16-byte FP32 load in flight) over the first n4 quads, scalar after.
 template <bool ERR>
 __global__ void __launch_bounds__(BX_BLOCK)
-rkmixed_kernel(int64_t n, int64_t n4, int last, int first, float dta, double dtb, double dte,
+rkmixed_kernel(int64_t n, int64_t n4, int last, int first, StageCoef co,
                double *__restrict__ acc, const float *__restrict__ rhs, float *__restrict__ u32,
                double *__restrict__ rold, double *__restrict__ rerr) {
+    double da, dtb, dte;
+    stage_products(co, da, dtb, dte);
+    const float dta = (float)da;
     const int64_t stride = (int64_t)gridDim.x * BX_BLOCK;
     const int64_t tid = (int64_t)blockIdx.x * BX_BLOCK + threadIdx.x;
     double2 *acc2 = reinterpret_cast<double2 *>(acc);
@@ -216,16 +245,16 @@ unsigned grid_for(int64_t n) {
 }
 
 template <typename T>
-int rkvdh2(int64_t n, int stage, int nstages, int errest, double dt, double a, double b,
-           double e, T *r1, T *r2, T *rold, T *rerr, cudaStream_t s) {
+int rkvdh2(int64_t n, int stage, int nstages, int errest, const double *dtp, double dt, double a,
+           double b, double e, T *r1, T *r2, T *rold, T *rerr, cudaStream_t s) {
     if (n <= 0) return B200_OK;
     if (stage < 0 || stage >= nstages)
         return b200::set_error(B200_ERR_ARG, "rkvdh2: stage %d out of range", stage);
     if (errest && (!rold || !rerr))
         return b200::set_error(B200_ERR_ARG, "rkvdh2: error estimate needs rold and rerr");
-    rkvdh2_kernel<T><<<grid_for(n), BX_BLOCK, 0, s>>>(
-        n, stage == nstages - 1, errest, stage == 0, (T)(dt * a), (T)(dt * b), (T)(dt * e), r1,
-        r2, rold, rerr);
+    const StageCoef co{dtp, dt, stage == nstages - 1 ? 0.0 : a, b, e};
+    rkvdh2_kernel<T><<<grid_for(n), BX_BLOCK, 0, s>>>(n, stage == nstages - 1, errest, stage == 0,
+                                                      co, r1, r2, rold, rerr);
     B200_CHECK_LAUNCH("rkvdh2");
     return B200_OK;
 }
@@ -333,20 +362,36 @@ int b200_errest_static_f64(int nupts, int nvars, int64_t neles, int64_t ld, cons
 int b200_rkvdh2_f64(int64_t n, int stage, int nstages, int errest, double dt, double a,
                     double b, double e, double *r1, double *r2, double *rold, double *rerr,
                     void *stream) {
-    return rkvdh2<double>(n, stage, nstages, errest, dt, a, b, e, r1, r2, rold, rerr,
+    return rkvdh2<double>(n, stage, nstages, errest, nullptr, dt, a, b, e, r1, r2, rold, rerr,
                           (cudaStream_t)stream);
 }
 
 int b200_rkvdh2_f32(int64_t n, int stage, int nstages, int errest, double dt, double a,
                     double b, double e, float *r1, float *r2, float *rold, float *rerr,
                     void *stream) {
-    return rkvdh2<float>(n, stage, nstages, errest, dt, a, b, e, r1, r2, rold, rerr,
+    return rkvdh2<float>(n, stage, nstages, errest, nullptr, dt, a, b, e, r1, r2, rold, rerr,
                          (cudaStream_t)stream);
 }
 
-int b200_rkmixed_f64f32(int64_t n, int stage, int nstages, int errest, double dt, double a,
-                        double b, double e, double *acc, const float *rhs, float *u32,
-                        double *rold, double *rerr, void *stream) {
+int b200_rkvdh2_dt_f64(int64_t n, int stage, int nstages, int errest, const double *dt_dev,
+                       double a, double b, double e, double *r1, double *r2, double *rold,
+                       double *rerr, void *stream) {
+    if (!dt_dev) return b200::set_error(B200_ERR_ARG, "rkvdh2_dt: null step size");
+    return rkvdh2<double>(n, stage, nstages, errest, dt_dev, 0.0, a, b, e, r1, r2, rold, rerr,
+                          (cudaStream_t)stream);
+}
+
+int b200_rkvdh2_dt_f32(int64_t n, int stage, int nstages, int errest, const double *dt_dev,
+                       double a, double b, double e, float *r1, float *r2, float *rold,
+                       float *rerr, void *stream) {
+    if (!dt_dev) return b200::set_error(B200_ERR_ARG, "rkvdh2_dt: null step size");
+    return rkvdh2<float>(n, stage, nstages, errest, dt_dev, 0.0, a, b, e, r1, r2, rold, rerr,
+                         (cudaStream_t)stream);
+}
+
+static int rkmixed(int64_t n, int stage, int nstages, int errest, const double *dtp, double dt,
+                   double a, double b, double e, double *acc, const float *rhs, float *u32,
+                   double *rold, double *rerr, cudaStream_t s) {
     if (n <= 0) return B200_OK;
     if (stage < 0 || stage >= nstages)
         return b200::set_error(B200_ERR_ARG, "rkmixed: stage %d out of range", stage);
@@ -355,16 +400,30 @@ int b200_rkmixed_f64f32(int64_t n, int stage, int nstages, int errest, double dt
     const int last = stage == nstages - 1;
     const bool aligned = !(((uintptr_t)acc | (uintptr_t)rhs | (uintptr_t)u32) & 15);
     const int64_t n4 = aligned ? n / 4 : 0;
-    const float dta = (float)(dt * (last ? 0.0 : a));
-    auto s = (cudaStream_t)stream;
+    const StageCoef co{dtp, dt, last ? 0.0 : a, b, e};
     if (errest)
         rkmixed_kernel<true><<<grid_for(n / 4 + 1), BX_BLOCK, 0, s>>>(
-            n, n4, last, stage == 0, dta, dt * b, dt * e, acc, rhs, u32, rold, rerr);
+            n, n4, last, stage == 0, co, acc, rhs, u32, rold, rerr);
     else
         rkmixed_kernel<false><<<grid_for(n / 4 + 1), BX_BLOCK, 0, s>>>(
-            n, n4, last, stage == 0, dta, dt * b, dt * e, acc, rhs, u32, rold, rerr);
+            n, n4, last, stage == 0, co, acc, rhs, u32, rold, rerr);
     B200_CHECK_LAUNCH("rkmixed");
     return B200_OK;
+}
+
+int b200_rkmixed_f64f32(int64_t n, int stage, int nstages, int errest, double dt, double a,
+                        double b, double e, double *acc, const float *rhs, float *u32,
+                        double *rold, double *rerr, void *stream) {
+    return rkmixed(n, stage, nstages, errest, nullptr, dt, a, b, e, acc, rhs, u32, rold, rerr,
+                   (cudaStream_t)stream);
+}
+
+int b200_rkmixed_dt_f64f32(int64_t n, int stage, int nstages, int errest, const double *dt_dev,
+                           double a, double b, double e, double *acc, const float *rhs,
+                           float *u32, double *rold, double *rerr, void *stream) {
+    if (!dt_dev) return b200::set_error(B200_ERR_ARG, "rkmixed_dt: null step size");
+    return rkmixed(n, stage, nstages, errest, dt_dev, 0.0, a, b, e, acc, rhs, u32, rold, rerr,
+                   (cudaStream_t)stream);
 }
 
 int b200_cast_f64_f32(int64_t n, const double *src, float *dst, int nvars, const double *uref,

@@ -13,7 +13,9 @@ stage kernels) is captured once per starting register and replayed with a
 single launch.
 """
 
+import ctypes as C
 import math
+import weakref
 
 import numpy as np
 
@@ -76,10 +78,24 @@ class RKVdH2Integrator:
         self.dtmax = cfg.getfloat(sect, 'dt-max', 1e2)
         self.idxcurr = 0
         self.nacptsteps = self.nrjctsteps = self.nsteps = 0
+        self.dt_accepted = []
         self.nrhsevals = 0
         self._step_graphs = {}
         self._kcache = {}
         self.use_step_graph = backend.use_cuda_graphs
+
+        # The step size lives in device memory (staged through page-locked
+        # host memory), so that one captured graph per starting register
+        # serves every dt the controller picks
+        self._dt_dev = backend.matrix((1, 1), dtype=np.float64)
+        backend.commit()
+        self._dt_host = C.c_void_p()
+        backend.lib.host_alloc(C.byref(self._dt_host), 8)
+        weakref.finalize(self, backend.lib.host_free, self._dt_host.value)
+        self._dt_evt = C.c_void_p()
+        backend.lib.event_create(C.byref(self._dt_evt))
+        weakref.finalize(self, backend.lib.event_destroy, self._dt_evt.value)
+        self._dt_set = None
 
         if self.errest:
             self._rtol = cfg.getfloat(sect, 'rtol')
@@ -130,6 +146,8 @@ class RKVdH2Integrator:
                 kw = dict(r1=em[r1], r2=em[r2])
                 if rold is not None:
                     kw |= dict(rold=em[rold], rerr=em[rerr])
+                if self.use_step_graph:
+                    kw['dtdev'] = self._dt_dev
                 kerns.append(self.backend.kernel(
                     'rkvdh2', tplargs=tplargs, dims=[dims[0], dims[2]], **kw))
             self._kcache[key] = kerns
@@ -162,14 +180,25 @@ class RKVdH2Integrator:
             k.run(stream)
         return regs
 
+    def _set_dt(self, dt, stream):
+        """Enqueue the copy of a new step size to device memory (a no-op
+        while dt is unchanged)."""
+        if dt != self._dt_set:
+            lib = self.backend.lib
+            # The staging buffer is reused once the previous copy has run
+            if self._dt_set is not None:
+                lib.event_sync(self._dt_evt.value)
+            C.c_double.from_address(self._dt_host.value).value = dt
+            lib.memcpy_htod(self._dt_dev.data, self._dt_host.value, 8, stream)
+            lib.event_record(self._dt_evt.value, stream)
+            self._dt_set = dt
+
     def step(self, t, dt):
         be, stream = self.backend, self.backend.stream
         if self.use_step_graph:
-            key = (self.idxcurr, dt)
+            self._set_dt(dt, stream)
+            key = self.idxcurr
             if key not in self._step_graphs:
-                # Retire graphs captured for another dt
-                for k in [k for k in self._step_graphs if k[1] != dt]:
-                    be.release_gexec(self._step_graphs.pop(k)[0])
                 res = []
                 gexec = be.capture(
                     lambda s: res.append(self._enqueue_step(t, dt,
@@ -238,6 +267,7 @@ class RKVdH2Integrator:
             self.idxcurr = icurr
             self.tcurr += dt
             self.nacptsteps += 1
+            self.dt_accepted.append(dt)
             return True
 
         if dt <= self.dtmin:
@@ -418,9 +448,16 @@ class MixedRKIntegrator(RKVdH2Integrator):
         re = self.rerr[j].data if self.errest else None
         pa, pr, pu = acc.data, bank[1].data, bank[0].data
 
-        def run(stream):
-            lib.rkmixed_f64f32(n, i, nst, errest, dt, a, b, e, pa, pr, pu, ro,
-                               re, stream)
+        if self.use_step_graph:
+            pdt = self._dt_dev.data
+
+            def run(stream):
+                lib.rkmixed_dt_f64f32(n, i, nst, errest, pdt, a, b, e, pa, pr,
+                                      pu, ro, re, stream)
+        else:
+            def run(stream):
+                lib.rkmixed_f64f32(n, i, nst, errest, dt, a, b, e, pa, pr,
+                                   pu, ro, re, stream)
 
         return Kernel(run, mats=[acc, bank[0], bank[1]], name='rkmixed',
                       meta=dict(kind='rkmixed', n=n))

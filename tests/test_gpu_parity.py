@@ -183,6 +183,35 @@ def test_ns_rhs_large_memory_model(built, prec):
 
 
 @pytest.mark.parametrize('graphs', [True, False])
+def test_pi_controller_steps(built, graphs):
+    """Adaptive RK45 under the PI controller (the step size read from
+    device memory inside the captured step graphs): the accepted steps,
+    replayed with the same dt sequence on the oracle, agree to 1e-10."""
+    from pyfr_gb300.cases import ns_tgv
+    from pyfr_gb300.integrators import RKVdH2Integrator
+    from pyfr_gb300.solvers.system import NavierStokesSystem
+    cfg, mesh = ns_tgv(n=4, order=3, dt=2e-3)
+    sect = 'solver-time-integrator'
+    cfg.set(sect, 'controller', 'pi')
+    cfg.set(sect, 'rtol', '1e-7')
+    cfg.set(sect, 'atol', '1e-7')
+    be = _backend(cfg, graphs)
+    intg = RKVdH2Integrator(be, NavierStokesSystem, mesh, cfg)
+    (u,) = intg.soln
+    intg.run_pi_steps(6)
+    (ug,) = intg.soln
+    dts = intg.dt_accepted
+    assert len(dts) == 6 and len(set(dts)) > 1
+
+    d = disc_for_mesh(mesh, 3, ns=True)
+    c = cfg.items_as('constants', float) | cfg.items_as('solver-interfaces',
+                                                       float)
+    for dt in dts:
+        u = rk45_step(lambda x: d.rhs_ns(x, c), u, dt)
+    assert _relerr(ug, u) < TOL
+
+
+@pytest.mark.parametrize('graphs', [True, False])
 def test_rk45_vortex_steps(built, graphs):
     from pyfr_gb300.cases import euler_vortex
     from pyfr_gb300.integrators import RKVdH2Integrator
