@@ -446,6 +446,10 @@ def run_large(args, dist):
     n0, r0 = intg.nacptsteps, intg.nrjctsteps
     attempts, ms, clk = timed(intg, lambda: intg.run_pi_steps(args.large_steps))
     nrhs = attempts*intg.nstages
+    # The same integrator stepping at a fixed dt (the controller's error
+    # norm and host round trip left out), for the cost of adaptivity
+    _, ms_fixed, _ = timed(intg, lambda: intg.run_steps(args.large_steps,
+                                                         intg.dt))
     be = intg.backend
     res['chosen'] = {
         'neles': args.large_n**3, 'ndofs': intg.gndofs,
@@ -453,6 +457,8 @@ def run_large(args, dist):
         'rejected_steps': intg.nrjctsteps - r0,
         'dt_final': intg.dt, 't_final': intg.tcurr,
         'ms': ms, 'gdofs': dist.world*intg.gndofs*nrhs/(ms*1e-3)/1e9,
+        'fixed_dt_gdofs': dist.world*intg.gndofs*args.large_steps *
+        intg.nstages/(ms_fixed*1e-3)/1e9,
         'device_gb': be.memory_info().peak/1e9, 'setup_s': setup_s,
         'clocks': clk}
     del intg, be

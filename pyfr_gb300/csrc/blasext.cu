@@ -190,37 +190,55 @@ axnpby_kernel(int64_t n, int nv, T *__restrict__ x0, AxnpbyArgs<T> args) {
     }
 }
 
-// Block partials of the error norm over the valid points of one element
-// type; layout (nupts, nvars, neles) AoSoA with leading dimension ld.
+// Block partials of the error norm over the points of one element type;
+// layout (nupts, nvars, neles) AoSoA with leading dimension ld.  One warp
+// takes one (point, 32-element block) pair per iteration, lane = element
+// within the block; padding elements past neles hold zero error and add
+// nothing.  The quotient err/(atol + rtol*|u|) uses a reciprocal refined
+// by two Newton-Raphson steps, r <- r + r*(1 - d*r), from a single-
+// precision estimate (relative error about 2^-23 before, below 2^-52
+// after): GB300's FP64 unit is narrow and an IEEE double division costs
+// several times that.
+__device__ __forceinline__ double rcp_newton(double d) {
+    float r0;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(b200::narrow_f64(d)));
+    double r = b200::widen_f32(r0);
+    r = fma(r, fma(-d, r, 1.0), r);
+    r = fma(r, fma(-d, r, 1.0), r);
+    return r;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(BX_BLOCK)
 errest_partial_kernel(int nupts, int nvars, int64_t neles, int64_t ld, const T *__restrict__ curr,
                       const T *__restrict__ err, const double *__restrict__ atol, double rtol,
                       int uniform, RefState ref, double *__restrict__ partial) {
     __shared__ double red[BX_BLOCK / 32];
-    const int64_t npts = (int64_t)nupts * neles;
+    const int lane = threadIdx.x & 31;
+    const int64_t nblk = (neles + 31) / 32, nwork = (int64_t)nupts * nblk;
+    const int64_t warp = ((int64_t)blockIdx.x * BX_BLOCK + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * BX_BLOCK) >> 5;
     double acc = 0;
-    for (int64_t p = (int64_t)blockIdx.x * BX_BLOCK + threadIdx.x; p < npts;
-         p += (int64_t)gridDim.x * BX_BLOCK) {
-        const int upt = (int)(p / neles);
-        const int64_t e = p % neles;
+    for (int64_t q = warp; q < nwork; q += nwarps) {
+        const int upt = (int)(q / nblk);
+        const int64_t base = upt * ld + (q - upt * nblk) * 32 * nvars + lane;
+        const double c0 = (double)curr[base];
         for (int v = 0; v < nvars; v++) {
-            const int64_t ix = upt * ld + b200::soa_off(e, v, nvars);
+            const int64_t ix = base + v * 32;
             double c = (double)curr[ix];
             if (ref.nvars) {
                 c += ref.v[v];
-                if (v == nvars - 1)
-                    c += ref.hcoef * (double)curr[upt * ld + b200::soa_off(e, 0, nvars)];
+                if (v == nvars - 1) c += ref.hcoef * c0;
             }
-            const double q = (double)err[ix] / (atol[v] + rtol * fabs(c));
-            acc = uniform ? fmax(acc, fabs(q)) : acc + q * q;
+            const double qv = (double)err[ix] * rcp_newton(fma(rtol, fabs(c), atol[v]));
+            acc = uniform ? fmax(acc, fabs(qv)) : fma(qv, qv, acc);
         }
     }
     for (int o = 16; o > 0; o >>= 1) {
         const double y = __shfl_xor_sync(0xffffffffu, acc, o);
         acc = uniform ? fmax(acc, y) : acc + y;
     }
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    if (lane == 0) red[threadIdx.x >> 5] = acc;
     __syncthreads();
     if (threadIdx.x == 0) {
         double s = red[0];
