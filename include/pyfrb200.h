@@ -309,7 +309,8 @@ int b200_errest_f64(int nupts, int nvars, int64_t neles, int64_t ld, const doubl
                     double *scratch, int nscratch, double *out, void *stream);
 /* Same for a solution stored relative to a reference state: curr holds q
  * with u_v = uref[v] + q_v, plus hcoef*q_0 for the last variable (uref:
- * nvars host doubles), and the norm uses |u|. */
+ * nvars host doubles); err holds the error estimate of q, mapped the same
+ * way without the offset; the norm is that of the error of u scaled by |u|. */
 int b200_errest_shifted_f64(int nupts, int nvars, int64_t neles, int64_t ld, const double *curr,
                             const double *err, const double *atol_dev, double rtol, int uniform,
                             const double *uref, double hcoef, double *scratch, int nscratch,

@@ -222,15 +222,20 @@ errest_partial_kernel(int nupts, int nvars, int64_t neles, int64_t ld, const T *
     for (int64_t q = warp; q < nwork; q += nwarps) {
         const int upt = (int)(q / nblk);
         const int64_t base = upt * ld + (q - upt * nblk) * 32 * nvars + lane;
-        const double c0 = (double)curr[base];
+        const double c0 = (double)curr[base], e0 = (double)err[base];
         for (int v = 0; v < nvars; v++) {
             const int64_t ix = base + v * 32;
-            double c = (double)curr[ix];
+            double c = (double)curr[ix], ev = (double)err[ix];
             if (ref.nvars) {
+                // u_v = uref_v + q_v (+ hcoef*q_0 for the last variable);
+                // the error estimate maps with the linear part alone
                 c += ref.v[v];
-                if (v == nvars - 1) c += ref.hcoef * c0;
+                if (v == nvars - 1) {
+                    c += ref.hcoef * c0;
+                    ev += ref.hcoef * e0;
+                }
             }
-            const double qv = (double)err[ix] * rcp_newton(fma(rtol, fabs(c), atol[v]));
+            const double qv = ev * rcp_newton(fma(rtol, fabs(c), atol[v]));
             acc = uniform ? fmax(acc, fabs(qv)) : fma(qv, qv, acc);
         }
     }

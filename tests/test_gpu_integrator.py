@@ -141,20 +141,27 @@ def test_rkmixed_stage_bit_exact(be, n, offset, errest):
 
 
 def test_shifted_error_norm(be):
-    """The error norm of a solution stored as u - u_ref equals the norm
-    of u itself."""
+    """The error norm of a solution stored as q = T(u - u_ref) (energy
+    component dE - h*drho), with its error estimate in q, equals the norm
+    of u and of its error."""
     rng = np.random.default_rng(5)
     shape = (16, 5, 45)
     uref = np.array([1.0, 0.0, 0.0, 0.0, 178.5])
+    h = 250.0
     cur = rng.normal(size=shape) + uref[None, :, None]
     err = 1e-6*rng.normal(size=shape)
+    q = cur - uref[None, :, None]
+    q[:, -1] -= h*q[:, 0]
+    eq = err.copy()
+    eq[:, -1] -= h*eq[:, 0]
     C_ = be.matrix(shape, cur, tags={'align'})
-    S = be.matrix(shape, cur - uref[None, :, None], tags={'align'})
+    S = be.matrix(shape, q, tags={'align'})
     E = be.matrix(shape, err, tags={'align'})
+    EQ = be.matrix(shape, eq, tags={'align'})
     be.commit()
     atols = [1e-6, 2e-6, 3e-6, 4e-6, 5e-6]
     ks = [be.kernel('errest', C_, E, atols),
-          be.kernel('errest', S, E, atols, uref=uref)]
+          be.kernel('errest', S, EQ, atols, uref=uref, hcoef=h)]
     vals = []
     for k in ks:
         k.bind(rtol=1e-5)
