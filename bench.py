@@ -481,6 +481,95 @@ def run_large(args, dist):
     return res
 
 
+def run_ensemble(args, dist):
+    """The batching configuration's ensemble: independent 2-D vortex cases
+    of uneven size (quads per side uniform in 16..96), order (2, 3, 4) and
+    strength (beta uniform in 2..6) from one seed, merged by order and
+    advanced in one CUDA graph per step; plain FP64 and the chosen form,
+    and for comparison the same cases advanced one system each."""
+    import ctypes as C
+
+    import __graft_entry__ as ge
+    from pyfr_gb300.backend import B200Backend
+    from pyfr_gb300.cases import euler_vortex
+    from pyfr_gb300.ensemble import Ensemble, vortex_cases
+    from pyfr_gb300.inifile import Inifile
+    from pyfr_gb300.integrators import RKVdH2Integrator
+    from pyfr_gb300.solvers.system import EulerSystem
+    ge.build_library()
+
+    def backend(prec, mul='native'):
+        cfg = Inifile()
+        cfg.set('backend', 'precision', prec)
+        cfg.set('backend-b200', 'device-id', str(args.local_rank))
+        cfg.set('backend-b200', 'mul-precision', mul)
+        cfg.set('backend-b200', 'split-products', str(args.chosen_products))
+        return B200Backend(cfg)
+
+    def timed(be, fn):
+        lib, stream = be.lib, be.stream
+        ev = [C.c_void_p(), C.c_void_p()]
+        for e in ev:
+            lib.event_create(C.byref(e))
+        be.wait()
+        dist.barrier()
+        with ClockSampler(args.local_rank) as clk:
+            lib.event_record(ev[0].value, stream)
+            fn()
+            lib.event_record(ev[1].value, stream)
+            lib.event_sync(ev[1].value)
+        ms = C.c_float()
+        lib.event_elapsed(C.byref(ms), ev[0].value, ev[1].value)
+        return dist.allmax(ms.value), clk.summary()
+
+    cases = vortex_cases(args.ens_cases, seed=args.ens_seed)
+    nsteps, dt = args.steps, args.ens_dt
+    res = {'ncases': len(cases), 'seed': args.ens_seed, 'dt': dt,
+           'orders': {p: sum(c['order'] == p for c in cases)
+                      for p in (2, 3, 4)}}
+    ens = {}
+    for form, prec, mul in [('plain', 'double', 'native'),
+                            ('chosen', 'single', 'bf16x3')]:
+        be = backend(prec, mul)
+        e = Ensemble(be, cases, dt, prec, mixed=form == 'chosen')
+        e.run_steps(args.warmup)
+        ms, clk = timed(be, lambda: e.run_steps(nsteps))
+        gd = dist.world*e.gndofs*e.nstages*nsteps/(ms*1e-3)/1e9
+        res[form] = {'gdofs': gd, 'ms_per_step': ms/nsteps, 'clocks': clk,
+                     'ndofs': e.gndofs, 'systems': len(e.intgs)}
+        ens[form] = e
+
+    # Per-case L2 error of the chosen form against plain FP64
+    up, uc = ens['plain'].case_solutions(), ens['chosen'].case_solutions()
+    res['chosen']['l2_err_vs_fp64_max'] = max(
+        float(np.linalg.norm(uc[k] - up[k])/np.linalg.norm(up[k]))
+        for k in up)
+    res['chosen']['accuracy_after_steps'] = args.warmup + nsteps
+    del ens
+
+    # The same cases one system each (plain FP64), for the batching gain
+    be = backend('double')
+    intgs = []
+    for c in cases:
+        cfg, mesh = euler_vortex(n=c['n'], order=c['order'], dt=dt,
+                                 beta=c['beta'])
+        intgs.append(RKVdH2Integrator(be, EulerSystem, mesh, cfg))
+    for i in intgs:
+        i.run_steps(args.warmup)
+
+    def one_by_one():
+        for _ in range(nsteps):
+            for i in intgs:
+                (i.idxcurr,) = i.step(i.tcurr, dt)[:1]
+                i.tcurr += dt
+        be.wait()
+    ms, clk = timed(be, one_by_one)
+    nd = sum(i.gndofs for i in intgs)
+    res['plain_unbatched'] = {'gdofs': dist.world*nd*5*nsteps/(ms*1e-3)/1e9,
+                              'ms_per_step': ms/nsteps, 'systems': len(intgs)}
+    return res
+
+
 # ---------------------------------------------------------------------------
 # CPU arm (the oracle restatement, bounded sample)
 # ---------------------------------------------------------------------------
@@ -542,6 +631,12 @@ def main():
     ap.add_argument('--large-steps', type=int, default=100)
     ap.add_argument('--large-plain-n', type=int, default=96)
     ap.add_argument('--large-plain-steps', type=int, default=5)
+    ap.add_argument('--ensemble', action='store_true',
+                    help='the batching configuration\'s ensemble of 2-D '
+                         'vortex cases instead of the headline run')
+    ap.add_argument('--ens-cases', type=int, default=64)
+    ap.add_argument('--ens-seed', type=int, default=0)
+    ap.add_argument('--ens-dt', type=float, default=1e-4)
     ap.add_argument('--only', choices=['plain', 'chosen', 'bf16x3', 'tf32',
                                        'fp32'],
                     help='time one precision form alone (no accuracy '
@@ -581,6 +676,18 @@ def main():
                              'sample': sample},
             'e2e': {'value': v, 'unit': 'GDoF/s', 'h2d_bytes_per_step': 0,
                     'd2h_bytes_per_step': 0}}))
+        return
+
+    if args.ensemble:
+        r = run_ensemble(args, Dist(world))
+        if rank == 0:
+            print(json.dumps({
+                'metric': METRIC, 'unit': 'GDoF/s', 'n_gpus': world,
+                'steps': args.steps, 'warmup': args.warmup,
+                'config': {'workload': '2-D Euler isentropic-vortex '
+                                       'ensemble, merged by order, one CUDA '
+                                       'graph per RK45 step'},
+                'data': 'synthetic'} | r))
         return
 
     if args.large:
