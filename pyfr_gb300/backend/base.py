@@ -322,7 +322,10 @@ class B200Backend:
                 return m
 
         m = self.const_matrix_cls(self, dtype, initval, tags)
-        m._host = np.array(initval, dtype=dtype)
+        # The host copy keeps the precision it was given: host-side
+        # computations from constants (metric terms from vertices, operator
+        # splits) must not inherit the device precision's rounding
+        m._host = np.array(initval)
         return m
 
     def release_host_copies(self):
