@@ -150,6 +150,15 @@ int b200_mul_bf16x3_apply(void *handle, const b200_mul_bf16x3_args_t *args, void
 int b200_mul_tf32_create(const double *a, int m, int k, void **handle, size_t *smem_bytes);
 int b200_mul_tf32_create_cat(const double *a1, int k1, const double *a2, int k2, int m,
                              void **handle, size_t *smem_bytes);
+/* The kernel's pipeline plan, for an autotuner: a handle with a given
+ * number of 16 KB ring stages (even, 4..10) and of epilogue staging tiles
+ * per set (1 or 2), split-BF16 (tf32 = 0) or TF32; fails with
+ * B200_ERR_UNSUPPORTED when the plan does not fit shared memory.  _plan
+ * reports a handle's plan (the _create entry points pick the deepest ring
+ * that fits). */
+int b200_mul_tc_create_plan(const double *a1, int k1, const double *a2, int k2, int m, int tf32,
+                            int nstages, int ntiles, void **handle, size_t *smem_bytes);
+int b200_mul_tc_plan(void *handle, int *nstages, int *ntiles);
 
 /* ---- element pointwise kernels over [nupts, neles] ------------------- */
 /* Geometry: linear != 0 computes the metric terms from the element

@@ -114,6 +114,10 @@ class B200Backend:
         if self.mul_precision not in {'native', 'bf16x3', 'tf32'}:
             raise ValueError('mul-precision must be native, bf16x3 or tf32')
 
+        # Tensor-core pipeline plans picked by timing (cached per device
+        # and operator); off: the deepest plan that fits
+        self.autotune = cfg.get('backend-b200', 'autotune', 'true') == 'true'
+
         # Split-BF16 products: 3 (Ahi Bhi + Ahi Blo + Alo Bhi) or 4 (plus
         # Alo Blo)
         self.split_products = cfg.getint('backend-b200', 'split-products', 3)

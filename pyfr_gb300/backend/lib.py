@@ -114,6 +114,9 @@ _SIGS = {
                                    C.POINTER(sz)],
     'b200_mul_bf16x3_apply': [vp, C.c_void_p, vp],
     'b200_mul_tf32_create': [pd, i32, i32, C.POINTER(vp), C.POINTER(sz)],
+    'b200_mul_tc_create_plan': [pd, i32, pd, i32, i32, i32, i32, i32,
+                                C.POINTER(vp), C.POINTER(sz)],
+    'b200_mul_tc_plan': [vp, C.POINTER(i32), C.POINTER(i32)],
     'b200_mul_tf32_create_cat': [pd, i32, pd, i32, i32, C.POINTER(vp),
                                  C.POINTER(sz)],
 }

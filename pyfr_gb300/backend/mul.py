@@ -18,6 +18,8 @@ kernel that applies it.
 """
 
 import ctypes as C
+import json
+import os
 import weakref
 
 import numpy as np
@@ -31,6 +33,39 @@ def _check_shapes(a, b, out):
         raise ValueError('Incompatible matrices for out = a*b')
     if 'const' not in a.tags:
         raise ValueError('The operator of mul must be a constant matrix')
+
+
+_PLANS = None
+
+
+def _plan_path():
+    root = os.environ.get('PYFR_GB300_CACHE',
+                          os.path.join(os.path.expanduser('~'), '.cache',
+                                       'pyfr_gb300'))
+    return os.path.join(root, 'mul-plans.json')
+
+
+def _plan_cache():
+    global _PLANS
+    if _PLANS is None:
+        try:
+            with open(_plan_path()) as f:
+                _PLANS = json.load(f)
+        except (OSError, ValueError):
+            _PLANS = {}
+    return _PLANS
+
+
+def _save_plan_cache():
+    try:
+        path = _plan_path()
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        tmp = f'{path}.{os.getpid()}'
+        with open(tmp, 'w') as f:
+            json.dump(_PLANS, f, indent=1, sort_keys=True)
+        os.replace(tmp, path)
+    except OSError:
+        pass
 
 
 def _destroy_handles(destroy, handles):
@@ -125,15 +160,20 @@ class TensorMulKernels:
             h, smem = C.c_void_p(), C.c_size_t()
             pd = C.POINTER(C.c_double)
             lib = self.backend.lib
-            create = lib.mul_tf32_create_cat \
-                if self.backend.mul_precision == 'tf32' else \
+            tf32 = self.backend.mul_precision == 'tf32'
+            create = lib.mul_tf32_create_cat if tf32 else \
                 lib.mul_bf16x3_create_cat
-            try:
-                create(
-                    a1.ctypes.data_as(pd), a1.shape[1],
+            args = (a1.ctypes.data_as(pd), a1.shape[1],
                     a2.ctypes.data_as(pd) if a2 is not None else None,
-                    a2.shape[1] if a2 is not None else 0, a1.shape[0],
-                    C.byref(h), C.byref(smem))
+                    a2.shape[1] if a2 is not None else 0, a1.shape[0])
+            try:
+                plan = self._tuned_plan(args, tf32) \
+                    if self.backend.autotune else None
+                if plan:
+                    lib.mul_tc_create_plan(*args, int(tf32), *plan,
+                                           C.byref(h), C.byref(smem))
+                else:
+                    create(*args, C.byref(h), C.byref(smem))
             except B200Error:
                 self._handles[key] = None
             else:
@@ -146,6 +186,75 @@ class TensorMulKernels:
     @staticmethod
     def _aligned(*mats):
         return all(m.leaddim % 4 == 0 for m in mats)
+
+    def _tuned_plan(self, args, tf32):
+        """Pipeline plan (ring stages, epilogue staging tiles) of an
+        operator, picked by timing every plan that fits on a
+        representative width (8 tiles of 128 columns per SM) and cached per
+        device and operator, in memory and in a JSON file
+        (``$PYFR_GB300_CACHE`` or ``~/.cache/pyfr_gb300``)."""
+        be, lib = self.backend, self.backend.lib
+        m, k1, k2 = args[4], args[1], args[3]
+        key = '|'.join(map(str, (be.platform_id, 'tf32' if tf32 else 'bf16',
+                                 be.split_products, m, k1, k2)))
+        cache = _plan_cache()
+        if key in cache:
+            return tuple(cache[key]) if cache[key] else None
+
+        sms = C.c_int()
+        lib.device_info(C.byref(sms), None, None, None, None, None, 0)
+        ncol = sms.value*128*8
+        bufs = []
+
+        def dev(nbytes):
+            p = C.c_void_p()
+            lib.malloc(C.byref(p), nbytes)
+            bufs.append(p.value)
+            return p.value
+
+        b1, c = dev(4*k1*ncol), dev(4*m*ncol)
+        b2 = dev(4*k2*ncol) if k2 else None
+        err = be.status_word
+        ev0, ev1 = C.c_void_p(), C.c_void_p()
+        lib.event_create(C.byref(ev0))
+        lib.event_create(C.byref(ev1))
+        times = {}
+        try:
+            for ntiles in (1, 2):
+                for nstages in (4, 6, 8, 10):
+                    h, smem = C.c_void_p(), C.c_size_t()
+                    try:
+                        lib.mul_tc_create_plan(*args, int(tf32), nstages,
+                                               ntiles, C.byref(h),
+                                               C.byref(smem))
+                    except B200Error:
+                        continue
+                    a = MulArgs(b1=b1, ldb1=ncol, b2=b2, ldb2=ncol, c=c,
+                                ldc=ncol, ncol=ncol, nbatch=1, alpha=1.0,
+                                beta=0.0, products=be.split_products, err=err)
+                    pa = C.addressof(a)
+                    for _ in range(2):
+                        lib.mul_bf16x3_apply(h.value, pa, be.stream)
+                    lib.event_record(ev0.value, be.stream)
+                    for _ in range(5):
+                        lib.mul_bf16x3_apply(h.value, pa, be.stream)
+                    lib.event_record(ev1.value, be.stream)
+                    lib.event_sync(ev1.value)
+                    ms = C.c_float()
+                    lib.event_elapsed(C.byref(ms), ev0.value, ev1.value)
+                    times[(nstages, ntiles)] = ms.value
+                    lib.mul_bf16x3_destroy(h.value)
+        finally:
+            for p in bufs:
+                lib.free(p)
+            lib.event_destroy(ev0.value)
+            lib.event_destroy(ev1.value)
+        be.check_status()
+
+        best = min(times, key=times.get) if times else None
+        cache[key] = list(best) if best else None
+        _save_plan_cache()
+        return best
 
     def _kernel(self, handle, args, mats, meta):
         be = self.backend

@@ -648,7 +648,7 @@ extern "C" {
 namespace {
 
 int create_impl(const double *a1, int k1, const double *a2, int k2, int m, int tf32,
-                void **handle, size_t *smem_bytes) {
+                int want_ns, int want_eb, void **handle, size_t *smem_bytes) {
     if (!a1 || !handle || m <= 0 || k1 <= 0 || k2 < 0 || (k2 > 0 && !a2))
         return b200::set_error(B200_ERR_ARG, "mul_bf16x3_create: bad arguments");
     const int nch1 = (k1 + KC - 1) / KC, nch2 = (k2 + KC - 1) / KC;
@@ -659,23 +659,34 @@ int create_impl(const double *a1, int k1, const double *a2, int k2, int m, int t
     // group takes every other chunk, so with an even ring a stage's previous
     // chunk belongs to the same group, which has consumed it before it waits
     // for the stage again (with an odd ring the group could take the phase
-    // of the other group's pending chunk, one phase back, for its own).  An operator of at most 64 rows gives each set one
-    // store per tile, which a second staging tile would not overlap with
-    // anything: it takes one and the ring the room.
+    // of the other group's pending chunk, one phase back, for its own).  An
+    // operator of at most 64 rows gives each set one store per tile, which
+    // a second staging tile would not overlap with anything: it takes one
+    // and the ring the room.  A caller (the autotuner) may ask for a given
+    // plan instead (want_ns even, 4..MAX_S; want_eb 1 or 2).
     int ns = 0, eb = npad <= 64 ? 1 : MAX_EB;
     Layout L = make_layout(npad, kfull, 2, eb);
-    for (; eb >= 1 && ns < 4; eb--) {
-        ns = 0;
-        for (int cand = MAX_S; cand >= 4 && !ns; cand -= 2) {
-            Layout c = make_layout(npad, kfull, cand, eb);
-            if (c.total <= 227 * 1024) {
-                ns = cand;
-                L = c;
+    if (want_ns || want_eb) {
+        if ((want_ns & 1) || want_ns < 4 || want_ns > MAX_S || want_eb < 1 || want_eb > MAX_EB)
+            return b200::set_error(B200_ERR_ARG, "mul_bf16x3: plan (%d stages, %d tiles) invalid",
+                                   want_ns, want_eb);
+        ns = want_ns;
+        eb = want_eb;
+        L = make_layout(npad, kfull, ns, eb);
+    } else {
+        for (; eb >= 1 && ns < 4; eb--) {
+            ns = 0;
+            for (int cand = MAX_S; cand >= 4 && !ns; cand -= 2) {
+                Layout c = make_layout(npad, kfull, cand, eb);
+                if (c.total <= 227 * 1024) {
+                    ns = cand;
+                    L = c;
+                }
             }
+            if (ns >= 4) break;
         }
-        if (ns >= 4) break;
+        if (eb < 1) eb = 1;
     }
-    if (eb < 1) eb = 1;
     if (smem_bytes) *smem_bytes = L.total;
     if (npad > MAX_N || !ns || (ns & 1) || L.total > 227 * 1024)
         return b200::set_error(B200_ERR_UNSUPPORTED,
@@ -750,20 +761,33 @@ extern "C" {
 
 int b200_mul_bf16x3_create_cat(const double *a1, int k1, const double *a2, int k2, int m,
                                 void **handle, size_t *smem_bytes) {
-    return create_impl(a1, k1, a2, k2, m, 0, handle, smem_bytes);
+    return create_impl(a1, k1, a2, k2, m, 0, 0, 0, handle, smem_bytes);
 }
 
 int b200_mul_bf16x3_create(const double *a, int m, int k, void **handle, size_t *smem_bytes) {
-    return create_impl(a, k, nullptr, 0, m, 0, handle, smem_bytes);
+    return create_impl(a, k, nullptr, 0, m, 0, 0, 0, handle, smem_bytes);
 }
 
 int b200_mul_tf32_create_cat(const double *a1, int k1, const double *a2, int k2, int m,
                              void **handle, size_t *smem_bytes) {
-    return create_impl(a1, k1, a2, k2, m, 1, handle, smem_bytes);
+    return create_impl(a1, k1, a2, k2, m, 1, 0, 0, handle, smem_bytes);
 }
 
 int b200_mul_tf32_create(const double *a, int m, int k, void **handle, size_t *smem_bytes) {
-    return create_impl(a, k, nullptr, 0, m, 1, handle, smem_bytes);
+    return create_impl(a, k, nullptr, 0, m, 1, 0, 0, handle, smem_bytes);
+}
+
+int b200_mul_tc_create_plan(const double *a1, int k1, const double *a2, int k2, int m, int tf32,
+                            int nstages, int ntiles, void **handle, size_t *smem_bytes) {
+    return create_impl(a1, k1, a2, k2, m, tf32 ? 1 : 0, nstages, ntiles, handle, smem_bytes);
+}
+
+int b200_mul_tc_plan(void *handle, int *nstages, int *ntiles) {
+    UmmaHandle *h = (UmmaHandle *)handle;
+    if (!h) return b200::set_error(B200_ERR_ARG, "mul_tc_plan: null handle");
+    if (nstages) *nstages = h->ns;
+    if (ntiles) *ntiles = h->eb;
+    return B200_OK;
 }
 
 int b200_mul_bf16x3_destroy(void *handle) {

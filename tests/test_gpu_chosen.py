@@ -313,3 +313,43 @@ def test_kinetic_energy_history(built, mul):
         hist[form] = np.array(h)
 
     assert np.abs(hist['chosen'] - hist['plain']).max() <= 1e-8
+
+
+def test_autotuned_plan_same_result(built, golden, tmp_path, monkeypatch):
+    """The autotuner's pipeline plan (ring depth, epilogue tiles) changes
+    the schedule, not the arithmetic: results equal the default plan's bit
+    for bit, and the plan is cached."""
+    import ctypes as C
+    import json
+    from pyfr_gb300.backend import B200Backend
+    from pyfr_gb300.backend import mul as mulmod
+    from pyfr_gb300.inifile import Inifile
+    monkeypatch.setenv('PYFR_GB300_CACHE', str(tmp_path))
+    monkeypatch.setattr(mulmod, '_PLANS', None)
+    a = golden['operators']['hex_p3_gauss-legendre/M460']
+    rng = np.random.default_rng(9)
+    b = rng.normal(size=(a.shape[1], 5, 900))
+    out = {}
+    for tune in ('true', 'false'):
+        cfg = Inifile()
+        cfg.set('backend', 'precision', 'single')
+        cfg.set('backend-b200', 'mul-precision', 'bf16x3')
+        cfg.set('backend-b200', 'autotune', tune)
+        be = B200Backend(cfg)
+        A = be.const_matrix(a)
+        B = be.matrix(b.shape, b, tags={'align'})
+        Cm = be.matrix((a.shape[0], 5, 900), tags={'align'})
+        be.commit()
+        k = be.kernel('mul', A, B, out=Cm)
+        be.run_kernels([k], wait=True)
+        out[tune] = Cm.get()
+        ns, nt = C.c_int(), C.c_int()
+        h = be._providers[2]._handles[(A.mid,)][0] if hasattr(
+            be, '_providers') else None
+        if h is not None:
+            be.lib.mul_tc_plan(h, C.byref(ns), C.byref(nt))
+            assert ns.value % 2 == 0 and 4 <= ns.value <= 10
+            assert nt.value in (1, 2)
+    assert np.array_equal(out['true'], out['false'])
+    plans = json.loads((tmp_path / 'mul-plans.json').read_text())
+    assert any(k.endswith('|192|64|0') for k in plans)
