@@ -1,13 +1,24 @@
-"""Orthonormal and nodal polynomial bases on the reference line, quad and hex.
+"""Orthonormal and nodal polynomial bases on the reference elements.
 
 The flux-reconstruction operators are built from the same mathematical
 objects as ``pyfr/polys.py`` (orthonormal Legendre products, Vandermonde
 inversion to a nodal basis at the solution points,
 ``pyfr/polys.py:46-88`` and ``pyfr/polys.py:126-150,402-433``).  This
 module is a fresh, vectorised statement of that mathematics: the nodal
-basis that results is independent of how the orthonormal modes are
-enumerated, so only the ordering of the nodal points has to agree with the
-reference (x fastest, then y, then z).
+basis that results is independent of how the modes are enumerated, so only
+the ordering of the nodal points has to agree with the reference (x
+fastest, then y, then z).
+
+The simplex and prism spaces (total degree <= p on the triangle and the
+tetrahedron; total degree <= p in (x, y) times degree <= p in z on the
+prism, the spaces of ``pyfr/polys.py:112-330``) are spanned here by
+products of Legendre polynomials restricted to those degrees.  Unlike the
+reference's collapsed-coordinate (Dubiner) modes these are not orthogonal
+on the element, but they span the same space, have derivatives without
+the collapsed coordinates' singular points, and are well conditioned at
+the orders of interest; the nodal bases and operators are the same.  The
+shapes that use them integrate with explicit mass matrices where the
+reference relies on orthonormality.
 """
 
 import itertools as it
@@ -41,17 +52,40 @@ def legendre_orthonormal(order, x):
     return scale.reshape(shp)*p, scale.reshape(shp)*dp
 
 
-class TensorProdBasis:
-    """Tensor-product orthonormal basis of degree ``order`` in each of
-    ``ndims`` reference coordinates, with a nodal basis at ``pts``."""
+def space_modes(kind, order):
+    """Multi-indices (Legendre degree per coordinate) spanning the
+    polynomial space of order ``order`` on element type ``kind``."""
+    p = order
+    if kind == 'line':
+        return [(i,) for i in range(p + 1)]
+    if kind in ('quad', 'hex'):
+        nd = 2 if kind == 'quad' else 3
+        return [m[::-1] for m in it.product(range(p + 1), repeat=nd)]
+    if kind == 'tri':
+        return [(i, j) for j in range(p + 1) for i in range(p + 1 - j)]
+    if kind == 'tet':
+        return [(i, j, k) for k in range(p + 1) for j in range(p + 1 - k)
+                for i in range(p + 1 - j - k)]
+    if kind == 'pri':
+        return [(i, j, k) for k in range(p + 1) for j in range(p + 1)
+                for i in range(p + 1 - j)]
+    raise ValueError(f'No polynomial space for {kind!r}')
 
-    def __init__(self, ndims, order, pts=None):
+
+class TensorProdBasis:
+    """Basis of Legendre products of degree ``order`` in each of ``ndims``
+    reference coordinates (orthonormal on the square/cube), or of the
+    products listed in ``modes``, with a nodal basis at ``pts``."""
+
+    def __init__(self, ndims, order, pts=None, modes=None):
         self.ndims = ndims
         self.order = order
         self.pts = None if pts is None else np.atleast_2d(pts)
 
         # Multi-indices of the modes
-        self.modes = list(it.product(range(order + 1), repeat=ndims))
+        if modes is None:
+            modes = list(it.product(range(order + 1), repeat=ndims))
+        self.modes = modes
 
     def _factors(self, pts):
         pts = np.atleast_2d(np.asarray(pts, dtype=float))

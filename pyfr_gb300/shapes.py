@@ -9,62 +9,40 @@ matrices that the right-hand side applies:
   field held at the solution points;
 * ``M2`` (nfpts x ndims*nupts): normal component of that field at the flux
   points;
-* ``M3`` (nupts x nfpts): the correction (lifting) operator, here the DG
-  correction obtained by L2-projecting the face nodal basis onto the
-  element's orthonormal basis;
+* ``M3`` (nupts x nfpts): the correction (lifting) operator, the DG
+  correction: the lift g_f of flux point f is the polynomial of the
+  solution space with  int_E g_f phi = int_face L_f phi  for every phi of
+  the space (L_f the face's nodal basis function of f);
 * ``M4`` (ndims*nupts x nupts): reference gradient of a scalar field;
 * ``M6`` (ndims*nupts x nfpts): normal-weighted lift.
 
 These follow the definitions of ``pyfr/shapes.py:80-125`` and
-``pyfr/shapes.py:232-259`` (the lifting coefficients), with the same point
-orderings, face orderings and normals (``pyfr/shapes.py:341-438``) so that
-operators, element data and interface maps line up one-to-one with the
-reference.  Only tensor-product shapes (quad, hex) with Gauss-Legendre or
-Gauss-Legendre-Lobatto points are provided.
+``pyfr/shapes.py:232-259`` (the lifting coefficients), with the same face
+orderings, face parametrisations and normals (``pyfr/shapes.py:341-566``)
+so that operators, element data and interface maps line up one-to-one with
+the reference.  Quadrilaterals and hexahedra (Gauss-Legendre or
+Gauss-Legendre-Lobatto points), triangles, tetrahedra ('alpha-opt' points)
+and prisms (triangle points times line points) are provided; any shape
+also takes literal point sets in the reference's rule text format.
+
+The tensor-product shapes form the lift from orthonormal modes, as the
+reference does; the simplex and prism shapes solve with the element mass
+matrix instead (same lift, basis-independent), both with quadrature exact
+for the integrands.
 """
 
 from functools import cached_property
-import itertools as it
 import re
 
 import numpy as np
 
-from pyfr_gb300.polys import TensorProdBasis, tidy
+from pyfr_gb300.polys import TensorProdBasis, space_modes, tidy
+from pyfr_gb300.quadrules import (EXACT_RULES, gauss_legendre,
+                                  gauss_legendre_lobatto, point_set,
+                                  tensor_rule)
 
-
-def gauss_legendre(n):
-    """n-point Gauss-Legendre rule on [-1, 1] (ascending abscissae)."""
-    return np.polynomial.legendre.leggauss(n)
-
-
-def gauss_legendre_lobatto(n):
-    """n-point Gauss-Legendre-Lobatto rule on [-1, 1]."""
-    if n < 2:
-        raise ValueError('Lobatto rules need at least two points')
-
-    # Interior nodes are the roots of P'_{n-1}
-    c = np.zeros(n)
-    c[-1] = 1
-    inner = np.polynomial.legendre.legroots(np.polynomial.legendre.legder(c))
-    x = np.concatenate([[-1.0], np.sort(inner.real), [1.0]])
-    pn1 = np.polynomial.legendre.legval(x, c)
-    w = 2.0 / (n*(n - 1)*pn1**2)
-    return x, w
-
-
-_RULES_1D = {
-    'gauss-legendre': gauss_legendre,
-    'gauss-legendre-lobatto': gauss_legendre_lobatto,
-}
-
-
-def tensor_rule(name, n1d, ndims):
-    """Tensor-product rule with the first coordinate varying fastest, the
-    ordering of the tabulated rules in ``pyfr/quadrules/{quad,hex}``."""
-    x, w = _RULES_1D[name](n1d)
-    pts = np.array([p[::-1] for p in it.product(x, repeat=ndims)])
-    wts = np.array([np.prod(q) for q in it.product(w, repeat=ndims)])
-    return pts.reshape(-1, ndims), wts
+__all__ = ['gauss_legendre', 'gauss_legendre_lobatto', 'tensor_rule',
+           'get_shape', 'adjugate_det', 'linear_shape_jac', 'SHAPES']
 
 
 def _proj(fn, pts):
@@ -73,34 +51,56 @@ def _proj(fn, pts):
     return np.vstack(cols).T.astype(float)
 
 
-class TensorProdShape:
+FACE_KIND = {'quad': 'line', 'hex': 'quad', 'tri': 'line', 'tet': 'tri'}
+
+
+class BaseShape:
     name = None
     ndims = None
+
+    # (face kind, reference-to-face projection, outward normal), in the
+    # reference's face order
     faces = None
-    facekind = None
 
     def __init__(self, order, upts_rule='gauss-legendre',
                  fpts_rule='gauss-legendre'):
         self.order = order
         self.upts_rule = upts_rule
-        self.fpts_rule = fpts_rule
+        kinds = {k for k, _, _ in self.faces}
+        if isinstance(fpts_rule, str):
+            fpts_rule = {k: fpts_rule for k in kinds}
+        self.fpts_rules = {k: fpts_rule[k] for k in kinds}
 
-        self.upts, _ = tensor_rule(upts_rule, order + 1, self.ndims)
-        self.ubasis = TensorProdBasis(self.ndims, order, self.upts)
+        self.upts = point_set(self.name, upts_rule, order)
+        self.ubasis = TensorProdBasis(self.ndims, order, self.upts,
+                                      self._modes(self.name))
 
-    # Vertex (linear shape point) ordering: x fastest; std_ele(1)
-    @cached_property
-    def linspts(self):
-        return np.array([p[::-1] for p in it.product([-1.0, 1.0],
-                                                      repeat=self.ndims)])
+    def _modes(self, kind):
+        return space_modes(kind, self.order)
+
+    @property
+    def fpts_rule(self):
+        (r,) = set(self.fpts_rules.values())
+        return r
 
     @property
     def nupts(self):
-        return (self.order + 1)**self.ndims
+        return len(self.upts)
+
+    @property
+    def facekind(self):
+        (k,) = {k for k, _, _ in self.faces}
+        return k
+
+    @cached_property
+    def face_pts(self):
+        """Flux points of each face kind in face coordinates."""
+        return {k: point_set(k, r, self.order)
+                for k, r in self.fpts_rules.items()}
 
     @cached_property
     def nfacefpts(self):
-        return [(self.order + 1)**(self.ndims - 1)]*len(self.faces)
+        return [len(self.face_pts[k]) for k, _, _ in self.faces]
 
     @property
     def nfpts(self):
@@ -113,42 +113,20 @@ class TensorProdShape:
                 for i in range(len(self.faces))]
 
     @cached_property
-    def _face_rule(self):
-        return tensor_rule(self.fpts_rule, self.order + 1, self.ndims - 1)
-
-    @cached_property
     def fpts(self):
-        fp, _ = self._face_rule
-        return np.vstack([_proj(proj, fp) for proj, norm in self.faces])
-
-    @cached_property
-    def fpts_wts(self):
-        _, fw = self._face_rule
-        return np.hstack([fw]*len(self.faces))
+        return np.vstack([_proj(proj, self.face_pts[k])
+                          for k, proj, norm in self.faces])
 
     @cached_property
     def norm_fpts(self):
-        return np.vstack([[norm]*n for (proj, norm), n
+        return np.vstack([[norm]*n for (k, proj, norm), n
                           in zip(self.faces, self.nfacefpts)]).astype(float)
 
     @cached_property
-    def facebasis(self):
-        fp, _ = self._face_rule
-        return TensorProdBasis(self.ndims - 1, self.order, fp)
-
-    @cached_property
-    def lift_coeffs(self):
-        """Modal coefficients (nfpts x nmodes) of the DG lifting functions:
-        the face nodal basis integrated against the element's orthonormal
-        modes restricted to the face (exact Gauss-Legendre quadrature)."""
-        qp, qw = tensor_rule('gauss-legendre', self.order + 1, self.ndims - 1)
-        lq = self.facebasis.nodal_basis_at(qp)          # (nq, nfacefpts)
-
-        blocks = []
-        for proj, norm in self.faces:
-            mq = self.ubasis.ortho_basis_at(_proj(proj, qp))   # (nmodes, nq)
-            blocks.append((lq*qw[:, None]).T @ mq.T)
-        return np.vstack(blocks)
+    def facebases(self):
+        return {k: TensorProdBasis(self.ndims - 1, self.order, p,
+                                   self._modes(k))
+                for k, p in self.face_pts.items()}
 
     # Operator matrices -----------------------------------------------------
 
@@ -168,7 +146,7 @@ class TensorProdShape:
 
     @cached_property
     def m3(self):
-        return tidy((self.lift_coeffs @ self.ubasis.ortho_basis_at(self.upts)).T)
+        return tidy(self._lift_at_upts())
 
     @cached_property
     def m4(self):
@@ -189,66 +167,234 @@ class TensorProdShape:
         names = {m: getattr(self, m) for m in set(re.findall(r'm\d+', e))}
         return tidy(eval(e, {'__builtins__': {}}, names))
 
-    # Geometry of linear (affine or multilinear) elements --------------------
+    def _lift_at_upts(self):
+        """Lift via the element mass matrix of the nodal basis:
+        M c_f = b_f with M_ij = int_E l_i l_j, b_f,i = int_face L_f l_i
+        (face integrals in the face parametrisation, whose measure the
+        unnormalised reference normals account for); returns the
+        (nupts, nfpts) values g_f(upts) = c_f."""
+        q = 2*self.order
+        qp, qw = EXACT_RULES[self.name](q)
+        L = self.ubasis.nodal_basis_at(qp)                 # (nq, nupts)
+        mass = L.T @ (qw[:, None]*L)
+
+        cols = []
+        for kind, proj, norm in self.faces:
+            fq, fw = EXACT_RULES[kind](q)
+            lf = self.facebases[kind].nodal_basis_at(fq)   # (nfq, nff)
+            le = self.ubasis.nodal_basis_at(_proj(proj, fq))
+            cols.append(le.T @ (fw[:, None]*lf))
+        return np.linalg.solve(mass, np.hstack(cols))
+
+    # Geometry of linear elements --------------------------------------------
 
     def shape_fn(self, x):
-        """Multilinear shape functions of the vertices at points ``x``;
+        """Linear shape functions of the vertices at points ``x``;
         shape (npts, nverts)."""
-        x = np.atleast_2d(x)
-        v = self.linspts
-        return np.prod(1 + x[:, None, :]*v[None, :, :], axis=2) / 2**self.ndims
+        return linear_shape_fn(self.name, np.atleast_2d(x))
 
     def shape_jac(self, x):
         """d(shape fn)/d(xi_i); shape (npts, ndims, nverts)."""
-        x = np.atleast_2d(x)
-        v = self.linspts
-        out = np.empty((len(x), self.ndims, len(v)))
-        for i in range(self.ndims):
-            t = np.ones((len(x), len(v)))
-            for d in range(self.ndims):
-                t = t*(v[None, :, d] if d == i else 1 + x[:, None, d]*v[None, :, d])
-            out[:, i] = t / 2**self.ndims
-        return out
+        return linear_shape_jac(self.name, np.atleast_2d(x))
+
+
+class TensorProdShape(BaseShape):
+    # Vertex (linear shape point) ordering: x fastest; std_ele(1)
+    @cached_property
+    def linspts(self):
+        return np.array(VERTICES[self.name], dtype=float)
+
+    @cached_property
+    def _face_rule(self):
+        return tensor_rule(self.fpts_rule, self.order + 1, self.ndims - 1)
+
+    @cached_property
+    def fpts_wts(self):
+        _, fw = self._face_rule
+        return np.hstack([fw]*len(self.faces))
+
+    @cached_property
+    def facebasis(self):
+        return self.facebases[self.facekind]
+
+    @cached_property
+    def lift_coeffs(self):
+        """Modal coefficients (nfpts x nmodes) of the DG lifting functions:
+        the face nodal basis integrated against the element's orthonormal
+        modes restricted to the face (exact Gauss-Legendre quadrature)."""
+        qp, qw = tensor_rule('gauss-legendre', self.order + 1, self.ndims - 1)
+        lq = self.facebasis.nodal_basis_at(qp)          # (nq, nfacefpts)
+
+        blocks = []
+        for kind, proj, norm in self.faces:
+            mq = self.ubasis.ortho_basis_at(_proj(proj, qp))   # (nmodes, nq)
+            blocks.append((lq*qw[:, None]).T @ mq.T)
+        return np.vstack(blocks)
+
+    def _lift_at_upts(self):
+        return (self.lift_coeffs @ self.ubasis.ortho_basis_at(self.upts)).T
+
+    def _modes(self, kind):
+        return None
+
+
+class SimplexLikeShape(BaseShape):
+    @cached_property
+    def linspts(self):
+        return np.array(VERTICES[self.name], dtype=float)
 
 
 class QuadShape(TensorProdShape):
     name = 'quad'
     ndims = 2
-    facekind = 'line'
 
-    # (reference-to-face projection, outward normal) in reference order
     faces = [
-        (lambda s: (s, -1), (0, -1)),
-        (lambda s: (1, s), (1, 0)),
-        (lambda s: (s, 1), (0, 1)),
-        (lambda s: (-1, s), (-1, 0)),
+        ('line', lambda s: (s, -1), (0, -1)),
+        ('line', lambda s: (1, s), (1, 0)),
+        ('line', lambda s: (s, 1), (0, 1)),
+        ('line', lambda s: (-1, s), (-1, 0)),
     ]
 
 
 class HexShape(TensorProdShape):
     name = 'hex'
     ndims = 3
-    facekind = 'quad'
 
     faces = [
-        (lambda s, t: (s, t, -1), (0, 0, -1)),
-        (lambda s, t: (s, -1, t), (0, -1, 0)),
-        (lambda s, t: (1, s, t), (1, 0, 0)),
-        (lambda s, t: (s, 1, t), (0, 1, 0)),
-        (lambda s, t: (-1, s, t), (-1, 0, 0)),
-        (lambda s, t: (s, t, 1), (0, 0, 1)),
+        ('quad', lambda s, t: (s, t, -1), (0, 0, -1)),
+        ('quad', lambda s, t: (s, -1, t), (0, -1, 0)),
+        ('quad', lambda s, t: (1, s, t), (1, 0, 0)),
+        ('quad', lambda s, t: (s, 1, t), (0, 1, 0)),
+        ('quad', lambda s, t: (-1, s, t), (-1, 0, 0)),
+        ('quad', lambda s, t: (s, t, 1), (0, 0, 1)),
     ]
 
 
-SHAPES = {'quad': QuadShape, 'hex': HexShape}
+class TriShape(SimplexLikeShape):
+    name = 'tri'
+    ndims = 2
+
+    faces = [
+        ('line', lambda s: (s, -1), (0, -1)),
+        ('line', lambda s: (-s, s), (1, 1)),
+        ('line', lambda s: (-1, s), (-1, 0)),
+    ]
+
+
+class TetShape(SimplexLikeShape):
+    name = 'tet'
+    ndims = 3
+
+    faces = [
+        ('tri', lambda s, t: (s, t, -1), (0, 0, -1)),
+        ('tri', lambda s, t: (s, -1, t), (0, -1, 0)),
+        ('tri', lambda s, t: (-1, t, s), (-1, 0, 0)),
+        ('tri', lambda s, t: (s, t, -s - t - 1), (1, 1, 1)),
+    ]
+
+
+class PriShape(SimplexLikeShape):
+    name = 'pri'
+    ndims = 3
+
+    faces = [
+        ('tri', lambda s, t: (s, t, -1), (0, 0, -1)),
+        ('tri', lambda s, t: (s, t, 1), (0, 0, 1)),
+        ('quad', lambda s, t: (s, -1, t), (0, -1, 0)),
+        ('quad', lambda s, t: (-s, s, t), (1, 1, 0)),
+        ('quad', lambda s, t: (-1, s, t), (-1, 0, 0)),
+    ]
+
+
+# Vertices of the linear elements, in the reference's order (std_ele(1)
+# of pyfr/shapes.py)
+VERTICES = {
+    'quad': [(-1, -1), (1, -1), (-1, 1), (1, 1)],
+    'hex': [(-1, -1, -1), (1, -1, -1), (-1, 1, -1), (1, 1, -1),
+            (-1, -1, 1), (1, -1, 1), (-1, 1, 1), (1, 1, 1)],
+    'tri': [(-1, -1), (1, -1), (-1, 1)],
+    'tet': [(-1, -1, -1), (1, -1, -1), (-1, 1, -1), (-1, -1, 1)],
+    'pri': [(-1, -1, -1), (1, -1, -1), (-1, 1, -1),
+            (-1, -1, 1), (1, -1, 1), (-1, 1, 1)],
+}
+
+# Element type from (ndims, number of vertices)
+ETYPE_OF = {(2, 4): 'quad', (3, 8): 'hex', (2, 3): 'tri', (3, 4): 'tet',
+            (3, 6): 'pri'}
+
+
+def _simplex_bary(x):
+    """Barycentric coordinates of the reference triangle/tetrahedron:
+    vertex 0 then one per coordinate; with their constant gradients."""
+    nd = x.shape[1]
+    lam = np.empty((len(x), nd + 1))
+    lam[:, 0] = -(x.sum(axis=1) + nd - 2)/2
+    lam[:, 1:] = (1 + x)/2
+    grad = np.zeros((nd, nd + 1))
+    grad[:, 0] = -0.5
+    grad[np.arange(nd), np.arange(1, nd + 1)] = 0.5
+    return lam, grad
+
+
+def linear_shape_fn(etype, x):
+    """Shape functions (npts, nverts) of the linear element of ``etype``
+    (the interpolation expressions of pyfr/shapes.py)."""
+    x = np.asarray(x, dtype=float)
+    if etype in ('quad', 'hex'):
+        v = np.array(VERTICES[etype], dtype=float)
+        return np.prod(1 + x[:, None, :]*v[None, :, :], axis=2)/len(v)
+    if etype in ('tri', 'tet'):
+        return _simplex_bary(x)[0]
+    if etype == 'pri':
+        lam, _ = _simplex_bary(x[:, :2])
+        z = x[:, 2:3]
+        return np.hstack([lam*(1 - z)/2, lam*(1 + z)/2])
+    raise ValueError(etype)
+
+
+def linear_shape_jac(etype, x):
+    """Reference gradients (npts, ndims, nverts) of the linear shape
+    functions of ``etype`` (the Jacobian expressions of pyfr/shapes.py)."""
+    x = np.atleast_2d(np.asarray(x, dtype=float))
+    npt, nd = x.shape
+    if etype in ('quad', 'hex'):
+        v = np.array(VERTICES[etype], dtype=float)
+        out = np.empty((npt, nd, len(v)))
+        for i in range(nd):
+            t = np.ones((npt, len(v)))
+            for d in range(nd):
+                t = t*(v[None, :, d] if d == i else 1 + x[:, None, d]*v[None, :, d])
+            out[:, i] = t/len(v)
+        return out
+    if etype in ('tri', 'tet'):
+        _, g = _simplex_bary(x)
+        return np.broadcast_to(g, (npt,) + g.shape).copy()
+    if etype == 'pri':
+        lam, g = _simplex_bary(x[:, :2])
+        z = x[:, 2][:, None]
+        out = np.empty((npt, 3, 6))
+        for i in range(2):
+            out[:, i, :3] = g[i]*(1 - z)/2
+            out[:, i, 3:] = g[i]*(1 + z)/2
+        out[:, 2, :3] = -lam/2
+        out[:, 2, 3:] = lam/2
+        return out
+    raise ValueError(etype)
+
+
+SHAPES = {'quad': QuadShape, 'hex': HexShape, 'tri': TriShape,
+          'tet': TetShape, 'pri': PriShape}
 
 
 def get_shape(name, order, upts_rule='gauss-legendre',
               fpts_rule='gauss-legendre'):
+    """Shape ``name`` of order ``order``; ``fpts_rule`` names the flux
+    point rule of every face kind, or maps face kinds to rules."""
     try:
-        return SHAPES[name](order, upts_rule, fpts_rule)
+        cls = SHAPES[name]
     except KeyError:
         raise ValueError(f'Unsupported element type {name!r}') from None
+    return cls(order, upts_rule, fpts_rule)
 
 
 def adjugate_det(J):

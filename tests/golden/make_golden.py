@@ -73,8 +73,12 @@ def _cfg(etype, order, upts, fpts, consts=None, ics=None, extra=()):
 
     cfg = Inifile()
     cfg.set('solver', 'order', str(order))
-    fkind = {'quad': 'line', 'hex': 'quad'}[etype]
-    cfg.set(f'solver-interfaces-{fkind}', 'flux-pts', fpts)
+    if isinstance(fpts, str):
+        fkind = {'quad': 'line', 'hex': 'quad', 'tri': 'line',
+                 'tet': 'tri'}[etype]
+        fpts = {fkind: fpts}
+    for fkind, rule in fpts.items():
+        cfg.set(f'solver-interfaces-{fkind}', 'flux-pts', rule)
     cfg.set(f'solver-elements-{etype}', 'soln-pts', upts)
     for k, v in (consts or {}).items():
         cfg.set('constants', k, repr(v))
@@ -93,11 +97,39 @@ OPERATOR_CASES = [
 ]
 
 
-def make_operators():
-    from pyfr.shapes import HexShape, QuadShape
+# Simplex and prism shapes with the reference's named 'alpha-opt' point
+# sets: (etype, order, solution points, flux points per face kind)
+SIMPLEX_CASES = [
+    ('tri', p, 'alpha-opt', {'line': 'gauss-legendre'}) for p in (2, 3, 4)
+] + [
+    ('tet', p, 'alpha-opt', {'tri': 'alpha-opt'}) for p in (2, 3, 4)
+] + [
+    ('pri', p, 'alpha-opt~gauss-legendre-lobatto',
+     {'tri': 'alpha-opt', 'quad': 'gauss-legendre'}) for p in (2, 3, 4)
+]
 
-    shapes = {'quad': QuadShape, 'hex': HexShape}
+
+def _store_shape(out, key, s):
+    for m in ('m0', 'm1', 'm2', 'm3', 'm4', 'm6'):
+        out[f'{key}/{m}'] = getattr(s, m)
+    out[f'{key}/M132'] = s.opmat('M1 - M3*M2')
+    out[f'{key}/M460'] = s.opmat('M4 - M6*M0')
+    out[f'{key}/upts'] = s.upts
+    out[f'{key}/fpts'] = s.fpts
+    out[f'{key}/norm_fpts'] = s.norm_fpts
+    out[f'{key}/nfacefpts'] = np.array(s.nfacefpts)
+
+
+def make_operators():
+    from pyfr.shapes import HexShape, PriShape, QuadShape, TetShape, TriShape
+
+    shapes = {'quad': QuadShape, 'hex': HexShape, 'tri': TriShape,
+              'tet': TetShape, 'pri': PriShape}
     out = {}
+    for etype, order, upts, fpts in SIMPLEX_CASES:
+        cfg = _cfg(etype, order, upts, fpts)
+        _store_shape(out, f'{etype}_p{order}_{upts}', shapes[etype](None, cfg))
+
     for etype, order, pts in OPERATOR_CASES:
         cfg = _cfg(etype, order, pts, pts)
         s = shapes[etype](None, cfg)

@@ -53,3 +53,47 @@ def test_opmat_rejects_bad_expression():
     s = get_shape('quad', 2)
     with pytest.raises(ValueError):
         s.opmat('M0.__class__')
+
+
+# Simplex and prism shapes: the reference's named 'alpha-opt' point sets
+# are computed here (warp and blend), listed in lattice order; the
+# triangle table of the reference lists the same points grouped by
+# symmetry orbit.  Points are matched by coordinates, then every operator
+# must agree entry for entry under that permutation.
+SIMPLEX = [('tri', p, 'alpha-opt', 'gauss-legendre') for p in (2, 3, 4)] + \
+    [('tet', p, 'alpha-opt', {'tri': 'alpha-opt'}) for p in (2, 3, 4)] + \
+    [('pri', p, 'alpha-opt~gauss-legendre-lobatto',
+      {'tri': 'alpha-opt', 'quad': 'gauss-legendre'}) for p in (2, 3, 4)]
+
+
+def _perm(mine, ref, tol=1e-13):
+    d = np.linalg.norm(mine[None, :, :] - ref[:, None, :], axis=2)
+    idx = d.argmin(axis=1)
+    assert d[np.arange(len(ref)), idx].max() < tol
+    assert len(set(idx)) == len(ref)
+    return idx
+
+
+@pytest.mark.parametrize('etype,order,upts,fpts', SIMPLEX)
+def test_simplex_operators_match_reference(golden, etype, order, upts, fpts):
+    ref = golden['operators']
+    key = f'{etype}_p{order}_{upts}'
+    s = get_shape(etype, order, upts, fpts)
+    pu = _perm(s.upts, ref[f'{key}/upts'])
+    # Flux points on face edges appear once per face: match face by face
+    pf = np.concatenate([np.array(f)[_perm(s.fpts[f], ref[f'{key}/fpts'][f])]
+                         for f in s.facefpts])
+    np.testing.assert_array_equal(s.nfacefpts, ref[f'{key}/nfacefpts'])
+    np.testing.assert_array_equal(s.norm_fpts[pf], ref[f'{key}/norm_fpts'])
+
+    # Operators over (dim, point) index pairs order them dim-major
+    nd = s.ndims
+    pdu = (np.arange(nd)[:, None]*s.nupts + pu[None, :]).ravel()
+    cases = {'m0': (pf, pu), 'm1': (pu, pdu), 'm2': (pf, pdu),
+             'm3': (pu, pf), 'm4': (pdu, pu), 'm6': (pdu, pf),
+             'M132': (pu, pdu), 'M460': (pdu, pu)}
+    exprs = {'M132': 'M1 - M3*M2', 'M460': 'M4 - M6*M0'}
+    for m, (r, c) in cases.items():
+        mine = s.opmat(exprs[m]) if m in exprs else getattr(s, m)
+        np.testing.assert_allclose(mine[np.ix_(r, c)], ref[f'{key}/{m}'],
+                                   rtol=0, atol=1e-11, err_msg=m)
