@@ -24,6 +24,7 @@ arithmetic of the reference's OpenMP/CUDA kernels on this path:
                              pyfr/integrators/explicit/steppers.py:165-243
   graph order (Euler, NS)    pyfr/solvers/baseadvec/system.py:58-136,
                              pyfr/solvers/baseadvecdiff/system.py:54-231
+  linear element geometry    pyfr/shapes.py:306-566 (interp_expr, jac_exprs)
 
 Everything the oracle needs about the discretisation is passed in: the
 operator matrices (tests feed the ones generated by the reference's own
@@ -351,6 +352,198 @@ class Discretisation:
         r = self.apply(self.ops['M132'], ft.reshape(nd*nupts, -1, ne))
         r += self.apply(self.ops['M3'], uf)
         return -r/self.djac_u[:, None, :]
+
+
+# ---------------------------------------------------------------------------
+# Meshes of several element types
+# ---------------------------------------------------------------------------
+
+def linear_shape(etype, pts):
+    """Values (npts, nverts) and reference gradients (npts, ndims, nverts)
+    of the linear shape functions of ``etype`` (the interpolation and
+    Jacobian expressions of pyfr/shapes.py:306-566), vertices in the
+    reference's order."""
+    pts = np.asarray(pts, dtype=float)
+    n = len(pts)
+    if etype in ('quad', 'hex'):
+        nd = pts.shape[1]
+        s = vertex_signs(nd)
+        N = shape_values(pts, nd)
+        dN = np.empty((n, nd, len(s)))
+        for i in range(nd):
+            t = np.ones((n, len(s)))
+            for d in range(nd):
+                t = t*(s[None, :, d] if d == i
+                       else 1 + pts[:, None, d]*s[None, :, d])
+            dN[:, i] = t/2**nd
+        return N, dN
+    if etype == 'tri':
+        r, q = pts.T
+        N = np.stack([-(r + q)/2, (1 + r)/2, (1 + q)/2], axis=1)
+        g = np.array([[-0.5, 0.5, 0.0], [-0.5, 0.0, 0.5]])
+        return N, np.broadcast_to(g, (n, 2, 3)).copy()
+    if etype == 'tet':
+        r, q, t = pts.T
+        N = np.stack([-(1 + r + q + t)/2, (1 + r)/2, (1 + q)/2, (1 + t)/2],
+                     axis=1)
+        g = np.array([[-0.5, 0.5, 0.0, 0.0], [-0.5, 0.0, 0.5, 0.0],
+                      [-0.5, 0.0, 0.0, 0.5]])
+        return N, np.broadcast_to(g, (n, 3, 4)).copy()
+    if etype == 'pri':
+        r, q, t = pts.T
+        tri = np.stack([-(r + q)/2, (1 + r)/2, (1 + q)/2], axis=1)
+        lo, hi = (1 - t)/2, (1 + t)/2
+        N = np.hstack([tri*lo[:, None], tri*hi[:, None]])
+        dN = np.empty((n, 3, 6))
+        gt = np.array([[-0.5, 0.5, 0.0], [-0.5, 0.0, 0.5]])
+        for i in range(2):
+            dN[:, i, :3] = gt[i][None, :]*lo[:, None]
+            dN[:, i, 3:] = gt[i][None, :]*hi[:, None]
+        dN[:, 2, :3] = -tri/2
+        dN[:, 2, 3:] = tri/2
+        return N, dN
+    raise ValueError(etype)
+
+
+def linear_smats_djac(etype, verts, pts):
+    """Adjugate metric S[p, i, :, e] and |J| of linear elements."""
+    _, dN = linear_shape(etype, pts)
+    J = np.einsum('piv,vej->pije', dN, verts)
+    nd = J.shape[1]
+    s = np.empty_like(J)
+    if nd == 2:
+        s[:, 0, 0], s[:, 0, 1] = J[:, 1, 1], -J[:, 1, 0]
+        s[:, 1, 0], s[:, 1, 1] = -J[:, 0, 1], J[:, 0, 0]
+        d = s[:, 0, 0]*s[:, 1, 1] - s[:, 0, 1]*s[:, 1, 0]
+    else:
+        for i in range(3):
+            a, b = (i + 1) % 3, (i + 2) % 3
+            s[:, i] = np.cross(J[:, a], J[:, b], axisa=1, axisb=1, axisc=1)
+        d = np.einsum('pje,pje->pe', J[:, 0], s[:, 0])
+    return s, d
+
+
+class MixedDiscretisation:
+    """The Euler right-hand side on a mesh of several element types
+    (pyfr/solvers/baseadvec/system.py:58-136 over every element type).
+
+    parts: {etype: dict(ops=..., basis=..., verts=...)} as for
+    ``Discretisation``; lhs/rhs: sequences of (etype, element, face) of
+    the interfaces; periods as for ``Discretisation``.  Fields are dicts
+    {etype: (npts, nvars, neles)}; ``pack``/``unpack`` flatten them for
+    ``rk45_step``.
+    """
+
+    def __init__(self, parts, lhs, rhs, periods=None):
+        self.etypes = list(parts)
+        self.p = {}
+        for et, d in parts.items():
+            e = dict(ops={k: np.asarray(v, dtype=float)
+                          for k, v in d['ops'].items()},
+                     upts=np.asarray(d['basis']['upts'], dtype=float),
+                     fpts=np.asarray(d['basis']['fpts'], dtype=float),
+                     norm=np.asarray(d['basis']['norm_fpts'], dtype=float),
+                     facefpts=[np.asarray(f) for f in d['basis']['facefpts']],
+                     verts=np.asarray(d['verts'], dtype=float))
+            e['neles'] = e['verts'].shape[1]
+            e['smats_u'], e['djac_u'] = linear_smats_djac(et, e['verts'],
+                                                          e['upts'])
+            s_f, _ = linear_smats_djac(et, e['verts'], e['fpts'])
+            e['pnorm'] = np.einsum('plke,pl->pke', s_f, e['norm'])
+            N, _ = linear_shape(et, e['fpts'])
+            e['ploc_f'] = np.einsum('pv,ved->pde', N, e['verts'])
+            self.p[et] = e
+        self.ndims = next(iter(self.p.values()))['verts'].shape[2]
+        self._pair(lhs, rhs, periods)
+
+    def _pair(self, lhs, rhs, periods):
+        """Pair the flux points of every interface by coordinates."""
+        lhs = [(str(a), int(b), int(c)) for a, b, c in lhs]
+        rhs = [(str(a), int(b), int(c)) for a, b, c in rhs]
+        groups = {}
+        for (tl, el, fl), (tr, er, fr) in zip(lhs, rhs):
+            groups.setdefault((tl, fl, tr, fr), []).append((el, er))
+
+        sides = {'l': [], 'r': []}
+        for (tl, fl, tr, fr), ee in groups.items():
+            ee = np.array(ee)
+            el, er = ee[:, 0], ee[:, 1]
+            pl = self.p[tl]['facefpts'][fl]
+            pr = self.p[tr]['facefpts'][fr]
+            xl = self.p[tl]['ploc_f'][pl][:, :, el]
+            xr = self.p[tr]['ploc_f'][pr][:, :, er]
+            d = xl[:, None] - xr[None, :]
+            if periods is not None:
+                P = np.asarray(periods)[:, None]
+                d = d - P*np.rint(d/P)
+            match = np.argmin(np.sum(d*d, axis=2), axis=1)      # (nfp, n)
+            nfp = len(pl)
+            if np.any(np.sort(match, axis=0) != np.arange(nfp)[:, None]):
+                raise RuntimeError('Flux points of an interface do not pair')
+            n = len(el)
+            sides['l'].append((np.full(n*nfp, self.etypes.index(tl)),
+                               np.tile(pl, n), np.repeat(el, nfp)))
+            sides['r'].append((np.full(n*nfp, self.etypes.index(tr)),
+                               pr[match.T].ravel(), np.repeat(er, nfp)))
+        self.side = {k: tuple(np.concatenate(a) for a in zip(*v))
+                     for k, v in sides.items()}
+        t, f, e = self.side['l']
+        nl = np.empty((self.ndims, len(t)))
+        for i, et in enumerate(self.etypes):
+            m = t == i
+            nl[:, m] = self.p[et]['pnorm'][f[m], :, e[m]].T
+        self.nl = nl
+
+    def _gather(self, fld, side):
+        t, f, e = self.side[side]
+        nv = next(iter(fld.values())).shape[1]
+        out = np.empty((nv, len(t)))
+        for i, et in enumerate(self.etypes):
+            m = t == i
+            out[:, m] = fld[et][f[m], :, e[m]].T
+        return out
+
+    def _scatter(self, fld, side, vals):
+        t, f, e = self.side[side]
+        for i, et in enumerate(self.etypes):
+            m = t == i
+            fld[et][f[m], :, e[m]] = vals[:, m].T
+
+    def rhs_euler(self, u, c, rsolver='rusanov'):
+        gamma, nd = c['gamma'], self.ndims
+        uf = {et: Discretisation.apply(self.p[et]['ops']['M0'], u[et])
+              for et in self.etypes}
+        ul, ur = self._gather(uf, 'l'), self._gather(uf, 'r')
+        mag = np.sqrt(np.sum(self.nl**2, axis=0))
+        fn = RSOLVERS[rsolver](ul, ur, self.nl/mag, gamma)
+        self._scatter(uf, 'l', mag*fn)
+        self._scatter(uf, 'r', -mag*fn)
+
+        out = {}
+        for et in self.etypes:
+            e = self.p[et]
+            nupts, ne = len(e['upts']), e['neles']
+            fp, _, _ = inviscid_flux(u[et].transpose(1, 0, 2), gamma)
+            ft = np.einsum('pike,kpve->ipve', e['smats_u'],
+                           fp.transpose(0, 2, 1, 3))
+            r = Discretisation.apply(e['ops']['M132'],
+                                     ft.reshape(nd*nupts, -1, ne))
+            r += Discretisation.apply(e['ops']['M3'], uf[et])
+            out[et] = -r/e['djac_u'][:, None, :]
+        return out
+
+    def pack(self, fld):
+        return np.concatenate([fld[et].ravel() for et in self.etypes])
+
+    def unpack(self, flat, nvars):
+        out, off = {}, 0
+        for et in self.etypes:
+            e = self.p[et]
+            shp = (len(e['upts']), nvars, e['neles'])
+            n = int(np.prod(shp))
+            out[et] = flat[off:off + n].reshape(shp)
+            off += n
+        return out
 
 
 # ---------------------------------------------------------------------------

@@ -14,7 +14,7 @@ import ctypes as C
 
 import numpy as np
 
-from pyfr_gb300.shapes import adjugate_det
+from pyfr_gb300.shapes import ETYPE_OF, adjugate_det, linear_shape_jac
 
 from pyfr_gb300.backend.lib import Gas
 from pyfr_gb300.backend.types import BindableKernel, Kernel, NullKernel
@@ -41,20 +41,20 @@ def _mat(m):
 
 def linear_metrics(verts, upts):
     """Adjugate metric terms S[i][j] (ndims, nupts, ndims, neles) and 1/|J|
-    (nupts, neles) of multilinear elements at reference points ``upts``;
-    verts has io-shape (nverts, ndims, neles), vertex order
-    first-coordinate-fastest.  Same arithmetic as the kernels' in-place
-    computation (pyfr/solvers/baseadvec/kernels/smats.mako:3-25)."""
+    (nupts, neles) of linear elements at reference points ``upts``; verts
+    has io-shape (nverts, ndims, neles) in the reference's vertex order,
+    which with ndims identifies the element type.  Same arithmetic as the
+    kernels' in-place computation for multilinear elements
+    (pyfr/solvers/baseadvec/kernels/smats.mako:3-25) and the Jacobian
+    expressions of the other linear shapes (pyfr/shapes.py)."""
     nverts, nd, ne = verts.shape
-    sg = np.array([[1.0 if (v >> d) & 1 else -1.0 for d in range(nd)]
-                   for v in range(nverts)])
+    try:
+        etype = ETYPE_OF[nd, nverts]
+    except KeyError:
+        raise ValueError(f'No linear element with {nverts} vertices in '
+                         f'{nd} dimensions') from None
     x = np.asarray(upts, dtype=float)
-    dN = np.empty((len(x), nd, nverts))
-    for i in range(nd):
-        t = np.ones((len(x), nverts))
-        for k in range(nd):
-            t = t*(sg[None, :, k] if k == i else 1 + x[:, None, k]*sg[None, :, k])
-        dN[:, i] = t/nverts
+    dN = linear_shape_jac(etype, x)                     # (npts, nd, nverts)
     # J[p, i, j, e] as one matrix product over the vertex index
     npt = len(x)
     J = (dN.reshape(npt*nd, nverts) @ verts.reshape(nverts, nd*ne))
@@ -115,7 +115,11 @@ class PointwiseKernelProvider:
 
     def _geom(self, tplargs, smats=None, rcpdjac=None, verts=None, upts=None):
         linear = 'linear' in tplargs.get('ktype', 'curved')
-        if linear and self.backend.precompute_metrics:
+        # The kernels rebuild metrics in place for multilinear elements
+        # only; other linear shapes always read stored terms
+        multilin = tplargs.get('nverts', 2**tplargs['ndims']) == \
+            2**tplargs['ndims']
+        if linear and (self.backend.precompute_metrics or not multilin):
             # FP64 arithmetic is scarce on this GPU while bandwidth is not:
             # read stored per-point metric terms (10 values) instead of
             # rebuilding the Jacobian from the vertices (~200 flops)
@@ -124,6 +128,9 @@ class PointwiseKernelProvider:
                 smats, rcpdjac = m
                 linear = False
         if linear:
+            if not multilin:
+                raise ValueError('Linear-element kernels of this shape need '
+                                 'the host copies of its vertices')
             return 1, (None, 0), (None, 0), _mat(verts), _mat(upts)
         return 0, _mat(smats), _mat(rcpdjac), (None, 0), (None, 0)
 

@@ -9,12 +9,17 @@
 * ``ns_tgv``: 3-D compressible Taylor-Green vortex on [-pi, pi]^3,
   Re=1600, Ma=0.1, Pr=0.71, rho0=1, isothermal initial density
   rho = rho0 p/p0, Rusanov + LDG (beta=1/2, tau=0.1), RK45.
+* ``euler_mixed``: 3-D Euler on a conforming periodic box of n^3 cells on
+  [-pi, pi]^3 made of hexahedra and prisms, or of prisms and tetrahedra:
+  a density wave rho = 1 + A sin(x + y + z) carried by the uniform
+  velocity (u, v, w) at uniform pressure, whose exact solution is the
+  initial field translated by (u, v, w) t.
 """
 
 import math
 
 from pyfr_gb300.inifile import Inifile
-from pyfr_gb300.mesh import periodic_box
+from pyfr_gb300.mesh import mixed_box, periodic_box
 
 
 def euler_vortex(n=40, order=3, dt=1e-3, beta=5.0, radius=1.0,
@@ -97,3 +102,41 @@ def ns_tgv(n=48, order=3, dt=5e-4, rsolver='rusanov', precision='double',
 
     mesh = periodic_box('hex', n, -math.pi, math.pi)
     return cfg, mesh
+
+
+def euler_mixed(n=32, order=3, kinds='hex-pri', dt=1e-3, amp=0.2,
+                vel=(1.0, 0.5, 0.25), rsolver='rusanov', precision='double'):
+    cfg = Inifile()
+    cfg.set('backend', 'precision', precision)
+    for k, v in dict(gamma=1.4, amp=amp, uc=vel[0], vc=vel[1],
+                     wc=vel[2]).items():
+        cfg.set('constants', k, repr(v))
+    cfg.set('solver', 'system', 'euler')
+    cfg.set('solver', 'order', order)
+    cfg.set('solver-interfaces', 'riemann-solver', rsolver)
+    cfg.set('solver-interfaces-quad', 'flux-pts', 'gauss-legendre')
+    cfg.set('solver-interfaces-tri', 'flux-pts', 'alpha-opt')
+    cfg.set('solver-elements-hex', 'soln-pts', 'gauss-legendre')
+    cfg.set('solver-elements-pri', 'soln-pts',
+            'alpha-opt~gauss-legendre-lobatto')
+    cfg.set('solver-elements-tet', 'soln-pts', 'alpha-opt')
+    cfg.set('solver-time-integrator', 'scheme', 'rk45')
+    cfg.set('solver-time-integrator', 'controller', 'none')
+    cfg.set('solver-time-integrator', 'dt', repr(dt))
+
+    cfg.set('soln-ics', 'rho', '1 + amp*sin(x + y + z)')
+    cfg.set('soln-ics', 'u', 'uc + 0*x')
+    cfg.set('soln-ics', 'v', 'vc + 0*x')
+    cfg.set('soln-ics', 'w', 'wc + 0*x')
+    cfg.set('soln-ics', 'p', '1 + 0*x')
+
+    mesh = mixed_box(n, -math.pi, math.pi, kinds)
+    return cfg, mesh
+
+
+def density_wave_exact(x, y, z, t, cfg):
+    """Exact density of the advected wave of ``euler_mixed``."""
+    import numpy as np
+
+    c = cfg.items_as('constants', float)
+    return 1 + c['amp']*np.sin(x + y + z - (c['uc'] + c['vc'] + c['wc'])*t)

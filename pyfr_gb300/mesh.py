@@ -108,6 +108,149 @@ def periodic_box(etype, ncells, lo, hi):
                 periods=periods)
 
 
+def face_vertices(etype):
+    """Vertex indices of each face of a linear ``etype`` element, in the
+    reference's face order (from the face projections of the shape)."""
+    from pyfr_gb300.shapes import SHAPES, VERTICES
+
+    corners = {'line': [(-1,), (1,)], 'tri': [(-1, -1), (1, -1), (-1, 1)],
+               'quad': [(-1, -1), (1, -1), (-1, 1), (1, 1)]}
+    verts = np.array(VERTICES[etype], dtype=float)
+    out = []
+    for kind, proj, norm in SHAPES[etype].faces:
+        fv = []
+        for c in corners[kind]:
+            x = np.array(proj(*c), dtype=float)
+            (i,) = np.flatnonzero(np.all(np.abs(verts - x) < 1e-12, axis=1))
+            fv.append(int(i))
+        out.append(fv)
+    return out
+
+
+def connect(spts, periods=None, lo=None, tol=1e-8):
+    """Interior interfaces of a conforming mesh: faces of linear elements
+    paired by their centroids (reduced modulo ``periods`` measured from
+    ``lo``) and their vertex offsets from the centroid, so that a periodic
+    box of any size pairs unambiguously.  ``spts`` maps element types to
+    their vertices (nverts, neles, ndims).  Every face must pair up (no
+    boundaries).  Returns the (lhs, rhs) sides; of the two faces of an
+    interface the one met first (types in ``spts`` order, then element,
+    then face) is the left one."""
+    keys, ids = [], []
+    for et, sp in spts.items():
+        ndims = sp.shape[2]
+        for fi, fv in enumerate(face_vertices(et)):
+            c = sp[fv]                                 # (nfv, neles, ndims)
+            cen = c.mean(axis=0)
+            rel = np.rint((c - cen)/tol).astype(np.int64)
+            if periods is not None:
+                per = np.asarray(periods, dtype=float)
+                cen = np.mod(cen - np.asarray(lo, dtype=float), per)
+                cen[np.abs(cen - per) < tol*per] = 0.0
+            qc = np.rint(cen/tol).astype(np.int64)     # (neles, ndims)
+
+            # Order the face's vertices to make the key orientation-free
+            rel = rel.transpose(1, 0, 2)               # (neles, nfv, ndims)
+            o = np.lexsort(tuple(rel[:, :, d]
+                                 for d in reversed(range(ndims))), axis=1)
+            rel = np.take_along_axis(rel, o[:, :, None], axis=1)
+            keys.append(np.hstack([qc, rel.reshape(rel.shape[0], -1)]))
+            ids.append(np.stack([np.full(len(qc), list(spts).index(et)),
+                                 np.arange(len(qc)), np.full(len(qc), fi)],
+                                1))
+
+    nk = max(k.shape[1] for k in keys)
+    keys = np.vstack([np.pad(k, ((0, 0), (0, nk - k.shape[1])),
+                             constant_values=-1) for k in keys])
+    ids = np.vstack(ids)
+    order = np.lexsort(keys.T[::-1])
+    ks = keys[order]
+    same = np.all(ks[1:] == ks[:-1], axis=1)
+    if len(ks) % 2 or not np.all(same[::2]) or np.any(same[1::2]):
+        raise ValueError('Mesh faces do not pair up into interfaces')
+    a, b = ids[order[0::2]], ids[order[1::2]]
+
+    # Left side: the earlier face
+    swap = (a[:, 0]*2**40 + a[:, 1]*8 + a[:, 2]) > \
+        (b[:, 0]*2**40 + b[:, 1]*8 + b[:, 2])
+    a[swap], b[swap] = b[swap], a[swap].copy()
+    o = np.lexsort((a[:, 2], a[:, 1], a[:, 0]))
+    a, b = a[o], b[o]
+    names = np.array(list(spts))
+    return (Side(names[a[:, 0]], a[:, 1], a[:, 2]),
+            Side(names[b[:, 0]], b[:, 1], b[:, 2]))
+
+
+def _cube_cells(n, lo, hi):
+    """Cell corner coordinates of a uniform n^3 grid: (8, ncells, 3) with
+    corners in first-coordinate-fastest order, and the cell indices."""
+    axes = [np.linspace(lo, hi, n + 1)]*3
+    idx = np.indices((n, n, n)).reshape(3, -1)[::-1]       # i fastest
+    c = np.empty((8, idx.shape[1], 3))
+    for v in range(8):
+        for d in range(3):
+            c[v, :, d] = axes[d][idx[d] + ((v >> d) & 1)]
+    return c, idx
+
+
+# Corners (first-coordinate-fastest numbering of the cube) of the two
+# prisms of a cube cut along the diagonal plane through its (0,0)-(1,1)
+# edge pairs, each with the right-angle vertex first and positive volume
+_PRI_OF_CUBE = [[1, 3, 0, 5, 7, 4], [2, 0, 3, 6, 4, 7]]
+
+
+def _tets_of_cube():
+    """Corners of the six tetrahedra of the cube's Kuhn subdivision (one
+    per path (0,0,0) -> (1,1,1) along the axes), in the reference's vertex
+    order with positive volume.  All cubes cut this way conform, and each
+    of their z faces is cut along the same diagonal as the prisms'."""
+    out = []
+    for perm in [(0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1),
+                 (2, 1, 0)]:
+        path, v = [0], 0
+        for d in perm:
+            v |= 1 << d
+            path.append(v)
+        pts = np.array([[(c >> d) & 1 for d in range(3)] for c in path], float)
+        if np.linalg.det((pts[1:] - pts[0]).T) < 0:
+            path[1], path[2] = path[2], path[1]
+        out.append(path)
+    return out
+
+
+def mixed_box(n, lo, hi, kinds):
+    """Conforming periodic box of n^3 cubic cells of side (hi - lo)/n.
+
+    ``kinds`` is 'hex-pri' (cells with x index below n/2 are hexes, the
+    others are cut into two prisms extruded along z) or 'pri-tet' (cells
+    with z index below n/2 are cut into two prisms, the others into the six
+    tetrahedra of the Kuhn subdivision).  A hex face never meets a
+    tetrahedron: their quadrilateral and triangular faces do not conform.
+    Elements of each type are numbered cell by cell, x fastest."""
+    corners, idx = _cube_cells(n, lo, hi)
+    if kinds == 'hex-pri':
+        first = idx[0] < n//2
+        spts = {'hex': corners[:, first],
+                'pri': np.stack([corners[c][:, ~first]
+                                 for c in _PRI_OF_CUBE], axis=2)}
+    elif kinds == 'pri-tet':
+        first = idx[2] < n//2
+        spts = {'pri': np.stack([corners[c][:, first]
+                                 for c in _PRI_OF_CUBE], axis=2),
+                'tet': np.stack([corners[c][:, ~first]
+                                 for c in _tets_of_cube()], axis=2)}
+    else:
+        raise ValueError(f'Unknown mixed mesh {kinds!r}')
+
+    # (nverts, ncells, nsub, 3) -> (nverts, ncells*nsub, 3), cell major
+    spts = {k: v.reshape(v.shape[0], -1, 3) for k, v in spts.items()}
+    con = connect(spts, periods=(hi - lo,)*3, lo=(lo,)*3)
+    return Mesh(ndims=3, spts=spts, con=con,
+                spts_curved={k: np.zeros(v.shape[1], dtype=bool)
+                             for k, v in spts.items()},
+                periods=(hi - lo,)*3)
+
+
 def fuzzy_face_order(coords, tol=1e-6):
     """Per-face ordering of flux points by their physical coordinates,
     lexicographic with the first coordinate most significant and values

@@ -22,7 +22,17 @@ import numpy as np
 
 from pyfr_gb300.backend.types import NullKernel
 from pyfr_gb300.mesh import fuzzy_face_order
-from pyfr_gb300.shapes import adjugate_det, get_shape
+from pyfr_gb300.shapes import SHAPES, adjugate_det, get_shape
+
+
+# Point sets used when the configuration names none (the reference requires
+# them in the configuration: solver-elements-<etype> soln-pts and
+# solver-interfaces-<kind> flux-pts)
+DEFAULT_UPTS = {'quad': 'gauss-legendre', 'hex': 'gauss-legendre',
+                'tri': 'alpha-opt', 'tet': 'alpha-opt',
+                'pri': 'alpha-opt~gauss-legendre-lobatto'}
+DEFAULT_FPTS = {'line': 'gauss-legendre', 'quad': 'gauss-legendre',
+                'tri': 'alpha-opt'}
 
 
 _NPEVAL_SYMS = {k: getattr(np, k) for k in
@@ -49,10 +59,10 @@ class BaseElements:
 
         order = cfg.getint('solver', 'order')
         upts = cfg.get(f'solver-elements-{etype}', 'soln-pts',
-                       'gauss-legendre')
-        kind = 'line' if self.ndims == 2 else 'quad'
-        fpts = cfg.get(f'solver-interfaces-{kind}', 'flux-pts',
-                       'gauss-legendre')
+                       DEFAULT_UPTS[etype])
+        fpts = {k: cfg.get(f'solver-interfaces-{k}', 'flux-pts',
+                           DEFAULT_FPTS[k])
+                for k in {k for k, _, _ in SHAPES[etype].faces}}
         self.basis = get_shape(etype, order, upts, fpts)
         self.name = etype
 

@@ -222,8 +222,83 @@ def make_geometry():
         print(f'geometry_{name}.npz')
 
 
+def _literal(pts):
+    """A point set in the reference's literal rule syntax."""
+    return ', '.join('(' + ', '.join(repr(float(x)) for x in p) + ')'
+                     for p in pts)
+
+
+def perturbed_mixed_box(kinds, n, lo, hi, amp, seed):
+    """Mixed periodic box with every grid vertex jittered (periodic images
+    and all elements sharing a vertex move together)."""
+    sys.path.insert(0, str(REPO))
+    from pyfr_gb300.mesh import mixed_box
+
+    mesh = mixed_box(n, lo, hi, kinds)
+    h = (hi - lo)/n
+    rng = np.random.default_rng(seed)
+    jit = rng.uniform(-amp*h, amp*h, size=(n, n, n, 3))
+    for sp in mesh.spts.values():
+        for v in range(sp.shape[0]):
+            idx = np.rint((sp[v] - lo)/h).astype(int) % n
+            sp[v] += jit[idx[:, 0], idx[:, 1], idx[:, 2]]
+    return mesh
+
+
+MIXED_CASES = {'hexpri_p3': ('hex-pri', 3), 'pritet_p3': ('pri-tet', 3)}
+
+
+def make_mixed():
+    """Operators (in this package's point order, handed to the reference
+    as literal point sets) and element geometry of the mixed meshes."""
+    from pyfr.shapes import HexShape, PriShape, TetShape
+    from pyfr.solvers.euler.elements import EulerElements
+    from pyfr_gb300.quadrules import point_set
+
+    shapes = {'hex': HexShape, 'pri': PriShape, 'tet': TetShape}
+    ops = dict(np.load(HERE / 'operators.npz'))
+    for name, (kinds, order) in MIXED_CASES.items():
+        mesh = perturbed_mixed_box(kinds, 2, -1.0, 1.0, 0.1, seed=11)
+        upts = {'hex': 'gauss-legendre',
+                'pri': _literal(point_set(
+                    'pri', 'alpha-opt~gauss-legendre-lobatto', order)),
+                'tet': _literal(point_set('tet', 'alpha-opt', order))}
+        fpts = {'quad': 'gauss-legendre',
+                'tri': _literal(point_set('tri', 'alpha-opt', order))}
+        ics = dict(rho='1 + 0.2*sin(pi*x)*cos(pi*y)*cos(pi*z)',
+                   u='0.5 + 0.1*y', v='-0.3 + 0.1*z', w='0.2*x',
+                   p='1 + 0.1*cos(pi*x)')
+        out = {}
+        for et, spts in mesh.spts.items():
+            cfg = _cfg(et, order, upts[et], fpts, consts=dict(gamma=1.4),
+                       ics=ics)
+            e = EulerElements(shapes[et], spts, cfg)
+            b = e.basis
+            key = f'{et}_p{order}_mixed'
+            _store_shape(ops, key, b)
+            out[f'{et}/spts'] = spts
+            for fi, sf in enumerate(e.srtd_face_fpts):
+                out[f'{et}/srtd_face_fpts/{fi}'] = sf
+            out[f'{et}/pnorm_fpts'] = e._pnorm_fpts
+            out[f'{et}/rcpdjac_upts'] = e.rcpdjac_at_np('upts')
+            out[f'{et}/smat_upts'] = e.smat_at_np('upts')
+            out[f'{et}/ploc_upts'] = e.ploc_at_np('upts')
+            out[f'{et}/ics'] = e.set_ics_from_cfg()
+        lhs, rhs = mesh.con
+        out['lhs'] = np.stack([lhs.etypes, lhs.eidxs.astype(str),
+                               lhs.fidxs.astype(str)], axis=1)
+        out['rhs'] = np.stack([rhs.etypes, rhs.eidxs.astype(str),
+                               rhs.fidxs.astype(str)], axis=1)
+        for k, v in ics.items():
+            out[f'icexpr/{k}'] = np.array(v)
+        np.savez_compressed(HERE / f'geometry_{name}.npz', **out)
+        print(f'geometry_{name}.npz')
+    np.savez_compressed(HERE / 'operators.npz', **ops)
+
+
 if __name__ == '__main__':
     sys.path.insert(0, str(REF))
     _install_standins()
     make_operators()
     make_geometry()
+    make_mixed()

@@ -76,3 +76,85 @@ def test_discrete_conservation(golden, case, etype):
     tot = np.einsum('p,pve,pe->v', wts, r, d.djac_u)
     scale = np.einsum('p,pve,pe->v', wts, np.abs(r), d.djac_u)
     assert np.all(np.abs(tot) <= 1e-12*scale)
+
+
+# ---------------------------------------------------------------------------
+# Meshes of several element types
+# ---------------------------------------------------------------------------
+
+MIXED_UPTS = {'hex': 'gauss-legendre', 'pri': 'alpha-opt~gauss-legendre-lobatto',
+              'tet': 'alpha-opt'}
+MIXED_FPTS = {'tri': 'alpha-opt', 'quad': 'gauss-legendre'}
+
+
+def mixed_disc(golden, case):
+    """Oracle discretisation of a golden mixed mesh with the reference's
+    operators (hexes: the reference's Gauss-Legendre hex operators)."""
+    from oracle.fr_oracle import MixedDiscretisation
+    g = golden[f'geometry_{case}']
+    ops = golden['operators']
+    parts = {}
+    for et in ('hex', 'pri', 'tet'):
+        if f'{et}/spts' not in g:
+            continue
+        key = 'hex_p3_gauss-legendre' if et == 'hex' else f'{et}_p3_mixed'
+        s = get_shape(et, 3, MIXED_UPTS[et], MIXED_FPTS)
+        parts[et] = dict(ops=ops_from_golden(ops, key), basis=basis_of(s),
+                         verts=g[f'{et}/spts'])
+    return MixedDiscretisation(parts, g['lhs'], g['rhs'],
+                               periods=(2.0,)*3), g
+
+
+@pytest.mark.parametrize('case', ['hexpri_p3', 'pritet_p3'])
+def test_mixed_oracle_geometry_is_the_references(golden, case):
+    d, g = mixed_disc(golden, case)
+    for et, e in d.p.items():
+        np.testing.assert_allclose(1/e['djac_u'], g[f'{et}/rcpdjac_upts'],
+                                   rtol=1e-11)
+        np.testing.assert_allclose(e['pnorm'].transpose(0, 2, 1),
+                                   g[f'{et}/pnorm_fpts'], rtol=1e-11,
+                                   atol=1e-13)
+
+
+@pytest.mark.parametrize('case', ['hexpri_p3', 'pritet_p3'])
+def test_mixed_oracle_pairing_is_the_references(golden, case):
+    # The reference pairs the k-th sorted flux point of each side
+    d, g = mixed_disc(golden, case)
+    srt = {et: [g[f'{et}/srtd_face_fpts/{f}'] for f in range(len(e['facefpts']))]
+           for et, e in d.p.items()}
+    ref = set()
+    for (tl, el, fl), (tr, er, fr) in zip(g['lhs'], g['rhs']):
+        el, fl, er, fr = int(el), int(fl), int(er), int(fr)
+        for a, b in zip(srt[tl][fl][el], srt[tr][fr][er]):
+            ref.add((tl, int(a), el, tr, int(b), er))
+    tl, fl, el = d.side['l']
+    tr, fr, er = d.side['r']
+    mine = {(d.etypes[a], int(b), int(c), d.etypes[x], int(y), int(z))
+            for a, b, c, x, y, z in zip(tl, fl, el, tr, fr, er)}
+    assert mine == ref
+
+
+@pytest.mark.parametrize('case', ['hexpri_p3', 'pritet_p3'])
+def test_mixed_free_stream_and_conservation(golden, case):
+    from pyfr_gb300.quadrules import EXACT_RULES
+    d, g = mixed_disc(golden, case)
+    cons = np.array([1.2, 0.3, 0.6, 0.9, 3.0])
+    u = {et: np.broadcast_to(cons[None, :, None],
+                             (len(e['upts']), 5, e['neles'])).copy()
+         for et, e in d.p.items()}
+    r = d.rhs_euler(u, GAS)
+    assert max(np.abs(v).max() for v in r.values()) < 1e-11
+
+    # The integral of the right-hand side over the mesh vanishes: |J| R is
+    # the polynomial -(M132 F + M3 Fc) of the solution space, integrated
+    # exactly by interpolation to an exact rule
+    r = d.rhs_euler({et: g[f'{et}/ics'] for et in d.p}, GAS)
+    tot, scale = 0, 0
+    for et, e in d.p.items():
+        s = get_shape(et, 3, MIXED_UPTS[et], MIXED_FPTS)
+        qp, qw = EXACT_RULES[et](6)
+        L = s.ubasis.nodal_basis_at(qp)
+        rq = np.einsum('qp,pve->qve', L, r[et]*e['djac_u'][:, None, :])
+        tot = tot + np.einsum('q,qve->v', qw, rq)
+        scale = scale + np.einsum('q,qve->v', qw, np.abs(rq))
+    assert np.all(np.abs(tot) <= 1e-12*scale)
