@@ -570,6 +570,77 @@ def run_ensemble(args, dist):
     return res
 
 
+def run_mixed(args, dist):
+    """The batching configuration's mixed meshes: 3-D Euler on a periodic
+    box of n^3 cells, hexahedra and prisms, or prisms and tetrahedra
+    (p = 3; an advected density wave), plain FP64 and the chosen form;
+    one CUDA graph per RK45 step over every element type."""
+    import ctypes as C
+
+    import __graft_entry__ as ge
+    from pyfr_gb300.backend import B200Backend
+    from pyfr_gb300.cases import euler_mixed
+    from pyfr_gb300.integrators import MixedRKIntegrator, RKVdH2Integrator
+    from pyfr_gb300.solvers.system import EulerSystem
+    ge.build_library()
+
+    def timed(be, fn):
+        lib, stream = be.lib, be.stream
+        ev = [C.c_void_p(), C.c_void_p()]
+        for e in ev:
+            lib.event_create(C.byref(e))
+        be.wait()
+        dist.barrier()
+        with ClockSampler(args.local_rank) as clk:
+            lib.event_record(ev[0].value, stream)
+            fn()
+            lib.event_record(ev[1].value, stream)
+            lib.event_sync(ev[1].value)
+        ms = C.c_float()
+        lib.event_elapsed(C.byref(ms), ev[0].value, ev[1].value)
+        return dist.allmax(ms.value), clk.summary()
+
+    res = {}
+    for kinds in ('hex-pri', 'pri-tet'):
+        out, solns = {}, {}
+        for form in ('plain', 'chosen', 'tf32'):
+            prec = 'double' if form == 'plain' else 'single'
+            cfg, mesh = euler_mixed(n=args.mixed_n, order=3, kinds=kinds,
+                                    dt=args.mixed_dt, precision=prec)
+            cfg.set('backend-b200', 'device-id', str(args.local_rank))
+            icls = RKVdH2Integrator
+            if form == 'chosen':
+                cfg.set('backend-b200', 'mul-precision', 'bf16x3')
+                cfg.set('backend-b200', 'split-products',
+                        str(args.chosen_products))
+                icls = MixedRKIntegrator
+            elif form == 'tf32':
+                cfg.set('backend-b200', 'mul-precision', 'tf32')
+                icls = MixedRKIntegrator
+            be = B200Backend(cfg)
+            intg = icls(be, EulerSystem, mesh, cfg)
+            intg.run_steps(args.warmup)
+            ms, clk = timed(be, lambda: intg.run_steps(args.steps))
+            nrhs = args.steps*intg.nstages
+            out[form] = {
+                'gdofs': dist.world*intg.gndofs*nrhs/(ms*1e-3)/1e9,
+                'ms_per_step': ms/args.steps, 'clocks': clk,
+                'ndofs': intg.gndofs,
+                'neles': {et: int(v.shape[1]) for et, v in mesh.spts.items()}}
+            solns[form] = [np.asarray(u, dtype=np.float64)
+                           for u in intg.soln]
+            del intg, be
+        for form in ('chosen', 'tf32'):
+            out[form]['l2_err_vs_fp64'] = max(
+                float(np.linalg.norm(a - b)/np.linalg.norm(b))
+                for a, b in zip(solns[form], solns['plain']))
+            out[form]['accuracy_after_steps'] = args.warmup + args.steps
+            out[f'speedup_{form}_vs_plain'] = \
+                out[form]['gdofs']/out['plain']['gdofs']
+        res[kinds] = out
+    return res
+
+
 # ---------------------------------------------------------------------------
 # CPU arm (the oracle restatement, bounded sample)
 # ---------------------------------------------------------------------------
@@ -617,7 +688,7 @@ def main():
     ap.add_argument('--cpu-seconds', type=float, default=10.0)
     ap.add_argument('--no-chosen', dest='chosen', action='store_false',
                     help='skip the chosen precision form')
-    ap.add_argument('--chosen-products', type=int, default=4, choices=[3, 4],
+    ap.add_argument('--chosen-products', type=int, default=4, choices=[3, 4, 5],
                     help='split-BF16 products of the chosen form')
     ap.add_argument('--accuracy-steps', type=int, default=200,
                     help='steps after which the chosen form is compared '
@@ -631,6 +702,11 @@ def main():
     ap.add_argument('--large-steps', type=int, default=100)
     ap.add_argument('--large-plain-n', type=int, default=96)
     ap.add_argument('--large-plain-steps', type=int, default=5)
+    ap.add_argument('--mixed', action='store_true',
+                    help='time the mixed hexahedron/prism and '
+                    'prism/tetrahedron meshes instead')
+    ap.add_argument('--mixed-n', type=int, default=32)
+    ap.add_argument('--mixed-dt', type=float, default=1e-3)
     ap.add_argument('--ensemble', action='store_true',
                     help='the batching configuration\'s ensemble of 2-D '
                          'vortex cases instead of the headline run')
@@ -687,6 +763,21 @@ def main():
                 'config': {'workload': '2-D Euler isentropic-vortex '
                                        'ensemble, merged by order, one CUDA '
                                        'graph per RK45 step'},
+                'data': 'synthetic'} | r))
+        return
+
+    if args.mixed:
+        r = run_mixed(args, Dist(world))
+        if rank == 0:
+            print(json.dumps({
+                'metric': METRIC, 'unit': 'GDoF/s', 'n_gpus': world,
+                'steps': args.steps, 'warmup': args.warmup,
+                'config': {'workload': f'3-D Euler, periodic '
+                                       f'{args.mixed_n}^3-cell box of '
+                                       'hexahedra+prisms and of '
+                                       'prisms+tetrahedra, p=3, density '
+                                       'wave, one CUDA graph per RK45 step',
+                           'dt': args.mixed_dt},
                 'data': 'synthetic'} | r))
         return
 

@@ -136,7 +136,8 @@ typedef struct {
     int64_t ldr;
     int nvars;
     int products;               /* 3 (or 0): Ahi*Bhi + Ahi*Blo + Alo*Bhi;
-                                   4: plus Alo*Blo */
+                                   4: plus Alo*Blo; 5: plus Ax3*Bhi (a
+                                   handle with a three-term operator) */
     int *err;                   /* device int: pipeline timeout code */
 } b200_mul_bf16x3_args_t;
 int b200_mul_bf16x3_create_cat(const double *a1, int k1, const double *a2, int k2, int m,
@@ -159,6 +160,15 @@ int b200_mul_tf32_create_cat(const double *a1, int k1, const double *a2, int k2,
 int b200_mul_tc_create_plan(const double *a1, int k1, const double *a2, int k2, int m, int tf32,
                             int nstages, int ntiles, void **handle, size_t *smem_bytes);
 int b200_mul_tc_plan(void *handle, int *nstages, int *ntiles);
+/* As _create_plan with the operator split into nterms BF16 terms: 2 (hi,
+ * lo) or 3 (hi, lo and the rounded remainder, 24 significant bits; split-
+ * BF16 only, applied with products = 5).  nstages = ntiles = 0 picks the
+ * deepest ring that fits; B200_ERR_UNSUPPORTED when no plan fits shared
+ * memory.  _terms reports a handle's operator terms. */
+int b200_mul_tc_create_terms(const double *a1, int k1, const double *a2, int k2, int m,
+                             int tf32, int nterms, int nstages, int ntiles, void **handle,
+                             size_t *smem_bytes);
+int b200_mul_tc_terms(void *handle, int *nterms);
 
 /* ---- element pointwise kernels over [nupts, neles] ------------------- */
 /* Geometry: linear != 0 computes the metric terms from the element

@@ -120,9 +120,12 @@ class B200Backend:
 
         # Split-BF16 products: 3 (Ahi Bhi + Ahi Blo + Alo Bhi) or 4 (plus
         # Alo Blo)
+        # 3: Ahi*Bhi + Ahi*Blo + Alo*Bhi; 4: plus Alo*Blo; 5: the operator in
+        # three BF16 terms, plus Ax3*Bhi (operators whose three-term image
+        # does not fit shared memory fall back to four products)
         self.split_products = cfg.getint('backend-b200', 'split-products', 3)
-        if self.split_products not in {3, 4}:
-            raise ValueError('split-products must be 3 or 4')
+        if self.split_products not in {3, 4, 5}:
+            raise ValueError('split-products must be 3, 4 or 5')
 
         # Fused operator applies (mul_cat, mul_batched): the tensor-core
         # provider serves them, so by default they follow mul-precision

@@ -117,6 +117,9 @@ _SIGS = {
     'b200_mul_tc_create_plan': [pd, i32, pd, i32, i32, i32, i32, i32,
                                 C.POINTER(vp), C.POINTER(sz)],
     'b200_mul_tc_plan': [vp, C.POINTER(i32), C.POINTER(i32)],
+    'b200_mul_tc_create_terms': [pd, i32, pd, i32, i32, i32, i32, i32, i32,
+                                 C.POINTER(vp), C.POINTER(sz)],
+    'b200_mul_tc_terms': [vp, C.POINTER(i32)],
     'b200_mul_tf32_create_cat': [pd, i32, pd, i32, i32, C.POINTER(vp),
                                  C.POINTER(sz)],
 }

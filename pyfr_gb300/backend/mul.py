@@ -136,6 +136,7 @@ class TensorMulKernels:
         from pyfr_gb300.backend.base import release
         self.backend = backend
         self._handles = {}
+        self._nterms = {}
         weakref.finalize(self, release, _destroy_handles,
                          backend.lib.mul_bf16x3_destroy, self._handles)
 
@@ -161,23 +162,26 @@ class TensorMulKernels:
             pd = C.POINTER(C.c_double)
             lib = self.backend.lib
             tf32 = self.backend.mul_precision == 'tf32'
-            create = lib.mul_tf32_create_cat if tf32 else \
-                lib.mul_bf16x3_create_cat
             args = (a1.ctypes.data_as(pd), a1.shape[1],
                     a2.ctypes.data_as(pd) if a2 is not None else None,
                     a2.shape[1] if a2 is not None else 0, a1.shape[0])
-            try:
-                plan = self._tuned_plan(args, tf32) \
-                    if self.backend.autotune else None
-                if plan:
-                    lib.mul_tc_create_plan(*args, int(tf32), *plan,
-                                           C.byref(h), C.byref(smem))
-                else:
-                    create(*args, C.byref(h), C.byref(smem))
-            except B200Error:
-                self._handles[key] = None
-            else:
+
+            # Five products need the operator in three terms; where that
+            # image leaves no room for the ring, two terms and four products
+            want = 3 if self.backend.split_products == 5 and not tf32 else 2
+            self._handles[key] = None
+            for nterms in range(want, 1, -1):
+                try:
+                    plan = self._tuned_plan(args, tf32, nterms) \
+                        if self.backend.autotune else None
+                    lib.mul_tc_create_terms(*args, int(tf32), nterms,
+                                            *(plan or (0, 0)), C.byref(h),
+                                            C.byref(smem))
+                except B200Error:
+                    continue
                 self._handles[key] = (h.value, smem.value, hosts)
+                self._nterms[h.value] = nterms
+                break
 
         if self._handles[key] is None:
             raise NotSuitableError('operator too large for the tensor tiles')
@@ -187,7 +191,11 @@ class TensorMulKernels:
     def _aligned(*mats):
         return all(m.leaddim % 4 == 0 for m in mats)
 
-    def _tuned_plan(self, args, tf32):
+    def _products(self, nterms):
+        p = self.backend.split_products
+        return 5 if nterms == 3 else min(p, 4)
+
+    def _tuned_plan(self, args, tf32, nterms=2):
         """Pipeline plan (ring stages, epilogue staging tiles) of an
         operator, picked by timing every plan that fits on a
         representative width (8 tiles of 128 columns per SM) and cached per
@@ -196,7 +204,7 @@ class TensorMulKernels:
         be, lib = self.backend, self.backend.lib
         m, k1, k2 = args[4], args[1], args[3]
         key = '|'.join(map(str, (be.platform_id, 'tf32' if tf32 else 'bf16',
-                                 be.split_products, m, k1, k2)))
+                                 self._products(nterms), m, k1, k2)))
         cache = _plan_cache()
         if key in cache:
             return tuple(cache[key]) if cache[key] else None
@@ -224,14 +232,15 @@ class TensorMulKernels:
                 for nstages in (4, 6, 8, 10):
                     h, smem = C.c_void_p(), C.c_size_t()
                     try:
-                        lib.mul_tc_create_plan(*args, int(tf32), nstages,
-                                               ntiles, C.byref(h),
-                                               C.byref(smem))
+                        lib.mul_tc_create_terms(*args, int(tf32), nterms,
+                                                nstages, ntiles, C.byref(h),
+                                                C.byref(smem))
                     except B200Error:
                         continue
                     a = MulArgs(b1=b1, ldb1=ncol, b2=b2, ldb2=ncol, c=c,
                                 ldc=ncol, ncol=ncol, nbatch=1, alpha=1.0,
-                                beta=0.0, products=be.split_products, err=err)
+                                beta=0.0, products=self._products(nterms),
+                                err=err)
                     pa = C.addressof(a)
                     for _ in range(2):
                         lib.mul_bf16x3_apply(h.value, pa, be.stream)
@@ -259,8 +268,8 @@ class TensorMulKernels:
     def _kernel(self, handle, args, mats, meta):
         be = self.backend
         args.err = be.status_word
-        args.products = be.split_products
-        meta['products'] = be.split_products
+        args.products = self._products(self._nterms.get(handle, 2))
+        meta['products'] = args.products
         if be.mul_precision == 'tf32':
             meta['impl'] = meta['impl'].replace('bf16x3', 'tf32')
         fn = be.lib.mul_bf16x3_apply

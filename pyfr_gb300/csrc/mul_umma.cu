@@ -3,7 +3,11 @@
 // with A = Ahi + Alo and B = Bhi + Blo split into BF16 halves and the
 // product formed as Ahi*Bhi + Ahi*Blo + Alo*Bhi (three tcgen05.mma per K
 // step, FP32 accumulation in tensor memory), or with Alo*Blo as a fourth
-// product (the exact product of the split operands).  This is the chosen-precision
+// product (the exact product of the split operands).  A handle may also hold
+// the operator in three BF16 terms (24 significant bits, as FP32): the fifth
+// product Ax3*Bhi then removes the operator's representation error, which
+// is systematic (the same in every apply) and against data with a large
+// mean it dominates that of the data's split.  This is the chosen-precision
 // replacement of the reference's `mul` providers
 // (pyfr/backends/cuda/gimmik.py:23-121, pyfr/backends/cuda/cublaslt.py:169-280).
 //
@@ -82,7 +86,9 @@ constexpr uint32_t EPI_BUF = 32 * TCOLS * 4;       // one 32-row x 128-column st
 struct UmmaHandle {
     int m, k1, k2, nch1, npad, kfull, ns, eb;
     int tf32;              // operator image and MMAs in TF32 (one product)
-    unsigned char *aimg;   // device: [hi | lo], each npad x kfull bf16 canonical
+    int nterms;            // BF16 terms of the operator split (2 or 3)
+    unsigned char *aimg;   // device: [hi | lo (| third)], each npad x kfull
+                           // bf16 canonical
     size_t aimg_bytes;
     size_t smem_bytes;
 };
@@ -90,19 +96,21 @@ struct UmmaHandle {
 // Shared-memory plan; stage buffers are addressed arithmetically (a
 // runtime-indexed array here would live in local memory)
 struct Layout {
-    uint32_t a_hi, a_lo;
+    uint32_t a_hi, a_lo, a_x3;    // operator terms (a_x3: third, if any)
     uint32_t ring;                // stage s at ring + s*CHUNK32: FP32 chunk, then
                                   // BF16 hi (first 8 KB) and lo (second 8 KB)
     uint32_t epi;                 // staging tile b of set h at epi + (h*eb + b)*EPI_BUF
     uint32_t bar, tslot, abort_flag, total;
 };
 
-__host__ __device__ inline Layout make_layout(int npad, int kfull, int ns, int eb) {
+__host__ __device__ inline Layout make_layout(int npad, int kfull, int ns, int eb,
+                                              int nterms) {
     Layout L;
     uint32_t off = 0;
     const uint32_t abytes = (uint32_t)npad * kfull * 2;
     L.a_hi = off; off += abytes;
     L.a_lo = off; off += abytes;
+    L.a_x3 = off; off += nterms == 3 ? abytes : 0;
     off = (off + 1023) & ~1023u;
     L.ring = off; off += ns * CHUNK32;
     L.epi = off; off += 2 * eb * EPI_BUF;
@@ -250,6 +258,7 @@ struct UmmaArgs {
     const float *rs;            // row scale S (null: none), S[row*ldr + element]
     int64_t ncol, ntc, ldr;     // ntc: column tiles per slice
     int m, npad, kfull, nch1, ns, eb, nbatch, nvars, products;
+    int nterms;                 // operator terms in the image (2 or 3)
     float alpha;
     int epi;            // 0: store, 1: add to out
     int *err;
@@ -258,7 +267,7 @@ struct UmmaArgs {
 template <bool TF32>
 __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_constant__ UmmaArgs p) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    const Layout L = make_layout(p.npad, p.kfull, p.ns, p.eb);
+    const Layout L = make_layout(p.npad, p.kfull, p.ns, p.eb, p.nterms);
     const int eb = p.eb;
     const int NS = p.ns;
     // (the host plans an even ring of at least four stages; see create)
@@ -305,6 +314,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
     const uint32_t tmem = *tslot;
 
     const uint32_t abytes = (uint32_t)npad * p.kfull * 2;
+    const uint32_t imgbytes = (uint32_t)p.nterms * abytes;
     // 8-row group strides of the operator image and of a converted chunk:
     // (K extent / elements per 16-byte core-matrix row) x 128 bytes
     const uint32_t SBO_OP = (uint32_t)p.kfull * (TF32 ? 32 : 16), LBO = 128;
@@ -312,13 +322,13 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
 
     if (warp == WARP_PROD) {
         // ---- producer: operator image once, then the FP32 chunks of B ----
-        if (lane == 0) bar_arrive_tx(bar(BAR_A), 2 * abytes);
+        if (lane == 0) bar_arrive_tx(bar(BAR_A), imgbytes);
         __syncwarp();
         {
-            const uint32_t chunk = ((2 * abytes / 32) + 15) & ~15u;
+            const uint32_t chunk = ((imgbytes / 32) + 15) & ~15u;
             const uint32_t a0 = lane * chunk;
-            if (a0 < 2 * abytes) {
-                const uint32_t nb = 2 * abytes - a0 < chunk ? 2 * abytes - a0 : chunk;
+            if (a0 < imgbytes) {
+                const uint32_t nb = imgbytes - a0 < chunk ? imgbytes - a0 : chunk;
                 bulk_g2s(sbase + L.a_hi + a0, p.aimg + a0, nb, bar(BAR_A));
             }
         }
@@ -456,7 +466,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
                         umma(d, dh, oh, idesc, (c | ks) != 0);
                         umma(d, dl, oh, idesc, 1);
                         umma(d, dh, ol, idesc, 1);
-                        if (p.products == 4) umma(d, dl, ol, idesc, 1);
+                        if (p.products >= 4) umma(d, dl, ol, idesc, 1);
+                        if (p.products == 5)
+                            umma(d, dh, sdesc(sbase + L.a_x3 + kg, LBO, SBO_OP), idesc, 1);
                     }
                     umma_commit(bar(BAR_FREE + s2));
                 }
@@ -561,22 +573,25 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
                      :: "r"(tmem), "r"(tcols));
 }
 
-// Host: split [A1 | A2] into BF16 hi/lo and lay both out in the canonical
-// K-major no-swizzle layout ((r/8)*SBO + (k/8)*128 + (r%8)*16 + (k%8)*2
-// bytes, SBO = kfull*16), A2's columns starting at column k2off (a chunk
-// boundary); rows past m and the padding columns are zero.
-void build_block(const double *a, int m, int k, int koff, int kfull, size_t n,
+// Host: split [A1 | A2] into BF16 terms (hi, lo and, with three terms, the
+// rounded remainder: 8, 16 or 24 leading significant bits of each entry) and
+// lay each out in the canonical K-major no-swizzle layout ((r/8)*SBO +
+// (k/8)*128 + (r%8)*16 + (k%8)*2 bytes, SBO = kfull*16), A2's columns
+// starting at column k2off (a chunk boundary); rows past m and the padding
+// columns are zero.  Remainders are formed in FP64 from the FP64 operator.
+void build_block(const double *a, int m, int k, int koff, int kfull, size_t n, int nterms,
                  std::vector<uint16_t> &img) {
     const size_t SBO = (size_t)kfull * 16;
     for (int r = 0; r < m; r++)
         for (int c0 = 0; c0 < k; c0++) {
             const int c = koff + c0;
-            const float x = (float)a[(size_t)r * k + c0];
-            const __nv_bfloat16 h = __float2bfloat16_rn(x);
-            const __nv_bfloat16 l = __float2bfloat16_rn(x - __bfloat162float(h));
             const size_t off = (r / 8) * SBO + (c / 8) * 128 + (r % 8) * 16 + (c % 8) * 2;
-            img[off / 2] = __bfloat16_as_ushort(h);
-            img[n + off / 2] = __bfloat16_as_ushort(l);
+            double rem = a[(size_t)r * k + c0];
+            for (int t = 0; t < nterms; t++) {
+                const __nv_bfloat16 h = __float2bfloat16_rn((float)rem);
+                img[t * n + off / 2] = __bfloat16_as_ushort(h);
+                rem -= (double)__bfloat162float(h);
+            }
         }
 }
 
@@ -648,9 +663,11 @@ extern "C" {
 namespace {
 
 int create_impl(const double *a1, int k1, const double *a2, int k2, int m, int tf32,
-                int want_ns, int want_eb, void **handle, size_t *smem_bytes) {
+                int nterms, int want_ns, int want_eb, void **handle, size_t *smem_bytes) {
     if (!a1 || !handle || m <= 0 || k1 <= 0 || k2 < 0 || (k2 > 0 && !a2))
         return b200::set_error(B200_ERR_ARG, "mul_bf16x3_create: bad arguments");
+    if (nterms != 2 && !(nterms == 3 && !tf32))
+        return b200::set_error(B200_ERR_ARG, "mul_bf16x3_create: %d operator terms", nterms);
     const int nch1 = (k1 + KC - 1) / KC, nch2 = (k2 + KC - 1) / KC;
     const int npad = (m + 31) / 32 * 32, kfull = (nch1 + nch2) * KC;
     // The deepest ring (bytes in flight per SM) that fits in shared memory
@@ -665,19 +682,19 @@ int create_impl(const double *a1, int k1, const double *a2, int k2, int m, int t
     // and the ring the room.  A caller (the autotuner) may ask for a given
     // plan instead (want_ns even, 4..MAX_S; want_eb 1 or 2).
     int ns = 0, eb = npad <= 64 ? 1 : MAX_EB;
-    Layout L = make_layout(npad, kfull, 2, eb);
+    Layout L = make_layout(npad, kfull, 2, eb, nterms);
     if (want_ns || want_eb) {
         if ((want_ns & 1) || want_ns < 4 || want_ns > MAX_S || want_eb < 1 || want_eb > MAX_EB)
             return b200::set_error(B200_ERR_ARG, "mul_bf16x3: plan (%d stages, %d tiles) invalid",
                                    want_ns, want_eb);
         ns = want_ns;
         eb = want_eb;
-        L = make_layout(npad, kfull, ns, eb);
+        L = make_layout(npad, kfull, ns, eb, nterms);
     } else {
         for (; eb >= 1 && ns < 4; eb--) {
             ns = 0;
             for (int cand = MAX_S; cand >= 4 && !ns; cand -= 2) {
-                Layout c = make_layout(npad, kfull, cand, eb);
+                Layout c = make_layout(npad, kfull, cand, eb, nterms);
                 if (c.total <= 227 * 1024) {
                     ns = cand;
                     L = c;
@@ -727,19 +744,19 @@ int create_impl(const double *a1, int k1, const double *a2, int k2, int m, int t
     }
 
     const size_t n = (size_t)npad * kfull;
-    std::vector<uint16_t> img(2 * n, 0);
+    std::vector<uint16_t> img((size_t)nterms * n, 0);
     if (tf32) {
         build_block_tf32(a1, m, k1, 0, kfull, img);
         if (k2) build_block_tf32(a2, m, k2, nch1 * KC, kfull, img);
     } else {
-        build_block(a1, m, k1, 0, kfull, n, img);
-        if (k2) build_block(a2, m, k2, nch1 * KC, kfull, n, img);
+        build_block(a1, m, k1, 0, kfull, n, nterms, img);
+        if (k2) build_block(a2, m, k2, nch1 * KC, kfull, n, nterms, img);
     }
 
     UmmaHandle *h = (UmmaHandle *)calloc(1, sizeof(UmmaHandle));
     if (!h) return b200::set_error(B200_ERR_STATE, "mul_bf16x3_create: out of host memory");
     h->m = m; h->k1 = k1; h->k2 = k2; h->nch1 = nch1; h->npad = npad; h->kfull = kfull;
-    h->ns = ns; h->eb = eb; h->tf32 = tf32;
+    h->ns = ns; h->eb = eb; h->tf32 = tf32; h->nterms = nterms;
     h->aimg_bytes = img.size() * 2;
     h->smem_bytes = L.total;
     int rc = b200::check_cuda(cudaMalloc(&h->aimg, h->aimg_bytes), "mul_bf16x3_create");
@@ -761,25 +778,39 @@ extern "C" {
 
 int b200_mul_bf16x3_create_cat(const double *a1, int k1, const double *a2, int k2, int m,
                                 void **handle, size_t *smem_bytes) {
-    return create_impl(a1, k1, a2, k2, m, 0, 0, 0, handle, smem_bytes);
+    return create_impl(a1, k1, a2, k2, m, 0, 2, 0, 0, handle, smem_bytes);
 }
 
 int b200_mul_bf16x3_create(const double *a, int m, int k, void **handle, size_t *smem_bytes) {
-    return create_impl(a, k, nullptr, 0, m, 0, 0, 0, handle, smem_bytes);
+    return create_impl(a, k, nullptr, 0, m, 0, 2, 0, 0, handle, smem_bytes);
 }
 
 int b200_mul_tf32_create_cat(const double *a1, int k1, const double *a2, int k2, int m,
                              void **handle, size_t *smem_bytes) {
-    return create_impl(a1, k1, a2, k2, m, 1, 0, 0, handle, smem_bytes);
+    return create_impl(a1, k1, a2, k2, m, 1, 2, 0, 0, handle, smem_bytes);
 }
 
 int b200_mul_tf32_create(const double *a, int m, int k, void **handle, size_t *smem_bytes) {
-    return create_impl(a, k, nullptr, 0, m, 1, 0, 0, handle, smem_bytes);
+    return create_impl(a, k, nullptr, 0, m, 1, 2, 0, 0, handle, smem_bytes);
 }
 
 int b200_mul_tc_create_plan(const double *a1, int k1, const double *a2, int k2, int m, int tf32,
                             int nstages, int ntiles, void **handle, size_t *smem_bytes) {
-    return create_impl(a1, k1, a2, k2, m, tf32 ? 1 : 0, nstages, ntiles, handle, smem_bytes);
+    return create_impl(a1, k1, a2, k2, m, tf32 ? 1 : 0, 2, nstages, ntiles, handle, smem_bytes);
+}
+
+int b200_mul_tc_create_terms(const double *a1, int k1, const double *a2, int k2, int m,
+                             int tf32, int nterms, int nstages, int ntiles, void **handle,
+                             size_t *smem_bytes) {
+    return create_impl(a1, k1, a2, k2, m, tf32 ? 1 : 0, nterms, nstages, ntiles, handle,
+                       smem_bytes);
+}
+
+int b200_mul_tc_terms(void *handle, int *nterms) {
+    UmmaHandle *h = (UmmaHandle *)handle;
+    if (!h || !nterms) return b200::set_error(B200_ERR_ARG, "mul_tc_terms: null argument");
+    *nterms = h->nterms;
+    return B200_OK;
 }
 
 int b200_mul_tc_plan(void *handle, int *nstages, int *ntiles) {
@@ -813,8 +844,11 @@ int b200_mul_bf16x3_apply(void *handle, const b200_mul_bf16x3_args_t *a, void *s
         (h->k2 && a->ldb2 % 4) ||
         (a->nbatch > 1 && ((a->bstride1 % 4) || (a->cstride % 4) || (h->k2 && a->bstride2 % 4))))
         return b200::set_error(B200_ERR_ARG, "mul_bf16x3: operands must be 16-byte aligned");
-    if (a->products != 0 && a->products != 3 && a->products != 4)
-        return b200::set_error(B200_ERR_ARG, "mul_bf16x3: products must be 3 or 4");
+    if (a->products != 0 && a->products != 3 && a->products != 4 && a->products != 5)
+        return b200::set_error(B200_ERR_ARG, "mul_bf16x3: products must be 3, 4 or 5");
+    if (a->products == 5 && (h->nterms != 3 || h->tf32))
+        return b200::set_error(B200_ERR_ARG,
+                               "mul_bf16x3: five products need a three-term operator");
     if (a->rowscale && (a->nvars <= 0 || a->ldr <= 0 || a->nbatch != 1))
         return b200::set_error(B200_ERR_ARG, "mul_bf16x3: row scale needs nvars, ldr, one slice");
 
@@ -843,7 +877,8 @@ int b200_mul_bf16x3_apply(void *handle, const b200_mul_bf16x3_args_t *a, void *s
     p.eb = h->eb;
     p.nbatch = a->nbatch;
     p.alpha = a->alpha; p.epi = a->beta != 0.0f; p.err = a->err;
-    p.products = a->products == 4 ? 4 : 3;
+    p.products = a->products == 0 ? 3 : a->products;
+    p.nterms = h->nterms;
 
     const int64_t ntiles = p.ntc * p.nbatch;
     const unsigned grid = (unsigned)(ntiles < g_sm_count ? ntiles : g_sm_count);

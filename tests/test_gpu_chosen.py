@@ -64,6 +64,43 @@ def test_mul_tensor_cores(built, golden, key, opname, prec):
                           1e-6*np.abs(ref))
 
 
+def _bf16_pair_exact(x):
+    """Values with at most 16 significant bits (exact as BF16 hi + lo)."""
+    x = np.asarray(x, dtype=np.float32)
+    u = x.view(np.uint32) & np.uint32(0xffff8000)
+    return u.view(np.float32).astype(np.float64)
+
+
+@pytest.mark.parametrize('key', ['hex_p3_gauss-legendre', 'quad_p3_gauss-legendre',
+                                 'pri_p3_mixed', 'tet_p3_mixed'])
+@pytest.mark.parametrize('opname', ['m0', 'M132', 'm3', 'M460', 'm6'])
+def test_mul_three_term_operator(built, golden, key, opname):
+    """Five products (operator in three BF16 terms): on data whose split
+    is exact, a large uniform offset included, the only error left is the
+    FP32 accumulation (bound 2e-6 sum|a||b|, where the two-term operator's
+    own error is ~2^-17 sum|a||b|)."""
+    from pyfr_gb300.backend import B200Backend
+    from pyfr_gb300.inifile import Inifile
+    a = golden['operators'][f'{key}/{opname}']
+    cfg = Inifile()
+    cfg.set('backend', 'precision', 'single')
+    cfg.set('backend-b200', 'mul-precision', 'bf16x3')
+    cfg.set('backend-b200', 'split-products', '5')
+    be = B200Backend(cfg)
+    rng = np.random.default_rng(9)
+    b = _bf16_pair_exact(3.0 + 0.1*rng.normal(size=(a.shape[1], 5, 333)))
+    A = be.const_matrix(a)
+    B = be.matrix(b.shape, b, tags={'align'})
+    C = be.matrix((a.shape[0], 5, 333), tags={'align'})
+    be.commit()
+    k = be.kernel('mul', A, B, out=C)
+    assert k.meta['products'] == 5
+    be.run_kernels([k], wait=True)
+    ref = np.einsum('mk,kve->mve', a, b)
+    bound = 2e-6*np.einsum('mk,kve->mve', np.abs(a), np.abs(b)) + 1e-7
+    assert np.all(np.abs(C.get() - ref) <= bound)
+
+
 @pytest.mark.parametrize('neles', [77, 1000])
 def test_mul_bf16x3_cat_rowscale(built, golden, neles):
     """Fused apply out = alpha*S*(A1@B1 + A2@B2) (+ out): the divergence,
