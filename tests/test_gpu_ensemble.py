@@ -22,7 +22,7 @@ def _backend(prec, mul='native'):
     cfg.set('backend', 'precision', prec)
     cfg.set('backend-b200', 'mul-precision', mul)
     if mul != 'native':
-        cfg.set('backend-b200', 'split-products', '4')
+        cfg.set('backend-b200', 'split-products', '5')
     return B200Backend(cfg)
 
 
