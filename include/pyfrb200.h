@@ -202,6 +202,21 @@ int b200_tflux_ns_f32(int ndims, int nupts, int64_t neles, int linear, const b20
                       int64_t ldr, const float *verts, int64_t ldv, const float *upts,
                       int64_t ldup, void *stream);
 
+/* Largest reference-space wave speed of each element for the CFL
+ * controller: wspd[e] = max over the solution points of
+ * sum_i |sum_j (S_ij/|J|) v_j| + c*sqrt(sum_j (S_ij/|J|)^2);
+ * pyfr/solvers/euler/kernels/wavespeed.mako:9-44, provider call
+ * pyfr/solvers/euler/elements.py:38-66.  With gas->shifted the input is the
+ * reference-state perturbation q (see b200_gas_t). */
+int b200_wavespeed_f64(int ndims, int nupts, int64_t neles, int linear, const b200_gas_t *gas,
+                       const double *u, int64_t ldu, const double *smats, int64_t lds,
+                       const double *rcpdjac, int64_t ldr, const double *verts, int64_t ldv,
+                       const double *upts, int64_t ldup, double *wspd, void *stream);
+int b200_wavespeed_f32(int ndims, int nupts, int64_t neles, int linear, const b200_gas_t *gas,
+                       const float *u, int64_t ldu, const float *smats, int64_t lds,
+                       const float *rcpdjac, int64_t ldr, const float *verts, int64_t ldv,
+                       const float *upts, int64_t ldup, float *wspd, void *stream);
+
 /* Physical gradient; pyfr/solvers/baseadvecdiff/kernels/gradcoru.mako:10-24. */
 int b200_gradcoru_f64(int ndims, int nupts, int64_t neles, int linear, double *gradu,
                       int64_t ldg, const double *smats, int64_t lds, const double *rcpdjac,
@@ -337,6 +352,13 @@ int b200_errest_shifted_f64(int nupts, int nvars, int64_t neles, int64_t ld, con
 int b200_errest_f32(int nupts, int nvars, int64_t neles, int64_t ld, const float *curr,
                     const float *err, const double *atol_dev, double rtol, int uniform,
                     double *scratch, int nscratch, double *out, void *stream);
+
+/* out[0] (a device double) = max of the n values of x; key is 8 bytes of
+ * device scratch.  The 'max' reduction of pyfr/backends/base/blasext.py:21-46
+ * (pyfr/backends/cuda/kernels/reduction.mako) over one variable, as the
+ * CFL controller uses it (pyfr/solvers/baseadvec/system.py:48-52). */
+int b200_reduce_max_f64(int64_t n, const double *x, void *key, double *out, void *stream);
+int b200_reduce_max_f32(int64_t n, const float *x, void *key, double *out, void *stream);
 
 /* Allocation-free variant of b200_errest_f64; it has no counterpart in the
  * reference.  It is for callers that cannot give the library scratch memory:

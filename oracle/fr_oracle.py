@@ -25,6 +25,8 @@ arithmetic of the reference's OpenMP/CUDA kernels on this path:
   graph order (Euler, NS)    pyfr/solvers/baseadvec/system.py:58-136,
                              pyfr/solvers/baseadvecdiff/system.py:54-231
   linear element geometry    pyfr/shapes.py:306-566 (interp_expr, jac_exprs)
+  wave speed (CFL)           pyfr/solvers/euler/kernels/wavespeed.mako:9-44,
+                             pyfr/integrators/controllers.py:22-26
 
 Everything the oracle needs about the discretisation is passed in: the
 operator matrices (tests feed the ones generated by the reference's own
@@ -352,6 +354,24 @@ class Discretisation:
         r = self.apply(self.ops['M132'], ft.reshape(nd*nupts, -1, ne))
         r += self.apply(self.ops['M3'], uf)
         return -r/self.djac_u[:, None, :]
+
+
+def wavespeed(u, smats, djac, gamma):
+    """Largest reference-space wave speed of each element
+    (pyfr/solvers/euler/kernels/wavespeed.mako:9-44): max over the points
+    of sum_i |sum_j (S_ij/|J|) v_j| + c sqrt(sum_j (S_ij/|J|)^2);
+    u (npts, nvars, neles), smats S[p, i, j, e], djac (npts, neles)."""
+    nd = u.shape[1] - 2
+    rho, E = u[:, 0], u[:, -1]
+    v = u[:, 1:nd + 1]/rho[:, None]
+    p = (gamma - 1)*(E - 0.5*rho*np.sum(v*v, axis=1))
+    c = np.sqrt(gamma*p/rho)
+    sij = smats/djac[:, None, None, :]
+    vn = np.einsum('pije,pje->pie', sij, v)
+    lam = np.sum(np.abs(vn), axis=1) + c*np.sum(np.sqrt(np.sum(sij*sij,
+                                                                axis=2)),
+                                                 axis=1)
+    return lam.max(axis=0)
 
 
 # ---------------------------------------------------------------------------

@@ -23,6 +23,18 @@ class ErrestKernel(BindableKernel):
         return [float(self._host[0])]
 
 
+class ReductionKernel(Kernel):
+    """Device reduction to one value, read back by ``retval``."""
+
+    def __init__(self, fn, host, **kwargs):
+        super().__init__(fn, **kwargs)
+        self._host = host
+
+    @property
+    def retval(self):
+        return [float(self._host[0])]
+
+
 class BlasExtKernels:
     MAX_ERREST_BLOCKS = 4096
 
@@ -75,6 +87,32 @@ class BlasExtKernels:
             be.lib.memset(p, 0, nbytes, stream)
 
         return Kernel(run, mats=[m], name='zero')
+
+    def reduction(self, rop, exprs, vvars, svars=None, pvars=None):
+        """``reduction(rop, exprs, vvars)`` of
+        pyfr/backends/base/blasext.py:21-46 for the form the CFL controller
+        uses (pyfr/solvers/baseadvec/system.py:48-52): the maximum of one
+        variable, ``exprs == [name]`` with ``vvars == {name: matrix}``.
+        Other operators and expressions are not provided."""
+        if rop != 'max' or len(exprs) != 1 or exprs[0] not in vvars or \
+                len(vvars) != 1 or svars or pvars:
+            raise NotImplementedError('Only the maximum of one variable is '
+                                      'provided')
+        be, x = self.backend, vvars[exprs[0]]
+        n = x.nrow*x.leaddim if x.nrow > 1 else x.ncol
+        fn = be.lib.reduce_max_f64 if x.dtype == np.float64 else \
+            be.lib.reduce_max_f32
+        out = be.matrix((1, 2), dtype=np.float64)
+        be.commit()
+        host = np.zeros(1)
+        xp, kp = x.data, out.data
+        op = out.data + 8
+
+        def run(stream):
+            fn(n, xp, kp, op, stream)
+            be.lib.memcpy_dtoh(host.ctypes.data, op, 8, stream)
+
+        return ReductionKernel(run, host, mats=[x, out], name='reduction')
 
     def errest(self, curr, err, atols, norm='l2', uref=None, hcoef=0.0):
         """Error norm of the PI controller over one element type's

@@ -194,6 +194,27 @@ class PointwiseKernelProvider:
                                 u=u, f=f, gradu=gradu, smats=smats,
                                 rcpdjac=rcpdjac, verts=verts, upts=upts))
 
+    def _wavespeed(self, tplargs, dims, extrns, u, wspd, smats=None,
+                   rcpdjac=None, verts=None, upts=None):
+        """Per-element largest wave speed in reference space
+        (pyfr/solvers/euler/kernels/wavespeed.mako:9-44)."""
+        nupts, neles = dims
+        lin, (sp, sl), (rp, rl), (vp, vl), (upp, upl) = self._geom(
+            tplargs, smats, rcpdjac, verts, upts)
+        gas = _gas(tplargs['c'], 'none', self.backend.ref_state)
+        fn, nd = self._fn('wavespeed'), tplargs['ndims']
+        up, ul = _mat(u)
+        wp = wspd.data
+
+        def run(stream):
+            fn(nd, nupts, neles, lin, C.byref(gas), up, ul, sp, sl, rp, rl, vp,
+               vl, upp, upl, wp, stream)
+
+        return Kernel(run, mats=[u, wspd, smats, rcpdjac, verts, upts],
+                      misc=[gas], name='wavespeed',
+                      meta=dict(kind='wavespeed', tplargs=tplargs, dims=dims,
+                                u=u, wspd=wspd))
+
     def _gradcoru(self, tplargs, dims, extrns, gradu, smats=None,
                   rcpdjac=None, verts=None, upts=None):
         nupts, neles = dims
@@ -354,4 +375,6 @@ _BUILDERS = {
     'pyfr.solvers.navstokes.kernels.intconu': PointwiseKernelProvider._intconu,
     'pyfr.integrators.explicit.kernels.rkvdh2':
         PointwiseKernelProvider._rkvdh2,
+    'pyfr.solvers.euler.kernels.wavespeed':
+        PointwiseKernelProvider._wavespeed,
 }

@@ -252,6 +252,58 @@ errest_partial_kernel(int nupts, int nvars, int64_t neles, int64_t ld, const T *
     }
 }
 
+// Order-preserving map of doubles onto unsigned integers (negative values
+// reversed below the positive ones), so that an integer atomicMax is a max
+// over the doubles
+__device__ __forceinline__ unsigned long long max_key(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(BX_BLOCK)
+reduce_max_kernel(int64_t n, const T *__restrict__ x, unsigned long long *__restrict__ key) {
+    double m = -INFINITY;
+    for (int64_t i = (int64_t)blockIdx.x * BX_BLOCK + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * BX_BLOCK)
+        m = fmax(m, (double)x[i]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    __shared__ double wm[BX_BLOCK / 32];
+    if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < BX_BLOCK / 32; w++) m = fmax(m, wm[w]);
+        atomicMax(key, max_key(m));
+    }
+}
+
+__global__ void reduce_max_final_kernel(const unsigned long long *__restrict__ key,
+                                        double *__restrict__ out) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        const unsigned long long k = *key;
+        const unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+        out[0] = __longlong_as_double((long long)b);
+    }
+}
+
+template <typename T>
+int reduce_max(int64_t n, const T *x, void *key, double *out, cudaStream_t st) {
+    if (!key || !out || (n > 0 && !x))
+        return b200::set_error(B200_ERR_ARG, "reduce_max: null argument");
+    int rc = b200::check_cuda(cudaMemsetAsync(key, 0, 8, st), "reduce_max");
+    if (rc) return rc;
+    if (n > 0) {
+        const int64_t nb = b200::ceil_div(n, BX_BLOCK);
+        const unsigned grid = (unsigned)(nb < 4096 ? nb : 4096);
+        reduce_max_kernel<T><<<grid, BX_BLOCK, 0, st>>>(n, x, (unsigned long long *)key);
+        B200_CHECK_LAUNCH("reduce_max");
+    }
+    reduce_max_final_kernel<<<1, 32, 0, st>>>((const unsigned long long *)key, out);
+    B200_CHECK_LAUNCH("reduce_max_final");
+    return B200_OK;
+}
+
 __global__ void errest_final_kernel(int nblk, int uniform, const double *__restrict__ partial,
                                     double *__restrict__ out) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
@@ -494,6 +546,14 @@ int b200_errest_f32(int nupts, int nvars, int64_t neles, int64_t ld, const float
                     double *scratch, int nscratch, double *out, void *stream) {
     return errest<float>(nupts, nvars, neles, ld, curr, err, atol_dev, rtol, uniform, scratch,
                          nscratch, out, (cudaStream_t)stream);
+}
+
+int b200_reduce_max_f64(int64_t n, const double *x, void *key, double *out, void *stream) {
+    return reduce_max<double>(n, x, key, out, (cudaStream_t)stream);
+}
+
+int b200_reduce_max_f32(int64_t n, const float *x, void *key, double *out, void *stream) {
+    return reduce_max<float>(n, x, key, out, (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -90,6 +90,59 @@ tflux_euler_kernel(int nupts, int64_t neles, T gamma, const T *__restrict__ u, i
         }
 }
 
+// Largest characteristic wave speed of each element in reference space,
+// for the CFL controller (pyfr/solvers/euler/kernels/wavespeed.mako:9-44):
+// max over the solution points of sum_i |sum_j (S_ij/|J|) v_j| +
+// c sqrt(sum_j (S_ij/|J|)^2).  One thread per element walks the points.
+template <int ND, typename T>
+__global__ void __launch_bounds__(PW_BLOCK)
+wavespeed_kernel(int nupts, int64_t neles, b200::GasK<T> gas, const T *__restrict__ u,
+                 int64_t ldu, ElemGeom<T> geo, T *__restrict__ wspd) {
+    constexpr int NV = ND + 2;
+    const int64_t e = (int64_t)blockIdx.x * PW_BLOCK + threadIdx.x;
+    if (e >= neles) return;
+
+    T lmax = 0;
+    for (int upt = 0; upt < nupts; upt++) {
+        T s[ND][ND], rcp;
+        elem_metrics<ND, T>(geo, nupts, upt, e, s, rcp, true);
+
+        T uu[NV];
+#pragma unroll
+        for (int v = 0; v < NV; v++) uu[v] = u[upt * ldu + soa_off(e, v, NV)];
+        if (gas.shifted) {
+            // q = T(u - u_ref): rho = rho_ref + q0, E = E_ref + qE + h_s q0
+            uu[NV - 1] += gas.e_ref + gas.hs_ref * uu[0];
+            uu[0] += gas.rho_ref;
+        }
+
+        const T rho = uu[0], rcprho = T(1) / rho;
+        T vel[ND], k2 = 0;
+#pragma unroll
+        for (int d = 0; d < ND; d++) {
+            vel[d] = rcprho * uu[d + 1];
+            k2 += uu[d + 1] * vel[d];
+        }
+        const T p = gas.gm1 * (uu[NV - 1] - T(0.5) * k2);
+        const T csnd = sqrt(gas.gamma * p * rcprho);
+
+        T lam = 0;
+#pragma unroll
+        for (int i = 0; i < ND; i++) {
+            T vn = 0, nn = 0;
+#pragma unroll
+            for (int j = 0; j < ND; j++) {
+                const T sij = s[i][j] * rcp;
+                vn += sij * vel[j];
+                nn += sij * sij;
+            }
+            lam += fabs(vn) + csnd * sqrt(nn);
+        }
+        lmax = fmax(lmax, lam);
+    }
+    wspd[e] = lmax;
+}
+
 template <int ND, typename T>
 __global__ void __launch_bounds__(PW_BLOCK)
 tflux_ns_kernel(int nupts, int64_t neles, b200::GasK<T> gas, const T *__restrict__ u, int64_t ldu,
@@ -412,6 +465,28 @@ int tflux_euler(int ndims, int nupts, int64_t neles, int linear, double gamma, c
 }
 
 template <typename T>
+int wavespeed(int ndims, int nupts, int64_t neles, int linear, const b200_gas_t *gas, const T *u,
+              int64_t ldu, const T *smats, int64_t lds, const T *rcpdjac, int64_t ldr,
+              const T *verts, int64_t ldv, const T *upts, int64_t ldup, T *wspd,
+              cudaStream_t st) {
+    if (neles <= 0 || nupts <= 0) return B200_OK;
+    if (!gas || !wspd) return b200::set_error(B200_ERR_ARG, "wavespeed: null argument");
+    int rc = check_geom(linear, smats, rcpdjac, verts, upts, true);
+    if (rc) return rc;
+    auto geo = make_geom<T>(linear, smats, lds, rcpdjac, ldr, verts, ldv, upts, ldup);
+    const auto g = b200::gas_consts<T>(*reinterpret_cast<const Gas *>(gas));
+    const unsigned grid = (unsigned)b200::ceil_div(neles, PW_BLOCK);
+    if (ndims == 2)
+        wavespeed_kernel<2, T><<<grid, PW_BLOCK, 0, st>>>(nupts, neles, g, u, ldu, geo, wspd);
+    else if (ndims == 3)
+        wavespeed_kernel<3, T><<<grid, PW_BLOCK, 0, st>>>(nupts, neles, g, u, ldu, geo, wspd);
+    else
+        return b200::set_error(B200_ERR_ARG, "wavespeed: ndims must be 2 or 3");
+    B200_CHECK_LAUNCH("wavespeed");
+    return B200_OK;
+}
+
+template <typename T>
 int tflux_ns(int ndims, int nupts, int64_t neles, int linear, const b200_gas_t *gas,
              const T *u, int64_t ldu, T *f, int64_t ldf, T *gradu, int64_t ldg, const T *smats,
              int64_t lds, const T *rcpdjac, int64_t ldr, const T *verts, int64_t ldv,
@@ -650,6 +725,22 @@ int b200_intconu_both_f32(int nvars, int64_t n, double beta, const float *lin_ba
                           const void *rout_map, int ix64, void *stream) {
     return intconu<float>(nvars, n, beta, lin_base, lin_map, rin_base, rin_map, lout_base,
                           lout_map, rout_base, rout_map, ix64, 1, (cudaStream_t)stream);
+}
+
+int b200_wavespeed_f64(int ndims, int nupts, int64_t neles, int linear, const b200_gas_t *gas,
+                       const double *u, int64_t ldu, const double *smats, int64_t lds,
+                       const double *rcpdjac, int64_t ldr, const double *verts, int64_t ldv,
+                       const double *upts, int64_t ldup, double *wspd, void *stream) {
+    return wavespeed<double>(ndims, nupts, neles, linear, gas, u, ldu, smats, lds, rcpdjac, ldr,
+                             verts, ldv, upts, ldup, wspd, (cudaStream_t)stream);
+}
+
+int b200_wavespeed_f32(int ndims, int nupts, int64_t neles, int linear, const b200_gas_t *gas,
+                       const float *u, int64_t ldu, const float *smats, int64_t lds,
+                       const float *rcpdjac, int64_t ldr, const float *verts, int64_t ldv,
+                       const float *upts, int64_t ldup, float *wspd, void *stream) {
+    return wavespeed<float>(ndims, nupts, neles, linear, gas, u, ldu, smats, lds, rcpdjac, ldr,
+                            verts, ldv, upts, ldup, wspd, (cudaStream_t)stream);
 }
 
 }  // extern "C"

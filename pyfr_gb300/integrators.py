@@ -60,9 +60,10 @@ class RKVdH2Integrator:
         self.nstages = len(self.c)
 
         self.controller = cfg.get(sect, 'controller', 'none')
-        if self.controller not in ('none', 'pi'):
+        if self.controller not in ('none', 'pi', 'cfl'):
             raise ValueError(f'Unsupported controller {self.controller!r}')
         self.errest = self.controller == 'pi'
+        self.needs_cfl = self.controller == 'cfl'
         nregs = 4 if self.errest else 2
 
         self._nregs = nregs
@@ -73,7 +74,9 @@ class RKVdH2Integrator:
         backend.commit()
 
         self.tcurr = cfg.getfloat(sect, 'tstart', 0.0)
-        self.dt = cfg.getfloat(sect, 'dt')
+        # (the CFL controller computes its own first step size)
+        self.dt = cfg.getfloat(sect, 'dt', 0.0) if self.needs_cfl else \
+            cfg.getfloat(sect, 'dt')
         self.dtmin = cfg.getfloat(sect, 'dt-min', 1e-12)
         self.dtmax = cfg.getfloat(sect, 'dt-max', 1e2)
         self.idxcurr = 0
@@ -96,6 +99,12 @@ class RKVdH2Integrator:
         backend.lib.event_create(C.byref(self._dt_evt))
         weakref.finalize(self, backend.lib.event_destroy, self._dt_evt.value)
         self._dt_set = None
+
+        if self.needs_cfl:
+            # pyfr/integrators/controllers.py:7-38
+            self._cfl = cfg.getfloat(sect, 'cfl')
+            self._cfl_nsteps = cfg.getint(sect, 'cfl-nsteps', 1)
+            self._order = cfg.getint('solver', 'order')
 
         if self.errest:
             self._rtol = cfg.getfloat(sect, 'rtol')
@@ -122,7 +131,14 @@ class RKVdH2Integrator:
         return self.system.gndofs
 
     def _make_system(self, backend, systemcls, mesh, initsoln, cfg):
-        return systemcls(backend, mesh, initsoln, self._nregs, cfg)
+        return systemcls(backend, mesh, initsoln, self._nregs, cfg,
+                         needs_cfl=self.needs_cfl)
+
+    def compute_dt_cfl(self):
+        """Step size cfl/((2p + 1) max wave speed) of the current solution
+        (pyfr/integrators/controllers.py:22-26)."""
+        wmax = self.system.compute_max_wavespeed(self.idxcurr)
+        return self._cfl/(wmax*(2*self._order + 1))
 
     def _setup_registers(self, initsoln):
         pass
@@ -236,12 +252,15 @@ class RKVdH2Integrator:
             raise ValueError('Advance time is in the past')
 
         while self.tcurr < t - 1e-12*max(1.0, abs(t)):
+            if self.needs_cfl and self.nacptsteps % self._cfl_nsteps == 0:
+                self.dt = self.compute_dt_cfl()
             dt = min(self.dt, self.dtmax, t - self.tcurr)
-            if self.controller == 'none':
+            if self.controller in ('none', 'cfl'):
                 (idx,) = self.step(self.tcurr, dt)
                 self.idxcurr = idx
                 self.tcurr += dt
                 self.nacptsteps += 1
+                self.dt_accepted.append(dt)
                 continue
 
             self._pi_step(dt)
@@ -357,7 +376,8 @@ class MixedRKIntegrator(RKVdH2Integrator):
         super().__init__(backend, systemcls, mesh, cfg, initsoln)
 
     def _make_system(self, backend, systemcls, mesh, initsoln, cfg):
-        sysm = systemcls(backend, mesh, initsoln, 2, cfg)
+        sysm = systemcls(backend, mesh, initsoln, 2, cfg,
+                         needs_cfl=self.needs_cfl)
 
         if initsoln is not None:
             self._ics = [np.asarray(initsoln[et], dtype=np.float64)

@@ -311,6 +311,45 @@ class FluidElements:
         return [rho, *vs, p]
 
 
+class _WavespeedMixin:
+    def init_wavespeed(self):
+        """Per-element wave speed for the CFL controller
+        (pyfr/solvers/euler/elements.py:21-66)."""
+        be = self._be
+        be.pointwise.register('pyfr.solvers.euler.kernels.wavespeed')
+        self._wspd = be.matrix((1, self.neles), tags={'align'})
+        self.kernels['wavespeed'] = lambda uin: self._wavespeed_kernel(uin)
+        return self._wspd
+
+    def _wavespeed_kernel(self, uin):
+        be, r, s = self._be, self.mesh_regions, self._slice_mat
+        tplargs = dict(ndims=self.ndims, nvars=self.nvars,
+                       nverts=len(self.basis.linspts),
+                       c=self.cfg.items_as('constants', float))
+        kerns = []
+        for rgn in ('curved', 'linear'):
+            if rgn not in r:
+                continue
+            if rgn == 'curved':
+                kw = dict(smats=self.curved_smat_at('upts'),
+                          rcpdjac=self.rcpdjac_at('upts', 'curved'))
+            else:
+                kw = dict(verts=self.ploc_at('linspts', 'linear'),
+                          upts=self.upts)
+            # (each region writes its own elements' entries)
+            kerns.append(be.kernel(
+                'wavespeed', tplargs=tplargs | {'ktype': rgn},
+                dims=[self.nupts, r[rgn]], u=s(self.scal_upts[uin], rgn),
+                wspd=s(self._wspd, rgn), **kw))
+        return self._make_sliced_kernel(kerns)
+
+    def dt_cfl(self):
+        """Largest stable step of each element: 1/((2p + 1) wspd)."""
+        with np.errstate(divide='ignore'):
+            w = (2*self.basis.order + 1)*self._wspd.get()[0]
+            return np.nan_to_num(1/w, posinf=0.0)
+
+
 class _DivergenceMixin:
     def _divergence_kernels(self):
         """tdivtpcorf, tdivtconf and negdivconf
@@ -338,7 +377,8 @@ class _DivergenceMixin:
             rcpdjac=self.rcpdjac_at('upts'))
 
 
-class EulerElements(_DivergenceMixin, FluidElements, BaseElements):
+class EulerElements(_WavespeedMixin, _DivergenceMixin, FluidElements,
+                    BaseElements):
     _scratch_bufs = {'scal_fpts', 'vect_upts'}
 
     def set_backend(self, backend, nonce, linoff):
@@ -379,7 +419,8 @@ class EulerElements(_DivergenceMixin, FluidElements, BaseElements):
         self._divergence_kernels()
 
 
-class NavierStokesElements(_DivergenceMixin, FluidElements, BaseElements):
+class NavierStokesElements(_WavespeedMixin, _DivergenceMixin, FluidElements,
+                           BaseElements):
     _scratch_bufs = {'scal_fpts', 'vect_fpts', 'vect_upts', 'grad_upts'}
 
     def set_backend(self, backend, nonce, linoff):

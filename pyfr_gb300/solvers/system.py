@@ -25,8 +25,9 @@ class BaseSystem:
     intinterscls = None
     _nonce_seq = count()
 
-    def __init__(self, backend, mesh, initsoln, nregs, cfg):
+    def __init__(self, backend, mesh, initsoln, nregs, cfg, needs_cfl=False):
         self.backend = backend
+        self._needs_cfl = needs_cfl
         self.mesh = mesh
         self.cfg = cfg
         self.ndims = mesh.ndims
@@ -47,6 +48,8 @@ class BaseSystem:
             curved = mesh.spts_curved.get(et, np.zeros(e.neles, dtype=bool))
             linoff = np.max(*np.nonzero(curved), initial=-1) + 1
             e.set_backend(backend, nonce, linoff)
+            if needs_cfl:
+                e.init_wavespeed()
         backend.commit()
 
         self.ele_map = elemap
@@ -107,6 +110,12 @@ class BaseSystem:
 
         self.backend.commit()
         self._gen_kernels()
+        # Maximum wave speed over each element type
+        # (pyfr/solvers/baseadvec/system.py:48-52)
+        if self._needs_cfl:
+            self._wspd_red_kerns = [
+                self.backend.kernel('reduction', 'max', ['x'], {'x': e._wspd})
+                for e in self.ele_map.values()]
         self.backend.commit()
         self._graph_cache = {}
 
@@ -174,6 +183,14 @@ class BaseSystem:
             raise ValueError('Invalid register numbers')
         for g in self._rhs_graphs_cached(uinbank, foutbank):
             self.backend.run_graph(g)
+
+    def compute_max_wavespeed(self, uinbank):
+        """Largest element wave speed of the solution in bank uinbank
+        (pyfr/solvers/baseadvec/system.py:157-161)."""
+        k = self._get_kernels(uinbank, None)
+        self.backend.run_kernels(k['eles/wavespeed'] + self._wspd_red_kerns,
+                                 wait=True)
+        return max(k.retval[0] for k in self._wspd_red_kerns)
 
     def ele_scal_upts(self, idx):
         return [eb[idx].get() for eb in self.ele_banks]
