@@ -20,6 +20,7 @@ arithmetic of the reference's OpenMP/CUDA kernels on this path:
   viscous flux               pyfr/solvers/navstokes/kernels/flux.mako:48-105
   gradient transform         pyfr/solvers/baseadvecdiff/kernels/transform_grad.mako:3-10
   negdivconf                 pyfr/solvers/baseadvec/kernels/negdivconf.mako:7-22
+  flux anti-aliasing         pyfr/solvers/baseadvec/elements.py:79-90
   rkvdh2 / RK45              pyfr/integrators/explicit/kernels/rkvdh2.mako:4-31,
                              pyfr/integrators/explicit/steppers.py:165-243
   graph order (Euler, NS)    pyfr/solvers/baseadvec/system.py:58-136,
@@ -207,8 +208,12 @@ class Discretisation:
     period of the mesh (or None).
     """
 
-    def __init__(self, ops, basis, verts, lhs, rhs, periods=None):
+    def __init__(self, ops, basis, verts, lhs, rhs, periods=None, aa=None):
         self.ops = {k: np.asarray(v, dtype=float) for k, v in ops.items()}
+        # Flux anti-aliasing (pyfr/solvers/baseadvec/elements.py:79-90):
+        # aa = dict(M7=..., M1329=(M1 - M3 M2) M9, qpts=...)
+        self.aa = None if aa is None else \
+            {k: np.asarray(v, dtype=float) for k, v in aa.items()}
         self.upts = np.asarray(basis['upts'], dtype=float)
         self.fpts = np.asarray(basis['fpts'], dtype=float)
         self.norm_fpts = np.asarray(basis['norm_fpts'], dtype=float)
@@ -219,6 +224,8 @@ class Discretisation:
 
         # Metric terms at the solution and flux points
         self.smats_u, self.djac_u = smats_djac(self.verts, self.upts)
+        if self.aa is not None:
+            self.smats_q, _ = smats_djac(self.verts, self.aa['qpts'])
         s_f, _ = smats_djac(self.verts, self.fpts)
         # Scaled normals S^T n at the flux points: (nfpts, ndims, neles)
         self.pnorm = np.einsum('plke,pl->pke', s_f, self.norm_fpts)
@@ -293,7 +300,18 @@ class Discretisation:
         self._scatter(uf, 'l', mag*fn)
         self._scatter(uf, 'r', -mag*fn)
 
-        # Transformed flux at the solution points (tflux)
+        # Transformed flux at the solution points (tflux), or at the
+        # quadrature points and projected back
+        if self.aa is not None:
+            uq = self.apply(self.aa['M7'], u)
+            fq, _, _ = inviscid_flux(uq.transpose(1, 0, 2), gamma)
+            ft = np.einsum('pike,kpve->ipve', self.smats_q,
+                           fq.transpose(0, 2, 1, 3))
+            r = self.apply(self.aa['M1329'],
+                           ft.reshape(nd*len(self.aa['qpts']), -1, self.neles))
+            r += self.apply(self.ops['M3'], uf)
+            return -r/self.djac_u[:, None, :]
+
         fp, _, _ = inviscid_flux(u.transpose(1, 0, 2), gamma)   # (nd, nv, p, e)
         ft = self._transform_flux(fp.transpose(0, 2, 1, 3))
 

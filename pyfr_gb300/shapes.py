@@ -158,6 +158,62 @@ class BaseShape:
         m = self.norm_fpts.T[:, None, :]*self.m3[None, :, :]
         return tidy(m.reshape(-1, self.nfpts))
 
+    # Flux anti-aliasing (pyfr/shapes.py:126-138) ------------------------
+
+    def set_qrule(self, pts, wts):
+        """Quadrature rule of the element for flux anti-aliasing."""
+        self._qrule = (np.asarray(pts, dtype=float).reshape(-1, self.ndims),
+                       np.asarray(wts, dtype=float))
+        for k in ('m7', 'm8'):
+            self.__dict__.pop(k, None)
+
+    @property
+    def qrule(self):
+        if getattr(self, '_qrule', None) is None:
+            if not isinstance(self, TensorProdShape):
+                raise ValueError(f'{self.name}: anti-aliasing needs a '
+                                 'quadrature rule (quad-pts)')
+            # The reference's default: Gauss-Legendre, (p + 2)^ndims points
+            self._qrule = tensor_rule('gauss-legendre', self.order + 2,
+                                      self.ndims)
+        return self._qrule
+
+    @property
+    def qpts(self):
+        return self.qrule[0]
+
+    @property
+    def nqpts(self):
+        return len(self.qpts)
+
+    @cached_property
+    def m7(self):
+        """Interpolation from the solution points to the quadrature
+        points."""
+        return tidy(self.ubasis.nodal_basis_at(self.qpts))
+
+    @cached_property
+    def m8(self):
+        """L2 projection of values at the quadrature points onto the
+        solution space, at the solution points: with the element's exact
+        mass matrix M, c = M^-1 sum_q w_q l_i(x_q) f_q (the reference's
+        orthonormal-mode form, pyfr/shapes.py:17-19,131-133)."""
+        qp, qw = EXACT_RULES[self.name](2*self.order)
+        L = self.ubasis.nodal_basis_at(qp)
+        mass = L.T @ (qw[:, None]*L)
+        lq = self.ubasis.nodal_basis_at(self.qpts)          # (nq, nupts)
+        pts, wts = self.qrule
+        return tidy(np.linalg.solve(mass, lq.T*wts[None, :]))
+
+    @property
+    def m9(self):
+        m8 = self.m8
+        nu, nq = m8.shape
+        out = np.zeros((self.ndims*nu, self.ndims*nq))
+        for d in range(self.ndims):
+            out[d*nu:(d + 1)*nu, d*nq:(d + 1)*nq] = m8
+        return out
+
     def opmat(self, expr):
         """Evaluate an operator expression such as ``'M1 - M3*M2'``."""
         e = expr.lower().replace('*', '@')

@@ -66,8 +66,23 @@ class BaseElements:
         self.basis = get_shape(etype, order, upts, fpts)
         self.name = etype
 
-        if cfg.get('solver', 'anti-alias', 'none') != 'none':
-            raise NotImplementedError('Anti-aliasing is not supported')
+        # Flux anti-aliasing (pyfr/solvers/baseadvec/elements.py:69-90):
+        # the flux is evaluated at the points of a quadrature rule and
+        # projected back; 'surf-flux' is not provided
+        aa = {a.strip() for a in cfg.get('solver', 'anti-alias',
+                                         'none').split(',')} - {'none'}
+        if aa - {'flux'}:
+            raise NotImplementedError(f'Anti-aliasing {aa - {"flux"}} is not '
+                                      'supported')
+        self.antialias = 'flux' in aa and order > 0
+        if self.antialias:
+            rule = cfg.get(f'solver-elements-{etype}', 'quad-pts', None)
+            if rule is not None:
+                from pyfr_gb300.quadrules import parse_rule
+                pts, wts = parse_rule(rule, self.ndims)
+                if wts is None:
+                    raise ValueError('quad-pts needs quadrature weights')
+                self.basis.set_qrule(pts, wts)
 
         self.convars = self.convarnames(self.ndims)
         self.nvars = len(self.convars)
@@ -185,6 +200,7 @@ class BaseElements:
 
     def set_backend(self, backend, nonce, linoff):
         self._be = be = backend
+        self._nonce = nonce
         self.grad_fusion = not be.blocks
 
         csub = backend.csubsz
@@ -201,7 +217,10 @@ class BaseElements:
         sbufs = self._scratch_bufs
         if 'scal_fpts' in sbufs:
             self._scal_fpts = alloc('scal_fpts', (self.nfpts, nvars, neles))
-        if 'vect_upts' in sbufs:
+        # (with flux anti-aliasing the Euler flux lives at the quadrature
+        # points instead)
+        if 'vect_upts' in sbufs and not (self.antialias and
+                                         'grad_upts' not in sbufs):
             self._vect_upts = alloc('vect_upts', (ndims, self.nupts, nvars, neles))
         if 'vect_fpts' in sbufs:
             self._vect_fpts = alloc('vect_fpts', (ndims, self.nfpts, nvars, neles))
@@ -254,6 +273,10 @@ class BaseElements:
     @cached_property
     def upts(self):
         return self._be.const_matrix(self.basis.upts)
+
+    @cached_property
+    def qpts(self):
+        return self._be.const_matrix(self.basis.qpts)
 
     # ---- interface helpers (pyfr/solvers/base/elements.py:446-469) --------
 
@@ -357,16 +380,20 @@ class _DivergenceMixin:
         operators, all three as one kernel:
         R = -(1/|J|)((M1 - M3.M2) F + M3 Fc)."""
         be, kernels = self._be, self.kernels
+        # (with flux anti-aliasing the flux lives at the quadrature points
+        # and is projected back by M9)
+        m132, vect = ('(M1 - M3*M2)*M9', self._vect_qpts) if \
+            getattr(self, 'antialias', False) else \
+            ('M1 - M3*M2', self._vect_upts)
         if be.fuse_operators:
             kernels['tdivtconf_cat'] = lambda fout: be.kernel(
-                'mul_cat', self.opmat('M1 - M3*M2'), self._vect_upts,
+                'mul_cat', self.opmat(m132), vect,
                 self.opmat('M3'), self._scal_fpts, out=self.scal_upts[fout],
                 alpha=-1.0, rowscale=self.rcpdjac_at('upts'))
             return
 
         kernels['tdivtpcorf'] = lambda fout: be.kernel(
-            'mul', self.opmat('M1 - M3*M2'), self._vect_upts,
-            out=self.scal_upts[fout])
+            'mul', self.opmat(m132), vect, out=self.scal_upts[fout])
         kernels['tdivtconf'] = lambda fout: be.kernel(
             'mul', self.opmat('M3'), self._scal_fpts,
             out=self.scal_upts[fout], beta=1.0)
@@ -392,26 +419,46 @@ class EulerElements(_WavespeedMixin, _DivergenceMixin, FluidElements,
         kernels['disu'] = lambda uin: be.kernel(
             'mul', self.opmat('M0'), self.scal_upts[uin], out=self._scal_fpts)
 
-        # Transformed flux
+        # Transformed flux, at the solution points or, with flux
+        # anti-aliasing, at the quadrature points
         tplargs = dict(ndims=self.ndims, nvars=self.nvars,
                        nverts=len(self.basis.linspts),
                        c=self.cfg.items_as('constants', float))
         r, s = self.mesh_regions, self._slice_mat
+        if self.antialias:
+            nd, nq = self.ndims, self.basis.nqpts
+            ex = be.matrix((nq, self.nvars, self.neles), tags={'align'},
+                           extent=self._nonce + 'scal_qpts')
+            self._scal_qpts = ex
+            self._vect_qpts = be.matrix((nd, nq, self.nvars, self.neles),
+                                        tags={'align'},
+                                        extent=self._nonce + 'vect_qpts')
+            kernels['qptsu'] = lambda uin: be.kernel(
+                'mul', self.opmat('M7'), self.scal_upts[uin],
+                out=self._scal_qpts)
+            npts, where = nq, 'qpts'
+
+            def uin_mat(uin):
+                return self._scal_qpts
+            fmat = self._vect_qpts
+        else:
+            npts, where = self.nupts, 'upts'
+
+            def uin_mat(uin):
+                return self.scal_upts[uin]
+            fmat = self._vect_upts
         tdisf = []
         if 'curved' in r:
             tdisf.append(lambda uin: be.kernel(
                 'tflux', tplargs=tplargs | {'ktype': 'curved'},
-                dims=[self.nupts, r['curved']],
-                u=s(self.scal_upts[uin], 'curved'),
-                f=s(self._vect_upts, 'curved'),
-                smats=self.curved_smat_at('upts')))
+                dims=[npts, r['curved']], u=s(uin_mat(uin), 'curved'),
+                f=s(fmat, 'curved'), smats=self.curved_smat_at(where)))
         if 'linear' in r:
             tdisf.append(lambda uin: be.kernel(
                 'tflux', tplargs=tplargs | {'ktype': 'linear'},
-                dims=[self.nupts, r['linear']],
-                u=s(self.scal_upts[uin], 'linear'),
-                f=s(self._vect_upts, 'linear'),
-                verts=self.ploc_at('linspts', 'linear'), upts=self.upts))
+                dims=[npts, r['linear']], u=s(uin_mat(uin), 'linear'),
+                f=s(fmat, 'linear'), verts=self.ploc_at('linspts', 'linear'),
+                upts=getattr(self, where)))
         kernels['tdisf'] = lambda uin: self._make_sliced_kernel(
             k(uin) for k in tdisf)
 
@@ -424,6 +471,9 @@ class NavierStokesElements(_WavespeedMixin, _DivergenceMixin, FluidElements,
     _scratch_bufs = {'scal_fpts', 'vect_fpts', 'vect_upts', 'grad_upts'}
 
     def set_backend(self, backend, nonce, linoff):
+        if self.antialias:
+            raise NotImplementedError('Flux anti-aliasing is provided for '
+                                      'the Euler equations only')
         super().set_backend(backend, nonce, linoff)
         be, kernels = self._be, self.kernels
 

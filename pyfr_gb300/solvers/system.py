@@ -217,8 +217,10 @@ class EulerSystem(BaseSystem):
         g_intf.commit()
 
         g_flux_div = self.backend.graph()
+        # (flux anti-aliasing: the solution at the quadrature points first)
+        g_flux_div.add_all(k['eles/qptsu'])
         for l in k['eles/tdisf']:
-            g_flux_div.add(l)
+            g_flux_div.add(l, deps=deps(l, 'eles/qptsu'))
         if k['eles/tdivtconf_cat']:
             # Fused divergence, correction and negdivconf
             for l in k['eles/tdivtconf_cat']:

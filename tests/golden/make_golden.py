@@ -143,6 +143,18 @@ def make_operators():
         out[f'{key}/norm_fpts'] = s.norm_fpts
         out[f'{key}/nfacefpts'] = np.array(s.nfacefpts)
 
+    # Flux anti-aliasing operators (default quadrature: Gauss-Legendre,
+    # (p + 2)^ndims points)
+    for etype in ('quad', 'hex'):
+        cfg = _cfg(etype, 3, 'gauss-legendre', 'gauss-legendre',
+                   extra=[('solver', 'anti-alias', 'flux')])
+        s = shapes[etype](None, cfg)
+        key = f'{etype}_p3_aa'
+        out[f'{key}/m7'] = s.m7
+        out[f'{key}/m9'] = s.m9
+        out[f'{key}/M1329'] = s.opmat('(M1 - M3*M2)*M9')
+        out[f'{key}/qpts'] = s.qpts
+
     # The reference's own golden values for hex p=3 (test_ele_mats.py)
     ref = np.load(BytesIO((REF / 'pyfr/tests/hex-gleg-ord3.npz').read_bytes()))
     for m in ('m0', 'm1', 'm2', 'm3'):

@@ -97,3 +97,17 @@ def test_simplex_operators_match_reference(golden, etype, order, upts, fpts):
         mine = s.opmat(exprs[m]) if m in exprs else getattr(s, m)
         np.testing.assert_allclose(mine[np.ix_(r, c)], ref[f'{key}/{m}'],
                                    rtol=0, atol=1e-11, err_msg=m)
+
+
+@pytest.mark.parametrize('etype', ['quad', 'hex'])
+def test_antialias_operators_match_reference(golden, etype):
+    """Flux anti-aliasing: interpolation to the quadrature points (M7) and
+    the L2 projection back (M9), default Gauss-Legendre (p+2)^d rule."""
+    ref = golden['operators']
+    key = f'{etype}_p3_aa'
+    s = get_shape(etype, 3)
+    np.testing.assert_allclose(s.qpts, ref[f'{key}/qpts'], atol=1e-14)
+    np.testing.assert_allclose(s.m7, ref[f'{key}/m7'], rtol=0, atol=1e-11)
+    np.testing.assert_allclose(s.m9, ref[f'{key}/m9'], rtol=0, atol=1e-11)
+    np.testing.assert_allclose(s.opmat('(M1 - M3*M2)*M9'),
+                               ref[f'{key}/M1329'], rtol=0, atol=1e-11)
