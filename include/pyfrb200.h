@@ -46,6 +46,24 @@ typedef struct {
     double rho_ref, p_ref;
 } b200_gas_t;
 
+/* Boundary conditions: the types of pyfr/solvers/euler/inters.py:83-112
+ * and pyfr/solvers/navstokes/inters.py:101-150 with uniform constants
+ * (free-stream or inflow state rho, p, u; wall velocity u and cpTw for the
+ * isothermal wall). */
+enum {
+    B200_BC_SUP_IN_FA = 1,        /* supersonic inflow: the given state */
+    B200_BC_SUP_OUT_FN = 2,       /* supersonic outflow: the interior state */
+    B200_BC_SLP_ADIA_WALL = 3,    /* slip adiabatic wall */
+    B200_BC_CHAR_RIEM_INV = 4,    /* characteristic Riemann invariants */
+    B200_BC_NO_SLP_ADIA_WALL = 5, /* no-slip adiabatic wall (NS) */
+    B200_BC_NO_SLP_ISOT_WALL = 6  /* no-slip isothermal wall (NS) */
+};
+typedef struct {
+    int type;
+    double rho, p, u[3];
+    double cpTw;
+} b200_bc_t;
+
 /* Riemann solver ids: [solver-interfaces] riemann-solver */
 #define B200_RSOLVER_RUSANOV 0
 #define B200_RSOLVER_HLLC 1
@@ -201,6 +219,39 @@ int b200_tflux_ns_f32(int ndims, int nupts, int64_t neles, int linear, const b20
                       int64_t ldg, const float *smats, int64_t lds, const float *rcpdjac,
                       int64_t ldr, const float *verts, int64_t ldv, const float *upts,
                       int64_t ldup, void *stream);
+
+/* Common normal flux at boundary flux points, written over the interior
+ * state in the flux-point field (view ul, n points; nl: scaled normals,
+ * ndims x n with leading dimension ldn); Euler types 1-4;
+ * pyfr/solvers/euler/kernels/bccflux.mako:7-26. */
+int b200_bccflux_euler_f64(int ndims, int64_t n, int rsolver, double gamma, const b200_bc_t *bc,
+                           double *ul_base, const void *ul_map, int ix64, const double *nl,
+                           int64_t ldn, void *stream);
+int b200_bccflux_euler_f32(int ndims, int64_t n, int rsolver, double gamma, const b200_bc_t *bc,
+                           float *ul_base, const void *ul_map, int ix64, const float *nl,
+                           int64_t ldn, void *stream);
+/* LDG common solution at boundary flux points (view ulin -> view ulout);
+ * pyfr/solvers/navstokes/kernels/bcconu.mako:6-14. */
+int b200_bcconu_f64(int ndims, int64_t n, double gamma, const b200_bc_t *bc,
+                    const double *ulin_base, const void *ulin_map, double *ulout_base,
+                    const void *ulout_map, int ix64, const double *nl, int64_t ldn,
+                    void *stream);
+int b200_bcconu_f32(int ndims, int64_t n, double gamma, const b200_bc_t *bc,
+                    const float *ulin_base, const void *ulin_map, float *ulout_base,
+                    const void *ulout_map, int ix64, const float *nl, int64_t ldn,
+                    void *stream);
+/* Navier-Stokes common flux (inviscid + LDG viscous) at boundary flux
+ * points from the interior state and gradient (vector view gl); the gas
+ * must not be shifted; pyfr/solvers/navstokes/kernels/bccflux.mako:10-20
+ * with the ghost, ghost-imperm and slip-wall flux states. */
+int b200_bccflux_ns_f64(int ndims, int64_t n, int rsolver, const b200_gas_t *gas, double tau,
+                        const b200_bc_t *bc, double *ul_base, const void *ul_map,
+                        const double *gl_base, const void *gl_map, const void *gl_rstr,
+                        int ix64, const double *nl, int64_t ldn, void *stream);
+int b200_bccflux_ns_f32(int ndims, int64_t n, int rsolver, const b200_gas_t *gas, double tau,
+                        const b200_bc_t *bc, float *ul_base, const void *ul_map,
+                        const float *gl_base, const void *gl_map, const void *gl_rstr,
+                        int ix64, const float *nl, int64_t ldn, void *stream);
 
 /* Largest reference-space wave speed of each element for the CFL
  * controller: wspd[e] = max over the solution points of

@@ -152,6 +152,126 @@ RSOLVERS = {'rusanov': rusanov, 'hllc': hllc}
 
 
 # ---------------------------------------------------------------------------
+# Boundary conditions
+# ---------------------------------------------------------------------------
+
+def bc_rsolve_state(bc, ul, n, gamma):
+    """Ghost state of the boundary Riemann solve; ul (nvars, npts), n unit
+    normals (ndims, npts).  pyfr/solvers/euler/kernels/bcs/*.mako and
+    pyfr/solvers/navstokes/kernels/bcs/no-slp-*.mako (bc_rsolve_state)."""
+    nd = ul.shape[0] - 2
+    t = bc['type']
+    ur = np.empty_like(ul)
+    gm1 = gamma - 1
+    uvw = np.array(bc.get('u', [0.0]*3)[:nd])[:, None]
+    if t == 'sup-in-fa':
+        ur[0] = bc['rho']
+        ur[1:nd + 1] = bc['rho']*uvw
+        ur[-1] = bc['p']/gm1 + 0.5*np.sum(ur[1:nd + 1]**2, axis=0)/ur[0]
+    elif t == 'sup-out-fn':
+        ur[:] = ul
+    elif t == 'slp-adia-wall':
+        nor = np.sum(ul[1:nd + 1]*n, axis=0)
+        ur[0], ur[-1] = ul[0], ul[-1]
+        ur[1:nd + 1] = ul[1:nd + 1] - 2*nor*n
+    elif t == 'char-riem-inv':
+        rho_e, p_e = bc['rho'], bc['p']
+        cs = np.sqrt(gamma*p_e/rho_e)
+        se = p_e*rho_e**-gamma
+        ratio = 2*cs/gm1
+        inv = 1/ul[0]
+        ve = np.sum(uvw*n, axis=0)
+        vi = inv*np.sum(ul[1:nd + 1]*n, axis=0)
+        pi = gm1*ul[-1] - 0.5*gm1*inv*np.sum(ul[1:nd + 1]**2, axis=0)
+        ci = np.sqrt(gamma*pi*inv)
+        sup = np.abs(ve) >= cs
+        re = np.where(sup & (vi >= 0), vi - 2*ci/gm1, ve - ratio)
+        ri = np.where(sup & (vi < 0), ve + ratio, vi + 2*ci/gm1)
+        vb, cb = 0.5*(re + ri), 0.25*gm1*(ri - re)
+        rhob = np.where(vi < 0, (cb*cb/(gamma*se))**(1/gm1),
+                        ul[0]*(ul[0]*cb*cb/(gamma*pi))**(1/gm1))
+        pb = rhob*cb*cb/gamma
+        ur[0] = rhob
+        ur[1:nd + 1] = np.where(vi >= 0,
+                                rhob*(ul[1:nd + 1]*inv + (vb - vi)*n),
+                                rhob*(uvw + (vb - ve)*n))
+        ur[-1] = pb/gm1 + 0.5*np.sum(ur[1:nd + 1]**2, axis=0)/ur[0]
+    elif t == 'no-slp-adia-wall':
+        ur[0], ur[-1] = ul[0], ul[-1]
+        ur[1:nd + 1] = -ul[1:nd + 1]
+    elif t == 'no-slp-isot-wall':
+        ur[0] = ul[0]
+        ur[1:nd + 1] = -ul[1:nd + 1] + 2*uvw*ul[0]
+        ur[-1] = bc['cpTw']/gamma*ur[0] + \
+            0.5*np.sum(ur[1:nd + 1]**2, axis=0)/ur[0]
+    else:
+        raise ValueError(t)
+    return ur
+
+
+def bc_ldg_state(bc, ul, n, gamma):
+    """Boundary state of the LDG common solution (bc_ldg_state of
+    pyfr/solvers/navstokes/kernels/bcs/*.mako)."""
+    nd = ul.shape[0] - 2
+    t = bc['type']
+    if t == 'no-slp-adia-wall':
+        ur = np.empty_like(ul)
+        ur[0] = ul[0]
+        ur[1:nd + 1] = 0
+        ur[-1] = ul[-1] - 0.5/ul[0]*np.sum(ul[1:nd + 1]**2, axis=0)
+        return ur
+    if t == 'no-slp-isot-wall':
+        uvw = np.array(bc.get('u', [0.0]*3)[:nd])[:, None]
+        ur = np.empty_like(ul)
+        ur[0] = ul[0]
+        ur[1:nd + 1] = uvw*ul[0]
+        ur[-1] = bc['cpTw']/gamma*ur[0] + \
+            0.5*np.sum(ur[1:nd + 1]**2, axis=0)/ur[0]
+        return ur
+    return bc_rsolve_state(bc, ul, n, gamma)
+
+
+def bc_ldg_grad_state(bc, us, n, gl):
+    """Boundary gradient (bc_ldg_grad_state); gl (ndims, nvars, npts)."""
+    t = bc['type']
+    if t in ('sup-in-fa', 'char-riem-inv'):
+        return np.zeros_like(gl)
+    gr = gl.copy()
+    if t == 'no-slp-adia-wall':
+        nd = gl.shape[0]
+        rcprho = 1/us[0]
+        vel = rcprho*us[1:nd + 1]
+        tl = np.empty((nd,) + us.shape[1:])
+        for d in range(nd):
+            kd = sum(vel[i]*(gl[d, i + 1] - vel[i]*gl[d, 0])
+                     for i in range(nd))
+            tl[d] = gl[d, -1] - (rcprho*gl[d, 0]*us[-1] + kd)
+        for d in range(nd):
+            gr[d, -1] -= sum(n[d]*n[e]*tl[e] for e in range(nd))
+    return gr
+
+
+def bc_flux_ns(bc, ul, gl, n, c, rsolver):
+    """Common normal flux at a boundary (per unit normal): ghost,
+    ghost-imperm or slip-wall flux state of
+    pyfr/solvers/navstokes/kernels/bcs/{ghost,ghost-imperm,slp-adia-wall}
+    .mako."""
+    gamma, tau = c['gamma'], c['ldg-tau']
+    t = bc['type']
+    ur = bc_rsolve_state(bc, ul, n, gamma)
+    fi = RSOLVERS[rsolver](ul, ur, n, gamma)
+    if t == 'slp-adia-wall':
+        return fi
+    imperm = t in ('no-slp-adia-wall', 'no-slp-isot-wall')
+    ul_dg = bc_ldg_state(bc, ul, n, gamma)
+    gr = bc_ldg_grad_state(bc, ul_dg if imperm else ul, n, gl)
+    fv = np.einsum('dn,dvn->vn', n, viscous_flux(ul_dg, gr, c))
+    if not imperm:
+        fv = fv + tau*(ul - ur)
+    return fi + fv
+
+
+# ---------------------------------------------------------------------------
 # Geometry of linear elements
 # ---------------------------------------------------------------------------
 
@@ -208,7 +328,8 @@ class Discretisation:
     period of the mesh (or None).
     """
 
-    def __init__(self, ops, basis, verts, lhs, rhs, periods=None, aa=None):
+    def __init__(self, ops, basis, verts, lhs, rhs, periods=None, aa=None,
+                 bcs=()):
         self.ops = {k: np.asarray(v, dtype=float) for k, v in ops.items()}
         # Flux anti-aliasing (pyfr/solvers/baseadvec/elements.py:79-90):
         # aa = dict(M7=..., M1329=(M1 - M3 M2) M9, qpts=...)
@@ -234,6 +355,18 @@ class Discretisation:
 
         self._pair(np.asarray(lhs), np.asarray(rhs), periods)
 
+        # Boundaries: bcs is a sequence of (faces (n, 2) of (element, face),
+        # boundary spec dict)
+        self.bcs = []
+        for faces, spec in bcs:
+            faces = np.asarray(faces)
+            fp = np.concatenate([self.facefpts[f] for _, f in faces])
+            ee = np.concatenate([np.full(len(self.facefpts[f]), e)
+                                 for e, f in faces])
+            nl = self.pnorm[fp, :, ee].T                       # (nd, n)
+            mag = np.sqrt(np.sum(nl**2, axis=0))
+            self.bcs.append((fp, ee, nl/mag, mag, spec))
+
     def _pair(self, lhs, rhs, periods):
         """Pair the flux points of the two sides of every interface by
         matching physical coordinates (modulo periods)."""
@@ -253,8 +386,9 @@ class Discretisation:
             xr = self.ploc_f[pr][:, :, er]
             d = xl[:, None] - xr[None, :]                     # (nfp, nfp, nd, n)
             if periods is not None:
-                P = np.asarray(periods)[:, None]
-                d = d - P*np.rint(d/P)
+                for k, P in enumerate(periods):
+                    if P is not None:
+                        d[:, :, k] -= P*np.rint(d[:, :, k]/P)
             match = np.argmin(np.sum(d*d, axis=2), axis=1)    # (nfp, n)
             if np.any(np.sort(match, axis=0) != np.arange(nfp)[:, None]):
                 raise RuntimeError('Flux points of an interface do not pair')
@@ -300,6 +434,12 @@ class Discretisation:
         self._scatter(uf, 'l', mag*fn)
         self._scatter(uf, 'r', -mag*fn)
 
+        # Boundary common fluxes (bccflux)
+        for fp, ee, n, bmag, spec in self.bcs:
+            ub = uf[fp, :, ee].T
+            ug = bc_rsolve_state(spec, ub, n, gamma)
+            uf[fp, :, ee] = (bmag*RSOLVERS[rsolver](ub, ug, n, gamma)).T
+
         # Transformed flux at the solution points (tflux), or at the
         # quadrature points and projected back
         if self.aa is not None:
@@ -335,6 +475,8 @@ class Discretisation:
         comm = uf.copy()
         self._scatter(comm, 'l', cl)
         self._scatter(comm, 'r', cr)
+        for fp, ee, n, bmag, spec in self.bcs:
+            comm[fp, :, ee] = bc_ldg_state(spec, uf[fp, :, ee].T, n, gamma).T
 
         # Corrected reference gradient, transformed to physical space
         g = self.apply(self.ops['M460'], u) + self.apply(self.ops['M6'], comm)
@@ -366,8 +508,16 @@ class Discretisation:
         else:
             fvc = (0.5 + beta)*fvl + (0.5 - beta)*fvr
         fvc = fvc + tau*(ul - ur)
+        # (boundary states first: the interior scatter overwrites uf)
+        bflux = []
+        for fp, ee, n, bmag, spec in self.bcs:
+            ub = uf[fp, :, ee].T
+            gb = gf[:, fp, :, ee].transpose(1, 2, 0)
+            bflux.append(bmag*bc_flux_ns(spec, ub, gb, n, c, rsolver))
         self._scatter(uf, 'l', mag*(fic + fvc))
         self._scatter(uf, 'r', -mag*(fic + fvc))
+        for (fp, ee, *_), f in zip(self.bcs, bflux):
+            uf[fp, :, ee] = f.T
 
         r = self.apply(self.ops['M132'], ft.reshape(nd*nupts, -1, ne))
         r += self.apply(self.ops['M3'], uf)

@@ -40,6 +40,16 @@ class Gas(C.Structure):
                 ('rho_ref', f64), ('p_ref', f64)]
 
 
+# Boundary-condition types and constants (b200_bc_t)
+BC_TYPES = {'sup-in-fa': 1, 'sup-out-fn': 2, 'slp-adia-wall': 3,
+            'char-riem-inv': 4, 'no-slp-adia-wall': 5, 'no-slp-isot-wall': 6}
+
+
+class BC(C.Structure):
+    _fields_ = [('type', i32), ('rho', f64), ('p', f64), ('u', f64*3),
+                ('cpTw', f64)]
+
+
 def _sig_pointwise(fp):
     return {
         'tflux_euler': [i32, i32, i64, i32, f64, vp, i64, vp, i64, vp, i64, vp,
@@ -64,6 +74,12 @@ def _sig_pointwise(fp):
         'mul': [vp, vp, i64, vp, i64, i64, fp, fp, vp],
         'wavespeed': [i32, i32, i64, i32, C.POINTER(Gas), vp, i64, vp, i64,
                       vp, i64, vp, i64, vp, i64, vp, vp],
+        'bccflux_euler': [i32, i64, i32, f64, C.POINTER(BC), vp, vp, i32, vp,
+                          i64, vp],
+        'bcconu': [i32, i64, f64, C.POINTER(BC), vp, vp, vp, vp, i32, vp, i64,
+                   vp],
+        'bccflux_ns': [i32, i64, i32, C.POINTER(Gas), f64, C.POINTER(BC), vp,
+                       vp, vp, vp, vp, i32, vp, i64, vp],
         'reduce_max': [i64, vp, vp, vp, vp],
     }
 

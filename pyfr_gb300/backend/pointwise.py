@@ -306,6 +306,74 @@ class PointwiseKernelProvider:
                       meta=dict(kind='intcflux_ns', tplargs=tplargs,
                                 dims=dims))
 
+    # ---- boundary kernels -------------------------------------------------
+
+    def _bc(self, tplargs):
+        from pyfr_gb300.backend.lib import BC, BC_TYPES
+        bc = tplargs.get('bc')
+        if bc is None:
+            bc = BC(type=BC_TYPES[tplargs['bctype']])
+        return bc
+
+    def _bccflux_euler(self, tplargs, dims, extrns, ul, nl, **kw):
+        (n,) = dims
+        rs = RSOLVERS[tplargs['rsolver']]
+        fn, nd, gamma = (self._fn('bccflux_euler'), tplargs['ndims'],
+                         tplargs['c']['gamma'])
+        bc = self._bc(tplargs)
+        lb, lm, _ = _view(ul)
+        np_, nlp = _mat(nl)
+        ix64 = self._ix64
+
+        def run(stream):
+            fn(nd, n, rs, gamma, C.byref(bc), lb, lm, ix64, np_, nlp, stream)
+
+        return Kernel(run, mats=[nl], views=[ul], misc=[bc], name='bccflux',
+                      meta=dict(kind='bccflux_euler', tplargs=tplargs,
+                                dims=dims))
+
+    def _bcconu(self, tplargs, dims, extrns, ulin, ulout, nlin, **kw):
+        (n,) = dims
+        fn, nd, gamma = (self._fn('bcconu'), tplargs['ndims'],
+                         tplargs['c']['gamma'])
+        bc = self._bc(tplargs)
+        ib, im, _ = _view(ulin)
+        ob, om, _ = _view(ulout)
+        np_, nlp = _mat(nlin)
+        ix64 = self._ix64
+
+        def run(stream):
+            fn(nd, n, gamma, C.byref(bc), ib, im, ob, om, ix64, np_, nlp,
+               stream)
+
+        return Kernel(run, mats=[nlin], views=[ulin, ulout], misc=[bc],
+                      name='bcconu', meta=dict(kind='bcconu', dims=dims))
+
+    def _bccflux_ns(self, tplargs, dims, extrns, ul, gradul, nl,
+                    artvisc=None, **kw):
+        if artvisc is not None:
+            raise NotImplementedError('Artificial viscosity is not supported')
+        if self.backend.ref_state is not None:
+            raise NotImplementedError('Boundaries take unshifted states')
+        (n,) = dims
+        c = tplargs['c']
+        rs = RSOLVERS[tplargs['rsolver']]
+        gas = _gas(c, tplargs.get('visc_corr', 'none'))
+        fn, nd = self._fn('bccflux_ns'), tplargs['ndims']
+        bc = self._bc(tplargs)
+        lb, lm, _ = _view(ul)
+        gb, gm, gr = _view(gradul)
+        np_, nlp = _mat(nl)
+        ix64 = self._ix64
+        tau = c['ldg-tau']
+
+        def run(stream):
+            fn(nd, n, rs, C.byref(gas), tau, C.byref(bc), lb, lm, gb, gm, gr,
+               ix64, np_, nlp, stream)
+
+        return Kernel(run, mats=[nl], views=[ul, gradul], misc=[gas, bc],
+                      name='bccflux', meta=dict(kind='bccflux_ns', dims=dims))
+
     def _intconu(self, tplargs, dims, extrns, ulin, urin, ulout, urout):
         (n,) = dims
         beta = tplargs['c']['ldg-beta']
@@ -377,4 +445,9 @@ _BUILDERS = {
         PointwiseKernelProvider._rkvdh2,
     'pyfr.solvers.euler.kernels.wavespeed':
         PointwiseKernelProvider._wavespeed,
+    'pyfr.solvers.euler.kernels.bccflux':
+        PointwiseKernelProvider._bccflux_euler,
+    'pyfr.solvers.navstokes.kernels.bcconu': PointwiseKernelProvider._bcconu,
+    'pyfr.solvers.navstokes.kernels.bccflux':
+        PointwiseKernelProvider._bccflux_ns,
 }

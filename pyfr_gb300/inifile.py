@@ -28,6 +28,9 @@ class Inifile:
             self._cp.add_section(section)
         self._cp.set(section, option, str(value))
 
+    def hassect(self, section):
+        return self._cp.has_section(section)
+
     def hasopt(self, section, option):
         return self._cp.has_option(section, option)
 

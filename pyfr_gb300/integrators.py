@@ -386,12 +386,14 @@ class MixedRKIntegrator(RKVdH2Integrator):
             self._ics = [e.set_ics_from_cfg() for e in sysm.ele_map.values()]
 
         # Reference-state shift of the FP32 right-hand side (Navier-Stokes
-        # with the Rusanov solver): the volume means of rho and p of the
-        # initial condition.  Must be set before the kernels are built.
+        # with the Rusanov solver, no boundaries): the volume means of rho
+        # and p of the initial condition.  Must be set before the kernels
+        # are built.
         self.uref, self.hs_ref = None, 0.0
         shift = cfg.get('backend-b200', 'reference-shift', 'auto')
         rs = cfg.get('solver-interfaces', 'riemann-solver')
-        if shift == 'auto' and sysm.name == 'navier-stokes' and rs == 'rusanov':
+        if shift == 'auto' and sysm.name == 'navier-stokes' and \
+                rs == 'rusanov' and not sysm._bc_inters:
             gamma = cfg.getfloat('constants', 'gamma')
             rho = np.concatenate([u[:, 0].ravel() for u in self._ics])
             pri = [e.con_to_pri(list(u.swapaxes(0, 1)), cfg)[-1]

@@ -47,6 +47,9 @@ class Mesh:
     con: tuple
     spts_curved: dict = field(default_factory=dict)
     periods: tuple = None
+    # Boundary faces by boundary name: Side of (etype, element, face)
+    # (the reference's bcon_<name> arrays, pyfr/readers/native.py:15-86)
+    bcon: dict = field(default_factory=dict)
 
     @property
     def etypes(self):
@@ -106,6 +109,72 @@ def periodic_box(etype, ncells, lo, hi):
     return Mesh(ndims=ndims, spts={etype: spts}, con=(lhs, rhs),
                 spts_curved={etype: np.zeros(neles, dtype=bool)},
                 periods=periods)
+
+
+def box(etype, ncells, lo, hi, periodic, bcnames=None):
+    """Uniform box of quads (2-D) or hexes (3-D), periodic in the directions
+    flagged in ``periodic`` and bounded in the others.  The faces at the
+    low and high ends of a bounded direction d form the boundaries named
+    ``bcnames[d] = (low name, high name)`` (default 'xlo'/'xhi' and so on).
+    Elements are numbered x fastest."""
+    ndims = {'quad': 2, 'hex': 3}[etype]
+    n = (ncells,)*ndims if np.isscalar(ncells) else tuple(ncells)
+    lo = (lo,)*ndims if np.isscalar(lo) else tuple(lo)
+    hi = (hi,)*ndims if np.isscalar(hi) else tuple(hi)
+    periodic = tuple(periodic)
+
+    axes = [np.linspace(lo[d], hi[d], n[d] + 1) for d in range(ndims)]
+    idx = np.indices(n[::-1]).reshape(ndims, -1)[::-1]
+    neles = idx.shape[1]
+    spts = np.empty((2**ndims, neles, ndims))
+    for v in range(2**ndims):
+        for d in range(ndims):
+            spts[v, :, d] = axes[d][idx[d] + ((v >> d) & 1)]
+
+    def eid(ijk):
+        e = np.zeros(ijk.shape[1], dtype=np.int64)
+        stride = 1
+        for d in range(ndims):
+            e += (ijk[d] % n[d])*stride
+            stride *= n[d]
+        return e
+
+    # (face at the high end, face at the low end) of each direction
+    facepairs = {'quad': [(1, 3), (2, 0)],
+                 'hex': [(2, 4), (3, 1), (5, 0)]}[etype]
+    names = bcnames or [(f'{a}lo', f'{a}hi') for a in 'xyz'[:ndims]]
+    le, lf, re, rf = [], [], [], []
+    bcon = {}
+    here = eid(idx)
+    for d, (fhi, flo) in enumerate(facepairs):
+        inner = np.ones(neles, dtype=bool) if periodic[d] else \
+            idx[d] < n[d] - 1
+        nb = idx.copy()
+        nb[d] += 1
+        le.append(here[inner])
+        lf.append(np.full(inner.sum(), fhi))
+        re.append(eid(nb[:, inner]))
+        rf.append(np.full(inner.sum(), flo))
+        if not periodic[d]:
+            for name, sel, f in ((names[d][0], idx[d] == 0, flo),
+                                 (names[d][1], idx[d] == n[d] - 1, fhi)):
+                e = here[sel]
+                prev = bcon.get(name)
+                sd = Side([etype]*len(e), e, np.full(len(e), f))
+                if prev is not None:
+                    sd = Side(np.concatenate([prev.etypes, sd.etypes]),
+                              np.concatenate([prev.eidxs, sd.eidxs]),
+                              np.concatenate([prev.fidxs, sd.fidxs]))
+                bcon[name] = sd
+
+    nint = sum(len(x) for x in le)
+    lhs = Side([etype]*nint, np.concatenate(le), np.concatenate(lf))
+    rhs = Side([etype]*nint, np.concatenate(re), np.concatenate(rf))
+    periods = tuple((hi[d] - lo[d]) if periodic[d] else None
+                    for d in range(ndims))
+    return Mesh(ndims=ndims, spts={etype: spts}, con=(lhs, rhs),
+                spts_curved={etype: np.zeros(neles, dtype=bool)},
+                periods=periods, bcon=bcon)
 
 
 def face_vertices(etype):

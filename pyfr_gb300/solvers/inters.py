@@ -147,3 +147,114 @@ class NavierStokesIntInters(BaseIntInters):
         # (pyfr/solvers/baseadvecdiff/inters.py:21-28)
         beta = self.cfg.getfloat('solver-interfaces', 'ldg-beta')
         return self.lhs if beta != -0.5 else self.rhs
+
+
+# ---------------------------------------------------------------------------
+# Boundary conditions (pyfr/solvers/baseadvec/inters.py:74-116,
+# pyfr/solvers/euler/inters.py:53-112, pyfr/solvers/navstokes/inters.py:66-150)
+# ---------------------------------------------------------------------------
+
+# The constants each boundary type reads from its [soln-bcs-<name>] section
+BC_OPTS = {
+    'sup-in-fa': ['rho', 'p', 'u', 'v', 'w'],
+    'char-riem-inv': ['rho', 'p', 'u', 'v', 'w'],
+    'no-slp-isot-wall': ['u', 'v', 'w'],
+    'sup-out-fn': [], 'slp-adia-wall': [], 'no-slp-adia-wall': [],
+}
+EULER_BCS = {'sup-in-fa', 'sup-out-fn', 'slp-adia-wall', 'char-riem-inv'}
+
+
+class BaseBCInters(BaseIntInters):
+    """One boundary: its faces (the left side only), the view of the
+    flux-point field over them, scaled normals, and the boundary type with
+    its constants from ``[soln-bcs-<name>]``."""
+
+    def __init__(self, be, lhs, elemap, cfgsect, cfg):
+        from pyfr_gb300.backend.lib import BC, BC_TYPES
+        from pyfr_gb300.solvers.elements import npeval
+
+        self._be = be
+        self.elemap = elemap
+        self.cfg = cfg
+        self.lhs, self.rhs = lhs, None
+        self.cfgsect = cfgsect
+        self.name = cfgsect.removeprefix('soln-bcs-')
+
+        first = next(iter(elemap.values()))
+        self.ndims, self.nvars = first.ndims, first.nvars
+        self.ninters = len(lhs)
+        self.ninterfpts = sum(elemap[et].nfacefpts[fi]*len(ei)
+                              for et, fi, ei in lhs.items())
+        self.c = cfg.items_as('constants', float)
+        self.kernels = {}
+
+        self.type = cfg.get(cfgsect, 'type')
+        if self.type not in self.bctypes:
+            raise NotImplementedError(f'Boundary type {self.type!r} is not '
+                                      'provided')
+
+        # Uniform constants, which may use [constants]
+        # (pyfr/solvers/baseadvec/inters.py:84-96)
+        vals = {}
+        for k in BC_OPTS[self.type]:
+            if k in 'uvw' and 'uvw'.index(k) >= self.ndims:
+                continue
+            default = '0' if self.type == 'no-slp-isot-wall' else None
+            expr = cfg.get(cfgsect, k, default)
+            if expr is None:
+                raise ValueError(f'{cfgsect}: {k} is required')
+            vals[k] = float(npeval(str(expr), dict(self.c)))
+        if self.type == 'no-slp-isot-wall':
+            vals['cpTw'] = float(npeval(cfg.get(cfgsect, 'cpTw'),
+                                        dict(self.c)))
+        self.bcvals = vals
+        self.bc = BC(type=BC_TYPES[self.type], rho=vals.get('rho', 0.0),
+                     p=vals.get('p', 0.0), cpTw=vals.get('cpTw', 0.0))
+        for i, k in enumerate('uvw'[:self.ndims]):
+            self.bc.u[i] = vals.get(k, 0.0)
+
+        # Memory order of the one side (pyfr/solvers/baseadvec/inters.py:90)
+        scal = {t: e._scal_fpts for t, e in elemap.items()}
+        self._perm = self._perm_for_field(lhs, scal)
+        self._pnorm_lhs = self._const_mat(lhs, 'get_pnorms_for_inters')
+
+
+class EulerBCInters(BaseBCInters):
+    bctypes = EULER_BCS
+
+    def __init__(self, *args, **kwargs):
+        super().__init__(*args, **kwargs)
+        rsolver = self.cfg.get('solver-interfaces', 'riemann-solver')
+        self._tplargs = dict(ndims=self.ndims, nvars=self.nvars,
+                             rsolver=rsolver, c=self.c, bctype=self.type,
+                             bc=self.bc)
+        self._be.pointwise.register('pyfr.solvers.euler.kernels.bccflux')
+        self.kernels['comm_flux'] = lambda: self._be.kernel(
+            'bccflux', tplargs=self._tplargs, dims=[self.ninterfpts],
+            ul=self.scal_lhs, nl=self._pnorm_lhs)
+
+
+class NavierStokesBCInters(BaseBCInters):
+    bctypes = set(BC_OPTS)
+
+    def __init__(self, *args, **kwargs):
+        super().__init__(*args, **kwargs)
+        be, cfg = self._be, self.cfg
+        self._vect_lhs = self._vect_view(self.lhs, 'get_vect_fpts_for_inters')
+        self._comm_lhs = self._scal_view(self.lhs, 'get_comm_fpts_for_inters')
+        self.c |= cfg.items_as('solver-interfaces', float)
+
+        rsolver = cfg.get('solver-interfaces', 'riemann-solver')
+        visc_corr = cfg.get('solver', 'viscosity-correction', 'none')
+        self._tplargs = dict(ndims=self.ndims, nvars=self.nvars,
+                             rsolver=rsolver, visc_corr=visc_corr,
+                             shock_capturing='none', c=self.c,
+                             bctype=self.type, bc=self.bc)
+        be.pointwise.register('pyfr.solvers.navstokes.kernels.bcconu')
+        be.pointwise.register('pyfr.solvers.navstokes.kernels.bccflux')
+        self.kernels['con_u'] = lambda: be.kernel(
+            'bcconu', tplargs=self._tplargs, dims=[self.ninterfpts],
+            ulin=self.scal_lhs, ulout=self._comm_lhs, nlin=self._pnorm_lhs)
+        self.kernels['comm_flux'] = lambda: be.kernel(
+            'bccflux', tplargs=self._tplargs, dims=[self.ninterfpts],
+            ul=self.scal_lhs, gradul=self._vect_lhs, nl=self._pnorm_lhs)

@@ -16,7 +16,9 @@ import numpy as np
 
 from pyfr_gb300.backend.types import NullKernel
 from pyfr_gb300.solvers.elements import EulerElements, NavierStokesElements
-from pyfr_gb300.solvers.inters import (EulerIntInters, NavierStokesIntInters,
+from pyfr_gb300.solvers.inters import (EulerBCInters, EulerIntInters,
+                                       NavierStokesBCInters,
+                                       NavierStokesIntInters,
                                        field_view_arrays)
 
 
@@ -69,15 +71,29 @@ class BaseSystem:
         lhs, rhs = mesh.con
         self._int_inters = [self.intinterscls(backend, lhs, rhs, elemap, cfg)]
 
+        # Boundaries: one interface object per named boundary, its type from
+        # [soln-bcs-<name>] (pyfr/solvers/base/system.py:183-198)
+        self._bc_inters = []
+        for name, side in sorted(getattr(mesh, 'bcon', {}).items()):
+            sect = f'soln-bcs-{name}'
+            if not cfg.hassect(sect):
+                raise ValueError(f'No [{sect}] section for boundary {name!r}')
+            self._bc_inters.append(self.bcinterscls(backend, side, elemap,
+                                                    sect, cfg))
+
     @property
     def gndofs(self):
         return sum(self.ele_ndofs)
 
     def make_field_views(self, field, vshape=()):
+        """(left, right) views of a flux-point field for every interior
+        interface, then (left,) for every boundary."""
         out = []
-        for i in self._int_inters:
+        for i in self._int_inters + self._bc_inters:
             views = []
             for side in (i.lhs, i.rhs):
+                if side is None:
+                    continue
                 m, r, c = field_view_arrays(side, field, self.ele_map)
                 p = i._perm
                 views.append(self.backend.view(m[p], r[p], c[p],
@@ -90,8 +106,10 @@ class BaseSystem:
         interface (a fully periodic mesh): the common solution can then be
         written to both sides of each interface point with no copy."""
         nside = defaultdict(int)
-        for i in self._int_inters:
+        for i in self._int_inters + self._bc_inters:
             for side in (i.lhs, i.rhs):
+                if side is None:
+                    continue
                 for et in side.etypes.tolist():
                     nside[et] += 1
         return all(nside[et] == e.neles*len(e.basis.faces)
@@ -104,9 +122,10 @@ class BaseSystem:
         for i in self._int_inters:
             i.covers = covered
         scal = {et: e._scal_fpts for et, e in self.ele_map.items()}
-        for i, (l, r) in zip(self._int_inters, self.make_field_views(
-                scal, vshape=(self.nvars,))):
-            i.scal_lhs, i.scal_rhs = l, r
+        for i, v in zip(self._int_inters + self._bc_inters,
+                        self.make_field_views(scal, vshape=(self.nvars,))):
+            i.scal_lhs = v[0]
+            i.scal_rhs = v[1] if len(v) > 1 else None
 
         self.backend.commit()
         self._gen_kernels()
@@ -130,7 +149,7 @@ class BaseSystem:
         self._ktags = {}
 
         provs = [('eles', list(self.ele_map.values())),
-                 ('iint', self._int_inters)]
+                 ('iint', self._int_inters), ('bcint', self._bc_inters)]
         for pn, plist in provs:
             for p in plist:
                 for kn, kget in p.kernels.items():
@@ -204,6 +223,7 @@ class EulerSystem(BaseSystem):
     name = 'euler'
     elementscls = EulerElements
     intinterscls = EulerIntInters
+    bcinterscls = EulerBCInters
 
     def _rhs_graphs(self, uinbank, foutbank):
         k = self._get_kernels(uinbank, foutbank)
@@ -214,6 +234,7 @@ class EulerSystem(BaseSystem):
         g_intf = self.backend.graph()
         g_intf.add_all(k['eles/disu'])
         g_intf.add_all(k['iint/comm_flux'], deps=k['eles/disu'])
+        g_intf.add_all(k['bcint/comm_flux'], deps=k['eles/disu'])
         g_intf.commit()
 
         g_flux_div = self.backend.graph()
@@ -248,6 +269,7 @@ class NavierStokesSystem(BaseSystem):
     name = 'navier-stokes'
     elementscls = NavierStokesElements
     intinterscls = NavierStokesIntInters
+    bcinterscls = NavierStokesBCInters
 
     def _rhs_graphs(self, uinbank, foutbank):
         k = self._get_kernels(uinbank, foutbank)
@@ -262,6 +284,7 @@ class NavierStokesSystem(BaseSystem):
             g_soln.add(l, deps=deps(l, 'eles/disu'))
         kdeps = k['eles/copy_fpts'] or k['eles/disu']
         g_soln.add_all(k['iint/con_u'], deps=kdeps)
+        g_soln.add_all(k['bcint/con_u'], deps=kdeps)
         g_soln.commit()
 
         if k['eles/tgradcoru_upts_cat']:
@@ -278,6 +301,7 @@ class NavierStokesSystem(BaseSystem):
         for l in k['eles/gradcoru_fpts']:
             g_grad_flux.add(l, deps=deps(l, 'eles/tdisf_fused'))
         g_grad_flux.add_all(k['iint/comm_flux'], deps=k['eles/gradcoru_fpts'])
+        g_grad_flux.add_all(k['bcint/comm_flux'], deps=k['eles/gradcoru_fpts'])
         for l in k['eles/tdivtpcorf']:
             g_grad_flux.add(l, deps=deps(l, 'eles/tdisf_fused'))
 
@@ -315,6 +339,7 @@ class NavierStokesSystem(BaseSystem):
         for l in k['eles/gradcoru_fpts']:
             g_grad_flux.add(l, deps=deps(l, 'eles/tdisf_fused'))
         g_grad_flux.add_all(k['iint/comm_flux'], deps=k['eles/gradcoru_fpts'])
+        g_grad_flux.add_all(k['bcint/comm_flux'], deps=k['eles/gradcoru_fpts'])
         g_grad_flux.commit()
 
         g_div = self.backend.graph()

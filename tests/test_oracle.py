@@ -189,3 +189,79 @@ def test_antialiased_free_stream_and_conservation(golden, case, etype):
     d0 = Discretisation(ops, basis_of(s), g['spts'], g['lhs'], g['rhs'],
                         periods=(2.0,)*s.ndims)
     assert np.abs(r - d0.rhs_euler(u, GAS)).max() > 1e-8
+
+
+# ---------------------------------------------------------------------------
+# Boundary conditions
+# ---------------------------------------------------------------------------
+
+def bc_disc(etype, n, periodic, bcspecs, ns=False):
+    """Oracle discretisation of a box with boundaries (product operators;
+    the boundary arithmetic is what is under test here)."""
+    from pyfr_gb300.mesh import box
+    from tests.oracle_util import ops_from_shape
+    mesh = box(etype, n, 0.0, 1.0, periodic)
+    s = get_shape(etype, 3)
+    lhs, rhs = mesh.con
+    bcs = [(np.stack([side.eidxs, side.fidxs], 1), bcspecs[name])
+           for name, side in sorted(mesh.bcon.items())]
+    d = Discretisation(ops_from_shape(s, ns), basis_of(s),
+                       mesh.spts[etype], np.stack([lhs.eidxs, lhs.fidxs], 1),
+                       np.stack([rhs.eidxs, rhs.fidxs], 1),
+                       periods=mesh.periods, bcs=bcs)
+    return d, mesh
+
+
+def _uniform(d, prim, gamma=1.4):
+    nd = d.ndims
+    rho, vel, p = prim[0], np.array(prim[1:nd + 1]), prim[-1]
+    cons = np.array([rho, *(rho*vel), p/(gamma - 1) + 0.5*rho*vel @ vel])
+    return np.broadcast_to(cons[None, :, None],
+                           (d.nupts, nd + 2, d.neles)).copy()
+
+
+FREE = dict(rho=1.2, p=0.9, u=[0.4, -0.2, 0.3])
+
+
+@pytest.mark.parametrize('bctypes', [('sup-in-fa', 'sup-out-fn'),
+                                     ('char-riem-inv', 'char-riem-inv'),
+                                     ('sup-out-fn', 'char-riem-inv')])
+def test_bc_free_stream_euler(bctypes):
+    """A free stream at the boundary state is steady through inflow,
+    outflow and characteristic boundaries."""
+    specs = {'xlo': dict(type=bctypes[0], **FREE),
+             'xhi': dict(type=bctypes[1], **FREE)}
+    d, _ = bc_disc('quad', (3, 3), (False, True), specs)
+    u = _uniform(d, [FREE['rho'], *FREE['u'][:2], FREE['p']])
+    assert np.abs(d.rhs_euler(u, GAS)).max() < 1e-11
+
+
+def test_bc_slip_wall_tangential_stream_and_mass():
+    """A stream along slip walls is steady; with any state, no mass crosses
+    a slip wall (the total mass is conserved)."""
+    specs = {'ylo': dict(type='slp-adia-wall'), 'yhi': dict(type='slp-adia-wall')}
+    d, mesh = bc_disc('quad', (3, 4), (True, False), specs)
+    u = _uniform(d, [1.1, 0.6, 0.0, 1.3])
+    assert np.abs(d.rhs_euler(u, GAS)).max() < 1e-11
+
+    rng = np.random.default_rng(2)
+    u = u*(1 + 0.05*rng.normal(size=u.shape))
+    r = d.rhs_euler(u, GAS)
+    x, w = np.polynomial.legendre.leggauss(4)
+    wts = np.outer(w, w).reshape(-1)
+    tot = np.einsum('p,pe,pe->', wts, r[:, 0], d.djac_u)
+    scale = np.einsum('p,pe,pe->', wts, np.abs(r[:, 0]), d.djac_u)
+    assert abs(tot) <= 1e-12*scale
+
+
+@pytest.mark.parametrize('walls', [('no-slp-adia-wall', 'no-slp-adia-wall'),
+                                   ('no-slp-isot-wall', 'slp-adia-wall')])
+def test_bc_walls_navier_stokes_rest_state(walls):
+    """A gas at rest at the wall temperature is steady between walls."""
+    gamma, rho, p = 1.4, 1.0, 1.0/1.4
+    cpTw = gamma/(gamma - 1)*p/rho
+    specs = {'zlo': dict(type=walls[0], u=[0, 0, 0], cpTw=cpTw),
+             'zhi': dict(type=walls[1], u=[0, 0, 0], cpTw=cpTw)}
+    d, _ = bc_disc('hex', (2, 2, 3), (True, True, False), specs, ns=True)
+    u = _uniform(d, [rho, 0, 0, 0, p])
+    assert np.abs(d.rhs_ns(u, GAS)).max() < 1e-11
