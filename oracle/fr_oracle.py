@@ -720,6 +720,78 @@ class MixedDiscretisation:
             out[et] = -r/e['djac_u'][:, None, :]
         return out
 
+    def rhs_ns(self, u, c, rsolver='rusanov'):
+        """Navier-Stokes right-hand side over every element type (the
+        graphs of pyfr/solvers/baseadvecdiff/system.py:54-231)."""
+        gamma, beta, tau = c['gamma'], c['ldg-beta'], c['ldg-tau']
+        nd = self.ndims
+        ap = Discretisation.apply
+        uf = {et: ap(self.p[et]['ops']['M0'], u[et]) for et in self.etypes}
+
+        # Common solution at the interface points (intconu)
+        ul, ur = self._gather(uf, 'l'), self._gather(uf, 'r')
+        if beta == -0.5:
+            cl = cr = ul
+        elif beta == 0.5:
+            cl = cr = ur
+        else:
+            cl = cr = ur*(0.5 + beta) + ul*(0.5 - beta)
+        comm = {et: v.copy() for et, v in uf.items()}
+        self._scatter(comm, 'l', cl)
+        self._scatter(comm, 'r', cr)
+
+        # Corrected physical gradient at the solution points, interpolated
+        # to the flux points
+        grad, gfp, ft = {}, {}, {}
+        for et in self.etypes:
+            e = self.p[et]
+            nup, ne = len(e['upts']), e['neles']
+            g = ap(e['ops']['M460'], u[et]) + ap(e['ops']['M6'], comm[et])
+            g = g.reshape(nd, nup, -1, ne)
+            g = np.einsum('pkie,kpve->ipve', e['smats_u'], g) / \
+                e['djac_u'][None, :, None, :]
+            grad[et] = g
+            gfp[et] = np.stack([ap(e['ops']['M0'], g[d]) for d in range(nd)])
+            ut = u[et].transpose(1, 0, 2)
+            fi, _, _ = inviscid_flux(ut, gamma)
+            fv = viscous_flux(ut, g.transpose(0, 2, 1, 3), c)
+            ft[et] = np.einsum('pike,kpve->ipve', e['smats_u'],
+                               (fi + fv).transpose(0, 2, 1, 3))
+
+        # Common flux at the interface points
+        def gather_grad(side):
+            t, f, ee = self.side[side]
+            out = np.empty((nd, nd + 2, len(t)))
+            for i, et in enumerate(self.etypes):
+                m = t == i
+                out[:, :, m] = gfp[et][:, f[m], :, ee[m]].transpose(1, 2, 0)
+            return out
+
+        gl, gr = gather_grad('l'), gather_grad('r')
+        mag = np.sqrt(np.sum(self.nl**2, axis=0))
+        n = self.nl/mag
+        fic = RSOLVERS[rsolver](ul, ur, n, gamma)
+        fvl = np.einsum('dn,dvn->vn', n, viscous_flux(ul, gl, c))
+        fvr = np.einsum('dn,dvn->vn', n, viscous_flux(ur, gr, c))
+        if beta == -0.5:
+            fvc = fvr
+        elif beta == 0.5:
+            fvc = fvl
+        else:
+            fvc = (0.5 + beta)*fvl + (0.5 - beta)*fvr
+        fvc = fvc + tau*(ul - ur)
+        self._scatter(uf, 'l', mag*(fic + fvc))
+        self._scatter(uf, 'r', -mag*(fic + fvc))
+
+        out = {}
+        for et in self.etypes:
+            e = self.p[et]
+            nup, ne = len(e['upts']), e['neles']
+            r = ap(e['ops']['M132'], ft[et].reshape(nd*nup, -1, ne))
+            r += ap(e['ops']['M3'], uf[et])
+            out[et] = -r/e['djac_u'][:, None, :]
+        return out
+
     def pack(self, fld):
         return np.concatenate([fld[et].ravel() for et in self.etypes])
 

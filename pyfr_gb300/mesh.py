@@ -320,6 +320,25 @@ def mixed_box(n, lo, hi, kinds):
                 periods=(hi - lo,)*3)
 
 
+def tri_box(n, lo, hi):
+    """Periodic square of n x n cells, each cut into two triangles along its
+    (0,0)-(1,1) diagonal (vertices in the reference's order with positive
+    area); elements numbered cell by cell, x fastest."""
+    axes = np.linspace(lo, hi, n + 1)
+    idx = np.indices((n, n)).reshape(2, -1)[::-1]          # i fastest
+    corners = np.empty((4, idx.shape[1], 2))
+    for v in range(4):
+        for d in range(2):
+            corners[v, :, d] = axes[idx[d] + ((v >> d) & 1)]
+    # corners 0 (0,0), 1 (1,0), 2 (0,1), 3 (1,1): triangles (1,3,0), (2,0,3)
+    spts = np.stack([corners[[1, 3, 0]], corners[[2, 0, 3]]], axis=2)
+    spts = {'tri': spts.reshape(3, -1, 2)}
+    con = connect(spts, periods=(hi - lo,)*2, lo=(lo,)*2)
+    return Mesh(ndims=2, spts=spts, con=con,
+                spts_curved={'tri': np.zeros(spts['tri'].shape[1], bool)},
+                periods=(hi - lo,)*2)
+
+
 def fuzzy_face_order(coords, tol=1e-6):
     """Per-face ordering of flux points by their physical coordinates,
     lexicographic with the first coordinate most significant and values

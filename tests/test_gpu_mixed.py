@@ -172,3 +172,81 @@ def test_mixed_mesh_density_wave_accuracy(built, kinds):
         rho = density_wave_exact(ploc[:, 0], ploc[:, 1], ploc[:, 2],
                                  intg.tcurr, cfg)
         assert np.abs(u[:, 0] - rho).max() < 2e-2
+
+
+@pytest.mark.parametrize('case', ['hexpri_p3', 'pritet_p3'])
+@pytest.mark.parametrize('beta', [0.5, 0.0])
+def test_ns_rhs_mixed_mesh(built, golden, case, beta):
+    """Navier-Stokes on the perturbed mixed meshes (gradient operators of
+    prisms and tetrahedra included) against the multi-type oracle."""
+    from oracle.fr_oracle import MixedDiscretisation
+    from pyfr_gb300.shapes import get_shape
+    from pyfr_gb300.solvers.system import NavierStokesSystem
+    from tests.oracle_util import basis_of, ops_from_golden
+    g = golden[f'geometry_{case}']
+    mesh = _golden_mesh(g)
+    cfg = _cfg('rusanov')
+    gas = dict(gamma=1.4, mu=0.03, Pr=0.72, **{'ldg-beta': beta,
+                                              'ldg-tau': 0.1})
+    for k in ('mu', 'Pr'):
+        cfg.set('constants', k, gas[k])
+    cfg.set('solver-interfaces', 'ldg-beta', beta)
+    cfg.set('solver-interfaces', 'ldg-tau', 0.1)
+    ics = {et: g[f'{et}/ics'] for et in mesh.spts}
+    s = NavierStokesSystem(_backend(cfg), mesh, ics, 2, cfg)
+    s.commit()
+    s.rhs(0.0, 0, 1)
+    got = dict(zip(s.ele_types, s.ele_scal_upts(1)))
+
+    ops = golden['operators']
+    parts = {}
+    for et in mesh.spts:
+        key = 'hex_p3_gauss-legendre' if et == 'hex' else f'{et}_p3_mixed'
+        sh = get_shape(et, 3, MIXED_UPTS[et], MIXED_FPTS)
+        parts[et] = dict(ops=ops_from_golden(ops, key, True),
+                         basis=basis_of(sh), verts=mesh.spts[et])
+    d = MixedDiscretisation(parts, g['lhs'], g['rhs'], periods=(2.0,)*3)
+    ref = d.rhs_ns(ics, gas)
+    for et in mesh.spts:
+        assert _relerr(got[et], ref[et]) < TOL, et
+
+
+@pytest.mark.parametrize('system', ['euler', 'navier-stokes'])
+def test_triangle_mesh_rhs(built, system):
+    """2-D triangles (each cell of a periodic square cut in two)."""
+    from oracle.fr_oracle import MixedDiscretisation
+    from pyfr_gb300.inifile import Inifile
+    from pyfr_gb300.mesh import tri_box
+    from pyfr_gb300.shapes import get_shape
+    from pyfr_gb300.solvers.system import EulerSystem, NavierStokesSystem
+    from tests.oracle_util import basis_of, ops_from_shape
+    mesh = tri_box(5, -1.0, 1.0)
+    cfg = Inifile()
+    gas = dict(gamma=1.4, mu=0.02, Pr=0.72, **{'ldg-beta': 0.5,
+                                              'ldg-tau': 0.1})
+    for k in ('gamma', 'mu', 'Pr'):
+        cfg.set('constants', k, gas[k])
+    cfg.set('solver', 'order', 3)
+    cfg.set('solver-interfaces', 'riemann-solver', 'rusanov')
+    cfg.set('solver-interfaces', 'ldg-beta', 0.5)
+    cfg.set('solver-interfaces', 'ldg-tau', 0.1)
+    cfg.set('soln-ics', 'rho', '1 + 0.2*sin(pi*x)*cos(pi*y)')
+    cfg.set('soln-ics', 'u', '0.4 + 0.1*y')
+    cfg.set('soln-ics', 'v', '-0.2 + 0.1*sin(pi*x)')
+    cfg.set('soln-ics', 'p', '1 + 0.1*cos(pi*x)')
+    ns = system == 'navier-stokes'
+    scls = NavierStokesSystem if ns else EulerSystem
+    s = scls(_backend(cfg), mesh, None, 2, cfg)
+    s.commit()
+    s.rhs(0.0, 0, 1)
+    (u,), (r,) = s.ele_scal_upts(0), s.ele_scal_upts(1)
+
+    sh = get_shape('tri', 3, 'alpha-opt', 'gauss-legendre')
+    lhs, rhs = mesh.con
+    d = MixedDiscretisation(
+        {'tri': dict(ops=ops_from_shape(sh, ns), basis=basis_of(sh),
+                     verts=mesh.spts['tri'])},
+        zip(lhs.etypes, lhs.eidxs, lhs.fidxs),
+        zip(rhs.etypes, rhs.eidxs, rhs.fidxs), periods=mesh.periods)
+    ref = (d.rhs_ns if ns else d.rhs_euler)({'tri': u}, gas)['tri']
+    assert _relerr(r, ref) < TOL

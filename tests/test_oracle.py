@@ -265,3 +265,53 @@ def test_bc_walls_navier_stokes_rest_state(walls):
     d, _ = bc_disc('hex', (2, 2, 3), (True, True, False), specs, ns=True)
     u = _uniform(d, [rho, 0, 0, 0, p])
     assert np.abs(d.rhs_ns(u, GAS)).max() < 1e-11
+
+
+def test_mixed_ns_oracle_equals_single_type_oracle(golden):
+    """The multi-type Navier-Stokes RHS on a one-type mesh is the
+    single-type oracle's."""
+    from oracle.fr_oracle import MixedDiscretisation
+    d, g = _disc(golden, 'hex_p3', 'hex', True)
+    ops = ops_from_golden(golden['operators'], 'hex_p3_gauss-legendre', True)
+    n = len(g['lhs'])
+    m = MixedDiscretisation(
+        {'hex': dict(ops=ops, basis=basis_of(get_shape('hex', 3)),
+                     verts=g['spts'])},
+        [('hex', e, f) for e, f in g['lhs']],
+        [('hex', e, f) for e, f in g['rhs']], periods=(2.0,)*3)
+    a = m.rhs_ns({'hex': g['ics']}, GAS)['hex']
+    b = d.rhs_ns(g['ics'], GAS)
+    assert n > 0 and np.abs(a - b).max() <= 1e-13*np.abs(b).max()
+
+
+@pytest.mark.parametrize('case', ['hexpri_p3', 'pritet_p3'])
+def test_mixed_ns_free_stream_and_conservation(golden, case):
+    from oracle.fr_oracle import MixedDiscretisation
+    from pyfr_gb300.quadrules import EXACT_RULES
+    g = golden[f'geometry_{case}']
+    ops = golden['operators']
+    parts = {}
+    for et in ('hex', 'pri', 'tet'):
+        if f'{et}/spts' not in g:
+            continue
+        key = 'hex_p3_gauss-legendre' if et == 'hex' else f'{et}_p3_mixed'
+        s = get_shape(et, 3, MIXED_UPTS[et], MIXED_FPTS)
+        parts[et] = dict(ops=ops_from_golden(ops, key, True), basis=basis_of(s),
+                         verts=g[f'{et}/spts'])
+    d = MixedDiscretisation(parts, g['lhs'], g['rhs'], periods=(2.0,)*3)
+    cons = np.array([1.2, 0.3, 0.6, 0.9, 3.0])
+    u = {et: np.broadcast_to(cons[None, :, None],
+                             (len(e['upts']), 5, e['neles'])).copy()
+         for et, e in d.p.items()}
+    assert max(np.abs(v).max() for v in d.rhs_ns(u, GAS).values()) < 1e-11
+
+    r = d.rhs_ns({et: g[f'{et}/ics'] for et in d.p}, GAS)
+    tot, scale = 0, 0
+    for et, e in d.p.items():
+        s = get_shape(et, 3, MIXED_UPTS[et], MIXED_FPTS)
+        qp, qw = EXACT_RULES[et](6)
+        L = s.ubasis.nodal_basis_at(qp)
+        rq = np.einsum('qp,pve->qve', L, r[et]*e['djac_u'][:, None, :])
+        tot = tot + np.einsum('q,qve->v', qw, rq)
+        scale = scale + np.einsum('q,qve->v', qw, np.abs(rq))
+    assert np.all(np.abs(tot) <= 1e-12*scale)
