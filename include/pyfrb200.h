@@ -56,12 +56,17 @@ enum {
     B200_BC_SLP_ADIA_WALL = 3,    /* slip adiabatic wall */
     B200_BC_CHAR_RIEM_INV = 4,    /* characteristic Riemann invariants */
     B200_BC_NO_SLP_ADIA_WALL = 5, /* no-slip adiabatic wall (NS) */
-    B200_BC_NO_SLP_ISOT_WALL = 6  /* no-slip isothermal wall (NS) */
+    B200_BC_NO_SLP_ISOT_WALL = 6, /* no-slip isothermal wall (NS) */
+    B200_BC_SUB_IN_FRV = 7,       /* subsonic inflow, given rho and velocity (NS) */
+    B200_BC_SUB_IN_FTPTTANG = 8,  /* subsonic inflow, given total state and direction (NS) */
+    B200_BC_SUB_OUT_FP = 9        /* subsonic outflow, given pressure (NS) */
 };
 typedef struct {
     int type;
     double rho, p, u[3];
     double cpTw;
+    /* sub-in-ftpttang: total cp*T, total pressure, flow direction */
+    double cpTt, pt, vc[3];
 } b200_bc_t;
 
 /* Riemann solver ids: [solver-interfaces] riemann-solver */

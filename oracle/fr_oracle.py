@@ -204,6 +204,22 @@ def bc_rsolve_state(bc, ul, n, gamma):
         ur[1:nd + 1] = -ul[1:nd + 1] + 2*uvw*ul[0]
         ur[-1] = bc['cpTw']/gamma*ur[0] + \
             0.5*np.sum(ur[1:nd + 1]**2, axis=0)/ur[0]
+    elif t == 'sub-in-frv':
+        ur[0] = bc['rho']
+        ur[1:nd + 1] = bc['rho']*uvw
+        ur[-1] = ul[-1] - 0.5*np.sum(ul[1:nd + 1]**2, axis=0)/ul[0] + \
+            0.5*np.sum(ur[1:nd + 1]**2, axis=0)/ur[0]
+    elif t == 'sub-in-ftpttang':
+        rdcp = gm1/gamma
+        vc = np.array(bc['vc'][:nd])[:, None]
+        pl = gm1*(ul[-1] - 0.5/ul[0]*np.sum(ul[1:nd + 1]**2, axis=0))
+        udotu = np.maximum(0, 2*bc['cpTt']*(1 - bc['pt']**-rdcp*pl**rdcp))
+        ur[0] = pl/(rdcp*(bc['cpTt'] - 0.5*udotu))
+        ur[1:nd + 1] = vc*ur[0]*np.sqrt(udotu)
+        ur[-1] = pl/gm1 + 0.5*ur[0]*udotu
+    elif t == 'sub-out-fp':
+        ur[:-1] = ul[:-1]
+        ur[-1] = bc['p']/gm1 + 0.5*np.sum(ul[1:nd + 1]**2, axis=0)/ul[0]
     else:
         raise ValueError(t)
     return ur
@@ -234,7 +250,7 @@ def bc_ldg_state(bc, ul, n, gamma):
 def bc_ldg_grad_state(bc, us, n, gl):
     """Boundary gradient (bc_ldg_grad_state); gl (ndims, nvars, npts)."""
     t = bc['type']
-    if t in ('sup-in-fa', 'char-riem-inv'):
+    if t in ('sup-in-fa', 'char-riem-inv', 'sub-in-frv', 'sub-out-fp'):
         return np.zeros_like(gl)
     gr = gl.copy()
     if t == 'no-slp-adia-wall':

@@ -42,12 +42,13 @@ class Gas(C.Structure):
 
 # Boundary-condition types and constants (b200_bc_t)
 BC_TYPES = {'sup-in-fa': 1, 'sup-out-fn': 2, 'slp-adia-wall': 3,
-            'char-riem-inv': 4, 'no-slp-adia-wall': 5, 'no-slp-isot-wall': 6}
+            'char-riem-inv': 4, 'no-slp-adia-wall': 5, 'no-slp-isot-wall': 6,
+            'sub-in-frv': 7, 'sub-in-ftpttang': 8, 'sub-out-fp': 9}
 
 
 class BC(C.Structure):
     _fields_ = [('type', i32), ('rho', f64), ('p', f64), ('u', f64*3),
-                ('cpTw', f64)]
+                ('cpTw', f64), ('cpTt', f64), ('pt', f64), ('vc', f64*3)]
 
 
 def _sig_pointwise(fp):

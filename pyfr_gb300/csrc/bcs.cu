@@ -8,7 +8,8 @@
 //   ghost states      pyfr/solvers/euler/kernels/bcs/{sup-in-fa,sup-out-fn,
 //                     slp-adia-wall,char-riem-inv}.mako,
 //                     pyfr/solvers/navstokes/kernels/bcs/{no-slp-adia-wall,
-//                     no-slp-isot-wall,slp-adia-wall,common,ghost,
+//                     no-slp-isot-wall,slp-adia-wall,sub-in-frv,
+//                     sub-in-ftpttang,sub-out-fp,common,ghost,
 //                     ghost-imperm}.mako
 //
 // The boundary constants are uniform (the reference also allows
@@ -34,6 +35,8 @@ struct BcK {
     T rho, p, u[3], cpTw_g;        // cpTw_g = cpTw / gamma
     // char-riem-inv: free-stream sound speed, entropy, 2 cs/(gamma - 1)
     T cs, s, ratio;
+    // sub-in-ftpttang: cpTt, pt^-Rdcp, Rdcp = (gamma - 1)/gamma, direction
+    T cpTt, ptfac, rdcp, vc[3];
 };
 
 template <typename T>
@@ -48,6 +51,11 @@ BcK<T> bc_consts(const b200_bc_t &b, double gamma) {
     k.cs = (T)cs;
     k.s = (T)(b.rho > 0 ? b.p * pow(b.rho, -gamma) : 0.0);
     k.ratio = (T)(cs * 2.0 / (gamma - 1.0));
+    const double rdcp = (gamma - 1.0) / gamma;
+    k.cpTt = (T)b.cpTt;
+    k.ptfac = (T)(b.pt > 0 ? pow(b.pt, -rdcp) : 0.0);
+    k.rdcp = (T)rdcp;
+    for (int i = 0; i < 3; i++) k.vc[i] = (T)b.vc[i];
     return k;
 }
 
@@ -133,6 +141,44 @@ __device__ __forceinline__ void bc_rsolve_state(const BcK<T> &bc, T gamma, const
         ur[NV - 1] = bc.cpTw_g * ur[0] + T(0.5) * (T(1) / ur[0]) * k2;
         break;
     }
+    case B200_BC_SUB_IN_FRV: {
+        // Given density and velocity, the interior internal energy
+        T kl = 0, kr = 0;
+        ur[0] = bc.rho;
+#pragma unroll
+        for (int i = 0; i < ND; i++) {
+            ur[i + 1] = bc.rho * bc.u[i];
+            kl += ul[i + 1] * ul[i + 1];
+            kr += ur[i + 1] * ur[i + 1];
+        }
+        ur[NV - 1] = ul[NV - 1] - T(0.5) * (T(1) / ul[0]) * kl + T(0.5) * (T(1) / ur[0]) * kr;
+        break;
+    }
+    case B200_BC_SUB_IN_FTPTTANG: {
+        // Total enthalpy and pressure with the interior static pressure
+        T kl = 0;
+#pragma unroll
+        for (int i = 0; i < ND; i++) kl += ul[i + 1] * ul[i + 1];
+        const T pl = gm1 * (ul[NV - 1] - (T(0.5) / ul[0]) * kl);
+        T udotu = T(2) * bc.cpTt * (T(1) - bc.ptfac * pow(pl, bc.rdcp));
+        udotu = fmax(T(0), udotu);
+        ur[0] = (T(1) / bc.rdcp) * pl / (bc.cpTt - T(0.5) * udotu);
+        const T speed = sqrt(udotu);
+#pragma unroll
+        for (int i = 0; i < ND; i++) ur[i + 1] = bc.vc[i] * ur[0] * speed;
+        ur[NV - 1] = (T(1) / gm1) * pl + T(0.5) * ur[0] * udotu;
+        break;
+    }
+    case B200_BC_SUB_OUT_FP: {
+        // Given pressure, the interior density and momentum
+        T kl = 0;
+#pragma unroll
+        for (int v = 0; v < NV - 1; v++) ur[v] = ul[v];
+#pragma unroll
+        for (int i = 0; i < ND; i++) kl += ul[i + 1] * ul[i + 1];
+        ur[NV - 1] = bc.p / gm1 + T(0.5) * (T(1) / ul[0]) * kl;
+        break;
+    }
     default:  // B200_BC_SUP_OUT_FN: the interior state
 #pragma unroll
         for (int v = 0; v < NV; v++) ur[v] = ul[v];
@@ -176,7 +222,8 @@ template <int ND, typename T>
 __device__ __forceinline__ void bc_ldg_grad_state(const BcK<T> &bc, const T *us, const T *n,
                                                   const T gl[ND][ND + 2], T gr[ND][ND + 2]) {
     constexpr int NV = ND + 2;
-    const bool zero = bc.type == B200_BC_SUP_IN_FA || bc.type == B200_BC_CHAR_RIEM_INV;
+    const bool zero = bc.type == B200_BC_SUP_IN_FA || bc.type == B200_BC_CHAR_RIEM_INV ||
+                      bc.type == B200_BC_SUB_IN_FRV || bc.type == B200_BC_SUB_OUT_FP;
 #pragma unroll
     for (int d = 0; d < ND; d++)
 #pragma unroll
@@ -321,7 +368,7 @@ bccflux_ns_kernel(int64_t n, int rs, b200::GasK<T> gas, T tau, BcK<T> bc, ScalVi
     }
 }
 
-bool bc_type_ok(int t) { return t >= B200_BC_SUP_IN_FA && t <= B200_BC_NO_SLP_ISOT_WALL; }
+bool bc_type_ok(int t) { return t >= B200_BC_SUP_IN_FA && t <= B200_BC_SUB_OUT_FP; }
 
 template <typename T>
 int bccflux_euler(int ndims, int64_t n, int rs, double gamma, const b200_bc_t *bc, T *ul_base,

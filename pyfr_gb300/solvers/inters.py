@@ -159,8 +159,13 @@ BC_OPTS = {
     'sup-in-fa': ['rho', 'p', 'u', 'v', 'w'],
     'char-riem-inv': ['rho', 'p', 'u', 'v', 'w'],
     'no-slp-isot-wall': ['u', 'v', 'w'],
+    'sub-in-frv': ['rho', 'u', 'v', 'w'],
+    'sub-out-fp': ['p'],
+    'sub-in-ftpttang': [],
     'sup-out-fn': [], 'slp-adia-wall': [], 'no-slp-adia-wall': [],
 }
+# Velocity components that default to zero
+_ZERO_UVW = {'no-slp-isot-wall', 'sub-in-frv'}
 EULER_BCS = {'sup-in-fa', 'sup-out-fn', 'slp-adia-wall', 'char-riem-inv'}
 
 
@@ -199,19 +204,35 @@ class BaseBCInters(BaseIntInters):
         for k in BC_OPTS[self.type]:
             if k in 'uvw' and 'uvw'.index(k) >= self.ndims:
                 continue
-            default = '0' if self.type == 'no-slp-isot-wall' else None
+            default = '0' if self.type in _ZERO_UVW and k in 'uvw' else None
             expr = cfg.get(cfgsect, k, default)
             if expr is None:
                 raise ValueError(f'{cfgsect}: {k} is required')
             vals[k] = float(npeval(str(expr), dict(self.c)))
+        def ev(k):
+            return float(npeval(cfg.get(cfgsect, k), dict(self.c)))
+
+        vc = []
         if self.type == 'no-slp-isot-wall':
-            vals['cpTw'] = float(npeval(cfg.get(cfgsect, 'cpTw'),
-                                        dict(self.c)))
+            vals['cpTw'] = ev('cpTw')
+        elif self.type == 'sub-in-ftpttang':
+            # Total state and inflow direction
+            # (pyfr/solvers/navstokes/inters.py:169-193)
+            vals['cpTt'], vals['pt'] = ev('cpTt'), ev('pt')
+            theta = ev('theta')*np.pi/180
+            vc = [np.cos(theta), np.sin(theta), 1.0]
+            if self.ndims == 3:
+                phi = ev('phi')*np.pi/180
+                vc = [vc[0]*np.sin(phi), vc[1]*np.sin(phi), np.cos(phi)]
+            vc = vc[:self.ndims]
         self.bcvals = vals
         self.bc = BC(type=BC_TYPES[self.type], rho=vals.get('rho', 0.0),
-                     p=vals.get('p', 0.0), cpTw=vals.get('cpTw', 0.0))
+                     p=vals.get('p', 0.0), cpTw=vals.get('cpTw', 0.0),
+                     cpTt=vals.get('cpTt', 0.0), pt=vals.get('pt', 0.0))
         for i, k in enumerate('uvw'[:self.ndims]):
             self.bc.u[i] = vals.get(k, 0.0)
+        for i, v in enumerate(vc):
+            self.bc.vc[i] = v
 
         # Memory order of the one side (pyfr/solvers/baseadvec/inters.py:90)
         scal = {t: e._scal_fpts for t, e in elemap.items()}

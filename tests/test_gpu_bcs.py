@@ -44,7 +44,7 @@ def _cfg(ndims, specs, rsolver='rusanov', precision='double', ns=False):
     for name, spec in specs.items():
         sect = f'soln-bcs-{name}'
         cfg.set(sect, 'type', spec['type'])
-        for k in ('rho', 'p', 'cpTw'):
+        for k in ('rho', 'p', 'cpTw', 'cpTt', 'pt', 'theta', 'phi'):
             if k in spec:
                 cfg.set(sect, k, spec[k])
         for k, v in zip('uvw', spec.get('u', [])):
@@ -85,14 +85,25 @@ def test_euler_bcs_rhs(built, types, rsolver):
 
 NS = [('no-slp-adia-wall', 'no-slp-adia-wall'),
       ('no-slp-isot-wall', 'slp-adia-wall'),
-      ('sup-in-fa', 'sup-out-fn'), ('char-riem-inv', 'no-slp-isot-wall')]
+      ('sup-in-fa', 'sup-out-fn'), ('char-riem-inv', 'no-slp-isot-wall'),
+      ('sub-in-frv', 'sub-out-fp'), ('sub-in-ftpttang', 'sup-out-fn')]
+
+# Total state of the sub-in-ftpttang inflow: cp*T_t, p_t and the direction
+# (theta, phi) in degrees
+TOTAL = dict(cpTt=3.9, pt=1.08, theta=20.0, phi=80.0)
+
+
+def _vc(theta, phi):
+    t, f = np.radians(theta), np.radians(phi)
+    return [np.cos(t)*np.sin(f), np.sin(t)*np.sin(f), np.cos(f)]
 
 
 @pytest.mark.parametrize('types', NS)
 def test_ns_bcs_rhs(built, types):
     from pyfr_gb300.solvers.system import NavierStokesSystem
-    specs = {'zlo': dict(type=types[0], cpTw=3.2, **FREE),
-             'zhi': dict(type=types[1], cpTw=3.6, **FREE)}
+    extra = dict(TOTAL, vc=_vc(TOTAL['theta'], TOTAL['phi']))
+    specs = {'zlo': dict(type=types[0], cpTw=3.2, **FREE, **extra),
+             'zhi': dict(type=types[1], cpTw=3.6, **FREE, **extra)}
     d, mesh = bc_disc('hex', (2, 2, 3), (True, True, False), specs, ns=True)
     cfg = _cfg(3, specs, ns=True)
     s = NavierStokesSystem(_backend(cfg), mesh, None, 2, cfg)
