@@ -69,8 +69,9 @@ def _save_plan_cache():
 
 
 def _destroy_handles(destroy, handles):
+    # (entries are handle tuples, failures (None) and piece lists)
     for h in handles.values():
-        if h is not None:
+        if isinstance(h, tuple):
             destroy(h[0])
     handles.clear()
 
@@ -149,15 +150,16 @@ class TensorMulKernels:
             raise NotSuitableError('tensor-core mul serves bf16x3 or tf32 '
                                    'FP32 data')
 
-    def _handle(self, *ops):
-        from pyfr_gb300.backend.base import NotSuitableError
+    MAX_ROWS = 256          # UMMA N limit of one handle (operator rows)
 
-        key = tuple(a.mid for a in ops)
+    def _handle_arrays(self, key, hosts):
+        """Handle of the K-concatenation of one or two FP64 operator blocks
+        (host arrays of equal row count), cached under ``key``; None when no
+        pipeline plan fits shared memory."""
         if key not in self._handles:
-            hosts = [np.ascontiguousarray(a._host, dtype=np.float64)
-                     for a in ops]
-            a1 = hosts[0]
-            a2 = hosts[1] if len(hosts) > 1 else None
+            a1 = np.ascontiguousarray(hosts[0], dtype=np.float64)
+            a2 = np.ascontiguousarray(hosts[1], dtype=np.float64) \
+                if len(hosts) > 1 else None
             h, smem = C.c_void_p(), C.c_size_t()
             pd = C.POINTER(C.c_double)
             lib = self.backend.lib
@@ -170,22 +172,141 @@ class TensorMulKernels:
             # image leaves no room for the ring, two terms and four products
             want = 3 if self.backend.split_products == 5 and not tf32 else 2
             self._handles[key] = None
-            for nterms in range(want, 1, -1):
-                try:
-                    plan = self._tuned_plan(args, tf32, nterms) \
-                        if self.backend.autotune else None
-                    lib.mul_tc_create_terms(*args, int(tf32), nterms,
-                                            *(plan or (0, 0)), C.byref(h),
-                                            C.byref(smem))
-                except B200Error:
-                    continue
-                self._handles[key] = (h.value, smem.value, hosts)
-                self._nterms[h.value] = nterms
-                break
-
-        if self._handles[key] is None:
-            raise NotSuitableError('operator too large for the tensor tiles')
+            if a1.shape[0] <= self.MAX_ROWS:
+                for nterms in range(want, 1, -1):
+                    try:
+                        plan = self._tuned_plan(args, tf32, nterms) \
+                            if self.backend.autotune else None
+                        lib.mul_tc_create_terms(*args, int(tf32), nterms,
+                                                *(plan or (0, 0)),
+                                                C.byref(h), C.byref(smem))
+                    except B200Error:
+                        continue
+                    self._handles[key] = (h.value, smem.value,
+                                          [a1] + ([a2] if a2 is not None
+                                                  else []))
+                    self._nterms[h.value] = nterms
+                    break
         return self._handles[key]
+
+    def _pieces(self, ops):
+        """Cover the operator [A1 | A2] (constant matrices of equal row
+        count) with handles that fit: a list of (r0, r1, blocks, handle),
+        blocks being up to two (operator index, k0, k1) column ranges.
+        The whole operator when it fits, else row ranges of at most
+        MAX_ROWS rows, each split along K into 32-aligned ranges until
+        every piece fits."""
+        from pyfr_gb300.backend.base import NotSuitableError
+
+        key = tuple(a.mid for a in ops)
+        if ('pieces', key) in self._handles:
+            return self._handles['pieces', key]
+
+        hosts = [np.ascontiguousarray(a._host, dtype=np.float64) for a in ops]
+        m = hosts[0].shape[0]
+        whole = [(i, 0, h.shape[1]) for i, h in enumerate(hosts)]
+        h = self._handle_arrays(key, hosts)
+        if h is not None:
+            pieces = [(0, m, whole, h)]
+        else:
+            pieces = []
+            nr = -(-m // self.MAX_ROWS)
+            step = -(-(-(-m // nr)) // 32)*32
+            for r0 in range(0, m, step):
+                r1 = min(m, r0 + step)
+                queue = list(whole)
+                while queue:
+                    cand = queue[:2]
+                    while True:
+                        subs = [hosts[i][r0:r1, k0:k1] for i, k0, k1 in cand]
+                        hk = key + ((r0, r1),) + tuple(cand)
+                        h = self._handle_arrays(hk, subs)
+                        if h is not None:
+                            break
+                        if len(cand) == 2:
+                            cand = cand[:1]
+                            continue
+                        i, k0, k1 = cand[0]
+                        if k1 - k0 <= 32:
+                            self._handles['pieces', key] = None
+                            raise NotSuitableError('operator too large for '
+                                                   'the tensor tiles')
+                        mid = k0 + -(-((k1 - k0)//2) // 32)*32
+                        queue[0:1] = [(i, k0, mid), (i, mid, k1)]
+                        cand = queue[:1]
+                    pieces.append((r0, r1, cand, h))
+                    del queue[:len(cand)]
+        self._handles['pieces', key] = pieces
+        return pieces
+
+    def _build(self, ops, bs, out, alpha, beta, rowscale=None, nbatch=1,
+               bstrides=(0, 0), cstride=0, meta=None):
+        """The kernel applying [A1 | A2] to [B1; B2] piece by piece: each row
+        range's first piece stores (or adds, with beta = 1), the others
+        add; the row scale applies to every piece (it is linear)."""
+        from pyfr_gb300.backend.base import NotSuitableError
+
+        pieces = self._pieces(ops)
+        if pieces is None:
+            raise NotSuitableError('operator too large for the tensor tiles')
+        isz = 4
+        nvars = ldr = 0
+        if rowscale is not None:
+            nvars, ldr = out.ioshape[1], rowscale.leaddim
+        arglist, seen = [], set()
+        for r0, r1, blocks, (h, smem, hosts) in pieces:
+            first = r0 not in seen
+            seen.add(r0)
+            bp = [bs[i].data + k0*bs[i].leaddim*isz for i, k0, _ in blocks]
+            a = MulArgs(b1=bp[0], ldb1=bs[blocks[0][0]].leaddim,
+                        b2=bp[1] if len(bp) > 1 else None,
+                        ldb2=bs[blocks[1][0]].leaddim if len(bp) > 1 else 0,
+                        c=out.data + r0*out.leaddim*isz, ldc=out.leaddim,
+                        ncol=out.ncol, nbatch=nbatch,
+                        bstride1=bstrides[blocks[0][0]],
+                        bstride2=bstrides[blocks[1][0]] if len(bp) > 1 else 0,
+                        cstride=cstride, alpha=alpha,
+                        beta=beta if first else 1.0,
+                        rowscale=(rowscale.data + r0*ldr*isz
+                                  if rowscale is not None else None),
+                        ldr=ldr, nvars=nvars)
+            arglist.append((h, a))
+
+        meta = dict(meta or {}, smem=max(p[3][1] for p in pieces),
+                    pieces=len(pieces))
+        if len(pieces) == 1:
+            h, a = arglist[0]
+            return self._kernel(h, a, list(ops) + list(bs) + [out] +
+                                ([rowscale] if rowscale is not None else []),
+                                meta)
+
+        be = self.backend
+        for h, a in arglist:
+            a.err = be.status_word
+            a.products = self._products(self._nterms.get(h, 2))
+        meta['products'] = min(a.products for _, a in arglist)
+        if be.mul_precision == 'tf32':
+            meta['impl'] = meta['impl'].replace('bf16x3', 'tf32')
+        fn = be.lib.mul_bf16x3_apply
+        calls = [(h, C.addressof(a)) for h, a in arglist]
+
+        def run(stream):
+            for h, pa in calls:
+                fn(h, pa, stream)
+
+        k = Kernel(run, mats=list(ops) + list(bs) + [out] +
+                   ([rowscale] if rowscale is not None else []),
+                   misc=[a for _, a in arglist], name='mul', meta=meta)
+        return k
+
+    def _handle(self, *ops):
+        from pyfr_gb300.backend.base import NotSuitableError
+
+        key = tuple(a.mid for a in ops)
+        h = self._handle_arrays(key, [a._host for a in ops])
+        if h is None:
+            raise NotSuitableError('operator too large for the tensor tiles')
+        return h
 
     @staticmethod
     def _aligned(*mats):
@@ -292,12 +413,10 @@ class TensorMulKernels:
         if beta not in (0.0, 1.0):
             raise NotSuitableError('the tensor-core epilogue stores or adds')
 
-        h, smem, (host,) = self._handle(a)
-        args = MulArgs(b1=b.data, ldb1=b.leaddim, c=out.data, ldc=out.leaddim,
-                       ncol=b.ncol, nbatch=1, alpha=alpha, beta=beta)
-        return self._kernel(h, args, [a, b, out],
-                            dict(a=a, b=b, out=out, alpha=alpha, beta=beta,
-                                 op=host, impl='bf16x3', smem=smem))
+        return self._build([a], [b], out, alpha, beta,
+                           meta=dict(a=a, b=b, out=out, alpha=alpha,
+                                     beta=beta, op=np.asarray(a._host),
+                                     impl='bf16x3'))
 
     def mul_cat(self, a1, b1, a2, b2, out, alpha=1.0, beta=0.0,
                 rowscale=None):
@@ -321,18 +440,13 @@ class TensorMulKernels:
             if rowscale.dtype != np.float32:
                 raise ValueError('The row scale must be FP32')
 
-        h, smem, (h1, h2) = self._handle(a1, a2)
-        args = MulArgs(b1=b1.data, ldb1=b1.leaddim, b2=b2.data,
-                       ldb2=b2.leaddim, c=out.data, ldc=out.leaddim,
-                       ncol=b1.ncol, nbatch=1, alpha=alpha, beta=beta,
-                       rowscale=rowscale.data if rowscale is not None else None,
-                       ldr=ldr, nvars=nvars)
-        mats = [a1, b1, a2, b2, out] + ([rowscale] if rowscale is not None else [])
-        return self._kernel(h, args, mats,
-                            dict(a=a1, b=b1, a2=a2, b2=b2, out=out,
-                                 alpha=alpha, beta=beta, op=h1, op2=h2,
-                                 rowscale=rowscale, impl='bf16x3-cat',
-                                 smem=smem))
+        return self._build([a1, a2], [b1, b2], out, alpha, beta,
+                           rowscale=rowscale,
+                           meta=dict(a=a1, b=b1, a2=a2, b2=b2, out=out,
+                                     alpha=alpha, beta=beta,
+                                     op=np.asarray(a1._host),
+                                     op2=np.asarray(a2._host),
+                                     rowscale=rowscale, impl='bf16x3-cat'))
 
     def mul_batched(self, a, b, out, nbatch, alpha=1.0, beta=0.0):
         from pyfr_gb300.backend.base import NotSuitableError
@@ -348,11 +462,8 @@ class TensorMulKernels:
         if beta not in (0.0, 1.0):
             raise NotSuitableError('the tensor-core epilogue stores or adds')
 
-        h, smem, (host,) = self._handle(a)
-        args = MulArgs(b1=b.data, ldb1=b.leaddim, c=out.data, ldc=out.leaddim,
-                       ncol=b.ncol, nbatch=nbatch, bstride1=k*b.leaddim,
-                       cstride=m*out.leaddim, alpha=alpha, beta=beta)
-        return self._kernel(h, args, [a, b, out],
-                            dict(a=a, b=b, out=out, alpha=alpha, beta=beta,
-                                 op=host, nbatch=nbatch,
-                                 impl='bf16x3-batched', smem=smem))
+        return self._build([a], [b], out, alpha, beta, nbatch=nbatch,
+                           bstrides=(k*b.leaddim, 0), cstride=m*out.leaddim,
+                           meta=dict(a=a, b=b, out=out, alpha=alpha,
+                                     beta=beta, op=np.asarray(a._host),
+                                     nbatch=nbatch, impl='bf16x3-batched'))

@@ -24,14 +24,16 @@ def built():
 
 
 @pytest.mark.parametrize('key', ['hex_p3_gauss-legendre', 'quad_p3_gauss-legendre',
-                                 'hex_p2_gauss-legendre'])
+                                 'hex_p2_gauss-legendre',
+                                 'hex_p4_gauss-legendre'])
 @pytest.mark.parametrize('opname', ['m0', 'M132', 'm3', 'M460', 'm6'])
 @pytest.mark.parametrize('prec', ['bf16x3-3', 'bf16x3-4', 'tf32'])
 def test_mul_tensor_cores(built, golden, key, opname, prec):
     """tcgen05 operator apply against an FP64 product.  Split BF16 with
     three products is bounded by ~2^-16 sum|a||b| (bound 1e-4), with four
     by ~2^-17 (bound 5e-5); TF32 rounds both operands to 11 significant
-    bits, ~2^-10 sum|a||b| (bound 2e-3)."""
+    bits, ~2^-10 sum|a||b| (bound 2e-3).  Operators that do not fit one
+    handle (p = 4: 375 rows, or K = 375) run as row and K pieces."""
     from pyfr_gb300.backend import B200Backend
     from pyfr_gb300.inifile import Inifile
     a = golden['operators'][f'{key}/{opname}']
@@ -101,18 +103,21 @@ def test_mul_three_term_operator(built, golden, key, opname):
     assert np.all(np.abs(C.get() - ref) <= bound)
 
 
-@pytest.mark.parametrize('neles', [77, 1000])
-def test_mul_bf16x3_cat_rowscale(built, golden, neles):
+@pytest.mark.parametrize('neles,order,nprod', [(77, 3, '3'), (1000, 3, '3'),
+                                              (333, 4, '5'), (333, 3, '5')])
+def test_mul_bf16x3_cat_rowscale(built, golden, neles, order, nprod):
     """Fused apply out = alpha*S*(A1@B1 + A2@B2) (+ out): the divergence,
-    correction and negdivconf of the reference in one kernel."""
+    correction and negdivconf of the reference in one kernel (at p = 4 in
+    K pieces, each scaled and the later ones added)."""
     from pyfr_gb300.backend import B200Backend
     from pyfr_gb300.inifile import Inifile
     ops = golden['operators']
-    a1 = ops['hex_p3_gauss-legendre/M132']
-    a2 = ops['hex_p3_gauss-legendre/m3']
+    a1 = ops[f'hex_p{order}_gauss-legendre/M132']
+    a2 = ops[f'hex_p{order}_gauss-legendre/m3']
     cfg = Inifile()
     cfg.set('backend', 'precision', 'single')
     cfg.set('backend-b200', 'mul-precision', 'bf16x3')
+    cfg.set('backend-b200', 'split-products', nprod)
     be = B200Backend(cfg)
     rng = np.random.default_rng(11)
     nv = 5
@@ -142,11 +147,14 @@ def test_mul_bf16x3_cat_rowscale(built, golden, neles):
                       1e-6*np.abs(ref))
 
 
-def test_mul_bf16x3_batched(built, golden):
+@pytest.mark.parametrize('op', ['hex_p3_gauss-legendre/m0',
+                                'hex_p4_gauss-legendre/m0',
+                                'hex_p4_gauss-legendre/m6'])
+def test_mul_bf16x3_batched(built, golden, op):
     """ndims products of one operator as one launch over row slices."""
     from pyfr_gb300.backend import B200Backend
     from pyfr_gb300.inifile import Inifile
-    a = golden['operators']['hex_p3_gauss-legendre/m0']
+    a = golden['operators'][op]
     cfg = Inifile()
     cfg.set('backend', 'precision', 'single')
     cfg.set('backend-b200', 'mul-precision', 'bf16x3')
@@ -390,3 +398,23 @@ def test_autotuned_plan_same_result(built, golden, tmp_path, monkeypatch):
     assert np.array_equal(out['true'], out['false'])
     plans = json.loads((tmp_path / 'mul-plans.json').read_text())
     assert any(k.endswith('|192|64|0') for k in plans)
+
+
+def test_chosen_form_order4(built):
+    """The fused chosen-form graph at p = 4 (operators in pieces) against
+    FP64 on the TGV."""
+    from pyfr_gb300.backend import B200Backend
+    from pyfr_gb300.cases import ns_tgv
+    from pyfr_gb300.integrators import MixedRKIntegrator, RKVdH2Integrator
+    from pyfr_gb300.solvers.system import NavierStokesSystem
+    cfg, mesh = ns_tgv(n=4, order=4, dt=2e-4)
+    plain = RKVdH2Integrator(B200Backend(cfg), NavierStokesSystem, mesh, cfg)
+    cfg, mesh = ns_tgv(n=4, order=4, dt=2e-4, precision='single')
+    cfg.set('backend-b200', 'mul-precision', 'bf16x3')
+    cfg.set('backend-b200', 'split-products', '5')
+    chosen = MixedRKIntegrator(B200Backend(cfg), NavierStokesSystem, mesh,
+                               cfg)
+    plain.run_steps(10)
+    chosen.run_steps(10)
+    (a,), (b,) = chosen.soln, plain.soln
+    assert np.linalg.norm(a - b)/np.linalg.norm(b) <= 1e-6
