@@ -606,8 +606,9 @@ def run_mixed(args, dist):
         out, solns = {}, {}
         for form in ('plain', 'chosen', 'tf32'):
             prec = 'double' if form == 'plain' else 'single'
-            cfg, mesh = euler_mixed(n=args.mixed_n, order=3, kinds=kinds,
-                                    dt=args.mixed_dt, precision=prec)
+            cfg, mesh = euler_mixed(n=args.mixed_n, order=args.mixed_order,
+                                    kinds=kinds, dt=args.mixed_dt,
+                                    precision=prec)
             cfg.set('backend-b200', 'device-id', str(args.local_rank))
             icls = RKVdH2Integrator
             if form == 'chosen':
@@ -707,6 +708,7 @@ def main():
                     help='time the mixed hexahedron/prism and '
                     'prism/tetrahedron meshes instead')
     ap.add_argument('--mixed-n', type=int, default=32)
+    ap.add_argument('--mixed-order', type=int, default=3)
     ap.add_argument('--mixed-dt', type=float, default=1e-3)
     ap.add_argument('--ensemble', action='store_true',
                     help='the batching configuration\'s ensemble of 2-D '
@@ -776,7 +778,8 @@ def main():
                 'config': {'workload': f'3-D Euler, periodic '
                                        f'{args.mixed_n}^3-cell box of '
                                        'hexahedra+prisms and of '
-                                       'prisms+tetrahedra, p=3, density '
+                                       f'prisms+tetrahedra, '
+                                       f'p={args.mixed_order}, density '
                                        'wave, one CUDA graph per RK45 step',
                            'dt': args.mixed_dt},
                 'data': 'synthetic'} | r))
