@@ -258,6 +258,56 @@ int b200_bccflux_ns_f32(int ndims, int64_t n, int rsolver, const b200_gas_t *gas
                         const float *gl_base, const void *gl_map, const void *gl_rstr,
                         int ix64, const float *nl, int64_t ldn, void *stream);
 
+/* ---- entropy filter -------------------------------------------------- */
+/* Shock capturing by the bounds-preserving entropy filter
+ * (pyfr/solvers/baseadvec/entfilter.py:5-213).  Elements of one type:
+ * ndims, nupts solution points (quads of order 1-5, hexes of order 1-4),
+ * nfpts flux points on nfaces faces, nefpts = nupts (+ nfpts when the flux
+ * points are not solution points); bounds d_min, p_min, entropy tolerance
+ * e_tol; bisection tolerance f_tol and at most niters steps. */
+typedef struct {
+    int ndims, nupts, nfpts, nefpts, nfaces, order;
+    int fpts_in_upts, linearise, niters;
+    double gamma, d_min, p_min, e_tol, f_tol;
+} b200_ef_t;
+/* Filter the solution u (nupts x nvars x neles AoSoA) in place against
+ * the smallest entropy of each element's faces entmin (nfaces x neles),
+ * then store the element's new minimum in entmin and its filter strength
+ * in ef_filter; vdm (nefpts x nupts) modal->nodal, invvdm (nupts x nupts)
+ * nodal->modal, m0 (nfpts x nupts), mean_wts (nupts x neles, leading
+ * dimension ldw), degs (nupts device ints, the degree of each mode);
+ * pyfr/solvers/euler/kernels/entropyfilter.mako:153-221. */
+int b200_entropyfilter_f64(const b200_ef_t *p, int64_t neles, double *u, int64_t ldu,
+                           double *entmin, int64_t lde, double *ef_filter, const double *vdm,
+                           const double *invvdm, const double *m0, const double *mean_wts,
+                           int64_t ldw, const int *degs, void *stream);
+int b200_entropyfilter_f32(const b200_ef_t *p, int64_t neles, float *u, int64_t ldu,
+                           float *entmin, int64_t lde, float *ef_filter, const float *vdm,
+                           const float *invvdm, const float *m0, const float *mean_wts,
+                           int64_t ldw, const int *degs, void *stream);
+/* Minimum entropy of each element on all its faces;
+ * pyfr/solvers/euler/kernels/entropylocal.mako:5-40. */
+int b200_entropylocal_f64(const b200_ef_t *p, int64_t neles, const double *u, int64_t ldu,
+                          double *entmin, int64_t lde, const double *m0, void *stream);
+int b200_entropylocal_f32(const b200_ef_t *p, int64_t neles, const float *u, int64_t ldu,
+                          float *entmin, int64_t lde, const float *m0, void *stream);
+/* Both faces of each interface take the smaller entropy (views of one
+ * value per face); pyfr/solvers/baseadvec/kernels/intcent.mako:4-8. */
+int b200_intcent_f64(int64_t n, double *lbase, const void *lmap, double *rbase,
+                     const void *rmap, int ix64, void *stream);
+int b200_intcent_f32(int64_t n, float *lbase, const void *lmap, float *rbase, const void *rmap,
+                     int ix64, void *stream);
+/* Boundary faces take the smaller of their value and the entropy of the
+ * boundary ghost state at each of their flux points (ent: a view mapping
+ * every flux point of a face to the face's value);
+ * pyfr/solvers/euler/kernels/bccent.mako:7-25. */
+int b200_bccent_f64(int ndims, int64_t n, double gamma, const b200_bc_t *bc,
+                    const double *ul_base, const void *ul_map, double *ent_base,
+                    const void *ent_map, int ix64, const double *nl, int64_t ldn, void *stream);
+int b200_bccent_f32(int ndims, int64_t n, double gamma, const b200_bc_t *bc,
+                    const float *ul_base, const void *ul_map, float *ent_base,
+                    const void *ent_map, int ix64, const float *nl, int64_t ldn, void *stream);
+
 /* Largest reference-space wave speed of each element for the CFL
  * controller: wspd[e] = max over the solution points of
  * sum_i |sum_j (S_ij/|J|) v_j| + c*sqrt(sum_j (S_ij/|J|)^2);

@@ -369,6 +369,7 @@ class Discretisation:
         self.ploc_f = np.einsum('pv,ved->pde',
                                 shape_values(self.fpts, self.ndims), self.verts)
 
+        self.faces_l, self.faces_r = np.asarray(lhs), np.asarray(rhs)
         self._pair(np.asarray(lhs), np.asarray(rhs), periods)
 
         # Boundaries: bcs is a sequence of (faces (n, 2) of (element, face),
@@ -820,6 +821,172 @@ class MixedDiscretisation:
             out[et] = flat[off:off + n].reshape(shp)
             off += n
         return out
+
+
+# ---------------------------------------------------------------------------
+# Entropy filter (pyfr/solvers/baseadvec/entfilter.py,
+# pyfr/solvers/euler/kernels/{entropy,entropylocal,entropyfilter}.mako)
+# ---------------------------------------------------------------------------
+
+def entropy_state(u, gamma, big):
+    """Density, pressure and entropy function of states u (nvars, ...)."""
+    nd = u.shape[0] - 2
+    d = u[0]
+    with np.errstate(divide='ignore', invalid='ignore'):
+        rcpd = 1/d
+        p = (gamma - 1)*(u[-1] - 0.5*rcpd*np.sum(u[1:nd + 1]**2, axis=0))
+        e = np.where((d > 0) & (p > 0), p*np.abs(rcpd)**gamma, big)
+    return d, p, e
+
+
+class EntropyFilterOracle:
+    """The entropy filter over one element type of a Discretisation:
+    ops = dict(vdm (nefpts, nupts), invvdm (nupts, nupts: nodal -> modal),
+    m0 or None, degs, mean_wts (nupts, neles)); opts = d_min, p_min, e_tol,
+    f_tol, niters, order, linearise; bcs as the Discretisation's, with
+    their ghost states."""
+
+    def __init__(self, disc, ops, opts, gamma, big=np.finfo(float).max):
+        self.d, self.ops, self.o, self.gamma, self.big = disc, ops, opts, \
+            gamma, big
+        self.nfaces = len(disc.facefpts)
+        self.entmin = np.full((self.nfaces, disc.neles), -big)
+
+    def _minima(self, ue):
+        """ue (nupts, nvars) -> (dmin, pmin, emin) over the points (and the
+        flux points when they are not solution points)."""
+        pts = ue
+        if self.ops['m0'] is not None:
+            pts = np.vstack([ue, self.ops['m0'] @ ue])
+        d, p, e = entropy_state(pts.T, self.gamma, self.big)
+        return d.min(), p.min(), e.min()
+
+    def _bad(self, d, p, e, entmin):
+        o = self.o
+        return d < o['d_min'] or p < o['p_min'] or e < entmin - o['e_tol']
+
+    def _filter_point(self, up, f):
+        ui = up[0].copy()
+        v = v2 = 1.0
+        for k in range(1, self.o['order'] + 1):
+            v2 *= v*v*f
+            v *= f
+            ui += v2*up[k]
+        return entropy_state(ui[:, None], self.gamma, self.big)
+
+    def filter_element(self, ue, e):
+        """Filter one element's solution (nupts, nvars) in place; returns
+        (filter strength, new minimum entropy)."""
+        o, ops = self.o, self.ops
+        entmin = self.entmin[:, e].min()
+        dmin, pmin, emin = self._minima(ue)
+        uavg = ops['mean_wts'][:, e] @ ue
+        f = 1.0
+        if not o['linearise'] and self._bad(dmin, pmin, emin, entmin):
+            um = ops['invvdm'] @ ue
+            degs = ops['degs']
+            for i in range(ops['vdm'].shape[0]):
+                up = np.zeros((o['order'] + 1, ue.shape[1]))
+                for m in range(len(degs)):
+                    up[degs[m]] += ops['vdm'][i, m]*um[m]
+                d, p, s = (x[0] for x in self._filter_point(up, f))
+                if self._bad(d, p, s, entmin):
+                    fhi, flo = f, 0.0
+                    it = 0
+                    while it < o['niters'] and fhi - flo > o['f_tol']:
+                        fnew = 0.5*(flo + fhi)
+                        d, p, s = (x[0] for x in self._filter_point(up, fnew))
+                        if self._bad(d, p, s, entmin):
+                            fhi = fnew
+                        else:
+                            flo = fnew
+                        it += 1
+                    f = flo
+            ffac = np.empty(o['order'] + 1)
+            v = ffac[0] = 1.0
+            for k in range(1, o['order'] + 1):
+                ffac[k] = ffac[k - 1]*v*v*f
+                v *= f
+            nup = ue.shape[0]
+            ue[:] = (ops['vdm'][:nup]*ffac[degs][None, :]) @ um
+            ue += uavg - ops['mean_wts'][:, e] @ ue
+            dmin, pmin, emin = self._minima(ue)
+
+        if self._bad(dmin, pmin, emin, entmin):
+            davg, pavg, eavg = (x[0] for x in entropy_state(uavg[:, None],
+                                                            self.gamma,
+                                                            self.big))
+            for vmin, vavg, bound, nv in (
+                    ('d', davg, o['d_min'], 1), ('p', pavg, o['p_min'], None),
+                    ('e', eavg, entmin - o['e_tol'], None)):
+                cur = dict(d=dmin, p=pmin, e=emin)[vmin]
+                if cur < bound:
+                    alpha = min(max((cur - bound)/(cur - vavg), 0.0), 1.0)
+                    f = min(f, 1.0 - alpha)
+                    sl = slice(0, nv)
+                    ue[:, sl] += alpha*(uavg[sl] - ue[:, sl])
+                    dmin, pmin, emin = self._minima(ue)
+        self.entmin[:, e] = emin
+        return f, emin
+
+    def filter(self, u):
+        """Filter every element of u (nupts, nvars, neles) in place."""
+        fs = np.empty(u.shape[2])
+        for e in range(u.shape[2]):
+            ue = u[:, :, e].copy()
+            fs[e], _ = self.filter_element(ue, e)
+            u[:, :, e] = ue
+        return fs
+
+    def local(self, u):
+        for e in range(u.shape[2]):
+            self.entmin[:, e] = self._minima(u[:, :, e])[2]
+
+    def exchange(self):
+        """Interfaces take the smaller of their two faces' minima."""
+        fl, fr = self.d.faces_l, self.d.faces_r
+        m = np.minimum(self.entmin[fl[:, 1], fl[:, 0]],
+                       self.entmin[fr[:, 1], fr[:, 0]])
+        self.entmin[fl[:, 1], fl[:, 0]] = m
+        self.entmin[fr[:, 1], fr[:, 0]] = m
+
+    def exchange_bcs(self, u):
+        """Boundary faces take the smaller of their minimum and the entropy
+        of the ghost state at their flux points."""
+        uf = Discretisation.apply(self.d.ops['M0'], u)
+        for fp, ee, n, bmag, spec in self.d.bcs:
+            ub = uf[fp, :, ee].T
+            ug = bc_rsolve_state(spec, ub, n, self.gamma)
+            _, _, s = entropy_state(ug, self.gamma, self.big)
+            # faces of the points: the face whose point list holds fp
+            face = np.array([next(f for f, pts in enumerate(self.d.facefpts)
+                                  if q in pts) for q in fp])
+            np.minimum.at(self.entmin, (face, ee), s)
+
+
+def rk45_step_ef(rhs, u, dt, ef):
+    """rk45_step with the entropy filter: every right-hand side filters its
+    input register in place first and exchanges the new minima, and the
+    step ends with a filter of the result."""
+    def frhs(x):
+        ef.filter(x)
+        ef.exchange()
+        ef.exchange_bcs(x)
+        return rhs(x)
+
+    r1, r2 = u.copy(), u
+    ns = len(RK45_B)
+    for i in range(ns):
+        if i == 0:
+            r2 = frhs(r1)
+        else:
+            r2 = frhs(r2)
+        if i < ns - 1:
+            r1, r2 = r1 + dt*RK45_B[i]*r2, r1 + dt*RK45_A[i]*r2
+        else:
+            r1 = r1 + dt*RK45_B[i]*r2
+    ef.filter(r1)
+    return r1
 
 
 # ---------------------------------------------------------------------------

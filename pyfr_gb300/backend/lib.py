@@ -51,6 +51,15 @@ class BC(C.Structure):
                 ('cpTw', f64), ('cpTt', f64), ('pt', f64), ('vc', f64*3)]
 
 
+class EF(C.Structure):
+    """``b200_ef_t``"""
+    _fields_ = [('ndims', i32), ('nupts', i32), ('nfpts', i32),
+                ('nefpts', i32), ('nfaces', i32), ('order', i32),
+                ('fpts_in_upts', i32), ('linearise', i32), ('niters', i32),
+                ('gamma', f64), ('d_min', f64), ('p_min', f64), ('e_tol', f64),
+                ('f_tol', f64)]
+
+
 def _sig_pointwise(fp):
     return {
         'tflux_euler': [i32, i32, i64, i32, f64, vp, i64, vp, i64, vp, i64, vp,
@@ -81,6 +90,12 @@ def _sig_pointwise(fp):
                    vp],
         'bccflux_ns': [i32, i64, i32, C.POINTER(Gas), f64, C.POINTER(BC), vp,
                        vp, vp, vp, vp, i32, vp, i64, vp],
+        'bccent': [i32, i64, f64, C.POINTER(BC), vp, vp, vp, vp, i32, vp, i64,
+                   vp],
+        'entropyfilter': [C.POINTER(EF), i64, vp, i64, vp, i64, vp, vp, vp,
+                          vp, vp, i64, vp, vp],
+        'entropylocal': [C.POINTER(EF), i64, vp, i64, vp, i64, vp, vp],
+        'intcent': [i64, vp, vp, vp, vp, i32, vp],
         'reduce_max': [i64, vp, vp, vp, vp],
     }
 

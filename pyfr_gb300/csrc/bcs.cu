@@ -368,6 +368,40 @@ bccflux_ns_kernel(int64_t n, int rs, b200::GasK<T> gas, T tau, BcK<T> bc, ScalVi
     }
 }
 
+// Order-preserving integer key of a non-negative value (its bit pattern)
+__device__ __forceinline__ void atomic_min_nonneg(double *a, double v) {
+    atomicMin(reinterpret_cast<unsigned long long *>(a),
+              (unsigned long long)__double_as_longlong(v));
+}
+__device__ __forceinline__ void atomic_min_nonneg(float *a, float v) {
+    atomicMin(reinterpret_cast<unsigned int *>(a), __float_as_uint(v));
+}
+
+template <int ND, typename T>
+__global__ void __launch_bounds__(BC_BLOCK)
+bccent_kernel(int64_t n, T gamma, BcK<T> bc, ScalView<T> vl, ScalView<T> ve, int ix64,
+              const T *__restrict__ nl, int64_t ldn, T big) {
+    constexpr int NV = ND + 2;
+    const int64_t i = (int64_t)blockIdx.x * BC_BLOCK + threadIdx.x;
+    if (i >= n) return;
+    const T *pl = vl.base + b200::load_ix(vl.map, ix64, i);
+    T *pe = ve.base + b200::load_ix(ve.map, ix64, i);
+    T ul[NV], ur[NV], nn[ND];
+#pragma unroll
+    for (int v = 0; v < NV; v++) ul[v] = pl[v * B200_SOASZ];
+    unit_normal<ND, T>(nl, ldn, i, nn);
+    bc_rsolve_state<ND, T>(bc, gamma, ul, nn, ur);
+    // Entropy p rho^-gamma of the ghost state (largest value when it has
+    // no positive density and pressure)
+    const T rcpd = T(1) / ur[0];
+    T k2 = 0;
+#pragma unroll
+    for (int d = 0; d < ND; d++) k2 += ur[d + 1] * ur[d + 1];
+    const T p = (gamma - T(1)) * (ur[NV - 1] - T(0.5) * rcpd * k2);
+    const T e = (ur[0] > 0 && p > 0) ? p * pow(rcpd, gamma) : big;
+    atomic_min_nonneg(pe, e);
+}
+
 bool bc_type_ok(int t) { return t >= B200_BC_SUP_IN_FA && t <= B200_BC_SUB_OUT_FP; }
 
 template <typename T>
@@ -436,9 +470,44 @@ int bccflux_ns(int ndims, int64_t n, int rs, const b200_gas_t *gas, double tau,
     return B200_OK;
 }
 
+template <typename T>
+int bccent(int ndims, int64_t n, double gamma, const b200_bc_t *bc, const T *ul_base,
+           const void *ul_map, T *ent_base, const void *ent_map, int ix64, const T *nl,
+           int64_t ldn, cudaStream_t st) {
+    if (n <= 0) return B200_OK;
+    if (!bc || !bc_type_ok(bc->type))
+        return b200::set_error(B200_ERR_ARG, "bccent: bad boundary type");
+    const auto k = bc_consts<T>(*bc, gamma);
+    ScalView<T> l{const_cast<T *>(ul_base), ul_map}, e{ent_base, ent_map};
+    const T big = sizeof(T) == 8 ? (T)1.7976931348623157e308 : (T)3.4028234663852886e38;
+    const unsigned grid = b200::ceil_div(n, BC_BLOCK);
+    if (ndims == 2)
+        bccent_kernel<2, T><<<grid, BC_BLOCK, 0, st>>>(n, (T)gamma, k, l, e, ix64, nl, ldn, big);
+    else if (ndims == 3)
+        bccent_kernel<3, T><<<grid, BC_BLOCK, 0, st>>>(n, (T)gamma, k, l, e, ix64, nl, ldn, big);
+    else
+        return b200::set_error(B200_ERR_ARG, "bccent: ndims must be 2 or 3");
+    B200_CHECK_LAUNCH("bccent");
+    return B200_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+int b200_bccent_f64(int ndims, int64_t n, double gamma, const b200_bc_t *bc,
+                    const double *ul_base, const void *ul_map, double *ent_base,
+                    const void *ent_map, int ix64, const double *nl, int64_t ldn, void *stream) {
+    return bccent<double>(ndims, n, gamma, bc, ul_base, ul_map, ent_base, ent_map, ix64, nl, ldn,
+                          (cudaStream_t)stream);
+}
+
+int b200_bccent_f32(int ndims, int64_t n, double gamma, const b200_bc_t *bc,
+                    const float *ul_base, const void *ul_map, float *ent_base,
+                    const void *ent_map, int ix64, const float *nl, int64_t ldn, void *stream) {
+    return bccent<float>(ndims, n, gamma, bc, ul_base, ul_map, ent_base, ent_map, ix64, nl, ldn,
+                         (cudaStream_t)stream);
+}
 
 int b200_bccflux_euler_f64(int ndims, int64_t n, int rsolver, double gamma, const b200_bc_t *bc,
                            double *ul_base, const void *ul_map, int ix64, const double *nl,

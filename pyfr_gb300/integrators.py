@@ -73,6 +73,11 @@ class RKVdH2Integrator:
         self._setup_registers(initsoln)
         backend.commit()
 
+        # Entropy filter: the starting minima (the integrator's preproc,
+        # pyfr/integrators/explicit/base.py:39)
+        for k in self.system.preproc_kernels(0):
+            k.run(backend.stream)
+
         self.tcurr = cfg.getfloat(sect, 'tstart', 0.0)
         # (the CFL controller computes its own first step size)
         self.dt = cfg.getfloat(sect, 'dt', 0.0) if self.needs_cfl else \
@@ -187,6 +192,8 @@ class RKVdH2Integrator:
                 k.bind(dt=dt)
                 kl.append(k)
             r1, r2 = r2, r1
+        # (the entropy filter's postproc of the new solution)
+        kl.extend(self.system.postproc_kernels(r2))
         return kl, ((r2, *rs) if rs else (r2,))
 
     def _enqueue_step(self, t, dt, idx, stream):
@@ -373,6 +380,10 @@ class MixedRKIntegrator(RKVdH2Integrator):
         if backend.fpdtype != np.float32:
             raise ValueError('The mixed-precision integrator needs a '
                              'single-precision backend')
+        if cfg.get('solver', 'shock-capturing', 'none') != 'none':
+            raise NotImplementedError('Shock capturing needs the FP64 '
+                                      'solution in the system (the plain '
+                                      'integrator)')
         super().__init__(backend, systemcls, mesh, cfg, initsoln)
 
     def _make_system(self, backend, systemcls, mesh, initsoln, cfg):

@@ -129,6 +129,19 @@ class BaseSystem:
 
         self.backend.commit()
         self._gen_kernels()
+
+        # Shock capturing by the entropy filter
+        # (pyfr/solvers/baseadvec/system.py:36-44)
+        sc = self.cfg.get('solver', 'shock-capturing', 'none')
+        if sc not in ('none', 'entropy-filter'):
+            raise NotImplementedError(f'Shock capturing {sc!r} is not '
+                                      'provided')
+        self._ef = None
+        if sc == 'entropy-filter':
+            from pyfr_gb300.solvers.entfilter import EntropyFilter
+            self._ef = EntropyFilter(self, self.cfg)
+            self._ef.add_kernels(self._kernels, self._ktags)
+
         # Maximum wave speed over each element type
         # (pyfr/solvers/baseadvec/system.py:48-52)
         if self._needs_cfl:
@@ -203,6 +216,22 @@ class BaseSystem:
         for g in self._rhs_graphs_cached(uinbank, foutbank):
             self.backend.run_graph(g)
 
+    def preproc_kernels(self, uinbank):
+        """Before the first step: filter, then every element's and face's
+        minimum entropy (pyfr/solvers/baseadvec/entfilter.py:160-194)."""
+        if not self._ef:
+            return []
+        k = self._get_kernels(uinbank, None)
+        return (k['eles/entropy_filter'] + k['eles/local_entropy'] +
+                k['eles/disu'] + k['iint/comm_entropy'] +
+                k['bcint/comm_entropy'])
+
+    def postproc_kernels(self, uinbank):
+        """After every step: filter the new solution."""
+        if not self._ef:
+            return []
+        return self._get_kernels(uinbank, None)['eles/entropy_filter']
+
     def compute_max_wavespeed(self, uinbank):
         """Largest element wave speed of the solution in bank uinbank
         (pyfr/solvers/baseadvec/system.py:157-161)."""
@@ -232,9 +261,17 @@ class EulerSystem(BaseSystem):
             return self._kdeps(k, dk, *names)
 
         g_intf = self.backend.graph()
-        g_intf.add_all(k['eles/disu'])
+        # (with the entropy filter: filter the input first, then exchange
+        # the new face minima; pyfr/solvers/baseadvec/system.py:58-90)
+        g_intf.add_all(k['eles/entropy_filter'])
+        for l in k['eles/disu']:
+            g_intf.add(l, deps=deps(l, 'eles/entropy_filter'))
+        g_intf.add_all(k['iint/comm_entropy'], deps=k['eles/entropy_filter'])
+        g_intf.add_all(k['bcint/comm_entropy'],
+                       deps=k['eles/disu'] + k['iint/comm_entropy'])
         g_intf.add_all(k['iint/comm_flux'], deps=k['eles/disu'])
-        g_intf.add_all(k['bcint/comm_flux'], deps=k['eles/disu'])
+        g_intf.add_all(k['bcint/comm_flux'],
+                       deps=k['eles/disu'] + k['bcint/comm_entropy'])
         g_intf.commit()
 
         g_flux_div = self.backend.graph()
@@ -279,7 +316,12 @@ class NavierStokesSystem(BaseSystem):
 
         # Graph 1: solution at the flux points and the common solution
         g_soln = self.backend.graph()
-        g_soln.add_all(k['eles/disu'])
+        g_soln.add_all(k['eles/entropy_filter'])
+        for l in k['eles/disu']:
+            g_soln.add(l, deps=deps(l, 'eles/entropy_filter'))
+        g_soln.add_all(k['iint/comm_entropy'], deps=k['eles/entropy_filter'])
+        g_soln.add_all(k['bcint/comm_entropy'],
+                       deps=k['eles/disu'] + k['iint/comm_entropy'])
         for l in k['eles/copy_fpts']:
             g_soln.add(l, deps=deps(l, 'eles/disu'))
         kdeps = k['eles/copy_fpts'] or k['eles/disu']
