@@ -274,23 +274,27 @@ typedef struct {
  * the smallest entropy of each element's faces entmin (nfaces x neles),
  * then store the element's new minimum in entmin and its filter strength
  * in ef_filter; vdm (nefpts x nupts) modal->nodal, invvdm (nupts x nupts)
- * nodal->modal, m0 (nfpts x nupts), mean_wts (nupts x neles, leading
- * dimension ldw), degs (nupts device ints, the degree of each mode);
+ * nodal->modal, m0 (nfpts x nupts), mean_wts (nupts x neles), each with its
+ * leading dimension, degs (nupts device ints, the degree of each mode);
  * pyfr/solvers/euler/kernels/entropyfilter.mako:153-221. */
 int b200_entropyfilter_f64(const b200_ef_t *p, int64_t neles, double *u, int64_t ldu,
                            double *entmin, int64_t lde, double *ef_filter, const double *vdm,
-                           const double *invvdm, const double *m0, const double *mean_wts,
-                           int64_t ldw, const int *degs, void *stream);
+                           int64_t ldv, const double *invvdm, int64_t ldi, const double *m0,
+                           int64_t ldm, const double *mean_wts, int64_t ldw, const int *degs,
+                           void *stream);
 int b200_entropyfilter_f32(const b200_ef_t *p, int64_t neles, float *u, int64_t ldu,
                            float *entmin, int64_t lde, float *ef_filter, const float *vdm,
-                           const float *invvdm, const float *m0, const float *mean_wts,
-                           int64_t ldw, const int *degs, void *stream);
+                           int64_t ldv, const float *invvdm, int64_t ldi, const float *m0,
+                           int64_t ldm, const float *mean_wts, int64_t ldw, const int *degs,
+                           void *stream);
 /* Minimum entropy of each element on all its faces;
  * pyfr/solvers/euler/kernels/entropylocal.mako:5-40. */
 int b200_entropylocal_f64(const b200_ef_t *p, int64_t neles, const double *u, int64_t ldu,
-                          double *entmin, int64_t lde, const double *m0, void *stream);
+                          double *entmin, int64_t lde, const double *m0, int64_t ldm,
+                          void *stream);
 int b200_entropylocal_f32(const b200_ef_t *p, int64_t neles, const float *u, int64_t ldu,
-                          float *entmin, int64_t lde, const float *m0, void *stream);
+                          float *entmin, int64_t lde, const float *m0, int64_t ldm,
+                          void *stream);
 /* Both faces of each interface take the smaller entropy (views of one
  * value per face); pyfr/solvers/baseadvec/kernels/intcent.mako:4-8. */
 int b200_intcent_f64(int64_t n, double *lbase, const void *lmap, double *rbase,

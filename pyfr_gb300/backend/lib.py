@@ -92,9 +92,9 @@ def _sig_pointwise(fp):
                        vp, vp, vp, vp, i32, vp, i64, vp],
         'bccent': [i32, i64, f64, C.POINTER(BC), vp, vp, vp, vp, i32, vp, i64,
                    vp],
-        'entropyfilter': [C.POINTER(EF), i64, vp, i64, vp, i64, vp, vp, vp,
-                          vp, vp, i64, vp, vp],
-        'entropylocal': [C.POINTER(EF), i64, vp, i64, vp, i64, vp, vp],
+        'entropyfilter': [C.POINTER(EF), i64, vp, i64, vp, i64, vp, vp, i64,
+                          vp, i64, vp, i64, vp, i64, vp, vp],
+        'entropylocal': [C.POINTER(EF), i64, vp, i64, vp, i64, vp, i64, vp],
         'intcent': [i64, vp, vp, vp, vp, i32, vp],
         'reduce_max': [i64, vp, vp, vp, vp],
     }

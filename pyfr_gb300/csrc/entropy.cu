@@ -57,8 +57,8 @@ __device__ __forceinline__ bool violates(T d, T p, T e, T entmin, const EfConsts
 // when they are not among them, the flux points (m0 interpolation)
 template <int NV, int NU, typename T>
 __device__ void get_minima(const T *__restrict__ u, int64_t ldu, int64_t e, int nfpts,
-                           const T *__restrict__ m0, const EfConsts<T> &c, T &dmin, T &pmin,
-                           T &emin) {
+                           const T *__restrict__ m0, int64_t ldm, const EfConsts<T> &c, T &dmin,
+                           T &pmin, T &emin) {
     dmin = pmin = emin = fp_max<T>();
     T ui[NV], d, p, s;
     for (int i = 0; i < NU; i++) {
@@ -74,7 +74,7 @@ __device__ void get_minima(const T *__restrict__ u, int64_t ldu, int64_t e, int 
 #pragma unroll
             for (int v = 0; v < NV; v++) ui[v] = 0;
             for (int k = 0; k < NU; k++) {
-                const T w = m0[f * NU + k];
+                const T w = m0[f * ldm + k];
 #pragma unroll
                 for (int v = 0; v < NV; v++) ui[v] += w * u[k * ldu + b200::soa_off(e, v, NV)];
             }
@@ -109,9 +109,9 @@ template <int ND, int NU, typename T>
 __global__ void __launch_bounds__(EF_BLOCK)
 entropyfilter_kernel(int64_t neles, EfConsts<T> c, int nfaces, int nfpts, int nefpts,
                      T *__restrict__ u, int64_t ldu, T *__restrict__ entmin_int, int64_t lde,
-                     T *__restrict__ ef_filter, const T *__restrict__ vdm,
-                     const T *__restrict__ invvdm, const T *__restrict__ m0,
-                     const T *__restrict__ mean_wts, int64_t ldw,
+                     T *__restrict__ ef_filter, const T *__restrict__ vdm, int64_t ldv,
+                     const T *__restrict__ invvdm, int64_t ldi, const T *__restrict__ m0,
+                     int64_t ldm, const T *__restrict__ mean_wts, int64_t ldw,
                      const int *__restrict__ degs) {
     constexpr int NV = ND + 2;
     const int64_t e = (int64_t)blockIdx.x * EF_BLOCK + threadIdx.x;
@@ -123,7 +123,7 @@ entropyfilter_kernel(int64_t neles, EfConsts<T> c, int nfaces, int nfpts, int ne
     for (int f = 0; f < nfaces; f++) entmin = fmin(entmin, entmin_int[f * lde + e]);
 
     T dmin, pmin, emin;
-    get_minima<NV, NU, T>(u, ldu, e, nfpts, m0, c, dmin, pmin, emin);
+    get_minima<NV, NU, T>(u, ldu, e, nfpts, m0, ldm, c, dmin, pmin, emin);
 
     // Element mean (Jacobian-weighted)
     T uavg[NV];
@@ -143,7 +143,7 @@ entropyfilter_kernel(int64_t neles, EfConsts<T> c, int nfaces, int nfpts, int ne
 #pragma unroll
             for (int v = 0; v < NV; v++) um[m][v] = 0;
             for (int k = 0; k < NU; k++) {
-                const T w = invvdm[m * NU + k];
+                const T w = invvdm[m * ldi + k];
 #pragma unroll
                 for (int v = 0; v < NV; v++) um[m][v] += w * u[k * ldu + b200::soa_off(e, v, NV)];
             }
@@ -157,7 +157,7 @@ entropyfilter_kernel(int64_t neles, EfConsts<T> c, int nfaces, int nfpts, int ne
 #pragma unroll
                 for (int v = 0; v < NV; v++) up[k][v] = 0;
             for (int m = 0; m < NU; m++) {
-                const T w = vdm[i * NU + m];
+                const T w = vdm[i * ldv + m];
                 const int dg = degs[m];
 #pragma unroll
                 for (int v = 0; v < NV; v++) up[dg][v] += w * um[m][v];
@@ -190,7 +190,7 @@ entropyfilter_kernel(int64_t neles, EfConsts<T> c, int nfaces, int nfpts, int ne
 #pragma unroll
             for (int v = 0; v < NV; v++) acc[v] = 0;
             for (int m = 0; m < NU; m++) {
-                const T w = ffac[degs[m]] * vdm[i * NU + m];
+                const T w = ffac[degs[m]] * vdm[i * ldv + m];
 #pragma unroll
                 for (int v = 0; v < NV; v++) acc[v] += w * um[m][v];
             }
@@ -211,7 +211,7 @@ entropyfilter_kernel(int64_t neles, EfConsts<T> c, int nfaces, int nfpts, int ne
 #pragma unroll
             for (int v = 0; v < NV; v++) u[k * ldu + b200::soa_off(e, v, NV)] += dav[v];
 
-        get_minima<NV, NU, T>(u, ldu, e, nfpts, m0, c, dmin, pmin, emin);
+        get_minima<NV, NU, T>(u, ldu, e, nfpts, m0, ldm, c, dmin, pmin, emin);
     }
 
     // Linear limiting towards the mean: density, then pressure, then entropy
@@ -232,7 +232,7 @@ entropyfilter_kernel(int64_t neles, EfConsts<T> c, int nfaces, int nfpts, int ne
                         T &x = u[k * ldu + b200::soa_off(e, v, NV)];
                         x += alpha * (uavg[v] - x);
                     }
-                get_minima<NV, NU, T>(u, ldu, e, nfpts, m0, c, dmin, pmin, emin);
+                get_minima<NV, NU, T>(u, ldu, e, nfpts, m0, ldm, c, dmin, pmin, emin);
             }
         }
     }
@@ -245,12 +245,12 @@ template <int ND, int NU, typename T>
 __global__ void __launch_bounds__(EF_BLOCK)
 entropylocal_kernel(int64_t neles, EfConsts<T> c, int nfaces, int nfpts, const T *__restrict__ u,
                     int64_t ldu, T *__restrict__ entmin_int, int64_t lde,
-                    const T *__restrict__ m0) {
+                    const T *__restrict__ m0, int64_t ldm) {
     constexpr int NV = ND + 2;
     const int64_t e = (int64_t)blockIdx.x * EF_BLOCK + threadIdx.x;
     if (e >= neles) return;
     T dmin, pmin, emin;
-    get_minima<NV, NU, T>(u, ldu, e, nfpts, m0, c, dmin, pmin, emin);
+    get_minima<NV, NU, T>(u, ldu, e, nfpts, m0, ldm, c, dmin, pmin, emin);
     for (int f = 0; f < nfaces; f++) entmin_int[f * lde + e] = emin;
 }
 
@@ -288,8 +288,9 @@ EfConsts<T> ef_consts(const b200_ef_t &p) {
 
 template <typename T>
 int entropyfilter(const b200_ef_t *p, int64_t neles, T *u, int64_t ldu, T *entmin, int64_t lde,
-                  T *ef_filter, const T *vdm, const T *invvdm, const T *m0, const T *mean_wts,
-                  int64_t ldw, const int *degs, cudaStream_t st) {
+                  T *ef_filter, const T *vdm, int64_t ldv, const T *invvdm, int64_t ldi,
+                  const T *m0, int64_t ldm, const T *mean_wts, int64_t ldw, const int *degs,
+                  cudaStream_t st) {
     if (neles <= 0) return B200_OK;
     if (!p || !u || !entmin || !ef_filter || !vdm || !invvdm || !mean_wts || !degs ||
         (!p->fpts_in_upts && !m0))
@@ -302,7 +303,7 @@ int entropyfilter(const b200_ef_t *p, int64_t neles, T *u, int64_t ldu, T *entmi
     if (p->ndims == nd && p->nupts == nu) {                                        \
         entropyfilter_kernel<nd, nu, T><<<grid, EF_BLOCK, 0, st>>>(                \
             neles, c, p->nfaces, p->nfpts, p->nefpts, u, ldu, entmin, lde, ef_filter, \
-            vdm, invvdm, m0, mean_wts, ldw, degs);                                 \
+            vdm, ldv, invvdm, ldi, m0, ldm, mean_wts, ldw, degs);                  \
         B200_CHECK_LAUNCH("entropyfilter");                                        \
         return B200_OK;                                                            \
     }
@@ -314,7 +315,7 @@ int entropyfilter(const b200_ef_t *p, int64_t neles, T *u, int64_t ldu, T *entmi
 
 template <typename T>
 int entropylocal(const b200_ef_t *p, int64_t neles, const T *u, int64_t ldu, T *entmin,
-                 int64_t lde, const T *m0, cudaStream_t st) {
+                 int64_t lde, const T *m0, int64_t ldm, cudaStream_t st) {
     if (neles <= 0) return B200_OK;
     if (!p || !u || !entmin || (!p->fpts_in_upts && !m0))
         return b200::set_error(B200_ERR_ARG, "entropylocal: null argument");
@@ -323,7 +324,7 @@ int entropylocal(const b200_ef_t *p, int64_t neles, const T *u, int64_t ldu, T *
 #define X(nd, nu)                                                                  \
     if (p->ndims == nd && p->nupts == nu) {                                        \
         entropylocal_kernel<nd, nu, T><<<grid, EF_BLOCK, 0, st>>>(                 \
-            neles, c, p->nfaces, p->nfpts, u, ldu, entmin, lde, m0);               \
+            neles, c, p->nfaces, p->nfpts, u, ldu, entmin, lde, m0, ldm);          \
         B200_CHECK_LAUNCH("entropylocal");                                         \
         return B200_OK;                                                            \
     }
@@ -348,28 +349,32 @@ extern "C" {
 
 int b200_entropyfilter_f64(const b200_ef_t *p, int64_t neles, double *u, int64_t ldu,
                            double *entmin, int64_t lde, double *ef_filter, const double *vdm,
-                           const double *invvdm, const double *m0, const double *mean_wts,
-                           int64_t ldw, const int *degs, void *stream) {
-    return entropyfilter<double>(p, neles, u, ldu, entmin, lde, ef_filter, vdm, invvdm, m0,
-                                 mean_wts, ldw, degs, (cudaStream_t)stream);
+                           int64_t ldv, const double *invvdm, int64_t ldi, const double *m0,
+                           int64_t ldm, const double *mean_wts, int64_t ldw, const int *degs,
+                           void *stream) {
+    return entropyfilter<double>(p, neles, u, ldu, entmin, lde, ef_filter, vdm, ldv, invvdm, ldi,
+                                 m0, ldm, mean_wts, ldw, degs, (cudaStream_t)stream);
 }
 
 int b200_entropyfilter_f32(const b200_ef_t *p, int64_t neles, float *u, int64_t ldu,
                            float *entmin, int64_t lde, float *ef_filter, const float *vdm,
-                           const float *invvdm, const float *m0, const float *mean_wts,
-                           int64_t ldw, const int *degs, void *stream) {
-    return entropyfilter<float>(p, neles, u, ldu, entmin, lde, ef_filter, vdm, invvdm, m0,
-                                mean_wts, ldw, degs, (cudaStream_t)stream);
+                           int64_t ldv, const float *invvdm, int64_t ldi, const float *m0,
+                           int64_t ldm, const float *mean_wts, int64_t ldw, const int *degs,
+                           void *stream) {
+    return entropyfilter<float>(p, neles, u, ldu, entmin, lde, ef_filter, vdm, ldv, invvdm, ldi,
+                                 m0, ldm, mean_wts, ldw, degs, (cudaStream_t)stream);
 }
 
 int b200_entropylocal_f64(const b200_ef_t *p, int64_t neles, const double *u, int64_t ldu,
-                          double *entmin, int64_t lde, const double *m0, void *stream) {
-    return entropylocal<double>(p, neles, u, ldu, entmin, lde, m0, (cudaStream_t)stream);
+                          double *entmin, int64_t lde, const double *m0, int64_t ldm,
+                          void *stream) {
+    return entropylocal<double>(p, neles, u, ldu, entmin, lde, m0, ldm, (cudaStream_t)stream);
 }
 
 int b200_entropylocal_f32(const b200_ef_t *p, int64_t neles, const float *u, int64_t ldu,
-                          float *entmin, int64_t lde, const float *m0, void *stream) {
-    return entropylocal<float>(p, neles, u, ldu, entmin, lde, m0, (cudaStream_t)stream);
+                          float *entmin, int64_t lde, const float *m0, int64_t ldm,
+                          void *stream) {
+    return entropylocal<float>(p, neles, u, ldu, entmin, lde, m0, ldm, (cudaStream_t)stream);
 }
 
 int b200_intcent_f64(int64_t n, double *lbase, const void *lmap, double *rbase,

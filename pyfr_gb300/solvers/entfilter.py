@@ -90,9 +90,11 @@ class EntropyFilter:
         fn = getattr(be.lib, f'entropyfilter_{self._sfx()}')
         e = self.system.ele_map[et]
         ent, eff = self.entmin[et], self.ef_filter[et]
-        m0 = q['m0'].data if q['m0'] is not None else None
+        m0, ldm = (q['m0'].data, q['m0'].leaddim) if q['m0'] is not None \
+            else (None, 0)
         args = (C.byref(q['p']), e.neles, u.data, u.leaddim, ent.data,
-                ent.leaddim, eff.data, q['vdm'].data, q['invvdm'].data, m0,
+                ent.leaddim, eff.data, q['vdm'].data, q['vdm'].leaddim,
+                q['invvdm'].data, q['invvdm'].leaddim, m0, ldm,
                 q['wts'].data, q['wts'].leaddim, q['degs'].data)
 
         def run(stream):
@@ -108,9 +110,10 @@ class EntropyFilter:
         fn = getattr(be.lib, f'entropylocal_{self._sfx()}')
         e = self.system.ele_map[et]
         ent = self.entmin[et]
-        m0 = q['m0'].data if q['m0'] is not None else None
+        m0, ldm = (q['m0'].data, q['m0'].leaddim) if q['m0'] is not None \
+            else (None, 0)
         args = (C.byref(q['p']), e.neles, u.data, u.leaddim, ent.data,
-                ent.leaddim, m0)
+                ent.leaddim, m0, ldm)
 
         def run(stream):
             fn(*args, stream)
