@@ -48,6 +48,20 @@ class RKVdH2Integrator:
         self.backend = backend
         self.cfg = cfg
 
+        # A solution read from a file restarts the run from its time, with
+        # its configuration history and controller state
+        # (pyfr/integrators/base.py:48-65)
+        from pyfr_gb300.native import Solution
+        self.isrestart = isinstance(initsoln, Solution)
+        self._restart = initsoln if self.isrestart else None
+        self.prevcfgs = {k: v.tostr() for k, v in
+                         initsoln.prevcfgs.items()} if self.isrestart else {}
+        if self.isrestart:
+            initsoln = initsoln.data
+        self.mesh_uuid = getattr(mesh, 'uuid', None)
+        self.plugins = []
+        self._plugin_times = []
+
         sect = 'solver-time-integrator'
         self.scheme = cfg.get(sect, 'scheme', 'rk45')
         if self.scheme not in RK_COEFFS:
@@ -78,7 +92,10 @@ class RKVdH2Integrator:
         for k in self.system.preproc_kernels(0):
             k.run(backend.stream)
 
-        self.tcurr = cfg.getfloat(sect, 'tstart', 0.0)
+        self.tstart = cfg.getfloat(sect, 'tstart', 0.0)
+        self.tend = cfg.getfloat(sect, 'tend', None)
+        self.tcurr = self._restart.stats.getfloat(sect, 'tcurr') \
+            if self.isrestart else self.tstart
         # (the CFL controller computes its own first step size)
         self.dt = cfg.getfloat(sect, 'dt', 0.0) if self.needs_cfl else \
             cfg.getfloat(sect, 'dt')
@@ -131,9 +148,82 @@ class RKVdH2Integrator:
             self._errprev = 1.0
             self._ekerns = {}
 
+            # Controller state of a restart; a change of tolerances resets
+            # the previous error (pyfr/integrators/explicit/controllers.py:
+            # 77-85)
+            sd = self._restart.state.get('intg/ctrl') if self.isrestart \
+                else None
+            if sd is not None:
+                self.dt, self._errprev = float(sd[0]), float(sd[1])
+                old = self._restart.config
+                keys = {k for c in (cfg, old) for k in c.items(sect)
+                        if k.startswith(('atol', 'rtol'))}
+                if any(cfg.get(sect, k, None) != old.get(sect, k, None)
+                       for k in keys):
+                    self._errprev = 1.0
+
     @property
     def gndofs(self):
         return self.system.gndofs
+
+    # ---- plugins and output ------------------------------------------------
+
+    def add_plugin(self, plugin):
+        """Attach a solution plugin, called after every accepted step; a
+        run that is not a restart calls it once at once (the initial
+        output, pyfr/integrators/explicit/controllers.py:13-15)."""
+        self.plugins.append(plugin)
+        if not self.isrestart:
+            self.backend.wait()
+            plugin(self)
+
+    def call_plugin_dt(self, tstart, dt):
+        """Have ``advance_to`` land on tstart + k*dt (a plugin's output
+        times, pyfr/integrators/base.py:254-270)."""
+        self._plugin_times.append((tstart, dt))
+
+    def _next_plugin_time(self):
+        ts = [t0 + (math.floor((self.tcurr - t0)/dt + 1e-9) + 1)*dt
+              for t0, dt in self._plugin_times]
+        return min(ts, default=math.inf)
+
+    def _run_plugins(self):
+        if self.plugins:
+            self.backend.wait()
+            for p in self.plugins:
+                p(self)
+
+    @property
+    def cfgmeta(self):
+        """The configuration records of an output: ``config`` and the
+        ``config-<n>`` chain (pyfr/integrators/base.py:369-381)."""
+        cfg = self.cfg.tostr()
+        n = len(self.prevcfgs)
+        ret = dict(self.prevcfgs, config=cfg)
+        if n == 0 or cfg != ret[f'config-{n - 1}']:
+            ret[f'config-{n}'] = cfg
+        return ret
+
+    def collect_stats(self, stats):
+        """Run statistics of an output (pyfr/integrators/base.py:328-
+        348)."""
+        sect = 'solver-time-integrator'
+        stats.set(sect, 'tcurr', repr(self.tcurr))
+        stats.set(sect, 'nacptsteps', self.nacptsteps)
+        stats.set(sect, 'nrjctsteps', self.nrjctsteps)
+        stats.set(sect, 'nsteps', self.nacptsteps + self.nrjctsteps)
+
+    def serialise(self):
+        """Serialised state restored by a restart."""
+        if self.errest:
+            return {'intg/ctrl': np.array([self.dt, self._errprev])}
+        return {}
+
+    def run(self):
+        """Advance to the configured ``tend``."""
+        if self.tend is None:
+            raise ValueError('No tend in [solver-time-integrator]')
+        self.advance_to(self.tend)
 
     def _make_system(self, backend, systemcls, mesh, initsoln, cfg):
         return systemcls(backend, mesh, initsoln, self._nregs, cfg,
@@ -261,16 +351,19 @@ class RKVdH2Integrator:
         while self.tcurr < t - 1e-12*max(1.0, abs(t)):
             if self.needs_cfl and self.nacptsteps % self._cfl_nsteps == 0:
                 self.dt = self.compute_dt_cfl()
-            dt = min(self.dt, self.dtmax, t - self.tcurr)
+            dt = min(self.dt, self.dtmax, t - self.tcurr,
+                     self._next_plugin_time() - self.tcurr)
             if self.controller in ('none', 'cfl'):
                 (idx,) = self.step(self.tcurr, dt)
                 self.idxcurr = idx
                 self.tcurr += dt
                 self.nacptsteps += 1
                 self.dt_accepted.append(dt)
+                self._run_plugins()
                 continue
 
-            self._pi_step(dt)
+            if self._pi_step(dt):
+                self._run_plugins()
 
         self.backend.wait()
 
@@ -311,7 +404,8 @@ class RKVdH2Integrator:
         attempts = 0
         target = self.nacptsteps + nsteps
         while self.nacptsteps < target:
-            self._pi_step(min(self.dt, self.dtmax))
+            if self._pi_step(min(self.dt, self.dtmax)):
+                self._run_plugins()
             attempts += 1
         self.backend.wait()
         return attempts
@@ -324,6 +418,8 @@ class RKVdH2Integrator:
             (idx,) = self.step(self.tcurr, dt)[:1]
             self.idxcurr = idx
             self.tcurr += dt
+            self.nacptsteps += 1
+            self._run_plugins()
         self.backend.wait()
 
     @property

@@ -50,6 +50,16 @@ class Mesh:
     # Boundary faces by boundary name: Side of (etype, element, face)
     # (the reference's bcon_<name> arrays, pyfr/readers/native.py:15-86)
     bcon: dict = field(default_factory=dict)
+    # Records of a mesh read from a file: its identifier, codec, the file's
+    # numbers of the elements of each type (local order), and so on
+    uuid: str = None
+    codec: list = None
+    eidxs: dict = None
+    fname: str = None
+    creator: str = None
+    colours: dict = None
+    tags: dict = None
+    spts_nodes: dict = None
 
     @property
     def etypes(self):

@@ -70,3 +70,62 @@ class FieldIntegrals:
             total += self._host
 
         return {'E': total[0], 'enst': total[1], 'vol': total[2]}
+
+
+class WriterPlugin:
+    """Solution output of ``[soln-plugin-writer]`` (``pyfr/plugins/
+    writer.py:8-160``): every ``dt-out`` of simulated time (and at the
+    start of a run that is not a restart) the solution is written to
+    ``basedir/basename`` (formatted with the time ``t`` and the output
+    count ``n``; the ``.pyfrs`` extension is added), with the
+    configuration chain, the run statistics and the integrator's
+    serialised state.  ``files`` lists what was written."""
+
+    name = 'writer'
+
+    def __init__(self, intg, cfgsect='soln-plugin-writer'):
+        from pathlib import Path
+
+        from pyfr_gb300.native import file_path_gen
+
+        cfg = intg.cfg
+        if cfg.getbool(cfgsect, 'write-gradients', False):
+            raise NotImplementedError('Gradient output is not provided')
+        basedir = Path(cfg.get(cfgsect, 'basedir', '.')).absolute()
+        basename = cfg.get(cfgsect, 'basename')
+        if not basename.endswith('.pyfrs'):
+            basename += '.pyfrs'
+        self._fgen = file_path_gen(basedir, basename)
+        next(self._fgen)
+
+        emap = intg.system.ele_map
+        self.fields = list(next(iter(emap.values())).convars)
+        self._upts = {et: e.basis.upts for et, e in emap.items()}
+
+        self.dt_out = cfg.getfloat(cfgsect, 'dt-out')
+        self.tol = 5*intg.dtmin
+        self.tout_last = intg.tcurr
+        intg.call_plugin_dt(intg.tcurr, self.dt_out)
+        if not intg.isrestart:
+            self.tout_last -= self.dt_out
+        self.files = []
+
+    def __call__(self, intg):
+        if intg.tcurr - self.tout_last < self.dt_out - self.tol:
+            return
+        self.write(intg)
+        self.tout_last = intg.tcurr
+
+    def write(self, intg):
+        from pyfr_gb300.inifile import Inifile
+        from pyfr_gb300.native import write_soln
+
+        stats = Inifile()
+        stats.set('data', 'prefix', 'soln')
+        intg.collect_stats(stats)
+        path = self._fgen.send(intg.tcurr)
+        sysm = intg.system
+        write_soln(path, sysm.mesh, dict(zip(sysm.ele_types, intg.soln)),
+                   self._upts, self.fields, intg.cfg, stats,
+                   prevcfgs=intg.prevcfgs, state=intg.serialise())
+        self.files.append(path)

@@ -1,0 +1,132 @@
+"""Runs on meshes read from files, solution output and restarts
+(pyfr/readers/native.py, pyfr/plugins/writer.py, the restart path of
+pyfr/integrators/base.py:48-65).
+
+* the right-hand side on a Gmsh-imported box equals the one on the same
+  box generated in memory (relative max-norm 1e-12; the interfaces come in
+  another order);
+* a run that writes its solution every two steps and is restarted from the
+  middle output ends bit-identical to the uninterrupted run, with the
+  fixed-step and the PI controllers and with the mixed-precision form."""
+import numpy as np
+import pytest
+
+from tests.gmsh_util import box_msh
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope='module')
+def built():
+    import __graft_entry__ as ge
+    ge.build_library()
+
+
+def _backend(cfg):
+    from pyfr_gb300.backend import B200Backend
+    return B200Backend(cfg)
+
+
+@pytest.mark.parametrize('system', ['euler', 'navier-stokes'])
+def test_rhs_on_imported_mesh(built, tmp_path, system):
+    """The file's interfaces take their left side by the reference's rule
+    (the face with the smaller codec key), the generated box by its own, so
+    the comparison uses fluxes that do not favour a side: Rusanov, and for
+    Navier-Stokes an LDG common solution with beta = 0."""
+    from pyfr_gb300.gmsh import import_mesh
+    from pyfr_gb300.mesh import box
+    from pyfr_gb300.native import read_mesh
+    from pyfr_gb300.solvers.system import EulerSystem, NavierStokesSystem
+    from tests.test_gpu_bcs import FREE, _cfg
+
+    n, per = (3, 2, 2), (True, False, True)
+    import_mesh(box_msh(n, per, '4.1'), tmp_path / 'b.pyfrm')
+    mfile = read_mesh(tmp_path / 'b.pyfrm')
+    mgen = box('hex', n, 0.0, 1.0, per)
+    specs = {'ylo': dict(type='no-slp-isot-wall', cpTw=3.2, **FREE),
+             'yhi': dict(type='char-riem-inv', **FREE)}
+
+    ns = system == 'navier-stokes'
+    scls = NavierStokesSystem if ns else EulerSystem
+    if not ns:
+        specs['ylo'] = dict(type='slp-adia-wall')
+    out = []
+    for m in (mfile, mgen):
+        cfg = _cfg(3, specs, ns=ns)
+        cfg.set('solver-interfaces', 'ldg-beta', '0.0')
+        s = scls(_backend(cfg), m, None, 2, cfg)
+        s.commit()
+        s.rhs(0.0, 0, 1)
+        (r,) = s.ele_scal_upts(1)
+        out.append(r)
+    a, b = out
+    assert np.abs(a - b).max()/np.abs(b).max() < 1e-12
+
+
+def _vortex(tmp_path, controller, precision='double'):
+    from pyfr_gb300.cases import euler_vortex
+    from pyfr_gb300.native import read_mesh, save_mesh
+
+    cfg, mesh = euler_vortex(n=8, order=3, dt=2e-3, precision=precision)
+    save_mesh(tmp_path / 'v.pyfrm', mesh)
+    sect = 'solver-time-integrator'
+    if controller == 'pi':
+        cfg.set(sect, 'controller', 'pi')
+        cfg.set(sect, 'rtol', '1e-6')
+        cfg.set(sect, 'atol', '1e-6')
+    w = 'soln-plugin-writer'
+    cfg.set(w, 'dt-out', '0.004')
+    cfg.set(w, 'basedir', str(tmp_path))
+    cfg.set(w, 'basename', 'vortex-{n:03d}')
+    if precision == 'single':
+        cfg.set('backend-b200', 'mul-precision', 'bf16x3')
+        cfg.set('backend-b200', 'split-products', '5')
+    return cfg, read_mesh(tmp_path / 'v.pyfrm')
+
+
+@pytest.mark.parametrize('controller,form', [('none', 'plain'),
+                                             ('pi', 'plain'),
+                                             ('none', 'mixed')])
+def test_restart_bit_identical(built, tmp_path, controller, form):
+    from pyfr_gb300.integrators import MixedRKIntegrator, RKVdH2Integrator
+    from pyfr_gb300.native import read_soln
+    from pyfr_gb300.plugins import WriterPlugin
+    from pyfr_gb300.solvers.system import EulerSystem
+
+    icls = MixedRKIntegrator if form == 'mixed' else RKVdH2Integrator
+    prec = 'single' if form == 'mixed' else 'double'
+    cfg, mesh = _vortex(tmp_path, controller, prec)
+
+    intg = icls(_backend(cfg), EulerSystem, mesh, cfg)
+    wr = WriterPlugin(intg)
+    intg.add_plugin(wr)
+    intg.advance_to(0.012)
+    (ufull,) = intg.soln
+    names = [p.name for p in wr.files]
+    assert names[:4] == ['vortex-000.pyfrs', 'vortex-001.pyfrs',
+                         'vortex-002.pyfrs', 'vortex-003.pyfrs']
+    assert len(names) == 4
+
+    # Restart from the output at t = 0.004
+    soln = read_soln(wr.files[1], mesh)
+    assert soln.stats.getfloat('solver-time-integrator', 'tcurr') == \
+        pytest.approx(0.004, abs=1e-15)
+    if controller == 'pi':
+        assert 'intg/ctrl' in soln.state
+    cfg2 = soln.config
+    cfg2.set('soln-plugin-writer', 'basename', 'restart-{n:03d}')
+    intg2 = icls(_backend(cfg2), EulerSystem, mesh, cfg2, soln)
+    assert intg2.isrestart and intg2.tcurr == \
+        soln.stats.getfloat('solver-time-integrator', 'tcurr')
+    wr2 = WriterPlugin(intg2)
+    intg2.add_plugin(wr2)
+    assert wr2.files == []                  # no initial output on restart
+    intg2.advance_to(0.012)
+    (urest,) = intg2.soln
+    assert np.array_equal(urest, ufull)
+    assert [p.name for p in wr2.files] == ['restart-000.pyfrs',
+                                           'restart-001.pyfrs']
+
+    s2 = read_soln(wr2.files[-1], mesh)
+    assert np.array_equal(s2.data['quad'], ufull)
+    assert sorted(s2.prevcfgs) == ['config-0', 'config-1']
