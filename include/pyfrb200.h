@@ -287,6 +287,76 @@ int b200_entropyfilter_f32(const b200_ef_t *p, int64_t neles, float *u, int64_t 
                            int64_t ldv, const float *invvdm, int64_t ldi, const float *m0,
                            int64_t ldm, const float *mean_wts, int64_t ldw, const int *degs,
                            void *stream);
+/* Artificial viscosity (pyfr/solvers/baseadvecdiff/artvisc.py:24-200):
+ * the sensor's sizes and constants.  kwh selects the Klockner-Warburton-
+ * Hesthaven decay fit (orders >= 2) over the Persson-Peraire modal ratio;
+ * s_weights and baseline hold the fit weights and baseline decay of
+ * degrees 1..ndeg-1, se0 = log10(s0 / order^4). */
+typedef struct {
+    int nupts, nvars, svar, nverts, nmodes, ndeg, kwh;
+    double kappa, max_av, se0;
+    double s_weights[16], baseline[16];
+} b200_av_t;
+/* Shock sensor of the variable svar of u (nupts x nvars x neles AoSoA):
+ * per element the viscosity of its modal content (invvdm: nmodes x nupts
+ * nodal->modal, degs: the degree of each mode, ind: 1 for the modes of
+ * the highest degree), maximised into vtx at the element's vertices
+ * (vnodes: nverts x neles node numbers, leading dimension ldn); vtx must be
+ * zeroed first; pyfr/solvers/baseadvecdiff/kernels/shocksensor.mako. */
+int b200_shocksensor_f64(const b200_av_t *p, int64_t neles, const double *u, int64_t ldu,
+                         const double *invvdm, int64_t ldi, const int *degs, const int *ind,
+                         const int *vnodes, int64_t ldn, double *vtx, void *stream);
+int b200_shocksensor_f32(const b200_av_t *p, int64_t neles, const float *u, int64_t ldu,
+                         const float *invvdm, int64_t ldi, const int *degs, const int *ind,
+                         const int *vnodes, int64_t ldn, float *vtx, void *stream);
+/* Viscosity at npts points of each element, linear in its vertex values:
+ * out (npts x neles) = op (npts x nverts) . vtx[vnodes];
+ * pyfr/solvers/baseadvecdiff/kernels/avfill.mako (and the interpolation
+ * at the solution points of pyfr/solvers/navstokes/kernels/tflux.mako). */
+int b200_avfill_f64(int nverts, int npts, int64_t neles, const double *vtx, const int *vnodes,
+                    int64_t ldn, const double *op, int64_t ldo, double *out, int64_t ldout,
+                    void *stream);
+int b200_avfill_f32(int nverts, int npts, int64_t neles, const float *vtx, const int *vnodes,
+                    int64_t ldn, const float *op, int64_t ldo, float *out, int64_t ldout,
+                    void *stream);
+/* The Navier-Stokes flux, interface flux and boundary flux with artificial
+ * viscosity: as b200_tflux_ns_*, b200_intcflux_ns_* and b200_bccflux_ns_*,
+ * with -mu grad u added to the viscous flux (mu at the solution points,
+ * av (nupts x neles, leading dimension lda); at the interface and
+ * boundary points through the scalar view av_base/av_map of the left
+ * side); pyfr/solvers/baseadvecdiff/kernels/artvisc.mako. */
+int b200_tflux_ns_av_f64(int ndims, int nupts, int64_t neles, int linear, const b200_gas_t *gas,
+                         const double *u, int64_t ldu, double *f, int64_t ldf, double *gradu,
+                         int64_t ldg, const double *smats, int64_t lds, const double *rcpdjac,
+                         int64_t ldr, const double *verts, int64_t ldv, const double *upts,
+                         int64_t ldup, const double *av, int64_t lda, void *stream);
+int b200_tflux_ns_av_f32(int ndims, int nupts, int64_t neles, int linear, const b200_gas_t *gas,
+                         const float *u, int64_t ldu, float *f, int64_t ldf, float *gradu,
+                         int64_t ldg, const float *smats, int64_t lds, const float *rcpdjac,
+                         int64_t ldr, const float *verts, int64_t ldv, const float *upts,
+                         int64_t ldup, const float *av, int64_t lda, void *stream);
+int b200_intcflux_ns_av_f64(int ndims, int64_t n, int rsolver, const b200_gas_t *gas,
+                            double beta, double tau, double *ul_base, const void *ul_map,
+                            double *ur_base, const void *ur_map, const double *gl_base,
+                            const void *gl_map, const void *gl_rstr, const double *gr_base,
+                            const void *gr_map, const void *gr_rstr, int ix64, const double *nl,
+                            int64_t ldn, const double *av_base, const void *av_map, void *stream);
+int b200_intcflux_ns_av_f32(int ndims, int64_t n, int rsolver, const b200_gas_t *gas,
+                            double beta, double tau, float *ul_base, const void *ul_map,
+                            float *ur_base, const void *ur_map, const float *gl_base,
+                            const void *gl_map, const void *gl_rstr, const float *gr_base,
+                            const void *gr_map, const void *gr_rstr, int ix64, const float *nl,
+                            int64_t ldn, const float *av_base, const void *av_map, void *stream);
+int b200_bccflux_ns_av_f64(int ndims, int64_t n, int rsolver, const b200_gas_t *gas,
+                           double tau, const b200_bc_t *bc, double *ul_base, const void *ul_map,
+                           const double *gl_base, const void *gl_map, const void *gl_rstr,
+                           int ix64, const double *nl, int64_t ldn, const double *av_base,
+                           const void *av_map, void *stream);
+int b200_bccflux_ns_av_f32(int ndims, int64_t n, int rsolver, const b200_gas_t *gas,
+                           double tau, const b200_bc_t *bc, float *ul_base, const void *ul_map,
+                           const float *gl_base, const void *gl_map, const void *gl_rstr,
+                           int ix64, const float *nl, int64_t ldn, const float *av_base,
+                           const void *av_map, void *stream);
 /* Minimum entropy of each element on all its faces;
  * pyfr/solvers/euler/kernels/entropylocal.mako:5-40. */
 int b200_entropylocal_f64(const b200_ef_t *p, int64_t neles, const double *u, int64_t ldu,

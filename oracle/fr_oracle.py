@@ -267,11 +267,11 @@ def bc_ldg_grad_state(bc, us, n, gl):
     return gr
 
 
-def bc_flux_ns(bc, ul, gl, n, c, rsolver):
+def bc_flux_ns(bc, ul, gl, n, c, rsolver, av=None):
     """Common normal flux at a boundary (per unit normal): ghost,
     ghost-imperm or slip-wall flux state of
     pyfr/solvers/navstokes/kernels/bcs/{ghost,ghost-imperm,slp-adia-wall}
-    .mako."""
+    .mako; av: the artificial viscosity at the points (or None)."""
     gamma, tau = c['gamma'], c['ldg-tau']
     t = bc['type']
     ur = bc_rsolve_state(bc, ul, n, gamma)
@@ -281,7 +281,10 @@ def bc_flux_ns(bc, ul, gl, n, c, rsolver):
     imperm = t in ('no-slp-adia-wall', 'no-slp-isot-wall')
     ul_dg = bc_ldg_state(bc, ul, n, gamma)
     gr = bc_ldg_grad_state(bc, ul_dg if imperm else ul, n, gl)
-    fv = np.einsum('dn,dvn->vn', n, viscous_flux(ul_dg, gr, c))
+    fvs = viscous_flux(ul_dg, gr, c)
+    if av is not None:
+        fvs = fvs - av*gr
+    fv = np.einsum('dn,dvn->vn', n, fvs)
     if not imperm:
         fv = fv + tau*(ul - ur)
     return fi + fv
@@ -476,10 +479,14 @@ class Discretisation:
         r += self.apply(self.ops['M3'], uf)
         return -r/self.djac_u[:, None, :]
 
-    def rhs_ns(self, u, c, rsolver='rusanov', grads_out=None):
+    def rhs_ns(self, u, c, rsolver='rusanov', grads_out=None, av=None):
+        """av: the artificial-viscosity parameters of shock_sensor and
+        artvisc_points (pyfr/solvers/baseadvecdiff/artvisc.py), or None."""
         gamma, beta, tau = c['gamma'], c['ldg-beta'], c['ldg-tau']
         nd, nupts, nfpts, ne = self.ndims, self.nupts, self.nfpts, self.neles
         uf = self.apply(self.ops['M0'], u)
+        if av is not None:
+            avf, avu = artvisc_points(shock_sensor(u, av), av)
 
         # Common solution (intconu) on the flux points
         ul, ur = self._gather(uf, 'l'), self._gather(uf, 'r')
@@ -505,7 +512,10 @@ class Discretisation:
         # Flux at the solution points
         ut = u.transpose(1, 0, 2)
         fi, _, _ = inviscid_flux(ut, gamma)
-        fv = viscous_flux(ut, g.transpose(0, 2, 1, 3), c)
+        gt = g.transpose(0, 2, 1, 3)
+        fv = viscous_flux(ut, gt, c)
+        if av is not None:
+            fv = fv - avu[None, None]*gt
         ft = self._transform_flux((fi + fv).transpose(0, 2, 1, 3))
 
         # Physical gradient at the flux points and the common flux
@@ -516,8 +526,13 @@ class Discretisation:
         mag = np.sqrt(np.sum(self.nl**2, axis=0))
         n = self.nl/mag
         fic = RSOLVERS[rsolver](ul, ur, n, gamma)
-        fvl = np.einsum('dn,dvn->vn', n, viscous_flux(ul, gl, c))
-        fvr = np.einsum('dn,dvn->vn', n, viscous_flux(ur, gr, c))
+        fvl_, fvr_ = viscous_flux(ul, gl, c), viscous_flux(ur, gr, c)
+        if av is not None:
+            # (the left side's viscosity for both sides)
+            a = avf[self.pl[:, 0], self.pl[:, 1]]
+            fvl_, fvr_ = fvl_ - a*gl, fvr_ - a*gr
+        fvl = np.einsum('dn,dvn->vn', n, fvl_)
+        fvr = np.einsum('dn,dvn->vn', n, fvr_)
         if beta == -0.5:
             fvc = fvr
         elif beta == 0.5:
@@ -530,7 +545,8 @@ class Discretisation:
         for fp, ee, n, bmag, spec in self.bcs:
             ub = uf[fp, :, ee].T
             gb = gf[:, fp, :, ee].transpose(1, 2, 0)
-            bflux.append(bmag*bc_flux_ns(spec, ub, gb, n, c, rsolver))
+            ab = avf[fp, ee] if av is not None else None
+            bflux.append(bmag*bc_flux_ns(spec, ub, gb, n, c, rsolver, ab))
         self._scatter(uf, 'l', mag*(fic + fvc))
         self._scatter(uf, 'r', -mag*(fic + fvc))
         for (fp, ee, *_), f in zip(self.bcs, bflux):
@@ -539,6 +555,61 @@ class Discretisation:
         r = self.apply(self.ops['M132'], ft.reshape(nd*nupts, -1, ne))
         r += self.apply(self.ops['M3'], uf)
         return -r/self.djac_u[:, None, :]
+
+
+def shock_sensor(u, av):
+    """Artificial viscosity of every element from the modal content of
+    its density (pyfr/solvers/baseadvecdiff/kernels/shocksensor.mako, with
+    the parameters of pyfr/solvers/baseadvecdiff/artvisc.py:160-196).
+
+    av: invvdm (nmodes, nupts) nodal->modal, degs (largest degree of each
+    mode), order, and c = {'max-artvisc', 'kappa', 's0'}; u (nupts, nvars,
+    neles).  Orders from 2 up take the Klockner-Warburton-Hesthaven decay
+    fit, order 1 the Persson-Peraire modal ratio."""
+    c, order = av['c'], av['order']
+    kappa, amax = c['kappa'], c['max-artvisc']
+    degs = list(av['degs'])
+    modes = av['invvdm'] @ u[:, 0, :]                        # (nmodes, ne)
+    ne = u.shape[2]
+    fit = list(range(1, order + 1))
+    if len(fit) >= 2:
+        x = np.log(np.array(fit, dtype=float) + 1)
+        w = np.linalg.pinv(np.column_stack([np.ones(len(x)), x]))[1]
+        bd = np.array([1.0/(d + 1)**(2*order) for d in fit])
+        bd /= bd.sum()
+        en = np.zeros((order + 1, ne))
+        for k, d in enumerate(degs):
+            en[d] += modes[k]**2
+        tot = en.sum(axis=0)
+        for i, d in enumerate(fit):
+            en[d] += tot*bd[i]
+        for d in range(order - 1, -1, -1):
+            en[d] = np.maximum(en[d], en[d + 1])
+        s = -0.5*sum(w[i]*np.log(en[d]) for i, d in enumerate(fit))
+        mu = np.where(s > 2 + kappa, 0.0,
+                      0.5*amax*(1 - np.sin(0.5*np.pi/kappa*(s - 2))))
+        return np.where(s < 2 - kappa, amax, mu)
+
+    tot = np.sum(modes**2, axis=0)
+    top = np.array([d == order for d in degs])
+    pn = 1e-15 + np.sum(modes[top]**2, axis=0)
+    se = np.log10(pn/tot)
+    se0 = np.log10(c['s0']/order**4)
+    mu = np.where(se < se0 - kappa, 0.0,
+                  0.5*amax*(1 + np.sin(0.5*np.pi/kappa*(se - se0))))
+    return np.where(se < se0 + kappa, mu, amax)
+
+
+def artvisc_points(mu, av):
+    """Vertex maxima of the element viscosities, interpolated linearly to
+    the flux and solution points: (nfpts, neles), (nupts, neles); av adds
+    vnodes (nverts, neles) node numbers, nnodes, and the linear shape
+    functions opf (nfpts, nverts), opu (nupts, nverts)."""
+    vn = av['vnodes']
+    vtx = np.zeros(av['nnodes'])
+    np.maximum.at(vtx, vn.ravel(), np.broadcast_to(mu, vn.shape).ravel())
+    ve = vtx[vn]                                             # (nverts, ne)
+    return av['opf'] @ ve, av['opu'] @ ve
 
 
 def wavespeed(u, smats, djac, gamma):

@@ -60,6 +60,14 @@ class EF(C.Structure):
                 ('f_tol', f64)]
 
 
+class AV(C.Structure):
+    """``b200_av_t``"""
+    _fields_ = [('nupts', i32), ('nvars', i32), ('svar', i32), ('nverts', i32),
+                ('nmodes', i32), ('ndeg', i32), ('kwh', i32), ('kappa', f64),
+                ('max_av', f64), ('se0', f64), ('s_weights', f64*16),
+                ('baseline', f64*16)]
+
+
 def _sig_pointwise(fp):
     return {
         'tflux_euler': [i32, i32, i64, i32, f64, vp, i64, vp, i64, vp, i64, vp,
@@ -90,6 +98,17 @@ def _sig_pointwise(fp):
                    vp],
         'bccflux_ns': [i32, i64, i32, C.POINTER(Gas), f64, C.POINTER(BC), vp,
                        vp, vp, vp, vp, i32, vp, i64, vp],
+        'bccflux_ns_av': [i32, i64, i32, C.POINTER(Gas), f64, C.POINTER(BC),
+                          vp, vp, vp, vp, vp, i32, vp, i64, vp, vp, vp],
+        'tflux_ns_av': [i32, i32, i64, i32, C.POINTER(Gas), vp, i64, vp, i64,
+                        vp, i64, vp, i64, vp, i64, vp, i64, vp, i64, vp, i64,
+                        vp],
+        'intcflux_ns_av': [i32, i64, i32, C.POINTER(Gas), f64, f64, vp, vp,
+                           vp, vp, vp, vp, vp, vp, vp, vp, i32, vp, i64, vp,
+                           vp, vp],
+        'shocksensor': [C.POINTER(AV), i64, vp, i64, vp, i64, vp, vp, vp, i64,
+                        vp, vp],
+        'avfill': [i32, i32, i64, vp, vp, i64, vp, i64, vp, i64, vp],
         'bccent': [i32, i64, f64, C.POINTER(BC), vp, vp, vp, vp, i32, vp, i64,
                    vp],
         'entropyfilter': [C.POINTER(EF), i64, vp, i64, vp, i64, vp, vp, i64,

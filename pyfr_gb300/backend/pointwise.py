@@ -167,9 +167,14 @@ class PointwiseKernelProvider:
                                 verts=verts, upts=upts))
 
     def _tflux_ns(self, tplargs, dims, extrns, u, f, gradu=None, smats=None,
-                  rcpdjac=None, verts=None, upts=None, artvisc_vtx=None):
-        if tplargs.get('shock_capturing', 'none') not in (None, 'none'):
-            raise NotImplementedError('Artificial viscosity is not supported')
+                  rcpdjac=None, verts=None, upts=None, artvisc=None):
+        """``artvisc``: the artificial viscosity at the solution points
+        (nupts, neles), when shock capturing is 'artificial-viscosity'
+        (the vertex interpolation of pyfr/solvers/navstokes/kernels/
+        tflux.mako:39-43, done by the avfill kernel)."""
+        av_on = tplargs.get('shock_capturing') == 'artificial-viscosity'
+        if av_on != (artvisc is not None):
+            raise ValueError('Artificial viscosity needs its field')
         if 'fused' not in tplargs.get('ktype', ''):
             raise NotImplementedError('Only the fused gradient/flux form of '
                                       'the Navier-Stokes flux is provided')
@@ -179,16 +184,27 @@ class PointwiseKernelProvider:
             tplargs, smats, rcpdjac, verts, upts)
         gas = _gas(tplargs['c'], tplargs.get('visc_corr', 'none'),
                    self.backend.ref_state)
-        fn, nd = self._fn('tflux_ns'), tplargs['ndims']
+        nd = tplargs['ndims']
         up, ul = _mat(u)
         fp, fl = _mat(f)
         gp, gl = _mat(gradu)
 
-        def run(stream):
-            fn(nd, nupts, neles, lin, C.byref(gas), up, ul, fp, fl, gp, gl,
-               sp, sl, rp, rl, vp, vl, upp, upl, stream)
+        if artvisc is not None:
+            fn = self._fn('tflux_ns_av')
+            ap, al = _mat(artvisc)
 
-        return Kernel(run, mats=[u, f, gradu, smats, rcpdjac, verts, upts],
+            def run(stream):
+                fn(nd, nupts, neles, lin, C.byref(gas), up, ul, fp, fl, gp, gl,
+                   sp, sl, rp, rl, vp, vl, upp, upl, ap, al, stream)
+        else:
+            fn = self._fn('tflux_ns')
+
+            def run(stream):
+                fn(nd, nupts, neles, lin, C.byref(gas), up, ul, fp, fl, gp, gl,
+                   sp, sl, rp, rl, vp, vl, upp, upl, stream)
+
+        return Kernel(run, mats=[u, f, gradu, smats, rcpdjac, verts, upts,
+                                 artvisc],
                       misc=[gas], name='tflux',
                       meta=dict(kind='tflux_ns', tplargs=tplargs, dims=dims,
                                 u=u, f=f, gradu=gradu, smats=smats,
@@ -278,8 +294,9 @@ class PointwiseKernelProvider:
 
     def _intcflux_ns(self, tplargs, dims, extrns, ul, ur, gradul, gradur, nl,
                      artvisc=None):
-        if artvisc is not None:
-            raise NotImplementedError('Artificial viscosity is not supported')
+        if (tplargs.get('shock_capturing') == 'artificial-viscosity') != \
+                (artvisc is not None):
+            raise ValueError('Artificial viscosity needs its field')
 
         (n,) = dims
         c = tplargs['c']
@@ -297,11 +314,21 @@ class PointwiseKernelProvider:
         np_, nlp = _mat(nl)
         ix64 = self._ix64
 
-        def run(stream):
-            fn(nd, n, rs, C.byref(gas), beta, tau, lb, lm, rb, rm, glb, glm,
-               glr, grb, grm, grr, ix64, np_, nlp, stream)
+        if artvisc is not None:
+            fn = self._fn('intcflux_ns_av')
+            ab, am, _ = _view(artvisc)
 
-        return Kernel(run, mats=[nl], views=[ul, ur, gradul, gradur],
+            def run(stream):
+                fn(nd, n, rs, C.byref(gas), beta, tau, lb, lm, rb, rm, glb,
+                   glm, glr, grb, grm, grr, ix64, np_, nlp, ab, am, stream)
+        else:
+            def run(stream):
+                fn(nd, n, rs, C.byref(gas), beta, tau, lb, lm, rb, rm, glb,
+                   glm, glr, grb, grm, grr, ix64, np_, nlp, stream)
+
+        return Kernel(run, mats=[nl],
+                      views=[ul, ur, gradul, gradur] +
+                      ([artvisc] if artvisc is not None else []),
                       misc=[gas], name='intcflux',
                       meta=dict(kind='intcflux_ns', tplargs=tplargs,
                                 dims=dims))
@@ -351,8 +378,9 @@ class PointwiseKernelProvider:
 
     def _bccflux_ns(self, tplargs, dims, extrns, ul, gradul, nl,
                     artvisc=None, **kw):
-        if artvisc is not None:
-            raise NotImplementedError('Artificial viscosity is not supported')
+        if (tplargs.get('shock_capturing') == 'artificial-viscosity') != \
+                (artvisc is not None):
+            raise ValueError('Artificial viscosity needs its field')
         if self.backend.ref_state is not None:
             raise NotImplementedError('Boundaries take unshifted states')
         (n,) = dims
@@ -367,11 +395,22 @@ class PointwiseKernelProvider:
         ix64 = self._ix64
         tau = c['ldg-tau']
 
-        def run(stream):
-            fn(nd, n, rs, C.byref(gas), tau, C.byref(bc), lb, lm, gb, gm, gr,
-               ix64, np_, nlp, stream)
+        if artvisc is not None:
+            fn = self._fn('bccflux_ns_av')
+            ab, am, _ = _view(artvisc)
 
-        return Kernel(run, mats=[nl], views=[ul, gradul], misc=[gas, bc],
+            def run(stream):
+                fn(nd, n, rs, C.byref(gas), tau, C.byref(bc), lb, lm, gb, gm,
+                   gr, ix64, np_, nlp, ab, am, stream)
+        else:
+            def run(stream):
+                fn(nd, n, rs, C.byref(gas), tau, C.byref(bc), lb, lm, gb, gm,
+                   gr, ix64, np_, nlp, stream)
+
+        return Kernel(run, mats=[nl],
+                      views=[ul, gradul] +
+                      ([artvisc] if artvisc is not None else []),
+                      misc=[gas, bc],
                       name='bccflux', meta=dict(kind='bccflux_ns', dims=dims))
 
     def _intconu(self, tplargs, dims, extrns, ulin, urin, ulout, urout):

@@ -321,7 +321,8 @@ bcconu_kernel(int64_t n, T gamma, BcK<T> bc, ScalView<T> vin, ScalView<T> vout, 
 template <int ND, typename T>
 __global__ void __launch_bounds__(BC_BLOCK)
 bccflux_ns_kernel(int64_t n, int rs, b200::GasK<T> gas, T tau, BcK<T> bc, ScalView<T> vl,
-                  VectView<T> gl, int ix64, const T *__restrict__ nl, int64_t ldn) {
+                  VectView<T> gl, int ix64, const T *__restrict__ nl, int64_t ldn,
+                  ScalView<T> va) {
     constexpr int NV = ND + 2;
     const int64_t i = (int64_t)blockIdx.x * BC_BLOCK + threadIdx.x;
     if (i >= n) return;
@@ -352,6 +353,14 @@ bccflux_ns_kernel(int64_t n, int rs, b200::GasK<T> gas, T tau, BcK<T> bc, ScalVi
         bc_ldg_state<ND, T>(bc, gas.gamma, ul, nn, ur);
         bc_ldg_grad_state<ND, T>(bc, imperm ? ur : ul, nn, gg, gr);
         b200::viscous_flux_add<ND, T>(ur, gr, fvr, gas);
+        // Artificial viscosity of the boundary gradient
+        if (va.base) {
+            const T a = va.base[b200::load_ix(va.map, ix64, i)];
+#pragma unroll
+            for (int d = 0; d < ND; d++)
+#pragma unroll
+                for (int v = 0; v < NV; v++) fvr[d][v] -= a * gr[d][v];
+        }
     }
 
     // Inviscid part: Riemann solve against the ghost state
@@ -447,10 +456,11 @@ template <typename T>
 int bccflux_ns(int ndims, int64_t n, int rs, const b200_gas_t *gas, double tau,
                const b200_bc_t *bc, T *ul_base, const void *ul_map, const T *gl_base,
                const void *gl_map, const void *gl_rstr, int ix64, const T *nl, int64_t ldn,
-               cudaStream_t st) {
+               const T *av_base, const void *av_map, cudaStream_t st) {
     if (n <= 0) return B200_OK;
-    if (!gas || !bc || !bc_type_ok(bc->type))
+    if (!gas || !bc || !bc_type_ok(bc->type) || (av_base && !av_map))
         return b200::set_error(B200_ERR_ARG, "bccflux_ns: bad arguments");
+    ScalView<T> va{const_cast<T *>(av_base), av_map};
     const Gas &g0 = *reinterpret_cast<const Gas *>(gas);
     if (g0.shifted)
         return b200::set_error(B200_ERR_UNSUPPORTED,
@@ -461,9 +471,9 @@ int bccflux_ns(int ndims, int64_t n, int rs, const b200_gas_t *gas, double tau,
     VectView<T> gv{gl_base, gl_map, gl_rstr};
     const unsigned grid = b200::ceil_div(n, BC_BLOCK);
     if (ndims == 2)
-        bccflux_ns_kernel<2, T><<<grid, BC_BLOCK, 0, st>>>(n, rs, g, (T)tau, k, l, gv, ix64, nl, ldn);
+        bccflux_ns_kernel<2, T><<<grid, BC_BLOCK, 0, st>>>(n, rs, g, (T)tau, k, l, gv, ix64, nl, ldn, va);
     else if (ndims == 3)
-        bccflux_ns_kernel<3, T><<<grid, BC_BLOCK, 0, st>>>(n, rs, g, (T)tau, k, l, gv, ix64, nl, ldn);
+        bccflux_ns_kernel<3, T><<<grid, BC_BLOCK, 0, st>>>(n, rs, g, (T)tau, k, l, gv, ix64, nl, ldn, va);
     else
         return b200::set_error(B200_ERR_ARG, "bccflux_ns: ndims must be 2 or 3");
     B200_CHECK_LAUNCH("bccflux_ns");
@@ -544,7 +554,17 @@ int b200_bccflux_ns_f64(int ndims, int64_t n, int rsolver, const b200_gas_t *gas
                         const double *gl_base, const void *gl_map, const void *gl_rstr,
                         int ix64, const double *nl, int64_t ldn, void *stream) {
     return bccflux_ns<double>(ndims, n, rsolver, gas, tau, bc, ul_base, ul_map, gl_base, gl_map,
-                              gl_rstr, ix64, nl, ldn, (cudaStream_t)stream);
+                              gl_rstr, ix64, nl, ldn, nullptr, nullptr, (cudaStream_t)stream);
+}
+
+int b200_bccflux_ns_av_f64(int ndims, int64_t n, int rsolver, const b200_gas_t *gas,
+                           double tau, const b200_bc_t *bc, double *ul_base, const void *ul_map,
+                           const double *gl_base, const void *gl_map, const void *gl_rstr,
+                           int ix64, const double *nl, int64_t ldn, const double *av_base,
+                           const void *av_map, void *stream) {
+    if (!av_base) return b200::set_error(B200_ERR_ARG, "bccflux_ns_av: null viscosity");
+    return bccflux_ns<double>(ndims, n, rsolver, gas, tau, bc, ul_base, ul_map, gl_base, gl_map,
+                          gl_rstr, ix64, nl, ldn, av_base, av_map, (cudaStream_t)stream);
 }
 
 int b200_bccflux_ns_f32(int ndims, int64_t n, int rsolver, const b200_gas_t *gas, double tau,
@@ -552,7 +572,17 @@ int b200_bccflux_ns_f32(int ndims, int64_t n, int rsolver, const b200_gas_t *gas
                         const float *gl_base, const void *gl_map, const void *gl_rstr,
                         int ix64, const float *nl, int64_t ldn, void *stream) {
     return bccflux_ns<float>(ndims, n, rsolver, gas, tau, bc, ul_base, ul_map, gl_base, gl_map,
-                             gl_rstr, ix64, nl, ldn, (cudaStream_t)stream);
+                             gl_rstr, ix64, nl, ldn, nullptr, nullptr, (cudaStream_t)stream);
+}
+
+int b200_bccflux_ns_av_f32(int ndims, int64_t n, int rsolver, const b200_gas_t *gas,
+                           double tau, const b200_bc_t *bc, float *ul_base, const void *ul_map,
+                           const float *gl_base, const void *gl_map, const void *gl_rstr,
+                           int ix64, const float *nl, int64_t ldn, const float *av_base,
+                           const void *av_map, void *stream) {
+    if (!av_base) return b200::set_error(B200_ERR_ARG, "bccflux_ns_av: null viscosity");
+    return bccflux_ns<float>(ndims, n, rsolver, gas, tau, bc, ul_base, ul_map, gl_base, gl_map,
+                          gl_rstr, ix64, nl, ldn, av_base, av_map, (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -147,7 +147,7 @@ template <int ND, typename T>
 __global__ void __launch_bounds__(PW_BLOCK)
 tflux_ns_kernel(int nupts, int64_t neles, b200::GasK<T> gas, const T *__restrict__ u, int64_t ldu,
                 T *__restrict__ f, int64_t ldf, T *__restrict__ gradu, int64_t ldg,
-                ElemGeom<T> geo) {
+                ElemGeom<T> geo, const T *__restrict__ av, int64_t lda) {
     constexpr int NV = ND + 2;
     const int64_t e = (int64_t)blockIdx.x * PW_BLOCK + threadIdx.x;
     const int upt = blockIdx.y;
@@ -186,6 +186,16 @@ tflux_ns_kernel(int nupts, int64_t neles, b200::GasK<T> gas, const T *__restrict
     } else {
         b200::inviscid_flux<ND, T>(uu, ft, p, vel, gas.gamma);
         b200::viscous_flux_add<ND, T>(uu, gr, ft, gas);
+    }
+
+    // Artificial viscosity (pyfr/solvers/baseadvecdiff/kernels/
+    // artvisc.mako: F -= mu_av grad u)
+    if (av) {
+        const T a = av[(int64_t)upt * lda + e];
+#pragma unroll
+        for (int d = 0; d < ND; d++)
+#pragma unroll
+            for (int v = 0; v < NV; v++) ft[d][v] -= a * gr[d][v];
     }
 
 #pragma unroll
@@ -294,7 +304,7 @@ template <int ND, typename T>
 __global__ void __launch_bounds__(PW_BLOCK)
 intcflux_ns_kernel(int64_t n, int rs, b200::GasK<T> gas, T beta, T tau, ScalView<T> vl, ScalView<T> vr,
                    VectView<T> gl, VectView<T> gr, int ix64, const T *__restrict__ nl,
-                   int64_t ldn) {
+                   int64_t ldn, ScalView<T> va) {
     constexpr int NV = ND + 2;
     const int64_t i = (int64_t)blockIdx.x * PW_BLOCK + threadIdx.x;
     if (i >= n) return;
@@ -332,6 +342,9 @@ intcflux_ns_kernel(int64_t n, int rs, b200::GasK<T> gas, T beta, T tau, ScalView
         }
     }
 
+    // Artificial viscosity at the point (the left side's value)
+    const T a = va.base ? va.base[b200::load_ix(va.map, ix64, i)] : T(0);
+
     // LDG viscous common flux from the left and/or right states
     T fvl[ND][NV], fvr[ND][NV];
 #pragma unroll
@@ -353,6 +366,12 @@ intcflux_ns_kernel(int64_t n, int rs, b200::GasK<T> gas, T beta, T tau, ScalView
             b200::viscous_flux_add<ND, T>(ufl, gu, fvl, gas);
         } else {
             b200::viscous_flux_add<ND, T>(ufl, gg, fvl, gas);
+            if (va.base) {
+#pragma unroll
+                for (int d = 0; d < ND; d++)
+#pragma unroll
+                    for (int v = 0; v < NV; v++) fvl[d][v] -= a * gg[d][v];
+            }
         }
     }
     if (beta != T(0.5)) {
@@ -369,6 +388,12 @@ intcflux_ns_kernel(int64_t n, int rs, b200::GasK<T> gas, T beta, T tau, ScalView
             b200::viscous_flux_add<ND, T>(ufr, gu, fvr, gas);
         } else {
             b200::viscous_flux_add<ND, T>(ufr, gg, fvr, gas);
+            if (va.base) {
+#pragma unroll
+                for (int d = 0; d < ND; d++)
+#pragma unroll
+                    for (int v = 0; v < NV; v++) fvr[d][v] -= a * gg[d][v];
+            }
         }
     }
 
@@ -490,18 +515,21 @@ template <typename T>
 int tflux_ns(int ndims, int nupts, int64_t neles, int linear, const b200_gas_t *gas,
              const T *u, int64_t ldu, T *f, int64_t ldf, T *gradu, int64_t ldg, const T *smats,
              int64_t lds, const T *rcpdjac, int64_t ldr, const T *verts, int64_t ldv,
-             const T *upts, int64_t ldup, cudaStream_t st) {
+             const T *upts, int64_t ldup, const T *av, int64_t lda, cudaStream_t st) {
     if (neles <= 0 || nupts <= 0) return B200_OK;
     if (!gas) return b200::set_error(B200_ERR_ARG, "tflux_ns: null gas constants");
+    if (av && reinterpret_cast<const Gas *>(gas)->shifted)
+        return b200::set_error(B200_ERR_UNSUPPORTED,
+                               "tflux_ns: artificial viscosity takes unshifted states");
     int rc = check_geom(linear, smats, rcpdjac, verts, upts, true);
     if (rc) return rc;
     auto geo = make_geom<T>(linear, smats, lds, rcpdjac, ldr, verts, ldv, upts, ldup);
     const auto g = b200::gas_consts<T>(*reinterpret_cast<const Gas *>(gas));
     dim3 grid(b200::ceil_div(neles, PW_BLOCK), nupts);
     if (ndims == 2)
-        tflux_ns_kernel<2, T><<<grid, PW_BLOCK, 0, st>>>(nupts, neles, g, u, ldu, f, ldf, gradu, ldg, geo);
+        tflux_ns_kernel<2, T><<<grid, PW_BLOCK, 0, st>>>(nupts, neles, g, u, ldu, f, ldf, gradu, ldg, geo, av, lda);
     else if (ndims == 3)
-        tflux_ns_kernel<3, T><<<grid, PW_BLOCK, 0, st>>>(nupts, neles, g, u, ldu, f, ldf, gradu, ldg, geo);
+        tflux_ns_kernel<3, T><<<grid, PW_BLOCK, 0, st>>>(nupts, neles, g, u, ldu, f, ldf, gradu, ldg, geo, av, lda);
     else
         return b200::set_error(B200_ERR_ARG, "tflux_ns: ndims must be 2 or 3");
     B200_CHECK_LAUNCH("tflux_ns");
@@ -551,9 +579,13 @@ int intcflux_ns(int ndims, int64_t n, int rsolver, const b200_gas_t *gas, double
                 double tau, T *ul_base, const void *ul_map, T *ur_base, const void *ur_map,
                 const T *gl_base, const void *gl_map, const void *gl_rstr, const T *gr_base,
                 const void *gr_map, const void *gr_rstr, int ix64, const T *nl, int64_t ldn,
-                cudaStream_t st) {
+                const T *av_base, const void *av_map, cudaStream_t st) {
     if (n <= 0) return B200_OK;
     if (!gas) return b200::set_error(B200_ERR_ARG, "intcflux_ns: null gas constants");
+    if (av_base && (!av_map || reinterpret_cast<const Gas *>(gas)->shifted))
+        return b200::set_error(B200_ERR_ARG,
+                               "intcflux_ns: artificial viscosity needs a view and unshifted states");
+    ScalView<T> va{const_cast<T *>(av_base), av_map};
     if (rsolver != b200::RS_RUSANOV && rsolver != b200::RS_HLLC)
         return b200::set_error(B200_ERR_ARG, "intcflux: unknown Riemann solver %d", rsolver);
     ScalView<T> l{ul_base, ul_map}, r{ur_base, ur_map};
@@ -564,9 +596,9 @@ int intcflux_ns(int ndims, int64_t n, int rsolver, const b200_gas_t *gas, double
                                "intcflux_ns: shifted inputs need the Rusanov solver");
     unsigned grid = b200::ceil_div(n, PW_BLOCK);
     if (ndims == 2)
-        intcflux_ns_kernel<2, T><<<grid, PW_BLOCK, 0, st>>>(n, rsolver, g, (T)beta, (T)tau, l, r, gl, gr, ix64, nl, ldn);
+        intcflux_ns_kernel<2, T><<<grid, PW_BLOCK, 0, st>>>(n, rsolver, g, (T)beta, (T)tau, l, r, gl, gr, ix64, nl, ldn, va);
     else if (ndims == 3)
-        intcflux_ns_kernel<3, T><<<grid, PW_BLOCK, 0, st>>>(n, rsolver, g, (T)beta, (T)tau, l, r, gl, gr, ix64, nl, ldn);
+        intcflux_ns_kernel<3, T><<<grid, PW_BLOCK, 0, st>>>(n, rsolver, g, (T)beta, (T)tau, l, r, gl, gr, ix64, nl, ldn, va);
     else
         return b200::set_error(B200_ERR_ARG, "intcflux_ns: ndims must be 2 or 3");
     B200_CHECK_LAUNCH("intcflux_ns");
@@ -613,7 +645,18 @@ int b200_tflux_ns_f64(int ndims, int nupts, int64_t neles, int linear, const b20
                       int64_t ldr, const double *verts, int64_t ldv, const double *upts,
                       int64_t ldup, void *stream) {
     return tflux_ns<double>(ndims, nupts, neles, linear, gas, u, ldu, f, ldf, gradu, ldg, smats,
-                            lds, rcpdjac, ldr, verts, ldv, upts, ldup, (cudaStream_t)stream);
+                            lds, rcpdjac, ldr, verts, ldv, upts, ldup, nullptr, 0,
+                            (cudaStream_t)stream);
+}
+
+int b200_tflux_ns_av_f64(int ndims, int nupts, int64_t neles, int linear, const b200_gas_t *gas,
+                         const double *u, int64_t ldu, double *f, int64_t ldf, double *gradu,
+                         int64_t ldg, const double *smats, int64_t lds, const double *rcpdjac,
+                         int64_t ldr, const double *verts, int64_t ldv, const double *upts,
+                         int64_t ldup, const double *av, int64_t lda, void *stream) {
+    if (!av) return b200::set_error(B200_ERR_ARG, "tflux_ns_av: null viscosity");
+    return tflux_ns<double>(ndims, nupts, neles, linear, gas, u, ldu, f, ldf, gradu, ldg, smats,
+                        lds, rcpdjac, ldr, verts, ldv, upts, ldup, av, lda, (cudaStream_t)stream);
 }
 
 int b200_tflux_ns_f32(int ndims, int nupts, int64_t neles, int linear, const b200_gas_t *gas,
@@ -622,7 +665,18 @@ int b200_tflux_ns_f32(int ndims, int nupts, int64_t neles, int linear, const b20
                       int64_t ldr, const float *verts, int64_t ldv, const float *upts,
                       int64_t ldup, void *stream) {
     return tflux_ns<float>(ndims, nupts, neles, linear, gas, u, ldu, f, ldf, gradu, ldg, smats,
-                           lds, rcpdjac, ldr, verts, ldv, upts, ldup, (cudaStream_t)stream);
+                           lds, rcpdjac, ldr, verts, ldv, upts, ldup, nullptr, 0,
+                            (cudaStream_t)stream);
+}
+
+int b200_tflux_ns_av_f32(int ndims, int nupts, int64_t neles, int linear, const b200_gas_t *gas,
+                         const float *u, int64_t ldu, float *f, int64_t ldf, float *gradu,
+                         int64_t ldg, const float *smats, int64_t lds, const float *rcpdjac,
+                         int64_t ldr, const float *verts, int64_t ldv, const float *upts,
+                         int64_t ldup, const float *av, int64_t lda, void *stream) {
+    if (!av) return b200::set_error(B200_ERR_ARG, "tflux_ns_av: null viscosity");
+    return tflux_ns<float>(ndims, nupts, neles, linear, gas, u, ldu, f, ldf, gradu, ldg, smats,
+                        lds, rcpdjac, ldr, verts, ldv, upts, ldup, av, lda, (cudaStream_t)stream);
 }
 
 int b200_gradcoru_f64(int ndims, int nupts, int64_t neles, int linear, double *gradu,
@@ -681,7 +735,19 @@ int b200_intcflux_ns_f64(int ndims, int64_t n, int rsolver, const b200_gas_t *ga
                          void *stream) {
     return intcflux_ns<double>(ndims, n, rsolver, gas, beta, tau, ul_base, ul_map, ur_base,
                                ur_map, gl_base, gl_map, gl_rstr, gr_base, gr_map, gr_rstr, ix64,
-                               nl, ldn, (cudaStream_t)stream);
+                               nl, ldn, nullptr, nullptr, (cudaStream_t)stream);
+}
+
+int b200_intcflux_ns_av_f64(int ndims, int64_t n, int rsolver, const b200_gas_t *gas,
+                            double beta, double tau, double *ul_base, const void *ul_map,
+                            double *ur_base, const void *ur_map, const double *gl_base,
+                            const void *gl_map, const void *gl_rstr, const double *gr_base,
+                            const void *gr_map, const void *gr_rstr, int ix64, const double *nl,
+                            int64_t ldn, const double *av_base, const void *av_map, void *stream) {
+    if (!av_base) return b200::set_error(B200_ERR_ARG, "intcflux_ns_av: null viscosity");
+    return intcflux_ns<double>(ndims, n, rsolver, gas, beta, tau, ul_base, ul_map, ur_base, ur_map,
+                           gl_base, gl_map, gl_rstr, gr_base, gr_map, gr_rstr, ix64, nl, ldn,
+                           av_base, av_map, (cudaStream_t)stream);
 }
 
 int b200_intcflux_ns_f32(int ndims, int64_t n, int rsolver, const b200_gas_t *gas, double beta,
@@ -692,7 +758,19 @@ int b200_intcflux_ns_f32(int ndims, int64_t n, int rsolver, const b200_gas_t *ga
                          void *stream) {
     return intcflux_ns<float>(ndims, n, rsolver, gas, beta, tau, ul_base, ul_map, ur_base,
                               ur_map, gl_base, gl_map, gl_rstr, gr_base, gr_map, gr_rstr, ix64,
-                              nl, ldn, (cudaStream_t)stream);
+                              nl, ldn, nullptr, nullptr, (cudaStream_t)stream);
+}
+
+int b200_intcflux_ns_av_f32(int ndims, int64_t n, int rsolver, const b200_gas_t *gas,
+                            double beta, double tau, float *ul_base, const void *ul_map,
+                            float *ur_base, const void *ur_map, const float *gl_base,
+                            const void *gl_map, const void *gl_rstr, const float *gr_base,
+                            const void *gr_map, const void *gr_rstr, int ix64, const float *nl,
+                            int64_t ldn, const float *av_base, const void *av_map, void *stream) {
+    if (!av_base) return b200::set_error(B200_ERR_ARG, "intcflux_ns_av: null viscosity");
+    return intcflux_ns<float>(ndims, n, rsolver, gas, beta, tau, ul_base, ul_map, ur_base, ur_map,
+                           gl_base, gl_map, gl_rstr, gr_base, gr_map, gr_rstr, ix64, nl, ldn,
+                           av_base, av_map, (cudaStream_t)stream);
 }
 
 int b200_intconu_f64(int nvars, int64_t n, double beta, const double *lin_base,

@@ -66,6 +66,49 @@ class Mesh:
         return list(self.spts)
 
 
+def vertex_nodes(mesh, tol=1e-9):
+    """Global node numbers of the vertices of every element: per element
+    type an array (nverts, neles), and the number of nodes.  A mesh read
+    from a file numbers them by its node table (``spts_nodes``); otherwise
+    coincident vertices (within ``tol`` of the mesh extent) share a node,
+    numbered by first appearance over the types in ``spts`` order.  As in
+    a mesh file, the two sides of a periodic boundary have distinct
+    nodes."""
+    if mesh.spts_nodes:
+        from pyfr_gb300.native import corner_nodes, _order_from_nnodes
+        from pyfr_gb300.shapes import VERTICES
+        out = {}
+        for et, sn in mesh.spts_nodes.items():
+            nn = sn.shape[1]
+            cn = list(range(nn)) if nn == len(VERTICES[et]) else \
+                corner_nodes(et, _order_from_nnodes(et, nn))
+            out[et] = sn[:, cn].T
+        allv = np.concatenate([v.ravel() for v in out.values()])
+        uniq, inv = np.unique(allv, return_inverse=True)
+        off = 0
+        for et, v in out.items():
+            out[et] = inv[off:off + v.size].reshape(v.shape)
+            off += v.size
+        return out, len(uniq)
+
+    etypes = list(mesh.spts)
+    allpts = np.concatenate([mesh.spts[et].reshape(-1, mesh.ndims)
+                             for et in etypes])
+    scale = max(np.ptp(allpts, axis=0).max(), 1.0)
+    q = np.rint(allpts / (tol*scale)).astype(np.int64)
+    _, first, inv = np.unique(q, axis=0, return_index=True,
+                              return_inverse=True)
+    remap = np.empty(len(first), dtype=np.int64)
+    remap[np.argsort(first)] = np.arange(len(first))
+    nid = remap[inv.ravel()]
+    out, off = {}, 0
+    for et in etypes:
+        nv, ne = mesh.spts[et].shape[:2]
+        out[et] = nid[off:off + nv*ne].reshape(nv, ne)
+        off += nv*ne
+    return out, len(first)
+
+
 def periodic_box(etype, ncells, lo, hi):
     """Uniform periodic box of quads (2-D) or hexes (3-D).
 

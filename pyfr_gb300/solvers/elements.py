@@ -540,10 +540,11 @@ class NavierStokesElements(_WavespeedMixin, _DivergenceMixin, FluidElements,
         kernels['gradcoru_fpts'] = gradcoru_fpts
 
         visc_corr = self.cfg.get('solver', 'viscosity-correction', 'none')
+        sc = self.cfg.get('solver', 'shock-capturing', 'none')
         tplargs = dict(ndims=self.ndims, nvars=self.nvars,
                        nverts=len(self.basis.linspts),
                        c=self.cfg.items_as('constants', float),
-                       shock_capturing='none', visc_corr=visc_corr)
+                       shock_capturing=sc, visc_corr=visc_corr)
         tdisf = []
         for rgn in ('curved', 'linear'):
             if rgn not in r:
@@ -557,10 +558,17 @@ class NavierStokesElements(_WavespeedMixin, _DivergenceMixin, FluidElements,
             kw |= dict(f=s(self._vect_upts, rgn), gradu=s(self._grad_upts, rgn))
             tdisf.append((f'{rgn}-fused', r[rgn], rgn, kw))
 
+        # (artificial viscosity at the solution points: set by the system
+        # before the kernels are made)
+        def avkw(rgn):
+            if sc != 'artificial-viscosity':
+                return {}
+            return dict(artvisc=s(self.artvisc_upts, rgn))
+
         kernels['tdisf_fused'] = lambda uin: self._make_sliced_kernel(
             be.kernel('tflux', tplargs=tplargs | {'ktype': kt},
                       dims=[self.nupts, n], u=s(self.scal_upts[uin], rgn),
-                      **kw)
+                      **kw, **avkw(rgn))
             for kt, n, rgn, kw in tdisf)
 
         self._divergence_kernels()

@@ -124,9 +124,13 @@ class NavierStokesIntInters(BaseIntInters):
         visc_corr = cfg.get('solver', 'viscosity-correction', 'none')
         p_min = cfg.getfloat('solver-interfaces', 'p-min',
                              5*self._be.fpdtype_eps)
+        sc = cfg.get('solver', 'shock-capturing', 'none')
         self._tplargs = dict(ndims=self.ndims, nvars=self.nvars,
                              rsolver=rsolver, visc_corr=visc_corr,
-                             shock_capturing='none', c=self.c, p_min=p_min)
+                             shock_capturing=sc, c=self.c, p_min=p_min)
+        # (the view of the artificial viscosity of the left side, set by
+        # the system when shock capturing is artificial viscosity)
+        self.artvisc = None
 
         be = self._be
         be.pointwise.register('pyfr.solvers.navstokes.kernels.intconu')
@@ -140,7 +144,8 @@ class NavierStokesIntInters(BaseIntInters):
         self.kernels['comm_flux'] = lambda: be.kernel(
             'intcflux', tplargs=self._tplargs, dims=[self.ninterfpts],
             ul=self.scal_lhs, ur=self.scal_rhs,
-            gradul=self._vect_lhs, gradur=self._vect_rhs, nl=self._pnorm_lhs)
+            gradul=self._vect_lhs, gradur=self._vect_rhs, nl=self._pnorm_lhs,
+            **({'artvisc': self.artvisc} if self.artvisc is not None else {}))
 
     def _perm_side(self):
         # For beta = -1/2 order by the right side instead
@@ -269,8 +274,11 @@ class NavierStokesBCInters(BaseBCInters):
         visc_corr = cfg.get('solver', 'viscosity-correction', 'none')
         self._tplargs = dict(ndims=self.ndims, nvars=self.nvars,
                              rsolver=rsolver, visc_corr=visc_corr,
-                             shock_capturing='none', c=self.c,
-                             bctype=self.type, bc=self.bc)
+                             shock_capturing=cfg.get('solver',
+                                                     'shock-capturing',
+                                                     'none'),
+                             c=self.c, bctype=self.type, bc=self.bc)
+        self.artvisc = None
         be.pointwise.register('pyfr.solvers.navstokes.kernels.bcconu')
         be.pointwise.register('pyfr.solvers.navstokes.kernels.bccflux')
         self.kernels['con_u'] = lambda: be.kernel(
@@ -278,4 +286,5 @@ class NavierStokesBCInters(BaseBCInters):
             ulin=self.scal_lhs, ulout=self._comm_lhs, nlin=self._pnorm_lhs)
         self.kernels['comm_flux'] = lambda: be.kernel(
             'bccflux', tplargs=self._tplargs, dims=[self.ninterfpts],
-            ul=self.scal_lhs, gradul=self._vect_lhs, nl=self._pnorm_lhs)
+            ul=self.scal_lhs, gradul=self._vect_lhs, nl=self._pnorm_lhs,
+            **({'artvisc': self.artvisc} if self.artvisc is not None else {}))

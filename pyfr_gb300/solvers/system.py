@@ -127,15 +127,32 @@ class BaseSystem:
             i.scal_lhs = v[0]
             i.scal_rhs = v[1] if len(v) > 1 else None
 
+        # Shock capturing by artificial viscosity: its fields exist before
+        # the flux kernels that read them are made
+        # (pyfr/solvers/baseadvecdiff/system.py:9-34)
+        sc = self.cfg.get('solver', 'shock-capturing', 'none')
+        if sc not in ('none', 'entropy-filter', 'artificial-viscosity'):
+            raise NotImplementedError(f'Shock capturing {sc!r} is not '
+                                      'provided')
+        self._av = None
+        if sc == 'artificial-viscosity':
+            if self.name != 'navier-stokes':
+                raise ValueError('Artificial viscosity needs the '
+                                 'Navier-Stokes system')
+            from pyfr_gb300.solvers.artvisc import ArtificialViscosity
+            self._av = ArtificialViscosity(self, self.cfg)
+            av = {et: e.artvisc_fpts for et, e in self.ele_map.items()}
+            for i, v in zip(self._int_inters + self._bc_inters,
+                            self.make_field_views(av)):
+                i.artvisc = v[0]
+
         self.backend.commit()
         self._gen_kernels()
+        if self._av:
+            self._av.add_kernels(self._kernels, self._ktags)
 
         # Shock capturing by the entropy filter
         # (pyfr/solvers/baseadvec/system.py:36-44)
-        sc = self.cfg.get('solver', 'shock-capturing', 'none')
-        if sc not in ('none', 'entropy-filter'):
-            raise NotImplementedError(f'Shock capturing {sc!r} is not '
-                                      'provided')
         self._ef = None
         if sc == 'entropy-filter':
             from pyfr_gb300.solvers.entfilter import EntropyFilter
@@ -327,6 +344,12 @@ class NavierStokesSystem(BaseSystem):
         kdeps = k['eles/copy_fpts'] or k['eles/disu']
         g_soln.add_all(k['iint/con_u'], deps=kdeps)
         g_soln.add_all(k['bcint/con_u'], deps=kdeps)
+        # Artificial viscosity: zero the vertex values, sense every
+        # element, then fill the point values once all sensors are done
+        # (pyfr/solvers/baseadvecdiff/artvisc.py:246-264)
+        g_soln.add_all(k['vtx/vtx_zero'])
+        g_soln.add_all(k['eles/shocksensor'], deps=k['vtx/vtx_zero'])
+        g_soln.add_all(k['eles/avfill'], deps=k['eles/shocksensor'])
         g_soln.commit()
 
         if k['eles/tgradcoru_upts_cat']:
