@@ -213,7 +213,9 @@ int b200_tflux_euler_f32(int ndims, int nupts, int64_t neles, int linear, double
 
 /* Navier-Stokes fused gradient transform + transformed flux;
  * pyfr/solvers/navstokes/kernels/tflux.mako:13-50, provider call
- * pyfr/solvers/navstokes/elements.py:64-128.  gradu is updated in place. */
+ * pyfr/solvers/navstokes/elements.py:64-128.  gradu is updated in place.
+ * With gradu NULL (the unfused kernel of flux anti-aliasing) f holds the
+ * physical gradient at the points on entry, and rcpdjac is not read. */
 int b200_tflux_ns_f64(int ndims, int nupts, int64_t neles, int linear, const b200_gas_t *gas,
                       const double *u, int64_t ldu, double *f, int64_t ldf, double *gradu,
                       int64_t ldg, const double *smats, int64_t lds, const double *rcpdjac,

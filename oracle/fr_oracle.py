@@ -509,14 +509,24 @@ class Discretisation:
         if grads_out is not None:
             grads_out.append(g)
 
-        # Flux at the solution points
-        ut = u.transpose(1, 0, 2)
+        # Flux at the solution points or, with flux anti-aliasing, at the
+        # quadrature points from the interpolated solution and physical
+        # gradient (pyfr/solvers/baseadvecdiff/elements.py:103-116); the
+        # artificial viscosity av['opu'] is then taken at those points
+        if self.aa is not None:
+            m7 = self.aa['M7']
+            uq = self.apply(m7, u)
+            gq = np.stack([self.apply(m7, g[d]) for d in range(nd)])
+            ut, gt, sm = uq.transpose(1, 0, 2), gq.transpose(0, 2, 1, 3), \
+                self.smats_q
+        else:
+            ut, gt, sm = u.transpose(1, 0, 2), g.transpose(0, 2, 1, 3), \
+                self.smats_u
         fi, _, _ = inviscid_flux(ut, gamma)
-        gt = g.transpose(0, 2, 1, 3)
         fv = viscous_flux(ut, gt, c)
         if av is not None:
             fv = fv - avu[None, None]*gt
-        ft = self._transform_flux((fi + fv).transpose(0, 2, 1, 3))
+        ft = np.einsum('pike,kpve->ipve', sm, (fi + fv).transpose(0, 2, 1, 3))
 
         # Physical gradient at the flux points and the common flux
         gf = np.stack([self.apply(self.ops['M0'], g[d]) for d in range(nd)])
@@ -552,7 +562,11 @@ class Discretisation:
         for (fp, ee, *_), f in zip(self.bcs, bflux):
             uf[fp, :, ee] = f.T
 
-        r = self.apply(self.ops['M132'], ft.reshape(nd*nupts, -1, ne))
+        if self.aa is not None:
+            r = self.apply(self.aa['M1329'],
+                           ft.reshape(nd*len(self.aa['qpts']), -1, ne))
+        else:
+            r = self.apply(self.ops['M132'], ft.reshape(nd*nupts, -1, ne))
         r += self.apply(self.ops['M3'], uf)
         return -r/self.djac_u[:, None, :]
 

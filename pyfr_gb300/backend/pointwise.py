@@ -175,9 +175,10 @@ class PointwiseKernelProvider:
         av_on = tplargs.get('shock_capturing') == 'artificial-viscosity'
         if av_on != (artvisc is not None):
             raise ValueError('Artificial viscosity needs its field')
-        if 'fused' not in tplargs.get('ktype', ''):
-            raise NotImplementedError('Only the fused gradient/flux form of '
-                                      'the Navier-Stokes flux is provided')
+        # Unfused (flux anti-aliasing): f holds the physical gradient
+        if ('fused' in tplargs.get('ktype', '')) != (gradu is not None):
+            raise ValueError('The fused flux takes gradu, the unfused one '
+                             'its gradient in f')
 
         nupts, neles = dims
         lin, (sp, sl), (rp, rl), (vp, vl), (upp, upl) = self._geom(

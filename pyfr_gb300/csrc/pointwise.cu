@@ -153,25 +153,36 @@ tflux_ns_kernel(int nupts, int64_t neles, b200::GasK<T> gas, const T *__restrict
     const int upt = blockIdx.y;
     if (e >= neles) return;
 
+    // Fused form: the corrected reference gradient is in gradu and is
+    // transformed here (and written back); otherwise (flux anti-aliasing)
+    // the physical gradient at the point is in f, which the flux replaces
+    const bool fused = gradu != nullptr;
     T s[ND][ND], rcp;
-    elem_metrics<ND, T>(geo, nupts, upt, e, s, rcp, true);
+    elem_metrics<ND, T>(geo, nupts, upt, e, s, rcp, fused);
 
-    // Transform the corrected reference gradient to physical space, in place
-    T tg[ND][NV], gr[ND][NV];
+    T gr[ND][NV];
+    if (fused) {
+        T tg[ND][NV];
 #pragma unroll
-    for (int d = 0; d < ND; d++)
+        for (int d = 0; d < ND; d++)
 #pragma unroll
-        for (int v = 0; v < NV; v++) tg[d][v] = gradu[(int64_t)(d * nupts + upt) * ldg + soa_off(e, v, NV)];
+            for (int v = 0; v < NV; v++) tg[d][v] = gradu[(int64_t)(d * nupts + upt) * ldg + soa_off(e, v, NV)];
 #pragma unroll
-    for (int i = 0; i < ND; i++)
+        for (int i = 0; i < ND; i++)
 #pragma unroll
-        for (int j = 0; j < NV; j++) {
-            T acc = 0;
+            for (int j = 0; j < NV; j++) {
+                T acc = 0;
 #pragma unroll
-            for (int k = 0; k < ND; k++) acc += s[k][i] * tg[k][j];
-            gr[i][j] = rcp * acc;
-            gradu[(int64_t)(i * nupts + upt) * ldg + soa_off(e, j, NV)] = gr[i][j];
-        }
+                for (int k = 0; k < ND; k++) acc += s[k][i] * tg[k][j];
+                gr[i][j] = rcp * acc;
+                gradu[(int64_t)(i * nupts + upt) * ldg + soa_off(e, j, NV)] = gr[i][j];
+            }
+    } else {
+#pragma unroll
+        for (int d = 0; d < ND; d++)
+#pragma unroll
+            for (int v = 0; v < NV; v++) gr[d][v] = f[(int64_t)(d * nupts + upt) * ldf + soa_off(e, v, NV)];
+    }
 
     T uu[NV];
 #pragma unroll
@@ -521,7 +532,7 @@ int tflux_ns(int ndims, int nupts, int64_t neles, int linear, const b200_gas_t *
     if (av && reinterpret_cast<const Gas *>(gas)->shifted)
         return b200::set_error(B200_ERR_UNSUPPORTED,
                                "tflux_ns: artificial viscosity takes unshifted states");
-    int rc = check_geom(linear, smats, rcpdjac, verts, upts, true);
+    int rc = check_geom(linear, smats, rcpdjac, verts, upts, gradu != nullptr);
     if (rc) return rc;
     auto geo = make_geom<T>(linear, smats, lds, rcpdjac, ldr, verts, ldv, upts, ldup);
     const auto g = b200::gas_consts<T>(*reinterpret_cast<const Gas *>(gas));

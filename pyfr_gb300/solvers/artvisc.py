@@ -70,7 +70,11 @@ class ArtificialViscosity:
             b = e.basis
             e.artvisc_fpts = be.matrix((e.nfpts, e.neles), tags={'align'},
                                        extent=system.nonce + 'artvisc_fpts')
-            e.artvisc_upts = be.matrix((e.nupts, e.neles), tags={'align'})
+            # (at the points of the volume flux: the solution points, or
+            # the quadrature points with flux anti-aliasing)
+            fpts_vol = b.qpts if e.antialias else b.upts
+            e.artvisc_upts = be.matrix((len(fpts_vol), e.neles),
+                                       tags={'align'})
 
             ub, order = b.ubasis, b.order
             degs, ind, w, bd = sensor_params(ub, order)
@@ -93,7 +97,7 @@ class ArtificialViscosity:
                 vnodes=be.const_matrix(vnodes[et].astype(np.int32),
                                        dtype=np.int32, tags={'align'}),
                 opf=be.const_matrix(linear_shape_fn(et, b.fpts)),
-                opu=be.const_matrix(linear_shape_fn(et, b.upts)))
+                opu=be.const_matrix(linear_shape_fn(et, fpts_vol)))
         be.commit()
 
     def _sfx(self):

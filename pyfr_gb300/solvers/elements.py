@@ -471,9 +471,6 @@ class NavierStokesElements(_WavespeedMixin, _DivergenceMixin, FluidElements,
     _scratch_bufs = {'scal_fpts', 'vect_fpts', 'vect_upts', 'grad_upts'}
 
     def set_backend(self, backend, nonce, linoff):
-        if self.antialias:
-            raise NotImplementedError('Flux anti-aliasing is provided for '
-                                      'the Euler equations only')
         super().set_backend(backend, nonce, linoff)
         be, kernels = self._be, self.kernels
 
@@ -506,6 +503,34 @@ class NavierStokesElements(_WavespeedMixin, _DivergenceMixin, FluidElements,
                 out=self._grad_upts, beta=1.0)
 
         r, s = self.mesh_regions, self._slice_mat
+        if self.antialias:
+            # Flux anti-aliasing: the solution and the physical gradient
+            # interpolated to the quadrature points, where the unfused flux
+            # kernel runs (pyfr/solvers/baseadvecdiff/elements.py:103-116,
+            # pyfr/solvers/navstokes/elements.py:60-123)
+            nd, nq = self.ndims, self.basis.nqpts
+            self._scal_qpts = be.matrix((nq, self.nvars, self.neles),
+                                        tags={'align'},
+                                        extent=self._nonce + 'scal_qpts')
+            self._vect_qpts = be.matrix((nd, nq, self.nvars, self.neles),
+                                        tags={'align'},
+                                        extent=self._nonce + 'vect_qpts')
+            kernels['qptsu'] = lambda uin: be.kernel(
+                'mul', self.opmat('M7'), self.scal_upts[uin],
+                out=self._scal_qpts)
+
+            def gradcoru_qpts():
+                nupts, vu, vq = self.nupts, self._grad_upts, self._vect_qpts
+                if be.fuse_operators:
+                    return be.kernel('mul_batched', self.opmat('M7'), vu, vq,
+                                     nbatch=self.ndims)
+                return be.unordered_meta_kernel([
+                    be.kernel('mul', self.opmat('M7'),
+                              vu.slice(i*nupts, (i + 1)*nupts),
+                              vq.slice(i*nq, (i + 1)*nq))
+                    for i in range(self.ndims)])
+            kernels['gradcoru_qpts'] = gradcoru_qpts
+
         gtpl = dict(ndims=self.ndims, nvars=self.nvars,
                     nverts=len(self.basis.linspts))
         gradcoru_u = []
@@ -545,30 +570,46 @@ class NavierStokesElements(_WavespeedMixin, _DivergenceMixin, FluidElements,
                        nverts=len(self.basis.linspts),
                        c=self.cfg.items_as('constants', float),
                        shock_capturing=sc, visc_corr=visc_corr)
+        aa = self.antialias
+        pts = 'qpts' if aa else 'upts'
+        npts = self.basis.nqpts if aa else self.nupts
         tdisf = []
         for rgn in ('curved', 'linear'):
             if rgn not in r:
                 continue
-            kw = dict(upts=self.upts)
+            kw = dict(upts=getattr(self, pts))
             if rgn == 'curved':
-                kw |= dict(smats=self.curved_smat_at('upts'),
-                           rcpdjac=self.rcpdjac_at('upts', 'curved'))
+                kw |= dict(smats=self.curved_smat_at(pts))
+                if not aa:
+                    kw |= dict(rcpdjac=self.rcpdjac_at('upts', 'curved'))
             else:
                 kw |= dict(verts=self.ploc_at('linspts', 'linear'))
-            kw |= dict(f=s(self._vect_upts, rgn), gradu=s(self._grad_upts, rgn))
-            tdisf.append((f'{rgn}-fused', r[rgn], rgn, kw))
+            if aa:
+                kw |= dict(f=s(self._vect_qpts, rgn))
+                tdisf.append((rgn, r[rgn], rgn, kw))
+            else:
+                kw |= dict(f=s(self._vect_upts, rgn),
+                           gradu=s(self._grad_upts, rgn))
+                tdisf.append((f'{rgn}-fused', r[rgn], rgn, kw))
 
-        # (artificial viscosity at the solution points: set by the system
+        # (artificial viscosity at the points of the flux: set by the system
         # before the kernels are made)
         def avkw(rgn):
             if sc != 'artificial-viscosity':
                 return {}
             return dict(artvisc=s(self.artvisc_upts, rgn))
 
-        kernels['tdisf_fused'] = lambda uin: self._make_sliced_kernel(
-            be.kernel('tflux', tplargs=tplargs | {'ktype': kt},
-                      dims=[self.nupts, n], u=s(self.scal_upts[uin], rgn),
-                      **kw, **avkw(rgn))
-            for kt, n, rgn, kw in tdisf)
+        if aa:
+            kernels['tdisf'] = lambda: self._make_sliced_kernel(
+                be.kernel('tflux', tplargs=tplargs | {'ktype': kt},
+                          dims=[npts, n], u=s(self._scal_qpts, rgn), **kw,
+                          **avkw(rgn))
+                for kt, n, rgn, kw in tdisf)
+        else:
+            kernels['tdisf_fused'] = lambda uin: self._make_sliced_kernel(
+                be.kernel('tflux', tplargs=tplargs | {'ktype': kt},
+                          dims=[npts, n], u=s(self.scal_upts[uin], rgn),
+                          **kw, **avkw(rgn))
+                for kt, n, rgn, kw in tdisf)
 
         self._divergence_kernels()

@@ -352,6 +352,8 @@ class NavierStokesSystem(BaseSystem):
         g_soln.add_all(k['eles/avfill'], deps=k['eles/shocksensor'])
         g_soln.commit()
 
+        if k['eles/qptsu']:
+            return (g_soln,) + self._rhs_graphs_antialias(k, deps)
         if k['eles/tgradcoru_upts_cat']:
             return (g_soln,) + self._rhs_graphs_fused(k, deps)
 
@@ -391,6 +393,47 @@ class NavierStokesSystem(BaseSystem):
         g_div.commit()
 
         return g_soln, g_grad_flux, g_div
+
+    def _rhs_graphs_antialias(self, k, deps):
+        """Graphs 2 and 3 with flux anti-aliasing
+        (pyfr/solvers/baseadvecdiff/system.py:107-200 without gradient
+        fusion): the corrected gradient, transformed in place to physical
+        space, goes to the flux points and to the quadrature points, where
+        the flux is evaluated with the interpolated solution; the
+        divergence projects it back with M9."""
+        g = self.backend.graph()
+        if k['eles/tgradcoru_upts_cat']:
+            g.add_all(k['eles/tgradcoru_upts_cat'])
+            gdeps = 'eles/tgradcoru_upts_cat'
+        else:
+            g.add_all(k['eles/tgradpcoru_upts'])
+            for l in k['eles/tgradcoru_upts']:
+                g.add(l, deps=deps(l, 'eles/tgradpcoru_upts'))
+            gdeps = 'eles/tgradcoru_upts'
+        for l in k['eles/gradcoru_u']:
+            g.add(l, deps=deps(l, gdeps))
+        for l in k['eles/gradcoru_fpts']:
+            g.add(l, deps=deps(l, 'eles/gradcoru_u'))
+        for l in k['eles/gradcoru_qpts']:
+            g.add(l, deps=deps(l, 'eles/gradcoru_u'))
+        g.add_all(k['eles/qptsu'])
+        g.add_all(k['iint/comm_flux'], deps=k['eles/gradcoru_fpts'])
+        g.add_all(k['bcint/comm_flux'], deps=k['eles/gradcoru_fpts'])
+        for l in k['eles/tdisf']:
+            g.add(l, deps=deps(l, 'eles/gradcoru_qpts', 'eles/qptsu'))
+        for l in k['eles/tdivtpcorf']:
+            g.add(l, deps=deps(l, 'eles/tdisf'))
+        g.commit()
+
+        g_div = self.backend.graph()
+        if k['eles/tdivtconf_cat']:
+            g_div.add_all(k['eles/tdivtconf_cat'])
+        else:
+            g_div.add_all(k['eles/tdivtconf'])
+            for l in k['eles/negdivconf']:
+                g_div.add(l, deps=deps(l, 'eles/tdivtconf'))
+        g_div.commit()
+        return g, g_div
 
     def _rhs_graphs_fused(self, k, deps):
         """Graphs 2 and 3 with fused operator applies: the corrected

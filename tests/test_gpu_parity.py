@@ -142,6 +142,62 @@ def test_euler_rhs_flux_antialiasing(built, golden, case, etype, graphs):
     assert _relerr(r, d.rhs_euler(ics, dict(gamma=1.4))) < TOL
 
 
+@pytest.mark.parametrize('case,etype', [('quad_p3', 'quad'), ('hex_p3', 'hex')])
+@pytest.mark.parametrize('artvisc', [False, True])
+def test_ns_rhs_flux_antialiasing(built, golden, case, etype, artvisc):
+    """Navier-Stokes flux anti-aliasing: the solution and the physical
+    gradient interpolated to the quadrature points, the unfused flux there
+    (with the artificial viscosity at those points), projected back by M9,
+    on distorted meshes against the oracle with the reference's
+    operators."""
+    from pyfr_gb300.inifile import Inifile
+    from pyfr_gb300.mesh import vertex_nodes
+    from pyfr_gb300.shapes import get_shape, linear_shape_fn
+    from pyfr_gb300.solvers.artvisc import sensor_params
+    from pyfr_gb300.solvers.system import NavierStokesSystem
+    g = golden[f'geometry_{case}']
+    mesh = _golden_mesh(g, etype)
+    nd = mesh.ndims
+    c = dict(gamma=1.4, mu=0.05, Pr=0.72, **{'ldg-beta': 0.5,
+                                             'ldg-tau': 0.1})
+    cfg = Inifile()
+    for k in ('gamma', 'mu', 'Pr'):
+        cfg.set('constants', k, c[k])
+    cfg.set('solver', 'order', 3)
+    cfg.set('solver', 'anti-alias', 'flux')
+    cfg.set('solver-interfaces', 'riemann-solver', 'rusanov')
+    cfg.set('solver-interfaces', 'ldg-beta', 0.5)
+    cfg.set('solver-interfaces', 'ldg-tau', 0.1)
+    avc = {'max-artvisc': 0.02, 'kappa': 1.5, 's0': 0.01}
+    if artvisc:
+        cfg.set('solver', 'shock-capturing', 'artificial-viscosity')
+        for k, v in avc.items():
+            cfg.set('solver-artificial-viscosity', k, v)
+    ics = g['ics'][:, :nd + 2]
+    s = NavierStokesSystem(_backend(cfg, True), mesh, {etype: ics}, 2, cfg)
+    s.commit()
+    s.rhs(0.0, 0, 1)
+    (r,) = s.ele_scal_upts(1)
+
+    ops = ops_from_golden(golden['operators'], f'{etype}_p3_gauss-legendre',
+                          ns=True)
+    ref = golden['operators']
+    aa = dict(M7=ref[f'{etype}_p3_aa/m7'], M1329=ref[f'{etype}_p3_aa/M1329'],
+              qpts=ref[f'{etype}_p3_aa/qpts'])
+    shp = get_shape(etype, 3)
+    av = None
+    if artvisc:
+        degs, *_ = sensor_params(shp.ubasis, 3)
+        vn, nn = vertex_nodes(mesh)
+        av = dict(invvdm=np.linalg.inv(shp.ubasis.vdm).T, degs=degs, order=3,
+                  c=avc, vnodes=vn[etype], nnodes=nn,
+                  opf=linear_shape_fn(etype, shp.fpts),
+                  opu=linear_shape_fn(etype, aa['qpts']))
+    d = Discretisation(ops, basis_of(shp), g['spts'], g['lhs'], g['rhs'],
+                       periods=(2.0,)*nd, aa=aa)
+    assert _relerr(r, d.rhs_ns(ics, c, av=av)) < TOL
+
+
 def test_ns_rhs_distorted_hex_reference_geometry(built, golden):
     from pyfr_gb300.inifile import Inifile
     from pyfr_gb300.solvers.system import NavierStokesSystem
