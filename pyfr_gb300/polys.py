@@ -168,3 +168,123 @@ def tidy(arr, tol=1e-10):
             flat[idx] = np.copysign(rep, flat[idx])
 
     return a
+
+
+def jacobi_orthonormal(order, a, b, x):
+    """Jacobi polynomials P_k^(a,b)(x), k = 0..order, normalised to unit
+    norm under the weight (1 - x)^a (1 + x)^b on [-1, 1]; shape
+    (order + 1, len(x)).  The standard three-term recurrence in its
+    orthonormal form (as in Hesthaven and Warburton, Nodal Discontinuous
+    Galerkin Methods, 2008, appendix A)."""
+    from math import gamma as G
+    x = np.asarray(x, dtype=float)
+    p = np.zeros((order + 1,) + x.shape)
+    g0 = 2**(a + b + 1)/(a + b + 1)*G(a + 1)*G(b + 1)/G(a + b + 1)
+    p[0] = 1/np.sqrt(g0)
+    if order == 0:
+        return p
+    g1 = (a + 1)*(b + 1)/(a + b + 3)*g0
+    p[1] = ((a + b + 2)*x/2 + (a - b)/2)/np.sqrt(g1)
+    aold = 2/(2 + a + b)*np.sqrt((a + 1)*(b + 1)/(a + b + 3))
+    for n in range(1, order):
+        h1 = 2*n + a + b
+        anew = 2/(h1 + 2)*np.sqrt((n + 1)*(n + 1 + a + b)*(n + 1 + a) *
+                                  (n + 1 + b)/((h1 + 1)*(h1 + 3)))
+        bnew = -(a*a - b*b)/(h1*(h1 + 2))
+        p[n + 1] = ((x - bnew)*p[n] - aold*p[n - 1])/anew
+        aold = anew
+    return p
+
+
+class SimplexOrthoBasis:
+    """The collapsed-coordinate orthonormal (Proriol-Koornwinder-Dubiner)
+    bases of the triangle, tetrahedron and prism, with their degree tuples
+    in the reference's order (``pyfr/polys.py:112-330``): on the triangle
+    psi_ij = sqrt(2) P_i(a) P_j^(2i+1,0)(b) (1 - b)^i, on the tetrahedron
+    psi_ijk = 2 sqrt(2) P_i(a) P_j^(2i+1,0)(b) (1 - b)^i
+    P_k^(2i+2j+2,0)(c) (1 - c)^(i+j), on the prism the triangle's modes
+    times the line's, each factor orthonormal (Sherwin and Karniadakis,
+    Spectral/hp Element Methods, 2005, ch. 3; Hesthaven and Warburton
+    2008, ch. 6 and 10).  Orthonormal on the reference elements; used where
+    a filter or sensor groups modes by degree, which depends on the basis
+    (the operators do not)."""
+
+    def __init__(self, kind, order, pts=None):
+        self.kind, self.order = kind, order
+        p = order
+        if kind == 'tri':
+            self.degrees = [(i, j) for i in range(p + 1)
+                            for j in range(p - i + 1)]
+        elif kind == 'tet':
+            self.degrees = [(i, j, k) for i in range(p + 1)
+                            for j in range(p - i + 1)
+                            for k in range(p - i - j + 1)]
+        elif kind == 'pri':
+            self.degrees = [(i, j, k) for i in range(p + 1)
+                            for j in range(p - i + 1) for k in range(p + 1)]
+        else:
+            raise ValueError(f'No simplex basis for {kind!r}')
+        self.pts = None if pts is None else np.asarray(pts, dtype=float)
+
+    @staticmethod
+    def _tri(p, r, s):
+        with np.errstate(divide='ignore', invalid='ignore'):
+            a = np.where(s != 1, 2*(1 + r)/(1 - s) - 1, -1.0)
+        pa = jacobi_orthonormal(p, 0, 0, a)
+        out = []
+        for i in range(p + 1):
+            pb = jacobi_orthonormal(p - i, 2*i + 1, 0, s)
+            for j in range(p - i + 1):
+                out.append(np.sqrt(2)*pa[i]*pb[j]*(1 - s)**i)
+        return out
+
+    def ortho_basis_at(self, pts):
+        pts = np.atleast_2d(np.asarray(pts, dtype=float))
+        p = self.order
+        if self.kind == 'tri':
+            r, s = pts.T
+            return np.array(self._tri(p, r, s))
+        if self.kind == 'pri':
+            r, s, t = pts.T
+            tri = self._tri(p, r, s)
+            line = jacobi_orthonormal(p, 0, 0, t)
+            return np.array([f*line[k] for f in tri for k in range(p + 1)])
+        r, s, t = pts.T
+        with np.errstate(divide='ignore', invalid='ignore'):
+            a = np.where(s + t != 0, -2*(1 + r)/(s + t) - 1, -1.0)
+            b = np.where(t != 1, 2*(1 + s)/(1 - t) - 1, -1.0)
+        pa = jacobi_orthonormal(p, 0, 0, a)
+        out = []
+        for i in range(p + 1):
+            pb = jacobi_orthonormal(p - i, 2*i + 1, 0, b)
+            for j in range(p - i + 1):
+                pc = jacobi_orthonormal(p - i - j, 2*(i + j + 1), 0, t)
+                for k in range(p - i - j + 1):
+                    out.append(2*np.sqrt(2)*pa[i]*pb[j]*(1 - b)**i *
+                               pc[k]*(1 - t)**(i + j))
+        return np.array(out)
+
+    @property
+    def vdm(self):
+        return self.ortho_basis_at(self.pts)
+
+    @property
+    def modes(self):
+        return self.degrees
+
+
+def modal_basis(shape):
+    """The orthonormal modal basis whose degree groups a filter or sensor
+    works with: the Legendre products of a quadrilateral or hexahedron (the
+    shape's own basis), the collapsed-coordinate bases of the other types.
+    Returns (basis at the solution points, degree tuples of its modes,
+    degree tuples of the basis one order lower)."""
+    if shape.name in ('quad', 'hex'):
+        ub = shape.ubasis
+        lower = [m for m in ub.modes if max(m) < shape.order]
+        return ub, list(ub.modes), lower
+    b = SimplexOrthoBasis(shape.name, shape.order, shape.upts)
+    lower = SimplexOrthoBasis(shape.name, shape.order - 1).degrees \
+        if shape.order > 0 else []
+    return b, b.degrees, lower
+

@@ -13,9 +13,8 @@ The sensor (``pyfr/solvers/baseadvecdiff/kernels/shocksensor.mako``) is the
 Klockner-Warburton-Hesthaven decay fit from order 2 up and the
 Persson-Peraire modal ratio at order 1, with the constants ``max-artvisc``,
 ``kappa`` and ``s0`` of ``[solver-artificial-viscosity]``.  It works on the
-orthonormal modes grouped by degree, so it is provided for quadrilaterals
-and hexahedra (orthonormal Legendre products, the reference's modes), with
-the plain integrator.
+orthonormal modes grouped by degree (``modal_basis``: the reference's modes
+for every element type), with the plain integrator.
 """
 
 import ctypes as C
@@ -26,15 +25,18 @@ import numpy as np
 from pyfr_gb300.backend.lib import AV
 from pyfr_gb300.backend.types import Kernel
 from pyfr_gb300.mesh import vertex_nodes
+from pyfr_gb300.polys import modal_basis
 from pyfr_gb300.shapes import linear_shape_fn
 
 
-def sensor_params(ubasis, order):
-    """The sensor's per-mode degree (the largest of the mode's degrees),
-    highest-degree flags, and the decay-fit weights and baseline decay
-    of degrees 1..order (pyfr/solvers/baseadvecdiff/artvisc.py:160-196)."""
-    degs = [max(m) for m in ubasis.modes]
-    ind = [int(d == order) for d in degs]
+def sensor_params(modes, lower, order):
+    """The sensor's per-mode degree (the largest entry of the mode's
+    degree tuple), the flags of the modes missing from the basis one order
+    lower, and the decay-fit weights and baseline decay of degrees
+    1..order (pyfr/solvers/baseadvecdiff/artvisc.py:160-196)."""
+    degs = [max(m) for m in modes]
+    low = set(map(tuple, lower))
+    ind = [int(tuple(m) not in low) for m in modes]
     fit = list(range(1, order + 1))
     if len(fit) >= 2:
         x = np.log(np.array(fit, dtype=float) + 1)
@@ -64,9 +66,6 @@ class ArtificialViscosity:
 
         self._params = {}
         for et, e in system.ele_map.items():
-            if et not in ('quad', 'hex'):
-                raise NotImplementedError('Artificial viscosity is provided '
-                                          'for quadrilaterals and hexahedra')
             b = e.basis
             e.artvisc_fpts = be.matrix((e.nfpts, e.neles), tags={'align'},
                                        extent=system.nonce + 'artvisc_fpts')
@@ -76,8 +75,9 @@ class ArtificialViscosity:
             e.artvisc_upts = be.matrix((len(fpts_vol), e.neles),
                                        tags={'align'})
 
-            ub, order = b.ubasis, b.order
-            degs, ind, w, bd = sensor_params(ub, order)
+            ub, modes, lower = modal_basis(b)
+            order = b.order
+            degs, ind, w, bd = sensor_params(modes, lower, order)
             invvdm = np.linalg.inv(ub.vdm).T               # (nmodes, nupts)
             nv = vnodes[et].shape[0]
             p = AV(nupts=e.nupts, nvars=e.nvars,

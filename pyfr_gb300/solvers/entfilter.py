@@ -10,9 +10,10 @@ boundaries the smaller of theirs and their ghost state's.  Before the first
 step the minima are formed without filtering, and every step ends with a
 filter of the new solution.
 
-The filter acts on the orthonormal modes grouped by degree, so it is
-provided for quadrilaterals and hexahedra (orthonormal Legendre products,
-the reference's modes).
+The filter acts on the orthonormal modes grouped by the largest entry of
+their degree tuples: Legendre products on quadrilaterals and hexahedra,
+the collapsed-coordinate bases on triangles, tetrahedra and prisms (the
+reference's modes, ``pyfr/polys.py``).
 """
 
 import ctypes as C
@@ -21,6 +22,7 @@ import numpy as np
 
 from pyfr_gb300.backend.lib import EF
 from pyfr_gb300.backend.types import Kernel
+from pyfr_gb300.polys import modal_basis
 
 
 class EntropyFilter:
@@ -42,9 +44,6 @@ class EntropyFilter:
 
         self.entmin, self.ef_filter, self._params = {}, {}, {}
         for et, e in system.ele_map.items():
-            if et not in ('quad', 'hex'):
-                raise NotImplementedError('The entropy filter is provided for '
-                                          'quadrilaterals and hexahedra')
             b = e.basis
             nfaces = len(b.faces)
             init = np.full((nfaces, e.neles), -be.fpdtype_max)
@@ -53,13 +52,13 @@ class EntropyFilter:
                                         tags={'align'})
             self.ef_filter[et] = be.matrix((1, e.neles), tags={'align'})
 
-            ub = b.ubasis
+            ub, modes, _ = modal_basis(b)
             vdm = ub.vdm                                   # (nmodes, nupts)
             invvdm = np.linalg.inv(vdm)                    # (nupts, nmodes)
             fin = bool(np.all(np.count_nonzero(b.m0, axis=1) == 1))
             vdm_ef = vdm.T if fin else \
                 np.vstack([vdm.T, ub.ortho_basis_at(b.fpts).T])
-            degs = np.array([max(m) for m in ub.modes], dtype=np.int32)
+            degs = np.array([max(m) for m in modes], dtype=np.int32)
 
             # Jacobian-weighted element mean (pyfr/solvers/base/elements.py:
             # 331-335)

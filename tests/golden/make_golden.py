@@ -15,6 +15,7 @@ What is generated (all with the reference's own code):
   the hex p=3 Gauss-Legendre matrices are checked against the reference's
   own golden file ``pyfr/tests/hex-gleg-ord3.npz`` (its unit test
   ``pyfr/tests/test_ele_mats.py``).
+* ``bases.npz``: the orthonormal simplex bases at the solution points.
 * ``geometry_<case>.npz``: element geometry computed by the reference's
   ``EulerElements``/``NavierStokesElements`` (``pyfr/solvers/base/elements.py``)
   on small periodic meshes whose interior vertices are randomly perturbed
@@ -308,9 +309,33 @@ def make_mixed():
     np.savez_compressed(HERE / 'operators.npz', **ops)
 
 
+def make_bases():
+    """``bases.npz``: the reference's orthonormal simplex bases
+    (``pyfr.polys``) at the solution points of tri, tet and pri at orders
+    1-4 (their degree tuples too), which the entropy filter and the shock
+    sensor group by degree."""
+    from pyfr.polys import get_polybasis
+    from pyfr.quadrules import get_quadrule
+
+    rules = {'tri': 'alpha-opt', 'tet': 'alpha-opt',
+             'pri': 'alpha-opt~gauss-legendre-lobatto'}
+    out = {}
+    for kind, rule in rules.items():
+        for p in range(1, 5):
+            npts = len(get_polybasis(kind, p, None).degrees)
+            pts = get_quadrule(kind, rule, npts).pts
+            b = get_polybasis(kind, p, pts)
+            out[f'{kind}_p{p}/pts'] = np.asarray(pts)
+            out[f'{kind}_p{p}/vdm'] = np.asarray(b.vdm)
+            out[f'{kind}_p{p}/degrees'] = np.asarray(b.degrees)
+    np.savez_compressed(HERE / 'bases.npz', **out)
+    print('bases.npz')
+
+
 if __name__ == '__main__':
     sys.path.insert(0, str(REF))
     _install_standins()
-    make_operators()
-    make_geometry()
-    make_mixed()
+    steps = dict(operators=make_operators, geometry=make_geometry,
+                 mixed=make_mixed, bases=make_bases)
+    for name in sys.argv[1:] or list(steps):
+        steps[name]()

@@ -8,6 +8,7 @@ import pytest
 from oracle.fr_oracle import artvisc_points, shock_sensor
 from pyfr_gb300.mesh import box, mixed_box, periodic_box, vertex_nodes
 from pyfr_gb300.shapes import get_shape, linear_shape_fn
+from pyfr_gb300.polys import modal_basis
 from pyfr_gb300.solvers.artvisc import sensor_params
 from tests.oracle_util import disc_for_mesh
 
@@ -18,7 +19,7 @@ def av_case(et, mesh, order, c, seed=5):
     maximum) all occur."""
     nd = mesh.ndims
     s = get_shape(et, order, 'gauss-legendre', 'gauss-legendre')
-    degs, ind, w, bd = sensor_params(s.ubasis, order)
+    degs, ind, w, bd = sensor_params(*modal_basis(s)[1:], order)
     vn, nn = vertex_nodes(mesh)
     av = dict(invvdm=np.linalg.inv(s.ubasis.vdm).T, degs=degs, order=order,
               c=c, vnodes=vn[et], nnodes=nn, opf=linear_shape_fn(et, s.fpts),
@@ -51,12 +52,12 @@ def test_vertex_nodes():
 
 def test_sensor_params():
     s = get_shape('hex', 3)
-    degs, ind, w, bd = sensor_params(s.ubasis, 3)
+    degs, ind, w, bd = sensor_params(*modal_basis(s)[1:], 3)
     assert len(degs) == 64 and max(degs) == 3 and sum(ind) == 64 - 27
     # Least-squares slope of ln(e) against ln(d + 1): w . ln(d + 1) = 1
     assert np.isclose(w @ np.log(np.arange(2, 5)), 1.0)
     assert np.isclose(w.sum(), 0.0) and np.isclose(bd.sum(), 1.0)
-    assert sensor_params(get_shape('quad', 1).ubasis, 1)[2] is None
+    assert sensor_params(*modal_basis(get_shape('quad', 1))[1:], 1)[2] is None
 
 
 # Sensor constants per order: the decay fit's rate stays near 2.3-3 for a

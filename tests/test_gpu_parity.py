@@ -153,6 +153,7 @@ def test_ns_rhs_flux_antialiasing(built, golden, case, etype, artvisc):
     from pyfr_gb300.inifile import Inifile
     from pyfr_gb300.mesh import vertex_nodes
     from pyfr_gb300.shapes import get_shape, linear_shape_fn
+    from pyfr_gb300.polys import modal_basis
     from pyfr_gb300.solvers.artvisc import sensor_params
     from pyfr_gb300.solvers.system import NavierStokesSystem
     g = golden[f'geometry_{case}']
@@ -187,7 +188,7 @@ def test_ns_rhs_flux_antialiasing(built, golden, case, etype, artvisc):
     shp = get_shape(etype, 3)
     av = None
     if artvisc:
-        degs, *_ = sensor_params(shp.ubasis, 3)
+        degs, *_ = sensor_params(*modal_basis(shp)[1:], 3)
         vn, nn = vertex_nodes(mesh)
         av = dict(invvdm=np.linalg.inv(shp.ubasis.vdm).T, degs=degs, order=3,
                   c=avc, vnodes=vn[etype], nnodes=nn,

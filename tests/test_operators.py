@@ -111,3 +111,18 @@ def test_antialias_operators_match_reference(golden, etype):
     np.testing.assert_allclose(s.m9, ref[f'{key}/m9'], rtol=0, atol=1e-11)
     np.testing.assert_allclose(s.opmat('(M1 - M3*M2)*M9'),
                                ref[f'{key}/M1329'], rtol=0, atol=1e-11)
+
+
+@pytest.mark.parametrize('kind', ['tri', 'tet', 'pri'])
+@pytest.mark.parametrize('order', [1, 2, 3, 4])
+def test_simplex_ortho_basis_matches_reference(kind, order):
+    """The collapsed-coordinate orthonormal bases (degree tuples, order and
+    sign of the modes) against the reference's at its solution points
+    (tests/golden/bases.npz, made by tests/golden/make_golden.py)."""
+    from pathlib import Path
+    from pyfr_gb300.polys import SimplexOrthoBasis
+    g = np.load(Path(__file__).parent / 'golden' / 'bases.npz')
+    key = f'{kind}_p{order}'
+    b = SimplexOrthoBasis(kind, order, g[f'{key}/pts'])
+    assert [tuple(d) for d in g[f'{key}/degrees']] == b.degrees
+    np.testing.assert_allclose(b.vdm, g[f'{key}/vdm'], rtol=0, atol=1e-12)
