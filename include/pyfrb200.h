@@ -61,13 +61,37 @@ enum {
     B200_BC_SUB_IN_FTPTTANG = 8,  /* subsonic inflow, given total state and direction (NS) */
     B200_BC_SUB_OUT_FP = 9        /* subsonic outflow, given pressure (NS) */
 };
+/* One instruction of a boundary-value program: postfix code evaluated per
+ * boundary point on a stack of at most 16 values.  Opcodes: 0 push val,
+ * 1-3 push x, y, z of the point, 4 push t, 5-9 + - * / pow, 10 negate,
+ * 11-23 sin cos tan exp log sqrt tanh fabs asin acos atan sinh cosh,
+ * 24-26 atan2 fmin fmax, 27-28 floor ceil. */
+typedef struct {
+    int op, pad;
+    double val;
+} b200_bcop_t;
 typedef struct {
     int type;
     double rho, p, u[3];
     double cpTw;
     /* sub-in-ftpttang: total cp*T, total pressure, flow direction */
     double cpTt, pt, vc[3];
+    /* Values given as expressions of position and time
+     * (pyfr/solvers/baseadvec/inters.py:95-116): for rho, p, u, v, w and
+     * cpTw the start and length of its program in prog (length 0: the
+     * constant above); the point coordinates ploc (ndims x n, leading
+     * dimension ldp, in the boundary's point order and the kernels'
+     * precision); the time at t_dev[0] (device memory). */
+    const b200_bcop_t *prog;
+    int expr_start[6], expr_len[6];
+    const void *ploc;
+    int64_t ldp;
+    const double *t_dev;
 } b200_bc_t;
+/* t[1] = t[0] + c*dt (dt from dt_dev when it is not NULL): the time of an
+ * RK stage for the boundary values, enqueued before each stage so that a
+ * captured step graph serves every step. */
+int b200_stage_time(double *t, const double *dt_dev, double dt, double c, void *stream);
 
 /* Riemann solver ids: [solver-interfaces] riemann-solver */
 #define B200_RSOLVER_RUSANOV 0

@@ -155,6 +155,14 @@ RSOLVERS = {'rusanov': rusanov, 'hllc': hllc}
 # Boundary conditions
 # ---------------------------------------------------------------------------
 
+def _uvw(bc, nd, npts):
+    """The boundary velocity (ndims, npts): constants or per-point
+    values."""
+    u = bc.get('u', [0.0]*3)[:nd]
+    return np.stack([np.broadcast_to(np.asarray(v, dtype=float), (npts,))
+                     for v in u])
+
+
 def bc_rsolve_state(bc, ul, n, gamma):
     """Ghost state of the boundary Riemann solve; ul (nvars, npts), n unit
     normals (ndims, npts).  pyfr/solvers/euler/kernels/bcs/*.mako and
@@ -163,7 +171,7 @@ def bc_rsolve_state(bc, ul, n, gamma):
     t = bc['type']
     ur = np.empty_like(ul)
     gm1 = gamma - 1
-    uvw = np.array(bc.get('u', [0.0]*3)[:nd])[:, None]
+    uvw = _uvw(bc, nd, ul.shape[1])
     if t == 'sup-in-fa':
         ur[0] = bc['rho']
         ur[1:nd + 1] = bc['rho']*uvw
@@ -237,7 +245,7 @@ def bc_ldg_state(bc, ul, n, gamma):
         ur[-1] = ul[-1] - 0.5/ul[0]*np.sum(ul[1:nd + 1]**2, axis=0)
         return ur
     if t == 'no-slp-isot-wall':
-        uvw = np.array(bc.get('u', [0.0]*3)[:nd])[:, None]
+        uvw = _uvw(bc, nd, ul.shape[1])
         ur = np.empty_like(ul)
         ur[0] = ul[0]
         ur[1:nd + 1] = uvw*ul[0]
@@ -387,6 +395,26 @@ class Discretisation:
             mag = np.sqrt(np.sum(nl**2, axis=0))
             self.bcs.append((fp, ee, nl/mag, mag, spec))
 
+    def _bcs_at(self, t):
+        """The boundaries with any value that is a function of (x, t)
+        (x: (ndims, npts) coordinates of the boundary's points) evaluated
+        at time t (expressions of pyfr/solvers/baseadvec/inters.py:95-116)."""
+        out = []
+        for fp, ee, n, mag, spec in self.bcs:
+            if any(callable(v) for v in spec.values()) or \
+                    any(callable(v) for v in spec.get('u', [])):
+                x = self.ploc_f[fp, :, ee].T
+                ev = dict(spec)
+                for k, v in spec.items():
+                    if callable(v):
+                        ev[k] = v(x, t)
+                if 'u' in spec:
+                    ev['u'] = [v(x, t) if callable(v) else v
+                               for v in spec['u']]
+                spec = ev
+            out.append((fp, ee, n, mag, spec))
+        return out
+
     def _pair(self, lhs, rhs, periods):
         """Pair the flux points of the two sides of every interface by
         matching physical coordinates (modulo periods)."""
@@ -442,9 +470,10 @@ class Discretisation:
         # f: (ndims, nupts, nvars, neles) physical -> reference (smats)
         return np.einsum('pike,kpve->ipve', self.smats_u, f)
 
-    def rhs_euler(self, u, c, rsolver='rusanov'):
+    def rhs_euler(self, u, c, rsolver='rusanov', t=0.0):
         gamma = c['gamma']
         nd = self.ndims
+        bcs = self._bcs_at(t)
         uf = self.apply(self.ops['M0'], u)
 
         # Common interface flux (intcflux)
@@ -455,7 +484,7 @@ class Discretisation:
         self._scatter(uf, 'r', -mag*fn)
 
         # Boundary common fluxes (bccflux)
-        for fp, ee, n, bmag, spec in self.bcs:
+        for fp, ee, n, bmag, spec in bcs:
             ub = uf[fp, :, ee].T
             ug = bc_rsolve_state(spec, ub, n, gamma)
             uf[fp, :, ee] = (bmag*RSOLVERS[rsolver](ub, ug, n, gamma)).T
@@ -479,10 +508,12 @@ class Discretisation:
         r += self.apply(self.ops['M3'], uf)
         return -r/self.djac_u[:, None, :]
 
-    def rhs_ns(self, u, c, rsolver='rusanov', grads_out=None, av=None):
+    def rhs_ns(self, u, c, rsolver='rusanov', grads_out=None, av=None,
+               t=0.0):
         """av: the artificial-viscosity parameters of shock_sensor and
         artvisc_points (pyfr/solvers/baseadvecdiff/artvisc.py), or None."""
         gamma, beta, tau = c['gamma'], c['ldg-beta'], c['ldg-tau']
+        bcs = self._bcs_at(t)
         nd, nupts, nfpts, ne = self.ndims, self.nupts, self.nfpts, self.neles
         uf = self.apply(self.ops['M0'], u)
         if av is not None:
@@ -499,7 +530,7 @@ class Discretisation:
         comm = uf.copy()
         self._scatter(comm, 'l', cl)
         self._scatter(comm, 'r', cr)
-        for fp, ee, n, bmag, spec in self.bcs:
+        for fp, ee, n, bmag, spec in bcs:
             comm[fp, :, ee] = bc_ldg_state(spec, uf[fp, :, ee].T, n, gamma).T
 
         # Corrected reference gradient, transformed to physical space
@@ -552,14 +583,14 @@ class Discretisation:
         fvc = fvc + tau*(ul - ur)
         # (boundary states first: the interior scatter overwrites uf)
         bflux = []
-        for fp, ee, n, bmag, spec in self.bcs:
+        for fp, ee, n, bmag, spec in bcs:
             ub = uf[fp, :, ee].T
             gb = gf[:, fp, :, ee].transpose(1, 2, 0)
             ab = avf[fp, ee] if av is not None else None
             bflux.append(bmag*bc_flux_ns(spec, ub, gb, n, c, rsolver, ab))
         self._scatter(uf, 'l', mag*(fic + fvc))
         self._scatter(uf, 'r', -mag*(fic + fvc))
-        for (fp, ee, *_), f in zip(self.bcs, bflux):
+        for (fp, ee, *_), f in zip(bcs, bflux):
             uf[fp, :, ee] = f.T
 
         if self.aa is not None:
@@ -1083,6 +1114,22 @@ RK45_A = [970286171893 / 4311952581923, 6584761158862 / 12103376702013,
 RK45_B = [1153189308089 / 22510343858157, 1772645290293 / 4653164025191,
           -1672844663538 / 4480602732383, 2114624349019 / 3568978502595,
           5198255086312 / 14908931495163]
+
+
+def rk45_step_t(rhs, u, t, dt):
+    """rk45_step with the stage times passed to rhs(u, t): stage i at
+    t + c_i dt, c_0 = 0 and c_i = sum(b[:i-1]) + a[i-1] (the low-storage
+    scheme's abscissae)."""
+    cs = [0.0] + [sum(RK45_B[:i]) + a for i, a in enumerate(RK45_A)]
+    r1, r2 = u.copy(), u
+    ns = len(RK45_B)
+    for i in range(ns):
+        r2 = rhs(r2 if i else r1, t + cs[i]*dt)
+        if i < ns - 1:
+            r1, r2 = r1 + dt*RK45_B[i]*r2, r1 + dt*RK45_A[i]*r2
+        else:
+            r1 = r1 + dt*RK45_B[i]*r2
+    return r1
 
 
 def rk45_step(rhs, u, dt):

@@ -46,9 +46,17 @@ BC_TYPES = {'sup-in-fa': 1, 'sup-out-fn': 2, 'slp-adia-wall': 3,
             'sub-in-frv': 7, 'sub-in-ftpttang': 8, 'sub-out-fp': 9}
 
 
+class BCOp(C.Structure):
+    """``b200_bcop_t``"""
+    _fields_ = [('op', i32), ('pad', i32), ('val', f64)]
+
+
 class BC(C.Structure):
     _fields_ = [('type', i32), ('rho', f64), ('p', f64), ('u', f64*3),
-                ('cpTw', f64), ('cpTt', f64), ('pt', f64), ('vc', f64*3)]
+                ('cpTw', f64), ('cpTt', f64), ('pt', f64), ('vc', f64*3),
+                ('prog', C.c_void_p), ('expr_start', i32*6),
+                ('expr_len', i32*6), ('ploc', C.c_void_p), ('ldp', i64),
+                ('t_dev', C.c_void_p)]
 
 
 class EF(C.Structure):
@@ -129,6 +137,7 @@ _SIGS = {
     'b200_host_alloc': [C.POINTER(vp), sz],
     'b200_host_free': [vp],
     'b200_memset': [vp, i32, sz, vp],
+    'b200_stage_time': [vp, vp, f64, f64, vp],
     'b200_memcpy_htod': [vp, vp, sz, vp],
     'b200_memcpy_dtoh': [vp, vp, sz, vp],
     'b200_memcpy_dtod': [vp, vp, sz, vp],

@@ -12,11 +12,12 @@
 //                     sub-in-ftpttang,sub-out-fp,common,ghost,
 //                     ghost-imperm}.mako
 //
-// The boundary constants are uniform (the reference also allows
-// expressions of position and time; those are not provided).  One thread
-// per boundary flux point; the interior state is read through a view
-// (element offsets into the flux-point field) and the flux written back in
-// place.
+// A boundary value is a constant or a postfix program of the point's
+// coordinates and the time (compiled on the host, pyfr_gb300/bcexpr.py),
+// evaluated by each thread for its point before the ghost state is formed.
+// One thread per boundary flux point; the interior state is read through a
+// view (element offsets into the flux-point field) and the flux written
+// back in place.
 #include <cstdint>
 
 #include "common.cuh"
@@ -29,6 +30,8 @@ constexpr int BC_BLOCK = 128;
 
 using b200::Gas;
 
+constexpr int BC_STACK = 16;
+
 template <typename T>
 struct BcK {
     int type;
@@ -37,7 +40,90 @@ struct BcK {
     T cs, s, ratio;
     // sub-in-ftpttang: cpTt, pt^-Rdcp, Rdcp = (gamma - 1)/gamma, direction
     T cpTt, ptfac, rdcp, vc[3];
+    // Expressions: programs of rho, p, u, v, w, cpTw (length 0: constant)
+    const b200_bcop_t *prog;
+    int estart[6], elen[6], nexpr;
+    const T *ploc;
+    int64_t ldp;
+    const double *t_dev;
 };
+
+// The value of a boundary program at a point (x) and time (t)
+template <typename T>
+__device__ T bc_program(const b200_bcop_t *prog, int start, int len, const T *x, T t) {
+    T st[BC_STACK];
+    int sp = 0;
+    // (a malformed program, which the host compiler never makes, gives NaN
+    // instead of leaving the stack)
+    const T bad = T(0) / T(0);
+    for (int i = start; i < start + len; i++) {
+        const int op = prog[i].op;
+        if (op < 0 || op > 28) return bad;
+        if (op <= 4) {
+            if (sp >= BC_STACK) return bad;
+            st[sp++] = op == 0 ? (T)prog[i].val : (op == 4 ? t : x[op - 1]);
+        } else if (op <= 9 || op >= 24 && op <= 26) {
+            if (sp < 2) return bad;
+            const T b = st[--sp], a = st[sp - 1];
+            T r;
+            switch (op) {
+            case 5: r = a + b; break;
+            case 6: r = a - b; break;
+            case 7: r = a * b; break;
+            case 8: r = a / b; break;
+            case 9: r = pow(a, b); break;
+            case 24: r = atan2(a, b); break;
+            case 25: r = fmin(a, b); break;
+            default: r = fmax(a, b); break;
+            }
+            st[sp - 1] = r;
+        } else {
+            if (sp < 1) return bad;
+            const T a = st[sp - 1];
+            T r;
+            switch (op) {
+            case 10: r = -a; break;
+            case 11: r = sin(a); break;
+            case 12: r = cos(a); break;
+            case 13: r = tan(a); break;
+            case 14: r = exp(a); break;
+            case 15: r = log(a); break;
+            case 16: r = sqrt(a); break;
+            case 17: r = tanh(a); break;
+            case 18: r = fabs(a); break;
+            case 19: r = asin(a); break;
+            case 20: r = acos(a); break;
+            case 21: r = atan(a); break;
+            case 22: r = sinh(a); break;
+            case 23: r = cosh(a); break;
+            case 27: r = floor(a); break;
+            default: r = ceil(a); break;
+            }
+            st[sp - 1] = r;
+        }
+    }
+    return sp == 1 ? st[0] : bad;
+}
+
+// The boundary values at point i: the programs evaluated and the derived
+// constants formed again from them
+template <int ND, typename T>
+__device__ __forceinline__ void bc_at_point(BcK<T> &b, int64_t i, T gamma) {
+    T x[3] = {0, 0, 0};
+#pragma unroll
+    for (int d = 0; d < ND; d++) x[d] = b.ploc[d * b.ldp + i];
+    const T t = (T)b.t_dev[0];
+    T *dst[6] = {&b.rho, &b.p, &b.u[0], &b.u[1], &b.u[2], &b.cpTw_g};
+    for (int f = 0; f < 6; f++)
+        if (b.elen[f]) *dst[f] = bc_program<T>(b.prog, b.estart[f], b.elen[f], x, t);
+    if (b.elen[5]) b.cpTw_g /= gamma;
+    if (b.elen[0] || b.elen[1]) {
+        const T cs = b.rho > 0 && b.p > 0 ? sqrt(gamma * b.p / b.rho) : T(0);
+        b.cs = cs;
+        b.s = b.rho > 0 ? b.p * pow(b.rho, -gamma) : T(0);
+        b.ratio = cs * T(2) / (gamma - T(1));
+    }
+}
 
 template <typename T>
 BcK<T> bc_consts(const b200_bc_t &b, double gamma) {
@@ -56,7 +142,23 @@ BcK<T> bc_consts(const b200_bc_t &b, double gamma) {
     k.ptfac = (T)(b.pt > 0 ? pow(b.pt, -rdcp) : 0.0);
     k.rdcp = (T)rdcp;
     for (int i = 0; i < 3; i++) k.vc[i] = (T)b.vc[i];
+    k.prog = b.prog;
+    k.nexpr = 0;
+    for (int f = 0; f < 6; f++) {
+        k.estart[f] = b.expr_start[f];
+        k.elen[f] = b.prog ? b.expr_len[f] : 0;
+        k.nexpr += k.elen[f] > 0;
+    }
+    k.ploc = static_cast<const T *>(b.ploc);
+    k.ldp = b.ldp;
+    k.t_dev = b.t_dev;
     return k;
+}
+
+// Programs need the point coordinates and the time
+template <typename T>
+bool bc_exprs_ok(const BcK<T> &k) {
+    return !k.nexpr || (k.ploc && k.t_dev);
 }
 
 // Ghost state of the Riemann solve (bc_rsolve_state)
@@ -284,11 +386,13 @@ __device__ __forceinline__ T unit_normal(const T *__restrict__ nl, int64_t ldn, 
 
 template <int ND, typename T>
 __global__ void __launch_bounds__(BC_BLOCK)
-bccflux_euler_kernel(int64_t n, int rs, T gamma, BcK<T> bc, ScalView<T> vl, int ix64,
+bccflux_euler_kernel(int64_t n, int rs, T gamma, BcK<T> bc0, ScalView<T> vl, int ix64,
                      const T *__restrict__ nl, int64_t ldn) {
     constexpr int NV = ND + 2;
     const int64_t i = (int64_t)blockIdx.x * BC_BLOCK + threadIdx.x;
     if (i >= n) return;
+    BcK<T> bc = bc0;
+    if (bc.nexpr) bc_at_point<ND, T>(bc, i, gamma);
     T *pl = vl.base + b200::load_ix(vl.map, ix64, i);
     T ul[NV], ur[NV], nn[ND], fn[NV];
 #pragma unroll
@@ -302,11 +406,13 @@ bccflux_euler_kernel(int64_t n, int rs, T gamma, BcK<T> bc, ScalView<T> vl, int 
 
 template <int ND, typename T>
 __global__ void __launch_bounds__(BC_BLOCK)
-bcconu_kernel(int64_t n, T gamma, BcK<T> bc, ScalView<T> vin, ScalView<T> vout, int ix64,
+bcconu_kernel(int64_t n, T gamma, BcK<T> bc0, ScalView<T> vin, ScalView<T> vout, int ix64,
               const T *__restrict__ nl, int64_t ldn) {
     constexpr int NV = ND + 2;
     const int64_t i = (int64_t)blockIdx.x * BC_BLOCK + threadIdx.x;
     if (i >= n) return;
+    BcK<T> bc = bc0;
+    if (bc.nexpr) bc_at_point<ND, T>(bc, i, gamma);
     const T *pi = vin.base + b200::load_ix(vin.map, ix64, i);
     T *po = vout.base + b200::load_ix(vout.map, ix64, i);
     T ul[NV], ur[NV], nn[ND];
@@ -320,12 +426,14 @@ bcconu_kernel(int64_t n, T gamma, BcK<T> bc, ScalView<T> vin, ScalView<T> vout, 
 
 template <int ND, typename T>
 __global__ void __launch_bounds__(BC_BLOCK)
-bccflux_ns_kernel(int64_t n, int rs, b200::GasK<T> gas, T tau, BcK<T> bc, ScalView<T> vl,
+bccflux_ns_kernel(int64_t n, int rs, b200::GasK<T> gas, T tau, BcK<T> bc0, ScalView<T> vl,
                   VectView<T> gl, int ix64, const T *__restrict__ nl, int64_t ldn,
                   ScalView<T> va) {
     constexpr int NV = ND + 2;
     const int64_t i = (int64_t)blockIdx.x * BC_BLOCK + threadIdx.x;
     if (i >= n) return;
+    BcK<T> bc = bc0;
+    if (bc.nexpr) bc_at_point<ND, T>(bc, i, gas.gamma);
     T *pl = vl.base + b200::load_ix(vl.map, ix64, i);
     T ul[NV], ur[NV], nn[ND], fi[NV];
 #pragma unroll
@@ -388,11 +496,13 @@ __device__ __forceinline__ void atomic_min_nonneg(float *a, float v) {
 
 template <int ND, typename T>
 __global__ void __launch_bounds__(BC_BLOCK)
-bccent_kernel(int64_t n, T gamma, BcK<T> bc, ScalView<T> vl, ScalView<T> ve, int ix64,
+bccent_kernel(int64_t n, T gamma, BcK<T> bc0, ScalView<T> vl, ScalView<T> ve, int ix64,
               const T *__restrict__ nl, int64_t ldn, T big) {
     constexpr int NV = ND + 2;
     const int64_t i = (int64_t)blockIdx.x * BC_BLOCK + threadIdx.x;
     if (i >= n) return;
+    BcK<T> bc = bc0;
+    if (bc.nexpr) bc_at_point<ND, T>(bc, i, gamma);
     const T *pl = vl.base + b200::load_ix(vl.map, ix64, i);
     T *pe = ve.base + b200::load_ix(ve.map, ix64, i);
     T ul[NV], ur[NV], nn[ND];
@@ -420,6 +530,8 @@ int bccflux_euler(int ndims, int64_t n, int rs, double gamma, const b200_bc_t *b
     if (!bc || !bc_type_ok(bc->type) || bc->type > B200_BC_CHAR_RIEM_INV)
         return b200::set_error(B200_ERR_ARG, "bccflux_euler: bad boundary type");
     const auto k = bc_consts<T>(*bc, gamma);
+    if (!bc_exprs_ok(k))
+        return b200::set_error(B200_ERR_ARG, "boundary expressions need ploc and t");
     ScalView<T> l{ul_base, ul_map};
     const unsigned grid = b200::ceil_div(n, BC_BLOCK);
     if (ndims == 2)
@@ -440,6 +552,8 @@ int bcconu(int ndims, int64_t n, double gamma, const b200_bc_t *bc, const T *in_
     if (!bc || !bc_type_ok(bc->type))
         return b200::set_error(B200_ERR_ARG, "bcconu: bad boundary type");
     const auto k = bc_consts<T>(*bc, gamma);
+    if (!bc_exprs_ok(k))
+        return b200::set_error(B200_ERR_ARG, "boundary expressions need ploc and t");
     ScalView<T> vi{const_cast<T *>(in_base), in_map}, vo{out_base, out_map};
     const unsigned grid = b200::ceil_div(n, BC_BLOCK);
     if (ndims == 2)
@@ -467,6 +581,8 @@ int bccflux_ns(int ndims, int64_t n, int rs, const b200_gas_t *gas, double tau,
                                "bccflux_ns: boundaries take unshifted states");
     const auto g = b200::gas_consts<T>(g0);
     const auto k = bc_consts<T>(*bc, g0.gamma);
+    if (!bc_exprs_ok(k))
+        return b200::set_error(B200_ERR_ARG, "boundary expressions need ploc and t");
     ScalView<T> l{ul_base, ul_map};
     VectView<T> gv{gl_base, gl_map, gl_rstr};
     const unsigned grid = b200::ceil_div(n, BC_BLOCK);
@@ -488,6 +604,8 @@ int bccent(int ndims, int64_t n, double gamma, const b200_bc_t *bc, const T *ul_
     if (!bc || !bc_type_ok(bc->type))
         return b200::set_error(B200_ERR_ARG, "bccent: bad boundary type");
     const auto k = bc_consts<T>(*bc, gamma);
+    if (!bc_exprs_ok(k))
+        return b200::set_error(B200_ERR_ARG, "boundary expressions need ploc and t");
     ScalView<T> l{const_cast<T *>(ul_base), ul_map}, e{ent_base, ent_map};
     const T big = sizeof(T) == 8 ? (T)1.7976931348623157e308 : (T)3.4028234663852886e38;
     const unsigned grid = b200::ceil_div(n, BC_BLOCK);
@@ -501,9 +619,21 @@ int bccent(int ndims, int64_t n, double gamma, const b200_bc_t *bc, const T *ul_
     return B200_OK;
 }
 
+__global__ void stage_time_kernel(double *t, const double *dt_dev, double dt, double c) {
+    t[1] = t[0] + c * (dt_dev ? dt_dev[0] : dt);
+}
+
 }  // namespace
 
 extern "C" {
+
+int b200_stage_time(double *t, const double *dt_dev, double dt, double c, void *stream) {
+    if (!t) return b200::set_error(B200_ERR_ARG, "stage_time: null time");
+    stage_time_kernel<<<1, 1, 0, (cudaStream_t)stream>>>(t, dt_dev, dt, c);
+    B200_CHECK_LAUNCH("stage_time");
+    return B200_OK;
+}
+
 
 int b200_bccent_f64(int ndims, int64_t n, double gamma, const b200_bc_t *bc,
                     const double *ul_base, const void *ul_map, double *ent_base,

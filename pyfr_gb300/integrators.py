@@ -122,6 +122,23 @@ class RKVdH2Integrator:
         weakref.finalize(self, backend.lib.event_destroy, self._dt_evt.value)
         self._dt_set = None
 
+        # Boundary values that depend on the time: the step's start time
+        # goes to device memory before each step (staged like dt) and a
+        # one-thread kernel sets each stage's time t0 + c_i dt
+        self._tdep = self.system.time_dependent
+        if self._tdep:
+            self._t_host = C.c_void_p()
+            backend.lib.host_alloc(C.byref(self._t_host), 8)
+            weakref.finalize(self, backend.lib.host_free, self._t_host.value)
+            self._t_evt = C.c_void_p()
+            backend.lib.event_create(C.byref(self._t_evt))
+            weakref.finalize(self, backend.lib.event_destroy,
+                             self._t_evt.value)
+            self._t_pending = False
+            self._tkerns = [self.system.stage_time_kernel(ci,
+                                                          dt_dev=self._dt_dev)
+                            for ci in self.c]
+
         if self.needs_cfl:
             # pyfr/integrators/controllers.py:7-38
             self._cfl = cfg.getfloat(sect, 'cfl')
@@ -270,12 +287,27 @@ class RKVdH2Integrator:
         r2, *rs = [r for r in regs if r != r1]
         return r1, r2, rs
 
+    def _time_kernels(self, i):
+        return [self._tkerns[i]] if self._tdep else []
+
+    def _set_t0(self, t, stream):
+        """Enqueue the copy of the step's start time to device memory."""
+        lib = self.backend.lib
+        if self._t_pending:
+            lib.event_sync(self._t_evt.value)
+        C.c_double.from_address(self._t_host.value).value = t
+        lib.memcpy_htod(self.system._tmat.data, self._t_host.value, 8,
+                        stream)
+        lib.event_record(self._t_evt.value, stream)
+        self._t_pending = True
+
     def step_kernels(self, idx, dt):
         """The kernels of one step starting from register ``idx``, in launch
         order, and the resulting register indices."""
         r1, r2, rs = self._regs(idx)
         kl = []
         for i in range(self.nstages):
+            kl.extend(self._time_kernels(i))
             for g in self.system.rhs_graphs(r2 if i else r1, r2):
                 kl.extend(g.klist)
             for k in self._rk_kerns(i, r1, r2, *rs):
@@ -308,6 +340,9 @@ class RKVdH2Integrator:
 
     def step(self, t, dt):
         be, stream = self.backend, self.backend.stream
+        if self._tdep:
+            self._set_t0(t, stream)
+            self._set_dt(dt, stream)
         if self.use_step_graph:
             self._set_dt(dt, stream)
             key = self.idxcurr
@@ -594,6 +629,7 @@ class MixedRKIntegrator(RKVdH2Integrator):
     def step_kernels(self, idx, dt):
         kl = []
         for i in range(self.nstages):
+            kl.extend(self._time_kernels(i))
             for g in self.system.rhs_graphs(0, 1):
                 kl.extend(g.klist)
             kl.extend(self._stage_kernel(i, j, dt)

@@ -280,6 +280,15 @@ class BaseElements:
 
     # ---- interface helpers (pyfr/solvers/base/elements.py:446-469) --------
 
+    def get_ploc_for_inters(self, eidxs, fidx):
+        """Physical coordinates of the face's flux points in their sorted
+        order (pyfr/solvers/base/elements.py, get_ploc_for_inters)."""
+        if not hasattr(self, '_ploc_fpts_np'):
+            self._ploc_fpts_np = self.ploc_at_np('fpts')  # (nfpts, nd, ne)
+        fpts_idx = self.srtd_face_fpts[fidx][eidxs]
+        pl = self._ploc_fpts_np[fpts_idx, :, eidxs[:, None]]
+        return pl.reshape(-1, self.ndims),
+
     def get_pnorms_for_inters(self, eidxs, fidx):
         fpts_idx = self.srtd_face_fpts[fidx][eidxs]
         pn = self._pnorm_fpts[fpts_idx, eidxs[:, None]]

@@ -9,6 +9,8 @@ kernels (``pyfr/solvers/euler/inters.py:28-38``,
 ``pyfr/solvers/navstokes/inters.py:29-48``).
 """
 
+import ctypes as C
+
 import numpy as np
 
 
@@ -203,23 +205,33 @@ class BaseBCInters(BaseIntInters):
             raise NotImplementedError(f'Boundary type {self.type!r} is not '
                                       'provided')
 
-        # Uniform constants, which may use [constants]
-        # (pyfr/solvers/baseadvec/inters.py:84-96)
-        vals = {}
-        for k in BC_OPTS[self.type]:
-            if k in 'uvw' and 'uvw'.index(k) >= self.ndims:
-                continue
+        # Values: expressions of position and time, with [constants]
+        # substituted (pyfr/solvers/baseadvec/inters.py:81-116); constant
+        # ones are folded to numbers
+        from pyfr_gb300.bcexpr import BCExpr
+        vals, self.exprs = {}, {}
+        opts = [k for k in BC_OPTS[self.type]
+                if not (k in 'uvw' and 'uvw'.index(k) >= self.ndims)]
+        if self.type == 'no-slp-isot-wall':
+            opts.append('cpTw')
+        for k in opts:
             default = '0' if self.type in _ZERO_UVW and k in 'uvw' else None
-            expr = cfg.get(cfgsect, k, default)
+            expr = cfg.getexpr(cfgsect, k, default)
             if expr is None:
                 raise ValueError(f'{cfgsect}: {k} is required')
-            vals[k] = float(npeval(str(expr), dict(self.c)))
+            ex = BCExpr(str(expr), self.ndims)
+            if ex.const is not None:
+                vals[k] = ex.const
+            else:
+                vals[k] = 0.0
+                self.exprs[k] = ex
+
         def ev(k):
             return float(npeval(cfg.get(cfgsect, k), dict(self.c)))
 
         vc = []
         if self.type == 'no-slp-isot-wall':
-            vals['cpTw'] = ev('cpTw')
+            pass
         elif self.type == 'sub-in-ftpttang':
             # Total state and inflow direction
             # (pyfr/solvers/navstokes/inters.py:169-193)
@@ -243,6 +255,47 @@ class BaseBCInters(BaseIntInters):
         scal = {t: e._scal_fpts for t, e in elemap.items()}
         self._perm = self._perm_for_field(lhs, scal)
         self._pnorm_lhs = self._const_mat(lhs, 'get_pnorms_for_inters')
+
+        # Programs of the expression values and the point coordinates
+        self.time_dependent = any(e.uses_t for e in self.exprs.values())
+        self._prog = self._ploc = None
+        if self.exprs:
+            from pyfr_gb300.backend.lib import BCOp
+            ops = []
+            for f, k in enumerate(['rho', 'p', 'u', 'v', 'w', 'cpTw']):
+                if k in self.exprs:
+                    prog = self.exprs[k].prog
+                    self.bc.expr_start[f], self.bc.expr_len[f] = \
+                        len(ops), len(prog)
+                    ops.extend(prog)
+            arr = np.zeros(len(ops), dtype=[('op', '<i4'), ('pad', '<i4'),
+                                            ('val', '<f8')])
+            arr['op'] = [o for o, _ in ops]
+            arr['val'] = [v for _, v in ops]
+            assert arr.itemsize == C.sizeof(BCOp)
+            self._prog = be.const_matrix(arr.view(np.int64)[None, :],
+                                         dtype=np.int64)
+            self._ploc = self._const_mat(lhs, 'get_ploc_for_inters')
+
+    def bind_device(self, tmat):
+        """Point the boundary values at their programs, coordinates and
+        the stage time (element 1 of ``tmat``), once memory is committed."""
+        if self.exprs:
+            self.bc.prog = self._prog.data
+            self.bc.ploc = self._ploc.data
+            self.bc.ldp = self._ploc.leaddim
+            self.bc.t_dev = tmat.data + 8
+
+    def values_at(self, t):
+        """Host values of the options at every boundary point at time t,
+        in the kernels' point order (for checking)."""
+        out = dict(self.bcvals)
+        if self.exprs:
+            x = inter_arrays(self.lhs, 'get_ploc_for_inters', self.elemap,
+                             self._perm)[0].T
+            for k, ex in self.exprs.items():
+                out[k] = ex.eval_np(x, t)
+        return out
 
 
 class EulerBCInters(BaseBCInters):

@@ -14,7 +14,7 @@ import inspect
 
 import numpy as np
 
-from pyfr_gb300.backend.types import NullKernel
+from pyfr_gb300.backend.types import Kernel, NullKernel
 from pyfr_gb300.solvers.elements import EulerElements, NavierStokesElements
 from pyfr_gb300.solvers.inters import (EulerBCInters, EulerIntInters,
                                        NavierStokesBCInters,
@@ -73,6 +73,10 @@ class BaseSystem:
 
         # Boundaries: one interface object per named boundary, its type from
         # [soln-bcs-<name>] (pyfr/solvers/base/system.py:183-198)
+        # The step-start and stage times (device memory) that boundary
+        # values given as expressions of t read
+        self._tmat = backend.matrix((1, 2), dtype=np.float64)
+
         self._bc_inters = []
         for name, side in sorted(getattr(mesh, 'bcon', {}).items()):
             sect = f'soln-bcs-{name}'
@@ -147,6 +151,8 @@ class BaseSystem:
                 i.artvisc = v[0]
 
         self.backend.commit()
+        for b in self._bc_inters:
+            b.bind_device(self._tmat)
         self._gen_kernels()
         if self._av:
             self._av.add_kernels(self._kernels, self._ktags)
@@ -227,9 +233,34 @@ class BaseSystem:
     def rhs_graphs(self, uinbank, foutbank):
         return self._rhs_graphs_cached(uinbank, foutbank)
 
+    @property
+    def time_dependent(self):
+        """Whether a boundary value depends on the time."""
+        return any(getattr(b, 'time_dependent', False)
+                   for b in self._bc_inters)
+
+    def set_time(self, t):
+        """Set the stage time read by the boundary values (an RHS called
+        outside an integrator step)."""
+        self._tmat.set(np.array([[t, t]]))
+
+    def stage_time_kernel(self, c, dt=None, dt_dev=None):
+        """A kernel setting the stage time t0 + c*dt, dt from device
+        memory (``dt_dev``) or the given value."""
+        lib, tm = self.backend.lib, self._tmat
+        dp = dt_dev.data if dt_dev is not None else None
+
+        def run(stream):
+            lib.stage_time(tm.data, dp, float(dt or 0.0), float(c), stream)
+
+        return Kernel(run, mats=[tm] + ([dt_dev] if dt_dev is not None
+                                        else []), name='stage_time')
+
     def rhs(self, t, uinbank, foutbank):
         if uinbank >= self.nrhs or foutbank >= self.nrhs:
             raise ValueError('Invalid register numbers')
+        if any(b.exprs for b in self._bc_inters):
+            self.set_time(t)
         for g in self._rhs_graphs_cached(uinbank, foutbank):
             self.backend.run_graph(g)
 
