@@ -511,8 +511,8 @@ class MixedRKIntegrator(RKVdH2Integrator):
         if backend.fpdtype != np.float32:
             raise ValueError('The mixed-precision integrator needs a '
                              'single-precision backend')
-        if cfg.get('solver', 'shock-capturing', 'none') != 'none':
-            raise NotImplementedError('Shock capturing needs the FP64 '
+        if cfg.get('solver', 'shock-capturing', 'none') == 'entropy-filter':
+            raise NotImplementedError('The entropy filter needs the FP64 '
                                       'solution in the system (the plain '
                                       'integrator)')
         super().__init__(backend, systemcls, mesh, cfg, initsoln)
@@ -534,8 +534,11 @@ class MixedRKIntegrator(RKVdH2Integrator):
         self.uref, self.hs_ref = None, 0.0
         shift = cfg.get('backend-b200', 'reference-shift', 'auto')
         rs = cfg.get('solver-interfaces', 'riemann-solver')
+        # (artificial viscosity senses the density itself, so it keeps the
+        # unshifted state, as boundaries do)
+        sc = cfg.get('solver', 'shock-capturing', 'none')
         if shift == 'auto' and sysm.name == 'navier-stokes' and \
-                rs == 'rusanov' and not sysm._bc_inters:
+                rs == 'rusanov' and not sysm._bc_inters and sc == 'none':
             gamma = cfg.getfloat('constants', 'gamma')
             rho = np.concatenate([u[:, 0].ravel() for u in self._ics])
             pri = [e.con_to_pri(list(u.swapaxes(0, 1)), cfg)[-1]

@@ -118,3 +118,31 @@ def test_rk45_artvisc(built):
     for _ in range(3):
         u = rk45_step(lambda x: d.rhs_ns(x, GAS, av=av), u, 1e-4)
     assert _relerr(got, u) < TOL
+
+
+def test_chosen_form_artvisc(built):
+    """Artificial viscosity in the chosen form (split-BF16 operators, FP32
+    fluxes and sensor, FP64 accumulation; no reference-state shift): ten
+    steps of the 5^3 hex box with a steep front within the chosen form's
+    L2 bound of the FP64 plain form."""
+    from pyfr_gb300.integrators import MixedRKIntegrator, RKVdH2Integrator
+    from pyfr_gb300.mesh import periodic_box
+    from pyfr_gb300.solvers.system import NavierStokesSystem
+
+    mesh = periodic_box('hex', 5, 0.0, 1.0)
+    av, u0 = av_case('hex', mesh, 3, AV_C[3])
+    assert np.any(shock_sensor(u0, av) > 0)
+    cfg = _cfg(3, AV_C[3])
+    plain = RKVdH2Integrator(_backend(cfg), NavierStokesSystem, mesh, cfg,
+                             {'hex': u0})
+    cfg = _cfg(3, AV_C[3])
+    cfg.set('backend', 'precision', 'single')
+    cfg.set('backend-b200', 'mul-precision', 'bf16x3')
+    cfg.set('backend-b200', 'split-products', '5')
+    chosen = MixedRKIntegrator(_backend(cfg), NavierStokesSystem, mesh, cfg,
+                               {'hex': u0})
+    assert chosen.uref is None
+    plain.run_steps(10)
+    chosen.run_steps(10)
+    (a,), (b,) = chosen.soln, plain.soln
+    assert np.linalg.norm(a - b)/np.linalg.norm(b) < 1e-6
