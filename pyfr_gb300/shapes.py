@@ -93,10 +93,32 @@ class BaseShape:
         return k
 
     @cached_property
-    def face_pts(self):
-        """Flux points of each face kind in face coordinates."""
+    def std_face_pts(self):
+        """The face points of the flux-point rules in face coordinates
+        (the points of the face bases)."""
         return {k: point_set(k, r, self.order)
                 for k, r in self.fpts_rules.items()}
+
+    @cached_property
+    def face_pts(self):
+        """Flux points of each face kind in face coordinates: those of
+        the flux-point rule, or with surface-flux anti-aliasing the points
+        of the face quadrature rule."""
+        if getattr(self, '_surf_rules', None):
+            return {k: pw[0] for k, pw in self._surf_rules.items()}
+        return self.std_face_pts
+
+    def set_surf_rules(self, rules):
+        """Surface-flux anti-aliasing (pyfr/shapes.py:103-113,194-227):
+        the flux points become the points of a quadrature rule per face
+        kind, rules = {kind: (pts, wts)}, and the correction lift takes the
+        L2 projection of the face flux onto the face basis."""
+        self._surf_rules = {k: (np.asarray(p, dtype=float).reshape(
+            len(w), -1), np.asarray(w, dtype=float))
+            for k, (p, w) in rules.items()}
+        for k in ('face_pts', 'nfacefpts', 'facefpts', 'fpts', 'norm_fpts',
+                  'm0', 'm2', 'm3', 'm6', 'fpts_wts'):
+            self.__dict__.pop(k, None)
 
     @cached_property
     def nfacefpts(self):
@@ -126,7 +148,7 @@ class BaseShape:
     def facebases(self):
         return {k: TensorProdBasis(self.ndims - 1, self.order, p,
                                    self._modes(k))
-                for k, p in self.face_pts.items()}
+                for k, p in self.std_face_pts.items()}
 
     # Operator matrices -----------------------------------------------------
 
@@ -146,7 +168,19 @@ class BaseShape:
 
     @cached_property
     def m3(self):
-        return tidy(self._lift_at_upts())
+        m = self._lift_at_upts()
+        if getattr(self, '_surf_rules', None):
+            # proj_l2 of each face: the face basis' nodal values of the L2
+            # projection of values at the face quadrature points (the face
+            # bases are orthonormal Legendre products)
+            from scipy.linalg import block_diag
+            blocks = []
+            for kind, _, _ in self.faces:
+                fb = self.facebases[kind]
+                qp, qw = self._surf_rules[kind]
+                blocks.append(fb.vdm.T @ (qw[None, :]*fb.ortho_basis_at(qp)))
+            m = m @ block_diag(*blocks)
+        return tidy(m)
 
     @cached_property
     def m4(self):
@@ -266,6 +300,8 @@ class TensorProdShape(BaseShape):
 
     @cached_property
     def fpts_wts(self):
+        if getattr(self, '_surf_rules', None):
+            return np.hstack([self._surf_rules[k][1] for k, _, _ in self.faces])
         _, fw = self._face_rule
         return np.hstack([fw]*len(self.faces))
 

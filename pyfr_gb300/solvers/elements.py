@@ -68,12 +68,14 @@ class BaseElements:
 
         # Flux anti-aliasing (pyfr/solvers/baseadvec/elements.py:69-90):
         # the flux is evaluated at the points of a quadrature rule and
-        # projected back; 'surf-flux' is not provided
+        # projected back; with 'surf-flux' the flux points are those of a
+        # face quadrature rule (pyfr/shapes.py:147-227)
         aa = {a.strip() for a in cfg.get('solver', 'anti-alias',
                                          'none').split(',')} - {'none'}
-        if aa - {'flux'}:
-            raise NotImplementedError(f'Anti-aliasing {aa - {"flux"}} is not '
-                                      'supported')
+        if aa - {'flux', 'surf-flux'}:
+            raise ValueError('Invalid anti-alias options')
+        if 'surf-flux' in aa and order > 0:
+            self.basis.set_surf_rules(self._surf_rules(cfg, order))
         self.antialias = 'flux' in aa and order > 0
         if self.antialias:
             rule = cfg.get(f'solver-elements-{etype}', 'quad-pts', None)
@@ -91,6 +93,41 @@ class BaseElements:
         self.nfacefpts = self.basis.nfacefpts
         self.kernels = {}
         self._be = None
+
+    def _surf_rules(self, cfg, order):
+        """The face quadrature rule of each face kind for surface-flux
+        anti-aliasing: ``[solver-interfaces-<kind>] quad-pts`` given
+        literally, or Gauss-Legendre with ``quad-npts`` points (a square
+        number on quadrilaterals), by default (p + 2) points per
+        direction, the reference's default rules for lines and
+        quadrilaterals."""
+        from pyfr_gb300.quadrules import parse_rule, tensor_rule
+        rules = {}
+        for kind in {k for k, _, _ in self.basis.faces}:
+            sect = f'solver-interfaces-{kind}'
+            nd = {'line': 1, 'quad': 2, 'tri': 2}[kind]
+            if cfg.hasopt(sect, 'quad-pts'):
+                pts, wts = parse_rule(cfg.get(sect, 'quad-pts'), nd)
+                if wts is None:
+                    raise ValueError('quad-pts needs quadrature weights')
+            elif kind == 'tri':
+                raise NotImplementedError('Surface anti-aliasing on '
+                                          'triangular faces needs a '
+                                          'literal quad-pts rule')
+            else:
+                n1 = order + 2
+                if cfg.hasopt(sect, 'quad-npts'):
+                    n = cfg.getint(sect, 'quad-npts')
+                    n1 = round(n**(1/nd))
+                    if n1**nd != n:
+                        raise ValueError(f'{sect}: quad-npts {n} is not a '
+                                         'tensor-product rule')
+                elif cfg.hasopt(sect, 'quad-deg'):
+                    raise NotImplementedError(f'{sect}: give quad-pts or '
+                                              'quad-npts')
+                pts, wts = tensor_rule('gauss-legendre', n1, nd)
+            rules[kind] = (pts, wts)
+        return rules
 
     # ---- geometry (linear elements) -----------------------------------------
 

@@ -16,6 +16,7 @@ What is generated (all with the reference's own code):
   own golden file ``pyfr/tests/hex-gleg-ord3.npz`` (its unit test
   ``pyfr/tests/test_ele_mats.py``).
 * ``bases.npz``: the orthonormal simplex bases at the solution points.
+* ``surf_flux.npz``: operators with surface-flux anti-aliasing.
 * ``geometry_<case>.npz``: element geometry computed by the reference's
   ``EulerElements``/``NavierStokesElements`` (``pyfr/solvers/base/elements.py``)
   on small periodic meshes whose interior vertices are randomly perturbed
@@ -332,10 +333,35 @@ def make_bases():
     print('bases.npz')
 
 
+def make_surf():
+    """``surf_flux.npz``: the reference's operators with surface-flux
+    anti-aliasing (``anti-alias = surf-flux``, its default face rules) for
+    quadrilaterals and hexahedra at orders 2 and 3: flux points, M0, M3."""
+    from pyfr.inifile import Inifile
+    from pyfr.shapes import HexShape, QuadShape
+
+    out = {}
+    for name, cls, fk in (('quad', QuadShape, 'line'),
+                          ('hex', HexShape, 'quad')):
+        for p in (2, 3):
+            cfg = Inifile()
+            cfg.set('solver', 'order', p)
+            cfg.set('solver', 'anti-alias', 'surf-flux')
+            cfg.set(f'solver-elements-{name}', 'soln-pts', 'gauss-legendre')
+            cfg.set(f'solver-interfaces-{fk}', 'flux-pts', 'gauss-legendre')
+            s = cls(None, cfg)
+            key = f'{name}_p{p}'
+            out[f'{key}/fpts'] = np.asarray(s.fpts)
+            out[f'{key}/m0'] = np.asarray(s.m0)
+            out[f'{key}/m3'] = np.asarray(s.m3)
+    np.savez_compressed(HERE / 'surf_flux.npz', **out)
+    print('surf_flux.npz')
+
+
 if __name__ == '__main__':
     sys.path.insert(0, str(REF))
     _install_standins()
     steps = dict(operators=make_operators, geometry=make_geometry,
-                 mixed=make_mixed, bases=make_bases)
+                 mixed=make_mixed, bases=make_bases, surf=make_surf)
     for name in sys.argv[1:] or list(steps):
         steps[name]()

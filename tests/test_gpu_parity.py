@@ -411,3 +411,51 @@ def test_field_integrals_plain(built):
     assert abs(got['E'] - E) <= 1e-12*E
     assert abs(got['enst'] - enst) <= 1e-10*enst
     assert abs(got['vol'] - (2*np.pi)**3) <= 1e-12*(2*np.pi)**3
+
+
+@pytest.mark.parametrize('case,etype', [('quad_p3', 'quad'), ('hex_p3', 'hex')])
+@pytest.mark.parametrize('system', ['euler', 'navier-stokes'])
+@pytest.mark.parametrize('aa', ['surf-flux', 'flux, surf-flux'])
+def test_rhs_surface_antialiasing(built, golden, case, etype, system, aa):
+    """Surface-flux anti-aliasing (flux points at the (p+2)^(d-1)
+    Gauss-Legendre face points, the correction lift through the L2
+    projection onto the face basis), alone and with flux anti-aliasing, on
+    the reference's distorted meshes against the oracle with the shape's
+    operators (pinned to the reference's in tests/test_operators.py)."""
+    from pyfr_gb300.inifile import Inifile
+    from pyfr_gb300.quadrules import tensor_rule
+    from pyfr_gb300.shapes import get_shape
+    from pyfr_gb300.solvers.system import EulerSystem, NavierStokesSystem
+    from tests.oracle_util import ops_from_shape
+    g = golden[f'geometry_{case}']
+    mesh = _golden_mesh(g, etype)
+    nd = mesh.ndims
+    ns = system == 'navier-stokes'
+    c = dict(gamma=1.4, mu=0.05, Pr=0.72, **{'ldg-beta': 0.5,
+                                             'ldg-tau': 0.1})
+    cfg = Inifile()
+    for k in ('gamma', 'mu', 'Pr'):
+        cfg.set('constants', k, c[k])
+    cfg.set('solver', 'order', 3)
+    cfg.set('solver', 'anti-alias', aa)
+    cfg.set('solver-interfaces', 'riemann-solver', 'rusanov')
+    cfg.set('solver-interfaces', 'ldg-beta', 0.5)
+    cfg.set('solver-interfaces', 'ldg-tau', 0.1)
+    ics = g['ics'][:, :nd + 2]
+    scls = NavierStokesSystem if ns else EulerSystem
+    s = scls(_backend(cfg), mesh, {etype: ics}, 2, cfg)
+    s.commit()
+    s.rhs(0.0, 0, 1)
+    (r,) = s.ele_scal_upts(1)
+
+    shp = get_shape(etype, 3)
+    shp.set_surf_rules({('line' if nd == 2 else 'quad'):
+                        tensor_rule('gauss-legendre', 5, nd - 1)})
+    daa = None
+    if 'flux,' in aa:
+        daa = dict(M7=shp.m7, M1329=shp.opmat('(M1 - M3*M2)*M9'),
+                   qpts=shp.qpts)
+    d = Discretisation(ops_from_shape(shp, ns), basis_of(shp), g['spts'],
+                       g['lhs'], g['rhs'], periods=(2.0,)*nd, aa=daa)
+    ref = d.rhs_ns(ics, c) if ns else d.rhs_euler(ics, dict(gamma=1.4))
+    assert _relerr(r, ref) < TOL

@@ -126,3 +126,26 @@ def test_simplex_ortho_basis_matches_reference(kind, order):
     b = SimplexOrthoBasis(kind, order, g[f'{key}/pts'])
     assert [tuple(d) for d in g[f'{key}/degrees']] == b.degrees
     np.testing.assert_allclose(b.vdm, g[f'{key}/vdm'], rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize('name', ['quad', 'hex'])
+@pytest.mark.parametrize('order', [2, 3])
+def test_surface_antialiasing_operators(name, order):
+    """Surface-flux anti-aliasing: flux points at the face quadrature
+    points, M0 there and M3 with the L2 projection onto the face bases,
+    against the reference's (tests/golden/surf_flux.npz), up to the order
+    of the points."""
+    from pathlib import Path
+    from pyfr_gb300.quadrules import tensor_rule
+    g = np.load(Path(__file__).parent / 'golden' / 'surf_flux.npz')
+    key = f'{name}_p{order}'
+    s = get_shape(name, order)
+    nd = s.ndims
+    fk = 'line' if nd == 2 else 'quad'
+    s.set_surf_rules({fk: tensor_rule('gauss-legendre', order + 2, nd - 1)})
+    rf = g[f'{key}/fpts']
+    perm = [int(np.argmin(np.linalg.norm(s.fpts - p, axis=1))) for p in rf]
+    assert sorted(perm) == list(range(len(rf)))
+    np.testing.assert_allclose(s.fpts[perm], rf, atol=1e-14)
+    np.testing.assert_allclose(s.m0[perm], g[f'{key}/m0'], atol=1e-12)
+    np.testing.assert_allclose(s.m3[:, perm], g[f'{key}/m3'], atol=1e-12)
