@@ -549,18 +549,24 @@ class Solution:
     prevcfgs: dict = field(default_factory=dict)
     state: dict = field(default_factory=dict)
     uuid: str = None
+    grad_data: dict = field(default_factory=dict)
 
 
-def soln_dtype(fields, nupts, fpdtype, aux=()):
+def soln_dtype(fields, nupts, fpdtype, aux=(), ndims=0):
     """Nested compound dtype of one element's solution record
-    (``pyfr/writers/native.py:222-235``)."""
+    (``pyfr/writers/native.py:222-235``); with ``ndims`` a ``grad`` group
+    of (ndims, nupts) per field."""
+    groups = [('soln', [(n, fpdtype, (nupts,)) for n in fields])]
+    if ndims:
+        groups.append(('grad', [(n, fpdtype, (ndims, nupts))
+                                for n in fields]))
     afields = [('part-id', np.int64)] + list(aux)
-    return np.dtype([('soln', [(n, fpdtype, (nupts,)) for n in fields]),
-                     ('aux', afields)])
+    return np.dtype(groups + [('aux', afields)])
 
 
 def write_soln(fname, mesh, data, upts, fields, config, stats, *,
-               prefix='soln', prevcfgs=None, state=None, fpdtype=None):
+               prefix='soln', prevcfgs=None, state=None, fpdtype=None,
+               grads=None):
     """Write a solution file.
 
     ``data`` maps element types to (nupts, nvars, neles) arrays in the
@@ -570,7 +576,8 @@ def write_soln(fname, mesh, data, upts, fields, config, stats, *,
     Inifile and ``prevcfgs`` the {'config-<n>': INI text} history, to which
     the current configuration is appended when it differs from the last
     entry (``pyfr/integrators/base.py:369-381``); ``state`` holds
-    serialised arrays such as ``intg/ctrl``."""
+    serialised arrays such as ``intg/ctrl``; ``grads`` maps element types
+    to their physical gradients (ndims, nupts, nvars, neles)."""
     order = config.getint('solver', 'order')
     w = NativeFileWriter()
     cfgtxt = config.tostr()
@@ -594,7 +601,9 @@ def write_soln(fname, mesh, data, upts, fields, config, stats, *,
     for et, u in data.items():
         u = np.asarray(u)
         nupts, nvars, neles = u.shape
-        dt = soln_dtype(fields, nupts, fpdtype or u.dtype)
+        g = None if grads is None else np.asarray(grads[et])
+        dt = soln_dtype(fields, nupts, fpdtype or u.dtype,
+                        ndims=0 if g is None else g.shape[0])
         gi = (mesh.eidxs or {}).get(et)
         ntot = neles if gi is None else int(gi.max()) + 1
         if gi is not None and ntot != neles:
@@ -603,6 +612,8 @@ def write_soln(fname, mesh, data, upts, fields, config, stats, *,
         rows = np.arange(neles) if gi is None else gi
         for i, name in enumerate(fields):
             arr['soln'][name][rows] = u[:, i, :].T
+            if g is not None:
+                arr['grad'][name][rows] = g[:, :, i, :].transpose(2, 0, 1)
         ek = f'{prefix}/p{order}-{et}'
         w[ek] = arr
         w.set_attr(ek, 'pts', np.asarray(upts[et], dtype=np.float64))
@@ -651,6 +662,11 @@ def read_soln(fname, mesh, prefix=None):
             u = np.stack([rec['soln'][n] for n in names], axis=1)
             soln.data[et] = np.ascontiguousarray(u.transpose(2, 1, 0))
             soln.aux[et] = {n: rec['aux'][n] for n in rec.dtype['aux'].names}
+            if 'grad' in rec.dtype.names:
+                g = np.stack([rec['grad'][n] for n in names], axis=1)
+                # (neles, nvars, ndims, nupts) -> (ndims, nupts, nvars, neles)
+                soln.grad_data[et] = np.ascontiguousarray(
+                    g.transpose(2, 3, 1, 0))
     return soln
 
 

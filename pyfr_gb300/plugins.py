@@ -79,7 +79,8 @@ class WriterPlugin:
     ``basedir/basename`` (formatted with the time ``t`` and the output
     count ``n``; the ``.pyfrs`` extension is added), with the
     configuration chain, the run statistics and the integrator's
-    serialised state.  ``files`` lists what was written."""
+    serialised state, and with ``write-gradients`` the physical gradients.
+    ``files`` lists what was written."""
 
     name = 'writer'
 
@@ -89,8 +90,10 @@ class WriterPlugin:
         from pyfr_gb300.native import file_path_gen
 
         cfg = intg.cfg
-        if cfg.getbool(cfgsect, 'write-gradients', False):
-            raise NotImplementedError('Gradient output is not provided')
+        self._grads = cfg.getbool(cfgsect, 'write-gradients', False)
+        if self._grads and not hasattr(intg.system, 'compute_grads'):
+            raise ValueError('Gradient output needs a system with '
+                             'gradients')
         basedir = Path(cfg.get(cfgsect, 'basedir', '.')).absolute()
         basename = cfg.get(cfgsect, 'basename')
         if not basename.endswith('.pyfrs'):
@@ -125,7 +128,21 @@ class WriterPlugin:
         intg.collect_stats(stats)
         path = self._fgen.send(intg.tcurr)
         sysm = intg.system
+        grads = None
+        if self._grads:
+            # (the mixed-precision integrator's FP32 input is refreshed
+            # from its FP64 solution at every step start)
+            uidx = 0 if hasattr(intg, 'acc') else intg.idxcurr
+            sysm.compute_grads(intg.tcurr, uidx)
+            gl = sysm.grad_upts()
+            if getattr(intg, 'uref', None) is not None:
+                # Gradients of the shifted variables q: grad E = grad q_E +
+                # h_ref grad rho
+                for g in gl:
+                    g[:, :, -1] += intg.hs_ref*g[:, :, 0]
+            grads = dict(zip(sysm.ele_types, gl))
         write_soln(path, sysm.mesh, dict(zip(sysm.ele_types, intg.soln)),
                    self._upts, self.fields, intg.cfg, stats,
-                   prevcfgs=intg.prevcfgs, state=intg.serialise())
+                   prevcfgs=intg.prevcfgs, state=intg.serialise(),
+                   grads=grads)
         self.files.append(path)

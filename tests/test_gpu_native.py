@@ -130,3 +130,42 @@ def test_restart_bit_identical(built, tmp_path, controller, form):
     s2 = read_soln(wr2.files[-1], mesh)
     assert np.array_equal(s2.data['quad'], ufull)
     assert sorted(s2.prevcfgs) == ['config-0', 'config-1']
+
+
+def test_writer_gradients(built, tmp_path):
+    """write-gradients: the physical gradients of the written solution
+    (the system's gradient pass, pyfr/plugins/writer.py:27-33,113-116)
+    against the oracle's corrected gradients of the same solution."""
+    from pyfr_gb300.backend import B200Backend
+    from pyfr_gb300.cases import ns_tgv
+    from pyfr_gb300.integrators import RKVdH2Integrator
+    from pyfr_gb300.native import read_soln, save_mesh, read_mesh
+    from pyfr_gb300.plugins import WriterPlugin
+    from pyfr_gb300.solvers.system import NavierStokesSystem
+    from tests.oracle_util import disc_for_mesh
+
+    cfg, mesh = ns_tgv(n=3, order=3, dt=5e-4)
+    w = 'soln-plugin-writer'
+    cfg.set(w, 'dt-out', '0.001')
+    cfg.set(w, 'basedir', str(tmp_path))
+    cfg.set(w, 'basename', 'tgv-{t:.3f}')
+    cfg.set(w, 'write-gradients', 'true')
+    save_mesh(tmp_path / 't.pyfrm', mesh)
+    fmesh = read_mesh(tmp_path / 't.pyfrm')
+    intg = RKVdH2Integrator(B200Backend(cfg), NavierStokesSystem, fmesh, cfg)
+    wr = WriterPlugin(intg)
+    intg.add_plugin(wr)
+    intg.advance_to(0.001)
+    s = read_soln(wr.files[-1], fmesh)
+    u = s.data['hex']
+    # (the oracle on the mesh read from the file: its interfaces take the
+    # left side by the file's rule, which the LDG common solution sees)
+    fmesh.periods = mesh.periods
+    d = disc_for_mesh(fmesh, 3, ns=True)
+    c = cfg.items_as('constants', float) | cfg.items_as('solver-interfaces',
+                                                       float)
+    gout = []
+    d.rhs_ns(u, c, grads_out=gout)
+    g = s.grad_data['hex']
+    assert g.shape == gout[0].shape
+    assert np.abs(g - gout[0]).max()/np.abs(gout[0]).max() < 1e-10

@@ -321,3 +321,20 @@ def test_restart_records_without_gpu(tmp_path):
     r = read_mesh(tmp_path / 'm.pyfrm')
     assert set(r.bcon) == {'lo', 'hi'}
     assert len(r.con[0]) == 2
+
+
+def test_soln_gradients_round_trip(tmp_path):
+    m = _soln_mesh()
+    rng = np.random.default_rng(4)
+    u = rng.standard_normal((16, 4, 6))
+    g = rng.standard_normal((2, 16, 4, 6))
+    cfg = Inifile()
+    cfg.set('solver', 'order', 3)
+    write_soln(tmp_path / 'g.pyfrs', m, {'quad': u}, {'quad': np.zeros((16, 2))},
+               ['rho', 'rhou', 'rhov', 'E'], cfg, None, grads={'quad': g})
+    s = read_soln(tmp_path / 'g.pyfrs', m)
+    assert np.array_equal(s.grad_data['quad'], g)
+    with NativeFile(tmp_path / 'g.pyfrs') as f:
+        rec = f['soln/p3-quad']
+        # grad.rhou of the element stored first (file number 0 = local 1)
+        assert np.array_equal(rec['grad']['rhou'][0], g[:, :, 1, 1])
