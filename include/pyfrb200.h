@@ -383,6 +383,12 @@ int b200_bccflux_ns_av_f32(int ndims, int64_t n, int rsolver, const b200_gas_t *
                            const float *gl_base, const void *gl_map, const void *gl_rstr,
                            int ix64, const float *nl, int64_t ldn, const float *av_base,
                            const void *av_map, void *stream);
+/* The chosen form's FP64 solution acc takes the FP32 values u32 of the
+ * elements whose filter strength is below 1 (both nupts x nvars x neles
+ * AoSoA, leading dimensions ldu and lda). */
+int b200_ef_merge_f64f32(int nupts, int nvars, int64_t neles, const float *ef_filter,
+                         const float *u32, int64_t ldu, double *acc, int64_t lda,
+                         void *stream);
 /* Minimum entropy of each element on all its faces;
  * pyfr/solvers/euler/kernels/entropylocal.mako:5-40. */
 int b200_entropylocal_f64(const b200_ef_t *p, int64_t neles, const double *u, int64_t ldu,

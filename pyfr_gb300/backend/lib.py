@@ -138,6 +138,7 @@ _SIGS = {
     'b200_host_free': [vp],
     'b200_memset': [vp, i32, sz, vp],
     'b200_stage_time': [vp, vp, f64, f64, vp],
+    'b200_ef_merge_f64f32': [i32, i32, i64, vp, vp, i64, vp, i64, vp],
     'b200_memcpy_htod': [vp, vp, sz, vp],
     'b200_memcpy_dtoh': [vp, vp, sz, vp],
     'b200_memcpy_dtod': [vp, vp, sz, vp],

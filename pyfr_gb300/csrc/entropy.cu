@@ -55,9 +55,35 @@ int intcent(int64_t n, T *lbase, const void *lmap, T *rbase, const void *rmap, i
     return B200_OK;
 }
 
+// The chosen form keeps its solution in FP64 outside the system: the
+// elements that the FP32 filter changed (strength below 1) replace their
+// FP64 values by the filtered FP32 ones
+__global__ void ef_merge_kernel(int nupts, int nvars, int64_t neles, const float *ef,
+                                const float *u32, int64_t ldu, double *acc, int64_t lda) {
+    const int64_t e = (int64_t)blockIdx.x * 128 + threadIdx.x;
+    const int k = blockIdx.y;
+    if (e >= neles || !(ef[e] < 1.0f)) return;
+    for (int v = 0; v < nvars; v++) {
+        const int64_t o = b200::soa_off(e, v, nvars);
+        acc[k * lda + o] = (double)u32[k * ldu + o];
+    }
+}
+
 }  // namespace
 
 extern "C" {
+
+int b200_ef_merge_f64f32(int nupts, int nvars, int64_t neles, const float *ef_filter,
+                         const float *u32, int64_t ldu, double *acc, int64_t lda,
+                         void *stream) {
+    if (neles <= 0 || nupts <= 0) return B200_OK;
+    if (!ef_filter || !u32 || !acc) return b200::set_error(B200_ERR_ARG, "ef_merge: null argument");
+    dim3 grid(b200::ceil_div(neles, 128), nupts);
+    ef_merge_kernel<<<grid, 128, 0, (cudaStream_t)stream>>>(nupts, nvars, neles, ef_filter, u32,
+                                                             ldu, acc, lda);
+    B200_CHECK_LAUNCH("ef_merge");
+    return B200_OK;
+}
 
 int b200_entropyfilter_f64(const b200_ef_t *p, int64_t neles, double *u, int64_t ldu,
                            double *entmin, int64_t lde, double *ef_filter, const double *vdm,

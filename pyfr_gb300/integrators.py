@@ -511,11 +511,29 @@ class MixedRKIntegrator(RKVdH2Integrator):
         if backend.fpdtype != np.float32:
             raise ValueError('The mixed-precision integrator needs a '
                              'single-precision backend')
-        if cfg.get('solver', 'shock-capturing', 'none') == 'entropy-filter':
-            raise NotImplementedError('The entropy filter needs the FP64 '
-                                      'solution in the system (the plain '
-                                      'integrator)')
         super().__init__(backend, systemcls, mesh, cfg, initsoln)
+
+        # Entropy filter: the filter runs in FP32 on the system's copy of
+        # the solution (the step's last stage leaves it there), and the
+        # elements it changed go back to the FP64 solution; the starting
+        # minima pass too (run by the base class) is merged here
+        self._ef_merge = []
+        if self.system._ef:
+            ef = self.system._ef
+            for j, (et, e) in enumerate(self.system.ele_map.items()):
+                acc, u32, eff = self.acc[j], self.system.ele_banks[j][0], \
+                    ef.ef_filter[et]
+                args = (e.nupts, e.nvars, e.neles, eff.data, u32.data,
+                        u32.leaddim, acc.data, acc.leaddim)
+
+                def run(stream, args=args):
+                    backend.lib.ef_merge_f64f32(*args, stream)
+
+                self._ef_merge.append(Kernel(run, mats=[acc, u32, eff],
+                                             name='ef_merge'))
+            for k in self._ef_merge:
+                k.run(backend.stream)
+            backend.wait()
 
     def _make_system(self, backend, systemcls, mesh, initsoln, cfg):
         sysm = systemcls(backend, mesh, initsoln, 2, cfg,
@@ -637,6 +655,11 @@ class MixedRKIntegrator(RKVdH2Integrator):
                 kl.extend(g.klist)
             kl.extend(self._stage_kernel(i, j, dt)
                       for j in range(len(self.acc)))
+        # (the entropy filter of the new solution, merged back into FP64)
+        post = self.system.postproc_kernels(0)
+        if post:
+            kl.extend(post)
+            kl.extend(self._ef_merge)
         return kl, ((0, 1, 2) if self.errest else (0,))
 
     def _reject(self, iprev):
