@@ -1037,7 +1037,11 @@ class EntropyFilterOracle:
                     ('e', eavg, entmin - o['e_tol'], None)):
                 cur = dict(d=dmin, p=pmin, e=emin)[vmin]
                 if cur < bound:
-                    alpha = min(max((cur - bound)/(cur - vavg), 0.0), 1.0)
+                    # (fmax/fmin semantics: a 0/0 ratio gives 0, an
+                    # infinite one the clamp, as in the kernel)
+                    with np.errstate(divide='ignore', invalid='ignore'):
+                        ratio = np.float64(cur - bound)/np.float64(cur - vavg)
+                    alpha = float(np.fmin(np.fmax(ratio, 0.0), 1.0))
                     f = min(f, 1.0 - alpha)
                     sl = slice(0, nv)
                     ue[:, sl] += alpha*(uavg[sl] - ue[:, sl])
