@@ -15,8 +15,9 @@ Behaviour of ``pyfr/readers/gmsh.py`` and ``pyfr/readers/base.py:108-497``:
   left over is an error.
 * the node table is the dense range of the file's node numbers.
 
-Only first-order elements are read: the geometry of this solver is linear,
-and a high-order Gmsh element type raises.
+The geometry of this solver is linear: high-order Gmsh elements are read
+when they are straight (their nodes on the linear element's lattice) and
+kept as their vertices; curved ones raise.
 """
 
 from collections import defaultdict
@@ -39,9 +40,19 @@ GMSH_VERTEX_ORDER = {'line': [0, 1], 'tri': [0, 1, 2], 'quad': [0, 1, 3, 2],
                      'tet': [0, 1, 2, 3], 'hex': [0, 1, 3, 2, 4, 5, 7, 6],
                      'pri': [0, 1, 2, 3, 4, 5], 'pyr': [0, 1, 3, 2, 4]}
 
-# Higher-order Gmsh element types (curved geometry)
-GMSH_CURVED = {8, 9, 10, 11, 12, 13, 14, 21, 23, 26, 27, 29, 30, 36, 37,
-               90, 91, 92, 93, 118, 119}
+# Higher-order Gmsh element types (Gmsh's element-type numbering): native
+# type, node count and order.  Gmsh lists the vertices first, in the
+# first-order element's order.
+GMSH_HIGH_ORDER = {
+    8: ('line', 3, 2), 26: ('line', 4, 3), 27: ('line', 5, 4),
+    9: ('tri', 6, 2), 21: ('tri', 10, 3), 23: ('tri', 15, 4),
+    10: ('quad', 9, 2), 36: ('quad', 16, 3), 37: ('quad', 25, 4),
+    11: ('tet', 10, 2), 29: ('tet', 20, 3), 30: ('tet', 35, 4),
+    12: ('hex', 27, 2), 92: ('hex', 64, 3), 93: ('hex', 125, 4),
+    13: ('pri', 18, 2), 90: ('pri', 40, 3), 91: ('pri', 75, 4)}
+
+# Pyramids of any order and higher-order types without a linear reading
+GMSH_UNSUPPORTED = {14, 118, 119}
 
 _NDIMS = {'tri': 2, 'quad': 2, 'tet': 3, 'hex': 3, 'pri': 3, 'pyr': 3}
 
@@ -182,11 +193,45 @@ class GmshReader:
         self._nodeoff = lo
 
     def _check_type(self, etype):
-        if etype in GMSH_CURVED:
-            raise ValueError(f'High-order element type {etype} is not '
-                             'supported (linear geometry only)')
-        if etype not in GMSH_ETYPES:
+        if etype in GMSH_UNSUPPORTED or (etype not in GMSH_ETYPES and
+                                         etype not in GMSH_HIGH_ORDER):
             raise ValueError(f'Unsupported element type {etype}')
+
+    def _nnodes(self, etype):
+        return GMSH_HIGH_ORDER[etype][1] if etype in GMSH_HIGH_ORDER else \
+            GMSH_ETYPES[etype][1]
+
+    def _linearise(self, etype, nodes, lintol=1e-5):
+        """The vertices of high-order elements whose other nodes all lie on
+        the equi-spaced lattice of their linear element (within ``lintol``
+        of the element's extent): straight elements stored at a higher
+        order (the reference snaps these too, pyfr/readers/base.py:
+        464-497).  Curved elements raise: the geometry path is linear."""
+        if etype not in GMSH_HIGH_ORDER:
+            return etype, nodes
+        from pyfr_gb300.native import std_ele
+        from pyfr_gb300.shapes import VERTICES, linear_shape_fn
+        petype, nn, order = GMSH_HIGH_ORDER[etype]
+        lin = {v[0]: k for k, v in GMSH_ETYPES.items()}
+        nv = len(VERTICES[petype]) if petype != 'line' else 2
+        verts = nodes[:, :nv] - self._nodeoff
+        if petype != 'line':
+            nd = {'tri': 2, 'quad': 2, 'tet': 3, 'hex': 3, 'pri': 3}[petype]
+            lat = std_ele(petype, order)
+            # Lattice positions from the vertices (Gmsh vertex order ->
+            # the format's)
+            sf = linear_shape_fn(petype, lat)                # (nlat, nv)
+            gv = self._nodepts[verts][:, GMSH_VERTEX_ORDER[petype], :nd]
+            want = np.einsum('lv,evd->eld', sf, gv)          # (ne, nlat, nd)
+            have = self._nodepts[nodes - self._nodeoff][:, :, :nd]
+            ext = np.ptp(gv, axis=1).max(axis=1)[:, None, None]
+            d = np.linalg.norm(have[:, :, None] - want[:, None], axis=3)
+            ok = np.all(d.min(axis=2) <= lintol*ext[:, :, 0], axis=1)
+            if not np.all(ok):
+                raise ValueError(f'Curved high-order elements (type {etype}) '
+                                 'are not supported: the geometry path is '
+                                 'linear')
+        return lin[petype], nodes[:, :nv]
 
     def _read_eles(self, it):
         elenodes = defaultdict(list)
@@ -196,6 +241,8 @@ class GmshReader:
                 etype, ntags = v[1], v[2]
                 self._check_type(etype)
                 tags, nodes = v[3:3 + ntags], v[3 + ntags:]
+                if len(nodes) != self._nnodes(etype):
+                    raise ValueError(f'Element {v[0]}: wrong node count')
                 elenodes[etype, (tags[0],)].append(nodes)
         else:
             nb, ne = (int(i) for i in next(it).split()[:2])
@@ -203,7 +250,7 @@ class GmshReader:
             for _ in range(nb):
                 edim, etag, etype, ecount = (int(j) for j in next(it).split())
                 self._check_type(etype)
-                nn = GMSH_ETYPES[etype][1]
+                nn = self._nnodes(etype)
                 pents = self._tagpents[edim, etag]
                 for _ in range(ecount):
                     v = [int(i) for i in next(it).split()]
@@ -211,8 +258,11 @@ class GmshReader:
                 count += ecount
             if count != ne:
                 raise ValueError('Invalid element count')
-        self._elenodes = {k: np.array(v, dtype=np.int64)
-                          for k, v in elenodes.items()}
+        out = defaultdict(list)
+        for (etype, pents), v in elenodes.items():
+            lt, nodes = self._linearise(etype, np.array(v, dtype=np.int64))
+            out[lt, pents].append(nodes)
+        self._elenodes = {k: np.vstack(v) for k, v in out.items()}
 
     # ---- assembly ------------------------------------------------------------
 

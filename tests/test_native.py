@@ -233,9 +233,9 @@ def test_gmsh_errors(bad, msg):
     txt = '\n'.join(lines[:i] + lines[i + 1:]).replace('\n8\n1 1', '\n7\n1 1')
     with pytest.raises(ValueError, match='Unpaired'):
         GmshReader(txt + '\n').records()
-    # High-order elements are refused
+    # A second-order type with a first-order node list is refused
     txt = TWO_QUADS.replace('7 3 2 20 4 1 2 5 4', '7 10 2 20 4 1 2 5 4')
-    with pytest.raises(ValueError, match='High-order'):
+    with pytest.raises(ValueError, match='node count'):
         GmshReader(txt)
     # One side of a periodic pair alone
     txt = TWO_QUADS.replace('"inlet"', '"periodic_0_l"')
@@ -338,3 +338,66 @@ def test_soln_gradients_round_trip(tmp_path):
         rec = f['soln/p3-quad']
         # grad.rhou of the element stored first (file number 0 = local 1)
         assert np.array_equal(rec['grad']['rhou'][0], g[:, :, 1, 1])
+
+
+# The two quads as second-order elements: 9-node quadrilaterals and 3-node
+# lines (vertices first, then edge midpoints, then the centre, as Gmsh
+# lists them); nodes 7-13 are the extra nodes
+TWO_QUADS_P2 = """$MeshFormat
+2.2 0 8
+$EndMeshFormat
+$PhysicalNames
+4
+1 10 "Wall"
+1 11 "inlet"
+1 12 "outlet"
+2 20 "fluid"
+$EndPhysicalNames
+$Nodes
+13
+1 0 0 0
+2 1 0 0
+3 2 0 0
+4 0 1 0
+5 1 1 0
+6 2 1 0
+7 0.5 0 0
+8 1.5 0 0
+9 0.5 1 0
+10 1.5 1 0
+11 0 0.5 0
+12 1 0.5 0
+13 2 0.5 0
+14 0.5 0.5 0
+15 1.5 0.5 0
+$EndNodes
+$Elements
+8
+1 8 2 10 1 1 2 7
+2 8 2 10 1 2 3 8
+3 8 2 10 1 4 5 9
+4 8 2 10 1 5 6 10
+5 8 2 11 2 1 4 11
+6 8 2 12 3 3 6 13
+7 10 2 20 4 1 2 5 4 7 12 9 11 14
+8 10 2 20 4 2 3 6 5 8 13 10 12 15
+$EndElements
+"""
+
+
+def test_gmsh_straight_high_order(tmp_path):
+    """Straight second-order elements read as their vertices, giving the
+    connectivity of the first-order file; a curved one raises."""
+    txt = TWO_QUADS_P2.replace('\n13\n1 0 0 0', '\n15\n1 0 0 0')
+    nodes, eles, codec, pmap = GmshReader(txt).records()
+    _, eles1, codec1, _ = GmshReader(TWO_QUADS).records()
+    assert codec == codec1
+    assert eles['quad']['faces'].tolist() == eles1['quad']['faces'].tolist()
+    assert eles['quad']['nodes'].tolist() == eles1['quad']['nodes'].tolist()
+    import_mesh(txt, tmp_path / 'p2.pyfrm')
+    assert _pairs(read_mesh(tmp_path / 'p2.pyfrm')) == \
+        {(('quad', 0, 1), ('quad', 1, 3))}
+
+    curved = txt.replace('\n14 0.5 0.5 0\n', '\n14 0.55 0.5 0\n')
+    with pytest.raises(ValueError, match='Curved'):
+        GmshReader(curved)
