@@ -190,7 +190,7 @@ typedef struct {
 int b200_mul_bf16x3_create_cat(const double *a1, int k1, const double *a2, int k2, int m,
                                 void **handle, size_t *smem_bytes);
 int b200_mul_bf16x3_apply(void *handle, const b200_mul_bf16x3_args_t *args, void *stream);
-/* TF32 variant (the benchmark spec's second contraction precision): operator
+/* TF32 variant (the second reduced contraction precision): operator
  * and data rounded to TF32, one tcgen05.mma.kind::tf32 product per K step,
  * FP32 accumulation.  The handles are applied and destroyed with the
  * _bf16x3 entry points (b200_mul_bf16x3, _apply, _destroy); `products` is
