@@ -566,7 +566,7 @@ def soln_dtype(fields, nupts, fpdtype, aux=(), ndims=0):
 
 def write_soln(fname, mesh, data, upts, fields, config, stats, *,
                prefix='soln', prevcfgs=None, state=None, fpdtype=None,
-               grads=None):
+               grads=None, subset=None):
     """Write a solution file.
 
     ``data`` maps element types to (nupts, nvars, neles) arrays in the
@@ -577,7 +577,10 @@ def write_soln(fname, mesh, data, upts, fields, config, stats, *,
     the current configuration is appended when it differs from the last
     entry (``pyfr/integrators/base.py:369-381``); ``state`` holds
     serialised arrays such as ``intg/ctrl``; ``grads`` maps element types
-    to their physical gradients (ndims, nupts, nvars, neles)."""
+    to their physical gradients (ndims, nupts, nvars, neles); ``subset``
+    maps element types to the local elements to write (the others are
+    left out and a ``<key>-idxs`` array lists the elements' numbers,
+    ascending, ``pyfr/writers/native.py:237-245``)."""
     order = config.getint('solver', 'order')
     w = NativeFileWriter()
     cfgtxt = config.tostr()
@@ -605,24 +608,43 @@ def write_soln(fname, mesh, data, upts, fields, config, stats, *,
         dt = soln_dtype(fields, nupts, fpdtype or u.dtype,
                         ndims=0 if g is None else g.shape[0])
         gi = (mesh.eidxs or {}).get(et)
-        ntot = neles if gi is None else int(gi.max()) + 1
-        if gi is not None and ntot != neles:
-            raise ValueError('Subset solutions are not written')
-        arr = np.zeros(ntot, dtype=dt)
-        rows = np.arange(neles) if gi is None else gi
+        gi = np.arange(neles) if gi is None else np.asarray(gi)
+        sel = np.arange(neles) if subset is None or et not in subset else \
+            np.asarray(subset[et], dtype=np.int64)
+        # Records in ascending order of the elements' numbers
+        o = np.argsort(gi[sel], kind='stable')
+        sel, nums = sel[o], gi[sel][o]
+        if subset is None and len(nums) and int(nums[-1]) + 1 != len(nums):
+            raise ValueError('Element numbers do not cover the mesh')
+        arr = np.zeros(len(sel), dtype=dt)
         for i, name in enumerate(fields):
-            arr['soln'][name][rows] = u[:, i, :].T
+            arr['soln'][name] = u[:, i, sel].T
             if g is not None:
-                arr['grad'][name][rows] = g[:, :, i, :].transpose(2, 0, 1)
+                arr['grad'][name] = g[:, :, i, sel].transpose(2, 0, 1)
         ek = f'{prefix}/p{order}-{et}'
         w[ek] = arr
         w.set_attr(ek, 'pts', np.asarray(upts[et], dtype=np.float64))
+        if subset is not None and et in subset:
+            w[f'{ek}-idxs'] = nums.astype(np.int64)
     w.save(fname)
 
 
 def read_soln(fname, mesh, prefix=None):
     """Read a solution file written for ``mesh`` (identifiers must agree;
-    ``pyfr/readers/native.py:113-235``)."""
+    ``pyfr/readers/native.py:113-235``).  Subset solutions raise (a
+    restart needs every element); ``read_subset_soln`` reads them."""
+    return _read_soln(fname, mesh, prefix, False)[1]
+
+
+def read_subset_soln(fname, mesh, prefix=None):
+    """(mesh, solution) of a solution file that may hold a subset of the
+    elements: the mesh is then cut down to the elements present, in their
+    order in the file, and has no interfaces
+    (``pyfr/readers/native.py:196-271``)."""
+    return _read_soln(fname, mesh, prefix, True)
+
+
+def _read_soln(fname, mesh, prefix, allow_subset):
     with NativeFile(fname) as f:
         uuid = f.string('mesh-uuid')
         if mesh.uuid is not None and uuid != mesh.uuid:
@@ -646,16 +668,27 @@ def read_soln(fname, mesh, prefix=None):
                         state=state, uuid=uuid)
         order = soln.config.getint('solver', 'order')
         prefix = prefix or stats.get('data', 'prefix')
+        subset = {}
         for et in mesh.etypes:
             ek = f'{prefix}/p{order}-{et}'
-            if ek not in f:
-                raise RuntimeError(f'Solution has no {ek}')
-            if f'{ek}-idxs' in f:
-                raise RuntimeError('Subset solutions are not supported')
-            rec = f[ek]
             gi = (mesh.eidxs or {}).get(et)
-            if gi is not None:
-                rec = rec[gi]
+            gi = np.arange(mesh.spts[et].shape[1]) if gi is None else gi
+            if ek not in f or f'{ek}-idxs' in f:
+                if not allow_subset:
+                    raise RuntimeError('Subset solutions are not supported'
+                                       if ek in f else
+                                       f'Solution has no {ek}')
+                if ek not in f:
+                    subset[et] = np.empty(0, dtype=np.int64)
+                    continue
+                nums = f[f'{ek}-idxs']
+                # Local elements of the file's element numbers
+                pos = np.full(int(max(gi.max(), nums.max())) + 1, -1)
+                pos[gi] = np.arange(len(gi))
+                subset[et] = pos[nums]
+                rec = f[ek]
+            else:
+                rec = f[ek][gi]
             names = list(rec.dtype['soln'].names)
             if soln.fields is None:
                 soln.fields = names
@@ -667,7 +700,24 @@ def read_soln(fname, mesh, prefix=None):
                 # (neles, nvars, ndims, nupts) -> (ndims, nupts, nvars, neles)
                 soln.grad_data[et] = np.ascontiguousarray(
                     g.transpose(2, 3, 1, 0))
-    return soln
+
+    if not subset:
+        return mesh, soln
+    from dataclasses import replace
+    spts, eidxs = {}, {}
+    for et in mesh.etypes:
+        sel = subset.get(et)
+        gi = (mesh.eidxs or {}).get(et)
+        gi = np.arange(mesh.spts[et].shape[1]) if gi is None else gi
+        if sel is None:
+            spts[et], eidxs[et] = mesh.spts[et], gi
+        elif len(sel):
+            spts[et], eidxs[et] = mesh.spts[et][:, sel], gi[sel]
+    sub = replace(mesh, spts=spts, eidxs=eidxs, con=None, bcon={},
+                  spts_curved={et: np.zeros(v.shape[1], bool)
+                               for et, v in spts.items()})
+    soln.data = {et: v for et, v in soln.data.items() if et in spts}
+    return sub, soln
 
 
 def file_path_gen(basedir, basename):

@@ -15,8 +15,8 @@ from pyfr_gb300.gmsh import GmshReader, fuzzy_lexsort, import_mesh
 from pyfr_gb300.inifile import Inifile
 from pyfr_gb300.mesh import Mesh, Side, box, mixed_box, periodic_box, tri_box
 from pyfr_gb300.native import (NativeFile, NativeFileWriter, corner_nodes,
-                               read_mesh, read_soln, save_mesh, std_ele,
-                               write_soln)
+                               read_mesh, read_soln, read_subset_soln,
+                               save_mesh, std_ele, write_soln)
 from tests.gmsh_util import box_msh
 
 
@@ -401,3 +401,29 @@ def test_gmsh_straight_high_order(tmp_path):
     curved = txt.replace('\n14 0.5 0.5 0\n', '\n14 0.55 0.5 0\n')
     with pytest.raises(ValueError, match='Curved'):
         GmshReader(curved)
+
+
+def test_subset_solution(tmp_path):
+    """A solution of some elements only: records in ascending element
+    number with a -idxs array; read back as a cut-down mesh, refused for a
+    restart (pyfr/writers/native.py:237-245, pyfr/readers/native.py:
+    113-271)."""
+    m = _soln_mesh()
+    u = np.random.default_rng(5).standard_normal((16, 4, 6))
+    cfg = Inifile()
+    cfg.set('solver', 'order', 3)
+    sel = np.array([3, 0, 5])               # local elements; numbers 1, 4, 2
+    write_soln(tmp_path / 's.pyfrs', m, {'quad': u}, {'quad': np.zeros((16, 2))},
+               ['rho', 'rhou', 'rhov', 'E'], cfg, None,
+               subset={'quad': sel})
+    with NativeFile(tmp_path / 's.pyfrs') as f:
+        assert f['soln/p3-quad-idxs'].tolist() == [1, 2, 4]
+        assert len(f['soln/p3-quad']) == 3
+    with pytest.raises(RuntimeError, match='Subset'):
+        read_soln(tmp_path / 's.pyfrs', m)
+    sub, s = read_subset_soln(tmp_path / 's.pyfrs', m)
+    assert sub.eidxs['quad'].tolist() == [1, 2, 4]
+    loc = [3, 5, 0]
+    assert np.array_equal(s.data['quad'], u[:, :, loc])
+    assert np.array_equal(sub.spts['quad'], m.spts['quad'][:, loc])
+    assert sub.con is None
