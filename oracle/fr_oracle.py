@@ -148,7 +148,288 @@ def hllc(ul, ur, n, gamma):
                              np.where((ss <= 0) & (0 <= sr), nfsr, nfr)))
 
 
-RSOLVERS = {'rusanov': rusanov, 'hllc': hllc}
+def _nflux(n, f):
+    return np.einsum('d...,dv...->v...', n, f)
+
+
+def _roe_avg(ul, ur, vl, vr, pl, pr):
+    """Roe averages shared by HLL and HLLC: normal speed, enthalpy and
+    velocity (pyfr/solvers/euler/kernels/rsolvers/hll.mako:21-36)."""
+    sql, sqr = np.sqrt(ul[0]), np.sqrt(ur[0])
+    H = (sql*(pr + ur[-1]) + sqr*(pl + ul[-1]))/(sql*ur[0] + sqr*ul[0])
+    va = (vl*sql + vr*sqr)*(1/(sql + sqr))
+    return sql, sqr, H, va
+
+
+def hll(ul, ur, n, gamma):
+    """HLL flux (pyfr/solvers/euler/kernels/rsolvers/hll.mako:4-53)."""
+    fl, pl, vl = inviscid_flux(ul, gamma)
+    fr, pr, vr = inviscid_flux(ur, gamma)
+    nvl, nvr = np.sum(n*vl, axis=0), np.sum(n*vr, axis=0)
+    ar = np.sqrt(gamma*pr/ur[0])
+    sql, sqr, H, va = _roe_avg(ul, ur, vl, vr, pl, pr)
+    nv = (sql*nvl + sqr*nvr)/(sql + sqr)
+    a = np.sqrt((gamma - 1)*(H - 0.5*np.sum(va*va, axis=0)))
+    # The reference takes the right state's sound speed on both sides
+    sl = np.minimum(nv - a, nvl - ar)
+    sr = np.maximum(nv + a, nvr + ar)
+    nfl, nfr = _nflux(n, fl), _nflux(n, fr)
+    sub = (sr*nfl - sl*nfr + sl*sr*(ur - ul))*(1/(sr - sl))
+    return np.where(0 <= sl, nfl, np.where(0 >= sr, nfr, sub))
+
+
+def _rot_to(n, u):
+    """Momentum in the frame whose first axis is n (Moler and Hughes 1999;
+    pyfr/solvers/baseadvec/kernels/transform.mako:5-38)."""
+    t = u.copy()
+    m = u[1:-1]
+    if len(n) == 2:
+        t[1] = n[0]*m[0] + n[1]*m[1]
+        t[2] = n[0]*m[1] - n[1]*m[0]
+        return t
+    with np.errstate(all='ignore'):
+        h1, h2, h3 = 1/(1 + n[0]), 1/(1 - n[1]), 1/(1 - n[2])
+        a = (n[0]*m[0] + n[1]*m[1] + n[2]*m[2],
+             (n[0] + h1*n[2]*n[2])*m[1] - n[1]*m[0] - h1*n[1]*n[2]*m[2],
+             (n[0] + h1*n[1]*n[1])*m[2] - n[2]*m[0] - h1*n[1]*n[2]*m[1])
+        b = (a[0],
+             (1 - h2*n[0]*n[0])*m[0] + n[0]*m[1] - h2*n[0]*n[2]*m[2],
+             n[2]*m[1] - h2*n[0]*n[2]*m[0] + (1 - h2*n[2]*n[2])*m[2])
+        c = (a[0],
+             (1 - h3*n[1]*n[1])*m[1] - h3*n[0]*n[1]*m[0] + n[1]*m[2],
+             (1 - h3*n[0]*n[0])*m[0] - h3*n[0]*n[1]*m[1] + n[0]*m[2])
+    ca, cb = np.abs(n[0]) < 0.99, np.abs(n[1]) < np.abs(n[2])
+    for k in range(3):
+        t[1 + k] = np.where(ca, a[k], np.where(cb, b[k], c[k]))
+    return t
+
+
+def _rot_from(n, t):
+    """Inverse of _rot_to (transform.mako:41-75)."""
+    u = t.copy()
+    m = t[1:-1]
+    if len(n) == 2:
+        u[1] = n[0]*m[0] - n[1]*m[1]
+        u[2] = n[1]*m[0] + n[0]*m[1]
+        return u
+    with np.errstate(all='ignore'):
+        h1, h2, h3 = 1/(1 + n[0]), 1/(1 - n[1]), 1/(1 - n[2])
+        a = (n[0]*m[0] - n[1]*m[1] - n[2]*m[2],
+             n[1]*m[0] + (n[0] + h1*n[2]*n[2])*m[1] - h1*n[1]*n[2]*m[2],
+             n[2]*m[0] - h1*n[1]*n[2]*m[1] + (n[0] + h1*n[1]*n[1])*m[2])
+        b = (n[0]*m[0] + (1 - h2*n[0]*n[0])*m[1] - h2*n[0]*n[2]*m[2],
+             n[1]*m[0] + n[0]*m[1] + n[2]*m[2],
+             n[2]*m[0] - h2*n[0]*n[2]*m[1] + (1 - h2*n[2]*n[2])*m[2])
+        c = (n[0]*m[0] - h3*n[0]*n[1]*m[1] + (1 - h3*n[0]*n[0])*m[2],
+             n[1]*m[0] + (1 - h3*n[1]*n[1])*m[1] - h3*n[0]*n[1]*m[2],
+             n[2]*m[0] + n[1]*m[1] + n[0]*m[2])
+    ca, cb = np.abs(n[0]) < 0.99, np.abs(n[1]) < np.abs(n[2])
+    for k in range(3):
+        u[1 + k] = np.where(ca, a[k], np.where(cb, b[k], c[k]))
+    return u
+
+
+def _rsolve_rotated(solve1d, ul, ur, n, gamma):
+    """A one-dimensional solver applied in the normal frame
+    (pyfr/solvers/euler/kernels/rsolvers/rsolve1d.mako:5-22)."""
+    return _rot_from(n, solve1d(_rot_to(n, ul), _rot_to(n, ur), gamma))
+
+
+def _flux_1d(s, gamma):
+    """x-direction flux of a rotated state (flux.mako:28-48)."""
+    nd = s.shape[0] - 2
+    invrho, E = 1/s[0], s[-1]
+    v = invrho*s[1:nd + 1]
+    p = (gamma - 1)*(E - 0.5*invrho*np.sum(s[1:nd + 1]**2, axis=0))
+    f = np.empty_like(s)
+    f[0] = s[1]
+    f[-1] = (E + p)*v[0]
+    f[1] = s[1]*v[0] + p
+    for j in range(1, nd):
+        f[j + 1] = s[1]*v[j]
+    return f, p, v
+
+
+def roe_1d(ul, ur, gamma, eps=0.001):
+    """Roe flux with the entropy fix of
+    pyfr/solvers/euler/kernels/rsolvers/roe.mako:6-84."""
+    nd = ul.shape[0] - 2
+    fl, pl, vl = _flux_1d(ul, gamma)
+    fr, pr, vr = _flux_1d(ur, gamma)
+    sql, sqr = np.sqrt(ul[0]), np.sqrt(ur[0])
+    roa = sql*sqr
+    ha = (sql*(pr + ur[-1]) + sqr*(pl + ul[-1]))/(sql*ur[0] + sqr*ul[0])
+    va = (vl*sql + vr*sqr)*(1/(sql + sqr))
+    qq = np.sum(va*va, axis=0)
+    a = np.sqrt((gamma - 1)*(ha - 0.5*qq))
+    l1, l2, l3 = np.abs(va[0] - a), np.abs(va[0]), np.abs(va[0] + a)
+    l1 = np.where(l1 < eps, (0.5/eps)*(l1*l1 + eps**2), l1)
+    l3 = np.where(l3 < eps, (0.5/eps)*(l3*l3 + eps**2), l3)
+    dv = vr - vl
+    dro, dp = ur[0] - ul[0], pr - pl
+    ia2 = 1/(2*a*a)
+    w1 = (dp - roa*a*dv[0])*ia2
+    w2 = dro - dp*2*ia2
+    w3 = (dp + roa*a*dv[0])*ia2
+    nf = np.empty_like(ul)
+    nf[0] = 0.5*(fl[0] + fr[0]) - (l1*w1 + l2*w2 + l3*w3)
+    for i in range(nd):
+        if i == 0:
+            v1, v2, v3 = w1*(va[0] - a), w2*va[0], w3*(va[0] + a)
+        else:
+            v1, v2, v3 = w1*va[i], w2*va[i] + roa*dv[i], w3*va[i]
+        nf[i + 1] = 0.5*(fl[i + 1] + fr[i + 1]) - (l1*v1 + l2*v2 + l3*v3)
+    v1 = w1*(ha - a*va[0])
+    v2 = roa*(np.sum(va*dv, axis=0) - va[0]*dv[0]) + w2*qq*0.5
+    v3 = w3*(ha + a*va[0])
+    nf[-1] = 0.5*(fl[-1] + fr[-1]) - (l1*v1 + l2*v2 + l3*v3)
+    return nf
+
+
+def roe(ul, ur, n, gamma):
+    return _rsolve_rotated(roe_1d, ul, ur, n, gamma)
+
+
+def roem(ul, ur, n, gamma):
+    """RoeM flux (Kim, Kim and Rho, JCP 185(2), 2003;
+    pyfr/solvers/euler/kernels/rsolvers/roem.mako:5-96)."""
+    fl, pl, vl = inviscid_flux(ul, gamma)
+    fr, pr, vr = inviscid_flux(ur, gamma)
+    hl, hr = (ul[-1] + pl)/ul[0], (ur[-1] + pr)/ur[0]
+    cl, cr = np.sum(n*vl, axis=0), np.sum(n*vr, axis=0)
+    drho, dp, dh, dc = ur[0] - ul[0], pr - pl, hr - hl, cr - cl
+    dv = vr - vl
+    rrr = np.sqrt(ur[0]/ul[0])
+    ratl = 1.0/(1.0 + rrr)
+    ratr = rrr*ratl
+    ra = rrr*ul[0]
+    ha = hl*ratl + hr*ratr
+    va = vl*ratl + vr*ratr
+    qq = np.sum(va*va, axis=0)
+    ca = np.sum(n*va, axis=0)
+    aa = np.sqrt((gamma - 1)*(ha - 0.5*qq))
+    rcp_aa = 1.0/aa
+    abs_ma = np.abs(ca*rcp_aa) + 1e-15
+    b1 = np.maximum(0.0, np.maximum(ca + aa, cr + aa))
+    b2 = np.minimum(0.0, np.minimum(ca - aa, cl - aa))
+    b1b2 = b1*b2
+    rb = 1.0/(b1 - b2)
+    b1, b2, b1b2 = b1*rb, b2*rb, b1b2*rb
+    sdst = np.where(pl < pr, pl/pr, pr/pl)
+    f = abs_ma**(1.0 - sdst)
+    g = f/(1.0 + abs_ma)
+    du = ur - ul
+    du[-1] = ur[0]*hr - ul[0]*hl
+    bdq = np.empty_like(ul)
+    bdq[0] = drho - f*dp*rcp_aa*rcp_aa
+    bdq[-1] = bdq[0]*ha + ra*dh
+    for i in range(len(n)):
+        bdq[i + 1] = bdq[0]*va[i] + ra*(dv[i] - n[i]*dc)
+    return _nflux(n, b1*fl - b2*fr) + b1b2*(du - g*bdq)
+
+
+def exact_1d(ul, ur, gamma, p_min):
+    """Exact Riemann solution sampled at x/t = 0, three Newton iterations
+    from the adaptive initial guess (Toro 2009, ch. 4 and 9;
+    pyfr/solvers/euler/kernels/rsolvers/exact.mako:14-185)."""
+    nd = ul.shape[0] - 2
+    g = gamma
+    hgm, grgm, trgm, trgp = 0.5*(g - 1), g/(g - 1), 2/(g - 1), 2/(g + 1)
+    gmrtg, gprtg = (g - 1)/(2*g), (g + 1)/(2*g)
+    tgrgm, gmrgp = 2*g/(g - 1), (g - 1)/(g + 1)
+
+    def prim(s):
+        inv = 1/s[0]
+        v = inv*s[1:nd + 1]
+        p = (g - 1)*(s[-1] - 0.5*inv*np.sum(s[1:nd + 1]**2, axis=0))
+        return p, v, np.sqrt(g*p*inv)
+
+    def star(p, ps, rs, cs):
+        with np.errstate(all='ignore'):
+            pr = p/ps
+            prg = pr**(-gprtg)
+            fd1, f1 = prg/(rs*cs), trgm*cs*(prg*pr - 1)
+            pbs = 1/(p + gmrgp*ps)
+            sapb = np.sqrt(trgp*pbs/rs)
+            f2 = (p - ps)*sapb
+            fd2 = sapb - 0.5*f2*pbs
+        return np.where(p <= ps, f1, f2), np.where(p <= ps, fd1, fd2)
+
+    pl, vl, cl = prim(ul)
+    pr, vr, cr = prim(ur)
+    rl, rr = ul[0], ur[0]
+    with np.errstate(all='ignore'):
+        bpv = np.maximum(0, 0.125*(vl[0] - vr[0])*(rl + rr)*(cl + cr) +
+                         0.5*(pl + pr))
+        pmin, pmax = np.minimum(pl, pr), np.maximum(pl, pr)
+        pre = (pl/pr)**gmrtg
+        um = (pre*vl[0]*cr + vr[0]*cl + trgm*(pre - 1)*cl*cr)/(pre*cr + cl)
+        ptl = 1 - hgm*(um - vl[0])/cl
+        ptr = 1 + hgm*(um - vr[0])/cr
+        p_rr = 0.5*(pl*ptl**tgrgm + pr*ptr**tgrgm)
+        gl = np.sqrt(trgp/(rl*(gmrgp*pl + bpv)))
+        gr = np.sqrt(trgp/(rr*(gmrgp*pr + bpv)))
+        p_ss = (gl*pl + gr*pr - vr[0] + vl[0])/(gl + gr)
+    p0 = np.where((pmax <= 2*pmin) & (pmin <= bpv) & (bpv <= pmax), bpv,
+                  np.where(bpv < pmin, p_rr, p_ss))
+
+    for _ in range(3):
+        fsl, fdl = star(p0, pl, rl, cl)
+        fsr, fdr = star(p0, pr, rr, cr)
+        p1 = p0 - (fsl + fsr + vr[0] - vl[0])/(fdl + fdr)
+        p0 = np.where(p1 < 0, p_min, p1)
+    us = 0.5*(vl[0] + vr[0] + fsr - fsl)
+
+    with np.errstate(all='ignore'):
+        # Left of the contact
+        c_l = trgp + gmrgp*vl[0]/cl
+        lfan = (rl*c_l**trgm, trgp*cl + gmrgp*vl[0], pl*c_l**tgrgm)
+        lstar_r = (rl*(p0/pl)**(1/g), us, p0)
+        lraref = np.where(vl[0] >= cl, 0,
+                          np.where(us < cl*(p0/pl)**gmrtg, 1, 2))
+        p0pl = p0/pl
+        sl = vl[0] - cl*np.sqrt(gprtg*p0pl + gmrtg)
+        lstar_s = (rl*(p0pl + gmrgp)/(p0pl*gmrgp + 1), us, p0)
+        # Right of the contact
+        c_r = trgp - gmrgp*vr[0]/cr
+        rfan = (rr*c_r**trgm, gmrgp*vr[0] - trgp*cr, pr*c_r**tgrgm)
+        p0pr = p0/pr
+        sr = vr[0] + cr*np.sqrt(gprtg*p0pr + gmrtg)
+        rstar_s = (rr*(p0pr + gmrgp)/(p0pr*gmrgp + 1), us, p0)
+        rstar_r = (rr*p0pr**(1/g), us, p0)
+        rraref = np.where(vr[0] + cr <= 0, 0,
+                          np.where(us + cr*p0pr**gmrtg >= 0, 1, 2))
+
+    lw = (rl, vl[0], pl)
+    rw = (rr, vr[0], pr)
+    w = []
+    for k in range(3):
+        left = np.where(p0 <= pl,
+                        np.choose(lraref, [lw[k], lstar_r[k], lfan[k]]),
+                        np.where(0 <= sl, lw[k], lstar_s[k]))
+        right = np.where(p0 > pr,
+                         np.where(sr <= 0, rw[k], rstar_s[k]),
+                         np.choose(rraref, [rw[k], rstar_r[k], rfan[k]]))
+        w.append(np.where(0 <= us, left, right))
+    wt = [np.where(0 <= us, vl[i], vr[i]) for i in range(1, nd)]
+
+    nf = np.empty_like(ul)
+    nf[0] = w[0]*w[1]
+    nf[1] = nf[0]*w[1] + w[2]
+    for i, t in enumerate(wt):
+        nf[i + 2] = nf[0]*t
+    ke = w[1]**2 + sum(t**2 for t in wt)
+    nf[-1] = (grgm*w[2] + 0.5*w[0]*ke)*w[1]
+    return nf
+
+
+def exact(ul, ur, n, gamma, p_min=5*np.finfo(float).eps):
+    return _rsolve_rotated(lambda a, b, g: exact_1d(a, b, g, p_min), ul, ur,
+                           n, gamma)
+
+
+RSOLVERS = {'rusanov': rusanov, 'hllc': hllc, 'hll': hll, 'roe': roe,
+            'roem': roem, 'exact': exact}
 
 
 # ---------------------------------------------------------------------------
@@ -1134,6 +1415,22 @@ def rk45_step_t(rhs, u, t, dt):
         else:
             r1 = r1 + dt*RK45_B[i]*r2
     return r1
+
+
+def rkvdh2_stage(stage, nstages, a, b, e, dt, r1, r2, rold=None, rerr=None,
+                 errest=False):
+    """One stage of the two-register scheme with the optional embedded
+    error register (pyfr/integrators/explicit/kernels/rkvdh2.mako:4-31);
+    returns the new (r1, r2, rold, rerr)."""
+    t1, t2 = r1.copy(), r2.copy()
+    if errest and stage == 0:
+        rerr = dt*e[stage]*t2
+        rold = t1.copy()
+    elif errest:
+        rerr = rerr + dt*e[stage]*t2
+    if stage < nstages - 1:
+        return t1 + dt*a[stage]*t2, t1 + dt*b[stage]*t2, rold, rerr
+    return t1 + dt*b[stage]*t2, r2, rold, rerr
 
 
 def rk45_step(rhs, u, dt):

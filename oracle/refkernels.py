@@ -1,0 +1,265 @@
+"""Recipe for ``oracle/_ref``: the reference's own pointwise kernels,
+rendered from its ``.mako`` sources and compiled for the host.  Test
+infrastructure only (it builds the checker, never the product).
+
+The reference renders each kernel module with Mako and a backend-specific
+kernel generator (``pyfr/backends/base/provider.py:74-101``,
+``pyfr/backends/base/makoutil.py``).  Here the same module sources are
+rendered by ``oracle/mako_lite.py`` with the reference's own
+``makoutil`` helpers (macro expansion, ``pyfr.dot``, ``pyfr.array``...), and
+a point generator of this package's own turns each ``<%pyfr:kernel>`` body
+into a C function of one point whose arguments are that point's arrays,
+plus a loop over ``n`` points.  The kernel bodies, and so every arithmetic
+operation and its order, are the reference's text; gcc compiles them with
+``-O2 -fno-fast-math -ffp-contract=off`` so that each operation is one IEEE
+FP64 operation.
+
+Sources are read from the reference checkout (``PYFR_REFERENCE``, default
+``/root/reference``); outputs go to ``oracle/_ref/`` only.  The checkout is
+only present where fixtures are made; ``tests/golden/make_pointwise.py``
+evaluates the compiled kernels and commits their inputs and outputs as
+``tests/golden/pointwise.npz``.
+"""
+
+import ctypes as C
+import hashlib
+import math
+import os
+import re
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(HERE, '_ref')
+
+
+def reference_root():
+    return os.environ.get('PYFR_REFERENCE', '/root/reference')
+
+
+def available():
+    return os.path.isfile(os.path.join(reference_root(), 'pyfr', 'backends',
+                                       'base', 'makoutil.py'))
+
+
+# The backend "base" template of this checker: C99 on the host in FP64
+_BASE = r"""<%namespace module='pyfr.backends.base.makoutil' name='pyfr'/>
+#include <math.h>
+#include <stdint.h>
+
+#define min(a, b) ((a) < (b) ? (a) : (b))
+#define max(a, b) ((a) > (b) ? (a) : (b))
+#define PYFR_FP_PRECISE_BEGIN
+
+typedef double fpdtype_t;
+typedef int32_t ixdtype_t;
+
+${next.body()}
+"""
+
+
+class _Arg:
+    """One kernel argument from its specification string, e.g.
+    ``'inout view fpdtype_t[5]'`` or ``'in broadcast-col view(8) fpdtype_t'``
+    (the grammar of pyfr/backends/base/generator.py:8-32)."""
+
+    def __init__(self, name, spec):
+        self.name = name
+        words = spec.split()
+        self.intent = 'in'
+        if words[0] in ('in', 'out', 'inout'):
+            self.intent = words.pop(0)
+        *attrs, last = words
+        self.attrs = attrs
+        m = re.fullmatch(r'([A-Za-z_]\w*)((?:\[\d+\])*)', last)
+        if not m:
+            raise ValueError(f'Bad argument specification {spec!r}')
+        self.dtype = m[1]
+        self.dims = [int(d) for d in re.findall(r'\d+', m[2])]
+        vs = [int(re.search(r'\((\d+)\)', a)[1]) for a in attrs
+              if a.startswith('view(')]
+        self.viewstride = vs[0] if vs else 1
+        self.isscalar = 'scalar' in attrs
+        self.reduce = next((re.search(r'\((\w+)\)', a)[1] for a in attrs
+                            if a.startswith('reduce(')), None)
+        if self.viewstride > 1 and not self.dims:
+            self.dims = [self.viewstride]
+            self.viewstride = 1
+
+    @property
+    def ctype(self):
+        return 'ixdtype_t' if self.dtype == 'ixdtype_t' else 'fpdtype_t'
+
+    @property
+    def size(self):
+        return math.prod(self.dims) if self.dims else 1
+
+
+class PointKernel:
+    """Kernel generator for makoutil.kernel: C for one point plus a loop.
+
+    ``void <cname>(long n, <vector args...>, <scalar args...>)``: vector
+    arguments (sorted by name) are pointers to ``n`` consecutive per-point
+    arrays of their declared shape; scalars are passed by value."""
+
+    def __init__(self, name, ndim, args, body, fpdtype, ixdtype, *, cname):
+        self.name = name
+        self.cname = cname
+        self.ndim = ndim
+        self.body = body
+        allargs = [_Arg(k, v) for k, v in sorted(args.items())]
+        used = [a for a in allargs
+                if re.search(rf'(?:^|[^\w]){a.name}\b', body)]
+        self.vectargs = [a for a in used if not a.isscalar]
+        self.scalargs = [a for a in used if a.isscalar]
+
+    def argspec(self):
+        return (self.ndim, [a.name for a in self.vectargs + self.scalargs],
+                [a.dims for a in self.vectargs + self.scalargs])
+
+    def render(self):
+        params, pre, post, call = [], [], [], []
+        for a in self.vectargs:
+            if a.dims:
+                decl = f'{a.ctype} {a.name}' + ''.join(f'[{d}]'
+                                                       for d in a.dims)
+                params.append(decl)
+            else:
+                params.append(f'{a.ctype} *_p_{a.name}')
+                pre.append(f'{a.ctype} {a.name} = *_p_{a.name};')
+                if a.intent != 'in':
+                    post.append(f'*_p_{a.name} = {a.name};')
+        for a in self.scalargs:
+            params.append(f'{a.ctype} {a.name}')
+
+        lines = [f'static void {self.cname}_point({", ".join(params)})',
+                 '{', *pre, '{', self.body, '}', *post, '}', '']
+        bparams = ['long _n']
+        for a in self.vectargs:
+            bparams.append(f'{a.ctype} *{a.name}')
+            cast = ''.join(f'[{d}]' for d in a.dims[1:])
+            if len(a.dims) > 1:
+                call.append(f'({a.ctype} (*){cast})({a.name} + _i*{a.size})')
+            else:
+                call.append(f'{a.name} + _i*{a.size}')
+        for a in self.scalargs:
+            bparams.append(f'{a.ctype} {a.name}')
+            call.append(a.name)
+        lines += [f'void {self.cname}({", ".join(bparams)})', '{',
+                  '    for (long _i = 0; _i < _n; _i++)',
+                  f'        {self.cname}_point({", ".join(call)});', '}', '']
+        return '\n'.join(lines)
+
+
+def _makoutil(root):
+    """The reference's ``pyfr/backends/base/makoutil.py``, loaded from its
+    file: importing it as a package member would run
+    ``pyfr/backends/__init__.py``, which needs the backends' dependencies."""
+    import importlib.util
+    name = 'pyfr.backends.base.makoutil'
+    if name not in sys.modules:
+        path = os.path.join(root, 'pyfr', 'backends', 'base', 'makoutil.py')
+        spec = importlib.util.spec_from_file_location(name, path)
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules[name] = mod
+        spec.loader.exec_module(mod)
+    return sys.modules[name]
+
+
+def _lookup():
+    from oracle import mako_lite
+    root = reference_root()
+    if root not in sys.path:
+        sys.path.insert(0, root)
+    mako_lite.install_runtime()
+    makoutil = _makoutil(root)
+    return mako_lite.Lookup(root, 'pyfr.backends.b200check.kernels',
+                            overrides={'base': _BASE},
+                            filters=[makoutil.mfilttag])
+
+
+def render(mod, kname, cname, tplargs, extrns=None):
+    """C source of kernel ``kname`` of module ``mod`` (e.g.
+    'pyfr.solvers.euler.kernels.intcflux'), named ``cname``, together with
+    its argument metadata."""
+    from functools import partial
+    specs = {}
+    args = dict(fpdtype=np.float64, ixdtype=np.int32,
+                fpdtype_max=float(np.finfo(np.float64).max), csubsz=1,
+                soasz=1, math=math)
+    args.update(tplargs)
+    args['_kernel_generator'] = partial(_Recorder, cname=cname, out=specs)
+    args['_macros'] = {}
+    args['_extrns'] = dict(extrns or {})
+    args['_kernel_argspecs'] = {}
+    src = _lookup().render(mod, **args)
+    if kname not in specs:
+        raise ValueError(f'Kernel {kname!r} not defined in {mod}')
+    return re.sub(r'\n\s*\n+', '\n\n', src), specs[kname]
+
+
+class _Recorder(PointKernel):
+    def __init__(self, *a, out, **kw):
+        super().__init__(*a, **kw)
+        out[self.name] = self
+
+
+def _cident(name):
+    """A C identifier for a variant name ('+' -> p, '-' -> m, '.' -> d)."""
+    return re.sub(r'\W', '_', name.translate(str.maketrans('+-.', 'pmd')))
+
+
+class RefLibrary:
+    """A set of rendered kernels compiled into one shared object under
+    ``oracle/_ref`` and called through ctypes."""
+
+    def __init__(self, variants):
+        """``variants``: {cname: (mod, kname, tplargs, extrns)}."""
+        self.kernels = {}
+        srcs = []
+        for cname, (mod, kname, tplargs, extrns) in sorted(variants.items()):
+            src, k = render(mod, kname, _cident(cname), tplargs, extrns)
+            srcs.append(f'/* {cname}: {mod} */\n' +
+                        src.split('typedef int32_t ixdtype_t;', 1)[1])
+            self.kernels[cname] = k
+        head = _BASE.split('${next.body()}')[0].split('\n', 1)[1]
+        full = head + '\n'.join(srcs)
+        os.makedirs(OUT, exist_ok=True)
+        tag = hashlib.sha256(full.encode()).hexdigest()[:12]
+        csrc = os.path.join(OUT, f'refkern_{tag}.c')
+        so = os.path.join(OUT, f'librefkern_{tag}.so')
+        if not os.path.exists(so):
+            with open(csrc, 'w') as f:
+                f.write(full)
+            subprocess.run(['gcc', '-std=gnu11', '-O2', '-fPIC', '-shared',
+                            '-fno-fast-math', '-ffp-contract=off', csrc,
+                            '-o', so + '.tmp', '-lm'], check=True)
+            os.replace(so + '.tmp', so)
+        self.lib = C.CDLL(so)
+        self.path = so
+
+    def __call__(self, cname, n, **arrays):
+        """Evaluate ``cname`` on ``n`` points.  Every vector argument is a
+        float64 array of shape (n, *dims) (in/inout) and is updated in place
+        for out/inout; missing outputs are allocated.  Returns the dict of
+        all vector arrays after the call."""
+        k = self.kernels[cname]
+        fn = getattr(self.lib, _cident(cname))
+        cargs, out = [C.c_long(n)], {}
+        for a in k.vectargs:
+            if a.name in arrays:
+                x = np.ascontiguousarray(arrays[a.name], dtype=np.float64)
+                x = x.reshape(n, *a.dims).copy()
+            elif a.intent == 'in':
+                raise KeyError(f'{cname}: missing input {a.name!r}')
+            else:
+                x = np.zeros((n, *a.dims))
+            out[a.name] = x
+            cargs.append(x.ctypes.data_as(C.c_void_p))
+        for a in k.scalargs:
+            cargs.append(C.c_double(float(arrays[a.name])))
+        fn.restype = None
+        fn(*cargs)
+        return out
