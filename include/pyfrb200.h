@@ -38,12 +38,15 @@ extern "C" {
  * (energy row minus h_ref times the mass row), with the constant fluxes
  * p_ref*I and H_ref*v left out.  Exact in exact arithmetic; the
  * low-precision rounding no longer scales with the mean pressure and
- * enthalpy. */
+ * enthalpy.
+ * p_min: the floor that the exact Riemann solver's Newton iterations put on
+ * the star pressure (pyfr/solvers/euler/inters.py:12-25). */
 typedef struct {
     double gamma, mu, pr, cpTref, cpTs;
     int sutherland;
     int shifted;
     double rho_ref, p_ref;
+    double p_min;   /* floor of the exact Riemann solver's star pressure */
 } b200_gas_t;
 
 /* Boundary conditions: the types of pyfr/solvers/euler/inters.py:83-112
@@ -96,6 +99,10 @@ int b200_stage_time(double *t, const double *dt_dev, double dt, double c, void *
 /* Riemann solver ids: [solver-interfaces] riemann-solver */
 #define B200_RSOLVER_RUSANOV 0
 #define B200_RSOLVER_HLLC 1
+#define B200_RSOLVER_HLL 2
+#define B200_RSOLVER_ROE 3
+#define B200_RSOLVER_ROEM 4
+#define B200_RSOLVER_EXACT 5
 
 /* ---- context, memory, streams, events, graphs ------------------------ */
 /* Replace the driver wrappers of pyfr/backends/cuda/driver.py (context,
@@ -255,10 +262,12 @@ int b200_tflux_ns_f32(int ndims, int nupts, int64_t neles, int linear, const b20
  * state in the flux-point field (view ul, n points; nl: scaled normals,
  * ndims x n with leading dimension ldn); Euler types 1-4;
  * pyfr/solvers/euler/kernels/bccflux.mako:7-26. */
-int b200_bccflux_euler_f64(int ndims, int64_t n, int rsolver, double gamma, const b200_bc_t *bc,
+int b200_bccflux_euler_f64(int ndims, int64_t n, int rsolver, double gamma, double p_min,
+                           const b200_bc_t *bc,
                            double *ul_base, const void *ul_map, int ix64, const double *nl,
                            int64_t ldn, void *stream);
-int b200_bccflux_euler_f32(int ndims, int64_t n, int rsolver, double gamma, const b200_bc_t *bc,
+int b200_bccflux_euler_f32(int ndims, int64_t n, int rsolver, double gamma, double p_min,
+                           const b200_bc_t *bc,
                            float *ul_base, const void *ul_map, int ix64, const float *nl,
                            int64_t ldn, void *stream);
 /* LDG common solution at boundary flux points (view ulin -> view ulout);
@@ -448,13 +457,17 @@ int b200_negdivconf_f32(int nvars, int nupts, int64_t neles, float *r, int64_t l
 
 /* ---- interface kernels over the interior flux-point pairs ------------ */
 /* Euler common normal flux, written +/- to both sides;
- * pyfr/solvers/euler/kernels/intcflux.mako:6-22 with
- * rsolvers/rusanov.mako:4-26 or rsolvers/hllc.mako:4-77.  nl is the
- * (ndims x n) matrix of scaled left normals, leading dimension ldn. */
-int b200_intcflux_euler_f64(int ndims, int64_t n, int rsolver, double gamma, double *ul_base,
-                            const void *ul_map, double *ur_base, const void *ur_map, int ix64,
-                            const double *nl, int64_t ldn, void *stream);
-int b200_intcflux_euler_f32(int ndims, int64_t n, int rsolver, double gamma, float *ul_base,
+ * pyfr/solvers/euler/kernels/intcflux.mako:6-22.  rsolver selects the
+ * Riemann solver of pyfr/solvers/euler/kernels/rsolvers/: 0 rusanov,
+ * 1 hllc, 2 hll, 3 roe, 4 roem, 5 exact (B200_RSOLVER_*); p_min is the
+ * exact solver's star-pressure floor.  nl is the (ndims x n) matrix of
+ * scaled left normals, leading dimension ldn. */
+int b200_intcflux_euler_f64(int ndims, int64_t n, int rsolver, double gamma, double p_min,
+                            double *ul_base, const void *ul_map, double *ur_base,
+                            const void *ur_map, int ix64, const double *nl, int64_t ldn,
+                            void *stream);
+int b200_intcflux_euler_f32(int ndims, int64_t n, int rsolver, double gamma, double p_min,
+                            float *ul_base,
                             const void *ul_map, float *ur_base, const void *ur_map, int ix64,
                             const float *nl, int64_t ldn, void *stream);
 

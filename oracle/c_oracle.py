@@ -48,6 +48,7 @@ class COracle:
         lib.fro_rhs.argtypes = [C.POINTER(Disc), i32, vp, vp, vp]
         lib.fro_scratch_size.argtypes = [C.POINTER(Disc)]
         lib.fro_scratch_size.restype = i64
+        lib.fro_integrals.argtypes = [C.POINTER(Disc), vp, vp, vp, vp]
 
         d = disc
         self.ndims, self.nupts, self.neles = d.ndims, d.nupts, d.neles
@@ -84,6 +85,18 @@ class COracle:
         self._lib.fro_rhs(C.byref(self.disc), int(self.ns), ue.ctypes.data,
                           r.ctypes.data, self._scratch.ctypes.data)
         return r
+
+    def integrals_native(self, ue, qw):
+        """(kinetic energy, enstrophy, volume) integrals of a 3-D
+        Navier-Stokes solution u[e][pt][var] with solution-point weights qw
+        (times |J|)."""
+        out = np.zeros(3)
+        qw = np.ascontiguousarray(qw, dtype=float)
+        if self._lib.fro_integrals(C.byref(self.disc), ue.ctypes.data,
+                                   qw.ctypes.data, self._scratch.ctypes.data,
+                                   out.ctypes.data):
+            raise ValueError('Integrals need a 3-D Navier-Stokes system')
+        return out
 
     def rhs(self, u):
         """RHS on (nupts, nvars, neles) data, as the numpy oracle."""

@@ -188,14 +188,13 @@ static void transform_store(const fro_disc *d, const double *S, double f[MAXD][M
         }
 }
 
-int fro_rhs(const fro_disc *d, int navier_stokes, const double *u, double *r, double *scratch) {
-    const int nd = d->ndims, nv = d->nvars, nupts = d->nupts, nfpts = d->nfpts;
+/* Solution at the flux points and, for Navier-Stokes, the LDG common
+ * solution (intconu) into comm */
+static void flux_point_states(const fro_disc *d, int navier_stokes, const double *u, double *uf,
+                              double *comm) {
+    const int nv = d->nvars, nupts = d->nupts, nfpts = d->nfpts;
     const int64_t ne = d->neles;
-    double *uf = scratch;                                   /* [e][nfpts][nv] */
-    double *comm = uf + ne * nfpts * nv;                    /* [e][nfpts][nv] */
-    double *gf = comm + ne * nfpts * nv;                    /* [e][nd*nfpts][nv] */
 
-    /* Solution at the flux points (and a copy for the common solution) */
     #pragma omp parallel for schedule(static)
     for (int64_t e = 0; e < ne; e++) {
         csr_apply(&d->M0, u + e * nupts * nv, uf + e * nfpts * nv, nv, 0);
@@ -203,7 +202,6 @@ int fro_rhs(const fro_disc *d, int navier_stokes, const double *u, double *r, do
     }
 
     if (navier_stokes) {
-        /* LDG common solution */
         #pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < d->npairs; i++) {
             const double *ul = uf + (d->le[i] * nfpts + d->lpt[i]) * nv;
@@ -216,6 +214,85 @@ int fro_rhs(const fro_disc *d, int navier_stokes, const double *u, double *r, do
                 else cl[v] = cr[v] = ur[v] * (0.5 + d->beta) + ul[v] * (0.5 - d->beta);
             }
         }
+    }
+}
+
+/* Physical corrected gradient of element e at its solution points into
+ * g[d][upt][v] (tgradpcoru + tgradcoru + gradcoru) */
+static void element_gradient(const fro_disc *d, const double *u, const double *comm, int64_t e,
+                             double *g) {
+    const int nd = d->ndims, nv = d->nvars, nupts = d->nupts, nfpts = d->nfpts;
+    csr_apply(&d->M460, u + e * nupts * nv, g, nv, 0);
+    csr_apply(&d->M6, comm + e * nfpts * nv, g, nv, 1);
+    for (int p = 0; p < nupts; p++) {
+        const double *S = d->smats + (e * nupts + p) * nd * nd;
+        const double rj = d->rcpdjac[e * nupts + p];
+        double tg[MAXD][MAXV];
+        for (int k = 0; k < nd; k++)
+            for (int v = 0; v < nv; v++) tg[k][v] = g[((int64_t)k * nupts + p) * nv + v];
+        for (int i = 0; i < nd; i++)
+            for (int v = 0; v < nv; v++) {
+                double acc = 0;
+                for (int k = 0; k < nd; k++) acc += S[k * nd + i] * tg[k][v];
+                g[((int64_t)i * nupts + p) * nv + v] = rj * acc;
+            }
+    }
+}
+
+/* Kinetic energy, enstrophy and volume integrals of a 3-D Navier-Stokes
+ * solution with solution-point quadrature weights qw (per point; times
+ * |J|): out = {sum w rho |v|^2, sum w rho |curl v|^2, sum w}
+ * (pyfr/plugins/integrate.py:58-77 with the expressions of the
+ * Taylor-Green diagnostics). */
+int fro_integrals(const fro_disc *d, const double *u, const double *qw, double *scratch,
+                  double *out) {
+    const int nd = d->ndims, nv = d->nvars, nupts = d->nupts, nfpts = d->nfpts;
+    const int64_t ne = d->neles;
+    if (nd != 3) return 1;
+    double *uf = scratch, *comm = uf + ne * nfpts * nv;
+    flux_point_states(d, 1, u, uf, comm);
+    double ke = 0, en = 0, vol = 0;
+    #pragma omp parallel reduction(+:ke, en, vol)
+    {
+        double *g = malloc(sizeof(double) * nd * nupts * nv);
+        #pragma omp for schedule(static)
+        for (int64_t e = 0; e < ne; e++) {
+            element_gradient(d, u, comm, e, g);
+            for (int p = 0; p < nupts; p++) {
+                const double *up = u + (e * nupts + p) * nv;
+                const double w = qw[p] / d->rcpdjac[e * nupts + p];
+                const double rho = up[0];
+                double vel[3], du[3][3];
+                for (int i = 0; i < 3; i++) vel[i] = up[i + 1] / rho;
+                for (int k = 0; k < 3; k++)
+                    for (int i = 0; i < 3; i++)
+                        du[k][i] = (g[((int64_t)k * nupts + p) * nv + i + 1] -
+                                    vel[i] * g[((int64_t)k * nupts + p) * nv]) / rho;
+                const double w1 = du[1][2] - du[2][1], w2 = du[2][0] - du[0][2],
+                             w3 = du[0][1] - du[1][0];
+                ke += w * rho * (vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]);
+                en += w * rho * (w1 * w1 + w2 * w2 + w3 * w3);
+                vol += w;
+            }
+        }
+        free(g);
+    }
+    out[0] = ke;
+    out[1] = en;
+    out[2] = vol;
+    return 0;
+}
+
+int fro_rhs(const fro_disc *d, int navier_stokes, const double *u, double *r, double *scratch) {
+    const int nd = d->ndims, nv = d->nvars, nupts = d->nupts, nfpts = d->nfpts;
+    const int64_t ne = d->neles;
+    double *uf = scratch;                                   /* [e][nfpts][nv] */
+    double *comm = uf + ne * nfpts * nv;                    /* [e][nfpts][nv] */
+    double *gf = comm + ne * nfpts * nv;                    /* [e][nd*nfpts][nv] */
+
+    flux_point_states(d, navier_stokes, u, uf, comm);
+
+    if (navier_stokes) {
 
         /* Corrected gradient, flux, gradients at the flux points, divergence */
         #pragma omp parallel

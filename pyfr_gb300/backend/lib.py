@@ -37,7 +37,7 @@ class MulArgs(C.Structure):
 class Gas(C.Structure):
     _fields_ = [('gamma', f64), ('mu', f64), ('pr', f64), ('cpTref', f64),
                 ('cpTs', f64), ('sutherland', i32), ('shifted', i32),
-                ('rho_ref', f64), ('p_ref', f64)]
+                ('rho_ref', f64), ('p_ref', f64), ('p_min', f64)]
 
 
 # Boundary-condition types and constants (b200_bc_t)
@@ -85,8 +85,8 @@ def _sig_pointwise(fp):
         'gradcoru': [i32, i32, i64, i32, vp, i64, vp, i64, vp, i64, vp, i64,
                      vp, i64, vp],
         'negdivconf': [i32, i32, i64, vp, i64, vp, i64, vp],
-        'intcflux_euler': [i32, i64, i32, f64, vp, vp, vp, vp, i32, vp, i64,
-                           vp],
+        'intcflux_euler': [i32, i64, i32, f64, f64, vp, vp, vp, vp, i32, vp,
+                           i64, vp],
         'intcflux_ns': [i32, i64, i32, C.POINTER(Gas), f64, f64, vp, vp, vp,
                         vp, vp, vp, vp, vp, vp, vp, i32, vp, i64, vp],
         'intconu': [i32, i64, f64, vp, vp, vp, vp, vp, vp, vp, vp, i32, vp],
@@ -100,8 +100,8 @@ def _sig_pointwise(fp):
         'mul': [vp, vp, i64, vp, i64, i64, fp, fp, vp],
         'wavespeed': [i32, i32, i64, i32, C.POINTER(Gas), vp, i64, vp, i64,
                       vp, i64, vp, i64, vp, i64, vp, vp],
-        'bccflux_euler': [i32, i64, i32, f64, C.POINTER(BC), vp, vp, i32, vp,
-                          i64, vp],
+        'bccflux_euler': [i32, i64, i32, f64, f64, C.POINTER(BC), vp, vp, i32,
+                          vp, i64, vp],
         'bcconu': [i32, i64, f64, C.POINTER(BC), vp, vp, vp, vp, i32, vp, i64,
                    vp],
         'bccflux_ns': [i32, i64, i32, C.POINTER(Gas), f64, C.POINTER(BC), vp,

@@ -19,13 +19,28 @@ from pyfr_gb300.shapes import ETYPE_OF, adjugate_det, linear_shape_jac
 from pyfr_gb300.backend.lib import Gas
 from pyfr_gb300.backend.types import BindableKernel, Kernel, NullKernel
 
-RSOLVERS = {'rusanov': 0, 'hllc': 1}
+# The Riemann solvers of pyfr/solvers/euler/kernels/rsolvers/ by the index
+# the C ABI takes
+RSOLVERS = {'rusanov': 0, 'hllc': 1, 'hll': 2, 'roe': 3, 'roem': 4,
+            'exact': 5}
+
+# Star-pressure floor of the exact solver when the caller gives none
+# (pyfr/solvers/euler/inters.py:21-22: five FP64 machine epsilons)
+P_MIN_DEFAULT = 5*float(np.finfo(np.float64).eps)
 
 
-def _gas(c, visc_corr='none', ref_state=None):
+def _rsolver(tplargs):
+    try:
+        return RSOLVERS[tplargs['rsolver']]
+    except KeyError:
+        raise ValueError(f'Unknown Riemann solver '
+                         f'{tplargs.get("rsolver")!r}') from None
+
+
+def _gas(c, visc_corr='none', ref_state=None, p_min=P_MIN_DEFAULT):
     g = Gas(gamma=c['gamma'], mu=c.get('mu', 0.0), pr=c.get('Pr', 1.0),
             cpTref=c.get('cpTref', 1.0), cpTs=c.get('cpTs', 1.0),
-            sutherland=int(visc_corr == 'sutherland'))
+            sutherland=int(visc_corr == 'sutherland'), p_min=p_min)
     if ref_state is not None:
         g.shifted = 1
         g.rho_ref, g.p_ref = ref_state
@@ -278,16 +293,18 @@ class PointwiseKernelProvider:
 
     def _intcflux_euler(self, tplargs, dims, extrns, ul, ur, nl):
         (n,) = dims
-        rs = RSOLVERS[tplargs['rsolver']]
+        rs = _rsolver(tplargs)
         fn, nd, gamma = (self._fn('intcflux_euler'), tplargs['ndims'],
                          tplargs['c']['gamma'])
+        p_min = tplargs.get('p_min', P_MIN_DEFAULT)
         lb, lm, _ = _view(ul)
         rb, rm, _ = _view(ur)
         np_, nlp = _mat(nl)
         ix64 = self._ix64
 
         def run(stream):
-            fn(nd, n, rs, gamma, lb, lm, rb, rm, ix64, np_, nlp, stream)
+            fn(nd, n, rs, gamma, p_min, lb, lm, rb, rm, ix64, np_, nlp,
+               stream)
 
         return Kernel(run, mats=[nl], views=[ul, ur], name='intcflux',
                       meta=dict(kind='intcflux_euler', tplargs=tplargs,
@@ -301,11 +318,12 @@ class PointwiseKernelProvider:
 
         (n,) = dims
         c = tplargs['c']
-        rs = RSOLVERS[tplargs['rsolver']]
+        rs = _rsolver(tplargs)
         if self.backend.ref_state is not None and tplargs['rsolver'] != 'rusanov':
             raise NotImplementedError('The reference-state shift needs the '
                                       'Rusanov Riemann solver')
-        gas = _gas(c, tplargs.get('visc_corr', 'none'), self.backend.ref_state)
+        gas = _gas(c, tplargs.get('visc_corr', 'none'), self.backend.ref_state,
+                   tplargs.get('p_min', P_MIN_DEFAULT))
         beta, tau = c['ldg-beta'], c['ldg-tau']
         fn, nd = self._fn('intcflux_ns'), tplargs['ndims']
         lb, lm, _ = _view(ul)
@@ -345,16 +363,18 @@ class PointwiseKernelProvider:
 
     def _bccflux_euler(self, tplargs, dims, extrns, ul, nl, **kw):
         (n,) = dims
-        rs = RSOLVERS[tplargs['rsolver']]
+        rs = _rsolver(tplargs)
         fn, nd, gamma = (self._fn('bccflux_euler'), tplargs['ndims'],
                          tplargs['c']['gamma'])
+        p_min = tplargs.get('p_min', P_MIN_DEFAULT)
         bc = self._bc(tplargs)
         lb, lm, _ = _view(ul)
         np_, nlp = _mat(nl)
         ix64 = self._ix64
 
         def run(stream):
-            fn(nd, n, rs, gamma, C.byref(bc), lb, lm, ix64, np_, nlp, stream)
+            fn(nd, n, rs, gamma, p_min, C.byref(bc), lb, lm, ix64, np_, nlp,
+               stream)
 
         return Kernel(run, mats=[nl], views=[ul], misc=[bc], name='bccflux',
                       meta=dict(kind='bccflux_euler', tplargs=tplargs,
@@ -386,8 +406,9 @@ class PointwiseKernelProvider:
             raise NotImplementedError('Boundaries take unshifted states')
         (n,) = dims
         c = tplargs['c']
-        rs = RSOLVERS[tplargs['rsolver']]
-        gas = _gas(c, tplargs.get('visc_corr', 'none'))
+        rs = _rsolver(tplargs)
+        gas = _gas(c, tplargs.get('visc_corr', 'none'),
+                   p_min=tplargs.get('p_min', P_MIN_DEFAULT))
         fn, nd = self._fn('bccflux_ns'), tplargs['ndims']
         bc = self._bc(tplargs)
         lb, lm, _ = _view(ul)

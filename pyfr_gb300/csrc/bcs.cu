@@ -384,9 +384,9 @@ __device__ __forceinline__ T unit_normal(const T *__restrict__ nl, int64_t ldn, 
     return mag;
 }
 
-template <int ND, typename T>
+template <int RS, int ND, typename T>
 __global__ void __launch_bounds__(BC_BLOCK)
-bccflux_euler_kernel(int64_t n, int rs, T gamma, BcK<T> bc0, ScalView<T> vl, int ix64,
+bccflux_euler_kernel(int64_t n, T gamma, T p_min, BcK<T> bc0, ScalView<T> vl, int ix64,
                      const T *__restrict__ nl, int64_t ldn) {
     constexpr int NV = ND + 2;
     const int64_t i = (int64_t)blockIdx.x * BC_BLOCK + threadIdx.x;
@@ -399,7 +399,7 @@ bccflux_euler_kernel(int64_t n, int rs, T gamma, BcK<T> bc0, ScalView<T> vl, int
     for (int v = 0; v < NV; v++) ul[v] = pl[v * B200_SOASZ];
     const T mag = unit_normal<ND, T>(nl, ldn, i, nn);
     bc_rsolve_state<ND, T>(bc, gamma, ul, nn, ur);
-    b200::rsolve<ND, T>(rs, ul, ur, nn, fn, gamma);
+    b200::rsolve_t<RS, ND, T>(ul, ur, nn, fn, gamma, p_min);
 #pragma unroll
     for (int v = 0; v < NV; v++) pl[v * B200_SOASZ] = mag * fn[v];
 }
@@ -424,9 +424,9 @@ bcconu_kernel(int64_t n, T gamma, BcK<T> bc0, ScalView<T> vin, ScalView<T> vout,
     for (int v = 0; v < NV; v++) po[v * B200_SOASZ] = ur[v];
 }
 
-template <int ND, typename T>
+template <int RS, int ND, typename T>
 __global__ void __launch_bounds__(BC_BLOCK)
-bccflux_ns_kernel(int64_t n, int rs, b200::GasK<T> gas, T tau, BcK<T> bc0, ScalView<T> vl,
+bccflux_ns_kernel(int64_t n, b200::GasK<T> gas, T tau, BcK<T> bc0, ScalView<T> vl,
                   VectView<T> gl, int ix64, const T *__restrict__ nl, int64_t ldn,
                   ScalView<T> va) {
     constexpr int NV = ND + 2;
@@ -473,7 +473,7 @@ bccflux_ns_kernel(int64_t n, int rs, b200::GasK<T> gas, T tau, BcK<T> bc0, ScalV
 
     // Inviscid part: Riemann solve against the ghost state
     bc_rsolve_state<ND, T>(bc, gas.gamma, ul, nn, ur);
-    b200::rsolve<ND, T>(rs, ul, ur, nn, fi, gas.gamma);
+    b200::rsolve_t<RS, ND, T>(ul, ur, nn, fi, gas.gamma, gas.p_min);
 
 #pragma unroll
     for (int v = 0; v < NV; v++) {
@@ -524,8 +524,9 @@ bccent_kernel(int64_t n, T gamma, BcK<T> bc0, ScalView<T> vl, ScalView<T> ve, in
 bool bc_type_ok(int t) { return t >= B200_BC_SUP_IN_FA && t <= B200_BC_SUB_OUT_FP; }
 
 template <typename T>
-int bccflux_euler(int ndims, int64_t n, int rs, double gamma, const b200_bc_t *bc, T *ul_base,
-                  const void *ul_map, int ix64, const T *nl, int64_t ldn, cudaStream_t st) {
+int bccflux_euler(int ndims, int64_t n, int rs, double gamma, double p_min, const b200_bc_t *bc,
+                  T *ul_base, const void *ul_map, int ix64, const T *nl, int64_t ldn,
+                  cudaStream_t st) {
     if (n <= 0) return B200_OK;
     if (!bc || !bc_type_ok(bc->type) || bc->type > B200_BC_CHAR_RIEM_INV)
         return b200::set_error(B200_ERR_ARG, "bccflux_euler: bad boundary type");
@@ -534,12 +535,16 @@ int bccflux_euler(int ndims, int64_t n, int rs, double gamma, const b200_bc_t *b
         return b200::set_error(B200_ERR_ARG, "boundary expressions need ploc and t");
     ScalView<T> l{ul_base, ul_map};
     const unsigned grid = b200::ceil_div(n, BC_BLOCK);
-    if (ndims == 2)
-        bccflux_euler_kernel<2, T><<<grid, BC_BLOCK, 0, st>>>(n, rs, (T)gamma, k, l, ix64, nl, ldn);
-    else if (ndims == 3)
-        bccflux_euler_kernel<3, T><<<grid, BC_BLOCK, 0, st>>>(n, rs, (T)gamma, k, l, ix64, nl, ldn);
-    else
+    if (ndims != 2 && ndims != 3)
         return b200::set_error(B200_ERR_ARG, "bccflux_euler: ndims must be 2 or 3");
+    const bool ok = b200::with_rsolver(rs, [&](auto rsc) {
+        constexpr int RS = decltype(rsc)::value;
+        if (ndims == 2)
+            bccflux_euler_kernel<RS, 2, T><<<grid, BC_BLOCK, 0, st>>>(n, (T)gamma, (T)p_min, k, l, ix64, nl, ldn);
+        else
+            bccflux_euler_kernel<RS, 3, T><<<grid, BC_BLOCK, 0, st>>>(n, (T)gamma, (T)p_min, k, l, ix64, nl, ldn);
+    });
+    if (!ok) return b200::set_error(B200_ERR_ARG, "bccflux_euler: unknown Riemann solver %d", rs);
     B200_CHECK_LAUNCH("bccflux_euler");
     return B200_OK;
 }
@@ -586,12 +591,16 @@ int bccflux_ns(int ndims, int64_t n, int rs, const b200_gas_t *gas, double tau,
     ScalView<T> l{ul_base, ul_map};
     VectView<T> gv{gl_base, gl_map, gl_rstr};
     const unsigned grid = b200::ceil_div(n, BC_BLOCK);
-    if (ndims == 2)
-        bccflux_ns_kernel<2, T><<<grid, BC_BLOCK, 0, st>>>(n, rs, g, (T)tau, k, l, gv, ix64, nl, ldn, va);
-    else if (ndims == 3)
-        bccflux_ns_kernel<3, T><<<grid, BC_BLOCK, 0, st>>>(n, rs, g, (T)tau, k, l, gv, ix64, nl, ldn, va);
-    else
+    if (ndims != 2 && ndims != 3)
         return b200::set_error(B200_ERR_ARG, "bccflux_ns: ndims must be 2 or 3");
+    const bool ok = b200::with_rsolver(rs, [&](auto rsc) {
+        constexpr int RS = decltype(rsc)::value;
+        if (ndims == 2)
+            bccflux_ns_kernel<RS, 2, T><<<grid, BC_BLOCK, 0, st>>>(n, g, (T)tau, k, l, gv, ix64, nl, ldn, va);
+        else
+            bccflux_ns_kernel<RS, 3, T><<<grid, BC_BLOCK, 0, st>>>(n, g, (T)tau, k, l, gv, ix64, nl, ldn, va);
+    });
+    if (!ok) return b200::set_error(B200_ERR_ARG, "bccflux_ns: unknown Riemann solver %d", rs);
     B200_CHECK_LAUNCH("bccflux_ns");
     return B200_OK;
 }
@@ -649,17 +658,19 @@ int b200_bccent_f32(int ndims, int64_t n, double gamma, const b200_bc_t *bc,
                          (cudaStream_t)stream);
 }
 
-int b200_bccflux_euler_f64(int ndims, int64_t n, int rsolver, double gamma, const b200_bc_t *bc,
+int b200_bccflux_euler_f64(int ndims, int64_t n, int rsolver, double gamma, double p_min,
+                           const b200_bc_t *bc,
                            double *ul_base, const void *ul_map, int ix64, const double *nl,
                            int64_t ldn, void *stream) {
-    return bccflux_euler<double>(ndims, n, rsolver, gamma, bc, ul_base, ul_map, ix64, nl, ldn,
+    return bccflux_euler<double>(ndims, n, rsolver, gamma, p_min, bc, ul_base, ul_map, ix64, nl, ldn,
                                  (cudaStream_t)stream);
 }
 
-int b200_bccflux_euler_f32(int ndims, int64_t n, int rsolver, double gamma, const b200_bc_t *bc,
+int b200_bccflux_euler_f32(int ndims, int64_t n, int rsolver, double gamma, double p_min,
+                           const b200_bc_t *bc,
                            float *ul_base, const void *ul_map, int ix64, const float *nl,
                            int64_t ldn, void *stream) {
-    return bccflux_euler<float>(ndims, n, rsolver, gamma, bc, ul_base, ul_map, ix64, nl, ldn,
+    return bccflux_euler<float>(ndims, n, rsolver, gamma, p_min, bc, ul_base, ul_map, ix64, nl, ldn,
                                 (cudaStream_t)stream);
 }
 

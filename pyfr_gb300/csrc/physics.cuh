@@ -5,10 +5,17 @@
 //   viscous_flux_add   pyfr/solvers/navstokes/kernels/flux.mako:3-105
 //   rsolve (Rusanov)   pyfr/solvers/euler/kernels/rsolvers/rusanov.mako:4-26
 //   rsolve (HLLC)      pyfr/solvers/euler/kernels/rsolvers/hllc.mako:4-77
+//   rsolve (HLL)       pyfr/solvers/euler/kernels/rsolvers/hll.mako:4-53
+//   rsolve (Roe)       pyfr/solvers/euler/kernels/rsolvers/roe.mako:6-84
+//   rsolve (RoeM)      pyfr/solvers/euler/kernels/rsolvers/roem.mako:5-96
+//   rsolve (exact)     pyfr/solvers/euler/kernels/rsolvers/exact.mako:14-185
+//   normal frame       pyfr/solvers/baseadvec/kernels/transform.mako:5-75
 //   calc_smats_detj    pyfr/solvers/baseadvec/kernels/smats.mako:3-25
 //   transform_grad     pyfr/solvers/baseadvecdiff/kernels/transform_grad.mako:3-10
 // NV = ND + 2 conserved variables: rho, rho*u_i, E.
 #pragma once
+
+#include <type_traits>
 
 #include "common.cuh"
 
@@ -32,6 +39,7 @@ struct Gas {
     int sutherland;
     int shifted;
     double rho_ref, p_ref;
+    double p_min;
 };
 
 // The same constants in the kernel's arithmetic type, with every derived
@@ -40,7 +48,7 @@ struct Gas {
 template <typename T>
 struct GasK {
     T gamma, gm1, mu, gamma_pr, rcp_cpTref, mu_ctt, cpTs, quarter_gamma;
-    T rho_ref, p_ref, e_ref, h_ref, hs_ref;
+    T rho_ref, p_ref, e_ref, h_ref, hs_ref, p_min;
     int sutherland, shifted;
 };
 
@@ -60,12 +68,14 @@ inline GasK<T> gas_consts(const Gas &g) {
     k.e_ref = (T)(g.p_ref / (g.gamma - 1.0));
     k.h_ref = (T)(g.gamma / (g.gamma - 1.0) * g.p_ref);
     k.hs_ref = (T)(g.rho_ref != 0.0 ? g.gamma / (g.gamma - 1.0) * g.p_ref / g.rho_ref : 0.0);
+    k.p_min = (T)g.p_min;
     k.sutherland = g.sutherland;
     k.shifted = g.shifted;
     return k;
 }
 
-enum RSolver { RS_RUSANOV = 0, RS_HLLC = 1 };
+// Riemann solvers by the index the C ABI takes (rsolver argument)
+enum RSolver { RS_RUSANOV = 0, RS_HLLC = 1, RS_HLL = 2, RS_ROE = 3, RS_ROEM = 4, RS_EXACT = 5 };
 
 template <int ND, typename T>
 __device__ __forceinline__ void inviscid_flux(const T *s, T f[ND][ND + 2], T &p, T v[ND],
@@ -322,13 +332,465 @@ __device__ __forceinline__ void rsolve_hllc(const T *ul, const T *ur, const T *n
     }
 }
 
+// HLL (pyfr/solvers/euler/kernels/rsolvers/hll.mako:4-53): Roe-averaged
+// wave-speed estimates; the reference takes the right state's sound speed
+// in both the left and the right estimate, and so does this.
 template <int ND, typename T>
-__device__ __forceinline__ void rsolve(int rs, const T *ul, const T *ur, const T *n, T *nf,
-                                       T gamma) {
-    if (rs == RS_HLLC)
+__device__ __forceinline__ void rsolve_hll(const T *ul, const T *ur, const T *n, T *nf,
+                                           T gamma) {
+    constexpr int NV = ND + 2;
+    T fl[ND][NV], fr[ND][NV], vl[ND], vr[ND], pl, pr;
+    inviscid_flux<ND, T>(ul, fl, pl, vl, gamma);
+    inviscid_flux<ND, T>(ur, fr, pr, vr, gamma);
+
+    T nvl = 0, nvr = 0;
+#pragma unroll
+    for (int i = 0; i < ND; i++) {
+        nvl += n[i] * vl[i];
+        nvr += n[i] * vr[i];
+    }
+    const T ar = sqrt(gamma * pr / ur[0]);
+    const T sql = sqrt(ul[0]), sqr = sqrt(ur[0]);
+    const T nv = (sql * nvl + sqr * nvr) / (sql + sqr);
+    const T H = (sql * (pr + ur[NV - 1]) + sqr * (pl + ul[NV - 1])) / (sql * ur[0] + sqr * ul[0]);
+    const T inv_rar = T(1) / (sql + sqr);
+    T qq = 0;
+#pragma unroll
+    for (int i = 0; i < ND; i++) {
+        const T va = (vl[i] * sql + vr[i] * sqr) * inv_rar;
+        qq += va * va;
+    }
+    const T a = sqrt((gamma - T(1)) * (H - T(0.5) * qq));
+    const T sl = fmin(nv - a, nvl - ar);
+    const T sr = fmax(nv + a, nvr + ar);
+    const T rcpsrsl = T(1) / (sr - sl);
+
+#pragma unroll
+    for (int i = 0; i < NV; i++) {
+        T nf_fl = 0, nf_fr = 0;
+#pragma unroll
+        for (int j = 0; j < ND; j++) {
+            nf_fl += n[j] * fl[j][i];
+            nf_fr += n[j] * fr[j][i];
+        }
+        const T sub = (sr * nf_fl - sl * nf_fr + sl * sr * (ur[i] - ul[i])) * rcpsrsl;
+        nf[i] = (T(0) <= sl) ? nf_fl : (T(0) >= sr) ? nf_fr : sub;
+    }
+}
+
+// Momentum components u[1..ND] expressed in the frame whose first axis is
+// the unit normal n (Moler and Hughes 1999), and back:
+// pyfr/solvers/baseadvec/kernels/transform.mako:5-75.  Density and energy
+// are frame-independent.
+template <int ND, typename T>
+__device__ __forceinline__ void rot_to(const T *n, const T *u, T *t) {
+    const T *m = u + 1;
+    T *r = t + 1;
+    if (ND == 2) {
+        r[0] = n[0] * m[0] + n[1] * m[1];
+        r[1] = n[0] * m[1] - n[1] * m[0];
+    } else if (fabs(n[0]) < T(0.99)) {
+        const T h = T(1) / (T(1) + n[0]);
+        r[0] = n[0] * m[0] + n[1] * m[1] + n[2] * m[2];
+        r[1] = (n[0] + h * n[2] * n[2]) * m[1] - n[1] * m[0] - h * n[1] * n[2] * m[2];
+        r[2] = (n[0] + h * n[1] * n[1]) * m[2] - n[2] * m[0] - h * n[1] * n[2] * m[1];
+    } else if (fabs(n[1]) < fabs(n[2])) {
+        const T h = T(1) / (T(1) - n[1]);
+        r[0] = n[0] * m[0] + n[1] * m[1] + n[2] * m[2];
+        r[1] = (T(1) - h * n[0] * n[0]) * m[0] + n[0] * m[1] - h * n[0] * n[2] * m[2];
+        r[2] = n[2] * m[1] - h * n[0] * n[2] * m[0] + (T(1) - h * n[2] * n[2]) * m[2];
+    } else {
+        const T h = T(1) / (T(1) - n[2]);
+        r[0] = n[0] * m[0] + n[1] * m[1] + n[2] * m[2];
+        r[1] = (T(1) - h * n[1] * n[1]) * m[1] - h * n[0] * n[1] * m[0] + n[1] * m[2];
+        r[2] = (T(1) - h * n[0] * n[0]) * m[0] - h * n[0] * n[1] * m[1] + n[0] * m[2];
+    }
+}
+
+template <int ND, typename T>
+__device__ __forceinline__ void rot_from(const T *n, const T *t, T *u) {
+    const T *m = t + 1;
+    T *r = u + 1;
+    if (ND == 2) {
+        r[0] = n[0] * m[0] - n[1] * m[1];
+        r[1] = n[1] * m[0] + n[0] * m[1];
+    } else if (fabs(n[0]) < T(0.99)) {
+        const T h = T(1) / (T(1) + n[0]);
+        r[0] = n[0] * m[0] - n[1] * m[1] - n[2] * m[2];
+        r[1] = n[1] * m[0] + (n[0] + h * n[2] * n[2]) * m[1] - h * n[1] * n[2] * m[2];
+        r[2] = n[2] * m[0] - h * n[1] * n[2] * m[1] + (n[0] + h * n[1] * n[1]) * m[2];
+    } else if (fabs(n[1]) < fabs(n[2])) {
+        const T h = T(1) / (T(1) - n[1]);
+        r[0] = n[0] * m[0] + (T(1) - h * n[0] * n[0]) * m[1] - h * n[0] * n[2] * m[2];
+        r[1] = n[1] * m[0] + n[0] * m[1] + n[2] * m[2];
+        r[2] = n[2] * m[0] - h * n[0] * n[2] * m[1] + (T(1) - h * n[2] * n[2]) * m[2];
+    } else {
+        const T h = T(1) / (T(1) - n[2]);
+        r[0] = n[0] * m[0] - h * n[0] * n[1] * m[1] + (T(1) - h * n[0] * n[0]) * m[2];
+        r[1] = n[1] * m[0] + (T(1) - h * n[1] * n[1]) * m[1] - h * n[0] * n[1] * m[2];
+        r[2] = n[2] * m[0] + n[1] * m[1] + n[0] * m[2];
+    }
+}
+
+// x-direction flux, pressure and velocity of a state in the normal frame
+// (pyfr/solvers/euler/kernels/flux.mako:28-48)
+template <int ND, typename T>
+__device__ __forceinline__ void inviscid_flux_1d(const T *s, T *f, T &p, T *v, T gamma) {
+    constexpr int NV = ND + 2;
+    const T invrho = T(1) / s[0], E = s[NV - 1];
+    T k2 = 0;
+#pragma unroll
+    for (int i = 0; i < ND; i++) {
+        v[i] = invrho * s[i + 1];
+        k2 += s[i + 1] * s[i + 1];
+    }
+    p = (gamma - T(1)) * (E - T(0.5) * invrho * k2);
+    f[0] = s[1];
+    f[NV - 1] = (E + p) * v[0];
+    f[1] = s[1] * v[0] + p;
+#pragma unroll
+    for (int j = 1; j < ND; j++) f[j + 1] = s[1] * v[j];
+}
+
+// Roe flux with a parabolic entropy fix of width 1e-3 on the acoustic
+// eigenvalues, in the normal frame
+// (pyfr/solvers/euler/kernels/rsolvers/roe.mako:6-84)
+template <int ND, typename T>
+__device__ __forceinline__ void roe_1d(const T *ul, const T *ur, T *nf, T gamma) {
+    constexpr int NV = ND + 2;
+    constexpr double eps = 0.001;
+    T fl[NV], fr[NV], vl[ND], vr[ND], pl, pr, va[ND], dv[ND];
+    inviscid_flux_1d<ND, T>(ul, fl, pl, vl, gamma);
+    inviscid_flux_1d<ND, T>(ur, fr, pr, vr, gamma);
+
+    const T sql = sqrt(ul[0]), sqr = sqrt(ur[0]);
+    const T roa = sql * sqr;
+    const T ha = (sql * (pr + ur[NV - 1]) + sqr * (pl + ul[NV - 1])) / (sql * ur[0] + sqr * ul[0]);
+    const T inv_rar = T(1) / (sql + sqr);
+    T qq = 0, vdv = 0;
+#pragma unroll
+    for (int i = 0; i < ND; i++) {
+        va[i] = (vl[i] * sql + vr[i] * sqr) * inv_rar;
+        qq += va[i] * va[i];
+    }
+    const T a = sqrt((gamma - T(1)) * (ha - T(0.5) * qq));
+
+    T l1 = fabs(va[0] - a);
+    const T l2 = fabs(va[0]);
+    T l3 = fabs(va[0] + a);
+    l1 = (l1 < T(eps)) ? T(0.5 / eps) * (l1 * l1 + T(eps * eps)) : l1;
+    l3 = (l3 < T(eps)) ? T(0.5 / eps) * (l3 * l3 + T(eps * eps)) : l3;
+
+#pragma unroll
+    for (int i = 0; i < ND; i++) {
+        dv[i] = vr[i] - vl[i];
+        vdv += va[i] * dv[i];
+    }
+    const T dro = ur[0] - ul[0];
+    const T dp = pr - pl;
+    const T inv_a2 = T(1) / (T(2) * a * a);
+
+    // Wave strengths of the acoustic and entropy waves
+    const T w1 = (dp - roa * a * dv[0]) * inv_a2;
+    const T w2 = dro - dp * T(2) * inv_a2;
+    const T w3 = (dp + roa * a * dv[0]) * inv_a2;
+
+    nf[0] = T(0.5) * (fl[0] + fr[0]) - (l1 * w1 + l2 * w2 + l3 * w3);
+#pragma unroll
+    for (int i = 0; i < ND; i++) {
+        T v1, v2, v3;
+        if (i == 0) {
+            v1 = w1 * (va[0] - a);
+            v2 = w2 * va[0];
+            v3 = w3 * (va[0] + a);
+        } else {
+            v1 = w1 * va[i];
+            v2 = w2 * va[i] + roa * dv[i];
+            v3 = w3 * va[i];
+        }
+        nf[i + 1] = T(0.5) * (fl[i + 1] + fr[i + 1]) - (l1 * v1 + l2 * v2 + l3 * v3);
+    }
+    const T v1 = w1 * (ha - a * va[0]);
+    const T v2 = roa * (vdv - va[0] * dv[0]) + w2 * qq * T(0.5);
+    const T v3 = w3 * (ha + a * va[0]);
+    nf[NV - 1] = T(0.5) * (fl[NV - 1] + fr[NV - 1]) - (l1 * v1 + l2 * v2 + l3 * v3);
+}
+
+// RoeM (Kim, Kim and Rho, J. Comput. Phys. 185(2), 2003;
+// pyfr/solvers/euler/kernels/rsolvers/roem.mako:5-96)
+template <int ND, typename T>
+__device__ __forceinline__ void rsolve_roem(const T *ul, const T *ur, const T *n, T *nf,
+                                            T gamma) {
+    constexpr int NV = ND + 2;
+    T fl[ND][NV], fr[ND][NV], vl[ND], vr[ND], va[ND], dv[ND], du[NV], bdq[NV], pl, pr;
+    inviscid_flux<ND, T>(ul, fl, pl, vl, gamma);
+    inviscid_flux<ND, T>(ur, fr, pr, vr, gamma);
+
+    const T hl = (ul[NV - 1] + pl) / ul[0];
+    const T hr = (ur[NV - 1] + pr) / ur[0];
+    T contral = 0, contrar = 0;
+#pragma unroll
+    for (int i = 0; i < ND; i++) {
+        contral += n[i] * vl[i];
+        contrar += n[i] * vr[i];
+    }
+    const T drho = ur[0] - ul[0];
+    const T dp = pr - pl;
+    const T dh = hr - hl;
+    const T dcontra = contrar - contral;
+
+    // Roe averages
+    const T rrr = sqrt(ur[0] / ul[0]);
+    const T ratl = T(1) / (T(1) + rrr);
+    const T ratr = rrr * ratl;
+    const T ra = rrr * ul[0];
+    const T ha = hl * ratl + hr * ratr;
+    T qq = 0, contraa = 0;
+#pragma unroll
+    for (int i = 0; i < ND; i++) {
+        dv[i] = vr[i] - vl[i];
+        va[i] = vl[i] * ratl + vr[i] * ratr;
+        qq += va[i] * va[i];
+        contraa += n[i] * va[i];
+    }
+    const T aa = sqrt((gamma - T(1)) * (ha - T(0.5) * qq));
+    const T rcp_aa = T(1) / aa;
+    const T abs_ma = fabs(contraa * rcp_aa) + T(1e-15);
+
+    // Normalised wave speeds
+    T b1 = fmax(T(0), fmax(contraa + aa, contrar + aa));
+    T b2 = fmin(T(0), fmin(contraa - aa, contral - aa));
+    T b1b2 = b1 * b2;
+    const T rcp_b1_b2 = T(1) / (b1 - b2);
+    b1 = b1 * rcp_b1_b2;
+    b2 = b2 * rcp_b1_b2;
+    b1b2 = b1b2 * rcp_b1_b2;
+
+    // Shock sensing and the Mach-number functions f and g
+    const T sdst = (pl < pr) ? pl / pr : pr / pl;
+    const T h = T(1) - sdst;
+    const T f = pow(abs_ma, h);
+    const T g = f / (T(1) + abs_ma);
+
+#pragma unroll
+    for (int i = 0; i < NV - 1; i++) du[i] = ur[i] - ul[i];
+    du[NV - 1] = ur[0] * hr - ul[0] * hl;
+
+    bdq[0] = drho - f * dp * rcp_aa * rcp_aa;
+    bdq[NV - 1] = bdq[0] * ha + ra * dh;
+#pragma unroll
+    for (int i = 0; i < ND; i++) bdq[i + 1] = bdq[0] * va[i] + ra * (dv[i] - n[i] * dcontra);
+
+#pragma unroll
+    for (int i = 0; i < NV; i++) {
+        T s = 0;
+#pragma unroll
+        for (int j = 0; j < ND; j++) s += n[j] * (b1 * fl[j][i] - b2 * fr[j][i]);
+        nf[i] = s + b1b2 * (du[i] - g * bdq[i]);
+    }
+}
+
+// Flux f(p) of the pressure function and its derivative for one side of
+// the exact Riemann problem, covolume zero (Toro 2009, eqs. 4.86-4.87;
+// pyfr/solvers/euler/kernels/rsolvers/exact.mako:14-30)
+template <typename T>
+__device__ __forceinline__ void exact_star_flux(T p, T ps, T rs, T cs, T gamma, T &f, T &fd) {
+    const double g = (double)gamma;
+    if (p <= ps) {
+        const T pr = p / ps;
+        const T pr_g = pow(pr, T(-(g + 1) / (2 * g)));
+        fd = pr_g / (rs * cs);
+        f = T(2 / (g - 1)) * cs * (pr_g * pr - T(1));
+    } else {
+        const T pbs_inv = T(1) / (p + T((g - 1) / (g + 1)) * ps);
+        const T sapb = sqrt(T(2 / (g + 1)) * pbs_inv / rs);
+        f = (p - ps) * sapb;
+        fd = sapb - T(0.5) * f * pbs_inv;
+    }
+}
+
+// Exact Riemann solution sampled at x/t = 0 in the normal frame: adaptive
+// initial guess (primitive-variable, two-rarefaction or two-shock), three
+// Newton iterations on the star pressure, then the sampling decision tree
+// (Toro 2009, ch. 4 and 9; pyfr/solvers/euler/kernels/rsolvers/exact.mako)
+template <int ND, typename T>
+__device__ __forceinline__ void exact_1d(const T *ul, const T *ur, T *nf, T gamma, T p_min) {
+    constexpr int NV = ND + 2;
+    const double g = (double)gamma;
+    const T hgm = T(0.5 * (g - 1)), grgm = T(g / (g - 1)), trgm = T(2 / (g - 1));
+    const T trgp = T(2 / (g + 1)), gmrtg = T((g - 1) / (2 * g)), gprtg = T((g + 1) / (2 * g));
+    const T tgrgm = T((2 * g) / (g - 1)), gmrgp = T((g - 1) / (g + 1)), rg = T(1 / g);
+
+    T vl[ND], vr[ND], w0[NV];
+    T pl, pr, cl, cr;
+    {
+        T k2 = 0;
+        const T inv = T(1) / ul[0];
+#pragma unroll
+        for (int i = 0; i < ND; i++) {
+            vl[i] = inv * ul[i + 1];
+            k2 += ul[i + 1] * ul[i + 1];
+        }
+        pl = (gamma - T(1)) * (ul[NV - 1] - T(0.5) * inv * k2);
+        cl = sqrt(gamma * pl * inv);
+    }
+    {
+        T k2 = 0;
+        const T inv = T(1) / ur[0];
+#pragma unroll
+        for (int i = 0; i < ND; i++) {
+            vr[i] = inv * ur[i + 1];
+            k2 += ur[i + 1] * ur[i + 1];
+        }
+        pr = (gamma - T(1)) * (ur[NV - 1] - T(0.5) * inv * k2);
+        cr = sqrt(gamma * pr * inv);
+    }
+
+    const T rl = ul[0], rr = ur[0];
+    const T bpv = fmax(T(0), T(0.125) * (vl[0] - vr[0]) * (rl + rr) * (cl + cr) +
+                                 T(0.5) * (pl + pr));
+    const T pmin = fmin(pl, pr), pmax = fmax(pl, pr);
+    T p0;
+    if (pmax <= T(2) * pmin && pmin <= bpv && bpv <= pmax) {
+        p0 = bpv;
+    } else if (bpv < pmin) {
+        // Two-rarefaction guess
+        const T pre = pow(pl / pr, gmrtg);
+        const T um = (pre * vl[0] * cr + vr[0] * cl + trgm * (pre - T(1)) * cl * cr) /
+                     (pre * cr + cl);
+        const T ptl = T(1) - hgm * (um - vl[0]) / cl;
+        const T ptr = T(1) + hgm * (um - vr[0]) / cr;
+        p0 = T(0.5) * (pl * pow(ptl, tgrgm) + pr * pow(ptr, tgrgm));
+    } else {
+        // Two-shock guess
+        const T gl = sqrt(trgp / (rl * (gmrgp * pl + bpv)));
+        const T gr = sqrt(trgp / (rr * (gmrgp * pr + bpv)));
+        p0 = (gl * pl + gr * pr - vr[0] + vl[0]) / (gl + gr);
+    }
+
+    T fsl, fdl, fsr, fdr;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        exact_star_flux<T>(p0, pl, rl, cl, gamma, fsl, fdl);
+        exact_star_flux<T>(p0, pr, rr, cr, gamma, fsr, fdr);
+        const T p1 = p0 - (fsl + fsr + vr[0] - vl[0]) / (fdl + fdr);
+        p0 = (p1 < T(0)) ? p_min : p1;
+    }
+    const T us = T(0.5) * (vl[0] + vr[0] + fsr - fsl);
+
+    if (T(0) <= us) {
+#pragma unroll
+        for (int i = 1; i < ND; i++) w0[i + 1] = vl[i];
+        if (p0 <= pl) {
+            if (vl[0] >= cl) {
+                w0[0] = rl; w0[1] = vl[0]; w0[NV - 1] = pl;
+            } else if (us < cl * pow(p0 / pl, gmrtg)) {
+                w0[0] = rl * pow(p0 / pl, rg); w0[1] = us; w0[NV - 1] = p0;
+            } else {
+                const T c = trgp + gmrgp * vl[0] / cl;
+                w0[0] = rl * pow(c, trgm);
+                w0[1] = trgp * cl + gmrgp * vl[0];
+                w0[NV - 1] = pl * pow(c, tgrgm);
+            }
+        } else {
+            const T p0p = p0 / pl;
+            const T sl = vl[0] - cl * sqrt(gprtg * p0p + gmrtg);
+            if (T(0) <= sl) {
+                w0[0] = rl; w0[1] = vl[0]; w0[NV - 1] = pl;
+            } else {
+                w0[0] = rl * (p0p + gmrgp) / (p0p * gmrgp + T(1)); w0[1] = us; w0[NV - 1] = p0;
+            }
+        }
+    } else {
+#pragma unroll
+        for (int i = 1; i < ND; i++) w0[i + 1] = vr[i];
+        if (p0 > pr) {
+            const T p0p = p0 / pr;
+            const T sr = vr[0] + cr * sqrt(gprtg * p0p + gmrtg);
+            if (sr <= T(0)) {
+                w0[0] = rr; w0[1] = vr[0]; w0[NV - 1] = pr;
+            } else {
+                w0[0] = rr * (p0p + gmrgp) / (p0p * gmrgp + T(1)); w0[1] = us; w0[NV - 1] = p0;
+            }
+        } else if (vr[0] + cr <= T(0)) {
+            w0[0] = rr; w0[1] = vr[0]; w0[NV - 1] = pr;
+        } else {
+            const T p0p = p0 / pr;
+            if (us + cr * pow(p0p, gmrtg) >= T(0)) {
+                w0[0] = rr * pow(p0p, rg); w0[1] = us; w0[NV - 1] = p0;
+            } else {
+                const T c = trgp - gmrgp * vr[0] / cr;
+                w0[0] = rr * pow(c, trgm);
+                w0[1] = gmrgp * vr[0] - trgp * cr;
+                w0[NV - 1] = pr * pow(c, tgrgm);
+            }
+        }
+    }
+
+    // Primitive state to the x-direction flux
+    nf[0] = w0[0] * w0[1];
+    nf[1] = nf[0] * w0[1] + w0[NV - 1];
+    T k2 = 0;
+#pragma unroll
+    for (int i = 1; i < ND + 1; i++) k2 += w0[i] * w0[i];
+#pragma unroll
+    for (int i = 2; i < ND + 1; i++) nf[i] = nf[0] * w0[i];
+    nf[NV - 1] = (grgm * w0[NV - 1] + T(0.5) * w0[0] * k2) * w0[1];
+}
+
+// A one-dimensional solver applied in the normal frame
+// (pyfr/solvers/euler/kernels/rsolvers/rsolve1d.mako:5-22)
+template <int RS, int ND, typename T>
+__device__ __forceinline__ void rsolve_rotated(const T *ul, const T *ur, const T *n, T *nf,
+                                               T gamma, T p_min) {
+    constexpr int NV = ND + 2;
+    T utl[NV], utr[NV], ntf[NV];
+    utl[0] = ul[0];
+    utr[0] = ur[0];
+    utl[NV - 1] = ul[NV - 1];
+    utr[NV - 1] = ur[NV - 1];
+    rot_to<ND, T>(n, ul, utl);
+    rot_to<ND, T>(n, ur, utr);
+    if (RS == RS_ROE)
+        roe_1d<ND, T>(utl, utr, ntf, gamma);
+    else
+        exact_1d<ND, T>(utl, utr, ntf, gamma, p_min);
+    nf[0] = ntf[0];
+    nf[NV - 1] = ntf[NV - 1];
+    rot_from<ND, T>(n, ntf, nf);
+}
+
+// The Riemann solver as a compile-time choice: each interface kernel is
+// instantiated per solver, so it carries the registers of its own solver
+// only.  p_min: the floor of the exact solver's Newton iterations
+// (pyfr/solvers/euler/inters.py:12-25).
+template <int RS, int ND, typename T>
+__device__ __forceinline__ void rsolve_t(const T *ul, const T *ur, const T *n, T *nf, T gamma,
+                                         T p_min) {
+    if constexpr (RS == RS_HLLC)
         rsolve_hllc<ND, T>(ul, ur, n, nf, gamma);
+    else if constexpr (RS == RS_HLL)
+        rsolve_hll<ND, T>(ul, ur, n, nf, gamma);
+    else if constexpr (RS == RS_ROEM)
+        rsolve_roem<ND, T>(ul, ur, n, nf, gamma);
+    else if constexpr (RS == RS_ROE || RS == RS_EXACT)
+        rsolve_rotated<RS, ND, T>(ul, ur, n, nf, gamma, p_min);
     else
         rsolve_rusanov<ND, T>(ul, ur, n, nf, gamma);
+}
+
+// Host-side dispatch of a launch over the solvers: fn(integral_constant<RS>)
+template <typename F>
+inline bool with_rsolver(int rs, F &&fn) {
+    switch (rs) {
+    case RS_RUSANOV: fn(std::integral_constant<int, RS_RUSANOV>()); return true;
+    case RS_HLLC: fn(std::integral_constant<int, RS_HLLC>()); return true;
+    case RS_HLL: fn(std::integral_constant<int, RS_HLL>()); return true;
+    case RS_ROE: fn(std::integral_constant<int, RS_ROE>()); return true;
+    case RS_ROEM: fn(std::integral_constant<int, RS_ROEM>()); return true;
+    case RS_EXACT: fn(std::integral_constant<int, RS_EXACT>()); return true;
+    default: return false;
+    }
 }
 
 // Metric terms of a linear (multilinear) element at reference point x from

@@ -11,7 +11,8 @@
 //   tflux (NS, fused)  pyfr/solvers/navstokes/kernels/tflux.mako:13-50
 //   gradcoru           pyfr/solvers/baseadvecdiff/kernels/gradcoru.mako:10-24
 //   negdivconf         pyfr/solvers/baseadvec/kernels/negdivconf.mako:7-22
-//   intcflux (Euler)   pyfr/solvers/euler/kernels/intcflux.mako:6-22
+//   intcflux (Euler)   pyfr/solvers/euler/kernels/intcflux.mako:6-22 (any of the
+//                      six Riemann solvers, a template argument)
 //   intcflux (NS)      pyfr/solvers/navstokes/kernels/intcflux.mako:10-54
 //   intconu            pyfr/solvers/navstokes/kernels/intconu.mako:4-19
 #include "common.cuh"
@@ -274,9 +275,9 @@ struct VectView {
     const void *rstr;
 };
 
-template <int ND, typename T>
+template <int RS, int ND, typename T>
 __global__ void __launch_bounds__(PW_BLOCK)
-intcflux_euler_kernel(int64_t n, int rs, T gamma, ScalView<T> vl, ScalView<T> vr, int ix64,
+intcflux_euler_kernel(int64_t n, T gamma, T p_min, ScalView<T> vl, ScalView<T> vr, int ix64,
                       const T *__restrict__ nl, int64_t ldn) {
     constexpr int NV = ND + 2;
     const int64_t i = (int64_t)blockIdx.x * PW_BLOCK + threadIdx.x;
@@ -302,7 +303,7 @@ intcflux_euler_kernel(int64_t n, int rs, T gamma, ScalView<T> vl, ScalView<T> vr
     for (int d = 0; d < ND; d++) nn[d] = inv * nn[d];
 
     T fn[NV];
-    b200::rsolve<ND, T>(rs, ul, ur, nn, fn, gamma);
+    b200::rsolve_t<RS, ND, T>(ul, ur, nn, fn, gamma, p_min);
 
 #pragma unroll
     for (int v = 0; v < NV; v++) {
@@ -311,9 +312,9 @@ intcflux_euler_kernel(int64_t n, int rs, T gamma, ScalView<T> vl, ScalView<T> vr
     }
 }
 
-template <int ND, typename T>
+template <int RS, int ND, typename T>
 __global__ void __launch_bounds__(PW_BLOCK)
-intcflux_ns_kernel(int64_t n, int rs, b200::GasK<T> gas, T beta, T tau, ScalView<T> vl, ScalView<T> vr,
+intcflux_ns_kernel(int64_t n, b200::GasK<T> gas, T beta, T tau, ScalView<T> vl, ScalView<T> vr,
                    VectView<T> gl, VectView<T> gr, int ix64, const T *__restrict__ nl,
                    int64_t ldn, ScalView<T> va) {
     constexpr int NV = ND + 2;
@@ -342,10 +343,10 @@ intcflux_ns_kernel(int64_t n, int rs, b200::GasK<T> gas, T beta, T tau, ScalView
     // Riemann flux; with a shifted input the viscous terms need the full
     // states, which the shifted flux reconstructs
     T fi[NV], ufl[NV], ufr[NV];
-    if (gas.shifted) {
+    if (RS == b200::RS_RUSANOV && gas.shifted) {
         b200::rsolve_rusanov_shift<ND, T>(ul, ur, nn, fi, ufl, ufr, gas);
     } else {
-        b200::rsolve<ND, T>(rs, ul, ur, nn, fi, gas.gamma);
+        b200::rsolve_t<RS, ND, T>(ul, ur, nn, fi, gas.gamma, gas.p_min);
 #pragma unroll
         for (int v = 0; v < NV; v++) {
             ufl[v] = ul[v];
@@ -567,20 +568,22 @@ int gradcoru(int ndims, int nupts, int64_t neles, int linear, T *gradu, int64_t 
 }
 
 template <typename T>
-int intcflux_euler(int ndims, int64_t n, int rsolver, double gamma, T *ul_base,
+int intcflux_euler(int ndims, int64_t n, int rsolver, double gamma, double p_min, T *ul_base,
                    const void *ul_map, T *ur_base, const void *ur_map, int ix64, const T *nl,
                    int64_t ldn, cudaStream_t st) {
     if (n <= 0) return B200_OK;
-    if (rsolver != b200::RS_RUSANOV && rsolver != b200::RS_HLLC)
-        return b200::set_error(B200_ERR_ARG, "intcflux: unknown Riemann solver %d", rsolver);
+    if (ndims != 2 && ndims != 3)
+        return b200::set_error(B200_ERR_ARG, "intcflux: ndims must be 2 or 3");
     ScalView<T> l{ul_base, ul_map}, r{ur_base, ur_map};
     unsigned grid = b200::ceil_div(n, PW_BLOCK);
-    if (ndims == 2)
-        intcflux_euler_kernel<2, T><<<grid, PW_BLOCK, 0, st>>>(n, rsolver, (T)gamma, l, r, ix64, nl, ldn);
-    else if (ndims == 3)
-        intcflux_euler_kernel<3, T><<<grid, PW_BLOCK, 0, st>>>(n, rsolver, (T)gamma, l, r, ix64, nl, ldn);
-    else
-        return b200::set_error(B200_ERR_ARG, "intcflux: ndims must be 2 or 3");
+    const bool ok = b200::with_rsolver(rsolver, [&](auto rsc) {
+        constexpr int RS = decltype(rsc)::value;
+        if (ndims == 2)
+            intcflux_euler_kernel<RS, 2, T><<<grid, PW_BLOCK, 0, st>>>(n, (T)gamma, (T)p_min, l, r, ix64, nl, ldn);
+        else
+            intcflux_euler_kernel<RS, 3, T><<<grid, PW_BLOCK, 0, st>>>(n, (T)gamma, (T)p_min, l, r, ix64, nl, ldn);
+    });
+    if (!ok) return b200::set_error(B200_ERR_ARG, "intcflux: unknown Riemann solver %d", rsolver);
     B200_CHECK_LAUNCH("intcflux_euler");
     return B200_OK;
 }
@@ -597,21 +600,23 @@ int intcflux_ns(int ndims, int64_t n, int rsolver, const b200_gas_t *gas, double
         return b200::set_error(B200_ERR_ARG,
                                "intcflux_ns: artificial viscosity needs a view and unshifted states");
     ScalView<T> va{const_cast<T *>(av_base), av_map};
-    if (rsolver != b200::RS_RUSANOV && rsolver != b200::RS_HLLC)
-        return b200::set_error(B200_ERR_ARG, "intcflux: unknown Riemann solver %d", rsolver);
     ScalView<T> l{ul_base, ul_map}, r{ur_base, ur_map};
     VectView<T> gl{gl_base, gl_map, gl_rstr}, gr{gr_base, gr_map, gr_rstr};
     const auto g = b200::gas_consts<T>(*reinterpret_cast<const Gas *>(gas));
     if (g.shifted && rsolver != b200::RS_RUSANOV)
         return b200::set_error(B200_ERR_UNSUPPORTED,
                                "intcflux_ns: shifted inputs need the Rusanov solver");
-    unsigned grid = b200::ceil_div(n, PW_BLOCK);
-    if (ndims == 2)
-        intcflux_ns_kernel<2, T><<<grid, PW_BLOCK, 0, st>>>(n, rsolver, g, (T)beta, (T)tau, l, r, gl, gr, ix64, nl, ldn, va);
-    else if (ndims == 3)
-        intcflux_ns_kernel<3, T><<<grid, PW_BLOCK, 0, st>>>(n, rsolver, g, (T)beta, (T)tau, l, r, gl, gr, ix64, nl, ldn, va);
-    else
+    if (ndims != 2 && ndims != 3)
         return b200::set_error(B200_ERR_ARG, "intcflux_ns: ndims must be 2 or 3");
+    unsigned grid = b200::ceil_div(n, PW_BLOCK);
+    const bool ok = b200::with_rsolver(rsolver, [&](auto rsc) {
+        constexpr int RS = decltype(rsc)::value;
+        if (ndims == 2)
+            intcflux_ns_kernel<RS, 2, T><<<grid, PW_BLOCK, 0, st>>>(n, g, (T)beta, (T)tau, l, r, gl, gr, ix64, nl, ldn, va);
+        else
+            intcflux_ns_kernel<RS, 3, T><<<grid, PW_BLOCK, 0, st>>>(n, g, (T)beta, (T)tau, l, r, gl, gr, ix64, nl, ldn, va);
+    });
+    if (!ok) return b200::set_error(B200_ERR_ARG, "intcflux: unknown Riemann solver %d", rsolver);
     B200_CHECK_LAUNCH("intcflux_ns");
     return B200_OK;
 }
@@ -724,17 +729,19 @@ int b200_negdivconf_f32(int nvars, int nupts, int64_t neles, float *r, int64_t l
     return B200_OK;
 }
 
-int b200_intcflux_euler_f64(int ndims, int64_t n, int rsolver, double gamma, double *ul_base,
+int b200_intcflux_euler_f64(int ndims, int64_t n, int rsolver, double gamma, double p_min,
+                            double *ul_base,
                             const void *ul_map, double *ur_base, const void *ur_map, int ix64,
                             const double *nl, int64_t ldn, void *stream) {
-    return intcflux_euler<double>(ndims, n, rsolver, gamma, ul_base, ul_map, ur_base, ur_map,
+    return intcflux_euler<double>(ndims, n, rsolver, gamma, p_min, ul_base, ul_map, ur_base, ur_map,
                                   ix64, nl, ldn, (cudaStream_t)stream);
 }
 
-int b200_intcflux_euler_f32(int ndims, int64_t n, int rsolver, double gamma, float *ul_base,
+int b200_intcflux_euler_f32(int ndims, int64_t n, int rsolver, double gamma, double p_min,
+                            float *ul_base,
                             const void *ul_map, float *ur_base, const void *ur_map, int ix64,
                             const float *nl, int64_t ldn, void *stream) {
-    return intcflux_euler<float>(ndims, n, rsolver, gamma, ul_base, ul_map, ur_base, ur_map,
+    return intcflux_euler<float>(ndims, n, rsolver, gamma, p_min, ul_base, ul_map, ur_base, ur_map,
                                  ix64, nl, ldn, (cudaStream_t)stream);
 }
 

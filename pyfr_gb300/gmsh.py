@@ -201,6 +201,8 @@ class GmshReader:
         return GMSH_HIGH_ORDER[etype][1] if etype in GMSH_HIGH_ORDER else \
             GMSH_ETYPES[etype][1]
 
+    LINEARISE_CHUNK = 512
+
     def _linearise(self, etype, nodes, lintol=1e-5):
         """The vertices of high-order elements whose other nodes all lie on
         the equi-spaced lattice of their linear element (within ``lintol``
@@ -216,21 +218,26 @@ class GmshReader:
         nv = len(VERTICES[petype]) if petype != 'line' else 2
         verts = nodes[:, :nv] - self._nodeoff
         if petype != 'line':
-            nd = {'tri': 2, 'quad': 2, 'tet': 3, 'hex': 3, 'pri': 3}[petype]
             lat = std_ele(petype, order)
             # Lattice positions from the vertices (Gmsh vertex order ->
-            # the format's)
+            # the format's), in all three coordinates: a boundary face of a
+            # 3-D mesh may bend out of its plane in any of them
             sf = linear_shape_fn(petype, lat)                # (nlat, nv)
-            gv = self._nodepts[verts][:, GMSH_VERTEX_ORDER[petype], :nd]
-            want = np.einsum('lv,evd->eld', sf, gv)          # (ne, nlat, nd)
-            have = self._nodepts[nodes - self._nodeoff][:, :, :nd]
-            ext = np.ptp(gv, axis=1).max(axis=1)[:, None, None]
-            d = np.linalg.norm(have[:, :, None] - want[:, None], axis=3)
-            ok = np.all(d.min(axis=2) <= lintol*ext[:, :, 0], axis=1)
-            if not np.all(ok):
-                raise ValueError(f'Curved high-order elements (type {etype}) '
-                                 'are not supported: the geometry path is '
-                                 'linear')
+            vo = GMSH_VERTEX_ORDER[petype]
+            # Elements in fixed-size chunks: the node-to-lattice distance
+            # table is (chunk, nnodes, nlattice), so memory stays bounded
+            # whatever the mesh size
+            for i in range(0, len(nodes), self.LINEARISE_CHUNK):
+                sl = slice(i, i + self.LINEARISE_CHUNK)
+                gv = self._nodepts[verts[sl]][:, vo]
+                want = np.einsum('lv,evd->eld', sf, gv)      # (ne, nlat, 3)
+                have = self._nodepts[nodes[sl] - self._nodeoff]
+                ext = np.ptp(gv, axis=1).max(axis=1)[:, None]
+                d = np.linalg.norm(have[:, :, None] - want[:, None], axis=3)
+                if not np.all(d.min(axis=2) <= lintol*ext):
+                    raise ValueError(f'Curved high-order elements (type '
+                                     f'{etype}) are not supported: the '
+                                     'geometry path is linear')
         return lin[petype], nodes[:, :nv]
 
     def _read_eles(self, it):

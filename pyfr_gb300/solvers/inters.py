@@ -94,13 +94,21 @@ class BaseIntInters:
         return self._view(side, meth, (self.ndims, self.nvars))
 
 
+def riemann_p_min(cfg, be):
+    """Star-pressure floor of the exact Riemann solver: the entropy
+    filter's p-min when it is on, else [solver-interfaces] p-min
+    (pyfr/solvers/euler/inters.py:12-25)."""
+    if cfg.get('solver', 'shock-capturing', 'none') == 'entropy-filter':
+        return cfg.getfloat('solver-entropy-filter', 'p-min', 1e-6)
+    return cfg.getfloat('solver-interfaces', 'p-min', 5*be.fpdtype_eps)
+
+
 class EulerIntInters(BaseIntInters):
     def __init__(self, *args, **kwargs):
         super().__init__(*args, **kwargs)
 
         rsolver = self.cfg.get('solver-interfaces', 'riemann-solver')
-        p_min = self.cfg.getfloat('solver-interfaces', 'p-min',
-                                  5*self._be.fpdtype_eps)
+        p_min = riemann_p_min(self.cfg, self._be)
         self._tplargs = dict(ndims=self.ndims, nvars=self.nvars,
                              rsolver=rsolver, c=self.c, p_min=p_min)
 
@@ -124,8 +132,7 @@ class NavierStokesIntInters(BaseIntInters):
 
         rsolver = cfg.get('solver-interfaces', 'riemann-solver')
         visc_corr = cfg.get('solver', 'viscosity-correction', 'none')
-        p_min = cfg.getfloat('solver-interfaces', 'p-min',
-                             5*self._be.fpdtype_eps)
+        p_min = riemann_p_min(cfg, self._be)
         sc = cfg.get('solver', 'shock-capturing', 'none')
         self._tplargs = dict(ndims=self.ndims, nvars=self.nvars,
                              rsolver=rsolver, visc_corr=visc_corr,
@@ -306,7 +313,8 @@ class EulerBCInters(BaseBCInters):
         rsolver = self.cfg.get('solver-interfaces', 'riemann-solver')
         self._tplargs = dict(ndims=self.ndims, nvars=self.nvars,
                              rsolver=rsolver, c=self.c, bctype=self.type,
-                             bc=self.bc)
+                             bc=self.bc, p_min=riemann_p_min(self.cfg,
+                                                             self._be))
         self._be.pointwise.register('pyfr.solvers.euler.kernels.bccflux')
         self.kernels['comm_flux'] = lambda: self._be.kernel(
             'bccflux', tplargs=self._tplargs, dims=[self.ninterfpts],
@@ -330,7 +338,8 @@ class NavierStokesBCInters(BaseBCInters):
                              shock_capturing=cfg.get('solver',
                                                      'shock-capturing',
                                                      'none'),
-                             c=self.c, bctype=self.type, bc=self.bc)
+                             c=self.c, bctype=self.type, bc=self.bc,
+                             p_min=riemann_p_min(cfg, be))
         self.artvisc = None
         be.pointwise.register('pyfr.solvers.navstokes.kernels.bcconu')
         be.pointwise.register('pyfr.solvers.navstokes.kernels.bccflux')

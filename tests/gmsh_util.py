@@ -109,3 +109,57 @@ def box_msh(n, periodic, version='2.2', lo=0.0, hi=1.0, vol='fluid'):
             k += 1
         out.append('$EndElements')
     return '\n'.join(out) + '\n'
+
+
+def raise_order(txt, order, perturb=None):
+    """A version-2.2 Gmsh text of straight elements of ``order`` from the
+    first-order text of ``box_msh``: each quadrilateral and hexahedron
+    gets the nodes of the equi-spaced lattice of its vertices after them
+    (the importer matches nodes to lattice points whatever their order).
+    ``perturb``: (element number, lattice node index, offset) moves one
+    added node off the lattice."""
+    hexq = {3: (10, 36, 37), 5: (12, 92, 93)}        # linear -> order 2-4
+    inv = {2: [0, 1, 3, 2], 3: [0, 1, 3, 2, 4, 5, 7, 6]}
+    lines = txt.split('\n')
+    i0, i1 = lines.index('$Nodes'), lines.index('$EndNodes')
+    pts = {}
+    for ln in lines[i0 + 2:i1]:
+        v = ln.split()
+        pts[int(v[0])] = np.array([float(x) for x in v[1:4]])
+    nxt = max(pts) + 1
+    e0, e1 = lines.index('$Elements'), lines.index('$EndElements')
+    els, new = [], []
+    for ln in lines[e0 + 2:e1]:
+        v = [int(x) for x in ln.split()]
+        num, et, nt = v[0], v[1], v[2]
+        vs = v[3 + nt:]
+        if et not in hexq:
+            els.append(ln)
+            continue
+        nd = 2 if et == 3 else 3
+        # Vertices in first-coordinate-fastest order
+        corner = np.array([pts[vs[inv[nd].index(k)]] for k in range(2**nd)])
+        extra = []
+        for ijk in np.ndindex(*(order + 1,)*nd):
+            t = np.array(ijk[::-1], dtype=float)/order
+            if np.all((t == 0) | (t == 1)):
+                continue
+            w = np.ones(2**nd)
+            for k in range(2**nd):
+                for d in range(nd):
+                    w[k] *= t[d] if (k >> d) & 1 else 1 - t[d]
+            x = w @ corner
+            if perturb and perturb[0] == num and perturb[1] == len(extra):
+                x = x + np.asarray(perturb[2])
+            pts[nxt] = x
+            new.append(nxt)
+            extra.append(nxt)
+            nxt += 1
+        ht = hexq[et][order - 2]
+        els.append(' '.join(map(str, [num, ht, nt, *v[3:3 + nt], *vs,
+                                      *extra])))
+    nodes = [f'{k} {float(x[0])!r} {float(x[1])!r} {float(x[2])!r}'
+             for k, x in sorted(pts.items())]
+    out = lines[:i0 + 1] + [str(len(nodes))] + nodes + lines[i1:e0 + 1]
+    out += [str(len(els))] + els + lines[e1:]
+    return '\n'.join(out)

@@ -1,10 +1,11 @@
 """Generate golden fixtures from the reference implementation itself.
 
-Run in a container that has the PyFR source tree (read-only) at
-/root/reference; the GPU hosts do not need it, they use the committed
-``.npz`` files this script writes next to itself:
+Run where the PyFR source tree is present (read-only), named by the
+``PYFR_REFERENCE`` environment variable (default ``/root/reference``); the
+GPU hosts do not need it, they use the committed ``.npz`` files this script
+writes next to itself:
 
-  python tests/golden/make_golden.py
+  PYFR_REFERENCE=/path/to/PyFR python tests/golden/make_golden.py [step...]
 
 What is generated (all with the reference's own code):
 
@@ -31,13 +32,14 @@ before importing it.
 """
 
 from io import BytesIO
+import os
 from pathlib import Path
 import sys
 import types
 
 import numpy as np
 
-REF = Path('/root/reference')
+REF = Path(os.environ.get('PYFR_REFERENCE', '/root/reference'))
 HERE = Path(__file__).resolve().parent
 REPO = HERE.parent.parent
 

@@ -17,7 +17,7 @@ from pyfr_gb300.mesh import Mesh, Side, box, mixed_box, periodic_box, tri_box
 from pyfr_gb300.native import (NativeFile, NativeFileWriter, corner_nodes,
                                read_mesh, read_soln, read_subset_soln,
                                save_mesh, std_ele, write_soln)
-from tests.gmsh_util import box_msh
+from tests.gmsh_util import box_msh, raise_order
 
 
 def _pairs(m):
@@ -401,6 +401,42 @@ def test_gmsh_straight_high_order(tmp_path):
     curved = txt.replace('\n14 0.5 0.5 0\n', '\n14 0.55 0.5 0\n')
     with pytest.raises(ValueError, match='Curved'):
         GmshReader(curved)
+
+
+@pytest.mark.parametrize('order', [2, 3, 4])
+def test_gmsh_straight_high_order_hexes(order):
+    """Straight hexahedra (and their quadrilateral boundary faces) of
+    orders 2-4 read as the first-order mesh; a node moved off the lattice
+    raises, also when it moves out of a boundary face's plane in z."""
+    lin = box_msh((2, 2, 2), (True, False, False))
+    _, eles1, codec1, _ = GmshReader(lin).records()
+    _, eles, codec, _ = GmshReader(raise_order(lin, order)).records()
+    assert codec == codec1
+    for k in ('nodes', 'faces'):
+        assert eles['hex'][k].tolist() == eles1['hex'][k].tolist()
+
+    # An interior lattice node of the first hexahedron, moved in x
+    first_hex = 1 + sum(1 for ln in lin.split('\n') if ' 3 2 ' in ln[:12])
+    with pytest.raises(ValueError, match='Curved'):
+        GmshReader(raise_order(lin, order, (first_hex, 0, (0.02, 0, 0))))
+    # A boundary quadrilateral (the first facet, on y = lo) bent in z
+    with pytest.raises(ValueError, match='Curved'):
+        GmshReader(raise_order(lin, order, (1, 0, (0, 0, 0.02))))
+
+
+def test_gmsh_high_order_import_memory():
+    """The straightness check of high-order elements works in bounded
+    chunks: importing 3072 order-3 hexahedra stays far below the
+    (elements x nodes x lattice points) distance table of one pass (about
+    three times that table when done at once)."""
+    import tracemalloc
+    txt = raise_order(box_msh((16, 16, 12), (True, True, True)), 3)
+    tracemalloc.start()
+    GmshReader(txt)
+    _, peak = tracemalloc.get_traced_memory()
+    tracemalloc.stop()
+    one_pass = 3072*64*64*3*8
+    assert peak < one_pass, peak
 
 
 def test_subset_solution(tmp_path):
