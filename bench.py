@@ -122,6 +122,10 @@ def kernel_bytes(k, be):
         ncol, nb = b.ncol, m.get('nbatch', 1)
         kin = a.ncol + (m['a2'].ncol if m.get('a2') is not None else 0)
         nout = a.nrow*ncol*(2 if m['beta'] else 1)
+        if m.get('rk_stage'):
+            # RK stage in the epilogue: the output is not stored; the FP64
+            # solution is read and written and the FP32 input written
+            nout = a.nrow*ncol*(8 + 8 + 4)//itemsize
         rs = m.get('rowscale')
         srows = rs.nrow*rs.ncol if rs is not None else 0
         return (nb*(kin*ncol + nout) + srows)*itemsize
@@ -129,8 +133,10 @@ def kernel_bytes(k, be):
         nupts, neles = m['dims']
         nd, nv = m['tplargs']['ndims'], m['tplargs']['nvars']
         per_pt = nv + nd*nv + (2*nd*nv if kind == 'tflux_ns' else 0)
-        geo = (2**nd)*nd*neles if m.get('verts') is not None else \
-            nupts*neles*(nd*nd + 1)
+        # Metric terms (nd*nd + 1 values) stored per point or, for affine
+        # elements, per element; or the vertices they are rebuilt from
+        geo = {1: (2**nd)*nd*neles, 2: neles*(nd*nd + 1)}.get(
+            m.get('geom_mode'), nupts*neles*(nd*nd + 1))
         return (per_pt*nupts*neles + geo)*itemsize
     if kind in ('intcflux_ns', 'intcflux_euler'):
         (n,) = m['dims']
@@ -139,7 +145,8 @@ def kernel_bytes(k, be):
         nsides = 0
         if kind == 'intcflux_ns':
             nsides = 1 if abs(m['tplargs']['c']['ldg-beta']) == 0.5 else 2
-        vals = 4*nv + nd + nsides*nd*nv
+        # (the unit normal and its magnitude: nd + 1 values)
+        vals = 4*nv + nd + 1 + nsides*nd*nv
         maps = 2 + 2*nsides
         return n*(vals*itemsize + maps*4)
     if kind == 'intconu':
@@ -157,6 +164,66 @@ def kernel_bytes(k, be):
         # FP64 accumulator read + write, FP32 RHS read, FP32 input write
         return m['n']*(8 + 8 + 4 + 4)
     return 0
+
+
+def kernel_flops64(k):
+    """FP64 flops of one launch of an FP64 operator apply (the sparse
+    kernel: one FMA per operator nonzero and column, plus one per output
+    when it accumulates into the output)."""
+    m = k.meta
+    if k.name != 'mul':
+        return 0
+    ncol, nb = m['b'].ncol, m.get('nbatch', 1)
+    nnz = 0
+    for a in (m['a'], m.get('a2')):
+        h = getattr(a, '_host', None) if a is not None else None
+        if h is not None:
+            nnz += int(np.count_nonzero(h))
+    return nb*ncol*(2*nnz + (2*m['a'].nrow if m['beta'] else 0))
+
+
+def fp64_peak(be):
+    """Measured FP64 FMA throughput of the device, TFLOP/s."""
+    import ctypes as C
+    f = C.c_double()
+    be.lib.probe_fp64_fma(1 << 14, C.byref(f), be.stream)
+    return f.value/1e12
+
+
+# Per-DoF HBM floor of one right-hand side (read the solution, write the
+# RHS, vertices, face states and common fluxes; FP64, halved for FP32
+# state) of the Navier-Stokes hex p=3 workload: 51 392 B per element of
+# 320 DoF
+FLOOR_BYTES_PER_DOF_F64 = 51392/320
+
+
+def dram_traffic(form, kernel, n):
+    """ncu DRAM bytes per launch of the dominant kernel, scaled from the
+    committed capture (profiles/dram_traffic.json: bytes per column at the
+    captured size) to n^3 elements; None without a capture."""
+    p = ROOT / 'profiles' / 'dram_traffic.json'
+    if not p.exists():
+        return None
+    d = json.loads(p.read_text()).get(form, {}).get(kernel)
+    if not d:
+        return None
+    return int(d['bytes_per_element']*n**3)
+
+
+def cpu_model():
+    try:
+        for line in Path('/proc/cpuinfo').read_text().splitlines():
+            k, _, v = line.partition(':')
+            if k.strip() in ('model name', 'Model'):
+                return v.strip()
+        out = subprocess.run(['lscpu'], capture_output=True, text=True,
+                             timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith('Model name'):
+                return line.split(':', 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return None
 
 
 def flat_kernels(klist):
@@ -208,6 +275,9 @@ def make_form(form, args):
                 str(args.chosen_products) if form == 'chosen' else '3')
     elif form == 'tf32':
         cfg.set('backend-b200', 'mul-precision', 'tf32')
+    if not args.autotune:
+        cfg.set('backend-b200', 'autotune', 'false')
+    cfg.set('backend-b200', 'fuse-stage', args.fuse_stage)
     be = B200Backend(cfg)
     icls = RKVdH2Integrator if form == 'plain' else MixedRKIntegrator
     return icls(be, NavierStokesSystem, mesh, cfg)
@@ -298,6 +368,9 @@ def measure(intg, args, dist, e2e=True, profile=True):
         d = per[dom]
         peak, peak_kind = _peaks()
         achieved = d['bytes']/(d['ms']*1e-3)/1e9
+        # FP64 flops of the dominant kernel over the three replayed steps
+        flops = 3*sum(kernel_flops64(k) for k in klist
+                      if k.meta.get('kind', k.name) == dom)
         res['kernels'] = {
             n: {'share': round(v['ms']/tot, 4),
                 'avg_us': round(1e3*v['ms']/v['n'], 2),
@@ -307,12 +380,30 @@ def measure(intg, args, dist, e2e=True, profile=True):
             n: {'avg_us': round(1e3*v['ms']/v['n'], 2),
                 'gbs': round(v['bytes']/(v['ms']*1e-3)/1e9, 1)}
             for n, v in sorted(ops.items(), key=lambda x: -x[1]['ms'])}
-        res['roofline'] = {
-            'bound': 'hbm', 'kernel': dom, 'achieved': round(achieved, 1),
-            'peak': peak, 'unit': 'GB/s', 'frac': round(achieved/peak, 4),
-            'traffic': None, 'peak_source': peak_kind,
-            'alg_bytes_per_launch': int(d['bytes']/d['n']),
-            'avg_launch_us': round(1e3*d['ms']/d['n'], 2)}
+        traffic = dram_traffic('plain' if be.fpdtype == np.float64
+                               else 'chosen', dom, args.n)
+        hbm = {'bound': 'hbm', 'kernel': dom, 'achieved': round(achieved, 1),
+               'peak': peak, 'unit': 'GB/s', 'frac': round(achieved/peak, 4),
+               'traffic': traffic, 'peak_source': f'{peak_kind} (HBM copy)',
+               'alg_bytes_per_launch': int(d['bytes']/d['n']),
+               'avg_launch_us': round(1e3*d['ms']/d['n'], 2)}
+        if be.fpdtype == np.float64 and flops:
+            # The FP64 sparse applies are bound by the FP64 pipe on this
+            # GPU, not by HBM: report against the measured FMA throughput,
+            # with the HBM fraction beside it
+            pk = fp64_peak(be)
+            tf = flops/(d['ms']*1e-3)/1e12
+            res['roofline'] = {
+                'bound': 'fp64', 'kernel': dom, 'achieved': round(tf, 4),
+                'peak': round(pk, 4), 'unit': 'TFLOP/s',
+                'frac': round(tf/pk, 4), 'traffic': traffic,
+                'peak_source': 'measured (FP64 FMA-chain probe, '
+                               'b200_probe_fp64_fma, this run)',
+                'flops_per_launch': int(flops/d['n']),
+                'avg_launch_us': round(1e3*d['ms']/d['n'], 2),
+                'hbm': hbm}
+        else:
+            res['roofline'] = hbm
 
     if e2e:
         # End to end through the public API: the solution goes in from
@@ -686,7 +777,9 @@ def main():
     ap.add_argument('--impl', default='b200', choices=['b200', 'reference'])
     ap.add_argument('--n', type=int, default=48)
     ap.add_argument('--dt', type=float, default=5e-4)
-    ap.add_argument('--cpu-sample', type=int, default=24)
+    ap.add_argument('--cpu-sample', type=int, default=None,
+                    help='mesh size n^3 of the CPU timing (default: --n, '
+                         'the benchmark mesh itself)')
     ap.add_argument('--cpu-seconds', type=float, default=10.0)
     ap.add_argument('--no-chosen', dest='chosen', action='store_false',
                     help='skip the chosen precision form')
@@ -716,12 +809,22 @@ def main():
     ap.add_argument('--ens-cases', type=int, default=64)
     ap.add_argument('--ens-seed', type=int, default=0)
     ap.add_argument('--ens-dt', type=float, default=1e-4)
+    ap.add_argument('--fuse-stage', default='auto',
+                    choices=['auto', 'true', 'false'],
+                    help='the RK stage in the divergence apply\'s epilogue '
+                         '(chosen form)')
+    ap.add_argument('--no-autotune', dest='autotune', action='store_false',
+                    help='the deepest pipeline plan of each operator instead '
+                         'of timing them (no tuning launches before the '
+                         'timed ones: a fixed launch sequence to profile)')
     ap.add_argument('--only', choices=['plain', 'chosen', 'bf16x3', 'tf32',
                                        'fp32'],
                     help='time one precision form alone (no accuracy '
                          'history, end-to-end loop or CPU sample): the '
                          'command to run under a profiler')
     args = ap.parse_args()
+    if args.cpu_sample is None:
+        args.cpu_sample = args.n
 
     world = int(os.environ.get('WORLD_SIZE', '1'))
     rank = int(os.environ.get('RANK', '0'))
@@ -743,16 +846,19 @@ def main():
         secs = min(max(2.0, 2.0*args.steps), 60.0)
         v, dt, ndofs, nrhs = run_cpu_sample(args.cpu_sample, secs)
         sample = (f'{args.cpu_sample}^3-element TGV ({ndofs} DoF), {nrhs} '
-                  f'RHS evaluations in {dt:.1f} s, C/OpenMP restatement')
+                  f'RHS evaluations in {dt:.1f} s, C/OpenMP restatement of '
+                  'the reference kernels (-O3 -ffast-math, the reference '
+                  'OpenMP backend\'s flags)')
         print(json.dumps({
             'impl': 'reference', 'metric': METRIC, 'value': v,
             'unit': 'GDoF/s', 'n_gpus': args.gpus, 'steps': args.steps,
             'warmup': args.warmup, 'higher_is_better': True,
             'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
             'data': 'synthetic', 'config': workload,
+            'same_mesh': args.cpu_sample == args.n,
             'cpu_baseline': {'value': v, 'unit': 'GDoF/s',
                              'cores': cpu_cores(), 'kind': 'port',
-                             'sample': sample},
+                             'cpu_model': cpu_model(), 'sample': sample},
             'e2e': {'value': v, 'unit': 'GDoF/s', 'h2d_bytes_per_step': 0,
                     'd2h_bytes_per_step': 0}}))
         return
@@ -874,6 +980,15 @@ def main():
     if chosen is not None:
         chosen['other_variants'] = variants
 
+    # Step-level fraction of the HBM floor: the algorithmic floor bytes of
+    # every right-hand side of the timed steps over the time, against the
+    # measured copy bandwidth
+    peak, _ = _peaks()
+
+    def floor_frac(r, itemsize):
+        b = FLOOR_BYTES_PER_DOF_F64*itemsize/8*r['gndofs']*r['nstages']
+        return round(b*args.steps/(r['t_ms']*1e-3)/1e9/peak, 4)
+
     out = {
         'metric': METRIC, 'value': value, 'unit': 'GDoF/s',
         'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
@@ -892,13 +1007,33 @@ def main():
         'kernels': res['kernels'],
         'mul_ops': res['mul_ops'],
         'chosen': chosen,
+        'floor_frac': floor_frac(res, 8),
         'cpu_baseline': {'value': cpu_v, 'unit': 'GDoF/s',
                          'cores': cpu_cores(), 'kind': 'port',
+                         'cpu_model': cpu_model(),
+                         'same_mesh': args.cpu_sample == args.n,
                          'sample': f'{cpu_nrhs} RHS evaluations of the '
                                    f'C/OpenMP oracle (-O3 -ffast-math) on a '
                                    f'{args.cpu_sample}^3 TGV mesh '
                                    f'({cpu_ndofs} DoF, {cpu_dt:.1f} s)'},
     }
+    if chosen is not None:
+        rc = allres['chosen']
+        chosen['floor_frac'] = floor_frac(rc, 4)
+        # A compact summary of the chosen form last, so that a reader of a
+        # truncated line still sees it
+        out['chosen_summary'] = {
+            'value': round(chosen['value'], 3), 'unit': 'GDoF/s',
+            'ms_per_step': round(chosen['ms_per_step'], 3),
+            'speedup_vs_plain': round(chosen['speedup_vs_plain'], 2),
+            'l2_err_vs_fp64': chosen['l2_err_vs_fp64'],
+            'ke_hist_max_abs_err_vs_fp64':
+                chosen['ke_hist_max_abs_err_vs_fp64'],
+            'after_steps': args.accuracy_steps,
+            'roofline_frac': chosen.get('roofline', {}).get('frac'),
+            'floor_frac': chosen['floor_frac'],
+            'e2e': round(chosen['e2e']['value'], 3) if 'e2e' in chosen
+            else None}
     print(json.dumps(out))
 
 

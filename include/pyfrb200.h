@@ -130,6 +130,13 @@ int b200_event_destroy(void *evt);
 int b200_event_record(void *evt, void *stream);
 int b200_event_sync(void *evt);
 int b200_event_elapsed(float *ms, void *start, void *stop);
+
+/* Measured FP64 FMA throughput of this device (flops per second): eight
+ * independent FMA chains per thread over 8 blocks of 256 threads per SM,
+ * timed with events on `stream`.  The roofline denominator of the plain
+ * FP64 form's kernels, which the FP64 pipe bounds on this GPU.  No
+ * counterpart in the reference (a measurement utility). */
+int b200_probe_fp64_fma(int iters, double *flops_per_s, void *stream);
 /* Graph capture of a kernel sequence; replaces CUDAGraph
  * (pyfr/backends/cuda/types.py:79-116). */
 int b200_graph_begin_capture(void *stream);
@@ -193,6 +200,21 @@ typedef struct {
                                    4: plus Alo*Blo; 5: plus Ax3*Bhi (a
                                    handle with a three-term operator) */
     int *err;                   /* device int: pipeline timeout code */
+    /* Low-storage RK stage in the epilogue (pyfr/integrators/explicit/
+     * kernels/rkvdh2.mako:4-31 in the mixed form of b200_rkmixed_f64f32):
+     * with rk_stage != 0 the output R = alpha*S(.)(...) is not stored;
+     * instead, for every output value, the FP64 solution acc (leading
+     * dimension ldc, the output's layout) becomes acc + dt*b*R and the FP32
+     * next-stage input u becomes fl32(acc_old) + fl32(dt*a)*R (rk_stage 1)
+     * or fl32(acc_new) (rk_stage 2, the last stage).  dt is read from
+     * rk_dt_dev when it is not null, else rk_dt.  One slice, beta = 0, no
+     * error estimate.  Replaces the separate stage kernel after the
+     * divergence apply of the chosen form. */
+    double *rk_acc;
+    float *rk_u;
+    const double *rk_dt_dev;
+    double rk_dt, rk_a, rk_b;
+    int rk_stage;
 } b200_mul_bf16x3_args_t;
 int b200_mul_bf16x3_create_cat(const double *a1, int k1, const double *a2, int k2, int m,
                                 void **handle, size_t *smem_bytes);
@@ -225,11 +247,13 @@ int b200_mul_tc_create_terms(const double *a1, int k1, const double *a2, int k2,
 int b200_mul_tc_terms(void *handle, int *nterms);
 
 /* ---- element pointwise kernels over [nupts, neles] ------------------- */
-/* Geometry: linear != 0 computes the metric terms from the element
+/* Geometry mode `linear`: 1 computes the metric terms from the element
  * vertices `verts` (nverts, ndims, neles) at the reference solution points
- * `upts` (nupts x ndims, row-major with leading dimension ldup); linear == 0
- * reads stored metric terms `smats` (ndims, nupts, ndims, neles) and
- * `rcpdjac` (nupts x neles, leading dimension ldr). */
+ * `upts` (nupts x ndims, row-major with leading dimension ldup); 0 reads
+ * stored metric terms `smats` (ndims, nupts, ndims, neles) and `rcpdjac`
+ * (nupts x neles, leading dimension ldr); 2 reads one stored set per
+ * element, smats (ndims, 1, ndims, neles) and rcpdjac (1 x neles), for
+ * affine elements whose Jacobian is the same at every point. */
 
 /* Euler transformed flux; pyfr/solvers/euler/kernels/tflux.mako:8-30,
  * provider call pyfr/solvers/euler/elements.py:149-206. */
@@ -375,13 +399,13 @@ int b200_intcflux_ns_av_f64(int ndims, int64_t n, int rsolver, const b200_gas_t 
                             double *ur_base, const void *ur_map, const double *gl_base,
                             const void *gl_map, const void *gl_rstr, const double *gr_base,
                             const void *gr_map, const void *gr_rstr, int ix64, const double *nl,
-                            int64_t ldn, const double *av_base, const void *av_map, void *stream);
+                            int64_t ldn, int nl_unit, const double *av_base, const void *av_map, void *stream);
 int b200_intcflux_ns_av_f32(int ndims, int64_t n, int rsolver, const b200_gas_t *gas,
                             double beta, double tau, float *ul_base, const void *ul_map,
                             float *ur_base, const void *ur_map, const float *gl_base,
                             const void *gl_map, const void *gl_rstr, const float *gr_base,
                             const void *gr_map, const void *gr_rstr, int ix64, const float *nl,
-                            int64_t ldn, const float *av_base, const void *av_map, void *stream);
+                            int64_t ldn, int nl_unit, const float *av_base, const void *av_map, void *stream);
 int b200_bccflux_ns_av_f64(int ndims, int64_t n, int rsolver, const b200_gas_t *gas,
                            double tau, const b200_bc_t *bc, double *ul_base, const void *ul_map,
                            const double *gl_base, const void *gl_map, const void *gl_rstr,
@@ -461,15 +485,18 @@ int b200_negdivconf_f32(int nvars, int nupts, int64_t neles, float *r, int64_t l
  * Riemann solver of pyfr/solvers/euler/kernels/rsolvers/: 0 rusanov,
  * 1 hllc, 2 hll, 3 roe, 4 roem, 5 exact (B200_RSOLVER_*); p_min is the
  * exact solver's star-pressure floor.  nl is the (ndims x n) matrix of
- * scaled left normals, leading dimension ldn. */
+ * scaled left normals, leading dimension ldn; with nl_unit != 0 it is the
+ * (ndims + 1) x n matrix of the unit normals (rows 0..ndims-1) and their
+ * magnitudes (row ndims), formed once instead of per call (the NS
+ * interface kernels below take the same). */
 int b200_intcflux_euler_f64(int ndims, int64_t n, int rsolver, double gamma, double p_min,
                             double *ul_base, const void *ul_map, double *ur_base,
-                            const void *ur_map, int ix64, const double *nl, int64_t ldn,
+                            const void *ur_map, int ix64, const double *nl, int64_t ldn, int nl_unit,
                             void *stream);
 int b200_intcflux_euler_f32(int ndims, int64_t n, int rsolver, double gamma, double p_min,
                             float *ul_base,
                             const void *ul_map, float *ur_base, const void *ur_map, int ix64,
-                            const float *nl, int64_t ldn, void *stream);
+                            const float *nl, int64_t ldn, int nl_unit, void *stream);
 
 /* Navier-Stokes common flux (Riemann + LDG viscous with beta, tau);
  * pyfr/solvers/navstokes/kernels/intcflux.mako:10-54. */
@@ -477,13 +504,13 @@ int b200_intcflux_ns_f64(int ndims, int64_t n, int rsolver, const b200_gas_t *ga
                          double tau, double *ul_base, const void *ul_map, double *ur_base,
                          const void *ur_map, const double *gl_base, const void *gl_map,
                          const void *gl_rstr, const double *gr_base, const void *gr_map,
-                         const void *gr_rstr, int ix64, const double *nl, int64_t ldn,
+                         const void *gr_rstr, int ix64, const double *nl, int64_t ldn, int nl_unit,
                          void *stream);
 int b200_intcflux_ns_f32(int ndims, int64_t n, int rsolver, const b200_gas_t *gas, double beta,
                          double tau, float *ul_base, const void *ul_map, float *ur_base,
                          const void *ur_map, const float *gl_base, const void *gl_map,
                          const void *gl_rstr, const float *gr_base, const void *gr_map,
-                         const void *gr_rstr, int ix64, const float *nl, int64_t ldn,
+                         const void *gr_rstr, int ix64, const float *nl, int64_t ldn, int nl_unit,
                          void *stream);
 
 /* LDG common solution; pyfr/solvers/navstokes/kernels/intconu.mako:4-19. */

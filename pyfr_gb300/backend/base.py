@@ -106,6 +106,9 @@ class B200Backend:
         self.fusion = cfg.getbool('backend-b200', 'fusion', True)
         self.precompute_metrics = cfg.getbool('backend-b200',
                                               'precompute-metrics', True)
+        # Affine elements keep one set of metric terms per element
+        self.per_element_metrics = cfg.getbool('backend-b200',
+                                               'per-element-metrics', True)
         # Constant (rho_ref, p_ref) that Navier-Stokes kernels subtract from
         # their inputs; set by the mixed-precision integrator before the
         # kernels are built (None: inputs are the conserved variables)
@@ -138,6 +141,13 @@ class B200Backend:
             raise ValueError('fuse-operators needs single precision with '
                              'mul-precision = bf16x3 or tf32')
         self.fuse_operators = tensor and fuse != 'false'
+
+        # The mixed-precision RK stage in the epilogue of the divergence
+        # apply (with fused operator applies)
+        fstage = cfg.get('backend-b200', 'fuse-stage', 'auto')
+        if fstage not in {'auto', 'true', 'false'}:
+            raise ValueError('fuse-stage must be auto, true or false')
+        self.fuse_stage = self.fuse_operators and fstage != 'false'
 
         self.mats = WeakValueDictionary()
         self._mat_counter = it.count()

@@ -31,7 +31,10 @@ class MulArgs(C.Structure):
                 ('alpha', C.c_float), ('beta', C.c_float),
                 ('rowscale', C.c_void_p), ('ldr', C.c_int64),
                 ('nvars', C.c_int), ('products', C.c_int),
-                ('err', C.c_void_p)]
+                ('err', C.c_void_p), ('rk_acc', C.c_void_p),
+                ('rk_u', C.c_void_p), ('rk_dt_dev', C.c_void_p),
+                ('rk_dt', C.c_double), ('rk_a', C.c_double),
+                ('rk_b', C.c_double), ('rk_stage', C.c_int)]
 
 
 class Gas(C.Structure):
@@ -86,9 +89,9 @@ def _sig_pointwise(fp):
                      vp, i64, vp],
         'negdivconf': [i32, i32, i64, vp, i64, vp, i64, vp],
         'intcflux_euler': [i32, i64, i32, f64, f64, vp, vp, vp, vp, i32, vp,
-                           i64, vp],
+                           i64, i32, vp],
         'intcflux_ns': [i32, i64, i32, C.POINTER(Gas), f64, f64, vp, vp, vp,
-                        vp, vp, vp, vp, vp, vp, vp, i32, vp, i64, vp],
+                        vp, vp, vp, vp, vp, vp, vp, i32, vp, i64, i32, vp],
         'intconu': [i32, i64, f64, vp, vp, vp, vp, vp, vp, vp, vp, i32, vp],
         'intconu_both': [i32, i64, f64, vp, vp, vp, vp, vp, vp, vp, vp, i32,
                          vp],
@@ -112,8 +115,8 @@ def _sig_pointwise(fp):
                         vp, i64, vp, i64, vp, i64, vp, i64, vp, i64, vp, i64,
                         vp],
         'intcflux_ns_av': [i32, i64, i32, C.POINTER(Gas), f64, f64, vp, vp,
-                           vp, vp, vp, vp, vp, vp, vp, vp, i32, vp, i64, vp,
-                           vp, vp],
+                           vp, vp, vp, vp, vp, vp, vp, vp, i32, vp, i64, i32,
+                           vp, vp, vp],
         'shocksensor': [C.POINTER(AV), i64, vp, i64, vp, i64, vp, vp, vp, i64,
                         vp, vp],
         'avfill': [i32, i32, i64, vp, vp, i64, vp, i64, vp, i64, vp],
@@ -151,6 +154,7 @@ _SIGS = {
     'b200_event_record': [vp, vp],
     'b200_event_sync': [vp],
     'b200_event_elapsed': [C.POINTER(f32), vp, vp],
+    'b200_probe_fp64_fma': [i32, C.POINTER(f64), vp],
     'b200_graph_begin_capture': [vp],
     'b200_graph_end_capture': [vp, C.POINTER(vp)],
     'b200_graph_launch': [vp, vp],

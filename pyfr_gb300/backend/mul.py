@@ -401,7 +401,40 @@ class TensorMulKernels:
 
         k = Kernel(run, mats=mats, name='mul', meta=meta)
         k._args = args
+        k._handle = handle
         return k
+
+    def with_stage(self, k, acc, u, a, b, last, dt=0.0, dtdev=None):
+        """A copy of the one-piece apply ``k`` whose epilogue performs the
+        mixed-precision two-register RK stage instead of storing its output
+        R: acc += dt*b*R (FP64) and the next FP32 input u = fl32(acc_old) +
+        fl32(dt*a)*R, or fl32(acc_new) at the last stage (the arithmetic of
+        ``b200_rkmixed_f64f32``, bit for bit).  acc and u have the output's
+        layout.  None when ``k`` cannot take it (several pieces, slices, an
+        accumulating output)."""
+        args = getattr(k, '_args', None)
+        out = k.meta.get('out')
+        if args is None or args.nbatch != 1 or args.beta != 0.0 or \
+                out is None or acc.leaddim != out.leaddim or \
+                u.leaddim != out.leaddim or acc.nrow != out.nrow:
+            return None
+        new = MulArgs()
+        C.memmove(C.addressof(new), C.addressof(args), C.sizeof(MulArgs))
+        new.rk_acc, new.rk_u = acc.data, u.data
+        new.rk_dt_dev = dtdev.data if dtdev is not None else None
+        new.rk_dt, new.rk_a, new.rk_b = dt, a, b
+        new.rk_stage = 2 if last else 1
+        fn, h = self.backend.lib.mul_bf16x3_apply, k._handle
+        pa = C.addressof(new)
+
+        def run(stream):
+            fn(h, pa, stream)
+
+        kk = Kernel(run, mats=list(k.mats) + [acc, u], misc=[new], name='mul',
+                    meta=dict(k.meta, rk_stage=new.rk_stage, acc=acc, u=u))
+        kk._args = new
+        kk._handle = h
+        return kk
 
     def mul(self, a, b, out, alpha=1.0, beta=0.0):
         from pyfr_gb300.backend.base import NotSuitableError

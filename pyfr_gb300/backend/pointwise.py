@@ -77,6 +77,18 @@ def linear_metrics(verts, upts):
     return S.transpose(1, 0, 2, 3), 1.0/d
 
 
+# Geometry modes of the element kernels (the C ABI's `linear` argument)
+GEOM_STORED, GEOM_VERTICES, GEOM_PER_ELEMENT = 0, 1, 2
+
+
+def affine(smats, rtol=1e-13):
+    """Whether every element's metric terms S (ndims, npts, ndims, neles)
+    are the same at all its points (to rounding): true of affine elements
+    (parallelograms, parallelepipeds, simplices)."""
+    dev = np.abs(smats - smats[:, :1]).max(axis=(0, 1, 2))
+    return bool(np.all(dev <= rtol*np.abs(smats).max(axis=(0, 1, 2))))
+
+
 def _host_of(m):
     """Host copy of a constant matrix or of a whole-width slice of one."""
     if hasattr(m, '_host'):
@@ -86,6 +98,16 @@ def _host_of(m):
             m.cb == p.ncol and m.ra == 0 and m.rb == p.nrow:
         return p._host
     return None
+
+
+def _unit_normal_rows(nlh):
+    """(ndims + 1, n) rows of the unit normals and magnitudes of the
+    scaled normals nlh (ndims, n), formed as the reference's interface
+    kernels form them (pyfr/solvers/euler/kernels/intcflux.mako:12-13):
+    mag = sqrt(n.n), unit = (1/mag) n."""
+    nlh = np.asarray(nlh, dtype=np.float64)
+    mag = np.sqrt(np.sum(nlh*nlh, axis=0))
+    return np.vstack([(1/mag)*nlh, mag[None]])
 
 
 def _view(v):
@@ -136,18 +158,37 @@ class PointwiseKernelProvider:
             2**tplargs['ndims']
         if linear and (self.backend.precompute_metrics or not multilin):
             # FP64 arithmetic is scarce on this GPU while bandwidth is not:
-            # read stored per-point metric terms (10 values) instead of
-            # rebuilding the Jacobian from the vertices (~200 flops)
+            # read stored metric terms (10 values) instead of rebuilding the
+            # Jacobian from the vertices (~200 flops); affine elements keep
+            # one set per element
             m = self._stored_metrics(verts, upts)
             if m is not None:
-                smats, rcpdjac = m
-                linear = False
+                smats, rcpdjac, per_ele = m
+                return (GEOM_PER_ELEMENT if per_ele else GEOM_STORED,
+                        _mat(smats), _mat(rcpdjac), (None, 0), (None, 0))
         if linear:
             if not multilin:
                 raise ValueError('Linear-element kernels of this shape need '
                                  'the host copies of its vertices')
-            return 1, (None, 0), (None, 0), _mat(verts), _mat(upts)
-        return 0, _mat(smats), _mat(rcpdjac), (None, 0), (None, 0)
+            return GEOM_VERTICES, (None, 0), (None, 0), _mat(verts), \
+                _mat(upts)
+        return GEOM_STORED, _mat(smats), _mat(rcpdjac), (None, 0), (None, 0)
+
+    def _normals(self, nl):
+        """(pointer, leading dimension, stored-unit flag) of the normals
+        of an interface kernel: the unit normals and magnitudes formed
+        once on the host when nl has a host copy, else nl itself."""
+        h = _host_of(nl)
+        if h is None:
+            np_, nlp = _mat(nl)
+            return np_, nlp, 0, nl
+        key = ('unit', id(h))
+        if key not in self._metrics:
+            m = self.backend.const_matrix(_unit_normal_rows(h),
+                                          tags={'align'})
+            self._metrics[key] = (m, h)
+        m = self._metrics[key][0]
+        return m.data, m.leaddim, 1, m
 
     def _stored_metrics(self, verts, upts):
         vh, uh = _host_of(verts), _host_of(upts)
@@ -157,10 +198,13 @@ class PointwiseKernelProvider:
         if key not in self._metrics:
             be = self.backend
             sm, rj = linear_metrics(vh, uh)
+            per_ele = self.backend.per_element_metrics and affine(sm)
+            if per_ele:
+                sm, rj = sm[:, :1], rj[:1]
             self._metrics[key] = (be.const_matrix(sm, tags={'align'}),
                                   be.const_matrix(rj, tags={'align'}),
-                                  vh, uh)
-        return self._metrics[key][:2]
+                                  per_ele, vh, uh)
+        return self._metrics[key][:3]
 
     def _tflux_euler(self, tplargs, dims, extrns, u, f, smats=None,
                      verts=None, upts=None):
@@ -179,14 +223,22 @@ class PointwiseKernelProvider:
         return Kernel(run, mats=[u, f, smats, verts, upts], name='tflux',
                       meta=dict(kind='tflux_euler', tplargs=tplargs,
                                 dims=dims, u=u, f=f, smats=smats,
-                                verts=verts, upts=upts))
+                                verts=verts, upts=upts,
+                                geom_mode=lin))
 
     def _tflux_ns(self, tplargs, dims, extrns, u, f, gradu=None, smats=None,
-                  rcpdjac=None, verts=None, upts=None, artvisc=None):
+                  rcpdjac=None, verts=None, upts=None, artvisc=None,
+                  artvisc_vtx=None):
         """``artvisc``: the artificial viscosity at the solution points
         (nupts, neles), when shock capturing is 'artificial-viscosity'
         (the vertex interpolation of pyfr/solvers/navstokes/kernels/
-        tflux.mako:39-43, done by the avfill kernel)."""
+        tflux.mako:39-43, done by the avfill kernel).  ``artvisc_vtx`` is
+        the argument of the reference's own elements (a view of the vertex
+        values, None without artificial viscosity)."""
+        if artvisc_vtx is not None:
+            raise NotImplementedError(
+                'Artificial viscosity from vertex views: the b200 systems '
+                'interpolate it to the points first (avfill)')
         av_on = tplargs.get('shock_capturing') == 'artificial-viscosity'
         if av_on != (artvisc is not None):
             raise ValueError('Artificial viscosity needs its field')
@@ -224,7 +276,8 @@ class PointwiseKernelProvider:
                       misc=[gas], name='tflux',
                       meta=dict(kind='tflux_ns', tplargs=tplargs, dims=dims,
                                 u=u, f=f, gradu=gradu, smats=smats,
-                                rcpdjac=rcpdjac, verts=verts, upts=upts))
+                                rcpdjac=rcpdjac, verts=verts, upts=upts,
+                                geom_mode=lin))
 
     def _wavespeed(self, tplargs, dims, extrns, u, wspd, smats=None,
                    rcpdjac=None, verts=None, upts=None):
@@ -299,14 +352,14 @@ class PointwiseKernelProvider:
         p_min = tplargs.get('p_min', P_MIN_DEFAULT)
         lb, lm, _ = _view(ul)
         rb, rm, _ = _view(ur)
-        np_, nlp = _mat(nl)
+        np_, nlp, nlu, nlm = self._normals(nl)
         ix64 = self._ix64
 
         def run(stream):
-            fn(nd, n, rs, gamma, p_min, lb, lm, rb, rm, ix64, np_, nlp,
+            fn(nd, n, rs, gamma, p_min, lb, lm, rb, rm, ix64, np_, nlp, nlu,
                stream)
 
-        return Kernel(run, mats=[nl], views=[ul, ur], name='intcflux',
+        return Kernel(run, mats=[nl, nlm], views=[ul, ur], name='intcflux',
                       meta=dict(kind='intcflux_euler', tplargs=tplargs,
                                 dims=dims, ul=ul, ur=ur, nl=nl))
 
@@ -330,7 +383,7 @@ class PointwiseKernelProvider:
         rb, rm, _ = _view(ur)
         glb, glm, glr = _view(gradul)
         grb, grm, grr = _view(gradur)
-        np_, nlp = _mat(nl)
+        np_, nlp, nlu, nlm = self._normals(nl)
         ix64 = self._ix64
 
         if artvisc is not None:
@@ -339,13 +392,14 @@ class PointwiseKernelProvider:
 
             def run(stream):
                 fn(nd, n, rs, C.byref(gas), beta, tau, lb, lm, rb, rm, glb,
-                   glm, glr, grb, grm, grr, ix64, np_, nlp, ab, am, stream)
+                   glm, glr, grb, grm, grr, ix64, np_, nlp, nlu, ab, am,
+                   stream)
         else:
             def run(stream):
                 fn(nd, n, rs, C.byref(gas), beta, tau, lb, lm, rb, rm, glb,
-                   glm, glr, grb, grm, grr, ix64, np_, nlp, stream)
+                   glm, glr, grb, grm, grr, ix64, np_, nlp, nlu, stream)
 
-        return Kernel(run, mats=[nl],
+        return Kernel(run, mats=[nl, nlm],
                       views=[ul, ur, gradul, gradur] +
                       ([artvisc] if artvisc is not None else []),
                       misc=[gas], name='intcflux',

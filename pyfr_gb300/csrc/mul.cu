@@ -7,7 +7,12 @@
 // pyfr/backends/cuda/cublaslt.py:169-280) with one sparsity-aware kernel.
 //
 // Each CTA stages a k x 64 column tile of B into shared memory with
-// coalesced loads; every warp then produces whole rows of the output tile,
+// asynchronous 16-byte copies (cp.async: every copy of the tile is in
+// flight at once, so staging costs one memory latency rather than one per
+// row; with large K the tile limits residency to a few CTAs per SM, which
+// then cannot hide a row-by-row staging behind each other's FMAs), or with
+// coalesced loads when B is not 16-byte aligned; every warp then produces
+// whole rows of the output tile,
 // walking the nonzeros of A (CSR, read through the read-only cache and
 // broadcast across the warp).  Structural zeros of A cost nothing, so the
 // sparse tensor-product operators run at their nonzero count.
@@ -43,21 +48,42 @@ __device__ __forceinline__ const float *vals<float>(const MulHandle &h) { return
 // beyond the FMAs of the product (beta = 1 accumulates onto the loaded C).
 enum { EPI_SET = 0, EPI_ADD = 1, EPI_GENERAL = 2, EPI_SCALE = 3 };
 
+// 16-byte global -> shared copy; bytes < 16 reads that many and zero-fills
+// the rest
+__device__ __forceinline__ void cp_async16(void *dst, const void *src, int bytes) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;"
+                 :: "r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src), "r"(bytes)
+                 : "memory");
+}
+
 template <typename T, int EPI>
 __global__ void __launch_bounds__(MUL_WARPS * 32)
 mul_csr_kernel(MulHandle h, const T *__restrict__ b, int64_t ldb, T *__restrict__ c,
-               int64_t ldc, int64_t ncol, T alpha, T beta) {
-    extern __shared__ unsigned char smem_raw[];
+               int64_t ldc, int64_t ncol, T alpha, T beta, int vec) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     T *bs = reinterpret_cast<T *>(smem_raw);   // [k][MUL_NCOL]
 
     const int64_t col0 = (int64_t)blockIdx.x * MUL_NCOL;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
     // Stage the B tile (zero-filled beyond ncol)
-    for (int idx = threadIdx.x; idx < h.k * MUL_NCOL; idx += blockDim.x) {
-        int r = idx / MUL_NCOL, cc = idx % MUL_NCOL;
-        int64_t col = col0 + cc;
-        bs[idx] = (col < ncol) ? b[r * ldb + col] : T(0);
+    if (vec) {
+        constexpr int VEC = 16 / sizeof(T), NV = MUL_NCOL / VEC;
+        for (int idx = threadIdx.x; idx < h.k * NV; idx += blockDim.x) {
+            const int r = idx / NV, cv = (idx % NV) * VEC;
+            const int64_t col = col0 + cv;
+            const int64_t rem = ncol - col;
+            const int bytes = rem >= VEC ? 16 : (rem > 0 ? (int)rem * (int)sizeof(T) : 0);
+            // (with nothing to read the source is any valid address)
+            cp_async16(bs + r * MUL_NCOL + cv, bytes ? b + r * ldb + col : b, bytes);
+        }
+        asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
+    } else {
+        for (int idx = threadIdx.x; idx < h.k * MUL_NCOL; idx += blockDim.x) {
+            int r = idx / MUL_NCOL, cc = idx % MUL_NCOL;
+            int64_t col = col0 + cc;
+            bs[idx] = (col < ncol) ? b[r * ldb + col] : T(0);
+        }
     }
     __syncthreads();
 
@@ -103,14 +129,16 @@ int launch_mul(const MulHandle *h, const T *b, int64_t ldb, T *c, int64_t ldc, i
     if (smem > 227 * 1024)
         return b200::set_error(B200_ERR_UNSUPPORTED, "mul: k=%d too large for the tile", h->k);
     unsigned grid = b200::ceil_div(ncol, MUL_NCOL);
+    // 16-byte copies need a 16-byte aligned base and row stride
+    const int vec = !((uintptr_t)b & 15) && !((ldb * (int64_t)sizeof(T)) & 15);
     if (alpha == T(1) && beta == T(0))
-        mul_csr_kernel<T, EPI_SET><<<grid, MUL_WARPS * 32, smem, s>>>(*h, b, ldb, c, ldc, ncol, alpha, beta);
+        mul_csr_kernel<T, EPI_SET><<<grid, MUL_WARPS * 32, smem, s>>>(*h, b, ldb, c, ldc, ncol, alpha, beta, vec);
     else if (alpha == T(1) && beta == T(1))
-        mul_csr_kernel<T, EPI_ADD><<<grid, MUL_WARPS * 32, smem, s>>>(*h, b, ldb, c, ldc, ncol, alpha, beta);
+        mul_csr_kernel<T, EPI_ADD><<<grid, MUL_WARPS * 32, smem, s>>>(*h, b, ldb, c, ldc, ncol, alpha, beta, vec);
     else if (beta == T(0))
-        mul_csr_kernel<T, EPI_SCALE><<<grid, MUL_WARPS * 32, smem, s>>>(*h, b, ldb, c, ldc, ncol, alpha, beta);
+        mul_csr_kernel<T, EPI_SCALE><<<grid, MUL_WARPS * 32, smem, s>>>(*h, b, ldb, c, ldc, ncol, alpha, beta, vec);
     else
-        mul_csr_kernel<T, EPI_GENERAL><<<grid, MUL_WARPS * 32, smem, s>>>(*h, b, ldb, c, ldc, ncol, alpha, beta);
+        mul_csr_kernel<T, EPI_GENERAL><<<grid, MUL_WARPS * 32, smem, s>>>(*h, b, ldb, c, ldc, ncol, alpha, beta, vec);
     B200_CHECK_LAUNCH("mul_csr_kernel");
     return B200_OK;
 }
@@ -120,7 +148,7 @@ int launch_mul(const MulHandle *h, const T *b, int64_t ldb, T *c, int64_t ldc, i
 // function attribute while a capture is open invalidates the capture.
 template <typename T>
 int opt_in_smem() {
-    void (*fns[4])(MulHandle, const T *, int64_t, T *, int64_t, int64_t, T, T) = {
+    void (*fns[4])(MulHandle, const T *, int64_t, T *, int64_t, int64_t, T, T, int) = {
         mul_csr_kernel<T, EPI_SET>, mul_csr_kernel<T, EPI_ADD>,
         mul_csr_kernel<T, EPI_GENERAL>, mul_csr_kernel<T, EPI_SCALE>};
     for (auto fn : fns) {

@@ -257,14 +257,21 @@ struct UmmaArgs {
     const unsigned char *aimg;
     const float *rs;            // row scale S (null: none), S[row*ldr + element]
     int64_t ncol, ntc, ldr;     // ntc: column tiles per slice
+    int64_t ldc;                // leading dimension of out (and of the RK registers)
     int m, npad, kfull, nch1, ns, eb, nbatch, nvars, products;
     int nterms;                 // operator terms in the image (2 or 3)
     float alpha;
     int epi;            // 0: store, 1: add to out
     int *err;
+    // RK stage in the epilogue (rk 1: a stage, 2: the last stage; 0: off)
+    double *rk_acc;
+    float *rk_u;
+    const double *rk_dtp;
+    double rk_dt, rk_a, rk_b;
+    int rk;
 };
 
-template <bool TF32>
+template <bool TF32, bool RK>
 __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_constant__ UmmaArgs p) {
     extern __shared__ __align__(1024) unsigned char smem[];
     const Layout L = make_layout(p.npad, p.kfull, p.ns, p.eb, p.nterms);
@@ -491,6 +498,15 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
         const int quad = warp % 4, half = warp / 4;
         const bool issuer = quad == 0 && lane == 0;
         int i = 0, sb = 0;
+        // RK stage products, as the stage kernel forms them: dt*a rounded
+        // to FP32, dt*b in FP64
+        double rk_dtb = 0;
+        float rk_dta = 0;
+        if (RK) {
+            const double h = p.rk_dtp ? *p.rk_dtp : p.rk_dt;
+            rk_dtb = h * p.rk_b;
+            rk_dta = (float)(h * p.rk_a);
+        }
         // Row-scale factors alpha*S[row, element] of row group g for this
         // thread's column (alpha alone without a scale)
         auto load_scale = [&](float *f, int g, int64_t col, int64_t ele) {
@@ -516,6 +532,21 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
             // The first group's scale loads are in flight during the wait
             float f[32];
             load_scale(f, half, col, ele);
+            // RK stage: the tile's FP64 solution rows are brought into L2
+            // while its MMAs run, so that the epilogue's loads of them do
+            // not wait on HBM (one bulk prefetch of up to 1 KB per row, by
+            // the first warp of each set)
+            if (RK && quad == 0) {
+                const int64_t nc = p.ncol - x0 < TCOLS ? p.ncol - x0 : TCOLS;
+                const uint32_t bytes = (uint32_t)(nc * 8) & ~15u;
+                for (int g = half; g < npad / 32; g += 2) {
+                    const int row = g * 32 + lane;
+                    if (row < p.m && bytes)
+                        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;"
+                                     :: "l"(p.rk_acc + (int64_t)row * p.ldc + x0), "r"(bytes)
+                                     : "memory");
+                }
+            }
             const bool ok = bar_wait(bar(BAR_ACCFULL + bsel), (i >> 1) & 1, abort_flag, p.err, 8);
             asm volatile("bar.sync %0, %1;" :: "r"(EPI_BARRIER + half), "n"(128) : "memory");
             if (!ok || *abort_flag) break;
@@ -537,6 +568,51 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
                       "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
                     : "r"(taddr));
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+
+                if (RK) {
+                    // R never goes to memory: the stage update of this
+                    // thread's column in place, RKB rows at a time (one warp
+                    // reads 32 consecutive FP64 values per row).  Each
+                    // value is read and then written by this thread only,
+                    // so the reads take the non-coherent path, and the next
+                    // rows are in flight while the current ones are
+                    // updated.
+#pragma unroll
+                    for (int r = 0; r < 32; r++) f[r] *= __uint_as_float(v[r]);
+                    if (col < p.ncol) {
+                        const double *acc = p.rk_acc + col;
+                        constexpr int RKB = 4;
+                        auto loadb = [&](double *t, int h2) {
+#pragma unroll
+                            for (int r = 0; r < RKB; r++) {
+                                const int row = g * 32 + h2 * RKB + r;
+                                t[r] = row < p.m ? __ldg(acc + (int64_t)row * p.ldc) : 0.0;
+                            }
+                        };
+                        double t[RKB], tn[RKB];
+                        loadb(t, 0);
+#pragma unroll
+                        for (int h2 = 0; h2 < 32 / RKB; h2++) {
+                            if (h2 < 32 / RKB - 1) loadb(tn, h2 + 1);
+#pragma unroll
+                            for (int r = 0; r < RKB; r++) {
+                                const int row = g * 32 + h2 * RKB + r;
+                                if (row < p.m) {
+                                    const float rf = f[h2 * RKB + r];
+                                    const float t32 = b200::narrow_f64(t[r]);
+                                    const double tw = fma(rk_dtb, b200::widen_f32(rf), t[r]);
+                                    const int64_t ix = (int64_t)row * p.ldc + col;
+                                    p.rk_acc[ix] = tw;
+                                    p.rk_u[ix] = p.rk == 2 ? b200::narrow_f64(tw)
+                                                           : fmaf(rk_dta, rf, t32);
+                                }
+                            }
+#pragma unroll
+                            for (int r = 0; r < RKB; r++) t[r] = tn[r];
+                        }
+                    }
+                    continue;
+                }
 
                 // The store issued eb stores ago from this staging tile
                 // must have finished reading it
@@ -720,15 +796,25 @@ int create_impl(const double *a1, int k1, const double *a2, int k2, int m, int t
                 cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev),
                 "mul_bf16x3_create");
         if (!rc0)
-            rc0 = b200::check_cuda(cudaFuncSetAttribute(mul_umma_kernel<false>,
+            rc0 = b200::check_cuda(cudaFuncSetAttribute(mul_umma_kernel<false, false>,
                                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                         227 * 1024),
                                    "mul_bf16x3: smem attribute");
         if (!rc0)
-            rc0 = b200::check_cuda(cudaFuncSetAttribute(mul_umma_kernel<true>,
+            rc0 = b200::check_cuda(cudaFuncSetAttribute(mul_umma_kernel<true, false>,
                                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                         227 * 1024),
                                    "mul_tf32: smem attribute");
+        if (!rc0)
+            rc0 = b200::check_cuda(cudaFuncSetAttribute(mul_umma_kernel<false, true>,
+                                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                        227 * 1024),
+                                   "mul_bf16x3 (RK stage): smem attribute");
+        if (!rc0)
+            rc0 = b200::check_cuda(cudaFuncSetAttribute(mul_umma_kernel<true, true>,
+                                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                        227 * 1024),
+                                   "mul_tf32 (RK stage): smem attribute");
         if (!rc0) {
             void *fn = nullptr;
             cudaDriverEntryPointQueryResult q;
@@ -858,6 +944,12 @@ int b200_mul_bf16x3_apply(void *handle, const b200_mul_bf16x3_args_t *a, void *s
     // The epilogue stores (beta = 0) or adds (beta = 1) through the TMA
     if (a->beta != 0.0f && a->beta != 1.0f)
         return b200::set_error(B200_ERR_UNSUPPORTED, "mul_bf16x3: beta must be 0 or 1");
+    if (a->rk_stage < 0 || a->rk_stage > 2)
+        return b200::set_error(B200_ERR_ARG, "mul_bf16x3: rk_stage must be 0, 1 or 2");
+    if (a->rk_stage && (!a->rk_acc || !a->rk_u || a->nbatch != 1 || a->beta != 0.0f ||
+                        (((uintptr_t)a->rk_acc) & 7) || (((uintptr_t)a->rk_u) & 3)))
+        return b200::set_error(B200_ERR_ARG,
+                               "mul_bf16x3: the RK stage needs acc and u, one slice, beta = 0");
     UmmaArgs p;
     const int one = a->nbatch == 1;
     int rc = encode_b_map(&p.tmap[0], a->b1, a->ldb1, a->ncol, h->k1, a->nbatch,
@@ -879,13 +971,21 @@ int b200_mul_bf16x3_apply(void *handle, const b200_mul_bf16x3_args_t *a, void *s
     p.alpha = a->alpha; p.epi = a->beta != 0.0f; p.err = a->err;
     p.products = a->products == 0 ? 3 : a->products;
     p.nterms = h->nterms;
+    p.rk = a->rk_stage; p.rk_acc = a->rk_acc; p.rk_u = a->rk_u; p.rk_dtp = a->rk_dt_dev;
+    p.rk_dt = a->rk_dt; p.rk_a = a->rk_a; p.rk_b = a->rk_b;
+    p.ldc = a->ldc;
 
     const int64_t ntiles = p.ntc * p.nbatch;
     const unsigned grid = (unsigned)(ntiles < g_sm_count ? ntiles : g_sm_count);
-    if (h->tf32)
-        mul_umma_kernel<true><<<grid, NTHREADS, h->smem_bytes, (cudaStream_t)stream>>>(p);
+    const cudaStream_t st = (cudaStream_t)stream;
+    if (h->tf32 && p.rk)
+        mul_umma_kernel<true, true><<<grid, NTHREADS, h->smem_bytes, st>>>(p);
+    else if (h->tf32)
+        mul_umma_kernel<true, false><<<grid, NTHREADS, h->smem_bytes, st>>>(p);
+    else if (p.rk)
+        mul_umma_kernel<false, true><<<grid, NTHREADS, h->smem_bytes, st>>>(p);
     else
-        mul_umma_kernel<false><<<grid, NTHREADS, h->smem_bytes, (cudaStream_t)stream>>>(p);
+        mul_umma_kernel<false, false><<<grid, NTHREADS, h->smem_bytes, st>>>(p);
     B200_CHECK_LAUNCH("mul_umma_kernel");
     return B200_OK;
 }

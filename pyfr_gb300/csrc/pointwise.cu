@@ -35,13 +35,24 @@ struct ElemGeom {
     int linear;
 };
 
+// Geometry modes (the `linear` argument of the element kernels)
+enum { GEOM_STORED = 0, GEOM_VERTICES = 1, GEOM_PER_ELEMENT = 2 };
+
 // Metric terms at solution point `upt` of element `e`: from the vertices
-// (linear elements) or from the stored per-point smats and 1/|J|.
+// (GEOM_VERTICES, multilinear elements), from the stored per-point smats
+// and 1/|J| (GEOM_STORED), or from one stored set per element
+// (GEOM_PER_ELEMENT: affine elements, whose Jacobian is constant, keep
+// only the rows of their first point: io-shapes (ndims, 1, ndims, neles)
+// and (1, neles)).
 template <int ND, typename T>
 __device__ __forceinline__ void elem_metrics(const ElemGeom<T> &g, int nupts, int upt,
                                              int64_t e, T s[ND][ND], T &rcpdjac,
                                              bool need_rcp) {
-    if (g.linear) {
+    if (g.linear == GEOM_PER_ELEMENT) {
+        nupts = 1;
+        upt = 0;
+    }
+    if (g.linear == GEOM_VERTICES) {
         T V[1 << ND][ND], x[ND], d;
 #pragma unroll
         for (int v = 0; v < (1 << ND); v++)
@@ -275,23 +286,19 @@ struct VectView {
     const void *rstr;
 };
 
-template <int RS, int ND, typename T>
-__global__ void __launch_bounds__(PW_BLOCK)
-intcflux_euler_kernel(int64_t n, T gamma, T p_min, ScalView<T> vl, ScalView<T> vr, int ix64,
-                      const T *__restrict__ nl, int64_t ldn) {
-    constexpr int NV = ND + 2;
-    const int64_t i = (int64_t)blockIdx.x * PW_BLOCK + threadIdx.x;
-    if (i >= n) return;
-
-    T *pl = vl.base + b200::load_ix(vl.map, ix64, i);
-    T *pr = vr.base + b200::load_ix(vr.map, ix64, i);
-
-    T ul[NV], ur[NV], nn[ND], mag = 0;
+// Unit normal and magnitude of pair i: stored (nl_unit: rows 0..ND-1 the
+// unit normal, row ND its magnitude, formed once on the host as the
+// reference forms them per call, mag = sqrt(n.n), n/mag = (1/mag) n) or
+// formed here from the scaled normal
+template <int ND, typename T>
+__device__ __forceinline__ T pair_normal(const T *__restrict__ nl, int64_t ldn, int64_t i,
+                                         int nl_unit, T nn[ND]) {
+    if (nl_unit) {
 #pragma unroll
-    for (int v = 0; v < NV; v++) {
-        ul[v] = pl[v * B200_SOASZ];
-        ur[v] = pr[v * B200_SOASZ];
+        for (int d = 0; d < ND; d++) nn[d] = nl[d * ldn + i];
+        return nl[ND * ldn + i];
     }
+    T mag = 0;
 #pragma unroll
     for (int d = 0; d < ND; d++) {
         nn[d] = nl[d * ldn + i];
@@ -301,6 +308,27 @@ intcflux_euler_kernel(int64_t n, T gamma, T p_min, ScalView<T> vl, ScalView<T> v
     const T inv = T(1) / mag;
 #pragma unroll
     for (int d = 0; d < ND; d++) nn[d] = inv * nn[d];
+    return mag;
+}
+
+template <int RS, int ND, typename T>
+__global__ void __launch_bounds__(PW_BLOCK)
+intcflux_euler_kernel(int64_t n, T gamma, T p_min, ScalView<T> vl, ScalView<T> vr, int ix64,
+                      const T *__restrict__ nl, int64_t ldn, int nl_unit) {
+    constexpr int NV = ND + 2;
+    const int64_t i = (int64_t)blockIdx.x * PW_BLOCK + threadIdx.x;
+    if (i >= n) return;
+
+    T *pl = vl.base + b200::load_ix(vl.map, ix64, i);
+    T *pr = vr.base + b200::load_ix(vr.map, ix64, i);
+
+    T ul[NV], ur[NV], nn[ND];
+#pragma unroll
+    for (int v = 0; v < NV; v++) {
+        ul[v] = pl[v * B200_SOASZ];
+        ur[v] = pr[v * B200_SOASZ];
+    }
+    const T mag = pair_normal<ND, T>(nl, ldn, i, nl_unit, nn);
 
     T fn[NV];
     b200::rsolve_t<RS, ND, T>(ul, ur, nn, fn, gamma, p_min);
@@ -316,7 +344,7 @@ template <int RS, int ND, typename T>
 __global__ void __launch_bounds__(PW_BLOCK)
 intcflux_ns_kernel(int64_t n, b200::GasK<T> gas, T beta, T tau, ScalView<T> vl, ScalView<T> vr,
                    VectView<T> gl, VectView<T> gr, int ix64, const T *__restrict__ nl,
-                   int64_t ldn, ScalView<T> va) {
+                   int64_t ldn, int nl_unit, ScalView<T> va) {
     constexpr int NV = ND + 2;
     const int64_t i = (int64_t)blockIdx.x * PW_BLOCK + threadIdx.x;
     if (i >= n) return;
@@ -324,21 +352,13 @@ intcflux_ns_kernel(int64_t n, b200::GasK<T> gas, T beta, T tau, ScalView<T> vl, 
     T *pl = vl.base + b200::load_ix(vl.map, ix64, i);
     T *pr = vr.base + b200::load_ix(vr.map, ix64, i);
 
-    T ul[NV], ur[NV], nn[ND], mag = 0;
+    T ul[NV], ur[NV], nn[ND];
 #pragma unroll
     for (int v = 0; v < NV; v++) {
         ul[v] = pl[v * B200_SOASZ];
         ur[v] = pr[v * B200_SOASZ];
     }
-#pragma unroll
-    for (int d = 0; d < ND; d++) {
-        nn[d] = nl[d * ldn + i];
-        mag += nn[d] * nn[d];
-    }
-    mag = sqrt(mag);
-    const T inv = T(1) / mag;
-#pragma unroll
-    for (int d = 0; d < ND; d++) nn[d] = inv * nn[d];
+    const T mag = pair_normal<ND, T>(nl, ldn, i, nl_unit, nn);
 
     // Riemann flux; with a shifted input the viscous terms need the full
     // states, which the shifted flux reconstructs
@@ -475,10 +495,12 @@ ElemGeom<T> make_geom(int linear, const T *smats, int64_t lds, const T *rcpdjac,
 
 int check_geom(int linear, const void *smats, const void *rcpdjac, const void *verts,
                const void *upts, bool need_rcp) {
-    if (linear && (!verts || !upts))
+    if (linear < GEOM_STORED || linear > GEOM_PER_ELEMENT)
+        return b200::set_error(B200_ERR_ARG, "unknown geometry mode %d", linear);
+    if (linear == GEOM_VERTICES && (!verts || !upts))
         return b200::set_error(B200_ERR_ARG, "linear elements need verts and upts");
-    if (!linear && (!smats || (need_rcp && !rcpdjac)))
-        return b200::set_error(B200_ERR_ARG, "curved elements need smats (and rcpdjac)");
+    if (linear != GEOM_VERTICES && (!smats || (need_rcp && !rcpdjac)))
+        return b200::set_error(B200_ERR_ARG, "stored metrics need smats (and rcpdjac)");
     return B200_OK;
 }
 
@@ -570,7 +592,7 @@ int gradcoru(int ndims, int nupts, int64_t neles, int linear, T *gradu, int64_t 
 template <typename T>
 int intcflux_euler(int ndims, int64_t n, int rsolver, double gamma, double p_min, T *ul_base,
                    const void *ul_map, T *ur_base, const void *ur_map, int ix64, const T *nl,
-                   int64_t ldn, cudaStream_t st) {
+                   int64_t ldn, int nl_unit, cudaStream_t st) {
     if (n <= 0) return B200_OK;
     if (ndims != 2 && ndims != 3)
         return b200::set_error(B200_ERR_ARG, "intcflux: ndims must be 2 or 3");
@@ -579,9 +601,9 @@ int intcflux_euler(int ndims, int64_t n, int rsolver, double gamma, double p_min
     const bool ok = b200::with_rsolver(rsolver, [&](auto rsc) {
         constexpr int RS = decltype(rsc)::value;
         if (ndims == 2)
-            intcflux_euler_kernel<RS, 2, T><<<grid, PW_BLOCK, 0, st>>>(n, (T)gamma, (T)p_min, l, r, ix64, nl, ldn);
+            intcflux_euler_kernel<RS, 2, T><<<grid, PW_BLOCK, 0, st>>>(n, (T)gamma, (T)p_min, l, r, ix64, nl, ldn, nl_unit);
         else
-            intcflux_euler_kernel<RS, 3, T><<<grid, PW_BLOCK, 0, st>>>(n, (T)gamma, (T)p_min, l, r, ix64, nl, ldn);
+            intcflux_euler_kernel<RS, 3, T><<<grid, PW_BLOCK, 0, st>>>(n, (T)gamma, (T)p_min, l, r, ix64, nl, ldn, nl_unit);
     });
     if (!ok) return b200::set_error(B200_ERR_ARG, "intcflux: unknown Riemann solver %d", rsolver);
     B200_CHECK_LAUNCH("intcflux_euler");
@@ -593,7 +615,7 @@ int intcflux_ns(int ndims, int64_t n, int rsolver, const b200_gas_t *gas, double
                 double tau, T *ul_base, const void *ul_map, T *ur_base, const void *ur_map,
                 const T *gl_base, const void *gl_map, const void *gl_rstr, const T *gr_base,
                 const void *gr_map, const void *gr_rstr, int ix64, const T *nl, int64_t ldn,
-                const T *av_base, const void *av_map, cudaStream_t st) {
+                int nl_unit, const T *av_base, const void *av_map, cudaStream_t st) {
     if (n <= 0) return B200_OK;
     if (!gas) return b200::set_error(B200_ERR_ARG, "intcflux_ns: null gas constants");
     if (av_base && (!av_map || reinterpret_cast<const Gas *>(gas)->shifted))
@@ -612,9 +634,9 @@ int intcflux_ns(int ndims, int64_t n, int rsolver, const b200_gas_t *gas, double
     const bool ok = b200::with_rsolver(rsolver, [&](auto rsc) {
         constexpr int RS = decltype(rsc)::value;
         if (ndims == 2)
-            intcflux_ns_kernel<RS, 2, T><<<grid, PW_BLOCK, 0, st>>>(n, g, (T)beta, (T)tau, l, r, gl, gr, ix64, nl, ldn, va);
+            intcflux_ns_kernel<RS, 2, T><<<grid, PW_BLOCK, 0, st>>>(n, g, (T)beta, (T)tau, l, r, gl, gr, ix64, nl, ldn, nl_unit, va);
         else
-            intcflux_ns_kernel<RS, 3, T><<<grid, PW_BLOCK, 0, st>>>(n, g, (T)beta, (T)tau, l, r, gl, gr, ix64, nl, ldn, va);
+            intcflux_ns_kernel<RS, 3, T><<<grid, PW_BLOCK, 0, st>>>(n, g, (T)beta, (T)tau, l, r, gl, gr, ix64, nl, ldn, nl_unit, va);
     });
     if (!ok) return b200::set_error(B200_ERR_ARG, "intcflux: unknown Riemann solver %d", rsolver);
     B200_CHECK_LAUNCH("intcflux_ns");
@@ -732,28 +754,28 @@ int b200_negdivconf_f32(int nvars, int nupts, int64_t neles, float *r, int64_t l
 int b200_intcflux_euler_f64(int ndims, int64_t n, int rsolver, double gamma, double p_min,
                             double *ul_base,
                             const void *ul_map, double *ur_base, const void *ur_map, int ix64,
-                            const double *nl, int64_t ldn, void *stream) {
+                            const double *nl, int64_t ldn, int nl_unit, void *stream) {
     return intcflux_euler<double>(ndims, n, rsolver, gamma, p_min, ul_base, ul_map, ur_base, ur_map,
-                                  ix64, nl, ldn, (cudaStream_t)stream);
+                                  ix64, nl, ldn, nl_unit, (cudaStream_t)stream);
 }
 
 int b200_intcflux_euler_f32(int ndims, int64_t n, int rsolver, double gamma, double p_min,
                             float *ul_base,
                             const void *ul_map, float *ur_base, const void *ur_map, int ix64,
-                            const float *nl, int64_t ldn, void *stream) {
+                            const float *nl, int64_t ldn, int nl_unit, void *stream) {
     return intcflux_euler<float>(ndims, n, rsolver, gamma, p_min, ul_base, ul_map, ur_base, ur_map,
-                                 ix64, nl, ldn, (cudaStream_t)stream);
+                                 ix64, nl, ldn, nl_unit, (cudaStream_t)stream);
 }
 
 int b200_intcflux_ns_f64(int ndims, int64_t n, int rsolver, const b200_gas_t *gas, double beta,
                          double tau, double *ul_base, const void *ul_map, double *ur_base,
                          const void *ur_map, const double *gl_base, const void *gl_map,
                          const void *gl_rstr, const double *gr_base, const void *gr_map,
-                         const void *gr_rstr, int ix64, const double *nl, int64_t ldn,
+                         const void *gr_rstr, int ix64, const double *nl, int64_t ldn, int nl_unit,
                          void *stream) {
     return intcflux_ns<double>(ndims, n, rsolver, gas, beta, tau, ul_base, ul_map, ur_base,
                                ur_map, gl_base, gl_map, gl_rstr, gr_base, gr_map, gr_rstr, ix64,
-                               nl, ldn, nullptr, nullptr, (cudaStream_t)stream);
+                               nl, ldn, nl_unit, nullptr, nullptr, (cudaStream_t)stream);
 }
 
 int b200_intcflux_ns_av_f64(int ndims, int64_t n, int rsolver, const b200_gas_t *gas,
@@ -761,10 +783,10 @@ int b200_intcflux_ns_av_f64(int ndims, int64_t n, int rsolver, const b200_gas_t 
                             double *ur_base, const void *ur_map, const double *gl_base,
                             const void *gl_map, const void *gl_rstr, const double *gr_base,
                             const void *gr_map, const void *gr_rstr, int ix64, const double *nl,
-                            int64_t ldn, const double *av_base, const void *av_map, void *stream) {
+                            int64_t ldn, int nl_unit, const double *av_base, const void *av_map, void *stream) {
     if (!av_base) return b200::set_error(B200_ERR_ARG, "intcflux_ns_av: null viscosity");
     return intcflux_ns<double>(ndims, n, rsolver, gas, beta, tau, ul_base, ul_map, ur_base, ur_map,
-                           gl_base, gl_map, gl_rstr, gr_base, gr_map, gr_rstr, ix64, nl, ldn,
+                           gl_base, gl_map, gl_rstr, gr_base, gr_map, gr_rstr, ix64, nl, ldn, nl_unit,
                            av_base, av_map, (cudaStream_t)stream);
 }
 
@@ -772,11 +794,11 @@ int b200_intcflux_ns_f32(int ndims, int64_t n, int rsolver, const b200_gas_t *ga
                          double tau, float *ul_base, const void *ul_map, float *ur_base,
                          const void *ur_map, const float *gl_base, const void *gl_map,
                          const void *gl_rstr, const float *gr_base, const void *gr_map,
-                         const void *gr_rstr, int ix64, const float *nl, int64_t ldn,
+                         const void *gr_rstr, int ix64, const float *nl, int64_t ldn, int nl_unit,
                          void *stream) {
     return intcflux_ns<float>(ndims, n, rsolver, gas, beta, tau, ul_base, ul_map, ur_base,
                               ur_map, gl_base, gl_map, gl_rstr, gr_base, gr_map, gr_rstr, ix64,
-                              nl, ldn, nullptr, nullptr, (cudaStream_t)stream);
+                              nl, ldn, nl_unit, nullptr, nullptr, (cudaStream_t)stream);
 }
 
 int b200_intcflux_ns_av_f32(int ndims, int64_t n, int rsolver, const b200_gas_t *gas,
@@ -784,10 +806,10 @@ int b200_intcflux_ns_av_f32(int ndims, int64_t n, int rsolver, const b200_gas_t 
                             float *ur_base, const void *ur_map, const float *gl_base,
                             const void *gl_map, const void *gl_rstr, const float *gr_base,
                             const void *gr_map, const void *gr_rstr, int ix64, const float *nl,
-                            int64_t ldn, const float *av_base, const void *av_map, void *stream) {
+                            int64_t ldn, int nl_unit, const float *av_base, const void *av_map, void *stream) {
     if (!av_base) return b200::set_error(B200_ERR_ARG, "intcflux_ns_av: null viscosity");
     return intcflux_ns<float>(ndims, n, rsolver, gas, beta, tau, ul_base, ul_map, ur_base, ur_map,
-                           gl_base, gl_map, gl_rstr, gr_base, gr_map, gr_rstr, ix64, nl, ldn,
+                           gl_base, gl_map, gl_rstr, gr_base, gr_map, gr_rstr, ix64, nl, ldn, nl_unit,
                            av_base, av_map, (cudaStream_t)stream);
 }
 

@@ -31,6 +31,31 @@ int check_cuda(cudaError_t err, const char *what) {
 using b200::check_cuda;
 using b200::set_error;
 
+namespace {
+
+// Eight independent FMA chains per thread: enough instruction-level
+// parallelism to keep the FP64 pipe issuing every cycle.  x -> a x + b with
+// 0 < a < 1 converges to b/(1 - a), so the values stay bounded.
+constexpr int PROBE_CHAINS = 8;
+
+__global__ void __launch_bounds__(256) fp64_fma_probe_kernel(double *out, int iters, double a,
+                                                             double b) {
+    double x[PROBE_CHAINS];
+#pragma unroll
+    for (int k = 0; k < PROBE_CHAINS; k++) x[k] = 1e-3 * (threadIdx.x + k);
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < PROBE_CHAINS; k++) x[k] = fma(x[k], a, b);
+    }
+    double s = 0;
+#pragma unroll
+    for (int k = 0; k < PROBE_CHAINS; k++) s += x[k];
+    // Never true for these inputs; keeps the chains live
+    if (s < -1.0) out[0] = s;
+}
+
+}  // namespace
+
 extern "C" {
 
 const char *b200_version(void) { return "pyfrb200 0.1 sm_103a"; }
@@ -173,6 +198,38 @@ int b200_graph_end_capture(void *stream, void **gexec) {
 int b200_graph_launch(void *gexec, void *stream) {
     return check_cuda(cudaGraphLaunch((cudaGraphExec_t)gexec, (cudaStream_t)stream),
                       "cudaGraphLaunch");
+}
+
+int b200_probe_fp64_fma(int iters, double *flops_per_s, void *stream) {
+    if (!flops_per_s || iters <= 0) return set_error(B200_ERR_ARG, "probe: bad arguments");
+    int dev, nsm;
+    int rc = check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+    if (rc) return rc;
+    rc = check_cuda(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev),
+                    "cudaDeviceGetAttribute");
+    if (rc) return rc;
+    const cudaStream_t st = (cudaStream_t)stream;
+    const int blocks = 8 * nsm, threads = 256;
+    cudaEvent_t e0, e1;
+    if ((rc = check_cuda(cudaEventCreate(&e0), "cudaEventCreate"))) return rc;
+    if ((rc = check_cuda(cudaEventCreate(&e1), "cudaEventCreate"))) {
+        cudaEventDestroy(e0);
+        return rc;
+    }
+    // One untimed launch, then the timed one
+    fp64_fma_probe_kernel<<<blocks, threads, 0, st>>>(nullptr, iters, 0.999999, 1e-6);
+    cudaEventRecord(e0, st);
+    fp64_fma_probe_kernel<<<blocks, threads, 0, st>>>(nullptr, iters, 0.999999, 1e-6);
+    cudaEventRecord(e1, st);
+    rc = check_cuda(cudaGetLastError(), "fp64 probe launch");
+    if (!rc) rc = check_cuda(cudaEventSynchronize(e1), "cudaEventSynchronize");
+    float ms = 0;
+    if (!rc) rc = check_cuda(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    *flops_per_s = 2.0 * PROBE_CHAINS * (double)iters * blocks * threads / (ms * 1e-3);
+    return B200_OK;
 }
 
 int b200_graph_destroy(void *gexec) {

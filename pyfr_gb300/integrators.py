@@ -647,14 +647,47 @@ class MixedRKIntegrator(RKVdH2Integrator):
         return Kernel(run, mats=[acc, bank[0], bank[1]], name='rkmixed',
                       meta=dict(kind='rkmixed', n=n))
 
+    def _fuse_stage(self, rhs, i, dt):
+        """Move the stage update of each element type into the epilogue of
+        the apply that writes its right-hand side (the fused divergence,
+        correction and negdivconf), when that apply is the last kernel to
+        touch it: R then never goes to memory.  Returns the kernel list and
+        the element types done."""
+        be, sysm = self.backend, self.system
+        if not be.fuse_stage or self.errest or sysm._ef:
+            return rhs, set()
+        tc = next((p for p in be._providers
+                   if hasattr(p, 'with_stage')), None)
+        nst = self.nstages
+        a = self.a[i] if i < nst - 1 else 0.0
+        dtdev = self._dt_dev if self.use_step_graph else None
+        out, done = list(rhs), set()
+        for j, bank in enumerate(sysm.ele_banks):
+            r = bank[1]
+            idx = [n for n, k in enumerate(out)
+                   if any(m is r for m in getattr(k, 'mats', ()))]
+            if not idx:
+                continue
+            k = out[idx[-1]]
+            if k.name != 'mul' or k.meta.get('out') is not r or \
+                    sum(1 for n in idx if out[n].meta.get('out') is r) != 1:
+                continue
+            kk = tc.with_stage(k, self.acc[j], bank[0], a, self.b[i],
+                               i == nst - 1, dt=dt, dtdev=dtdev)
+            if kk is not None:
+                out[idx[-1]] = kk
+                done.add(j)
+        return out, done
+
     def step_kernels(self, idx, dt):
         kl = []
         for i in range(self.nstages):
             kl.extend(self._time_kernels(i))
-            for g in self.system.rhs_graphs(0, 1):
-                kl.extend(g.klist)
+            rhs = [k for g in self.system.rhs_graphs(0, 1) for k in g.klist]
+            rhs, done = self._fuse_stage(rhs, i, dt)
+            kl.extend(rhs)
             kl.extend(self._stage_kernel(i, j, dt)
-                      for j in range(len(self.acc)))
+                      for j in range(len(self.acc)) if j not in done)
         # (the entropy filter of the new solution, merged back into FP64)
         post = self.system.postproc_kernels(0)
         if post:

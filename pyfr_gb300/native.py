@@ -685,6 +685,9 @@ def _read_soln(fname, mesh, prefix, allow_subset):
                 # Local elements of the file's element numbers
                 pos = np.full(int(max(gi.max(), nums.max())) + 1, -1)
                 pos[gi] = np.arange(len(gi))
+                if (pos[nums] < 0).any():
+                    raise ValueError(f'{ek}-idxs names elements that are '
+                                     'not in the mesh')
                 subset[et] = pos[nums]
                 rec = f[ek]
             else:
@@ -704,18 +707,22 @@ def _read_soln(fname, mesh, prefix, allow_subset):
     if not subset:
         return mesh, soln
     from dataclasses import replace
-    spts, eidxs = {}, {}
+    spts, eidxs, curved = {}, {}, {}
     for et in mesh.etypes:
         sel = subset.get(et)
         gi = (mesh.eidxs or {}).get(et)
         gi = np.arange(mesh.spts[et].shape[1]) if gi is None else gi
+        cv = (mesh.spts_curved or {}).get(et)
+        cv = np.zeros(mesh.spts[et].shape[1], bool) if cv is None else cv
         if sel is None:
-            spts[et], eidxs[et] = mesh.spts[et], gi
+            spts[et], eidxs[et], curved[et] = mesh.spts[et], gi, cv
         elif len(sel):
             spts[et], eidxs[et] = mesh.spts[et][:, sel], gi[sel]
+            # (curved flags follow their elements, as the reference's
+            # _subset_mesh keeps them: pyfr/readers/native.py:255-271)
+            curved[et] = cv[sel]
     sub = replace(mesh, spts=spts, eidxs=eidxs, con=None, bcon={},
-                  spts_curved={et: np.zeros(v.shape[1], bool)
-                               for et, v in spts.items()})
+                  spts_curved=curved)
     soln.data = {et: v for et, v in soln.data.items() if et in spts}
     return sub, soln
 

@@ -35,21 +35,11 @@ HERE = Path(__file__).resolve().parent
 REPO = HERE.parent.parent
 sys.path.insert(0, str(REPO))
 
-GAMMA = 1.4
-NPTS = 96
-RSOLVERS = ['rusanov', 'hllc', 'hll', 'roe', 'roem', 'exact']
-SENTINEL = -777.0
+from oracle.refkernels import (GAMMA, RK45_A, RK45_B,  # noqa: E402
+                               RK45_BHAT, standard_variants as variants)
 
-# RK45 (Kennedy-Carpenter 2N) coefficients as the reference states them
-# (pyfr/integrators/explicit/steppers.py:218-243)
-RK45_A = [970286171893 / 4311952581923, 6584761158862 / 12103376702013,
-          2251764453980 / 15575788980749, 26877169314380 / 34165994151039]
-RK45_B = [1153189308089 / 22510343858157, 1772645290293 / 4653164025191,
-          -1672844663538 / 4480602732383, 2114624349019 / 3568978502595,
-          5198255086312 / 14908931495163]
-RK45_BHAT = [1016888040809 / 7410784769900, 11231460423587 / 58533540763752,
-             -1563879915014 / 6823010717585, 606302364029 / 971179775848,
-             1097981568119 / 3980877426909]
+NPTS = 96
+SENTINEL = -777.0
 
 
 def states(rng, n, nd):
@@ -79,70 +69,6 @@ def normals(rng, n, nd):
 
 def smats(rng, n, nd):
     return np.eye(nd)[None] + 0.3*rng.normal(size=(n, nd, nd))
-
-
-def constants(visc=False, sutherland=False, beta=0.5, tau=0.1):
-    c = {'gamma': GAMMA}
-    if visc:
-        c |= {'mu': 0.05, 'Pr': 0.72, 'ldg-beta': beta, 'ldg-tau': tau}
-        if sutherland:
-            c |= {'cpTref': 3.0, 'cpTs': 1.2}
-    return c
-
-
-def variants():
-    """{cname: (module, kernel, tplargs, family)}."""
-    v = {}
-    for nd in (2, 3):
-        nv = nd + 2
-        base = dict(ndims=nd, nvars=nv, nverts=2**nd)
-        v[f'euler{nd}_tflux'] = (
-            'pyfr.solvers.euler.kernels.tflux', 'tflux',
-            base | dict(c=constants(), ktype='curved'), f'euler{nd}_elem')
-        v[f'euler{nd}_wavespeed'] = (
-            'pyfr.solvers.euler.kernels.wavespeed', 'wavespeed',
-            base | dict(c=constants(), ktype='curved'), f'euler{nd}_elem')
-        for rs in RSOLVERS:
-            v[f'euler{nd}_intcflux_{rs}'] = (
-                'pyfr.solvers.euler.kernels.intcflux', 'intcflux',
-                dict(ndims=nd, nvars=nv, rsolver=rs, c=constants(),
-                     p_min=5*np.finfo(float).eps), f'euler{nd}_iface')
-        for suth in (False, True):
-            name = f'ns{nd}_tflux' + ('_suth' if suth else '')
-            v[name] = (
-                'pyfr.solvers.navstokes.kernels.tflux', 'tflux',
-                base | dict(c=constants(True, suth), ktype='curved-fused',
-                            visc_corr='sutherland' if suth else 'none',
-                            shock_capturing='none'), f'ns{nd}_elem')
-        combos = [(rs, b, t) for rs in ('rusanov', 'hllc')
-                  for b in (0.5, 0.0, -0.5) for t in (0.1, 0.0)]
-        combos += [(rs, 0.5, 0.1) for rs in ('hll', 'roe', 'roem', 'exact')]
-        for rs, b, t in combos:
-            name = f'ns{nd}_intcflux_{rs}_b{b:+.1f}_t{t:.1f}'
-            v[name] = (
-                'pyfr.solvers.navstokes.kernels.intcflux', 'intcflux',
-                dict(ndims=nd, nvars=nv, rsolver=rs,
-                     c=constants(True, beta=b, tau=t), visc_corr='none',
-                     shock_capturing='none', p_min=5*np.finfo(float).eps),
-                f'ns{nd}_iface')
-        v[f'gradcoru{nd}'] = (
-            'pyfr.solvers.baseadvecdiff.kernels.gradcoru', 'gradcoru',
-            base | dict(ktype='curved'), f'ns{nd}_elem')
-    for b in (0.5, 0.0, -0.5):
-        v[f'intconu_b{b:+.1f}'] = (
-            'pyfr.solvers.navstokes.kernels.intconu', 'intconu',
-            dict(ndims=3, nvars=5, c=constants(True, beta=b)), 'conu')
-    v['negdivconf'] = (
-        'pyfr.solvers.baseadvec.kernels.negdivconf', 'negdivconf',
-        dict(ndims=3, nvars=5, src_macros=[]), 'negdivconf')
-    e = [b - bh for b, bh in zip(RK45_B, RK45_BHAT)]
-    for errest in (False, True):
-        for s in range(5):
-            v[f'rkvdh2_s{s}_e{int(errest)}'] = (
-                'pyfr.integrators.explicit.kernels.rkvdh2', 'rkvdh2',
-                dict(nvars=5, stage=s, nstages=5, errest=errest, a=RK45_A,
-                     b=RK45_B, e=e), 'rk')
-    return v
 
 
 def inputs(rng):

@@ -120,3 +120,33 @@ def test_mixed_mesh_connectivity():
                 ca = np.mod(va.mean(0) + 1e-9, 1.0)
                 cb = np.mod(vb.mean(0) + 1e-9, 1.0)
                 assert np.allclose(ca, cb)
+
+
+def test_affine_elements_detected():
+    """Metric terms are kept per element exactly when every element's
+    Jacobian is constant: uniform boxes, skewed parallelepipeds and linear
+    tetrahedra; not a box with one moved interior vertex, not prisms."""
+    from pyfr_gb300.backend.pointwise import affine, linear_metrics
+    from pyfr_gb300.mesh import mixed_box, periodic_box
+    from pyfr_gb300.shapes import get_shape
+
+    upts = get_shape('hex', 3, 'gauss-legendre', 'gauss-legendre').upts
+    m = periodic_box('hex', 4, -np.pi, np.pi)
+    v = m.spts['hex'].transpose(0, 2, 1)          # (nverts, ndims, neles)
+    assert affine(linear_metrics(v, upts)[0])
+
+    # A shear keeps elements affine; moving one vertex does not
+    sv = v.copy()
+    sv[:, 0] += 0.3*sv[:, 1]
+    assert affine(linear_metrics(sv, upts)[0])
+    sv[3, 1, 5] += 0.05
+    assert not affine(linear_metrics(sv, upts)[0])
+
+    mb = mixed_box(2, 0.0, 1.0, 'pri-tet')
+    for et, want in (('tet', True), ('pri', None)):
+        x = get_shape(et, 3, 'alpha-opt', 'alpha-opt').upts if et == 'tet' \
+            else get_shape(et, 3, 'alpha-opt~gauss-legendre-lobatto',
+                           'alpha-opt~gauss-legendre').upts
+        got = affine(linear_metrics(mb.spts[et].transpose(0, 2, 1), x)[0])
+        if want is not None:
+            assert got == want

@@ -449,3 +449,42 @@ def test_chosen_form_ns_antialiasing(built, mulprec):
     chosen.run_steps(10)
     (a,), (b,) = chosen.soln, plain.soln
     assert _l2rel(a, b) <= L2_TOL
+
+
+@pytest.mark.parametrize('case', ['vortex', 'tgv'])
+@pytest.mark.parametrize('graphs', [True, False])
+def test_stage_in_divergence_epilogue(built, case, graphs):
+    """The RK stage done in the epilogue of the divergence apply (the
+    right-hand side never stored) gives the solution of the separate stage
+    kernel bit for bit, and the stage kernel is gone from the step."""
+    from pyfr_gb300.backend import B200Backend
+    from pyfr_gb300.cases import euler_vortex, ns_tgv
+    from pyfr_gb300.integrators import MixedRKIntegrator
+    from pyfr_gb300.solvers.system import EulerSystem, NavierStokesSystem
+
+    sols = {}
+    for fuse in ('true', 'false'):
+        if case == 'vortex':
+            cfg, mesh = euler_vortex(n=10, order=3, dt=2e-3,
+                                     precision='single')
+            scls = EulerSystem
+        else:
+            cfg, mesh = ns_tgv(n=5, order=3, dt=5e-4, precision='single')
+            scls = NavierStokesSystem
+        cfg.set('backend-b200', 'mul-precision', 'bf16x3')
+        cfg.set('backend-b200', 'split-products', '5')
+        cfg.set('backend-b200', 'cuda-graphs', str(graphs).lower())
+        cfg.set('backend-b200', 'fuse-stage', fuse)
+        intg = MixedRKIntegrator(B200Backend(cfg), scls, mesh, cfg)
+        kl, _ = intg.step_kernels(intg.idxcurr, intg.dt)
+        names = [k.name for k in kl]
+        fused = [k for k in kl if k.meta.get('rk_stage')]
+        if fuse == 'true':
+            assert 'rkmixed' not in names
+            assert len(fused) == intg.nstages
+            assert fused[-1].meta['rk_stage'] == 2
+        else:
+            assert names.count('rkmixed') == intg.nstages and not fused
+        intg.run_steps(6)
+        (sols[fuse],) = intg.soln
+    assert np.array_equal(sols['true'], sols['false'])

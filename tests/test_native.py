@@ -463,3 +463,15 @@ def test_subset_solution(tmp_path):
     assert np.array_equal(s.data['quad'], u[:, :, loc])
     assert np.array_equal(sub.spts['quad'], m.spts['quad'][:, loc])
     assert sub.con is None
+
+    # Curved flags follow their elements
+    from dataclasses import replace
+    mc = replace(m, spts_curved={'quad': np.array([0, 1, 0, 1, 0, 0], bool)})
+    subc, _ = read_subset_soln(tmp_path / 's.pyfrs', mc)
+    assert subc.spts_curved['quad'].tolist() == [True, False, False]
+
+    # A file element number that the mesh lacks is an error
+    mcut = replace(m, spts={'quad': m.spts['quad'][:, :4]},
+                   eidxs={'quad': m.eidxs['quad'][:4]} if m.eidxs else None)
+    with pytest.raises(ValueError, match='not in the mesh'):
+        read_subset_soln(tmp_path / 's.pyfrs', mcut)

@@ -6,7 +6,7 @@ its step loop asynchronous cannot afford cudaFree's device-wide
 synchronisation.  An application whose own pool allocator owns all device
 memory cannot make a raw allocation.  The test calls it through the C ABI
 and checks it against b200_errest_f64, which takes caller-provided
-scratch.  It makes two calls in a row: the second is smaller, so stale
+scratch, and against a numpy restatement of the norm.  It makes two calls in a row: the second is smaller, so stale
 partials left by the first call must not leak into its result.  The file
 is collected last, so a run that stops at the first failure has already
 run every other test.
@@ -64,19 +64,38 @@ def _case(lib, nupts, nvars, neles, seed):
     curr = rng.normal(size=nupts*ld)
     err = 1e-6*rng.normal(size=nupts*ld)
     atol = np.linspace(1e-6, 4e-6, nvars)
-    return ld, [_dev(lib, a) for a in (curr, err, atol)]
+    host = (curr, err, atol)
+    return ld, host, [_dev(lib, a) for a in host]
+
+
+def _norm_numpy(curr, err, atol, rtol, uniform, nupts, nvars, neles, ld):
+    """The error norm restated with numpy: over the valid elements of
+    each point and variable (AoSoA, blocks of 32 elements), the sum of
+    (err/(atol_v + rtol |curr|))^2, or the largest |.| when uniform."""
+    e = np.arange(neles)
+    idx = ((e // 32)*32*nvars + e % 32)[None, :] + \
+        (32*np.arange(nvars))[:, None]              # (nvars, neles)
+    idx = np.arange(nupts)[:, None, None]*ld + idx[None]
+    q = err[idx]/(atol[None, :, None] + rtol*np.abs(curr[idx]))
+    return np.abs(q).max() if uniform else np.sum(q*q)
 
 
 @pytest.mark.parametrize('uniform', [0, 1])
 def test_static_errest_matches_scratch_errest(lib, uniform):
-    cases = [(64, 5, 20000, 11, 1000), (16, 4, 333, 12, 7)]
+    # (nupts, nvars, neles, seed, nblocks): the second call is smaller than
+    # the first; nblocks = 4096 fills the whole static array; the last case
+    # has fewer work items (nupts x element blocks) than partial sums
+    cases = [(64, 5, 20000, 11, 1000), (16, 4, 333, 12, 7),
+             (27, 5, 40000, 13, MAX_BLOCKS), (8, 5, 100, 14, 1000)]
     out = _dev(lib, np.zeros(2))
     scratch = _dev(lib, np.zeros(MAX_BLOCKS))
     bufs = []
     try:
         for nupts, nvars, neles, seed, nblocks in cases:
-            ld, (curr, err, atol) = _case(lib, nupts, nvars, neles, seed)
+            ld, host, (curr, err, atol) = _case(lib, nupts, nvars, neles,
+                                                seed)
             bufs += [curr, err, atol]
+            want = _norm_numpy(*host, 1e-5, uniform, nupts, nvars, neles, ld)
 
             assert lib.b200_errest_f64(nupts, nvars, neles, ld, curr, err,
                                        atol, 1e-5, uniform, scratch, nblocks,
@@ -90,6 +109,7 @@ def test_static_errest_matches_scratch_errest(lib, uniform):
 
             assert ref > 0
             assert abs(got - ref) <= RTOL*abs(ref)
+            assert abs(got - want) <= RTOL*abs(want), (got, want)
     finally:
         for p in bufs + [out, scratch]:
             lib.b200_free(p)
