@@ -584,6 +584,21 @@ int b200_axnpby_f64(int64_t n, int nv, double *x0, const double *const *xs, cons
 int b200_axnpby_f32(int64_t n, int nv, float *x0, const float *const *xs, const double *a,
                     void *stream);
 
+/* Scaled linear combination, per variable v of each value (AoSoA with
+ * nvars variables): the terms a[k]*x_k of the registers k whose bit is set
+ * in in_mask are multiplied by in_scale[v], the sum by out_scale[v] (null:
+ * no scaling); a[0] = 0 stores the sum of the terms k >= 1, a[0] = 1 adds
+ * it to x0, any other a[0] stores the sum over all terms including x0.
+ * in_scale and out_scale are host arrays of nvars (<= 16) doubles;
+ * pyfr/backends/base/blasext.py:9-19 with in_scale, in_scale_idxs and
+ * out_scale (pyfr/backends/cuda/kernels/axnpby.mako). */
+int b200_axnpby_scaled_f64(int64_t n, int nv, int nvars, double *x0, const double *const *xs,
+                           const double *a, const double *in_scale, unsigned in_mask,
+                           const double *out_scale, void *stream);
+int b200_axnpby_scaled_f32(int64_t n, int nv, int nvars, float *x0, const float *const *xs,
+                           const double *a, const double *in_scale, unsigned in_mask,
+                           const double *out_scale, void *stream);
+
 /* PI-controller error norm: out[0] = sum (or max when uniform != 0) over
  * the valid points of (err/(atol[v] + rtol*|curr|))^2 (|.| when uniform);
  * atol_dev holds nvars device doubles, scratch at least one double per

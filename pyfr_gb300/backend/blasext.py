@@ -47,16 +47,38 @@ class BlasExtKernels:
         return 'f64' if self.backend.fpdtype == np.float64 else 'f32'
 
     def axnpby(self, *arr, in_scale=(), in_scale_idxs=(), out_scale=()):
+        """x0 <- a0 x0 + sum a_i x_i (pyfr/backends/base/blasext.py:9-19),
+        with the coefficients bound at run time (a0, a1, ...).  in_scale
+        and out_scale are per-variable factors (one per variable of the
+        registers' io-shape (..., nvars, neles)): in_scale multiplies the
+        terms of the registers listed in in_scale_idxs, out_scale the
+        sum."""
         if any(arr[0].traits != x.traits for x in arr[1:]):
             raise ValueError('Incompatible matrix types')
-        if in_scale or out_scale:
-            raise NotImplementedError('Scaled axnpby is not provided')
 
         be, nv = self.backend, len(arr)
         n = arr[0].nrow*arr[0].leaddim
-        fn = getattr(be.lib, f'axnpby_{self._sfx}')
         ptrs = (C.c_void_p*nv)(*[a.data for a in arr])
         coeffs = (C.c_double*nv)()
+        if in_scale or out_scale:
+            nvars = arr[0].ioshape[-2]
+            for sc in (in_scale, out_scale):
+                if sc and len(sc) != nvars:
+                    raise ValueError('Scales need one value per variable')
+            if in_scale and not in_scale_idxs:
+                raise ValueError('in_scale needs in_scale_idxs')
+            if any(not 0 <= k < nv for k in in_scale_idxs):
+                raise ValueError('in_scale_idxs out of range')
+            insc = (C.c_double*nvars)(*in_scale) if in_scale else None
+            outsc = (C.c_double*nvars)(*out_scale) if out_scale else None
+            mask = sum(1 << k for k in in_scale_idxs) if in_scale else 0
+            fs = getattr(be.lib, f'axnpby_scaled_{self._sfx}')
+
+            def fn(n, nv, x0, ptrs, coeffs, stream):
+                fs(n, nv, nvars, x0, ptrs, coeffs, insc, mask, outsc, stream)
+            keep = [insc, outsc]
+        else:
+            fn, keep = getattr(be.lib, f'axnpby_{self._sfx}'), []
 
         def run(stream, **kw):
             for i in range(nv):
@@ -65,7 +87,7 @@ class BlasExtKernels:
 
         return BindableKernel(run, [f'a{i}' for i in range(nv)],
                               {f'a{i}': 0.0 for i in range(nv)},
-                              mats=list(arr), misc=[ptrs, coeffs],
+                              mats=list(arr), misc=[ptrs, coeffs, *keep],
                               name='axnpby')
 
     def copy(self, dst, src):
@@ -88,16 +110,43 @@ class BlasExtKernels:
 
         return Kernel(run, mats=[m], name='zero')
 
+    # The error norm of PyFR's PI controller as a reduction expression
+    # (pyfr/integrators/controllers.py:105-117): squared and summed for the
+    # l2 norm, absolute and maximised for the uniform norm
+    _ERR_EXPR = 'err/(atol+rtol*fabs(curr))'
+
+    @classmethod
+    def _errest_form(cls, rop, exprs, vvars, svars, pvars):
+        """'l2' or 'uniform' when (rop, exprs, ...) is the PI controller's
+        error norm over registers curr and err, else None."""
+        if len(exprs) != 1 or set(vvars) != {'curr', 'err'} or \
+                list(svars or []) != ['rtol'] or set(pvars or {}) != {'atol'}:
+            return None
+        e, q = exprs[0].replace(' ', ''), cls._ERR_EXPR
+        if rop == 'sum' and e == f'({q})*({q})':
+            return 'l2'
+        if rop == 'max' and e == f'fabs({q})':
+            return 'uniform'
+        return None
+
     def reduction(self, rop, exprs, vvars, svars=None, pvars=None):
-        """``reduction(rop, exprs, vvars)`` of
-        pyfr/backends/base/blasext.py:21-46 for the form the CFL controller
-        uses (pyfr/solvers/baseadvec/system.py:48-52): the maximum of one
-        variable, ``exprs == [name]`` with ``vvars == {name: matrix}``.
-        Other operators and expressions are not provided."""
+        """``reduction(rop, exprs, vvars, svars, pvars)`` of
+        pyfr/backends/base/blasext.py:21-46 in the forms that PyFR's
+        explicit path makes: the PI controller's error norm (l2 or
+        uniform; ``retval`` is the sum of squares or the largest value, the
+        scalar ``rtol`` bound at run time, ``atol`` one value per variable)
+        and the maximum of one variable (the CFL controller's wave speed,
+        pyfr/solvers/baseadvec/system.py:48-52).  Other expressions are not
+        provided."""
+        norm = self._errest_form(rop, exprs, vvars, svars, pvars)
+        if norm is not None:
+            return self.errest(vvars['curr'], vvars['err'],
+                               list(np.ravel(pvars['atol'])), norm=norm)
         if rop != 'max' or len(exprs) != 1 or exprs[0] not in vvars or \
                 len(vvars) != 1 or svars or pvars:
-            raise NotImplementedError('Only the maximum of one variable is '
-                                      'provided')
+            raise NotImplementedError('Reductions other than the error norm '
+                                      'and the maximum of one variable are '
+                                      'not provided')
         be, x = self.backend, vvars[exprs[0]]
         n = x.nrow*x.leaddim if x.nrow > 1 else x.ncol
         fn = be.lib.reduce_max_f64 if x.dtype == np.float64 else \

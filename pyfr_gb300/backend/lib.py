@@ -99,6 +99,8 @@ def _sig_pointwise(fp):
         'rkvdh2_dt': [i64, i32, i32, i32, vp, f64, f64, f64, vp, vp, vp, vp,
                       vp],
         'axnpby': [i64, i32, vp, C.POINTER(vp), C.POINTER(f64), vp],
+        'axnpby_scaled': [i64, i32, i32, vp, C.POINTER(vp), C.POINTER(f64),
+                          C.POINTER(f64), C.c_uint, C.POINTER(f64), vp],
         'errest': [i32, i32, i64, i64, vp, vp, vp, f64, i32, vp, i32, vp, vp],
         'mul': [vp, vp, i64, vp, i64, i64, fp, fp, vp],
         'wavespeed': [i32, i32, i64, i32, C.POINTER(Gas), vp, i64, vp, i64,

@@ -190,11 +190,47 @@ axnpby_kernel(int64_t n, int nv, T *__restrict__ x0, AxnpbyArgs<T> args) {
     }
 }
 
+// The scaled form (pyfr/backends/cuda/kernels/axnpby.mako with in_scale,
+// in_scale_idxs and out_scale; pyfr/backends/base/makoutil.py:43-58): with
+// v the variable of the value (AoSoA: (i mod 32*nvars)/32), the terms of
+// the registers whose bit is set in in_mask are multiplied by in_scale[v]
+// and the sum by out_scale[v]; a0 = 0 stores, a0 = 1 adds the sum of the
+// other terms, any other a0 includes x0 among the terms.
+constexpr int MAX_SCALE_VARS = 16;
+
+template <typename T>
+struct AxnpbyScale {
+    T in[MAX_SCALE_VARS], out[MAX_SCALE_VARS];
+    unsigned in_mask;
+    int has_out, nvars;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(BX_BLOCK)
+axnpby_scaled_kernel(int64_t n, int nv, T *__restrict__ x0, AxnpbyArgs<T> args,
+                     AxnpbyScale<T> sc) {
+    const T a0 = args.a[0];
+    const int first = (a0 == T(0) || a0 == T(1)) ? 1 : 0;
+    for (int64_t i = (int64_t)blockIdx.x * BX_BLOCK + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * BX_BLOCK) {
+        const int v = (int)((i % (32 * sc.nvars)) / 32);
+        T acc = 0;
+        for (int k = first; k < nv; k++) {
+            const T xk = k ? args.x[k][i] : x0[i];
+            acc += ((sc.in_mask >> k) & 1) ? args.a[k] * sc.in[v] * xk : args.a[k] * xk;
+        }
+        if (sc.has_out) acc = sc.out[v] * acc;
+        if (a0 == T(1))
+            x0[i] += acc;
+        else
+            x0[i] = acc;
+    }
+}
+
 // Block partials of the error norm over the points of one element type;
 // layout (nupts, nvars, neles) AoSoA with leading dimension ld.  One warp
 // takes one (point, 32-element block) pair per iteration, lane = element
-// within the block; padding elements past neles hold zero error and add
-// nothing.  The quotient err/(atol + rtol*|u|) uses a reciprocal refined
+// within the block; lanes of padding elements past neles are skipped.  The quotient err/(atol + rtol*|u|) uses a reciprocal refined
 // by two Newton-Raphson steps, r <- r + r*(1 - d*r), from a single-
 // precision estimate (relative error about 2^-23 before, below 2^-52
 // after): GB300's FP64 unit is narrow and an IEEE double division costs
@@ -221,7 +257,11 @@ errest_partial_kernel(int nupts, int nvars, int64_t neles, int64_t ld, const T *
     double acc = 0;
     for (int64_t q = warp; q < nwork; q += nwarps) {
         const int upt = (int)(q / nblk);
-        const int64_t base = upt * ld + (q - upt * nblk) * 32 * nvars + lane;
+        const int64_t blk = q - upt * nblk;
+        // Padding lanes of the last element block add nothing, whatever
+        // they hold
+        if (blk * 32 + lane >= neles) continue;
+        const int64_t base = upt * ld + blk * 32 * nvars + lane;
         const double c0 = (double)curr[base], e0 = (double)err[base];
         for (int v = 0; v < nvars; v++) {
             const int64_t ix = base + v * 32;
@@ -346,6 +386,35 @@ int axnpby(int64_t n, int nv, T *x0, const T *const *xs, const double *a, cudaSt
     }
     axnpby_kernel<T><<<grid_for(n), BX_BLOCK, 0, s>>>(n, nv, x0, args);
     B200_CHECK_LAUNCH("axnpby");
+    return B200_OK;
+}
+
+template <typename T>
+int axnpby_scaled(int64_t n, int nv, int nvars, T *x0, const T *const *xs, const double *a,
+                  const double *in_scale, unsigned in_mask, const double *out_scale,
+                  cudaStream_t s) {
+    if (n <= 0) return B200_OK;
+    if (nv < 1 || nv > MAX_AXNPBY)
+        return b200::set_error(B200_ERR_ARG, "axnpby_scaled: nv=%d out of range", nv);
+    if (nvars < 1 || nvars > MAX_SCALE_VARS)
+        return b200::set_error(B200_ERR_ARG, "axnpby_scaled: nvars=%d out of range", nvars);
+    if ((in_mask >> nv) || (in_mask && !in_scale))
+        return b200::set_error(B200_ERR_ARG, "axnpby_scaled: bad input-scale mask");
+    AxnpbyArgs<T> args = {};
+    for (int k = 0; k < nv; k++) {
+        args.x[k] = k ? xs[k] : x0;
+        args.a[k] = (T)a[k];
+    }
+    AxnpbyScale<T> sc = {};
+    sc.nvars = nvars;
+    sc.in_mask = in_mask;
+    sc.has_out = out_scale != nullptr;
+    for (int v = 0; v < nvars; v++) {
+        sc.in[v] = in_scale ? (T)in_scale[v] : T(1);
+        sc.out[v] = out_scale ? (T)out_scale[v] : T(1);
+    }
+    axnpby_scaled_kernel<T><<<grid_for(n), BX_BLOCK, 0, s>>>(n, nv, x0, args, sc);
+    B200_CHECK_LAUNCH("axnpby_scaled");
     return B200_OK;
 }
 
@@ -520,6 +589,20 @@ int b200_axnpby_f64(int64_t n, int nv, double *x0, const double *const *xs, cons
 int b200_axnpby_f32(int64_t n, int nv, float *x0, const float *const *xs, const double *a,
                     void *stream) {
     return axnpby<float>(n, nv, x0, xs, a, (cudaStream_t)stream);
+}
+
+int b200_axnpby_scaled_f64(int64_t n, int nv, int nvars, double *x0, const double *const *xs,
+                           const double *a, const double *in_scale, unsigned in_mask,
+                           const double *out_scale, void *stream) {
+    return axnpby_scaled<double>(n, nv, nvars, x0, xs, a, in_scale, in_mask, out_scale,
+                                 (cudaStream_t)stream);
+}
+
+int b200_axnpby_scaled_f32(int64_t n, int nv, int nvars, float *x0, const float *const *xs,
+                           const double *a, const double *in_scale, unsigned in_mask,
+                           const double *out_scale, void *stream) {
+    return axnpby_scaled<float>(n, nv, nvars, x0, xs, a, in_scale, in_mask, out_scale,
+                                (cudaStream_t)stream);
 }
 
 int b200_errest_f64(int nupts, int nvars, int64_t neles, int64_t ld, const double *curr,

@@ -131,6 +131,25 @@ __device__ __forceinline__ uint32_t smem_addr(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
 }
 
+// Shared-memory accesses by 32-bit shared address, so that they are
+// shared-window loads and stores whatever the compiler infers about a
+// pointer's address space
+__device__ __forceinline__ float lds_f32(uint32_t a) {
+    float x;
+    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(x) : "r"(a) : "memory");
+    return x;
+}
+
+__device__ __forceinline__ void sts_f32(uint32_t a, float x) {
+    asm volatile("st.shared.f32 [%0], %1;" :: "r"(a), "f"(x) : "memory");
+}
+
+__device__ __forceinline__ void sts_v4(uint32_t a, uint32_t x, uint32_t y, uint32_t z,
+                                       uint32_t w) {
+    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};"
+                 :: "r"(a), "r"(x), "r"(y), "r"(z), "r"(w) : "memory");
+}
+
 __device__ __forceinline__ void bar_init(uint32_t bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(bar), "r"(count));
 }
@@ -385,12 +404,12 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
                 // group at the named barrier below, so none of them waits
                 // there forever)
                 ok = bar_wait(bar(BAR_LOADED + s), (uint32_t)((j / NS) & 1), abort_flag, p.err, 2);
-                unsigned char *stage = smem + L.ring + s * CHUNK32;
-                const float *b32 = reinterpret_cast<const float *>(stage);
+                const uint32_t stage = sbase + L.ring + (uint32_t)s * CHUNK32;
                 float x[KC];
                 if (ok) {
 #pragma unroll
-                    for (int r = 0; r < KC; r++) x[r] = b32[r * TCOLS + cc];
+                    for (int r = 0; r < KC; r++)
+                        x[r] = lds_f32(stage + (uint32_t)(r * TCOLS + cc) * 4);
                 }
                 asm volatile("bar.sync %0, %1;" :: "r"(gbar), "n"(NCONV / 2) : "memory");
                 if (!ok || *abort_flag) {
@@ -402,9 +421,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
 #pragma unroll
                     for (int q = 0; q < KC / 4; q++) {
                         const uint32_t off = coff + (uint32_t)q * LBO;
-                        *reinterpret_cast<uint4 *>(stage + off) =
-                            make_uint4(to_tf32(x[4 * q]), to_tf32(x[4 * q + 1]),
-                                       to_tf32(x[4 * q + 2]), to_tf32(x[4 * q + 3]));
+                        sts_v4(stage + off, to_tf32(x[4 * q]), to_tf32(x[4 * q + 1]),
+                               to_tf32(x[4 * q + 2]), to_tf32(x[4 * q + 3]));
                     }
                 }
 #pragma unroll
@@ -421,9 +439,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
                         lw[jj / 2] = *reinterpret_cast<const uint32_t *>(&l2);
                     }
                     const uint32_t off = coff + (uint32_t)q * LBO;
-                    *reinterpret_cast<uint4 *>(stage + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-                    *reinterpret_cast<uint4 *>(stage + CHUNK16 + off) =
-                        make_uint4(lw[0], lw[1], lw[2], lw[3]);
+                    sts_v4(stage + off, hw[0], hw[1], hw[2], hw[3]);
+                    sts_v4(stage + CHUNK16 + off, lw[0], lw[1], lw[2], lw[3]);
                 }
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 bar_arrive(bar(BAR_CONVERTED + s));
@@ -624,9 +641,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
                 }
                 asm volatile("bar.sync %0, %1;" :: "r"(EPI_BARRIER + half), "n"(128) : "memory");
                 const uint32_t boff = L.epi + (uint32_t)(half * eb + sb) * EPI_BUF;
-                float *buf = reinterpret_cast<float *>(smem + boff) + quad * 32 + lane;
+                const uint32_t buf = sbase + boff + (uint32_t)(quad * 32 + lane) * 4;
 #pragma unroll
-                for (int r = 0; r < 32; r++) buf[r * TCOLS] = f[r] * __uint_as_float(v[r]);
+                for (int r = 0; r < 32; r++)
+                    sts_f32(buf + (uint32_t)(r * TCOLS) * 4, f[r] * __uint_as_float(v[r]));
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 asm volatile("bar.sync %0, %1;" :: "r"(EPI_BARRIER + half), "n"(128) : "memory");
                 // (columns past ncol are clipped by the TMA)
