@@ -64,11 +64,12 @@ enum {
     B200_BC_SUB_IN_FTPTTANG = 8,  /* subsonic inflow, given total state and direction (NS) */
     B200_BC_SUB_OUT_FP = 9        /* subsonic outflow, given pressure (NS) */
 };
-/* One instruction of a boundary-value program: postfix code evaluated per
- * boundary point on a stack of at most 16 values.  Opcodes: 0 push val,
- * 1-3 push x, y, z of the point, 4 push t, 5-9 + - * / pow, 10 negate,
- * 11-23 sin cos tan exp log sqrt tanh fabs asin acos atan sinh cosh,
- * 24-26 atan2 fmin fmax, 27-28 floor ceil. */
+/* One instruction of a boundary-value or source-term program: postfix
+ * code evaluated per point on a stack of at most 16 values.  Opcodes:
+ * 0 push val, 1-3 push x, y, z of the point, 4 push t, 5-9 + - * / pow,
+ * 10 negate, 11-23 sin cos tan exp log sqrt tanh fabs asin acos atan sinh
+ * cosh, 24-26 atan2 fmin fmax, 27-28 floor ceil, 29 push solution
+ * variable pad (source terms only). */
 typedef struct {
     int op, pad;
     double val;
@@ -478,6 +479,42 @@ int b200_negdivconf_f64(int nvars, int nupts, int64_t neles, double *r, int64_t 
                         const double *rcpdjac, int64_t ldj, void *stream);
 int b200_negdivconf_f32(int nvars, int nupts, int64_t neles, float *r, int64_t ldr,
                         const float *rcpdjac, int64_t ldj, void *stream);
+
+/* Source terms: the [solver-plugin-source] expressions of each variable
+ * (pyfr/plugins/source.py:15-31, pyfr/plugins/kernels/source.mako) as
+ * programs of the point's coordinates ploc, the time and the solution u,
+ * evaluated at every solution point by
+ *   mode B200_SRC_NEGDIVCONF: R <- -R/|J| + src (negdivconf with its source
+ *     macros, pyfr/solvers/baseadvec/kernels/negdivconf.mako:7-22);
+ *   mode B200_SRC_ADD: R <- R + src (after an operator apply that already
+ *     formed -R/|J|; rcpdjac unused);
+ *   mode B200_SRC_EVAL: R <- src (evalsrcmacros,
+ *     pyfr/solvers/baseadvec/kernels/evalsrcmacros.mako:7-22; u may be R).
+ * prog holds the programs, expr_start/expr_len each variable's (length 0:
+ * no source for it); ploc is (nupts x ndims x neles) with leading
+ * dimension ldp and u (nupts x nvars x neles) with ldu, both in the
+ * kernels' precision and AoSoA layout, u NULL when no program reads it;
+ * the time is t_dev[0] (device memory) when t_dev is not NULL, else t.
+ * nvars <= 8. */
+#define B200_SRC_NEGDIVCONF 0
+#define B200_SRC_ADD 1
+#define B200_SRC_EVAL 2
+typedef struct {
+    const b200_bcop_t *prog;
+    int expr_start[8], expr_len[8];
+    const void *ploc;
+    int64_t ldp;
+    const void *u;
+    int64_t ldu;
+    double t;
+    const double *t_dev;
+} b200_src_t;
+int b200_srcterms_f64(int mode, int ndims, int nvars, int nupts, int64_t neles, double *r,
+                      int64_t ldr, const double *rcpdjac, int64_t ldj, const b200_src_t *src,
+                      void *stream);
+int b200_srcterms_f32(int mode, int ndims, int nvars, int nupts, int64_t neles, float *r,
+                      int64_t ldr, const float *rcpdjac, int64_t ldj, const b200_src_t *src,
+                      void *stream);
 
 /* ---- interface kernels over the interior flux-point pairs ------------ */
 /* Euler common normal flux, written +/- to both sides;

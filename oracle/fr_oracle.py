@@ -20,6 +20,8 @@ arithmetic of the reference's OpenMP/CUDA kernels on this path:
   viscous flux               pyfr/solvers/navstokes/kernels/flux.mako:48-105
   gradient transform         pyfr/solvers/baseadvecdiff/kernels/transform_grad.mako:3-10
   negdivconf                 pyfr/solvers/baseadvec/kernels/negdivconf.mako:7-22
+  source terms               pyfr/plugins/kernels/source.mako:3-7,
+                             pyfr/plugins/source.py:15-31
   flux anti-aliasing         pyfr/solvers/baseadvec/elements.py:79-90
   rkvdh2 / RK45              pyfr/integrators/explicit/kernels/rkvdh2.mako:4-31,
                              pyfr/integrators/explicit/steppers.py:165-243
@@ -623,6 +625,34 @@ def smats_djac(verts, pts):
 
 
 # ---------------------------------------------------------------------------
+# Source terms
+# ---------------------------------------------------------------------------
+
+_SRC_FUNCS = {'sin': np.sin, 'cos': np.cos, 'tan': np.tan, 'exp': np.exp,
+              'log': np.log, 'sqrt': np.sqrt, 'tanh': np.tanh,
+              'sinh': np.sinh, 'cosh': np.cosh, 'asin': np.arcsin,
+              'acos': np.arccos, 'atan': np.arctan, 'atan2': np.arctan2,
+              'pow': np.power, 'fabs': np.abs, 'floor': np.floor,
+              'ceil': np.ceil, 'min': np.minimum, 'max': np.maximum,
+              'fmin': np.fmin, 'fmax': np.fmax}
+
+
+def source_terms(exprs, t, u, ploc):
+    """The source plugin's terms: src[i] = exprs[i] at every point
+    (pyfr/plugins/kernels/source.mako:3-7 expanded in
+    pyfr/solvers/baseadvec/kernels/negdivconf.mako:13-19).  ``exprs`` are
+    the kernel's C expressions of ploc[j], u[j] and t (as the source plugin
+    writes them, pyfr/plugins/source.py:15-24); u is (nvars, ...) and ploc
+    (ndims, ...).  Variables past len(exprs) get no source."""
+    env = dict(_SRC_FUNCS, ploc=ploc, u=u, t=t)
+    out = np.zeros_like(np.asarray(u, dtype=float))
+    for i, e in enumerate(exprs):
+        out[i] = eval(compile(e, '<source>', 'eval'),
+                      {'__builtins__': {}}, env)
+    return out
+
+
+# ---------------------------------------------------------------------------
 # The discretisation
 # ---------------------------------------------------------------------------
 
@@ -751,7 +781,22 @@ class Discretisation:
         # f: (ndims, nupts, nvars, neles) physical -> reference (smats)
         return np.einsum('pike,kpve->ipve', self.smats_u, f)
 
-    def rhs_euler(self, u, c, rsolver='rusanov', t=0.0):
+    @property
+    def ploc_upts(self):
+        """Physical coordinates of the solution points (nupts, ndims,
+        neles)."""
+        return np.einsum('pv,ved->pde',
+                         shape_values(self.upts, self.ndims), self.verts)
+
+    def _add_src(self, r, u, src, t):
+        """r + the source terms ``src`` (expressions) at time t."""
+        if not src:
+            return r
+        s = source_terms(src, t, u.transpose(1, 0, 2),
+                         self.ploc_upts.transpose(1, 0, 2))
+        return r + s.transpose(1, 0, 2)
+
+    def rhs_euler(self, u, c, rsolver='rusanov', t=0.0, src=None):
         gamma = c['gamma']
         nd = self.ndims
         bcs = self._bcs_at(t)
@@ -780,17 +825,17 @@ class Discretisation:
             r = self.apply(self.aa['M1329'],
                            ft.reshape(nd*len(self.aa['qpts']), -1, self.neles))
             r += self.apply(self.ops['M3'], uf)
-            return -r/self.djac_u[:, None, :]
+            return self._add_src(-r/self.djac_u[:, None, :], u, src, t)
 
         fp, _, _ = inviscid_flux(u.transpose(1, 0, 2), gamma)   # (nd, nv, p, e)
         ft = self._transform_flux(fp.transpose(0, 2, 1, 3))
 
         r = self.apply(self.ops['M132'], ft.reshape(nd*self.nupts, -1, self.neles))
         r += self.apply(self.ops['M3'], uf)
-        return -r/self.djac_u[:, None, :]
+        return self._add_src(-r/self.djac_u[:, None, :], u, src, t)
 
     def rhs_ns(self, u, c, rsolver='rusanov', grads_out=None, av=None,
-               t=0.0):
+               t=0.0, src=None):
         """av: the artificial-viscosity parameters of shock_sensor and
         artvisc_points (pyfr/solvers/baseadvecdiff/artvisc.py), or None."""
         gamma, beta, tau = c['gamma'], c['ldg-beta'], c['ldg-tau']
@@ -880,7 +925,7 @@ class Discretisation:
         else:
             r = self.apply(self.ops['M132'], ft.reshape(nd*nupts, -1, ne))
         r += self.apply(self.ops['M3'], uf)
-        return -r/self.djac_u[:, None, :]
+        return self._add_src(-r/self.djac_u[:, None, :], u, src, t)
 
 
 def shock_sensor(u, av):

@@ -52,6 +52,44 @@ RK45_BHAT = [1016888040809 / 7410784769900, 11231460423587 / 58533540763752,
              1097981568119 / 3980877426909]
 
 
+# A [solver-plugin-source] section exercising every kind of term the source
+# plugin substitutes: coordinates, conserved variables, the time, a
+# constant, abs and pi (pyfr/plugins/source.py:15-24)
+SOURCE_OPTS = {'rho': '0.1*sin(x)*cos(y) + 0.01*t',
+               'rhou': '-0.2*rhou*exp(-z*z) + pow(abs(rho), 0.5)',
+               'rhov': 'mu*(x + y)/(1 + z*z) - 2*t*t',
+               'rhow': 'min(rhov, y) - max(E, 0.5)*1e-3',
+               'E': 'atan2(y, x)*t + tanh(E)*0.1 + pi/4'}
+SOURCE_CONSTS = {'mu': '0.05'}
+CONVARS3 = ['rho', 'rhou', 'rhov', 'rhow', 'E']
+
+
+def _reference_module(name, relpath):
+    """A module of the reference loaded from its file (importing it as a
+    package member would run the package's __init__)."""
+    import importlib.util
+    if name not in sys.modules:
+        path = os.path.join(reference_root(), relpath)
+        spec = importlib.util.spec_from_file_location(name, path)
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules[name] = mod
+        spec.loader.exec_module(mod)
+    return sys.modules[name]
+
+
+def source_exprs(opts=SOURCE_OPTS, consts=SOURCE_CONSTS, convars=CONVARS3):
+    """The source plugin's kernel expressions for ``opts``, made by the
+    reference's own substitution (pyfr/plugins/source.py:15-24 with
+    pyfr/inifile.py process_expr)."""
+    process_expr = _reference_module('pyfr.inifile',
+                                     'pyfr/inifile.py').process_expr
+    subs = dict(consts)
+    subs |= dict(x='ploc[0]', y='ploc[1]', z='ploc[2]')
+    subs |= dict(abs='fabs', pi=math.pi)
+    subs |= {v: f'u[{i}]' for i, v in enumerate(convars)}
+    return [process_expr(opts[v], subs) for v in convars]
+
+
 def constants(visc=False, sutherland=False, beta=0.5, tau=0.1):
     c = {'gamma': GAMMA}
     if visc:
@@ -106,6 +144,15 @@ def standard_variants():
     v['negdivconf'] = (
         'pyfr.solvers.baseadvec.kernels.negdivconf', 'negdivconf',
         dict(ndims=3, nvars=5, src_macros=[]), 'negdivconf')
+    srctp = dict(ndims=3, nvars=5,
+                 src_macros=[('pyfr.plugins.kernels.source', 'source')],
+                 src_exprs=source_exprs())
+    v['negdivconf_src'] = (
+        'pyfr.solvers.baseadvec.kernels.negdivconf', 'negdivconf', srctp,
+        'src')
+    v['evalsrcmacros_src'] = (
+        'pyfr.solvers.baseadvec.kernels.evalsrcmacros', 'evalsrcmacros',
+        srctp, 'src')
     e = [b - bh for b, bh in zip(RK45_B, RK45_BHAT)]
     for errest in (False, True):
         for s in range(5):

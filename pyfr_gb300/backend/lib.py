@@ -62,6 +62,18 @@ class BC(C.Structure):
                 ('t_dev', C.c_void_p)]
 
 
+class Src(C.Structure):
+    """``b200_src_t``"""
+    _fields_ = [('prog', C.c_void_p), ('expr_start', i32*8),
+                ('expr_len', i32*8), ('ploc', C.c_void_p), ('ldp', i64),
+                ('u', C.c_void_p), ('ldu', i64), ('t', f64),
+                ('t_dev', C.c_void_p)]
+
+
+# Source-term kernel modes (B200_SRC_*)
+SRC_NEGDIVCONF, SRC_ADD, SRC_EVAL = 0, 1, 2
+
+
 class EF(C.Structure):
     """``b200_ef_t``"""
     _fields_ = [('ndims', i32), ('nupts', i32), ('nfpts', i32),
@@ -88,6 +100,8 @@ def _sig_pointwise(fp):
         'gradcoru': [i32, i32, i64, i32, vp, i64, vp, i64, vp, i64, vp, i64,
                      vp, i64, vp],
         'negdivconf': [i32, i32, i64, vp, i64, vp, i64, vp],
+        'srcterms': [i32, i32, i32, i32, i64, vp, i64, vp, i64,
+                     C.POINTER(Src), vp],
         'intcflux_euler': [i32, i64, i32, f64, f64, vp, vp, vp, vp, i32, vp,
                            i64, i32, vp],
         'intcflux_ns': [i32, i64, i32, C.POINTER(Gas), f64, f64, vp, vp, vp,

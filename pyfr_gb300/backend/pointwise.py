@@ -317,10 +317,89 @@ class PointwiseKernelProvider:
                       meta=dict(kind='gradcoru', tplargs=tplargs, dims=dims,
                                 gradu=gradu))
 
+    def _source(self, tplargs, ploc, u):
+        """The source macros of ``tplargs`` as a ``b200_src_t`` and the
+        program matrix it points at, or (None, None) without any.  The one
+        macro provided is the source plugin's (pyfr/plugins/source.py:8-31,
+        pyfr/plugins/kernels/source.mako): src[i] += src_exprs[i]."""
+        from pyfr_gb300.backend.lib import Src
+        from pyfr_gb300.bcexpr import OPS, BCExpr, pack
+
+        macros = [tuple(m) for m in tplargs.get('src_macros', [])]
+        if not macros:
+            return None, None
+        if macros != [('pyfr.plugins.kernels.source', 'source')]:
+            raise NotImplementedError(f'Source macros {macros} are not '
+                                      'supported')
+        if self.backend.ref_state is not None:
+            raise NotImplementedError('Source terms take unshifted states')
+        nd, nv = tplargs['ndims'], tplargs['nvars']
+        exprs = list(tplargs['src_exprs'])
+        if len(exprs) > nv or nv > 8:
+            raise ValueError('More source terms than variables')
+        progs, uses_x, uses_u = [], False, False
+        for text in exprs:
+            ex = BCExpr(str(text), nd, nv)
+            if ex.const is not None:
+                progs.append([(OPS['const'], ex.const)] if ex.const else [])
+            else:
+                progs.append(ex.prog)
+            uses_x |= ex.uses_x
+            uses_u |= ex.uses_u
+        if uses_x and ploc is None:
+            raise ValueError('Source terms of position need ploc')
+        if uses_u and u is None:
+            raise ValueError('Source terms of the solution need u')
+
+        arr, spans = pack(progs)
+        src = Src()
+        for i, (start, n) in enumerate(spans):
+            src.expr_start[i], src.expr_len[i] = start, n
+        prog = None
+        if len(arr):
+            prog = self.backend.const_matrix(arr.view(np.int64)[None, :],
+                                             dtype=np.int64)
+            src.prog = prog.data
+        if uses_x:
+            src.ploc, src.ldp = _mat(ploc)
+        if uses_u:
+            src.u, src.ldu = _mat(u)
+        return src, prog
+
+    def _srcterms(self, mode, tplargs, dims, r, rcpdjac, ploc, u, tmat):
+        """The source-term kernel in ``mode`` over r; the time is bound at
+        run time (``t``) or read from element 1 of the device matrix
+        ``tmat``."""
+        src, prog = self._source(tplargs, ploc, u)
+        nupts, neles = dims
+        fn = self._fn('srcterms')
+        nd, nv = tplargs['ndims'], tplargs['nvars']
+        rp, rl = _mat(r)
+        jp, jl = _mat(rcpdjac)
+        if tmat is not None:
+            src.t_dev = tmat.data + 8
+
+        def run(stream, t=0.0):
+            src.t = float(t)
+            fn(mode, nd, nv, nupts, neles, rp, rl, jp, jl, C.byref(src),
+               stream)
+
+        mats = [r, rcpdjac, ploc, u, prog, tmat]
+        return BindableKernel(run, ['t'], {'t': 0.0},
+                              mats=[m for m in mats if m is not None],
+                              misc=[src], name='srcterms',
+                              meta=dict(kind='srcterms', mode=mode,
+                                        tplargs=tplargs, dims=dims))
+
     def _negdivconf(self, tplargs, dims, extrns, tdivtconf, rcpdjac,
-                    ploc=None, u=None, **kw):
+                    ploc=None, u=None, tmat=None, **kw):
         if tplargs.get('src_macros'):
-            raise NotImplementedError('Source terms are not supported')
+            from pyfr_gb300.backend.lib import SRC_NEGDIVCONF
+            k = self._srcterms(SRC_NEGDIVCONF, tplargs, dims, tdivtconf,
+                               rcpdjac, ploc, u, tmat)
+            if 't' in kw:
+                k.bind(t=kw['t'])
+            return k
 
         nupts, neles = dims
         fn, nv = self._fn('negdivconf'), tplargs['nvars']
@@ -337,10 +416,25 @@ class PointwiseKernelProvider:
                                         dims=dims, tdivtconf=tdivtconf,
                                         rcpdjac=rcpdjac))
 
-    def _evalsrcmacros(self, tplargs, dims, extrns, **kw):
-        if tplargs.get('src_macros'):
-            raise NotImplementedError('Source terms are not supported')
-        return NullKernel()
+    def _addsrc(self, tplargs, dims, extrns, r, ploc=None, u=None,
+                tmat=None, **kw):
+        """R <- R + src: the source terms after an operator apply that
+        already formed -(1/|J|) div F."""
+        from pyfr_gb300.backend.lib import SRC_ADD
+        k = self._srcterms(SRC_ADD, tplargs, dims, r, None, ploc, u, tmat)
+        if 't' in kw:
+            k.bind(t=kw['t'])
+        return k
+
+    def _evalsrcmacros(self, tplargs, dims, extrns, u, ploc=None,
+                       tmat=None, **kw):
+        if not tplargs.get('src_macros'):
+            return NullKernel()
+        from pyfr_gb300.backend.lib import SRC_EVAL
+        k = self._srcterms(SRC_EVAL, tplargs, dims, u, None, ploc, u, tmat)
+        if 't' in kw:
+            k.bind(t=kw['t'])
+        return k
 
     # ---- interface kernels ---------------------------------------------------
 
@@ -551,6 +645,7 @@ _BUILDERS = {
         PointwiseKernelProvider._negdivconf,
     'pyfr.solvers.baseadvec.kernels.evalsrcmacros':
         PointwiseKernelProvider._evalsrcmacros,
+    'pyfr_gb300.kernels.addsrc': PointwiseKernelProvider._addsrc,
     'pyfr.solvers.euler.kernels.intcflux':
         PointwiseKernelProvider._intcflux_euler,
     'pyfr.solvers.navstokes.kernels.intcflux':

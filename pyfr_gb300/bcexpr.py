@@ -1,14 +1,17 @@
-"""Boundary values given as expressions of position and time.
+"""Boundary values and source terms given as expressions.
 
 The reference substitutes the options of a ``[soln-bcs-<name>]`` section
 (``rho``, ``p``, ``u``, ``v``, ``w``, ``cpTw``) into its boundary kernels as C
 expressions of the flux point's coordinates ``x``, ``y``, ``z`` and the time
 ``t``, with ``[constants]`` substituted (``pyfr/solvers/baseadvec/
-inters.py:95-116``).  Here an expression is compiled once, on the host,
-into a short postfix program that the boundary kernels evaluate per point;
-a subexpression of constants is folded to a number, so a constant option
-costs nothing.  Programs are straight-line (no jumps), and their stack
-depth is checked against the kernels' fixed stack.
+inters.py:95-116``), and the options of ``[solver-plugin-source]`` into the
+``negdivconf`` kernel as C expressions of ``ploc[i]``, the solution ``u[i]``
+and ``t`` (``pyfr/plugins/source.py:15-31``,
+``pyfr/plugins/kernels/source.mako``).  Here an expression is compiled
+once, on the host, into a short postfix program that the kernels evaluate
+per point; a subexpression of constants is folded to a number, so a
+constant option costs nothing.  Programs are straight-line (no jumps), and
+their stack depth is checked against the kernels' fixed stack.
 """
 
 import ast
@@ -21,7 +24,7 @@ OPS = {name: i for i, name in enumerate(
     ['const', 'x', 'y', 'z', 't', 'add', 'sub', 'mul', 'div', 'pow', 'neg',
      'sin', 'cos', 'tan', 'exp', 'log', 'sqrt', 'tanh', 'abs', 'asin',
      'acos', 'atan', 'sinh', 'cosh', 'atan2', 'min', 'max', 'floor',
-     'ceil'])}
+     'ceil', 'u'])}
 
 # Largest stack depth of a program (the kernels' stack size)
 MAX_DEPTH = 16
@@ -43,14 +46,19 @@ _VARS = {'x': 0, 'y': 1, 'z': 2}
 
 class BCExpr:
     """A compiled expression: ``const`` (a float) when it depends on
-    neither position nor time, otherwise ``prog`` (a list of (opcode,
-    value)) with ``depth`` and the flags ``uses_x`` and ``uses_t``."""
+    neither position, time nor solution, otherwise ``prog`` (a list of
+    (opcode, value); for ``u`` the value is the variable's index) with
+    ``depth`` and the flags ``uses_x``, ``uses_t`` and ``uses_u``.
 
-    def __init__(self, text, ndims):
+    Coordinates are written ``x``, ``y``, ``z`` or ``ploc[i]``; solution
+    variables (``nvars`` of them, 0 for boundary values) ``u[i]``."""
+
+    def __init__(self, text, ndims, nvars=0):
         self.text = text
         self.ndims = ndims
+        self.nvars = nvars
         tree = ast.parse(text.strip(), mode='eval').body
-        self.uses_x = self.uses_t = False
+        self.uses_x = self.uses_t = self.uses_u = False
         node = self._fold(tree)
         if isinstance(node, float):
             self.const, self.prog, self.depth = node, [], 1
@@ -66,6 +74,17 @@ class BCExpr:
     def _fold(self, n):
         if isinstance(n, ast.Constant) and isinstance(n.value, (int, float)):
             return float(n.value)
+        if isinstance(n, ast.Subscript) and isinstance(n.value, ast.Name) \
+                and isinstance(n.slice, ast.Constant) and \
+                type(n.slice.value) is int:
+            a, i = n.value.id, n.slice.value
+            if a == 'ploc' and 0 <= i < self.ndims:
+                self.uses_x = True
+                return ('var', 'xyz'[i])
+            if a == 'u' and 0 <= i < self.nvars:
+                self.uses_u = True
+                return ('u', i)
+            raise ValueError(f'{a}[{i}] in {self.text!r}')
         if isinstance(n, ast.Name):
             if n.id in _VARS:
                 if _VARS[n.id] >= self.ndims:
@@ -114,6 +133,9 @@ class BCExpr:
         if node[0] == 'var':
             self.prog.append((OPS[node[1]], 0.0))
             return 1
+        if node[0] == 'u':
+            self.prog.append((OPS['u'], float(node[1])))
+            return 1
         op, *args = node
         depths = []
         for i, a in enumerate(args):
@@ -121,9 +143,10 @@ class BCExpr:
         self.prog.append((OPS[op], 0.0))
         return max(depths)
 
-    def eval_np(self, x, t):
-        """numpy evaluation at the points x (ndims, n) and time t (the
-        same operations, for the host and for tests)."""
+    def eval_np(self, x, t, u=None):
+        """numpy evaluation at the points x (ndims, n), time t and
+        solution u (nvars, n) (the same operations, for the host and for
+        tests)."""
         if self.const is not None:
             return np.full(x.shape[1], self.const)
         st = []
@@ -133,6 +156,8 @@ class BCExpr:
                 st.append(np.full(x.shape[1], v))
             elif name in _VARS:
                 st.append(np.asarray(x[_VARS[name]], dtype=float))
+            elif name == 'u':
+                st.append(np.asarray(u[int(v)], dtype=float))
             elif name == 't':
                 st.append(np.full(x.shape[1], float(t)))
             elif name == 'neg':
@@ -143,6 +168,23 @@ class BCExpr:
             else:
                 st.append(_NPUN[name](st.pop()))
         return st[0]
+
+
+def pack(progs):
+    """The programs ``progs`` (lists of (opcode, value)) one after the
+    other as an array of ``b200_bcop_t`` (op, pad, val; pad holds the
+    variable index of a ``u`` instruction), with each program's start and
+    length."""
+    ops, spans = [], []
+    for p in progs:
+        spans.append((len(ops), len(p)))
+        ops.extend(p)
+    arr = np.zeros(len(ops), dtype=[('op', '<i4'), ('pad', '<i4'),
+                                    ('val', '<f8')])
+    arr['op'] = [o for o, _ in ops]
+    arr['val'] = [v for _, v in ops]
+    arr['pad'] = [int(v) if o == OPS['u'] else 0 for o, v in ops]
+    return arr, spans
 
 
 _NAMES = {v: k for k, v in OPS.items()}

@@ -21,6 +21,7 @@
 #include <cstdint>
 
 #include "common.cuh"
+#include "exprprog.cuh"
 #include "physics.cuh"
 #include "pyfrb200.h"
 
@@ -29,8 +30,6 @@ namespace {
 constexpr int BC_BLOCK = 128;
 
 using b200::Gas;
-
-constexpr int BC_STACK = 16;
 
 template <typename T>
 struct BcK {
@@ -48,63 +47,6 @@ struct BcK {
     const double *t_dev;
 };
 
-// The value of a boundary program at a point (x) and time (t)
-template <typename T>
-__device__ T bc_program(const b200_bcop_t *prog, int start, int len, const T *x, T t) {
-    T st[BC_STACK];
-    int sp = 0;
-    // (a malformed program, which the host compiler never makes, gives NaN
-    // instead of leaving the stack)
-    const T bad = T(0) / T(0);
-    for (int i = start; i < start + len; i++) {
-        const int op = prog[i].op;
-        if (op < 0 || op > 28) return bad;
-        if (op <= 4) {
-            if (sp >= BC_STACK) return bad;
-            st[sp++] = op == 0 ? (T)prog[i].val : (op == 4 ? t : x[op - 1]);
-        } else if (op <= 9 || op >= 24 && op <= 26) {
-            if (sp < 2) return bad;
-            const T b = st[--sp], a = st[sp - 1];
-            T r;
-            switch (op) {
-            case 5: r = a + b; break;
-            case 6: r = a - b; break;
-            case 7: r = a * b; break;
-            case 8: r = a / b; break;
-            case 9: r = pow(a, b); break;
-            case 24: r = atan2(a, b); break;
-            case 25: r = fmin(a, b); break;
-            default: r = fmax(a, b); break;
-            }
-            st[sp - 1] = r;
-        } else {
-            if (sp < 1) return bad;
-            const T a = st[sp - 1];
-            T r;
-            switch (op) {
-            case 10: r = -a; break;
-            case 11: r = sin(a); break;
-            case 12: r = cos(a); break;
-            case 13: r = tan(a); break;
-            case 14: r = exp(a); break;
-            case 15: r = log(a); break;
-            case 16: r = sqrt(a); break;
-            case 17: r = tanh(a); break;
-            case 18: r = fabs(a); break;
-            case 19: r = asin(a); break;
-            case 20: r = acos(a); break;
-            case 21: r = atan(a); break;
-            case 22: r = sinh(a); break;
-            case 23: r = cosh(a); break;
-            case 27: r = floor(a); break;
-            default: r = ceil(a); break;
-            }
-            st[sp - 1] = r;
-        }
-    }
-    return sp == 1 ? st[0] : bad;
-}
-
 // The boundary values at point i: the programs evaluated and the derived
 // constants formed again from them
 template <int ND, typename T>
@@ -115,7 +57,7 @@ __device__ __forceinline__ void bc_at_point(BcK<T> &b, int64_t i, T gamma) {
     const T t = (T)b.t_dev[0];
     T *dst[6] = {&b.rho, &b.p, &b.u[0], &b.u[1], &b.u[2], &b.cpTw_g};
     for (int f = 0; f < 6; f++)
-        if (b.elen[f]) *dst[f] = bc_program<T>(b.prog, b.estart[f], b.elen[f], x, t);
+        if (b.elen[f]) *dst[f] = b200::expr_program<T>(b.prog, b.estart[f], b.elen[f], x, t);
     if (b.elen[5]) b.cpTw_g /= gamma;
     if (b.elen[0] || b.elen[1]) {
         const T cs = b.rho > 0 && b.p > 0 ? sqrt(gamma * b.p / b.rho) : T(0);

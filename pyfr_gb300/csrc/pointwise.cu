@@ -11,11 +11,14 @@
 //   tflux (NS, fused)  pyfr/solvers/navstokes/kernels/tflux.mako:13-50
 //   gradcoru           pyfr/solvers/baseadvecdiff/kernels/gradcoru.mako:10-24
 //   negdivconf         pyfr/solvers/baseadvec/kernels/negdivconf.mako:7-22
+//   srcterms           negdivconf with source macros, evalsrcmacros.mako:7-22,
+//                      pyfr/plugins/kernels/source.mako
 //   intcflux (Euler)   pyfr/solvers/euler/kernels/intcflux.mako:6-22 (any of the
 //                      six Riemann solvers, a template argument)
 //   intcflux (NS)      pyfr/solvers/navstokes/kernels/intcflux.mako:10-54
 //   intconu            pyfr/solvers/navstokes/kernels/intconu.mako:4-19
 #include "common.cuh"
+#include "exprprog.cuh"
 #include "physics.cuh"
 #include "../../include/pyfrb200.h"
 
@@ -271,6 +274,90 @@ negdivconf_kernel(int nvars, int64_t neles, T *__restrict__ r, int64_t ldr,
         T *p = r + upt * ldr + soa_off(e, v, nvars);
         *p = -rj * *p;
     }
+}
+
+// Source terms at the solution points (b200_src_t in the kernels'
+// precision)
+constexpr int SRC_MAXV = 8;
+
+template <typename T>
+struct SrcK {
+    const b200_bcop_t *prog;
+    int estart[SRC_MAXV], elen[SRC_MAXV];
+    const T *ploc;
+    int64_t ldp;
+    const T *u;
+    int64_t ldu;
+    T t;
+    const double *t_dev;
+};
+
+// One thread per element of one solution point: the source of every
+// variable, then (MODE) -R/|J| + src, R + src or src.  u may be R itself in
+// the evaluation mode: every read of the point precedes its writes.
+template <typename T, int MODE>
+__global__ void __launch_bounds__(PW_BLOCK)
+srcterms_kernel(int ndims, int nvars, int64_t neles, T *r, int64_t ldr,
+                const T *__restrict__ rcpdjac, int64_t ldj, SrcK<T> s) {
+    const int64_t e = (int64_t)blockIdx.x * PW_BLOCK + threadIdx.x;
+    const int upt = blockIdx.y;
+    if (e >= neles) return;
+    T x[3] = {0, 0, 0};
+    if (s.ploc)
+        for (int d = 0; d < ndims; d++) x[d] = s.ploc[upt * s.ldp + soa_off(e, d, ndims)];
+    T u[SRC_MAXV];
+    if (s.u)
+        for (int v = 0; v < nvars; v++) u[v] = s.u[upt * s.ldu + soa_off(e, v, nvars)];
+    const T t = s.t_dev ? (T)s.t_dev[0] : s.t;
+    T src[SRC_MAXV];
+    for (int v = 0; v < nvars; v++)
+        src[v] = s.elen[v] ? b200::expr_program<T>(s.prog, s.estart[v], s.elen[v], x, t,
+                                                    s.u ? u : nullptr, nvars)
+                           : T(0);
+    const T rj = MODE == B200_SRC_NEGDIVCONF ? rcpdjac[(int64_t)upt * ldj + e] : T(0);
+    for (int v = 0; v < nvars; v++) {
+        T *p = r + upt * ldr + soa_off(e, v, nvars);
+        if (MODE == B200_SRC_NEGDIVCONF)
+            *p = -rj * *p + src[v];
+        else if (MODE == B200_SRC_ADD)
+            *p += src[v];
+        else
+            *p = src[v];
+    }
+}
+
+template <typename T>
+int srcterms(int mode, int ndims, int nvars, int nupts, int64_t neles, T *r, int64_t ldr,
+             const T *rcpdjac, int64_t ldj, const b200_src_t *src, cudaStream_t stream) {
+    if (!src || nvars < 1 || nvars > SRC_MAXV || ndims < 1 || ndims > 3 || mode < 0 ||
+        mode > 2 || (mode == B200_SRC_NEGDIVCONF && !rcpdjac))
+        return B200_ERR_ARG;
+    if (neles <= 0 || nupts <= 0) return B200_OK;
+    SrcK<T> k;
+    k.prog = src->prog;
+    for (int v = 0; v < SRC_MAXV; v++) {
+        k.estart[v] = src->expr_start[v];
+        k.elen[v] = src->prog && v < nvars ? src->expr_len[v] : 0;
+        if (k.elen[v] < 0 || k.estart[v] < 0) return B200_ERR_ARG;
+    }
+    k.ploc = static_cast<const T *>(src->ploc);
+    k.ldp = src->ldp;
+    k.u = static_cast<const T *>(src->u);
+    k.ldu = src->ldu;
+    k.t = (T)src->t;
+    k.t_dev = src->t_dev;
+    dim3 grid(b200::ceil_div(neles, PW_BLOCK), nupts);
+    if (mode == B200_SRC_NEGDIVCONF)
+        srcterms_kernel<T, B200_SRC_NEGDIVCONF><<<grid, PW_BLOCK, 0, stream>>>(
+            ndims, nvars, neles, r, ldr, rcpdjac, ldj, k);
+    else if (mode == B200_SRC_ADD)
+        srcterms_kernel<T, B200_SRC_ADD><<<grid, PW_BLOCK, 0, stream>>>(ndims, nvars, neles, r,
+                                                                       ldr, rcpdjac, ldj, k);
+    else
+        srcterms_kernel<T, B200_SRC_EVAL><<<grid, PW_BLOCK, 0, stream>>>(ndims, nvars, neles, r,
+                                                                        ldr, rcpdjac, ldj, k);
+    B200_CHECK_LAUNCH("srcterms");
+    return B200_OK;
 }
 
 template <typename T>
@@ -749,6 +836,20 @@ int b200_negdivconf_f32(int nvars, int nupts, int64_t neles, float *r, int64_t l
     negdivconf_kernel<float><<<grid, PW_BLOCK, 0, (cudaStream_t)stream>>>(nvars, neles, r, ldr, rcpdjac, ldj);
     B200_CHECK_LAUNCH("negdivconf");
     return B200_OK;
+}
+
+int b200_srcterms_f64(int mode, int ndims, int nvars, int nupts, int64_t neles, double *r,
+                      int64_t ldr, const double *rcpdjac, int64_t ldj, const b200_src_t *src,
+                      void *stream) {
+    return srcterms<double>(mode, ndims, nvars, nupts, neles, r, ldr, rcpdjac, ldj, src,
+                            (cudaStream_t)stream);
+}
+
+int b200_srcterms_f32(int mode, int ndims, int nvars, int nupts, int64_t neles, float *r,
+                      int64_t ldr, const float *rcpdjac, int64_t ldj, const b200_src_t *src,
+                      void *stream) {
+    return srcterms<float>(mode, ndims, nvars, nupts, neles, r, ldr, rcpdjac, ldj, src,
+                           (cudaStream_t)stream);
 }
 
 int b200_intcflux_euler_f64(int ndims, int64_t n, int rsolver, double gamma, double p_min,

@@ -552,11 +552,13 @@ class MixedRKIntegrator(RKVdH2Integrator):
         self.uref, self.hs_ref = None, 0.0
         shift = cfg.get('backend-b200', 'reference-shift', 'auto')
         rs = cfg.get('solver-interfaces', 'riemann-solver')
-        # (artificial viscosity senses the density itself, so it keeps the
-        # unshifted state, as boundaries do)
+        # (artificial viscosity senses the density itself and source terms
+        # read the solution, so they keep the unshifted state, as
+        # boundaries do)
         sc = cfg.get('solver', 'shock-capturing', 'none')
         if shift == 'auto' and sysm.name == 'navier-stokes' and \
-                rs == 'rusanov' and not sysm._bc_inters and sc == 'none':
+                rs == 'rusanov' and not sysm._bc_inters and sc == 'none' \
+                and not sysm.has_src_macros:
             gamma = cfg.getfloat('constants', 'gamma')
             rho = np.concatenate([u[:, 0].ravel() for u in self._ics])
             pri = [e.con_to_pri(list(u.swapaxes(0, 1)), cfg)[-1]

@@ -52,6 +52,9 @@ def npeval(expr, env):
 class BaseElements:
     # Set by the system: every flux point lies on an interior interface
     comm_covered = False
+    # Set by the system: the device matrix whose element 1 is the stage time
+    tmat = None
+    src_uses_x = src_uses_u = src_uses_t = False
     def __init__(self, etype, eles, cfg):
         self.cfg = cfg
         self.eles = eles
@@ -88,11 +91,37 @@ class BaseElements:
 
         self.convars = self.convarnames(self.ndims)
         self.nvars = len(self.convars)
+        self._srctplargs = self._source_tplargs(cfg)
         self.nupts = self.basis.nupts
         self.nfpts = self.basis.nfpts
         self.nfacefpts = self.basis.nfacefpts
         self.kernels = {}
         self._be = None
+
+    def _source_tplargs(self, cfg):
+        """Template arguments of the source plugin's macro
+        (pyfr/plugins/source.py:15-31): one expression per conserved
+        variable of x, y, z (as ploc[i]), the conserved variables (as u[i])
+        and t, with [constants] substituted; None without the plugin."""
+        sect = 'solver-plugin-source'
+        if not cfg.hassect(sect):
+            return None
+        from pyfr_gb300.bcexpr import BCExpr
+        subs = dict(x='ploc[0]', y='ploc[1]', z='ploc[2]', abs='fabs',
+                    pi=repr(np.pi))
+        subs |= {v: f'u[{i}]' for i, v in enumerate(self.convars)}
+        exprs = [cfg.getexpr(sect, v, subs=subs) for v in self.convars]
+        parsed = [BCExpr(e, self.ndims, self.nvars) for e in exprs]
+        self.src_uses_x = any(p.uses_x for p in parsed)
+        self.src_uses_u = any(p.uses_u for p in parsed)
+        self.src_uses_t = any(p.uses_t for p in parsed)
+        return dict(ndims=self.ndims, nvars=self.nvars,
+                    src_macros=[('pyfr.plugins.kernels.source', 'source')],
+                    src_exprs=exprs)
+
+    @property
+    def has_src_macros(self):
+        return self._srctplargs is not None
 
     def _surf_rules(self, cfg, order):
         """The face quadrature rule of each face kind for surface-flux
@@ -426,6 +455,7 @@ class _DivergenceMixin:
         operators, all three as one kernel:
         R = -(1/|J|)((M1 - M3.M2) F + M3 Fc)."""
         be, kernels = self._be, self.kernels
+        src = self._source_kernels()
         # (with flux anti-aliasing the flux lives at the quadrature points
         # and is projected back by M9)
         m132, vect = ('(M1 - M3*M2)*M9', self._vect_qpts) if \
@@ -436,6 +466,12 @@ class _DivergenceMixin:
                 'mul_cat', self.opmat(m132), vect,
                 self.opmat('M3'), self._scal_fpts, out=self.scal_upts[fout],
                 alpha=-1.0, rowscale=self.rcpdjac_at('upts'))
+            # (then the source terms, added to -(1/|J|) div F)
+            if src:
+                kernels['addsrc'] = lambda fout: be.kernel(
+                    'addsrc', tplargs=self._srctplargs,
+                    dims=[self.nupts, self.neles], r=self.scal_upts[fout],
+                    **src())
             return
 
         kernels['tdivtpcorf'] = lambda fout: be.kernel(
@@ -444,10 +480,39 @@ class _DivergenceMixin:
             'mul', self.opmat('M3'), self._scal_fpts,
             out=self.scal_upts[fout], beta=1.0)
         kernels['negdivconf'] = lambda fout: be.kernel(
-            'negdivconf', tplargs=dict(ndims=self.ndims, nvars=self.nvars,
-                                       src_macros=[]),
+            'negdivconf', tplargs=self._srctplargs or dict(
+                ndims=self.ndims, nvars=self.nvars, src_macros=[]),
             dims=[self.nupts, self.neles], tdivtconf=self.scal_upts[fout],
-            rcpdjac=self.rcpdjac_at('upts'))
+            rcpdjac=self.rcpdjac_at('upts'), **(src() if src else {}))
+
+    def _source_kernels(self):
+        """With source terms: the copy of the solution they read (the
+        right-hand side may overwrite its input bank) and evalsrcmacros
+        (pyfr/solvers/baseadvec/elements.py:100-126); returns a function
+        giving the source arguments of negdivconf, or None."""
+        if self._srctplargs is None:
+            return None
+        be, kernels = self._be, self.kernels
+        be.pointwise.register('pyfr.solvers.baseadvec.kernels.evalsrcmacros')
+        be.pointwise.register('pyfr_gb300.kernels.addsrc')
+        if self.src_uses_u:
+            self._scal_upts_cpy = be.matrix(
+                (self.nupts, self.nvars, self.neles), tags={'align'})
+            kernels['copy_soln'] = lambda uin: be.kernel(
+                'copy', self._scal_upts_cpy, self.scal_upts[uin])
+
+        def args():
+            return dict(
+                ploc=self.ploc_at('upts') if self.src_uses_x else None,
+                u=self._scal_upts_cpy if self.src_uses_u else None,
+                tmat=self.tmat)
+
+        kernels['evalsrcmacros'] = lambda uin: be.kernel(
+            'evalsrcmacros', tplargs=self._srctplargs,
+            dims=[self.nupts, self.neles], u=self.scal_upts[uin],
+            ploc=self.ploc_at('upts') if self.src_uses_x else None,
+            tmat=self.tmat)
+        return args
 
 
 class EulerElements(_WavespeedMixin, _DivergenceMixin, FluidElements,

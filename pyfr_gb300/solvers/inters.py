@@ -268,17 +268,12 @@ class BaseBCInters(BaseIntInters):
         self._prog = self._ploc = None
         if self.exprs:
             from pyfr_gb300.backend.lib import BCOp
-            ops = []
-            for f, k in enumerate(['rho', 'p', 'u', 'v', 'w', 'cpTw']):
-                if k in self.exprs:
-                    prog = self.exprs[k].prog
-                    self.bc.expr_start[f], self.bc.expr_len[f] = \
-                        len(ops), len(prog)
-                    ops.extend(prog)
-            arr = np.zeros(len(ops), dtype=[('op', '<i4'), ('pad', '<i4'),
-                                            ('val', '<f8')])
-            arr['op'] = [o for o, _ in ops]
-            arr['val'] = [v for _, v in ops]
+            from pyfr_gb300.bcexpr import pack
+            names = ['rho', 'p', 'u', 'v', 'w', 'cpTw']
+            arr, spans = pack([self.exprs[k].prog if k in self.exprs else []
+                               for k in names])
+            for f, (start, n) in enumerate(spans):
+                self.bc.expr_start[f], self.bc.expr_len[f] = start, n
             assert arr.itemsize == C.sizeof(BCOp)
             self._prog = be.const_matrix(arr.view(np.int64)[None, :],
                                          dtype=np.int64)

@@ -153,6 +153,8 @@ class BaseSystem:
         self.backend.commit()
         for b in self._bc_inters:
             b.bind_device(self._tmat)
+        for e in self.ele_map.values():
+            e.tmat = self._tmat
         self._gen_kernels()
         if self._av:
             self._av.add_kernels(self._kernels, self._ktags)
@@ -235,9 +237,26 @@ class BaseSystem:
 
     @property
     def time_dependent(self):
-        """Whether a boundary value depends on the time."""
-        return any(getattr(b, 'time_dependent', False)
-                   for b in self._bc_inters)
+        """Whether a boundary value or a source term depends on the
+        time."""
+        return (any(getattr(b, 'time_dependent', False)
+                    for b in self._bc_inters) or
+                any(e.src_uses_t for e in self.ele_map.values()))
+
+    @property
+    def has_src_macros(self):
+        return any(e.has_src_macros for e in self.ele_map.values())
+
+    def evalsrcmacros(self, uinoutbank):
+        """Overwrite a bank with the source terms evaluated from it
+        (pyfr/solvers/base/system.py:478-481)."""
+        k = self._get_kernels(uinoutbank, None)['eles/evalsrcmacros']
+        self.backend.run_kernels(k, wait=True)
+
+    def _add_src(self, g, k, deps):
+        """The source terms after a fused divergence apply."""
+        for l in k['eles/addsrc']:
+            g.add(l, deps=deps(l, 'eles/tdivtconf_cat'))
 
     def set_time(self, t):
         """Set the stage time read by the boundary values (an RHS called
@@ -259,7 +278,7 @@ class BaseSystem:
     def rhs(self, t, uinbank, foutbank):
         if uinbank >= self.nrhs or foutbank >= self.nrhs:
             raise ValueError('Invalid register numbers')
-        if any(b.exprs for b in self._bc_inters):
+        if self.time_dependent:
             self.set_time(t)
         for g in self._rhs_graphs_cached(uinbank, foutbank):
             self.backend.run_graph(g)
@@ -310,8 +329,11 @@ class EulerSystem(BaseSystem):
 
         g_intf = self.backend.graph()
         # (with the entropy filter: filter the input first, then exchange
-        # the new face minima; pyfr/solvers/baseadvec/system.py:58-90)
+        # the new face minima; pyfr/solvers/baseadvec/system.py:58-90;
+        # source terms of the solution read a copy of it)
         g_intf.add_all(k['eles/entropy_filter'])
+        for l in k['eles/copy_soln']:
+            g_intf.add(l, deps=deps(l, 'eles/entropy_filter'))
         for l in k['eles/disu']:
             g_intf.add(l, deps=deps(l, 'eles/entropy_filter'))
         g_intf.add_all(k['iint/comm_entropy'], deps=k['eles/entropy_filter'])
@@ -331,6 +353,7 @@ class EulerSystem(BaseSystem):
             # Fused divergence, correction and negdivconf
             for l in k['eles/tdivtconf_cat']:
                 g_flux_div.add(l, deps=deps(l, 'eles/tdisf'))
+            self._add_src(g_flux_div, k, deps)
             g_flux_div.commit()
             return g_intf, g_flux_div
 
@@ -365,6 +388,8 @@ class NavierStokesSystem(BaseSystem):
         # Graph 1: solution at the flux points and the common solution
         g_soln = self.backend.graph()
         g_soln.add_all(k['eles/entropy_filter'])
+        for l in k['eles/copy_soln']:
+            g_soln.add(l, deps=deps(l, 'eles/entropy_filter'))
         for l in k['eles/disu']:
             g_soln.add(l, deps=deps(l, 'eles/entropy_filter'))
         g_soln.add_all(k['iint/comm_entropy'], deps=k['eles/entropy_filter'])
@@ -459,6 +484,7 @@ class NavierStokesSystem(BaseSystem):
         g_div = self.backend.graph()
         if k['eles/tdivtconf_cat']:
             g_div.add_all(k['eles/tdivtconf_cat'])
+            self._add_src(g_div, k, deps)
         else:
             g_div.add_all(k['eles/tdivtconf'])
             for l in k['eles/negdivconf']:
@@ -483,6 +509,7 @@ class NavierStokesSystem(BaseSystem):
 
         g_div = self.backend.graph()
         g_div.add_all(k['eles/tdivtconf_cat'])
+        self._add_src(g_div, k, deps)
         g_div.commit()
         return g_grad_flux, g_div
 

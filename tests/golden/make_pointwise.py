@@ -20,6 +20,9 @@ Kernels covered (reference module, variants):
   {0.1, 0}, Rusanov and HLLC (plus the other solvers at beta = 1/2);
 * ``navstokes.kernels.intconu`` for the three betas;
 * ``baseadvecdiff.kernels.gradcoru``, ``baseadvec.kernels.negdivconf``;
+* ``baseadvec.kernels.negdivconf`` and ``evalsrcmacros`` with the source
+  plugin's macro (``plugins/kernels/source.mako``), its expressions made by
+  the reference's own substitution (``oracle.refkernels.source_exprs``);
 * ``integrators.explicit.kernels.rkvdh2`` for every RK45 stage, with and
   without the embedded error register.
 """
@@ -99,6 +102,12 @@ def inputs(rng):
     fam['rk'] = dict(r1=rng.normal(size=(n, 5)), r2=rng.normal(size=(n, 5)),
                      rold=np.full((n, 5), SENTINEL),
                      rerr=rng.normal(size=(n, 5)), dt=np.array(2.5e-3))
+    # Source terms: any solution values (both branches of min and max),
+    # coordinates in every quadrant (atan2)
+    fam['src'] = dict(tdivtconf=rng.normal(size=(n, 5)),
+                      ploc=rng.uniform(-2.0, 2.0, (n, 3)),
+                      u=rng.normal(0.5, 1.0, (n, 5)),
+                      rcpdjac=rng.uniform(0.5, 2.0, n), t=np.array(0.37))
     return fam
 
 

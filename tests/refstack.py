@@ -196,10 +196,13 @@ def reference_cfg(cfg):
     return Inifile(cfg.tostr())
 
 
-def run(case, n, steps, out=None, fake=False):
+def run(case, n, steps, out=None, fake=False, source=False, single=False):
     """Advance ``case`` ('vortex' or 'tgv') on an n-cell mesh by ``steps``
-    RK45 steps with PyFR's own integrator on the b200 backend; returns the
-    initial and final solutions, the step size and the integrator."""
+    RK45 steps with PyFR's own integrator on the b200 backend (with
+    ``source``, and the case's [solver-plugin-source] terms through PyFR's
+    own source plugin); returns the initial and final solutions, the step
+    size and the integrator.  With ``single``: FP32 with split-BF16
+    tensor-core operator applies and fused applies."""
     if fake:
         from tests import fake_lib
         fake_lib.install()
@@ -212,6 +215,12 @@ def run(case, n, steps, out=None, fake=False):
         cfg, mesh = euler_vortex(n=n, order=3, dt=1e-3)
     else:
         cfg, mesh = ns_tgv(n=n, order=3, dt=1e-3)
+    if source:
+        from tests.oracle_util import add_source
+        add_source(cfg, case)
+    if single:
+        cfg.set('backend', 'precision', 'single')
+        cfg.set('backend-b200', 'mul-precision', 'bf16x3')
     rcfg = reference_cfg(cfg)
     rcfg.set('solver-time-integrator', 'tstart', '0.0')
     rcfg.set('solver-time-integrator', 'tend', repr(1e3))
@@ -238,8 +247,21 @@ def main():
     ap.add_argument('--out')
     ap.add_argument('--fake', action='store_true',
                     help='host logic only: the library stand-in, no GPU')
+    ap.add_argument('--source', action='store_true',
+                    help='with the case\'s [solver-plugin-source] terms')
+    ap.add_argument('--single', action='store_true',
+                    help='FP32 with split-BF16 tensor-core applies')
+    ap.add_argument('--report', action='store_true',
+                    help='print the kernels of the first RHS\'s graphs')
     a = ap.parse_args()
-    run(a.case, a.n, a.steps, a.out, a.fake)
+    _, _, _, solver = run(a.case, a.n, a.steps, a.out, a.fake, a.source,
+                          a.single)
+    if a.report:
+        import json
+        graphs = solver.system._rhs_graphs(0, 1)
+        print(json.dumps([[k.name if k.name != 'mul' else
+                           f"mul:{k.meta.get('impl')}" for k in g.klist]
+                          for g in graphs]))
 
 
 if __name__ == '__main__':

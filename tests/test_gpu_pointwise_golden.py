@@ -170,6 +170,25 @@ def run_variant(be, m, x):
         return {'ulout': get_scal(mats['ulout']),
                 'urout': get_scal(mats['urout'])}
 
+    if tp.get('src_macros'):
+        # negdivconf and evalsrcmacros with the source plugin's macro
+        ploc, u = P.scal(x['ploc']), P.scal(x['u'])
+        if kname == 'negdivconf':
+            t = P.scal(x['tdivtconf'])
+            r = be.const_matrix(x['rcpdjac'][None], tags={'align'})
+            be.commit()
+            k = be.kernel('negdivconf', tplargs=tp, dims=[1, n], tdivtconf=t,
+                          rcpdjac=r, ploc=ploc, u=u)
+            out = {'tdivtconf': t}
+        else:
+            be.commit()
+            k = be.kernel('evalsrcmacros', tplargs=tp, dims=[1, n], u=u,
+                          ploc=ploc)
+            out = {'u': u}
+        k.bind(t=float(x['t']))
+        be.run_kernels([k], wait=True)
+        return {a: get_scal(M) for a, M in out.items()}
+
     if mod.endswith('negdivconf'):
         t = P.scal(x['tdivtconf'])
         r = be.const_matrix(x['rcpdjac'][None], tags={'align'})

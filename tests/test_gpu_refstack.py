@@ -22,19 +22,23 @@ def built():
     ge.build_library()
 
 
+@pytest.mark.parametrize('source', [False, True])
 @pytest.mark.parametrize('case,n,steps', [('vortex', 8, 5), ('tgv', 3, 2)])
-def test_reference_solver_on_b200(built, tmp_path, case, n, steps):
+def test_reference_solver_on_b200(built, tmp_path, case, n, steps, source):
+    """With ``source`` the case's [solver-plugin-source] terms go through
+    PyFR's own source plugin (functions of position, solution and time;
+    the oracle advances with the same stage times)."""
     if reference_tree() is None:
         pytest.skip('reference source tree not present')
-    from oracle.fr_oracle import rk45_step
+    from oracle.fr_oracle import rk45_step_t
     from pyfr_gb300.cases import euler_vortex, ns_tgv
-    from tests.oracle_util import disc_for_mesh
+    from tests.oracle_util import SOURCES, disc_for_mesh, source_c_exprs
 
     out = tmp_path / 'soln.npz'
     r = subprocess.run([sys.executable, '-m', 'tests.refstack', '--case',
                         case, '--n', str(n), '--steps', str(steps), '--out',
-                        str(out)], cwd=ROOT, capture_output=True, text=True,
-                       timeout=900)
+                        str(out)] + (['--source'] if source else []),
+                       cwd=ROOT, capture_output=True, text=True, timeout=900)
     assert r.returncode == 0, r.stderr[-3000:]
     d = np.load(out)
     assert str(d['backend']) == 'B200Backend'
@@ -44,16 +48,55 @@ def test_reference_solver_on_b200(built, tmp_path, case, n, steps):
         cfg, mesh = euler_vortex(n=n, order=3, dt=1e-3)
         disc = disc_for_mesh(mesh, 3)
         c = cfg.items_as('constants', float)
-        rhs = lambda x: disc.rhs_euler(x, c)           # noqa: E731
+        src = source_c_exprs(SOURCES[case], ['rho', 'rhou', 'rhov', 'E'],
+                             c) if source else None
+        rhs = lambda x, t: disc.rhs_euler(x, c, t=t, src=src)   # noqa: E731
     else:
         cfg, mesh = ns_tgv(n=n, order=3, dt=1e-3)
         disc = disc_for_mesh(mesh, 3, ns=True)
         c = cfg.items_as('constants', float) | \
             cfg.items_as('solver-interfaces', float)
-        rhs = lambda x: disc.rhs_ns(x, c)              # noqa: E731
-    u = d['u0']
-    for _ in range(steps):
-        u = rk45_step(rhs, u, float(d['dt']))
+        src = source_c_exprs(SOURCES[case],
+                             ['rho', 'rhou', 'rhov', 'rhow', 'E'],
+                             cfg.items_as('constants', float)) \
+            if source else None
+        rhs = lambda x, t: disc.rhs_ns(x, c, t=t, src=src)      # noqa: E731
+    u, dt = d['u0'], float(d['dt'])
+    for i in range(steps):
+        u = rk45_step_t(rhs, u, i*dt, dt)
     err = max(np.abs(d['u1'][:, v] - u[:, v]).max()/np.abs(u[:, v]).max()
               for v in range(u.shape[1]))
     assert err < 1e-10, err
+
+
+def test_reference_solver_single_fused(built, tmp_path):
+    """PyFR's Euler system in single precision on the tensor-core applies,
+    its divergence chain fused into one apply by the backend's fuser, five
+    RK45 steps of the vortex against the oracle's FP64 steps: the FP32
+    right-hand side is good to about 1e-4 of its scale, so the solution
+    after five steps of 1e-3 to well under 1e-5."""
+    import json
+    if reference_tree() is None:
+        pytest.skip('reference source tree not present')
+    from oracle.fr_oracle import rk45_step
+    from pyfr_gb300.cases import euler_vortex
+    from tests.oracle_util import disc_for_mesh
+
+    out = tmp_path / 'soln.npz'
+    r = subprocess.run([sys.executable, '-m', 'tests.refstack', '--case',
+                        'vortex', '--n', '8', '--steps', '5', '--single',
+                        '--report', '--out', str(out)], cwd=ROOT,
+                       capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr[-3000:]
+    graphs = json.loads(r.stdout.strip().splitlines()[-1])
+    assert graphs[-1] == ['tflux', 'mul:bf16x3-cat']
+    d = np.load(out)
+    cfg, mesh = euler_vortex(n=8, order=3, dt=1e-3)
+    disc = disc_for_mesh(mesh, 3)
+    c = cfg.items_as('constants', float)
+    u = d['u0'].astype(np.float64)
+    for _ in range(5):
+        u = rk45_step(lambda x: disc.rhs_euler(x, c), u, float(d['dt']))
+    err = max(np.abs(d['u1'][:, v] - u[:, v]).max()/np.abs(u[:, v]).max()
+              for v in range(u.shape[1]))
+    assert err < 1e-5, err

@@ -103,8 +103,14 @@ def oracle_eval(m, x):
     if mod.endswith('gradcoru'):
         return {'gradu': np.einsum('n,nki,nkv->niv', x['rcpdjac'],
                                    x['smats'], x['gradu'])}
-    if mod.endswith('negdivconf'):
-        return {'tdivtconf': -x['rcpdjac'][:, None]*x['tdivtconf']}
+    if mod.endswith('negdivconf') or mod.endswith('evalsrcmacros'):
+        src = 0.0
+        if tp.get('src_macros'):
+            src = fo.source_terms(tp['src_exprs'], float(x['t']), x['u'].T,
+                                  x['ploc'].T).T
+        if mod.endswith('evalsrcmacros'):
+            return {'u': src}
+        return {'tdivtconf': -x['rcpdjac'][:, None]*x['tdivtconf'] + src}
     if mod.endswith('rkvdh2'):
         r1, r2, rold, rerr = fo.rkvdh2_stage(
             tp['stage'], tp['nstages'], tp['a'], tp['b'], tp['e'],
@@ -118,7 +124,8 @@ def test_fixtures_cover_the_path(pw):
     g, meta = pw
     mods = {m['module'].rsplit('.', 1)[-1] for m in meta.values()}
     assert {'tflux', 'intcflux', 'intconu', 'gradcoru', 'negdivconf',
-            'rkvdh2', 'wavespeed'} <= mods
+            'rkvdh2', 'wavespeed', 'evalsrcmacros'} <= mods
+    assert any(m['tplargs'].get('src_macros') for m in meta.values())
     rs = {m['tplargs']['rsolver'] for m in meta.values()
           if 'rsolver' in m['tplargs']}
     assert rs == set(fo.RSOLVERS)
