@@ -62,7 +62,10 @@ enum {
     B200_BC_NO_SLP_ISOT_WALL = 6, /* no-slip isothermal wall (NS) */
     B200_BC_SUB_IN_FRV = 7,       /* subsonic inflow, given rho and velocity (NS) */
     B200_BC_SUB_IN_FTPTTANG = 8,  /* subsonic inflow, given total state and direction (NS) */
-    B200_BC_SUB_OUT_FP = 9        /* subsonic outflow, given pressure (NS) */
+    B200_BC_SUB_OUT_FP = 9,       /* subsonic outflow, given pressure (NS) */
+    B200_BC_CHAR_RIEM_INV_CTRL = 10 /* characteristic Riemann invariants with a controlled
+                                     * pressure p = ic + im*t (char-riem-inv-mass-flow and
+                                     * char-riem-inv-pressure; Euler and NS) */
 };
 /* One instruction of a boundary-value or source-term program: postfix
  * code evaluated per point on a stack of at most 16 values.  Opcodes:
@@ -91,6 +94,14 @@ typedef struct {
     const void *ploc;
     int64_t ldp;
     const double *t_dev;
+    /* The time when t_dev is NULL (a value bound on the host) */
+    double t;
+    /* B200_BC_CHAR_RIEM_INV_CTRL: the controller's pressure interpolation
+     * p(t) = ic + im*t (pyfr/solvers/euler/kernels/bcs/
+     * char-riem-inv-controlled.mako), from ctrl[0], ctrl[1] (device
+     * memory) when ctrl is not NULL, else from ic and im */
+    double ic, im;
+    const double *ctrl;
 } b200_bc_t;
 /* t[1] = t[0] + c*dt (dt from dt_dev when it is not NULL): the time of an
  * RK stage for the boundary values, enqueued before each stage so that a

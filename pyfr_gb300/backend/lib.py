@@ -46,7 +46,8 @@ class Gas(C.Structure):
 # Boundary-condition types and constants (b200_bc_t)
 BC_TYPES = {'sup-in-fa': 1, 'sup-out-fn': 2, 'slp-adia-wall': 3,
             'char-riem-inv': 4, 'no-slp-adia-wall': 5, 'no-slp-isot-wall': 6,
-            'sub-in-frv': 7, 'sub-in-ftpttang': 8, 'sub-out-fp': 9}
+            'sub-in-frv': 7, 'sub-in-ftpttang': 8, 'sub-out-fp': 9,
+            'char-riem-inv-mass-flow': 10, 'char-riem-inv-pressure': 10}
 
 
 class BCOp(C.Structure):
@@ -59,7 +60,8 @@ class BC(C.Structure):
                 ('cpTw', f64), ('cpTt', f64), ('pt', f64), ('vc', f64*3),
                 ('prog', C.c_void_p), ('expr_start', i32*6),
                 ('expr_len', i32*6), ('ploc', C.c_void_p), ('ldp', i64),
-                ('t_dev', C.c_void_p)]
+                ('t_dev', C.c_void_p), ('t', f64), ('ic', f64), ('im', f64),
+                ('ctrl', C.c_void_p)]
 
 
 class Src(C.Structure):

@@ -502,20 +502,86 @@ class PointwiseKernelProvider:
 
     # ---- boundary kernels -------------------------------------------------
 
-    def _bc(self, tplargs):
+    def _bc(self, tplargs, ploc=None):
+        """(b200_bc_t, matrices it points at, run-time arguments) of a
+        boundary kernel.  This package's own interfaces pass the struct
+        ready (tplargs['bc']); PyFR's own interfaces pass the boundary type
+        and its values in tplargs['c'] as numbers or as C expressions of
+        ploc[i] and t (pyfr/solvers/baseadvec/inters.py:81-116), the
+        coordinates as ``ploc``, and bind ``t`` (and, for the controlled
+        characteristic boundaries, ``ic`` and ``im``,
+        pyfr/solvers/euler/inters.py:108-215) at run time."""
         from pyfr_gb300.backend.lib import BC, BC_TYPES
-        bc = tplargs.get('bc')
-        if bc is None:
-            bc = BC(type=BC_TYPES[tplargs['bctype']])
-        return bc
+        from pyfr_gb300.bcexpr import BCExpr, pack
 
-    def _bccflux_euler(self, tplargs, dims, extrns, ul, nl, **kw):
+        bc = tplargs.get('bc')
+        if bc is not None:
+            return bc, [], []
+        bctype, c, nd = tplargs['bctype'], tplargs['c'], tplargs['ndims']
+        if bctype not in BC_TYPES:
+            raise NotImplementedError(f'Boundary type {bctype!r} is not '
+                                      'provided')
+        bc = BC(type=BC_TYPES[bctype])
+        progs, fields = [], ['rho', 'p', 'u', 'v', 'w', 'cpTw']
+        for f, k in enumerate(fields):
+            v = c.get(k)
+            if k in 'uvw' and 'uvw'.index(k) >= nd:
+                v = None
+            if v is None or k == 'cpTw':
+                progs.append([])
+                continue
+            ex = BCExpr(str(v), nd)
+            progs.append(ex.prog)
+            val = ex.const if ex.const is not None else 0.0
+            if k in 'uvw':
+                bc.u['uvw'.index(k)] = val
+            else:
+                setattr(bc, k, val)
+            if ex.uses_x and ploc is None:
+                raise ValueError('Boundary expressions of position need '
+                                 'ploc')
+        bc.cpTw = float(c.get('cpTw', 0.0))
+        bc.cpTt, bc.pt = float(c.get('cpTt', 0.0)), float(c.get('pt', 0.0))
+        for i, v in enumerate(c.get('vc', [])):
+            bc.vc[i] = float(v)
+
+        mats, rt = [], ['t']
+        if any(progs):
+            arr, spans = pack(progs)
+            prog = self.backend.const_matrix(arr.view(np.int64)[None, :],
+                                             dtype=np.int64)
+            bc.prog = prog.data
+            for f, (start, n) in enumerate(spans):
+                bc.expr_start[f], bc.expr_len[f] = start, n
+            mats.append(prog)
+            if ploc is not None:
+                bc.ploc, bc.ldp = ploc.data, ploc.leaddim
+                mats.append(ploc)
+        if bctype in ('char-riem-inv-mass-flow', 'char-riem-inv-pressure'):
+            rt += ['ic', 'im']
+        return bc, mats, rt
+
+    @staticmethod
+    def _bc_kernel(run, bc, rt, **kw):
+        """A boundary kernel whose struct takes the run-time arguments
+        (the time, the controller's interpolation) before each launch."""
+        def brun(stream, **args):
+            for k, v in args.items():
+                setattr(bc, k, float(v))
+            run(stream)
+
+        if not rt:
+            return Kernel(run, **kw)
+        return BindableKernel(brun, rt, {k: 0.0 for k in rt}, **kw)
+
+    def _bccflux_euler(self, tplargs, dims, extrns, ul, nl, ploc=None,
+                       **kw):
         (n,) = dims
         rs = _rsolver(tplargs)
         fn, nd, gamma = (self._fn('bccflux_euler'), tplargs['ndims'],
                          tplargs['c']['gamma'])
         p_min = tplargs.get('p_min', P_MIN_DEFAULT)
-        bc = self._bc(tplargs)
+        bc, bmats, rt = self._bc(tplargs, ploc)
         lb, lm, _ = _view(ul)
         np_, nlp = _mat(nl)
         ix64 = self._ix64
@@ -524,15 +590,17 @@ class PointwiseKernelProvider:
             fn(nd, n, rs, gamma, p_min, C.byref(bc), lb, lm, ix64, np_, nlp,
                stream)
 
-        return Kernel(run, mats=[nl], views=[ul], misc=[bc], name='bccflux',
-                      meta=dict(kind='bccflux_euler', tplargs=tplargs,
-                                dims=dims))
+        return self._bc_kernel(run, bc, rt, mats=[nl] + bmats, views=[ul],
+                               misc=[bc], name='bccflux',
+                               meta=dict(kind='bccflux_euler',
+                                         tplargs=tplargs, dims=dims))
 
-    def _bcconu(self, tplargs, dims, extrns, ulin, ulout, nlin, **kw):
+    def _bcconu(self, tplargs, dims, extrns, ulin, ulout, nlin, ploc=None,
+                **kw):
         (n,) = dims
         fn, nd, gamma = (self._fn('bcconu'), tplargs['ndims'],
                          tplargs['c']['gamma'])
-        bc = self._bc(tplargs)
+        bc, bmats, rt = self._bc(tplargs, ploc)
         ib, im, _ = _view(ulin)
         ob, om, _ = _view(ulout)
         np_, nlp = _mat(nlin)
@@ -542,11 +610,12 @@ class PointwiseKernelProvider:
             fn(nd, n, gamma, C.byref(bc), ib, im, ob, om, ix64, np_, nlp,
                stream)
 
-        return Kernel(run, mats=[nlin], views=[ulin, ulout], misc=[bc],
-                      name='bcconu', meta=dict(kind='bcconu', dims=dims))
+        return self._bc_kernel(run, bc, rt, mats=[nlin] + bmats,
+                               views=[ulin, ulout], misc=[bc], name='bcconu',
+                               meta=dict(kind='bcconu', dims=dims))
 
     def _bccflux_ns(self, tplargs, dims, extrns, ul, gradul, nl,
-                    artvisc=None, **kw):
+                    artvisc=None, ploc=None, **kw):
         if (tplargs.get('shock_capturing') == 'artificial-viscosity') != \
                 (artvisc is not None):
             raise ValueError('Artificial viscosity needs its field')
@@ -558,7 +627,7 @@ class PointwiseKernelProvider:
         gas = _gas(c, tplargs.get('visc_corr', 'none'),
                    p_min=tplargs.get('p_min', P_MIN_DEFAULT))
         fn, nd = self._fn('bccflux_ns'), tplargs['ndims']
-        bc = self._bc(tplargs)
+        bc, bmats, rt = self._bc(tplargs, ploc)
         lb, lm, _ = _view(ul)
         gb, gm, gr = _view(gradul)
         np_, nlp = _mat(nl)
@@ -577,11 +646,11 @@ class PointwiseKernelProvider:
                 fn(nd, n, rs, C.byref(gas), tau, C.byref(bc), lb, lm, gb, gm,
                    gr, ix64, np_, nlp, stream)
 
-        return Kernel(run, mats=[nl],
-                      views=[ul, gradul] +
-                      ([artvisc] if artvisc is not None else []),
-                      misc=[gas, bc],
-                      name='bccflux', meta=dict(kind='bccflux_ns', dims=dims))
+        return self._bc_kernel(run, bc, rt, mats=[nl] + bmats,
+                               views=[ul, gradul] +
+                               ([artvisc] if artvisc is not None else []),
+                               misc=[gas, bc], name='bccflux',
+                               meta=dict(kind='bccflux_ns', dims=dims))
 
     def _intconu(self, tplargs, dims, extrns, ulin, urin, ulout, urout):
         (n,) = dims

@@ -45,6 +45,12 @@ struct BcK {
     const T *ploc;
     int64_t ldp;
     const double *t_dev;
+    T t;
+    // Controlled pressure p = ic + im*t (type B200_BC_CHAR_RIEM_INV_CTRL)
+    T ic, im;
+    const double *ctrl;
+    // Values to form per point: programs or the controlled pressure
+    int perpt;
 };
 
 // The boundary values at point i: the programs evaluated and the derived
@@ -52,14 +58,18 @@ struct BcK {
 template <int ND, typename T>
 __device__ __forceinline__ void bc_at_point(BcK<T> &b, int64_t i, T gamma) {
     T x[3] = {0, 0, 0};
+    if (b.ploc)
 #pragma unroll
-    for (int d = 0; d < ND; d++) x[d] = b.ploc[d * b.ldp + i];
-    const T t = (T)b.t_dev[0];
+        for (int d = 0; d < ND; d++) x[d] = b.ploc[d * b.ldp + i];
+    const T t = b.t_dev ? (T)b.t_dev[0] : b.t;
     T *dst[6] = {&b.rho, &b.p, &b.u[0], &b.u[1], &b.u[2], &b.cpTw_g};
     for (int f = 0; f < 6; f++)
         if (b.elen[f]) *dst[f] = b200::expr_program<T>(b.prog, b.estart[f], b.elen[f], x, t);
     if (b.elen[5]) b.cpTw_g /= gamma;
-    if (b.elen[0] || b.elen[1]) {
+    const bool ctrl = b.type == B200_BC_CHAR_RIEM_INV_CTRL;
+    if (ctrl)
+        b.p = b.ctrl ? (T)(b.ctrl[0] + b.ctrl[1] * (double)t) : b.ic + b.im * t;
+    if (ctrl || b.elen[0] || b.elen[1]) {
         const T cs = b.rho > 0 && b.p > 0 ? sqrt(gamma * b.p / b.rho) : T(0);
         b.cs = cs;
         b.s = b.rho > 0 ? b.p * pow(b.rho, -gamma) : T(0);
@@ -94,13 +104,18 @@ BcK<T> bc_consts(const b200_bc_t &b, double gamma) {
     k.ploc = static_cast<const T *>(b.ploc);
     k.ldp = b.ldp;
     k.t_dev = b.t_dev;
+    k.t = (T)b.t;
+    k.ic = (T)b.ic;
+    k.im = (T)b.im;
+    k.ctrl = b.ctrl;
+    k.perpt = k.nexpr > 0 || b.type == B200_BC_CHAR_RIEM_INV_CTRL;
     return k;
 }
 
-// Programs need the point coordinates and the time
+// Programs need the point coordinates
 template <typename T>
 bool bc_exprs_ok(const BcK<T> &k) {
-    return !k.nexpr || (k.ploc && k.t_dev);
+    return !k.nexpr || k.ploc;
 }
 
 // Ghost state of the Riemann solve (bc_rsolve_state)
@@ -133,7 +148,8 @@ __device__ __forceinline__ void bc_rsolve_state(const BcK<T> &bc, T gamma, const
         ur[NV - 1] = ul[NV - 1];
         break;
     }
-    case B200_BC_CHAR_RIEM_INV: {
+    case B200_BC_CHAR_RIEM_INV:
+    case B200_BC_CHAR_RIEM_INV_CTRL: {
         // Riemann invariants of the free stream and of the interior
         const T inv = T(1) / ul[0];
         T ve = 0, vi = 0, k2 = 0;
@@ -267,7 +283,8 @@ __device__ __forceinline__ void bc_ldg_grad_state(const BcK<T> &bc, const T *us,
                                                   const T gl[ND][ND + 2], T gr[ND][ND + 2]) {
     constexpr int NV = ND + 2;
     const bool zero = bc.type == B200_BC_SUP_IN_FA || bc.type == B200_BC_CHAR_RIEM_INV ||
-                      bc.type == B200_BC_SUB_IN_FRV || bc.type == B200_BC_SUB_OUT_FP;
+                      bc.type == B200_BC_CHAR_RIEM_INV_CTRL || bc.type == B200_BC_SUB_IN_FRV ||
+                      bc.type == B200_BC_SUB_OUT_FP;
 #pragma unroll
     for (int d = 0; d < ND; d++)
 #pragma unroll
@@ -334,7 +351,7 @@ bccflux_euler_kernel(int64_t n, T gamma, T p_min, BcK<T> bc0, ScalView<T> vl, in
     const int64_t i = (int64_t)blockIdx.x * BC_BLOCK + threadIdx.x;
     if (i >= n) return;
     BcK<T> bc = bc0;
-    if (bc.nexpr) bc_at_point<ND, T>(bc, i, gamma);
+    if (bc.perpt) bc_at_point<ND, T>(bc, i, gamma);
     T *pl = vl.base + b200::load_ix(vl.map, ix64, i);
     T ul[NV], ur[NV], nn[ND], fn[NV];
 #pragma unroll
@@ -354,7 +371,7 @@ bcconu_kernel(int64_t n, T gamma, BcK<T> bc0, ScalView<T> vin, ScalView<T> vout,
     const int64_t i = (int64_t)blockIdx.x * BC_BLOCK + threadIdx.x;
     if (i >= n) return;
     BcK<T> bc = bc0;
-    if (bc.nexpr) bc_at_point<ND, T>(bc, i, gamma);
+    if (bc.perpt) bc_at_point<ND, T>(bc, i, gamma);
     const T *pi = vin.base + b200::load_ix(vin.map, ix64, i);
     T *po = vout.base + b200::load_ix(vout.map, ix64, i);
     T ul[NV], ur[NV], nn[ND];
@@ -375,7 +392,7 @@ bccflux_ns_kernel(int64_t n, b200::GasK<T> gas, T tau, BcK<T> bc0, ScalView<T> v
     const int64_t i = (int64_t)blockIdx.x * BC_BLOCK + threadIdx.x;
     if (i >= n) return;
     BcK<T> bc = bc0;
-    if (bc.nexpr) bc_at_point<ND, T>(bc, i, gas.gamma);
+    if (bc.perpt) bc_at_point<ND, T>(bc, i, gas.gamma);
     T *pl = vl.base + b200::load_ix(vl.map, ix64, i);
     T ul[NV], ur[NV], nn[ND], fi[NV];
 #pragma unroll
@@ -444,7 +461,7 @@ bccent_kernel(int64_t n, T gamma, BcK<T> bc0, ScalView<T> vl, ScalView<T> ve, in
     const int64_t i = (int64_t)blockIdx.x * BC_BLOCK + threadIdx.x;
     if (i >= n) return;
     BcK<T> bc = bc0;
-    if (bc.nexpr) bc_at_point<ND, T>(bc, i, gamma);
+    if (bc.perpt) bc_at_point<ND, T>(bc, i, gamma);
     const T *pl = vl.base + b200::load_ix(vl.map, ix64, i);
     T *pe = ve.base + b200::load_ix(ve.map, ix64, i);
     T ul[NV], ur[NV], nn[ND];
@@ -463,18 +480,24 @@ bccent_kernel(int64_t n, T gamma, BcK<T> bc0, ScalView<T> vl, ScalView<T> ve, in
     atomic_min_nonneg(pe, e);
 }
 
-bool bc_type_ok(int t) { return t >= B200_BC_SUP_IN_FA && t <= B200_BC_SUB_OUT_FP; }
+bool bc_type_ok(int t) { return t >= B200_BC_SUP_IN_FA && t <= B200_BC_CHAR_RIEM_INV_CTRL; }
+
+// The boundary types of the Euler system
+bool bc_euler_type(int t) {
+    return (t >= B200_BC_SUP_IN_FA && t <= B200_BC_CHAR_RIEM_INV) ||
+           t == B200_BC_CHAR_RIEM_INV_CTRL;
+}
 
 template <typename T>
 int bccflux_euler(int ndims, int64_t n, int rs, double gamma, double p_min, const b200_bc_t *bc,
                   T *ul_base, const void *ul_map, int ix64, const T *nl, int64_t ldn,
                   cudaStream_t st) {
     if (n <= 0) return B200_OK;
-    if (!bc || !bc_type_ok(bc->type) || bc->type > B200_BC_CHAR_RIEM_INV)
+    if (!bc || !bc_euler_type(bc->type))
         return b200::set_error(B200_ERR_ARG, "bccflux_euler: bad boundary type");
     const auto k = bc_consts<T>(*bc, gamma);
     if (!bc_exprs_ok(k))
-        return b200::set_error(B200_ERR_ARG, "boundary expressions need ploc and t");
+        return b200::set_error(B200_ERR_ARG, "boundary expressions need ploc");
     ScalView<T> l{ul_base, ul_map};
     const unsigned grid = b200::ceil_div(n, BC_BLOCK);
     if (ndims != 2 && ndims != 3)
@@ -500,7 +523,7 @@ int bcconu(int ndims, int64_t n, double gamma, const b200_bc_t *bc, const T *in_
         return b200::set_error(B200_ERR_ARG, "bcconu: bad boundary type");
     const auto k = bc_consts<T>(*bc, gamma);
     if (!bc_exprs_ok(k))
-        return b200::set_error(B200_ERR_ARG, "boundary expressions need ploc and t");
+        return b200::set_error(B200_ERR_ARG, "boundary expressions need ploc");
     ScalView<T> vi{const_cast<T *>(in_base), in_map}, vo{out_base, out_map};
     const unsigned grid = b200::ceil_div(n, BC_BLOCK);
     if (ndims == 2)
@@ -529,7 +552,7 @@ int bccflux_ns(int ndims, int64_t n, int rs, const b200_gas_t *gas, double tau,
     const auto g = b200::gas_consts<T>(g0);
     const auto k = bc_consts<T>(*bc, g0.gamma);
     if (!bc_exprs_ok(k))
-        return b200::set_error(B200_ERR_ARG, "boundary expressions need ploc and t");
+        return b200::set_error(B200_ERR_ARG, "boundary expressions need ploc");
     ScalView<T> l{ul_base, ul_map};
     VectView<T> gv{gl_base, gl_map, gl_rstr};
     const unsigned grid = b200::ceil_div(n, BC_BLOCK);
@@ -556,7 +579,7 @@ int bccent(int ndims, int64_t n, double gamma, const b200_bc_t *bc, const T *ul_
         return b200::set_error(B200_ERR_ARG, "bccent: bad boundary type");
     const auto k = bc_consts<T>(*bc, gamma);
     if (!bc_exprs_ok(k))
-        return b200::set_error(B200_ERR_ARG, "boundary expressions need ploc and t");
+        return b200::set_error(B200_ERR_ARG, "boundary expressions need ploc");
     ScalView<T> l{const_cast<T *>(ul_base), ul_map}, e{ent_base, ent_map};
     const T big = sizeof(T) == 8 ? (T)1.7976931348623157e308 : (T)3.4028234663852886e38;
     const unsigned grid = b200::ceil_div(n, BC_BLOCK);

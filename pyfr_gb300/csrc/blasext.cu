@@ -230,19 +230,10 @@ axnpby_scaled_kernel(int64_t n, int nv, T *__restrict__ x0, AxnpbyArgs<T> args,
 // Block partials of the error norm over the points of one element type;
 // layout (nupts, nvars, neles) AoSoA with leading dimension ld.  One warp
 // takes one (point, 32-element block) pair per iteration, lane = element
-// within the block; lanes of padding elements past neles are skipped.  The quotient err/(atol + rtol*|u|) uses a reciprocal refined
-// by two Newton-Raphson steps, r <- r + r*(1 - d*r), from a single-
-// precision estimate (relative error about 2^-23 before, below 2^-52
-// after): GB300's FP64 unit is narrow and an IEEE double division costs
-// several times that.
-__device__ __forceinline__ double rcp_newton(double d) {
-    float r0;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(b200::narrow_f64(d)));
-    double r = b200::widen_f32(r0);
-    r = fma(r, fma(-d, r, 1.0), r);
-    r = fma(r, fma(-d, r, 1.0), r);
-    return r;
-}
+// within the block; lanes of padding elements past neles are skipped.
+// The quotient err/(atol + rtol*|u|) uses the Newton-refined reciprocal
+// b200::rcp_f64.
+__device__ __forceinline__ double rcp_newton(double d) { return b200::rcp_f64(d); }
 
 template <typename T>
 __global__ void __launch_bounds__(BX_BLOCK)

@@ -69,6 +69,27 @@ __device__ __forceinline__ float narrow_f64(double d) {
     return (float)d;
 }
 
+// 1/d in FP64 without an IEEE division.  A single-precision estimate
+// (rcp.approx.ftz.f32, relative error about 2^-23) refined by two
+// Newton-Raphson steps for f(r) = 1/r - d, r <- r + r*(1 - d*r), each of
+// which squares the relative error (2^-46, then below the rounding of the
+// last step): the result is within about one unit in the last place of
+// the correctly rounded quotient, for 4 FP64 FMAs instead of the several
+// FP64 operations, fix-up tests and slow path of an IEEE division on a GPU
+// whose FP64 unit is narrow.  Operands with |d| outside [2^-100, 2^100]
+// (where the estimate or its reciprocal could leave the binary32 normal
+// range) take the IEEE division.
+__device__ __forceinline__ double rcp_f64(double d) {
+    const uint64_t a = (uint64_t)__double_as_longlong(d) & 0x7fffffffffffffffull;
+    if (a - ((1023ull - 100) << 52) >= (200ull << 52)) return 1.0 / d;
+    float r0;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(narrow_f64(d)));
+    double r = widen_f32(r0);
+    r = fma(r, fma(-d, r, 1.0), r);
+    r = fma(r, fma(-d, r, 1.0), r);
+    return r;
+}
+
 }  // namespace b200
 
 // Status codes of the C ABI

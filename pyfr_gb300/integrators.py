@@ -96,6 +96,12 @@ class RKVdH2Integrator:
         self.tend = cfg.getfloat(sect, 'tend', None)
         self.tcurr = self._restart.stats.getfloat(sect, 'tcurr') \
             if self.isrestart else self.tstart
+
+        # The reference's preproc prepares the boundary controllers once
+        # before the first step (pyfr/integrators/explicit/base.py:39,
+        # pyfr/solvers/base/system.py:435-439)
+        for k in self.system.prepare_kernels(0, self.tcurr):
+            k.run(backend.stream)
         # (the CFL controller computes its own first step size)
         self.dt = cfg.getfloat(sect, 'dt', 0.0) if self.needs_cfl else \
             cfg.getfloat(sect, 'dt')
@@ -107,7 +113,10 @@ class RKVdH2Integrator:
         self.nrhsevals = 0
         self._step_graphs = {}
         self._kcache = {}
-        self.use_step_graph = backend.use_cuda_graphs
+        # (boundary controllers read the solution on the host before every
+        # right-hand side, which a captured step cannot stop for)
+        self.use_step_graph = backend.use_cuda_graphs and \
+            not self.system.controlled_bcs
 
         # The step size lives in device memory (staged through page-locked
         # host memory), so that one captured graph per starting register
@@ -301,13 +310,23 @@ class RKVdH2Integrator:
         lib.event_record(self._t_evt.value, stream)
         self._t_pending = True
 
-    def step_kernels(self, idx, dt):
-        """The kernels of one step starting from register ``idx``, in launch
-        order, and the resulting register indices."""
+    def _prepare_kernels(self, ubank, i, t, dt):
+        """The host steps before stage i's right-hand side (boundary
+        controllers), at the stage time t + c_i dt."""
+        if not self.system.controlled_bcs:
+            return []
+        if t is None:
+            raise ValueError('Boundary controllers need the step time')
+        return self.system.prepare_kernels(ubank, t + self.c[i]*dt)
+
+    def step_kernels(self, idx, dt, t=None):
+        """The kernels of one step starting from register ``idx`` at time
+        ``t``, in launch order, and the resulting register indices."""
         r1, r2, rs = self._regs(idx)
         kl = []
         for i in range(self.nstages):
             kl.extend(self._time_kernels(i))
+            kl.extend(self._prepare_kernels(r2 if i else r1, i, t, dt))
             for g in self.system.rhs_graphs(r2 if i else r1, r2):
                 kl.extend(g.klist)
             for k in self._rk_kerns(i, r1, r2, *rs):
@@ -320,7 +339,7 @@ class RKVdH2Integrator:
 
     def _enqueue_step(self, t, dt, idx, stream):
         """Enqueue every stage of one step; returns the register indices."""
-        kl, regs = self.step_kernels(idx, dt)
+        kl, regs = self.step_kernels(idx, dt, t)
         for k in kl:
             k.run(stream)
         return regs
@@ -681,10 +700,11 @@ class MixedRKIntegrator(RKVdH2Integrator):
                 done.add(j)
         return out, done
 
-    def step_kernels(self, idx, dt):
+    def step_kernels(self, idx, dt, t=None):
         kl = []
         for i in range(self.nstages):
             kl.extend(self._time_kernels(i))
+            kl.extend(self._prepare_kernels(0, i, t, dt))
             rhs = [k for g in self.system.rhs_graphs(0, 1) for k in g.klist]
             rhs, done = self._fuse_stage(rhs, i, dt)
             kl.extend(rhs)

@@ -177,10 +177,17 @@ BC_OPTS = {
     'sub-out-fp': ['p'],
     'sub-in-ftpttang': [],
     'sup-out-fn': [], 'slp-adia-wall': [], 'no-slp-adia-wall': [],
+    # (the pressure comes from the controller, pyfr_gb300/solvers/
+    # bccontrol.py)
+    'char-riem-inv-mass-flow': ['rho', 'u', 'v', 'w'],
+    'char-riem-inv-pressure': ['rho', 'u', 'v', 'w'],
 }
 # Velocity components that default to zero
 _ZERO_UVW = {'no-slp-isot-wall', 'sub-in-frv'}
-EULER_BCS = {'sup-in-fa', 'sup-out-fn', 'slp-adia-wall', 'char-riem-inv'}
+EULER_BCS = {'sup-in-fa', 'sup-out-fn', 'slp-adia-wall', 'char-riem-inv',
+             'char-riem-inv-mass-flow', 'char-riem-inv-pressure'}
+CONTROLLED_BCS = {'char-riem-inv-mass-flow': 'mass-flow',
+                  'char-riem-inv-pressure': 'pressure'}
 
 
 class BaseBCInters(BaseIntInters):
@@ -263,8 +270,18 @@ class BaseBCInters(BaseIntInters):
         self._perm = self._perm_for_field(lhs, scal)
         self._pnorm_lhs = self._const_mat(lhs, 'get_pnorms_for_inters')
 
+        # The controller of a controlled characteristic boundary, whose
+        # pressure p(t) = ic + im*t the kernels form with the stage time
+        self.controller = None
+        if self.type in CONTROLLED_BCS:
+            from pyfr_gb300.solvers.bccontrol import ControlledBC
+            self.controller = ControlledBC(be, cfg, cfgsect, elemap, lhs,
+                                           CONTROLLED_BCS[self.type],
+                                           first.con_to_pri)
+
         # Programs of the expression values and the point coordinates
-        self.time_dependent = any(e.uses_t for e in self.exprs.values())
+        self.time_dependent = any(e.uses_t for e in self.exprs.values()) \
+            or self.controller is not None
         self._prog = self._ploc = None
         if self.exprs:
             from pyfr_gb300.backend.lib import BCOp
@@ -286,7 +303,10 @@ class BaseBCInters(BaseIntInters):
             self.bc.prog = self._prog.data
             self.bc.ploc = self._ploc.data
             self.bc.ldp = self._ploc.leaddim
+        if self.exprs or self.controller:
             self.bc.t_dev = tmat.data + 8
+        if self.controller:
+            self.bc.ctrl = self.controller.ctrl.data
 
     def values_at(self, t):
         """Host values of the options at every boundary point at time t,

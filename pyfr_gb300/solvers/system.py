@@ -244,6 +244,30 @@ class BaseSystem:
                 any(e.src_uses_t for e in self.ele_map.values()))
 
     @property
+    def controlled_bcs(self):
+        """The controllers of the controlled characteristic boundaries."""
+        return [b.controller for b in self._bc_inters
+                if getattr(b, 'controller', None) is not None]
+
+    def prepare_kernels(self, ubank, t):
+        """Host steps before a right-hand side at time t from bank ubank:
+        the boundary controllers (pyfr/solvers/base/system.py:408-415).
+        They read the solution on the host, so they run outside captured
+        graphs."""
+        ctrls = self.controlled_bcs
+        if not ctrls:
+            return []
+
+        def solns():
+            return dict(zip(self.ele_types, self.ele_scal_upts(ubank)))
+
+        def run(stream):
+            for c in ctrls:
+                c.prepare(solns, t, stream)
+
+        return [Kernel(run, name='bcprepare')]
+
+    @property
     def has_src_macros(self):
         return any(e.has_src_macros for e in self.ele_map.values())
 
@@ -280,6 +304,8 @@ class BaseSystem:
             raise ValueError('Invalid register numbers')
         if self.time_dependent:
             self.set_time(t)
+        for k in self.prepare_kernels(uinbank, t):
+            k.run(self.backend.stream)
         for g in self._rhs_graphs_cached(uinbank, foutbank):
             self.backend.run_graph(g)
 

@@ -58,6 +58,10 @@ class _Comm:
     def reduce(self, obj, op=None, root=0):
         return obj
 
+    def exscan(self, obj, op=None):
+        # (undefined on the first rank: mpi4py returns None there)
+        return None
+
     def Allreduce(self, sendbuf, recvbuf, op=None):
         src = sendbuf[0] if isinstance(sendbuf, (list, tuple)) else sendbuf
         dst = recvbuf[0] if isinstance(recvbuf, (list, tuple)) else recvbuf
@@ -167,10 +171,13 @@ def reference_mesh(mesh):
     from pyfr_gb300.shapes import SHAPES
 
     etypes = sorted(mesh.spts)
+    bnames = sorted(getattr(mesh, 'bcon', {}))
     codec = [f'eles/{et}/face/{f}' for et in etypes
              for f in range(len(SHAPES[et].faces))]
+    codec += [f'bc/{b}' for b in bnames]
     cidx = {c: i for i, c in enumerate(codec)}
     cidxmap = {i: (et, int(f)) for i, c in enumerate(codec)
+               if c.startswith('eles/')
                for et, f in [c[5:].split('/face/')]}
 
     def con(side):
@@ -186,7 +193,8 @@ def reference_mesh(mesh):
              spts={et: mesh.spts[et] for et in etypes},
              spts_curved={et: np.zeros(mesh.spts[et].shape[1], bool)
                           for et in etypes},
-             con=(con(lhs), con(rhs)), cidxmap=cidxmap)
+             con=(con(lhs), con(rhs)), cidxmap=cidxmap,
+             bcon={b: con(mesh.bcon[b]) for b in bnames})
     return m
 
 
@@ -197,7 +205,9 @@ def reference_cfg(cfg):
 
 
 def run(case, n, steps, out=None, fake=False, source=False, single=False):
-    """Advance ``case`` ('vortex' or 'tgv') on an n-cell mesh by ``steps``
+    """Advance ``case`` ('vortex' or 'tgv' on an n-cell mesh, or a
+    boundary case 'bc-euler:<type>,<type>' / 'bc-ns:<type>,<type>' of
+    ``tests/bc_cases.py``) by ``steps``
     RK45 steps with PyFR's own integrator on the b200 backend (with
     ``source``, and the case's [solver-plugin-source] terms through PyFR's
     own source plugin); returns the initial and final solutions, the step
@@ -213,6 +223,11 @@ def run(case, n, steps, out=None, fake=False, source=False, single=False):
 
     if case == 'vortex':
         cfg, mesh = euler_vortex(n=n, order=3, dt=1e-3)
+    elif case.startswith('bc-'):
+        # 'bc-euler:<type>,<type>' or 'bc-ns:<type>,<type>'
+        from tests.bc_cases import bc_case
+        kind, types = case[3:].split(':')
+        cfg, mesh, _ = bc_case(kind, types.split(','))
     else:
         cfg, mesh = ns_tgv(n=n, order=3, dt=1e-3)
     if source:
@@ -241,7 +256,8 @@ def run(case, n, steps, out=None, fake=False, source=False, single=False):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument('--case', default='vortex', choices=['vortex', 'tgv'])
+    ap.add_argument('--case', default='vortex',
+                    help="'vortex', 'tgv' or 'bc-euler|bc-ns:<type>,<type>'")
     ap.add_argument('--n', type=int, default=8)
     ap.add_argument('--steps', type=int, default=5)
     ap.add_argument('--out')

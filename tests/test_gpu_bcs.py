@@ -9,6 +9,8 @@ import numpy as np
 import pytest
 
 from oracle.fr_oracle import rk45_step
+from tests.bc_cases import FREE, GAS, TOTAL, vc as _vc
+from tests.bc_cases import bc_cfg as _cfg
 from tests.test_oracle import bc_disc
 
 pytestmark = pytest.mark.gpu
@@ -24,39 +26,6 @@ def built():
 
 def _relerr(a, b):
     return np.abs(a - b).max()/max(np.abs(b).max(), 1e-300)
-
-
-GAS = dict(gamma=1.4, mu=0.02, Pr=0.72, **{'ldg-beta': 0.5, 'ldg-tau': 0.1})
-FREE = dict(rho=1.1, p=0.95, u=[0.35, -0.15, 0.2])
-
-
-def _cfg(ndims, specs, rsolver='rusanov', precision='double', ns=False):
-    from pyfr_gb300.inifile import Inifile
-    cfg = Inifile()
-    cfg.set('backend', 'precision', precision)
-    for k in ('gamma', 'mu', 'Pr'):
-        cfg.set('constants', k, GAS[k])
-    cfg.set('solver', 'order', 3)
-    cfg.set('solver-interfaces', 'riemann-solver', rsolver)
-    cfg.set('solver-interfaces', 'ldg-beta', GAS['ldg-beta'])
-    cfg.set('solver-interfaces', 'ldg-tau', GAS['ldg-tau'])
-    cfg.set('solver-time-integrator', 'dt', 1e-3)
-    for name, spec in specs.items():
-        sect = f'soln-bcs-{name}'
-        cfg.set(sect, 'type', spec['type'])
-        for k in ('rho', 'p', 'cpTw', 'cpTt', 'pt', 'theta', 'phi'):
-            if k in spec:
-                cfg.set(sect, k, spec[k])
-        for k, v in zip('uvw', spec.get('u', [])):
-            cfg.set(sect, k, v)
-    x = '2*pi*x'
-    cfg.set('soln-ics', 'rho', f'1 + 0.1*sin({x})*cos(2*pi*y)')
-    cfg.set('soln-ics', 'u', '0.3 + 0.1*y')
-    cfg.set('soln-ics', 'v', f'0.1*sin({x})')
-    if ndims == 3:
-        cfg.set('soln-ics', 'w', '0.05*cos(2*pi*z)')
-    cfg.set('soln-ics', 'p', '1 + 0.05*cos(2*pi*y)')
-    return cfg
 
 
 def _backend(cfg):
@@ -87,16 +56,6 @@ NS = [('no-slp-adia-wall', 'no-slp-adia-wall'),
       ('no-slp-isot-wall', 'slp-adia-wall'),
       ('sup-in-fa', 'sup-out-fn'), ('char-riem-inv', 'no-slp-isot-wall'),
       ('sub-in-frv', 'sub-out-fp'), ('sub-in-ftpttang', 'sup-out-fn')]
-
-# Total state of the sub-in-ftpttang inflow: cp*T_t, p_t and the direction
-# (theta, phi) in degrees
-TOTAL = dict(cpTt=3.9, pt=1.08, theta=20.0, phi=80.0)
-
-
-def _vc(theta, phi):
-    t, f = np.radians(theta), np.radians(phi)
-    return [np.cos(t)*np.sin(f), np.sin(t)*np.sin(f), np.cos(f)]
-
 
 @pytest.mark.parametrize('types', NS)
 def test_ns_bcs_rhs(built, types):
@@ -152,3 +111,40 @@ def test_euler_bcs_chosen_form(built, types):
     chosen.run_steps(10)
     (a,), (b,) = chosen.soln, plain.soln
     assert np.linalg.norm(a - b)/np.linalg.norm(b) < 1e-6
+
+
+@pytest.mark.parametrize('kind,types', [
+    ('euler', ('char-riem-inv-mass-flow', 'sup-out-fn')),
+    ('euler', ('char-riem-inv-pressure', 'char-riem-inv')),
+    ('ns', ('char-riem-inv-pressure', 'no-slp-adia-wall')),
+    ('ns', ('no-slp-isot-wall', 'char-riem-inv-mass-flow'))])
+def test_controlled_bcs_rhs(built, kind, types):
+    """The controlled characteristic boundaries' ghost state with the
+    pressure p(t) = ic + im*t of their controller (set here, with the
+    controller between updates) against the oracle's char-riem-inv at that
+    pressure, t = 0.3."""
+    from pyfr_gb300.solvers.system import EulerSystem, NavierStokesSystem
+    from tests.bc_cases import bc_case
+    cfg, mesh, specs = bc_case(kind, types)
+    cls = EulerSystem if kind == 'euler' else NavierStokesSystem
+    s = cls(_backend(cfg), mesh, None, 2, cfg)
+    s.commit()
+    ctrls = s.controlled_bcs
+    assert len(ctrls) == 1 and s.time_dependent
+    (c,) = ctrls
+    c.interp_c, c.interp_m = 0.8, 0.5
+    c.tprev, c.nstep_counter = 0.1, 1
+    s.rhs(0.3, 0, 1)
+    assert c.nstep_counter == 2 and not c.history
+    (u,), (r,) = s.ele_scal_upts(0), s.ele_scal_upts(1)
+    ospecs = {n: dict(sp, type='char-riem-inv', p=0.8 + 0.5*0.3)
+              if sp['type'].startswith('char-riem-inv-') else sp
+              for n, sp in specs.items()}
+    if kind == 'euler':
+        d, _ = bc_disc('quad', (4, 3), (True, False), ospecs)
+        ref = d.rhs_euler(u, GAS)
+    else:
+        d, _ = bc_disc('hex', (2, 2, 3), (True, True, False), ospecs,
+                       ns=True)
+        ref = d.rhs_ns(u, GAS)
+    assert _relerr(r, ref) < TOL

@@ -100,3 +100,85 @@ def test_reference_solver_single_fused(built, tmp_path):
     err = max(np.abs(d['u1'][:, v] - u[:, v]).max()/np.abs(u[:, v]).max()
               for v in range(u.shape[1]))
     assert err < 1e-5, err
+
+
+BC_CASES = [('euler', ('sup-in-fa', 'sup-out-fn')),
+            ('euler', ('char-riem-inv', 'slp-adia-wall')),
+            ('ns', ('no-slp-isot-wall', 'sub-out-fp')),
+            ('ns', ('sub-in-frv', 'sub-in-ftpttang')),
+            ('ns', ('char-riem-inv', 'no-slp-adia-wall'))]
+
+
+@pytest.mark.parametrize('kind,types', BC_CASES)
+def test_reference_solver_boundaries(built, tmp_path, kind, types):
+    """PyFR's own boundary interfaces (their values in the kernels'
+    template arguments, pyfr/solvers/{euler,navstokes}/inters.py) on the
+    b200 backend: three RK45 steps of a box bounded in one direction
+    against the oracle's at 1e-10."""
+    if reference_tree() is None:
+        pytest.skip('reference source tree not present')
+    from oracle.fr_oracle import rk45_step
+    from tests.bc_cases import GAS, bc_case
+    from tests.test_oracle import bc_disc
+
+    out = tmp_path / 'soln.npz'
+    r = subprocess.run([sys.executable, '-m', 'tests.refstack', '--case',
+                        f'bc-{kind}:{",".join(types)}', '--steps', '3',
+                        '--out', str(out)], cwd=ROOT, capture_output=True,
+                       text=True, timeout=900)
+    assert r.returncode == 0, r.stderr[-3000:]
+    d = np.load(out)
+    _, _, specs = bc_case(kind, types)
+    if kind == 'euler':
+        disc, _ = bc_disc('quad', (4, 3), (True, False), specs)
+        rhs = lambda x: disc.rhs_euler(x, GAS)           # noqa: E731
+    else:
+        disc, _ = bc_disc('hex', (2, 2, 3), (True, True, False), specs,
+                          ns=True)
+        rhs = lambda x: disc.rhs_ns(x, GAS)              # noqa: E731
+    u = d['u0']
+    for _ in range(3):
+        u = rk45_step(rhs, u, float(d['dt']))
+    err = max(np.abs(d['u1'][:, v] - u[:, v]).max()/np.abs(u[:, v]).max()
+              for v in range(u.shape[1]))
+    assert err < 1e-10, err
+
+
+@pytest.mark.parametrize('kind,types', [
+    ('euler', ('char-riem-inv-mass-flow', 'sup-out-fn')),
+    ('ns', ('char-riem-inv-pressure', 'no-slp-adia-wall'))])
+def test_reference_controlled_bcs(built, tmp_path, kind, types):
+    """PyFR's own controlled boundaries (its host controller,
+    pyfr/solvers/euler/inters.py:108-294, measuring the b200 solution and
+    binding ic and im into the b200 kernels every right-hand side) against
+    this package's controller on the same case: eight RK45 steps, with
+    controller updates every three right-hand sides, agree at 1e-10."""
+    if reference_tree() is None:
+        pytest.skip('reference source tree not present')
+    from pyfr_gb300.backend import B200Backend
+    from pyfr_gb300.integrators import RKVdH2Integrator
+    from pyfr_gb300.solvers.system import EulerSystem, NavierStokesSystem
+    from tests.bc_cases import bc_case
+
+    out = tmp_path / 'soln.npz'
+    r = subprocess.run([sys.executable, '-m', 'tests.refstack', '--case',
+                        f'bc-{kind}:{",".join(types)}', '--steps', '8',
+                        '--out', str(out)], cwd=ROOT, capture_output=True,
+                       text=True, timeout=900)
+    assert r.returncode == 0, r.stderr[-3000:]
+    d = np.load(out)
+    cfg, mesh, _ = bc_case(kind, types)
+    cls = EulerSystem if kind == 'euler' else NavierStokesSystem
+    intg = RKVdH2Integrator(B200Backend(cfg), cls, mesh, cfg)
+    (u0,) = intg.soln
+    assert np.abs(u0 - d['u0']).max() < 1e-14
+    intg.run_steps(8)
+    (u1,) = intg.soln
+    (c,) = intg.system.controlled_bcs
+    assert len(c.history) >= 10
+    err = max(np.abs(d['u1'][:, v] - u1[:, v]).max()/np.abs(u1[:, v]).max()
+              for v in range(u1.shape[1]))
+    assert err < 1e-10, err
+    # The controller moved the pressure: the run differs from one at the
+    # initial pressure
+    assert abs(c.interp_m) > 0
