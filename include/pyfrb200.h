@@ -491,6 +491,20 @@ int b200_negdivconf_f64(int nvars, int nupts, int64_t neles, double *r, int64_t 
 int b200_negdivconf_f32(int nvars, int nupts, int64_t neles, float *r, int64_t ldr,
                         const float *rcpdjac, int64_t ldj, void *stream);
 
+/* Pack the n points of a view (base, map and, for nrow > 1, the row
+ * strides rstr; int64 maps when ix64) into the exchange buffer out of
+ * leading dimension ldo: out[r*ldo + (i/32)*32*ncol + c*32 + i%32] = the
+ * view's value (r, c) of point i -- the layout of a matrix of io-shape
+ * (nrow, ncol, n), which a view of identity map reads back.  Replaces the
+ * pack kernel of pyfr/backends/cuda/packing.py:8-60 (and
+ * pyfr/backends/base/kernels/packing.mako) for the faces shared with
+ * another partition; the unpack is a host-to-device copy of the peer's
+ * buffer. */
+int b200_pack_view_f64(int64_t n, int nrow, int ncol, const double *base, const void *map,
+                       const void *rstr, int ix64, double *out, int64_t ldo, void *stream);
+int b200_pack_view_f32(int64_t n, int nrow, int ncol, const float *base, const void *map,
+                       const void *rstr, int ix64, float *out, int64_t ldo, void *stream);
+
 /* Source terms: the [solver-plugin-source] expressions of each variable
  * (pyfr/plugins/source.py:15-31, pyfr/plugins/kernels/source.mako) as
  * programs of the point's coordinates ploc, the time and the solution u,

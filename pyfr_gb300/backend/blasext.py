@@ -101,6 +101,23 @@ class BlasExtKernels:
 
         return Kernel(run, mats=[dst, src], name='copy')
 
+    def pack_view(self, view, out):
+        """Gather the points of ``view`` into the exchange buffer ``out``
+        (io-shape (nvrow, nvcol, n)): b200_pack_view_*."""
+        if out.ioshape != (view.nvrow, view.nvcol, view.n):
+            raise ValueError('Exchange buffer does not match the view')
+        be = self.backend
+        fn = getattr(be.lib, f'pack_view_{self._sfx}')
+        n, nr, nc = view.n, view.nvrow, view.nvcol
+        b, m = view.basedata, view.mapping.data
+        r = view.rstrides.data if view.rstrides is not None else None
+        ix64, op, ld = int(be.ixdtype == np.int64), out.data, out.leaddim
+
+        def run(stream):
+            fn(n, nr, nc, b, m, r, ix64, op, ld, stream)
+
+        return Kernel(run, mats=[out], views=[view], name='pack')
+
     def zero(self, m):
         be, nbytes = self.backend, m.nrow*m.leaddim*m.itemsize
         p = m.data

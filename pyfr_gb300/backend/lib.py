@@ -104,6 +104,7 @@ def _sig_pointwise(fp):
         'negdivconf': [i32, i32, i64, vp, i64, vp, i64, vp],
         'srcterms': [i32, i32, i32, i32, i64, vp, i64, vp, i64,
                      C.POINTER(Src), vp],
+        'pack_view': [i64, i32, i32, vp, vp, vp, i32, vp, i64, vp],
         'intcflux_euler': [i32, i64, i32, f64, f64, vp, vp, vp, vp, i32, vp,
                            i64, i32, vp],
         'intcflux_ns': [i32, i64, i32, C.POINTER(Gas), f64, f64, vp, vp, vp,

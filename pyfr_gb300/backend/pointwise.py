@@ -652,6 +652,34 @@ class PointwiseKernelProvider:
                                misc=[gas, bc], name='bccflux',
                                meta=dict(kind='bccflux_ns', dims=dims))
 
+    def _mpiconu(self, tplargs, dims, extrns, ulin, urin, ulout,
+                 urout=None):
+        """The common solution at faces shared with another partition,
+        written to this side only (pyfr/solvers/navstokes/kernels/
+        mpiconu.mako:4-19): the two-sided kernel in its both-sides form
+        with the received data as the right side and a scratch view (urout)
+        for the other side's copy."""
+        if urout is None:
+            raise NotImplementedError('mpiconu needs a scratch view for the '
+                                      'other side')
+        return self._intconu(tplargs | {'both_sides': True}, dims, extrns,
+                             ulin, urin, ulout, urout)
+
+    def _mpicflux(self, tplargs, dims, extrns, ul, ur, nl, gradul=None,
+                  gradur=None, artvisc=None):
+        """The common flux at faces shared with another partition
+        (pyfr/solvers/{euler,navstokes}/kernels/mpicflux.mako): the
+        interface kernel with the received data, seen through a view, as
+        its right side (which it also writes, unread)."""
+        from pyfr_gb300.backend.types import View
+        if not isinstance(ur, View):
+            raise NotImplementedError('mpicflux reads the received data '
+                                      'through a view')
+        if gradul is None:
+            return self._intcflux_euler(tplargs, dims, extrns, ul, ur, nl)
+        return self._intcflux_ns(tplargs, dims, extrns, ul, ur, gradul,
+                                 gradur, nl, artvisc=artvisc)
+
     def _intconu(self, tplargs, dims, extrns, ulin, urin, ulout, urout):
         (n,) = dims
         beta = tplargs['c']['ldg-beta']
@@ -720,6 +748,10 @@ _BUILDERS = {
     'pyfr.solvers.navstokes.kernels.intcflux':
         PointwiseKernelProvider._intcflux_ns,
     'pyfr.solvers.navstokes.kernels.intconu': PointwiseKernelProvider._intconu,
+    'pyfr.solvers.navstokes.kernels.mpiconu': PointwiseKernelProvider._mpiconu,
+    'pyfr.solvers.euler.kernels.mpicflux': PointwiseKernelProvider._mpicflux,
+    'pyfr.solvers.navstokes.kernels.mpicflux':
+        PointwiseKernelProvider._mpicflux,
     'pyfr.integrators.explicit.kernels.rkvdh2':
         PointwiseKernelProvider._rkvdh2,
     'pyfr.solvers.euler.kernels.wavespeed':

@@ -360,6 +360,36 @@ int srcterms(int mode, int ndims, int nvars, int nupts, int64_t neles, T *r, int
     return B200_OK;
 }
 
+// Pack a view into an AoSoA buffer: out[r*ldo + soa(i, c, ncol)] = the
+// view's (r, c) value of point i (pyfr/backends/base/kernels/
+// packing.mako:1-11, in this package's AoSoA exchange layout, which a view
+// of identity map reads back directly).  One thread per point.
+template <typename T>
+__global__ void __launch_bounds__(PW_BLOCK)
+pack_view_kernel(int64_t n, int nrow, int ncol, const T *__restrict__ base, const void *map,
+                 const void *rstr, int ix64, T *__restrict__ out, int64_t ldo) {
+    const int64_t i = (int64_t)blockIdx.x * PW_BLOCK + threadIdx.x;
+    if (i >= n) return;
+    const T *p = base + b200::load_ix(map, ix64, i);
+    const int64_t rs = rstr ? b200::load_ix(rstr, ix64, i) : 0;
+    for (int r = 0; r < nrow; r++)
+        for (int c = 0; c < ncol; c++)
+            out[r * ldo + soa_off(i, c, ncol)] = p[r * rs + c * B200_SOASZ];
+}
+
+template <typename T>
+int pack_view(int64_t n, int nrow, int ncol, const T *base, const void *map, const void *rstr,
+              int ix64, T *out, int64_t ldo, cudaStream_t stream) {
+    if (n <= 0) return B200_OK;
+    if (!base || !map || !out || nrow < 1 || ncol < 1 || (nrow > 1 && !rstr) ||
+        ldo < b200::ceil_div(n, B200_SOASZ) * (int64_t)B200_SOASZ * ncol)
+        return b200::set_error(B200_ERR_ARG, "pack_view: bad arguments");
+    pack_view_kernel<T><<<b200::ceil_div(n, PW_BLOCK), PW_BLOCK, 0, stream>>>(
+        n, nrow, ncol, base, map, rstr, ix64, out, ldo);
+    B200_CHECK_LAUNCH("pack_view");
+    return B200_OK;
+}
+
 template <typename T>
 struct ScalView {
     T *base;
@@ -836,6 +866,18 @@ int b200_negdivconf_f32(int nvars, int nupts, int64_t neles, float *r, int64_t l
     negdivconf_kernel<float><<<grid, PW_BLOCK, 0, (cudaStream_t)stream>>>(nvars, neles, r, ldr, rcpdjac, ldj);
     B200_CHECK_LAUNCH("negdivconf");
     return B200_OK;
+}
+
+int b200_pack_view_f64(int64_t n, int nrow, int ncol, const double *base, const void *map,
+                       const void *rstr, int ix64, double *out, int64_t ldo, void *stream) {
+    return pack_view<double>(n, nrow, ncol, base, map, rstr, ix64, out, ldo,
+                             (cudaStream_t)stream);
+}
+
+int b200_pack_view_f32(int64_t n, int nrow, int ncol, const float *base, const void *map,
+                       const void *rstr, int ix64, float *out, int64_t ldo, void *stream) {
+    return pack_view<float>(n, nrow, ncol, base, map, rstr, ix64, out, ldo,
+                            (cudaStream_t)stream);
 }
 
 int b200_srcterms_f64(int mode, int ndims, int nvars, int nupts, int64_t neles, double *r,

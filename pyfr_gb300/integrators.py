@@ -114,9 +114,13 @@ class RKVdH2Integrator:
         self._step_graphs = {}
         self._kcache = {}
         # (boundary controllers read the solution on the host before every
-        # right-hand side, which a captured step cannot stop for)
+        # right-hand side, and partitions exchange face data through the
+        # host, which a captured step cannot stop for)
         self.use_step_graph = backend.use_cuda_graphs and \
-            not self.system.controlled_bcs
+            not self.system.controlled_bcs and not self.system._mpi_inters
+        if self.system._mpi_inters and self.controller != 'none':
+            raise NotImplementedError('Step-size controllers across '
+                                      'partitions are not provided')
 
         # The step size lives in device memory (staged through page-locked
         # host memory), so that one captured graph per starting register

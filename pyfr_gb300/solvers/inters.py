@@ -164,6 +164,122 @@ class NavierStokesIntInters(BaseIntInters):
 
 
 # ---------------------------------------------------------------------------
+# Interfaces with another partition (pyfr/solvers/baseadvec/inters.py:31-47,
+# pyfr/solvers/baseadvecdiff/inters.py:33-60, pyfr/solvers/euler/
+# inters.py:40-49, pyfr/solvers/navstokes/inters.py:50-66)
+# ---------------------------------------------------------------------------
+
+class _Xchg:
+    """Exchange buffers of one field over the shared faces: what this side
+    packs (send), what it receives (recv) and a scratch target (junk) for
+    the other side's outputs of the two-sided interface kernels, all of
+    io-shape (nrow, nvars, n); views of recv and junk read them point by
+    point; host copies for the transfer."""
+
+    def __init__(self, be, nrow, nvars, n):
+        shape = (nrow, nvars, n)
+        self.send, self.recv, self.junk = (
+            be.matrix(shape, tags={'align'}) for _ in range(3))
+        vshape = (nvars,) if nrow == 1 else (nrow, nvars)
+
+        def ident(m):
+            return be.view([m.mid]*n, [0]*n, np.arange(n),
+                           *([[1]*n] if nrow > 1 else []), vshape=vshape)
+
+        self.rview, self.jview = ident(self.recv), ident(self.junk)
+        nb = self.send.nrow*self.send.leaddim*self.send.itemsize
+        self.nbytes = nb
+        self.hsend = np.empty(nb, dtype=np.uint8)
+        self.hrecv = np.empty(nb, dtype=np.uint8)
+
+
+class BaseMPIInters(BaseIntInters):
+    """The faces shared with partition ``rhsrank``: the local side, whose
+    views keep the shared face order (no reordering, so that the packed
+    data of both partitions line up), the exchange buffers, and the
+    interface kernels with the received data as their right side."""
+
+    def __init__(self, be, lhs, rhsrank, elemap, cfg, rank):
+        self._be = be
+        self.elemap = elemap
+        self.cfg = cfg
+        self.lhs, self.rhs = lhs, None
+        self.rhsrank, self.rank = rhsrank, rank
+
+        first = next(iter(elemap.values()))
+        self.ndims, self.nvars = first.ndims, first.nvars
+        self.ninters = len(lhs)
+        self.ninterfpts = sum(elemap[et].nfacefpts[fi]*len(ei)
+                              for et, fi, ei in lhs.items())
+        self.c = cfg.items_as('constants', float)
+        self.kernels = {}
+        self._perm = np.arange(self.ninterfpts)
+        self._pnorm_lhs = self._const_mat(lhs, 'get_pnorms_for_inters')
+        self._xs = _Xchg(be, 1, self.nvars, self.ninterfpts)
+
+    def xchg_items(self, field):
+        """(peer, tag, host send, host receive) of a field's exchange."""
+        x = self._xs if field == 'scal' else self._xv
+        return x, (self.rhsrank, 0 if field == 'scal' else 1, x.hsend,
+                   x.hrecv)
+
+
+class EulerMPIInters(BaseMPIInters):
+    def __init__(self, *args, **kwargs):
+        super().__init__(*args, **kwargs)
+        be = self._be
+        rsolver = self.cfg.get('solver-interfaces', 'riemann-solver')
+        p_min = riemann_p_min(self.cfg, be)
+        self._tplargs = dict(ndims=self.ndims, nvars=self.nvars,
+                             rsolver=rsolver, c=self.c, p_min=p_min)
+        be.pointwise.register('pyfr.solvers.euler.kernels.mpicflux')
+        self.kernels['scal_pack'] = lambda: be.kernel(
+            'pack_view', self.scal_lhs, self._xs.send)
+        self.kernels['comm_flux'] = lambda: be.kernel(
+            'mpicflux', tplargs=self._tplargs, dims=[self.ninterfpts],
+            ul=self.scal_lhs, ur=self._xs.rview, nl=self._pnorm_lhs)
+
+
+class NavierStokesMPIInters(BaseMPIInters):
+    def __init__(self, be, lhs, rhsrank, elemap, cfg, rank):
+        super().__init__(be, lhs, rhsrank, elemap, cfg, rank)
+        self._vect_lhs = self._vect_view(lhs, 'get_vect_fpts_for_inters')
+        self._comm_lhs = self._scal_view(lhs, 'get_comm_fpts_for_inters')
+        self._xv = _Xchg(be, self.ndims, self.nvars, self.ninterfpts)
+        self.c |= cfg.items_as('solver-interfaces', float)
+
+        # cflux(l, r, n_l) = -cflux(r, l, n_r) and conu(l, r) = conu(r, l)
+        # need one of the two partitions to take -beta; which one follows
+        # from the two ranks as in pyfr/solvers/baseadvecdiff/
+        # inters.py:47-56
+        if (rank + rhsrank) % 2:
+            self.c['ldg-beta'] *= 1.0 if rank > rhsrank else -1.0
+        else:
+            self.c['ldg-beta'] *= 1.0 if rhsrank > rank else -1.0
+
+        rsolver = cfg.get('solver-interfaces', 'riemann-solver')
+        visc_corr = cfg.get('solver', 'viscosity-correction', 'none')
+        self._tplargs = dict(ndims=self.ndims, nvars=self.nvars,
+                             rsolver=rsolver, visc_corr=visc_corr,
+                             shock_capturing='none', c=self.c,
+                             p_min=riemann_p_min(cfg, be))
+        be.pointwise.register('pyfr.solvers.navstokes.kernels.mpiconu')
+        be.pointwise.register('pyfr.solvers.navstokes.kernels.mpicflux')
+        self.kernels['scal_pack'] = lambda: be.kernel(
+            'pack_view', self.scal_lhs, self._xs.send)
+        self.kernels['vect_pack'] = lambda: be.kernel(
+            'pack_view', self._vect_lhs, self._xv.send)
+        self.kernels['con_u'] = lambda: be.kernel(
+            'mpiconu', tplargs=self._tplargs, dims=[self.ninterfpts],
+            ulin=self.scal_lhs, urin=self._xs.rview, ulout=self._comm_lhs,
+            urout=self._xs.jview)
+        self.kernels['comm_flux'] = lambda: be.kernel(
+            'mpicflux', tplargs=self._tplargs, dims=[self.ninterfpts],
+            ul=self.scal_lhs, ur=self._xs.rview, gradul=self._vect_lhs,
+            gradur=self._xv.rview, nl=self._pnorm_lhs)
+
+
+# ---------------------------------------------------------------------------
 # Boundary conditions (pyfr/solvers/baseadvec/inters.py:74-116,
 # pyfr/solvers/euler/inters.py:53-112, pyfr/solvers/navstokes/inters.py:66-150)
 # ---------------------------------------------------------------------------

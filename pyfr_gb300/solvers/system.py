@@ -17,9 +17,24 @@ import numpy as np
 from pyfr_gb300.backend.types import Kernel, NullKernel
 from pyfr_gb300.solvers.elements import EulerElements, NavierStokesElements
 from pyfr_gb300.solvers.inters import (EulerBCInters, EulerIntInters,
-                                       NavierStokesBCInters,
+                                       EulerMPIInters, NavierStokesBCInters,
                                        NavierStokesIntInters,
+                                       NavierStokesMPIInters,
                                        field_view_arrays)
+
+
+class HostStep:
+    """A step between graphs that the host runs (the exchange of packed
+    face data with other partitions): its kernels post and complete the
+    transfers.  It runs like a graph but is never captured."""
+
+    def __init__(self, post, complete, name):
+        self.klist = [Kernel(post, name=f'{name}_post'),
+                      Kernel(complete, name=f'{name}_complete')]
+
+    def run(self, stream):
+        for k in self.klist:
+            k.run(stream)
 
 
 class BaseSystem:
@@ -71,6 +86,15 @@ class BaseSystem:
         lhs, rhs = mesh.con
         self._int_inters = [self.intinterscls(backend, lhs, rhs, elemap, cfg)]
 
+        # Faces shared with other partitions (a part of
+        # pyfr_gb300.partition.partition: its rank and con_p)
+        self.rank = getattr(mesh, 'rank', 0)
+        self._mpi_inters = [
+            self.mpiinterscls(backend, side, peer, elemap, cfg, self.rank)
+            for peer, side in sorted(getattr(mesh, 'con_p', {}).items())]
+        # (set before the first right-hand side: pyfr_gb300.exchange)
+        self.exchanger = None
+
         # Boundaries: one interface object per named boundary, its type from
         # [soln-bcs-<name>] (pyfr/solvers/base/system.py:183-198)
         # The step-start and stage times (device memory) that boundary
@@ -89,11 +113,16 @@ class BaseSystem:
     def gndofs(self):
         return sum(self.ele_ndofs)
 
+    @property
+    def _sided_inters(self):
+        return self._int_inters + self._mpi_inters + self._bc_inters
+
     def make_field_views(self, field, vshape=()):
         """(left, right) views of a flux-point field for every interior
-        interface, then (left,) for every boundary."""
+        interface, then (left,) for every interface with another partition
+        and every boundary."""
         out = []
-        for i in self._int_inters + self._bc_inters:
+        for i in self._sided_inters:
             views = []
             for side in (i.lhs, i.rhs):
                 if side is None:
@@ -110,7 +139,7 @@ class BaseSystem:
         interface (a fully periodic mesh): the common solution can then be
         written to both sides of each interface point with no copy."""
         nside = defaultdict(int)
-        for i in self._int_inters + self._bc_inters:
+        for i in self._sided_inters:
             for side in (i.lhs, i.rhs):
                 if side is None:
                     continue
@@ -126,7 +155,7 @@ class BaseSystem:
         for i in self._int_inters:
             i.covers = covered
         scal = {et: e._scal_fpts for et, e in self.ele_map.items()}
-        for i, v in zip(self._int_inters + self._bc_inters,
+        for i, v in zip(self._sided_inters,
                         self.make_field_views(scal, vshape=(self.nvars,))):
             i.scal_lhs = v[0]
             i.scal_rhs = v[1] if len(v) > 1 else None
@@ -139,6 +168,9 @@ class BaseSystem:
             raise NotImplementedError(f'Shock capturing {sc!r} is not '
                                       'provided')
         self._av = None
+        if self._mpi_inters and sc != 'none':
+            raise NotImplementedError('Shock capturing across partitions is '
+                                      'not provided')
         if sc == 'artificial-viscosity':
             if self.name != 'navier-stokes':
                 raise ValueError('Artificial viscosity needs the '
@@ -146,8 +178,7 @@ class BaseSystem:
             from pyfr_gb300.solvers.artvisc import ArtificialViscosity
             self._av = ArtificialViscosity(self, self.cfg)
             av = {et: e.artvisc_fpts for et, e in self.ele_map.items()}
-            for i, v in zip(self._int_inters + self._bc_inters,
-                            self.make_field_views(av)):
+            for i, v in zip(self._sided_inters, self.make_field_views(av)):
                 i.artvisc = v[0]
 
         self.backend.commit()
@@ -187,7 +218,8 @@ class BaseSystem:
         self._ktags = {}
 
         provs = [('eles', list(self.ele_map.values())),
-                 ('iint', self._int_inters), ('bcint', self._bc_inters)]
+                 ('iint', self._int_inters), ('mpiint', self._mpi_inters),
+                 ('bcint', self._bc_inters)]
         for pn, plist in provs:
             for p in plist:
                 for kn, kget in p.kernels.items():
@@ -229,8 +261,84 @@ class BaseSystem:
     def _rhs_graphs_cached(self, uin, fout):
         key = ('rhs', uin, fout)
         if key not in self._graph_cache:
-            self._graph_cache[key] = self._rhs_graphs(uin, fout)
+            gs = self._rhs_graphs(uin, fout)
+            if self._mpi_inters:
+                gs = self._with_exchanges(gs, uin, fout)
+            self._graph_cache[key] = gs
         return self._graph_cache[key]
+
+    # ---- faces shared with other partitions -------------------------------
+
+    def _exchange(self, field):
+        """The host step exchanging one field's packed face data with every
+        neighbouring partition: device-to-host copies and posted transfers,
+        then the received data to the device."""
+        lib, be = self.backend.lib, self.backend
+
+        def post(stream):
+            if self.exchanger is None:
+                raise RuntimeError('Partitions need an exchanger')
+            items = []
+            for m in self._mpi_inters:
+                x, item = m.xchg_items(field)
+                lib.memcpy_dtoh(x.hsend.ctypes.data, x.send.data, x.nbytes,
+                                stream)
+                items.append(item)
+            lib.stream_sync(stream)
+            self.exchanger.post(items)
+
+        def complete(stream):
+            self.exchanger.complete()
+            for m in self._mpi_inters:
+                x, _ = m.xchg_items(field)
+                lib.memcpy_htod(x.recv.data, x.hrecv.ctypes.data, x.nbytes,
+                                stream)
+            be.wait()
+
+        return HostStep(post, complete, f'xchg_{field}')
+
+    def _mpi_graph(self, kerns):
+        g = self.backend.graph()
+        g.add_all(kerns)
+        g.commit()
+        return g
+
+    def _with_exchanges(self, gs, uin, fout):
+        """The right-hand side's graphs with the exchanges: after the first
+        graph (the solution at the flux points) the packed solution, and
+        for Navier-Stokes after the second (the gradient at the flux
+        points) the packed gradient; the interface kernels of the shared
+        faces run just before the graph that reads their results
+        (pyfr/solvers/baseadvec/system.py:58-136,
+        pyfr/solvers/baseadvecdiff/system.py:54-231)."""
+        k = self._get_kernels(uin, fout)
+        out = [gs[0], self._mpi_graph(k['mpiint/scal_pack']),
+               self._exchange('scal')]
+        if len(gs) == 2:
+            out += [self._mpi_graph(k['mpiint/comm_flux']), gs[1]]
+        else:
+            out += [self._mpi_graph(k['mpiint/con_u']), gs[1],
+                    self._mpi_graph(k['mpiint/vect_pack']),
+                    self._exchange('vect'),
+                    self._mpi_graph(k['mpiint/comm_flux']), *gs[2:]]
+        return tuple(out)
+
+    def rhs_phases(self, t, uinbank, foutbank):
+        """The right-hand side as a list of callables, each exchange split
+        into its post and its completion, for driving several partitions
+        of one process in lockstep."""
+        stream = self.backend.stream
+        phases = []
+        if self.time_dependent:
+            phases.append(lambda: self.set_time(t))
+        for k in self.prepare_kernels(uinbank, t):
+            phases.append(lambda k=k: k.run(stream))
+        for g in self._rhs_graphs_cached(uinbank, foutbank):
+            if isinstance(g, HostStep):
+                phases.extend(lambda k=k: k.run(stream) for k in g.klist)
+            else:
+                phases.append(lambda g=g: self.backend.run_graph(g))
+        return phases
 
     def rhs_graphs(self, uinbank, foutbank):
         return self._rhs_graphs_cached(uinbank, foutbank)
@@ -345,6 +453,7 @@ class EulerSystem(BaseSystem):
     name = 'euler'
     elementscls = EulerElements
     intinterscls = EulerIntInters
+    mpiinterscls = EulerMPIInters
     bcinterscls = EulerBCInters
 
     def _rhs_graphs(self, uinbank, foutbank):
@@ -403,6 +512,7 @@ class NavierStokesSystem(BaseSystem):
     name = 'navier-stokes'
     elementscls = NavierStokesElements
     intinterscls = NavierStokesIntInters
+    mpiinterscls = NavierStokesMPIInters
     bcinterscls = NavierStokesBCInters
 
     def _rhs_graphs(self, uinbank, foutbank):
