@@ -206,7 +206,8 @@ typedef struct {
     int64_t bstride1, bstride2, cstride;
     float alpha, beta;          /* beta 0 or 1 */
     const float *rowscale;      /* null: none */
-    int64_t ldr;
+    int64_t ldr;                /* 0: one row of scales for every output
+                                   row (S[row, e] = rowscale[e]) */
     int nvars;
     int products;               /* 3 (or 0): Ahi*Bhi + Ahi*Blo + Alo*Bhi;
                                    4: plus Alo*Blo; 5: plus Ax3*Bhi (a

@@ -253,6 +253,11 @@ class TensorMulKernels:
         nvars = ldr = 0
         if rowscale is not None:
             nvars, ldr = out.ioshape[1], rowscale.leaddim
+            # One scale per element when every row holds the same (1/|J|
+            # of affine elements): the epilogue loads it once per column
+            uni = self._uniform_rows(rowscale)
+            if uni is not None:
+                rowscale, ldr = uni, 0
         arglist, seen = [], set()
         for r0, r1, blocks, (h, smem, hosts) in pieces:
             first = r0 not in seen
@@ -324,8 +329,9 @@ class TensorMulKernels:
         (``$PYFR_GB300_CACHE`` or ``~/.cache/pyfr_gb300``)."""
         be, lib = self.backend, self.backend.lib
         m, k1, k2 = args[4], args[1], args[3]
+        # (plans of kernels with rings of any length)
         key = '|'.join(map(str, (be.platform_id, 'tf32' if tf32 else 'bf16',
-                                 self._products(nterms), m, k1, k2)))
+                                 self._products(nterms), m, k1, k2, 'r2')))
         cache = _plan_cache()
         if key in cache:
             return tuple(cache[key]) if cache[key] else None
@@ -350,7 +356,7 @@ class TensorMulKernels:
         times = {}
         try:
             for ntiles in (1, 2):
-                for nstages in (4, 6, 8, 10):
+                for nstages in range(4, 11):
                     h, smem = C.c_void_p(), C.c_size_t()
                     try:
                         lib.mul_tc_create_terms(*args, int(tf32), nterms,
@@ -450,6 +456,21 @@ class TensorMulKernels:
                            meta=dict(a=a, b=b, out=out, alpha=alpha,
                                      beta=beta, op=np.asarray(a._host),
                                      impl='bf16x3'))
+
+    def _uniform_rows(self, rs):
+        """The first row of a row-scale matrix as a one-row matrix when
+        every row is equal to it (known from the host copy), else None."""
+        h = getattr(rs, '_host', None)
+        if h is None or h.ndim != 2 or h.shape[0] < 2:
+            return None
+        key = ('uniform', rs.mid)
+        if key not in self._handles:
+            # (compared as the kernel reads them: in the matrix's precision)
+            hd = np.asarray(h, dtype=rs.dtype)
+            same = bool(np.all(hd == hd[:1]))
+            self._handles[key] = self.backend.const_matrix(
+                hd[:1], dtype=rs.dtype, tags={'align'}) if same else None
+        return self._handles[key]
 
     def mul_cat(self, a1, b1, a2, b2, out, alpha=1.0, beta=0.0,
                 rowscale=None):

@@ -279,6 +279,12 @@ struct UmmaArgs {
     int64_t ldc;                // leading dimension of out (and of the RK registers)
     int m, npad, kfull, nch1, ns, eb, nbatch, nvars, products;
     int nterms;                 // operator terms in the image (2 or 3)
+    // Stacked issue: the operator's terms lie one after the other along N
+    // in the image, so one MMA applies all of them to a data half; the
+    // products land in npart partial accumulators of npad columns (hh;
+    // hl + lh; x3h + ll) that the epilogue sums.  accols: TMEM columns of
+    // one accumulator (npad, or npart*npad stacked)
+    int stack, npart, accols;
     float alpha;
     int epi;            // 0: store, 1: add to out
     int *err;
@@ -290,14 +296,37 @@ struct UmmaArgs {
     int rk;
 };
 
+// 32 columns of one TMEM lane quadrant (32x32b shape, 32 repetitions):
+// v[r] is column r of this thread's lane; completes at tcgen05.wait::ld
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t *v) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
+          "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]),
+          "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]),
+          "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+          "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]),
+          "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+        : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t *v) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
+                   "=r"(v[6]), "=r"(v[7])
+                 : "r"(taddr));
+}
+
 template <bool TF32, bool RK>
 __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_constant__ UmmaArgs p) {
     extern __shared__ __align__(1024) unsigned char smem[];
     const Layout L = make_layout(p.npad, p.kfull, p.ns, p.eb, p.nterms);
     const int eb = p.eb;
     const int NS = p.ns;
-    // (the host plans an even ring of at least four stages; see create)
-    if ((NS & 1) || NS < 4 || NS > MAX_S) {
+    // (the host plans a ring of at least four stages; see create)
+    if (NS < 4 || NS > MAX_S) {
         if (threadIdx.x == 0) atomicCAS(p.err, 0, 9);
         return;
     }
@@ -311,8 +340,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
     // tile T covers columns (T % ntc)*TCOLS.. of slice T / ntc
     const int64_t ntiles = p.ntc * p.nbatch;
     const int npad = p.npad, nch = p.kfull / KC;
-    const uint32_t tcols = 2 * npad <= 32 ? 32 : (2 * npad <= 64 ? 64 :
-                          (2 * npad <= 128 ? 128 : (2 * npad <= 256 ? 256 : 512)));
+    const int acc2 = 2 * p.accols;
+    const uint32_t tcols = acc2 <= 32 ? 32 : (acc2 <= 64 ? 64 :
+                          (acc2 <= 128 ? 128 : (acc2 <= 256 ? 256 : 512)));
 
     if (tid == 0) {
         *abort_flag = 0;
@@ -359,23 +389,29 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
             }
         }
         if (lane == 0) {
+            // (ring stage s and phase ph of chunk j, advanced per chunk: no
+            // 64-bit divisions on the hand-off path)
             int64_t j = 0;
+            int s = 0;
+            uint32_t ph = 0;
             for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
                 bool ok = true;
+                const int tx = (int)((t % p.ntc) * TCOLS), tz = (int)(t / p.ntc);
                 for (int c = 0; c < nch; c++, j++) {
-                    const int s = (int)(j % NS);
                     if (j >= NS &&
-                        !bar_wait(bar(BAR_FREE + s), (uint32_t)((j / NS) & 1) ^ 1, abort_flag,
-                                  p.err, 1)) {
+                        !bar_wait(bar(BAR_FREE + s), ph ^ 1, abort_flag, p.err, 1)) {
                         ok = false;
                         break;
                     }
                     // chunks of the first block, then of the second
                     const int src = c < p.nch1 ? 0 : 1;
                     bar_arrive_tx(bar(BAR_LOADED + s), CHUNK32);
-                    tma_load_3d(sbase + L.ring + (uint32_t)s * CHUNK32, &p.tmap[src],
-                                (int)((t % p.ntc) * TCOLS), (src ? c - p.nch1 : c) * KC,
-                                (int)(t / p.ntc), bar(BAR_LOADED + s));
+                    tma_load_3d(sbase + L.ring + (uint32_t)s * CHUNK32, &p.tmap[src], tx,
+                                (src ? c - p.nch1 : c) * KC, tz, bar(BAR_LOADED + s));
+                    if (++s == NS) {
+                        s = 0;
+                        ph ^= 1;
+                    }
                 }
                 if (!ok) break;
             }
@@ -388,22 +424,31 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
         __syncwarp();
     } else if (warp >= WARP_CONV && warp < WARP_CONV + NCONV / 32) {
         // ---- converters: FP32 chunk -> BF16 hi/lo (or TF32) canonical
-        // K-major, in place.  Two groups of four warps take alternate
-        // chunks, so that two chunks are converted at once; thread ct of a
-        // group owns column cc of its chunks.
+        // K-major, in place.  Two groups of four warps take the chunks of
+        // alternate ring stages (even stages, odd stages), so that two
+        // chunks are converted at once and every stage has one group,
+        // which meets its phases in order whatever the ring's length;
+        // thread ct of a group owns column cc of its chunks.
         const int ct = tid - WARP_CONV * 32, cc = ct % TCOLS, grp = ct / TCOLS;
         const uint32_t gbar = grp ? CONV_BARRIER2 : CONV_BARRIER;
         const uint32_t coff = (uint32_t)(cc / 8) * SBO_D + (uint32_t)(cc % 8) * 16;
         int64_t j = 0;
+        int sn = 0;
+        uint32_t phn = 0;
         bool ok = true;
         for (int64_t t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
             for (int c = 0; c < nch; c++, j++) {
-                if ((int)(j & 1) != grp) continue;
-                const int s = (int)(j % NS);
+                const int s = sn;
+                const uint32_t ph = phn;
+                if (++sn == NS) {
+                    sn = 0;
+                    phn ^= 1;
+                }
+                if ((s & 1) != grp) continue;
                 // (a converter that gives up still meets the others of its
                 // group at the named barrier below, so none of them waits
                 // there forever)
-                ok = bar_wait(bar(BAR_LOADED + s), (uint32_t)((j / NS) & 1), abort_flag, p.err, 2);
+                ok = bar_wait(bar(BAR_LOADED + s), ph, abort_flag, p.err, 2);
                 const uint32_t stage = sbase + L.ring + (uint32_t)s * CHUNK32;
                 float x[KC];
                 if (ok) {
@@ -450,20 +495,32 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
         // ---- MMA issuer ----
         if (lane == 0) {
             const uint32_t idesc = TF32 ? idesc_tf32(TCOLS, npad) : idesc_bf16(TCOLS, npad);
+            // Stacked: the data's hi half against hi | lo (| x3) and its lo
+            // half against hi | lo (five products: hh, hl, hx3 and lh, ll
+            // into partials hh, hl + lh, hx3 + ll), or hi | lo and hi
+            // (three products); four products add ll as a third MMA
+            const int n1 = p.products == 5 ? 3 * npad : 2 * npad;
+            const int n2 = p.products == 5 ? 2 * npad : npad;
+            const uint32_t idesc1 = idesc_bf16(TCOLS, n1), idesc2 = idesc_bf16(TCOLS, n2);
             bool ok = bar_wait(bar(BAR_A), 0, abort_flag, p.err, 4);
             int64_t j = 0;
-            int i = 0;
+            int i = 0, sn = 0;
+            uint32_t phn = 0;
             for (int64_t t = blockIdx.x; ok && t < ntiles; t += gridDim.x, i++) {
                 const int bsel = i & 1;
                 if (i >= 2 &&
                     !bar_wait(bar(BAR_ACCEMPTY + bsel), ((i >> 1) & 1) ^ 1, abort_flag, p.err, 6))
                     break;
                 asm volatile("tcgen05.fence::after_thread_sync;");
-                const uint32_t d = tmem + (uint32_t)(bsel * npad);
+                const uint32_t d = tmem + (uint32_t)(bsel * p.accols);
                 for (int c = 0; c < nch; c++, j++) {
-                    const int s2 = (int)(j % NS);
-                    if (!bar_wait(bar(BAR_CONVERTED + s2), (uint32_t)((j / NS) & 1), abort_flag,
-                                  p.err, 5)) {
+                    const int s2 = sn;
+                    const uint32_t ph = phn;
+                    if (++sn == NS) {
+                        sn = 0;
+                        phn ^= 1;
+                    }
+                    if (!bar_wait(bar(BAR_CONVERTED + s2), ph, abort_flag, p.err, 5)) {
                         ok = false;
                         break;
                     }
@@ -480,7 +537,20 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
                         }
                     }
 #pragma unroll
-                    for (int ks = 0; ks < KC / 16 && !TF32; ks++) {
+                    for (int ks = 0; ks < KC / 16 && !TF32 && p.stack; ks++) {
+                        const uint32_t ko = (uint32_t)ks * 2 * LBO;
+                        const uint32_t kg = (uint32_t)(c * (KC / 16) + ks) * 2 * LBO;
+                        const uint64_t dh = sdesc(bhi + ko, LBO, SBO_CHUNK);
+                        const uint64_t dl = sdesc(bhi + CHUNK16 + ko, LBO, SBO_CHUNK);
+                        const uint64_t oh = sdesc(sbase + L.a_hi + kg, LBO, SBO_OP);
+                        umma(d, dh, oh, idesc1, (c | ks) != 0);
+                        umma(d + (uint32_t)npad, dl, oh, idesc2, 1);
+                        if (p.products == 4)
+                            umma(d + (uint32_t)(2 * npad), dl,
+                                 sdesc(sbase + L.a_lo + kg, LBO, SBO_OP), idesc, (c | ks) != 0);
+                    }
+#pragma unroll
+                    for (int ks = 0; ks < KC / 16 && !TF32 && !p.stack; ks++) {
                         const uint32_t ko = (uint32_t)ks * 2 * LBO;
                         const uint32_t kg = (uint32_t)(c * (KC / 16) + ks) * 2 * LBO;
                         const uint64_t dh = sdesc(bhi + ko, LBO, SBO_CHUNK);
@@ -527,7 +597,13 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
         // Row-scale factors alpha*S[row, element] of row group g for this
         // thread's column (alpha alone without a scale)
         auto load_scale = [&](float *f, int g, int64_t col, int64_t ele) {
-            if (p.rs) {
+            if (p.rs && p.ldr == 0) {
+                // One scale for every row (affine elements: 1/|J| is the
+                // same at every solution point)
+                const float fu = col < p.ncol ? p.alpha * __ldg(p.rs + ele) : 0.f;
+#pragma unroll
+                for (int r = 0; r < 32; r++) f[r] = g * 32 + r < p.m ? fu : 0.f;
+            } else if (p.rs) {
 #pragma unroll
                 for (int r = 0; r < 32; r++)
                     f[r] = col < p.ncol && g * 32 + r < p.m
@@ -572,18 +648,36 @@ __global__ void __launch_bounds__(NTHREADS, 1) mul_umma_kernel(const __grid_cons
                 if (g != half) load_scale(f, g, col, ele);
                 uint32_t v[32];
                 const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) +
-                                       (uint32_t)(bsel * npad + g * 32);
-                asm volatile(
-                    "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-                    "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-                    "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
-                      "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]),
-                      "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]),
-                      "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
-                      "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]),
-                      "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-                    : "r"(taddr));
+                                       (uint32_t)(bsel * p.accols + g * 32);
+                if (!TF32 && p.stack) {
+                    // The partials, eight columns at a time: the small ones
+                    // first (hl + lh, plus x3h + ll when there are three),
+                    // then hh onto their sum
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        uint32_t u[8], w[8];
+                        tmem_ld8(taddr + (uint32_t)(npad + 8 * q), u);
+                        if (p.npart == 3) tmem_ld8(taddr + (uint32_t)(2 * npad + 8 * q), w);
+                        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                        for (int r = 0; r < 8; r++)
+                            v[8 * q + r] = p.npart == 3 ? __float_as_uint(__uint_as_float(u[r]) +
+                                                                          __uint_as_float(w[r]))
+                                                        : u[r];
+                    }
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        uint32_t u[8];
+                        tmem_ld8(taddr + (uint32_t)(8 * q), u);
+                        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                        for (int r = 0; r < 8; r++)
+                            v[8 * q + r] = __float_as_uint(__uint_as_float(u[r]) +
+                                                           __uint_as_float(v[8 * q + r]));
+                    }
+                } else {
+                    tmem_ld32(taddr, v);
+                }
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 
                 if (RK) {
@@ -766,19 +860,16 @@ int create_impl(const double *a1, int k1, const double *a2, int k2, int m, int t
     const int npad = (m + 31) / 32 * 32, kfull = (nch1 + nch2) * KC;
     // The deepest ring (bytes in flight per SM) that fits in shared memory
     // with two staging tiles per epilogue set, or failing four stages that
-    // way, with one.  The ring has an even number of stages: each converter
-    // group takes every other chunk, so with an even ring a stage's previous
-    // chunk belongs to the same group, which has consumed it before it waits
-    // for the stage again (with an odd ring the group could take the phase
-    // of the other group's pending chunk, one phase back, for its own).  An
-    // operator of at most 64 rows gives each set one store per tile, which
-    // a second staging tile would not overlap with anything: it takes one
-    // and the ring the room.  A caller (the autotuner) may ask for a given
-    // plan instead (want_ns even, 4..MAX_S; want_eb 1 or 2).
+    // way, with one (each converter group owns the even or the odd stages,
+    // so the ring may have any length).  An operator of at most 64 rows
+    // gives each set one store per tile, which a second staging tile would
+    // not overlap with anything: it takes one and the ring the room.  A
+    // caller (the autotuner) may ask for a given plan instead (want_ns
+    // 4..MAX_S; want_eb 1 or 2).
     int ns = 0, eb = npad <= 64 ? 1 : MAX_EB;
     Layout L = make_layout(npad, kfull, 2, eb, nterms);
     if (want_ns || want_eb) {
-        if ((want_ns & 1) || want_ns < 4 || want_ns > MAX_S || want_eb < 1 || want_eb > MAX_EB)
+        if (want_ns < 4 || want_ns > MAX_S || want_eb < 1 || want_eb > MAX_EB)
             return b200::set_error(B200_ERR_ARG, "mul_bf16x3: plan (%d stages, %d tiles) invalid",
                                    want_ns, want_eb);
         ns = want_ns;
@@ -787,7 +878,7 @@ int create_impl(const double *a1, int k1, const double *a2, int k2, int m, int t
     } else {
         for (; eb >= 1 && ns < 4; eb--) {
             ns = 0;
-            for (int cand = MAX_S; cand >= 4 && !ns; cand -= 2) {
+            for (int cand = MAX_S; cand >= 4 && !ns; cand--) {
                 Layout c = make_layout(npad, kfull, cand, eb, nterms);
                 if (c.total <= 227 * 1024) {
                     ns = cand;
@@ -799,7 +890,7 @@ int create_impl(const double *a1, int k1, const double *a2, int k2, int m, int t
         if (eb < 1) eb = 1;
     }
     if (smem_bytes) *smem_bytes = L.total;
-    if (npad > MAX_N || !ns || (ns & 1) || L.total > 227 * 1024)
+    if (npad > MAX_N || !ns || L.total > 227 * 1024)
         return b200::set_error(B200_ERR_UNSUPPORTED,
                                "mul_bf16x3: operator %dx(%d+%d) needs %u bytes of shared memory "
                                "(or more than %d rows)", m, k1, k2, L.total, MAX_N);
@@ -953,7 +1044,7 @@ int b200_mul_bf16x3_apply(void *handle, const b200_mul_bf16x3_args_t *a, void *s
     if (a->products == 5 && (h->nterms != 3 || h->tf32))
         return b200::set_error(B200_ERR_ARG,
                                "mul_bf16x3: five products need a three-term operator");
-    if (a->rowscale && (a->nvars <= 0 || a->ldr <= 0 || a->nbatch != 1))
+    if (a->rowscale && (a->nvars <= 0 || a->ldr < 0 || a->nbatch != 1))
         return b200::set_error(B200_ERR_ARG, "mul_bf16x3: row scale needs nvars, ldr, one slice");
 
     if (!g_sm_count)
@@ -989,6 +1080,12 @@ int b200_mul_bf16x3_apply(void *handle, const b200_mul_bf16x3_args_t *a, void *s
     p.alpha = a->alpha; p.epi = a->beta != 0.0f; p.err = a->err;
     p.products = a->products == 0 ? 3 : a->products;
     p.nterms = h->nterms;
+    // Stacked issue where the stacked operand (N <= 256) and two
+    // accumulators of the partials fit tensor memory (512 columns)
+    p.npart = p.products == 3 ? 2 : 3;
+    p.stack = !h->tf32 && (p.products == 5 ? 3 : 2) * h->npad <= 256 &&
+              2 * p.npart * h->npad <= 512;
+    p.accols = p.stack ? p.npart * h->npad : h->npad;
     p.rk = a->rk_stage; p.rk_acc = a->rk_acc; p.rk_u = a->rk_u; p.rk_dtp = a->rk_dt_dev;
     p.rk_dt = a->rk_dt; p.rk_a = a->rk_a; p.rk_b = a->rk_b;
     p.ldc = a->ldc;

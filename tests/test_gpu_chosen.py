@@ -393,11 +393,11 @@ def test_autotuned_plan_same_result(built, golden, tmp_path, monkeypatch):
             be, '_providers') else None
         if h is not None:
             be.lib.mul_tc_plan(h, C.byref(ns), C.byref(nt))
-            assert ns.value % 2 == 0 and 4 <= ns.value <= 10
+            assert 4 <= ns.value <= 10
             assert nt.value in (1, 2)
     assert np.array_equal(out['true'], out['false'])
     plans = json.loads((tmp_path / 'mul-plans.json').read_text())
-    assert any(k.endswith('|192|64|0') for k in plans)
+    assert any('|192|64|0|' in k for k in plans)
 
 
 def test_chosen_form_order4(built):
