@@ -457,8 +457,11 @@ intcflux_euler_kernel(int64_t n, T gamma, T p_min, ScalView<T> vl, ScalView<T> v
     }
 }
 
+// (FP32: 64 registers, so that eight blocks share an SM -- the kernel waits
+// on its gathers, and occupancy hides them better than the spill-free 80
+// registers do)
 template <int RS, int ND, typename T>
-__global__ void __launch_bounds__(PW_BLOCK)
+__global__ void __launch_bounds__(PW_BLOCK, sizeof(T) == 4 ? 8 : 1)
 intcflux_ns_kernel(int64_t n, b200::GasK<T> gas, T beta, T tau, ScalView<T> vl, ScalView<T> vr,
                    VectView<T> gl, VectView<T> gr, int ix64, const T *__restrict__ nl,
                    int64_t ldn, int nl_unit, ScalView<T> va) {
