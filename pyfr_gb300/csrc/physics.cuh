@@ -168,28 +168,104 @@ __device__ __forceinline__ void viscous_flux_add(const T *uin, const T grad[ND][
     }
 }
 
+// The inviscid flux of state s along n, formed directly
+// (pyfr/solvers/euler/kernels/flux.mako:3-26 contracted with n): mass
+// rho v.n, momentum rho u_i v.n + p n_i, energy (E + p) v.n; returns the
+// pressure and the normal velocity.  Fewer operations than the full flux
+// followed by its projection, which matters where FP64 throughput bounds.
+template <int ND, typename T>
+__device__ __forceinline__ void inviscid_nflux(const T *s, const T *n, T *fn, T &p, T &vn,
+                                               T gamma) {
+    constexpr int NV = ND + 2;
+    const T invrho = T(1) / s[0], E = s[NV - 1];
+    T dot = 0, mn = 0;
+#pragma unroll
+    for (int i = 0; i < ND; i++) {
+        dot += s[i + 1] * s[i + 1];
+        mn += s[i + 1] * n[i];
+    }
+    p = (gamma - T(1)) * (E - T(0.5) * invrho * dot);
+    vn = invrho * mn;
+    fn[0] = mn;
+#pragma unroll
+    for (int i = 0; i < ND; i++) fn[i + 1] = s[i + 1] * vn + p * n[i];
+    fn[NV - 1] = (E + p) * vn;
+}
+
+// The (negated-stress) viscous flux of uin along n, formed directly: the
+// normal component of viscous_flux_add's flux, momentum tau.n and energy
+// u.(tau.n) + kcoef dT.n, added to fn (mass untouched).
+template <int ND, typename T>
+__device__ __forceinline__ void viscous_nflux_add(const T *uin, const T grad[ND][ND + 2],
+                                                  const T *n, T *fn, const GasK<T> &g) {
+    constexpr int NV = ND + 2;
+    const T rho = uin[0], E = uin[NV - 1];
+    const T rcprho = T(1) / rho;
+    T vel[ND];
+#pragma unroll
+    for (int i = 0; i < ND; i++) vel[i] = rcprho * uin[i + 1];
+
+    T dv[ND][ND];
+#pragma unroll
+    for (int i = 0; i < ND; i++)
+#pragma unroll
+        for (int d = 0; d < ND; d++) dv[i][d] = grad[d][i + 1] - vel[i] * grad[d][0];
+
+    T mu_c;
+    if (g.sutherland) {
+        T ke = 0;
+#pragma unroll
+        for (int i = 0; i < ND; i++) ke += vel[i] * vel[i];
+        const T cpT = g.gamma * (rcprho * E - T(0.5) * ke);
+        const T Trat = g.rcp_cpTref * cpT;
+        mu_c = g.mu_ctt * Trat * sqrt(Trat) / (cpT + g.cpTs);
+    } else {
+        mu_c = g.mu;
+    }
+
+    // Normal temperature derivative (c_v dT/dn)
+    T dTn = 0;
+#pragma unroll
+    for (int d = 0; d < ND; d++) {
+        T t = rcprho * grad[d][0] * E;
+#pragma unroll
+        for (int i = 0; i < ND; i++) t += vel[i] * dv[i][d];
+        dTn += n[d] * (rcprho * (grad[d][NV - 1] - t));
+    }
+
+    T div = 0;
+#pragma unroll
+    for (int i = 0; i < ND; i++) div += dv[i][i];
+
+    // (tau.n)_i with the negated stress tau_ij = -mu/rho (dv_ij + dv_ji -
+    // 2/3 div delta_ij)
+    const T mr = -mu_c * rcprho;
+    T e = -mu_c * g.gamma_pr * dTn;
+#pragma unroll
+    for (int i = 0; i < ND; i++) {
+        T tn = T(-2.0 / 3.0) * div * n[i];
+#pragma unroll
+        for (int j = 0; j < ND; j++) tn += (dv[j][i] + dv[i][j]) * n[j];
+        tn *= mr;
+        fn[i + 1] += tn;
+        e += vel[i] * tn;
+    }
+    fn[NV - 1] += e;
+}
+
 template <int ND, typename T>
 __device__ __forceinline__ void rsolve_rusanov(const T *ul, const T *ur, const T *n, T *nf,
                                                T gamma) {
     constexpr int NV = ND + 2;
-    T fl[ND][NV], fr[ND][NV], vl[ND], vr[ND], pl, pr;
-    inviscid_flux<ND, T>(ul, fl, pl, vl, gamma);
-    inviscid_flux<ND, T>(ur, fr, pr, vr, gamma);
-
-    T nv = 0;
-#pragma unroll
-    for (int i = 0; i < ND; i++) nv += n[i] * (vl[i] + vr[i]);
+    T fl[NV], fr[NV], pl, pr, vnl, vnr;
+    inviscid_nflux<ND, T>(ul, n, fl, pl, vnl, gamma);
+    inviscid_nflux<ND, T>(ur, n, fr, pr, vnr, gamma);
 
     // Maximum wave speed estimate (halved)
-    const T a = sqrt(T(0.25) * gamma * (pl + pr) / (ul[0] + ur[0])) + T(0.25) * fabs(nv);
+    const T a = sqrt(T(0.25) * gamma * (pl + pr) / (ul[0] + ur[0])) + T(0.25) * fabs(vnl + vnr);
 
 #pragma unroll
-    for (int i = 0; i < NV; i++) {
-        T s = 0;
-#pragma unroll
-        for (int j = 0; j < ND; j++) s += n[j] * (fl[j][i] + fr[j][i]);
-        nf[i] = T(0.5) * s + a * (ul[i] - ur[i]);
-    }
+    for (int i = 0; i < NV; i++) nf[i] = T(0.5) * (fl[i] + fr[i]) + a * (ul[i] - ur[i]);
 }
 
 // Inviscid flux from the transformed input s = q = T(u - u_ref) (see Gas):

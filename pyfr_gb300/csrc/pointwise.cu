@@ -497,12 +497,11 @@ intcflux_ns_kernel(int64_t n, b200::GasK<T> gas, T beta, T tau, ScalView<T> vl, 
     // Artificial viscosity at the point (the left side's value)
     const T a = va.base ? va.base[b200::load_ix(va.map, ix64, i)] : T(0);
 
-    // LDG viscous common flux from the left and/or right states
-    T fvl[ND][NV], fvr[ND][NV];
+    // LDG viscous common flux from the left and/or right states, each
+    // formed along the normal directly
+    T nfl[NV], nfr[NV];
 #pragma unroll
-    for (int d = 0; d < ND; d++)
-#pragma unroll
-        for (int v = 0; v < NV; v++) fvl[d][v] = fvr[d][v] = 0;
+    for (int v = 0; v < NV; v++) nfl[v] = nfr[v] = 0;
 
     if (beta != T(-0.5)) {
         const T *g = gl.base + b200::load_ix(gl.map, ix64, i);
@@ -515,14 +514,17 @@ intcflux_ns_kernel(int64_t n, b200::GasK<T> gas, T beta, T tau, ScalView<T> vl, 
         if (gas.shifted) {
             T gu[ND][NV];
             b200::unshift_grad<ND, T>(gg, gu, gas);
-            b200::viscous_flux_add<ND, T>(ufl, gu, fvl, gas);
+            b200::viscous_nflux_add<ND, T>(ufl, gu, nn, nfl, gas);
         } else {
-            b200::viscous_flux_add<ND, T>(ufl, gg, fvl, gas);
+            b200::viscous_nflux_add<ND, T>(ufl, gg, nn, nfl, gas);
             if (va.base) {
 #pragma unroll
-                for (int d = 0; d < ND; d++)
+                for (int v = 0; v < NV; v++) {
+                    T gn = 0;
 #pragma unroll
-                    for (int v = 0; v < NV; v++) fvl[d][v] -= a * gg[d][v];
+                    for (int d = 0; d < ND; d++) gn += nn[d] * gg[d][v];
+                    nfl[v] -= a * gn;
+                }
             }
         }
     }
@@ -537,33 +539,30 @@ intcflux_ns_kernel(int64_t n, b200::GasK<T> gas, T beta, T tau, ScalView<T> vl, 
         if (gas.shifted) {
             T gu[ND][NV];
             b200::unshift_grad<ND, T>(gg, gu, gas);
-            b200::viscous_flux_add<ND, T>(ufr, gu, fvr, gas);
+            b200::viscous_nflux_add<ND, T>(ufr, gu, nn, nfr, gas);
         } else {
-            b200::viscous_flux_add<ND, T>(ufr, gg, fvr, gas);
+            b200::viscous_nflux_add<ND, T>(ufr, gg, nn, nfr, gas);
             if (va.base) {
 #pragma unroll
-                for (int d = 0; d < ND; d++)
+                for (int v = 0; v < NV; v++) {
+                    T gn = 0;
 #pragma unroll
-                    for (int v = 0; v < NV; v++) fvr[d][v] -= a * gg[d][v];
+                    for (int d = 0; d < ND; d++) gn += nn[d] * gg[d][v];
+                    nfr[v] -= a * gn;
+                }
             }
         }
     }
 
 #pragma unroll
     for (int v = 0; v < NV; v++) {
-        T nfl = 0, nfr = 0;
-#pragma unroll
-        for (int d = 0; d < ND; d++) {
-            nfl += nn[d] * fvl[d][v];
-            nfr += nn[d] * fvr[d][v];
-        }
         T fvc;
         if (beta == T(-0.5))
-            fvc = nfr;
+            fvc = nfr[v];
         else if (beta == T(0.5))
-            fvc = nfl;
+            fvc = nfl[v];
         else
-            fvc = (T(0.5) + beta) * nfl + (T(0.5) - beta) * nfr;
+            fvc = (T(0.5) + beta) * nfl[v] + (T(0.5) - beta) * nfr[v];
         if (tau != T(0)) fvc += tau * (ul[v] - ur[v]);
 
         pl[v * B200_SOASZ] = mag * (fi[v] + fvc);
