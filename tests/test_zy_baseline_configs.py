@@ -5,7 +5,8 @@ reference's kernels by ``tests/test_pointwise_golden.py``).
 
 * 2-D isentropic vortex: periodic [-10, 10]^2 of 40 x 40 quadrilaterals,
   p = 3, beta = 5, Rusanov, RK45 with dt = 1e-3 for 1000 steps: the plain
-  FP64 form within 1e-10 (relative max-norm per conserved variable).
+  FP64 form within 1e-10 (relative max-norm per conserved variable:
+  density, momentum, energy).
 * 3-D Taylor-Green vortex: 48^3 hexahedra, p = 3, Re = 1600, Ma = 0.1,
   Rusanov + LDG, RK45 with dt = 5e-4: the plain FP64 form within 1e-10
   after 20 steps, with the kinetic energy and enstrophy integrals compared
@@ -35,10 +36,18 @@ def built():
 
 
 def _relerr_per_var(a, b):
-    """Largest over the conserved variables of max|a - b| / max|b|; a and
-    b are (nupts, nvars, neles)."""
-    return max(np.abs(a[:, v] - b[:, v]).max()/np.abs(b[:, v]).max()
-               for v in range(b.shape[1]))
+    """Largest over the conserved variables (density, momentum, energy) of
+    max|a - b| / max|b|; a and b are (nupts, nvars, neles).  Momentum is
+    one (vector) variable: its components' errors are measured against
+    the momentum's largest magnitude.  A component on its own is no scale:
+    the TGV's z-momentum starts at exactly zero and is 2.5e-3 after 20
+    steps, so rounding differences of 1e-13 in it -- the size they have in
+    the other components, against which the IEEE oracle and the GPU's
+    contracted FP64 differ -- would read as 1.5e-10."""
+    nv = b.shape[1]
+    groups = [[0], list(range(1, nv - 1)), [nv - 1]]
+    return max(np.abs(a[:, g] - b[:, g]).max()/np.abs(b[:, g]).max()
+               for g in groups)
 
 
 def _c_oracle(mesh, cfg, ns):
