@@ -664,9 +664,10 @@ def run_ensemble(args, dist):
 
 def run_mixed(args, dist):
     """The batching configuration's mixed meshes: 3-D Euler on a periodic
-    box of n^3 cells, hexahedra and prisms, or prisms and tetrahedra
-    (p = 3; an advected density wave), plain FP64 and the chosen form;
-    one CUDA graph per RK45 step over every element type."""
+    box of n^3 cells, hexahedra and prisms, prisms and tetrahedra, or
+    hexahedra and tetrahedra joined by pyramids (p = 3; an advected
+    density wave), plain FP64 and the chosen form; one CUDA graph per RK45
+    step over every element type."""
     import ctypes as C
 
     import __graft_entry__ as ge
@@ -693,7 +694,7 @@ def run_mixed(args, dist):
         return dist.allmax(ms.value), clk.summary()
 
     res = {}
-    for kinds in ('hex-pri', 'pri-tet'):
+    for kinds in args.mixed_kinds.split(','):
         out, solns = {}, {}
         for form in ('plain', 'chosen', 'tf32'):
             prec = 'double' if form == 'plain' else 'single'
@@ -798,11 +799,14 @@ def main():
     ap.add_argument('--large-plain-n', type=int, default=96)
     ap.add_argument('--large-plain-steps', type=int, default=5)
     ap.add_argument('--mixed', action='store_true',
-                    help='time the mixed hexahedron/prism and '
-                    'prism/tetrahedron meshes instead')
+                    help='time the mixed meshes (hexahedra/prisms, '
+                    'prisms/tetrahedra, hexahedra/pyramids/tetrahedra) '
+                    'instead')
     ap.add_argument('--mixed-n', type=int, default=32)
     ap.add_argument('--mixed-order', type=int, default=3)
     ap.add_argument('--mixed-dt', type=float, default=1e-3)
+    ap.add_argument('--mixed-kinds', default='hex-pri,pri-tet,hex-pyr-tet',
+                    help='comma-separated mixed meshes for --mixed')
     ap.add_argument('--ensemble', action='store_true',
                     help='the batching configuration\'s ensemble of 2-D '
                          'vortex cases instead of the headline run')
@@ -882,9 +886,8 @@ def main():
                 'metric': METRIC, 'unit': 'GDoF/s', 'n_gpus': world,
                 'steps': args.steps, 'warmup': args.warmup,
                 'config': {'workload': f'3-D Euler, periodic '
-                                       f'{args.mixed_n}^3-cell box of '
-                                       'hexahedra+prisms and of '
-                                       f'prisms+tetrahedra, '
+                                       f'{args.mixed_n}^3-cell boxes '
+                                       f'({args.mixed_kinds}), '
                                        f'p={args.mixed_order}, density '
                                        'wave, one CUDA graph per RK45 step',
                            'dt': args.mixed_dt},

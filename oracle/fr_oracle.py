@@ -1049,6 +1049,20 @@ def linear_shape(etype, pts):
         dN[:, 2, :3] = -tri/2
         dN[:, 2, 3:] = tri/2
         return N, dN
+    if etype == 'pyr':
+        # The pyramid's interpolation and Jacobian expressions term by term
+        # (pyfr/shapes.py:590-616)
+        x, y, z = pts.T
+        N = np.stack([2*x*y - 2*x - 2*y - z + 1, -2*x*y + 2*x - 2*y - z + 1,
+                      -2*x*y - 2*x + 2*y - z + 1, 2*x*y + 2*x + 2*y - z + 1,
+                      4*(1 + z)], axis=1)/8
+        zero, eighth = np.zeros(n), np.full(n, 1/8)
+        dN = np.stack([
+            np.stack([y - 1, 1 - y, -y - 1, y + 1, zero], axis=1)/4,
+            np.stack([x - 1, -x - 1, 1 - x, x + 1, zero], axis=1)/4,
+            np.stack([-eighth, -eighth, -eighth, -eighth, 4*eighth], axis=1)
+        ], axis=1)
+        return N, dN
     raise ValueError(etype)
 
 

@@ -120,6 +120,7 @@ def euler_mixed(n=32, order=3, kinds='hex-pri', dt=1e-3, amp=0.2,
     cfg.set('solver-elements-pri', 'soln-pts',
             'alpha-opt~gauss-legendre-lobatto')
     cfg.set('solver-elements-tet', 'soln-pts', 'alpha-opt')
+    cfg.set('solver-elements-pyr', 'soln-pts', 'gauss-legendre')
     cfg.set('solver-time-integrator', 'scheme', 'rk45')
     cfg.set('solver-time-integrator', 'controller', 'none')
     cfg.set('solver-time-integrator', 'dt', repr(dt))

@@ -340,16 +340,98 @@ def _tets_of_cube():
     return out
 
 
+def _orient(v, ref):
+    """Swap vertices ref[1] and ref[2] of the elements (v: (nverts, neles,
+    3)) whose frame (v[r1] - v[r0]) x (v[r2] - v[r0]) . (v[r3] - v[r0]) is
+    negative, ref = (r0, r1, r2, r3)."""
+    r0, r1, r2, r3 = ref
+    a, b, c = v[r1] - v[r0], v[r2] - v[r0], v[r3] - v[r0]
+    neg = np.einsum('ei,ei->e', np.cross(a, b), c) < 0
+    t = v[r1, neg].copy()
+    v[r1, neg] = v[r2, neg]
+    v[r2, neg] = t
+    return v
+
+
+def _pyr_tet_cells(corners, idx, sel, n, cut=True):
+    """The cells ``sel`` cut into six pyramids, one on each face with its
+    apex at the cell centre; the pyramid on a face shared with a hex cell
+    (x index below n/2) is kept, every other one (with ``cut``) is cut
+    into two tetrahedra along the face diagonal through the face's corners
+    of even in-plane lattice parity, which the cell across the face (and a
+    periodic image) cuts the same way.  Returns pyramid and tetrahedron
+    vertices (nverts, neles, 3)."""
+    cen = corners[:, sel].mean(axis=0)
+    ci = idx[:, sel]
+    pyrs, tets = [], []
+    for a in range(3):
+        u, v = [d for d in range(3) if d != a]
+        for side in (0, 1):
+            # Face corners in tensor order (u fastest), cube numbering
+            # first-coordinate-fastest
+            fc = [(side << a) | (bu << u) | (bv << v)
+                  for bv in (0, 1) for bu in (0, 1)]
+            base = corners[fc][:, sel]                   # (4, ncell, 3)
+            if not cut:
+                keep = np.ones(ci.shape[1], dtype=bool)
+            elif a == 0:
+                nb = (ci[0] + (1 if side else -1)) % n
+                keep = nb < n//2
+            else:
+                keep = np.zeros(ci.shape[1], dtype=bool)
+            if keep.any():
+                pv = np.concatenate([base[:, keep], cen[None, keep]])
+                pyrs.append(_orient(pv, (0, 1, 2, 4)))
+            cut_here = ~keep
+            if not cut_here.any():
+                continue
+            even = ((ci[u] + ci[v]) % 2 == 0)[cut_here]
+            b, c = base[:, cut_here], cen[cut_here]
+            # Diagonal (0, 3) where the corner 0 has even parity, else (1, 2)
+            d0 = np.where(even[:, None], b[0], b[1])
+            d1 = np.where(even[:, None], b[3], b[2])
+            o1 = np.where(even[:, None], b[1], b[0])
+            o2 = np.where(even[:, None], b[2], b[3])
+            for o in (o1, o2):
+                tv = np.stack([d0, d1, o, c])
+                tets.append(_orient(tv, (0, 1, 2, 3)))
+    return (np.concatenate(pyrs, axis=1),
+            np.concatenate(tets, axis=1) if tets else None)
+
+
 def mixed_box(n, lo, hi, kinds):
     """Conforming periodic box of n^3 cubic cells of side (hi - lo)/n.
 
     ``kinds`` is 'hex-pri' (cells with x index below n/2 are hexes, the
-    others are cut into two prisms extruded along z) or 'pri-tet' (cells
+    others are cut into two prisms extruded along z), 'pri-tet' (cells
     with z index below n/2 are cut into two prisms, the others into the six
-    tetrahedra of the Kuhn subdivision).  A hex face never meets a
-    tetrahedron: their quadrilateral and triangular faces do not conform.
-    Elements of each type are numbered cell by cell, x fastest."""
+    tetrahedra of the Kuhn subdivision) or 'hex-pyr-tet' (cells with x
+    index below n/2 are hexes; the others are cut into six pyramids about
+    their centres, and every pyramid whose base is not shared with a hex
+    into two tetrahedra, so that hexes and tetrahedra meet through
+    pyramids) or 'pyr' (every cell cut into its six pyramids).  A hex face
+    never meets a tetrahedron: their quadrilateral and triangular faces do
+    not conform.  Elements of each type are numbered cell by cell, x
+    fastest, except in 'hex-pyr-tet' and 'pyr', where the pyramids and
+    tetrahedra are numbered face by face."""
     corners, idx = _cube_cells(n, lo, hi)
+    if kinds in ('hex-pyr-tet', 'pyr'):
+        if n < 2:
+            raise ValueError(f'{kinds} needs at least two cells a side')
+        if kinds == 'pyr':
+            pyr, _ = _pyr_tet_cells(corners, idx,
+                                    np.ones(idx.shape[1], dtype=bool), n,
+                                    cut=False)
+            spts = {'pyr': pyr}
+        else:
+            first = idx[0] < n//2
+            pyr, tet = _pyr_tet_cells(corners, idx, ~first, n)
+            spts = {'hex': corners[:, first], 'pyr': pyr, 'tet': tet}
+        con = connect(spts, periods=(hi - lo,)*3, lo=(lo,)*3)
+        return Mesh(ndims=3, spts=spts, con=con,
+                    spts_curved={k: np.zeros(v.shape[1], dtype=bool)
+                                 for k, v in spts.items()},
+                    periods=(hi - lo,)*3)
     if kinds == 'hex-pri':
         first = idx[0] < n//2
         spts = {'hex': corners[:, first],

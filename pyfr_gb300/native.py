@@ -175,6 +175,14 @@ def std_ele(etype, order):
         return np.array([(t[i], t[j], z) for z in t
                          for j in range(order + 1)
                          for i in range(order + 1 - j)])
+    if etype == 'pyr':
+        # Layer k at z = -1 + 2k/order holds (order + 1 - k)^2 nodes at
+        # x, y = -1 + (k + 2m)/order (pyfr/shapes.py:618-626)
+        return np.array([(-1 + (k + 2*i)/order, -1 + (k + 2*j)/order,
+                          -1 + 2*k/order)
+                         for k in range(order + 1)
+                         for j in range(order + 1 - k)
+                         for i in range(order + 1 - k)], dtype=float)
     raise ValueError(f'Unknown element type {etype!r}')
 
 

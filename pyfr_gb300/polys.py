@@ -140,6 +140,81 @@ class TensorProdBasis:
         return self.invvdm @ self.jac_ortho_basis_at(epts)
 
 
+def homogeneous_legendre(order, x, s):
+    """H_k(x, s) = s^k P_k(x/s), k = 0..order, with the partial derivatives
+    dH_k/dx and dH_k/ds: Bonnet's recursion multiplied through by s^k,
+    H_k = ((2k - 1) x H_(k-1) - (k - 1) s^2 H_(k-2))/k, which keeps every
+    H_k a polynomial in x and s (no division by s, so the pyramid's apex
+    s = 0 is an ordinary point).  Three arrays of shape
+    (order + 1, len(x))."""
+    x, s = np.broadcast_arrays(np.asarray(x, dtype=float),
+                               np.asarray(s, dtype=float))
+    h = np.zeros((order + 1,) + x.shape)
+    hx, hs = np.zeros_like(h), np.zeros_like(h)
+    h[0] = 1.0
+    if order >= 1:
+        h[1], hx[1] = x, 1.0
+    for k in range(2, order + 1):
+        a, b = 2*k - 1, k - 1
+        h[k] = (a*x*h[k - 1] - b*s*s*h[k - 2])/k
+        hx[k] = (a*(h[k - 1] + x*hx[k - 1]) - b*s*s*hx[k - 2])/k
+        hs[k] = (a*x*hs[k - 1] - b*(2*s*h[k - 2] + s*s*hs[k - 2]))/k
+    return h, hx, hs
+
+
+class PyrBasis(TensorProdBasis):
+    """The pyramid's polynomial space of order p (``pyfr/polys.py:333-402``):
+    spanned by (1 - z)^(i+j) P_i(2x/(1 - z)) P_j(2y/(1 - z)) times every
+    polynomial in z of degree <= p - max(i, j), for 0 <= i, j <= p.  With
+    s = (1 - z)/2 the first factor is 2^(i+j) H_i(x, s) H_j(y, s) for the
+    homogeneous Legendre polynomials H, so the modes here are
+    H_i(x, s) H_j(y, s) L_k(z) with L_k the orthonormal Legendre
+    polynomials, k <= p - max(i, j): polynomials (the reference's
+    collapsed-coordinate modes, orthonormal on the pyramid, span the same
+    space; the nodal basis at the solution points is the same).  They are
+    made orthonormal on the pyramid by a Gram-Schmidt step (the Cholesky
+    factor of their Gram matrix, integrated exactly), which keeps the
+    Vandermonde matrices as well conditioned as the reference's.  The mode
+    tuples (i, j, k) are listed in the reference's order."""
+
+    def __init__(self, order, pts=None):
+        from pyfr_gb300.quadrules import pyr_gauss
+        modes = [(i, j, k) for i in range(order + 1)
+                 for j in range(order + 1)
+                 for k in range(order - max(i, j) + 1)]
+        super().__init__(3, order, pts, modes)
+        self._orth = np.eye(len(modes))
+        qp, qw = pyr_gauss(4*order)
+        for _ in range(2):          # twice: Gram-Schmidt's reorthogonalisation
+            raw = self.ortho_basis_at(qp)
+            c = np.linalg.cholesky((raw*qw) @ raw.T)
+            self._orth = np.linalg.solve(c, self._orth)
+
+    def _parts(self, pts):
+        pts = np.atleast_2d(np.asarray(pts, dtype=float)).reshape(-1, 3)
+        x, y, z = pts.T
+        s = (1 - z)/2
+        return (homogeneous_legendre(self.order, x, s),
+                homogeneous_legendre(self.order, y, s),
+                legendre_orthonormal(self.order, z))
+
+    def ortho_basis_at(self, pts):
+        (hx, _, _), (hy, _, _), (lz, _) = self._parts(pts)
+        return self._orth @ np.array([hx[i]*hy[j]*lz[k]
+                                      for i, j, k in self.modes])
+
+    def jac_ortho_basis_at(self, pts):
+        (hx, hxx, hxs), (hy, hyy, hys), (lz, dlz) = self._parts(pts)
+        out = np.empty((3, len(self.modes), hx.shape[1]))
+        for m, (i, j, k) in enumerate(self.modes):
+            out[0, m] = hxx[i]*hy[j]*lz[k]
+            out[1, m] = hx[i]*hyy[j]*lz[k]
+            # d/dz = -1/2 d/ds on the H factors
+            out[2, m] = (hx[i]*hy[j]*dlz[k] -
+                         0.5*(hxs[i]*hy[j] + hx[i]*hys[j])*lz[k])
+        return self._orth @ out
+
+
 def tidy(arr, tol=1e-10):
     """Flush entries below ``tol`` to exact zero and give entries whose
     magnitudes agree to a relative ``tol`` one common magnitude.

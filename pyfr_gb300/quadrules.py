@@ -15,6 +15,8 @@ Everything here is computed, not tabulated:
   where the reference uses tabulated symmetric rules of at least the same
   degree (``pyfr/shapes.py:232-255``) -- exact rules give the same
   integrals up to rounding;
+* the collapsed Gauss rule of the pyramid and its layered Gauss-Legendre
+  and Gauss-Legendre-Lobatto point sets (``pyfr/quadrules/pyr``);
 * the warp-and-blend 'alpha-optimised' interpolation nodes on the triangle
   and tetrahedron (T. Warburton, J. Eng. Math. 56, 2006, 247-262; the
   optimised blending parameters are the ones published there), the point
@@ -116,6 +118,48 @@ def pri_gauss(qdeg):
     return pts, wts
 
 
+def pyr_gauss(qdeg):
+    """Collapsed Gauss-Legendre rule on the reference pyramid (base
+    [-1,1]^2 at z = -1, apex (0, 0, 1)) exact for total degree ``qdeg``:
+    the cube [-1,1]^3 mapped by x = u(1 - w)/2, y = v(1 - w)/2, z = w,
+    whose Jacobian ((1 - w)/2)^2 raises the degree in w by two."""
+    n, nz = qdeg//2 + 1, (qdeg + 2)//2 + 1
+    x, wx = gauss_legendre(n)
+    z, wz = gauss_legendre(nz)
+    pts, wts = [], []
+    for w, ww in zip(z, wz):
+        h = (1 - w)/2
+        for v, wv in zip(x, wx):
+            for u, wu in zip(x, wx):
+                pts.append((u*h, v*h, w))
+                wts.append(wu*wv*ww*h*h)
+    return np.array(pts), np.array(wts)
+
+
+def pyr_layers(rule, order):
+    """The layered pyramid point sets of the reference's tables
+    ``pyfr/quadrules/pyr/gauss-legendre-n*`` and
+    ``gauss-legendre-lobatto-n*``: with n = order + 1, the k-th point of
+    the n-point line rule (ascending) is the height z of a layer holding
+    the (n - k)^2 tensor points of the (n - k)-point line rule scaled by
+    (1 - z)/2 (x fastest, then y); layers in ascending z, except that the
+    Lobatto set lists its apex, the one-point top layer, first."""
+    n = order + 1
+    zs, _ = RULES_1D[rule](n)
+    layers = []
+    for k, z in enumerate(zs):
+        m = n - k
+        if m == 1:
+            xs = np.zeros(1)
+        else:
+            xs, _ = RULES_1D[rule](m)
+        h = (1 - z)/2
+        layers.append([(x*h, y*h, z) for y in xs for x in xs])
+    if rule == 'gauss-legendre-lobatto' and n > 1:
+        layers = [layers[-1]] + layers[:-1]
+    return np.array([p for layer in layers for p in layer], dtype=float)
+
+
 def quad_gauss(qdeg):
     return tensor_rule('gauss-legendre', qdeg//2 + 1, 2)
 
@@ -130,7 +174,8 @@ def line_gauss(qdeg):
 
 
 EXACT_RULES = {'line': line_gauss, 'tri': tri_gauss, 'quad': quad_gauss,
-               'tet': tet_gauss, 'pri': pri_gauss, 'hex': hex_gauss}
+               'tet': tet_gauss, 'pri': pri_gauss, 'hex': hex_gauss,
+               'pyr': pyr_gauss}
 
 
 # ---------------------------------------------------------------------------
@@ -306,7 +351,7 @@ def parse_rule(text, ndims):
     return np.array(pts, dtype=float), (np.array(wts) if wts else None)
 
 
-_NDIMS = dict(line=1, tri=2, quad=2, tet=3, pri=3, hex=3)
+_NDIMS = dict(line=1, tri=2, quad=2, tet=3, pri=3, hex=3, pyr=3)
 
 
 def is_literal(rule):
@@ -325,6 +370,8 @@ def point_set(kind, rule, order):
         pts = alpha_opt_tri(order)
     elif kind == 'tet' and rule == 'alpha-opt':
         pts = alpha_opt_tet(order)
+    elif kind == 'pyr' and rule in RULES_1D:
+        pts = pyr_layers(rule, order)
     elif kind == 'pri' and '~' in rule:
         trule, lrule = rule.split('~')
         tp = point_set('tri', trule, order)
@@ -334,7 +381,8 @@ def point_set(kind, rule, order):
         raise ValueError(f'No point set {rule!r} for {kind}')
 
     npts = {'line': n, 'quad': n**2, 'hex': n**3, 'tri': n*(n + 1)//2,
-            'tet': n*(n + 1)*(n + 2)//6, 'pri': n*n*(n + 1)//2}[kind]
+            'tet': n*(n + 1)*(n + 2)//6, 'pri': n*n*(n + 1)//2,
+            'pyr': n*(n + 1)*(2*n + 1)//6}[kind]
     if len(pts) != npts:
         raise ValueError(f'Rule {rule!r} has {len(pts)} points; {kind} '
                          f'order {order} needs {npts}')

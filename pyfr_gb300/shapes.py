@@ -21,8 +21,9 @@ These follow the definitions of ``pyfr/shapes.py:80-125`` and
 orderings, face parametrisations and normals (``pyfr/shapes.py:341-566``)
 so that operators, element data and interface maps line up one-to-one with
 the reference.  Quadrilaterals and hexahedra (Gauss-Legendre or
-Gauss-Legendre-Lobatto points), triangles, tetrahedra ('alpha-opt' points)
-and prisms (triangle points times line points) are provided; any shape
+Gauss-Legendre-Lobatto points), triangles, tetrahedra ('alpha-opt' points),
+prisms (triangle points times line points) and pyramids (layered
+Gauss-Legendre or Gauss-Legendre-Lobatto points) are provided; any shape
 also takes literal point sets in the reference's rule text format.
 
 The tensor-product shapes form the lift from orthonormal modes, as the
@@ -36,7 +37,7 @@ import re
 
 import numpy as np
 
-from pyfr_gb300.polys import TensorProdBasis, space_modes, tidy
+from pyfr_gb300.polys import PyrBasis, TensorProdBasis, space_modes, tidy
 from pyfr_gb300.quadrules import (EXACT_RULES, gauss_legendre,
                                   gauss_legendre_lobatto, point_set,
                                   tensor_rule)
@@ -62,6 +63,11 @@ class BaseShape:
     # reference's face order
     faces = None
 
+    # Largest total degree of the solution space, in multiples of the
+    # order (the pyramid's modes reach twice the order); it sets the
+    # degrees of the quadratures that integrate mass matrices and lifts
+    space_degree = 1
+
     def __init__(self, order, upts_rule='gauss-legendre',
                  fpts_rule='gauss-legendre'):
         self.order = order
@@ -72,8 +78,11 @@ class BaseShape:
         self.fpts_rules = {k: fpts_rule[k] for k in kinds}
 
         self.upts = point_set(self.name, upts_rule, order)
-        self.ubasis = TensorProdBasis(self.ndims, order, self.upts,
-                                      self._modes(self.name))
+        self.ubasis = self._solution_basis()
+
+    def _solution_basis(self):
+        return TensorProdBasis(self.ndims, self.order, self.upts,
+                               self._modes(self.name))
 
     def _modes(self, kind):
         return space_modes(kind, self.order)
@@ -232,7 +241,7 @@ class BaseShape:
         solution space, at the solution points: with the element's exact
         mass matrix M, c = M^-1 sum_q w_q l_i(x_q) f_q (the reference's
         orthonormal-mode form, pyfr/shapes.py:17-19,131-133)."""
-        qp, qw = EXACT_RULES[self.name](2*self.order)
+        qp, qw = EXACT_RULES[self.name](2*self.space_degree*self.order)
         L = self.ubasis.nodal_basis_at(qp)
         mass = L.T @ (qw[:, None]*L)
         lq = self.ubasis.nodal_basis_at(self.qpts)          # (nq, nupts)
@@ -263,14 +272,14 @@ class BaseShape:
         (face integrals in the face parametrisation, whose measure the
         unnormalised reference normals account for); returns the
         (nupts, nfpts) values g_f(upts) = c_f."""
-        q = 2*self.order
-        qp, qw = EXACT_RULES[self.name](q)
+        f = self.space_degree
+        qp, qw = EXACT_RULES[self.name](2*f*self.order)
         L = self.ubasis.nodal_basis_at(qp)                 # (nq, nupts)
         mass = L.T @ (qw[:, None]*L)
 
         cols = []
         for kind, proj, norm in self.faces:
-            fq, fw = EXACT_RULES[kind](q)
+            fq, fw = EXACT_RULES[kind]((f + 1)*self.order)
             lf = self.facebases[kind].nodal_basis_at(fq)   # (nfq, nff)
             le = self.ubasis.nodal_basis_at(_proj(proj, fq))
             cols.append(le.T @ (fw[:, None]*lf))
@@ -398,6 +407,26 @@ class PriShape(SimplexLikeShape):
     ]
 
 
+class PyrShape(SimplexLikeShape):
+    """The pyramid: square base at z = -1, apex (0, 0, 1)
+    (pyfr/shapes.py:573-635); its solution space holds modes of total
+    degree up to twice the order."""
+    name = 'pyr'
+    ndims = 3
+    space_degree = 2
+
+    faces = [
+        ('quad', lambda s, t: (s, t, -1), (0, 0, -1)),
+        ('tri', lambda s, t: (s + (t + 1)/2, (t - 1)/2, t), (0, -1, 0.5)),
+        ('tri', lambda s, t: ((1 - t)/2, -s - (t + 1)/2, t), (1, 0, 0.5)),
+        ('tri', lambda s, t: (-s - (t + 1)/2, (1 - t)/2, t), (0, 1, 0.5)),
+        ('tri', lambda s, t: ((t - 1)/2, s + (t + 1)/2, t), (-1, 0, 0.5)),
+    ]
+
+    def _solution_basis(self):
+        return PyrBasis(self.order, self.upts)
+
+
 # Vertices of the linear elements, in the reference's order (std_ele(1)
 # of pyfr/shapes.py)
 VERTICES = {
@@ -408,11 +437,12 @@ VERTICES = {
     'tet': [(-1, -1, -1), (1, -1, -1), (-1, 1, -1), (-1, -1, 1)],
     'pri': [(-1, -1, -1), (1, -1, -1), (-1, 1, -1),
             (-1, -1, 1), (1, -1, 1), (-1, 1, 1)],
+    'pyr': [(-1, -1, -1), (1, -1, -1), (-1, 1, -1), (1, 1, -1), (0, 0, 1)],
 }
 
 # Element type from (ndims, number of vertices)
 ETYPE_OF = {(2, 4): 'quad', (3, 8): 'hex', (2, 3): 'tri', (3, 4): 'tet',
-            (3, 6): 'pri'}
+            (3, 6): 'pri', (3, 5): 'pyr'}
 
 
 def _simplex_bary(x):
@@ -441,6 +471,8 @@ def linear_shape_fn(etype, x):
         lam, _ = _simplex_bary(x[:, :2])
         z = x[:, 2:3]
         return np.hstack([lam*(1 - z)/2, lam*(1 + z)/2])
+    if etype == 'pyr':
+        return _pyr_shape(x)[0]
     raise ValueError(etype)
 
 
@@ -471,11 +503,33 @@ def linear_shape_jac(etype, x):
         out[:, 2, :3] = -lam/2
         out[:, 2, 3:] = lam/2
         return out
+    if etype == 'pyr':
+        return _pyr_shape(x)[1]
     raise ValueError(etype)
 
 
+def _pyr_shape(x):
+    """Shape functions and their reference gradients of the linear pyramid
+    (the space {1, x, y, z, xy} of the reference's interpolation and
+    Jacobian expressions, pyfr/shapes.py:590-616): a base vertex
+    (xv, yv, -1) has N = (2 (1 + xv x)(1 + yv y) - (1 + z))/8, the apex
+    N = (1 + z)/2.  The map is affine when the base is a parallelogram."""
+    npt = len(x)
+    v = np.array(VERTICES['pyr'][:4], dtype=float)
+    px, py, pz = x[:, 0:1], x[:, 1:2], x[:, 2:3]
+    fx, fy = 1 + v[None, :, 0]*px, 1 + v[None, :, 1]*py
+    N = np.hstack([(2*fx*fy - (1 + pz))/8, (1 + pz)/2])
+    dN = np.empty((npt, 3, 5))
+    dN[:, 0, :4] = v[None, :, 0]*fy/4
+    dN[:, 1, :4] = v[None, :, 1]*fx/4
+    dN[:, 2, :4] = -1/8
+    dN[:, 0, 4] = dN[:, 1, 4] = 0
+    dN[:, 2, 4] = 1/2
+    return N, dN
+
+
 SHAPES = {'quad': QuadShape, 'hex': HexShape, 'tri': TriShape,
-          'tet': TetShape, 'pri': PriShape}
+          'tet': TetShape, 'pri': PriShape, 'pyr': PyrShape}
 
 
 def get_shape(name, order, upts_rule='gauss-legendre',

@@ -30,7 +30,8 @@ from pyfr_gb300.shapes import SHAPES, adjugate_det, get_shape
 # solver-interfaces-<kind> flux-pts)
 DEFAULT_UPTS = {'quad': 'gauss-legendre', 'hex': 'gauss-legendre',
                 'tri': 'alpha-opt', 'tet': 'alpha-opt',
-                'pri': 'alpha-opt~gauss-legendre-lobatto'}
+                'pri': 'alpha-opt~gauss-legendre-lobatto',
+                'pyr': 'gauss-legendre'}
 DEFAULT_FPTS = {'line': 'gauss-legendre', 'quad': 'gauss-legendre',
                 'tri': 'alpha-opt'}
 

@@ -18,6 +18,9 @@ What is generated (all with the reference's own code):
   ``pyfr/tests/test_ele_mats.py``).
 * ``bases.npz``: the orthonormal simplex bases at the solution points.
 * ``surf_flux.npz``: operators with surface-flux anti-aliasing.
+* pyramids (``make_pyr``): the pyramid's operators at orders 1-4, the
+  geometry of pyramids whose maps are not affine, and a periodic box where
+  hexahedra meet tetrahedra through pyramids.
 * ``geometry_<case>.npz``: element geometry computed by the reference's
   ``EulerElements``/``NavierStokesElements`` (``pyfr/solvers/base/elements.py``)
   on small periodic meshes whose interior vertices are randomly perturbed
@@ -312,6 +315,102 @@ def make_mixed():
     np.savez_compressed(HERE / 'operators.npz', **ops)
 
 
+PYR_CASES = [(p, r) for p in (1, 2, 3, 4)
+             for r in ('gauss-legendre', 'gauss-legendre-lobatto')]
+
+
+def hexpyrtet_box(n, lo, hi, amp, seed):
+    """The hexahedron-pyramid-tetrahedron box with the centre vertex of
+    every cut cell (the apex of its pyramids, a vertex of its tetrahedra)
+    moved by a random offset: watertight, every element affine, the
+    pyramids oblique."""
+    sys.path.insert(0, str(REPO))
+    from pyfr_gb300.mesh import mixed_box
+
+    mesh = mixed_box(n, lo, hi, 'hex-pyr-tet')
+    h = (hi - lo)/n
+    rng = np.random.default_rng(seed)
+    jit = rng.uniform(-amp*h, amp*h, size=(n, n, n, 3))
+    for et, v in (('pyr', 4), ('tet', 3)):
+        c = mesh.spts[et][v]
+        cell = np.floor((c - lo)/h).astype(int)
+        c += jit[cell[:, 0], cell[:, 1], cell[:, 2]]
+    return mesh
+
+
+def make_pyr():
+    """Pyramids (appended to ``operators.npz``; ``geometry_pyrskew_p3.npz``
+    and ``geometry_hexpyrtet_p3.npz``): the reference's pyramid operators
+    at orders 1-4 with its tabulated 'gauss-legendre' and
+    'gauss-legendre-lobatto' solution points (Gauss-Legendre flux points on
+    the square face, this package's 'alpha-opt' points given literally on
+    the triangular faces); the geometry of pyramids with random vertices
+    (bases that are not parallelograms: maps that are not affine); and the
+    geometry and initial conditions of a periodic box where hexahedra meet
+    tetrahedra through pyramids."""
+    sys.path.insert(0, str(REPO))
+    from pyfr.shapes import HexShape, PyrShape, TetShape
+    from pyfr.solvers.euler.elements import EulerElements
+    from pyfr_gb300.quadrules import point_set
+
+    ops = dict(np.load(HERE / 'operators.npz'))
+    for p, r in PYR_CASES:
+        fpts = {'quad': 'gauss-legendre',
+                'tri': _literal(point_set('tri', 'alpha-opt', p))}
+        _store_shape(ops, f'pyr_p{p}_{r}', PyrShape(None, _cfg('pyr', p, r,
+                                                             fpts)))
+    np.savez_compressed(HERE / 'operators.npz', **ops)
+    print('operators.npz:', len(ops), 'arrays')
+
+    fpts = {'quad': 'gauss-legendre',
+            'tri': _literal(point_set('tri', 'alpha-opt', 3))}
+    upts = {'hex': 'gauss-legendre', 'pyr': 'gauss-legendre',
+            'tet': _literal(point_set('tet', 'alpha-opt', 3))}
+    shapes = {'hex': HexShape, 'pyr': PyrShape, 'tet': TetShape}
+    ics = dict(rho='1 + 0.2*sin(pi*x)*cos(pi*y)*cos(pi*z)',
+               u='0.5 + 0.1*y', v='-0.3 + 0.1*z', w='0.2*x',
+               p='1 + 0.1*cos(pi*x)')
+
+    def elements(et, spts):
+        cfg = _cfg(et, 3, upts[et], fpts, consts=dict(gamma=1.4), ics=ics)
+        return EulerElements(shapes[et], spts, cfg)
+
+    # Pyramids with random vertices about the reference pyramid
+    rng = np.random.default_rng(5)
+    base = np.array([(-1, -1, -1), (1, -1, -1), (-1, 1, -1), (1, 1, -1),
+                     (0, 0, 1)], dtype=float)
+    spts = base[:, None, :]*0.5 + rng.uniform(-0.12, 0.12, size=(5, 6, 3))
+    e = elements('pyr', spts)
+    out = dict(spts=spts, pnorm_fpts=e._pnorm_fpts,
+               rcpdjac_upts=e.rcpdjac_at_np('upts'),
+               smat_upts=e.smat_at_np('upts'), ploc_upts=e.ploc_at_np('upts'),
+               ics=e.set_ics_from_cfg())
+    np.savez_compressed(HERE / 'geometry_pyrskew_p3.npz', **out)
+    print('geometry_pyrskew_p3.npz')
+
+    mesh = hexpyrtet_box(2, -1.0, 1.0, 0.15, seed=13)
+    out = {}
+    for et, spts in mesh.spts.items():
+        e = elements(et, spts)
+        out[f'{et}/spts'] = spts
+        for fi, sf in enumerate(e.srtd_face_fpts):
+            out[f'{et}/srtd_face_fpts/{fi}'] = sf
+        out[f'{et}/pnorm_fpts'] = e._pnorm_fpts
+        out[f'{et}/rcpdjac_upts'] = e.rcpdjac_at_np('upts')
+        out[f'{et}/smat_upts'] = e.smat_at_np('upts')
+        out[f'{et}/ploc_upts'] = e.ploc_at_np('upts')
+        out[f'{et}/ics'] = e.set_ics_from_cfg()
+    lhs, rhs = mesh.con
+    out['lhs'] = np.stack([lhs.etypes, lhs.eidxs.astype(str),
+                           lhs.fidxs.astype(str)], axis=1)
+    out['rhs'] = np.stack([rhs.etypes, rhs.eidxs.astype(str),
+                           rhs.fidxs.astype(str)], axis=1)
+    for k, v in ics.items():
+        out[f'icexpr/{k}'] = np.array(v)
+    np.savez_compressed(HERE / 'geometry_hexpyrtet_p3.npz', **out)
+    print('geometry_hexpyrtet_p3.npz')
+
+
 def make_bases():
     """``bases.npz``: the reference's orthonormal simplex bases
     (``pyfr.polys``) at the solution points of tri, tet and pri at orders
@@ -364,6 +463,7 @@ if __name__ == '__main__':
     sys.path.insert(0, str(REF))
     _install_standins()
     steps = dict(operators=make_operators, geometry=make_geometry,
-                 mixed=make_mixed, bases=make_bases, surf=make_surf)
+                 mixed=make_mixed, bases=make_bases, surf=make_surf,
+                 pyr=make_pyr)
     for name in sys.argv[1:] or list(steps):
         steps[name]()

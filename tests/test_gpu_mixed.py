@@ -1,5 +1,6 @@
 """Meshes of several element types (hexahedra with prisms, prisms with
-tetrahedra) through the CUDA path against the CPU oracle.
+tetrahedra, hexahedra with tetrahedra through pyramids) through the CUDA
+path against the CPU oracle.
 
 Plain FP64: relative max-norm tolerance 1e-10 on every conserved variable
 of every element type, for the right-hand side on perturbed meshes (the
@@ -10,7 +11,7 @@ import numpy as np
 import pytest
 
 from oracle.fr_oracle import rk45_step
-from tests.test_oracle import MIXED_FPTS, MIXED_UPTS, mixed_disc
+from tests.test_oracle import MIXED_FPTS, MIXED_UPTS, mixed_disc, mixed_key
 
 pytestmark = pytest.mark.gpu
 
@@ -42,7 +43,7 @@ def _cfg(rsolver='rusanov'):
 
 def _golden_mesh(g):
     from pyfr_gb300.mesh import Mesh, Side
-    spts = {et: g[f'{et}/spts'] for et in ('hex', 'pri', 'tet')
+    spts = {et: g[f'{et}/spts'] for et in ('hex', 'pri', 'tet', 'pyr')
             if f'{et}/spts' in g}
     sides = [Side(s[:, 0], s[:, 1].astype(int), s[:, 2].astype(int))
              for s in (g['lhs'], g['rhs'])]
@@ -57,7 +58,7 @@ def _backend(cfg):
     return B200Backend(cfg)
 
 
-@pytest.mark.parametrize('case', ['hexpri_p3', 'pritet_p3'])
+@pytest.mark.parametrize('case', ['hexpri_p3', 'pritet_p3', 'hexpyrtet_p3'])
 @pytest.mark.parametrize('rsolver', ['rusanov', 'hllc'])
 def test_euler_rhs_mixed_mesh(built, golden, case, rsolver):
     from pyfr_gb300.solvers.system import EulerSystem
@@ -76,7 +77,7 @@ def test_euler_rhs_mixed_mesh(built, golden, case, rsolver):
         assert _relerr(got[et], ref[et]) < TOL, et
 
 
-@pytest.mark.parametrize('kinds', ['hex-pri', 'pri-tet'])
+@pytest.mark.parametrize('kinds', ['hex-pri', 'pri-tet', 'hex-pyr-tet'])
 def test_rk45_mixed_mesh(built, golden, kinds):
     """Three RK45 steps of the advected density wave, CUDA graphs on."""
     from oracle.fr_oracle import MixedDiscretisation
@@ -95,10 +96,9 @@ def test_rk45_mixed_mesh(built, golden, kinds):
     ops = golden['operators']
     parts = {}
     for et, verts in mesh.spts.items():
-        key = 'hex_p3_gauss-legendre' if et == 'hex' else f'{et}_p3_mixed'
         s = get_shape(et, 3, MIXED_UPTS[et], MIXED_FPTS)
-        parts[et] = dict(ops=ops_from_golden(ops, key), basis=basis_of(s),
-                         verts=verts)
+        parts[et] = dict(ops=ops_from_golden(ops, mixed_key(et)),
+                         basis=basis_of(s), verts=verts)
     lhs, rhs = mesh.con
     d = MixedDiscretisation(parts, zip(lhs.etypes, lhs.eidxs, lhs.fidxs),
                             zip(rhs.etypes, rhs.eidxs, rhs.fidxs),
@@ -113,7 +113,7 @@ def test_rk45_mixed_mesh(built, golden, kinds):
         assert _relerr(got[et], ref[et]) < TOL, et
 
 
-@pytest.mark.parametrize('kinds', ['hex-pri', 'pri-tet'])
+@pytest.mark.parametrize('kinds', ['hex-pri', 'pri-tet', 'hex-pyr-tet'])
 def test_mixed_mesh_precision_forms(built, kinds):
     """The precision forms (FP32 fluxes, FP64 RK accumulation) against the
     FP64 solution after ten steps.  This flow carries O(1) mean fluxes
@@ -154,7 +154,7 @@ def test_mixed_mesh_precision_forms(built, kinds):
         assert e5 <= 1e-6, (e5, eb, e32)
 
 
-@pytest.mark.parametrize('kinds', ['hex-pri', 'pri-tet'])
+@pytest.mark.parametrize('kinds', ['hex-pri', 'pri-tet', 'hex-pyr-tet'])
 def test_mixed_mesh_density_wave_accuracy(built, kinds):
     """The advected density wave stays close to its exact translation
     (a discretisation check, independent of the oracle).  With six cells
@@ -174,7 +174,7 @@ def test_mixed_mesh_density_wave_accuracy(built, kinds):
         assert np.abs(u[:, 0] - rho).max() < 2e-2
 
 
-@pytest.mark.parametrize('case', ['hexpri_p3', 'pritet_p3'])
+@pytest.mark.parametrize('case', ['hexpri_p3', 'pritet_p3', 'hexpyrtet_p3'])
 @pytest.mark.parametrize('beta', [0.5, 0.0])
 def test_ns_rhs_mixed_mesh(built, golden, case, beta):
     """Navier-Stokes on the perturbed mixed meshes (gradient operators of
@@ -201,9 +201,8 @@ def test_ns_rhs_mixed_mesh(built, golden, case, beta):
     ops = golden['operators']
     parts = {}
     for et in mesh.spts:
-        key = 'hex_p3_gauss-legendre' if et == 'hex' else f'{et}_p3_mixed'
         sh = get_shape(et, 3, MIXED_UPTS[et], MIXED_FPTS)
-        parts[et] = dict(ops=ops_from_golden(ops, key, True),
+        parts[et] = dict(ops=ops_from_golden(ops, mixed_key(et), True),
                          basis=basis_of(sh), verts=mesh.spts[et])
     d = MixedDiscretisation(parts, g['lhs'], g['rhs'], periods=(2.0,)*3)
     ref = d.rhs_ns(ics, gas)

@@ -83,8 +83,15 @@ def test_discrete_conservation(golden, case, etype):
 # ---------------------------------------------------------------------------
 
 MIXED_UPTS = {'hex': 'gauss-legendre', 'pri': 'alpha-opt~gauss-legendre-lobatto',
-              'tet': 'alpha-opt'}
+              'tet': 'alpha-opt', 'pyr': 'gauss-legendre'}
 MIXED_FPTS = {'tri': 'alpha-opt', 'quad': 'gauss-legendre'}
+
+
+def mixed_key(et):
+    """Key of the reference's order-3 operators of ``et`` with the mixed
+    meshes' point sets in the golden operators."""
+    return {'hex': 'hex_p3_gauss-legendre',
+            'pyr': 'pyr_p3_gauss-legendre'}.get(et, f'{et}_p3_mixed')
 
 
 def mixed_disc(golden, case):
@@ -94,13 +101,12 @@ def mixed_disc(golden, case):
     g = golden[f'geometry_{case}']
     ops = golden['operators']
     parts = {}
-    for et in ('hex', 'pri', 'tet'):
+    for et in ('hex', 'pri', 'tet', 'pyr'):
         if f'{et}/spts' not in g:
             continue
-        key = 'hex_p3_gauss-legendre' if et == 'hex' else f'{et}_p3_mixed'
         s = get_shape(et, 3, MIXED_UPTS[et], MIXED_FPTS)
-        parts[et] = dict(ops=ops_from_golden(ops, key), basis=basis_of(s),
-                         verts=g[f'{et}/spts'])
+        parts[et] = dict(ops=ops_from_golden(ops, mixed_key(et)),
+                         basis=basis_of(s), verts=g[f'{et}/spts'])
     return MixedDiscretisation(parts, g['lhs'], g['rhs'],
                                periods=(2.0,)*3), g
 
