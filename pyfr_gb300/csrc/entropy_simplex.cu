@@ -1,13 +1,13 @@
-// Entropy filter kernels for triangles, tetrahedra and prisms of orders
-// 1-4 (a separate translation unit so that the library's parallel build
-// stays short); the kernels are in entropy.cuh.
+// Entropy filter kernels for triangles, tetrahedra, prisms and pyramids of
+// orders 1-4 (a separate translation unit so that the library's parallel
+// build stays short); the kernels are in entropy.cuh.
 #include "entropy.cuh"
 
 namespace b200_ef {
 
 #define EF_SIMPLEX_SHAPES(X)                                                       \
     X(2, 3) X(2, 6) X(2, 10) X(2, 15) X(3, 4) X(3, 10) X(3, 20) X(3, 35)            \
-    X(3, 6) X(3, 18) X(3, 40) X(3, 75)
+    X(3, 6) X(3, 18) X(3, 40) X(3, 75) X(3, 5) X(3, 14) X(3, 30) X(3, 55)
 
 template <typename T>
 int filter_simplex(const b200_ef_t *p, int64_t neles, T *u, int64_t ldu, T *entmin,

@@ -9,6 +9,11 @@ basis that results is independent of how the modes are enumerated, so only
 the ordering of the nodal points has to agree with the reference (x
 fastest, then y, then z).
 
+The pyramid's space (``pyfr/polys.py:333-402``) is not a set of Legendre
+products; ``PyrBasis`` spans it with homogeneous Legendre polynomials and
+orthonormalises them on the element, which reproduces the reference's
+orthonormal pyramid modes.
+
 The simplex and prism spaces (total degree <= p on the triangle and the
 tetrahedron; total degree <= p in (x, y) times degree <= p in z on the
 prism, the spaces of ``pyfr/polys.py:112-330``) are spanned here by
@@ -350,14 +355,20 @@ class SimplexOrthoBasis:
 
 def modal_basis(shape):
     """The orthonormal modal basis whose degree groups a filter or sensor
-    works with: the Legendre products of a quadrilateral or hexahedron (the
-    shape's own basis), the collapsed-coordinate bases of the other types.
+    works with: the Legendre products of a quadrilateral or hexahedron and
+    the pyramid's orthonormalised modes (the shapes' own bases), the
+    collapsed-coordinate bases of the other types.
     Returns (basis at the solution points, degree tuples of its modes,
     degree tuples of the basis one order lower)."""
     if shape.name in ('quad', 'hex'):
         ub = shape.ubasis
         lower = [m for m in ub.modes if max(m) < shape.order]
         return ub, list(ub.modes), lower
+    if shape.name == 'pyr':
+        # Orthonormalised in the reference's mode order, the pyramid's
+        # basis is the reference's orthonormal one
+        lower = PyrBasis(shape.order - 1).modes if shape.order > 0 else []
+        return shape.ubasis, list(shape.ubasis.modes), lower
     b = SimplexOrthoBasis(shape.name, shape.order, shape.upts)
     lower = SimplexOrthoBasis(shape.name, shape.order - 1).degrees \
         if shape.order > 0 else []

@@ -412,15 +412,16 @@ def make_pyr():
 
 
 def make_bases():
-    """``bases.npz``: the reference's orthonormal simplex bases
-    (``pyfr.polys``) at the solution points of tri, tet and pri at orders
-    1-4 (their degree tuples too), which the entropy filter and the shock
-    sensor group by degree."""
+    """``bases.npz``: the reference's orthonormal simplex and pyramid bases
+    (``pyfr.polys``) at the solution points of tri, tet, pri and pyr at
+    orders 1-4 (their degree tuples too), which the entropy filter and the
+    shock sensor group by degree."""
     from pyfr.polys import get_polybasis
     from pyfr.quadrules import get_quadrule
 
     rules = {'tri': 'alpha-opt', 'tet': 'alpha-opt',
-             'pri': 'alpha-opt~gauss-legendre-lobatto'}
+             'pri': 'alpha-opt~gauss-legendre-lobatto',
+             'pyr': 'gauss-legendre'}
     out = {}
     for kind, rule in rules.items():
         for p in range(1, 5):

@@ -1,5 +1,5 @@
-"""Shock capturing on triangles, tetrahedra and prisms (the collapsed-
-coordinate modal bases of pyfr/polys.py grouped by degree, as
+"""Shock capturing on triangles, tetrahedra, prisms and pyramids (the
+orthonormal modal bases of pyfr/polys.py grouped by degree, as
 pyfr/solvers/baseadvec/entfilter.py:93-116 and
 pyfr/solvers/baseadvecdiff/artvisc.py:160-196 group them).
 
@@ -31,7 +31,7 @@ def _relerr(a, b):
     return np.abs(a - b).max()/max(np.abs(b).max(), 1e-300)
 
 
-MESHES = ['tri', 'pri-tet', 'hex-pri']
+MESHES = ['tri', 'pri-tet', 'hex-pri', 'hex-pyr-tet']
 
 
 def _mesh(kinds):

@@ -238,3 +238,20 @@ def test_pyramid_box_free_stream(golden, order):
                                 (sh.nupts, 5, 48)).copy()}
     assert np.abs(d.rhs_euler(u, GAS)['pyr']).max() < 1e-11
     assert np.abs(d.rhs_ns(u, GAS)['pyr']).max() < 1e-11
+
+
+@pytest.mark.parametrize('order', [1, 2, 3, 4])
+def test_pyramid_modal_basis_is_the_references(golden, order):
+    """The modes the entropy filter and the shock sensor group by degree:
+    orthonormalised in the reference's mode order, they are the reference's
+    orthonormal pyramid modes, sign included (tests/golden/bases.npz)."""
+    from pyfr_gb300.polys import modal_basis
+    g = golden['bases']
+    key = f'pyr_p{order}'
+    s = get_shape('pyr', order, 'gauss-legendre', FPTS)
+    np.testing.assert_allclose(s.upts, g[f'{key}/pts'], atol=1e-15)
+    ub, modes, lower = modal_basis(s)
+    assert [tuple(d) for d in g[f'{key}/degrees']] == list(modes)
+    np.testing.assert_allclose(ub.vdm, g[f'{key}/vdm'], rtol=0,
+                               atol=1e-12 if order < 4 else 1e-10)
+    assert set(lower) < set(modes)
