@@ -573,7 +573,7 @@ def run_large(args, dist):
     return res
 
 
-def run_ensemble(args, dist):
+def run_ensemble(args, dist, unbatched=True):
     """The batching configuration's ensemble: independent 2-D vortex cases
     of uneven size (quads per side uniform in 16..96), order (2, 3, 4) and
     strength (beta uniform in 2..6) from one seed, merged by order and
@@ -639,6 +639,9 @@ def run_ensemble(args, dist):
     res['chosen']['accuracy_after_steps'] = args.warmup + nsteps
     del ens
 
+    if not unbatched:
+        return res
+
     # The same cases one system each (plain FP64), for the batching gain
     be = backend('double')
     intgs = []
@@ -662,7 +665,7 @@ def run_ensemble(args, dist):
     return res
 
 
-def run_mixed(args, dist):
+def run_mixed(args, dist, forms=('plain', 'chosen', 'tf32')):
     """The batching configuration's mixed meshes: 3-D Euler on a periodic
     box of n^3 cells, hexahedra and prisms, prisms and tetrahedra, or
     hexahedra and tetrahedra joined by pyramids (p = 3; an advected
@@ -696,7 +699,7 @@ def run_mixed(args, dist):
     res = {}
     for kinds in args.mixed_kinds.split(','):
         out, solns = {}, {}
-        for form in ('plain', 'chosen', 'tf32'):
+        for form in forms:
             prec = 'double' if form == 'plain' else 'single'
             cfg, mesh = euler_mixed(n=args.mixed_n, order=args.mixed_order,
                                     kinds=kinds, dt=args.mixed_dt,
@@ -724,7 +727,7 @@ def run_mixed(args, dist):
             solns[form] = [np.asarray(u, dtype=np.float64)
                            for u in intg.soln]
             del intg, be
-        for form in ('chosen', 'tf32'):
+        for form in forms[1:]:
             out[form]['l2_err_vs_fp64'] = max(
                 float(np.linalg.norm(a - b)/np.linalg.norm(b))
                 for a, b in zip(solns[form], solns['plain']))
@@ -733,6 +736,43 @@ def run_mixed(args, dist):
                 out[form]['gdofs']/out['plain']['gdofs']
         res[kinds] = out
     return res
+
+
+def run_batching(args, dist):
+    """The batching configuration in the default run, compactly: the
+    32^3-cell box where hexahedra meet tetrahedra through pyramids (3-D
+    Euler density wave, p = 3) and the 64-case vortex ensemble, each in
+    plain FP64 and the chosen form, 20 timed RK45 steps after 3 warm-up
+    steps, with the chosen form's L2 error against plain FP64."""
+    a = argparse.Namespace(**vars(args))
+    a.steps, a.warmup = 20, 3
+    a.mixed_kinds = 'hex-pyr-tet'
+    m = run_mixed(a, dist, forms=('plain', 'chosen'))['hex-pyr-tet']
+    e = run_ensemble(a, dist, unbatched=False)
+
+    def short(r, f):
+        d = {'gdofs': round(r[f]['gdofs'], 3),
+             'ms_per_step': round(r[f]['ms_per_step'], 3)}
+        for k in ('l2_err_vs_fp64', 'l2_err_vs_fp64_max'):
+            if k in r[f]:
+                d[k] = r[f][k]
+        return d
+
+    return {
+        'mixed_hex_pyr_tet': {
+            'config': f'{args.mixed_n}^3 cells: '
+                      + ', '.join(f'{n} {k}' for k, n in
+                                  m['plain']['neles'].items())
+                      + f', p=3, {m["plain"]["ndofs"]} DoF',
+            'plain': short(m, 'plain'), 'chosen': short(m, 'chosen'),
+            'speedup': round(m['speedup_chosen_vs_plain'], 2)},
+        'ensemble': {
+            'config': f'{e["ncases"]} 2-D vortex cases, p in 2-4, '
+                      f'{e["plain"]["ndofs"]} DoF, {e["plain"]["systems"]} '
+                      'systems in one graph per step',
+            'plain': short(e, 'plain'), 'chosen': short(e, 'chosen'),
+            'speedup': round(e['chosen']['gdofs']/e['plain']['gdofs'], 2)},
+        'steps': a.steps, 'warmup': a.warmup}
 
 
 # ---------------------------------------------------------------------------
@@ -807,6 +847,10 @@ def main():
     ap.add_argument('--mixed-dt', type=float, default=1e-3)
     ap.add_argument('--mixed-kinds', default='hex-pri,pri-tet,hex-pyr-tet',
                     help='comma-separated mixed meshes for --mixed')
+    ap.add_argument('--no-batching', dest='batching', action='store_false',
+                    help='leave out the batching summary of the default run '
+                         '(the hexahedron-pyramid-tetrahedron box and the '
+                         'vortex ensemble, plain FP64 and chosen form)')
     ap.add_argument('--ensemble', action='store_true',
                     help='the batching configuration\'s ensemble of 2-D '
                          'vortex cases instead of the headline run')
@@ -927,6 +971,7 @@ def main():
         return
 
     allres = run_gpu(args, Dist(world))
+    batching = run_batching(args, Dist(world)) if args.batching else None
     if rank != 0:
         return
 
@@ -1020,6 +1065,8 @@ def main():
                                    f'{args.cpu_sample}^3 TGV mesh '
                                    f'({cpu_ndofs} DoF, {cpu_dt:.1f} s)'},
     }
+    if batching is not None:
+        out['batching_summary'] = batching
     if chosen is not None:
         rc = allres['chosen']
         chosen['floor_frac'] = floor_frac(rc, 4)
