@@ -407,10 +407,14 @@ def measure(intg, args, dist, e2e=True, profile=True):
 
     if e2e:
         # End to end through the public API: the solution goes in from
-        # pinned host memory and comes back every step
-        mats = intg.acc if hasattr(intg, 'acc') else \
-            [b[intg.idxcurr] for b in intg.system.ele_banks]
-        m = mats[0]
+        # pinned host memory and comes back every step.  Each step's result
+        # makes a pipelined host round trip (b200_memcpy_roundtrip: down and
+        # back up chunk by chunk, the two directions overlapping) into the
+        # next step's input; the first input goes up whole and the last
+        # result only comes down
+        acc = hasattr(intg, 'acc')
+        m = intg.acc[0] if acc else \
+            intg.system.ele_banks[0][intg.idxcurr]
         nbytes = m.nbytes
         hbuf = C.c_void_p()
         lib.host_alloc(C.byref(hbuf), nbytes)
@@ -418,17 +422,18 @@ def measure(intg, args, dist, e2e=True, profile=True):
         be.wait()
         dist.barrier()
         lib.event_record(e0, stream)
-        for _ in range(args.steps):
-            if hasattr(intg, 'acc'):
-                lib.memcpy_htod(m.data, hbuf.value, nbytes, stream)
+        lib.memcpy_htod(m.data, hbuf.value, nbytes, stream)
+        for i in range(args.steps):
+            if acc:
                 intg.refresh_input(stream)
-                one_step()
-            else:
-                dst = intg.system.ele_banks[0][intg.idxcurr]
-                lib.memcpy_htod(dst.data, hbuf.value, nbytes, stream)
-                one_step()
+            one_step()
+            if not acc:
+                # The result is the next step's input register
                 m = intg.system.ele_banks[0][intg.idxcurr]
-            lib.memcpy_dtoh(hbuf.value, m.data, nbytes, stream)
+            last = i == args.steps - 1
+            lib.memcpy_roundtrip(hbuf.value, m.data, None if last else m.data,
+                                 nbytes, args.e2e_chunks, args.e2e_streams,
+                                 stream)
         lib.event_record(e1, stream)
         lib.event_sync(e1)
         dist.barrier()
@@ -847,6 +852,11 @@ def main():
     ap.add_argument('--mixed-dt', type=float, default=1e-3)
     ap.add_argument('--mixed-kinds', default='hex-pri,pri-tet,hex-pyr-tet',
                     help='comma-separated mixed meshes for --mixed')
+    ap.add_argument('--e2e-chunks', type=int, default=16,
+                    help='pieces of the pipelined host round trip of the '
+                         'end-to-end loop')
+    ap.add_argument('--e2e-streams', type=int, default=2,
+                    help='copy streams per direction of the round trip')
     ap.add_argument('--no-batching', dest='batching', action='store_false',
                     help='leave out the batching summary of the default run '
                          '(the hexahedron-pyramid-tetrahedron box and the '

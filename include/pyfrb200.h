@@ -127,12 +127,24 @@ int b200_device_info(int *sm_count, int *cc_major, int *cc_minor, size_t *free_b
                      size_t *total_bytes, char *name, size_t namelen);
 int b200_malloc(void **ptr, size_t nbytes);          /* zero-filled, as base.py:137-144 */
 int b200_free(void *ptr);
-int b200_host_alloc(void **ptr, size_t nbytes);      /* page-locked host memory */
+int b200_host_alloc(void **ptr, size_t nbytes);      /* page-locked, device-mapped host memory */
 int b200_host_free(void *ptr);
 int b200_memset(void *ptr, int value, size_t nbytes, void *stream);
 int b200_memcpy_htod(void *dst, const void *src, size_t nbytes, void *stream);
 int b200_memcpy_dtoh(void *dst, const void *src, size_t nbytes, void *stream);
 int b200_memcpy_dtod(void *dst, const void *src, size_t nbytes, void *stream);
+/* Host round trip of a device array, pipelined: after the work queued on
+ * `stream`, `dsrc` goes down to page-locked `host` and back up into `ddst`
+ * in `nchunks` pieces (1-64) on `nstreams` copy streams per direction
+ * (1-2), each piece going up as soon as it has come down, so that the two
+ * directions overlap; `stream` then waits for the last piece.  `ddst` null:
+ * down only.  `ddst` may equal `dsrc`.  nstreams -1 or -2: the pieces are
+ * copied by kernels through the host buffer's device mapping (memory from
+ * b200_host_alloc) instead of the copy engines.  No counterpart in the reference
+ * (its MPI exchanges stage through host memory, pyfr/backends/cuda/
+ * packing.py:8-112, without this overlap). */
+int b200_memcpy_roundtrip(void *host, const void *dsrc, void *ddst, size_t nbytes,
+                          int nchunks, int nstreams, void *stream);
 int b200_stream_create(void **stream);
 int b200_stream_destroy(void *stream);
 int b200_stream_sync(void *stream);

@@ -164,6 +164,7 @@ _SIGS = {
     'b200_memcpy_htod': [vp, vp, sz, vp],
     'b200_memcpy_dtoh': [vp, vp, sz, vp],
     'b200_memcpy_dtod': [vp, vp, sz, vp],
+    'b200_memcpy_roundtrip': [vp, vp, vp, sz, C.c_int, C.c_int, vp],
     'b200_stream_create': [C.POINTER(vp)],
     'b200_stream_destroy': [vp],
     'b200_stream_sync': [vp],

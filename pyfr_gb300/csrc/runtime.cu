@@ -115,7 +115,9 @@ int b200_free(void *ptr) { return check_cuda(cudaFree(ptr), "cudaFree"); }
 
 int b200_host_alloc(void **ptr, size_t nbytes) {
     if (!ptr) return set_error(B200_ERR_ARG, "null pointer");
-    return check_cuda(cudaMallocHost(ptr, nbytes ? nbytes : 1), "cudaMallocHost");
+    // Mapped, so that kernels may also reach it (b200_memcpy_roundtrip)
+    return check_cuda(cudaHostAlloc(ptr, nbytes ? nbytes : 1, cudaHostAllocMapped),
+                      "cudaHostAlloc");
 }
 
 int b200_host_free(void *ptr) { return check_cuda(cudaFreeHost(ptr), "cudaFreeHost"); }
@@ -138,6 +140,129 @@ int b200_memcpy_dtoh(void *dst, const void *src, size_t nbytes, void *stream) {
 int b200_memcpy_dtod(void *dst, const void *src, size_t nbytes, void *stream) {
     return check_cuda(cudaMemcpyAsync(dst, src, nbytes, cudaMemcpyDeviceToDevice,
                                       (cudaStream_t)stream), "memcpy DtoD");
+}
+
+// Copy streams and events of the pipelined round trip, made on first use
+namespace {
+constexpr int RT_MAX_CHUNKS = 64;
+struct RoundTrip {
+    cudaStream_t down[2] = {nullptr, nullptr}, up[2] = {nullptr, nullptr};
+    cudaEvent_t ready = nullptr, done[2] = {nullptr, nullptr};
+    cudaEvent_t chunk[RT_MAX_CHUNKS] = {};
+    bool made = false;
+};
+RoundTrip g_rt;
+
+int roundtrip_make() {
+    if (g_rt.made) return 0;
+    for (int i = 0; i < 2; i++) {
+        if (int rc = check_cuda(cudaStreamCreateWithFlags(&g_rt.down[i], cudaStreamNonBlocking),
+                                "cudaStreamCreate")) return rc;
+        if (int rc = check_cuda(cudaStreamCreateWithFlags(&g_rt.up[i], cudaStreamNonBlocking),
+                                "cudaStreamCreate")) return rc;
+        if (int rc = check_cuda(cudaEventCreateWithFlags(&g_rt.done[i], cudaEventDisableTiming),
+                                "cudaEventCreate")) return rc;
+    }
+    if (int rc = check_cuda(cudaEventCreateWithFlags(&g_rt.ready, cudaEventDisableTiming),
+                            "cudaEventCreate")) return rc;
+    for (int k = 0; k < RT_MAX_CHUNKS; k++)
+        if (int rc = check_cuda(cudaEventCreateWithFlags(&g_rt.chunk[k], cudaEventDisableTiming),
+                                "cudaEventCreate")) return rc;
+    g_rt.made = true;
+    return 0;
+}
+}  // namespace
+
+namespace {
+
+// Copy by the SMs: 16-byte loads and stores over a grid-stride loop (the
+// tail, under 16 bytes, byte by byte); src or dst may be page-locked host
+// memory mapped into the device's address space
+__global__ void sm_copy_kernel(const uint4 *__restrict__ src, uint4 *__restrict__ dst, size_t n16,
+                               const unsigned char *__restrict__ src_tail,
+                               unsigned char *__restrict__ dst_tail, int ntail) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += stride)
+        dst[i] = src[i];
+    if (blockIdx.x == 0 && (int)threadIdx.x < ntail) dst_tail[threadIdx.x] = src_tail[threadIdx.x];
+}
+
+int sm_copy(const void *src, void *dst, size_t len, cudaStream_t st) {
+    if (((uintptr_t)src | (uintptr_t)dst) & 15)
+        return set_error(B200_ERR_ARG, "memcpy_roundtrip: kernel copies need 16-byte alignment");
+    const size_t n16 = len / 16;
+    const int ntail = (int)(len - 16 * n16);
+    int nsm = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    size_t blocks = (n16 + 255) / 256;
+    const size_t cap = (size_t)(nsm > 0 ? nsm : 1) * 4;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    sm_copy_kernel<<<(unsigned)blocks, 256, 0, st>>>(
+        (const uint4 *)src, (uint4 *)dst, n16, (const unsigned char *)src + 16 * n16,
+        (unsigned char *)dst + 16 * n16, ntail);
+    return check_cuda(cudaGetLastError(), "sm_copy");
+}
+
+}  // namespace
+
+int b200_memcpy_roundtrip(void *host, const void *dsrc, void *ddst, size_t nbytes,
+                          int nchunks, int nstreams, void *stream) {
+    if (!host || !dsrc) return set_error(B200_ERR_ARG, "null pointer");
+    // nstreams < 0: the copies run as kernels on |nstreams| streams per
+    // direction, reading and writing the host buffer through its device
+    // mapping (which must exist: page-locked memory of this context)
+    const bool by_sm = nstreams < 0;
+    if (by_sm) nstreams = -nstreams;
+    if (nchunks < 1 || nchunks > RT_MAX_CHUNKS || nstreams < 1 || nstreams > 2)
+        return set_error(B200_ERR_ARG, "memcpy_roundtrip: 1-%d chunks on 1-2 streams",
+                         RT_MAX_CHUNKS);
+    if (int rc = roundtrip_make()) return rc;
+    void *hdev = host;
+    if (by_sm &&
+        check_cuda(cudaHostGetDevicePointer(&hdev, host, 0), "cudaHostGetDevicePointer"))
+        return set_error(B200_ERR_ARG, "memcpy_roundtrip: host buffer not mapped for the device");
+    cudaStream_t st = (cudaStream_t)stream;
+    // Both directions start after the work queued on `stream` (which
+    // produced dsrc and may still read ddst)
+    if (int rc = check_cuda(cudaEventRecord(g_rt.ready, st), "cudaEventRecord")) return rc;
+    for (int i = 0; i < nstreams; i++) {
+        if (int rc = check_cuda(cudaStreamWaitEvent(g_rt.down[i], g_rt.ready, 0), "wait")) return rc;
+        if (int rc = check_cuda(cudaStreamWaitEvent(g_rt.up[i], g_rt.ready, 0), "wait")) return rc;
+    }
+    // Chunk k goes down on stream k % nstreams and, once it has landed,
+    // back up on the matching up stream
+    const size_t per = ((nbytes + nchunks - 1) / nchunks + 255) / 256 * 256;
+    int k = 0;
+    for (size_t off = 0; off < nbytes; off += per, k++) {
+        const size_t len = nbytes - off < per ? nbytes - off : per;
+        const int i = k % nstreams;
+        char *h = (char *)host + off;
+        char *hd = (char *)hdev + off;
+        if (by_sm) {
+            if (int rc = sm_copy((const char *)dsrc + off, hd, len, g_rt.down[i])) return rc;
+        } else if (int rc = check_cuda(cudaMemcpyAsync(h, (const char *)dsrc + off, len,
+                                                       cudaMemcpyDeviceToHost, g_rt.down[i]),
+                                       "memcpy DtoH")) return rc;
+        if (!ddst) continue;
+        if (int rc = check_cuda(cudaEventRecord(g_rt.chunk[k], g_rt.down[i]), "cudaEventRecord"))
+            return rc;
+        if (int rc = check_cuda(cudaStreamWaitEvent(g_rt.up[i], g_rt.chunk[k], 0), "wait"))
+            return rc;
+        if (by_sm) {
+            if (int rc = sm_copy(hd, (char *)ddst + off, len, g_rt.up[i])) return rc;
+        } else if (int rc = check_cuda(cudaMemcpyAsync((char *)ddst + off, h, len,
+                                                       cudaMemcpyHostToDevice, g_rt.up[i]),
+                                       "memcpy HtoD")) return rc;
+    }
+    // `stream` continues once every chunk is back (or, without ddst, down)
+    for (int i = 0; i < nstreams; i++) {
+        cudaStream_t last = ddst ? g_rt.up[i] : g_rt.down[i];
+        if (int rc = check_cuda(cudaEventRecord(g_rt.done[i], last), "cudaEventRecord")) return rc;
+        if (int rc = check_cuda(cudaStreamWaitEvent(st, g_rt.done[i], 0), "wait")) return rc;
+    }
+    return 0;
 }
 
 int b200_stream_create(void **stream) {

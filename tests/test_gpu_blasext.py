@@ -98,3 +98,46 @@ def test_reduction_other_forms_refused(be):
     be.commit()
     with pytest.raises(NotImplementedError):
         be.kernel('reduction', 'sum', ['x*x'], {'x': X})
+
+
+@pytest.mark.parametrize('chunks,streams', [(1, 1), (16, 1), (7, 2),
+                                            (16, -1), (5, -2)])
+def test_memcpy_roundtrip(be, chunks, streams):
+    """The pipelined host round trip of the end-to-end loop: a device array
+    goes down to page-locked host memory and back into another (or the
+    same) device array, by the copy engines or by kernels through the
+    buffer's device mapping; an odd byte count exercises the last piece
+    and the kernels' byte tail."""
+    import ctypes as C
+    rng = np.random.default_rng(chunks + 10*streams)
+    x = rng.normal(size=(8, 5, 77))
+    a = be.matrix(x.shape, x, tags={'align'})
+    b = be.matrix(x.shape, tags={'align'})
+    be.commit()
+    lib, st = be.lib, be.stream
+    nbytes = a.nbytes - 3
+    h = C.c_void_p()
+    lib.host_alloc(C.byref(h), a.nbytes)
+    try:
+        lib.memcpy_roundtrip(h.value, a.data, b.data, nbytes, chunks, streams,
+                             st)
+        be.wait()
+        got = np.frombuffer((C.c_char*nbytes).from_address(h.value),
+                            dtype=np.uint8)
+        want = np.empty(a.nbytes, dtype=np.uint8)
+        lib.memcpy_dtoh(want.ctypes.data, a.data, a.nbytes, st)
+        back = np.empty(a.nbytes, dtype=np.uint8)
+        lib.memcpy_dtoh(back.ctypes.data, b.data, a.nbytes, st)
+        be.wait()
+        np.testing.assert_array_equal(got, want[:nbytes])
+        np.testing.assert_array_equal(back[:nbytes], want[:nbytes])
+        assert not back[nbytes:].any()
+        # In place, down only
+        lib.memcpy_roundtrip(h.value, a.data, None, a.nbytes, chunks, streams,
+                             st)
+        lib.memcpy_roundtrip(h.value, a.data, a.data, a.nbytes, chunks,
+                             streams, st)
+        be.wait()
+        np.testing.assert_array_equal(a.get(), x)
+    finally:
+        lib.host_free(h.value)
