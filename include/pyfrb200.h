@@ -306,6 +306,22 @@ int b200_tflux_ns_f32(int ndims, int nupts, int64_t neles, int linear, const b20
                       int64_t ldg, const float *smats, int64_t lds, const float *rcpdjac,
                       int64_t ldr, const float *verts, int64_t ldv, const float *upts,
                       int64_t ldup, void *stream);
+/* The same, leaving gradu in reference space (the transformed gradient is
+ * used at the points and not stored): for affine elements whose interface
+ * kernels transform the face gradients themselves
+ * (b200_intcflux_ns_refgrad_*).  No counterpart in the reference, which
+ * always stores the transformed gradient. */
+int b200_tflux_ns_refgrad_f64(int ndims, int nupts, int64_t neles, int linear,
+                              const b200_gas_t *gas, const double *u, int64_t ldu, double *f,
+                              int64_t ldf, double *gradu, int64_t ldg, const double *smats,
+                              int64_t lds, const double *rcpdjac, int64_t ldr,
+                              const double *verts, int64_t ldv, const double *upts,
+                              int64_t ldup, void *stream);
+int b200_tflux_ns_refgrad_f32(int ndims, int nupts, int64_t neles, int linear,
+                              const b200_gas_t *gas, const float *u, int64_t ldu, float *f,
+                              int64_t ldf, float *gradu, int64_t ldg, const float *smats,
+                              int64_t lds, const float *rcpdjac, int64_t ldr, const float *verts,
+                              int64_t ldv, const float *upts, int64_t ldup, void *stream);
 
 /* Common normal flux at boundary flux points, written over the interior
  * state in the flux-point field (view ul, n points; nl: scaled normals,
@@ -587,6 +603,26 @@ int b200_intcflux_ns_f32(int ndims, int64_t n, int rsolver, const b200_gas_t *ga
                          const void *gl_rstr, const float *gr_base, const void *gr_map,
                          const void *gr_rstr, int ix64, const float *nl, int64_t ldn, int nl_unit,
                          void *stream);
+/* The same with face gradients in reference space, transformed here with
+ * the metric terms of affine elements: emet holds (ndims*ndims + 1) rows of
+ * one column per element (S[i][j] in row i*ndims + j, 1/|J| in the last
+ * row; leading dimension ldm), eidx_l/eidx_r the column of each pair's left
+ * and right element (the side that beta = +-1/2 does not read may be
+ * NULL).  Pairs with b200_tflux_ns_refgrad_*. */
+int b200_intcflux_ns_refgrad_f64(int ndims, int64_t n, int rsolver, const b200_gas_t *gas,
+                                 double beta, double tau, double *ul_base, const void *ul_map,
+                                 double *ur_base, const void *ur_map, const double *gl_base,
+                                 const void *gl_map, const void *gl_rstr, const double *gr_base,
+                                 const void *gr_map, const void *gr_rstr, int ix64,
+                                 const double *nl, int64_t ldn, int nl_unit, const double *emet,
+                                 int64_t ldm, const int *eidx_l, const int *eidx_r, void *stream);
+int b200_intcflux_ns_refgrad_f32(int ndims, int64_t n, int rsolver, const b200_gas_t *gas,
+                                 double beta, double tau, float *ul_base, const void *ul_map,
+                                 float *ur_base, const void *ur_map, const float *gl_base,
+                                 const void *gl_map, const void *gl_rstr, const float *gr_base,
+                                 const void *gr_map, const void *gr_rstr, int ix64,
+                                 const float *nl, int64_t ldn, int nl_unit, const float *emet,
+                                 int64_t ldm, const int *eidx_l, const int *eidx_r, void *stream);
 
 /* LDG common solution; pyfr/solvers/navstokes/kernels/intconu.mako:4-19. */
 int b200_intconu_f64(int nvars, int64_t n, double beta, const double *lin_base,

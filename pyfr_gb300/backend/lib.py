@@ -130,6 +130,12 @@ def _sig_pointwise(fp):
                        vp, vp, vp, vp, i32, vp, i64, vp],
         'bccflux_ns_av': [i32, i64, i32, C.POINTER(Gas), f64, C.POINTER(BC),
                           vp, vp, vp, vp, vp, i32, vp, i64, vp, vp, vp],
+        'tflux_ns_refgrad': [i32, i32, i64, i32, C.POINTER(Gas), vp, i64, vp,
+                             i64, vp, i64, vp, i64, vp, i64, vp, i64, vp, i64,
+                             vp],
+        'intcflux_ns_refgrad': [i32, i64, i32, C.POINTER(Gas), f64, f64, vp,
+                                vp, vp, vp, vp, vp, vp, vp, vp, vp, i32, vp,
+                                i64, i32, vp, i64, vp, vp, vp],
         'tflux_ns_av': [i32, i32, i64, i32, C.POINTER(Gas), vp, i64, vp, i64,
                         vp, i64, vp, i64, vp, i64, vp, i64, vp, i64, vp, i64,
                         vp],

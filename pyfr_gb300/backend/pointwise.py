@@ -228,13 +228,15 @@ class PointwiseKernelProvider:
 
     def _tflux_ns(self, tplargs, dims, extrns, u, f, gradu=None, smats=None,
                   rcpdjac=None, verts=None, upts=None, artvisc=None,
-                  artvisc_vtx=None):
+                  artvisc_vtx=None, gradwb=True):
         """``artvisc``: the artificial viscosity at the solution points
         (nupts, neles), when shock capturing is 'artificial-viscosity'
         (the vertex interpolation of pyfr/solvers/navstokes/kernels/
         tflux.mako:39-43, done by the avfill kernel).  ``artvisc_vtx`` is
         the argument of the reference's own elements (a view of the vertex
-        values, None without artificial viscosity)."""
+        values, None without artificial viscosity).  ``gradwb`` False
+        leaves gradu in reference space (affine elements whose interface
+        kernels transform the face gradients, ``facemet`` of intcflux)."""
         if artvisc_vtx is not None:
             raise NotImplementedError(
                 'Artificial viscosity from vertex views: the b200 systems '
@@ -257,6 +259,9 @@ class PointwiseKernelProvider:
         fp, fl = _mat(f)
         gp, gl = _mat(gradu)
 
+        if not gradwb and (gradu is None or artvisc is not None):
+            raise ValueError('Leaving the gradient untransformed needs the '
+                             'fused flux without artificial viscosity')
         if artvisc is not None:
             fn = self._fn('tflux_ns_av')
             ap, al = _mat(artvisc)
@@ -265,7 +270,7 @@ class PointwiseKernelProvider:
                 fn(nd, nupts, neles, lin, C.byref(gas), up, ul, fp, fl, gp, gl,
                    sp, sl, rp, rl, vp, vl, upp, upl, ap, al, stream)
         else:
-            fn = self._fn('tflux_ns')
+            fn = self._fn('tflux_ns' if gradwb else 'tflux_ns_refgrad')
 
             def run(stream):
                 fn(nd, nupts, neles, lin, C.byref(gas), up, ul, fp, fl, gp, gl,
@@ -458,10 +463,18 @@ class PointwiseKernelProvider:
                                 dims=dims, ul=ul, ur=ur, nl=nl))
 
     def _intcflux_ns(self, tplargs, dims, extrns, ul, ur, gradul, gradur, nl,
-                     artvisc=None):
+                     artvisc=None, facemet=None):
+        """``facemet``: (metric matrix, left element columns, right element
+        columns) when the face gradients are in reference space (the
+        elements' flux kernel left them untransformed): the metric matrix
+        holds S[i][j] of each affine element in row i*ndims + j and 1/|J|
+        in the last row."""
         if (tplargs.get('shock_capturing') == 'artificial-viscosity') != \
                 (artvisc is not None):
             raise ValueError('Artificial viscosity needs its field')
+        if facemet is not None and artvisc is not None:
+            raise ValueError('Face metrics and artificial viscosity do not '
+                             'combine')
 
         (n,) = dims
         c = tplargs['c']
@@ -488,12 +501,21 @@ class PointwiseKernelProvider:
                 fn(nd, n, rs, C.byref(gas), beta, tau, lb, lm, rb, rm, glb,
                    glm, glr, grb, grm, grr, ix64, np_, nlp, nlu, ab, am,
                    stream)
+        elif facemet is not None:
+            fn = self._fn('intcflux_ns_refgrad')
+            fm, fl_, fr_ = facemet
+            fmp, fml = _mat(fm)
+
+            def run(stream):
+                fn(nd, n, rs, C.byref(gas), beta, tau, lb, lm, rb, rm, glb,
+                   glm, glr, grb, grm, grr, ix64, np_, nlp, nlu, fmp, fml,
+                   fl_.data, fr_.data, stream)
         else:
             def run(stream):
                 fn(nd, n, rs, C.byref(gas), beta, tau, lb, lm, rb, rm, glb,
                    glm, glr, grb, grm, grr, ix64, np_, nlp, nlu, stream)
 
-        return Kernel(run, mats=[nl, nlm],
+        return Kernel(run, mats=[nl, nlm] + list(facemet or ()),
                       views=[ul, ur, gradul, gradur] +
                       ([artvisc] if artvisc is not None else []),
                       misc=[gas], name='intcflux',

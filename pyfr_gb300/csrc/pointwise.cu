@@ -162,15 +162,17 @@ template <int ND, typename T>
 __global__ void __launch_bounds__(PW_BLOCK)
 tflux_ns_kernel(int nupts, int64_t neles, b200::GasK<T> gas, const T *__restrict__ u, int64_t ldu,
                 T *__restrict__ f, int64_t ldf, T *__restrict__ gradu, int64_t ldg,
-                ElemGeom<T> geo, const T *__restrict__ av, int64_t lda) {
+                ElemGeom<T> geo, const T *__restrict__ av, int64_t lda, int gradwb) {
     constexpr int NV = ND + 2;
     const int64_t e = (int64_t)blockIdx.x * PW_BLOCK + threadIdx.x;
     const int upt = blockIdx.y;
     if (e >= neles) return;
 
     // Fused form: the corrected reference gradient is in gradu and is
-    // transformed here (and written back); otherwise (flux anti-aliasing)
-    // the physical gradient at the point is in f, which the flux replaces
+    // transformed here (and written back, unless gradwb is 0: then the
+    // interface kernel transforms the face values); otherwise (flux
+    // anti-aliasing) the physical gradient at the point is in f, which the
+    // flux replaces
     const bool fused = gradu != nullptr;
     T s[ND][ND], rcp;
     elem_metrics<ND, T>(geo, nupts, upt, e, s, rcp, fused);
@@ -190,7 +192,7 @@ tflux_ns_kernel(int nupts, int64_t neles, b200::GasK<T> gas, const T *__restrict
 #pragma unroll
                 for (int k = 0; k < ND; k++) acc += s[k][i] * tg[k][j];
                 gr[i][j] = rcp * acc;
-                gradu[(int64_t)(i * nupts + upt) * ldg + soa_off(e, j, NV)] = gr[i][j];
+                if (gradwb) gradu[(int64_t)(i * nupts + upt) * ldg + soa_off(e, j, NV)] = gr[i][j];
             }
     } else {
 #pragma unroll
@@ -460,11 +462,52 @@ intcflux_euler_kernel(int64_t n, T gamma, T p_min, ScalView<T> vl, ScalView<T> v
 // (FP32: 64 registers, so that eight blocks share an SM -- the kernel waits
 // on its gathers, and occupancy hides them better than the spill-free 80
 // registers do)
-template <int RS, int ND, typename T>
+// Per-element metric terms of affine elements for the interface kernels
+// that take face gradients in reference space (their elements' flux kernel
+// left the solution-point gradient untransformed): rows i*ND + j hold
+// S[i][j] and row ND*ND holds 1/|J| of element k in column k; il/ir give
+// the column of each pair's left and right element.
+template <typename T>
+struct FaceMetrics {
+    const T *m;
+    int64_t ld;
+    const int *il, *ir;
+};
+
+// grad <- (1/|J|) S^T grad at a face point of element column k
+template <int ND, int NV, typename T>
+__device__ __forceinline__ void face_grad_to_phys(const FaceMetrics<T> &fm, int k,
+                                                  T gg[ND][NV]) {
+    const T *m = fm.m + k;
+    const T rcp = m[(int64_t)(ND * ND) * fm.ld];
+    // One output component at a time over every variable; the metric terms
+    // are re-read rather than held (L1 hits: the pairs of one face share
+    // their element), which keeps the kernel within its register bound
+    T out[ND][NV];
+#pragma unroll
+    for (int i = 0; i < ND; i++) {
+        T c[ND];
+#pragma unroll
+        for (int q = 0; q < ND; q++) c[q] = rcp * m[(int64_t)(q * ND + i) * fm.ld];
+#pragma unroll
+        for (int v = 0; v < NV; v++) {
+            T acc = 0;
+#pragma unroll
+            for (int q = 0; q < ND; q++) acc += c[q] * gg[q][v];
+            out[i][v] = acc;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < ND; i++)
+#pragma unroll
+        for (int v = 0; v < NV; v++) gg[i][v] = out[i][v];
+}
+
+template <int RS, int ND, typename T, bool FM>
 __global__ void __launch_bounds__(PW_BLOCK, sizeof(T) == 4 ? 8 : 1)
 intcflux_ns_kernel(int64_t n, b200::GasK<T> gas, T beta, T tau, ScalView<T> vl, ScalView<T> vr,
                    VectView<T> gl, VectView<T> gr, int ix64, const T *__restrict__ nl,
-                   int64_t ldn, int nl_unit, ScalView<T> va) {
+                   int64_t ldn, int nl_unit, ScalView<T> va, FaceMetrics<T> fm) {
     constexpr int NV = ND + 2;
     const int64_t i = (int64_t)blockIdx.x * PW_BLOCK + threadIdx.x;
     if (i >= n) return;
@@ -511,6 +554,7 @@ intcflux_ns_kernel(int64_t n, b200::GasK<T> gas, T beta, T tau, ScalView<T> vl, 
         for (int d = 0; d < ND; d++)
 #pragma unroll
             for (int v = 0; v < NV; v++) gg[d][v] = g[d * rstr + v * B200_SOASZ];
+        if (FM) face_grad_to_phys<ND, NV, T>(fm, fm.il[i], gg);
         if (gas.shifted) {
             T gu[ND][NV];
             b200::unshift_grad<ND, T>(gg, gu, gas);
@@ -536,6 +580,7 @@ intcflux_ns_kernel(int64_t n, b200::GasK<T> gas, T beta, T tau, ScalView<T> vl, 
         for (int d = 0; d < ND; d++)
 #pragma unroll
             for (int v = 0; v < NV; v++) gg[d][v] = g[d * rstr + v * B200_SOASZ];
+        if (FM) face_grad_to_phys<ND, NV, T>(fm, fm.ir[i], gg);
         if (gas.shifted) {
             T gu[ND][NV];
             b200::unshift_grad<ND, T>(gg, gu, gas);
@@ -668,9 +713,11 @@ template <typename T>
 int tflux_ns(int ndims, int nupts, int64_t neles, int linear, const b200_gas_t *gas,
              const T *u, int64_t ldu, T *f, int64_t ldf, T *gradu, int64_t ldg, const T *smats,
              int64_t lds, const T *rcpdjac, int64_t ldr, const T *verts, int64_t ldv,
-             const T *upts, int64_t ldup, const T *av, int64_t lda, cudaStream_t st) {
+             const T *upts, int64_t ldup, const T *av, int64_t lda, int gradwb, cudaStream_t st) {
     if (neles <= 0 || nupts <= 0) return B200_OK;
     if (!gas) return b200::set_error(B200_ERR_ARG, "tflux_ns: null gas constants");
+    if (!gradwb && !gradu)
+        return b200::set_error(B200_ERR_ARG, "tflux_ns: a reference gradient to leave needs gradu");
     if (av && reinterpret_cast<const Gas *>(gas)->shifted)
         return b200::set_error(B200_ERR_UNSUPPORTED,
                                "tflux_ns: artificial viscosity takes unshifted states");
@@ -680,9 +727,9 @@ int tflux_ns(int ndims, int nupts, int64_t neles, int linear, const b200_gas_t *
     const auto g = b200::gas_consts<T>(*reinterpret_cast<const Gas *>(gas));
     dim3 grid(b200::ceil_div(neles, PW_BLOCK), nupts);
     if (ndims == 2)
-        tflux_ns_kernel<2, T><<<grid, PW_BLOCK, 0, st>>>(nupts, neles, g, u, ldu, f, ldf, gradu, ldg, geo, av, lda);
+        tflux_ns_kernel<2, T><<<grid, PW_BLOCK, 0, st>>>(nupts, neles, g, u, ldu, f, ldf, gradu, ldg, geo, av, lda, gradwb);
     else if (ndims == 3)
-        tflux_ns_kernel<3, T><<<grid, PW_BLOCK, 0, st>>>(nupts, neles, g, u, ldu, f, ldf, gradu, ldg, geo, av, lda);
+        tflux_ns_kernel<3, T><<<grid, PW_BLOCK, 0, st>>>(nupts, neles, g, u, ldu, f, ldf, gradu, ldg, geo, av, lda, gradwb);
     else
         return b200::set_error(B200_ERR_ARG, "tflux_ns: ndims must be 2 or 3");
     B200_CHECK_LAUNCH("tflux_ns");
@@ -734,9 +781,12 @@ int intcflux_ns(int ndims, int64_t n, int rsolver, const b200_gas_t *gas, double
                 double tau, T *ul_base, const void *ul_map, T *ur_base, const void *ur_map,
                 const T *gl_base, const void *gl_map, const void *gl_rstr, const T *gr_base,
                 const void *gr_map, const void *gr_rstr, int ix64, const T *nl, int64_t ldn,
-                int nl_unit, const T *av_base, const void *av_map, cudaStream_t st) {
+                int nl_unit, const T *av_base, const void *av_map, FaceMetrics<T> fm,
+                cudaStream_t st) {
     if (n <= 0) return B200_OK;
     if (!gas) return b200::set_error(B200_ERR_ARG, "intcflux_ns: null gas constants");
+    if (fm.m && ((beta != -0.5 && !fm.il) || (beta != 0.5 && !fm.ir) || fm.ld <= 0))
+        return b200::set_error(B200_ERR_ARG, "intcflux_ns: face metrics need the element columns");
     if (av_base && (!av_map || reinterpret_cast<const Gas *>(gas)->shifted))
         return b200::set_error(B200_ERR_ARG,
                                "intcflux_ns: artificial viscosity needs a view and unshifted states");
@@ -753,9 +803,11 @@ int intcflux_ns(int ndims, int64_t n, int rsolver, const b200_gas_t *gas, double
     const bool ok = b200::with_rsolver(rsolver, [&](auto rsc) {
         constexpr int RS = decltype(rsc)::value;
         if (ndims == 2)
-            intcflux_ns_kernel<RS, 2, T><<<grid, PW_BLOCK, 0, st>>>(n, g, (T)beta, (T)tau, l, r, gl, gr, ix64, nl, ldn, nl_unit, va);
+            intcflux_ns_kernel<RS, 2, T, false><<<grid, PW_BLOCK, 0, st>>>(n, g, (T)beta, (T)tau, l, r, gl, gr, ix64, nl, ldn, nl_unit, va, fm);
+        else if (!fm.m)
+            intcflux_ns_kernel<RS, 3, T, false><<<grid, PW_BLOCK, 0, st>>>(n, g, (T)beta, (T)tau, l, r, gl, gr, ix64, nl, ldn, nl_unit, va, fm);
         else
-            intcflux_ns_kernel<RS, 3, T><<<grid, PW_BLOCK, 0, st>>>(n, g, (T)beta, (T)tau, l, r, gl, gr, ix64, nl, ldn, nl_unit, va);
+            intcflux_ns_kernel<RS, 3, T, true><<<grid, PW_BLOCK, 0, st>>>(n, g, (T)beta, (T)tau, l, r, gl, gr, ix64, nl, ldn, nl_unit, va, fm);
     });
     if (!ok) return b200::set_error(B200_ERR_ARG, "intcflux: unknown Riemann solver %d", rsolver);
     B200_CHECK_LAUNCH("intcflux_ns");
@@ -802,7 +854,7 @@ int b200_tflux_ns_f64(int ndims, int nupts, int64_t neles, int linear, const b20
                       int64_t ldr, const double *verts, int64_t ldv, const double *upts,
                       int64_t ldup, void *stream) {
     return tflux_ns<double>(ndims, nupts, neles, linear, gas, u, ldu, f, ldf, gradu, ldg, smats,
-                            lds, rcpdjac, ldr, verts, ldv, upts, ldup, nullptr, 0,
+                            lds, rcpdjac, ldr, verts, ldv, upts, ldup, nullptr, 0, 1,
                             (cudaStream_t)stream);
 }
 
@@ -813,7 +865,7 @@ int b200_tflux_ns_av_f64(int ndims, int nupts, int64_t neles, int linear, const 
                          int64_t ldup, const double *av, int64_t lda, void *stream) {
     if (!av) return b200::set_error(B200_ERR_ARG, "tflux_ns_av: null viscosity");
     return tflux_ns<double>(ndims, nupts, neles, linear, gas, u, ldu, f, ldf, gradu, ldg, smats,
-                        lds, rcpdjac, ldr, verts, ldv, upts, ldup, av, lda, (cudaStream_t)stream);
+                        lds, rcpdjac, ldr, verts, ldv, upts, ldup, av, lda, 1, (cudaStream_t)stream);
 }
 
 int b200_tflux_ns_f32(int ndims, int nupts, int64_t neles, int linear, const b200_gas_t *gas,
@@ -822,8 +874,29 @@ int b200_tflux_ns_f32(int ndims, int nupts, int64_t neles, int linear, const b20
                       int64_t ldr, const float *verts, int64_t ldv, const float *upts,
                       int64_t ldup, void *stream) {
     return tflux_ns<float>(ndims, nupts, neles, linear, gas, u, ldu, f, ldf, gradu, ldg, smats,
-                           lds, rcpdjac, ldr, verts, ldv, upts, ldup, nullptr, 0,
+                           lds, rcpdjac, ldr, verts, ldv, upts, ldup, nullptr, 0, 1,
                             (cudaStream_t)stream);
+}
+
+int b200_tflux_ns_refgrad_f64(int ndims, int nupts, int64_t neles, int linear,
+                              const b200_gas_t *gas, const double *u, int64_t ldu, double *f,
+                              int64_t ldf, double *gradu, int64_t ldg, const double *smats,
+                              int64_t lds, const double *rcpdjac, int64_t ldr,
+                              const double *verts, int64_t ldv, const double *upts,
+                              int64_t ldup, void *stream) {
+    return tflux_ns<double>(ndims, nupts, neles, linear, gas, u, ldu, f, ldf, gradu, ldg, smats,
+                            lds, rcpdjac, ldr, verts, ldv, upts, ldup, nullptr, 0, 0,
+                            (cudaStream_t)stream);
+}
+
+int b200_tflux_ns_refgrad_f32(int ndims, int nupts, int64_t neles, int linear,
+                              const b200_gas_t *gas, const float *u, int64_t ldu, float *f,
+                              int64_t ldf, float *gradu, int64_t ldg, const float *smats,
+                              int64_t lds, const float *rcpdjac, int64_t ldr, const float *verts,
+                              int64_t ldv, const float *upts, int64_t ldup, void *stream) {
+    return tflux_ns<float>(ndims, nupts, neles, linear, gas, u, ldu, f, ldf, gradu, ldg, smats,
+                           lds, rcpdjac, ldr, verts, ldv, upts, ldup, nullptr, 0, 0,
+                           (cudaStream_t)stream);
 }
 
 int b200_tflux_ns_av_f32(int ndims, int nupts, int64_t neles, int linear, const b200_gas_t *gas,
@@ -833,7 +906,7 @@ int b200_tflux_ns_av_f32(int ndims, int nupts, int64_t neles, int linear, const 
                          int64_t ldup, const float *av, int64_t lda, void *stream) {
     if (!av) return b200::set_error(B200_ERR_ARG, "tflux_ns_av: null viscosity");
     return tflux_ns<float>(ndims, nupts, neles, linear, gas, u, ldu, f, ldf, gradu, ldg, smats,
-                        lds, rcpdjac, ldr, verts, ldv, upts, ldup, av, lda, (cudaStream_t)stream);
+                        lds, rcpdjac, ldr, verts, ldv, upts, ldup, av, lda, 1, (cudaStream_t)stream);
 }
 
 int b200_gradcoru_f64(int ndims, int nupts, int64_t neles, int linear, double *gradu,
@@ -920,7 +993,8 @@ int b200_intcflux_ns_f64(int ndims, int64_t n, int rsolver, const b200_gas_t *ga
                          void *stream) {
     return intcflux_ns<double>(ndims, n, rsolver, gas, beta, tau, ul_base, ul_map, ur_base,
                                ur_map, gl_base, gl_map, gl_rstr, gr_base, gr_map, gr_rstr, ix64,
-                               nl, ldn, nl_unit, nullptr, nullptr, (cudaStream_t)stream);
+                               nl, ldn, nl_unit, nullptr, nullptr, FaceMetrics<double>{},
+                               (cudaStream_t)stream);
 }
 
 int b200_intcflux_ns_av_f64(int ndims, int64_t n, int rsolver, const b200_gas_t *gas,
@@ -932,7 +1006,7 @@ int b200_intcflux_ns_av_f64(int ndims, int64_t n, int rsolver, const b200_gas_t 
     if (!av_base) return b200::set_error(B200_ERR_ARG, "intcflux_ns_av: null viscosity");
     return intcflux_ns<double>(ndims, n, rsolver, gas, beta, tau, ul_base, ul_map, ur_base, ur_map,
                            gl_base, gl_map, gl_rstr, gr_base, gr_map, gr_rstr, ix64, nl, ldn, nl_unit,
-                           av_base, av_map, (cudaStream_t)stream);
+                           av_base, av_map, FaceMetrics<double>{}, (cudaStream_t)stream);
 }
 
 int b200_intcflux_ns_f32(int ndims, int64_t n, int rsolver, const b200_gas_t *gas, double beta,
@@ -943,7 +1017,38 @@ int b200_intcflux_ns_f32(int ndims, int64_t n, int rsolver, const b200_gas_t *ga
                          void *stream) {
     return intcflux_ns<float>(ndims, n, rsolver, gas, beta, tau, ul_base, ul_map, ur_base,
                               ur_map, gl_base, gl_map, gl_rstr, gr_base, gr_map, gr_rstr, ix64,
-                              nl, ldn, nl_unit, nullptr, nullptr, (cudaStream_t)stream);
+                              nl, ldn, nl_unit, nullptr, nullptr, FaceMetrics<float>{},
+                              (cudaStream_t)stream);
+}
+
+int b200_intcflux_ns_refgrad_f64(int ndims, int64_t n, int rsolver, const b200_gas_t *gas,
+                                 double beta, double tau, double *ul_base, const void *ul_map,
+                                 double *ur_base, const void *ur_map, const double *gl_base,
+                                 const void *gl_map, const void *gl_rstr, const double *gr_base,
+                                 const void *gr_map, const void *gr_rstr, int ix64,
+                                 const double *nl, int64_t ldn, int nl_unit, const double *emet,
+                                 int64_t ldm, const int *eidx_l, const int *eidx_r, void *stream) {
+    if (!emet) return b200::set_error(B200_ERR_ARG, "intcflux_ns_refgrad: null metrics");
+    return intcflux_ns<double>(ndims, n, rsolver, gas, beta, tau, ul_base, ul_map, ur_base, ur_map,
+                               gl_base, gl_map, gl_rstr, gr_base, gr_map, gr_rstr, ix64, nl, ldn,
+                               nl_unit, nullptr, nullptr,
+                               FaceMetrics<double>{emet, ldm, eidx_l, eidx_r},
+                               (cudaStream_t)stream);
+}
+
+int b200_intcflux_ns_refgrad_f32(int ndims, int64_t n, int rsolver, const b200_gas_t *gas,
+                                 double beta, double tau, float *ul_base, const void *ul_map,
+                                 float *ur_base, const void *ur_map, const float *gl_base,
+                                 const void *gl_map, const void *gl_rstr, const float *gr_base,
+                                 const void *gr_map, const void *gr_rstr, int ix64,
+                                 const float *nl, int64_t ldn, int nl_unit, const float *emet,
+                                 int64_t ldm, const int *eidx_l, const int *eidx_r, void *stream) {
+    if (!emet) return b200::set_error(B200_ERR_ARG, "intcflux_ns_refgrad: null metrics");
+    return intcflux_ns<float>(ndims, n, rsolver, gas, beta, tau, ul_base, ul_map, ur_base, ur_map,
+                              gl_base, gl_map, gl_rstr, gr_base, gr_map, gr_rstr, ix64, nl, ldn,
+                              nl_unit, nullptr, nullptr,
+                              FaceMetrics<float>{emet, ldm, eidx_l, eidx_r},
+                              (cudaStream_t)stream);
 }
 
 int b200_intcflux_ns_av_f32(int ndims, int64_t n, int rsolver, const b200_gas_t *gas,
@@ -955,7 +1060,7 @@ int b200_intcflux_ns_av_f32(int ndims, int64_t n, int rsolver, const b200_gas_t 
     if (!av_base) return b200::set_error(B200_ERR_ARG, "intcflux_ns_av: null viscosity");
     return intcflux_ns<float>(ndims, n, rsolver, gas, beta, tau, ul_base, ul_map, ur_base, ur_map,
                            gl_base, gl_map, gl_rstr, gr_base, gr_map, gr_rstr, ix64, nl, ldn, nl_unit,
-                           av_base, av_map, (cudaStream_t)stream);
+                           av_base, av_map, FaceMetrics<float>{}, (cudaStream_t)stream);
 }
 
 int b200_intconu_f64(int nvars, int64_t n, double beta, const double *lin_base,

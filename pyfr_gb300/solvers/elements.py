@@ -582,6 +582,30 @@ class NavierStokesElements(_WavespeedMixin, _DivergenceMixin, FluidElements,
                            BaseElements):
     _scratch_bufs = {'scal_fpts', 'vect_fpts', 'vect_upts', 'grad_upts'}
 
+    # Set by the system: the flux kernel stores the transformed gradient
+    # (False: it leaves it in reference space, and the interface kernels
+    # transform the face gradients with the affine elements' metrics)
+    grad_writeback = True
+    # Set by the system with the face metrics: this type's first column in
+    # the interface kernels' metric matrix
+    face_metric_col = 0
+
+    def affine_metrics(self):
+        """(S (ndims, ndims, neles) and 1/|J| (neles,)) of the elements
+        when every one is linear and affine (the same metric terms at every
+        point), else None."""
+        from pyfr_gb300.backend.pointwise import affine, linear_metrics
+        if self.linoff:
+            return None
+        sm, rj = linear_metrics(self.eles.transpose(0, 2, 1), self.basis.upts)
+        if not affine(sm):
+            return None
+        return sm[:, 0], rj[0]
+
+    def get_eidx_for_inters(self, eidxs, fidx):
+        return np.repeat(eidxs + self.face_metric_col,
+                         self.nfacefpts[fidx]).astype(np.int32),
+
     def set_backend(self, backend, nonce, linoff):
         super().set_backend(backend, nonce, linoff)
         be, kernels = self._be, self.kernels
@@ -721,7 +745,9 @@ class NavierStokesElements(_WavespeedMixin, _DivergenceMixin, FluidElements,
             kernels['tdisf_fused'] = lambda uin: self._make_sliced_kernel(
                 be.kernel('tflux', tplargs=tplargs | {'ktype': kt},
                           dims=[npts, n], u=s(self.scal_upts[uin], rgn),
-                          **kw, **avkw(rgn))
+                          **kw, **avkw(rgn),
+                          **({} if self.grad_writeback else
+                             {'gradwb': False}))
                 for kt, n, rgn, kw in tdisf)
 
         self._divergence_kernels()

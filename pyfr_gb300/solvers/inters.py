@@ -140,6 +140,9 @@ class NavierStokesIntInters(BaseIntInters):
         # (the view of the artificial viscosity of the left side, set by
         # the system when shock capturing is artificial viscosity)
         self.artvisc = None
+        # (metric matrix and element columns of both sides when the face
+        # gradients stay in reference space: set_face_metrics)
+        self.facemet = None
 
         be = self._be
         be.pointwise.register('pyfr.solvers.navstokes.kernels.intconu')
@@ -154,7 +157,19 @@ class NavierStokesIntInters(BaseIntInters):
             'intcflux', tplargs=self._tplargs, dims=[self.ninterfpts],
             ul=self.scal_lhs, ur=self.scal_rhs,
             gradul=self._vect_lhs, gradur=self._vect_rhs, nl=self._pnorm_lhs,
-            **({'artvisc': self.artvisc} if self.artvisc is not None else {}))
+            **({'artvisc': self.artvisc} if self.artvisc is not None else {}),
+            **({'facemet': self.facemet} if self.facemet is not None else {}))
+
+    def set_face_metrics(self, emet):
+        """The face gradients reach the interface kernel in reference
+        space: ``emet`` is the backend matrix of the affine elements'
+        metric terms (one column per element, each type from its
+        ``face_metric_col``)."""
+        cols = [self._be.const_matrix(
+            inter_arrays(side, 'get_eidx_for_inters', self.elemap,
+                         self._perm)[0][None, :], dtype=np.int32)
+            for side in (self.lhs, self.rhs)]
+        self.facemet = (emet, *cols)
 
     def _perm_side(self):
         # For beta = -1/2 order by the right side instead

@@ -515,6 +515,52 @@ class NavierStokesSystem(BaseSystem):
     mpiinterscls = NavierStokesMPIInters
     bcinterscls = NavierStokesBCInters
 
+    def __init__(self, *args, **kwargs):
+        super().__init__(*args, **kwargs)
+        self._setup_face_gradients()
+
+    def _setup_face_gradients(self):
+        """With single-precision state and every element affine, the flux
+        kernel leaves the corrected gradient in reference space instead of
+        storing its transform (one field write per right-hand side less),
+        the face gradients are interpolated from it, and the interface
+        kernel transforms them with the elements' metric terms (an affine
+        transform commutes with the interpolation).  ``[backend-b200]
+        face-gradients = auto`` (this when the conditions hold) or
+        ``physical`` (the reference's order: transform at the points)."""
+        be, cfg = self.backend, self.cfg
+        opt = cfg.get('backend-b200', 'face-gradients', 'auto')
+        if opt not in ('auto', 'physical'):
+            raise ValueError('face-gradients must be auto or physical')
+        if opt == 'physical' or be.fpdtype != np.float32 or \
+                self._bc_inters or self._mpi_inters or \
+                cfg.get('solver', 'shock-capturing', 'none') != 'none' or \
+                any(e.antialias for e in self.ele_map.values()):
+            return
+        mets = []
+        for e in self.ele_map.values():
+            m = e.affine_metrics()
+            if m is None:
+                return
+            mets.append(m)
+        nd = self.ndims
+        ncol = sum(len(r) for _, r in mets)
+        if ncol >= 2**31:
+            return
+        emet = np.empty((nd*nd + 1, ncol))
+        col = 0
+        for e, (sm, rj) in zip(self.ele_map.values(), mets):
+            n = len(rj)
+            emet[:nd*nd, col:col + n] = sm.reshape(nd*nd, n)
+            emet[nd*nd, col:col + n] = rj
+            e.face_metric_col = col
+            e.grad_writeback = False
+            col += n
+        mat = be.const_matrix(emet, tags={'align'})
+        for i in self._int_inters:
+            i.set_face_metrics(mat)
+        be.commit()
+
     def _rhs_graphs(self, uinbank, foutbank):
         k = self._get_kernels(uinbank, foutbank)
 

@@ -109,7 +109,7 @@ def test_memcpy_roundtrip(be, chunks, streams):
     buffer's device mapping; an odd byte count exercises the last piece
     and the kernels' byte tail."""
     import ctypes as C
-    rng = np.random.default_rng(chunks + 10*streams)
+    rng = np.random.default_rng(chunks + 10*abs(streams))
     x = rng.normal(size=(8, 5, 77))
     a = be.matrix(x.shape, x, tags={'align'})
     b = be.matrix(x.shape, tags={'align'})

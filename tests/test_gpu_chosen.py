@@ -488,3 +488,87 @@ def test_stage_in_divergence_epilogue(built, case, graphs):
         intg.run_steps(6)
         (sols[fuse],) = intg.soln
     assert np.array_equal(sols['true'], sols['false'])
+
+
+def _ns_rhs_single(mesh, cfg, facegrad, mul='native', shift=False):
+    from pyfr_gb300.backend import B200Backend
+    from pyfr_gb300.solvers.system import NavierStokesSystem
+    cfg.set('backend-b200', 'face-gradients', facegrad)
+    cfg.set('backend-b200', 'mul-precision', mul)
+    if mul == 'bf16x3':
+        cfg.set('backend-b200', 'split-products', 5)
+    be = B200Backend(cfg)
+    s = NavierStokesSystem(be, mesh, None, 2, cfg)
+    if shift:
+        # The TGV on its reference-state transform, as the chosen form runs
+        gamma = cfg.getfloat('constants', 'gamma')
+        rho_ref, p_ref = 1.0, cfg.getfloat('constants', 'p0')
+        hs = gamma/(gamma - 1)*p_ref/rho_ref
+        be.ref_state = (rho_ref, p_ref)
+        (eles,) = s.ele_map.values()
+        q = eles.set_ics_from_cfg() - \
+            np.array([rho_ref, 0, 0, 0, p_ref/(gamma - 1)])[None, :, None]
+        q[:, -1] -= hs*q[:, 0]
+    s.commit()
+    if shift:
+        s.ele_banks[0][0].set(q.astype(np.float32))
+    s.rhs(0.0, 0, 1)
+    wb = {e.grad_writeback for e in s.ele_map.values()}
+    return [r.astype(np.float64) for r in s.ele_scal_upts(1)], wb
+
+
+@pytest.mark.parametrize('mul', ['native', 'bf16x3'])
+@pytest.mark.parametrize('mesh', ['tgv', 'hex-pyr-tet', 'distorted'])
+def test_face_gradients_in_reference_space(built, mul, mesh):
+    """Single precision on affine elements: the flux kernel leaves the
+    corrected gradient in reference space and the interface kernel
+    transforms the face gradients with the elements' metric terms (one
+    column per element over every type).  The right-hand side equals the
+    one with the transform at the points (the reference's order) to FP32
+    rounding: 1e-5 of its scale in FP32 arithmetic; the split-BF16 applies
+    (the chosen form's five products) see different inputs in the two
+    orders, so there their own error (2^-17 of the data, amplified by the
+    operators) bounds the difference: 1e-4.  On the mixed mesh the lift of
+    its small tetrahedra (1/|J| near 50) amplifies a rounding of the face
+    gradients far more, against a right-hand side of 0.1: 1.0e-5 of it
+    measured in FP32 (bound 1e-4) and 128 times that with the BF16 split
+    data's 2^-17 (1.3e-3 measured, bound 3e-3).  A mesh with elements that
+    are not affine keeps the reference's order."""
+    from pyfr_gb300.cases import euler_mixed, ns_tgv
+    from pyfr_gb300.mesh import mixed_box
+    if mesh == 'tgv':
+        mk = lambda: ns_tgv(n=4, order=3, precision='single')
+    elif mesh == 'hex-pyr-tet':
+        def mk():
+            cfg, _ = euler_mixed(n=2, kinds='hex-pri', precision='single')
+            for k, v in (('mu', 0.02), ('Pr', 0.72)):
+                cfg.set('constants', k, v)
+            cfg.set('solver-interfaces', 'ldg-beta', 0.5)
+            cfg.set('solver-interfaces', 'ldg-tau', 0.1)
+            cfg.set('soln-ics', 'u', '0.4 + 0.1*sin(y)')
+            cfg.set('soln-ics', 'v', '-0.2 + 0.1*cos(z)')
+            cfg.set('soln-ics', 'w', '0.1*sin(x)')
+            return cfg, mixed_box(4, -np.pi, np.pi, 'hex-pyr-tet')
+    else:
+        def mk():
+            cfg, m = ns_tgv(n=4, order=3, precision='single')
+            sp = m.spts['hex']
+            rng = np.random.default_rng(3)
+            # Move every lattice vertex (periodic images together)
+            h = 2*np.pi/4
+            idx = np.rint((sp + np.pi)/h).astype(int) % 4
+            jit = rng.uniform(-0.1*h, 0.1*h, size=(4, 4, 4, 3))
+            sp += jit[idx[..., 0], idx[..., 1], idx[..., 2]]
+            return cfg, m
+    bf = mul == 'bf16x3'
+    out = {}
+    for fg in ('auto', 'physical'):
+        cfg, m = mk()
+        r, wb = _ns_rhs_single(m, cfg, fg, mul, shift=bf and mesh != 'hex-pyr-tet')
+        out[fg] = r
+        if fg == 'auto':
+            assert wb == ({True} if mesh == 'distorted' else {False})
+    tol = {(False, False): 1e-5, (True, False): 1e-4, (False, True): 1e-4,
+           (True, True): 3e-3}[bf, mesh == 'hex-pyr-tet']
+    for a, b in zip(out['auto'], out['physical']):
+        assert np.abs(a - b).max() <= tol*np.abs(b).max()
