@@ -132,7 +132,11 @@ def kernel_bytes(k, be):
     if kind in ('tflux_ns', 'tflux_euler'):
         nupts, neles = m['dims']
         nd, nv = m['tplargs']['ndims'], m['tplargs']['nvars']
-        per_pt = nv + nd*nv + (2*nd*nv if kind == 'tflux_ns' else 0)
+        # u in and F out; the NS flux also reads the gradient and, unless
+        # it leaves it in reference space, writes it back transformed
+        per_pt = nv + nd*nv
+        if kind == 'tflux_ns':
+            per_pt += nd*nv*(2 if m.get('gradwb', True) else 1)
         # Metric terms (nd*nd + 1 values) stored per point or, for affine
         # elements, per element; or the vertices they are rebuilt from
         geo = {1: (2**nd)*nd*neles, 2: neles*(nd*nd + 1)}.get(
@@ -145,9 +149,11 @@ def kernel_bytes(k, be):
         nsides = 0
         if kind == 'intcflux_ns':
             nsides = 1 if abs(m['tplargs']['c']['ldg-beta']) == 0.5 else 2
-        # (the unit normal and its magnitude: nd + 1 values)
+        # (the unit normal and its magnitude: nd + 1 values; with face
+        # gradients in reference space an element column per side read,
+        # whose metric terms are cache hits)
         vals = 4*nv + nd + 1 + nsides*nd*nv
-        maps = 2 + 2*nsides
+        maps = 2 + 2*nsides + (nsides if m.get('facemet') else 0)
         return n*(vals*itemsize + maps*4)
     if kind == 'intconu':
         (n,) = m['dims']

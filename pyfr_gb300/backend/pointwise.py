@@ -282,7 +282,7 @@ class PointwiseKernelProvider:
                       meta=dict(kind='tflux_ns', tplargs=tplargs, dims=dims,
                                 u=u, f=f, gradu=gradu, smats=smats,
                                 rcpdjac=rcpdjac, verts=verts, upts=upts,
-                                geom_mode=lin))
+                                geom_mode=lin, gradwb=gradwb))
 
     def _wavespeed(self, tplargs, dims, extrns, u, wspd, smats=None,
                    rcpdjac=None, verts=None, upts=None):
@@ -520,7 +520,7 @@ class PointwiseKernelProvider:
                       ([artvisc] if artvisc is not None else []),
                       misc=[gas], name='intcflux',
                       meta=dict(kind='intcflux_ns', tplargs=tplargs,
-                                dims=dims))
+                                dims=dims, facemet=facemet is not None))
 
     # ---- boundary kernels -------------------------------------------------
 
