@@ -157,8 +157,13 @@ def kernel_bytes(k, be):
         return n*(vals*itemsize + maps*4)
     if kind == 'intconu':
         (n,) = m['dims']
-        nv = m['tplargs']['nvars']
-        return n*(2*nv*itemsize + 4*4)
+        t = m['tplargs']
+        nv, one = t['nvars'], abs(t['c']['ldg-beta']) == 0.5
+        # One side read when ldg-beta = +-1/2 (else both); written to the
+        # other side, or to both with both_sides (always both otherwise)
+        nread = nv if one else 2*nv
+        nwrite = 2*nv if (t.get('both_sides') or not one) else nv
+        return n*((nread + nwrite)*itemsize + 4*4)
     if kind == 'negdivconf':
         nupts, neles = m['dims']
         nv = m['tplargs']['nvars']

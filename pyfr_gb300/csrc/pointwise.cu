@@ -627,21 +627,39 @@ intconu_kernel(int64_t n, int nvars, T beta, ScalView<T> lin, ScalView<T> rin,
     T *plo = lout.base + b200::load_ix(lout.map, ix64, i);
     T *pro = rout.base + b200::load_ix(rout.map, ix64, i);
 
-    for (int v = 0; v < nvars; v++) {
-        const int o = v * B200_SOASZ;
-        if (beta == T(-0.5)) {
-            const T c = pli[o];
-            pro[o] = c;
-            if (both) plo[o] = c;
-        } else if (beta == T(0.5)) {
-            const T c = pri[o];
-            plo[o] = c;
-            if (both) pro[o] = c;
-        } else {
-            const T c = pri[o] * (T(0.5) + beta) + pli[o] * (T(0.5) - beta);
-            plo[o] = c;
-            pro[o] = c;
-        }
+    // Every load before any store (the views may alias as far as the
+    // compiler knows, so interleaving would serialise one round trip to
+    // memory per variable)
+    constexpr int NVMAX = 8;
+    T c[NVMAX];
+    if (beta == T(-0.5) || beta == T(0.5)) {
+        const T *src = beta == T(-0.5) ? pli : pri;
+        T *dst = beta == T(-0.5) ? pro : plo;
+        T *other = beta == T(-0.5) ? plo : pro;
+#pragma unroll
+        for (int v = 0; v < NVMAX; v++)
+            if (v < nvars) c[v] = src[v * B200_SOASZ];
+#pragma unroll
+        for (int v = 0; v < NVMAX; v++)
+            if (v < nvars) {
+                dst[v * B200_SOASZ] = c[v];
+                if (both) other[v * B200_SOASZ] = c[v];
+            }
+    } else {
+        T l[NVMAX];
+#pragma unroll
+        for (int v = 0; v < NVMAX; v++)
+            if (v < nvars) {
+                c[v] = pri[v * B200_SOASZ];
+                l[v] = pli[v * B200_SOASZ];
+            }
+#pragma unroll
+        for (int v = 0; v < NVMAX; v++)
+            if (v < nvars) {
+                const T x = c[v] * (T(0.5) + beta) + l[v] * (T(0.5) - beta);
+                plo[v * B200_SOASZ] = x;
+                pro[v * B200_SOASZ] = x;
+            }
     }
 }
 
@@ -819,6 +837,7 @@ int intconu(int nvars, int64_t n, double beta, const T *lin_base, const void *li
             const T *rin_base, const void *rin_map, T *lout_base, const void *lout_map,
             T *rout_base, const void *rout_map, int ix64, int both, cudaStream_t st) {
     if (n <= 0) return B200_OK;
+    if (nvars < 1 || nvars > 8) return b200::set_error(B200_ERR_ARG, "intconu: 1-8 variables");
     ScalView<T> li{const_cast<T *>(lin_base), lin_map};
     ScalView<T> ri{const_cast<T *>(rin_base), rin_map};
     ScalView<T> lo{lout_base, lout_map}, ro{rout_base, rout_map};
