@@ -479,7 +479,7 @@ template <int ND, int NV, typename T>
 __device__ __forceinline__ void face_grad_to_phys(const FaceMetrics<T> &fm, int k,
                                                   T gg[ND][NV]) {
     const T *m = fm.m + k;
-    const T rcp = m[(int64_t)(ND * ND) * fm.ld];
+    const T rcp = __ldg(m + (int64_t)(ND * ND) * fm.ld);
     // One output component at a time over every variable; the metric terms
     // are re-read rather than held (L1 hits: the pairs of one face share
     // their element), which keeps the kernel within its register bound
@@ -488,7 +488,7 @@ __device__ __forceinline__ void face_grad_to_phys(const FaceMetrics<T> &fm, int 
     for (int i = 0; i < ND; i++) {
         T c[ND];
 #pragma unroll
-        for (int q = 0; q < ND; q++) c[q] = rcp * m[(int64_t)(q * ND + i) * fm.ld];
+        for (int q = 0; q < ND; q++) c[q] = rcp * __ldg(m + (int64_t)(q * ND + i) * fm.ld);
 #pragma unroll
         for (int v = 0; v < NV; v++) {
             T acc = 0;
@@ -514,6 +514,9 @@ intcflux_ns_kernel(int64_t n, b200::GasK<T> gas, T beta, T tau, ScalView<T> vl, 
 
     T *pl = vl.base + b200::load_ix(vl.map, ix64, i);
     T *pr = vr.base + b200::load_ix(vr.map, ix64, i);
+    // (the element columns of the face metrics, loaded early)
+    const int kl = FM && beta != T(-0.5) ? fm.il[i] : 0;
+    const int kr = FM && beta != T(0.5) ? fm.ir[i] : 0;
 
     T ul[NV], ur[NV], nn[ND];
 #pragma unroll
@@ -554,7 +557,7 @@ intcflux_ns_kernel(int64_t n, b200::GasK<T> gas, T beta, T tau, ScalView<T> vl, 
         for (int d = 0; d < ND; d++)
 #pragma unroll
             for (int v = 0; v < NV; v++) gg[d][v] = g[d * rstr + v * B200_SOASZ];
-        if (FM) face_grad_to_phys<ND, NV, T>(fm, fm.il[i], gg);
+        if (FM) face_grad_to_phys<ND, NV, T>(fm, kl, gg);
         if (gas.shifted) {
             T gu[ND][NV];
             b200::unshift_grad<ND, T>(gg, gu, gas);
@@ -580,7 +583,7 @@ intcflux_ns_kernel(int64_t n, b200::GasK<T> gas, T beta, T tau, ScalView<T> vl, 
         for (int d = 0; d < ND; d++)
 #pragma unroll
             for (int v = 0; v < NV; v++) gg[d][v] = g[d * rstr + v * B200_SOASZ];
-        if (FM) face_grad_to_phys<ND, NV, T>(fm, fm.ir[i], gg);
+        if (FM) face_grad_to_phys<ND, NV, T>(fm, kr, gg);
         if (gas.shifted) {
             T gu[ND][NV];
             b200::unshift_grad<ND, T>(gg, gu, gas);
