@@ -75,6 +75,8 @@ def test_std_ele_corners():
     assert corner_nodes('hex', 1) == list(range(8))
     assert corner_nodes('pri', 2) == [0, 2, 5, 12, 14, 17]
     assert len(std_ele('tet', 3)) == 20 and corner_nodes('tet', 3)[-1] == 19
+    assert len(std_ele('pyr', 2)) == 14
+    assert corner_nodes('pyr', 2) == [0, 2, 6, 8, 13]
 
 
 MESHES = {
@@ -83,6 +85,7 @@ MESHES = {
                                (True, False, True)),
     'hex-pri': lambda: mixed_box(2, -1.0, 1.0, 'hex-pri'),
     'pri-tet': lambda: mixed_box(2, -1.0, 1.0, 'pri-tet'),
+    'hex-pyr-tet': lambda: mixed_box(2, -1.0, 1.0, 'hex-pyr-tet'),
     'tri': lambda: tri_box(3, 0.0, 1.0),
 }
 
