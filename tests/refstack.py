@@ -221,8 +221,24 @@ def run(case, n, steps, out=None, fake=False, source=False, single=False):
     from pyfr.solvers import get_solver
     from pyfr_gb300.cases import euler_vortex, ns_tgv
 
+    lits = {}
     if case == 'vortex':
         cfg, mesh = euler_vortex(n=n, order=3, dt=1e-3)
+    elif case.startswith('mixed-'):
+        # 'mixed-<kinds>': a mixed box of pyfr_gb300.mesh.mixed_box (3-D
+        # Euler density wave), the simplex point sets of this package
+        # handed to the reference literally so that both order them alike
+        from pyfr_gb300.cases import euler_mixed
+        from pyfr_gb300.quadrules import point_set
+        cfg, mesh = euler_mixed(n=n, kinds=case[6:], dt=1e-3)
+
+        def lit(kind, rule):
+            return ', '.join('(' + ', '.join(repr(float(x)) for x in q) + ')'
+                             for q in point_set(kind, rule, 3))
+        lits = {('solver-elements-tet', 'soln-pts'): lit('tet', 'alpha-opt'),
+                ('solver-elements-pri', 'soln-pts'):
+                    lit('pri', 'alpha-opt~gauss-legendre-lobatto'),
+                ('solver-interfaces-tri', 'flux-pts'): lit('tri', 'alpha-opt')}
     elif case.startswith('bc-'):
         # 'bc-euler:<type>,<type>' or 'bc-ns:<type>,<type>'
         from tests.bc_cases import bc_case
@@ -237,6 +253,8 @@ def run(case, n, steps, out=None, fake=False, source=False, single=False):
         cfg.set('backend', 'precision', 'single')
         cfg.set('backend-b200', 'mul-precision', 'bf16x3')
     rcfg = reference_cfg(cfg)
+    for (sect, key), val in lits.items():
+        rcfg.set(sect, key, val)
     rcfg.set('solver-time-integrator', 'tstart', '0.0')
     rcfg.set('solver-time-integrator', 'tend', repr(1e3))
     dt = rcfg.getfloat('solver-time-integrator', 'dt')
@@ -248,16 +266,20 @@ def run(case, n, steps, out=None, fake=False, source=False, single=False):
         solver.advance_to(solver.tcurr + dt)
     u1 = [np.array(s) for s in solver.soln]
     if out:
+        ets = list(solver.system.ele_types)
         np.savez(out, u0=u0[0], u1=u1[0], dt=dt,
                  backend=type(backend).__mro__[1].__name__,
-                 nsteps=solver.nacptsteps)
+                 nsteps=solver.nacptsteps, etypes=np.array(ets),
+                 **{f'u0/{et}': a for et, a in zip(ets, u0)},
+                 **{f'u1/{et}': a for et, a in zip(ets, u1)})
     return u0, u1, dt, solver
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--case', default='vortex',
-                    help="'vortex', 'tgv' or 'bc-euler|bc-ns:<type>,<type>'")
+                    help="'vortex', 'tgv', 'mixed-<kinds>' or "
+                         "'bc-euler|bc-ns:<type>,<type>'")
     ap.add_argument('--n', type=int, default=8)
     ap.add_argument('--steps', type=int, default=5)
     ap.add_argument('--out')

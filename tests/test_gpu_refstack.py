@@ -182,3 +182,51 @@ def test_reference_controlled_bcs(built, tmp_path, kind, types):
     # The controller moved the pressure: the run differs from one at the
     # initial pressure
     assert abs(c.interp_m) > 0
+
+
+@pytest.mark.parametrize('kinds', ['hex-pyr-tet', 'pri-tet'])
+def test_reference_solver_mixed_mesh(built, tmp_path, kinds):
+    """PyFR's own Euler system and RK45 integrator on a mixed mesh
+    (hexahedra, pyramids and tetrahedra: the reference's own pyramid shape
+    and points) driven through the b200 backend, against the oracle with
+    this package's operators: 1e-10 relative max-norm per type."""
+    if reference_tree() is None:
+        pytest.skip('reference source tree not present')
+    from oracle.fr_oracle import MixedDiscretisation, rk45_step
+    from pyfr_gb300.cases import euler_mixed
+    from pyfr_gb300.shapes import get_shape
+    from tests.oracle_util import basis_of, ops_from_shape
+    from tests.test_oracle import MIXED_FPTS, MIXED_UPTS
+
+    out = tmp_path / 'soln.npz'
+    r = subprocess.run([sys.executable, '-m', 'tests.refstack', '--case',
+                        f'mixed-{kinds}', '--n', '2', '--steps', '3',
+                        '--out', str(out)],
+                       cwd=ROOT, capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr[-3000:]
+    d = np.load(out)
+    assert str(d['backend']) == 'B200Backend'
+    ets = [str(e) for e in d['etypes']]
+
+    cfg, mesh = euler_mixed(n=2, kinds=kinds, dt=1e-3)
+    assert set(ets) == set(mesh.spts)
+    parts = {}
+    for et, verts in mesh.spts.items():
+        s = get_shape(et, 3, MIXED_UPTS[et], MIXED_FPTS)
+        parts[et] = dict(ops=ops_from_shape(s), basis=basis_of(s),
+                         verts=verts)
+    lhs, rhs = mesh.con
+    disc = MixedDiscretisation(parts, zip(lhs.etypes, lhs.eidxs, lhs.fidxs),
+                               zip(rhs.etypes, rhs.eidxs, rhs.fidxs),
+                               periods=mesh.periods)
+    c = dict(gamma=1.4)
+    u = disc.pack({et: d[f'u0/{et}'] for et in ets})
+    for _ in range(3):
+        u = rk45_step(lambda x: disc.pack(disc.rhs_euler(disc.unpack(x, 5), c)),
+                      u, float(d['dt']))
+    ref = disc.unpack(u, 5)
+    for et in ets:
+        got = d[f'u1/{et}']
+        err = max(np.abs(got[:, v] - ref[et][:, v]).max() /
+                  np.abs(ref[et][:, v]).max() for v in range(5))
+        assert err < 1e-10, (et, err)
