@@ -30,15 +30,16 @@ extern "C" {
 /* Gas and viscosity constants of the flux kernels ([constants] gamma, mu,
  * Pr, cpTref, cpTs; viscosity-correction = sutherland when sutherland != 0);
  * pyfr/solvers/navstokes/kernels/flux.mako:48-105.
- * shifted != 0 (Navier-Stokes kernels, Rusanov only): the solution inputs
- * are q = T(u - u_ref), the perturbation from the constant state
- * (rho_ref, 0, E_ref = p_ref/(gamma - 1)) with its energy component
- * replaced by dE - h_ref*drho (h_ref = gamma/(gamma - 1) p_ref/rho_ref);
- * the kernels compute the right-hand side of q, i.e. T times that of u
- * (energy row minus h_ref times the mass row), with the constant fluxes
- * p_ref*I and H_ref*v left out.  Exact in exact arithmetic; the
- * low-precision rounding no longer scales with the mean pressure and
- * enthalpy.
+ * shifted != 0 (Navier-Stokes kernels and the *_shift Euler kernels,
+ * Rusanov only): the solution inputs are q = T(u - u_ref), the
+ * perturbation from the constant state (rho_ref, rho_ref*v_ref,
+ * E_ref = p_ref/(gamma - 1) + rho_ref |v_ref|^2/2) with its energy
+ * component replaced by dE - h_t*drho (h_t = (E_ref + p_ref)/rho_ref); the
+ * kernels compute the right-hand side of q, i.e. T times that of u (energy
+ * row minus h_t times the mass row), with the reference state's constant
+ * flux left out and the rest formed from the perturbation.  Exact in exact
+ * arithmetic; the low-precision rounding no longer scales with the mean
+ * pressure, enthalpy or flow.
  * p_min: the floor that the exact Riemann solver's Newton iterations put on
  * the star pressure (pyfr/solvers/euler/inters.py:12-25). */
 typedef struct {
@@ -47,6 +48,7 @@ typedef struct {
     int shifted;
     double rho_ref, p_ref;
     double p_min;   /* floor of the exact Riemann solver's star pressure */
+    double v_ref[3];    /* reference velocity (zeros: the fluid at rest) */
 } b200_gas_t;
 
 /* Boundary conditions: the types of pyfr/solvers/euler/inters.py:83-112
@@ -290,6 +292,18 @@ int b200_tflux_euler_f32(int ndims, int nupts, int64_t neles, int linear, double
                          const float *u, int64_t ldu, float *f, int64_t ldf,
                          const float *smats, int64_t lds, const float *verts, int64_t ldv,
                          const float *upts, int64_t ldup, void *stream);
+/* The Euler flux on shifted inputs q = T(u - u_ref) (b200_gas_t with
+ * `shifted`): the flux less the reference state's, formed from the
+ * perturbation.  No counterpart in the reference. */
+int b200_tflux_euler_shift_f64(int ndims, int nupts, int64_t neles, int linear,
+                               const b200_gas_t *gas, const double *u, int64_t ldu, double *f,
+                               int64_t ldf, const double *smats, int64_t lds,
+                               const double *verts, int64_t ldv, const double *upts,
+                               int64_t ldup, void *stream);
+int b200_tflux_euler_shift_f32(int ndims, int nupts, int64_t neles, int linear,
+                               const b200_gas_t *gas, const float *u, int64_t ldu, float *f,
+                               int64_t ldf, const float *smats, int64_t lds, const float *verts,
+                               int64_t ldv, const float *upts, int64_t ldup, void *stream);
 
 /* Navier-Stokes fused gradient transform + transformed flux;
  * pyfr/solvers/navstokes/kernels/tflux.mako:13-50, provider call
@@ -588,6 +602,16 @@ int b200_intcflux_euler_f32(int ndims, int64_t n, int rsolver, double gamma, dou
                             float *ul_base,
                             const void *ul_map, float *ur_base, const void *ur_map, int ix64,
                             const float *nl, int64_t ldn, int nl_unit, void *stream);
+/* The Rusanov common flux on shifted inputs (b200_gas_t with `shifted`).
+ * No counterpart in the reference. */
+int b200_intcflux_euler_shift_f64(int ndims, int64_t n, const b200_gas_t *gas, double *ul_base,
+                                  const void *ul_map, double *ur_base, const void *ur_map,
+                                  int ix64, const double *nl, int64_t ldn, int nl_unit,
+                                  void *stream);
+int b200_intcflux_euler_shift_f32(int ndims, int64_t n, const b200_gas_t *gas, float *ul_base,
+                                  const void *ul_map, float *ur_base, const void *ur_map,
+                                  int ix64, const float *nl, int64_t ldn, int nl_unit,
+                                  void *stream);
 
 /* Navier-Stokes common flux (Riemann + LDG viscous with beta, tau);
  * pyfr/solvers/navstokes/kernels/intcflux.mako:10-54. */

@@ -40,7 +40,8 @@ class MulArgs(C.Structure):
 class Gas(C.Structure):
     _fields_ = [('gamma', f64), ('mu', f64), ('pr', f64), ('cpTref', f64),
                 ('cpTs', f64), ('sutherland', i32), ('shifted', i32),
-                ('rho_ref', f64), ('p_ref', f64), ('p_min', f64)]
+                ('rho_ref', f64), ('p_ref', f64), ('p_min', f64),
+                ('v_ref', f64*3)]
 
 
 # Boundary-condition types and constants (b200_bc_t)
@@ -130,6 +131,10 @@ def _sig_pointwise(fp):
                        vp, vp, vp, vp, i32, vp, i64, vp],
         'bccflux_ns_av': [i32, i64, i32, C.POINTER(Gas), f64, C.POINTER(BC),
                           vp, vp, vp, vp, vp, i32, vp, i64, vp, vp, vp],
+        'tflux_euler_shift': [i32, i32, i64, i32, C.POINTER(Gas), vp, i64, vp,
+                              i64, vp, i64, vp, i64, vp, i64, vp],
+        'intcflux_euler_shift': [i32, i64, C.POINTER(Gas), vp, vp, vp, vp, i32,
+                                 vp, i64, i32, vp],
         'tflux_ns_refgrad': [i32, i32, i64, i32, C.POINTER(Gas), vp, i64, vp,
                              i64, vp, i64, vp, i64, vp, i64, vp, i64, vp, i64,
                              vp],

@@ -43,7 +43,9 @@ def _gas(c, visc_corr='none', ref_state=None, p_min=P_MIN_DEFAULT):
             sutherland=int(visc_corr == 'sutherland'), p_min=p_min)
     if ref_state is not None:
         g.shifted = 1
-        g.rho_ref, g.p_ref = ref_state
+        g.rho_ref, g.p_ref = ref_state[:2]
+        for i, v in enumerate(ref_state[2] if len(ref_state) > 2 else ()):
+            g.v_ref[i] = v
     return g
 
 
@@ -215,12 +217,23 @@ class PointwiseKernelProvider:
         up, ul = _mat(u)
         fp, fl = _mat(f)
         nd = tplargs['ndims']
+        gas = None
 
-        def run(stream):
-            fn(nd, nupts, neles, lin, gamma, up, ul, fp, fl, sp, sl, vp, vl,
-               upp, upl, stream)
+        if self.backend.ref_state is not None:
+            # Shifted inputs: the flux less the reference state's
+            fn = self._fn('tflux_euler_shift')
+            gas = _gas(tplargs['c'], 'none', self.backend.ref_state)
 
-        return Kernel(run, mats=[u, f, smats, verts, upts], name='tflux',
+            def run(stream):
+                fn(nd, nupts, neles, lin, C.byref(gas), up, ul, fp, fl, sp, sl,
+                   vp, vl, upp, upl, stream)
+        else:
+            def run(stream):
+                fn(nd, nupts, neles, lin, gamma, up, ul, fp, fl, sp, sl, vp,
+                   vl, upp, upl, stream)
+
+        return Kernel(run, mats=[u, f, smats, verts, upts], misc=[gas],
+                      name='tflux',
                       meta=dict(kind='tflux_euler', tplargs=tplargs,
                                 dims=dims, u=u, f=f, smats=smats,
                                 verts=verts, upts=upts,
@@ -453,12 +466,25 @@ class PointwiseKernelProvider:
         rb, rm, _ = _view(ur)
         np_, nlp, nlu, nlm = self._normals(nl)
         ix64 = self._ix64
+        gas = None
 
-        def run(stream):
-            fn(nd, n, rs, gamma, p_min, lb, lm, rb, rm, ix64, np_, nlp, nlu,
-               stream)
+        if self.backend.ref_state is not None:
+            if tplargs['rsolver'] != 'rusanov':
+                raise NotImplementedError('The reference-state shift needs '
+                                          'the Rusanov Riemann solver')
+            fn = self._fn('intcflux_euler_shift')
+            gas = _gas(tplargs['c'], 'none', self.backend.ref_state, p_min)
 
-        return Kernel(run, mats=[nl, nlm], views=[ul, ur], name='intcflux',
+            def run(stream):
+                fn(nd, n, C.byref(gas), lb, lm, rb, rm, ix64, np_, nlp, nlu,
+                   stream)
+        else:
+            def run(stream):
+                fn(nd, n, rs, gamma, p_min, lb, lm, rb, rm, ix64, np_, nlp,
+                   nlu, stream)
+
+        return Kernel(run, mats=[nl, nlm], views=[ul, ur], misc=[gas],
+                      name='intcflux',
                       meta=dict(kind='intcflux_euler', tplargs=tplargs,
                                 dims=dims, ul=ul, ur=ur, nl=nl))
 

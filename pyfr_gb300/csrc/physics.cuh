@@ -24,22 +24,25 @@ namespace b200 {
 // Gas / viscosity constants shared by all flux kernels (POD, matches the
 // b200_gas_t struct of the C ABI).  When `shifted` is set the kernels'
 // input is q = T(u - u_ref): the perturbation from a constant reference
-// state (rho_ref, 0, E_ref = p_ref/(gamma - 1)) with the energy component
-// replaced by dE - h_ref*drho, h_ref = gamma/(gamma - 1) p_ref/rho_ref the
-// reference specific enthalpy.  T is linear and constant, so the system in
-// q is the system in u multiplied by T: the mass and momentum equations are
-// unchanged and the energy equation is the energy equation minus h_ref
-// times the mass equation.  Its inviscid flux is (dE - h_ref*drho + dp) v
-// instead of (H_ref + dE + dp) v, and the constant part p_ref*I of the
-// momentum flux is dropped (the flux-reconstruction divergence of a
-// constant flux field is exactly zero).  Every flux is then of the size of
-// the perturbation, so FP32 rounding no longer scales with p_ref or H_ref.
+// state (rho_ref, rho_ref V, E_ref = p_ref/(gamma - 1) + rho_ref |V|^2/2)
+// with the energy component replaced by dE - h_t*drho, h_t = (E_ref +
+// p_ref)/rho_ref the reference total enthalpy per unit mass.  T is linear
+// and constant, so the system in q is the system in u multiplied by T: the
+// mass and momentum equations are unchanged and the energy equation is the
+// energy equation minus h_t times the mass equation.  The constant flux of
+// the reference state is dropped (the flux-reconstruction divergence of a
+// constant flux field is exactly zero), and what remains is formed from the
+// perturbation: with v = V + w, w = (dm - V drho)/rho, the momentum flux is
+// rho_ref V w + dm V + dm w + dp I and the energy flux (q_E + dp) v.  Every
+// flux is then of the size of the perturbation, so FP32 rounding no longer
+// scales with p_ref, the reference enthalpy or the mean flow.
 struct Gas {
     double gamma, mu, pr, cpTref, cpTs;
     int sutherland;
     int shifted;
     double rho_ref, p_ref;
     double p_min;
+    double v_ref[3];    // reference velocity V (zero: the fluid at rest)
 };
 
 // The same constants in the kernel's arithmetic type, with every derived
@@ -48,7 +51,8 @@ struct Gas {
 template <typename T>
 struct GasK {
     T gamma, gm1, mu, gamma_pr, rcp_cpTref, mu_ctt, cpTs, quarter_gamma;
-    T rho_ref, p_ref, e_ref, h_ref, hs_ref, p_min;
+    T rho_ref, p_ref, e_ref, hs_ref, p_min;
+    T v_ref[3], m_ref[3];
     int sutherland, shifted;
 };
 
@@ -65,9 +69,15 @@ inline GasK<T> gas_consts(const Gas &g) {
     k.quarter_gamma = (T)(0.25 * g.gamma);
     k.rho_ref = (T)g.rho_ref;
     k.p_ref = (T)g.p_ref;
-    k.e_ref = (T)(g.p_ref / (g.gamma - 1.0));
-    k.h_ref = (T)(g.gamma / (g.gamma - 1.0) * g.p_ref);
-    k.hs_ref = (T)(g.rho_ref != 0.0 ? g.gamma / (g.gamma - 1.0) * g.p_ref / g.rho_ref : 0.0);
+    double v2 = 0.0;
+    for (int i = 0; i < 3; i++) {
+        k.v_ref[i] = (T)g.v_ref[i];
+        k.m_ref[i] = (T)(g.rho_ref * g.v_ref[i]);
+        v2 += g.v_ref[i] * g.v_ref[i];
+    }
+    const double e_ref = g.p_ref / (g.gamma - 1.0) + 0.5 * g.rho_ref * v2;
+    k.e_ref = (T)e_ref;
+    k.hs_ref = (T)(g.rho_ref != 0.0 ? (e_ref + g.p_ref) / g.rho_ref : 0.0);
     k.p_min = (T)g.p_min;
     k.sutherland = g.sutherland;
     k.shifted = g.shifted;
@@ -268,11 +278,15 @@ __device__ __forceinline__ void rsolve_rusanov(const T *ul, const T *ur, const T
     for (int i = 0; i < NV; i++) nf[i] = T(0.5) * (fl[i] + fr[i]) + a * (ul[i] - ur[i]);
 }
 
-// Inviscid flux from the transformed input s = q = T(u - u_ref) (see Gas):
-// rho = rho_ref + s[0], m = s[1..ND], dE = s[E] + hs_ref*s[0], dp = p - p_ref
-// from (gamma - 1)(dE - |m|^2/(2 rho)); mass flux m, momentum flux
-// m v + dp I, energy flux (s[E] + dp) v.  Returns the full pressure in p and
-// the full state in ufull (for the viscous terms).
+// Inviscid flux, less the reference state's, from the transformed input
+// s = q = T(u - u_ref) (see Gas): rho = rho_ref + s[0], dm = s[1..ND],
+// dE = s[E] + h_t s[0]; the velocity v = V + w with w = (dm - V s[0])/rho;
+// dp = p - p_ref = (gamma - 1)(dE - (m.v - rho_ref |V|^2)/2) with
+// m.v - rho_ref |V|^2 = rho_ref V.w + dm.V + dm.w; mass flux dm, momentum
+// flux rho_ref V w + dm V + dm w + dp I, energy flux (s[E] + dp) v.  (With
+// V = 0 these are m, m v + dp I and (s[E] + dp) v.)  Returns the full
+// pressure in p, the full velocity in v and the full state in ufull (for
+// the viscous terms and the wave speeds).
 template <int ND, typename T>
 __device__ __forceinline__ void inviscid_flux_shift(const T *s, T f[ND][ND + 2], T &p, T v[ND],
                                                     T ufull[ND + 2], const GasK<T> &g) {
@@ -280,11 +294,12 @@ __device__ __forceinline__ void inviscid_flux_shift(const T *s, T f[ND][ND + 2],
     const T gm1 = g.gm1;
     const T rho = g.rho_ref + s[0], invrho = T(1) / rho;
     const T dE = s[NV - 1] + g.hs_ref * s[0];
-    T dot = 0;
+    T w[ND], dot = 0;
 #pragma unroll
     for (int i = 0; i < ND; i++) {
-        v[i] = invrho * s[i + 1];
-        dot += s[i + 1] * v[i];
+        w[i] = invrho * (s[i + 1] - g.v_ref[i] * s[0]);
+        v[i] = g.v_ref[i] + w[i];
+        dot += g.m_ref[i] * w[i] + s[i + 1] * (g.v_ref[i] + w[i]);
     }
     const T dp = gm1 * (dE - T(0.5) * dot);
     p = g.p_ref + dp;
@@ -294,11 +309,12 @@ __device__ __forceinline__ void inviscid_flux_shift(const T *s, T f[ND][ND + 2],
         f[i][0] = s[i + 1];
         f[i][NV - 1] = hv * v[i];
 #pragma unroll
-        for (int j = 0; j < ND; j++) f[i][j + 1] = s[i + 1] * v[j] + (i == j ? dp : T(0));
+        for (int j = 0; j < ND; j++)
+            f[i][j + 1] = g.m_ref[i] * w[j] + s[i + 1] * v[j] + (i == j ? dp : T(0));
     }
     ufull[0] = rho;
 #pragma unroll
-    for (int i = 0; i < ND; i++) ufull[i + 1] = s[i + 1];
+    for (int i = 0; i < ND; i++) ufull[i + 1] = g.m_ref[i] + s[i + 1];
     ufull[NV - 1] = g.e_ref + dE;
 }
 

@@ -105,6 +105,38 @@ tflux_euler_kernel(int nupts, int64_t neles, T gamma, const T *__restrict__ u, i
         }
 }
 
+// Euler transformed flux on shifted inputs q = T(u - u_ref) (b200::Gas):
+// the flux less the reference state's, formed from the perturbation
+template <int ND, typename T>
+__global__ void __launch_bounds__(PW_BLOCK)
+tflux_euler_shift_kernel(int nupts, int64_t neles, b200::GasK<T> gas, const T *__restrict__ u,
+                         int64_t ldu, T *__restrict__ f, int64_t ldf, ElemGeom<T> geo) {
+    constexpr int NV = ND + 2;
+    const int64_t e = (int64_t)blockIdx.x * PW_BLOCK + threadIdx.x;
+    const int upt = blockIdx.y;
+    if (e >= neles) return;
+
+    T s[ND][ND], rcp;
+    elem_metrics<ND, T>(geo, nupts, upt, e, s, rcp, false);
+
+    T uu[NV];
+#pragma unroll
+    for (int v = 0; v < NV; v++) uu[v] = u[upt * ldu + soa_off(e, v, NV)];
+
+    T ft[ND][NV], p, vel[ND], uf[NV];
+    b200::inviscid_flux_shift<ND, T>(uu, ft, p, vel, uf, gas);
+
+#pragma unroll
+    for (int i = 0; i < ND; i++)
+#pragma unroll
+        for (int j = 0; j < NV; j++) {
+            T acc = 0;
+#pragma unroll
+            for (int k = 0; k < ND; k++) acc += s[i][k] * ft[k][j];
+            f[(int64_t)(i * nupts + upt) * ldf + soa_off(e, j, NV)] = acc;
+        }
+}
+
 // Largest characteristic wave speed of each element in reference space,
 // for the CFL controller (pyfr/solvers/euler/kernels/wavespeed.mako:9-44):
 // max over the solution points of sum_i |sum_j (S_ij/|J|) v_j| +
@@ -129,6 +161,8 @@ wavespeed_kernel(int nupts, int64_t neles, b200::GasK<T> gas, const T *__restric
             // q = T(u - u_ref): rho = rho_ref + q0, E = E_ref + qE + h_s q0
             uu[NV - 1] += gas.e_ref + gas.hs_ref * uu[0];
             uu[0] += gas.rho_ref;
+#pragma unroll
+            for (int d = 0; d < ND; d++) uu[d + 1] += gas.m_ref[d];
         }
 
         const T rho = uu[0], rcprho = T(1) / rho;
@@ -451,6 +485,37 @@ intcflux_euler_kernel(int64_t n, T gamma, T p_min, ScalView<T> vl, ScalView<T> v
 
     T fn[NV];
     b200::rsolve_t<RS, ND, T>(ul, ur, nn, fn, gamma, p_min);
+
+#pragma unroll
+    for (int v = 0; v < NV; v++) {
+        pl[v * B200_SOASZ] = mag * fn[v];
+        pr[v * B200_SOASZ] = -mag * fn[v];
+    }
+}
+
+// Rusanov common flux on shifted inputs (the dissipation acts on
+// differences of q, which are T times the differences of u)
+template <int ND, typename T>
+__global__ void __launch_bounds__(PW_BLOCK)
+intcflux_euler_shift_kernel(int64_t n, b200::GasK<T> gas, ScalView<T> vl, ScalView<T> vr,
+                            int ix64, const T *__restrict__ nl, int64_t ldn, int nl_unit) {
+    constexpr int NV = ND + 2;
+    const int64_t i = (int64_t)blockIdx.x * PW_BLOCK + threadIdx.x;
+    if (i >= n) return;
+
+    T *pl = vl.base + b200::load_ix(vl.map, ix64, i);
+    T *pr = vr.base + b200::load_ix(vr.map, ix64, i);
+
+    T ul[NV], ur[NV], nn[ND];
+#pragma unroll
+    for (int v = 0; v < NV; v++) {
+        ul[v] = pl[v * B200_SOASZ];
+        ur[v] = pr[v * B200_SOASZ];
+    }
+    const T mag = pair_normal<ND, T>(nl, ldn, i, nl_unit, nn);
+
+    T fn[NV], ufl[NV], ufr[NV];
+    b200::rsolve_rusanov_shift<ND, T>(ul, ur, nn, fn, ufl, ufr, gas);
 
 #pragma unroll
     for (int v = 0; v < NV; v++) {
@@ -798,6 +863,46 @@ int intcflux_euler(int ndims, int64_t n, int rsolver, double gamma, double p_min
 }
 
 template <typename T>
+int tflux_euler_shift(int ndims, int nupts, int64_t neles, int linear, const b200_gas_t *gas,
+                      const T *u, int64_t ldu, T *f, int64_t ldf, const T *smats, int64_t lds,
+                      const T *verts, int64_t ldv, const T *upts, int64_t ldup, cudaStream_t st) {
+    if (neles <= 0 || nupts <= 0) return B200_OK;
+    if (!gas) return b200::set_error(B200_ERR_ARG, "tflux_euler_shift: null gas constants");
+    int rc = check_geom(linear, smats, nullptr, verts, upts, false);
+    if (rc) return rc;
+    auto geo = make_geom<T>(linear, smats, lds, nullptr, 0, verts, ldv, upts, ldup);
+    const auto g = b200::gas_consts<T>(*reinterpret_cast<const Gas *>(gas));
+    dim3 grid(b200::ceil_div(neles, PW_BLOCK), nupts);
+    if (ndims == 2)
+        tflux_euler_shift_kernel<2, T><<<grid, PW_BLOCK, 0, st>>>(nupts, neles, g, u, ldu, f, ldf, geo);
+    else if (ndims == 3)
+        tflux_euler_shift_kernel<3, T><<<grid, PW_BLOCK, 0, st>>>(nupts, neles, g, u, ldu, f, ldf, geo);
+    else
+        return b200::set_error(B200_ERR_ARG, "tflux: ndims must be 2 or 3");
+    B200_CHECK_LAUNCH("tflux_euler_shift");
+    return B200_OK;
+}
+
+template <typename T>
+int intcflux_euler_shift(int ndims, int64_t n, const b200_gas_t *gas, T *ul_base,
+                         const void *ul_map, T *ur_base, const void *ur_map, int ix64,
+                         const T *nl, int64_t ldn, int nl_unit, cudaStream_t st) {
+    if (n <= 0) return B200_OK;
+    if (!gas) return b200::set_error(B200_ERR_ARG, "intcflux_euler_shift: null gas constants");
+    if (ndims != 2 && ndims != 3)
+        return b200::set_error(B200_ERR_ARG, "intcflux: ndims must be 2 or 3");
+    ScalView<T> l{ul_base, ul_map}, r{ur_base, ur_map};
+    const auto g = b200::gas_consts<T>(*reinterpret_cast<const Gas *>(gas));
+    unsigned grid = b200::ceil_div(n, PW_BLOCK);
+    if (ndims == 2)
+        intcflux_euler_shift_kernel<2, T><<<grid, PW_BLOCK, 0, st>>>(n, g, l, r, ix64, nl, ldn, nl_unit);
+    else
+        intcflux_euler_shift_kernel<3, T><<<grid, PW_BLOCK, 0, st>>>(n, g, l, r, ix64, nl, ldn, nl_unit);
+    B200_CHECK_LAUNCH("intcflux_euler_shift");
+    return B200_OK;
+}
+
+template <typename T>
 int intcflux_ns(int ndims, int64_t n, int rsolver, const b200_gas_t *gas, double beta,
                 double tau, T *ul_base, const void *ul_map, T *ur_base, const void *ur_map,
                 const T *gl_base, const void *gl_map, const void *gl_rstr, const T *gr_base,
@@ -1005,6 +1110,39 @@ int b200_intcflux_euler_f32(int ndims, int64_t n, int rsolver, double gamma, dou
                             const float *nl, int64_t ldn, int nl_unit, void *stream) {
     return intcflux_euler<float>(ndims, n, rsolver, gamma, p_min, ul_base, ul_map, ur_base, ur_map,
                                  ix64, nl, ldn, nl_unit, (cudaStream_t)stream);
+}
+
+int b200_tflux_euler_shift_f64(int ndims, int nupts, int64_t neles, int linear,
+                               const b200_gas_t *gas, const double *u, int64_t ldu, double *f,
+                               int64_t ldf, const double *smats, int64_t lds,
+                               const double *verts, int64_t ldv, const double *upts,
+                               int64_t ldup, void *stream) {
+    return tflux_euler_shift<double>(ndims, nupts, neles, linear, gas, u, ldu, f, ldf, smats, lds,
+                                     verts, ldv, upts, ldup, (cudaStream_t)stream);
+}
+
+int b200_tflux_euler_shift_f32(int ndims, int nupts, int64_t neles, int linear,
+                               const b200_gas_t *gas, const float *u, int64_t ldu, float *f,
+                               int64_t ldf, const float *smats, int64_t lds, const float *verts,
+                               int64_t ldv, const float *upts, int64_t ldup, void *stream) {
+    return tflux_euler_shift<float>(ndims, nupts, neles, linear, gas, u, ldu, f, ldf, smats, lds,
+                                    verts, ldv, upts, ldup, (cudaStream_t)stream);
+}
+
+int b200_intcflux_euler_shift_f64(int ndims, int64_t n, const b200_gas_t *gas, double *ul_base,
+                                  const void *ul_map, double *ur_base, const void *ur_map,
+                                  int ix64, const double *nl, int64_t ldn, int nl_unit,
+                                  void *stream) {
+    return intcflux_euler_shift<double>(ndims, n, gas, ul_base, ul_map, ur_base, ur_map, ix64,
+                                        nl, ldn, nl_unit, (cudaStream_t)stream);
+}
+
+int b200_intcflux_euler_shift_f32(int ndims, int64_t n, const b200_gas_t *gas, float *ul_base,
+                                  const void *ul_map, float *ur_base, const void *ur_map,
+                                  int ix64, const float *nl, int64_t ldn, int nl_unit,
+                                  void *stream) {
+    return intcflux_euler_shift<float>(ndims, n, gas, ul_base, ul_map, ur_base, ur_map, ix64, nl,
+                                       ldn, nl_unit, (cudaStream_t)stream);
 }
 
 int b200_intcflux_ns_f64(int ndims, int64_t n, int rsolver, const b200_gas_t *gas, double beta,

@@ -568,10 +568,10 @@ class MixedRKIntegrator(RKVdH2Integrator):
         else:
             self._ics = [e.set_ics_from_cfg() for e in sysm.ele_map.values()]
 
-        # Reference-state shift of the FP32 right-hand side (Navier-Stokes
-        # with the Rusanov solver, no boundaries): the volume means of rho
-        # and p of the initial condition.  Must be set before the kernels
-        # are built.
+        # Reference-state shift of the FP32 right-hand side (Euler or
+        # Navier-Stokes with the Rusanov solver, no boundaries or
+        # partitions): the point means of rho, the momentum and p of the
+        # initial condition.  Must be set before the kernels are built.
         self.uref, self.hs_ref = None, 0.0
         shift = cfg.get('backend-b200', 'reference-shift', 'auto')
         rs = cfg.get('solver-interfaces', 'riemann-solver')
@@ -579,20 +579,28 @@ class MixedRKIntegrator(RKVdH2Integrator):
         # read the solution, so they keep the unshifted state, as
         # boundaries do)
         sc = cfg.get('solver', 'shock-capturing', 'none')
-        if shift == 'auto' and sysm.name == 'navier-stokes' and \
+        if shift == 'auto' and sysm.name in ('navier-stokes', 'euler') and \
                 rs == 'rusanov' and not sysm._bc_inters and sc == 'none' \
-                and not sysm.has_src_macros:
+                and not sysm.has_src_macros and not sysm._mpi_inters:
             gamma = cfg.getfloat('constants', 'gamma')
-            rho = np.concatenate([u[:, 0].ravel() for u in self._ics])
+            nd = sysm.ndims
+            cons = [np.concatenate([u[:, v].ravel() for u in self._ics])
+                    for v in range(nd + 1)]
             pri = [e.con_to_pri(list(u.swapaxes(0, 1)), cfg)[-1]
                    for e, u in zip(sysm.ele_map.values(), self._ics)]
             p = np.concatenate([x.ravel() for x in pri])
-            rho_ref, p_ref = float(rho.mean()), float(p.mean())
-            backend.ref_state = (rho_ref, p_ref)
-            nv = sysm.nvars
-            self.uref = np.zeros(nv)
-            self.uref[0], self.uref[-1] = rho_ref, p_ref/(gamma - 1)
-            self.hs_ref = gamma/(gamma - 1)*p_ref/rho_ref
+            rho_ref, p_ref = float(cons[0].mean()), float(p.mean())
+            mom = np.array([float(c.mean()) for c in cons[1:]])
+            # A mean momentum at the rounding level of the state (a flow
+            # with no mean motion) is taken as exactly zero
+            scale = max(float(np.sqrt(np.mean(c*c))) for c in cons[1:])
+            if np.abs(mom).max() <= 1e-10*max(scale, 1e-300):
+                mom[:] = 0.0
+            vref = mom/rho_ref
+            e_ref = p_ref/(gamma - 1) + 0.5*rho_ref*float(vref @ vref)
+            backend.ref_state = (rho_ref, p_ref, tuple(vref))
+            self.uref = np.concatenate([[rho_ref], mom, [e_ref]])
+            self.hs_ref = (e_ref + p_ref)/rho_ref
 
         return sysm
 
