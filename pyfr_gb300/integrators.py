@@ -584,23 +584,33 @@ class MixedRKIntegrator(RKVdH2Integrator):
                 and not sysm.has_src_macros and not sysm._mpi_inters:
             gamma = cfg.getfloat('constants', 'gamma')
             nd = sysm.ndims
-            cons = [np.concatenate([u[:, v].ravel() for u in self._ics])
-                    for v in range(nd + 1)]
-            pri = [e.con_to_pri(list(u.swapaxes(0, 1)), cfg)[-1]
-                   for e, u in zip(sysm.ele_map.values(), self._ics)]
-            p = np.concatenate([x.ravel() for x in pri])
-            rho_ref, p_ref = float(cons[0].mean()), float(p.mean())
-            mom = np.array([float(c.mean()) for c in cons[1:]])
-            # A mean momentum at the rounding level of the state (a flow
-            # with no mean motion) is taken as exactly zero
-            scale = max(float(np.sqrt(np.mean(c*c))) for c in cons[1:])
-            if np.abs(mom).max() <= 1e-10*max(scale, 1e-300):
-                mom[:] = 0.0
+            saved = self._restart.state.get('intg/uref') \
+                if self.isrestart else None
+            if saved is not None and len(saved) == nd + 3:
+                # A restart keeps the run's reference state, so that it
+                # continues bit for bit
+                saved = np.asarray(saved, dtype=np.float64)
+                rho_ref, mom, p_ref = float(saved[0]), saved[1:nd + 1].copy(), \
+                    float(saved[nd + 2])
+            else:
+                cons = [np.concatenate([u[:, v].ravel() for u in self._ics])
+                        for v in range(nd + 1)]
+                pri = [e.con_to_pri(list(u.swapaxes(0, 1)), cfg)[-1]
+                       for e, u in zip(sysm.ele_map.values(), self._ics)]
+                p = np.concatenate([x.ravel() for x in pri])
+                rho_ref, p_ref = float(cons[0].mean()), float(p.mean())
+                mom = np.array([float(c.mean()) for c in cons[1:]])
+                # A mean momentum at the rounding level of the state (a
+                # flow with no mean motion) is taken as exactly zero
+                scale = max(float(np.sqrt(np.mean(c*c))) for c in cons[1:])
+                if np.abs(mom).max() <= 1e-10*max(scale, 1e-300):
+                    mom[:] = 0.0
             vref = mom/rho_ref
             e_ref = p_ref/(gamma - 1) + 0.5*rho_ref*float(vref @ vref)
             backend.ref_state = (rho_ref, p_ref, tuple(vref))
             self.uref = np.concatenate([[rho_ref], mom, [e_ref]])
             self.hs_ref = (e_ref + p_ref)/rho_ref
+            self._ref_saved = np.concatenate([[rho_ref], mom, [e_ref, p_ref]])
 
         return sysm
 
@@ -625,6 +635,15 @@ class MixedRKIntegrator(RKVdH2Integrator):
         be.commit()
         self.refresh_input(be.stream)
         be.wait()
+
+    def serialise(self):
+        """The base state and, with the reference-state transform, the
+        reference state itself (rho, momentum, E and p), which a restart
+        keeps."""
+        out = super().serialise()
+        if self.uref is not None:
+            out['intg/uref'] = self._ref_saved.copy()
+        return out
 
     @property
     def state_eps(self):
