@@ -54,6 +54,7 @@ struct GasK {
     T rho_ref, p_ref, e_ref, hs_ref, p_min;
     T v_ref[3], m_ref[3];
     int sutherland, shifted;
+    int moving;     // v_ref is not zero
 };
 
 template <typename T>
@@ -75,6 +76,7 @@ inline GasK<T> gas_consts(const Gas &g) {
         k.m_ref[i] = (T)(g.rho_ref * g.v_ref[i]);
         v2 += g.v_ref[i] * g.v_ref[i];
     }
+    k.moving = v2 != 0.0;
     const double e_ref = g.p_ref / (g.gamma - 1.0) + 0.5 * g.rho_ref * v2;
     k.e_ref = (T)e_ref;
     k.hs_ref = (T)(g.rho_ref != 0.0 ? (e_ref + g.p_ref) / g.rho_ref : 0.0);
@@ -287,34 +289,59 @@ __device__ __forceinline__ void rsolve_rusanov(const T *ul, const T *ur, const T
 // V = 0 these are m, m v + dp I and (s[E] + dp) v.)  Returns the full
 // pressure in p, the full velocity in v and the full state in ufull (for
 // the viscous terms and the wave speeds).
-template <int ND, typename T>
+//
+// MOVING false takes V = 0 at compile time (the reference state at rest:
+// the Navier-Stokes kernels' case), which keeps those kernels as lean as
+// before the moving form existed.
+template <int ND, typename T, bool MOVING = false>
 __device__ __forceinline__ void inviscid_flux_shift(const T *s, T f[ND][ND + 2], T &p, T v[ND],
                                                     T ufull[ND + 2], const GasK<T> &g) {
     constexpr int NV = ND + 2;
     const T gm1 = g.gm1;
     const T rho = g.rho_ref + s[0], invrho = T(1) / rho;
     const T dE = s[NV - 1] + g.hs_ref * s[0];
-    T w[ND], dot = 0;
+    if constexpr (MOVING) {
+        T w[ND], dot = 0;
 #pragma unroll
-    for (int i = 0; i < ND; i++) {
-        w[i] = invrho * (s[i + 1] - g.v_ref[i] * s[0]);
-        v[i] = g.v_ref[i] + w[i];
-        dot += g.m_ref[i] * w[i] + s[i + 1] * (g.v_ref[i] + w[i]);
-    }
-    const T dp = gm1 * (dE - T(0.5) * dot);
-    p = g.p_ref + dp;
-    const T hv = s[NV - 1] + dp;
+        for (int i = 0; i < ND; i++) {
+            w[i] = invrho * (s[i + 1] - g.v_ref[i] * s[0]);
+            v[i] = g.v_ref[i] + w[i];
+            dot += g.m_ref[i] * w[i] + s[i + 1] * v[i];
+        }
+        const T dp = gm1 * (dE - T(0.5) * dot);
+        p = g.p_ref + dp;
+        const T hv = s[NV - 1] + dp;
 #pragma unroll
-    for (int i = 0; i < ND; i++) {
-        f[i][0] = s[i + 1];
-        f[i][NV - 1] = hv * v[i];
+        for (int i = 0; i < ND; i++) {
+            f[i][0] = s[i + 1];
+            f[i][NV - 1] = hv * v[i];
 #pragma unroll
-        for (int j = 0; j < ND; j++)
-            f[i][j + 1] = g.m_ref[i] * w[j] + s[i + 1] * v[j] + (i == j ? dp : T(0));
+            for (int j = 0; j < ND; j++)
+                f[i][j + 1] = g.m_ref[i] * w[j] + s[i + 1] * v[j] + (i == j ? dp : T(0));
+        }
+#pragma unroll
+        for (int i = 0; i < ND; i++) ufull[i + 1] = g.m_ref[i] + s[i + 1];
+    } else {
+        T dot = 0;
+#pragma unroll
+        for (int i = 0; i < ND; i++) {
+            v[i] = invrho * s[i + 1];
+            dot += s[i + 1] * v[i];
+        }
+        const T dp = gm1 * (dE - T(0.5) * dot);
+        p = g.p_ref + dp;
+        const T hv = s[NV - 1] + dp;
+#pragma unroll
+        for (int i = 0; i < ND; i++) {
+            f[i][0] = s[i + 1];
+            f[i][NV - 1] = hv * v[i];
+#pragma unroll
+            for (int j = 0; j < ND; j++) f[i][j + 1] = s[i + 1] * v[j] + (i == j ? dp : T(0));
+        }
+#pragma unroll
+        for (int i = 0; i < ND; i++) ufull[i + 1] = s[i + 1];
     }
     ufull[0] = rho;
-#pragma unroll
-    for (int i = 0; i < ND; i++) ufull[i + 1] = g.m_ref[i] + s[i + 1];
     ufull[NV - 1] = g.e_ref + dE;
 }
 
@@ -335,14 +362,14 @@ __device__ __forceinline__ void unshift_grad(const T gq[ND][ND + 2], T gu[ND][ND
 // Rusanov flux on transformed inputs: the dissipation acts on differences
 // of q, which are T times the differences of u, so the flux is T times the
 // Rusanov flux of the full states
-template <int ND, typename T>
+template <int ND, typename T, bool MOVING = false>
 __device__ __forceinline__ void rsolve_rusanov_shift(const T *ul, const T *ur, const T *n, T *nf,
                                                      T ufl[ND + 2], T ufr[ND + 2],
                                                      const GasK<T> &g) {
     constexpr int NV = ND + 2;
     T fl[ND][NV], fr[ND][NV], vl[ND], vr[ND], pl, pr;
-    inviscid_flux_shift<ND, T>(ul, fl, pl, vl, ufl, g);
-    inviscid_flux_shift<ND, T>(ur, fr, pr, vr, ufr, g);
+    inviscid_flux_shift<ND, T, MOVING>(ul, fl, pl, vl, ufl, g);
+    inviscid_flux_shift<ND, T, MOVING>(ur, fr, pr, vr, ufr, g);
 
     T nv = 0;
 #pragma unroll

@@ -107,7 +107,7 @@ tflux_euler_kernel(int nupts, int64_t neles, T gamma, const T *__restrict__ u, i
 
 // Euler transformed flux on shifted inputs q = T(u - u_ref) (b200::Gas):
 // the flux less the reference state's, formed from the perturbation
-template <int ND, typename T>
+template <int ND, typename T, bool MOVING>
 __global__ void __launch_bounds__(PW_BLOCK)
 tflux_euler_shift_kernel(int nupts, int64_t neles, b200::GasK<T> gas, const T *__restrict__ u,
                          int64_t ldu, T *__restrict__ f, int64_t ldf, ElemGeom<T> geo) {
@@ -124,7 +124,7 @@ tflux_euler_shift_kernel(int nupts, int64_t neles, b200::GasK<T> gas, const T *_
     for (int v = 0; v < NV; v++) uu[v] = u[upt * ldu + soa_off(e, v, NV)];
 
     T ft[ND][NV], p, vel[ND], uf[NV];
-    b200::inviscid_flux_shift<ND, T>(uu, ft, p, vel, uf, gas);
+    b200::inviscid_flux_shift<ND, T, MOVING>(uu, ft, p, vel, uf, gas);
 
 #pragma unroll
     for (int i = 0; i < ND; i++)
@@ -495,7 +495,7 @@ intcflux_euler_kernel(int64_t n, T gamma, T p_min, ScalView<T> vl, ScalView<T> v
 
 // Rusanov common flux on shifted inputs (the dissipation acts on
 // differences of q, which are T times the differences of u)
-template <int ND, typename T>
+template <int ND, typename T, bool MOVING>
 __global__ void __launch_bounds__(PW_BLOCK)
 intcflux_euler_shift_kernel(int64_t n, b200::GasK<T> gas, ScalView<T> vl, ScalView<T> vr,
                             int ix64, const T *__restrict__ nl, int64_t ldn, int nl_unit) {
@@ -515,7 +515,7 @@ intcflux_euler_shift_kernel(int64_t n, b200::GasK<T> gas, ScalView<T> vl, ScalVi
     const T mag = pair_normal<ND, T>(nl, ldn, i, nl_unit, nn);
 
     T fn[NV], ufl[NV], ufr[NV];
-    b200::rsolve_rusanov_shift<ND, T>(ul, ur, nn, fn, ufl, ufr, gas);
+    b200::rsolve_rusanov_shift<ND, T, MOVING>(ul, ur, nn, fn, ufl, ufr, gas);
 
 #pragma unroll
     for (int v = 0; v < NV; v++) {
@@ -811,6 +811,9 @@ int tflux_ns(int ndims, int nupts, int64_t neles, int linear, const b200_gas_t *
     if (rc) return rc;
     auto geo = make_geom<T>(linear, smats, lds, rcpdjac, ldr, verts, ldv, upts, ldup);
     const auto g = b200::gas_consts<T>(*reinterpret_cast<const Gas *>(gas));
+    if (g.moving)
+        return b200::set_error(B200_ERR_UNSUPPORTED,
+                               "tflux_ns: the reference state must be at rest");
     dim3 grid(b200::ceil_div(neles, PW_BLOCK), nupts);
     if (ndims == 2)
         tflux_ns_kernel<2, T><<<grid, PW_BLOCK, 0, st>>>(nupts, neles, g, u, ldu, f, ldf, gradu, ldg, geo, av, lda, gradwb);
@@ -873,10 +876,14 @@ int tflux_euler_shift(int ndims, int nupts, int64_t neles, int linear, const b20
     auto geo = make_geom<T>(linear, smats, lds, nullptr, 0, verts, ldv, upts, ldup);
     const auto g = b200::gas_consts<T>(*reinterpret_cast<const Gas *>(gas));
     dim3 grid(b200::ceil_div(neles, PW_BLOCK), nupts);
-    if (ndims == 2)
-        tflux_euler_shift_kernel<2, T><<<grid, PW_BLOCK, 0, st>>>(nupts, neles, g, u, ldu, f, ldf, geo);
+    if (ndims == 2 && g.moving)
+        tflux_euler_shift_kernel<2, T, true><<<grid, PW_BLOCK, 0, st>>>(nupts, neles, g, u, ldu, f, ldf, geo);
+    else if (ndims == 2)
+        tflux_euler_shift_kernel<2, T, false><<<grid, PW_BLOCK, 0, st>>>(nupts, neles, g, u, ldu, f, ldf, geo);
+    else if (ndims == 3 && g.moving)
+        tflux_euler_shift_kernel<3, T, true><<<grid, PW_BLOCK, 0, st>>>(nupts, neles, g, u, ldu, f, ldf, geo);
     else if (ndims == 3)
-        tflux_euler_shift_kernel<3, T><<<grid, PW_BLOCK, 0, st>>>(nupts, neles, g, u, ldu, f, ldf, geo);
+        tflux_euler_shift_kernel<3, T, false><<<grid, PW_BLOCK, 0, st>>>(nupts, neles, g, u, ldu, f, ldf, geo);
     else
         return b200::set_error(B200_ERR_ARG, "tflux: ndims must be 2 or 3");
     B200_CHECK_LAUNCH("tflux_euler_shift");
@@ -894,10 +901,14 @@ int intcflux_euler_shift(int ndims, int64_t n, const b200_gas_t *gas, T *ul_base
     ScalView<T> l{ul_base, ul_map}, r{ur_base, ur_map};
     const auto g = b200::gas_consts<T>(*reinterpret_cast<const Gas *>(gas));
     unsigned grid = b200::ceil_div(n, PW_BLOCK);
-    if (ndims == 2)
-        intcflux_euler_shift_kernel<2, T><<<grid, PW_BLOCK, 0, st>>>(n, g, l, r, ix64, nl, ldn, nl_unit);
+    if (ndims == 2 && g.moving)
+        intcflux_euler_shift_kernel<2, T, true><<<grid, PW_BLOCK, 0, st>>>(n, g, l, r, ix64, nl, ldn, nl_unit);
+    else if (ndims == 2)
+        intcflux_euler_shift_kernel<2, T, false><<<grid, PW_BLOCK, 0, st>>>(n, g, l, r, ix64, nl, ldn, nl_unit);
+    else if (g.moving)
+        intcflux_euler_shift_kernel<3, T, true><<<grid, PW_BLOCK, 0, st>>>(n, g, l, r, ix64, nl, ldn, nl_unit);
     else
-        intcflux_euler_shift_kernel<3, T><<<grid, PW_BLOCK, 0, st>>>(n, g, l, r, ix64, nl, ldn, nl_unit);
+        intcflux_euler_shift_kernel<3, T, false><<<grid, PW_BLOCK, 0, st>>>(n, g, l, r, ix64, nl, ldn, nl_unit);
     B200_CHECK_LAUNCH("intcflux_euler_shift");
     return B200_OK;
 }
@@ -923,6 +934,9 @@ int intcflux_ns(int ndims, int64_t n, int rsolver, const b200_gas_t *gas, double
     if (g.shifted && rsolver != b200::RS_RUSANOV)
         return b200::set_error(B200_ERR_UNSUPPORTED,
                                "intcflux_ns: shifted inputs need the Rusanov solver");
+    if (g.moving)
+        return b200::set_error(B200_ERR_UNSUPPORTED,
+                               "intcflux_ns: the reference state must be at rest");
     if (ndims != 2 && ndims != 3)
         return b200::set_error(B200_ERR_ARG, "intcflux_ns: ndims must be 2 or 3");
     unsigned grid = b200::ceil_div(n, PW_BLOCK);

@@ -601,9 +601,11 @@ class MixedRKIntegrator(RKVdH2Integrator):
                 rho_ref, p_ref = float(cons[0].mean()), float(p.mean())
                 mom = np.array([float(c.mean()) for c in cons[1:]])
                 # A mean momentum at the rounding level of the state (a
-                # flow with no mean motion) is taken as exactly zero
+                # flow with no mean motion) is taken as exactly zero, and
+                # the Navier-Stokes kernels take a reference state at rest
                 scale = max(float(np.sqrt(np.mean(c*c))) for c in cons[1:])
-                if np.abs(mom).max() <= 1e-10*max(scale, 1e-300):
+                if np.abs(mom).max() <= 1e-10*max(scale, 1e-300) or \
+                        sysm.name == 'navier-stokes':
                     mom[:] = 0.0
             vref = mom/rho_ref
             e_ref = p_ref/(gamma - 1) + 0.5*rho_ref*float(vref @ vref)
