@@ -49,3 +49,23 @@ def test_reference_divergence_chain_fused(tmp_path):
     assert 'mul:bf16x3-cat' in names
     assert 'negdivconf' not in names
     assert graphs[-1] == ['tflux', 'mul:bf16x3-cat']
+
+
+@pytest.mark.parametrize('kinds', ['hex-pyr-tet', 'pri-tet'])
+def test_reference_stack_mixed_mesh_builds_and_steps(tmp_path, kinds):
+    """PyFR's own Euler system on a mixed mesh (its own pyramid shape and
+    points with hexahedra and tetrahedra, or prisms with tetrahedra) builds
+    every kernel it asks for from the b200 backend and steps, against the
+    library stand-in (no GPU)."""
+    if reference_tree() is None:
+        pytest.skip('reference source tree not present')
+    out = tmp_path / 'soln.npz'
+    r = subprocess.run([sys.executable, '-m', 'tests.refstack', '--fake',
+                        '--case', f'mixed-{kinds}', '--n', '2', '--steps',
+                        '2', '--out', str(out)],
+                       cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-3000:]
+    d = np.load(out)
+    assert str(d['backend']) == 'B200Backend'
+    assert int(d['nsteps']) == 2
+    assert set(map(str, d['etypes'])) == set(kinds.split('-'))
