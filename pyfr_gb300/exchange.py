@@ -16,6 +16,10 @@ before any of them waits.
   (gloo for host buffers), point-to-point with one tag per field.
 * ``LocalExchanger``: several partitions in one process (one GPU, or
   tests); a posted buffer waits in a mailbox until its peer completes.
+
+``allreduce`` (``TorchExchanger``) combines the step-size controllers'
+per-part sums and maxima; parts driven in one process have no blocking
+rendezvous, so the controllers need one process per part.
 """
 
 
@@ -39,6 +43,20 @@ class TorchExchanger:
         for r in self._reqs:
             r.wait()
         self._reqs = []
+
+    def allreduce(self, values, op='sum'):
+        """Sum (or maximum, op='max') of ``values`` over every rank of the
+        group: the step-size controllers' global error norm and wave
+        speed (the reference's MPI Allreduce, pyfr/integrators/
+        controllers.py:105-117 and 22-26)."""
+        import numpy as np
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor(np.asarray(values, dtype=np.float64))
+        dist.all_reduce(t, op={'sum': dist.ReduceOp.SUM,
+                               'max': dist.ReduceOp.MAX}[op],
+                        group=self.group)
+        return t.numpy()
 
 
 class LocalExchanger:

@@ -118,9 +118,6 @@ class RKVdH2Integrator:
         # host, which a captured step cannot stop for)
         self.use_step_graph = backend.use_cuda_graphs and \
             not self.system.controlled_bcs and not self.system._mpi_inters
-        if self.system._mpi_inters and self.controller != 'none':
-            raise NotImplementedError('Step-size controllers across '
-                                      'partitions are not provided')
 
         # The step size lives in device memory (staged through page-locked
         # host memory), so that one captured graph per starting register
@@ -263,7 +260,27 @@ class RKVdH2Integrator:
         """Step size cfl/((2p + 1) max wave speed) of the current solution
         (pyfr/integrators/controllers.py:22-26)."""
         wmax = self.system.compute_max_wavespeed(self.idxcurr)
+        wmax = float(self._allreduce([wmax], 'max')[0])
         return self._cfl/(wmax*(2*self._order + 1))
+
+    def _allreduce(self, values, op='sum'):
+        """``values`` combined over every partition of a partitioned
+        system (through its exchanger), else as they are."""
+        if not self.system._mpi_inters:
+            return list(values)
+        xchg = self.system.exchanger
+        if xchg is None or not hasattr(xchg, 'allreduce'):
+            raise NotImplementedError(
+                'Step-size controllers across partitions need an exchanger '
+                'with allreduce (one process per part: TorchExchanger)')
+        return list(xchg.allreduce(values, op))
+
+    def _global_error(self, local_sum):
+        """The controller's error norm sqrt(sum / ndofs) over every
+        partition (pyfr/integrators/controllers.py:105-117)."""
+        tot, n = self._allreduce([local_sum, float(self.gndofs)])
+        err = math.sqrt(tot/n)
+        return err if not math.isnan(err) else 100
 
     def _setup_registers(self, initsoln):
         pass
@@ -399,8 +416,7 @@ class RKVdH2Integrator:
             k.bind(rtol=self._rtol)
             k.run(self.backend.stream)
         self.backend.wait()
-        err = math.sqrt(sum(k.retval[0] for k in ks) / self.gndofs)
-        return err if not math.isnan(err) else 100
+        return self._global_error(sum(k.retval[0] for k in ks))
 
     def advance_to(self, t):
         if t < self.tcurr:
@@ -771,8 +787,7 @@ class MixedRKIntegrator(RKVdH2Integrator):
             k.bind(rtol=self._rtol)
             k.run(self.backend.stream)
         self.backend.wait()
-        err = math.sqrt(sum(k.retval[0] for k in ks) / self.gndofs)
-        return err if not math.isnan(err) else 100
+        return self._global_error(sum(k.retval[0] for k in ks))
 
     @property
     def soln(self):

@@ -113,3 +113,66 @@ def test_exchange_pairs_points_across_ranks(world):
     for rank, err, npts in res:
         assert npts > 0
         assert err < 1e-12, (rank, err)
+
+
+def _controller_rank(rank, world, port, q):
+    """The step-size controllers' reductions across parts: each rank holds
+    its part's error sum, DoF count and largest wave speed; the
+    integrator's combination (sqrt of the summed sums over the summed DoF,
+    the largest wave speed) goes through TorchExchanger.allreduce."""
+    import math
+    from types import SimpleNamespace
+    import torch.distributed as dist
+    from pyfr_gb300.exchange import TorchExchanger
+    from pyfr_gb300.integrators import RKVdH2Integrator
+    os.environ.update(MASTER_ADDR='127.0.0.1', MASTER_PORT=str(port))
+    dist.init_process_group('gloo', rank=rank, world_size=world)
+    try:
+        intg = SimpleNamespace(
+            system=SimpleNamespace(_mpi_inters=[object()],
+                                   exchanger=TorchExchanger()),
+            gndofs=100*(rank + 1))
+        intg._allreduce = lambda v, op='sum': \
+            RKVdH2Integrator._allreduce(intg, v, op)
+        err = RKVdH2Integrator._global_error(intg, 2.0*(rank + 1)**2)
+        wmax = intg._allreduce([3.0 + rank], 'max')[0]
+        q.put((rank, err, wmax))
+    finally:
+        dist.destroy_process_group()
+
+
+@pytest.mark.parametrize('world', [2, 3])
+def test_controller_reductions_across_ranks(world):
+    import math
+    import socket
+    import torch.multiprocessing as mp
+    with socket.socket() as s:
+        s.bind(('127.0.0.1', 0))
+        port = s.getsockname()[1]
+    ctx = mp.get_context('spawn')
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_controller_rank, args=(r, world, port, q))
+             for r in range(world)]
+    for p in procs:
+        p.start()
+    res = [q.get(timeout=300) for _ in procs]
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    want = math.sqrt(sum(2.0*(r + 1)**2 for r in range(world)) /
+                     sum(100*(r + 1) for r in range(world)))
+    for rank, err, wmax in res:
+        assert abs(err - want) <= 1e-15*want, (rank, err, want)
+        assert wmax == 3.0 + world - 1
+
+
+def test_controller_needs_an_allreduce():
+    """Parts driven in one process (LocalExchanger) cannot rendezvous: a
+    controller across them is refused with a clear error."""
+    from types import SimpleNamespace
+    from pyfr_gb300.exchange import LocalExchanger
+    from pyfr_gb300.integrators import RKVdH2Integrator
+    intg = SimpleNamespace(system=SimpleNamespace(
+        _mpi_inters=[object()], exchanger=LocalExchanger().endpoint(0)))
+    with pytest.raises(NotImplementedError, match='allreduce'):
+        RKVdH2Integrator._allreduce(intg, [1.0])
